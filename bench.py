@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Throughput of the plain single-party prover on GB300.
+
+Workload (one step = one proof): a 2^24-evaluation witness of uniform
+base-field values (SplitMix64, seed 0x5EEF0000), Reed-Solomon rate 1/2
+(codeword 2^25), Blake3 Merkle tree over the codeword, quadratic sumcheck
+with Fiat-Shamir challenges, WHIR opening with folding factor 4 until at
+most 4 coefficients remain.  Every step emits the full transcript, which is
+checked against the CPU oracle once per run.
+
+Prints one JSON line:
+  value        proofs/s with the witness resident in HBM (device pointers)
+  e2e          proofs/s through gbz_prove with pinned HOST buffers: the
+               witness H2D copy and the transcript D2H copy are in the
+               timed region of every step
+  roofline     the dominant kernel category, timed with CUDA events on the
+               launching stream during a second timed pass
+  cpu_baseline the oracle port (oracle/gbz_oracle.c) proving the same
+               workload once on the host cores
+  --impl reference: the reference arm.  The reference's CPU prover does not
+               build on the Arm GPU host (x86-64 inline asm in
+               fieldElement.cpp), so this arm times the oracle port, which is
+               pinned byte for byte to the reference's transcripts.
+
+Multi-GPU: proofs are independent, so N GPUs run N replicas (weak scaling,
+no collective); `value` sums the proofs of all ranks over the slowest rank's
+time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "shorter-and-faster-post-quantum-secure-scalable-collaborative-snarks_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+sys.path.insert(0, PKG)
+sys.path.insert(0, ORACLE)
+
+LOGN, RATE = 24, 2
+SEED = 0x5EED0000 + 2 * 65536  # configuration 2, instance 0
+METRIC = "proofs/s (plain single-party prover: 2^24 witness, RS rate 1/2, Blake3 Merkle, sumcheck, WHIR k=4)"
+CONFIG = {
+    "workload": "plain prover, n=2^24 uniform base-field witness, rate 1/2 (NTT 2^25), Blake3 Merkle over "
+                "2^23 leaves of 4 elements, FS sumcheck (24 rounds), WHIR folding 4 (11 iterations)",
+    "logn": LOGN, "rate": RATE, "whir_k": 4,
+    "l2": "inputs larger than L2 (witness 256 MiB, codeword 512 MiB per step)",
+}
+
+# Algorithmic bytes per proof by kernel category (roofline).
+def algorithmic_bytes(logn, rate):
+    n, L = 1 << logn, (1 << logn) * rate
+    out = {}
+    # sumcheck: every round reads 2 vectors of length m and writes 2 of m/2;
+    # main sumcheck + WHIR sumcheck rounds over halving lengths (~96 n bytes each)
+    sc = 0
+    m = n
+    sc += 2 * 16 * m  # round 0 reads w and beta
+    while m > 1:
+        sc += 2 * 16 * m + 2 * 16 * (m // 2)
+        m //= 2
+    m, wsc = n, 0
+    while m > 4:
+        wsc += 2 * 16 * m + (2 * 16 * m + 2 * 16 * (m // 2)) + (2 * 16 * (m // 2) + 2 * 16 * (m // 4))
+        m //= 4
+    out["sumcheck"] = sc + wsc
+    # NTT: read valid input + write codeword, per commit
+    ntt, merkle = 16 * n + 16 * L, 16 * L + 32 * (L // 2)
+    m, cur = n, rate
+    while m > 4:
+        m //= 4
+        NL = 2 * cur * m
+        ntt += 16 * m + 16 * NL
+        merkle += 16 * NL + 32 * (NL // 2)
+        cur *= 2
+    out["ntt"], out["merkle"] = ntt, merkle
+    out["beta"] = 2 * 16 * n
+    m, cur, ub = n, rate, 0
+    while m > 4:
+        m //= 4
+        ub += 2 * 16 * m
+        cur *= 2
+    out["update_betas"] = ub
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return ws, rank, local
+
+
+def barrier_and_max(value, ws):
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference_arm(args, ws, rank):
+    """The reference arm: the oracle port on all host cores, same workload."""
+    if rank != 0:
+        return
+    import gbz_oracle as O
+    O.build()
+    w = O.witness(SEED, 1 << LOGN)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.prove(w, LOGN, RATE, 1, threads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.prove(w, LOGN, RATE, 1, threads=cores)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (F_{p^2}, p=2^61-1)",
+        "data": "synthetic", "config": CONFIG,
+        "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
+        "cpu_baseline": {"value": value, "unit": "proofs/s", "cores": cores, "kind": "port",
+                         "sample": "full proofs of the same workload (oracle/gbz_oracle.c, pthreads)"},
+        "e2e": {"value": value, "unit": "proofs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own CPU code needs x86-64 (inline mulx asm, AVX types) and does not build on the "
+                "Arm host; the port reproduces its transcripts byte for byte",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbz", choices=["gbz", "reference"])
+    ap.add_argument("--logn", type=int, default=LOGN)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference_arm(args, ws, rank)
+        return
+
+    import build_lib
+    build_lib.build()
+    import gbz
+    import gbz_oracle as O
+    O.build()
+    logn = args.logn
+    n = 1 << logn
+    w = O.witness(SEED + rank, n)  # each replica proves its own witness
+    tbytes = gbz.transcript_bytes(logn, RATE)
+    launches = gbz.prove_launches(logn, RATE)
+
+    ctx = gbz.Context(local)
+    rt = ctypes.CDLL("libcudart.so")
+    rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    rt.cudaEventCreate.argtypes = [ctypes.POINTER(ctypes.c_void_p)]
+    rt.cudaEventRecord.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    rt.cudaEventSynchronize.argtypes = [ctypes.c_void_p]
+    rt.cudaEventElapsedTime.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p]
+    stream = gbz.lib.gbz_get_stream(ctx.h)
+
+    # device-resident witness and transcript
+    dw, dt = ctypes.c_void_p(), ctypes.c_void_p()
+    ctx.check(gbz.lib.gbz_device_alloc(ctx.h, ctypes.byref(dw), w.nbytes))
+    ctx.check(gbz.lib.gbz_device_alloc(ctx.h, ctypes.byref(dt), tbytes))
+    assert rt.cudaMemcpy(dw, w.ctypes.data, w.nbytes, 1) == 0
+
+    def prove_device():
+        ctx.check(gbz.lib.gbz_prove(ctx.h, dw, logn, RATE, 1, dt, tbytes, gbz.MEM_DEVICE))
+
+    def events(k):
+        evs = []
+        for _ in range(k):
+            e = ctypes.c_void_p()
+            assert rt.cudaEventCreate(ctypes.byref(e)) == 0
+            evs.append(e)
+        return evs
+
+    # correctness: the device transcript equals the oracle's
+    prove_device()
+    ctx.synchronize()
+    got = np.zeros(tbytes, dtype=np.uint8)
+    assert rt.cudaMemcpy(got.ctypes.data, dt, tbytes, 2) == 0
+
+    for _ in range(args.warmup):
+        prove_device()
+    ctx.synchronize()
+
+    # timed pass 1: device-resident inputs
+    ev = events(args.steps + 1)
+    with ClockSampler(local) as clk:
+        rt.cudaEventRecord(ev[0], stream)
+        for i in range(args.steps):
+            prove_device()
+            rt.cudaEventRecord(ev[i + 1], stream)
+        rt.cudaEventSynchronize(ev[-1])
+    lat = []
+    for i in range(args.steps):
+        x = ctypes.c_float()
+        rt.cudaEventElapsedTime(ctypes.byref(x), ev[i], ev[i + 1])
+        lat.append(x.value)
+    total_ms = sum(lat)
+    total_ms = barrier_and_max(total_ms, ws)
+    value = ws * args.steps / (total_ms / 1e3)
+
+    # timed pass 2: per-category kernel time with events on the same stream
+    ctx.profile_enable(True)
+    ctx.profile_read(logn, RATE)
+    for _ in range(args.steps):
+        prove_device()
+    ctx.synchronize()
+    prof = ctx.profile_read(logn, RATE)
+    ctx.profile_enable(False)
+
+    # timed pass 3: end to end through the public API with pinned host buffers
+    hw_p, ht_p = ctypes.c_void_p(), ctypes.c_void_p()
+    ctx.check(gbz.lib.gbz_host_alloc(ctypes.byref(hw_p), w.nbytes))
+    ctx.check(gbz.lib.gbz_host_alloc(ctypes.byref(ht_p), tbytes))
+    ctypes.memmove(hw_p, w.ctypes.data, w.nbytes)
+    for _ in range(2):
+        ctx.check(gbz.lib.gbz_prove(ctx.h, hw_p, logn, RATE, 1, ht_p, tbytes, gbz.MEM_HOST))
+    t0 = time.perf_counter()
+    e2e_lat = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        ctx.check(gbz.lib.gbz_prove(ctx.h, hw_p, logn, RATE, 1, ht_p, tbytes, gbz.MEM_HOST))
+        e2e_lat.append(time.perf_counter() - t1)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = barrier_and_max(e2e_s, ws)
+    e2e = ws * args.steps / e2e_s
+    host_t = np.ctypeslib.as_array(ctypes.cast(ht_p, ctypes.POINTER(ctypes.c_uint8)), shape=(tbytes,)).copy()
+    assert host_t.tobytes() == got.tobytes()
+
+    # roofline of the dominant category
+    algo = algorithmic_bytes(logn, RATE)
+    per_proof_ms = {k: v[0] / args.steps for k, v in prof.items()}
+    dom = max(per_proof_ms, key=lambda k: per_proof_ms[k])
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        hbm_peak, peak_src = 6800.0, "fallback"
+    dom_bytes = algo.get(dom)
+    roof = None
+    if dom_bytes:
+        achieved = dom_bytes / (per_proof_ms[dom] / 1e3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": None,
+                "algorithmic_bytes_per_proof": dom_bytes, "ms_per_proof": per_proof_ms[dom]}
+    else:
+        roof = {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm_peak, "unit": "GB/s", "frac": None,
+                "peak_source": peak_src, "traffic": None, "ms_per_proof": per_proof_ms[dom]}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 (F_{p^2}, p=2^61-1)",
+        "data": "synthetic (SplitMix64 witness)", "config": dict(CONFIG, parallelism="replicas%d" % ws),
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "e2e": {"value": e2e, "unit": "proofs/s", "h2d_bytes_per_step": int(w.nbytes),
+                "d2h_bytes_per_step": int(tbytes), "p50_ms": 1e3 * float(np.percentile(e2e_lat, 50)),
+                "p99_ms": 1e3 * float(np.percentile(e2e_lat, 99))},
+        "gpu_launches": launches * args.steps,
+        "kernel_ms_per_proof": per_proof_ms,
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "transcript_bytes": tbytes,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = O.prove(w, logn, RATE, 1, threads=cores)
+        dt_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / dt_cpu, "unit": "proofs/s", "cores": cores, "kind": "port",
+                                "sample": "one full proof of the same workload (same witness) on the host"}
+        line["transcript_equals_oracle"] = ref == got.tobytes()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    gbz.lib.gbz_host_free(hw_p)
+    gbz.lib.gbz_host_free(ht_p)
+    gbz.lib.gbz_device_free(ctx.h, dw)
+    gbz.lib.gbz_device_free(ctx.h, dt)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+/*
+ * gbz.h — C ABI of the GB300 prover hot path (libgbz.so).
+ *
+ * Each entry point replaces one function (or one fixed call sequence) of the
+ * reference prover and names it as "replaces <file>:<line>" with paths
+ * relative to the reference's src/ directory.  Signatures use plain
+ * pointers and sizes only.
+ *
+ * Data layout
+ *   A field element of F_{p^2}, p = 2^61 - 1, is two uint64 words, `real`
+ *   then `img` (virgo::fieldElement, fieldElement.hpp:96-97).  Arrays of n
+ *   elements are 2n words.  Inputs must be canonical (each word < p), which
+ *   every value the reference produces on this path is.
+ *   A hash is 32 bytes (_hash, Blake3_hash.h:3-5).  Merkle levels are stored
+ *   back to back: N/4 leaf hashes, then N/8, ..., 1 (N/2 - 1 hashes).
+ *
+ * Memory
+ *   `mem` = GBZ_MEM_HOST: pointers are host memory; the call copies inputs
+ *   in and results out and returns when the results are in place.
+ *   `mem` = GBZ_MEM_DEVICE: pointers are device memory of the context's
+ *   device; the work is enqueued on the context's stream and the call may
+ *   return before it finishes (gbz_synchronize waits).
+ *
+ * Errors
+ *   Every call returns a gbz_status instead of the reference's printf+exit.
+ *   gbz_last_error() gives a message for the last failing call of a context.
+ *
+ * Threading
+ *   A context owns one CUDA stream and its scratch buffers; use one context
+ *   per host thread.  Contexts on the same device run concurrently.
+ */
+#ifndef GBZ_H
+#define GBZ_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbz_ctx gbz_ctx;
+typedef int gbz_status;
+
+#define GBZ_OK 0
+#define GBZ_EINVAL 1      /* bad size, length not a power of two, null pointer */
+#define GBZ_ENOMEM 2      /* device or pinned-host allocation failed */
+#define GBZ_ECUDA 3       /* a CUDA call failed */
+#define GBZ_ECHECK 4      /* a device-side protocol consistency check failed */
+#define GBZ_ESMALL 5      /* output capacity too small */
+
+#define GBZ_MEM_HOST 0
+#define GBZ_MEM_DEVICE 1
+
+/* ------------------------------------------------------------- context */
+gbz_status gbz_create(gbz_ctx **ctx, int device);
+void gbz_destroy(gbz_ctx *ctx);
+/* Use an existing cudaStream_t (passed as void*) instead of the context's own. */
+gbz_status gbz_set_stream(gbz_ctx *ctx, void *cuda_stream);
+void *gbz_get_stream(gbz_ctx *ctx);
+gbz_status gbz_synchronize(gbz_ctx *ctx);
+const char *gbz_status_string(gbz_status s);
+const char *gbz_last_error(const gbz_ctx *ctx);
+/* Pinned host memory (for GBZ_MEM_HOST calls that should not stage). */
+gbz_status gbz_host_alloc(void **ptr, uint64_t bytes);
+void gbz_host_free(void *ptr);
+gbz_status gbz_device_alloc(gbz_ctx *ctx, void **ptr, uint64_t bytes);
+void gbz_device_free(gbz_ctx *ctx, void *ptr);
+
+/* ---------------------------------------------------- field and hashes */
+
+/* Elementwise a+b, a-b, a*b (any output may be null).
+ * replaces fieldElement::operator+ / operator- / operator* (fieldElement.cpp:34-96). */
+gbz_status gbz_field_ops(gbz_ctx *ctx, const uint64_t *a, const uint64_t *b, uint64_t n, uint64_t *sum,
+                         uint64_t *diff, uint64_t *prod, int mem);
+
+/* count independent BLAKE3 hashes of 64-byte blocks (in: 64*count bytes,
+ * out: 32*count bytes).
+ * replaces blake3_hash (Blake3_hash.cpp:5-10). */
+gbz_status gbz_blake3_64(gbz_ctx *ctx, const uint8_t *in, uint8_t *out, uint64_t count, int mem);
+
+/* In-place transform of 2^logn elements: forward, or inverse scaled by 2^-logn.
+ * replaces fft (utils.cpp:904-964) and pfft (utils.cpp:1583-1673; forward only there). */
+gbz_status gbz_fft(gbz_ctx *ctx, uint64_t *data, int logn, int inverse, int mem);
+
+/* Reed-Solomon encoding as WHIR commits it: codeword (rate*m elements) =
+ * forward transform of arr (m elements) zero-padded to rate*m.
+ * replaces the padding + pfft of Whir_Commit_initial (Whir.cpp:160-163). */
+gbz_status gbz_rs_encode(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int rate, uint64_t *codeword,
+                         int mem);
+
+/* Blake3 Merkle tree over N elements (N a power of two >= 4): leaves hash
+ * four consecutive elements, each inner node hashes its left child twice.
+ * levels: (N/2 - 1) * 32 bytes.
+ * replaces MT_commit_Blake + create_tree_blake (merkle_tree.cpp:195-233, 267-299). */
+gbz_status gbz_merkle_commit_blake(gbz_ctx *ctx, const uint64_t *elems, uint64_t N, uint8_t *levels,
+                                   int mem);
+
+/* Authentication path of leaf pos: log2(N/4) sibling hashes (host memory).
+ * replaces open_tree_blake (merkle_tree.cpp:320-335). */
+gbz_status gbz_merkle_open_blake(const uint8_t *levels, uint64_t N, uint64_t pos, uint8_t *path,
+                                 uint32_t *depth);
+
+/* codeword = encode(arr, rate); levels = Merkle tree of the codeword.
+ * replaces Whir_Commit_initial (Whir.cpp:158-190). */
+gbz_status gbz_whir_commit(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int rate, uint64_t *codeword,
+                           uint8_t *levels, int mem);
+
+/* eq table B[x] = prod_i (bit_i(x) ? r_i : 1 - r_i), 2^nr elements.
+ * replaces precompute_beta (utils.cpp:198-243). */
+gbz_status gbz_precompute_beta(gbz_ctx *ctx, const uint64_t *r, int nr, uint64_t *B, int mem);
+
+/* ------------------------------------------------------------ sumcheck */
+
+/* Round message (a, b, c) of sum_j (v1 line_j)(v2 line_j) over m elements
+ * (coeffs: 6 words, host memory).
+ * replaces whir_sumcheck_step1 (Whir.cpp:215-221) and the round sums of
+ * _quadratic_cosumcheck (coSumcheck_MPI.cpp:199) / _quadratic_sumcheck
+ * (delegate_protocol.cpp:16-21). */
+gbz_status gbz_sumcheck_quadratic(gbz_ctx *ctx, const uint64_t *v1, const uint64_t *v2, uint64_t m,
+                                  uint64_t *coeffs, int mem);
+
+/* v[j] = r*(v[2j+1]-v[2j]) + v[2j] for j < m/2, in place (r: host memory).
+ * replaces the fold loops of whir_sumcheck_step2 (Whir.cpp:223-231) and
+ * _quadratic_cosumcheck (coSumcheck_MPI.cpp:215-218). */
+gbz_status gbz_sumcheck_fold(gbz_ctx *ctx, uint64_t *v, uint64_t m, const uint64_t *r, int mem);
+
+/* b[j] += c_i * omega_N^(q_i * j) with c_i = r^(i+1); challenges (l
+ * elements, host memory, may be null) receives the c_i.  r is the value the
+ * reference draws with F::_random() at Whir.cpp:327.
+ * replaces update_betas (Whir.cpp:325-342). */
+gbz_status gbz_whir_update_betas(gbz_ctx *ctx, uint64_t *b, uint64_t nb, const int32_t *queries, int l,
+                                 uint64_t N, const uint64_t *r, uint64_t *challenges, int mem);
+
+/* ---------------------------------------------- host-side protocol state */
+
+/* Fiat-Shamir: state[2] is the chain value (prev_challenge, initially 0);
+ * absorbs count elements and returns the new challenge in out[2].
+ * replaces hash_to_field / hash_F (Fiat_Shamir.cpp:8-34), with the chain
+ * held by the caller instead of a process global. */
+void gbz_hash_to_field(uint64_t *state, const uint64_t *elems, int count, uint64_t *out);
+
+/* glibc random()/rand() stream, seeded like srandom(seed).
+ * replaces the process-global generator behind F::_random
+ * (fieldElement.cpp:119-125, 363-368) and rand() (Whir.cpp:262-268). */
+typedef struct {
+  int32_t tbl[31];
+  int32_t f, r;
+} gbz_prng;
+void gbz_prng_seed(gbz_prng *g, uint32_t seed);
+int32_t gbz_prng_next(gbz_prng *g);
+/* F::_random(): out[2] = (randomNumber() % p, randomNumber() % p). */
+void gbz_prng_field(gbz_prng *g, uint64_t *out);
+
+/* Host twin of the device field arithmetic (same source), elementwise. */
+void gbz_field_ops_host(const uint64_t *a, const uint64_t *b, uint64_t n, uint64_t *sum, uint64_t *diff,
+                        uint64_t *prod);
+
+/* --------------------------------------------------------------- prover */
+
+/* Bytes of the transcript of one proof of a 2^logn witness at `rate`. */
+uint64_t gbz_prove_transcript_bytes(int logn, int rate);
+
+/* One single-party proof: Whir_Commit_initial of the witness (Whir.cpp:158),
+ * evaluation point hash_to_field({0}) x logn (main.cpp:83-85), quadratic
+ * sumcheck of sum_x w(x) eq(z, x) with Fiat-Shamir challenges
+ * (_quadratic_cosumcheck round body, coSumcheck_MPI.cpp:195-219), and
+ * Whir_Open of its claim with whir_k = 4 (Whir.cpp:388-467).  The glibc
+ * random() stream that the reference draws WHIR challenges and queries from
+ * starts from srandom(prng_seed) (1 = the unseeded reference process).
+ *
+ * The transcript is a sequence of records {u32 tag, u32 count, payload}:
+ *  1 COMMIT_ROOT 32B | 2 EVAL_POINT 16B x logn | 3 CLAIM 16B
+ *  per round: 4 SC_POLY 16B x3, 5 SC_CHALLENGE 16B | 6 SC_FINAL 16B x2
+ *  per WHIR iteration: 2 x (7 WHIR_POLY 16B x3, 8 WHIR_CHALLENGE 16B),
+ *    9 WHIR_ROOT 32B, 10 WHIR_QUERIES u32 x l, 11 WHIR_REPLIES 16B x 4l,
+ *    12 WHIR_ANSWERS 16B x l, 13 WHIR_PATHS 32B x l*depth,
+ *    14 WHIR_COMBINE 16B x l, 15 WHIR_K 16B
+ *  16 FINAL_POLY 16B x m | 17 FINAL_POINT 16B x log2 m | 18 FINAL_EVAL 16B
+ * witness: 2^logn elements; transcript: gbz_prove_transcript_bytes bytes.
+ * With GBZ_MEM_HOST the call also checks the device-side consistency flags
+ * (every round's claim) and returns GBZ_ECHECK if one failed. */
+gbz_status gbz_prove(gbz_ctx *ctx, const uint64_t *witness, int logn, int rate, uint32_t prng_seed,
+                     uint8_t *transcript, uint64_t capacity, int mem);
+
+/* Kernel launches of one proof (host-side count, no GPU needed); 0 for an
+ * unsupported shape. */
+int gbz_prove_launches(int logn, int rate);
+
+/* ------------------------------------------------------------ profiling */
+
+/* Per-category CUDA-event timing of the kernels gbz_prove enqueues, on the
+ * context's stream.  Categories: 0 NTT, 1 Merkle, 2 sumcheck fold/reduce,
+ * 3 eq table, 4 WHIR beta update, 5 WHIR queries, 6 protocol steps
+ * (Fiat-Shamir, PRNG draws, round messages). */
+#define GBZ_PROF_CATEGORIES 7
+gbz_status gbz_profile_enable(gbz_ctx *ctx, int enable);
+/* Milliseconds and event-bracketed launch groups per category summed over
+ * the proofs of shape (logn, rate) since the last read; resets the sums.
+ * Waits for those proofs to finish. */
+gbz_status gbz_profile_read(gbz_ctx *ctx, int logn, int rate, double *ms, int *groups);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBZ_H */

@@ -1,0 +1,882 @@
+/*
+ * gbz_oracle.c — CPU restatement of the reference prover's hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (see gbz_oracle.h).  Each function names the
+ * reference file:line it restates.  The arithmetic is exact; where the
+ * reference's operation order cannot change a canonical result (all field
+ * operations below return the unique representative in [0, p)), loops are
+ * reorganised for multi-threading, which is what the CPU baseline needs.
+ */
+#define _GNU_SOURCE
+#include "gbz_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+typedef unsigned __int128 u128;
+typedef struct { uint64_t re, im; } fe;
+
+static const uint64_t P = 2305843009213693951ULL; /* fieldElement.cpp:7 */
+
+/* ---------------------------------------------------------------- field */
+
+/* mymult (fieldElement.cpp:341-361): x*y mod p, lazily in [0, 2p). */
+static inline uint64_t mymult(uint64_t x, uint64_t y) {
+  u128 t = (u128)x * y;
+  uint64_t lo = (uint64_t)t, hi = (uint64_t)(t >> 64);
+  return ((hi << 3) | (lo >> 61)) + (lo & P);
+}
+/* myMod (fieldElement.cpp:337-339) */
+static inline uint64_t mymod(uint64_t x) { return (x >> 61) + (x & P); }
+
+/* operator+ (fieldElement.cpp:34-47) */
+static inline fe f_add(fe a, fe b) {
+  fe r;
+  r.im = a.im + b.im;
+  r.re = a.re + b.re;
+  if (P <= r.im) r.im -= P;
+  if (P <= r.re) r.re -= P;
+  return r;
+}
+/* operator- (fieldElement.cpp:80-96) */
+static inline fe f_sub(fe a, fe b) {
+  fe r;
+  r.re = a.re + (b.re ^ P);
+  r.im = a.im + (b.im ^ P);
+  if (r.re >= P) r.re -= P;
+  if (r.im >= P) r.im -= P;
+  return r;
+}
+/* operator* (fieldElement.cpp:49-78), step for step. */
+static inline fe f_mul(fe a, fe b) {
+  fe r;
+  uint64_t all = mymult(a.im + a.re, b.im + b.re);
+  uint64_t ac = mymult(a.re, b.re), bd = mymult(a.im, b.im);
+  uint64_t nac = ac;
+  if (bd >= P) bd -= P;
+  if (nac >= P) nac -= P;
+  nac ^= P;
+  bd ^= P;
+  uint64_t ti = all + nac + bd;
+  ti = mymod(ti);
+  if (ti >= P) ti -= P;
+  r.im = ti;
+  uint64_t tr = ac + bd;
+  /* `while (t_real >= mod) t_real -= mod` leaves t_real mod p for any
+   * 64-bit t_real; one Mersenne fold plus one subtraction computes the same. */
+  tr = mymod(tr);
+  if (tr >= P) tr -= P;
+  r.re = tr;
+  return r;
+}
+static inline fe f_make(uint64_t re, uint64_t im) { fe r = {re, im}; return r; }
+static inline fe f_one(void) { return f_make(1, 0); }
+static inline fe f_zero(void) { return f_make(0, 0); }
+static inline int f_eq(fe a, fe b) { return a.re == b.re && a.im == b.im; }
+/* operator-() (fieldElement.cpp:98-104) = zero() - x */
+static inline fe f_neg(fe a) { return f_sub(f_zero(), a); }
+
+/* fastPow (fieldElement.cpp:323-335) */
+static fe f_pow(fe x, u128 e) {
+  fe ret = f_one(), t = x;
+  while (e) {
+    if (e & 1) ret = f_mul(ret, t);
+    t = f_mul(t, t);
+    e >>= 1;
+  }
+  return ret;
+}
+/* inv (fieldElement.cpp:207-210): x^(p^2-2) */
+static fe f_inv(fe x) {
+  u128 p = P;
+  return f_pow(x, p * p - 2);
+}
+/* getRootOfUnity (utils.cpp:706-717 == fieldElement.cpp:238-250) */
+static fe f_rou(int n) {
+  fe r = f_make(2147483648ULL, 1033321771269002680ULL);
+  for (int i = 0; i < 62 - n; i++) r = f_mul(r, r);
+  return r;
+}
+static fe f_small(int64_t x) { /* fieldElement(long long) for small x >= 0 */
+  return f_make((uint64_t)x, 0);
+}
+
+static inline fe ld(const uint64_t *p, int64_t i) { return f_make(p[2 * i], p[2 * i + 1]); }
+static inline void st(uint64_t *p, int64_t i, fe x) { p[2 * i] = x.re; p[2 * i + 1] = x.im; }
+
+void orc_field_ops(int64_t n, const uint64_t *a, const uint64_t *b, uint64_t *add, uint64_t *sub,
+                   uint64_t *mul, uint64_t *neg, uint64_t *inv) {
+  for (int64_t i = 0; i < n; i++) {
+    fe x = ld(a, i), y = ld(b, i);
+    if (add) st(add, i, f_add(x, y));
+    if (sub) st(sub, i, f_sub(x, y));
+    if (mul) st(mul, i, f_mul(x, y));
+    if (neg) st(neg, i, f_neg(x));
+    if (inv) st(inv, i, f_inv(x));
+  }
+}
+
+void orc_root_of_unity(int log_order, uint64_t out[2]) {
+  fe r = f_rou(log_order);
+  out[0] = r.re;
+  out[1] = r.im;
+}
+
+/* ------------------------------------------------------ glibc random() */
+/* glibc's random_r TYPE_3 generator (31-word state, separation 3), seeded
+ * by srandom_r's 16807 LCG and 310 discarded outputs.  The reference never
+ * calls srand on the prover path, so its generator starts in the state of
+ * seed 1 (glibc's static initial table); rand() shares the same state. */
+void orc_prng_seed(orc_prng *g, uint32_t seed) {
+  if (seed == 0) seed = 1;
+  int32_t word = (int32_t)seed;
+  g->tbl[0] = word;
+  for (int i = 1; i < 31; i++) {
+    long hi = word / 127773, lo = word % 127773;
+    word = (int32_t)(16807 * lo - 2836 * hi);
+    if (word < 0) word += 2147483647;
+    g->tbl[i] = word;
+  }
+  g->f = 3;
+  g->r = 0;
+  for (int i = 0; i < 310; i++) (void)orc_prng_next(g);
+}
+
+int32_t orc_prng_next(orc_prng *g) {
+  uint32_t v = (uint32_t)g->tbl[g->f] + (uint32_t)g->tbl[g->r];
+  g->tbl[g->f] = (int32_t)v;
+  int32_t out = (int32_t)(v >> 1);
+  if (++g->f >= 31) {
+    g->f = 0;
+    ++g->r;
+  } else if (++g->r >= 31) {
+    g->r = 0;
+  }
+  return out;
+}
+
+/* randomNumber (fieldElement.cpp:363-368) */
+static uint64_t prng_number(orc_prng *g) {
+  uint64_t ret = (uint64_t)(orc_prng_next(g) % 10);
+  for (int i = 1; i < 20; i++) ret = (ret * 10ULL + (uint64_t)(orc_prng_next(g) % 10)) % P;
+  return ret;
+}
+/* _random (fieldElement.cpp:119-125) */
+static fe prng_field(orc_prng *g) {
+  fe r;
+  r.re = prng_number(g) % P;
+  r.im = prng_number(g) % P;
+  return r;
+}
+void orc_prng_field(orc_prng *g, uint64_t out[2]) {
+  fe r = prng_field(g);
+  out[0] = r.re;
+  out[1] = r.im;
+}
+
+/* -------------------------------------------------------------- BLAKE3 */
+/* One BLAKE3 compression of a single 64-byte block, which is the whole
+ * hash for a 64-byte input: chaining value = IV, counter 0, block length
+ * 64, flags CHUNK_START|CHUNK_END|ROOT.  Algorithm from the BLAKE3
+ * specification (vendored as Blake/blake3_portable.c:8-98 and
+ * Blake/blake3_impl.h:86-98). */
+static const uint32_t B3_IV[8] = {0x6A09E667u, 0xBB67AE85u, 0x3C6EF372u, 0xA54FF53Au,
+                                  0x510E527Fu, 0x9B05688Cu, 0x1F83D9ABu, 0x5BE0CD19u};
+static const uint8_t B3_PERM[16] = {2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8};
+
+static inline uint32_t rotr32(uint32_t x, int c) { return (x >> c) | (x << (32 - c)); }
+static inline void b3g(uint32_t *v, int a, int b, int c, int d, uint32_t x, uint32_t y) {
+  v[a] = v[a] + v[b] + x;
+  v[d] = rotr32(v[d] ^ v[a], 16);
+  v[c] = v[c] + v[d];
+  v[b] = rotr32(v[b] ^ v[c], 12);
+  v[a] = v[a] + v[b] + y;
+  v[d] = rotr32(v[d] ^ v[a], 8);
+  v[c] = v[c] + v[d];
+  v[b] = rotr32(v[b] ^ v[c], 7);
+}
+
+static void blake3_one(const uint8_t in[64], uint8_t out[32]) {
+  uint32_t m[16], v[16], t[16];
+  for (int i = 0; i < 16; i++)
+    m[i] = (uint32_t)in[4 * i] | ((uint32_t)in[4 * i + 1] << 8) | ((uint32_t)in[4 * i + 2] << 16) |
+           ((uint32_t)in[4 * i + 3] << 24);
+  for (int i = 0; i < 8; i++) v[i] = B3_IV[i];
+  v[8] = B3_IV[0]; v[9] = B3_IV[1]; v[10] = B3_IV[2]; v[11] = B3_IV[3];
+  v[12] = 0; v[13] = 0; v[14] = 64; v[15] = 1 | 2 | 8;
+  for (int r = 0; r < 7; r++) {
+    b3g(v, 0, 4, 8, 12, m[0], m[1]);
+    b3g(v, 1, 5, 9, 13, m[2], m[3]);
+    b3g(v, 2, 6, 10, 14, m[4], m[5]);
+    b3g(v, 3, 7, 11, 15, m[6], m[7]);
+    b3g(v, 0, 5, 10, 15, m[8], m[9]);
+    b3g(v, 1, 6, 11, 12, m[10], m[11]);
+    b3g(v, 2, 7, 8, 13, m[12], m[13]);
+    b3g(v, 3, 4, 9, 14, m[14], m[15]);
+    for (int i = 0; i < 16; i++) t[i] = m[B3_PERM[i]];
+    memcpy(m, t, sizeof m);
+  }
+  for (int i = 0; i < 8; i++) {
+    uint32_t o = v[i] ^ v[i + 8];
+    out[4 * i] = (uint8_t)o; out[4 * i + 1] = (uint8_t)(o >> 8);
+    out[4 * i + 2] = (uint8_t)(o >> 16); out[4 * i + 3] = (uint8_t)(o >> 24);
+  }
+}
+
+void orc_blake3_64(int64_t count, const uint8_t *in, uint8_t *out) {
+  for (int64_t i = 0; i < count; i++) blake3_one(in + 64 * i, out + 32 * i);
+}
+
+/* Field element bytes as memcpy'd by the reference: real LE then img LE. */
+static inline void fe_bytes(fe x, uint8_t *o) {
+  for (int i = 0; i < 8; i++) { o[i] = (uint8_t)(x.re >> (8 * i)); o[8 + i] = (uint8_t)(x.im >> (8 * i)); }
+}
+
+/* ------------------------------------------------------- thread helper */
+typedef void (*range_fn)(void *ctx, int64_t lo, int64_t hi);
+typedef struct { range_fn fn; void *ctx; int64_t lo, hi; } job_t;
+static void *job_run(void *p) { job_t *j = (job_t *)p; j->fn(j->ctx, j->lo, j->hi); return NULL; }
+
+static int resolve_threads(int threads) {
+  if (threads > 0) return threads;
+  long n = sysconf(_SC_NPROCESSORS_ONLN);
+  return n > 0 ? (int)n : 1;
+}
+/* Runs fn over [0, n) split into `threads` contiguous ranges. */
+static void parallel_for(int64_t n, int threads, int64_t min_chunk, range_fn fn, void *ctx) {
+  threads = resolve_threads(threads);
+  if (threads <= 1 || n < 2 * min_chunk) { fn(ctx, 0, n); return; }
+  if ((int64_t)threads * min_chunk > n) threads = (int)(n / min_chunk);
+  if (threads > 256) threads = 256;
+  pthread_t th[256];
+  job_t jobs[256];
+  for (int t = 0; t < threads; t++) {
+    jobs[t].fn = fn; jobs[t].ctx = ctx;
+    jobs[t].lo = n * t / threads; jobs[t].hi = n * (t + 1) / threads;
+  }
+  for (int t = 1; t < threads; t++) pthread_create(&th[t], NULL, job_run, &jobs[t]);
+  job_run(&jobs[0]);
+  for (int t = 1; t < threads; t++) pthread_join(th[t], NULL);
+}
+
+/* ---------------------------------------------------------------- NTT */
+/* fft (utils.cpp:904-964): bit-reversal permutation, then radix-2 DIT
+ * stages with twiddle w[len/i*k], w[k] = rou^k (rou inverted for the
+ * inverse), then scaling by len^{-1} for the inverse. */
+typedef struct { fe *a; const fe *w; int64_t len, half, stride; int lghalf; } ntt_stage_ctx;
+static void ntt_stage_range(void *p, int64_t lo, int64_t hi) {
+  ntt_stage_ctx *c = (ntt_stage_ctx *)p;
+  for (int64_t t = lo; t < hi; t++) { /* butterfly index t in [0, len/2) */
+    int64_t blk = t >> c->lghalf, k = t & (c->half - 1);
+    int64_t j = blk * 2 * c->half;
+    fe u = c->a[j + k];
+    fe v = f_mul(c->a[j + k + c->half], c->w[c->stride * k]);
+    c->a[j + k] = f_add(u, v);
+    c->a[j + k + c->half] = f_sub(u, v);
+  }
+}
+typedef struct { fe *w; fe w1; int64_t n; } pow_ctx;
+static void pow_range(void *p, int64_t lo, int64_t hi) {
+  pow_ctx *c = (pow_ctx *)p;
+  fe x = f_pow(c->w1, (u128)lo);
+  for (int64_t i = lo; i < hi; i++) { c->w[i] = x; x = f_mul(x, c->w1); }
+}
+typedef struct { fe *a; fe s; } scale_ctx;
+static void scale_range(void *p, int64_t lo, int64_t hi) {
+  scale_ctx *c = (scale_ctx *)p;
+  for (int64_t i = lo; i < hi; i++) c->a[i] = f_mul(c->a[i], c->s);
+}
+
+void orc_fft(uint64_t *data, int logn, int inverse, int threads) {
+  int64_t len = (int64_t)1 << logn;
+  fe *a = (fe *)data;
+  if (len == 1) { /* no butterflies; the inverse still scales by 1^{-1} = 1 */
+    if (inverse) a[0] = f_mul(a[0], f_inv(f_one()));
+    return;
+  }
+  for (int64_t i = 1, j = 0; i < len; i++) { /* rev[i] = rev[i>>1]>>1 | (i&1)<<(logn-1) */
+    int64_t bit = len >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) { fe t = a[i]; a[i] = a[j]; a[j] = t; }
+  }
+  fe w1 = f_rou(logn);
+  if (inverse) w1 = f_inv(w1);
+  fe *w = (fe *)malloc(sizeof(fe) * (size_t)(len / 2));
+  pow_ctx pc = {w, w1, len / 2};
+  parallel_for(len / 2, threads, 1 << 14, pow_range, &pc);
+  int lghalf = 0;
+  for (int64_t i = 2; i <= len; i <<= 1, lghalf++) {
+    ntt_stage_ctx c = {a, w, len, i >> 1, len / i, lghalf};
+    parallel_for(len / 2, threads, 1 << 14, ntt_stage_range, &c);
+  }
+  free(w);
+  if (inverse) {
+    scale_ctx sc = {a, f_inv(f_small(len))};
+    parallel_for(len, threads, 1 << 14, scale_range, &sc);
+  }
+}
+
+/* ------------------------------------------------------------- Merkle */
+typedef struct { const uint8_t *src; uint8_t *dst; int leaf; } mk_ctx;
+static void mk_range(void *p, int64_t lo, int64_t hi) {
+  mk_ctx *c = (mk_ctx *)p;
+  uint8_t blk[64];
+  for (int64_t i = lo; i < hi; i++) {
+    if (c->leaf) {
+      blake3_one(c->src + 64 * i, c->dst + 32 * i); /* 4 elements = 64 raw bytes */
+    } else {
+      /* create_tree_blake (merkle_tree.cpp:287-292): both halves of the
+       * block are the LEFT child. */
+      memcpy(blk, c->src + 32 * (2 * i), 32);
+      memcpy(blk + 32, c->src + 32 * (2 * i), 32);
+      blake3_one(blk, c->dst + 32 * i);
+    }
+  }
+}
+
+int orc_merkle_commit(const uint64_t *elems, int64_t N, uint8_t *levels_out, int threads) {
+  if (N < 4 || (N & (N - 1))) return -1;
+  int64_t cnt = N / 4;
+  mk_ctx c = {(const uint8_t *)elems, levels_out, 1};
+  parallel_for(cnt, threads, 1 << 12, mk_range, &c);
+  uint8_t *prev = levels_out;
+  while (cnt > 1) {
+    uint8_t *next = prev + 32 * cnt;
+    cnt /= 2;
+    mk_ctx d = {prev, next, 0};
+    parallel_for(cnt, threads, 1 << 12, mk_range, &d);
+    prev = next;
+  }
+  return 0;
+}
+
+int orc_merkle_open(const uint8_t *levels, int64_t N, int64_t pos, uint8_t *path_out) {
+  int64_t cnt = N / 4;
+  if (pos < 0 || pos >= cnt) return -1;
+  const uint8_t *lv = levels;
+  int d = 0;
+  while (cnt > 1) {
+    int64_t sib = 2 * (pos / 2) + (1 - (pos % 2));
+    memcpy(path_out + 32 * d, lv + 32 * sib, 32);
+    d++;
+    lv += 32 * cnt;
+    cnt /= 2;
+    pos /= 2;
+  }
+  return d;
+}
+
+/* -------------------------------------------------------- Fiat-Shamir */
+/* hash_F (Fiat_Shamir.cpp:8-27): blake3(x || 0 || y || 0), folded to two
+ * 56-bit-ish words with weights 2^{7i}. */
+static fe hash_F(fe x, fe y) {
+  uint8_t data[64], h[32];
+  fe z = f_zero();
+  fe_bytes(x, data); fe_bytes(z, data + 16); fe_bytes(y, data + 32); fe_bytes(z, data + 48);
+  blake3_one(data, h);
+  uint64_t re = 0, im = 0;
+  for (int i = 0; i < 8; i++) {
+    re += (1ULL << (7 * i)) * h[i];
+    im += (1ULL << (7 * i)) * h[i + 8];
+  }
+  return f_make(re, im);
+}
+void orc_hash_F(const uint64_t x[2], const uint64_t y[2], uint64_t out[2]) {
+  fe r = hash_F(f_make(x[0], x[1]), f_make(y[0], y[1]));
+  out[0] = r.re; out[1] = r.im;
+}
+/* hash_to_field (Fiat_Shamir.cpp:29-34) */
+static fe fs_absorb(fe *state, const fe *e, int count) {
+  for (int i = 0; i < count; i++) *state = hash_F(*state, e[i]);
+  return *state;
+}
+void orc_hash_to_field(uint64_t state[2], const uint64_t *elems, int count, uint64_t out[2]) {
+  fe s = f_make(state[0], state[1]);
+  fs_absorb(&s, (const fe *)elems, count);
+  state[0] = out[0] = s.re;
+  state[1] = out[1] = s.im;
+}
+
+/* ---------------------------------------------------- beta / evaluate */
+/* precompute_beta (utils.cpp:198-243): B[x] = prod_i (bit_i(x) ? r_i : 1-r_i)
+ * with bit 0 bound to r[0].  The reference expands r from the last entry;
+ * B[2j] = B_j - B_j*r_i, B[2j+1] = B_j*r_i. */
+typedef struct { fe *B; const fe *src; fe r; } beta_ctx;
+static void beta_range(void *p, int64_t lo, int64_t hi) {
+  beta_ctx *c = (beta_ctx *)p;
+  for (int64_t j = lo; j < hi; j++) {
+    fe t = f_mul(c->r, c->src[j]);
+    c->B[2 * j] = f_sub(c->src[j], t);
+    c->B[2 * j + 1] = t;
+  }
+}
+void orc_precompute_beta(const uint64_t *r, int nr, uint64_t *Bout, int threads) {
+  int64_t n = (int64_t)1 << nr;
+  fe *B = (fe *)Bout;
+  fe *tmp = (fe *)malloc(sizeof(fe) * (size_t)(n / 2 + 1));
+  B[0] = f_one();
+  for (int i = 0; i < nr; i++) {
+    int64_t cnt = (int64_t)1 << i;
+    memcpy(tmp, B, sizeof(fe) * (size_t)cnt);
+    beta_ctx c = {B, tmp, ld(r, nr - 1 - i)};
+    parallel_for(cnt, threads, 1 << 14, beta_range, &c);
+  }
+  free(tmp);
+}
+
+/* evaluate_vector (utils.cpp:1201-1214): uses the first log2(n) of r. */
+void orc_evaluate_vector(const uint64_t *vin, int64_t n, const uint64_t *r, uint64_t out[2]) {
+  int lg = 0;
+  while (((int64_t)1 << (lg + 1)) <= n) lg++;
+  fe *v = (fe *)malloc(sizeof(fe) * (size_t)n);
+  memcpy(v, vin, sizeof(fe) * (size_t)n);
+  for (int i = 0; i < lg; i++) {
+    fe ri = ld(r, i), om = f_sub(f_one(), ri);
+    int64_t L = (int64_t)1 << (lg - 1 - i);
+    for (int64_t j = 0; j < L; j++) v[j] = f_add(f_mul(om, v[2 * j]), f_mul(ri, v[2 * j + 1]));
+  }
+  out[0] = v[0].re; out[1] = v[0].im;
+  free(v);
+}
+
+/* beta_identity (utils.cpp:1337-1343) */
+void orc_beta_identity(const uint64_t *r1, const uint64_t *r2, int nr, uint64_t out[2]) {
+  fe e = f_one();
+  for (int i = 0; i < nr; i++) {
+    fe a = ld(r1, i), b = ld(r2, i);
+    e = f_mul(e, f_add(f_mul(f_sub(f_one(), a), f_sub(f_one(), b)), f_mul(a, b)));
+  }
+  out[0] = e.re; out[1] = e.im;
+}
+
+/* ----------------------------------------------------------- sumcheck */
+/* Round message sum_j (a1 x + b1)(a2 x + b2), a = v[2j+1]-v[2j], b = v[2j]
+ * (linear_poly * linear_poly, polynomial.cpp; summed in
+ * coSumcheck_MPI.cpp:199 and Whir.cpp:215-221). */
+typedef struct { const fe *v1, *v2; fe part[256][3]; int64_t chunk; } sc_ctx;
+typedef struct { sc_ctx *c; } sc_arg;
+static void sc_range_core(const fe *v1, const fe *v2, int64_t lo, int64_t hi, fe acc[3]) {
+  fe A = f_zero(), Bc = f_zero(), C = f_zero();
+  for (int64_t j = lo; j < hi; j++) {
+    fe a1 = f_sub(v1[2 * j + 1], v1[2 * j]), b1 = v1[2 * j];
+    fe a2 = f_sub(v2[2 * j + 1], v2[2 * j]), b2 = v2[2 * j];
+    A = f_add(A, f_mul(a1, a2));
+    Bc = f_add(Bc, f_add(f_mul(a1, b2), f_mul(b1, a2)));
+    C = f_add(C, f_mul(b1, b2));
+  }
+  acc[0] = A; acc[1] = Bc; acc[2] = C;
+}
+typedef struct { const fe *v1, *v2; int64_t pairs; int nt; fe part[256][3]; } scp_ctx;
+static void scp_range(void *p, int64_t lo, int64_t hi) {
+  scp_ctx *c = (scp_ctx *)p;
+  for (int64_t t = lo; t < hi; t++) {
+    int64_t a = c->pairs * t / c->nt, b = c->pairs * (t + 1) / c->nt;
+    sc_range_core(c->v1, c->v2, a, b, c->part[t]);
+  }
+}
+void orc_sumcheck_quadratic(const uint64_t *v1, const uint64_t *v2, int64_t m, uint64_t out[6],
+                            int threads) {
+  int64_t pairs = m / 2;
+  int nt = resolve_threads(threads);
+  if (nt > 256) nt = 256;
+  if (pairs < ((int64_t)nt << 12)) nt = 1;
+  scp_ctx *c = (scp_ctx *)malloc(sizeof(scp_ctx));
+  c->v1 = (const fe *)v1; c->v2 = (const fe *)v2; c->pairs = pairs; c->nt = nt;
+  parallel_for(nt, nt, 1, scp_range, c);
+  fe acc[3] = {f_zero(), f_zero(), f_zero()};
+  for (int t = 0; t < nt; t++)
+    for (int k = 0; k < 3; k++) acc[k] = f_add(acc[k], c->part[t][k]);
+  for (int k = 0; k < 3; k++) { out[2 * k] = acc[k].re; out[2 * k + 1] = acc[k].im; }
+  free(c);
+}
+
+typedef struct { fe *v, *dst; fe r; } fold_ctx;
+static void fold_range(void *p, int64_t lo, int64_t hi) {
+  fold_ctx *c = (fold_ctx *)p;
+  for (int64_t j = lo; j < hi; j++)
+    c->dst[j] = f_add(f_mul(c->r, f_sub(c->v[2 * j + 1], c->v[2 * j])), c->v[2 * j]);
+}
+/* v[j] = r*(v[2j+1]-v[2j]) + v[2j] (coSumcheck_MPI.cpp:215-218). The
+ * in-place reference loop reads index 2j >= j only after writing j, so a
+ * copy through a scratch buffer gives the same result in parallel. */
+void orc_sumcheck_fold(uint64_t *vin, int64_t m, const uint64_t r[2], int threads) {
+  fe *v = (fe *)vin;
+  int64_t h = m / 2;
+  fe *tmp = (fe *)malloc(sizeof(fe) * (size_t)(h > 0 ? h : 1));
+  fold_ctx c = {v, tmp, f_make(r[0], r[1])};
+  parallel_for(h, threads, 1 << 14, fold_range, &c);
+  memcpy(v, tmp, sizeof(fe) * (size_t)h);
+  free(tmp);
+}
+
+/* ------------------------------------------------------------ RS folds */
+static int ilog2_64(int64_t x) { int l = 0; while (((int64_t)1 << (l + 1)) <= x) l++; return l; }
+
+/* get_RS_multifold_segment_tensor (coPCS_utils.cpp:333-383) */
+static fe rs_fold_tensor(const fe *seg, int logk, const fe *r, int64_t n, int64_t idx) {
+  int64_t k = (int64_t)1 << logk;
+  fe len_inv = f_inv(f_small(k));
+  int logn = ilog2_64(n);
+  fe om_inv = f_inv(f_rou(logn));
+  fe omega = f_pow(om_inv, (u128)(n / k));
+  fe inv_om = f_pow(om_inv, (u128)idx);
+  fe part[64];
+  int64_t seg_n = k;
+  fe one = f_one();
+  for (int64_t j = 0; j < seg_n / 2; j++) {
+    fe s = f_add(seg[j], seg[j + seg_n / 2]), d = f_sub(seg[j], seg[j + seg_n / 2]);
+    part[j] = f_add(f_mul(f_sub(one, r[0]), s), f_mul(f_mul(r[0], inv_om), d));
+    inv_om = f_mul(inv_om, omega);
+  }
+  if (logk > 1) {
+    fe pw[64];
+    pw[0] = one;
+    pw[1] = f_mul(om_inv, om_inv);
+    for (int i = 2; i < logk; i++) pw[i] = f_mul(pw[i - 1], pw[i - 1]);
+    for (int i = 1; i < logk; i++) pw[i] = f_pow(pw[i], (u128)(n / seg_n));
+    for (int i = 1; i < logk; i++) {
+      seg_n /= 2;
+      fe o = f_inv(f_rou(ilog2_64(n >> i)));
+      fe po = f_pow(o, (u128)idx);
+      for (int64_t j = 0; j < seg_n / 2; j++) {
+        fe s = f_add(part[j], part[j + seg_n / 2]), d = f_sub(part[j], part[j + seg_n / 2]);
+        part[j] = f_add(f_mul(f_sub(one, r[i]), s), f_mul(r[i], f_mul(po, d)));
+        po = f_mul(po, pw[i]);
+      }
+    }
+  }
+  return f_mul(len_inv, part[0]);
+}
+void orc_rs_fold_tensor(const uint64_t *segment, int logk, const uint64_t *r, int64_t n, int64_t idx,
+                        uint64_t out[2]) {
+  fe y = rs_fold_tensor((const fe *)segment, logk, (const fe *)r, n, idx);
+  out[0] = y.re; out[1] = y.im;
+}
+
+/* RS_multifold5 (coPCS_utils.cpp:386-437): each output i gathers the d
+ * entries cw[i + t*n/d] through log2(d) inverse-twiddled butterfly levels,
+ * then y_i = d^{-1} * sum_j a_j * partial_i[j]. */
+typedef struct { const fe *cw; int64_t n; const fe *a; int logd; fe *out; fe len_inv, om_inv; const fe *pw; } mf5_ctx;
+static void mf5_range(void *p, int64_t lo, int64_t hi) {
+  mf5_ctx *c = (mf5_ctx *)p;
+  int64_t d = (int64_t)1 << c->logd, n = c->n;
+  fe buf[2][64];
+  for (int64_t i = lo; i < hi; i++) {
+    /* level 0 pairs (j, j + n/2) for the d/2 indices j = i + t*n/d */
+    fe cur[64];
+    int64_t cnt = d / 2;
+    for (int64_t t = 0; t < cnt; t++) {
+      int64_t j = i + t * (n / d);
+      fe s = f_add(c->cw[j], c->cw[j + n / 2]);
+      fe df = f_mul(f_pow(c->om_inv, (u128)j), f_sub(c->cw[j], c->cw[j + n / 2]));
+      buf[0][2 * t] = s; buf[0][2 * t + 1] = df; /* partial[j] = {s, df} */
+    }
+    /* partial index for position j (t-th) is a vector of length 2; now
+     * merge levels: at level lv the vector for j (j < n/2^{lv+1}) takes
+     * partner j + n/2^{lv+1}. */
+    int64_t width = 2, groups = cnt; /* groups of `width` entries */
+    fe *src = buf[0], *dst = buf[1];
+    for (int lv = 1; lv < c->logd; lv++) {
+      int64_t ng = groups / 2;
+      int64_t nn = n >> lv; /* n after halving */
+      for (int64_t g = 0; g < ng; g++) {
+        int64_t j = i + g * (n / d); /* index of the kept vector */
+        int64_t e = j; /* pow_omega exponent = loop index j in the reference */
+        fe po = f_pow(c->pw[lv], (u128)e);
+        for (int64_t k = 0; k < width; k++) {
+          fe x = src[g * width + k], y = src[(g + ng) * width + k];
+          dst[g * 2 * width + k] = f_add(x, y);
+          dst[g * 2 * width + k + width] = f_mul(po, f_sub(x, y));
+        }
+        (void)nn;
+      }
+      width *= 2;
+      groups = ng;
+      fe *t = src; src = dst; dst = t;
+    }
+    fe acc = f_zero();
+    for (int64_t k = 0; k < d; k++) acc = f_add(acc, f_mul(c->a[k], src[k]));
+    cur[0] = f_mul(acc, c->len_inv);
+    c->out[i] = cur[0];
+  }
+}
+void orc_rs_multifold5(const uint64_t *codeword, int64_t n, const uint64_t *a, int logd, uint64_t *out,
+                       int threads) {
+  int64_t d = (int64_t)1 << logd;
+  fe om_inv = f_inv(f_rou(ilog2_64(n)));
+  fe pw[64];
+  pw[0] = f_one();
+  if (logd > 1) pw[1] = f_mul(om_inv, om_inv);
+  for (int i = 2; i < logd; i++) pw[i] = f_mul(pw[i - 1], pw[i - 1]);
+  mf5_ctx c = {(const fe *)codeword, n, (const fe *)a, logd, (fe *)out, f_inv(f_small(d)), om_inv, pw};
+  parallel_for(n / d, threads, 1 << 10, mf5_range, &c);
+}
+
+/* ------------------------------------------------------- update_betas */
+typedef struct { fe *b; const fe *w, *c; int l; } ub_ctx;
+static void ub_range(void *p, int64_t lo, int64_t hi) {
+  ub_ctx *c = (ub_ctx *)p;
+  for (int i = 0; i < c->l; i++) {
+    fe x = f_mul(c->c[i], f_pow(c->w[i], (u128)lo));
+    for (int64_t j = lo; j < hi; j++) {
+      c->b[j] = f_add(c->b[j], x);
+      x = f_mul(x, c->w[i]);
+    }
+  }
+}
+/* update_betas (Whir.cpp:325-342) with compute_powers_vector (:316-323):
+ * b[j] += c_i * (omega_N^{q_i})^j; the sum over i is exact, so grouping
+ * the additions per j-range instead of per query gives the same values. */
+void orc_update_betas(uint64_t *b, int64_t nb, const int32_t *queries, int l, int64_t N, const uint64_t r[2],
+                      uint64_t *challenges_out, int threads) {
+  fe rr = f_make(r[0], r[1]);
+  fe *c = (fe *)malloc(sizeof(fe) * (size_t)(l > 0 ? l : 1));
+  fe *w = (fe *)malloc(sizeof(fe) * (size_t)(l > 0 ? l : 1));
+  fe om = f_rou(ilog2_64(N));
+  for (int i = 0; i < l; i++) {
+    c[i] = i == 0 ? rr : f_mul(c[i - 1], rr);
+    w[i] = f_pow(om, (u128)(uint32_t)queries[i]);
+    if (challenges_out) st(challenges_out, i, c[i]);
+  }
+  ub_ctx u = {(fe *)b, w, c, l};
+  parallel_for(nb, threads, 1 << 10, ub_range, &u);
+  free(c);
+  free(w);
+}
+
+int orc_whir_queries(int rate) {
+  return (int)(-100.0 / log2(sqrt(1.0 / (double)rate)));
+}
+
+/* --------------------------------------------------------- transcript */
+enum {
+  T_COMMIT_ROOT = 1, T_EVAL_POINT = 2, T_CLAIM = 3, T_SC_POLY = 4, T_SC_CHALLENGE = 5,
+  T_SC_FINAL = 6, T_WHIR_POLY = 7, T_WHIR_CHALLENGE = 8, T_WHIR_ROOT = 9,
+  T_WHIR_QUERIES = 10, T_WHIR_REPLIES = 11, T_WHIR_ANSWERS = 12, T_WHIR_PATHS = 13,
+  T_WHIR_COMBINE = 14, T_WHIR_K = 15, T_FINAL_POLY = 16, T_FINAL_POINT = 17,
+  T_FINAL_EVAL = 18
+};
+
+typedef struct { uint8_t *p; int64_t len, cap; int bad; } tw_t;
+static uint8_t *tw_rec(tw_t *t, uint32_t tag, uint32_t count, size_t unit) {
+  int64_t need = 8 + (int64_t)unit * count;
+  if (t->bad || t->len + need > t->cap) { t->bad = 1; t->len += need; return NULL; }
+  uint8_t *o = t->p + t->len;
+  memcpy(o, &tag, 4);
+  memcpy(o + 4, &count, 4);
+  t->len += need;
+  return o + 8;
+}
+static void tw_fe(tw_t *t, uint32_t tag, const fe *v, uint32_t count) {
+  uint8_t *o = tw_rec(t, tag, count, 16);
+  if (o) for (uint32_t i = 0; i < count; i++) fe_bytes(v[i], o + 16 * i);
+}
+static void tw_raw(tw_t *t, uint32_t tag, const void *v, uint32_t count, size_t unit) {
+  uint8_t *o = tw_rec(t, tag, count, unit);
+  if (o) memcpy(o, v, unit * count);
+}
+
+static fe quad_eval(const fe h[3], fe x) { /* ((a x) + b) x + c */
+  return f_add(f_mul(f_add(f_mul(h[0], x), h[1]), x), h[2]);
+}
+
+/* Whir_Commit_initial (Whir.cpp:158-190): codeword = pfft(arr padded to
+ * rate*|arr|), tree = MT_commit_Blake(codeword). */
+static void whir_commit(const fe *arr, int64_t m, int rate, fe **cw_out, uint8_t **tree_out, int threads) {
+  int64_t L = m * rate;
+  fe *cw = (fe *)calloc((size_t)L, sizeof(fe));
+  memcpy(cw, arr, sizeof(fe) * (size_t)m);
+  orc_fft((uint64_t *)cw, ilog2_64(L), 0, threads);
+  uint8_t *tree = (uint8_t *)malloc((size_t)32 * (size_t)(L / 2 > 1 ? L / 2 : 1));
+  orc_merkle_commit((const uint64_t *)cw, L, tree, threads);
+  *cw_out = cw;
+  *tree_out = tree;
+}
+static const uint8_t *tree_root(const uint8_t *tree, int64_t L) {
+  return tree + 32 * (L / 2 - 2); /* (L/2 - 1) hashes, root last */
+}
+
+int64_t orc_transcript_bytes(int logn, int rate) {
+  /* Exact length of orc_prove's record sequence. */
+  int64_t n = (int64_t)1 << logn;
+  int64_t bytes = 0;
+  bytes += 8 + 32 + 8 + 16 * logn + 8 + 16;           /* root, point, claim */
+  bytes += (int64_t)logn * (8 + 48 + 8 + 16) + 8 + 32; /* sumcheck */
+  int64_t m = n, L = n * rate;
+  int cur = rate;
+  for (;;) {
+    bytes += 2 * (8 + 48 + 8 + 16) + 8 + 32;
+    int l = orc_whir_queries(cur);
+    int depth = ilog2_64(L / 4);
+    bytes += 8 + 4 * l + 8 + 64 * l + 8 + 16 * l + 8 + 32 * (int64_t)l * depth + 8 + 16 * l + 8 + 16;
+    m /= 4;
+    L = m * 2 * cur;
+    cur *= 2;
+    if (m <= 4) break;
+  }
+  bytes += 8 + 16 * m + 8 + 16 * (int64_t)ilog2_64(m) + 8 + 16;
+  return bytes;
+}
+
+void orc_witness(uint64_t seed, int64_t n, uint64_t *out) {
+  uint64_t s = seed;
+  for (int64_t i = 0; i < n; i++) {
+    uint64_t v;
+    do {
+      uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+      z ^= z >> 31;
+      v = z >> 3;
+    } while (v == P);
+    out[2 * i] = v;
+    out[2 * i + 1] = 0;
+  }
+}
+
+/* The plain single-party prover (restating oracle/ref/ref_driver.cpp
+ * cmd_prove, which calls the reference's Whir_Commit_initial, hash_to_field,
+ * precompute_beta, the _quadratic_cosumcheck round body, whir_sumcheck_step1/2,
+ * whir_query, open_tree_blake, update_betas, evaluate_vector). */
+int64_t orc_prove(const uint64_t *witness, int logn, int rate, uint32_t prng_seed, uint8_t *transcript,
+                  int64_t cap, int threads) {
+  const int whir_k = 4, logk = 2;
+  if (logn < 3 || logn > 30 || rate < 2 || (rate & (rate - 1))) return -1;
+  int64_t n = (int64_t)1 << logn;
+  tw_t tw = {transcript, 0, cap, 0};
+  orc_prng g;
+  orc_prng_seed(&g, prng_seed);
+  fe fs = f_zero();
+  const fe *w = (const fe *)witness;
+
+  /* 1. commitment */
+  fe *cw;
+  uint8_t *tree;
+  whir_commit(w, n, rate, &cw, &tree, threads);
+  int64_t L = n * rate;
+  tw_raw(&tw, T_COMMIT_ROOT, tree_root(tree, L), 1, 32);
+
+  /* 2. evaluation point z_i = hash_to_field({0}) (main.cpp:83-85) */
+  fe *z = (fe *)malloc(sizeof(fe) * (size_t)logn);
+  fe zero = f_zero();
+  for (int i = 0; i < logn; i++) z[i] = fs_absorb(&fs, &zero, 1);
+  tw_fe(&tw, T_EVAL_POINT, z, (uint32_t)logn);
+  fe *v1 = (fe *)malloc(sizeof(fe) * (size_t)n), *v2 = (fe *)malloc(sizeof(fe) * (size_t)n);
+  orc_precompute_beta((const uint64_t *)z, logn, (uint64_t *)v2, threads);
+  memcpy(v1, w, sizeof(fe) * (size_t)n);
+
+  /* 3. sumcheck of sum_x w(x) eq(z, x) with Fiat-Shamir challenges */
+  fe *chal = (fe *)malloc(sizeof(fe) * (size_t)logn);
+  fe y = f_zero();
+  int64_t m = n;
+  for (int i = 0; i < logn; i++) {
+    uint64_t H6[6];
+    orc_sumcheck_quadratic((const uint64_t *)v1, (const uint64_t *)v2, m, H6, threads);
+    fe H[3] = {f_make(H6[0], H6[1]), f_make(H6[2], H6[3]), f_make(H6[4], H6[5])};
+    if (i == 0) {
+      y = f_add(quad_eval(H, f_zero()), quad_eval(H, f_one()));
+      tw_fe(&tw, T_CLAIM, &y, 1);
+    }
+    tw_fe(&tw, T_SC_POLY, H, 3);
+    chal[i] = fs_absorb(&fs, H, 3);
+    tw_fe(&tw, T_SC_CHALLENGE, &chal[i], 1);
+    y = quad_eval(H, chal[i]);
+    uint64_t c2[2] = {chal[i].re, chal[i].im};
+    orc_sumcheck_fold((uint64_t *)v1, m, c2, threads);
+    orc_sumcheck_fold((uint64_t *)v2, m, c2, threads);
+    m /= 2;
+  }
+  fe fin[2] = {v1[0], v2[0]};
+  tw_fe(&tw, T_SC_FINAL, fin, 2);
+
+  /* 4. WHIR open of (v1[0], chal) with whir_k = 4 (Whir_Open, Whir.cpp:388-467) */
+  fe K = v1[0];
+  fe *b = v2; /* reuse: b = precompute_beta(chal) */
+  orc_precompute_beta((const uint64_t *)chal, logn, (uint64_t *)b, threads);
+  fe *arr = v1;
+  memcpy(arr, w, sizeof(fe) * (size_t)n);
+  m = n;
+  int cur = rate;
+  for (;;) {
+    fe r[2];
+    for (int i = 0; i < logk; i++) {
+      uint64_t H6[6];
+      orc_sumcheck_quadratic((const uint64_t *)arr, (const uint64_t *)b, m, H6, threads);
+      fe h[3] = {f_make(H6[0], H6[1]), f_make(H6[2], H6[3]), f_make(H6[4], H6[5])};
+      tw_fe(&tw, T_WHIR_POLY, h, 3);
+      r[i] = prng_field(&g);
+      tw_fe(&tw, T_WHIR_CHALLENGE, &r[i], 1);
+      K = quad_eval(h, r[i]);
+      uint64_t c2[2] = {r[i].re, r[i].im};
+      orc_sumcheck_fold((uint64_t *)arr, m, c2, threads);
+      orc_sumcheck_fold((uint64_t *)b, m, c2, threads);
+      m /= 2;
+    }
+    fe *ncw;
+    uint8_t *ntree;
+    whir_commit(arr, m, 2 * cur, &ncw, &ntree, threads);
+    int64_t NL = m * 2 * cur;
+    tw_raw(&tw, T_WHIR_ROOT, tree_root(ntree, NL), 1, 32);
+
+    /* whir_query (Whir.cpp:251-314) on the previous codeword */
+    int l = orc_whir_queries(cur);
+    int32_t *q = (int32_t *)malloc(sizeof(int32_t) * (size_t)l);
+    for (int i = 0; i < l; i++) q[i] = orc_prng_next(&g) % (int32_t)(L / 4); /* whir_k <= 4 */
+    tw_raw(&tw, T_WHIR_QUERIES, q, (uint32_t)l, 4);
+    fe *rep = (fe *)malloc(sizeof(fe) * (size_t)l * whir_k);
+    fe *ans = (fe *)malloc(sizeof(fe) * (size_t)l);
+    for (int i = 0; i < l; i++) {
+      for (int j = 0; j < whir_k; j++) rep[i * whir_k + j] = cw[q[i] + j * (L / whir_k)];
+      ans[i] = rs_fold_tensor(rep + i * whir_k, logk, r, L, q[i]);
+    }
+    tw_fe(&tw, T_WHIR_REPLIES, rep, (uint32_t)(l * whir_k));
+    tw_fe(&tw, T_WHIR_ANSWERS, ans, (uint32_t)l);
+    int depth = ilog2_64(L / 4);
+    uint8_t *paths = (uint8_t *)malloc((size_t)32 * (size_t)l * (size_t)(depth > 0 ? depth : 1));
+    for (int i = 0; i < l; i++) orc_merkle_open(tree, L, q[i], paths + (size_t)32 * depth * i);
+    tw_raw(&tw, T_WHIR_PATHS, paths, (uint32_t)(l * depth), 32);
+    free(paths);
+    free(rep);
+
+    /* queries scaled to the new codeword (Whir.cpp:371-372), update_betas */
+    for (int i = 0; i < l; i++) q[i] = q[i] * (int32_t)(whir_k * NL / L);
+    free(cw);
+    free(tree);
+    cw = ncw;
+    tree = ntree;
+    L = NL;
+    fe rb = prng_field(&g);
+    fe *ch = (fe *)malloc(sizeof(fe) * (size_t)l);
+    uint64_t rb2[2] = {rb.re, rb.im};
+    orc_update_betas((uint64_t *)b, m, q, l, L, rb2, (uint64_t *)ch, threads);
+    tw_fe(&tw, T_WHIR_COMBINE, ch, (uint32_t)l);
+    for (int i = 0; i < l; i++) K = f_add(K, f_mul(ch[i], ans[i]));
+    tw_fe(&tw, T_WHIR_K, &K, 1);
+    free(ch);
+    free(ans);
+    free(q);
+    cur *= 2;
+    if (m <= whir_k) break;
+  }
+  tw_fe(&tw, T_FINAL_POLY, arr, (uint32_t)m);
+  int lgm = ilog2_64(m);
+  fe rf[8];
+  for (int i = 0; i < lgm; i++) rf[i] = prng_field(&g);
+  tw_fe(&tw, T_FINAL_POINT, rf, (uint32_t)lgm);
+  uint64_t ev[2];
+  orc_evaluate_vector((const uint64_t *)b, m, (const uint64_t *)rf, ev);
+  fe e = f_make(ev[0], ev[1]);
+  tw_fe(&tw, T_FINAL_EVAL, &e, 1);
+
+  free(cw);
+  free(tree);
+  free(z);
+  free(chal);
+  free(v1);
+  free(v2);
+  return tw.bad ? -1 : tw.len;
+}

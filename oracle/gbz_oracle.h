@@ -1,0 +1,98 @@
+/*
+ * gbz_oracle — CPU restatement of the reference prover's hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker the GPU path is
+ * compared against (tests/, __graft_entry__.smoke()) and the CPU baseline
+ * that bench.py times.  The product (libgbz) never links or calls it.
+ *
+ * Parity is pinned: tests/test_oracle_golden.py compares every function
+ * here with golden vectors written by the unmodified reference sources
+ * (oracle/ref/ref_driver.cpp, generated by tests/golden/make_golden.py).
+ *
+ * Field elements are two uint64 words, `real` then `img`, exactly the
+ * memory layout of virgo::fieldElement (fieldElement.hpp:96-97).
+ */
+#ifndef GBZ_ORACLE_H
+#define GBZ_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* glibc random()/rand() replica (TYPE_3 additive feedback generator). */
+typedef struct {
+  int32_t tbl[31];
+  int f, r;
+} orc_prng;
+
+void orc_prng_seed(orc_prng *g, uint32_t seed);
+int32_t orc_prng_next(orc_prng *g);
+/* F::_random (fieldElement.cpp:119-125, 363-368). */
+void orc_prng_field(orc_prng *g, uint64_t out[2]);
+
+/* Field F_{p^2}, p = 2^61-1 (fieldElement.cpp:34-103, 337-361). */
+void orc_field_ops(int64_t n, const uint64_t *a, const uint64_t *b, uint64_t *add,
+                   uint64_t *sub, uint64_t *mul, uint64_t *neg, uint64_t *inv);
+void orc_root_of_unity(int log_order, uint64_t out[2]);
+
+/* BLAKE3 of exactly 64 bytes (Blake3_hash.cpp:5-10). */
+void orc_blake3_64(int64_t count, const uint8_t *in, uint8_t *out);
+
+/* fft (utils.cpp:904-964); pfft (utils.cpp:1583-1673) computes the same
+ * forward transform.  threads <= 0 means "all online cores". */
+void orc_fft(uint64_t *a, int logn, int inverse, int threads);
+
+/* MT_commit_Blake (merkle_tree.cpp:195-233) + create_tree_blake (:267-299).
+ * levels_out holds level 0 (N/4 leaf hashes) then each upper level, 32 B
+ * per hash, (N/2 - 1) hashes in total.  Requires N >= 4. */
+int orc_merkle_commit(const uint64_t *elems, int64_t N, uint8_t *levels_out, int threads);
+/* open_tree_blake (merkle_tree.cpp:320-335): depth = log2(N/4) hashes. */
+int orc_merkle_open(const uint8_t *levels, int64_t N, int64_t pos, uint8_t *path_out);
+
+/* Fiat-Shamir (Fiat_Shamir.cpp:8-34).  state holds prev_challenge. */
+void orc_hash_F(const uint64_t x[2], const uint64_t y[2], uint64_t out[2]);
+void orc_hash_to_field(uint64_t state[2], const uint64_t *elems, int count, uint64_t out[2]);
+
+/* precompute_beta (utils.cpp:198-243), evaluate_vector (:1201-1214),
+ * beta_identity (:1337-1343). */
+void orc_precompute_beta(const uint64_t *r, int nr, uint64_t *B, int threads);
+void orc_evaluate_vector(const uint64_t *v, int64_t n, const uint64_t *r, uint64_t out[2]);
+void orc_beta_identity(const uint64_t *r1, const uint64_t *r2, int nr, uint64_t out[2]);
+
+/* One quadratic sumcheck round message over pairs (coSumcheck_MPI.cpp:199,
+ * Whir.cpp:215-221): out = (a, b, c) of sum_j (v1-line)(v2-line). */
+void orc_sumcheck_quadratic(const uint64_t *v1, const uint64_t *v2, int64_t m, uint64_t out[6],
+                            int threads);
+/* Fold v[j] = r*(v[2j+1]-v[2j]) + v[2j] for j < m/2, in place. */
+void orc_sumcheck_fold(uint64_t *v, int64_t m, const uint64_t r[2], int threads);
+
+/* get_RS_multifold_segment_tensor (coPCS_utils.cpp:333-383). */
+void orc_rs_fold_tensor(const uint64_t *segment, int logk, const uint64_t *r, int64_t n,
+                        int64_t idx, uint64_t out[2]);
+/* RS_multifold5 (coPCS_utils.cpp:386-437): codeword len n -> n/d. */
+void orc_rs_multifold5(const uint64_t *codeword, int64_t n, const uint64_t *a, int logd,
+                       uint64_t *out, int threads);
+
+/* update_betas (Whir.cpp:316-342) given the drawn r: b[j] += c_i * w_i^j,
+ * c_i = r^(i+1), w_i = omega_N^{q_i}.  challenges_out gets the l c_i. */
+void orc_update_betas(uint64_t *b, int64_t nb, const int32_t *queries, int l, int64_t N,
+                      const uint64_t r[2], uint64_t *challenges_out, int threads);
+
+/* WHIR query count (Whir.cpp:253-258, conjectured_security = false). */
+int orc_whir_queries(int rate);
+
+/* The plain single-party prover transcript (see oracle/ref/ref_driver.cpp
+ * cmd_prove for the call sequence it restates).  Returns the number of
+ * bytes written, or -1 when cap is too small / arguments are invalid. */
+int64_t orc_transcript_bytes(int logn, int rate);
+int64_t orc_prove(const uint64_t *witness, int logn, int rate, uint32_t prng_seed,
+                  uint8_t *transcript, int64_t cap, int threads);
+
+/* SplitMix64 witness generator shared by tests and bench. */
+void orc_witness(uint64_t seed, int64_t n, uint64_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

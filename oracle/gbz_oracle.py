@@ -1,0 +1,248 @@
+"""ctypes binding for the CPU oracle (oracle/gbz_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker.  The product never imports it.
+
+Field elements travel as numpy uint64 arrays of shape (n, 2): column 0 is
+`real`, column 1 is `img` (virgo::fieldElement layout).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libgbz_oracle.so")
+SRC = os.path.join(HERE, "gbz_oracle.c")
+
+P = (1 << 61) - 1
+
+
+def build(force=False):
+    """Compile the oracle with gcc (portable C11 + pthreads; x86-64 and Arm)."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.run(["gcc", "-O3", "-std=gnu11", "-fPIC", "-shared", "-o", tmp, SRC, "-lpthread", "-lm"],
+                   check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class _Prng(ctypes.Structure):
+    _fields_ = [("tbl", ctypes.c_int32 * 31), ("f", ctypes.c_int), ("r", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(build())
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        u8p = ctypes.POINTER(ctypes.c_uint8)
+        i64 = ctypes.c_int64
+        L.orc_prng_next.restype = ctypes.c_int32
+        L.orc_merkle_commit.restype = ctypes.c_int
+        L.orc_merkle_open.restype = ctypes.c_int
+        L.orc_whir_queries.restype = ctypes.c_int
+        L.orc_transcript_bytes.restype = i64
+        L.orc_transcript_bytes.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.orc_prove.restype = i64
+        L.orc_prove.argtypes = [u64p, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, u8p, i64, ctypes.c_int]
+        L.orc_fft.argtypes = [u64p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_merkle_commit.argtypes = [u64p, i64, u8p, ctypes.c_int]
+        L.orc_merkle_open.argtypes = [u8p, i64, i64, u8p]
+        L.orc_witness.argtypes = [ctypes.c_uint64, i64, u64p]
+        _lib = L
+    return _lib
+
+
+def _p64(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+
+
+def _p8(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+
+def fe_array(n):
+    return np.zeros((n, 2), dtype=np.uint64)
+
+
+def witness(seed, n):
+    out = fe_array(n)
+    lib().orc_witness(ctypes.c_uint64(seed), n, _p64(out))
+    return out
+
+
+def field_ops(a, b):
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    n = a.shape[0]
+    outs = [fe_array(n) for _ in range(5)]
+    lib().orc_field_ops(ctypes.c_int64(n), _p64(a), _p64(b), *[_p64(o) for o in outs])
+    return outs  # add, sub, mul, neg, inv
+
+
+def root_of_unity(log_order):
+    out = np.zeros(2, dtype=np.uint64)
+    lib().orc_root_of_unity(log_order, _p64(out))
+    return out
+
+
+def blake3_64(blocks):
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 64)
+    out = np.zeros((blocks.shape[0], 32), dtype=np.uint8)
+    lib().orc_blake3_64(ctypes.c_int64(blocks.shape[0]), _p8(blocks), _p8(out))
+    return out
+
+
+def fft(a, inverse=False, threads=0):
+    a = np.array(a, dtype=np.uint64, copy=True).reshape(-1, 2)
+    logn = int(a.shape[0]).bit_length() - 1
+    lib().orc_fft(_p64(a), logn, int(inverse), threads)
+    return a
+
+
+def merkle_commit(elems, threads=0):
+    elems = np.ascontiguousarray(elems, dtype=np.uint64).reshape(-1, 2)
+    N = elems.shape[0]
+    out = np.zeros((max(N // 2 - 1, 1), 32), dtype=np.uint8)
+    rc = lib().orc_merkle_commit(_p64(elems), N, _p8(out), threads)
+    if rc != 0:
+        raise ValueError("merkle_commit needs a power-of-two length >= 4")
+    return out
+
+
+def merkle_open(levels, N, pos):
+    levels = np.ascontiguousarray(levels, dtype=np.uint8)
+    depth = (N // 4).bit_length() - 1
+    out = np.zeros((max(depth, 1), 32), dtype=np.uint8)
+    d = lib().orc_merkle_open(_p8(levels), N, pos, _p8(out))
+    if d < 0:
+        raise ValueError("position out of range")
+    return out[:d]
+
+
+def hash_F(x, y):
+    x = np.ascontiguousarray(x, dtype=np.uint64)
+    y = np.ascontiguousarray(y, dtype=np.uint64)
+    out = np.zeros(2, dtype=np.uint64)
+    lib().orc_hash_F(_p64(x), _p64(y), _p64(out))
+    return out
+
+
+def hash_to_field(state, elems):
+    elems = np.ascontiguousarray(elems, dtype=np.uint64).reshape(-1, 2)
+    out = np.zeros(2, dtype=np.uint64)
+    lib().orc_hash_to_field(_p64(state), _p64(elems), ctypes.c_int(elems.shape[0]), _p64(out))
+    return out
+
+
+class Prng:
+    """glibc random()/rand() replica; F::_random via field()."""
+
+    def __init__(self, seed=1):
+        self.s = _Prng()
+        lib().orc_prng_seed(ctypes.byref(self.s), ctypes.c_uint32(seed))
+
+    def next(self):
+        return lib().orc_prng_next(ctypes.byref(self.s))
+
+    def field(self):
+        out = np.zeros(2, dtype=np.uint64)
+        lib().orc_prng_field(ctypes.byref(self.s), _p64(out))
+        return out
+
+
+def precompute_beta(r, threads=0):
+    r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+    out = fe_array(1 << r.shape[0])
+    lib().orc_precompute_beta(_p64(r), ctypes.c_int(r.shape[0]), _p64(out), ctypes.c_int(threads))
+    return out
+
+
+def evaluate_vector(v, r):
+    v = np.ascontiguousarray(v, dtype=np.uint64).reshape(-1, 2)
+    r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+    out = np.zeros(2, dtype=np.uint64)
+    lib().orc_evaluate_vector(_p64(v), ctypes.c_int64(v.shape[0]), _p64(r), _p64(out))
+    return out
+
+
+def beta_identity(r1, r2):
+    r1 = np.ascontiguousarray(r1, dtype=np.uint64).reshape(-1, 2)
+    r2 = np.ascontiguousarray(r2, dtype=np.uint64).reshape(-1, 2)
+    out = np.zeros(2, dtype=np.uint64)
+    lib().orc_beta_identity(_p64(r1), _p64(r2), ctypes.c_int(r1.shape[0]), _p64(out))
+    return out
+
+
+def sumcheck_quadratic(v1, v2, threads=0):
+    v1 = np.ascontiguousarray(v1, dtype=np.uint64).reshape(-1, 2)
+    v2 = np.ascontiguousarray(v2, dtype=np.uint64).reshape(-1, 2)
+    out = np.zeros(6, dtype=np.uint64)
+    lib().orc_sumcheck_quadratic(_p64(v1), _p64(v2), ctypes.c_int64(v1.shape[0]), _p64(out),
+                                 ctypes.c_int(threads))
+    return out.reshape(3, 2)
+
+
+def sumcheck_fold(v, r, threads=0):
+    v = np.array(v, dtype=np.uint64, copy=True).reshape(-1, 2)
+    r = np.ascontiguousarray(r, dtype=np.uint64)
+    lib().orc_sumcheck_fold(_p64(v), ctypes.c_int64(v.shape[0]), _p64(r), ctypes.c_int(threads))
+    return v[: v.shape[0] // 2].copy()
+
+
+def rs_fold_tensor(segment, r, n, idx):
+    segment = np.ascontiguousarray(segment, dtype=np.uint64).reshape(-1, 2)
+    r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+    logk = segment.shape[0].bit_length() - 1
+    out = np.zeros(2, dtype=np.uint64)
+    lib().orc_rs_fold_tensor(_p64(segment), ctypes.c_int(logk), _p64(r), ctypes.c_int64(n),
+                             ctypes.c_int64(idx), _p64(out))
+    return out
+
+
+def rs_multifold5(codeword, a, threads=0):
+    codeword = np.ascontiguousarray(codeword, dtype=np.uint64).reshape(-1, 2)
+    a = np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2)
+    logd = a.shape[0].bit_length() - 1
+    out = fe_array(codeword.shape[0] >> logd)
+    lib().orc_rs_multifold5(_p64(codeword), ctypes.c_int64(codeword.shape[0]), _p64(a), ctypes.c_int(logd),
+                            _p64(out), ctypes.c_int(threads))
+    return out
+
+
+def update_betas(b, queries, N, r, threads=0):
+    b = np.array(b, dtype=np.uint64, copy=True).reshape(-1, 2)
+    q = np.ascontiguousarray(queries, dtype=np.int32)
+    r = np.ascontiguousarray(r, dtype=np.uint64)
+    ch = fe_array(len(q))
+    lib().orc_update_betas(_p64(b), ctypes.c_int64(b.shape[0]), q.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                           ctypes.c_int(len(q)), ctypes.c_int64(N), _p64(r), _p64(ch), ctypes.c_int(threads))
+    return b, ch
+
+
+def whir_queries(rate):
+    return lib().orc_whir_queries(ctypes.c_int(rate))
+
+
+def transcript_bytes(logn, rate):
+    return lib().orc_transcript_bytes(logn, rate)
+
+
+def prove(w, logn, rate, prng_seed=1, threads=0):
+    w = np.ascontiguousarray(w, dtype=np.uint64).reshape(-1, 2)
+    assert w.shape[0] == 1 << logn
+    cap = transcript_bytes(logn, rate)
+    out = np.zeros(cap, dtype=np.uint8)
+    n = lib().orc_prove(_p64(w), logn, rate, prng_seed, _p8(out), cap, threads)
+    if n < 0:
+        raise ValueError("oracle prove failed")
+    return out[:n].tobytes()

@@ -1,0 +1,547 @@
+// extern "C" entry points of libgbz (declared in include/gbz.h).
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <utility>
+
+#include "../../include/gbz.h"
+#include "gbz_prover.cuh"
+
+using namespace gbz;
+
+struct gbz_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string last_error;
+  std::map<int, std::pair<void *, uint64_t>> scratch;
+  std::map<int, NttTables> ntt;
+  std::map<std::pair<int, int>, std::unique_ptr<ProofPlan>> plans;
+  ProofState *st = nullptr;
+  fe *ub_scratch = nullptr;
+  bool profiling = false;
+  std::map<std::pair<int, int>, std::unique_ptr<Profiler>> profilers;
+
+  void *buf(int slot, uint64_t bytes) {
+    auto &e = scratch[slot];
+    if (e.second < bytes) {
+      if (e.first) GBZ_CUDA(cudaFree(e.first));
+      e.first = nullptr;
+      e.second = 0;
+      GBZ_CUDA(cudaMalloc(&e.first, bytes ? bytes : 16));
+      e.second = bytes;
+    }
+    return e.first;
+  }
+  NttTables &tables(int lg) {
+    auto it = ntt.find(lg);
+    if (it != ntt.end()) return it->second;
+    NttTables t;
+    ntt_tables_build(t, lg);
+    return ntt.emplace(lg, t).first->second;
+  }
+};
+
+namespace {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) GBZ_CUDA(cudaSetDevice(dev));
+  }
+  ~DeviceGuard() {
+    int cur;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+gbz_status fail(gbz_ctx *ctx, gbz_status code, const std::string &msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+#define API_BEGIN(ctx)                                    \
+  if (!(ctx)) return GBZ_EINVAL;                          \
+  try {                                                   \
+    DeviceGuard guard_((ctx)->device);
+#define API_END(ctx)                                                                    \
+  }                                                                                     \
+  catch (const ArgError &e) {                                                           \
+    return fail(ctx, GBZ_EINVAL, e.what);                                               \
+  }                                                                                     \
+  catch (const CudaError &e) {                                                          \
+    return fail(ctx, e.err == cudaErrorMemoryAllocation ? GBZ_ENOMEM : GBZ_ECUDA, e.what); \
+  }                                                                                     \
+  catch (const std::bad_alloc &) {                                                      \
+    return fail(ctx, GBZ_ENOMEM, "host allocation failed");                              \
+  }                                                                                     \
+  return GBZ_OK;
+
+void check_mem(int mem) {
+  if (mem != GBZ_MEM_HOST && mem != GBZ_MEM_DEVICE) throw ArgError("mem must be GBZ_MEM_HOST or GBZ_MEM_DEVICE");
+}
+void need(const void *p, const char *what) {
+  if (!p) throw ArgError(std::string("null pointer: ") + what);
+}
+void check_pow2(uint64_t n, const char *what) {
+  if (!is_pow2(n)) throw ArgError(std::string(what) + " must be a power of two");
+}
+
+// Device view of a caller buffer: the pointer itself (device memory) or a
+// scratch copy (host memory), copied in when `in`.
+template <typename T>
+T *dev_view(gbz_ctx *ctx, int slot, T *p, uint64_t bytes, int mem, bool in) {
+  if (mem == GBZ_MEM_DEVICE) return p;
+  T *d = (T *)ctx->buf(slot, bytes);
+  if (in && bytes) GBZ_CUDA(cudaMemcpyAsync((void *)d, (const void *)p, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return d;
+}
+template <typename T>
+void copy_out(gbz_ctx *ctx, T *host, const T *dev, uint64_t bytes, int mem) {
+  if (mem == GBZ_MEM_DEVICE || !bytes) return;
+  GBZ_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+}
+void finish(gbz_ctx *ctx, int mem) {
+  if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+__global__ void field_ops_kernel(const fe *a, const fe *b, uint64_t n, fe *s, fe *d, fe *p) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  fe x = a[i], y = b[i];
+  if (s) s[i] = fadd(x, y);
+  if (d) d[i] = fsub(x, y);
+  if (p) p[i] = fmul(x, y);
+}
+
+// comb_i = r^(i+1), omega_q[i] = omega_N^{q_i}.
+__global__ void ub_prep_kernel(ProofState *st, const int32_t *q, int l, int logN, fe r) {
+  if (threadIdx.x == 0) {
+    fe c = r;
+    for (int i = 0; i < l; i++) {
+      st->comb[i] = c;
+      c = fmul(c, r);
+    }
+  }
+  const fe om = root_of_unity(logN);
+  for (int i = threadIdx.x; i < l; i += blockDim.x) st->omega_q[i] = fpow(om, (uint64_t)(uint32_t)q[i]);
+}
+
+}  // namespace
+
+extern "C" {
+
+gbz_status gbz_create(gbz_ctx **out, int device) {
+  if (!out) return GBZ_EINVAL;
+  *out = nullptr;
+  gbz_ctx *ctx = new (std::nothrow) gbz_ctx();
+  if (!ctx) return GBZ_ENOMEM;
+  ctx->device = device;
+  try {
+    DeviceGuard g(device);
+    GBZ_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    ctx->own_stream = true;
+  } catch (const CudaError &e) {
+    delete ctx;
+    return GBZ_ECUDA;
+  }
+  *out = ctx;
+  return GBZ_OK;
+}
+
+void gbz_destroy(gbz_ctx *ctx) {
+  if (!ctx) return;
+  try {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->plans.clear();
+    ctx->profilers.clear();
+    for (auto &kv : ctx->ntt) ntt_tables_free(kv.second);
+    for (auto &kv : ctx->scratch) cudaFree(kv.second.first);
+    cudaFree(ctx->st);
+    cudaFree(ctx->ub_scratch);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  } catch (...) {
+  }
+  delete ctx;
+}
+
+gbz_status gbz_set_stream(gbz_ctx *ctx, void *stream) {
+  API_BEGIN(ctx)
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (ctx->own_stream) GBZ_CUDA(cudaStreamDestroy(ctx->stream));
+  ctx->own_stream = false;
+  ctx->stream = (cudaStream_t)stream;
+  API_END(ctx)
+}
+
+void *gbz_get_stream(gbz_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+gbz_status gbz_synchronize(gbz_ctx *ctx) {
+  API_BEGIN(ctx)
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+const char *gbz_status_string(gbz_status s) {
+  switch (s) {
+    case GBZ_OK: return "ok";
+    case GBZ_EINVAL: return "invalid argument";
+    case GBZ_ENOMEM: return "out of memory";
+    case GBZ_ECUDA: return "CUDA error";
+    case GBZ_ECHECK: return "device consistency check failed";
+    case GBZ_ESMALL: return "output buffer too small";
+    default: return "unknown status";
+  }
+}
+
+const char *gbz_last_error(const gbz_ctx *ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+gbz_status gbz_host_alloc(void **ptr, uint64_t bytes) {
+  if (!ptr) return GBZ_EINVAL;
+  return cudaHostAlloc(ptr, bytes ? bytes : 16, cudaHostAllocDefault) == cudaSuccess ? GBZ_OK : GBZ_ENOMEM;
+}
+void gbz_host_free(void *ptr) {
+  if (ptr) cudaFreeHost(ptr);
+}
+gbz_status gbz_device_alloc(gbz_ctx *ctx, void **ptr, uint64_t bytes) {
+  API_BEGIN(ctx)
+  need(ptr, "ptr");
+  GBZ_CUDA(cudaMalloc(ptr, bytes ? bytes : 16));
+  API_END(ctx)
+}
+void gbz_device_free(gbz_ctx *ctx, void *ptr) {
+  if (!ctx || !ptr) return;
+  try {
+    DeviceGuard g(ctx->device);
+    cudaFree(ptr);
+  } catch (...) {
+  }
+}
+
+gbz_status gbz_field_ops(gbz_ctx *ctx, const uint64_t *a, const uint64_t *b, uint64_t n, uint64_t *sum,
+                         uint64_t *diff, uint64_t *prod, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(a, "a");
+  need(b, "b");
+  if (!n) return GBZ_OK;
+  const uint64_t bytes = 16 * n;
+  const fe *da = dev_view(ctx, 0, (const fe *)a, bytes, mem, true);
+  const fe *db = dev_view(ctx, 1, (const fe *)b, bytes, mem, true);
+  fe *ds = sum ? dev_view(ctx, 2, (fe *)sum, bytes, mem, false) : nullptr;
+  fe *dd = diff ? dev_view(ctx, 3, (fe *)diff, bytes, mem, false) : nullptr;
+  fe *dp = prod ? dev_view(ctx, 4, (fe *)prod, bytes, mem, false) : nullptr;
+  field_ops_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(da, db, n, ds, dd, dp);
+  GBZ_CUDA(cudaGetLastError());
+  if (sum) copy_out(ctx, (fe *)sum, ds, bytes, mem);
+  if (diff) copy_out(ctx, (fe *)diff, dd, bytes, mem);
+  if (prod) copy_out(ctx, (fe *)prod, dp, bytes, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_blake3_64(gbz_ctx *ctx, const uint8_t *in, uint8_t *out, uint64_t count, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(in, "in");
+  need(out, "out");
+  if (!count) return GBZ_OK;
+  const uint8_t *din = dev_view(ctx, 0, in, 64 * count, mem, true);
+  uint8_t *dout = dev_view(ctx, 1, out, 32 * count, mem, false);
+  blake3_batch_launch(din, dout, count, ctx->stream);
+  copy_out(ctx, out, dout, 32 * count, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_fft(gbz_ctx *ctx, uint64_t *data, int logn, int inverse, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(data, "data");
+  if (logn < 0 || logn > kMaxLogN) throw ArgError("fft: logn out of range [0, 28]");
+  const uint64_t L = 1ull << logn, bytes = 16 * L;
+  fe *d = dev_view(ctx, 0, (fe *)data, bytes, mem, true);
+  fe *tmp = (fe *)ctx->buf(1, bytes);
+  ntt_launch(ctx->tables(logn), d, L, d, tmp, inverse != 0, ctx->stream);
+  copy_out(ctx, (fe *)data, d, bytes, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_rs_encode(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int rate, uint64_t *codeword, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(arr, "arr");
+  need(codeword, "codeword");
+  check_pow2(m, "rs_encode: m");
+  if (rate < 1 || !is_pow2((uint64_t)rate)) throw ArgError("rs_encode: rate must be a power of two");
+  const uint64_t L = m * (uint64_t)rate;
+  if (ilog2(L) > kMaxLogN) throw ArgError("rs_encode: codeword longer than 2^28");
+  const fe *din = dev_view(ctx, 0, (const fe *)arr, 16 * m, mem, true);
+  fe *dout = dev_view(ctx, 1, (fe *)codeword, 16 * L, mem, false);
+  fe *tmp = (fe *)ctx->buf(2, 16 * L);
+  ntt_launch(ctx->tables(ilog2(L)), din, m, dout, tmp, false, ctx->stream);
+  copy_out(ctx, (fe *)codeword, dout, 16 * L, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_merkle_commit_blake(gbz_ctx *ctx, const uint64_t *elems, uint64_t N, uint8_t *levels, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(elems, "elems");
+  need(levels, "levels");
+  if (N < 4 || !is_pow2(N)) throw ArgError("merkle: N must be a power of two >= 4");
+  const fe *d = dev_view(ctx, 0, (const fe *)elems, 16 * N, mem, true);
+  uint8_t *lv = dev_view(ctx, 1, levels, 32 * merkle_hashes(N), mem, false);
+  merkle_commit_launch(d, N, lv, ctx->stream);
+  copy_out(ctx, levels, lv, 32 * merkle_hashes(N), mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_merkle_open_blake(const uint8_t *levels, uint64_t N, uint64_t pos, uint8_t *path, uint32_t *depth) {
+  if (!levels || !path || N < 4 || !is_pow2(N)) return GBZ_EINVAL;
+  uint64_t cnt = N / 4;
+  if (pos >= cnt) return GBZ_EINVAL;
+  const uint8_t *lv = levels;
+  uint32_t d = 0;
+  while (cnt > 1) {
+    const uint64_t sib = 2 * (pos / 2) + (1 - (pos % 2));
+    for (int k = 0; k < 32; k++) path[32 * d + k] = lv[32 * sib + k];
+    d++;
+    lv += 32 * cnt;
+    cnt /= 2;
+    pos /= 2;
+  }
+  if (depth) *depth = d;
+  return GBZ_OK;
+}
+
+gbz_status gbz_whir_commit(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int rate, uint64_t *codeword,
+                           uint8_t *levels, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(arr, "arr");
+  need(codeword, "codeword");
+  need(levels, "levels");
+  check_pow2(m, "whir_commit: m");
+  if (rate < 1 || !is_pow2((uint64_t)rate)) throw ArgError("whir_commit: rate must be a power of two");
+  const uint64_t L = m * (uint64_t)rate;
+  if (L < 4) throw ArgError("whir_commit: codeword shorter than one leaf");
+  if (ilog2(L) > kMaxLogN) throw ArgError("whir_commit: codeword longer than 2^28");
+  const fe *din = dev_view(ctx, 0, (const fe *)arr, 16 * m, mem, true);
+  fe *dcw = dev_view(ctx, 1, (fe *)codeword, 16 * L, mem, false);
+  uint8_t *dlv = dev_view(ctx, 2, levels, 32 * merkle_hashes(L), mem, false);
+  fe *tmp = (fe *)ctx->buf(3, 16 * L);
+  ntt_launch(ctx->tables(ilog2(L)), din, m, dcw, tmp, false, ctx->stream);
+  merkle_commit_launch(dcw, L, dlv, ctx->stream);
+  copy_out(ctx, (fe *)codeword, dcw, 16 * L, mem);
+  copy_out(ctx, levels, dlv, 32 * merkle_hashes(L), mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_precompute_beta(gbz_ctx *ctx, const uint64_t *r, int nr, uint64_t *B, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(r, "r");
+  need(B, "B");
+  if (nr < 0 || nr > kMaxLogN) throw ArgError("precompute_beta: nr out of range [0, 28]");
+  const fe *dr = dev_view(ctx, 0, (const fe *)r, 16 * (uint64_t)(nr ? nr : 1), mem, true);
+  fe *dB = dev_view(ctx, 1, (fe *)B, 16ull << nr, mem, false);
+  beta_launch(dr, nr, dB, ctx->stream);
+  copy_out(ctx, (fe *)B, dB, 16ull << nr, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_sumcheck_quadratic(gbz_ctx *ctx, const uint64_t *v1, const uint64_t *v2, uint64_t m,
+                                  uint64_t *coeffs, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(v1, "v1");
+  need(v2, "v2");
+  need(coeffs, "coeffs");
+  if (m < 2 || !is_pow2(m)) throw ArgError("sumcheck: m must be a power of two >= 2");
+  const fe *a = dev_view(ctx, 0, (const fe *)v1, 16 * m, mem, true);
+  const fe *b = dev_view(ctx, 1, (const fe *)v2, 16 * m, mem, true);
+  const int blocks = sc_blocks(m / 2);
+  fe *partial = (fe *)ctx->buf(2, 48ull * blocks);
+  fe *out = (fe *)ctx->buf(3, 48);
+  sc_step_launch(a, b, m, nullptr, nullptr, nullptr, true, partial, blocks, ctx->stream);
+  sc_sum_launch(partial, blocks, out, ctx->stream);
+  GBZ_CUDA(cudaMemcpyAsync(coeffs, out, 48, cudaMemcpyDeviceToHost, ctx->stream));
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+gbz_status gbz_sumcheck_fold(gbz_ctx *ctx, uint64_t *v, uint64_t m, const uint64_t *r, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(v, "v");
+  need(r, "r");
+  if (m < 2 || !is_pow2(m)) throw ArgError("sumcheck fold: m must be a power of two >= 2");
+  fe *d = dev_view(ctx, 0, (fe *)v, 16 * m, mem, true);
+  fe *dr = (fe *)ctx->buf(1, 16);
+  GBZ_CUDA(cudaMemcpyAsync(dr, r, 16, cudaMemcpyHostToDevice, ctx->stream));
+  fe *out = (fe *)ctx->buf(2, 8 * m);
+  fe *out2 = (fe *)ctx->buf(3, 8 * m);
+  // The fold kernel folds two vectors at once; the second one is a copy.
+  sc_step_launch(d, d, m, dr, out, out2, false, nullptr, sc_blocks(m / 4 ? m / 4 : 1), ctx->stream);
+  GBZ_CUDA(cudaMemcpyAsync(d, out, 8 * m, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaMemcpyAsync(v, out, 8 * m, cudaMemcpyDeviceToHost, ctx->stream));
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_whir_update_betas(gbz_ctx *ctx, uint64_t *b, uint64_t nb, const int32_t *queries, int l, uint64_t N,
+                                 const uint64_t *r, uint64_t *challenges, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(b, "b");
+  need(r, "r");
+  if (l < 0 || l > kMaxQueries) throw ArgError("update_betas: l out of range [0, 256]");
+  if (l && !queries) throw ArgError("null pointer: queries");
+  check_pow2(N, "update_betas: N");
+  if (ilog2(N) > kMaxLogN) throw ArgError("update_betas: N above 2^28");
+  if (!ctx->st) GBZ_CUDA(cudaMalloc(&ctx->st, sizeof(ProofState)));
+  if (!ctx->ub_scratch) GBZ_CUDA(cudaMalloc(&ctx->ub_scratch, sizeof(fe) * kUpdateBetasScratch));
+  fe *db = dev_view(ctx, 0, (fe *)b, 16 * nb, mem, true);
+  const int32_t *dq = dev_view(ctx, 1, queries, 4ull * (l ? l : 1), mem, true);
+  ub_prep_kernel<<<1, 256, 0, ctx->stream>>>(ctx->st, dq, l, ilog2(N), fe_make(r[0], r[1]));
+  GBZ_CUDA(cudaGetLastError());
+  update_betas_launch(db, nb, ctx->st, l, ctx->ub_scratch, ctx->stream);
+  copy_out(ctx, (fe *)b, db, 16 * nb, mem);
+  if (challenges && l) {
+    // challenges is host memory regardless of mem
+    GBZ_CUDA(cudaMemcpyAsync(challenges, ctx->st->comb, 16ull * l, cudaMemcpyDeviceToHost, ctx->stream));
+    GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+void gbz_hash_to_field(uint64_t *state, const uint64_t *elems, int count, uint64_t *out) {
+  fe s = fe_make(state[0], state[1]);
+  for (int i = 0; i < count; i++) s = hash_F(s, fe_make(elems[2 * i], elems[2 * i + 1]));
+  state[0] = s.re;
+  state[1] = s.im;
+  if (out) {
+    out[0] = s.re;
+    out[1] = s.im;
+  }
+}
+
+static_assert(sizeof(gbz_prng) == sizeof(glibc_prng), "gbz_prng layout");
+
+void gbz_prng_seed(gbz_prng *g, uint32_t seed) { prng_seed(*reinterpret_cast<glibc_prng *>(g), seed); }
+int32_t gbz_prng_next(gbz_prng *g) { return prng_next(*reinterpret_cast<glibc_prng *>(g)); }
+void gbz_prng_field(gbz_prng *g, uint64_t *out) {
+  fe r = prng_field(*reinterpret_cast<glibc_prng *>(g));
+  out[0] = r.re;
+  out[1] = r.im;
+}
+
+void gbz_field_ops_host(const uint64_t *a, const uint64_t *b, uint64_t n, uint64_t *sum, uint64_t *diff,
+                        uint64_t *prod) {
+  for (uint64_t i = 0; i < n; i++) {
+    fe x = fe_make(a[2 * i], a[2 * i + 1]), y = fe_make(b[2 * i], b[2 * i + 1]);
+    if (sum) { fe r = fadd(x, y); sum[2 * i] = r.re; sum[2 * i + 1] = r.im; }
+    if (diff) { fe r = fsub(x, y); diff[2 * i] = r.re; diff[2 * i + 1] = r.im; }
+    if (prod) { fe r = fmul(x, y); prod[2 * i] = r.re; prod[2 * i + 1] = r.im; }
+  }
+}
+
+int gbz_prove_launches(int logn, int rate) {
+  try {
+    if (logn < 3 || logn > 26 || rate < 2 || rate > 64 || !is_pow2((uint64_t)rate)) return 0;
+    ProofPlan p;
+    p.logn = logn;
+    p.rate = rate;
+    p.n = 1ull << logn;
+    p.L = p.n * (uint64_t)rate;
+    enqueue_proof(p, nullptr, 1, nullptr, true);
+    return p.launches;
+  } catch (...) {
+    return 0;
+  }
+}
+
+gbz_status gbz_profile_enable(gbz_ctx *ctx, int enable) {
+  API_BEGIN(ctx)
+  ctx->profiling = enable != 0;
+  API_END(ctx)
+}
+
+gbz_status gbz_profile_read(gbz_ctx *ctx, int logn, int rate, double *ms, int *groups) {
+  API_BEGIN(ctx)
+  need(ms, "ms");
+  auto it = ctx->profilers.find(std::make_pair(logn, rate));
+  if (it == ctx->profilers.end()) {
+    for (int c = 0; c < PC_COUNT; c++) {
+      ms[c] = 0;
+      if (groups) groups[c] = 0;
+    }
+    return GBZ_OK;
+  }
+  it->second->read(ms, groups);
+  it->second->reset();
+  API_END(ctx)
+}
+
+uint64_t gbz_prove_transcript_bytes(int logn, int rate) {
+  try {
+    // Layout only: build a throwaway plan-free layout by a dry enqueue.
+    ProofPlan p;
+    p.logn = logn;
+    p.rate = rate;
+    if (logn < 3 || logn > 26 || rate < 2 || rate > 64 || !is_pow2((uint64_t)rate)) return 0;
+    p.n = 1ull << logn;
+    p.L = p.n * (uint64_t)rate;
+    enqueue_proof(p, nullptr, 1, nullptr, true);
+    return p.layout.len;
+  } catch (...) {
+    return 0;
+  }
+}
+
+gbz_status gbz_prove(gbz_ctx *ctx, const uint64_t *witness, int logn, int rate, uint32_t prng_seed,
+                     uint8_t *transcript, uint64_t capacity, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(witness, "witness");
+  need(transcript, "transcript");
+  auto key = std::make_pair(logn, rate);
+  auto it = ctx->plans.find(key);
+  if (it == ctx->plans.end()) it = ctx->plans.emplace(key, plan_create(logn, rate)).first;
+  ProofPlan &p = *it->second;
+  if (ctx->profiling) {
+    auto &pr = ctx->profilers[key];
+    if (!pr) pr.reset(new Profiler());
+    pr->enabled = true;
+    p.prof = pr.get();
+  } else {
+    p.prof = nullptr;
+  }
+  if (capacity < p.transcript_bytes) return fail(ctx, GBZ_ESMALL, "transcript buffer smaller than gbz_prove_transcript_bytes");
+  const fe *w;
+  if (mem == GBZ_MEM_HOST) {
+    GBZ_CUDA(cudaMemcpyAsync(p.w, witness, 16 * p.n, cudaMemcpyHostToDevice, ctx->stream));
+    w = p.w;
+  } else {
+    w = (const fe *)witness;
+  }
+  enqueue_proof(p, w, prng_seed, ctx->stream, false);
+  GBZ_CUDA(cudaMemcpyAsync(transcript, p.transcript, p.transcript_bytes,
+                           mem == GBZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, ctx->stream));
+  if (mem == GBZ_MEM_HOST) {
+    if (plan_error_flags(p, ctx->stream)) return fail(ctx, GBZ_ECHECK, "a sumcheck round message did not match its claim");
+  }
+  API_END(ctx)
+}
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+// Internal declarations shared by the libgbz translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "gbz_blake3.cuh"
+#include "gbz_field.cuh"
+
+namespace gbz {
+
+constexpr int kMaxLogN = 28;        // largest NTT / codeword: 2^28 elements
+constexpr int kMaxQueries = 256;    // WHIR queries per iteration (rate 2 needs 200)
+constexpr int kWhirLogK = 2;        // folding factor 4 (whir_k = 4)
+constexpr int kWhirK = 1 << kWhirLogK;
+
+// Transcript record tags (one u32 tag, one u32 count, then count units).
+enum : uint32_t {
+  T_COMMIT_ROOT = 1, T_EVAL_POINT = 2, T_CLAIM = 3, T_SC_POLY = 4, T_SC_CHALLENGE = 5,
+  T_SC_FINAL = 6, T_WHIR_POLY = 7, T_WHIR_CHALLENGE = 8, T_WHIR_ROOT = 9,
+  T_WHIR_QUERIES = 10, T_WHIR_REPLIES = 11, T_WHIR_ANSWERS = 12, T_WHIR_PATHS = 13,
+  T_WHIR_COMBINE = 14, T_WHIR_K = 15, T_FINAL_POLY = 16, T_FINAL_POINT = 17,
+  T_FINAL_EVAL = 18
+};
+
+// Verifier-side randomness and running claims of one proof, resident in
+// device memory so that the whole proof is one stream of launches with no
+// host round trip (and can be captured in a CUDA graph).  Replaces the
+// reference's process-global prev_challenge (Fiat_Shamir.cpp:5) and glibc
+// generator state with per-proof state.
+struct ProofState {
+  fe fs;                      // Fiat-Shamir chain value (prev_challenge)
+  glibc_prng prng;            // glibc random() state
+  fe y;                       // running sumcheck claim
+  fe K;                       // WHIR running claim
+  fe chal[64];                // sumcheck challenges (the claim point)
+  fe z[64];                   // evaluation point
+  fe rw[kWhirLogK];           // WHIR round challenges of the current iteration
+  fe hw[kWhirLogK][3];        // WHIR round messages of the current iteration
+  fe fin_r[8];                // final point
+  int32_t q[kMaxQueries];     // queries scaled to the new codeword
+  fe comb[kMaxQueries];       // update_betas combination weights c_i = r^(i+1)
+  fe qw[kMaxQueries];         // c_i-weighted query roots, see whir kernels
+  fe omega_q[kMaxQueries];    // omega_N^{q_i}
+  uint32_t error;             // non-zero: a device-side consistency check failed
+};
+
+// Error capture for the C-ABI.
+struct Err {
+  int code = 0;
+  std::string msg;
+};
+
+#define GBZ_CUDA(call)                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) throw ::gbz::CudaError(e_, #call, __FILE__, __LINE__);         \
+  } while (0)
+
+struct CudaError {
+  cudaError_t err;
+  std::string what;
+  CudaError(cudaError_t e, const char *call, const char *file, int line) : err(e) {
+    what = std::string(cudaGetErrorString(e)) + " in " + call + " at " + file + ":" + std::to_string(line);
+  }
+};
+
+struct ArgError {
+  std::string what;
+  explicit ArgError(std::string w) : what(std::move(w)) {}
+};
+
+inline int ilog2(uint64_t x) {
+  int l = 0;
+  while ((1ull << (l + 1)) <= x) l++;
+  return l;
+}
+inline bool is_pow2(uint64_t x) { return x && !(x & (x - 1)); }
+
+// ------------------------------------------------------------------ NTT
+// Twiddle tables for one transform length, resident in device memory.
+struct NttTables {
+  int logn = -1;
+  fe *sub_fwd = nullptr;   // omega_S^t for every sub-length S = 2^s, s <= 13, packed
+  fe *sub_inv = nullptr;
+  fe *lo_fwd = nullptr, *hi_fwd = nullptr;  // omega_L^e = lo[e & 4095] * hi[e >> 12]
+  fe *lo_inv = nullptr, *hi_inv = nullptr;
+  fe inv_len;              // L^{-1}
+};
+
+// Forward (inverse = false) or inverse transform of length 2^logn with the
+// reference's semantics (utils.cpp:904-964): out[k] = sum_j in[j] w^{jk},
+// w = getRootOfUnity(logn) (inverted and scaled by 2^-logn for the inverse).
+// `in` holds n_valid elements; the rest of the length is zero (RS padding).
+// `tmp` must hold 2^logn elements when logn > 13.  in may equal out.
+void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
+                cudaStream_t s);
+void ntt_tables_build(NttTables &t, int logn);
+int ntt_launch_count(int logn);
+void ntt_tables_free(NttTables &t);
+
+// --------------------------------------------------------------- Merkle
+// MT_commit_Blake (merkle_tree.cpp:195-233) over N elements: levels holds
+// N/4 leaf hashes followed by every upper level (N/2 - 1 hashes, 32 B each).
+void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStream_t s);
+void blake3_batch_launch(const uint8_t *in, uint8_t *out, uint64_t count, cudaStream_t s);
+inline uint64_t merkle_hashes(uint64_t N) { return N / 2 - 1; }
+int merkle_launch_count(uint64_t N);
+
+// ------------------------------------------------------------- sumcheck
+// One fused sumcheck step over vectors (a, b) of length m:
+//   chal == nullptr : round message of (a, b) itself;
+//   chal != nullptr : fold a, b by *chal into (a2, b2) of length m/2 and,
+//                     when reduce, the round message of the folded vectors.
+// Per-block partial sums go to `partial` (3 fe per block).
+int sc_blocks(uint64_t pairs);
+void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2, fe *b2, bool reduce,
+                    fe *partial, int blocks, cudaStream_t s);
+// Round-message reduction of `blocks` partials into out[3].
+void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s);
+
+// precompute_beta (utils.cpp:198-243) of r (nr values, device) into B.
+void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s);
+
+// update_betas (Whir.cpp:325-342): b[j] += sum_i comb[i] * omega_q[i]^j.
+// pw_scratch holds kUpdateBetasScratch elements.
+constexpr uint64_t kUpdateBetasScratch = (uint64_t)kMaxQueries * 256;
+void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s);
+
+// RS_multifold5 (coPCS_utils.cpp:386-437).
+void rs_multifold5_launch(const fe *cw, uint64_t n, const fe *a, int logd, fe *out, cudaStream_t s);
+
+}  // namespace gbz

@@ -1,0 +1,541 @@
+// The plain single-party prover on one GPU.
+//
+// One proof = the reference's call sequence
+//   Whir_Commit_initial (Whir.cpp:158-190)          -> root
+//   hash_to_field({0}) x log n (main.cpp:83-85)      -> evaluation point z
+//   quadratic sumcheck of sum_x w(x) eq(z, x) with Fiat-Shamir challenges
+//     (round body of _quadratic_cosumcheck, coSumcheck_MPI.cpp:195-219)
+//   Whir_Open of the resulting claim, whir_k = 4 (Whir.cpp:388-467)
+// and its transcript is the ordered record stream documented in
+// include/gbz.h.  Everything, including the Fiat-Shamir chain and the glibc
+// random() draws that the reference uses for WHIR challenges and queries,
+// runs on the device: a proof is a fixed sequence of launches on one
+// stream with no host synchronisation, so it can be replayed from a CUDA
+// graph and overlapped with other proofs on other streams.
+#include <math.h>
+
+#include <cstring>
+#include <memory>
+#include <mutex>
+
+#include "gbz_prover.cuh"
+
+namespace gbz {
+
+namespace {
+
+// ------------------------------------------------------------ kernels
+
+// Transcript records start at 4-byte multiples (query records have 4-byte
+// units), so every store into the transcript is a 32-bit store.
+__device__ __forceinline__ void put_fe(uint8_t *tr, uint64_t off, fe v) {
+  uint32_t *p = reinterpret_cast<uint32_t *>(tr + off);
+  p[0] = (uint32_t)v.re;
+  p[1] = (uint32_t)(v.re >> 32);
+  p[2] = (uint32_t)v.im;
+  p[3] = (uint32_t)(v.im >> 32);
+}
+
+__global__ void k_init(ProofState *st, uint32_t seed) {
+  if (threadIdx.x) return;
+  st->fs = fe_zero();
+  prng_seed(st->prng, seed);
+  st->y = fe_zero();
+  st->K = fe_zero();
+  st->error = 0;
+}
+
+// z_i = hash_to_field({0}) for i < logn.
+__global__ void k_point(ProofState *st, int logn, uint8_t *tr, uint64_t off) {
+  if (threadIdx.x) return;
+  fe s = st->fs;
+  for (int i = 0; i < logn; i++) {
+    s = hash_F(s, fe_zero());
+    st->z[i] = s;
+    put_fe(tr, off + 16 * i, s);
+  }
+  st->fs = s;
+}
+
+__device__ void sum_partials(const fe *partial, int blocks, fe out[3]) {
+  __shared__ fe red[3][32];
+  fe A = fe_zero(), C = fe_zero(), D = fe_zero();
+  for (int i = threadIdx.x; i < blocks; i += blockDim.x) {
+    A = fadd(A, partial[3 * i]);
+    C = fadd(C, partial[3 * i + 1]);
+    D = fadd(D, partial[3 * i + 2]);
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    fe t;
+    t.re = __shfl_down_sync(0xffffffffu, A.re, d); t.im = __shfl_down_sync(0xffffffffu, A.im, d); A = fadd(A, t);
+    t.re = __shfl_down_sync(0xffffffffu, C.re, d); t.im = __shfl_down_sync(0xffffffffu, C.im, d); C = fadd(C, t);
+    t.re = __shfl_down_sync(0xffffffffu, D.re, d); t.im = __shfl_down_sync(0xffffffffu, D.im, d); D = fadd(D, t);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][w] = A; red[1][w] = C; red[2][w] = D; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    A = C = D = fe_zero();
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+      A = fadd(A, red[0][k]);
+      C = fadd(C, red[1][k]);
+      D = fadd(D, red[2][k]);
+    }
+    out[0] = A;
+    out[1] = fsub(fsub(D, A), C);
+    out[2] = C;
+  }
+}
+
+// Sumcheck round i: message H from partials; claim check; Fiat-Shamir
+// challenge hash_to_field({H.a, H.b, H.c}); y = H(c).
+__global__ void k_sc_round(const fe *partial, int blocks, ProofState *st, int round, uint8_t *tr,
+                           int64_t off_claim, uint64_t off_poly, uint64_t off_chal) {
+  fe H[3];
+  sum_partials(partial, blocks, H);
+  if (threadIdx.x) return;
+  fe h01 = fadd(quad_eval(H[0], H[1], H[2], fe_zero()), quad_eval(H[0], H[1], H[2], fe_one()));
+  if (off_claim >= 0) {
+    st->y = h01;
+    put_fe(tr, (uint64_t)off_claim, h01);
+  } else if (!fe_eq(h01, st->y)) {
+    st->error |= 1u;
+  }
+  for (int k = 0; k < 3; k++) put_fe(tr, off_poly + 16 * k, H[k]);
+  fe s = st->fs;
+  for (int k = 0; k < 3; k++) s = hash_F(s, H[k]);
+  st->fs = s;
+  st->chal[round] = s;
+  put_fe(tr, off_chal, s);
+  st->y = quad_eval(H[0], H[1], H[2], s);
+}
+
+__global__ void k_sc_final(ProofState *st, const fe *v1, const fe *v2, uint8_t *tr, uint64_t off) {
+  if (threadIdx.x) return;
+  fe a = v1[0], b = v2[0];
+  put_fe(tr, off, a);
+  put_fe(tr, off + 16, b);
+  st->K = a;  // Whir_Open: K = claims[0].first
+}
+
+// WHIR sumcheck round (whir_sumcheck, Whir.cpp:233-249): message h, the
+// consistency check K == h(0) + h(1), challenge F::_random(), K = h(r).
+__global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int i, uint8_t *tr,
+                             uint64_t off_poly, uint64_t off_chal) {
+  fe H[3];
+  sum_partials(partial, blocks, H);
+  if (threadIdx.x) return;
+  fe h01 = fadd(quad_eval(H[0], H[1], H[2], fe_zero()), quad_eval(H[0], H[1], H[2], fe_one()));
+  if (!fe_eq(h01, st->K)) st->error |= 2u;
+  for (int k = 0; k < 3; k++) {
+    put_fe(tr, off_poly + 16 * k, H[k]);
+    st->hw[i][k] = H[k];
+  }
+  fe r = prng_field(st->prng);
+  st->rw[i] = r;
+  put_fe(tr, off_chal, r);
+  st->K = quad_eval(H[0], H[1], H[2], r);
+}
+
+// get_RS_multifold_segment_tensor (coPCS_utils.cpp:333-383) for a segment
+// of kWhirK values.
+__device__ fe rs_fold_tensor_dev(const fe seg[kWhirK], const fe *r, uint64_t n, uint64_t idx, fe om_inv,
+                                 fe len_inv) {
+  const int logn = 63 - __clzll((long long)n);
+  fe omega = fpow(om_inv, n / kWhirK);
+  fe inv_om = fpow(om_inv, idx);
+  fe part[kWhirK / 2];
+  int seg_n = kWhirK;
+  const fe one = fe_one();
+  for (int j = 0; j < seg_n / 2; j++) {
+    fe s = fadd(seg[j], seg[j + seg_n / 2]), d = fsub(seg[j], seg[j + seg_n / 2]);
+    part[j] = fadd(fmul(fsub(one, r[0]), s), fmul(fmul(r[0], inv_om), d));
+    inv_om = fmul(inv_om, omega);
+  }
+  fe pw[kWhirLogK];
+  pw[0] = one;
+  if (kWhirLogK > 1) pw[1] = fmul(om_inv, om_inv);
+  for (int i = 2; i < kWhirLogK; i++) pw[i] = fmul(pw[i - 1], pw[i - 1]);
+  for (int i = 1; i < kWhirLogK; i++) pw[i] = fpow(pw[i], n / kWhirK);
+  for (int i = 1; i < kWhirLogK; i++) {
+    seg_n /= 2;
+    fe o = finv(root_of_unity(logn - i));
+    fe po = fpow(o, idx);
+    for (int j = 0; j < seg_n / 2; j++) {
+      fe s = fadd(part[j], part[j + seg_n / 2]), d = fsub(part[j], part[j + seg_n / 2]);
+      part[j] = fadd(fmul(fsub(one, r[i]), s), fmul(r[i], fmul(po, d)));
+      po = fmul(po, pw[i]);
+    }
+  }
+  return fmul(len_inv, part[0]);
+}
+
+struct QueryArgs {
+  ProofState *st;
+  const fe *cw;          // previous codeword
+  uint64_t L;            // its length
+  const uint8_t *tree;   // its Merkle levels
+  uint64_t NL;           // new codeword length
+  int l;                 // number of queries
+  uint8_t *tr;
+  uint64_t off_q, off_rep, off_ans, off_path, off_comb, off_K;
+};
+
+// whir_query (Whir.cpp:251-314), the query rescaling (:371-372) and the
+// combination weights / K update of update_betas (:325-342, :383-384).
+__global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
+  __shared__ int32_t q[kMaxQueries];
+  __shared__ fe ans[kMaxQueries];
+  __shared__ fe om_inv_s, len_inv_s, om_new_s;
+  ProofState *st = a.st;
+  if (threadIdx.x == 0) {
+    const int32_t mod = (int32_t)(a.L / 4);  // whir_k <= 4 branch
+    for (int i = 0; i < a.l; i++) q[i] = prng_next(st->prng) % mod;
+    om_inv_s = finv(root_of_unity(63 - __clzll((long long)a.L)));
+    len_inv_s = finv(fe_make(kWhirK, 0));
+    om_new_s = root_of_unity(63 - __clzll((long long)a.NL));
+  }
+  __syncthreads();
+  const int i = threadIdx.x;
+  const int depth = 63 - __clzll((long long)(a.L / 4));
+  if (i < a.l) {
+    const uint64_t qi = (uint64_t)q[i];
+    reinterpret_cast<int32_t *>(a.tr + a.off_q)[i] = q[i];
+    fe seg[kWhirK];
+    for (int j = 0; j < kWhirK; j++) {
+      seg[j] = a.cw[qi + j * (a.L / kWhirK)];
+      put_fe(a.tr, a.off_rep + 16 * (kWhirK * i + j), seg[j]);
+    }
+    fe y = rs_fold_tensor_dev(seg, st->rw, a.L, qi, om_inv_s, len_inv_s);
+    ans[i] = y;
+    put_fe(a.tr, a.off_ans + 16 * i, y);
+    // open_tree_blake: sibling 2*(pos/2) + (1 - pos%2) on every level below the root
+    uint64_t pos = qi, cnt = a.L / 4, lvl = 0;
+    uint8_t *path = a.tr + a.off_path + 32ull * depth * i;
+    for (int d = 0; d < depth; d++) {
+      uint64_t sib = pos ^ 1ull;
+      const uint4 *src = reinterpret_cast<const uint4 *>(a.tree + 32 * (lvl + sib));
+      uint32_t *dst = reinterpret_cast<uint32_t *>(path + 32 * d);
+      uint4 h0 = src[0], h1 = src[1];
+      dst[0] = h0.x; dst[1] = h0.y; dst[2] = h0.z; dst[3] = h0.w;
+      dst[4] = h1.x; dst[5] = h1.y; dst[6] = h1.z; dst[7] = h1.w;
+      lvl += cnt;
+      cnt >>= 1;
+      pos >>= 1;
+    }
+    const int32_t scaled = (int32_t)(q[i] * (int32_t)(kWhirK * a.NL / a.L));
+    st->q[i] = scaled;
+    st->omega_q[i] = fpow(om_new_s, (uint64_t)(uint32_t)scaled);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fe r = prng_field(st->prng);
+    fe c = r, K = st->K;
+    for (int k = 0; k < a.l; k++) {
+      st->comb[k] = c;
+      put_fe(a.tr, a.off_comb + 16 * k, c);
+      K = fadd(K, fmul(c, ans[k]));
+      c = fmul(c, r);
+    }
+    st->K = K;
+    put_fe(a.tr, a.off_K, K);
+  }
+}
+
+// Final round of Whir_Open (Whir.cpp:426-446): the remaining polynomial,
+// log2|arr| F::_random draws and evaluate_vector(b, r).
+__global__ void k_final(ProofState *st, const fe *arr, fe *b, int m, uint8_t *tr, uint64_t off_poly,
+                        uint64_t off_point, uint64_t off_eval) {
+  if (threadIdx.x) return;
+  for (int i = 0; i < m; i++) put_fe(tr, off_poly + 16 * i, arr[i]);
+  const int lg = 31 - __clz(m);
+  fe r[8];
+  for (int i = 0; i < lg; i++) {
+    r[i] = prng_field(st->prng);
+    put_fe(tr, off_point + 16 * i, r[i]);
+  }
+  fe v[8];
+  for (int i = 0; i < m; i++) v[i] = b[i];
+  for (int i = 0; i < lg; i++) {
+    fe om = fsub(fe_one(), r[i]);
+    int L = 1 << (lg - 1 - i);
+    for (int j = 0; j < L; j++) v[j] = fadd(fmul(om, v[2 * j]), fmul(r[i], v[2 * j + 1]));
+  }
+  put_fe(tr, off_eval, v[0]);
+}
+
+__global__ void k_copy32(const uint8_t *src, uint8_t *dst) {
+  if (threadIdx.x < 8)
+    reinterpret_cast<uint32_t *>(dst)[threadIdx.x] = reinterpret_cast<const uint32_t *>(src)[threadIdx.x];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ host side
+
+int whir_query_count(int rate) { return (int)(-100.0 / log2(sqrt(1.0 / (double)rate))); }
+
+uint64_t Layout::rec(uint32_t tag, uint32_t count, uint32_t unit) {
+  uint64_t off = len;
+  if (record_headers) {
+    headers.push_back({off, tag, count});
+  }
+  len += 8 + (uint64_t)count * unit;
+  return off + 8;
+}
+
+ProofPlan::~ProofPlan() {
+  for (auto &kv : ntt) ntt_tables_free(kv.second);
+  for (void *p : allocs) cudaFree(p);
+}
+
+void *ProofPlan::dalloc(uint64_t bytes) {
+  void *p = nullptr;
+  GBZ_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
+  allocs.push_back(p);
+  return p;
+}
+
+NttTables &ProofPlan::tables(int lg) {
+  auto it = ntt.find(lg);
+  if (it != ntt.end()) return it->second;
+  NttTables t;
+  ntt_tables_build(t, lg);
+  return ntt.emplace(lg, t).first->second;
+}
+
+std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
+  if (logn < 3 || logn > 26) throw ArgError("prover: log2 witness length must be in [3, 26]");
+  if (rate < 2 || rate > 64 || !is_pow2((uint64_t)rate)) throw ArgError("prover: rate must be a power of two in [2, 64]");
+  const uint64_t n = 1ull << logn, L = n * (uint64_t)rate;
+  if (ilog2(L) > kMaxLogN) throw ArgError("prover: codeword longer than 2^28");
+  auto p = std::unique_ptr<ProofPlan>(new ProofPlan());
+  p->logn = logn;
+  p->rate = rate;
+  p->n = n;
+  p->L = L;
+  p->w = (fe *)p->dalloc(sizeof(fe) * n);
+  p->cw[0] = (fe *)p->dalloc(sizeof(fe) * L);
+  p->cw[1] = (fe *)p->dalloc(sizeof(fe) * (L / 2));
+  p->tree[0] = (uint8_t *)p->dalloc(32 * merkle_hashes(L));
+  p->tree[1] = (uint8_t *)p->dalloc(32 * merkle_hashes(L / 2 >= 4 ? L / 2 : 4));
+  p->tmp = (fe *)p->dalloc(sizeof(fe) * L);
+  p->va[0] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
+  p->va[1] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
+  p->vb[0] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
+  p->vb[1] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
+  p->beta = (fe *)p->dalloc(sizeof(fe) * n);
+  p->partial = (fe *)p->dalloc(sizeof(fe) * 3 * (uint64_t)sc_blocks(n / 2));
+  p->ub_scratch = (fe *)p->dalloc(sizeof(fe) * kUpdateBetasScratch);
+  p->st = (ProofState *)p->dalloc(sizeof(ProofState));
+  // Build the transcript layout (record headers are constant).
+  p->layout.record_headers = true;
+  enqueue_proof(*p, nullptr, 1, nullptr, /*dry=*/true);  // layout and launch counts
+  p->layout.record_headers = false;
+  p->transcript_bytes = p->layout.len;
+  p->transcript = (uint8_t *)p->dalloc(p->transcript_bytes);
+  std::vector<uint8_t> img(p->transcript_bytes, 0);
+  for (auto &h : p->layout.headers) {
+    std::memcpy(&img[h.off], &h.tag, 4);
+    std::memcpy(&img[h.off + 4], &h.count, 4);
+  }
+  GBZ_CUDA(cudaMemcpy(p->transcript, img.data(), img.size(), cudaMemcpyHostToDevice));
+  // Twiddle tables for every transform length the proof uses.
+  p->tables(ilog2(L));
+  for (uint64_t m = n, cur = (uint64_t)rate; m > 4; m /= 4, cur *= 2) p->tables(ilog2(2 * cur * (m / 4)));
+  return p;
+}
+
+// Enqueue one proof.  witness: device pointer (nullptr: use plan->w).
+// The dry run (dry = true) launches nothing; it fixes the transcript layout
+// and counts the launches per category.
+void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry) {
+  Layout &lay = p.layout;
+  lay.len = 0;
+  if (dry) {
+    p.launches = 0;
+    for (int c = 0; c < PC_COUNT; c++) p.cat_launches[c] = 0;
+  }
+  const fe *w = witness ? witness : p.w;
+  const int logn = p.logn;
+  uint8_t *tr = p.transcript;
+  ProofState *st = p.st;
+  Profiler *prof = (!dry && p.prof && p.prof->enabled) ? p.prof : nullptr;
+  // RUN(category, kernel launches, statement): counts in the dry run, else
+  // runs the statement (bracketed by profiler events when enabled).
+#define RUN(cat, nlaunch, ...)                 \
+  do {                                         \
+    if (dry) {                                 \
+      p.launches += (nlaunch);                 \
+      p.cat_launches[cat] += (nlaunch);        \
+    } else {                                   \
+      if (prof) prof->begin(cat, s);           \
+      __VA_ARGS__;                             \
+      GBZ_CUDA(cudaGetLastError());            \
+      if (prof) prof->end(s);                  \
+    }                                          \
+  } while (0)
+
+  RUN(PC_PROTOCOL, 1, k_init<<<1, 32, 0, s>>>(st, prng_seed));
+
+  // 1. commitment: codeword = NTT(w padded to rate*n), Merkle tree.
+  uint64_t L = p.L;
+  int cwi = 0;
+  uint64_t off = lay.rec(T_COMMIT_ROOT, 1, 32);
+  RUN(PC_NTT, ntt_launch_count(ilog2(L)), ntt_launch(p.tables(ilog2(L)), w, p.n, p.cw[0], p.tmp, false, s));
+  RUN(PC_MERKLE, merkle_launch_count(L), merkle_commit_launch(p.cw[0], L, p.tree[0], s));
+  RUN(PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, s>>>(p.tree[0] + 32 * (merkle_hashes(L) - 1), tr + off));
+
+  // 2. evaluation point and its eq table.
+  off = lay.rec(T_EVAL_POINT, logn, 16);
+  RUN(PC_PROTOCOL, 1, k_point<<<1, 32, 0, s>>>(st, logn, tr, off));
+  RUN(PC_BETA, 1, beta_launch(st->z, logn, p.beta, s));
+
+  // 3. sumcheck of sum w(x) eq(z, x).
+  uint64_t off_claim = lay.rec(T_CLAIM, 1, 16);
+  uint64_t m = p.n;
+  const fe *a = w, *b = p.beta;
+  int pp = 0;
+  for (int i = 0; i < logn; i++) {
+    uint64_t off_poly = lay.rec(T_SC_POLY, 3, 16);
+    uint64_t off_chal = lay.rec(T_SC_CHALLENGE, 1, 16);
+    int blocks;
+    if (i == 0) {
+      blocks = sc_blocks(m / 2);
+      RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, nullptr, nullptr, nullptr, true, p.partial, blocks, s));
+    } else {
+      blocks = sc_blocks(m / 4);
+      fe *a2 = p.va[pp], *b2 = p.vb[pp];
+      RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, &st->chal[i - 1], a2, b2, true, p.partial, blocks, s));
+      a = a2;
+      b = b2;
+      pp ^= 1;
+      m /= 2;
+    }
+    RUN(PC_PROTOCOL, 1,
+        k_sc_round<<<1, 256, 0, s>>>(p.partial, blocks, st, i, tr, i == 0 ? (int64_t)off_claim : -1, off_poly,
+                                     off_chal));
+  }
+  {
+    fe *a2 = p.va[pp], *b2 = p.vb[pp];
+    RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, &st->chal[logn - 1], a2, b2, false, p.partial, 1, s));
+    off = lay.rec(T_SC_FINAL, 2, 16);
+    RUN(PC_PROTOCOL, 1, k_sc_final<<<1, 32, 0, s>>>(st, a2, b2, tr, off));
+    pp ^= 1;
+  }
+
+  // 4. WHIR open of (v1[0], chal): b = precompute_beta(chal), arr = w.
+  RUN(PC_BETA, 1, beta_launch(st->chal, logn, p.beta, s));
+  a = w;
+  b = p.beta;
+  m = p.n;
+  uint64_t cur = (uint64_t)p.rate;
+  // arr/b ping-pong: the first fold writes va/vb[0] (m/2), the second
+  // va/vb[1] (m/4), which the next iteration reads.
+  for (;;) {
+    // round 0
+    uint64_t op = lay.rec(T_WHIR_POLY, 3, 16), oc = lay.rec(T_WHIR_CHALLENGE, 1, 16);
+    int blocks = sc_blocks(m / 2);
+    RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, nullptr, nullptr, nullptr, true, p.partial, blocks, s));
+    RUN(PC_PROTOCOL, 1, k_whir_round<<<1, 256, 0, s>>>(p.partial, blocks, st, 0, tr, op, oc));
+    // round 1: fold by r0 into [0], message
+    op = lay.rec(T_WHIR_POLY, 3, 16);
+    oc = lay.rec(T_WHIR_CHALLENGE, 1, 16);
+    blocks = sc_blocks(m / 4);
+    RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, &st->rw[0], p.va[0], p.vb[0], true, p.partial, blocks, s));
+    RUN(PC_PROTOCOL, 1, k_whir_round<<<1, 256, 0, s>>>(p.partial, blocks, st, 1, tr, op, oc));
+    // fold by r1 into [1]
+    RUN(PC_SUMCHECK, 1,
+        sc_step_launch(p.va[0], p.vb[0], m / 2, &st->rw[1], p.va[1], p.vb[1], false, p.partial,
+                       sc_blocks(m / 8 ? m / 8 : 1), s));
+    a = p.va[1];
+    b = p.vb[1];
+    m /= 4;
+    // commit arr at rate 2*cur
+    const uint64_t NL = 2 * cur * m;
+    const int nci = cwi ^ 1;
+    off = lay.rec(T_WHIR_ROOT, 1, 32);
+    RUN(PC_NTT, ntt_launch_count(ilog2(NL)), ntt_launch(p.tables(ilog2(NL)), a, m, p.cw[nci], p.tmp, false, s));
+    RUN(PC_MERKLE, merkle_launch_count(NL), merkle_commit_launch(p.cw[nci], NL, p.tree[nci], s));
+    RUN(PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, s>>>(p.tree[nci] + 32 * (merkle_hashes(NL) - 1), tr + off));
+    // queries on the previous codeword
+    const int l = whir_query_count((int)cur);
+    if (l > kMaxQueries || l < 1) throw ArgError("prover: query count out of range");
+    const int depth = ilog2(L / 4);
+    QueryArgs qa;
+    qa.st = st;
+    qa.cw = p.cw[cwi];
+    qa.L = L;
+    qa.tree = p.tree[cwi];
+    qa.NL = NL;
+    qa.l = l;
+    qa.tr = tr;
+    qa.off_q = lay.rec(T_WHIR_QUERIES, l, 4);
+    qa.off_rep = lay.rec(T_WHIR_REPLIES, l * kWhirK, 16);
+    qa.off_ans = lay.rec(T_WHIR_ANSWERS, l, 16);
+    qa.off_path = lay.rec(T_WHIR_PATHS, l * depth, 32);
+    qa.off_comb = lay.rec(T_WHIR_COMBINE, l, 16);
+    qa.off_K = lay.rec(T_WHIR_K, 1, 16);
+    RUN(PC_QUERY, 1, k_whir_query<<<1, kMaxQueries, 0, s>>>(qa));
+    RUN(PC_UPDATE_BETAS, 2, update_betas_launch(p.vb[1], m, st, l, p.ub_scratch, s));
+    cwi = nci;
+    L = NL;
+    cur *= 2;
+    if (m <= (uint64_t)kWhirK) break;
+  }
+  uint64_t off_poly = lay.rec(T_FINAL_POLY, (uint32_t)m, 16);
+  uint64_t off_point = lay.rec(T_FINAL_POINT, ilog2(m), 16);
+  uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
+  RUN(PC_PROTOCOL, 1, k_final<<<1, 32, 0, s>>>(st, a, p.vb[1], (int)m, tr, off_poly, off_point, off_eval));
+#undef RUN
+}
+
+void Profiler::begin(int cat, cudaStream_t s) {
+  auto &v = ev[cat];
+  if (used[cat] == v.size()) {
+    cudaEvent_t a, b;
+    GBZ_CUDA(cudaEventCreate(&a));
+    GBZ_CUDA(cudaEventCreate(&b));
+    v.push_back({a, b});
+  }
+  GBZ_CUDA(cudaEventRecord(v[used[cat]].first, s));
+  open_cat = cat;
+}
+
+void Profiler::end(cudaStream_t s) {
+  auto &v = ev[open_cat];
+  GBZ_CUDA(cudaEventRecord(v[used[open_cat]].second, s));
+  used[open_cat]++;
+  open_cat = -1;
+}
+
+void Profiler::read(double ms[PC_COUNT], int counts[PC_COUNT]) {
+  for (int c = 0; c < PC_COUNT; c++) {
+    double t = 0;
+    for (size_t i = 0; i < used[c]; i++) {
+      float x = 0;
+      GBZ_CUDA(cudaEventSynchronize(ev[c][i].second));
+      GBZ_CUDA(cudaEventElapsedTime(&x, ev[c][i].first, ev[c][i].second));
+      t += x;
+    }
+    ms[c] = t;
+    if (counts) counts[c] = (int)used[c];
+  }
+}
+
+Profiler::~Profiler() {
+  for (int c = 0; c < PC_COUNT; c++)
+    for (auto &e : ev[c]) {
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+}
+
+uint32_t plan_error_flags(ProofPlan &p, cudaStream_t s) {
+  uint32_t e = 0;
+  GBZ_CUDA(cudaMemcpyAsync(&e, &p.st->error, 4, cudaMemcpyDeviceToHost, s));
+  GBZ_CUDA(cudaStreamSynchronize(s));
+  return e;
+}
+
+}  // namespace gbz

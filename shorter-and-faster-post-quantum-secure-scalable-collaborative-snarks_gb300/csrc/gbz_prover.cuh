@@ -1,0 +1,80 @@
+// Plan and enqueue interface of the single-party prover (gbz_prover.cu).
+#pragma once
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "gbz_internal.cuh"
+
+namespace gbz {
+
+// Transcript layout: record offsets are fixed by (logn, rate), so they are
+// computed once; the constant record headers are written at plan creation
+// and the kernels fill in the payloads.
+struct Layout {
+  struct Header {
+    uint64_t off;
+    uint32_t tag, count;
+  };
+  uint64_t len = 0;
+  bool record_headers = false;
+  std::vector<Header> headers;
+  // Appends a record of `count` units of `unit` bytes; returns the payload offset.
+  uint64_t rec(uint32_t tag, uint32_t count, uint32_t unit);
+};
+
+// Optional per-category CUDA-event timing of the kernels of a proof, on the
+// stream the kernels are launched on.
+enum ProfCat { PC_NTT = 0, PC_MERKLE, PC_SUMCHECK, PC_BETA, PC_UPDATE_BETAS, PC_QUERY, PC_PROTOCOL, PC_COUNT };
+struct Profiler {
+  bool enabled = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[PC_COUNT];
+  size_t used[PC_COUNT] = {0};
+  int open_cat = -1;
+  void begin(int cat, cudaStream_t s);
+  void end(cudaStream_t s);
+  void reset() { for (int c = 0; c < PC_COUNT; c++) used[c] = 0; }
+  // Total milliseconds per category since reset (synchronises on the events).
+  void read(double ms[PC_COUNT], int counts[PC_COUNT]);
+  ~Profiler();
+};
+
+// Device buffers and tables for proofs of one shape (n = 2^logn, rate).
+struct ProofPlan {
+  int logn = 0, rate = 0;
+  uint64_t n = 0, L = 0;
+  fe *w = nullptr;                // witness staging (host-input proofs)
+  fe *cw[2] = {nullptr, nullptr}; // codeword ping-pong (L, L/2)
+  uint8_t *tree[2] = {nullptr, nullptr};
+  fe *tmp = nullptr;              // NTT intermediate (L)
+  fe *va[2] = {nullptr, nullptr}; // folded first vector ping-pong (n/2 each)
+  fe *vb[2] = {nullptr, nullptr}; // folded second vector ping-pong
+  fe *beta = nullptr;             // eq table (n)
+  fe *partial = nullptr;          // per-CTA round-message partials
+  fe *ub_scratch = nullptr;       // update_betas power tables
+  ProofState *st = nullptr;
+  uint8_t *transcript = nullptr;
+  uint64_t transcript_bytes = 0;
+  Layout layout;
+  int launches = 0;               // kernel launches per proof (counted by the dry run)
+  int cat_launches[PC_COUNT] = {0};
+  Profiler *prof = nullptr;
+  std::map<int, NttTables> ntt;
+  std::vector<void *> allocs;
+
+  ProofPlan() = default;
+  ProofPlan(const ProofPlan &) = delete;
+  ProofPlan &operator=(const ProofPlan &) = delete;
+  ~ProofPlan();
+  void *dalloc(uint64_t bytes);
+  NttTables &tables(int lg);
+};
+
+std::unique_ptr<ProofPlan> plan_create(int logn, int rate);
+// Enqueues one proof on stream s (dry: only computes the layout).
+void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry);
+// Reads the device-side consistency flags (synchronises s).
+uint32_t plan_error_flags(ProofPlan &p, cudaStream_t s);
+int whir_query_count(int rate);
+
+}  // namespace gbz

@@ -1,0 +1,241 @@
+// Sumcheck round kernels, the eq (beta) table and the WHIR beta update.
+//
+// Round message (coSumcheck_MPI.cpp:199, Whir.cpp:215-221,
+// delegate_protocol.cpp:16-21): over pairs j of two vectors,
+//   H(x) = sum_j (a1 x + b1)(a2 x + b2),  a = v[2j+1] - v[2j], b = v[2j],
+// so H = (sum a1 a2, sum a1 b2 + b1 a2, sum b1 b2).  With
+// D = v1[2j+1] v2[2j+1] the middle term is D - A - C, three products per
+// pair instead of four (exact arithmetic, same value).
+// Fold (coSumcheck_MPI.cpp:215-218, Whir.cpp:223-231):
+//   v[j] = r (v[2j+1] - v[2j]) + v[2j].
+// The fold of round i and the message of round i+1 are one pass: each
+// thread reads four consecutive entries of both vectors, writes the two
+// folded entries of each and accumulates the next message from them.
+#include "gbz_internal.cuh"
+
+namespace gbz {
+
+namespace {
+
+constexpr int kScThreads = 256;
+
+__device__ __forceinline__ fe shfl_down_fe(fe v, int d) {
+  fe r;
+  r.re = __shfl_down_sync(0xffffffffu, v.re, d);
+  r.im = __shfl_down_sync(0xffffffffu, v.im, d);
+  return r;
+}
+
+// Block-wide sum of three field elements; result valid in thread 0.
+__device__ void block_sum3(fe &x, fe &y, fe &z) {
+  __shared__ fe red[3][kScThreads / 32];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    x = fadd(x, shfl_down_fe(x, d));
+    y = fadd(y, shfl_down_fe(y, d));
+    z = fadd(z, shfl_down_fe(z, d));
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][w] = x; red[1][w] = y; red[2][w] = z; }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    x = lane < nw ? red[0][lane] : fe_zero();
+    y = lane < nw ? red[1][lane] : fe_zero();
+    z = lane < nw ? red[2][lane] : fe_zero();
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      x = fadd(x, shfl_down_fe(x, d));
+      y = fadd(y, shfl_down_fe(y, d));
+      z = fadd(z, shfl_down_fe(z, d));
+    }
+  }
+}
+
+__device__ __forceinline__ void acc_pair(fe a0, fe a1, fe b0, fe b1, fe &A, fe &C, fe &D) {
+  A = fadd(A, fmul(fsub(a1, a0), fsub(b1, b0)));
+  C = fadd(C, fmul(a0, b0));
+  D = fadd(D, fmul(a1, b1));
+}
+
+// partial[3*blk + {0,1,2}] = (sum A, sum C, sum D) of the block.
+__global__ void __launch_bounds__(kScThreads)
+sc_reduce_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t pairs, fe *partial) {
+  fe A = fe_zero(), C = fe_zero(), D = fe_zero();
+  const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
+  for (uint64_t j = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; j < pairs; j += stride) {
+    fe a0 = a[2 * j], a1 = a[2 * j + 1], b0 = b[2 * j], b1 = b[2 * j + 1];
+    acc_pair(a0, a1, b0, b1, A, C, D);
+  }
+  block_sum3(A, C, D);
+  if (threadIdx.x == 0) {
+    partial[3 * blockIdx.x] = A;
+    partial[3 * blockIdx.x + 1] = C;
+    partial[3 * blockIdx.x + 2] = D;
+  }
+}
+
+// Fold (a, b) of length m by *chal into (a2, b2) of length m/2; when
+// reduce, accumulate the message of the folded pair sequence.
+__global__ void __launch_bounds__(kScThreads)
+sc_fold_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t m, const fe *chal,
+               fe *__restrict__ a2, fe *__restrict__ b2, int reduce, fe *partial) {
+  const fe r = *chal;
+  fe A = fe_zero(), C = fe_zero(), D = fe_zero();
+  const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
+  const uint64_t quads = m / 4;
+  for (uint64_t t = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; t < quads; t += stride) {
+    fe x0 = a[4 * t], x1 = a[4 * t + 1], x2 = a[4 * t + 2], x3 = a[4 * t + 3];
+    fe y0 = b[4 * t], y1 = b[4 * t + 1], y2 = b[4 * t + 2], y3 = b[4 * t + 3];
+    fe fa0 = fadd(fmul(r, fsub(x1, x0)), x0), fa1 = fadd(fmul(r, fsub(x3, x2)), x2);
+    fe fb0 = fadd(fmul(r, fsub(y1, y0)), y0), fb1 = fadd(fmul(r, fsub(y3, y2)), y2);
+    a2[2 * t] = fa0; a2[2 * t + 1] = fa1;
+    b2[2 * t] = fb0; b2[2 * t + 1] = fb1;
+    if (reduce) acc_pair(fa0, fa1, fb0, fb1, A, C, D);
+  }
+  if (m == 2 && blockIdx.x == 0 && threadIdx.x == 0) {  // fold to a single entry
+    a2[0] = fadd(fmul(r, fsub(a[1], a[0])), a[0]);
+    b2[0] = fadd(fmul(r, fsub(b[1], b[0])), b[0]);
+  }
+  if (!reduce) return;
+  block_sum3(A, C, D);
+  if (threadIdx.x == 0) {
+    partial[3 * blockIdx.x] = A;
+    partial[3 * blockIdx.x + 1] = C;
+    partial[3 * blockIdx.x + 2] = D;
+  }
+}
+
+// out = (a, b, c) of the round message from (A, C, D) partials.
+__global__ void __launch_bounds__(kScThreads) sc_sum_kernel(const fe *partial, int blocks, fe *out) {
+  fe A = fe_zero(), C = fe_zero(), D = fe_zero();
+  for (int i = threadIdx.x; i < blocks; i += kScThreads) {
+    A = fadd(A, partial[3 * i]);
+    C = fadd(C, partial[3 * i + 1]);
+    D = fadd(D, partial[3 * i + 2]);
+  }
+  block_sum3(A, C, D);
+  if (threadIdx.x == 0) {
+    out[0] = A;
+    out[1] = fsub(fsub(D, A), C);
+    out[2] = C;
+  }
+}
+
+// precompute_beta: thread t writes B[16t .. 16t+15].  The product over the
+// index bits above the low four is formed once, then the low four bits are
+// expanded like the reference (B[2j] = B_j - B_j r_i, B[2j+1] = B_j r_i).
+constexpr int kBetaLow = 4;
+__global__ void __launch_bounds__(256) beta_kernel(const fe *r, int nr, fe *B) {
+  __shared__ fe rs[64], om[64];
+  if (threadIdx.x < nr) {
+    rs[threadIdx.x] = r[threadIdx.x];
+    om[threadIdx.x] = fsub(fe_one(), r[threadIdx.x]);
+  }
+  __syncthreads();
+  const int low = nr < kBetaLow ? nr : kBetaLow;
+  const uint64_t groups = 1ull << (nr - low);
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= groups) return;
+  fe pre = fe_one();
+  for (int i = low; i < nr; i++) pre = fmul(pre, ((t >> (i - low)) & 1) ? rs[i] : om[i]);
+  fe e[1 << kBetaLow];
+  e[0] = pre;
+  int len = 1;
+  for (int i = low - 1; i >= 0; i--) {
+    for (int j = len - 1; j >= 0; j--) {
+      fe x = fmul(e[j], rs[i]);
+      e[2 * j + 1] = x;
+      e[2 * j] = fsub(e[j], x);
+    }
+    len <<= 1;
+  }
+  fe *o = B + (t << low);
+  for (int j = 0; j < (1 << low); j++) o[j] = e[j];
+}
+
+// update_betas: b[j] += sum_i c_i * w_i^j.  Thread tid of a CTA owns the
+// kUbPer consecutive entries starting at j0 = cta*kUbSpan + tid*kUbPer; it
+// starts each query's geometric run from s_i * pw_i[tid] (s_i = c_i w_i^{cta
+// start}, pw_i[t] = w_i^{t*kUbPer}) and steps it by w_i.
+constexpr int kUbThreads = 256;
+constexpr int kUbPer = 8;
+constexpr int kUbSpan = kUbThreads * kUbPer;
+
+__global__ void __launch_bounds__(kUbThreads) ub_table_kernel(const ProofState *st, int l, fe *pw) {
+  // pw[i*kUbThreads + t] = w_i^(t * kUbPer)
+  const int i = blockIdx.x, t = threadIdx.x;
+  if (i >= l) return;
+  pw[i * kUbThreads + t] = fpow(st->omega_q[i], (uint64_t)t * kUbPer);
+}
+
+__global__ void __launch_bounds__(kUbThreads)
+ub_kernel(fe *b, uint64_t nb, const ProofState *st, int l, const fe *pw) {
+  __shared__ fe s_start[kMaxQueries], s_w[kMaxQueries];
+  const uint64_t cta0 = (uint64_t)blockIdx.x * kUbSpan;
+  for (int i = threadIdx.x; i < l; i += kUbThreads) {
+    fe w = st->omega_q[i];
+    s_w[i] = w;
+    s_start[i] = fmul(st->comb[i], fpow(w, cta0));
+  }
+  __syncthreads();
+  const uint64_t j0 = cta0 + (uint64_t)threadIdx.x * kUbPer;
+  if (j0 >= nb) return;
+  fe acc[kUbPer];
+#pragma unroll
+  for (int k = 0; k < kUbPer; k++) acc[k] = fe_zero();
+  for (int i = 0; i < l; i++) {
+    fe w = s_w[i];
+    fe d = fmul(s_start[i], pw[i * kUbThreads + threadIdx.x]);
+#pragma unroll
+    for (int k = 0; k < kUbPer; k++) {
+      acc[k] = fadd(acc[k], d);
+      d = fmul(d, w);
+    }
+  }
+  const int cnt = (int)min((uint64_t)kUbPer, nb - j0);
+  for (int k = 0; k < cnt; k++) b[j0 + k] = fadd(b[j0 + k], acc[k]);
+}
+
+}  // namespace
+
+int sc_blocks(uint64_t pairs) {
+  uint64_t want = (pairs + kScThreads - 1) / kScThreads;
+  const uint64_t cap = 152 * 8;  // 8 CTAs per SM on 152 SMs, grid-stride beyond that
+  if (want > cap) want = cap;
+  return want ? (int)want : 1;
+}
+
+void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2, fe *b2, bool reduce,
+                    fe *partial, int blocks, cudaStream_t s) {
+  if (!chal) {
+    sc_reduce_kernel<<<blocks, kScThreads, 0, s>>>(a, b, m / 2, partial);
+  } else {
+    sc_fold_kernel<<<blocks, kScThreads, 0, s>>>(a, b, m, chal, a2, b2, reduce ? 1 : 0, partial);
+  }
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s) {
+  sc_sum_kernel<<<1, kScThreads, 0, s>>>(partial, blocks, out3);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s) {
+  if (nr < 0 || nr > 60) throw ArgError("beta table: bad number of variables");
+  const int low = nr < kBetaLow ? nr : kBetaLow;
+  const uint64_t groups = 1ull << (nr - low);
+  beta_kernel<<<(unsigned)((groups + 255) / 256), 256, 0, s>>>(r, nr, B);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s) {
+  if (l <= 0) return;
+  if (l > kMaxQueries) throw ArgError("update_betas: too many queries");
+  ub_table_kernel<<<l, kUbThreads, 0, s>>>(st, l, pw_scratch);
+  GBZ_CUDA(cudaGetLastError());
+  ub_kernel<<<(unsigned)((nb + kUbSpan - 1) / kUbSpan), kUbThreads, 0, s>>>(b, nb, st, l, pw_scratch);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+}  // namespace gbz

@@ -1,0 +1,355 @@
+"""Python binding of libgbz (include/gbz.h) with the reference's call names.
+
+The functions mirror the reference's C++ surface for the prover hot path:
+fft / pfft (utils.cpp:904, :1583), MT_commit_Blake (merkle_tree.cpp:195),
+open_tree_blake (merkle_tree.cpp:320), blake3_hash (Blake3_hash.cpp:5),
+Whir_Commit_initial (Whir.cpp:158), precompute_beta (utils.cpp:198),
+whir_sumcheck_step1/2 (Whir.cpp:215, :223), update_betas (Whir.cpp:325),
+hash_to_field (Fiat_Shamir.cpp:29), F::_random (fieldElement.cpp:119), and
+the single-party prover (prove).  Like the reference they operate in place
+where the reference does and return what the reference returns; unlike the
+reference they raise GbzError instead of calling exit().
+
+Field-element arrays are numpy uint64 arrays of shape (n, 2) (`real`,
+`img`) or torch tensors on the GPU with the same shape and dtype
+torch.uint64 / torch.int64 (device pointers are passed straight through).
+
+There is no CPU fallback: importing this module loads libgbz.so and every
+call runs on the GPU (host-side protocol helpers aside).  A missing library
+raises ImportError.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgbz.so")
+
+OK, EINVAL, ENOMEM, ECUDA, ECHECK, ESMALL = range(6)
+MEM_HOST, MEM_DEVICE = 0, 1
+P = (1 << 61) - 1
+
+# Every function include/gbz.h declares; tests check the library exports them.
+EXPORTS = (
+    "gbz_create", "gbz_destroy", "gbz_set_stream", "gbz_get_stream", "gbz_synchronize",
+    "gbz_status_string", "gbz_last_error", "gbz_host_alloc", "gbz_host_free", "gbz_device_alloc",
+    "gbz_device_free", "gbz_field_ops", "gbz_blake3_64", "gbz_fft", "gbz_rs_encode",
+    "gbz_merkle_commit_blake", "gbz_merkle_open_blake", "gbz_whir_commit", "gbz_precompute_beta",
+    "gbz_sumcheck_quadratic", "gbz_sumcheck_fold", "gbz_whir_update_betas", "gbz_hash_to_field",
+    "gbz_prng_seed", "gbz_prng_next", "gbz_prng_field", "gbz_field_ops_host",
+    "gbz_prove_transcript_bytes", "gbz_prove", "gbz_prove_launches", "gbz_profile_enable",
+    "gbz_profile_read",
+)
+
+PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
+
+
+class GbzError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (status %d): %s" % (_status_name(status), status, msg))
+        self.status = status
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libgbz.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, u64, i32, c_int = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_int
+    sig = {
+        "gbz_create": (c_int, [ctypes.POINTER(vp), c_int]),
+        "gbz_destroy": (None, [vp]),
+        "gbz_set_stream": (c_int, [vp, vp]),
+        "gbz_get_stream": (vp, [vp]),
+        "gbz_synchronize": (c_int, [vp]),
+        "gbz_status_string": (ctypes.c_char_p, [c_int]),
+        "gbz_last_error": (ctypes.c_char_p, [vp]),
+        "gbz_host_alloc": (c_int, [ctypes.POINTER(vp), u64]),
+        "gbz_host_free": (None, [vp]),
+        "gbz_device_alloc": (c_int, [vp, ctypes.POINTER(vp), u64]),
+        "gbz_device_free": (None, [vp, vp]),
+        "gbz_field_ops": (c_int, [vp, vp, vp, u64, vp, vp, vp, c_int]),
+        "gbz_blake3_64": (c_int, [vp, vp, vp, u64, c_int]),
+        "gbz_fft": (c_int, [vp, vp, c_int, c_int, c_int]),
+        "gbz_rs_encode": (c_int, [vp, vp, u64, c_int, vp, c_int]),
+        "gbz_merkle_commit_blake": (c_int, [vp, vp, u64, vp, c_int]),
+        "gbz_merkle_open_blake": (c_int, [vp, u64, u64, vp, ctypes.POINTER(ctypes.c_uint32)]),
+        "gbz_whir_commit": (c_int, [vp, vp, u64, c_int, vp, vp, c_int]),
+        "gbz_precompute_beta": (c_int, [vp, vp, c_int, vp, c_int]),
+        "gbz_sumcheck_quadratic": (c_int, [vp, vp, vp, u64, vp, c_int]),
+        "gbz_sumcheck_fold": (c_int, [vp, vp, u64, vp, c_int]),
+        "gbz_whir_update_betas": (c_int, [vp, vp, u64, vp, c_int, u64, vp, vp, c_int]),
+        "gbz_hash_to_field": (None, [vp, vp, c_int, vp]),
+        "gbz_prng_seed": (None, [vp, ctypes.c_uint32]),
+        "gbz_prng_next": (i32, [vp]),
+        "gbz_prng_field": (None, [vp, vp]),
+        "gbz_field_ops_host": (None, [vp, vp, u64, vp, vp, vp]),
+        "gbz_prove_transcript_bytes": (u64, [c_int, c_int]),
+        "gbz_prove": (c_int, [vp, vp, c_int, c_int, ctypes.c_uint32, vp, u64, c_int]),
+        "gbz_prove_launches": (c_int, [c_int, c_int]),
+        "gbz_profile_enable": (c_int, [vp, c_int]),
+        "gbz_profile_read": (c_int, [vp, c_int, c_int, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def _status_name(s):
+    return lib.gbz_status_string(s).decode()
+
+
+def _ptr(a):
+    """Address of a numpy array or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch.Tensor
+
+
+def _mem(a):
+    if isinstance(a, np.ndarray):
+        return MEM_HOST
+    return MEM_DEVICE if a.is_cuda else MEM_HOST
+
+
+def fe_array(n):
+    return np.zeros((n, 2), dtype=np.uint64)
+
+
+def _fe(a):
+    if isinstance(a, np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        return a.reshape(-1, 2)
+    return a
+
+
+class Context:
+    """One device, one stream (gbz_ctx)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        st = lib.gbz_create(ctypes.byref(h), device)
+        if st != OK:
+            raise GbzError(st, "gbz_create failed")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib.gbz_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st):
+        if st != OK:
+            raise GbzError(st, lib.gbz_last_error(self.h).decode())
+
+    def synchronize(self):
+        self.check(lib.gbz_synchronize(self.h))
+
+    def set_stream(self, stream_handle):
+        self.check(lib.gbz_set_stream(self.h, stream_handle))
+
+    # ---------------------------------------------------------- primitives
+    def field_ops(self, a, b):
+        a, b = _fe(a), _fe(b)
+        n = a.shape[0]
+        outs = [fe_array(n) for _ in range(3)]
+        self.check(lib.gbz_field_ops(self.h, _ptr(a), _ptr(b), n, *[_ptr(o) for o in outs], MEM_HOST))
+        return outs
+
+    def blake3_hash(self, blocks):
+        """blake3_hash over count 64-byte blocks -> (count, 32) uint8."""
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 64)
+        out = np.zeros((blocks.shape[0], 32), dtype=np.uint8)
+        self.check(lib.gbz_blake3_64(self.h, _ptr(blocks), _ptr(out), blocks.shape[0], MEM_HOST))
+        return out
+
+    def fft(self, arr, logn, inverse):
+        """fft(arr, logn, flag): in place (numpy or CUDA tensor)."""
+        if isinstance(arr, np.ndarray):
+            assert arr.dtype == np.uint64 and arr.flags.c_contiguous and arr.size == 2 << logn
+        self.check(lib.gbz_fft(self.h, _ptr(arr), logn, int(bool(inverse)), _mem(arr)))
+        return arr
+
+    def pfft(self, arr, logn, flag=False):
+        """pfft computes the forward transform whatever the flag (utils.cpp:1583-1593)."""
+        if (1 << logn) // (16 * 16) <= 4:
+            return self.fft(arr, logn, flag)
+        return self.fft(arr, logn, False)
+
+    def rs_encode(self, arr, rate):
+        arr = _fe(arr)
+        m = arr.shape[0]
+        out = fe_array(m * rate)
+        self.check(lib.gbz_rs_encode(self.h, _ptr(arr), m, rate, _ptr(out), MEM_HOST))
+        return out
+
+    def MT_commit_Blake(self, leafs):
+        """Merkle levels as a list of (count, 32) uint8 arrays, leaves first."""
+        leafs = _fe(leafs)
+        N = leafs.shape[0]
+        flat = np.zeros((N // 2 - 1, 32), dtype=np.uint8)
+        self.check(lib.gbz_merkle_commit_blake(self.h, _ptr(leafs), N, _ptr(flat), MEM_HOST))
+        return split_levels(flat, N)
+
+    def merkle_commit_flat(self, leafs):
+        leafs = _fe(leafs)
+        N = leafs.shape[0]
+        flat = np.zeros((N // 2 - 1, 32), dtype=np.uint8)
+        self.check(lib.gbz_merkle_commit_blake(self.h, _ptr(leafs), N, _ptr(flat), MEM_HOST))
+        return flat
+
+    def Whir_Commit_initial(self, arr, rate):
+        """(codeword, flat Merkle levels) of arr encoded at rate."""
+        arr = _fe(arr)
+        m = arr.shape[0]
+        L = m * rate
+        cw = fe_array(L)
+        flat = np.zeros((L // 2 - 1, 32), dtype=np.uint8)
+        self.check(lib.gbz_whir_commit(self.h, _ptr(arr), m, rate, _ptr(cw), _ptr(flat), MEM_HOST))
+        return cw, flat
+
+    def precompute_beta(self, r):
+        r = _fe(r)
+        nr = r.shape[0]
+        out = fe_array(1 << nr)
+        self.check(lib.gbz_precompute_beta(self.h, _ptr(r), nr, _ptr(out), MEM_HOST))
+        return out
+
+    def whir_sumcheck_step1(self, arr, b):
+        """quadratic_poly (a, b, c) as a (3, 2) array."""
+        arr, b = _fe(arr), _fe(b)
+        out = np.zeros(6, dtype=np.uint64)
+        self.check(lib.gbz_sumcheck_quadratic(self.h, _ptr(arr), _ptr(b), arr.shape[0], _ptr(out), _mem(arr)))
+        return out.reshape(3, 2)
+
+    def sumcheck_fold(self, v, r):
+        """Returns the folded half (the reference resizes v to it)."""
+        v = np.array(_fe(v), copy=True)
+        r = np.ascontiguousarray(r, dtype=np.uint64)
+        self.check(lib.gbz_sumcheck_fold(self.h, _ptr(v), v.shape[0], _ptr(r), MEM_HOST))
+        return v[: v.shape[0] // 2].copy()
+
+    def whir_sumcheck_step2(self, arr, b, c):
+        return self.sumcheck_fold(arr, c), self.sumcheck_fold(b, c)
+
+    def update_betas(self, b, queries, n, r):
+        """update_betas(b, queries, n) with the drawn r; returns (b', challenges)."""
+        b = np.array(_fe(b), copy=True)
+        q = np.ascontiguousarray(queries, dtype=np.int32)
+        r = np.ascontiguousarray(r, dtype=np.uint64)
+        ch = fe_array(len(q))
+        self.check(lib.gbz_whir_update_betas(self.h, _ptr(b), b.shape[0], _ptr(q), len(q), n, _ptr(r),
+                                             _ptr(ch), MEM_HOST))
+        return b, ch
+
+    # ------------------------------------------------------------ profiling
+    def profile_enable(self, on=True):
+        self.check(lib.gbz_profile_enable(self.h, int(bool(on))))
+
+    def profile_read(self, logn, rate):
+        """{category: (milliseconds, launch groups)} since the last read."""
+        ms = np.zeros(len(PROF_CATEGORIES), dtype=np.float64)
+        groups = np.zeros(len(PROF_CATEGORIES), dtype=np.int32)
+        self.check(lib.gbz_profile_read(self.h, logn, rate, _ptr(ms), _ptr(groups)))
+        return {c: (float(ms[i]), int(groups[i])) for i, c in enumerate(PROF_CATEGORIES)}
+
+    # --------------------------------------------------------------- prover
+    def prove(self, witness, logn, rate, prng_seed=1, out=None):
+        """Transcript bytes of one single-party proof (see include/gbz.h)."""
+        nbytes = transcript_bytes(logn, rate)
+        if nbytes == 0:
+            raise GbzError(EINVAL, "unsupported proof shape 2^%d at rate %d" % (logn, rate))
+        if out is None:
+            out = np.zeros(nbytes, dtype=np.uint8)
+        w = _fe(witness)
+        mem = _mem(w)
+        self.check(lib.gbz_prove(self.h, _ptr(w), logn, rate, prng_seed, _ptr(out), nbytes, mem))
+        return out
+
+
+def prove_launches(logn, rate):
+    return int(lib.gbz_prove_launches(logn, rate))
+
+
+def split_levels(flat, N):
+    levels, off, cnt = [], 0, N // 4
+    while cnt >= 1:
+        levels.append(flat[off:off + cnt])
+        off += cnt
+        cnt //= 2
+    return levels
+
+
+def open_tree_blake(flat_levels, N, pos):
+    flat_levels = np.ascontiguousarray(flat_levels, dtype=np.uint8)
+    depth = (N // 4).bit_length() - 1
+    path = np.zeros((max(depth, 1), 32), dtype=np.uint8)
+    d = ctypes.c_uint32()
+    st = lib.gbz_merkle_open_blake(_ptr(flat_levels), N, pos, _ptr(path), ctypes.byref(d))
+    if st != OK:
+        raise GbzError(st, "open_tree_blake: position out of range")
+    return path[: d.value]
+
+
+def transcript_bytes(logn, rate):
+    return int(lib.gbz_prove_transcript_bytes(logn, rate))
+
+
+def hash_to_field(state, elems):
+    """hash_to_field with an explicit chain state (numpy uint64[2], updated)."""
+    elems = np.ascontiguousarray(elems, dtype=np.uint64).reshape(-1, 2)
+    out = np.zeros(2, dtype=np.uint64)
+    lib.gbz_hash_to_field(_ptr(state), _ptr(elems), elems.shape[0], _ptr(out))
+    return out
+
+
+class Prng(ctypes.Structure):
+    """The glibc random() stream that F::_random and rand() draw from."""
+    _fields_ = [("tbl", ctypes.c_int32 * 31), ("f", ctypes.c_int32), ("r", ctypes.c_int32)]
+
+    def __init__(self, seed=1):
+        super().__init__()
+        lib.gbz_prng_seed(ctypes.addressof(self), seed)
+
+    def next(self):
+        return lib.gbz_prng_next(ctypes.addressof(self))
+
+    def field(self):
+        out = np.zeros(2, dtype=np.uint64)
+        lib.gbz_prng_field(ctypes.addressof(self), _ptr(out))
+        return out
+
+
+def field_ops_host(a, b):
+    a, b = _fe(a), _fe(b)
+    n = a.shape[0]
+    outs = [fe_array(n) for _ in range(3)]
+    lib.gbz_field_ops_host(_ptr(a), _ptr(b), n, *[_ptr(o) for o in outs])
+    return outs
+
+
+def parse_transcript(buf):
+    """[(tag, count, payload bytes)] of a transcript."""
+    buf = bytes(buf)
+    out, off = [], 0
+    units = {1: 32, 9: 32, 13: 32, 10: 4}
+    while off < len(buf):
+        tag, count = np.frombuffer(buf, dtype=np.uint32, count=2, offset=off)
+        unit = units.get(int(tag), 16)
+        out.append((int(tag), int(count), buf[off + 8: off + 8 + unit * int(count)]))
+        off += 8 + unit * int(count)
+    return out

@@ -1,0 +1,123 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs oracle/_ref/ref_driver (built from the unmodified reference sources by
+oracle/ref/Makefile; x86-64 only) and stores either the full output (small
+cases) or the SHA-256 of the exact output bytes (large cases) together with
+the parameters that regenerate the inputs.  Run from the repository root:
+
+    make -C oracle/ref && python tests/golden/make_golden.py
+
+The fixtures are what pins the CPU restatement in oracle/gbz_oracle.c; the
+GPU tests are then checked against that restatement and these fixtures.
+"""
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+# Witness seed convention: 0x5EED0000 + config * 2^16 + instance.
+SEED_C1 = 0x5EED0000 + 1 * 65536
+SEED_C2 = 0x5EED0000 + 2 * 65536
+
+
+def run(*args):
+    t = time.time()
+    out = subprocess.run([DRIVER, *map(str, args)], check=True, capture_output=True)
+    return out.stdout, time.time() - t
+
+
+def save(name, data):
+    with open(os.path.join(HERE, name), "wb") as f:
+        f.write(data)
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        sys.exit("build the reference driver first: make -C oracle/ref")
+    manifest = {"generator": "tests/golden/make_golden.py", "driver": "oracle/ref/ref_driver.cpp"}
+
+    data, _ = run("field", 200, 11)
+    save("field.bin", data)
+    manifest["field"] = {"file": "field.bin", "count": 200, "seed": 11}
+
+    data, _ = run("blake3", 64, 12)
+    save("blake3.bin", data)
+    manifest["blake3"] = {"file": "blake3.bin", "count": 64, "seed": 12}
+
+    data, _ = run("fs", 12, 13)
+    save("fs.bin", data)
+    manifest["fs"] = {"file": "fs.bin", "count": 12, "seed": 13}
+
+    prng = {}
+    for s in (1, 3396, 42, 123457):
+        data, _ = run("prng", 24, s)
+        save(f"prng_{s}.bin", data)
+        prng[str(s)] = {"file": f"prng_{s}.bin", "count": 24}
+    manifest["prng"] = prng
+
+    data, _ = run("beta", 6, 14)
+    save("beta.bin", data)
+    manifest["beta"] = {"file": "beta.bin", "logn": 6, "seed": 14}
+
+    data, _ = run("tensor", 12, 2, 32, 15)
+    save("tensor.bin", data)
+    manifest["tensor"] = {"file": "tensor.bin", "logn": 12, "logk": 2, "count": 32, "seed": 15}
+
+    data, _ = run("betas", 6, 10, 20, 16, 1)
+    save("betas.bin", data)
+    manifest["betas"] = {"file": "betas.bin", "logb": 6, "logN": 10, "l": 20, "seed": 16, "prng_seed": 1}
+
+    fft = []
+    data, _ = run("fft", 6, 0, 17)
+    save("fft_6_fwd.bin", data)
+    fft.append({"logn": 6, "inverse": 0, "seed": 17, "file": "fft_6_fwd.bin"})
+    data, _ = run("fft", 6, 1, 18)
+    save("fft_6_inv.bin", data)
+    fft.append({"logn": 6, "inverse": 1, "seed": 18, "file": "fft_6_inv.bin"})
+    for logn, inv, seed in [(1, 0, 19), (2, 1, 20), (10, 0, 21), (12, 1, 22), (16, 0, 23), (20, 0, 24)]:
+        data, _ = run("fft", logn, inv, seed)
+        fft.append({"logn": logn, "inverse": inv, "seed": seed, "sha256": hashlib.sha256(data).hexdigest()})
+    for logn, seed in [(14, 25), (18, 26)]:
+        data, _ = run("pfft", logn, seed)
+        fft.append({"logn": logn, "inverse": 0, "seed": seed, "pfft": 1,
+                    "sha256": hashlib.sha256(data).hexdigest()})
+    manifest["fft"] = fft
+
+    merkle = []
+    data, _ = run("merkle", 5, 27)
+    save("merkle_5.bin", data)
+    merkle.append({"logN": 5, "seed": 27, "file": "merkle_5.bin"})
+    for logN, seed in [(2, 28), (3, 29), (10, 30), (16, 31), (20, 32)]:
+        data, _ = run("merkle", logN, seed)
+        merkle.append({"logN": logN, "seed": seed, "sha256": hashlib.sha256(data).hexdigest()})
+    manifest["merkle"] = merkle
+
+    proofs = []
+    data, _ = run("prove", 6, 4, 33, 1, 1)
+    save("prove_6_4.bin", data)
+    proofs.append({"logn": 6, "rate": 4, "seed": 33, "prng_seed": 1, "file": "prove_6_4.bin"})
+    cases = [(5, 2, 34, 1), (7, 2, 35, 1), (8, 4, 36, 7), (10, 2, 37, 1), (11, 4, 38, 99),
+             (12, 2, 39, 1), (14, 4, 40, 1), (16, 2, 41, 5),
+             (18, 4, SEED_C1, 1),   # configuration 1: n = 2^18, rate 1/4
+             (24, 2, SEED_C2, 1)]   # configuration 2: n = 2^24, rate 1/2
+    for logn, rate, seed, ps in cases:
+        data, dt = run("prove", logn, rate, seed, ps, 1)
+        proofs.append({"logn": logn, "rate": rate, "seed": seed, "prng_seed": ps, "bytes": len(data),
+                       "sha256": hashlib.sha256(data).hexdigest(), "ref_seconds": round(dt, 3)})
+        print(f"prove 2^{logn} rate {rate}: {len(data)} B in {dt:.2f} s", flush=True)
+    manifest["prove"] = proofs
+
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+    print("wrote", os.path.join(HERE, "manifest.json"))
+
+
+if __name__ == "__main__":
+    main()

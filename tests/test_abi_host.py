@@ -1,0 +1,124 @@
+"""libgbz on the host: exports, host-side protocol helpers, transcript layout.
+
+CPU only: nothing here launches a kernel.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, edge_fe, rand_fe
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "gbz.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbz_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_function(gbz):
+    names = header_functions()
+    assert len(names) >= 25
+    out = subprocess.run(["nm", "-D", "--defined-only", gbz.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r"\bT (gbz_[a-z0-9_]+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    assert set(gbz.EXPORTS) == set(names)
+    for n in names:
+        assert hasattr(gbz.lib, n)
+
+
+def test_library_is_built_for_sm103a(gbz):
+    out = subprocess.run(["cuobjdump", "--list-elf", gbz.LIB_PATH], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_host_field_twin_matches_oracle(gbz, oracle):
+    rng = np.random.default_rng(5)
+    a, b = edge_fe()
+    ra, rb = rand_fe(rng, 4000), rand_fe(rng, 4000)
+    a, b = np.concatenate([a, ra]), np.concatenate([b, rb])
+    s, d, p = gbz.field_ops_host(a, b)
+    oa, osub, om, _, _ = oracle.field_ops(a, b)
+    assert np.array_equal(s, oa)
+    assert np.array_equal(d, osub)
+    assert np.array_equal(p, om)
+
+
+def test_host_fiat_shamir_matches_oracle(gbz, oracle):
+    rng = np.random.default_rng(6)
+    st1 = np.zeros(2, dtype=np.uint64)
+    st2 = np.zeros(2, dtype=np.uint64)
+    for k in range(1, 6):
+        e = rand_fe(rng, k)
+        assert np.array_equal(gbz.hash_to_field(st1, e), oracle.hash_to_field(st2, e))
+        assert np.array_equal(st1, st2)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 42, 3396, 2**32 - 1])
+def test_host_prng_matches_oracle(gbz, oracle, seed):
+    g1, g2 = gbz.Prng(seed), oracle.Prng(seed)
+    for _ in range(50):
+        assert np.array_equal(g1.field(), g2.field())
+    assert [g1.next() for _ in range(300)] == [g2.next() for _ in range(300)]
+
+
+@pytest.mark.parametrize("logn,rate", [(3, 2), (4, 4), (5, 2), (6, 4), (9, 8), (10, 2), (13, 4), (16, 2), (18, 4),
+                                       (20, 2), (24, 2)])
+def test_transcript_layout_matches_oracle(gbz, oracle, logn, rate):
+    assert gbz.transcript_bytes(logn, rate) == oracle.transcript_bytes(logn, rate)
+
+
+def test_transcript_layout_matches_oracle_records(gbz, oracle):
+    """Record tags and counts, not only the length (the oracle writes them)."""
+    for logn, rate in [(5, 2), (8, 4), (11, 4)]:
+        w = oracle.witness(3, 1 << logn)
+        t = oracle.prove(w, logn, rate)
+        recs = gbz.parse_transcript(t)
+        assert sum(8 + len(p) for _, _, p in recs) == len(t) == gbz.transcript_bytes(logn, rate)
+        assert recs[0][0] == 1 and recs[-1][0] == 18
+
+
+def test_invalid_shapes_are_rejected_without_gpu(gbz):
+    assert gbz.transcript_bytes(2, 4) == 0      # witness too small
+    assert gbz.transcript_bytes(10, 3) == 0     # rate not a power of two
+    assert gbz.transcript_bytes(27, 2) == 0     # beyond the supported size
+    flat = np.zeros((31, 32), dtype=np.uint8)
+    with pytest.raises(gbz.GbzError):
+        gbz.open_tree_blake(flat, 64, 16)       # only 16 leaves
+    path = gbz.open_tree_blake(flat, 64, 15)
+    assert path.shape == (4, 32)
+
+
+def _gpu_count():
+    try:
+        rt = ctypes.CDLL("libcudart.so")
+    except OSError:
+        return 0
+    n = ctypes.c_int(0)
+    return n.value if rt.cudaGetDeviceCount(ctypes.byref(n)) == 0 else 0
+
+
+def test_context_creation_fails_loudly_without_gpu(gbz):
+    if _gpu_count() > 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(gbz.GbzError) as e:
+        gbz.Context(0)
+    assert e.value.status == gbz.ECUDA
+
+
+def test_missing_library_is_an_import_error(tmp_path, monkeypatch):
+    """No CPU fallback: the binding refuses to load without libgbz.so."""
+    import importlib.util
+    import conftest
+    spec = importlib.util.spec_from_file_location("gbz_copy", os.path.join(conftest.PKG, "gbz.py"))
+    mod = importlib.util.module_from_spec(spec)
+    monkeypatch.setattr(os.path, "exists", lambda p: False if p.endswith("libgbz.so") else True)
+    with pytest.raises(ImportError):
+        spec.loader.exec_module(mod)
