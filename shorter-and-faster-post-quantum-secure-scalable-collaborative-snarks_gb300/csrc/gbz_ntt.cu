@@ -20,6 +20,8 @@
 // stages with __syncthreads between them, and applies the outer twiddle
 // and the inverse scale on the way out.  Groups of B >= 2 neighbouring
 // columns make the strided pass read whole 32-byte sectors.
+#include <algorithm>
+
 #include "gbz_internal.cuh"
 
 namespace gbz {
@@ -28,82 +30,233 @@ namespace {
 
 constexpr int kSubLog = 13;          // largest sub-transform held in shared memory
 constexpr int kTwLoBits = 12;        // outer twiddle table split
-constexpr int kThreads = 512;
+constexpr int kMaxThreads = 1024;
+constexpr int kCtaElems = 1 << kSubLog;  // most elements staged per CTA
+constexpr int kPerThread = 8;            // elements per thread (CTA = max(32, E/8) threads)
 
 struct PassArgs {
   const fe *in;
   fe *out;
   uint64_t n_valid;
   uint64_t in_gstride, in_jstride, out_gstride, out_kstride;
-  const fe *wsub;    // omega_{2^13}^t, t < 2^12
+  const fe *wh;      // omega_{2^13}^t, t < 2^12 (first half), direction-specific
   const fe *tw_lo;   // omega_L^t, t < 2^12 (nullptr: no outer twiddle)
   const fe *tw_hi;   // omega_L^{2^12 t}
   fe scale;
-  int logS, logB, has_scale;
+  int logS, logB, has_scale, inverse;
 };
 
-__device__ __forceinline__ uint32_t brev_bits(uint32_t x, int bits) {
-  return bits ? __brev(x) >> (32 - bits) : 0u;
+// Shared-memory swizzle: element a lives at a ^ ((a >> 3) & 7), which keeps
+// both contiguous runs and stride-8 runs of 16-byte elements free of bank
+// conflicts.
+__device__ __forceinline__ uint32_t swz(uint32_t a) { return a ^ ((a >> 3) & 7u); }
+
+// ---- lazy arithmetic inside one radix-8 butterfly -----------------------
+// Values are kept below k*p (k <= 8 < 2^64 / p) and reduced once at the end.
+// p - x for 0 <= x <= p is a bitwise complement within 61 bits.
+__device__ __forceinline__ uint64_t lz_add(uint64_t a, uint64_t b) { return a + b; }
+// a - b + m*p for b < m*p (m a power of two times p keeps it cheap: kp - b).
+__device__ __forceinline__ uint64_t lz_sub(uint64_t a, uint64_t b, uint64_t mp) { return a + (mp - b); }
+// Fold any 64-bit value to [0, p] (p itself stands for zero).
+__device__ __forceinline__ uint64_t fold(uint64_t x) { return (x & P) + (x >> 61); }
+__device__ __forceinline__ uint64_t fold2(uint64_t x) { return fold(fold(x)); }
+// x * 2^k mod p for x in [0, p]: a rotation of the 61-bit word (p maps to p).
+__device__ __forceinline__ uint64_t rotp(uint64_t x, int k) { return ((x << k) & P) | (x >> (61 - k)); }
+__device__ __forceinline__ uint64_t canon(uint64_t x) {  // [0, p + 7] -> [0, p)
+  return x >= P ? x - P : x;
 }
 
-__global__ void __launch_bounds__(kThreads) ntt_pass_kernel(PassArgs a) {
-  extern __shared__ fe sm[];
-  const int logS = a.logS, logB = a.logB;
-  const uint32_t S = 1u << logS, total = S << logB;
+struct lz {
+  uint64_t re, im;
+};
+__device__ __forceinline__ lz lz_of(fe x) { return lz{x.re, x.im}; }
+__device__ __forceinline__ lz lzadd(lz a, lz b) { return lz{lz_add(a.re, b.re), lz_add(a.im, b.im)}; }
+__device__ __forceinline__ lz lzsub(lz a, lz b, uint64_t mp) { return lz{lz_sub(a.re, b.re, mp), lz_sub(a.im, b.im, mp)}; }
+__device__ __forceinline__ fe lz_canon(lz a) { return fe_make(canon(fold(a.re)), canon(fold(a.im))); }
+
+// Multiplications by the small roots on lazy values below 2p.
+// getRootOfUnity(2) = -i and getRootOfUnity(3) = 2^30 (1 - i).
+template <bool INV>
+__device__ __forceinline__ lz lz_w4(lz x) {  // forward * (-i), inverse * i; input < 2p, output < 2p
+  const uint64_t p2 = 2 * P;
+  return INV ? lz{p2 - x.im, x.re} : lz{x.im, p2 - x.re};
+}
+template <bool INV>
+__device__ __forceinline__ lz lz_w8(lz x) {  // forward * 2^30 (1 - i), inverse * 2^30 (1 + i); output <= p
+  const uint64_t s = fold2(x.re + x.im), d = INV ? fold2(x.re + (2 * P - x.im)) : fold2(x.im + (2 * P - x.re));
+  return INV ? lz{rotp(d, 30), rotp(s, 30)} : lz{rotp(s, 30), rotp(d, 30)};
+}
+template <bool INV>
+__device__ __forceinline__ lz lz_w8_3(lz x) {  // forward * 2^30 (-1 - i), inverse * 2^30 (-1 + i); output <= p
+  const uint64_t s = fold2(x.re + x.im), ns = P - s;
+  const uint64_t d = INV ? fold2(x.re + (2 * P - x.im)) : fold2(x.im + (2 * P - x.re));
+  return INV ? lz{rotp(ns, 30), rotp(d, 30)} : lz{rotp(d, 30), rotp(ns, 30)};
+}
+
+// In-register DFTs with natural-order output: V[k] = sum_q v[q] w_R^{qk}.
+// Inputs canonical, outputs canonical; additions in between are lazy.
+template <bool INV>
+__device__ __forceinline__ void dft2(fe *v) {
+  fe a = v[0], b = v[1];
+  v[0] = fadd(a, b);
+  v[1] = fsub(a, b);
+}
+template <bool INV>
+__device__ __forceinline__ void dft4(fe *v) {
+  fe c0 = fadd(v[0], v[2]), c1 = fadd(v[1], v[3]);
+  fe d0 = fsub(v[0], v[2]), d1 = fsub(v[1], v[3]);
+  d1 = INV ? fe_make(subp(0, d1.im), d1.re) : fe_make(d1.im, subp(0, d1.re));
+  v[0] = fadd(c0, c1);
+  v[2] = fsub(c0, c1);
+  v[1] = fadd(d0, d1);
+  v[3] = fsub(d0, d1);
+}
+template <bool INV>
+__device__ __forceinline__ void dft8(fe *v) {
+  const uint64_t P2 = 2 * P, P4 = 4 * P;
+  lz a[4], b[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {  // < 2p
+    a[q] = lzadd(lz_of(v[q]), lz_of(v[q + 4]));
+    b[q] = lzsub(lz_of(v[q]), lz_of(v[q + 4]), P);
+  }
+  b[1] = lz_w8<INV>(b[1]);    // <= p
+  b[2] = lz_w4<INV>(b[2]);    // < 2p
+  b[3] = lz_w8_3<INV>(b[3]);  // <= p
+  // two radix-4 DFTs on inputs < 2p: c < 4p, d < 4p, outputs < 8p
+  lz out[8];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    lz *x = h ? b : a;
+    lz c0 = lzadd(x[0], x[2]), c1 = lzadd(x[1], x[3]);
+    lz d0 = lzsub(x[0], x[2], P2), d1 = lzsub(x[1], x[3], P2);
+    // d1 * w4 on a value < 4p: fold to <= p first
+    d1 = lz{fold(d1.re), fold(d1.im)};
+    d1 = INV ? lz{P2 - d1.im, d1.re} : lz{d1.im, P2 - d1.re};  // < 2p
+    out[h + 0] = lzadd(c0, c1);       // V[0 + h]
+    out[h + 4] = lzsub(c0, c1, P4);   // V[4 + h]
+    out[h + 2] = lzadd(d0, d1);       // V[2 + h]
+    out[h + 6] = lzsub(d0, d1, P4);   // V[6 + h]
+  }
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[k] = lz_canon(out[k]);
+}
+
+// omega_S^e from the half table T[t] = omega_S^t (t < S/2):
+// omega_S^{t + S/2} = -omega_S^t.
+__device__ __forceinline__ fe twiddle(const fe *T, uint32_t e, int logS) {
+  const uint32_t hshift = logS - 1;
+  const fe w = T[e & ((1u << hshift) - 1)];
+  if (e >> hshift) return fe_make(w.re ? P - w.re : 0, w.im ? P - w.im : 0);
+  return w;
+}
+
+// One radix-R Stockham stage over E staged elements (B sub-transforms of
+// length S = 2^logS), Ns = product of the earlier radices:
+//   butterfly (b, j): v[r] = x[j + r S/R] * omega_{Ns R}^{r (j mod Ns)},
+//   DFT_R(v), x'[(j/Ns) Ns R + (j mod Ns) + r Ns] = v[r].
+template <int R, bool INV>
+__device__ __forceinline__ void stockham_stage(fe *sm, const fe *T, int logS, int logE, int logNs) {
+  constexpr int LOGR = R == 8 ? 3 : (R == 4 ? 2 : 1);
+  constexpr int PER = kPerThread / R;
+  const int logSR = logS - LOGR;
+  const uint32_t nb = 1u << (logE - LOGR);
+  fe v[PER * R];
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const uint32_t u = threadIdx.x + i * blockDim.x;
+    if (u < nb) {
+      const uint32_t b = u >> logSR, j = u & ((1u << logSR) - 1);
+      const uint32_t base = (b << logS) + j;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[i * R + r] = sm[swz(base + ((uint32_t)r << logSR))];
+      if (logNs > 0) {
+        const uint32_t k = j & ((1u << logNs) - 1);
+        const int sh = logS - logNs - LOGR;
+#pragma unroll
+        for (int r = 1; r < R; r++) v[i * R + r] = fmul(v[i * R + r], twiddle(T, (r * k) << sh, logS));
+      }
+      if (R == 8) dft8<INV>(&v[i * R]);
+      else if (R == 4) dft4<INV>(&v[i * R]);
+      else dft2<INV>(&v[i * R]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const uint32_t u = threadIdx.x + i * blockDim.x;
+    if (u < nb) {
+      const uint32_t b = u >> logSR, j = u & ((1u << logSR) - 1);
+      const uint32_t k = j & ((1u << logNs) - 1);
+      const uint32_t dst = (b << logS) + ((j >> logNs) << (logNs + LOGR)) + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) sm[swz(dst + ((uint32_t)r << logNs))] = v[i * R + r];
+    }
+  }
+  __syncthreads();
+}
+
+template <bool INV>
+__device__ void stockham(fe *sm, const fe *T, int logS, int logE) {
+  int logNs = 0;
+  const int rem = logS % 3;
+  if (rem == 1) {
+    stockham_stage<2, INV>(sm, T, logS, logE, logNs);
+    logNs += 1;
+  } else if (rem == 2) {
+    stockham_stage<4, INV>(sm, T, logS, logE, logNs);
+    logNs += 2;
+  }
+  for (; logNs < logS; logNs += 3) stockham_stage<8, INV>(sm, T, logS, logE, logNs);
+}
+
+__global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
+  extern __shared__ fe smem[];
+  const int logS = a.logS, logB = a.logB, logE = logS + logB;
+  const uint32_t S = 1u << logS, total = 1u << logE;
+  fe *sm = smem;
+  fe *T = smem + total;  // S/2 twiddles omega_S^t
   const uint64_t g0 = (uint64_t)blockIdx.x << logB;
 
-  // Load: bit-reversed positions inside each sub-transform.
+  if (logS >= 1) {
+    const uint32_t nT = S >> 1;
+    for (uint32_t t = threadIdx.x; t < nT; t += blockDim.x) T[t] = a.wh[t << (kSubLog - logS)];
+  }
   if (a.in_jstride == 1) {
-    for (uint32_t e = threadIdx.x; e < total; e += kThreads) {
-      uint32_t b = e >> logS, j = e & (S - 1);
-      uint64_t addr = (g0 + b) * a.in_gstride + j;
-      fe v = addr < a.n_valid ? a.in[addr] : fe_zero();
-      sm[(b << logS) + brev_bits(j, logS)] = v;
+    for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
+      const uint32_t b = e >> logS, j = e & (S - 1);
+      const uint64_t addr = (g0 + b) * a.in_gstride + j;
+      sm[swz(e)] = addr < a.n_valid ? a.in[addr] : fe_zero();
     }
   } else {
-    for (uint32_t e = threadIdx.x; e < total; e += kThreads) {
-      uint32_t b = e & ((1u << logB) - 1), j = e >> logB;
-      uint64_t addr = (g0 + b) * a.in_gstride + (uint64_t)j * a.in_jstride;
-      fe v = addr < a.n_valid ? a.in[addr] : fe_zero();
-      sm[(b << logS) + brev_bits(j, logS)] = v;
+    for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
+      const uint32_t b = e & ((1u << logB) - 1), j = e >> logB;
+      const uint64_t addr = (g0 + b) * a.in_gstride + (uint64_t)j * a.in_jstride;
+      sm[swz((b << logS) + j)] = addr < a.n_valid ? a.in[addr] : fe_zero();
     }
   }
   __syncthreads();
 
-  // Radix-2 DIT stages.
-  const uint32_t half_total = total >> 1;
-  for (int lh = 0; lh < logS; lh++) {
-    const uint32_t h = 1u << lh;
-    for (uint32_t t = threadIdx.x; t < half_total; t += kThreads) {
-      uint32_t b = t >> (logS - 1), tt = t & ((S >> 1) - 1);
-      uint32_t k = tt & (h - 1);
-      uint32_t j = (b << logS) + ((tt >> lh) << (lh + 1)) + k;
-      fe u = sm[j], v = sm[j + h];
-      if (lh) v = fmul(v, a.wsub[k << (kSubLog - 1 - lh)]);
-      sm[j] = fadd(u, v);
-      sm[j + h] = fsub(u, v);
-    }
-    __syncthreads();
-  }
+  if (a.inverse) stockham<true>(sm, T, logS, logE);
+  else stockham<false>(sm, T, logS, logE);
 
-  // Store with the outer twiddle and scale.
   if (a.out_kstride == 1) {
-    for (uint32_t e = threadIdx.x; e < total; e += kThreads) {
-      uint32_t b = e >> logS, k = e & (S - 1);
-      fe v = sm[e];
+    for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
+      const uint32_t b = e >> logS, k = e & (S - 1);
+      fe v = sm[swz(e)];
       if (a.tw_lo) {
-        uint64_t ex = (g0 + b) * k;
+        const uint64_t ex = (g0 + b) * k;
         v = fmul(v, fmul(a.tw_lo[ex & ((1u << kTwLoBits) - 1)], a.tw_hi[ex >> kTwLoBits]));
       }
       if (a.has_scale) v = fmul(v, a.scale);
       a.out[(g0 + b) * a.out_gstride + k] = v;
     }
   } else {
-    for (uint32_t e = threadIdx.x; e < total; e += kThreads) {
-      uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
-      fe v = sm[(b << logS) + k];
+    for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
+      const uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
+      fe v = sm[swz((b << logS) + k)];
       if (a.tw_lo) {
-        uint64_t ex = (g0 + b) * k;
+        const uint64_t ex = (g0 + b) * k;
         v = fmul(v, fmul(a.tw_lo[ex & ((1u << kTwLoBits) - 1)], a.tw_hi[ex >> kTwLoBits]));
       }
       if (a.has_scale) v = fmul(v, a.scale);
@@ -112,14 +265,15 @@ __global__ void __launch_bounds__(kThreads) ntt_pass_kernel(PassArgs a) {
   }
 }
 
-// omega_{2^13}^t for t < 2^12, per direction; shared by every length.
-fe *g_wsub[2] = {nullptr, nullptr};
-int g_wsub_device = -1;
+// First half of the omega_{2^13} powers, per direction; shared by every length.
+fe *g_wq[2] = {nullptr, nullptr};
+int g_wq_device = -1;
+constexpr size_t kMaxSmem = sizeof(fe) * (kCtaElems + kCtaElems / 2);
 
-void ensure_wsub() {
+void ensure_wq() {
   int dev;
   GBZ_CUDA(cudaGetDevice(&dev));
-  if (g_wsub[0] && g_wsub_device == dev) return;
+  if (g_wq[0] && g_wq_device == dev) return;
   const int n = 1 << (kSubLog - 1);
   std::vector<fe> h(n);
   for (int dir = 0; dir < 2; dir++) {
@@ -127,30 +281,30 @@ void ensure_wsub() {
     if (dir) w = finv(w);
     fe x = fe_one();
     for (int t = 0; t < n; t++) { h[t] = x; x = fmul(x, w); }
-    GBZ_CUDA(cudaMalloc(&g_wsub[dir], sizeof(fe) * n));
-    GBZ_CUDA(cudaMemcpy(g_wsub[dir], h.data(), sizeof(fe) * n, cudaMemcpyHostToDevice));
+    GBZ_CUDA(cudaMalloc(&g_wq[dir], sizeof(fe) * n));
+    GBZ_CUDA(cudaMemcpy(g_wq[dir], h.data(), sizeof(fe) * n, cudaMemcpyHostToDevice));
   }
-  g_wsub_device = dev;
-  GBZ_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (1 << kSubLog) * (int)sizeof(fe)));
+  g_wq_device = dev;
+  GBZ_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
 }
 
 void launch_pass(const PassArgs &a, uint64_t groups, cudaStream_t s) {
-  uint64_t blocks = groups >> a.logB;
-  size_t smem = sizeof(fe) << (a.logS + a.logB);
-  ntt_pass_kernel<<<(unsigned)blocks, kThreads, smem, s>>>(a);
+  const uint64_t blocks = groups >> a.logB;
+  const uint32_t E = 1u << (a.logS + a.logB);
+  const size_t smem = sizeof(fe) * (E + (a.logS >= 1 ? (1u << (a.logS - 1)) : 0));
+  const unsigned threads = E / kPerThread > 32 ? E / kPerThread : 32;
+  ntt_pass_kernel<<<(unsigned)blocks, threads, smem, s>>>(a);
   GBZ_CUDA(cudaGetLastError());
 }
 
 }  // namespace
 
 void ntt_tables_build(NttTables &t, int logn) {
-  ensure_wsub();
+  ensure_wq();
   t.logn = logn;
-  t.sub_fwd = g_wsub[0];
-  t.sub_inv = g_wsub[1];
+  t.sub_fwd = g_wq[0];
+  t.sub_inv = g_wq[1];
   t.inv_len = finv(fe_make(1ull << logn, 0));
-  if (logn <= kSubLog) return;
   const uint64_t L = 1ull << logn;
   const int nlo = 1 << kTwLoBits;
   const uint64_t nhi = (L >> kTwLoBits) > 0 ? (L >> kTwLoBits) : 1;
@@ -188,8 +342,9 @@ void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe 
   const uint64_t L = 1ull << logn;
   if (n_valid > L) n_valid = L;
   PassArgs a{};
-  a.wsub = inverse ? t.sub_inv : t.sub_fwd;
+  a.wh = inverse ? t.sub_inv : t.sub_fwd;
   a.scale = t.inv_len;
+  a.inverse = inverse ? 1 : 0;
   if (logn <= kSubLog) {
     a.in = in;
     a.out = out;
@@ -218,8 +373,10 @@ void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe 
   a.out_gstride = 1;
   a.out_kstride = N1;
   a.logS = k2;
-  a.logB = k2 <= 12 ? (k2 >= 12 ? 1 : 12 - k2) : 0;
-  if ((1ull << a.logB) > N1) a.logB = k1;
+  // Strided pass: at least two neighbouring columns per CTA (whole 32-byte
+  // sectors) and up to 2^13 staged elements, fewer when the transform is
+  // small so that it still spreads over many CTAs.
+  a.logB = std::min(k1, std::max(k2 < kSubLog ? 1 : 0, std::min(kSubLog, logn - 8) - k2));
   a.tw_lo = inverse ? t.lo_inv : t.lo_fwd;
   a.tw_hi = inverse ? t.hi_inv : t.hi_fwd;
   a.has_scale = 0;
@@ -234,8 +391,7 @@ void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe 
   b.out_gstride = 1;
   b.out_kstride = N2;
   b.logS = k1;
-  b.logB = k1 >= 12 ? (k1 == 12 ? 1 : 0) : 12 - k1;
-  if ((1ull << b.logB) > N2) b.logB = k2;
+  b.logB = std::min(k2, std::max(0, std::min(kSubLog - 1, logn - 8) - k1));
   b.tw_lo = nullptr;
   b.tw_hi = nullptr;
   b.has_scale = inverse;

@@ -137,37 +137,9 @@ __global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int 
   st->K = quad_eval(H[0], H[1], H[2], r);
 }
 
-// get_RS_multifold_segment_tensor (coPCS_utils.cpp:333-383) for a segment
-// of kWhirK values.
-__device__ fe rs_fold_tensor_dev(const fe seg[kWhirK], const fe *r, uint64_t n, uint64_t idx, fe om_inv,
-                                 fe len_inv) {
-  const int logn = 63 - __clzll((long long)n);
-  fe omega = fpow(om_inv, n / kWhirK);
-  fe inv_om = fpow(om_inv, idx);
-  fe part[kWhirK / 2];
-  int seg_n = kWhirK;
-  const fe one = fe_one();
-  for (int j = 0; j < seg_n / 2; j++) {
-    fe s = fadd(seg[j], seg[j + seg_n / 2]), d = fsub(seg[j], seg[j + seg_n / 2]);
-    part[j] = fadd(fmul(fsub(one, r[0]), s), fmul(fmul(r[0], inv_om), d));
-    inv_om = fmul(inv_om, omega);
-  }
-  fe pw[kWhirLogK];
-  pw[0] = one;
-  if (kWhirLogK > 1) pw[1] = fmul(om_inv, om_inv);
-  for (int i = 2; i < kWhirLogK; i++) pw[i] = fmul(pw[i - 1], pw[i - 1]);
-  for (int i = 1; i < kWhirLogK; i++) pw[i] = fpow(pw[i], n / kWhirK);
-  for (int i = 1; i < kWhirLogK; i++) {
-    seg_n /= 2;
-    fe o = finv(root_of_unity(logn - i));
-    fe po = fpow(o, idx);
-    for (int j = 0; j < seg_n / 2; j++) {
-      fe s = fadd(part[j], part[j + seg_n / 2]), d = fsub(part[j], part[j + seg_n / 2]);
-      part[j] = fadd(fmul(fsub(one, r[i]), s), fmul(r[i], fmul(po, d)));
-      po = fmul(po, pw[i]);
-    }
-  }
-  return fmul(len_inv, part[0]);
+// omega^e from a two-level power table (lo[e & 4095] * hi[e >> 12]).
+__device__ __forceinline__ fe pow_table(const fe *lo, const fe *hi, uint64_t e) {
+  return fmul(lo[e & 4095u], hi[e >> 12]);
 }
 
 struct QueryArgs {
@@ -179,25 +151,30 @@ struct QueryArgs {
   int l;                 // number of queries
   uint8_t *tr;
   uint64_t off_q, off_rep, off_ans, off_path, off_comb, off_K;
+  // omega_L^{-e} and omega_NL^{e} tables, and per-iteration constants of
+  // get_RS_multifold_segment_tensor for a segment of 4 (coPCS_utils.cpp:333-383)
+  const fe *inv_lo, *inv_hi, *new_lo, *new_hi;
+  fe step0;    // (omega_L^{-1})^(L/4): advance of inv_omegas at level 0
+  fe len_inv;  // 4^{-1}
 };
 
 // whir_query (Whir.cpp:251-314), the query rescaling (:371-372) and the
 // combination weights / K update of update_betas (:325-342, :383-384).
+// Thread i handles query i.
 __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
   __shared__ int32_t q[kMaxQueries];
-  __shared__ fe ans[kMaxQueries];
-  __shared__ fe om_inv_s, len_inv_s, om_new_s;
+  __shared__ fe rb_s;
+  __shared__ fe red[kMaxQueries / 32];
   ProofState *st = a.st;
   if (threadIdx.x == 0) {
-    const int32_t mod = (int32_t)(a.L / 4);  // whir_k <= 4 branch
+    const int32_t mod = (int32_t)(a.L / 4);  // whir_k <= 4 branch of whir_query
     for (int i = 0; i < a.l; i++) q[i] = prng_next(st->prng) % mod;
-    om_inv_s = finv(root_of_unity(63 - __clzll((long long)a.L)));
-    len_inv_s = finv(fe_make(kWhirK, 0));
-    om_new_s = root_of_unity(63 - __clzll((long long)a.NL));
+    rb_s = prng_field(st->prng);  // update_betas' F::_random(), drawn after the queries
   }
   __syncthreads();
   const int i = threadIdx.x;
   const int depth = 63 - __clzll((long long)(a.L / 4));
+  fe contrib = fe_zero();
   if (i < a.l) {
     const uint64_t qi = (uint64_t)q[i];
     reinterpret_cast<int32_t *>(a.tr + a.off_q)[i] = q[i];
@@ -206,17 +183,28 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
       seg[j] = a.cw[qi + j * (a.L / kWhirK)];
       put_fe(a.tr, a.off_rep + 16 * (kWhirK * i + j), seg[j]);
     }
-    fe y = rs_fold_tensor_dev(seg, st->rw, a.L, qi, om_inv_s, len_inv_s);
-    ans[i] = y;
+    // get_RS_multifold_segment_tensor(seg, r, L, qi) with r = the two WHIR
+    // round challenges: level 0 pairs (j, j+2) with omega_L^{-(qi + j L/4)},
+    // level 1 pairs (0, 1) with omega_{L/2}^{-qi} = omega_L^{-2 qi}.
+    const fe one = fe_one(), r0 = st->rw[0], r1 = st->rw[1];
+    fe inv_om = pow_table(a.inv_lo, a.inv_hi, qi);
+    fe part[2];
+    for (int j = 0; j < 2; j++) {
+      fe s = fadd(seg[j], seg[j + 2]), d = fsub(seg[j], seg[j + 2]);
+      part[j] = fadd(fmul(fsub(one, r0), s), fmul(fmul(r0, inv_om), d));
+      inv_om = fmul(inv_om, a.step0);
+    }
+    fe po = pow_table(a.inv_lo, a.inv_hi, (2 * qi) & (a.L - 1));
+    fe s = fadd(part[0], part[1]), d = fsub(part[0], part[1]);
+    fe y = fmul(a.len_inv, fadd(fmul(fsub(one, r1), s), fmul(r1, fmul(po, d))));
     put_fe(a.tr, a.off_ans + 16 * i, y);
     // open_tree_blake: sibling 2*(pos/2) + (1 - pos%2) on every level below the root
     uint64_t pos = qi, cnt = a.L / 4, lvl = 0;
     uint8_t *path = a.tr + a.off_path + 32ull * depth * i;
-    for (int d = 0; d < depth; d++) {
-      uint64_t sib = pos ^ 1ull;
-      const uint4 *src = reinterpret_cast<const uint4 *>(a.tree + 32 * (lvl + sib));
-      uint32_t *dst = reinterpret_cast<uint32_t *>(path + 32 * d);
-      uint4 h0 = src[0], h1 = src[1];
+    for (int dd = 0; dd < depth; dd++) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(a.tree + 32 * (lvl + (pos ^ 1ull)));
+      uint32_t *dst = reinterpret_cast<uint32_t *>(path + 32 * dd);
+      const uint4 h0 = src[0], h1 = src[1];
       dst[0] = h0.x; dst[1] = h0.y; dst[2] = h0.z; dst[3] = h0.w;
       dst[4] = h1.x; dst[5] = h1.y; dst[6] = h1.z; dst[7] = h1.w;
       lvl += cnt;
@@ -225,18 +213,24 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
     }
     const int32_t scaled = (int32_t)(q[i] * (int32_t)(kWhirK * a.NL / a.L));
     st->q[i] = scaled;
-    st->omega_q[i] = fpow(om_new_s, (uint64_t)(uint32_t)scaled);
+    st->omega_q[i] = pow_table(a.new_lo, a.new_hi, (uint64_t)(uint32_t)scaled);
+    // combination weight c_i = r^(i+1) and its share of K += c_i * y_i
+    const fe c = fpow(rb_s, (uint64_t)i + 1);
+    st->comb[i] = c;
+    put_fe(a.tr, a.off_comb + 16 * i, c);
+    contrib = fmul(c, y);
   }
+  for (int dd = 16; dd > 0; dd >>= 1) {
+    fe t;
+    t.re = __shfl_down_sync(0xffffffffu, contrib.re, dd);
+    t.im = __shfl_down_sync(0xffffffffu, contrib.im, dd);
+    contrib = fadd(contrib, t);
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = contrib;
   __syncthreads();
   if (threadIdx.x == 0) {
-    fe r = prng_field(st->prng);
-    fe c = r, K = st->K;
-    for (int k = 0; k < a.l; k++) {
-      st->comb[k] = c;
-      put_fe(a.tr, a.off_comb + 16 * k, c);
-      K = fadd(K, fmul(c, ans[k]));
-      c = fmul(c, r);
-    }
+    fe K = st->K;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) K = fadd(K, red[w]);
     st->K = K;
     put_fe(a.tr, a.off_K, K);
   }
@@ -476,6 +470,16 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     qa.off_path = lay.rec(T_WHIR_PATHS, l * depth, 32);
     qa.off_comb = lay.rec(T_WHIR_COMBINE, l, 16);
     qa.off_K = lay.rec(T_WHIR_K, 1, 16);
+    if (!dry) {
+      const NttTables &told = p.tables(ilog2(L)), &tnew = p.tables(ilog2(NL));
+      qa.inv_lo = told.lo_inv;
+      qa.inv_hi = told.hi_inv;
+      qa.new_lo = tnew.lo_fwd;
+      qa.new_hi = tnew.hi_fwd;
+      const fe om_inv = finv(root_of_unity(ilog2(L)));
+      qa.step0 = fpow(om_inv, L / kWhirK);
+      qa.len_inv = finv(fe_make(kWhirK, 0));
+    }
     RUN(PC_QUERY, 1, k_whir_query<<<1, kMaxQueries, 0, s>>>(qa));
     RUN(PC_UPDATE_BETAS, 2, update_betas_launch(p.vb[1], m, st, l, p.ub_scratch, s));
     cwi = nci;

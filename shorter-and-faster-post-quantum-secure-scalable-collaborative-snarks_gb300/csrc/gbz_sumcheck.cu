@@ -125,6 +125,7 @@ __global__ void __launch_bounds__(kScThreads) sc_sum_kernel(const fe *partial, i
 // precompute_beta: thread t writes B[16t .. 16t+15].  The product over the
 // index bits above the low four is formed once, then the low four bits are
 // expanded like the reference (B[2j] = B_j - B_j r_i, B[2j+1] = B_j r_i).
+// Tables of fewer than 16 entries are written by one thread.
 constexpr int kBetaLow = 4;
 __global__ void __launch_bounds__(256) beta_kernel(const fe *r, int nr, fe *B) {
   __shared__ fe rs[64], om[64];
@@ -133,25 +134,34 @@ __global__ void __launch_bounds__(256) beta_kernel(const fe *r, int nr, fe *B) {
     om[threadIdx.x] = fsub(fe_one(), r[threadIdx.x]);
   }
   __syncthreads();
-  const int low = nr < kBetaLow ? nr : kBetaLow;
-  const uint64_t groups = 1ull << (nr - low);
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= groups) return;
+  if (nr < kBetaLow) {
+    if (t) return;
+    for (uint32_t x = 0; x < (1u << nr); x++) {
+      fe e = fe_one();
+      for (int i = 0; i < nr; i++) e = fmul(e, ((x >> i) & 1) ? rs[i] : om[i]);
+      B[x] = e;
+    }
+    return;
+  }
+  if (t >= (1ull << (nr - kBetaLow))) return;
   fe pre = fe_one();
-  for (int i = low; i < nr; i++) pre = fmul(pre, ((t >> (i - low)) & 1) ? rs[i] : om[i]);
+  for (int i = kBetaLow; i < nr; i++) pre = fmul(pre, ((t >> (i - kBetaLow)) & 1) ? rs[i] : om[i]);
   fe e[1 << kBetaLow];
   e[0] = pre;
-  int len = 1;
-  for (int i = low - 1; i >= 0; i--) {
+#pragma unroll
+  for (int i = kBetaLow - 1; i >= 0; i--) {
+    const int len = 1 << (kBetaLow - 1 - i);
+#pragma unroll
     for (int j = len - 1; j >= 0; j--) {
       fe x = fmul(e[j], rs[i]);
       e[2 * j + 1] = x;
       e[2 * j] = fsub(e[j], x);
     }
-    len <<= 1;
   }
-  fe *o = B + (t << low);
-  for (int j = 0; j < (1 << low); j++) o[j] = e[j];
+  fe *o = B + (t << kBetaLow);
+#pragma unroll
+  for (int j = 0; j < (1 << kBetaLow); j++) o[j] = e[j];
 }
 
 // update_betas: b[j] += sum_i c_i * w_i^j.  Thread tid of a CTA owns the
@@ -223,8 +233,7 @@ void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s) {
 
 void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s) {
   if (nr < 0 || nr > 60) throw ArgError("beta table: bad number of variables");
-  const int low = nr < kBetaLow ? nr : kBetaLow;
-  const uint64_t groups = 1ull << (nr - low);
+  const uint64_t groups = nr < kBetaLow ? 1 : 1ull << (nr - kBetaLow);
   beta_kernel<<<(unsigned)((groups + 255) / 256), 256, 0, s>>>(r, nr, B);
   GBZ_CUDA(cudaGetLastError());
 }

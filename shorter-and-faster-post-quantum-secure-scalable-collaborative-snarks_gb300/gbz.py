@@ -277,7 +277,8 @@ class Context:
             out = np.zeros(nbytes, dtype=np.uint8)
         w = _fe(witness)
         mem = _mem(w)
-        self.check(lib.gbz_prove(self.h, _ptr(w), logn, rate, prng_seed, _ptr(out), nbytes, mem))
+        cap = out.nbytes if isinstance(out, np.ndarray) else out.numel() * out.element_size()
+        self.check(lib.gbz_prove(self.h, _ptr(w), logn, rate, prng_seed, _ptr(out), cap, mem))
         return out
 
 
