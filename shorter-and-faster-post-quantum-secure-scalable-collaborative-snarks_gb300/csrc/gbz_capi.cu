@@ -125,8 +125,15 @@ __global__ void ub_prep_kernel(ProofState *st, const int32_t *q, int l, int logN
       c = fmul(c, r);
     }
   }
+  // omega_N^q depends on q mod N only (N divides 2^32, so this also holds for
+  // the reference's unsigned reading of a negative int).
   const fe om = root_of_unity(logN);
-  for (int i = threadIdx.x; i < l; i += blockDim.x) st->omega_q[i] = fpow(om, (uint64_t)(uint32_t)q[i]);
+  const uint32_t mask = (1u << logN) - 1;
+  for (int i = threadIdx.x; i < l; i += blockDim.x) {
+    const uint32_t qr = (uint32_t)q[i] & mask;
+    st->q[i] = (int32_t)qr;
+    st->omega_q[i] = fpow(om, (uint64_t)qr);
+  }
 }
 
 }  // namespace
@@ -414,7 +421,12 @@ gbz_status gbz_whir_update_betas(gbz_ctx *ctx, uint64_t *b, uint64_t nb, const i
   const int32_t *dq = dev_view(ctx, 1, queries, 4ull * (l ? l : 1), mem, true);
   ub_prep_kernel<<<1, 256, 0, ctx->stream>>>(ctx->st, dq, l, ilog2(N), fe_make(r[0], r[1]));
   GBZ_CUDA(cudaGetLastError());
-  update_betas_launch(db, nb, ctx->st, l, ctx->ub_scratch, ctx->stream);
+  if (update_betas_by_transform(l, nb, N)) {
+    fe *tmp = (fe *)ctx->buf(2, 16 * N);
+    ntt_sparse_accumulate(ctx->tables(ilog2(N)), ctx->st->q, ctx->st->comb, l, db, nb, tmp, ctx->stream);
+  } else {
+    update_betas_launch(db, nb, ctx->st, l, ctx->ub_scratch, ctx->stream);
+  }
   copy_out(ctx, (fe *)b, db, 16 * nb, mem);
   if (challenges && l) {
     // challenges is host memory regardless of mem

@@ -96,6 +96,12 @@ struct NttTables {
 // `tmp` must hold 2^logn elements when logn > 13.  in may equal out.
 void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                 cudaStream_t s);
+// acc[j] += sum_i c[i] * omega_L^{q[i] j} for j < nacc (L = 2^t.logn > 2^13):
+// the forward transform of the sparse vector sum_i c_i e_{q_i}, with the
+// empty columns of the first pass skipped and only the first nacc outputs
+// of the second pass accumulated.  tmp holds L elements.
+void ntt_sparse_accumulate(const NttTables &t, const int32_t *q, const fe *c, int l, fe *acc, uint64_t nacc,
+                           fe *tmp, cudaStream_t s);
 void ntt_tables_build(NttTables &t, int logn);
 int ntt_launch_count(int logn);
 void ntt_tables_free(NttTables &t);

@@ -44,6 +44,14 @@ struct PassArgs {
   const fe *tw_hi;   // omega_L^{2^12 t}
   fe scale;
   int logS, logB, has_scale, inverse;
+  // Sparse input (pass A only): x[sp_q[i]] += sp_c[i] for i < sp_l, zero
+  // elsewhere.  Columns without an entry skip the transform.
+  const int32_t *sp_q;
+  const fe *sp_c;
+  int sp_l;
+  // Accumulating output: out[addr] += v for addr < acc_n, other outputs dropped.
+  uint64_t acc_n;
+  int acc;
 };
 
 // Shared-memory swizzle: element a lives at a ^ ((a >> 3) & 7), which keeps
@@ -222,45 +230,75 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
     const uint32_t nT = S >> 1;
     for (uint32_t t = threadIdx.x; t < nT; t += blockDim.x) T[t] = a.wh[t << (kSubLog - logS)];
   }
-  if (a.in_jstride == 1) {
-    for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
-      const uint32_t b = e >> logS, j = e & (S - 1);
-      const uint64_t addr = (g0 + b) * a.in_gstride + j;
-      sm[swz(e)] = addr < a.n_valid ? a.in[addr] : fe_zero();
+  __shared__ int nonzero;
+  if (a.sp_l > 0) {
+    // Sparse input: zero the tile, then one thread adds the entries of this
+    // CTA's columns in list order (entries may share a position).
+    for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) sm[e] = fe_zero();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int nz = 0;
+      const uint64_t ncol = a.in_jstride;  // column stride = number of columns
+      for (int i = 0; i < a.sp_l; i++) {
+        const uint64_t q = (uint64_t)(uint32_t)a.sp_q[i];
+        const uint64_t g = q & (ncol - 1);
+        if (g >= g0 && g < g0 + (1u << logB)) {
+          const uint32_t idx = swz((uint32_t)((g - g0) << logS) + (uint32_t)(q / ncol));
+          sm[idx] = fadd(sm[idx], a.sp_c[i]);
+          nz = 1;
+        }
+      }
+      nonzero = nz;
     }
+    __syncthreads();
   } else {
-    for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
-      const uint32_t b = e & ((1u << logB) - 1), j = e >> logB;
-      const uint64_t addr = (g0 + b) * a.in_gstride + (uint64_t)j * a.in_jstride;
-      sm[swz((b << logS) + j)] = addr < a.n_valid ? a.in[addr] : fe_zero();
+    nonzero = 1;
+    if (a.in_jstride == 1) {
+      for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
+        const uint32_t b = e >> logS, j = e & (S - 1);
+        const uint64_t addr = (g0 + b) * a.in_gstride + j;
+        sm[swz(e)] = addr < a.n_valid ? a.in[addr] : fe_zero();
+      }
+    } else {
+      for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
+        const uint32_t b = e & ((1u << logB) - 1), j = e >> logB;
+        const uint64_t addr = (g0 + b) * a.in_gstride + (uint64_t)j * a.in_jstride;
+        sm[swz((b << logS) + j)] = addr < a.n_valid ? a.in[addr] : fe_zero();
+      }
     }
+    __syncthreads();
   }
-  __syncthreads();
 
-  if (a.inverse) stockham<true>(sm, T, logS, logE);
-  else stockham<false>(sm, T, logS, logE);
+  if (nonzero) {
+    if (a.inverse) stockham<true>(sm, T, logS, logE);
+    else stockham<false>(sm, T, logS, logE);
+  }
 
   if (a.out_kstride == 1) {
     for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
       const uint32_t b = e >> logS, k = e & (S - 1);
       fe v = sm[swz(e)];
-      if (a.tw_lo) {
+      if (a.tw_lo && nonzero) {
         const uint64_t ex = (g0 + b) * k;
         v = fmul(v, fmul(a.tw_lo[ex & ((1u << kTwLoBits) - 1)], a.tw_hi[ex >> kTwLoBits]));
       }
       if (a.has_scale) v = fmul(v, a.scale);
-      a.out[(g0 + b) * a.out_gstride + k] = v;
+      const uint64_t addr = (g0 + b) * a.out_gstride + k;
+      if (!a.acc) a.out[addr] = v;
+      else if (addr < a.acc_n) a.out[addr] = fadd(a.out[addr], v);
     }
   } else {
     for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
       const uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
       fe v = sm[swz((b << logS) + k)];
-      if (a.tw_lo) {
+      if (a.tw_lo && nonzero) {
         const uint64_t ex = (g0 + b) * k;
         v = fmul(v, fmul(a.tw_lo[ex & ((1u << kTwLoBits) - 1)], a.tw_hi[ex >> kTwLoBits]));
       }
       if (a.has_scale) v = fmul(v, a.scale);
-      a.out[(g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride] = v;
+      const uint64_t addr = (g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride;
+      if (!a.acc) a.out[addr] = v;
+      else if (addr < a.acc_n) a.out[addr] = fadd(a.out[addr], v);
     }
   }
 }
@@ -336,8 +374,11 @@ void ntt_tables_free(NttTables &t) {
   t.logn = -1;
 }
 
-void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
-                cudaStream_t s) {
+namespace {
+
+// Shared by the dense transform and the sparse/accumulating variant.
+void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
+                  const int32_t *sp_q, const fe *sp_c, int sp_l, uint64_t acc_n, cudaStream_t s) {
   const int logn = t.logn;
   const uint64_t L = 1ull << logn;
   if (n_valid > L) n_valid = L;
@@ -380,6 +421,9 @@ void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe 
   a.tw_lo = inverse ? t.lo_inv : t.lo_fwd;
   a.tw_hi = inverse ? t.hi_inv : t.hi_fwd;
   a.has_scale = 0;
+  a.sp_q = sp_q;
+  a.sp_c = sp_c;
+  a.sp_l = sp_l;
   launch_pass(a, N1, s);
   // pass B: rows k2 < N2, length N1, contiguous
   PassArgs b = a;
@@ -395,7 +439,25 @@ void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe 
   b.tw_lo = nullptr;
   b.tw_hi = nullptr;
   b.has_scale = inverse;
+  b.sp_q = nullptr;
+  b.sp_c = nullptr;
+  b.sp_l = 0;
+  b.acc = acc_n ? 1 : 0;
+  b.acc_n = acc_n;
   launch_pass(b, N2, s);
+}
+
+}  // namespace
+
+void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
+                cudaStream_t s) {
+  ntt_two_pass(t, in, n_valid, out, tmp, inverse, nullptr, nullptr, 0, 0, s);
+}
+
+void ntt_sparse_accumulate(const NttTables &t, const int32_t *q, const fe *c, int l, fe *acc, uint64_t nacc,
+                           fe *tmp, cudaStream_t s) {
+  if (t.logn <= kSubLog) throw ArgError("sparse transform needs a two-pass length");
+  ntt_two_pass(t, nullptr, 0, acc, tmp, false, q, c, l, nacc, s);
 }
 
 }  // namespace gbz

@@ -267,6 +267,10 @@ __global__ void k_copy32(const uint8_t *src, uint8_t *dst) {
 
 // ------------------------------------------------------------ host side
 
+bool update_betas_by_transform(int l, uint64_t nb, uint64_t N) {
+  return ilog2(N) > 13 && nb <= N && (uint64_t)l * nb > 4 * N;
+}
+
 int whir_query_count(int rate) { return (int)(-100.0 / log2(sqrt(1.0 / (double)rate))); }
 
 uint64_t Layout::rec(uint32_t tag, uint32_t count, uint32_t unit) {
@@ -481,7 +485,15 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
       qa.len_inv = finv(fe_make(kWhirK, 0));
     }
     RUN(PC_QUERY, 1, k_whir_query<<<1, kMaxQueries, 0, s>>>(qa));
-    RUN(PC_UPDATE_BETAS, 2, update_betas_launch(p.vb[1], m, st, l, p.ub_scratch, s));
+    // update_betas: b[j] += sum_i c_i omega_NL^{q_i j} is the forward
+    // transform of a vector with l nonzeros.  When l * |b| exceeds a few
+    // transform lengths, the sparse two-pass transform is cheaper than the
+    // direct sums.
+    if (update_betas_by_transform(l, m, NL)) {
+      RUN(PC_UPDATE_BETAS, 2, ntt_sparse_accumulate(p.tables(ilog2(NL)), st->q, st->comb, l, p.vb[1], m, p.tmp, s));
+    } else {
+      RUN(PC_UPDATE_BETAS, 2, update_betas_launch(p.vb[1], m, st, l, p.ub_scratch, s));
+    }
     cwi = nci;
     L = NL;
     cur *= 2;

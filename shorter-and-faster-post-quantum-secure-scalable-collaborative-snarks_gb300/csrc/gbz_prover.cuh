@@ -76,5 +76,8 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
 // Reads the device-side consistency flags (synchronises s).
 uint32_t plan_error_flags(ProofPlan &p, cudaStream_t s);
 int whir_query_count(int rate);
+// Whether update_betas over nb entries with l queries of a length-N codeword
+// runs as a sparse transform (else as direct geometric sums).
+bool update_betas_by_transform(int l, uint64_t nb, uint64_t N);
 
 }  // namespace gbz

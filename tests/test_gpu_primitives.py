@@ -196,11 +196,17 @@ def test_update_betas_golden(ctx, oracle, golden):
     assert np.array_equal(out, b2)
 
 
-@pytest.mark.parametrize("logb,logN,l", [(3, 6, 5), (10, 13, 100), (14, 16, 200), (16, 19, 33), (1, 4, 7)])
-def test_update_betas_vs_oracle(ctx, oracle, logb, logN, l):
+@pytest.mark.parametrize("logb,logN,l,dups", [(3, 6, 5, 0), (10, 13, 100, 0), (14, 16, 200, 0), (16, 19, 33, 0),
+                                               (1, 4, 7, 0), (15, 17, 150, 1), (20, 22, 200, 1), (18, 20, 16, 0)])
+def test_update_betas_vs_oracle(ctx, oracle, logb, logN, l, dups):
+    """Direct sums and the sparse-transform path (chosen by size); dups puts
+    several queries on the same position and in the same column."""
     rng = np.random.default_rng(logb * 7 + l)
     b = rand_fe(rng, 1 << logb)
     q = rng.integers(0, 1 << logN, size=l).astype(np.int32)
+    if dups:
+        q[1::3] = q[0]
+        q[2::5] = (q[0] + (1 << (logN // 2 + 1))) % (1 << logN)
     r = rand_fe(rng, 1)[0]
     out, ch = ctx.update_betas(b, q, 1 << logN, r)
     ob, och = oracle.update_betas(b, q, 1 << logN, r)
