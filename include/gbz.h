@@ -131,6 +131,27 @@ gbz_status gbz_sumcheck_fold(gbz_ctx *ctx, uint64_t *v, uint64_t m, const uint64
 gbz_status gbz_whir_update_betas(gbz_ctx *ctx, uint64_t *b, uint64_t nb, const int32_t *queries, int l,
                                  uint64_t N, const uint64_t *r, uint64_t *challenges, int mem);
 
+/* The same update as gbz_whir_update_betas, for callers that must not let
+ * the library allocate device memory at call time (a service that has
+ * already handed all device memory to request slots, or a host runtime with
+ * a fixed device budget behind a foreign-function boundary).  No
+ * counterpart in the reference.
+ *   b, queries and challenges (l elements, may be null) are device memory of
+ *   the current device; r (2 words) is host memory; the work is enqueued on
+ *   cuda_stream (a cudaStream_t; null = the default stream).
+ *   Working memory is one file-scope device array of about 1 MiB that
+ *   every GPU loading the library keeps until exit; it holds at most 256
+ *   queries, so l > 256 returns GBZ_EINVAL (as do a null b/r, a null queries
+ *   with l > 0, and N not a power of two or above 2^28).
+ *   The first call on a device looks up that array's device address (with
+ *   the device current); make that first call before any stream capture.
+ *   All calls share the array: calls that overlap on the GPU (other streams,
+ *   other host threads) race and must be serialised by the caller.  Nothing
+ *   in it needs to start at zero: each call writes every entry it reads.
+ *   The call allocates nothing: no cudaMalloc, no cudaFree, no pool. */
+gbz_status gbz_whir_update_betas_noalloc(uint64_t *b, uint64_t nb, const int32_t *queries, int l, uint64_t N,
+                                         const uint64_t *r, uint64_t *challenges, void *cuda_stream);
+
 /* ---------------------------------------------- host-side protocol state */
 
 /* Fiat-Shamir: state[2] is the chain value (prev_challenge, initially 0);

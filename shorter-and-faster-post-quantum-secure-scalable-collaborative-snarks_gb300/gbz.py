@@ -39,7 +39,7 @@ EXPORTS = (
     "gbz_sumcheck_quadratic", "gbz_sumcheck_fold", "gbz_whir_update_betas", "gbz_hash_to_field",
     "gbz_prng_seed", "gbz_prng_next", "gbz_prng_field", "gbz_field_ops_host",
     "gbz_prove_transcript_bytes", "gbz_prove", "gbz_prove_launches", "gbz_profile_enable",
-    "gbz_profile_read",
+    "gbz_profile_read", "gbz_whir_update_betas_noalloc",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -89,6 +89,7 @@ def _load():
         "gbz_prove_launches": (c_int, [c_int, c_int]),
         "gbz_profile_enable": (c_int, [vp, c_int]),
         "gbz_profile_read": (c_int, [vp, c_int, c_int, vp, vp]),
+        "gbz_whir_update_betas_noalloc": (c_int, [vp, u64, vp, c_int, u64, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
