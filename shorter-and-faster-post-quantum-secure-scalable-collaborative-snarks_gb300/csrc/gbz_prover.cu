@@ -283,8 +283,15 @@ uint64_t Layout::rec(uint32_t tag, uint32_t count, uint32_t unit) {
 }
 
 ProofPlan::~ProofPlan() {
+  if (s2) cudaStreamSynchronize(s2);
   for (auto &kv : ntt) ntt_tables_free(kv.second);
   for (void *p : allocs) cudaFree(p);
+  if (ev_in) cudaEventDestroy(ev_in);
+  for (auto &e : ev_fold)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : ev_commit)
+    if (e) cudaEventDestroy(e);
+  if (s2) cudaStreamDestroy(s2);
 }
 
 void *ProofPlan::dalloc(uint64_t bytes) {
@@ -318,6 +325,11 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   p->tree[0] = (uint8_t *)p->dalloc(32 * merkle_hashes(L));
   p->tree[1] = (uint8_t *)p->dalloc(32 * merkle_hashes(L / 2 >= 4 ? L / 2 : 4));
   p->tmp = (fe *)p->dalloc(sizeof(fe) * L);
+  p->tmp2 = (fe *)p->dalloc(sizeof(fe) * (L / 2));
+  GBZ_CUDA(cudaStreamCreateWithFlags(&p->s2, cudaStreamNonBlocking));
+  GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
+  for (auto &e : p->ev_fold) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  for (auto &e : p->ev_commit) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   p->va[0] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
   p->va[1] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
   p->vb[0] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
@@ -361,28 +373,38 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   Profiler *prof = (!dry && p.prof && p.prof->enabled) ? p.prof : nullptr;
   // RUN(category, kernel launches, statement): counts in the dry run, else
   // runs the statement (bracketed by profiler events when enabled).
-#define RUN(cat, nlaunch, ...)                 \
+#define RUN_ON(strm, cat, nlaunch, ...)        \
   do {                                         \
     if (dry) {                                 \
       p.launches += (nlaunch);                 \
       p.cat_launches[cat] += (nlaunch);        \
     } else {                                   \
-      if (prof) prof->begin(cat, s);           \
+      if (prof) prof->begin(cat, strm);        \
       __VA_ARGS__;                             \
       GBZ_CUDA(cudaGetLastError());            \
-      if (prof) prof->end(s);                  \
+      if (prof) prof->end(strm);               \
     }                                          \
   } while (0)
+#define RUN(cat, nlaunch, ...) RUN_ON(s, cat, nlaunch, __VA_ARGS__)
 
+  // Commits go to the plan's second stream c; it starts after everything
+  // the caller enqueued on s (the witness copy) and s joins it at the end.
+  cudaStream_t c = p.s2;
+  if (!dry) {
+    GBZ_CUDA(cudaEventRecord(p.ev_in, s));
+    GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_in, 0));
+  }
   RUN(PC_PROTOCOL, 1, k_init<<<1, 32, 0, s>>>(st, prng_seed));
 
   // 1. commitment: codeword = NTT(w padded to rate*n), Merkle tree.
   uint64_t L = p.L;
   int cwi = 0;
   uint64_t off = lay.rec(T_COMMIT_ROOT, 1, 32);
-  RUN(PC_NTT, ntt_launch_count(ilog2(L)), ntt_launch(p.tables(ilog2(L)), w, p.n, p.cw[0], p.tmp, false, s));
-  RUN(PC_MERKLE, merkle_launch_count(L), merkle_commit_launch(p.cw[0], L, p.tree[0], s));
-  RUN(PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, s>>>(p.tree[0] + 32 * (merkle_hashes(L) - 1), tr + off));
+  RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(L)), ntt_launch(p.tables(ilog2(L)), w, p.n, p.cw[0], p.tmp, false, c));
+  RUN_ON(c, PC_MERKLE, merkle_launch_count(L), merkle_commit_launch(p.cw[0], L, p.tree[0], c));
+  RUN_ON(c, PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, c>>>(p.tree[0] + 32 * (merkle_hashes(L) - 1), tr + off));
+  if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_commit[0], c));
+  int iter = 0;
 
   // 2. evaluation point and its eq table.
   off = lay.rec(T_EVAL_POINT, logn, 16);
@@ -449,13 +471,23 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     a = p.va[1];
     b = p.vb[1];
     m /= 4;
-    // commit arr at rate 2*cur
+    if (iter >= ProofPlan::kMaxIter) throw ArgError("prover: too many WHIR iterations");
+    // commit arr at rate 2*cur on the commit stream, after the folds
     const uint64_t NL = 2 * cur * m;
     const int nci = cwi ^ 1;
     off = lay.rec(T_WHIR_ROOT, 1, 32);
-    RUN(PC_NTT, ntt_launch_count(ilog2(NL)), ntt_launch(p.tables(ilog2(NL)), a, m, p.cw[nci], p.tmp, false, s));
-    RUN(PC_MERKLE, merkle_launch_count(NL), merkle_commit_launch(p.cw[nci], NL, p.tree[nci], s));
-    RUN(PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, s>>>(p.tree[nci] + 32 * (merkle_hashes(NL) - 1), tr + off));
+    if (!dry) {
+      GBZ_CUDA(cudaEventRecord(p.ev_fold[iter], s));
+      GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_fold[iter], 0));
+    }
+    RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(NL)), ntt_launch(p.tables(ilog2(NL)), a, m, p.cw[nci], p.tmp, false, c));
+    RUN_ON(c, PC_MERKLE, merkle_launch_count(NL), merkle_commit_launch(p.cw[nci], NL, p.tree[nci], c));
+    RUN_ON(c, PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, c>>>(p.tree[nci] + 32 * (merkle_hashes(NL) - 1), tr + off));
+    if (!dry) {
+      GBZ_CUDA(cudaEventRecord(p.ev_commit[iter + 1], c));
+      // the query opens the previous commit
+      GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_commit[iter], 0));
+    }
     // queries on the previous codeword
     const int l = whir_query_count((int)cur);
     if (l > kMaxQueries || l < 1) throw ArgError("prover: query count out of range");
@@ -490,20 +522,23 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     // transform lengths, the sparse two-pass transform is cheaper than the
     // direct sums.
     if (update_betas_by_transform(l, m, NL)) {
-      RUN(PC_UPDATE_BETAS, 2, ntt_sparse_accumulate(p.tables(ilog2(NL)), st->q, st->comb, l, p.vb[1], m, p.tmp, s));
+      RUN(PC_UPDATE_BETAS, 2, ntt_sparse_accumulate(p.tables(ilog2(NL)), st->q, st->comb, l, p.vb[1], m, p.tmp2, s));
     } else {
       RUN(PC_UPDATE_BETAS, 2, update_betas_launch(p.vb[1], m, st, l, p.ub_scratch, s));
     }
     cwi = nci;
     L = NL;
     cur *= 2;
+    iter++;
     if (m <= (uint64_t)kWhirK) break;
   }
   uint64_t off_poly = lay.rec(T_FINAL_POLY, (uint32_t)m, 16);
   uint64_t off_point = lay.rec(T_FINAL_POINT, ilog2(m), 16);
   uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
   RUN(PC_PROTOCOL, 1, k_final<<<1, 32, 0, s>>>(st, a, p.vb[1], (int)m, tr, off_poly, off_point, off_eval));
+  if (!dry) GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_commit[iter], 0));  // join the commit stream
 #undef RUN
+#undef RUN_ON
 }
 
 void Profiler::begin(int cat, cudaStream_t s) {

@@ -46,7 +46,13 @@ struct ProofPlan {
   fe *w = nullptr;                // witness staging (host-input proofs)
   fe *cw[2] = {nullptr, nullptr}; // codeword ping-pong (L, L/2)
   uint8_t *tree[2] = {nullptr, nullptr};
-  fe *tmp = nullptr;              // NTT intermediate (L)
+  fe *tmp = nullptr;              // NTT intermediate of the commits (L)
+  fe *tmp2 = nullptr;             // NTT intermediate of the sparse beta updates (L/2)
+  // The commits (NTT + Merkle) run on a second stream joined by events:
+  // each WHIR query waits for the commit whose codeword it opens.
+  cudaStream_t s2 = nullptr;
+  static constexpr int kMaxIter = 32;
+  cudaEvent_t ev_in = nullptr, ev_fold[kMaxIter] = {}, ev_commit[kMaxIter + 1] = {};
   fe *va[2] = {nullptr, nullptr}; // folded first vector ping-pong (n/2 each)
   fe *vb[2] = {nullptr, nullptr}; // folded second vector ping-pong
   fe *beta = nullptr;             // eq table (n)
