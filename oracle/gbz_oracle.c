@@ -880,3 +880,146 @@ int64_t orc_prove(const uint64_t *witness, int logn, int rate, uint32_t prng_see
   free(v2);
   return tw.bad ? -1 : tw.len;
 }
+
+/* ============================================================ coPCS side */
+
+void orc_lagrange_coeff(const uint64_t r[2], int logd, uint64_t *out) {
+  int64_t d = (int64_t)1 << logd;
+  fe rr = f_make(r[0], r[1]), x = f_one();
+  for (int64_t i = 0; i < d; i++) { st(out, i, x); x = f_mul(x, rr); }
+  orc_fft(out, logd, 1, 1);
+}
+
+void orc_encode_rows(const uint64_t *rows, int nrows, int logrow, int rate, int log_rate_offset, uint64_t *out,
+                     int threads) {
+  int64_t n = (int64_t)1 << logrow, L = n * rate;
+  fe w = f_inv(f_rou(1 + log_rate_offset + logrow));
+  for (int i = 0; i < nrows; i++) {
+    uint64_t *o = out + 2 * L * i;
+    memset(o, 0, sizeof(uint64_t) * 2 * L);
+    memcpy(o, rows + 2 * n * i, sizeof(uint64_t) * 2 * n);
+    orc_fft(o, logrow, 1, threads);
+    fe mul = f_one();
+    for (int64_t j = 0; j < n; j++) { st(o, j, f_mul(mul, ld(o, j))); mul = f_mul(mul, w); }
+    orc_fft(o, ilog2_64(L), 0, threads);
+  }
+}
+
+static void hash_self(const uint8_t in[32], uint8_t out[32]) {  /* blake3(x || x) */
+  uint8_t blk[64];
+  memcpy(blk, in, 32);
+  memcpy(blk + 32, in, 32);
+  blake3_one(blk, out);
+}
+
+void orc_column_merkle(const uint64_t *rows, int nrows, int logL, int N, uint8_t *levels, uint8_t root_out[32]) {
+  int64_t L = (int64_t)1 << logL;
+  /* column j: MT_commit_Blake over the 32-element batch vector; its root
+   * only depends on the first leaf (rows 0..3) because inner nodes hash
+   * their left child twice, but the full tree is built here as in the
+   * reference. */
+  for (int64_t j = 0; j < L; j++) {
+    uint64_t col[64];
+    memset(col, 0, sizeof col);
+    for (int k = 0; k < nrows && k < 32; k++) { col[2 * k] = rows[2 * (L * k + j)]; col[2 * k + 1] = rows[2 * (L * k + j) + 1]; }
+    uint8_t lv[15 * 32];
+    orc_merkle_commit(col, 32, lv, 1);
+    memcpy(levels + 32 * j, lv + 32 * 14, 32);
+  }
+  /* create_tree_blake over the column roots */
+  uint8_t *prev = levels;
+  int64_t cnt = L;
+  while (cnt > 1) {
+    uint8_t *next = prev + 32 * cnt;
+    cnt /= 2;
+    for (int64_t i = 0; i < cnt; i++) hash_self(prev + 32 * (2 * i), next + 32 * i);
+    prev = next;
+  }
+  /* leader: tree over {root, 0, ..., 0} of N parties; its root is the left chain */
+  uint8_t cur[32];
+  memcpy(cur, prev, 32);
+  for (int n = N; n > 1; n /= 2) { uint8_t t[32]; hash_self(cur, t); memcpy(cur, t, 32); }
+  memcpy(root_out, cur, 32);
+}
+
+void orc_secret_shares(const uint64_t *v, int64_t M, int N, int privacy, uint32_t prng_seed, uint64_t *shares) {
+  int k = N / 4, kk = N / 2;
+  int64_t groups = M / k;
+  orc_prng g;
+  orc_prng_seed(&g, prng_seed);
+  uint64_t buff[2 * 1024];
+  int lk = ilog2_64(kk), l2n = ilog2_64(2 * N);
+  for (int64_t i = 0; i < groups; i++) {
+    memset(buff, 0, sizeof(uint64_t) * 2 * 2 * N);
+    for (int j = 0; j < k; j++) { buff[2 * j] = v[2 * (i * k + j)]; buff[2 * j + 1] = v[2 * (i * k + j) + 1]; }
+    for (int j = k; j < kk; j++)
+      if (privacy) { buff[2 * j] = (uint64_t)orc_prng_next(&g); buff[2 * j + 1] = 0; } /* F(random()) */
+    orc_fft(buff, lk, 1, 1);
+    orc_fft(buff, l2n, 0, 1);  /* buff is zero beyond kk */
+    for (int j = 0; j < N; j++) {
+      shares[2 * (j * groups + i)] = buff[2 * (2 * j + 1)];
+      shares[2 * (j * groups + i) + 1] = buff[2 * (2 * j + 1) + 1];
+    }
+  }
+}
+
+/* unpack_secret_share (MPI_utils.cpp:2769-2785) with _k = k = N */
+static void unpack_all(uint64_t *sec, int N) {
+  int lg = ilog2_64(N);
+  orc_fft(sec, lg, 1, 1);
+  fe w = f_inv(f_rou(1 + lg)), mul = f_one();
+  for (int i = 0; i < N; i++) { st(sec, i, f_mul(mul, ld(sec, i))); mul = f_mul(w, mul); }
+  orc_fft(sec, lg, 0, 1);
+}
+
+void orc_party_aggregate(const uint64_t *msgs, int N, int64_t len, const uint64_t *b, uint64_t *out) {
+  uint64_t col[2 * 1024];
+  for (int64_t i = 0; i < len; i++) {
+    for (int p = 0; p < N; p++) { col[2 * p] = msgs[2 * (p * len + i)]; col[2 * p + 1] = msgs[2 * (p * len + i) + 1]; }
+    unpack_all(col, N);
+    fe acc = f_zero();
+    for (int j = 0; j < N / 4; j++) acc = f_add(acc, f_mul(ld(b, j), ld(col, 2 * j)));
+    st(out, i, acc);
+  }
+}
+
+static void extend_block(const uint64_t *src, int logd, int ext_log, uint64_t *dst) {
+  int64_t d = (int64_t)1 << logd, D = (int64_t)1 << (logd + ext_log);
+  memset(dst, 0, sizeof(uint64_t) * 2 * D);
+  memcpy(dst, src, sizeof(uint64_t) * 2 * d);
+  orc_fft(dst, logd, 1, 1);
+  orc_fft(dst, logd + ext_log, 0, 1);
+}
+
+void orc_cophase1(const uint64_t *p1, const uint64_t *p2, const uint64_t *p3, const uint64_t *b1, int64_t n,
+                  int logd, uint64_t *H, uint64_t *H4) {
+  int64_t d = (int64_t)1 << logd, blocks = n / d;
+  uint64_t *a = (uint64_t *)malloc(sizeof(uint64_t) * 2 * 4 * d), *bb = (uint64_t *)malloc(sizeof(uint64_t) * 2 * 4 * d);
+  uint64_t *c = (uint64_t *)malloc(sizeof(uint64_t) * 2 * 4 * d), *e = (uint64_t *)malloc(sizeof(uint64_t) * 2 * 4 * d);
+  for (int64_t k = 0; k < 2 * d; k++) st(H, k, f_zero());
+  for (int64_t k = 0; k < 4 * d; k++) st(H4, k, f_zero());
+  for (int64_t j = 0; j < blocks; j++) {
+    int zero = 1;
+    for (int64_t k = 0; k < d; k++) if (p1[2 * (j * d + k)] || p1[2 * (j * d + k) + 1]) { zero = 0; break; }
+    if (zero) continue;
+    extend_block(p1 + 2 * j * d, logd, 1, a);
+    extend_block(p2 + 2 * j * d, logd, 1, bb);
+    for (int64_t k = 0; k < 2 * d; k++) st(H, k, f_add(ld(H, k), f_mul(ld(a, k), ld(bb, k))));
+    extend_block(p1 + 2 * j * d, logd, 2, a);
+    extend_block(p2 + 2 * j * d, logd, 2, bb);
+    extend_block(b1 + 2 * j * d, logd, 2, c);
+    extend_block(p3 + 2 * j * d, logd, 2, e);
+    for (int64_t k = 0; k < 4 * d; k++)
+      st(H4, k, f_add(ld(H4, k), f_mul(f_sub(f_mul(ld(a, k), ld(bb, k)), ld(e, k)), ld(c, k))));
+  }
+  free(a); free(bb); free(c); free(e);
+}
+
+void orc_cophase2(const uint64_t *v, int64_t n, const uint64_t *L, int logd, uint64_t *out) {
+  int64_t d = (int64_t)1 << logd;
+  for (int64_t j = 0; j < n / d; j++) {
+    fe acc = f_zero();
+    for (int64_t k = 0; k < d; k++) acc = f_add(acc, f_mul(ld(L, k), ld(v, j * d + k)));
+    st(out, j, acc);
+  }
+}

@@ -89,6 +89,42 @@ int64_t orc_transcript_bytes(int logn, int rate);
 int64_t orc_prove(const uint64_t *witness, int logn, int rate, uint32_t prng_seed,
                   uint8_t *transcript, int64_t cap, int threads);
 
+/* ---- coPCS side ------------------------------------------------------ */
+
+/* compute_lagrange_coeff (utils.cpp:169-197): powers r^i, i < 2^logd, then
+ * the inverse transform. */
+void orc_lagrange_coeff(const uint64_t r[2], int logd, uint64_t *out);
+
+/* Encode (coPCS.cpp:131-147) of nrows rows of 2^logrow elements: inverse
+ * transform, scale by w^{-j} with w = getRootOfUnity(1 + log_ro + logrow),
+ * zero-pad to rate * 2^logrow, forward transform.  out: nrows rows of
+ * rate * 2^logrow. */
+void orc_encode_rows(const uint64_t *rows, int nrows, int logrow, int rate, int log_rate_offset, uint64_t *out,
+                     int threads);
+
+/* distributed_MT (coPCS.cpp:152-202) for one party: column roots of the
+ * 32-row batch (rows >= nrows are zero), the tree over them (levels: L + L/2
+ * + ... + 1 hashes), and the leader's root over {root, 0, ..., 0} of N
+ * parties (root_out). */
+void orc_column_merkle(const uint64_t *rows, int nrows, int logL, int N, uint8_t *levels, uint8_t root_out[32]);
+
+/* compute_secret_shares (MPI_utils.cpp:2738-2764), k = N/4, _k = N/2:
+ * shares[j][i] for party j and group i; with privacy the slots k.._k-1 of
+ * each group take random() from the glibc stream seeded with prng_seed. */
+void orc_secret_shares(const uint64_t *v, int64_t M, int N, int privacy, uint32_t prng_seed, uint64_t *shares);
+
+/* sumcheck_aggr leader computation (MPI_utils.cpp:2631-2644): msgs is N
+ * party messages of len elements; b has N/4 weights. */
+void orc_party_aggregate(const uint64_t *msgs, int N, int64_t len, const uint64_t *b, uint64_t *out);
+
+/* Local sums of quadratic_coSumcheck_phase1 (coSumcheck.cpp:153-179; H of
+ * 2d) and cubic_coSumcheck_phase1 (:11-46; H4 of 4d) over blocks of d. */
+void orc_cophase1(const uint64_t *p1, const uint64_t *p2, const uint64_t *p3, const uint64_t *b1, int64_t n,
+                  int logd, uint64_t *H, uint64_t *H4);
+/* quadratic/cubic_coSumcheck_phase2 fold of one vector by Lagrange weights
+ * L (coSumcheck.cpp:66-148, 201-213): out[j] = sum_k L[k] v[j*d + k]. */
+void orc_cophase2(const uint64_t *v, int64_t n, const uint64_t *L, int logd, uint64_t *out);
+
 /* SplitMix64 witness generator shared by tests and bench. */
 void orc_witness(uint64_t seed, int64_t n, uint64_t *out);
 

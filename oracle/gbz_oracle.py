@@ -246,3 +246,68 @@ def prove(w, logn, rate, prng_seed=1, threads=0):
     if n < 0:
         raise ValueError("oracle prove failed")
     return out[:n].tobytes()
+
+
+# ---------------------------------------------------------------- coPCS side
+
+def lagrange_coeff(r, logd):
+    r = np.ascontiguousarray(r, dtype=np.uint64)
+    out = fe_array(1 << logd)
+    lib().orc_lagrange_coeff(_p64(r), ctypes.c_int(logd), _p64(out))
+    return out
+
+
+def encode_rows(rows, rate, log_rate_offset, threads=0):
+    rows = np.ascontiguousarray(rows, dtype=np.uint64)
+    nrows, n = rows.shape[0], rows.shape[1]
+    logrow = n.bit_length() - 1
+    out = np.zeros((nrows, n * rate, 2), dtype=np.uint64)
+    lib().orc_encode_rows(_p64(rows), ctypes.c_int(nrows), ctypes.c_int(logrow), ctypes.c_int(rate),
+                          ctypes.c_int(log_rate_offset), _p64(out), ctypes.c_int(threads))
+    return out
+
+
+def column_merkle(rows, N):
+    rows = np.ascontiguousarray(rows, dtype=np.uint64)
+    nrows, L = rows.shape[0], rows.shape[1]
+    levels = np.zeros((2 * L - 1, 32), dtype=np.uint8)
+    root = np.zeros(32, dtype=np.uint8)
+    lib().orc_column_merkle(_p64(rows), ctypes.c_int(nrows), ctypes.c_int(L.bit_length() - 1), ctypes.c_int(N),
+                            _p8(levels), _p8(root))
+    return levels, root
+
+
+def secret_shares(v, N, privacy=False, prng_seed=1):
+    v = np.ascontiguousarray(v, dtype=np.uint64).reshape(-1, 2)
+    M = v.shape[0]
+    out = np.zeros((N, M // (N // 4), 2), dtype=np.uint64)
+    lib().orc_secret_shares(_p64(v), ctypes.c_int64(M), ctypes.c_int(N), ctypes.c_int(int(privacy)),
+                            ctypes.c_uint32(prng_seed), _p64(out))
+    return out
+
+
+def party_aggregate(msgs, b):
+    msgs = np.ascontiguousarray(msgs, dtype=np.uint64)
+    N, length = msgs.shape[0], msgs.shape[1]
+    b = np.ascontiguousarray(b, dtype=np.uint64).reshape(-1, 2)
+    out = fe_array(length)
+    lib().orc_party_aggregate(_p64(msgs), ctypes.c_int(N), ctypes.c_int64(length), _p64(b), _p64(out))
+    return out
+
+
+def cophase1(p1, p2, p3, b1, logd):
+    arrs = [np.ascontiguousarray(x, dtype=np.uint64).reshape(-1, 2) for x in (p1, p2, p3, b1)]
+    d = 1 << logd
+    H, H4 = fe_array(2 * d), fe_array(4 * d)
+    lib().orc_cophase1(*[_p64(a) for a in arrs], ctypes.c_int64(arrs[0].shape[0]), ctypes.c_int(logd), _p64(H),
+                       _p64(H4))
+    return H, H4
+
+
+def cophase2(v, L):
+    v = np.ascontiguousarray(v, dtype=np.uint64).reshape(-1, 2)
+    L = np.ascontiguousarray(L, dtype=np.uint64).reshape(-1, 2)
+    logd = L.shape[0].bit_length() - 1
+    out = fe_array(v.shape[0] // L.shape[0])
+    lib().orc_cophase2(_p64(v), ctypes.c_int64(v.shape[0]), _p64(L), ctypes.c_int(logd), _p64(out))
+    return out

@@ -1,0 +1,198 @@
+// Driver over the reference's coPCS-side functions (links every reference
+// translation unit except main.cpp; see the ref_full target of the Makefile).
+//
+// Test infrastructure only: it writes golden vectors for the C restatement
+// in oracle/gbz_oracle.c.  Each subcommand calls the reference function
+// named in its comment; where a reference function ends in an MPI exchange
+// that needs more than one rank (the coSumcheck phase 1 and sumcheck_aggr),
+// the driver calls the reference's building blocks in the same order up to
+// that exchange and writes the local result.
+//
+//   ref_full multifold5 <logn> <logd> <seed>            RS_multifold5 (coPCS_utils.cpp:386)
+//   ref_full lagrange <logd> <seed>                      compute_lagrange_coeff (utils.cpp:169)
+//   ref_full encode <rows> <logrow> <rate> <log_ro> <seed>  Encode (coPCS.cpp:131)
+//   ref_full colmerkle <rows> <logL> <N> <seed>          distributed_MT (coPCS.cpp:152)
+//   ref_full shares <logM> <N> <seed> <privacy> <prng>   compute_secret_shares (MPI_utils.cpp:2738)
+//   ref_full aggr <N> <len> <seed>                       sumcheck_aggr leader path (MPI_utils.cpp:2629-2644)
+//   ref_full cophase1 <logn> <logd> <seed>               local part of quadratic/cubic phase 1 (coSumcheck.cpp:9-64,150-198)
+//   ref_full cophase2 <logn> <logd> <seed>               quadratic/cubic phase 2 (coSumcheck.cpp:66-148, 201-213)
+#include "coPCS.h"
+#include "coPCS_utils.h"
+#include "coSumcheck.h"
+#include "config_pc.hpp"
+#include "utils.hpp"
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using std::vector;
+
+extern unsigned int rate_offset;  // coPCS.cpp:22
+void Encode(vector<vector<F>> &Codeword, int N, vector<int> rate);
+void quadratic_coSumcheck_phase2(vector<F> &p1, vector<F> &p2, vector<F> L, int d);
+void cubic_coSumcheck_phase2(vector<F> &p1, vector<F> &p2, vector<F> &p3, vector<F> &b1, vector<F> L, int d);
+void compute_secret_shares(vector<F> &v, vector<vector<F>> &v_shares, int N, int k, int _k, bool privacy_preserving);
+vector<F> unpack_secret_share(vector<F> &secret, int _k, int k);
+
+static const uint64_t P61 = 2305843009213693951ULL;
+struct SplitMix {
+  uint64_t s;
+  explicit SplitMix(uint64_t seed) : s(seed) {}
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+  }
+  uint64_t base() {
+    for (;;) {
+      uint64_t v = next() >> 3;
+      if (v != P61) return v;
+    }
+  }
+  F ext() { F x; x.real = base(); x.img = base(); return x; }
+  vector<F> vec(size_t n) { vector<F> v(n); for (auto &x : v) x = ext(); return v; }
+};
+
+static void put(const void *p, size_t n) { fwrite(p, 1, n, stdout); }
+static void putFs(const vector<F> &v) { for (auto &x : v) { put(&x.real, 8); put(&x.img, 8); } }
+
+int main(int argc, char **argv) {
+  if (argc < 2) return 1;
+  std::string c = argv[1];
+  auto I = [&](int k) { return atoi(argv[k]); };
+  auto U = [&](int k) { return (uint64_t)strtoull(argv[k], nullptr, 0); };
+  if (c == "multifold5") {
+    int logn = I(2), logd = I(3);
+    SplitMix g(U(4));
+    vector<F> cw = g.vec(1u << logn), a = g.vec(1u << logd);
+    putFs(cw); putFs(a);
+    RS_multifold5(cw, a, 1 << logd);
+    putFs(cw);
+    return 0;
+  }
+  if (c == "lagrange") {
+    int logd = I(2);
+    SplitMix g(U(3));
+    F r = g.ext();
+    putFs({r});
+    putFs(compute_lagrange_coeff(F(0), r, 1 << logd));
+    return 0;
+  }
+  if (c == "encode") {
+    int rows = I(2), logrow = I(3), rate = I(4), log_ro = I(5);
+    SplitMix g(U(6));
+    rate_offset = 1u << log_ro;
+    vector<vector<F>> cw(32);
+    for (int i = 0; i < rows; i++) cw[i] = g.vec(1u << logrow);
+    for (int i = 0; i < rows; i++) putFs(cw[i]);
+    Encode(cw, 0, {rate});
+    for (int i = 0; i < rows; i++) putFs(cw[i]);
+    return 0;
+  }
+  if (c == "colmerkle") {
+    int rows = I(2), logL = I(3), N = I(4);
+    SplitMix g(U(5));
+    vector<vector<F>> cw(32);
+    for (int i = 0; i < rows; i++) cw[i] = g.vec(1u << logL);
+    for (int i = 0; i < rows; i++) putFs(cw[i]);
+    MT com;
+    distributed_MT(cw, com, N);
+    uint32_t lv = (uint32_t)com.Base_MT.size();
+    put(&lv, 4);
+    for (auto &level : com.Base_MT) {
+      uint32_t cnt = (uint32_t)level.size();
+      put(&cnt, 4);
+      for (auto &h : level) put(h.arr, 32);
+    }
+    put(com.Root_MT.back()[0].arr, 32);
+    return 0;
+  }
+  if (c == "shares") {
+    int logM = I(2), N = I(3);
+    SplitMix g(U(4));
+    bool privacy = I(5) != 0;
+    srandom((unsigned)U(6));
+    vector<F> v = g.vec(1u << logM);
+    putFs(v);
+    vector<vector<F>> shares;
+    compute_secret_shares(v, shares, N, N / 4, N / 2, privacy);
+    for (auto &s : shares) putFs(s);
+    return 0;
+  }
+  if (c == "aggr") {
+    int N = I(2), len = I(3);
+    SplitMix g(U(4));
+    vector<vector<F>> P(N);
+    for (auto &p : P) p = g.vec(len);
+    vector<F> b = g.vec(N / 4);
+    for (auto &p : P) putFs(p);
+    putFs(b);
+    // sumcheck_aggr, leader path (MPI_utils.cpp:2631-2644)
+    P = transpose(P);
+    for (size_t i = 0; i < P.size(); i++) P[i] = unpack_secret_share(P[i], N, N);
+    vector<F> poly(len, F(0));
+    for (size_t i = 0; i < P.size(); i++)
+      for (size_t j = 0; j < P[i].size() / 4; j++) poly[i] += b[j] * P[i][2 * j];
+    putFs(poly);
+    return 0;
+  }
+  if (c == "cophase1") {
+    int logn = I(2), logd = I(3);
+    SplitMix g(U(4));
+    int n = 1 << logn, d = 1 << logd;
+    vector<F> p1 = g.vec(n), p2 = g.vec(n), p3 = g.vec(n), b1 = g.vec(n);
+    for (int k = 0; k < d; k++) p1[k] = F(0);  // block 0 of p1 is zero: skipped
+    putFs(p1); putFs(p2); putFs(p3); putFs(b1);
+    // quadratic_coSumcheck_phase1 local sum (coSumcheck.cpp:153-179)
+    vector<F> H(2 * d, F(0));
+    for (int j = 0; j < n / d; j++) {
+      vector<F> h1(d), h2(d);
+      bool zero = true;
+      for (int k = 0; k < d; k++) { h1[k] = p1[j * d + k]; h2[k] = p2[j * d + k]; if (h1[k] != 0) zero = false; }
+      if (zero) continue;
+      fft(h1, logd, true); fft(h2, logd, true);
+      h1.resize(2 * d, F(0)); h2.resize(2 * d, F(0));
+      fft(h1, logd + 1, false); fft(h2, logd + 1, false);
+      for (int k = 0; k < 2 * d; k++) H[k] += h1[k] * h2[k];
+    }
+    putFs(H);
+    // cubic_coSumcheck_phase1 local sum (coSumcheck.cpp:11-46)
+    vector<F> H4(4 * d, F(0));
+    for (int j = 0; j < n / d; j++) {
+      vector<F> h1(d), h2(d), h3(d), h4(d);
+      bool zero = true;
+      for (int k = 0; k < d; k++) {
+        h1[k] = p1[j * d + k]; h2[k] = p2[j * d + k]; h3[k] = b1[j * d + k]; h4[k] = p3[j * d + k];
+        if (h1[k] != 0) zero = false;
+      }
+      if (zero) continue;
+      fft(h1, logd, true); fft(h2, logd, true); fft(h3, logd, true); fft(h4, logd, true);
+      h1.resize(4 * d, F(0)); h2.resize(4 * d, F(0)); h3.resize(4 * d, F(0)); h4.resize(4 * d, F(0));
+      fft(h1, logd + 2, false); fft(h2, logd + 2, false); fft(h3, logd + 2, false); fft(h4, logd + 2, false);
+      for (int k = 0; k < 4 * d; k++) H4[k] += (h1[k] * h2[k] - h4[k]) * h3[k];
+    }
+    putFs(H4);
+    return 0;
+  }
+  if (c == "cophase2") {
+    int logn = I(2), logd = I(3);
+    SplitMix g(U(4));
+    int n = 1 << logn, d = 1 << logd;
+    vector<F> p1 = g.vec(n), p2 = g.vec(n), p3 = g.vec(n), b1 = g.vec(n), L = g.vec(d);
+    for (int k = 0; k < d; k++) { p1[d + k] = F(0); p3[2 * d + k] = F(0); }  // zero blocks
+    putFs(p1); putFs(p2); putFs(p3); putFs(b1); putFs(L);
+    vector<F> q1 = p1, q2 = p2;
+    quadratic_coSumcheck_phase2(q1, q2, L, d);
+    putFs(q1); putFs(q2);
+    vector<F> c1 = p1, c2 = p2, c3 = p3, c4 = b1;
+    cubic_coSumcheck_phase2(c1, c2, c3, c4, L, d);
+    putFs(c1); putFs(c2); putFs(c3); putFs(c4);
+    return 0;
+  }
+  fprintf(stderr, "unknown command %s\n", argv[1]);
+  return 1;
+}

@@ -5,11 +5,13 @@
  * Part of the test infrastructure: nothing in the product links it.
  *
  * The reference functions that the oracle drivers call (fft, pfft,
- * MT_commit_Blake, whir_*, Whir_Open, RS folds) touch MPI only through
- * MPI_Comm_rank in get_whir_rates (Whir.cpp:18-20).  This header therefore
- * models a world of exactly one rank.  Calls that would move data between
- * ranks abort loudly, so a driver that strays into collaborative code fails
- * instead of producing made-up bytes.
+ * MT_commit_Blake, whir_*, Whir_Open, RS folds, Encode, distributed_MT,
+ * the secret-sharing helpers) touch MPI only through MPI_Comm_rank and, in
+ * distributed_MT, an all-to-all of zero bytes.  This header models a world
+ * of exactly one rank: collectives deliver a rank's own block to itself, and
+ * point-to-point calls, which would need a second rank, abort loudly so a
+ * driver that strays into collaborative code fails instead of producing
+ * made-up bytes.
  */
 #pragma once
 #include <cstddef>
@@ -57,8 +59,21 @@ static inline int MPI_Wait(MPI_Request *, MPI_Status *) { return 0; }
 static inline int MPI_Waitall(int, MPI_Request *, MPI_Status *) { return 0; }
 static inline int MPI_Waitany(int, MPI_Request *, int *, MPI_Status *) { oracle_mpi_abort_("MPI_Waitany"); return 1; }
 static inline int MPI_Bcast(void *, int, MPI_Datatype, int, MPI_Comm) { return 0; }
-static inline int MPI_Alltoall(const void *, int, MPI_Datatype, void *, int, MPI_Datatype, MPI_Comm) { oracle_mpi_abort_("MPI_Alltoall"); return 1; }
-static inline int MPI_Ialltoall(const void *, int, MPI_Datatype, void *, int, MPI_Datatype, MPI_Comm, MPI_Request *) { oracle_mpi_abort_("MPI_Ialltoall"); return 1; }
+static inline size_t oracle_mpi_size_(MPI_Datatype t) {
+  switch (t) {
+    case MPI_UINT64_T: case MPI_DOUBLE: case MPI_UNSIGNED_LONG_LONG: return 8;
+    case MPI_INT: return 4;
+    default: return 1;
+  }
+}
+// With one rank an all-to-all delivers the rank's own block to itself.
+static inline int MPI_Alltoall(const void *s, int sc, MPI_Datatype st, void *r, int, MPI_Datatype, MPI_Comm) {
+  std::memcpy(r, s, (size_t)sc * oracle_mpi_size_(st));
+  return 0;
+}
+static inline int MPI_Ialltoall(const void *s, int sc, MPI_Datatype st, void *r, int rc, MPI_Datatype rt, MPI_Comm c, MPI_Request *) {
+  return MPI_Alltoall(s, sc, st, r, rc, rt, c);
+}
 static inline int MPI_Gather(const void *, int, MPI_Datatype, void *, int, MPI_Datatype, int, MPI_Comm) { oracle_mpi_abort_("MPI_Gather"); return 1; }
 static inline int MPI_Allreduce(const void *, void *, int, MPI_Datatype, MPI_Op, MPI_Comm) { oracle_mpi_abort_("MPI_Allreduce"); return 1; }
 static inline int MPI_Reduce(const void *, void *, int, MPI_Datatype, MPI_Op, int, MPI_Comm) { oracle_mpi_abort_("MPI_Reduce"); return 1; }

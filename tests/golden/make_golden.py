@@ -21,6 +21,7 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+FULL = os.path.join(ROOT, "oracle", "_ref", "ref_full")
 
 # Witness seed convention: 0x5EED0000 + config * 2^16 + instance.
 SEED_C1 = 0x5EED0000 + 1 * 65536
@@ -31,6 +32,11 @@ def run(*args):
     t = time.time()
     out = subprocess.run([DRIVER, *map(str, args)], check=True, capture_output=True)
     return out.stdout, time.time() - t
+
+
+def run_full(*args):
+    out = subprocess.run([FULL, *map(str, args)], check=True, capture_output=True)
+    return out.stdout
 
 
 def save(name, data):
@@ -113,6 +119,25 @@ def main():
                        "sha256": hashlib.sha256(data).hexdigest(), "ref_seconds": round(dt, 3)})
         print(f"prove 2^{logn} rate {rate}: {len(data)} B in {dt:.2f} s", flush=True)
     manifest["prove"] = proofs
+
+    # coPCS side (ref_full links every reference translation unit but main.cpp)
+    copcs = {}
+    for name, args in [
+        ("multifold5_10_2", ("multifold5", 10, 2, 51)), ("multifold5_12_3", ("multifold5", 12, 3, 52)),
+        ("multifold5_9_1", ("multifold5", 9, 1, 53)), ("lagrange_4", ("lagrange", 4, 54)),
+        ("lagrange_7", ("lagrange", 7, 55)), ("encode_3_8", ("encode", 3, 8, 4, 6, 56)),
+        ("encode_5_6", ("encode", 5, 6, 2, 3, 57)), ("colmerkle_5_8", ("colmerkle", 5, 8, 16, 58)),
+        ("colmerkle_2_6", ("colmerkle", 2, 6, 4, 59)), ("colmerkle_32_5", ("colmerkle", 32, 5, 8, 60)),
+        ("shares_8_16", ("shares", 8, 16, 61, 0, 1)), ("shares_9_16p", ("shares", 9, 16, 62, 1, 7)),
+        ("shares_7_8p", ("shares", 7, 8, 63, 1, 1)), ("aggr_16_24", ("aggr", 16, 24, 64)),
+        ("aggr_8_10", ("aggr", 8, 10, 65)), ("aggr_32_6", ("aggr", 32, 6, 66)),
+        ("cophase1_10_3", ("cophase1", 10, 3, 67)), ("cophase1_9_2", ("cophase1", 9, 2, 68)),
+        ("cophase2_10_3", ("cophase2", 10, 3, 69)), ("cophase2_8_4", ("cophase2", 8, 4, 70)),
+    ]:
+        data = run_full(*args)
+        save(name + ".bin", data)
+        copcs[name] = {"file": name + ".bin", "args": list(args)}
+    manifest["copcs"] = copcs
 
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
