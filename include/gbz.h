@@ -131,6 +131,70 @@ gbz_status gbz_sumcheck_fold(gbz_ctx *ctx, uint64_t *v, uint64_t m, const uint64
 gbz_status gbz_whir_update_betas(gbz_ctx *ctx, uint64_t *b, uint64_t nb, const int32_t *queries, int l,
                                  uint64_t N, const uint64_t *r, uint64_t *challenges, int mem);
 
+/* ----------------------------------------------------- coPCS-side rows */
+
+/* RS fold of a codeword of n elements by d = 2^logd (1 <= logd <= 4) with
+ * fold weights a (d elements, host memory); out has n/d elements.
+ * replaces RS_multifold5 (coPCS_utils.cpp:386-437). */
+gbz_status gbz_rs_multifold5(gbz_ctx *ctx, const uint64_t *codeword, uint64_t n, const uint64_t *a, int logd,
+                             uint64_t *out, int mem);
+
+/* Lagrange basis at r (2 words, host) over the 2^logd-point subgroup: the
+ * inverse transform of (1, r, r^2, ...); out has 2^logd elements.
+ * replaces compute_lagrange_coeff (utils.cpp:169-197). */
+gbz_status gbz_lagrange_coeff(gbz_ctx *ctx, const uint64_t *r, int logd, uint64_t *out, int mem);
+
+/* coPCS encoding of nrows rows of 2^logrow elements: inverse transform,
+ * scale by w^{-j} with w = getRootOfUnity(1 + log_rate_offset + logrow),
+ * zero-pad to rate * 2^logrow, forward transform.  out: nrows rows of
+ * rate * 2^logrow elements.
+ * replaces Encode (coPCS.cpp:131-147), rate_offset = 2^log_rate_offset. */
+gbz_status gbz_encode_rows(gbz_ctx *ctx, const uint64_t *rows, int nrows, int logrow, int rate, int log_rate_offset,
+                           uint64_t *out, int mem);
+
+/* One party's commitment of a batch of nrows <= 32 codeword rows of 2^logL
+ * elements: per-column Blake3 roots (MT_commit_Blake over the 32-entry
+ * column, missing rows zero), the tree over them (levels: 2^(logL+1) - 1
+ * hashes, column roots first) and the leader's root over nparties entries
+ * {root, 0, ..., 0} (root: 32 bytes).
+ * replaces distributed_MT (coPCS.cpp:152-202). */
+gbz_status gbz_column_merkle(gbz_ctx *ctx, const uint64_t *rows, int nrows, int logL, int nparties, uint8_t *levels,
+                             uint8_t *root, int mem);
+
+/* Packed Shamir shares of M values for N parties (N a power of two, 4..64):
+ * k = N/4 secrets per group padded to N/2 with zeros, or with the glibc
+ * random() stream from srandom(prng_seed) when privacy is set; shares holds
+ * N rows of 4M/N elements.
+ * replaces compute_secret_shares (MPI_utils.cpp:2738-2764). */
+gbz_status gbz_secret_shares(gbz_ctx *ctx, const uint64_t *v, uint64_t M, int N, int privacy, uint32_t prng_seed,
+                             uint64_t *shares, int mem);
+
+/* Leader aggregation of N party round messages (N rows of len elements)
+ * with weights b (N/4 elements, host): unpack every coefficient's shares
+ * and combine the secrets.  out: len elements.
+ * replaces the leader computation of sumcheck_aggr (MPI_utils.cpp:2604-2670). */
+gbz_status gbz_party_aggregate(gbz_ctx *ctx, const uint64_t *msgs, int N, uint64_t len, const uint64_t *b,
+                               uint64_t *out, int mem);
+
+/* Local round sums of the block-univariate sumcheck over blocks of d =
+ * 2^logd (n elements per vector).  Quadratic (p3 = b1 = NULL): H (2d
+ * elements, host) = sum over blocks of ext(p1) * ext(p2), ext = inverse
+ * transform of the block, zero-padded, forward transform of twice the
+ * length.  Cubic: H (4d elements) = sum over blocks whose p1 part is not
+ * all zero of (ext(p1) ext(p2) - ext(p3)) ext(b1) at four times the length.
+ * The extended length (2d or 4d) is at most 2^13.
+ * replaces the local loops of quadratic_coSumcheck_phase1
+ * (coSumcheck.cpp:150-179) and cubic_coSumcheck_phase1 (:9-46). */
+gbz_status gbz_cosumcheck_phase1(gbz_ctx *ctx, const uint64_t *p1, const uint64_t *p2, const uint64_t *p3,
+                                 const uint64_t *b1, uint64_t n, int logd, uint64_t *H, int mem);
+
+/* Fold of n elements by blocks of d = 2^logd with Lagrange weights L (d
+ * elements, host): out[j] = sum_k L[k] v[j d + k] (n/d elements).
+ * replaces quadratic_coSumcheck_phase2 / cubic_coSumcheck_phase2
+ * (coSumcheck.cpp:201-213, 66-148). */
+gbz_status gbz_cosumcheck_phase2(gbz_ctx *ctx, const uint64_t *v, uint64_t n, const uint64_t *L, int logd,
+                                 uint64_t *out, int mem);
+
 /* The same update as gbz_whir_update_betas, for callers that must not let
  * the library allocate device memory at call time (a service that has
  * already handed all device memory to request slots, or a host runtime with

@@ -1,4 +1,5 @@
 // extern "C" entry points of libgbz (declared in include/gbz.h).
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <new>
@@ -6,6 +7,7 @@
 #include <utility>
 
 #include "../../include/gbz.h"
+#include "gbz_copcs.cuh"
 #include "gbz_prover.cuh"
 
 using namespace gbz;
@@ -502,6 +504,203 @@ gbz_status gbz_profile_read(gbz_ctx *ctx, int logn, int rate, double *ms, int *g
   }
   it->second->read(ms, groups);
   it->second->reset();
+  API_END(ctx)
+}
+
+gbz_status gbz_rs_multifold5(gbz_ctx *ctx, const uint64_t *cw, uint64_t n, const uint64_t *a, int logd, uint64_t *out,
+                             int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(cw, "codeword");
+  need(a, "a");
+  need(out, "out");
+  check_pow2(n, "RS_multifold5: n");
+  if (ilog2(n) > kMaxLogN) throw ArgError("RS_multifold5: n above 2^28");
+  const uint64_t d = 1ull << logd;
+  const fe *dcw = dev_view(ctx, 0, (const fe *)cw, 16 * n, mem, true);
+  fe *da = (fe *)ctx->buf(1, 16 * d * 2);
+  GBZ_CUDA(cudaMemcpyAsync(da, a, 16 * d, cudaMemcpyHostToDevice, ctx->stream));
+  fe *dout = dev_view(ctx, 2, (fe *)out, 16 * (n >> logd), mem, false);
+  multifold5_launch(dcw, n, da, logd, dout, ctx->tables(ilog2(n)), ctx->stream);
+  copy_out(ctx, (fe *)out, dout, 16 * (n >> logd), mem);
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+gbz_status gbz_lagrange_coeff(gbz_ctx *ctx, const uint64_t *r, int logd, uint64_t *out, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(r, "r");
+  need(out, "out");
+  if (logd < 0 || logd > 20) throw ArgError("lagrange: logd out of range [0, 20]");
+  const uint64_t d = 1ull << logd;
+  fe *dout = dev_view(ctx, 0, (fe *)out, 16 * d, mem, false);
+  fe *tmp = (fe *)ctx->buf(1, 16 * d);
+  powers_launch(fe_make(r[0], r[1]), d, dout, ctx->stream);
+  ntt_launch(ctx->tables(logd), dout, d, dout, tmp, true, ctx->stream);
+  copy_out(ctx, (fe *)out, dout, 16 * d, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_encode_rows(gbz_ctx *ctx, const uint64_t *rows, int nrows, int logrow, int rate, int log_rate_offset,
+                           uint64_t *out, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(rows, "rows");
+  need(out, "out");
+  if (nrows < 0 || logrow < 0 || log_rate_offset < 0) throw ArgError("encode: negative size");
+  if (rate < 1 || !is_pow2((uint64_t)rate)) throw ArgError("encode: rate must be a power of two");
+  const uint64_t n = 1ull << logrow, L = n * (uint64_t)rate;
+  if (ilog2(L) > kMaxLogN || 1 + log_rate_offset + logrow > kMaxLogN) throw ArgError("encode: length above 2^28");
+  if (!nrows) return GBZ_OK;
+  const fe *drows = dev_view(ctx, 0, (const fe *)rows, 16 * n * nrows, mem, true);
+  fe *dout = dev_view(ctx, 1, (fe *)out, 16 * L * nrows, mem, false);
+  fe *tmp = (fe *)ctx->buf(2, 16 * L);
+  const NttTables &tn = ctx->tables(logrow), &tL = ctx->tables(ilog2(L));
+  const NttTables &tw = ctx->tables(1 + log_rate_offset + logrow);
+  for (int i = 0; i < nrows; i++) {
+    fe *o = dout + L * i;
+    ntt_launch(tn, drows + n * i, n, o, tmp, true, ctx->stream);
+    coset_launch(o, n, tw, ctx->stream);
+    ntt_launch(tL, o, n, o, tmp, false, ctx->stream);
+  }
+  copy_out(ctx, (fe *)out, dout, 16 * L * nrows, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_column_merkle(gbz_ctx *ctx, const uint64_t *rows, int nrows, int logL, int nparties, uint8_t *levels,
+                             uint8_t *root, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(rows, "rows");
+  need(levels, "levels");
+  need(root, "root");
+  if (nrows < 1 || nrows > 32) throw ArgError("column merkle: 1..32 rows");
+  if (logL < 0 || logL > kMaxLogN) throw ArgError("column merkle: logL out of range");
+  if (nparties < 1 || !is_pow2((uint64_t)nparties)) throw ArgError("column merkle: parties must be a power of two");
+  const uint64_t L = 1ull << logL, nh = 2 * L - 1;
+  const fe *drows = dev_view(ctx, 0, (const fe *)rows, 16 * L * nrows, mem, true);
+  uint8_t *dlv = dev_view(ctx, 1, levels, 32 * nh, mem, false);
+  uint8_t *droot = dev_view(ctx, 2, root, 32, mem, false);
+  column_merkle_launch(drows, nrows, L, dlv, ilog2(nparties), droot, ctx->stream);
+  copy_out(ctx, levels, dlv, 32 * nh, mem);
+  copy_out(ctx, root, droot, 32, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_secret_shares(gbz_ctx *ctx, const uint64_t *v, uint64_t M, int N, int privacy, uint32_t seed,
+                             uint64_t *shares, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(v, "v");
+  need(shares, "shares");
+  if (N < 4 || N > 64 || !is_pow2((uint64_t)N)) throw ArgError("secret shares: N must be a power of two in [4, 64]");
+  const int k = N / 4, kk = N / 2;
+  if (M % (uint64_t)k) throw ArgError("secret shares: M must be a multiple of N/4");
+  const uint64_t groups = M / k;
+  const fe *dv = dev_view(ctx, 0, (const fe *)v, 16 * M, mem, true);
+  fe *dsh = dev_view(ctx, 1, (fe *)shares, 16 * groups * N, mem, false);
+  std::vector<fe> mu = shamir_share_matrix(N);
+  fe *dmu = (fe *)ctx->buf(2, 16 * mu.size());
+  GBZ_CUDA(cudaMemcpyAsync(dmu, mu.data(), 16 * mu.size(), cudaMemcpyHostToDevice, ctx->stream));
+  fe *dfill = nullptr;
+  std::vector<fe> fill;
+  if (privacy) {  // F(random()) for the slots k.._k-1 of every group, in order
+    glibc_prng g;
+    prng_seed(g, seed);
+    fill.resize(groups * (kk - k));
+    for (auto &x : fill) x = fe_make((uint64_t)prng_next(g), 0);
+    dfill = (fe *)ctx->buf(3, 16 * fill.size());
+    GBZ_CUDA(cudaMemcpyAsync(dfill, fill.data(), 16 * fill.size(), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  shares_launch(dv, dfill, groups, N, dmu, dsh, ctx->stream);
+  copy_out(ctx, (fe *)shares, dsh, 16 * groups * N, mem);
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));  // host staging buffers above must outlive the copies
+  API_END(ctx)
+}
+
+gbz_status gbz_party_aggregate(gbz_ctx *ctx, const uint64_t *msgs, int N, uint64_t len, const uint64_t *b,
+                               uint64_t *out, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(msgs, "msgs");
+  need(b, "b");
+  need(out, "out");
+  if (N < 4 || N > 1024 || !is_pow2((uint64_t)N)) throw ArgError("aggregate: N must be a power of two in [4, 1024]");
+  std::vector<fe> lambda = aggregate_weights(N, reinterpret_cast<const fe *>(b));
+  const fe *dm = dev_view(ctx, 0, (const fe *)msgs, 16 * len * N, mem, true);
+  fe *dl = (fe *)ctx->buf(1, 16 * N);
+  GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16 * N, cudaMemcpyHostToDevice, ctx->stream));
+  fe *dout = dev_view(ctx, 2, (fe *)out, 16 * len, mem, false);
+  aggregate_launch(dm, N, len, dl, dout, ctx->stream);
+  copy_out(ctx, (fe *)out, dout, 16 * len, mem);
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+gbz_status gbz_cosumcheck_phase1(gbz_ctx *ctx, const uint64_t *p1, const uint64_t *p2, const uint64_t *p3,
+                                 const uint64_t *b1, uint64_t n, int logd, uint64_t *H, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(p1, "p1");
+  need(p2, "p2");
+  need(H, "H");
+  const bool cubic = p3 || b1;
+  if (cubic && !(p3 && b1)) throw ArgError("coSumcheck phase 1: the cubic form needs p3 and b1");
+  const int ext = cubic ? 2 : 1, logD = logd + ext;
+  if (logd < 0 || logD > kMaxCoLogD) throw ArgError("coSumcheck phase 1: extended block longer than 2^13");
+  check_pow2(n, "coSumcheck phase 1: n");
+  const uint64_t d = 1ull << logd, D = 1ull << logD;
+  if (n < d) throw ArgError("coSumcheck phase 1: n below one block");
+  const uint64_t nblocks = n / d;
+  const fe *src[4] = {(const fe *)p1, (const fe *)p2, cubic ? (const fe *)b1 : nullptr,
+                      cubic ? (const fe *)p3 : nullptr};
+  const fe *dsrc[4] = {nullptr, nullptr, nullptr, nullptr};
+  fe *ex[4] = {nullptr, nullptr, nullptr, nullptr};
+  fe *coef = (fe *)ctx->buf(10, 16 * n);
+  const NttTables &td = ctx->tables(logd), &tD = ctx->tables(logD);
+  const int nv = cubic ? 4 : 2;
+  for (int v = 0; v < nv; v++) {  // ext(v) per block: inverse of length d, forward of length D
+    dsrc[v] = dev_view(ctx, 11 + v, src[v], 16 * n, mem, true);
+    ex[v] = (fe *)ctx->buf(20 + v, 16 * nblocks * D);
+    ntt_batched(td, dsrc[v], d, (uint32_t)d, coef, nblocks, true, ctx->stream);
+    ntt_batched(tD, coef, d, (uint32_t)d, ex[v], nblocks, false, ctx->stream);
+  }
+  uint8_t *flags = nullptr;
+  if (cubic) {  // blocks whose p1 part is all zero are skipped (coSumcheck.cpp:21-27)
+    flags = (uint8_t *)ctx->buf(30, nblocks);
+    nonzero_blocks_launch(dsrc[0], nblocks, logd, flags, ctx->stream);
+  }
+  const int lanes = D >= 256 ? 1 : (int)(256 / D);
+  const int per_cta = (int)std::max<uint64_t>((uint64_t)lanes, (nblocks + 607) / 608);
+  fe *partial = (fe *)ctx->buf(31, 16 * D * cophase1_parts(nblocks, per_cta));
+  fe *dH = (fe *)ctx->buf(32, 16 * D);
+  cophase1_reduce_launch(ex[0], ex[1], ex[2], ex[3], flags, nblocks, logD, per_cta, partial, dH, ctx->stream);
+  GBZ_CUDA(cudaMemcpyAsync(H, dH, 16 * D, cudaMemcpyDeviceToHost, ctx->stream));
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+gbz_status gbz_cosumcheck_phase2(gbz_ctx *ctx, const uint64_t *v, uint64_t n, const uint64_t *L, int logd,
+                                 uint64_t *out, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(v, "v");
+  need(L, "L");
+  need(out, "out");
+  check_pow2(n, "coSumcheck phase 2: n");
+  if (logd < 0 || logd > 10 || (n >> logd) == 0) throw ArgError("coSumcheck phase 2: block size out of range");
+  const uint64_t d = 1ull << logd;
+  const fe *dv = dev_view(ctx, 0, (const fe *)v, 16 * n, mem, true);
+  fe *dL = (fe *)ctx->buf(1, 16 * d);
+  GBZ_CUDA(cudaMemcpyAsync(dL, L, 16 * d, cudaMemcpyHostToDevice, ctx->stream));
+  fe *dout = dev_view(ctx, 2, (fe *)out, 16 * (n >> logd), mem, false);
+  cophase2_launch(dv, n, dL, logd, dout, ctx->stream);
+  copy_out(ctx, (fe *)out, dout, 16 * (n >> logd), mem);
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
   API_END(ctx)
 }
 

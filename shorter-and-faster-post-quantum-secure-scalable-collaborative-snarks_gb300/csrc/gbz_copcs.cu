@@ -1,0 +1,322 @@
+// Kernels of the collaborative-PCS side of the prover: RS folding, the
+// coPCS encoding, per-column Merkle hashing, packed Shamir shares, the
+// leader's aggregation of party round messages, and the block-univariate
+// (coSumcheck) rounds.
+#include <vector>
+
+#include "gbz_copcs.cuh"
+
+namespace gbz {
+
+namespace {
+
+__device__ __forceinline__ fe pow_tab(const fe *lo, const fe *hi, uint64_t e) { return fmul(lo[e & 4095u], hi[e >> 12]); }
+
+// RS_multifold5 (coPCS_utils.cpp:386-437): output i combines the d = 2^logd
+// entries cw[i + t n/d] through log2(d) butterfly levels whose twiddles are
+// powers of omega_n^{-1} (level 0: omega_n^{-j}; level lv: omega_n^{-2^lv j}
+// for the kept index j), then y_i = d^{-1} sum_k a_k partial_i[k].
+constexpr int kMaxFoldLog = 4;
+__global__ void __launch_bounds__(256)
+multifold5_kernel(const fe *cw, uint64_t n, const fe *a, int logd, fe *out, const fe *inv_lo, const fe *inv_hi,
+                  fe len_inv) {
+  const uint64_t d = 1ull << logd, nout = n >> logd;
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nout) return;
+  fe buf[2][1 << kMaxFoldLog];
+  const uint64_t half = n / 2, step = n >> logd;
+  uint64_t groups = d / 2;
+  for (uint64_t t = 0; t < groups; t++) {
+    const uint64_t j = i + t * step;
+    const fe x = cw[j], y = cw[j + half];
+    buf[0][2 * t] = fadd(x, y);
+    buf[0][2 * t + 1] = fmul(pow_tab(inv_lo, inv_hi, j), fsub(x, y));
+  }
+  int src = 0;
+  uint64_t width = 2;
+  for (int lv = 1; lv < logd; lv++) {
+    const uint64_t ng = groups / 2;
+    for (uint64_t g = 0; g < ng; g++) {
+      const uint64_t j = i + g * step;
+      const fe po = pow_tab(inv_lo, inv_hi, (j << lv) & (n - 1));
+      for (uint64_t k = 0; k < width; k++) {
+        const fe x = buf[src][g * width + k], y = buf[src][(g + ng) * width + k];
+        buf[src ^ 1][g * 2 * width + k] = fadd(x, y);
+        buf[src ^ 1][g * 2 * width + k + width] = fmul(po, fsub(x, y));
+      }
+    }
+    width *= 2;
+    groups = ng;
+    src ^= 1;
+  }
+  fe acc = fe_zero();
+  for (uint64_t k = 0; k < d; k++) acc = fadd(acc, fmul(a[k], buf[src][k]));
+  out[i] = fmul(acc, len_inv);
+}
+
+__global__ void powers_kernel(fe r, uint64_t n, fe *out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = fpow(r, i);
+}
+
+// x[j] *= omega^{-j} for j < n (omega^{-e} from the inverse tables).
+__global__ void coset_kernel(fe *x, uint64_t n, const fe *inv_lo, const fe *inv_hi) {
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) x[j] = fmul(x[j], pow_tab(inv_lo, inv_hi, j));
+}
+
+// Column roots of distributed_MT (coPCS.cpp:168-176): the root of
+// MT_commit_Blake over the 32-entry column depends only on its first leaf
+// (rows 0..3), because every inner node hashes its left child twice; the
+// other seven leaves the reference hashes are discarded, so they are not
+// computed here.
+__global__ void column_root_kernel(const fe *rows, int nrows, uint64_t L, uint8_t *roots) {
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= L) return;
+  fe e[4];
+  for (int k = 0; k < 4; k++) e[k] = k < nrows ? rows[(uint64_t)k * L + j] : fe_zero();
+  uint32_t m[16], h[8];
+  fe4_words(e[0], e[1], e[2], e[3], m);
+  blake3_block64(m, h);
+  for (int lv = 0; lv < 3; lv++) {  // 8 leaves -> 4 -> 2 -> 1
+    for (int k = 0; k < 8; k++) { m[k] = h[k]; m[8 + k] = h[k]; }
+    blake3_block64(m, h);
+  }
+  uint4 *o = reinterpret_cast<uint4 *>(roots + 32 * j);
+  o[0] = make_uint4(h[0], h[1], h[2], h[3]);
+  o[1] = make_uint4(h[4], h[5], h[6], h[7]);
+}
+
+// The leader's root tree over {root, 0, ..., 0} of N parties: its root is
+// log2(N) self-hashes of the party root (coPCS.cpp:193-201).
+__global__ void party_root_kernel(const uint8_t *root, int logN, uint8_t *out) {
+  if (threadIdx.x) return;
+  uint32_t m[16], h[8];
+  for (int k = 0; k < 8; k++) h[k] = reinterpret_cast<const uint32_t *>(root)[k];
+  for (int lv = 0; lv < logN; lv++) {
+    for (int k = 0; k < 8; k++) { m[k] = h[k]; m[8 + k] = h[k]; }
+    blake3_block64(m, h);
+  }
+  for (int k = 0; k < 8; k++) reinterpret_cast<uint32_t *>(out)[k] = h[k];
+}
+
+// Packed Shamir shares: group i of k secrets (plus _k - k random values)
+// maps to party j's share by a fixed linear form mu[j][t].
+__global__ void __launch_bounds__(256)
+shares_kernel(const fe *v, const fe *fill, uint64_t groups, int N, int k, int kk, const fe *mu, fe *shares) {
+  __shared__ fe smu[64 * 32];
+  for (int t = threadIdx.x; t < N * kk; t += blockDim.x) smu[t] = mu[t];
+  __syncthreads();
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= groups) return;
+  fe buf[32];
+  for (int t = 0; t < k; t++) buf[t] = v[i * k + t];
+  for (int t = k; t < kk; t++) buf[t] = fill ? fill[i * (kk - k) + (t - k)] : fe_zero();
+  for (int j = 0; j < N; j++) {
+    fe acc = fe_zero();
+    for (int t = 0; t < kk; t++) acc = fadd(acc, fmul(smu[j * kk + t], buf[t]));
+    shares[(uint64_t)j * groups + i] = acc;
+  }
+}
+
+// out[i] = sum_p lambda_p msgs[p][i]
+__global__ void aggregate_kernel(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= len) return;
+  fe acc = fe_zero();
+  for (int p = 0; p < N; p++) acc = fadd(acc, fmul(lambda[p], msgs[(uint64_t)p * len + i]));
+  out[i] = acc;
+}
+
+// flags[blk] = 1 when block blk of v has a non-zero entry.
+__global__ void nonzero_blocks_kernel(const fe *v, uint64_t nblocks, int logd, uint8_t *flags) {
+  const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  const fe *p = v + (b << logd);
+  uint8_t nz = 0;
+  for (uint32_t k = 0; k < (1u << logd); k++) nz |= (p[k].re | p[k].im) ? 1 : 0;
+  flags[b] = nz;
+}
+
+// Per-CTA partial sums of the extended-block products:
+// quadratic: e1 * e2; cubic: (e1 * e2 - e4) * e3 over blocks with flags set.
+// blockIdx.y selects a chunk of Dc = min(D, 256) positions k; within the
+// CTA k = chunk * Dc + tid % Dc and lane = tid / Dc walks the blocks.
+__global__ void __launch_bounds__(256)
+cophase1_partial_kernel(const fe *e1, const fe *e2, const fe *e3, const fe *e4, const uint8_t *flags,
+                        uint64_t nblocks, int logD, int blocks_per_cta, fe *partial) {
+  __shared__ fe red[256];
+  const int logDc = logD < 8 ? logD : 8;
+  const uint32_t Dc = 1u << logDc, lane = threadIdx.x >> logDc, lanes = 256u >> logDc;
+  const uint32_t k = blockIdx.y * Dc + (threadIdx.x & (Dc - 1));
+  const uint64_t b0 = (uint64_t)blockIdx.x * blocks_per_cta;
+  const uint64_t b1 = min(b0 + blocks_per_cta, nblocks);
+  fe acc = fe_zero();
+  for (uint64_t b = b0 + lane; b < b1; b += lanes) {
+    if (flags && !flags[b]) continue;
+    const uint64_t at = (b << logD) + k;
+    fe t = fmul(e1[at], e2[at]);
+    if (e3) t = fmul(fsub(t, e4[at]), e3[at]);
+    acc = fadd(acc, t);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  if (lane == 0) {
+    for (uint32_t l = 1; l < lanes; l++) acc = fadd(acc, red[threadIdx.x + (l << logDc)]);
+    partial[((uint64_t)blockIdx.x << logD) + k] = acc;
+  }
+}
+
+__global__ void sum_partials_kernel(const fe *partial, uint64_t nparts, uint32_t D, fe *H) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= D) return;
+  fe acc = fe_zero();
+  for (uint64_t c = 0; c < nparts; c++) acc = fadd(acc, partial[c * D + k]);
+  H[k] = acc;
+}
+
+// coSumcheck phase 2: out[j] = sum_k L[k] v[j d + k].
+__global__ void __launch_bounds__(256) cophase2_kernel(const fe *v, uint64_t nout, const fe *L, int logd, fe *out) {
+  __shared__ fe sl[1024];
+  const uint32_t d = 1u << logd;
+  for (uint32_t k = threadIdx.x; k < d; k += blockDim.x) sl[k] = L[k];
+  __syncthreads();
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nout) return;
+  fe acc = fe_zero();
+  for (uint32_t k = 0; k < d; k++) acc = fadd(acc, fmul(sl[k], v[(j << logd) + k]));
+  out[j] = acc;
+}
+
+unsigned grid(uint64_t n, unsigned t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// ------------------------------------------------------------ host side
+
+// Naive DFT of length n over the host field code: out[k] = sum_j in[j] w^{jk}.
+static std::vector<fe> host_dft(const std::vector<fe> &in, fe w) {
+  const size_t n = in.size();
+  std::vector<fe> out(n, fe_zero());
+  fe wk = fe_one();
+  for (size_t k = 0; k < n; k++) {
+    fe x = fe_one(), acc = fe_zero();
+    for (size_t j = 0; j < n; j++) {
+      acc = fadd(acc, fmul(in[j], x));
+      x = fmul(x, wk);
+    }
+    out[k] = acc;
+    wk = fmul(wk, w);
+  }
+  return out;
+}
+static std::vector<fe> host_idft(const std::vector<fe> &in) {
+  const int lg = ilog2(in.size());
+  std::vector<fe> out = host_dft(in, finv(root_of_unity(lg)));
+  const fe s = finv(fe_make(in.size(), 0));
+  for (auto &x : out) x = fmul(x, s);
+  return out;
+}
+
+std::vector<fe> shamir_share_matrix(int N) {
+  // compute_secret_shares (MPI_utils.cpp:2747-2762): inverse transform of the
+  // _k = N/2 group values, zero-pad to 2N, forward transform, party j takes
+  // entry 2j+1.  Column t of the map is the image of the t-th unit vector.
+  const int kk = N / 2;
+  std::vector<fe> mu((size_t)N * kk);
+  for (int t = 0; t < kk; t++) {
+    std::vector<fe> e(kk, fe_zero());
+    e[t] = fe_one();
+    std::vector<fe> c = host_idft(e);
+    c.resize(2 * N, fe_zero());
+    std::vector<fe> ev = host_dft(c, root_of_unity(ilog2(2 * N)));
+    for (int j = 0; j < N; j++) mu[(size_t)j * kk + t] = ev[2 * j + 1];
+  }
+  return mu;
+}
+
+std::vector<fe> aggregate_weights(int N, const fe *b) {
+  // sumcheck_aggr (MPI_utils.cpp:2631-2644): per coefficient the N shares s
+  // are unpacked (unpack_secret_share with _k = k = N: E = DFT(D IDFT(s)),
+  // D = diag(omega_{2N}^{-i})) and combined as sum_{j < N/4} b_j E[2j] =
+  // g^T E with g[2j] = b_j.  Both transform matrices are symmetric, so the
+  // weights of the shares are lambda = IDFT(D DFT(g)).
+  const int lg = ilog2(N);
+  std::vector<fe> g(N, fe_zero());
+  for (int j = 0; j < N / 4; j++) g[2 * j] = b[j];
+  std::vector<fe> h = host_dft(g, root_of_unity(lg));
+  const fe w2n_inv = finv(root_of_unity(1 + lg));
+  fe mul = fe_one();
+  for (int i = 0; i < N; i++) {
+    h[i] = fmul(mul, h[i]);
+    mul = fmul(w2n_inv, mul);
+  }
+  return host_idft(h);
+}
+
+void multifold5_launch(const fe *cw, uint64_t n, const fe *a, int logd, fe *out, const NttTables &tn,
+                       cudaStream_t s) {
+  if (logd < 1 || logd > kMaxFoldLog) throw ArgError("RS_multifold5: fold degree must be 2..16");
+  if (n < (2ull << logd)) throw ArgError("RS_multifold5: codeword shorter than two folds");
+  const fe len_inv = finv(fe_make(1ull << logd, 0));
+  multifold5_kernel<<<grid(n >> logd), 256, 0, s>>>(cw, n, a, logd, out, tn.lo_inv, tn.hi_inv, len_inv);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void powers_launch(fe r, uint64_t n, fe *out, cudaStream_t s) {
+  powers_kernel<<<grid(n), 256, 0, s>>>(r, n, out);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s) {
+  coset_kernel<<<grid(n), 256, 0, s>>>(x, n, t.lo_inv, t.hi_inv);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void column_merkle_launch(const fe *rows, int nrows, uint64_t L, uint8_t *levels, int logN, uint8_t *root,
+                          cudaStream_t s) {
+  column_root_kernel<<<grid(L), 256, 0, s>>>(rows, nrows, L, levels);
+  GBZ_CUDA(cudaGetLastError());
+  merkle_from_leaves_launch(levels, L, s);
+  party_root_kernel<<<1, 32, 0, s>>>(levels + 32 * (2 * L - 2), logN, root);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void shares_launch(const fe *v, const fe *fill, uint64_t groups, int N, const fe *mu, fe *shares, cudaStream_t s) {
+  shares_kernel<<<grid(groups), 256, 0, s>>>(v, fill, groups, N, N / 4, N / 2, mu, shares);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void aggregate_launch(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out, cudaStream_t s) {
+  aggregate_kernel<<<grid(len), 256, 0, s>>>(msgs, N, len, lambda, out);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void nonzero_blocks_launch(const fe *v, uint64_t nblocks, int logd, uint8_t *flags, cudaStream_t s) {
+  nonzero_blocks_kernel<<<grid(nblocks), 256, 0, s>>>(v, nblocks, logd, flags);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+uint64_t cophase1_parts(uint64_t nblocks, int blocks_per_cta) {
+  return (nblocks + blocks_per_cta - 1) / blocks_per_cta;
+}
+
+void cophase1_reduce_launch(const fe *e1, const fe *e2, const fe *e3, const fe *e4, const uint8_t *flags,
+                            uint64_t nblocks, int logD, int blocks_per_cta, fe *partial, fe *H, cudaStream_t s) {
+  if (logD > kMaxCoLogD) throw ArgError("coSumcheck: extended block longer than 2^13");
+  const uint64_t parts = cophase1_parts(nblocks, blocks_per_cta);
+  const unsigned chunks = logD > 8 ? 1u << (logD - 8) : 1u;
+  cophase1_partial_kernel<<<dim3((unsigned)parts, chunks), 256, 0, s>>>(e1, e2, e3, e4, flags, nblocks, logD,
+                                                                        blocks_per_cta, partial);
+  GBZ_CUDA(cudaGetLastError());
+  sum_partials_kernel<<<grid(1ull << logD), 256, 0, s>>>(partial, parts, 1u << logD, H);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void cophase2_launch(const fe *v, uint64_t n, const fe *L, int logd, fe *out, cudaStream_t s) {
+  if (logd > 10) throw ArgError("coSumcheck phase 2: block longer than 1024");
+  cophase2_kernel<<<grid(n >> logd), 256, 0, s>>>(v, n >> logd, L, logd, out);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+}  // namespace gbz

@@ -1,0 +1,37 @@
+// Launchers of the coPCS-side kernels (gbz_copcs.cu).
+#pragma once
+#include <vector>
+
+#include "gbz_internal.cuh"
+
+namespace gbz {
+
+// RS_multifold5 (coPCS_utils.cpp:386-437): out (n / 2^logd) from cw (n),
+// fold weights a (2^logd, device); tn: twiddle tables of length n.
+void multifold5_launch(const fe *cw, uint64_t n, const fe *a, int logd, fe *out, const NttTables &tn,
+                       cudaStream_t s);
+// out[i] = r^i for i < n.
+void powers_launch(fe r, uint64_t n, fe *out, cudaStream_t s);
+// x[j] *= omega_T^{-j} for j < n, T = 2^t.logn.
+void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s);
+// distributed_MT for one party (coPCS.cpp:152-202): levels (2L - 1 hashes,
+// column roots first) and the leader's root over 2^logN parties.
+void column_merkle_launch(const fe *rows, int nrows, uint64_t L, uint8_t *levels, int logN, uint8_t *root,
+                          cudaStream_t s);
+// Packed Shamir shares (compute_secret_shares, MPI_utils.cpp:2738-2764).
+std::vector<fe> shamir_share_matrix(int N);
+void shares_launch(const fe *v, const fe *fill, uint64_t groups, int N, const fe *mu, fe *shares, cudaStream_t s);
+// Leader aggregation of party messages (sumcheck_aggr, MPI_utils.cpp:2604-2670).
+std::vector<fe> aggregate_weights(int N, const fe *b);
+void aggregate_launch(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out, cudaStream_t s);
+// coSumcheck phase 1 helpers; extended blocks of up to 2^13 entries (one
+// batched transform per block).
+constexpr int kMaxCoLogD = 13;
+void nonzero_blocks_launch(const fe *v, uint64_t nblocks, int logd, uint8_t *flags, cudaStream_t s);
+uint64_t cophase1_parts(uint64_t nblocks, int blocks_per_cta);
+void cophase1_reduce_launch(const fe *e1, const fe *e2, const fe *e3, const fe *e4, const uint8_t *flags,
+                            uint64_t nblocks, int logD, int blocks_per_cta, fe *partial, fe *H, cudaStream_t s);
+// coSumcheck phase 2 (coSumcheck.cpp:66-148, 201-213).
+void cophase2_launch(const fe *v, uint64_t n, const fe *L, int logd, fe *out, cudaStream_t s);
+
+}  // namespace gbz

@@ -104,6 +104,11 @@ void ntt_sparse_accumulate(const NttTables &t, const int32_t *q, const fe *c, in
                            fe *tmp, cudaStream_t s);
 void ntt_tables_build(NttTables &t, int logn);
 int ntt_launch_count(int logn);
+// count independent transforms of length 2^t.logn (<= 2^13): transform g
+// reads in[g * in_stride + j] for j < j_valid (zero beyond) and writes
+// out[g * 2^logn + k].
+void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t j_valid, fe *out, uint64_t count,
+                 bool inverse, cudaStream_t s);
 void ntt_tables_free(NttTables &t);
 
 // --------------------------------------------------------------- Merkle
@@ -113,6 +118,9 @@ void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStre
 void blake3_batch_launch(const uint8_t *in, uint8_t *out, uint64_t count, cudaStream_t s);
 inline uint64_t merkle_hashes(uint64_t N) { return N / 2 - 1; }
 int merkle_launch_count(uint64_t N);
+// create_tree_blake (merkle_tree.cpp:267-299) over L leaf hashes stored at
+// levels[0 .. L): writes levels 1.. after them (2L - 1 hashes in total).
+void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s);
 
 // ------------------------------------------------------------- sumcheck
 // One fused sumcheck step over vectors (a, b) of length m:

@@ -139,6 +139,25 @@ void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStre
   }
 }
 
+void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s) {
+  if (!is_pow2(L)) throw ArgError("Merkle tree over leaves needs a power-of-two count");
+  const int depth = ilog2(L);  // levels 1..depth above the leaves
+  uint64_t cnt = L / 2, off = L, child_off = 0;
+  int level = 1;
+  while (level <= depth) {
+    const int nlev = min(kLogNodesPerCta + 1, depth - level + 1);
+    const uint64_t blocks = (cnt + kNodesPerCta - 1) / kNodesPerCta;
+    merkle_levels_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(nullptr, levels + 32 * child_off, cnt, levels, off, nlev);
+    GBZ_CUDA(cudaGetLastError());
+    for (int k = 0; k < nlev; k++) {
+      child_off = off;
+      off += cnt;
+      cnt >>= 1;
+    }
+    level += nlev;
+  }
+}
+
 int merkle_launch_count(uint64_t N) {
   const int depth = ilog2(N / 4);
   int level = 0, k = 0;

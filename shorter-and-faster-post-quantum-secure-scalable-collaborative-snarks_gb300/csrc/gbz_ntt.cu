@@ -52,6 +52,9 @@ struct PassArgs {
   // Accumulating output: out[addr] += v for addr < acc_n, other outputs dropped.
   uint64_t acc_n;
   int acc;
+  // Entries j >= j_valid of every sub-transform are zero (per-transform
+  // padding of batched transforms; S when unused).
+  uint32_t j_valid;
 };
 
 // Shared-memory swizzle: element a lives at a ^ ((a >> 3) & 7), which keeps
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
       for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
         const uint32_t b = e >> logS, j = e & (S - 1);
         const uint64_t addr = (g0 + b) * a.in_gstride + j;
-        sm[swz(e)] = addr < a.n_valid ? a.in[addr] : fe_zero();
+        sm[swz(e)] = (addr < a.n_valid && j < a.j_valid) ? a.in[addr] : fe_zero();
       }
     } else {
       for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
@@ -386,6 +389,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   a.wh = inverse ? t.sub_inv : t.sub_fwd;
   a.scale = t.inv_len;
   a.inverse = inverse ? 1 : 0;
+  a.j_valid = 1u << kSubLog;
   if (logn <= kSubLog) {
     a.in = in;
     a.out = out;
@@ -452,6 +456,41 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
 void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                 cudaStream_t s) {
   ntt_two_pass(t, in, n_valid, out, tmp, inverse, nullptr, nullptr, 0, 0, s);
+}
+
+void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t j_valid, fe *out, uint64_t count,
+                 bool inverse, cudaStream_t s) {
+  const int logS = t.logn;
+  if (logS > kSubLog) throw ArgError("batched transform longer than 2^13");
+  if (!count) return;
+  PassArgs a{};
+  a.wh = inverse ? t.sub_inv : t.sub_fwd;
+  a.scale = t.inv_len;
+  a.inverse = inverse ? 1 : 0;
+  a.in = in;
+  a.out = out;
+  a.n_valid = ~0ull;
+  a.j_valid = j_valid;
+  a.in_gstride = in_stride;
+  a.in_jstride = 1;
+  a.out_gstride = 1ull << logS;
+  a.out_kstride = 1;
+  a.logS = logS;
+  a.has_scale = inverse;
+  // up to 2^12 staged elements per CTA, never more transforms than there are
+  int logB = std::max(0, 12 - logS);
+  while (logB > 0 && (1ull << logB) > count) logB--;
+  a.logB = logB;
+  const uint64_t B = 1ull << logB;
+  const uint64_t full = count / B * B;
+  if (full) launch_pass(a, full, s);
+  if (full < count) {  // remaining transforms one per CTA
+    PassArgs r = a;
+    r.in = in + full * in_stride;
+    r.out = out + (full << logS);
+    r.logB = 0;
+    launch_pass(r, count - full, s);
+  }
 }
 
 void ntt_sparse_accumulate(const NttTables &t, const int32_t *q, const fe *c, int l, fe *acc, uint64_t nacc,

@@ -39,7 +39,9 @@ EXPORTS = (
     "gbz_sumcheck_quadratic", "gbz_sumcheck_fold", "gbz_whir_update_betas", "gbz_hash_to_field",
     "gbz_prng_seed", "gbz_prng_next", "gbz_prng_field", "gbz_field_ops_host",
     "gbz_prove_transcript_bytes", "gbz_prove", "gbz_prove_launches", "gbz_profile_enable",
-    "gbz_profile_read", "gbz_whir_update_betas_noalloc",
+    "gbz_profile_read", "gbz_whir_update_betas_noalloc", "gbz_rs_multifold5", "gbz_lagrange_coeff",
+    "gbz_encode_rows", "gbz_column_merkle", "gbz_secret_shares", "gbz_party_aggregate",
+    "gbz_cosumcheck_phase1", "gbz_cosumcheck_phase2",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -90,6 +92,14 @@ def _load():
         "gbz_profile_enable": (c_int, [vp, c_int]),
         "gbz_profile_read": (c_int, [vp, c_int, c_int, vp, vp]),
         "gbz_whir_update_betas_noalloc": (c_int, [vp, u64, vp, c_int, u64, vp, vp, vp]),
+        "gbz_rs_multifold5": (c_int, [vp, vp, u64, vp, c_int, vp, c_int]),
+        "gbz_lagrange_coeff": (c_int, [vp, vp, c_int, vp, c_int]),
+        "gbz_encode_rows": (c_int, [vp, vp, c_int, c_int, c_int, c_int, vp, c_int]),
+        "gbz_column_merkle": (c_int, [vp, vp, c_int, c_int, c_int, vp, vp, c_int]),
+        "gbz_secret_shares": (c_int, [vp, vp, u64, c_int, c_int, ctypes.c_uint32, vp, c_int]),
+        "gbz_party_aggregate": (c_int, [vp, vp, c_int, u64, vp, vp, c_int]),
+        "gbz_cosumcheck_phase1": (c_int, [vp, vp, vp, vp, vp, u64, c_int, vp, c_int]),
+        "gbz_cosumcheck_phase2": (c_int, [vp, vp, u64, vp, c_int, vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -256,6 +266,79 @@ class Context:
         self.check(lib.gbz_whir_update_betas(self.h, _ptr(b), b.shape[0], _ptr(q), len(q), n, _ptr(r),
                                              _ptr(ch), MEM_HOST))
         return b, ch
+
+    # ----------------------------------------------------------- coPCS side
+    def RS_multifold5(self, codeword, a):
+        """RS_multifold5 (coPCS_utils.cpp:386-437): fold by d = len(a)."""
+        cw, a = _fe(codeword), _fe(a)
+        n, d = cw.shape[0], a.shape[0]
+        out = fe_array(n // d)
+        self.check(lib.gbz_rs_multifold5(self.h, _ptr(cw), n, _ptr(a), d.bit_length() - 1, _ptr(out), MEM_HOST))
+        return out
+
+    def compute_lagrange_coeff(self, r, logd):
+        """compute_lagrange_coeff (utils.cpp:169-197) over 2^logd points."""
+        r = np.ascontiguousarray(r, dtype=np.uint64).reshape(2)
+        out = fe_array(1 << logd)
+        self.check(lib.gbz_lagrange_coeff(self.h, _ptr(r), logd, _ptr(out), MEM_HOST))
+        return out
+
+    def Encode(self, rows, rate, log_rate_offset):
+        """Encode (coPCS.cpp:131-147) of a (rows, 2^logrow, 2) array."""
+        rows = np.ascontiguousarray(rows, dtype=np.uint64)
+        nrows, n = rows.shape[0], rows.shape[1]
+        out = np.zeros((nrows, n * rate, 2), dtype=np.uint64)
+        self.check(lib.gbz_encode_rows(self.h, _ptr(rows), nrows, n.bit_length() - 1, rate, log_rate_offset,
+                                       _ptr(out), MEM_HOST))
+        return out
+
+    def distributed_MT(self, rows, nparties):
+        """(levels (2L-1, 32), leader root (32,)) of one party's row batch."""
+        rows = np.ascontiguousarray(rows, dtype=np.uint64)
+        nrows, L = rows.shape[0], rows.shape[1]
+        levels = np.zeros((2 * L - 1, 32), dtype=np.uint8)
+        root = np.zeros(32, dtype=np.uint8)
+        self.check(lib.gbz_column_merkle(self.h, _ptr(rows), nrows, L.bit_length() - 1, nparties, _ptr(levels),
+                                         _ptr(root), MEM_HOST))
+        return levels, root
+
+    def compute_secret_shares(self, v, N, privacy=False, prng_seed=1):
+        """(N, 4M/N, 2) packed Shamir shares of v (MPI_utils.cpp:2738-2764)."""
+        v = _fe(v)
+        M = v.shape[0]
+        out = np.zeros((N, 4 * M // N, 2), dtype=np.uint64)
+        self.check(lib.gbz_secret_shares(self.h, _ptr(v), M, N, int(bool(privacy)), prng_seed, _ptr(out),
+                                         MEM_HOST))
+        return out
+
+    def sumcheck_aggr(self, msgs, b):
+        """Leader aggregation of (N, len, 2) party messages with N/4 weights b."""
+        msgs = np.ascontiguousarray(msgs, dtype=np.uint64)
+        b = _fe(b)
+        N, length = msgs.shape[0], msgs.shape[1]
+        out = fe_array(length)
+        self.check(lib.gbz_party_aggregate(self.h, _ptr(msgs), N, length, _ptr(b), _ptr(out), MEM_HOST))
+        return out
+
+    def coSumcheck_phase1(self, p1, p2, logd, p3=None, b1=None):
+        """Local round sums: 2d entries (quadratic) or 4d (cubic, p3 and b1 given)."""
+        p1, p2 = _fe(p1), _fe(p2)
+        p3 = None if p3 is None else _fe(p3)
+        b1 = None if b1 is None else _fe(b1)
+        mem = _mem(p1)
+        H = fe_array((4 if p3 is not None else 2) << logd)
+        self.check(lib.gbz_cosumcheck_phase1(self.h, _ptr(p1), _ptr(p2), _ptr(p3), _ptr(b1), p1.shape[0], logd,
+                                             _ptr(H), mem))
+        return H
+
+    def coSumcheck_phase2(self, v, L):
+        """out[j] = sum_k L[k] v[j d + k] (coSumcheck.cpp:201-213)."""
+        v, L = _fe(v), _fe(L)
+        d = L.shape[0]
+        out = fe_array(v.shape[0] // d)
+        self.check(lib.gbz_cosumcheck_phase2(self.h, _ptr(v), v.shape[0], _ptr(L), d.bit_length() - 1, _ptr(out),
+                                             MEM_HOST))
+        return out
 
     # ------------------------------------------------------------ profiling
     def profile_enable(self, on=True):
