@@ -131,6 +131,47 @@ gbz_status gbz_sumcheck_fold(gbz_ctx *ctx, uint64_t *v, uint64_t m, const uint64
 gbz_status gbz_whir_update_betas(gbz_ctx *ctx, uint64_t *b, uint64_t nb, const int32_t *queries, int l,
                                  uint64_t N, const uint64_t *r, uint64_t *challenges, int mem);
 
+/* ------------------------------------------- many proofs: batch, serving */
+
+/* Options of the many-proof scheduler.  A slot is one CUDA stream with its
+ * own per-shape plan (buffers, verifier state, transcript); proofs in
+ * different slots overlap on the device and never share memory, so every
+ * transcript is the one gbz_prove returns for the same inputs.  Plans (and
+ * their captured graphs) stay cached in the context across calls. */
+typedef struct gbz_sched_opts {
+  int lanes;               /* concurrent slots (0: 8) */
+  int depth;               /* serving: proofs in flight per slot before admission waits (0: 2) */
+  int graphs;              /* 1: replay one captured CUDA graph per (slot, shape); 0: direct launches */
+  uint64_t reserve_bytes;  /* device memory left free when a new shape is admitted (0: 1 GiB) */
+} gbz_sched_opts;
+
+/* Proves count independent statements of mixed shapes as one batch: the
+ * proofs are assigned longest-first to the least-loaded slot and enqueued
+ * round-robin over the slots.  witness[i] holds 2^logn[i] elements and
+ * transcript[i] capacity[i] >= gbz_prove_transcript_bytes(logn[i], rate[i])
+ * bytes, all host (pinned, e.g. gbz_host_alloc, for overlap) or all device
+ * per mem.  latency_s[i] (optional) = completion of proof i after the
+ * batch started; *makespan_s (optional) = completion of the last one.
+ * opts may be NULL (defaults).  No counterpart in the reference, which
+ * proves one statement per process (main.cpp). */
+gbz_status gbz_prove_batch(gbz_ctx *ctx, int count, const uint64_t *const *witness, const int *logn, const int *rate,
+                           const uint32_t *prng_seed, uint8_t *const *transcript, const uint64_t *capacity, int mem,
+                           const gbz_sched_opts *opts, double *latency_s, double *makespan_s);
+
+/* Serving loop over timed arrivals: proof i is admitted no earlier than
+ * arrival_s[i] seconds after the call starts, to the least-loaded slot with
+ * fewer than opts->depth proofs in flight, once its plan fits in free device
+ * memory (idle cached plans are evicted least recently used first).
+ * latency_s[i] = completion - arrival; other arguments as gbz_prove_batch. */
+gbz_status gbz_serve(gbz_ctx *ctx, int count, const double *arrival_s, const uint64_t *const *witness,
+                     const int *logn, const int *rate, const uint32_t *prng_seed, uint8_t *const *transcript,
+                     const uint64_t *capacity, int mem, const gbz_sched_opts *opts, double *latency_s,
+                     double *makespan_s);
+
+/* Frees the scheduler's cached slot plans; *cached_bytes (optional) gets
+ * the device bytes they held. */
+gbz_status gbz_sched_release(gbz_ctx *ctx, uint64_t *cached_bytes);
+
 /* ----------------------------------------------------- coPCS-side rows */
 
 /* RS fold of a codeword of n elements by d = 2^logd (1 <= logd <= 4) with

@@ -9,6 +9,7 @@
 #include "../../include/gbz.h"
 #include "gbz_copcs.cuh"
 #include "gbz_prover.cuh"
+#include "gbz_sched.cuh"
 
 using namespace gbz;
 
@@ -24,6 +25,7 @@ struct gbz_ctx {
   fe *ub_scratch = nullptr;
   bool profiling = false;
   std::map<std::pair<int, int>, std::unique_ptr<Profiler>> profilers;
+  std::unique_ptr<Scheduler> sched;
 
   void *buf(int slot, uint64_t bytes) {
     auto &e = scratch[slot];
@@ -165,6 +167,7 @@ void gbz_destroy(gbz_ctx *ctx) {
   try {
     DeviceGuard g(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    ctx->sched.reset();
     ctx->plans.clear();
     ctx->profilers.clear();
     for (auto &kv : ctx->ntt) ntt_tables_free(kv.second);
@@ -701,6 +704,89 @@ gbz_status gbz_cosumcheck_phase2(gbz_ctx *ctx, const uint64_t *v, uint64_t n, co
   cophase2_launch(dv, n, dL, logd, dout, ctx->stream);
   copy_out(ctx, (fe *)out, dout, 16 * (n >> logd), mem);
   GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+}  // extern "C"
+
+namespace {
+
+gbz_status prove_many(gbz_ctx *ctx, int count, const double *arrival_s, const uint64_t *const *witness,
+                      const int *logn, const int *rate, const uint32_t *prng_seed, uint8_t *const *transcript,
+                      const uint64_t *capacity, int mem, const gbz_sched_opts *opts, double *latency_s,
+                      double *makespan_s) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  if (count < 0) throw ArgError("count must be non-negative");
+  if (count > 0) {
+    need(witness, "witness");
+    need(logn, "logn");
+    need(rate, "rate");
+    need(prng_seed, "prng_seed");
+    need(transcript, "transcript");
+    need(capacity, "capacity");
+  }
+  SchedOpts o;
+  if (opts) {
+    if (opts->lanes < 0 || opts->lanes > 64) throw ArgError("sched: lanes must be in [0, 64]");
+    if (opts->depth < 0) throw ArgError("sched: depth must be non-negative");
+    if (opts->lanes) o.lanes = opts->lanes;
+    if (opts->depth) o.depth = opts->depth;
+    if (opts->graphs >= 0) o.graphs = opts->graphs != 0;
+    if (opts->reserve_bytes) o.reserve = opts->reserve_bytes;
+  }
+  std::vector<ProofJob> jobs(count);
+  for (int i = 0; i < count; i++) {
+    need(witness[i], "witness[i]");
+    need(transcript[i], "transcript[i]");
+    const uint64_t tb = gbz_prove_transcript_bytes(logn[i], rate[i]);
+    if (!tb) throw ArgError("proof " + std::to_string(i) + ": unsupported shape 2^" + std::to_string(logn[i]) +
+                            " at rate " + std::to_string(rate[i]));
+    if (capacity[i] < tb)
+      return fail(ctx, GBZ_ESMALL, "proof " + std::to_string(i) + ": transcript buffer smaller than gbz_prove_transcript_bytes");
+    if (arrival_s && !(arrival_s[i] >= 0)) throw ArgError("arrival times must be non-negative");
+    jobs[i].witness = (const fe *)witness[i];
+    jobs[i].logn = logn[i];
+    jobs[i].rate = rate[i];
+    jobs[i].seed = prng_seed[i];
+    jobs[i].transcript = transcript[i];
+  }
+  if (!ctx->sched) ctx->sched.reset(new Scheduler());
+  std::vector<uint32_t> errors;
+  ctx->sched->run(jobs, arrival_s, mem, o, latency_s, makespan_s, errors);
+  for (int i = 0; i < count; i++)
+    if (errors[i])
+      return fail(ctx, GBZ_ECHECK, "proof " + std::to_string(i) + ": a sumcheck round message did not match its claim");
+  API_END(ctx)
+}
+
+}  // namespace
+
+extern "C" {
+
+gbz_status gbz_prove_batch(gbz_ctx *ctx, int count, const uint64_t *const *witness, const int *logn, const int *rate,
+                           const uint32_t *prng_seed, uint8_t *const *transcript, const uint64_t *capacity, int mem,
+                           const gbz_sched_opts *opts, double *latency_s, double *makespan_s) {
+  return prove_many(ctx, count, nullptr, witness, logn, rate, prng_seed, transcript, capacity, mem, opts, latency_s,
+                    makespan_s);
+}
+
+gbz_status gbz_serve(gbz_ctx *ctx, int count, const double *arrival_s, const uint64_t *const *witness,
+                     const int *logn, const int *rate, const uint32_t *prng_seed, uint8_t *const *transcript,
+                     const uint64_t *capacity, int mem, const gbz_sched_opts *opts, double *latency_s,
+                     double *makespan_s) {
+  if (count > 0 && !arrival_s) {
+    if (!ctx) return GBZ_EINVAL;
+    return fail(ctx, GBZ_EINVAL, "null pointer: arrival_s");
+  }
+  return prove_many(ctx, count, arrival_s, witness, logn, rate, prng_seed, transcript, capacity, mem, opts,
+                    latency_s, makespan_s);
+}
+
+gbz_status gbz_sched_release(gbz_ctx *ctx, uint64_t *cached_bytes) {
+  API_BEGIN(ctx)
+  if (cached_bytes) *cached_bytes = ctx->sched ? ctx->sched->cached_bytes() : 0;
+  ctx->sched.reset();
   API_END(ctx)
 }
 

@@ -44,6 +44,7 @@ struct ProofState {
   fe qw[kMaxQueries];         // c_i-weighted query roots, see whir kernels
   fe omega_q[kMaxQueries];    // omega_N^{q_i}
   uint32_t error;             // non-zero: a device-side consistency check failed
+  uint32_t seed_in;           // PRNG seed of the next proof when it is replayed from a graph
 };
 
 // Error capture for the C-ABI.
@@ -141,8 +142,5 @@ void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s);
 // pw_scratch holds kUpdateBetasScratch elements.
 constexpr uint64_t kUpdateBetasScratch = (uint64_t)kMaxQueries * 256;
 void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s);
-
-// RS_multifold5 (coPCS_utils.cpp:386-437).
-void rs_multifold5_launch(const fe *cw, uint64_t n, const fe *a, int logd, fe *out, cudaStream_t s);
 
 }  // namespace gbz

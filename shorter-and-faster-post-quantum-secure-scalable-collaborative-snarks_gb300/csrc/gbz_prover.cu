@@ -36,10 +36,10 @@ __device__ __forceinline__ void put_fe(uint8_t *tr, uint64_t off, fe v) {
   p[3] = (uint32_t)(v.im >> 32);
 }
 
-__global__ void k_init(ProofState *st, uint32_t seed) {
+__global__ void k_init(ProofState *st, uint32_t seed, int seed_in_state) {
   if (threadIdx.x) return;
   st->fs = fe_zero();
-  prng_seed(st->prng, seed);
+  prng_seed(st->prng, seed_in_state ? st->seed_in : seed);
   st->y = fe_zero();
   st->K = fe_zero();
   st->error = 0;
@@ -359,7 +359,7 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
 // Enqueue one proof.  witness: device pointer (nullptr: use plan->w).
 // The dry run (dry = true) launches nothing; it fixes the transcript layout
 // and counts the launches per category.
-void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry) {
+void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry, bool seed_in_state) {
   Layout &lay = p.layout;
   lay.len = 0;
   if (dry) {
@@ -394,7 +394,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     GBZ_CUDA(cudaEventRecord(p.ev_in, s));
     GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_in, 0));
   }
-  RUN(PC_PROTOCOL, 1, k_init<<<1, 32, 0, s>>>(st, prng_seed));
+  RUN(PC_PROTOCOL, 1, k_init<<<1, 32, 0, s>>>(st, prng_seed, seed_in_state ? 1 : 0));
 
   // 1. commitment: codeword = NTT(w padded to rate*n), Merkle tree.
   uint64_t L = p.L;
@@ -580,6 +580,26 @@ Profiler::~Profiler() {
       cudaEventDestroy(e.first);
       cudaEventDestroy(e.second);
     }
+}
+
+namespace {
+__global__ void k_set_seed(ProofState *st, uint32_t seed) {
+  if (threadIdx.x == 0) st->seed_in = seed;
+}
+}  // namespace
+
+void set_seed_launch(ProofPlan &p, uint32_t seed, cudaStream_t s) {
+  k_set_seed<<<1, 32, 0, s>>>(p.st, seed);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+uint64_t plan_bytes(int logn, int rate) {
+  const uint64_t n = 1ull << logn, L = n * (uint64_t)rate;
+  uint64_t b = sizeof(fe) * (n + L + L / 2 + L + L / 2 + 4 * (n / 2) + n);
+  b += 32 * (merkle_hashes(L) + merkle_hashes(L / 2 >= 4 ? L / 2 : 4));
+  b += sizeof(fe) * (3 * (uint64_t)sc_blocks(n / 2) + kUpdateBetasScratch) + sizeof(ProofState);
+  b += 64ull << 20;  // transcript, twiddle tables and allocation granularity (upper bound)
+  return b;
 }
 
 uint32_t plan_error_flags(ProofPlan &p, cudaStream_t s) {

@@ -77,8 +77,15 @@ struct ProofPlan {
 };
 
 std::unique_ptr<ProofPlan> plan_create(int logn, int rate);
-// Enqueues one proof on stream s (dry: only computes the layout).
-void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry);
+// Enqueues one proof on stream s (dry: only computes the layout).  With
+// seed_in_state the PRNG seed is read from the plan's state (written by
+// set_seed_launch), so that the enqueued work can be captured once as a CUDA
+// graph and replayed for any seed.
+void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry,
+                   bool seed_in_state = false);
+void set_seed_launch(ProofPlan &p, uint32_t seed, cudaStream_t s);
+// Device bytes a plan of this shape allocates (an upper bound).
+uint64_t plan_bytes(int logn, int rate);
 // Reads the device-side consistency flags (synchronises s).
 uint32_t plan_error_flags(ProofPlan &p, cudaStream_t s);
 int whir_query_count(int rate);

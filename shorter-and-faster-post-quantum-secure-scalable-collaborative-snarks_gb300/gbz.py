@@ -41,10 +41,36 @@ EXPORTS = (
     "gbz_prove_transcript_bytes", "gbz_prove", "gbz_prove_launches", "gbz_profile_enable",
     "gbz_profile_read", "gbz_whir_update_betas_noalloc", "gbz_rs_multifold5", "gbz_lagrange_coeff",
     "gbz_encode_rows", "gbz_column_merkle", "gbz_secret_shares", "gbz_party_aggregate",
-    "gbz_cosumcheck_phase1", "gbz_cosumcheck_phase2",
+    "gbz_cosumcheck_phase1", "gbz_cosumcheck_phase2", "gbz_prove_batch", "gbz_serve", "gbz_sched_release",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
+
+
+class SchedOpts(ctypes.Structure):
+    """gbz_sched_opts: slots, in-flight depth per slot, graph replay, HBM reserve."""
+    _fields_ = [("lanes", ctypes.c_int), ("depth", ctypes.c_int), ("graphs", ctypes.c_int),
+                ("reserve_bytes", ctypes.c_uint64)]
+
+
+class PinnedArray:
+    """Page-locked host memory (gbz_host_alloc) viewed as a numpy array, so
+    that host<->device copies of the scheduler overlap with proving."""
+
+    def __init__(self, shape, dtype):
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.p = ctypes.c_void_p()
+        st = lib.gbz_host_alloc(ctypes.byref(self.p), max(self.nbytes, 1))
+        if st != OK:
+            raise GbzError(st, "gbz_host_alloc failed")
+        buf = (ctypes.c_uint8 * max(self.nbytes, 1)).from_address(self.p.value)
+        self.array = np.frombuffer(buf, dtype=np.uint8, count=self.nbytes).view(dtype).reshape(shape)
+
+    def __del__(self):
+        if getattr(self, "p", None) and self.p.value:
+            self.array = None
+            lib.gbz_host_free(self.p)
+            self.p = ctypes.c_void_p()
 
 
 class GbzError(RuntimeError):
@@ -100,6 +126,9 @@ def _load():
         "gbz_party_aggregate": (c_int, [vp, vp, c_int, u64, vp, vp, c_int]),
         "gbz_cosumcheck_phase1": (c_int, [vp, vp, vp, vp, vp, u64, c_int, vp, c_int]),
         "gbz_cosumcheck_phase2": (c_int, [vp, vp, u64, vp, c_int, vp, c_int]),
+        "gbz_prove_batch": (c_int, [vp, c_int, vp, vp, vp, vp, vp, vp, c_int, vp, vp, vp]),
+        "gbz_serve": (c_int, [vp, c_int, vp, vp, vp, vp, vp, vp, vp, c_int, vp, vp, vp]),
+        "gbz_sched_release": (c_int, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -266,6 +295,48 @@ class Context:
         self.check(lib.gbz_whir_update_betas(self.h, _ptr(b), b.shape[0], _ptr(q), len(q), n, _ptr(r),
                                              _ptr(ch), MEM_HOST))
         return b, ch
+
+    # ------------------------------------------------------ many proofs
+    def _prove_many(self, arrivals, witnesses, logns, rates, seeds, lanes, depth, graphs, reserve, out):
+        count = len(witnesses)
+        assert len(logns) == count and len(rates) == count and len(seeds) == count
+        mem = _mem(witnesses[0]) if count else MEM_HOST
+        if out is None:
+            out = [np.zeros(transcript_bytes(l, r), dtype=np.uint8) for l, r in zip(logns, rates)]
+        wp = (ctypes.c_void_p * max(count, 1))(*[_ptr(_fe(w)) for w in witnesses])
+        tp = (ctypes.c_void_p * max(count, 1))(*[_ptr(t) for t in out])
+        cap = np.array([t.nbytes if isinstance(t, np.ndarray) else t.numel() * t.element_size() for t in out]
+                       or [0], dtype=np.uint64)
+        ln = np.ascontiguousarray(list(logns) or [0], dtype=np.int32)
+        rt = np.ascontiguousarray(list(rates) or [0], dtype=np.int32)
+        sd = np.ascontiguousarray(list(seeds) or [0], dtype=np.uint32)
+        lat = np.zeros(max(count, 1), dtype=np.float64)
+        mk = ctypes.c_double()
+        opts = SchedOpts(lanes, depth, int(bool(graphs)), reserve)
+        args = [ctypes.cast(wp, ctypes.c_void_p), _ptr(ln), _ptr(rt), _ptr(sd), ctypes.cast(tp, ctypes.c_void_p),
+                _ptr(cap), mem, ctypes.byref(opts), _ptr(lat), ctypes.byref(mk)]
+        if arrivals is None:
+            st = lib.gbz_prove_batch(self.h, count, *args)
+        else:
+            arr = np.ascontiguousarray(list(arrivals) or [0.0], dtype=np.float64)
+            st = lib.gbz_serve(self.h, count, _ptr(arr), *args)
+        self.check(st)
+        return out, lat[:count], mk.value
+
+    def prove_batch(self, witnesses, logns, rates, seeds, lanes=8, graphs=True, reserve=0, out=None):
+        """Independent proofs of mixed shapes as one batch (gbz_prove_batch).
+        Returns (transcripts, per-proof completion seconds, makespan seconds)."""
+        return self._prove_many(None, witnesses, logns, rates, seeds, lanes, 0, graphs, reserve, out)
+
+    def serve(self, arrivals, witnesses, logns, rates, seeds, lanes=8, depth=2, graphs=True, reserve=0, out=None):
+        """Timed arrivals (seconds from the call) through the serving loop
+        (gbz_serve).  Returns (transcripts, latencies, makespan)."""
+        return self._prove_many(arrivals, witnesses, logns, rates, seeds, lanes, depth, graphs, reserve, out)
+
+    def sched_release(self):
+        b = ctypes.c_uint64()
+        self.check(lib.gbz_sched_release(self.h, ctypes.byref(b)))
+        return b.value
 
     # ----------------------------------------------------------- coPCS side
     def RS_multifold5(self, codeword, a):
