@@ -1023,3 +1023,164 @@ void orc_cophase2(const uint64_t *v, int64_t n, const uint64_t *L, int logd, uin
     st(out, j, acc);
   }
 }
+
+/* ----------------------------------------- sumcheck round forms (a11) */
+/* Line of a pair: linear_poly(v[2j+1] - v[2j], v[2j]) (polynomial.h:46-59). */
+typedef struct { fe a, b; } lin_t;
+static inline lin_t lin_at(const uint64_t *v, int64_t j) {
+  fe lo = ld(v, 2 * j), hi = ld(v, 2 * j + 1);
+  lin_t l = {f_sub(hi, lo), lo};
+  return l;
+}
+/* linear * linear -> (a, b, c) (polynomial.cpp:133-135) */
+static inline void lin_mul(lin_t x, lin_t y, fe q[3]) {
+  q[0] = f_mul(x.a, y.a);
+  q[1] = f_add(f_mul(x.a, y.b), f_mul(x.b, y.a));
+  q[2] = f_mul(x.b, y.b);
+}
+/* quadratic * linear -> cubic (polynomial.cpp:91-93) */
+static inline void quad_lin(const fe q[3], lin_t x, fe c[4]) {
+  c[0] = f_mul(q[0], x.a);
+  c[1] = f_add(f_mul(q[0], x.b), f_mul(q[1], x.a));
+  c[2] = f_add(f_mul(q[1], x.b), f_mul(q[2], x.a));
+  c[3] = f_mul(q[2], x.b);
+}
+
+int orc_sumcheck_form_vectors(int form) {
+  static const int nv[4] = {2, 3, 6, 6};
+  return form >= 0 && form < 4 ? nv[form] : 0;
+}
+int orc_sumcheck_form_degree(int form) {
+  static const int dg[4] = {2, 3, 2, 3};
+  return form >= 0 && form < 4 ? dg[form] : 0;
+}
+
+void orc_sumcheck_round(int form, const uint64_t *const *v, int64_t m, const uint64_t bb[2], uint64_t *out) {
+  fe acc[4] = {f_zero(), f_zero(), f_zero(), f_zero()};
+  fe accr[3] = {f_zero(), f_zero(), f_zero()};
+  fe b = bb ? f_make(bb[0], bb[1]) : f_zero();
+  for (int64_t j = 0; j < m / 2; j++) {
+    fe q[3], c[4];
+    if (form == 0) { /* coSumcheck_MPI.cpp:199 */
+      lin_mul(lin_at(v[0], j), lin_at(v[1], j), q);
+      for (int k = 0; k < 3; k++) acc[k] = f_add(acc[k], q[k]);
+    } else if (form == 1) { /* Distributed_Sumcheck.cpp:1144-1151 */
+      lin_mul(lin_at(v[0], j), lin_at(v[1], j), q);
+      quad_lin(q, lin_at(v[2], j), c);
+      for (int k = 0; k < 4; k++) acc[k] = f_add(acc[k], c[k]);
+    } else if (form == 2) { /* coSumcheck_MPI.cpp:156-176 */
+      lin_mul(lin_at(v[0], j), lin_at(v[1], j), q);
+      for (int k = 0; k < 3; k++) acc[k] = f_add(acc[k], q[k]);
+      lin_mul(lin_at(v[2], j), lin_at(v[3], j), q);
+      for (int k = 0; k < 3; k++) acc[k] = f_add(acc[k], q[k]);
+      lin_mul(lin_at(v[4], j), lin_at(v[5], j), q);
+      for (int k = 0; k < 3; k++) accr[k] = f_add(accr[k], q[k]);
+    } else { /* coSumcheck_MPI.cpp:12-32: v = (v1, v2, v3, beta1, r1, r2) */
+      fe qr[3];
+      lin_mul(lin_at(v[0], j), lin_at(v[1], j), q);
+      lin_mul(lin_at(v[4], j), lin_at(v[5], j), qr);
+      lin_t l3 = lin_at(v[2], j);
+      q[0] = f_add(q[0], f_mul(b, qr[0]));
+      q[1] = f_sub(f_add(q[1], f_mul(b, qr[1])), l3.a);
+      q[2] = f_sub(f_add(q[2], f_mul(b, qr[2])), l3.b);
+      quad_lin(q, lin_at(v[3], j), c);
+      for (int k = 0; k < 4; k++) acc[k] = f_add(acc[k], c[k]);
+    }
+  }
+  if (form == 2)
+    for (int k = 0; k < 3; k++) acc[k] = f_add(acc[k], f_mul(b, accr[k]));
+  for (int k = 0; k <= orc_sumcheck_form_degree(form); k++) st(out, k, acc[k]);
+}
+
+void orc_sumcheck_fold_many(int nvec, uint64_t *const *v, int64_t m, const uint64_t r[2]) {
+  fe rr = f_make(r[0], r[1]);
+  for (int k = 0; k < nvec; k++)
+    for (int64_t j = 0; j < m / 2; j++) {
+      fe lo = ld(v[k], 2 * j), hi = ld(v[k], 2 * j + 1);
+      st(v[k], j, f_add(lo, f_mul(rr, f_sub(hi, lo))));
+    }
+}
+
+static fe cubic_eval(const fe c[4], fe x) {
+  return f_add(f_mul(f_add(f_mul(f_add(f_mul(c[0], x), c[1]), x), c[2]), x), c[3]);
+}
+
+/* The distributed sumchecks of Distributed_Sumcheck.cpp for N parties held
+ * in one process: form 0 is _quadratic_sumcheck (:204-349, vectors v1, v2),
+ * form 1 is _cubic_sumcheck (:1122-1269, v1, v2, v3).  Party p owns entries
+ * [p*M, (p+1)*M) of each vector.  Each of the log2(M) - offset rounds
+ * combines the parties' round polynomials (a plain sum for form 0,
+ * aggregate_poly :86-138; weights w[p] for form 1, :140-170), draws the
+ * challenge hash_to_field of the coefficients from the chain fs
+ * (prev_challenge) and folds every party's vectors.  The leader then runs
+ * quadratic_sumcheck / cubic_sumcheck (sparse_eval.cpp:140-190, 419-475) over
+ * the parties' remaining 2^offset entries gathered party by party (form 1
+ * scales v3 by w[p], :1184-1189), taking the fourth F::_random() draw of each
+ * round from the glibc stream g.  For form 0 with N > 1 the reference's
+ * leader sizes its receive buffers for N parties each (:289-306) and so
+ * reads zeros for the other parties' v2 entries, after which its consistency
+ * check exits; the gathering here is the intended one, and parity with the
+ * reference is defined for N = 1.
+ * polys: (degree + 1) coefficients per round, chal: every challenge,
+ * fin: the leader's v1[0], v2[0] (, v3[0]).  y is updated. */
+void orc_party_sumcheck(int form, uint64_t *v1, uint64_t *v2, uint64_t *v3, int64_t M, int N, const uint64_t *w,
+                        int offset, uint64_t fs[2], orc_prng *g, uint64_t y_io[2], uint64_t *polys,
+                        uint64_t *chal, uint64_t *fin) {
+  const int nv = form == 1 ? 3 : 2, nc = nv + 1;
+  int lm = ilog2_64(M);
+  int rounds = lm - offset;
+  if (rounds <= 0) { rounds = 0; offset = lm; }
+  fe y = f_make(y_io[0], y_io[1]);
+  fe state = f_make(fs[0], fs[1]);
+  int64_t cur = M;
+  int r_i = 0;
+  uint64_t *vv[3] = {v1, v2, v3};
+  for (int i = 0; i < rounds; i++) {
+    fe H[4] = {f_zero(), f_zero(), f_zero(), f_zero()};
+    for (int p = 0; p < N; p++) {
+      const uint64_t *pv[3];
+      for (int k = 0; k < nv; k++) pv[k] = vv[k] + 2 * p * M;
+      uint64_t c[8];
+      orc_sumcheck_round(form, pv, cur, NULL, c);
+      fe wp = form == 1 ? ld(w, p) : f_one();
+      for (int k = 0; k < nc; k++) H[k] = f_add(H[k], form == 1 ? f_mul(wp, ld(c, k)) : ld(c, k));
+    }
+    for (int k = 0; k < nc; k++) st(polys, nc * r_i + k, H[k]);
+    fe rnd = fs_absorb(&state, H, nc);
+    st(chal, r_i, rnd);
+    y = nc == 4 ? cubic_eval(H, rnd) : f_add(f_mul(f_add(f_mul(H[0], rnd), H[1]), rnd), H[2]);
+    for (int p = 0; p < N; p++) {
+      uint64_t *pv[3];
+      for (int k = 0; k < nv; k++) pv[k] = vv[k] + 2 * p * M;
+      orc_sumcheck_fold_many(nv, pv, cur, chal + 2 * r_i);
+    }
+    cur /= 2;
+    r_i++;
+  }
+  int64_t S = (int64_t)1 << offset, T = S * N;
+  uint64_t *gv[3] = {NULL, NULL, NULL};
+  for (int k = 0; k < nv; k++) gv[k] = (uint64_t *)malloc(16 * T);
+  for (int p = 0; p < N; p++)
+    for (int64_t j = 0; j < S; j++)
+      for (int k = 0; k < nv; k++) {
+        fe x = ld(vv[k], p * M + j);
+        if (k == 2) x = f_mul(ld(w, p), x);
+        st(gv[k], p * S + j, x);
+      }
+  int lt = ilog2_64(T);
+  for (int i = 0; i < lt; i++) {
+    uint64_t c[8];
+    orc_sumcheck_round(form, (const uint64_t *const *)gv, T >> i, NULL, c);
+    for (int k = 0; k < nc; k++) st(polys, nc * r_i + k, ld(c, k));
+    fe rnd = f_zero();
+    for (int k = 0; k < 4; k++) rnd = prng_field(g);
+    st(chal, r_i, rnd);
+    const fe *cf = (const fe *)c;
+    y = nc == 4 ? cubic_eval(cf, rnd) : f_add(f_mul(f_add(f_mul(cf[0], rnd), cf[1]), rnd), cf[2]);
+    orc_sumcheck_fold_many(nv, gv, T >> i, chal + 2 * r_i);
+    r_i++;
+  }
+  for (int k = 0; k < nv; k++) { fin[2 * k] = gv[k][0]; fin[2 * k + 1] = gv[k][1]; free(gv[k]); }
+  fs[0] = state.re; fs[1] = state.im;
+  y_io[0] = y.re; y_io[1] = y.im;
+}

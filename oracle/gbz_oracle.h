@@ -125,6 +125,27 @@ void orc_cophase1(const uint64_t *p1, const uint64_t *p2, const uint64_t *p3, co
  * L (coSumcheck.cpp:66-148, 201-213): out[j] = sum_k L[k] v[j*d + k]. */
 void orc_cophase2(const uint64_t *v, int64_t n, const uint64_t *L, int logd, uint64_t *out);
 
+/* ---- sumcheck round forms ---------------------------------------------- */
+
+/* Round message over the m/2 pairs of the vectors v (l = linear_poly(v[2j+1]
+ * - v[2j], v[2j]), coefficients highest degree first):
+ *   form 0 quadratic (v1, v2): sum l1 l2                   (coSumcheck_MPI.cpp:199)
+ *   form 1 cubic (v1, v2, v3): sum l1 l2 l3                (Distributed_Sumcheck.cpp:1144-1151)
+ *   form 2 batch (v1, v2, v3, v4, r1, r2; b):
+ *          sum l1 l2 + l3 l4 + b sum lr1 lr2               (coSumcheck_MPI.cpp:156-176)
+ *   form 3 zero-check (v1, v2, v3, beta, r1, r2; b):
+ *          sum (l1 l2 + b lr1 lr2 - x l3) lbeta            (coSumcheck_MPI.cpp:12-32) */
+int orc_sumcheck_form_vectors(int form);
+int orc_sumcheck_form_degree(int form);
+void orc_sumcheck_round(int form, const uint64_t *const *v, int64_t m, const uint64_t b[2], uint64_t *out);
+/* v[j] = v[2j] + r (v[2j+1] - v[2j]) for j < m/2, every vector, in place. */
+void orc_sumcheck_fold_many(int nvec, uint64_t *const *v, int64_t m, const uint64_t r[2]);
+/* _quadratic_sumcheck (form 0) / _cubic_sumcheck (form 1) of
+ * Distributed_Sumcheck.cpp for N parties in one process (see the .c file). */
+void orc_party_sumcheck(int form, uint64_t *v1, uint64_t *v2, uint64_t *v3, int64_t M, int N, const uint64_t *w,
+                        int offset, uint64_t fs[2], orc_prng *g, uint64_t y_io[2], uint64_t *polys,
+                        uint64_t *chal, uint64_t *fin);
+
 /* SplitMix64 witness generator shared by tests and bench. */
 void orc_witness(uint64_t seed, int64_t n, uint64_t *out);
 

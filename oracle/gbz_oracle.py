@@ -311,3 +311,56 @@ def cophase2(v, L):
     out = fe_array(v.shape[0] // L.shape[0])
     lib().orc_cophase2(_p64(v), ctypes.c_int64(v.shape[0]), _p64(L), ctypes.c_int(logd), _p64(out))
     return out
+
+
+FORM_VECTORS = {0: 2, 1: 3, 2: 6, 3: 6}
+FORM_DEGREE = {0: 2, 1: 3, 2: 2, 3: 3}
+
+
+def sumcheck_round(form, vecs, b=None):
+    """Round message of a sumcheck form over the pairs of vecs (see gbz_oracle.h)."""
+    vs = [np.ascontiguousarray(v, dtype=np.uint64).reshape(-1, 2) for v in vecs]
+    assert len(vs) == FORM_VECTORS[form]
+    arr = (ctypes.c_void_p * len(vs))(*[v.ctypes.data for v in vs])
+    out = fe_array(FORM_DEGREE[form] + 1)
+    bb = None if b is None else np.ascontiguousarray(b, dtype=np.uint64).reshape(2)
+    lib().orc_sumcheck_round(ctypes.c_int(form), arr, ctypes.c_int64(vs[0].shape[0]),
+                             None if bb is None else _p64(bb), _p64(out))
+    return out
+
+
+def sumcheck_fold_many(vecs, r):
+    """Folded copies (first halves) of every vector."""
+    vs = [np.array(np.asarray(v, dtype=np.uint64).reshape(-1, 2), copy=True) for v in vecs]
+    arr = (ctypes.c_void_p * len(vs))(*[v.ctypes.data for v in vs])
+    rr = np.ascontiguousarray(r, dtype=np.uint64).reshape(2)
+    lib().orc_sumcheck_fold_many(ctypes.c_int(len(vs)), arr, ctypes.c_int64(vs[0].shape[0]), _p64(rr))
+    return [v[: v.shape[0] // 2].copy() for v in vs]
+
+
+def party_sumcheck(form, vecs, N, w=None, offset=4, fs=(0, 0), prng_seed=1, y=None):
+    """_quadratic_sumcheck (form 0) / _cubic_sumcheck (form 1) of N parties
+    (vectors of N*M entries, party-major).  Returns a dict with y (final
+    claim), polys, challenges, fin (leader's v[0] values) and fs (chain)."""
+    nv = FORM_VECTORS[form]
+    vs = [np.array(np.asarray(v, dtype=np.uint64).reshape(-1, 2), copy=True) for v in vecs]
+    assert len(vs) == nv
+    M = vs[0].shape[0] // N
+    lm = M.bit_length() - 1
+    rounds = max(lm - offset, 0)
+    S = (1 << offset) if rounds > 0 else M
+    nchal = rounds + (S * N).bit_length() - 1
+    nc = FORM_DEGREE[form] + 1
+    polys = fe_array(nc * max(nchal, 1))
+    chal = fe_array(max(nchal, 1))
+    fin = fe_array(nv)
+    w = np.ascontiguousarray(w if w is not None else np.tile([1, 0], (N, 1)), dtype=np.uint64).reshape(-1, 2)
+    fsa = np.ascontiguousarray(fs, dtype=np.uint64).reshape(2).copy()
+    ya = np.ascontiguousarray(y if y is not None else [0, 0], dtype=np.uint64).reshape(2).copy()
+    g = Prng(prng_seed)
+    v3 = vs[2] if nv == 3 else None
+    lib().orc_party_sumcheck(ctypes.c_int(form), _p64(vs[0]), _p64(vs[1]), None if v3 is None else _p64(v3),
+                             ctypes.c_int64(M), ctypes.c_int(N), _p64(w), ctypes.c_int(offset), _p64(fsa),
+                             ctypes.byref(g.s), _p64(ya), _p64(polys), _p64(chal), _p64(fin))
+    return {"y": ya, "polys": polys[: nc * nchal].reshape(nchal, nc, 2), "challenges": chal[:nchal], "fin": fin,
+            "fs": fsa, "prng": g}

@@ -16,6 +16,11 @@
 //   ref_full aggr <N> <len> <seed>                       sumcheck_aggr leader path (MPI_utils.cpp:2629-2644)
 //   ref_full cophase1 <logn> <logd> <seed>               local part of quadratic/cubic phase 1 (coSumcheck.cpp:9-64,150-198)
 //   ref_full cophase2 <logn> <logd> <seed>               quadratic/cubic phase 2 (coSumcheck.cpp:66-148, 201-213)
+//   ref_full zcround <logm> <iter> <seed>                _zero_check_sumcheck_phase1/2 (coSumcheck_MPI.cpp:12-44)
+//   ref_full bround <logm> <iter> <seed>                 _quadratic_batch_sumcheck_phase1/2 (coSumcheck_MPI.cpp:156-187)
+//   ref_full cubicsc <logM> <offset> <seed> <prng>       _cubic_sumcheck, one party (Distributed_Sumcheck.cpp:1122)
+//   ref_full quadsc <logM> <offset> <seed> <prng>        _quadratic_sumcheck, one party (Distributed_Sumcheck.cpp:204)
+#include "Distributed_Sumcheck.h"
 #include "coPCS.h"
 #include "coPCS_utils.h"
 #include "coSumcheck.h"
@@ -34,6 +39,15 @@ extern unsigned int rate_offset;  // coPCS.cpp:22
 void Encode(vector<vector<F>> &Codeword, int N, vector<int> rate);
 void quadratic_coSumcheck_phase2(vector<F> &p1, vector<F> &p2, vector<F> L, int d);
 void cubic_coSumcheck_phase2(vector<F> &p1, vector<F> &p2, vector<F> &p3, vector<F> &b1, vector<F> L, int d);
+cubic_poly _zero_check_sumcheck_phase1(int iter, F b, vector<F> &v1, vector<F> &v2, vector<F> &v3, vector<F> &beta1,
+                                       vector<F> &r1, vector<F> &r2);
+void _zero_check_sumcheck_phase2(int iter, F r, vector<F> &v1, vector<F> &v2, vector<F> &v3, vector<F> &beta1,
+                                 vector<F> &r1, vector<F> &r2);
+quadratic_poly _quadratic_batch_sumcheck_phase1(int iter, F b, vector<F> &v1, vector<F> &v2, vector<F> &v3,
+                                                vector<F> &v4, vector<F> &r1, vector<F> &r2);
+void _quadratic_batch_sumcheck_phase2(int iter, F r, vector<F> &v1, vector<F> &v2, vector<F> &v3, vector<F> &v4,
+                                      vector<F> &r1, vector<F> &r2);
+extern int sumcheck_offset;  // main.cpp:36
 void compute_secret_shares(vector<F> &v, vector<vector<F>> &v_shares, int N, int k, int _k, bool privacy_preserving);
 vector<F> unpack_secret_share(vector<F> &secret, int _k, int k);
 
@@ -60,11 +74,60 @@ struct SplitMix {
 static void put(const void *p, size_t n) { fwrite(p, 1, n, stdout); }
 static void putFs(const vector<F> &v) { for (auto &x : v) { put(&x.real, 8); put(&x.img, 8); } }
 
+static void put_prefix(const vector<F> &v, size_t n) {
+  for (size_t i = 0; i < n; i++) { put(&v[i].real, 8); put(&v[i].img, 8); }
+}
+
 int main(int argc, char **argv) {
   if (argc < 2) return 1;
   std::string c = argv[1];
   auto I = [&](int k) { return atoi(argv[k]); };
   auto U = [&](int k) { return (uint64_t)strtoull(argv[k], nullptr, 0); };
+  if (c == "zcround" || c == "bround") {
+    // inputs: six vectors of 2^logm, then b and r; output: the round
+    // polynomial at iteration iter and the first m / 2^(iter+1) entries of
+    // every vector after the phase-2 fold by r.
+    int logm = I(2), iter = I(3);
+    SplitMix g(U(4));
+    vector<vector<F>> v(6);
+    for (auto &x : v) x = g.vec(1u << logm);
+    F b = g.ext(), r = g.ext();
+    size_t half = (1u << logm) >> (iter + 1);
+    if (c == "zcround") {
+      cubic_poly H = _zero_check_sumcheck_phase1(iter, b, v[0], v[1], v[2], v[3], v[4], v[5]);
+      putFs({H.a, H.b, H.c, H.d});
+      _zero_check_sumcheck_phase2(iter, r, v[0], v[1], v[2], v[3], v[4], v[5]);
+    } else {
+      quadratic_poly H = _quadratic_batch_sumcheck_phase1(iter, b, v[0], v[1], v[2], v[3], v[4], v[5]);
+      putFs({H.a, H.b, H.c});
+      _quadratic_batch_sumcheck_phase2(iter, r, v[0], v[1], v[2], v[3], v[4], v[5]);
+    }
+    for (auto &x : v) put_prefix(x, half);
+    return 0;
+  }
+  if (c == "cubicsc" || c == "quadsc") {
+    // One party (N = 1, the MPI stub's single rank): inputs v1, v2 (, v3)
+    // of 2^logM and the party weight w from the seed; y is the true sum.
+    // Output: y, the reply values, the number of challenges, the challenges.
+    int logM = I(2);
+    sumcheck_offset = I(3);
+    SplitMix g(U(4));
+    srandom((unsigned)U(5));
+    size_t M = 1u << logM;
+    bool cubic = c == "cubicsc";
+    vector<F> v1 = g.vec(M), v2 = g.vec(M), v3 = cubic ? g.vec(M) : vector<F>();
+    vector<F> w = {g.ext()};
+    F y = F(0);
+    for (size_t i = 0; i < M; i++) y = y + (cubic ? v1[i] * v2[i] * v3[i] : v1[i] * v2[i]);
+    if (cubic) y = y * w[0];
+    putFs({y});
+    vector<std::pair<F, vector<F>>> res = cubic ? _cubic_sumcheck(y, v1, v2, v3, w, 1) : _quadratic_sumcheck(y, v1, v2, 1);
+    for (auto &pr : res) putFs({pr.first});
+    uint32_t nr = (uint32_t)res[0].second.size();
+    put(&nr, 4);
+    putFs(res[0].second);
+    return 0;
+  }
   if (c == "multifold5") {
     int logn = I(2), logd = I(3);
     SplitMix g(U(4));

@@ -6,7 +6,7 @@ oracle/ref/Makefile; x86-64 only) and stores either the full output (small
 cases) or the SHA-256 of the exact output bytes (large cases) together with
 the parameters that regenerate the inputs.  Run from the repository root:
 
-    make -C oracle/ref && python tests/golden/make_golden.py
+    make -C oracle/ref && python tests/golden/make_golden.py [section ...]
 
 The fixtures are what pins the CPU restatement in oracle/gbz_oracle.c; the
 GPU tests are then checked against that restatement and these fixtures.
@@ -47,6 +47,19 @@ def save(name, data):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -C oracle/ref")
+    # `make_golden.py copcs sumcheck` regenerates only those sections
+    only = set(sys.argv[1:])
+    if only:
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest = json.load(f)
+        if "copcs" in only:
+            manifest["copcs"] = gen_copcs()
+        if "sumcheck" in only:
+            manifest["sumcheck"] = gen_sumcheck()
+        with open(os.path.join(HERE, "manifest.json"), "w") as f:
+            json.dump(manifest, f, indent=1)
+        print("updated", sorted(only))
+        return
     manifest = {"generator": "tests/golden/make_golden.py", "driver": "oracle/ref/ref_driver.cpp"}
 
     data, _ = run("field", 200, 11)
@@ -120,7 +133,31 @@ def main():
         print(f"prove 2^{logn} rate {rate}: {len(data)} B in {dt:.2f} s", flush=True)
     manifest["prove"] = proofs
 
-    # coPCS side (ref_full links every reference translation unit but main.cpp)
+    manifest["copcs"] = gen_copcs()
+    manifest["sumcheck"] = gen_sumcheck()
+
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+    print("wrote", os.path.join(HERE, "manifest.json"))
+
+
+def gen_sumcheck():
+    """Sumcheck round forms and one-party distributed sumchecks (ref_full)."""
+    out = {}
+    for name, args in [
+        ("zcround_6_0", ("zcround", 6, 0, 71)), ("zcround_8_2", ("zcround", 8, 2, 72)),
+        ("bround_6_0", ("bround", 6, 0, 73)), ("bround_7_1", ("bround", 7, 1, 74)),
+        ("cubicsc_8_4", ("cubicsc", 8, 4, 75, 1)), ("cubicsc_10_3", ("cubicsc", 10, 3, 76, 9)),
+        ("cubicsc_3_4", ("cubicsc", 3, 4, 77, 1)), ("quadsc_8_4", ("quadsc", 8, 4, 78, 1)),
+        ("quadsc_11_2", ("quadsc", 11, 2, 79, 5)),
+    ]:
+        save(name + ".bin", run_full(*args))
+        out[name] = {"file": name + ".bin", "args": list(args)}
+    return out
+
+
+def gen_copcs():
+    """coPCS side (ref_full links every reference translation unit but main.cpp)."""
     copcs = {}
     for name, args in [
         ("multifold5_10_2", ("multifold5", 10, 2, 51)), ("multifold5_12_3", ("multifold5", 12, 3, 52)),
@@ -137,11 +174,7 @@ def main():
         data = run_full(*args)
         save(name + ".bin", data)
         copcs[name] = {"file": name + ".bin", "args": list(args)}
-    manifest["copcs"] = copcs
-
-    with open(os.path.join(HERE, "manifest.json"), "w") as f:
-        json.dump(manifest, f, indent=1)
-    print("wrote", os.path.join(HERE, "manifest.json"))
+    return copcs
 
 
 if __name__ == "__main__":
