@@ -17,6 +17,14 @@ Prints one JSON line:
                launching stream during a second timed pass
   cpu_baseline the oracle port (oracle/gbz_oracle.c) proving the same
                workload once on the host cores
+  batched      configuration 3 (64 proofs, 2^12..2^20, rate 1/4) through
+               gbz_prove_batch (8 slots, graph replay) beside the plain
+               prover (one synchronised gbz_prove per proof), same pinned
+               host buffers, transcripts compared byte for byte
+  served       configuration 5 (400 Poisson arrivals at 200/s, 2^14..2^22,
+               rate 1/2 or 1/4) through gbz_serve: proofs/s, p50/p99
+               latency, beside the plain prover on the same arrivals; and
+               both at saturation (every request at t = 0)
   --impl reference: the reference arm.  The reference's CPU prover does not
                build on the Arm GPU host (x86-64 inline asm in
                fieldElement.cpp), so this arm times the oracle port, which is
@@ -46,7 +54,7 @@ sys.path.insert(0, ORACLE)
 
 LOGN, RATE = 24, 2
 SEED = 0x5EED0000 + 2 * 65536  # configuration 2, instance 0
-METRIC = "proofs/s (plain single-party prover: 2^24 witness, RS rate 1/2, Blake3 Merkle, sumcheck, WHIR k=4)"
+METRIC = "proofs/s and p50/p99 latency, batched+served vs plain GPU prover, bit-exact"
 CONFIG = {
     "workload": "plain prover, n=2^24 uniform base-field witness, rate 1/2 (NTT 2^25), Blake3 Merkle over "
                 "2^23 leaves of 4 elements, FS sumcheck (24 rounds), WHIR folding 4 (11 iterations)",
@@ -192,6 +200,94 @@ def run_reference_arm(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def c3_jobs():
+    """Configuration 3: 64 witnesses, log2 n uniform in [12, 20], rate 1/4."""
+    rng = np.random.default_rng(0x5EEF3)
+    return [int(x) for x in rng.integers(12, 21, size=64)], [4] * 64
+
+
+def c5_requests(n_req, lam, seed=0x5EEF5):
+    """Configuration 5: Poisson arrivals (rate lam per second), log2 n uniform
+    in [14, 22], rate 1/2 or 1/4."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n_req))
+    arrivals -= arrivals[0]
+    logns = [int(x) for x in rng.integers(14, 23, size=n_req)]
+    rates = [int(x) for x in rng.choice([2, 4], size=n_req)]
+    return arrivals, logns, rates
+
+
+def run_many(gbz, O, ctx, repeats):
+    """Batched (C3) and served (C5) proving against the plain prover (one
+    gbz_prove call per proof, synchronised) on the same jobs, pinned host
+    buffers, transcripts compared byte for byte."""
+    out = {}
+    pinned = {}
+
+    def witness(logn, cfg):
+        key = (logn, cfg)
+        if key not in pinned:
+            p = gbz.PinnedArray((1 << logn, 2), np.uint64)
+            p.array[...] = O.witness(0x5EED0000 + cfg * 65536 + logn, 1 << logn)
+            pinned[key] = p
+        return pinned[key].array
+
+    def transcripts(logns, rates):
+        bufs = [gbz.PinnedArray((gbz.transcript_bytes(l, r),), np.uint8) for l, r in zip(logns, rates)]
+        return bufs, [b.array for b in bufs]
+
+    # ---- C3: batch
+    logns, rates = c3_jobs()
+    ws = [witness(l, 3) for l in logns]
+    seeds = list(range(1, len(logns) + 1))
+    keep, tb = transcripts(logns, rates)
+    for w, l, r, s, t in zip(ws, logns, rates, seeds, tb):
+        ctx.prove(w, l, r, s, out=t)
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        for w, l, r, s, t in zip(ws, logns, rates, seeds, tb):
+            ctx.prove(w, l, r, s, out=t)
+    plain = len(ws) * repeats / (time.perf_counter() - t0)
+    ref = [t.tobytes() for t in tb]
+    keep2, tb2 = transcripts(logns, rates)
+    ctx.prove_batch(ws, logns, rates, seeds, lanes=8, out=tb2)
+    mks = []
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        _, lat, mk = ctx.prove_batch(ws, logns, rates, seeds, lanes=8, out=tb2)
+        mks.append(mk)
+    batched = len(ws) * repeats / (time.perf_counter() - t0)
+    out["batched"] = {
+        "workload": "64 proofs, n = 2^12..2^20 log-uniform, rate 1/4 (configuration 3)",
+        "proofs_per_s": batched, "plain_proofs_per_s": plain, "speedup_vs_plain": batched / plain,
+        "device_makespan_ms": 1e3 * min(mks), "slots": 8, "graphs": True,
+        "bit_identical_to_plain": [t.tobytes() for t in tb2] == ref,
+    }
+    # ---- C5: serving at 200 requests/s, and at saturation (all at once)
+    arrivals, slog, srate = c5_requests(400, 200.0)
+    sws = [witness(l, 5) for l in slog]
+    sseeds = list(range(1, len(slog) + 1))
+    keep3, st3 = transcripts(slog, srate)
+    ctx.prove_batch(sws, slog, srate, sseeds, lanes=8, out=st3)  # warm plans and graphs
+    served = {}
+    for name, arr, kw in [("served", arrivals, dict(lanes=8, depth=2)),
+                          ("plain", arrivals, dict(lanes=1, depth=1, graphs=False)),
+                          ("served_saturated", np.zeros(len(slog)), dict(lanes=8, depth=2)),
+                          ("plain_saturated", np.zeros(len(slog)), dict(lanes=1, depth=1, graphs=False))]:
+        _, lat, mk = ctx.serve(arr, sws, slog, srate, sseeds, out=st3, **kw)
+        served[name] = {"proofs_per_s": len(slog) / mk, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                        "p99_ms": 1e3 * float(np.percentile(lat, 99))}
+    sref = []
+    for w, l, r, s in zip(sws[:32], slog[:32], srate[:32], sseeds[:32]):
+        sref.append(ctx.prove(w, l, r, s).tobytes())
+    out["served"] = {
+        "workload": "400 requests, Poisson 200/s, n = 2^14..2^22 log-uniform, rate 1/2 or 1/4 (configuration 5)",
+        "slots": 8, "depth": 2, **served,
+        "bit_identical_to_alone": [t.tobytes() for t in st3[:32]] == sref,
+    }
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -200,6 +296,7 @@ def main():
     ap.add_argument("--impl", default="gbz", choices=["gbz", "reference"])
     ap.add_argument("--logn", type=int, default=LOGN)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-many", action="store_true", help="skip the batched and served measurements")
     args = ap.parse_args()
     ws, rank, local = dist_info()
     if ws > 1:
@@ -338,6 +435,8 @@ def main():
         "clocks": clk.summary(),
         "transcript_bytes": tbytes,
     }
+    if rank == 0 and not args.no_many:
+        line.update(run_many(gbz, O, ctx, repeats=3))
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         t0 = time.perf_counter()

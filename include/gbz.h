@@ -281,6 +281,55 @@ void gbz_prng_field(gbz_prng *g, uint64_t *out);
 void gbz_field_ops_host(const uint64_t *a, const uint64_t *b, uint64_t n, uint64_t *sum, uint64_t *diff,
                         uint64_t *prod);
 
+/* ------------------------------------------------- sumcheck round forms */
+
+/* Round forms of the multilinear sumcheck provers.  Over the pairs
+ * (v[2j], v[2j+1]) with lines l(x) = (v[2j+1] - v[2j]) x + v[2j], the round
+ * polynomial (coefficients highest degree first) is */
+#define GBZ_SC_QUADRATIC 0 /* (v1, v2): sum l1 l2, 3 coefficients (coSumcheck_MPI.cpp:199) */
+#define GBZ_SC_CUBIC 1     /* (v1, v2, v3): sum l1 l2 l3, 4 (Distributed_Sumcheck.cpp:1144-1151) */
+#define GBZ_SC_BATCH 2     /* (v1, v2, v3, v4, r1, r2; b): sum l1 l2 + l3 l4 + b lr1 lr2, 3
+                              (_quadratic_batch_sumcheck_phase1, coSumcheck_MPI.cpp:156-176) */
+#define GBZ_SC_ZEROCHECK 3 /* (v1, v2, v3, beta1, r1, r2; b): sum (l1 l2 + b lr1 lr2 - x l3) lbeta1, 4
+                              (_zero_check_sumcheck_phase1, coSumcheck_MPI.cpp:12-32) */
+
+/* One round of a form over vectors v[0..k) of m entries (m a power of two).
+ * r == NULL: coeffs = the round polynomial of v (the reference's phase 1).
+ * r != NULL (2 words, host): every vector is first folded in place by r,
+ * v[j] = v[2j] + r (v[2j+1] - v[2j]) for j < m/2 (phase 2,
+ * coSumcheck_MPI.cpp:34-44, 178-187), and coeffs is the round polynomial
+ * of the folded vectors.  b (2 words, host) is required by the batch and
+ * zero-check forms.  coeffs (host) receives 3 or 4 elements. */
+gbz_status gbz_sumcheck_round(gbz_ctx *ctx, int form, uint64_t *const *v, uint64_t m, const uint64_t *b,
+                              const uint64_t *r, uint64_t *coeffs, int mem);
+
+/* Rounds of gbz_party_sumcheck: max(log2 M - offset, 0) Fiat-Shamir rounds
+ * plus log2(N 2^offset') leader rounds (offset' = log2 M when the first
+ * count is not positive). */
+int gbz_party_sumcheck_rounds(uint64_t M, int N, int offset);
+
+/* The distributed sumcheck of N parties held on this device:
+ * form GBZ_SC_QUADRATIC replaces _quadratic_sumcheck
+ * (Distributed_Sumcheck.cpp:204-349), form GBZ_SC_CUBIC _cubic_sumcheck
+ * (:1122-1269).  Party p owns entries [p M, (p+1) M) of v1, v2 (, v3), all
+ * read only.  The parties' round polynomials are combined as aggregate_poly
+ * does (a sum; for the cubic form weighted by w[p], N elements, host, NULL
+ * for ones), the first rounds draw hash_to_field of the coefficients from
+ * the chain fs_state (2 words, in/out: prev_challenge), and the leader's
+ * rounds over the gathered N 2^offset entries (cubic: v3 scaled by w[p])
+ * take the fourth F::_random() draw of each round from *prng (in/out).
+ * y (2 words, in/out) is the claim; every round is checked against it and
+ * GBZ_ECHECK is returned if one does not match (outputs are still written).
+ * Outputs (host): polys (3 or 4 per round), challenges (one per round), fin
+ * (the leader's final v1[0], v2[0] (, v3[0])).  For the quadratic form the
+ * reference's leader reads zeros for the other parties' v2 entries when
+ * N > 1 (its receive buffers are N times too long, :289-306) and its
+ * consistency check then exits; here the parties' entries are gathered as
+ * intended, so reference parity is defined for N = 1. */
+gbz_status gbz_party_sumcheck(gbz_ctx *ctx, int form, const uint64_t *v1, const uint64_t *v2, const uint64_t *v3,
+                              uint64_t M, int N, const uint64_t *w, int offset, uint64_t *fs_state, gbz_prng *prng,
+                              uint64_t *y, uint64_t *polys, uint64_t *challenges, uint64_t *fin, int mem);
+
 /* --------------------------------------------------------------- prover */
 
 /* Bytes of the transcript of one proof of a 2^logn witness at `rate`. */

@@ -1,5 +1,6 @@
 // extern "C" entry points of libgbz (declared in include/gbz.h).
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <new>
@@ -9,6 +10,7 @@
 #include "../../include/gbz.h"
 #include "gbz_copcs.cuh"
 #include "gbz_prover.cuh"
+#include "gbz_rounds.cuh"
 #include "gbz_sched.cuh"
 
 using namespace gbz;
@@ -787,6 +789,128 @@ gbz_status gbz_sched_release(gbz_ctx *ctx, uint64_t *cached_bytes) {
   API_BEGIN(ctx)
   if (cached_bytes) *cached_bytes = ctx->sched ? ctx->sched->cached_bytes() : 0;
   ctx->sched.reset();
+  API_END(ctx)
+}
+
+gbz_status gbz_sumcheck_round(gbz_ctx *ctx, int form, uint64_t *const *v, uint64_t m, const uint64_t *b,
+                              const uint64_t *r, uint64_t *coeffs, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  const int nv = form_vectors(form), nc = form_coeffs(form);
+  if (!nv) throw ArgError("sumcheck round: unknown form");
+  need(v, "v");
+  need(coeffs, "coeffs");
+  if ((form == SC_BATCH || form == SC_ZEROCHECK) && !b) throw ArgError("sumcheck round: this form needs b");
+  check_pow2(m, "sumcheck round: m");
+  if (m < 2) throw ArgError("sumcheck round: m must be at least 2");
+  RoundArgs a{};
+  fe *scal = (fe *)ctx->buf(50, 16 * 2);
+  fe hb[2] = {b ? fe_make(b[0], b[1]) : fe_zero(), r ? fe_make(r[0], r[1]) : fe_zero()};
+  GBZ_CUDA(cudaMemcpyAsync(scal, hb, sizeof(hb), cudaMemcpyHostToDevice, ctx->stream));
+  a.b = b ? scal : nullptr;
+  a.r = scal + 1;
+  fe *dv[6];
+  for (int k = 0; k < nv; k++) {
+    need(v[k], "v[k]");
+    dv[k] = dev_view(ctx, 40 + k, (fe *)v[k], 16 * m, mem, true);
+    a.in[k] = dv[k];
+  }
+  fe *dout = (fe *)ctx->buf(57, 16 * 4);
+  GBZ_CUDA(cudaMemsetAsync(dout, 0, 16 * 4, ctx->stream));
+  if (r) {
+    const uint64_t half = m / 2;
+    for (int k = 0; k < nv; k++) a.out[k] = (fe *)ctx->buf(60 + k, 16 * half);
+    if (m >= 4) {
+      a.pairs = m / 4;
+      const int blocks = round_blocks(a.pairs);
+      a.partial = (fe *)ctx->buf(56, 16 * 4 * (uint64_t)blocks);
+      form_step_launch(form, a, 1, blocks, ctx->stream);
+      form_sum_launch(a.partial, blocks, nc, dout, ctx->stream);
+    } else {
+      a.pairs = 1;  // the folded vectors have one entry: no pair, zero message
+      form_step_launch(form, a, 2, 1, ctx->stream);
+    }
+    for (int k = 0; k < nv; k++)
+      GBZ_CUDA(cudaMemcpyAsync(v[k], a.out[k], 16 * half,
+                               mem == GBZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    a.pairs = m / 2;
+    const int blocks = round_blocks(a.pairs);
+    a.partial = (fe *)ctx->buf(56, 16 * 4 * (uint64_t)blocks);
+    form_step_launch(form, a, 0, blocks, ctx->stream);
+    form_sum_launch(a.partial, blocks, nc, dout, ctx->stream);
+  }
+  GBZ_CUDA(cudaMemcpyAsync(coeffs, dout, 16 * nc, cudaMemcpyDeviceToHost, ctx->stream));
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+int gbz_party_sumcheck_rounds(uint64_t M, int N, int offset) {
+  if (!is_pow2(M) || N < 1 || !is_pow2((uint64_t)N) || offset < 0) return -1;
+  return party_sumcheck_rounds(M, N, offset, nullptr);
+}
+
+gbz_status gbz_party_sumcheck(gbz_ctx *ctx, int form, const uint64_t *v1, const uint64_t *v2, const uint64_t *v3,
+                              uint64_t M, int N, const uint64_t *w, int offset, uint64_t *fs_state, gbz_prng *prng,
+                              uint64_t *y, uint64_t *polys, uint64_t *challenges, uint64_t *fin, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  if (form != SC_QUADRATIC && form != SC_CUBIC) throw ArgError("party sumcheck: form must be quadratic or cubic");
+  const int nv = form_vectors(form), nc = form_coeffs(form);
+  need(v1, "v1");
+  need(v2, "v2");
+  if (form == SC_CUBIC) need(v3, "v3");
+  need(fs_state, "fs_state");
+  need(prng, "prng");
+  need(y, "y");
+  need(polys, "polys");
+  need(challenges, "challenges");
+  need(fin, "fin");
+  check_pow2(M, "party sumcheck: M");
+  if (N < 1 || N > 4096 || !is_pow2((uint64_t)N)) throw ArgError("party sumcheck: N must be a power of two in [1, 4096]");
+  if (offset < 0 || offset > 40) throw ArgError("party sumcheck: offset out of range");
+  const uint64_t total = M * (uint64_t)N;
+  if (ilog2(total) > kMaxLogN) throw ArgError("party sumcheck: N * M above 2^28");
+  const int rounds = party_sumcheck_rounds(M, N, offset, nullptr);
+  const fe *src[3] = {(const fe *)v1, (const fe *)v2, (const fe *)v3};
+  const fe *dv[3] = {nullptr, nullptr, nullptr};
+  for (int k = 0; k < nv; k++) dv[k] = dev_view(ctx, 40 + k, src[k], 16 * total, mem, true);
+  fe *dw = nullptr;
+  if (form == SC_CUBIC) {
+    std::vector<fe> hw(N, fe_one());
+    if (w)
+      for (int p = 0; p < N; p++) hw[p] = fe_make(w[2 * p], w[2 * p + 1]);
+    dw = (fe *)ctx->buf(43, 16 * (uint64_t)N);
+    GBZ_CUDA(cudaMemcpyAsync(dw, hw.data(), 16 * (uint64_t)N, cudaMemcpyHostToDevice, ctx->stream));
+    GBZ_CUDA(cudaStreamSynchronize(ctx->stream));  // hw is a host temporary
+  }
+  RoundState hs;
+  hs.fs = fe_make(fs_state[0], fs_state[1]);
+  std::memcpy(&hs.prng, prng, sizeof(glibc_prng));
+  hs.y = fe_make(y[0], y[1]);
+  hs.error = 0;
+  RoundState *dst = (RoundState *)ctx->buf(44, sizeof(RoundState));
+  GBZ_CUDA(cudaMemcpyAsync(dst, &hs, sizeof(hs), cudaMemcpyHostToDevice, ctx->stream));
+  fe *scratch[12];
+  for (int k = 0; k < 12; k++) scratch[k] = (fe *)ctx->buf(60 + k, 16 * std::max<uint64_t>(total / 2, 1));
+  fe *partial = (fe *)ctx->buf(56, 16 * 4 * (uint64_t)round_blocks(std::max<uint64_t>(total / 2, 1)));
+  fe *dpolys = (fe *)ctx->buf(45, 16 * (uint64_t)nc * std::max(rounds, 1));
+  fe *dchal = (fe *)ctx->buf(46, 16 * (uint64_t)std::max(rounds, 1));
+  fe *dfin = (fe *)ctx->buf(47, 16 * 3);
+  party_sumcheck_enqueue(form, dv, M, N, dw, offset, dst, scratch, partial, dpolys, dchal, dfin, ctx->stream);
+  if (rounds) {
+    GBZ_CUDA(cudaMemcpyAsync(polys, dpolys, 16 * (uint64_t)nc * rounds, cudaMemcpyDeviceToHost, ctx->stream));
+    GBZ_CUDA(cudaMemcpyAsync(challenges, dchal, 16 * (uint64_t)rounds, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  GBZ_CUDA(cudaMemcpyAsync(fin, dfin, 16 * (uint64_t)nv, cudaMemcpyDeviceToHost, ctx->stream));
+  GBZ_CUDA(cudaMemcpyAsync(&hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  fs_state[0] = hs.fs.re;
+  fs_state[1] = hs.fs.im;
+  std::memcpy(prng, &hs.prng, sizeof(glibc_prng));
+  y[0] = hs.y.re;
+  y[1] = hs.y.im;
+  if (hs.error) return fail(ctx, GBZ_ECHECK, "party sumcheck: a round polynomial did not match the running claim");
   API_END(ctx)
 }
 

@@ -42,9 +42,15 @@ EXPORTS = (
     "gbz_profile_read", "gbz_whir_update_betas_noalloc", "gbz_rs_multifold5", "gbz_lagrange_coeff",
     "gbz_encode_rows", "gbz_column_merkle", "gbz_secret_shares", "gbz_party_aggregate",
     "gbz_cosumcheck_phase1", "gbz_cosumcheck_phase2", "gbz_prove_batch", "gbz_serve", "gbz_sched_release",
+    "gbz_sumcheck_round", "gbz_party_sumcheck_rounds", "gbz_party_sumcheck",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
+
+
+SC_QUADRATIC, SC_CUBIC, SC_BATCH, SC_ZEROCHECK = range(4)
+FORM_VECTORS = {SC_QUADRATIC: 2, SC_CUBIC: 3, SC_BATCH: 6, SC_ZEROCHECK: 6}
+FORM_DEGREE = {SC_QUADRATIC: 2, SC_CUBIC: 3, SC_BATCH: 2, SC_ZEROCHECK: 3}
 
 
 class SchedOpts(ctypes.Structure):
@@ -129,6 +135,9 @@ def _load():
         "gbz_prove_batch": (c_int, [vp, c_int, vp, vp, vp, vp, vp, vp, c_int, vp, vp, vp]),
         "gbz_serve": (c_int, [vp, c_int, vp, vp, vp, vp, vp, vp, vp, c_int, vp, vp, vp]),
         "gbz_sched_release": (c_int, [vp, vp]),
+        "gbz_sumcheck_round": (c_int, [vp, c_int, vp, u64, vp, vp, vp, c_int]),
+        "gbz_party_sumcheck_rounds": (c_int, [u64, c_int, c_int]),
+        "gbz_party_sumcheck": (c_int, [vp, c_int, vp, vp, vp, u64, c_int, vp, c_int, vp, vp, vp, vp, vp, vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -295,6 +304,52 @@ class Context:
         self.check(lib.gbz_whir_update_betas(self.h, _ptr(b), b.shape[0], _ptr(q), len(q), n, _ptr(r),
                                              _ptr(ch), MEM_HOST))
         return b, ch
+
+    # ------------------------------------------------- sumcheck round forms
+    def sumcheck_round(self, form, vecs, b=None, r=None):
+        """Round polynomial of a form (SC_*); with r the vectors (numpy,
+        C-contiguous uint64 (m, 2), or CUDA tensors) are first folded in
+        place to their first halves."""
+        nv = FORM_VECTORS[form]
+        assert len(vecs) == nv
+        vs = [_fe(v) for v in vecs]
+        m = vs[0].shape[0]
+        for v in vs:
+            if isinstance(v, np.ndarray):
+                assert v.flags.c_contiguous and v.dtype == np.uint64
+        arr = (ctypes.c_void_p * nv)(*[_ptr(v) for v in vs])
+        bb = None if b is None else np.ascontiguousarray(b, dtype=np.uint64).reshape(2)
+        rr = None if r is None else np.ascontiguousarray(r, dtype=np.uint64).reshape(2)
+        out = fe_array(FORM_DEGREE[form] + 1)
+        self.check(lib.gbz_sumcheck_round(self.h, form, ctypes.cast(arr, ctypes.c_void_p), m, _ptr(bb), _ptr(rr),
+                                          _ptr(out), _mem(vs[0])))
+        return out
+
+    def party_sumcheck(self, form, vecs, N, w=None, offset=4, fs=(0, 0), prng=None, y=(0, 0)):
+        """_quadratic_sumcheck / _cubic_sumcheck of N parties on this device
+        (vectors of N*M entries, party-major).  Returns a dict with polys,
+        challenges, fin, y, fs, prng."""
+        nv = FORM_VECTORS[form]
+        vs = [_fe(v) for v in vecs]
+        assert len(vs) == nv
+        M = vs[0].shape[0] // N
+        rounds = lib.gbz_party_sumcheck_rounds(M, N, offset)
+        if rounds < 0:
+            raise GbzError(EINVAL, "party sumcheck: bad shape")
+        nc = FORM_DEGREE[form] + 1
+        polys = fe_array(max(rounds, 1) * nc)
+        chal = fe_array(max(rounds, 1))
+        fin = fe_array(nv)
+        ww = None if w is None else np.ascontiguousarray(w, dtype=np.uint64).reshape(-1, 2)
+        fsa = np.ascontiguousarray(fs, dtype=np.uint64).reshape(2).copy()
+        ya = np.ascontiguousarray(y, dtype=np.uint64).reshape(2).copy()
+        g = prng if isinstance(prng, Prng) else Prng(1 if prng is None else prng)
+        v3 = vs[2] if nv == 3 else None
+        self.check(lib.gbz_party_sumcheck(self.h, form, _ptr(vs[0]), _ptr(vs[1]), _ptr(v3), M, N, _ptr(ww), offset,
+                                          _ptr(fsa), ctypes.addressof(g), _ptr(ya), _ptr(polys), _ptr(chal),
+                                          _ptr(fin), _mem(vs[0])))
+        return {"polys": polys[: rounds * nc].reshape(rounds, nc, 2), "challenges": chal[:rounds], "fin": fin,
+                "y": ya, "fs": fsa, "prng": g}
 
     # ------------------------------------------------------ many proofs
     def _prove_many(self, arrivals, witnesses, logns, rates, seeds, lanes, depth, graphs, reserve, out):

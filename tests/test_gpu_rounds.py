@@ -1,0 +1,146 @@
+"""GPU sumcheck round forms and the distributed (party) sumcheck against the
+oracle and the reference's fixtures; bit-identical results required."""
+import numpy as np
+import pytest
+
+from conftest import rand_fe, splitmix_ext
+from test_oracle_sumcheck import case, fadd, feval
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name,form", [("zcround_6_0", 3), ("zcround_8_2", 3), ("bround_6_0", 2),
+                                       ("bround_7_1", 2)])
+def test_round_forms_golden(ctx, golden, name, form):
+    r, (_, logm, it, seed) = case(golden, name)
+    m = 1 << logm
+    raw = splitmix_ext(seed, 6 * m + 2)
+    vecs = [raw[k * m:(k + 1) * m] for k in range(6)]
+    b, ch = raw[6 * m], raw[6 * m + 1]
+    H = r.fe(4 if form == 3 else 3)
+    half = m >> (it + 1)
+    folded = [r.fe(half) for _ in range(6)]
+    cur = [np.ascontiguousarray(v[: m >> it]) for v in vecs]
+    assert np.array_equal(ctx.sumcheck_round(form, cur, b), H)
+    # fold by r then the message of the folded vectors (= the next round's)
+    nxt = ctx.sumcheck_round(form, cur, b, ch)
+    for c, f in zip(cur, folded):
+        assert np.array_equal(c[:half], f)
+    if half >= 2:
+        import gbz_oracle
+        assert np.array_equal(nxt, gbz_oracle.sumcheck_round(form, [f for f in folded], b))
+
+
+@pytest.mark.parametrize("form", [0, 1, 2, 3])
+@pytest.mark.parametrize("logm", [1, 2, 5, 11, 16, 20])
+def test_round_forms_vs_oracle(ctx, oracle, form, logm):
+    rng = np.random.default_rng(1000 + 10 * form + logm)
+    nv = oracle.FORM_VECTORS[form]
+    m = 1 << logm
+    vecs = [rand_fe(rng, m) for _ in range(nv)]
+    b = rand_fe(rng, 1)[0]
+    r = rand_fe(rng, 1)[0]
+    bb = b if form >= 2 else None
+    assert np.array_equal(ctx.sumcheck_round(form, [v.copy() for v in vecs], bb), oracle.sumcheck_round(form, vecs, bb))
+    got = [v.copy() for v in vecs]
+    H = ctx.sumcheck_round(form, got, bb, r)
+    ref = oracle.sumcheck_fold_many(vecs, r)
+    for g, f in zip(got, ref):
+        assert np.array_equal(g[: m // 2], f)
+    if m >= 4:
+        assert np.array_equal(H, oracle.sumcheck_round(form, ref, bb))
+    else:
+        assert not np.any(H)
+
+
+def test_round_forms_device_tensors(ctx, oracle):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(77)
+    m = 1 << 14
+    vecs = [rand_fe(rng, m) for _ in range(6)]
+    b, r = rand_fe(rng, 1)[0], rand_fe(rng, 1)[0]
+    dv = [torch.from_numpy(v.view(np.int64).copy()).cuda() for v in vecs]
+    H = ctx.sumcheck_round(3, dv, b, r)
+    ref = oracle.sumcheck_fold_many(vecs, r)
+    assert np.array_equal(H, oracle.sumcheck_round(3, ref, b))
+    for d, f in zip(dv, ref):
+        assert np.array_equal(d.cpu().numpy().view(np.uint64)[: m // 2], f)
+
+
+def test_round_forms_invalid(ctx, gbz):
+    v = [np.zeros((8, 2), np.uint64) for _ in range(6)]
+    with pytest.raises(gbz.GbzError):
+        ctx.sumcheck_round(3, v)  # zero-check needs b
+    with pytest.raises(gbz.GbzError):
+        ctx.sumcheck_round(0, [np.zeros((6, 2), np.uint64)] * 2)
+
+
+@pytest.mark.parametrize("name", ["cubicsc_8_4", "cubicsc_10_3", "cubicsc_3_4", "quadsc_8_4", "quadsc_11_2"])
+def test_party_sumcheck_golden(ctx, golden, name):
+    r, (cmd, logM, offset, seed, prng) = case(golden, name)
+    M = 1 << logM
+    cubic = cmd == "cubicsc"
+    nv = 3 if cubic else 2
+    raw = splitmix_ext(seed, nv * M + 1)
+    vecs = [np.ascontiguousarray(raw[k * M:(k + 1) * M]) for k in range(nv)]
+    w = raw[nv * M:nv * M + 1]
+    y = r.fe(1)[0]
+    fin = r.fe(nv)
+    nr = r.u32()
+    chal = r.fe(nr)
+    res = ctx.party_sumcheck(1 if cubic else 0, vecs, 1, w=w, offset=offset, prng=prng, y=y)
+    assert np.array_equal(res["challenges"], chal)
+    assert np.array_equal(res["fin"], fin)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("N,logM,offset", [(1, 0, 4), (2, 0, 4), (4, 1, 4), (2, 6, 4), (4, 10, 3), (16, 8, 4),
+                                           (16, 12, 2), (64, 6, 0), (1, 16, 4), (8, 3, 5)])
+def test_party_sumcheck_vs_oracle(ctx, oracle, form, N, logM, offset):
+    rng = np.random.default_rng(2000 + 100 * form + 10 * N + logM)
+    M = 1 << logM
+    nv = 3 if form else 2
+    vecs = [rand_fe(rng, N * M) for _ in range(nv)]
+    w = rand_fe(rng, N)
+    fs = rand_fe(rng, 1)[0]
+    # the claim: oracle's first round polynomial is consistent with it by
+    # construction, so take it from the oracle run with a zero claim
+    probe = oracle.party_sumcheck(form, vecs, N, w=w, offset=offset, fs=fs, prng_seed=3, y=[0, 0])
+    if len(probe["polys"]):
+        p0 = probe["polys"][0]
+        y = fadd(feval(p0, (0, 0)), feval(p0, (1, 0)))
+    else:
+        y = (0, 0)
+    y = np.array(y, dtype=np.uint64)
+    ref = oracle.party_sumcheck(form, vecs, N, w=w, offset=offset, fs=fs, prng_seed=3, y=y)
+    got = ctx.party_sumcheck(form, vecs, N, w=w, offset=offset, fs=fs, prng=3, y=y)
+    assert np.array_equal(got["polys"], ref["polys"])
+    assert np.array_equal(got["challenges"], ref["challenges"])
+    assert np.array_equal(got["fin"], ref["fin"])
+    assert np.array_equal(got["y"], ref["y"])
+    assert np.array_equal(got["fs"], ref["fs"])
+    assert got["prng"].next() == ref["prng"].next()
+
+
+def test_party_sumcheck_wrong_claim_is_reported(ctx, gbz, oracle):
+    rng = np.random.default_rng(9)
+    vecs = [rand_fe(rng, 1 << 10) for _ in range(3)]
+    with pytest.raises(gbz.GbzError) as ei:
+        ctx.party_sumcheck(1, vecs, 4, w=rand_fe(rng, 4), y=[1, 2])
+    assert ei.value.status == gbz.ECHECK
+
+
+def test_party_sumcheck_large_consistent(ctx, oracle):
+    """16 parties of 2^20 entries (2^24 in all): every round polynomial
+    matches the running claim (no ECHECK) and the transcript equals the
+    oracle's on the same inputs."""
+    rng = np.random.default_rng(10)
+    N, M = 16, 1 << 20
+    vecs = [rand_fe(rng, N * M) for _ in range(3)]
+    w = rand_fe(rng, N)
+    probe = oracle.party_sumcheck(1, vecs, N, w=w, offset=4, y=[0, 0])
+    p0 = probe["polys"][0]
+    y = np.array(fadd(feval(p0, (0, 0)), feval(p0, (1, 0))), dtype=np.uint64)
+    got = ctx.party_sumcheck(1, vecs, N, w=w, offset=4, y=y)
+    assert np.array_equal(got["challenges"], probe["challenges"])
+    assert np.array_equal(got["fin"], probe["fin"])
