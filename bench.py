@@ -99,6 +99,26 @@ def algorithmic_bytes(logn, rate):
     return out
 
 
+def commit_lengths(logn, rate):
+    """Codeword lengths of every commitment of one proof (initial + WHIR)."""
+    n = 1 << logn
+    out = [n * rate]
+    m, cur = n, rate
+    while m > 4:
+        m //= 4
+        out.append(2 * cur * m)
+        cur *= 2
+    return out
+
+
+def algorithmic_int_work(logn, rate):
+    """Integer-pipe work per proof: radix-2 butterfly count (L/2 log2 L) of
+    the commitment transforms, and Blake3 compressions (L/4 leaves + L/4 - 1
+    nodes) of their Merkle trees."""
+    ls = commit_lengths(logn, rate)
+    return {"ntt": sum(L // 2 * (L.bit_length() - 1) for L in ls), "merkle": sum(L // 2 - 1 for L in ls)}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -398,27 +418,49 @@ def main():
     host_t = np.ctypeslib.as_array(ctypes.cast(ht_p, ctypes.POINTER(ctypes.c_uint8)), shape=(tbytes,)).copy()
     assert host_t.tobytes() == got.tobytes()
 
-    # roofline of the dominant category
+    # rooflines per kernel category: HBM for the streaming kernels, the
+    # measured integer-pipe peaks for the NTT (F_{p^2} multiplies) and the
+    # Merkle levels (Blake3 compressions)
     algo = algorithmic_bytes(logn, RATE)
+    work = algorithmic_int_work(logn, RATE)
     per_proof_ms = {k: v[0] / args.steps for k, v in prof.items()}
     dom = max(per_proof_ms, key=lambda k: per_proof_ms[k])
-    peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-        hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+            hbm_peak, peak_src = float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json)"
     except (OSError, KeyError, ValueError):
         hbm_peak, peak_src = 6800.0, "fallback"
-    dom_bytes = algo.get(dom)
-    roof = None
-    if dom_bytes:
-        achieved = dom_bytes / (per_proof_ms[dom] / 1e3) / 1e9
-        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": None,
-                "algorithmic_bytes_per_proof": dom_bytes, "ms_per_proof": per_proof_ms[dom]}
-    else:
-        roof = {"kernel": dom, "bound": "hbm", "achieved": None, "peak": hbm_peak, "unit": "GB/s", "frac": None,
-                "peak_source": peak_src, "traffic": None, "ms_per_proof": per_proof_ms[dom]}
+    fmul_peak, b3_peak = ctx.calibrate()
+    rooflines = {}
+    for cat, ms in per_proof_ms.items():
+        t = ms / 1e3
+        if t <= 0:
+            continue
+        r = {"ms_per_proof": ms}
+        if cat in algo:
+            a = algo[cat] / t / 1e9
+            r["hbm"] = {"achieved": a, "peak": hbm_peak, "unit": "GB/s", "frac": a / hbm_peak,
+                        "algorithmic_bytes_per_proof": algo[cat]}
+        if cat == "ntt":
+            a = work["ntt"] / t / 1e9
+            r["int"] = {"achieved": a, "peak": fmul_peak / 1e9, "unit": "G F-mul/s (radix-2 butterflies)",
+                        "frac": a / (fmul_peak / 1e9), "butterflies_per_proof": work["ntt"]}
+        if cat == "merkle":
+            a = work["merkle"] / t / 1e9
+            r["int"] = {"achieved": a, "peak": b3_peak / 1e9, "unit": "G Blake3 compressions/s",
+                        "frac": a / (b3_peak / 1e9), "compressions_per_proof": work["merkle"]}
+        rooflines[cat] = r
+    d = rooflines.get(dom, {})
+    primary = d.get("int") or d.get("hbm")
+    roof = {"kernel": dom, "bound": "int" if "int" in d else "hbm", "ms_per_proof": per_proof_ms[dom],
+            "traffic": None}
+    if primary:
+        roof.update({"achieved": primary["achieved"], "peak": primary["peak"], "unit": primary["unit"],
+                     "frac": primary["frac"]})
+    if "hbm" in d:
+        roof["hbm"] = d["hbm"]
+    roof["peak_source"] = {"hbm": peak_src, "int": "gbz_calibrate on this GPU (F_{p^2} multiply chains, "
+                                                     "Blake3 compression chains on every SM)"}
 
     line = {
         "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": ws, "steps": args.steps,
@@ -432,6 +474,8 @@ def main():
         "gpu_launches": launches * args.steps,
         "kernel_ms_per_proof": per_proof_ms,
         "roofline": roof,
+        "rooflines": rooflines,
+        "int_peaks": {"fmul_per_s": fmul_peak, "blake3_per_s": b3_peak},
         "clocks": clk.summary(),
         "transcript_bytes": tbytes,
     }

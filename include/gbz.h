@@ -361,6 +361,15 @@ gbz_status gbz_prove(gbz_ctx *ctx, const uint64_t *witness, int logn, int rate, 
  * unsupported shape. */
 int gbz_prove_launches(int logn, int rate);
 
+/* ----------------------------------------------------------- calibration */
+
+/* Measures, on the context's device, the throughput of the F_{p^2} multiply
+ * (*fmul_per_s, independent multiply chains on every SM) and of the 64-byte
+ * Blake3 compression (*blake3_per_s): the integer-pipe peaks that the NTT,
+ * RS fold and Merkle kernels are bounded by.  Either output may be NULL.
+ * Takes a few tens of milliseconds.  No counterpart in the reference. */
+gbz_status gbz_calibrate(gbz_ctx *ctx, double *fmul_per_s, double *blake3_per_s);
+
 /* ------------------------------------------------------------ profiling */
 
 /* Per-category CUDA-event timing of the kernels gbz_prove enqueues, on the

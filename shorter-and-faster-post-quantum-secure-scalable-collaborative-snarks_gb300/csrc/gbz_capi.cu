@@ -845,6 +845,15 @@ gbz_status gbz_sumcheck_round(gbz_ctx *ctx, int form, uint64_t *const *v, uint64
   API_END(ctx)
 }
 
+gbz_status gbz_calibrate(gbz_ctx *ctx, double *fmul_per_s, double *blake3_per_s) {
+  API_BEGIN(ctx)
+  int sms = 0;
+  GBZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  void *scratch = ctx->buf(48, calibrate_scratch_bytes(sms));
+  calibrate_int_pipes(ctx->stream, scratch, fmul_per_s, blake3_per_s);
+  API_END(ctx)
+}
+
 int gbz_party_sumcheck_rounds(uint64_t M, int N, int offset) {
   if (!is_pow2(M) || N < 1 || !is_pow2((uint64_t)N) || offset < 0) return -1;
   return party_sumcheck_rounds(M, N, offset, nullptr);

@@ -143,4 +143,10 @@ void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s);
 constexpr uint64_t kUpdateBetasScratch = (uint64_t)kMaxQueries * 256;
 void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s);
 
+// ----------------------------------------------------------- calibration
+// Measured throughput of the F_{p^2} multiply and of the 64-byte Blake3
+// compression on the current device (scratch: calibrate_scratch_bytes).
+void calibrate_int_pipes(cudaStream_t s, void *scratch, double *fmul_per_s, double *blake3_per_s);
+uint64_t calibrate_scratch_bytes(int sms);
+
 }  // namespace gbz

@@ -389,7 +389,9 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
 
   // Commits go to the plan's second stream c; it starts after everything
   // the caller enqueued on s (the witness copy) and s joins it at the end.
-  cudaStream_t c = p.s2;
+  // With the profiler on, the commits stay on s so that the per-category
+  // event times do not include waits for the other stream's kernels.
+  cudaStream_t c = prof ? s : p.s2;
   if (!dry) {
     GBZ_CUDA(cudaEventRecord(p.ev_in, s));
     GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_in, 0));

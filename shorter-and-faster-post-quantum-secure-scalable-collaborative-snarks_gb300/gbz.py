@@ -42,7 +42,7 @@ EXPORTS = (
     "gbz_profile_read", "gbz_whir_update_betas_noalloc", "gbz_rs_multifold5", "gbz_lagrange_coeff",
     "gbz_encode_rows", "gbz_column_merkle", "gbz_secret_shares", "gbz_party_aggregate",
     "gbz_cosumcheck_phase1", "gbz_cosumcheck_phase2", "gbz_prove_batch", "gbz_serve", "gbz_sched_release",
-    "gbz_sumcheck_round", "gbz_party_sumcheck_rounds", "gbz_party_sumcheck",
+    "gbz_sumcheck_round", "gbz_party_sumcheck_rounds", "gbz_party_sumcheck", "gbz_calibrate",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -137,6 +137,7 @@ def _load():
         "gbz_sched_release": (c_int, [vp, vp]),
         "gbz_sumcheck_round": (c_int, [vp, c_int, vp, u64, vp, vp, vp, c_int]),
         "gbz_party_sumcheck_rounds": (c_int, [u64, c_int, c_int]),
+        "gbz_calibrate": (c_int, [vp, vp, vp]),
         "gbz_party_sumcheck": (c_int, [vp, c_int, vp, vp, vp, u64, c_int, vp, c_int, vp, vp, vp, vp, vp, vp, c_int]),
     }
     for name, (res, args) in sig.items():
@@ -467,6 +468,12 @@ class Context:
         return out
 
     # ------------------------------------------------------------ profiling
+    def calibrate(self):
+        """(F_{p^2} multiplies per second, Blake3 compressions per second)."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self.check(lib.gbz_calibrate(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def profile_enable(self, on=True):
         self.check(lib.gbz_profile_enable(self.h, int(bool(on))))
 
