@@ -330,6 +330,53 @@ gbz_status gbz_party_sumcheck(gbz_ctx *ctx, int form, const uint64_t *v1, const 
                               uint64_t M, int N, const uint64_t *w, int offset, uint64_t *fs_state, gbz_prng *prng,
                               uint64_t *y, uint64_t *polys, uint64_t *challenges, uint64_t *fin, int mem);
 
+/* ------------------------------------------------------ WHIR aggregation */
+
+/* aggregate_claims (Whir.cpp:608-668) for k arrays of n entries and c claim
+ * points of log2(n) coordinates (points: c*log2(n) elements, host):
+ * Sums[i][j] = <precompute_beta(point_j), array_i>; F::_random() draws c
+ * beta weights then k array weights from *prng (in/out); K = sum_ij
+ * bw_j aw_i Sums[i][j] (2 words, host); b_aggr = sum_j bw_j beta_j and
+ * arr = sum_i aw_i array_i (n entries each, mem); challenges (host) gets
+ * the c + k weights, sums (host, optional) the k x c inner products. */
+gbz_status gbz_whir_aggregate_claims(gbz_ctx *ctx, int k, const uint64_t *const *arrays, uint64_t n, int c,
+                                     const uint64_t *points, gbz_prng *prng, uint64_t *arr, uint64_t *b_aggr,
+                                     uint64_t *K, uint64_t *challenges, uint64_t *sums, int mem);
+
+/* aggregate_arrays (Whir.cpp:670-704): arr += sum_{i>=1} r1_i arrays_i and
+ * b += sum_{i>=1} r2_i B_i in place (n entries, mem); K (host) = sum over
+ * i < k, j < nB of r1_i r2_j <arrays_i, B_j>.  r1 (k) and r2 (nB) are host. */
+gbz_status gbz_whir_aggregate_arrays(gbz_ctx *ctx, int k, const uint64_t *const *arrays, int nB,
+                                     const uint64_t *const *B, uint64_t n, const uint64_t *r1, const uint64_t *r2,
+                                     uint64_t *arr, uint64_t *b, uint64_t *K, int mem);
+
+/* aggregate_commitments (Whir.cpp:547-606): codeword = sum_i r_i
+ * codewords_i (n entries, mem; r host); the query openings advance *prng
+ * by l rand() draws (l as the WHIR query count of `rate`); levels (mem)
+ * receives the new Merkle tree over n / whir_k leaves, 2 n / whir_k - 1
+ * hashes.  The reference's loop that hashes the strided leaf groups never
+ * stores its result (:594-601), so every leaf of that tree is the zero hash;
+ * the levels here are the same. */
+gbz_status gbz_whir_aggregate_commitments(gbz_ctx *ctx, int k, const uint64_t *const *codewords, uint64_t n,
+                                          const uint64_t *r, int rate, int whir_k, gbz_prng *prng,
+                                          uint64_t *codeword, uint8_t *levels, int mem);
+
+/* ------------------------------------------------ coPCS open rounds (a16) */
+
+/* tensor_eval_vector (coPCS.cpp:602-632) for party my_id (< 2 cols):
+ * out[j] = c w1^j for j < rows, w1 = omega_{rate rows}^{point[1]}, c the
+ * party's entry of the transformed powers of omega_{4 cols}^{2 point[0] + 1}. */
+gbz_status gbz_tensor_eval_vector(gbz_ctx *ctx, const uint32_t *point, int cols, uint64_t rows, int rate, int my_id,
+                                  uint64_t *out, int mem);
+
+/* pcs_sumcheck_phase3 (coPCS.cpp:634-648): B += sum_i s^(i+1)
+ * tensor_eval_vector(query_i, N/2, rows, rate) in place; queries holds l
+ * (point[0], point[1]) pairs (host), s 2 words (host); rate is the
+ * reference's _rates[iter+1][0] (the caller skips the call where the
+ * reference returns early). */
+gbz_status gbz_pcs_sumcheck_phase3(gbz_ctx *ctx, uint64_t *B, uint64_t rows, const uint32_t *queries, int l,
+                                   const uint64_t *s, int N, int rate, int my_id, int mem);
+
 /* --------------------------------------------------------------- prover */
 
 /* Bytes of the transcript of one proof of a 2^logn witness at `rate`. */

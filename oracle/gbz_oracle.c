@@ -1184,3 +1184,119 @@ void orc_party_sumcheck(int form, uint64_t *v1, uint64_t *v2, uint64_t *v3, int6
   fs[0] = state.re; fs[1] = state.im;
   y_io[0] = y.re; y_io[1] = y.im;
 }
+
+/* ------------------------------------------------ WHIR aggregation (a17) */
+static fe dot(const uint64_t *a, const uint64_t *b, int64_t n) {
+  fe acc = f_zero();
+  for (int64_t t = 0; t < n; t++) acc = f_add(acc, f_mul(ld(a, t), ld(b, t)));
+  return acc;
+}
+
+/* aggregate_claims (Whir.cpp:608-668) with every claim point of log2(n)
+ * coordinates: betas_j = precompute_beta(point_j); Sums[i][j] =
+ * <betas_j, arrays_i>; F::_random() draws c beta challenges then k array
+ * challenges; K = sum_i sum_j bc_j ac_i Sums[i][j]; b_aggr = sum_j bc_j
+ * betas_j; arr = sum_i ac_i arrays_i.  chal: the c + k challenges, sums: k*c
+ * (row i = array). */
+void orc_aggregate_claims(int k, const uint64_t *const *arrays, int64_t n, int c, const uint64_t *points,
+                          orc_prng *g, uint64_t *arr, uint64_t *b_aggr, uint64_t K[2], uint64_t *chal,
+                          uint64_t *sums) {
+  int lg = ilog2_64(n);
+  uint64_t *betas = (uint64_t *)malloc(16 * (size_t)n * (size_t)(c > 0 ? c : 1));
+  for (int j = 0; j < c; j++) orc_precompute_beta(points + 2 * (size_t)j * lg, lg, betas + 2 * (size_t)j * n, 1);
+  for (int i = 0; i < k; i++)
+    for (int j = 0; j < c; j++) st(sums, (int64_t)i * c + j, dot(betas + 2 * (size_t)j * n, arrays[i], n));
+  for (int j = 0; j < c + k; j++) st(chal, j, prng_field(g));
+  fe Kacc = f_zero();
+  for (int i = 0; i < k; i++)
+    for (int j = 0; j < c; j++)
+      Kacc = f_add(Kacc, f_mul(f_mul(ld(chal, j), ld(chal, c + i)), ld(sums, (int64_t)i * c + j)));
+  K[0] = Kacc.re; K[1] = Kacc.im;
+  for (int64_t t = 0; t < n; t++) {
+    fe sb = f_zero(), sa = f_zero();
+    for (int j = 0; j < c; j++) sb = f_add(sb, f_mul(ld(chal, j), ld(betas + 2 * (size_t)j * n, t)));
+    for (int i = 0; i < k; i++) sa = f_add(sa, f_mul(ld(chal, c + i), ld(arrays[i], t)));
+    st(b_aggr, t, sb);
+    st(arr, t, sa);
+  }
+  free(betas);
+}
+
+/* aggregate_arrays (Whir.cpp:670-704): evals[i][j] = <arrays_i, B_j>;
+ * arr += sum_{i>=1} r1_i arrays_i; b += sum_{i>=1} r2_i B_i; returns
+ * K = sum_i sum_j r1_i r2_j evals[i][j].  Requires nB >= k. */
+void orc_aggregate_arrays(uint64_t *arr, uint64_t *b, int k, const uint64_t *const *arrays, int nB,
+                          const uint64_t *const *B, int64_t n, const uint64_t *r1, const uint64_t *r2, uint64_t K[2]) {
+  fe Kacc = f_zero();
+  for (int i = 0; i < k; i++)
+    for (int j = 0; j < nB; j++)
+      Kacc = f_add(Kacc, f_mul(f_mul(ld(r1, i), ld(r2, j)), dot(arrays[i], B[j], n)));
+  for (int i = 1; i < k; i++)
+    for (int64_t t = 0; t < n; t++) {
+      st(arr, t, f_add(ld(arr, t), f_mul(ld(r1, i), ld(arrays[i], t))));
+      st(b, t, f_add(ld(b, t), f_mul(ld(r2, i), ld(B[i], t))));
+    }
+  K[0] = Kacc.re; K[1] = Kacc.im;
+}
+
+/* aggregate_commitments (Whir.cpp:547-606): codeword = sum_i r_i cw_i; l
+ * rand() draws for the (discarded) query openings, l as Whir.cpp:257; the
+ * new tree has n/whir_k leaves, and since the loop that hashes the strided
+ * leaf groups never stores its result (:594-601), every leaf is the zero
+ * hash and the levels are those of create_tree_blake over zeros.  levels
+ * gets 2 (n/whir_k) - 1 hashes, leaves first. */
+void orc_aggregate_commitments(int k, const uint64_t *const *cws, int64_t n, const uint64_t *r, int rate, int whir_k,
+                               orc_prng *g, uint64_t *codeword, uint8_t *levels) {
+  for (int64_t t = 0; t < n; t++) {
+    fe s = f_zero();
+    for (int i = 0; i < k; i++) s = f_add(s, f_mul(ld(r, i), ld(cws[i], t)));
+    st(codeword, t, s);
+  }
+  int l = orc_whir_queries(rate);
+  for (int i = 0; i < l; i++) (void)orc_prng_next(g);
+  int64_t leaves = n / whir_k;
+  memset(levels, 0, 32 * (size_t)leaves);
+  uint8_t *prev = levels;
+  int64_t cnt = leaves;
+  while (cnt > 1) {
+    uint8_t *next = prev + 32 * cnt;
+    cnt /= 2;
+    for (int64_t i = 0; i < cnt; i++) hash_self(prev + 32 * (2 * i), next + 32 * i);
+    prev = next;
+  }
+}
+
+/* ------------------------------------------- coPCS open rounds (a16) */
+/* tensor_eval_vector (coPCS.cpp:602-632): w1 = omega_{rate rows}^{p1},
+ * w2 = omega_{4 cols}^{2 p0 + 1}; pow2[t] = w2^t (t < cols) goes through two
+ * inverse transforms, is zero-padded to 2N = 4 cols and transformed; the
+ * party my_id takes entry 2 my_id + 1 as its scale of B[j] = w1^j. */
+void orc_tensor_eval_vector(uint32_t p0, uint32_t p1, int cols, int64_t rows, int rate, int my_id, uint64_t *B) {
+  int N = 2 * cols;
+  fe w1 = f_pow(f_rou(ilog2_64((int64_t)rate * rows)), (u128)p1);
+  fe w2 = f_pow(f_rou(ilog2_64(4 * (int64_t)cols)), (u128)(2 * (uint64_t)p0 + 1));
+  uint64_t *buf = (uint64_t *)calloc(2 * 2 * (size_t)N, sizeof(uint64_t));
+  fe x = f_one();
+  for (int t = 0; t < cols; t++) { st(buf, t, x); x = f_mul(x, w2); }
+  orc_fft(buf, ilog2_64(cols), 1, 1);
+  orc_fft(buf, ilog2_64(cols), 1, 1);
+  orc_fft(buf, ilog2_64(2 * N), 0, 1);
+  fe c = ld(buf, 2 * my_id + 1);
+  free(buf);
+  fe y = c;
+  for (int64_t j = 0; j < rows; j++) { st(B, j, y); y = f_mul(y, w1); }
+}
+
+/* pcs_sumcheck_phase3 (coPCS.cpp:634-648): B += sum_i s^{i+1}
+ * tensor_eval_vector(query_i); queries: l pairs (point[0], point[1]). */
+void orc_pcs_phase3(uint64_t *B, int64_t rows, const uint32_t *queries, int l, const uint64_t s[2], int N, int rate,
+                    int my_id) {
+  fe ss = f_make(s[0], s[1]), p = ss;
+  uint64_t *tmp = (uint64_t *)malloc(16 * (size_t)rows);
+  for (int i = 0; i < l; i++) {
+    orc_tensor_eval_vector(queries[2 * i], queries[2 * i + 1], N / 2, rows, rate, my_id, tmp);
+    for (int64_t j = 0; j < rows; j++) st(B, j, f_add(ld(B, j), f_mul(p, ld(tmp, j))));
+    p = f_mul(p, ss);
+  }
+  free(tmp);
+}

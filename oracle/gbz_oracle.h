@@ -146,6 +146,25 @@ void orc_party_sumcheck(int form, uint64_t *v1, uint64_t *v2, uint64_t *v3, int6
                         int offset, uint64_t fs[2], orc_prng *g, uint64_t y_io[2], uint64_t *polys,
                         uint64_t *chal, uint64_t *fin);
 
+/* ---- WHIR aggregation ------------------------------------------------- */
+/* aggregate_claims (Whir.cpp:608-668), every point with log2(n) coordinates. */
+void orc_aggregate_claims(int k, const uint64_t *const *arrays, int64_t n, int c, const uint64_t *points,
+                          orc_prng *g, uint64_t *arr, uint64_t *b_aggr, uint64_t K[2], uint64_t *chal,
+                          uint64_t *sums);
+/* aggregate_arrays (Whir.cpp:670-704); arr and b are updated in place. */
+void orc_aggregate_arrays(uint64_t *arr, uint64_t *b, int k, const uint64_t *const *arrays, int nB,
+                          const uint64_t *const *B, int64_t n, const uint64_t *r1, const uint64_t *r2, uint64_t K[2]);
+/* aggregate_commitments (Whir.cpp:547-606). */
+void orc_aggregate_commitments(int k, const uint64_t *const *cws, int64_t n, const uint64_t *r, int rate, int whir_k,
+                               orc_prng *g, uint64_t *codeword, uint8_t *levels);
+
+/* ---- coPCS open rounds ------------------------------------------------ */
+/* tensor_eval_vector (coPCS.cpp:602-632) for party my_id: B has rows entries. */
+void orc_tensor_eval_vector(uint32_t p0, uint32_t p1, int cols, int64_t rows, int rate, int my_id, uint64_t *B);
+/* pcs_sumcheck_phase3 (coPCS.cpp:634-648) with _rates[iter+1][0] = rate. */
+void orc_pcs_phase3(uint64_t *B, int64_t rows, const uint32_t *queries, int l, const uint64_t s[2], int N, int rate,
+                    int my_id);
+
 /* SplitMix64 witness generator shared by tests and bench. */
 void orc_witness(uint64_t seed, int64_t n, uint64_t *out);
 

@@ -364,3 +364,66 @@ def party_sumcheck(form, vecs, N, w=None, offset=4, fs=(0, 0), prng_seed=1, y=No
                              ctypes.byref(g.s), _p64(ya), _p64(polys), _p64(chal), _p64(fin))
     return {"y": ya, "polys": polys[: nc * nchal].reshape(nchal, nc, 2), "challenges": chal[:nchal], "fin": fin,
             "fs": fsa, "prng": g}
+
+
+def _ptr_array(vs):
+    return (ctypes.c_void_p * max(len(vs), 1))(*[v.ctypes.data for v in vs])
+
+
+def aggregate_claims(arrays, points, prng_seed=1, prng=None):
+    """aggregate_claims (Whir.cpp:608-668).  Returns arr, b_aggr, K,
+    challenges (c beta then k array challenges), sums (k x c)."""
+    arrs = [np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2) for a in arrays]
+    pts = np.ascontiguousarray(points, dtype=np.uint64).reshape(len(points), -1, 2)
+    k, n, c = len(arrs), arrs[0].shape[0], pts.shape[0]
+    arr, b, K = fe_array(n), fe_array(n), np.zeros(2, dtype=np.uint64)
+    chal, sums = fe_array(c + k), fe_array(max(k * c, 1))
+    g = prng if prng is not None else Prng(prng_seed)
+    lib().orc_aggregate_claims(ctypes.c_int(k), _ptr_array(arrs), ctypes.c_int64(n), ctypes.c_int(c), _p64(pts),
+                               ctypes.byref(g.s), _p64(arr), _p64(b), _p64(K), _p64(chal), _p64(sums))
+    return arr, b, K, chal, sums[: k * c].reshape(k, c, 2)
+
+
+def aggregate_arrays(arr, b, arrays, B, r1, r2):
+    """aggregate_arrays (Whir.cpp:670-704): returns (arr', b', K)."""
+    arr = np.array(np.asarray(arr, dtype=np.uint64).reshape(-1, 2), copy=True)
+    b = np.array(np.asarray(b, dtype=np.uint64).reshape(-1, 2), copy=True)
+    arrs = [np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2) for a in arrays]
+    Bs = [np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2) for a in B]
+    r1 = np.ascontiguousarray(r1, dtype=np.uint64).reshape(-1, 2)
+    r2 = np.ascontiguousarray(r2, dtype=np.uint64).reshape(-1, 2)
+    K = np.zeros(2, dtype=np.uint64)
+    lib().orc_aggregate_arrays(_p64(arr), _p64(b), ctypes.c_int(len(arrs)), _ptr_array(arrs), ctypes.c_int(len(Bs)),
+                               _ptr_array(Bs), ctypes.c_int64(arr.shape[0]), _p64(r1), _p64(r2), _p64(K))
+    return arr, b, K
+
+
+def aggregate_commitments(codewords, r, rate, whir_k=4, prng_seed=1, prng=None):
+    """aggregate_commitments (Whir.cpp:547-606): (codeword, levels, prng)."""
+    cws = [np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2) for a in codewords]
+    n = cws[0].shape[0]
+    r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+    cw = fe_array(n)
+    leaves = n // whir_k
+    levels = np.zeros((2 * leaves - 1, 32), dtype=np.uint8)
+    g = prng if prng is not None else Prng(prng_seed)
+    lib().orc_aggregate_commitments(ctypes.c_int(len(cws)), _ptr_array(cws), ctypes.c_int64(n), _p64(r),
+                                    ctypes.c_int(rate), ctypes.c_int(whir_k), ctypes.byref(g.s), _p64(cw),
+                                    _p8(levels))
+    return cw, levels, g
+
+
+def tensor_eval_vector(point, cols, rows, rate, my_id):
+    out = fe_array(rows)
+    lib().orc_tensor_eval_vector(ctypes.c_uint32(point[0]), ctypes.c_uint32(point[1]), ctypes.c_int(cols),
+                                 ctypes.c_int64(rows), ctypes.c_int(rate), ctypes.c_int(my_id), _p64(out))
+    return out
+
+
+def pcs_phase3(B, queries, s, N, rate, my_id):
+    B = np.array(np.asarray(B, dtype=np.uint64).reshape(-1, 2), copy=True)
+    q = np.ascontiguousarray(queries, dtype=np.uint32).reshape(-1, 2)
+    ss = np.ascontiguousarray(s, dtype=np.uint64).reshape(2)
+    lib().orc_pcs_phase3(_p64(B), ctypes.c_int64(B.shape[0]), ctypes.c_void_p(q.ctypes.data), ctypes.c_int(q.shape[0]), _p64(ss),
+                         ctypes.c_int(N), ctypes.c_int(rate), ctypes.c_int(my_id))
+    return B

@@ -20,7 +20,13 @@
 //   ref_full bround <logm> <iter> <seed>                 _quadratic_batch_sumcheck_phase1/2 (coSumcheck_MPI.cpp:156-187)
 //   ref_full cubicsc <logM> <offset> <seed> <prng>       _cubic_sumcheck, one party (Distributed_Sumcheck.cpp:1122)
 //   ref_full quadsc <logM> <offset> <seed> <prng>        _quadratic_sumcheck, one party (Distributed_Sumcheck.cpp:204)
+//   ref_full aggclaims <logn> <k> <c> <seed> <prng>      aggregate_claims (Whir.cpp:608)
+//   ref_full aggarrays <logn> <k> <seed>                 aggregate_arrays (Whir.cpp:670)
+//   ref_full aggcommit <logn> <k> <rate> <whir_k> <seed> <prng>  aggregate_commitments (Whir.cpp:547)
+//   ref_full tensor <logrows> <N> <rate> <my_id> <p0> <p1>         tensor_eval_vector (coPCS.cpp:602)
+//   ref_full phase3 <logrows> <N> <l> <rate> <my_id> <seed>        pcs_sumcheck_phase3 (coPCS.cpp:634)
 #include "Distributed_Sumcheck.h"
+#include "Whir.h"
 #include "coPCS.h"
 #include "coPCS_utils.h"
 #include "coSumcheck.h"
@@ -48,6 +54,12 @@ quadratic_poly _quadratic_batch_sumcheck_phase1(int iter, F b, vector<F> &v1, ve
 void _quadratic_batch_sumcheck_phase2(int iter, F r, vector<F> &v1, vector<F> &v2, vector<F> &v3, vector<F> &v4,
                                       vector<F> &r1, vector<F> &r2);
 extern int sumcheck_offset;  // main.cpp:36
+extern int my_id;                        // coPCS.cpp:19
+extern vector<vector<int>> _rates;       // New_PCS.cpp:6
+vector<F> tensor_eval_vector(vector<u32> point, int cols, int rows, int rate);
+void pcs_sumcheck_phase3(vector<F> &B, vector<vector<u32>> queries, F s, int iter, int N);
+F aggregate_arrays(vector<F> &arr, vector<F> &b, vector<vector<F>> &arrays, vector<vector<F>> &B, vector<F> r1,
+                   vector<F> r2);
 void compute_secret_shares(vector<F> &v, vector<vector<F>> &v_shares, int N, int k, int _k, bool privacy_preserving);
 vector<F> unpack_secret_share(vector<F> &secret, int _k, int k);
 
@@ -126,6 +138,86 @@ int main(int argc, char **argv) {
     uint32_t nr = (uint32_t)res[0].second.size();
     put(&nr, 4);
     putFs(res[0].second);
+    return 0;
+  }
+  if (c == "aggclaims") {
+    // inputs from the seed: k arrays of 2^logn, c points of logn; output:
+    // arr, b_aggr, K, the beta challenges then the array challenges
+    int logn = I(2), k = I(3), nc = I(4);
+    SplitMix g(U(5));
+    srandom((unsigned)U(6));
+    vector<vector<F>> arrays(k);
+    for (auto &a : arrays) a = g.vec(1u << logn);
+    vector<vector<std::pair<F, vector<F>>>> claims(1);
+    for (int j = 0; j < nc; j++) claims[0].push_back({F(0), g.vec(logn)});
+    vector<F> arr, b_aggr;
+    F K;
+    vector<vector<F>> ch = aggregate_claims(arrays, arr, b_aggr, claims, K);
+    putFs(arr); putFs(b_aggr); putFs({K}); putFs(ch[0]); putFs(ch[1]);
+    return 0;
+  }
+  if (c == "aggarrays") {
+    // k arrays and k B vectors of 2^logn, r1, r2 (k each); arr = arrays[0],
+    // b = B[0] on entry.  Output: arr, b, K.
+    int logn = I(2), k = I(3);
+    SplitMix g(U(4));
+    vector<vector<F>> arrays(k), B(k);
+    for (auto &a : arrays) a = g.vec(1u << logn);
+    for (auto &a : B) a = g.vec(1u << logn);
+    vector<F> r1 = g.vec(k), r2 = g.vec(k);
+    vector<F> arr = arrays[0], b = B[0];
+    F K = aggregate_arrays(arr, b, arrays, B, r1, r2);
+    putFs(arr); putFs(b); putFs({K});
+    return 0;
+  }
+  if (c == "aggcommit") {
+    // k codewords of 2^logn and r (k); the query openings use the Merkle
+    // tree of codeword 0.  Output: codeword, the new tree (levels, leaves
+    // first), then the next random() value (the generator's position).
+    int logn = I(2), k = I(3), rate = I(4);
+    whir_k = I(5);
+    SplitMix g(U(6));
+    srandom((unsigned)U(7));
+    vector<vector<F>> cws(k);
+    for (auto &a : cws) a = g.vec(1u << logn);
+    vector<F> r = g.vec(k);
+    vector<vector<vector<_hash>>> MT_aggr(1);
+    merkle_tree::merkle_tree_prover::MT_commit_Blake(cws[0].data(), MT_aggr[0], 1 << logn);
+    vector<F> codeword;
+    vector<vector<_hash>> MT;
+    aggregate_commitments(codeword, MT, cws, MT_aggr, r, rate);
+    putFs(codeword);
+    for (auto &lv : MT)
+      for (auto &h : lv) put(h.arr, 32);
+    int32_t nxt = (int32_t)random();
+    put(&nxt, 4);
+    return 0;
+  }
+  if (c == "tensor") {
+    int logrows = I(2), N = I(3), rate = I(4);
+    my_id = I(5);
+    vector<u32> point = {(u32)U(6), (u32)U(7)};
+    putFs(tensor_eval_vector(point, N / 2, 1 << logrows, rate));
+    return 0;
+  }
+  if (c == "phase3") {
+    // B (2^logrows) and s from the seed, then l queries (u32 pairs, written
+    // out); output: the queries and the updated B.
+    int logrows = I(2), N = I(3), l = I(4), rate = I(5);
+    my_id = I(6);
+    SplitMix g(U(7));
+    const uint32_t rows = 1u << logrows;
+    vector<F> B = g.vec(rows);
+    F s = g.ext();
+    vector<vector<u32>> queries(l, vector<u32>(2));
+    for (auto &q : queries) {
+      q[0] = (u32)(g.next() % (uint64_t)(N / 2));
+      q[1] = (u32)(g.next() % ((uint64_t)rate * rows));
+      put(q.data(), 8);
+    }
+    _rates = {{rate}, {rate}};
+    pcs_sumcheck_phase3(B, queries, s, 0, N);
+    putFs(B);
     return 0;
   }
   if (c == "multifold5") {

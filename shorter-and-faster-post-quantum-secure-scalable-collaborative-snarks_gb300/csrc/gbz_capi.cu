@@ -12,6 +12,7 @@
 #include "gbz_prover.cuh"
 #include "gbz_rounds.cuh"
 #include "gbz_sched.cuh"
+#include "gbz_whir_aggr.cuh"
 
 using namespace gbz;
 
@@ -142,7 +143,74 @@ __global__ void ub_prep_kernel(ProofState *st, const int32_t *q, int l, int logN
   }
 }
 
+// Loads arbitrary weights: comb_i = c_i, q_i = q_i mod N, omega_q_i = omega_N^{q_i}.
+__global__ void geo_prep_kernel(ProofState *st, const int32_t *q, const fe *c, int l, int logN) {
+  const fe om = root_of_unity(logN);
+  const uint32_t mask = (1u << logN) - 1;
+  for (int i = threadIdx.x; i < l; i += blockDim.x) {
+    const uint32_t qr = (uint32_t)q[i] & mask;
+    st->q[i] = (int32_t)qr;
+    st->comb[i] = c[i];
+    st->omega_q[i] = fpow(om, (uint64_t)qr);
+  }
+}
+
 }  // namespace
+
+// b[j] += sum_i c_i omega_N^{q_i j} for j < nb (host q, c), in chunks of at
+// most kMaxQueries terms, by the sparse transform or by direct sums.
+static void geometric_update(gbz_ctx *ctx, fe *db, uint64_t nb, const int32_t *hq, const fe *hc, int l, int logN) {
+  if (!ctx->st) GBZ_CUDA(cudaMalloc(&ctx->st, sizeof(ProofState)));
+  if (!ctx->ub_scratch) GBZ_CUDA(cudaMalloc(&ctx->ub_scratch, sizeof(fe) * kUpdateBetasScratch));
+  for (int i0 = 0; i0 < l; i0 += kMaxQueries) {
+    const int cnt = std::min(kMaxQueries, l - i0);
+    int32_t *dq = (int32_t *)ctx->buf(98, 4ull * kMaxQueries);
+    fe *dc = (fe *)ctx->buf(99, 16ull * kMaxQueries);
+    GBZ_CUDA(cudaMemcpyAsync(dq, hq + i0, 4ull * cnt, cudaMemcpyHostToDevice, ctx->stream));
+    GBZ_CUDA(cudaMemcpyAsync(dc, hc + i0, 16ull * cnt, cudaMemcpyHostToDevice, ctx->stream));
+    geo_prep_kernel<<<1, 256, 0, ctx->stream>>>(ctx->st, dq, dc, cnt, logN);
+    GBZ_CUDA(cudaGetLastError());
+    const uint64_t N = 1ull << logN;
+    if (nb <= N && update_betas_by_transform(cnt, nb, N)) {
+      fe *tmp = (fe *)ctx->buf(2, 16 * N);
+      ntt_sparse_accumulate(ctx->tables(logN), ctx->st->q, ctx->st->comb, cnt, db, nb, tmp, ctx->stream);
+    } else {
+      update_betas_launch(db, nb, ctx->st, cnt, ctx->ub_scratch, ctx->stream);
+    }
+    GBZ_CUDA(cudaStreamSynchronize(ctx->stream));  // hq / hc chunks are host memory of the caller
+  }
+}
+
+// The scale of tensor_eval_vector (coPCS.cpp:602-632) for party my_id:
+// entry 2 my_id + 1 of the length-2N transform of the twice inversely
+// transformed powers w2^t (t < cols, N = 2 cols).  Two inverse transforms of
+// length n map x to x[(n - t) mod n] / n, so the entry is
+// sum_t w2^{(cols - t) mod cols} / cols * omega_{2N}^{t (2 my_id + 1)}.
+static fe tensor_scale(uint32_t p0, int cols, int my_id) {
+  const int lg4 = ilog2(4ull * (uint64_t)cols);
+  const fe w2 = fpow(root_of_unity(lg4), 2ull * p0 + 1);
+  const fe step = fpow(root_of_unity(lg4), 2ull * (uint64_t)my_id + 1);
+  std::vector<fe> pw(cols);
+  fe x = fe_one();
+  for (int t = 0; t < cols; t++) {
+    pw[t] = x;
+    x = fmul(x, w2);
+  }
+  fe acc = fe_zero(), e = fe_one();
+  for (int t = 0; t < cols; t++) {
+    acc = fadd(acc, fmul(pw[(cols - t) % cols], e));
+    e = fmul(e, step);
+  }
+  return fmul(acc, finv(fe_make((uint64_t)cols, 0)));
+}
+
+static void check_tensor_shape(int cols, uint64_t rows, int rate, int my_id) {
+  if (cols < 1 || cols > (1 << 20) || !is_pow2((uint64_t)cols)) throw ArgError("tensor: cols must be a power of two");
+  if (my_id < 0 || my_id >= 2 * cols) throw ArgError("tensor: my_id must be below the number of parties");
+  if (rate < 1 || !is_pow2((uint64_t)rate)) throw ArgError("tensor: rate must be a power of two");
+  if (!is_pow2(rows) || ilog2(rows * (uint64_t)rate) > kMaxLogN)
+    throw ArgError("tensor: rows * rate must be a power of two <= 2^28");
+}
 
 extern "C" {
 
@@ -842,6 +910,207 @@ gbz_status gbz_sumcheck_round(gbz_ctx *ctx, int form, uint64_t *const *v, uint64
   }
   GBZ_CUDA(cudaMemcpyAsync(coeffs, dout, 16 * nc, cudaMemcpyDeviceToHost, ctx->stream));
   GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+namespace {
+// Device views of count vectors of n elements (slots base..base+count-1).
+VecList vec_views(gbz_ctx *ctx, int base, const uint64_t *const *v, int count, uint64_t n, int mem) {
+  if (count < 0 || count > kMaxVecs) throw ArgError("at most 64 vectors");
+  need(v, "vector list");
+  VecList l{};
+  for (int i = 0; i < count; i++) {
+    need(v[i], "vector");
+    l.p[i] = dev_view(ctx, base + i, (const fe *)v[i], 16 * n, mem, true);
+  }
+  return l;
+}
+fe host_fe(const uint64_t *p, int64_t i) { return fe_make(p[2 * i], p[2 * i + 1]); }
+}  // namespace
+
+gbz_status gbz_whir_aggregate_claims(gbz_ctx *ctx, int k, const uint64_t *const *arrays, uint64_t n, int c,
+                                     const uint64_t *points, gbz_prng *prng, uint64_t *arr, uint64_t *b_aggr,
+                                     uint64_t *K, uint64_t *challenges, uint64_t *sums, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(points, "points");
+  need(prng, "prng");
+  need(arr, "arr");
+  need(b_aggr, "b_aggr");
+  need(K, "K");
+  need(challenges, "challenges");
+  check_pow2(n, "aggregate_claims: n");
+  const int lg = ilog2(n);
+  if (lg > kMaxLogN) throw ArgError("aggregate_claims: n above 2^28");
+  if (k < 1 || c < 1 || k > 64 || c > 64) throw ArgError("aggregate_claims: 1..64 arrays and claims");
+  const VecList A = vec_views(ctx, 100, arrays, k, n, mem);
+  fe *dpts = (fe *)ctx->buf(90, 16 * (uint64_t)c * std::max(lg, 1));
+  GBZ_CUDA(cudaMemcpyAsync(dpts, points, 16 * (uint64_t)c * lg, cudaMemcpyHostToDevice, ctx->stream));
+  fe *betas = (fe *)ctx->buf(91, 16 * n * (uint64_t)c);
+  VecList Bt{};
+  for (int j = 0; j < c; j++) {
+    beta_launch(dpts + (uint64_t)j * lg, lg, betas + (uint64_t)j * n, ctx->stream);
+    Bt.p[j] = betas + (uint64_t)j * n;
+  }
+  fe *partial = (fe *)ctx->buf(92, 16 * multidot_scratch(n));
+  fe *dsums = (fe *)ctx->buf(93, 16 * (uint64_t)k * c);
+  multidot_launch(A, k, Bt, c, n, partial, dsums, ctx->stream);
+  std::vector<fe> hs((size_t)k * c);
+  GBZ_CUDA(cudaMemcpyAsync(hs.data(), dsums, 16 * hs.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  // verifier challenges: c beta weights, then k array weights (Whir.cpp:636-641)
+  glibc_prng g;
+  std::memcpy(&g, prng, sizeof(g));
+  std::vector<fe> ch(c + k);
+  for (auto &x : ch) x = prng_field(g);
+  std::memcpy(prng, &g, sizeof(g));
+  fe Kacc = fe_zero();
+  for (int i = 0; i < k; i++)
+    for (int j = 0; j < c; j++) Kacc = fadd(Kacc, fmul(fmul(ch[j], ch[c + i]), hs[(size_t)i * c + j]));
+  K[0] = Kacc.re;
+  K[1] = Kacc.im;
+  for (int i = 0; i < c + k; i++) {
+    challenges[2 * i] = ch[i].re;
+    challenges[2 * i + 1] = ch[i].im;
+  }
+  if (sums)
+    for (size_t q = 0; q < hs.size(); q++) {
+      sums[2 * q] = hs[q].re;
+      sums[2 * q + 1] = hs[q].im;
+    }
+  fe *dch = (fe *)ctx->buf(94, 16 * (uint64_t)(c + k));
+  GBZ_CUDA(cudaMemcpyAsync(dch, ch.data(), 16 * ch.size(), cudaMemcpyHostToDevice, ctx->stream));
+  fe *dba = dev_view(ctx, 95, (fe *)b_aggr, 16 * n, mem, false);
+  fe *darr = dev_view(ctx, 96, (fe *)arr, 16 * n, mem, false);
+  lincomb_launch(Bt, dch, c, n, dba, false, ctx->stream);
+  lincomb_launch(A, dch + c, k, n, darr, false, ctx->stream);
+  copy_out(ctx, (fe *)b_aggr, dba, 16 * n, mem);
+  copy_out(ctx, (fe *)arr, darr, 16 * n, mem);
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));  // ch is a host temporary
+  API_END(ctx)
+}
+
+gbz_status gbz_whir_aggregate_arrays(gbz_ctx *ctx, int k, const uint64_t *const *arrays, int nB,
+                                     const uint64_t *const *B, uint64_t n, const uint64_t *r1, const uint64_t *r2,
+                                     uint64_t *arr, uint64_t *b, uint64_t *K, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(r1, "r1");
+  need(r2, "r2");
+  need(arr, "arr");
+  need(b, "b");
+  need(K, "K");
+  if (k < 1 || nB < k || nB > 64) throw ArgError("aggregate_arrays: 1 <= k <= nB <= 64");
+  if (!n) throw ArgError("aggregate_arrays: empty arrays");
+  const VecList A = vec_views(ctx, 100, arrays, k, n, mem);
+  const VecList Bv = vec_views(ctx, 170, B, nB, n, mem);
+  fe *partial = (fe *)ctx->buf(92, 16 * multidot_scratch(n));
+  fe *dev = (fe *)ctx->buf(93, 16 * (uint64_t)k * nB);
+  multidot_launch(A, k, Bv, nB, n, partial, dev, ctx->stream);
+  std::vector<fe> ev((size_t)k * nB);
+  GBZ_CUDA(cudaMemcpyAsync(ev.data(), dev, 16 * ev.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  // arr += sum_{i>=1} r1_i arrays_i, b += sum_{i>=1} r2_i B_i (Whir.cpp:689-694)
+  std::vector<fe> coef(2 * (size_t)k);
+  for (int i = 0; i < k; i++) {
+    coef[i] = i ? host_fe(r1, i) : fe_zero();
+    coef[k + i] = i ? host_fe(r2, i) : fe_zero();
+  }
+  fe *dcoef = (fe *)ctx->buf(94, 16 * coef.size());
+  GBZ_CUDA(cudaMemcpyAsync(dcoef, coef.data(), 16 * coef.size(), cudaMemcpyHostToDevice, ctx->stream));
+  fe *darr = dev_view(ctx, 96, (fe *)arr, 16 * n, mem, true);
+  fe *db = dev_view(ctx, 95, (fe *)b, 16 * n, mem, true);
+  lincomb_launch(A, dcoef, k, n, darr, true, ctx->stream);
+  lincomb_launch(Bv, dcoef + k, k, n, db, true, ctx->stream);
+  copy_out(ctx, (fe *)arr, darr, 16 * n, mem);
+  copy_out(ctx, (fe *)b, db, 16 * n, mem);
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  fe Kacc = fe_zero();
+  for (int i = 0; i < k; i++)
+    for (int j = 0; j < nB; j++)
+      Kacc = fadd(Kacc, fmul(fmul(host_fe(r1, i), host_fe(r2, j)), ev[(size_t)i * nB + j]));
+  K[0] = Kacc.re;
+  K[1] = Kacc.im;
+  API_END(ctx)
+}
+
+gbz_status gbz_whir_aggregate_commitments(gbz_ctx *ctx, int k, const uint64_t *const *codewords, uint64_t n,
+                                          const uint64_t *r, int rate, int whir_k, gbz_prng *prng,
+                                          uint64_t *codeword, uint8_t *levels, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(r, "r");
+  need(prng, "prng");
+  need(codeword, "codeword");
+  need(levels, "levels");
+  if (k < 1 || k > 64) throw ArgError("aggregate_commitments: 1..64 codewords");
+  if (whir_k < 4 || !is_pow2((uint64_t)whir_k)) throw ArgError("aggregate_commitments: whir_k must be a power of two >= 4");
+  if (rate < 1) throw ArgError("aggregate_commitments: rate must be positive");
+  check_pow2(n, "aggregate_commitments: n");
+  if (n < (uint64_t)whir_k) throw ArgError("aggregate_commitments: codeword shorter than whir_k");
+  const VecList C = vec_views(ctx, 100, codewords, k, n, mem);
+  std::vector<fe> coef(k);
+  for (int i = 0; i < k; i++) coef[i] = host_fe(r, i);
+  fe *dcoef = (fe *)ctx->buf(94, 16 * coef.size());
+  GBZ_CUDA(cudaMemcpyAsync(dcoef, coef.data(), 16 * coef.size(), cudaMemcpyHostToDevice, ctx->stream));
+  fe *dcw = dev_view(ctx, 96, (fe *)codeword, 16 * n, mem, false);
+  lincomb_launch(C, dcoef, k, n, dcw, false, ctx->stream);
+  // query openings draw l values from rand() (Whir.cpp:574-576)
+  glibc_prng g;
+  std::memcpy(&g, prng, sizeof(g));
+  const int l = whir_query_count(rate);
+  for (int i = 0; i < l; i++) (void)prng_next(g);
+  std::memcpy(prng, &g, sizeof(g));
+  // the new tree over n / whir_k leaf hashes that the reference leaves zero (Whir.cpp:594-604)
+  const uint64_t leaves = n / whir_k, nh = 2 * leaves - 1;
+  uint8_t *dlv = dev_view(ctx, 97, levels, 32 * nh, mem, false);
+  GBZ_CUDA(cudaMemsetAsync(dlv, 0, 32 * leaves, ctx->stream));
+  merkle_from_leaves_launch(dlv, leaves, ctx->stream);
+  copy_out(ctx, (fe *)codeword, dcw, 16 * n, mem);
+  copy_out(ctx, levels, dlv, 32 * nh, mem);
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+gbz_status gbz_tensor_eval_vector(gbz_ctx *ctx, const uint32_t *point, int cols, uint64_t rows, int rate, int my_id,
+                                  uint64_t *out, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(point, "point");
+  need(out, "out");
+  check_tensor_shape(cols, rows, rate, my_id);
+  fe *dout = dev_view(ctx, 0, (fe *)out, 16 * rows, mem, false);
+  GBZ_CUDA(cudaMemsetAsync(dout, 0, 16 * rows, ctx->stream));
+  const int32_t q = (int32_t)point[1];
+  const fe c = tensor_scale(point[0], cols, my_id);
+  geometric_update(ctx, dout, rows, &q, &c, 1, ilog2(rows * (uint64_t)rate));
+  copy_out(ctx, (fe *)out, dout, 16 * rows, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_pcs_sumcheck_phase3(gbz_ctx *ctx, uint64_t *B, uint64_t rows, const uint32_t *queries, int l,
+                                   const uint64_t *s, int N, int rate, int my_id, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(B, "B");
+  need(s, "s");
+  if (l < 0) throw ArgError("phase 3: negative query count");
+  if (l && !queries) throw ArgError("null pointer: queries");
+  if (N < 2) throw ArgError("phase 3: at least two parties");
+  check_tensor_shape(N / 2, rows, rate, my_id);
+  std::vector<int32_t> q(l);
+  std::vector<fe> c(l);
+  const fe sv = fe_make(s[0], s[1]);
+  fe p = sv;
+  for (int i = 0; i < l; i++) {
+    q[i] = (int32_t)queries[2 * i + 1];
+    c[i] = fmul(p, tensor_scale(queries[2 * i], N / 2, my_id));
+    p = fmul(p, sv);
+  }
+  fe *dB = dev_view(ctx, 0, (fe *)B, 16 * rows, mem, true);
+  if (l) geometric_update(ctx, dB, rows, q.data(), c.data(), l, ilog2(rows * (uint64_t)rate));
+  copy_out(ctx, (fe *)B, dB, 16 * rows, mem);
+  finish(ctx, mem);
   API_END(ctx)
 }
 

@@ -1,0 +1,24 @@
+// Streaming kernels of the WHIR claim / commitment aggregation
+// (gbz_whir_aggr.cu).
+#pragma once
+#include <algorithm>
+
+#include "gbz_internal.cuh"
+
+namespace gbz {
+
+constexpr int kMaxVecs = 64;
+struct VecList {
+  const fe *p[kMaxVecs];
+};
+
+// out[t] = (accumulate ? out[t] : 0) + sum_{i<k} coef[i] v.p[i][t], t < n
+// (coef: k device elements).
+void lincomb_launch(const VecList &v, const fe *coef, int k, uint64_t n, fe *out, bool accumulate, cudaStream_t s);
+// out[i * kb + j] = <a_i, b_j> over n entries (device, row-major); partial
+// holds multidot_scratch(n) elements.
+uint64_t multidot_scratch(uint64_t n);
+void multidot_launch(const VecList &a, int ka, const VecList &b, int kb, uint64_t n, fe *partial, fe *out,
+                     cudaStream_t s);
+
+}  // namespace gbz

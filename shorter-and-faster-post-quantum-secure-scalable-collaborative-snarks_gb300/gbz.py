@@ -43,6 +43,8 @@ EXPORTS = (
     "gbz_encode_rows", "gbz_column_merkle", "gbz_secret_shares", "gbz_party_aggregate",
     "gbz_cosumcheck_phase1", "gbz_cosumcheck_phase2", "gbz_prove_batch", "gbz_serve", "gbz_sched_release",
     "gbz_sumcheck_round", "gbz_party_sumcheck_rounds", "gbz_party_sumcheck", "gbz_calibrate",
+    "gbz_whir_aggregate_claims", "gbz_whir_aggregate_arrays", "gbz_whir_aggregate_commitments",
+    "gbz_tensor_eval_vector", "gbz_pcs_sumcheck_phase3",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -138,6 +140,11 @@ def _load():
         "gbz_sumcheck_round": (c_int, [vp, c_int, vp, u64, vp, vp, vp, c_int]),
         "gbz_party_sumcheck_rounds": (c_int, [u64, c_int, c_int]),
         "gbz_calibrate": (c_int, [vp, vp, vp]),
+        "gbz_tensor_eval_vector": (c_int, [vp, vp, c_int, u64, c_int, c_int, vp, c_int]),
+        "gbz_pcs_sumcheck_phase3": (c_int, [vp, vp, u64, vp, c_int, vp, c_int, c_int, c_int, c_int]),
+        "gbz_whir_aggregate_claims": (c_int, [vp, c_int, vp, u64, c_int, vp, vp, vp, vp, vp, vp, vp, c_int]),
+        "gbz_whir_aggregate_arrays": (c_int, [vp, c_int, vp, c_int, vp, u64, vp, vp, vp, vp, vp, c_int]),
+        "gbz_whir_aggregate_commitments": (c_int, [vp, c_int, vp, u64, vp, c_int, c_int, vp, vp, vp, c_int]),
         "gbz_party_sumcheck": (c_int, [vp, c_int, vp, vp, vp, u64, c_int, vp, c_int, vp, vp, vp, vp, vp, vp, c_int]),
     }
     for name, (res, args) in sig.items():
@@ -393,6 +400,65 @@ class Context:
         b = ctypes.c_uint64()
         self.check(lib.gbz_sched_release(self.h, ctypes.byref(b)))
         return b.value
+
+    # ------------------------------------------------------ WHIR aggregation
+    @staticmethod
+    def _plist(vs):
+        return ctypes.cast((ctypes.c_void_p * max(len(vs), 1))(*[_ptr(v) for v in vs]), ctypes.c_void_p)
+
+    def aggregate_claims(self, arrays, points, prng=None):
+        """aggregate_claims (Whir.cpp:608): (arr, b_aggr, K, challenges, sums)."""
+        arrs = [_fe(a) for a in arrays]
+        pts = np.ascontiguousarray(points, dtype=np.uint64).reshape(len(points), -1, 2)
+        k, n, c = len(arrs), arrs[0].shape[0], pts.shape[0]
+        arr, b = fe_array(n), fe_array(n)
+        K = np.zeros(2, dtype=np.uint64)
+        ch, sums = fe_array(c + k), fe_array(k * c)
+        g = prng if isinstance(prng, Prng) else Prng(1 if prng is None else prng)
+        self.check(lib.gbz_whir_aggregate_claims(self.h, k, self._plist(arrs), n, c, _ptr(pts), ctypes.addressof(g),
+                                                 _ptr(arr), _ptr(b), _ptr(K), _ptr(ch), _ptr(sums), _mem(arrs[0])))
+        return arr, b, K, ch, sums.reshape(k, c, 2), g
+
+    def aggregate_arrays(self, arr, b, arrays, B, r1, r2):
+        """aggregate_arrays (Whir.cpp:670): returns (arr', b', K)."""
+        arr = np.array(_fe(arr), copy=True)
+        b = np.array(_fe(b), copy=True)
+        arrs, Bs = [_fe(a) for a in arrays], [_fe(x) for x in B]
+        r1 = np.ascontiguousarray(r1, dtype=np.uint64).reshape(-1, 2)
+        r2 = np.ascontiguousarray(r2, dtype=np.uint64).reshape(-1, 2)
+        K = np.zeros(2, dtype=np.uint64)
+        self.check(lib.gbz_whir_aggregate_arrays(self.h, len(arrs), self._plist(arrs), len(Bs), self._plist(Bs),
+                                                 arr.shape[0], _ptr(r1), _ptr(r2), _ptr(arr), _ptr(b), _ptr(K),
+                                                 MEM_HOST))
+        return arr, b, K
+
+    def aggregate_commitments(self, codewords, r, rate, whir_k=4, prng=None):
+        """aggregate_commitments (Whir.cpp:547): (codeword, levels, prng)."""
+        cws = [_fe(x) for x in codewords]
+        n = cws[0].shape[0]
+        r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+        cw = fe_array(n)
+        levels = np.zeros((2 * (n // whir_k) - 1, 32), dtype=np.uint8)
+        g = prng if isinstance(prng, Prng) else Prng(1 if prng is None else prng)
+        self.check(lib.gbz_whir_aggregate_commitments(self.h, len(cws), self._plist(cws), n, _ptr(r), rate, whir_k,
+                                                      ctypes.addressof(g), _ptr(cw), _ptr(levels), MEM_HOST))
+        return cw, levels, g
+
+    def tensor_eval_vector(self, point, cols, rows, rate, my_id):
+        """tensor_eval_vector (coPCS.cpp:602) for party my_id."""
+        pt = np.ascontiguousarray(point, dtype=np.uint32).reshape(2)
+        out = fe_array(rows)
+        self.check(lib.gbz_tensor_eval_vector(self.h, _ptr(pt), cols, rows, rate, my_id, _ptr(out), MEM_HOST))
+        return out
+
+    def pcs_sumcheck_phase3(self, B, queries, s, N, rate, my_id):
+        """pcs_sumcheck_phase3 (coPCS.cpp:634) on a copy of B, returned."""
+        B = np.array(_fe(B), copy=True)
+        q = np.ascontiguousarray(queries, dtype=np.uint32).reshape(-1, 2)
+        ss = np.ascontiguousarray(s, dtype=np.uint64).reshape(2)
+        self.check(lib.gbz_pcs_sumcheck_phase3(self.h, _ptr(B), B.shape[0], _ptr(q), q.shape[0], _ptr(ss), N, rate,
+                                               my_id, MEM_HOST))
+        return B
 
     # ----------------------------------------------------------- coPCS side
     def RS_multifold5(self, codeword, a):

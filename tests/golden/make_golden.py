@@ -142,7 +142,8 @@ def main():
 
 
 def gen_sumcheck():
-    """Sumcheck round forms and one-party distributed sumchecks (ref_full)."""
+    """Sumcheck round forms, one-party distributed sumchecks and the WHIR
+    aggregation functions (ref_full)."""
     out = {}
     for name, args in [
         ("zcround_6_0", ("zcround", 6, 0, 71)), ("zcround_8_2", ("zcround", 8, 2, 72)),
@@ -150,6 +151,15 @@ def gen_sumcheck():
         ("cubicsc_8_4", ("cubicsc", 8, 4, 75, 1)), ("cubicsc_10_3", ("cubicsc", 10, 3, 76, 9)),
         ("cubicsc_3_4", ("cubicsc", 3, 4, 77, 1)), ("quadsc_8_4", ("quadsc", 8, 4, 78, 1)),
         ("quadsc_11_2", ("quadsc", 11, 2, 79, 5)),
+        ("aggclaims_6_2_3", ("aggclaims", 6, 2, 3, 80, 1)), ("aggclaims_9_4_2", ("aggclaims", 9, 4, 2, 81, 7)),
+        ("aggclaims_5_1_1", ("aggclaims", 5, 1, 1, 82, 1)), ("aggarrays_6_3", ("aggarrays", 6, 3, 83)),
+        ("aggarrays_8_2", ("aggarrays", 8, 2, 84)), ("aggcommit_8_3_2_4", ("aggcommit", 8, 3, 2, 4, 85, 1)),
+        ("aggcommit_10_2_4_8", ("aggcommit", 10, 2, 4, 8, 86, 3)),
+        ("aggcommit_7_4_8_4", ("aggcommit", 7, 4, 8, 4, 87, 1)),
+        ("tensor_6_8_2_3", ("tensor", 6, 8, 2, 3, 1, 5)), ("tensor_9_16_4_0", ("tensor", 9, 16, 4, 0, 6, 300)),
+        ("tensor_4_4_8_1", ("tensor", 4, 4, 8, 1, 0, 0)), ("phase3_6_8_3_2_1", ("phase3", 6, 8, 3, 2, 1, 88)),
+        ("phase3_10_16_20_4_5", ("phase3", 10, 16, 20, 4, 5, 89)),
+        ("phase3_8_64_7_2_63", ("phase3", 8, 64, 7, 2, 63, 90)),
     ]:
         save(name + ".bin", run_full(*args))
         out[name] = {"file": name + ".bin", "args": list(args)}
