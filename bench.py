@@ -366,6 +366,164 @@ def run_party_shares(gbz, O, ctx, repeats, P=16, log_share=22, rate=2):
         "timing": "host wall clock around synchronised device calls, best of %d" % repeats}}
 
 
+def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
+    """One device-resident measurement per hot-path row outside the plain
+    prover: CUDA events on the context's stream around each C-ABI call
+    (best of 3 after a warm-up), with the algorithmic work of the call and
+    its roofline fraction (HBM bytes, or F_{p^2} multiplies / Blake3
+    compressions against the measured integer peaks).  shift divides every
+    size by 2^shift (small cases for profiler captures)."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(7)
+    P61 = (1 << 61) - 1
+
+    def rnd(n):  # canonical random field elements on the device
+        return torch.randint(0, P61, (n, 2), dtype=torch.int64, device="cuda", generator=g)
+
+    ev = []
+    for _ in range(2):
+        e = ctypes.c_void_p()
+        assert rt.cudaEventCreate(ctypes.byref(e)) == 0
+        ev.append(e)
+
+    def timed(fn):
+        fn()
+        ctx.synchronize()
+        best = 1e30
+        for _ in range(3):
+            rt.cudaEventRecord(ev[0], stream)
+            fn()
+            rt.cudaEventRecord(ev[1], stream)
+            rt.cudaEventSynchronize(ev[1])
+            x = ctypes.c_float()
+            rt.cudaEventElapsedTime(ctypes.byref(x), ev[0], ev[1])
+            best = min(best, x.value)
+        return best
+
+    rows = {}
+
+    def rec(name, ms, hbm_bytes=None, fmuls=None, comps=None, note=""):
+        r = {"ms": ms}
+        t = ms / 1e3
+        if hbm_bytes:
+            r["hbm_gbs"] = hbm_bytes / t / 1e9
+            r["hbm_frac"] = r["hbm_gbs"] / hbm_peak
+        if fmuls:
+            r["g_fmul_s"] = fmuls / t / 1e9
+            r["int_frac"] = fmuls / t / fmul_peak
+        if comps:
+            r["g_blake3_s"] = comps / t / 1e9
+            r["int_frac"] = comps / t / b3_peak
+        if note:
+            r["work"] = note
+        rows[name] = r
+
+    D = gbz.MEM_DEVICE
+    # a11: 16-party cubic distributed sumcheck over 2^24 entries (fused fold + message per round)
+    N, M = 16, 1 << (20 - shift)
+    v = [rnd(N * M) for _ in range(3)]
+    w = np.ascontiguousarray(np.random.default_rng(1).integers(0, P61, size=(N, 2), dtype=np.uint64))
+    nr = gbz.lib.gbz_party_sumcheck_rounds(M, N, 4)
+    polys, chal, fin = gbz.fe_array(4 * nr), gbz.fe_array(nr), gbz.fe_array(3)
+    fs, yy = np.zeros(2, np.uint64), np.zeros(2, np.uint64)
+
+    def party():
+        pr = gbz.Prng(1)
+        gbz.lib.gbz_party_sumcheck(ctx.h, gbz.SC_CUBIC, v[0].data_ptr(), v[1].data_ptr(), v[2].data_ptr(), M, N,
+                                   gbz._ptr(w), 4, gbz._ptr(fs), ctypes.addressof(pr), gbz._ptr(yy),
+                                   gbz._ptr(polys), gbz._ptr(chal), gbz._ptr(fin), D)  # y = 0: ECHECK, timed all the same
+    m, byts = N * M, 0
+    byts += 3 * 16 * m
+    while m >= 4:
+        byts += 3 * 16 * m + 3 * 16 * (m // 2)
+        m //= 2
+    rec("party_sumcheck_cubic_2^%d" % (24 - shift), timed(party), hbm_bytes=byts,
+        note="16 parties x 2^%d, 3 vectors" % (20 - shift))
+    del v
+    # a4: coPCS Encode, 16 rows of 2^20 at rate 2
+    R, lr = 16, 20 - shift
+    rows_in, cw = rnd(R << lr), torch.empty(((R << lr) * 2, 2), dtype=torch.int64, device="cuda")
+    enc = lambda: ctx.check(gbz.lib.gbz_encode_rows(ctx.h, rows_in.data_ptr(), R, lr, 2, 0, cw.data_ptr(), D))
+    bfly = R * ((1 << lr) // 2 * lr + (2 << lr) // 2 * (lr + 1))
+    rec("encode_rows_16x2^%d_rate2" % lr, timed(enc), fmuls=bfly, note="radix-2 butterflies of both transforms")
+    # a7: column Merkle over 32 rows of 2^20
+    lc = 20 - shift
+    cols = rnd(32 << lc)
+    lv = torch.empty(((2 << lc) - 1, 32), dtype=torch.uint8, device="cuda")
+    root = torch.empty(32, dtype=torch.uint8, device="cuda")
+    cm = lambda: ctx.check(gbz.lib.gbz_column_merkle(ctx.h, cols.data_ptr(), 32, lc, 16, lv.data_ptr(),
+                                                     root.data_ptr(), D))
+    rec("column_merkle_32x2^%d" % lc, timed(cm), comps=4 * (1 << lc) + (1 << lc) - 1,
+        note="4 compressions per column + tree over 2^20 column roots")
+    del cols, lv
+    # a15: RS_multifold5 of a 2^24 codeword by 16
+    lm = 24 - shift
+    cwb = rnd(1 << lm)
+    a16 = np.ascontiguousarray(np.random.default_rng(2).integers(0, P61, size=(16, 2), dtype=np.uint64))
+    mf = torch.empty((1 << (lm - 4), 2), dtype=torch.int64, device="cuda")
+    mfc = lambda: ctx.check(gbz.lib.gbz_rs_multifold5(ctx.h, cwb.data_ptr(), 1 << lm, gbz._ptr(a16), 4,
+                                                      mf.data_ptr(), D))
+    rec("rs_multifold5_2^%d_by16" % lm, timed(mfc), hbm_bytes=16 * (1 << lm) + 16 * (1 << (lm - 4)))
+    # a12: coSumcheck phase 2 (fold by Lagrange weights), 2^24 by 16
+    c2 = lambda: ctx.check(gbz.lib.gbz_cosumcheck_phase2(ctx.h, cwb.data_ptr(), 1 << lm, gbz._ptr(a16), 4,
+                                                         mf.data_ptr(), D))
+    rec("cosumcheck_phase2_2^%d_d16" % lm, timed(c2), hbm_bytes=16 * (1 << lm) + 16 * (1 << (lm - 4)))
+    # a12: coSumcheck phase 1, cubic, 2^22 per vector, blocks of 8
+    l1 = 22 - shift
+    p4 = [rnd(1 << l1) for _ in range(4)]
+    H = np.zeros((32, 2), dtype=np.uint64)
+    c1 = lambda: ctx.check(gbz.lib.gbz_cosumcheck_phase1(ctx.h, p4[0].data_ptr(), p4[1].data_ptr(),
+                                                         p4[2].data_ptr(), p4[3].data_ptr(), 1 << l1, 3,
+                                                         gbz._ptr(H), D))
+    nb = (1 << l1) // 8
+    rec("cosumcheck_phase1_cubic_2^%d_d8" % l1, timed(c1),
+        fmuls=4 * nb * (8 // 2 * 3 + 32 // 2 * 5) + 3 * nb * 32, note="block transforms (butterflies) + products")
+    del p4
+    # a14: packed Shamir shares, 2^22 values for 16 parties
+    ls = 22 - shift
+    sv = rnd(1 << ls)
+    sh = torch.empty((16, (1 << ls) // 4, 2), dtype=torch.int64, device="cuda")
+    ssh = lambda: ctx.check(gbz.lib.gbz_secret_shares(ctx.h, sv.data_ptr(), 1 << ls, 16, 0, 1, sh.data_ptr(), D))
+    rec("secret_shares_2^%d_N16" % ls, timed(ssh), fmuls=((1 << ls) // 4) * 16 * 8,
+        hbm_bytes=16 * (1 << ls) + 16 * 16 * ((1 << ls) // 4))
+    # a13: leader aggregation of 64 party messages of 2^16
+    msgs = rnd(64 << 16)
+    bb = np.ascontiguousarray(np.random.default_rng(3).integers(0, P61, size=(16, 2), dtype=np.uint64))
+    ao = torch.empty((1 << 16, 2), dtype=torch.int64, device="cuda")
+    ag = lambda: ctx.check(gbz.lib.gbz_party_aggregate(ctx.h, msgs.data_ptr(), 64, 1 << 16, gbz._ptr(bb),
+                                                       ao.data_ptr(), D))
+    rec("party_aggregate_64x2^16", timed(ag), hbm_bytes=16 * (65 << 16))
+    # a17: aggregate_claims, 4 arrays x 4 points of 2^22
+    la = 22 - shift
+    arrs = [rnd(1 << la) for _ in range(4)]
+    pts = np.ascontiguousarray(np.random.default_rng(4).integers(0, P61, size=(4, la, 2), dtype=np.uint64))
+    oa = torch.empty((1 << la, 2), dtype=torch.int64, device="cuda")
+    ob = torch.empty((1 << la, 2), dtype=torch.int64, device="cuda")
+    K, ch = np.zeros(2, np.uint64), gbz.fe_array(8)
+    plist = (ctypes.c_void_p * 4)(*[a.data_ptr() for a in arrs])
+
+    def aggc():
+        pr = gbz.Prng(1)
+        ctx.check(gbz.lib.gbz_whir_aggregate_claims(ctx.h, 4, ctypes.cast(plist, ctypes.c_void_p), 1 << la, 4,
+                                                    gbz._ptr(pts), ctypes.addressof(pr), oa.data_ptr(),
+                                                    ob.data_ptr(), gbz._ptr(K), gbz._ptr(ch), None, D))
+    n22 = 16 << la
+    rec("whir_aggregate_claims_4x4_2^%d" % la, timed(aggc),
+        hbm_bytes=4 * n22 + (4 + 4) * n22 + (4 + 1) * n22 + (4 + 1) * n22,
+        note="4 eq tables written, 16 inner products (one pass over 8 vectors), 2 combinations")
+    del arrs, msgs
+    # a16: pcs_sumcheck_phase3, 2^20 rows, 100 queries, 16 parties
+    lb = 20 - shift
+    Bv = rnd(1 << lb)
+    qs = np.ascontiguousarray(np.stack([np.random.default_rng(5).integers(0, 8, 100),
+                                        np.random.default_rng(6).integers(0, 2 << lb, 100)], 1).astype(np.uint32))
+    s3 = np.array([12345, 678], dtype=np.uint64)
+    ph3 = lambda: ctx.check(gbz.lib.gbz_pcs_sumcheck_phase3(ctx.h, Bv.data_ptr(), 1 << lb, gbz._ptr(qs), 100,
+                                                            gbz._ptr(s3), 16, 2, 3, D))
+    rec("pcs_phase3_2^%d_l100" % lb, timed(ph3), note="geometric update of 100 terms over 2^%d rows" % lb)
+    return {"rows": rows}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -375,6 +533,9 @@ def main():
     ap.add_argument("--logn", type=int, default=LOGN)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-many", action="store_true", help="skip the batched and served measurements")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default NTT and Merkle shapes")
+    ap.add_argument("--rows-only", action="store_true", help="only the per-row measurements (profiling)")
+    ap.add_argument("--rows-shift", type=int, default=0, help="divide the per-row sizes by 2^k")
     args = ap.parse_args()
     ws, rank, local = dist_info()
     if ws > 1:
@@ -404,6 +565,17 @@ def main():
     rt.cudaEventElapsedTime.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p]
     stream = gbz.lib.gbz_get_stream(ctx.h)
 
+    if args.rows_only:
+        fmul_peak, b3_peak = ctx.calibrate()
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                hbm = float(json.load(f)["hbm_gbs"])
+        except (OSError, KeyError, ValueError):
+            hbm = 6800.0
+        print(json.dumps(run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm, args.rows_shift)), flush=True)
+        ctx.close()
+        return
+
     # device-resident witness and transcript
     dw, dt = ctypes.c_void_p(), ctypes.c_void_p()
     ctx.check(gbz.lib.gbz_device_alloc(ctx.h, ctypes.byref(dw), w.nbytes))
@@ -420,6 +592,20 @@ def main():
             assert rt.cudaEventCreate(ctypes.byref(e)) == 0
             evs.append(e)
         return evs
+
+    # autotuning of the transform shapes and the Merkle level fusion for the
+    # lengths this proof commits to (identical results for every choice)
+    tuned = {}
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        for L in commit_lengths(logn, RATE):
+            lg = L.bit_length() - 1
+            if lg > 13:
+                sh, ms_d, ms_b = ctx.ntt_autotune(lg, reps=3)
+                tuned["ntt_2^%d" % lg] = {"shape": sh, "ms_default": ms_d, "ms_best": ms_b}
+        lgm, ms_d, ms_b = ctx.merkle_autotune((commit_lengths(logn, RATE)[0]).bit_length() - 1, reps=3)
+        tuned["merkle"] = {"log_nodes_per_cta": lgm, "ms_default": ms_d, "ms_best": ms_b}
+        tuned["seconds"] = time.perf_counter() - t0
 
     # correctness: the device transcript equals the oracle's
     prove_device()
@@ -536,8 +722,10 @@ def main():
         "int_peaks": {"fmul_per_s": fmul_peak, "blake3_per_s": b3_peak},
         "clocks": clk.summary(),
         "transcript_bytes": tbytes,
+        "autotune": tuned or None,
     }
     if rank == 0 and not args.no_many:
+        line.update(run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak))
         line.update(run_many(gbz, O, ctx, repeats=3))
         line.update(run_party_shares(gbz, O, ctx, repeats=3))
     if rank == 0 and not args.no_cpu_baseline:

@@ -417,6 +417,39 @@ int gbz_prove_launches(int logn, int rate);
  * Takes a few tens of milliseconds.  No counterpart in the reference. */
 gbz_status gbz_calibrate(gbz_ctx *ctx, double *fmul_per_s, double *blake3_per_s);
 
+/* ------------------------------------------------------------ autotuning */
+
+/* The shape of the two-pass (four-step) transforms of length 2^logn,
+ * 14 <= logn <= 28: k1 = log2 of the contiguous second pass (the first pass
+ * has length 2^(logn - k1)), 2^log_cols_a columns staged per CTA in the first
+ * pass and 2^log_rows_b rows per CTA in the second.  Every valid shape
+ * computes the same values; only speed differs.  Shapes are process-wide:
+ * change them while no transform is in flight. */
+gbz_status gbz_ntt_set_shape(int logn, int k1, int log_cols_a, int log_rows_b);
+gbz_status gbz_ntt_get_shape(int logn, int *shape);  /* shape: 3 ints */
+
+/* Times every candidate shape for 2^logn on the context's device (best of
+ * reps forward transforms each) and installs the fastest; shape (3 ints),
+ * ms_default and ms_best (optional) report the choice.  No counterpart in
+ * the reference, whose fft has a single radix-2 schedule. */
+gbz_status gbz_ntt_autotune(gbz_ctx *ctx, int logn, int reps, int *shape, double *ms_default, double *ms_best);
+
+/* Merkle level fusion: each launch computes 2^log_nodes_per_cta nodes of a
+ * level per CTA and the levels above them inside its subtree (10 or 11;
+ * process-wide; the hashes are the same either way). */
+gbz_status gbz_merkle_set_fusion(int log_nodes_per_cta);
+int gbz_merkle_get_fusion(void);
+/* Times both fusion depths on a tree over 2^logN elements and installs the
+ * faster. */
+gbz_status gbz_merkle_autotune(gbz_ctx *ctx, int logN, int reps, int *log_nodes, double *ms_default,
+                               double *ms_best);
+
+/* gbz_prove replays the proof as a captured CUDA graph (captured on first
+ * use of a witness address, at most four per shape; the seed is a graph
+ * parameter) unless disabled here, profiling is on, or the context's stream
+ * is a default stream (which cannot be captured).  Same transcript either way. */
+gbz_status gbz_set_graphs(gbz_ctx *ctx, int enable);
+
 /* ------------------------------------------------------------ profiling */
 
 /* Per-category CUDA-event timing of the kernels gbz_prove enqueues, on the

@@ -29,6 +29,7 @@ struct gbz_ctx {
   bool profiling = false;
   std::map<std::pair<int, int>, std::unique_ptr<Profiler>> profilers;
   std::unique_ptr<Scheduler> sched;
+  bool graphs = true;  // gbz_prove replays captured graphs (gbz_set_graphs)
 
   void *buf(int slot, uint64_t bytes) {
     auto &e = scratch[slot];
@@ -556,6 +557,12 @@ int gbz_prove_launches(int logn, int rate) {
   } catch (...) {
     return 0;
   }
+}
+
+gbz_status gbz_set_graphs(gbz_ctx *ctx, int enable) {
+  API_BEGIN(ctx)
+  ctx->graphs = enable != 0;
+  API_END(ctx)
 }
 
 gbz_status gbz_profile_enable(gbz_ctx *ctx, int enable) {
@@ -1114,6 +1121,138 @@ gbz_status gbz_pcs_sumcheck_phase3(gbz_ctx *ctx, uint64_t *B, uint64_t rows, con
   API_END(ctx)
 }
 
+gbz_status gbz_ntt_set_shape(int logn, int k1, int log_cols_a, int log_rows_b) {
+  try {
+    ntt_set_shape(logn, NttShape{k1, log_cols_a, log_rows_b});
+  } catch (const ArgError &) {
+    return GBZ_EINVAL;
+  }
+  return GBZ_OK;
+}
+
+gbz_status gbz_ntt_get_shape(int logn, int *shape) {
+  if (!shape) return GBZ_EINVAL;
+  const NttShape sh = ntt_get_shape(logn);
+  shape[0] = sh.k1;
+  shape[1] = sh.logBA;
+  shape[2] = sh.logBB;
+  return sh.k1 > 0 ? GBZ_OK : GBZ_EINVAL;
+}
+
+gbz_status gbz_merkle_set_fusion(int log_nodes_per_cta) {
+  try {
+    merkle_set_fusion(log_nodes_per_cta);
+  } catch (const ArgError &) {
+    return GBZ_EINVAL;
+  }
+  return GBZ_OK;
+}
+
+int gbz_merkle_get_fusion(void) { return merkle_get_fusion(); }
+
+gbz_status gbz_merkle_autotune(gbz_ctx *ctx, int logN, int reps, int *log_nodes, double *ms_default,
+                               double *ms_best) {
+  API_BEGIN(ctx)
+  if (logN < 2 || logN > kMaxLogN) throw ArgError("merkle autotune: logN out of range [2, 28]");
+  if (reps < 1) reps = 3;
+  const uint64_t N = 1ull << logN;
+  fe *elems = (fe *)ctx->buf(110, 16 * N);
+  uint8_t *lv = (uint8_t *)ctx->buf(111, 32 * merkle_hashes(N));
+  GBZ_CUDA(cudaMemsetAsync(elems, 0x11, 16 * N, ctx->stream));
+  cudaEvent_t a, b;
+  GBZ_CUDA(cudaEventCreate(&a));
+  GBZ_CUDA(cudaEventCreate(&b));
+  const int before = merkle_get_fusion();
+  double best_ms = 1e30, def_ms = 0;
+  int best = 10;
+  for (int lg : {10, 11}) {
+    merkle_set_fusion(lg);
+    merkle_commit_launch(elems, N, lv, ctx->stream);
+    double t = 1e30;
+    for (int r = 0; r < reps; r++) {
+      GBZ_CUDA(cudaEventRecord(a, ctx->stream));
+      merkle_commit_launch(elems, N, lv, ctx->stream);
+      GBZ_CUDA(cudaEventRecord(b, ctx->stream));
+      GBZ_CUDA(cudaEventSynchronize(b));
+      float ms = 0;
+      GBZ_CUDA(cudaEventElapsedTime(&ms, a, b));
+      t = std::min(t, (double)ms);
+    }
+    if (lg == 10) def_ms = t;
+    if (t < best_ms) {
+      best_ms = t;
+      best = lg;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  (void)before;
+  merkle_set_fusion(best);
+  if (log_nodes) *log_nodes = best;
+  if (ms_default) *ms_default = def_ms;
+  if (ms_best) *ms_best = best_ms;
+  API_END(ctx)
+}
+
+gbz_status gbz_ntt_autotune(gbz_ctx *ctx, int logn, int reps, int *shape, double *ms_default, double *ms_best) {
+  API_BEGIN(ctx)
+  if (logn <= 13 || logn > kMaxLogN) throw ArgError("ntt autotune: lengths 2^14 .. 2^28 (one pass below)");
+  if (reps < 1) reps = 3;
+  const uint64_t L = 1ull << logn;
+  fe *buf = (fe *)ctx->buf(110, 16 * L);
+  fe *tmp = (fe *)ctx->buf(111, 16 * L);
+  GBZ_CUDA(cudaMemsetAsync(buf, 0x11, 16 * L, ctx->stream));  // any canonical-looking data; timing only
+  const NttTables &t = ctx->tables(logn);
+  const NttShape before = ntt_get_shape(logn);
+  const NttShape dflt = ntt_default_shape(logn);
+  cudaEvent_t a, b;
+  GBZ_CUDA(cudaEventCreate(&a));
+  GBZ_CUDA(cudaEventCreate(&b));
+  auto time_shape = [&](const NttShape &sh) {
+    ntt_set_shape(logn, sh);
+    ntt_launch(t, buf, L, buf, tmp, false, ctx->stream);  // warm-up
+    double best = 1e30;
+    for (int r = 0; r < reps; r++) {
+      GBZ_CUDA(cudaEventRecord(a, ctx->stream));
+      ntt_launch(t, buf, L, buf, tmp, false, ctx->stream);
+      GBZ_CUDA(cudaEventRecord(b, ctx->stream));
+      GBZ_CUDA(cudaEventSynchronize(b));
+      float ms = 0;
+      GBZ_CUDA(cudaEventElapsedTime(&ms, a, b));
+      best = std::min(best, (double)ms);
+    }
+    return best;
+  };
+  NttShape best_sh = dflt;
+  double best_ms = 0, def_ms = 0;
+  try {
+    def_ms = best_ms = time_shape(dflt);
+    for (const NttShape &sh : ntt_shape_candidates(logn)) {
+      const double ms = time_shape(sh);
+      if (ms < best_ms * 0.98) {  // keep the default unless clearly faster
+        best_ms = ms;
+        best_sh = sh;
+      }
+    }
+  } catch (...) {
+    ntt_set_shape(logn, before);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    throw;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ntt_set_shape(logn, best_sh);
+  if (shape) {
+    shape[0] = best_sh.k1;
+    shape[1] = best_sh.logBA;
+    shape[2] = best_sh.logBB;
+  }
+  if (ms_default) *ms_default = def_ms;
+  if (ms_best) *ms_best = best_ms;
+  API_END(ctx)
+}
+
 gbz_status gbz_calibrate(gbz_ctx *ctx, double *fmul_per_s, double *blake3_per_s) {
   API_BEGIN(ctx)
   int sms = 0;
@@ -1234,7 +1373,13 @@ gbz_status gbz_prove(gbz_ctx *ctx, const uint64_t *witness, int logn, int rate, 
   } else {
     w = (const fe *)witness;
   }
-  enqueue_proof(p, w, prng_seed, ctx->stream, false);
+  // Replay a captured graph of the proof (fewer launch gaps between the
+  // many small protocol kernels); direct launches when profiling or when the
+  // stream is a default stream, which cannot be captured.
+  const bool capturable = ctx->stream != nullptr && ctx->stream != cudaStreamLegacy &&
+                          ctx->stream != cudaStreamPerThread;
+  if (!ctx->profiling && ctx->graphs && capturable) launch_proof_graph(p, w, prng_seed, ctx->stream);
+  else enqueue_proof(p, w, prng_seed, ctx->stream, false);
   GBZ_CUDA(cudaMemcpyAsync(transcript, p.transcript, p.transcript_bytes,
                            mem == GBZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, ctx->stream));
   if (mem == GBZ_MEM_HOST) {

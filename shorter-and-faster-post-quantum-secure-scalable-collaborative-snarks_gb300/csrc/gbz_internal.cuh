@@ -111,6 +111,17 @@ int ntt_launch_count(int logn);
 void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t j_valid, fe *out, uint64_t count,
                  bool inverse, cudaStream_t s);
 void ntt_tables_free(NttTables &t);
+// Four-step shape of the two-pass transforms (lengths above 2^13): pass B
+// length 2^k1 (contiguous rows), 2^logBA columns per CTA in pass A and
+// 2^logBB rows per CTA in pass B.  Every shape computes the same values.
+struct NttShape {
+  int k1 = -1, logBA = -1, logBB = -1;
+};
+NttShape ntt_default_shape(int logn);
+NttShape ntt_get_shape(int logn);
+bool ntt_shape_valid(int logn, const NttShape &sh);
+void ntt_set_shape(int logn, const NttShape &sh);  // process-wide
+std::vector<NttShape> ntt_shape_candidates(int logn);
 
 // --------------------------------------------------------------- Merkle
 // MT_commit_Blake (merkle_tree.cpp:195-233) over N elements: levels holds
@@ -119,6 +130,10 @@ void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStre
 void blake3_batch_launch(const uint8_t *in, uint8_t *out, uint64_t count, cudaStream_t s);
 inline uint64_t merkle_hashes(uint64_t N) { return N / 2 - 1; }
 int merkle_launch_count(uint64_t N);
+// Level-fusion depth of the Merkle launches: each CTA computes 2^log nodes
+// of a level and the log levels above them (log = 10 or 11; process-wide).
+void merkle_set_fusion(int log_nodes_per_cta);
+int merkle_get_fusion();
 // create_tree_blake (merkle_tree.cpp:267-299) over L leaf hashes stored at
 // levels[0 .. L): writes levels 1.. after them (2L - 1 hashes in total).
 void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s);

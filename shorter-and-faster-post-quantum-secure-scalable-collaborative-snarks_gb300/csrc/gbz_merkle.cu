@@ -21,8 +21,10 @@ namespace gbz {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kLogNodesPerCta = 10;
-constexpr int kNodesPerCta = 1 << kLogNodesPerCta;
+// Nodes of a CTA's first level: 2^10 or 2^11 (the even halves of two levels
+// in shared memory take 24 or 48 KiB).  Larger subtrees leave fewer threads
+// idle in the upper levels of a CTA; set by merkle_set_fusion.
+int g_log_nodes = 10;
 
 struct Hash {
   uint32_t w[8];
@@ -42,9 +44,11 @@ __device__ __forceinline__ void store_hash(uint8_t *p, const uint32_t w[8]) {
 
 // With elems != nullptr the first level is leaves over `elems`; otherwise
 // the first level is parents of the level stored at `child`.
+template <int LOGN>
 __global__ void __launch_bounds__(kThreads)
 merkle_levels_kernel(const fe *elems, const uint8_t *child, uint64_t cnt0, uint8_t *levels,
                      uint64_t level_off0, int nlevels) {
+  constexpr int kNodesPerCta = 1 << LOGN;
   // Only even nodes feed the level above (the right child is never read),
   // so each ping-pong buffer keeps the even half of a level.
   __shared__ Hash buf0[kNodesPerCta / 2];
@@ -115,20 +119,35 @@ __global__ void blake3_batch_kernel(const uint8_t *in, uint8_t *out, uint64_t co
     for (int b = 0; b < 4; b++) out[32 * i + 4 * k + b] = (uint8_t)(h[k] >> (8 * b));
 }
 
+void launch_levels(int logn_cta, const fe *elems, const uint8_t *child, uint64_t cnt, uint8_t *levels,
+                   uint64_t off, int nlev, cudaStream_t s) {
+  const uint64_t blocks = (cnt + (1ull << logn_cta) - 1) >> logn_cta;
+  if (logn_cta == 11)
+    merkle_levels_kernel<11><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev);
+  else
+    merkle_levels_kernel<10><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev);
+  GBZ_CUDA(cudaGetLastError());
+}
+
 }  // namespace
+
+void merkle_set_fusion(int log_nodes_per_cta) {
+  if (log_nodes_per_cta != 10 && log_nodes_per_cta != 11) throw ArgError("Merkle fusion: 10 or 11");
+  g_log_nodes = log_nodes_per_cta;
+}
+int merkle_get_fusion() { return g_log_nodes; }
 
 void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStream_t s) {
   if (N < 4 || !is_pow2(N)) throw ArgError("Merkle commitment needs a power-of-two length >= 4");
   const int depth = ilog2(N / 4);  // levels 0..depth
+  const int lg = g_log_nodes;
   uint64_t cnt = N / 4, off = 0;
   int level = 0;
   uint64_t child_off = 0;
   while (level <= depth) {
-    int nlev = min(kLogNodesPerCta + 1, depth - level + 1);
-    uint64_t blocks = (cnt + kNodesPerCta - 1) / kNodesPerCta;
-    merkle_levels_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(
-        level == 0 ? elems : nullptr, level == 0 ? nullptr : levels + 32 * child_off, cnt, levels, off, nlev);
-    GBZ_CUDA(cudaGetLastError());
+    int nlev = min(lg + 1, depth - level + 1);
+    launch_levels(lg, level == 0 ? elems : nullptr, level == 0 ? nullptr : levels + 32 * child_off, cnt, levels,
+                  off, nlev, s);
     // advance past the nlev levels just written
     for (int k = 0; k < nlev; k++) {
       child_off = off;
@@ -142,13 +161,12 @@ void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStre
 void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s) {
   if (!is_pow2(L)) throw ArgError("Merkle tree over leaves needs a power-of-two count");
   const int depth = ilog2(L);  // levels 1..depth above the leaves
+  const int lg = g_log_nodes;
   uint64_t cnt = L / 2, off = L, child_off = 0;
   int level = 1;
   while (level <= depth) {
-    const int nlev = min(kLogNodesPerCta + 1, depth - level + 1);
-    const uint64_t blocks = (cnt + kNodesPerCta - 1) / kNodesPerCta;
-    merkle_levels_kernel<<<(unsigned)blocks, kThreads, 0, s>>>(nullptr, levels + 32 * child_off, cnt, levels, off, nlev);
-    GBZ_CUDA(cudaGetLastError());
+    const int nlev = min(lg + 1, depth - level + 1);
+    launch_levels(lg, nullptr, levels + 32 * child_off, cnt, levels, off, nlev, s);
     for (int k = 0; k < nlev; k++) {
       child_off = off;
       off += cnt;
@@ -162,7 +180,7 @@ int merkle_launch_count(uint64_t N) {
   const int depth = ilog2(N / 4);
   int level = 0, k = 0;
   while (level <= depth) {
-    level += min(kLogNodesPerCta + 1, depth - level + 1);
+    level += min(g_log_nodes + 1, depth - level + 1);
     k++;
   }
   return k;

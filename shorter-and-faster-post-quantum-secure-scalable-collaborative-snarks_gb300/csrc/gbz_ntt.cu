@@ -34,6 +34,11 @@ constexpr int kMaxThreads = 1024;
 constexpr int kCtaElems = 1 << kSubLog;  // most elements staged per CTA
 constexpr int kPerThread = 8;            // elements per thread (CTA = max(32, E/8) threads)
 
+// Four-step shape per length: the pass split (k1 = log2 of the contiguous
+// pass B length) and the sub-transforms staged per CTA in each pass.  Set
+// by ntt_set_shape (the autotuner) or derived by ntt_default_shape.
+NttShape g_shape[kMaxLogN + 1];
+
 struct PassArgs {
   const fe *in;
   fe *out;
@@ -368,6 +373,52 @@ void ntt_tables_build(NttTables &t, int logn) {
 
 int ntt_launch_count(int logn) { return logn <= kSubLog ? 1 : 2; }
 
+NttShape ntt_default_shape(int logn) {
+  NttShape sh;
+  sh.k1 = (logn + 1) / 2;
+  const int k2 = logn - sh.k1;
+  // Strided pass: at least two neighbouring columns per CTA (whole 32-byte
+  // sectors) and up to 2^13 staged elements, fewer when the transform is
+  // small so that it still spreads over many CTAs.
+  sh.logBA = std::min(sh.k1, std::max(k2 < kSubLog ? 1 : 0, std::min(kSubLog, logn - 8) - k2));
+  sh.logBB = std::min(k2, std::max(0, std::min(kSubLog - 1, logn - 8) - sh.k1));
+  return sh;
+}
+
+bool ntt_shape_valid(int logn, const NttShape &sh) {
+  if (logn <= kSubLog || logn > kMaxLogN) return false;
+  const int k2 = logn - sh.k1;
+  if (sh.k1 < 1 || sh.k1 > kSubLog || k2 < 1 || k2 > kSubLog) return false;
+  if (sh.logBA < 0 || sh.logBA > sh.k1 || k2 + sh.logBA > kSubLog) return false;
+  if (sh.logBB < 0 || sh.logBB > k2 || sh.k1 + sh.logBB > kSubLog) return false;
+  return true;
+}
+
+NttShape ntt_get_shape(int logn) {
+  if (logn <= kSubLog || logn > kMaxLogN) return NttShape{};
+  return g_shape[logn].k1 > 0 ? g_shape[logn] : ntt_default_shape(logn);
+}
+
+void ntt_set_shape(int logn, const NttShape &sh) {
+  if (!ntt_shape_valid(logn, sh)) throw ArgError("ntt shape: invalid split or staging for this length");
+  g_shape[logn] = sh;
+}
+
+std::vector<NttShape> ntt_shape_candidates(int logn) {
+  std::vector<NttShape> out;
+  for (int k1 = 1; k1 <= kSubLog; k1++) {
+    const int k2 = logn - k1;
+    if (k2 < 1 || k2 > kSubLog || std::abs(k1 - k2) > 2) continue;
+    for (int a = 0; a <= std::min(k1, kSubLog - k2); a++)
+      for (int b = 0; b <= std::min(k2, kSubLog - k1); b++) {
+        NttShape sh{k1, a, b};
+        if ((a == 0 && k2 < kSubLog) || a > 4 || b > 3) continue;  // keep sector-sized column groups
+        if (ntt_shape_valid(logn, sh)) out.push_back(sh);
+      }
+  }
+  return out;
+}
+
 void ntt_tables_free(NttTables &t) {
   cudaFree(t.lo_fwd);
   cudaFree(t.hi_fwd);
@@ -406,8 +457,9 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
     launch_pass(a, 1, s);
     return;
   }
-  const int k1 = (logn + 1) / 2;  // pass B (contiguous rows)
-  const int k2 = logn - k1;       // pass A (strided columns)
+  const NttShape sh = g_shape[logn].k1 > 0 ? g_shape[logn] : ntt_default_shape(logn);
+  const int k1 = sh.k1;       // pass B (contiguous rows)
+  const int k2 = logn - k1;   // pass A (strided columns)
   const uint64_t N1 = 1ull << k1, N2 = 1ull << k2;
   // pass A: columns n1 < N1, length N2, stride N1
   a.in = in;
@@ -421,7 +473,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   // Strided pass: at least two neighbouring columns per CTA (whole 32-byte
   // sectors) and up to 2^13 staged elements, fewer when the transform is
   // small so that it still spreads over many CTAs.
-  a.logB = std::min(k1, std::max(k2 < kSubLog ? 1 : 0, std::min(kSubLog, logn - 8) - k2));
+  a.logB = sh.logBA;
   a.tw_lo = inverse ? t.lo_inv : t.lo_fwd;
   a.tw_hi = inverse ? t.hi_inv : t.hi_fwd;
   a.has_scale = 0;
@@ -439,7 +491,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   b.out_gstride = 1;
   b.out_kstride = N2;
   b.logS = k1;
-  b.logB = std::min(k2, std::max(0, std::min(kSubLog - 1, logn - 8) - k1));
+  b.logB = sh.logBB;
   b.tw_lo = nullptr;
   b.tw_hi = nullptr;
   b.has_scale = inverse;

@@ -284,6 +284,10 @@ uint64_t Layout::rec(uint32_t tag, uint32_t count, uint32_t unit) {
 
 ProofPlan::~ProofPlan() {
   if (s2) cudaStreamSynchronize(s2);
+  for (auto &g : graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+  }
   for (auto &kv : ntt) ntt_tables_free(kv.second);
   for (void *p : allocs) cudaFree(p);
   if (ev_in) cudaEventDestroy(ev_in);
@@ -593,6 +597,70 @@ __global__ void k_set_seed(ProofState *st, uint32_t seed) {
 void set_seed_launch(ProofPlan &p, uint32_t seed, cudaStream_t s) {
   k_set_seed<<<1, 32, 0, s>>>(p.st, seed);
   GBZ_CUDA(cudaGetLastError());
+}
+
+void launch_proof_graph(ProofPlan &p, const fe *w, uint32_t prng_seed, cudaStream_t s) {
+  ProofGraph *g = nullptr;
+  for (auto &e : p.graphs)
+    if (e.w == w) g = &e;
+  if (!g) {
+    constexpr size_t kMaxGraphs = 4;
+    if (p.graphs.size() >= kMaxGraphs) {  // drop the least recently used
+      size_t lru = 0;
+      for (size_t i = 1; i < p.graphs.size(); i++)
+        if (p.graphs[i].last_use < p.graphs[lru].last_use) lru = i;
+      GBZ_CUDA(cudaStreamSynchronize(s));
+      cudaGraphExecDestroy(p.graphs[lru].exec);
+      cudaGraphDestroy(p.graphs[lru].graph);
+      p.graphs.erase(p.graphs.begin() + lru);
+    }
+    ProofGraph ng;
+    ng.w = w;
+    GBZ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue_proof(p, w, prng_seed, s, false, false);
+    } catch (...) {
+      cudaGraph_t tmp = nullptr;
+      cudaStreamEndCapture(s, &tmp);
+      if (tmp) cudaGraphDestroy(tmp);
+      throw;
+    }
+    GBZ_CUDA(cudaStreamEndCapture(s, &ng.graph));
+    // the k_init node carries the seed
+    size_t count = 0;
+    GBZ_CUDA(cudaGraphGetNodes(ng.graph, nullptr, &count));
+    std::vector<cudaGraphNode_t> nodes(count);
+    GBZ_CUDA(cudaGraphGetNodes(ng.graph, nodes.data(), &count));
+    for (auto nd : nodes) {
+      cudaGraphNodeType ty;
+      GBZ_CUDA(cudaGraphNodeGetType(nd, &ty));
+      if (ty != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp{};
+      GBZ_CUDA(cudaGraphKernelNodeGetParams(nd, &kp));
+      if (kp.func == reinterpret_cast<void *>(k_init)) {
+        ng.init_node = nd;
+        ng.init_params = kp;
+        break;
+      }
+    }
+    if (!ng.init_node) {
+      cudaGraphDestroy(ng.graph);
+      throw ArgError("prover graph: initial node not found");
+    }
+    GBZ_CUDA(cudaGraphInstantiate(&ng.exec, ng.graph, 0));
+    p.graphs.push_back(ng);
+    g = &p.graphs.back();
+  }
+  g->last_use = ++p.graph_tick;
+  ProofState *st = p.st;
+  uint32_t seed_v = prng_seed;
+  int flag = 0;
+  void *args[3] = {&st, &seed_v, &flag};
+  cudaKernelNodeParams kp = g->init_params;
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  GBZ_CUDA(cudaGraphExecKernelNodeSetParams(g->exec, g->init_node, &kp));
+  GBZ_CUDA(cudaGraphLaunch(g->exec, s));
 }
 
 uint64_t plan_bytes(int logn, int rate) {

@@ -39,6 +39,17 @@ struct Profiler {
   ~Profiler();
 };
 
+// A proof captured as a CUDA graph for one witness address; the PRNG seed
+// is a parameter of the captured k_init node, updated before each launch.
+struct ProofGraph {
+  const fe *w = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t init_node = nullptr;
+  cudaKernelNodeParams init_params{};
+  uint64_t last_use = 0;
+};
+
 // Device buffers and tables for proofs of one shape (n = 2^logn, rate).
 struct ProofPlan {
   int logn = 0, rate = 0;
@@ -67,6 +78,8 @@ struct ProofPlan {
   Profiler *prof = nullptr;
   std::map<int, NttTables> ntt;
   std::vector<void *> allocs;
+  std::vector<ProofGraph> graphs;  // a few witness addresses, least recently used dropped
+  uint64_t graph_tick = 0;
 
   ProofPlan() = default;
   ProofPlan(const ProofPlan &) = delete;
@@ -84,6 +97,9 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate);
 void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry,
                    bool seed_in_state = false);
 void set_seed_launch(ProofPlan &p, uint32_t seed, cudaStream_t s);
+// Enqueues one proof of the witness at w by replaying a captured graph
+// (captured on first use of this address; s must be a capturable stream).
+void launch_proof_graph(ProofPlan &p, const fe *w, uint32_t prng_seed, cudaStream_t s);
 // Device bytes a plan of this shape allocates (an upper bound).
 uint64_t plan_bytes(int logn, int rate);
 // Reads the device-side consistency flags (synchronises s).

@@ -122,46 +122,43 @@ __global__ void __launch_bounds__(kScThreads) sc_sum_kernel(const fe *partial, i
   }
 }
 
-// precompute_beta: thread t writes B[16t .. 16t+15].  The product over the
-// index bits above the low four is formed once, then the low four bits are
-// expanded like the reference (B[2j] = B_j - B_j r_i, B[2j+1] = B_j r_i).
-// Tables of fewer than 16 entries are written by one thread.
-constexpr int kBetaLow = 4;
-__global__ void __launch_bounds__(256) beta_kernel(const fe *r, int nr, fe *B) {
-  __shared__ fe rs[64], om[64];
-  if (threadIdx.x < nr) {
-    rs[threadIdx.x] = r[threadIdx.x];
-    om[threadIdx.x] = fsub(fe_one(), r[threadIdx.x]);
+// precompute_beta, one CTA per block of 2^11 consecutive entries: thread 0
+// forms the product over the index bits from 11 up, then the CTA doubles the
+// table in shared memory from bit 10 down to bit 0 (T[2j+1] = T[j] r_i,
+// T[2j] = T[j] - T[j] r_i, one product per entry) and writes the block with
+// coalesced 16-byte stores.
+constexpr int kBetaBlockLog = 11;
+__global__ void __launch_bounds__(256) beta_block_kernel(const fe *r, int nr, fe *B) {
+  __shared__ fe T[1 << kBetaBlockLog];
+  __shared__ fe rs[64];
+  const int low = nr < kBetaBlockLog ? nr : kBetaBlockLog;
+  if ((int)threadIdx.x < nr) rs[threadIdx.x] = r[threadIdx.x];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fe pre = fe_one();
+    const uint64_t hi = (uint64_t)blockIdx.x;
+    for (int i = low; i < nr; i++) pre = fmul(pre, ((hi >> (i - low)) & 1) ? rs[i] : fsub(fe_one(), rs[i]));
+    T[0] = pre;
   }
   __syncthreads();
-  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (nr < kBetaLow) {
-    if (t) return;
-    for (uint32_t x = 0; x < (1u << nr); x++) {
-      fe e = fe_one();
-      for (int i = 0; i < nr; i++) e = fmul(e, ((x >> i) & 1) ? rs[i] : om[i]);
-      B[x] = e;
+  for (int i = low - 1; i >= 0; i--) {
+    const int len = 1 << (low - 1 - i);  // entries before this level (at most 2^10)
+    const fe ri = rs[i];
+    fe v[4];
+    int cnt = 0;
+    for (int j = threadIdx.x; j < len; j += blockDim.x) v[cnt++] = T[j];
+    __syncthreads();
+    cnt = 0;
+    for (int j = threadIdx.x; j < len; j += blockDim.x) {
+      const fe t = v[cnt++];
+      const fe x = fmul(t, ri);
+      T[2 * j + 1] = x;
+      T[2 * j] = fsub(t, x);
     }
-    return;
+    __syncthreads();
   }
-  if (t >= (1ull << (nr - kBetaLow))) return;
-  fe pre = fe_one();
-  for (int i = kBetaLow; i < nr; i++) pre = fmul(pre, ((t >> (i - kBetaLow)) & 1) ? rs[i] : om[i]);
-  fe e[1 << kBetaLow];
-  e[0] = pre;
-#pragma unroll
-  for (int i = kBetaLow - 1; i >= 0; i--) {
-    const int len = 1 << (kBetaLow - 1 - i);
-#pragma unroll
-    for (int j = len - 1; j >= 0; j--) {
-      fe x = fmul(e[j], rs[i]);
-      e[2 * j + 1] = x;
-      e[2 * j] = fsub(e[j], x);
-    }
-  }
-  fe *o = B + (t << kBetaLow);
-#pragma unroll
-  for (int j = 0; j < (1 << kBetaLow); j++) o[j] = e[j];
+  fe *o = B + ((uint64_t)blockIdx.x << low);
+  for (int j = threadIdx.x; j < (1 << low); j += blockDim.x) o[j] = T[j];
 }
 
 // update_betas: b[j] += sum_i c_i * w_i^j.  Thread tid of a CTA owns the
@@ -233,8 +230,8 @@ void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s) {
 
 void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s) {
   if (nr < 0 || nr > 60) throw ArgError("beta table: bad number of variables");
-  const uint64_t groups = nr < kBetaLow ? 1 : 1ull << (nr - kBetaLow);
-  beta_kernel<<<(unsigned)((groups + 255) / 256), 256, 0, s>>>(r, nr, B);
+  const int low = nr < kBetaBlockLog ? nr : kBetaBlockLog;
+  beta_block_kernel<<<(unsigned)(1ull << (nr - low)), 256, 0, s>>>(r, nr, B);
   GBZ_CUDA(cudaGetLastError());
 }
 

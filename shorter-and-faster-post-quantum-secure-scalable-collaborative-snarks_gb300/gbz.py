@@ -44,7 +44,9 @@ EXPORTS = (
     "gbz_cosumcheck_phase1", "gbz_cosumcheck_phase2", "gbz_prove_batch", "gbz_serve", "gbz_sched_release",
     "gbz_sumcheck_round", "gbz_party_sumcheck_rounds", "gbz_party_sumcheck", "gbz_calibrate",
     "gbz_whir_aggregate_claims", "gbz_whir_aggregate_arrays", "gbz_whir_aggregate_commitments",
-    "gbz_tensor_eval_vector", "gbz_pcs_sumcheck_phase3",
+    "gbz_tensor_eval_vector", "gbz_pcs_sumcheck_phase3", "gbz_ntt_set_shape", "gbz_ntt_get_shape",
+    "gbz_ntt_autotune", "gbz_merkle_set_fusion", "gbz_merkle_get_fusion", "gbz_merkle_autotune",
+    "gbz_set_graphs",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -140,6 +142,13 @@ def _load():
         "gbz_sumcheck_round": (c_int, [vp, c_int, vp, u64, vp, vp, vp, c_int]),
         "gbz_party_sumcheck_rounds": (c_int, [u64, c_int, c_int]),
         "gbz_calibrate": (c_int, [vp, vp, vp]),
+        "gbz_ntt_set_shape": (c_int, [c_int, c_int, c_int, c_int]),
+        "gbz_ntt_get_shape": (c_int, [c_int, vp]),
+        "gbz_ntt_autotune": (c_int, [vp, c_int, c_int, vp, vp, vp]),
+        "gbz_merkle_set_fusion": (c_int, [c_int]),
+        "gbz_set_graphs": (c_int, [vp, c_int]),
+        "gbz_merkle_get_fusion": (c_int, []),
+        "gbz_merkle_autotune": (c_int, [vp, c_int, c_int, vp, vp, vp]),
         "gbz_tensor_eval_vector": (c_int, [vp, vp, c_int, u64, c_int, c_int, vp, c_int]),
         "gbz_pcs_sumcheck_phase3": (c_int, [vp, vp, u64, vp, c_int, vp, c_int, c_int, c_int, c_int]),
         "gbz_whir_aggregate_claims": (c_int, [vp, c_int, vp, u64, c_int, vp, vp, vp, vp, vp, vp, vp, c_int]),
@@ -540,6 +549,24 @@ class Context:
         self.check(lib.gbz_calibrate(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
 
+    def ntt_autotune(self, logn, reps=3):
+        """Installs the fastest two-pass shape for 2^logn; returns
+        (shape (k1, log_cols_a, log_rows_b), ms_default, ms_best)."""
+        sh = np.zeros(3, dtype=np.int32)
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self.check(lib.gbz_ntt_autotune(self.h, logn, reps, _ptr(sh), ctypes.byref(a), ctypes.byref(b)))
+        return tuple(int(x) for x in sh), a.value, b.value
+
+    def merkle_autotune(self, logN, reps=3):
+        """Installs the faster Merkle level fusion; returns (log_nodes, ms_default, ms_best)."""
+        lg = ctypes.c_int()
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self.check(lib.gbz_merkle_autotune(self.h, logN, reps, ctypes.byref(lg), ctypes.byref(a), ctypes.byref(b)))
+        return lg.value, a.value, b.value
+
+    def set_graphs(self, on=True):
+        self.check(lib.gbz_set_graphs(self.h, int(bool(on))))
+
     def profile_enable(self, on=True):
         self.check(lib.gbz_profile_enable(self.h, int(bool(on))))
 
@@ -563,6 +590,19 @@ class Context:
         cap = out.nbytes if isinstance(out, np.ndarray) else out.numel() * out.element_size()
         self.check(lib.gbz_prove(self.h, _ptr(w), logn, rate, prng_seed, _ptr(out), cap, mem))
         return out
+
+
+def ntt_get_shape(logn):
+    sh = np.zeros(3, dtype=np.int32)
+    if lib.gbz_ntt_get_shape(logn, _ptr(sh)) != OK:
+        raise GbzError(EINVAL, "no two-pass shape for 2^%d" % logn)
+    return tuple(int(x) for x in sh)
+
+
+def ntt_set_shape(logn, k1, log_cols_a, log_rows_b):
+    st = lib.gbz_ntt_set_shape(logn, k1, log_cols_a, log_rows_b)
+    if st != OK:
+        raise GbzError(st, "invalid NTT shape")
 
 
 def prove_launches(logn, rate):

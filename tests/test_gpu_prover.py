@@ -105,3 +105,34 @@ def test_two_contexts_interleaved(gbz, oracle):
     finally:
         c1.close()
         c2.close()
+
+
+def test_prove_graph_replay_matches_direct_launches(ctx, oracle):
+    """gbz_prove replays a captured graph by default; the seed is a graph
+    parameter, so seeds and witnesses change freely between replays."""
+    w = oracle.witness(77, 1 << 13)
+    ctx.set_graphs(False)
+    try:
+        direct = [ctx.prove(w, 13, 4, s).tobytes() for s in (1, 2, 3)]
+    finally:
+        ctx.set_graphs(True)
+    replay = [ctx.prove(w, 13, 4, s).tobytes() for s in (1, 2, 3, 1)]
+    assert replay[:3] == direct
+    assert replay[3] == direct[0]
+    assert oracle.prove(w, 13, 4, 2) == direct[1]
+
+
+def test_prove_graph_per_device_address(ctx, gbz, oracle):
+    """More device witness addresses than cached graphs (least recently used
+    dropped): every transcript still equals the oracle's."""
+    torch = pytest.importorskip("torch")
+    logn, rate = 11, 2
+    ws = [oracle.witness(500 + k, 1 << logn) for k in range(6)]
+    dws = [torch.from_numpy(w.view(np.int64)).cuda() for w in ws]
+    tb = gbz.transcript_bytes(logn, rate)
+    for rep in range(2):
+        for k, dw in enumerate(dws):
+            out = torch.zeros(tb, dtype=torch.uint8, device="cuda")
+            ctx.prove(dw, logn, rate, 1 + k, out=out)
+            torch.cuda.synchronize()
+            assert out.cpu().numpy().tobytes() == oracle.prove(ws[k], logn, rate, 1 + k)
