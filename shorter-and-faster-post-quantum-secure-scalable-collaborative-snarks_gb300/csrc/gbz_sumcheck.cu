@@ -161,47 +161,109 @@ __global__ void __launch_bounds__(256) beta_block_kernel(const fe *r, int nr, fe
   for (int j = threadIdx.x; j < (1 << low); j += blockDim.x) o[j] = T[j];
 }
 
-// update_betas: b[j] += sum_i c_i * w_i^j.  Thread tid of a CTA owns the
-// kUbPer consecutive entries starting at j0 = cta*kUbSpan + tid*kUbPer; it
-// starts each query's geometric run from s_i * pw_i[tid] (s_i = c_i w_i^{cta
-// start}, pw_i[t] = w_i^{t*kUbPer}) and steps it by w_i.
+// Tables of 2^15 entries or more: a CTA writes 16 blocks of 2^11 entries.
+// The table is the tensor product of the eq table LO over the 11 low
+// variables (built once per CTA by doubling in shared memory) and the
+// products over the high variables of each block (16 threads, one block
+// each), so every output entry costs one product and the serial part of a
+// CTA is amortised over 2^15 entries.
+constexpr int kBetaChunksLog = 4;
+__global__ void __launch_bounds__(256) beta_tensor_kernel(const fe *r, int nr, fe *B) {
+  __shared__ fe T[1 << kBetaBlockLog];
+  __shared__ fe hi_pre[1 << kBetaChunksLog];
+  __shared__ fe rs[64];
+  if ((int)threadIdx.x < nr) rs[threadIdx.x] = r[threadIdx.x];
+  __syncthreads();
+  if (threadIdx.x < (1u << kBetaChunksLog)) {
+    const uint64_t c = ((uint64_t)blockIdx.x << kBetaChunksLog) + threadIdx.x;  // block of 2^11 entries
+    fe pre = fe_one();
+    for (int i = kBetaBlockLog; i < nr; i++)
+      pre = fmul(pre, ((c >> (i - kBetaBlockLog)) & 1) ? rs[i] : fsub(fe_one(), rs[i]));
+    hi_pre[threadIdx.x] = pre;
+  }
+  if (threadIdx.x == 32) T[0] = fe_one();
+  __syncthreads();
+  for (int i = kBetaBlockLog - 1; i >= 0; i--) {
+    const int len = 1 << (kBetaBlockLog - 1 - i);
+    const fe ri = rs[i];
+    fe v[4];
+    int cnt = 0;
+    for (int j = threadIdx.x; j < len; j += blockDim.x) v[cnt++] = T[j];
+    __syncthreads();
+    cnt = 0;
+    for (int j = threadIdx.x; j < len; j += blockDim.x) {
+      const fe t = v[cnt++];
+      const fe x = fmul(t, ri);
+      T[2 * j + 1] = x;
+      T[2 * j] = fsub(t, x);
+    }
+    __syncthreads();
+  }
+  fe lo[(1 << kBetaBlockLog) / 256];
+#pragma unroll
+  for (int k = 0; k < (1 << kBetaBlockLog) / 256; k++) lo[k] = T[threadIdx.x + 256 * k];
+  fe *o = B + ((uint64_t)blockIdx.x << (kBetaBlockLog + kBetaChunksLog));
+  for (int c = 0; c < (1 << kBetaChunksLog); c++) {
+    const fe h = hi_pre[c];
+#pragma unroll
+    for (int k = 0; k < (1 << kBetaBlockLog) / 256; k++)
+      o[((uint64_t)c << kBetaBlockLog) + threadIdx.x + 256 * k] = fmul(h, lo[k]);
+  }
+}
+
+// update_betas: b[j] += sum_i c_i * w_i^j.  A CTA owns kUbSpan = 256
+// consecutive entries: lane L of every warp owns the kUbPer = 8 entries
+// starting at cta0 + 8L, and warp g takes the queries i = g (mod 8), so the
+// l * 256 multiply-adds of a CTA are spread over all its threads; the eight
+// warps' partial sums are added in shared memory.  A thread starts each of
+// its queries' geometric runs from s_i * pw_i[L] (s_i = c_i w_i^{cta0},
+// pw_i[L] = w_i^{8L}) and steps it by w_i.
 constexpr int kUbThreads = 256;
+constexpr int kUbWarps = kUbThreads / 32;
 constexpr int kUbPer = 8;
-constexpr int kUbSpan = kUbThreads * kUbPer;
+constexpr int kUbSpan = 32 * kUbPer;
 
 __global__ void __launch_bounds__(kUbThreads) ub_table_kernel(const ProofState *st, int l, fe *pw) {
-  // pw[i*kUbThreads + t] = w_i^(t * kUbPer)
+  // pw[i*32 + L] = w_i^(L * kUbPer)
   const int i = blockIdx.x, t = threadIdx.x;
-  if (i >= l) return;
-  pw[i * kUbThreads + t] = fpow(st->omega_q[i], (uint64_t)t * kUbPer);
+  if (i >= l || t >= 32) return;
+  pw[i * 32 + t] = fpow(st->omega_q[i], (uint64_t)t * kUbPer);
 }
 
 __global__ void __launch_bounds__(kUbThreads)
 ub_kernel(fe *b, uint64_t nb, const ProofState *st, int l, const fe *pw) {
   __shared__ fe s_start[kMaxQueries], s_w[kMaxQueries];
+  __shared__ fe part[kUbWarps][kUbSpan];
   const uint64_t cta0 = (uint64_t)blockIdx.x * kUbSpan;
   for (int i = threadIdx.x; i < l; i += kUbThreads) {
-    fe w = st->omega_q[i];
+    const fe w = st->omega_q[i];
     s_w[i] = w;
     s_start[i] = fmul(st->comb[i], fpow(w, cta0));
   }
   __syncthreads();
-  const uint64_t j0 = cta0 + (uint64_t)threadIdx.x * kUbPer;
-  if (j0 >= nb) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   fe acc[kUbPer];
 #pragma unroll
   for (int k = 0; k < kUbPer; k++) acc[k] = fe_zero();
-  for (int i = 0; i < l; i++) {
-    fe w = s_w[i];
-    fe d = fmul(s_start[i], pw[i * kUbThreads + threadIdx.x]);
+  for (int i = warp; i < l; i += kUbWarps) {
+    const fe w = s_w[i];
+    fe d = fmul(s_start[i], pw[i * 32 + lane]);
 #pragma unroll
     for (int k = 0; k < kUbPer; k++) {
       acc[k] = fadd(acc[k], d);
       d = fmul(d, w);
     }
   }
-  const int cnt = (int)min((uint64_t)kUbPer, nb - j0);
-  for (int k = 0; k < cnt; k++) b[j0 + k] = fadd(b[j0 + k], acc[k]);
+#pragma unroll
+  for (int k = 0; k < kUbPer; k++) part[warp][lane * kUbPer + k] = acc[k];
+  __syncthreads();
+  // thread t finishes entry cta0 + t
+  const uint64_t j = cta0 + threadIdx.x;
+  if (j >= nb) return;
+  fe sum = part[0][threadIdx.x];
+#pragma unroll
+  for (int g = 1; g < kUbWarps; g++) sum = fadd(sum, part[g][threadIdx.x]);
+  b[j] = fadd(b[j], sum);
 }
 
 }  // namespace
@@ -230,6 +292,11 @@ void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s) {
 
 void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s) {
   if (nr < 0 || nr > 60) throw ArgError("beta table: bad number of variables");
+  if (nr >= kBetaBlockLog + kBetaChunksLog) {
+    beta_tensor_kernel<<<(unsigned)(1ull << (nr - kBetaBlockLog - kBetaChunksLog)), 256, 0, s>>>(r, nr, B);
+    GBZ_CUDA(cudaGetLastError());
+    return;
+  }
   const int low = nr < kBetaBlockLog ? nr : kBetaBlockLog;
   beta_block_kernel<<<(unsigned)(1ull << (nr - low)), 256, 0, s>>>(r, nr, B);
   GBZ_CUDA(cudaGetLastError());
@@ -238,7 +305,7 @@ void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s) {
 void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s) {
   if (l <= 0) return;
   if (l > kMaxQueries) throw ArgError("update_betas: too many queries");
-  ub_table_kernel<<<l, kUbThreads, 0, s>>>(st, l, pw_scratch);
+  ub_table_kernel<<<l, 32, 0, s>>>(st, l, pw_scratch);
   GBZ_CUDA(cudaGetLastError());
   ub_kernel<<<(unsigned)((nb + kUbSpan - 1) / kUbSpan), kUbThreads, 0, s>>>(b, nb, st, l, pw_scratch);
   GBZ_CUDA(cudaGetLastError());
