@@ -434,6 +434,13 @@ gbz_status gbz_ntt_get_shape(int logn, int *shape);  /* shape: 3 ints */
  * the reference, whose fft has a single radix-2 schedule. */
 gbz_status gbz_ntt_autotune(gbz_ctx *ctx, int logn, int reps, int *shape, double *ms_default, double *ms_best);
 
+/* The first pass of a two-pass transform multiplies by omega_L^(n1 k2) read
+ * from a table of L elements per (length, split, direction), built with the
+ * length's twiddles (2 L * 16 bytes of device memory, kept for the process);
+ * disabled, it forms each factor from two small tables with one more
+ * multiply.  Same values either way; process-wide. */
+void gbz_ntt_full_twiddles(int enable);
+
 /* Merkle level fusion: each launch computes 2^log_nodes_per_cta nodes of a
  * level per CTA and the levels above them inside its subtree (10 or 11;
  * process-wide; the hashes are the same either way). */

@@ -1139,6 +1139,8 @@ gbz_status gbz_ntt_get_shape(int logn, int *shape) {
   return sh.k1 > 0 ? GBZ_OK : GBZ_EINVAL;
 }
 
+void gbz_ntt_full_twiddles(int enable) { ntt_use_full_twiddles(enable != 0); }
+
 gbz_status gbz_merkle_set_fusion(int log_nodes_per_cta) {
   try {
     merkle_set_fusion(log_nodes_per_cta);
@@ -1243,6 +1245,7 @@ gbz_status gbz_ntt_autotune(gbz_ctx *ctx, int logn, int reps, int *shape, double
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   ntt_set_shape(logn, best_sh);
+  outer_table_keep_only(logn, best_sh.k1);
   if (shape) {
     shape[0] = best_sh.k1;
     shape[1] = best_sh.logBA;

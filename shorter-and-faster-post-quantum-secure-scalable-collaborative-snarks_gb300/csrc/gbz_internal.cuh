@@ -122,6 +122,11 @@ NttShape ntt_get_shape(int logn);
 bool ntt_shape_valid(int logn, const NttShape &sh);
 void ntt_set_shape(int logn, const NttShape &sh);  // process-wide
 std::vector<NttShape> ntt_shape_candidates(int logn);
+// Frees the first-pass twiddle tables of splits other than k1 (process-wide).
+void outer_table_keep_only(int logn, int k1);
+// Whether the first pass reads its twiddles from the full tables (default)
+// or forms them from the two-level tables; the values are the same.
+void ntt_use_full_twiddles(bool on);
 
 // --------------------------------------------------------------- Merkle
 // MT_commit_Blake (merkle_tree.cpp:195-233) over N elements: levels holds

@@ -21,6 +21,9 @@
 // and the inverse scale on the way out.  Groups of B >= 2 neighbouring
 // columns make the strided pass read whole 32-byte sectors.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "gbz_internal.cuh"
 
@@ -47,6 +50,7 @@ struct PassArgs {
   const fe *wh;      // omega_{2^13}^t, t < 2^12 (first half), direction-specific
   const fe *tw_lo;   // omega_L^t, t < 2^12 (nullptr: no outer twiddle)
   const fe *tw_hi;   // omega_L^{2^12 t}
+  const fe *tw_full; // pass A: omega_L^{n1 k2} at the output address n1 + N1 k2 (optional)
   fe scale;
   int logS, logB, has_scale, inverse;
   // Sparse input (pass A only): x[sp_q[i]] += sp_c[i] for i < sp_l, zero
@@ -299,12 +303,14 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
     for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
       const uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
       fe v = sm[swz((b << logS) + k)];
-      if (a.tw_lo && nonzero) {
+      const uint64_t addr = (g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride;
+      if (a.tw_full && nonzero) {
+        v = fmul(v, a.tw_full[addr]);
+      } else if (a.tw_lo && nonzero) {
         const uint64_t ex = (g0 + b) * k;
         v = fmul(v, fmul(a.tw_lo[ex & ((1u << kTwLoBits) - 1)], a.tw_hi[ex >> kTwLoBits]));
       }
       if (a.has_scale) v = fmul(v, a.scale);
-      const uint64_t addr = (g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride;
       if (!a.acc) a.out[addr] = v;
       else if (addr < a.acc_n) a.out[addr] = fadd(a.out[addr], v);
     }
@@ -345,6 +351,84 @@ void launch_pass(const PassArgs &a, uint64_t groups, cudaStream_t s) {
 
 }  // namespace
 
+// Full outer-twiddle tables of the first pass, per (device, length, split,
+// direction): T[n1 + N1 k2] = omega_L^{n1 k2}, so the pass multiplies once
+// per element instead of forming the twiddle from the two-level table.
+// The integer pipes bound the transform and HBM has room, so reading
+// 16 B per element is the cheaper side of the trade.
+std::mutex g_outer_mu;
+std::map<std::tuple<int, int, int, int>, fe *> g_outer;
+bool g_use_outer = true;  // gbz_ntt_full_twiddles
+
+// T[n1 + N1 k] = w^(n1 k) for n1 < N1, k < N2: thread (n1, chunk) walks 64
+// consecutive k from w^(n1 k0) by products with w^n1.
+__global__ void outer_table_kernel(fe w, int logL, int k1, fe *T) {
+  const uint64_t N1 = 1ull << k1, N2 = 1ull << (logL - k1);
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t chunks = (N2 + 63) / 64;
+  if (tid >= N1 * chunks) return;
+  const uint64_t n1 = tid % N1, k0 = (tid / N1) * 64;
+  const fe wn1 = fpow(w, n1);
+  fe x = fpow(wn1, k0);
+  for (uint64_t k = k0; k < k0 + 64 && k < N2; k++) {
+    T[n1 + N1 * k] = x;
+    x = fmul(x, wn1);
+  }
+}
+
+const fe *outer_table_get(int logn, int k1, bool inverse) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_outer_mu);
+  auto it = g_outer.find(std::make_tuple(dev, logn, k1, inverse ? 1 : 0));
+  return it == g_outer.end() ? nullptr : it->second;
+}
+
+void outer_table_build(int logn, int k1) {
+  if (logn <= kSubLog || k1 < 1 || k1 >= logn) return;
+  int dev = 0;
+  GBZ_CUDA(cudaGetDevice(&dev));
+  for (int dir = 0; dir < 2; dir++) {
+    const auto key = std::make_tuple(dev, logn, k1, dir);
+    {
+      std::lock_guard<std::mutex> lk(g_outer_mu);
+      if (g_outer.count(key)) continue;
+    }
+    const uint64_t L = 1ull << logn;
+    fe *T = nullptr;
+    if (cudaMalloc(&T, sizeof(fe) * L) != cudaSuccess) {
+      cudaGetLastError();  // no room: the pass keeps the two-level twiddles
+      return;
+    }
+    fe w = root_of_unity(logn);
+    if (dir) w = finv(w);
+    const uint64_t threads = (1ull << k1) * (((L >> k1) + 63) / 64);
+    outer_table_kernel<<<(unsigned)((threads + 255) / 256), 256>>>(w, logn, k1, T);
+    GBZ_CUDA(cudaGetLastError());
+    GBZ_CUDA(cudaDeviceSynchronize());
+    std::lock_guard<std::mutex> lk(g_outer_mu);
+    g_outer[key] = T;
+  }
+}
+
+// Frees the tables of other splits of this length (after autotuning).
+void outer_table_keep_only(int logn, int k1) {
+  int dev = 0;
+  GBZ_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_outer_mu);
+  for (auto it = g_outer.begin(); it != g_outer.end();) {
+    if (std::get<0>(it->first) == dev && std::get<1>(it->first) == logn && std::get<2>(it->first) != k1) {
+      GBZ_CUDA(cudaDeviceSynchronize());
+      cudaFree(it->second);
+      it = g_outer.erase(it);
+    } else {
+      ++it;
+    }
+  }
+}
+
+void ntt_use_full_twiddles(bool on) { g_use_outer = on; }
+
 void ntt_tables_build(NttTables &t, int logn) {
   ensure_wq();
   t.logn = logn;
@@ -369,6 +453,7 @@ void ntt_tables_build(NttTables &t, int logn) {
     GBZ_CUDA(cudaMemcpy(*plo, lo.data(), sizeof(fe) * nlo, cudaMemcpyHostToDevice));
     GBZ_CUDA(cudaMemcpy(*phi, hi.data(), sizeof(fe) * nhi, cudaMemcpyHostToDevice));
   }
+  if (logn > kSubLog) outer_table_build(logn, ntt_get_shape(logn).k1);
 }
 
 int ntt_launch_count(int logn) { return logn <= kSubLog ? 1 : 2; }
@@ -401,6 +486,7 @@ NttShape ntt_get_shape(int logn) {
 
 void ntt_set_shape(int logn, const NttShape &sh) {
   if (!ntt_shape_valid(logn, sh)) throw ArgError("ntt shape: invalid split or staging for this length");
+  outer_table_build(logn, sh.k1);
   g_shape[logn] = sh;
 }
 
@@ -476,6 +562,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   a.logB = sh.logBA;
   a.tw_lo = inverse ? t.lo_inv : t.lo_fwd;
   a.tw_hi = inverse ? t.hi_inv : t.hi_fwd;
+  a.tw_full = g_use_outer ? outer_table_get(logn, k1, inverse) : nullptr;
   a.has_scale = 0;
   a.sp_q = sp_q;
   a.sp_c = sp_c;
@@ -494,6 +581,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   b.logB = sh.logBB;
   b.tw_lo = nullptr;
   b.tw_hi = nullptr;
+  b.tw_full = nullptr;
   b.has_scale = inverse;
   b.sp_q = nullptr;
   b.sp_c = nullptr;

@@ -46,7 +46,7 @@ EXPORTS = (
     "gbz_whir_aggregate_claims", "gbz_whir_aggregate_arrays", "gbz_whir_aggregate_commitments",
     "gbz_tensor_eval_vector", "gbz_pcs_sumcheck_phase3", "gbz_ntt_set_shape", "gbz_ntt_get_shape",
     "gbz_ntt_autotune", "gbz_merkle_set_fusion", "gbz_merkle_get_fusion", "gbz_merkle_autotune",
-    "gbz_set_graphs",
+    "gbz_set_graphs", "gbz_ntt_full_twiddles",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -147,6 +147,7 @@ def _load():
         "gbz_ntt_autotune": (c_int, [vp, c_int, c_int, vp, vp, vp]),
         "gbz_merkle_set_fusion": (c_int, [c_int]),
         "gbz_set_graphs": (c_int, [vp, c_int]),
+        "gbz_ntt_full_twiddles": (None, [c_int]),
         "gbz_merkle_get_fusion": (c_int, []),
         "gbz_merkle_autotune": (c_int, [vp, c_int, c_int, vp, vp, vp]),
         "gbz_tensor_eval_vector": (c_int, [vp, vp, c_int, u64, c_int, c_int, vp, c_int]),

@@ -87,3 +87,18 @@ def test_merkle_autotune(ctx, gbz):
     finally:
         gbz.lib.gbz_merkle_set_fusion(saved)
     assert gbz.lib.gbz_merkle_set_fusion(12) == gbz.EINVAL
+
+
+@pytest.mark.parametrize("logn", [14, 19, 23])
+def test_full_twiddle_tables_same_transform(ctx, gbz, oracle, logn):
+    rng = np.random.default_rng(100 + logn)
+    x = rand_fe(rng, 1 << logn)
+    try:
+        gbz.lib.gbz_ntt_full_twiddles(0)
+        f0, i0 = ctx.fft(x.copy(), logn, False), ctx.fft(x.copy(), logn, True)
+    finally:
+        gbz.lib.gbz_ntt_full_twiddles(1)
+    f1, i1 = ctx.fft(x.copy(), logn, False), ctx.fft(x.copy(), logn, True)
+    assert np.array_equal(f0, f1) and np.array_equal(i0, i1)
+    if logn <= 19:
+        assert np.array_equal(f1, oracle.fft(x.copy(), False))
