@@ -193,6 +193,19 @@ gbz_status gbz_lagrange_coeff(gbz_ctx *ctx, const uint64_t *r, int logd, uint64_
 gbz_status gbz_encode_rows(gbz_ctx *ctx, const uint64_t *rows, int nrows, int logrow, int rate, int log_rate_offset,
                            uint64_t *out, int mem);
 
+/* encode_concatenated (coPCS.cpp:653-677): C' (optional, rate0 * n
+ * entries) = forward transform of data zero-padded to rate0 * n; column
+ * j < rate0 n / degree gathers C'[j + k rate0 n / degree] for k < degree,
+ * is zero-padded to degree * rate1 (<= 2^13) and transformed into row j of
+ * C (rate0 n / degree rows of degree * rate1 entries). */
+gbz_status gbz_encode_concatenated(gbz_ctx *ctx, const uint64_t *data, uint64_t n, int rate0, int rate1, int degree,
+                                   uint64_t *Cprime, uint64_t *C, int mem);
+
+/* The leader's root over {root, 0, ..., 0} of nparties commitments (the
+ * create_tree_blake of distributed_MT / commit_concatenated, coPCS.cpp:
+ * 193-201, 701-709): log2(nparties) self-hashes of root.  Host only. */
+void gbz_leader_root(const uint8_t *root, int nparties, uint8_t *out);
+
 /* One party's commitment of a batch of nrows <= 32 codeword rows of 2^logL
  * elements: per-column Blake3 roots (MT_commit_Blake over the 32-entry
  * column, missing rows zero), the tree over them (levels: 2^(logL+1) - 1

@@ -1300,3 +1300,21 @@ void orc_pcs_phase3(uint64_t *B, int64_t rows, const uint32_t *queries, int l, c
   }
   free(tmp);
 }
+
+/* encode_concatenated (coPCS.cpp:653-677): C' = forward transform of the
+ * data zero-padded to rate0 * n (L entries); column j < L/degree gathers
+ * C'[j + k L/degree] for k < degree, is zero-padded to degree * rate1 and
+ * transformed.  C: L/degree rows of degree * rate1 entries. */
+void orc_encode_concatenated(const uint64_t *data, int64_t n, int rate0, int rate1, int degree, uint64_t *Cprime,
+                             uint64_t *C) {
+  int64_t L = n * rate0, rows = L / degree, D = (int64_t)degree * rate1;
+  memset(Cprime, 0, 16 * (size_t)L);
+  memcpy(Cprime, data, 16 * (size_t)n);
+  orc_fft(Cprime, ilog2_64(L), 0, 0);
+  for (int64_t j = 0; j < rows; j++) {
+    uint64_t *row = C + 2 * j * D;
+    memset(row, 0, 16 * (size_t)D);
+    for (int k = 0; k < degree; k++) st(row, k, ld(Cprime, j + k * rows));
+    orc_fft(row, ilog2_64(D), 0, 1);
+  }
+}

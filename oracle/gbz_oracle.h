@@ -165,6 +165,11 @@ void orc_tensor_eval_vector(uint32_t p0, uint32_t p1, int cols, int64_t rows, in
 void orc_pcs_phase3(uint64_t *B, int64_t rows, const uint32_t *queries, int l, const uint64_t s[2], int N, int rate,
                     int my_id);
 
+/* encode_concatenated (coPCS.cpp:653-677): Cprime (rate0 * n), C
+ * (rate0 * n / degree rows of degree * rate1). */
+void orc_encode_concatenated(const uint64_t *data, int64_t n, int rate0, int rate1, int degree, uint64_t *Cprime,
+                             uint64_t *C);
+
 /* SplitMix64 witness generator shared by tests and bench. */
 void orc_witness(uint64_t seed, int64_t n, uint64_t *out);
 

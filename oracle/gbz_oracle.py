@@ -427,3 +427,15 @@ def pcs_phase3(B, queries, s, N, rate, my_id):
     lib().orc_pcs_phase3(_p64(B), ctypes.c_int64(B.shape[0]), ctypes.c_void_p(q.ctypes.data), ctypes.c_int(q.shape[0]), _p64(ss),
                          ctypes.c_int(N), ctypes.c_int(rate), ctypes.c_int(my_id))
     return B
+
+
+def encode_concatenated(data, rate0, rate1, degree):
+    """encode_concatenated (coPCS.cpp:653-677): (C', C rows)."""
+    data = np.ascontiguousarray(data, dtype=np.uint64).reshape(-1, 2)
+    n = data.shape[0]
+    L = n * rate0
+    Cp = fe_array(L)
+    C = np.zeros((L // degree, degree * rate1, 2), dtype=np.uint64)
+    lib().orc_encode_concatenated(_p64(data), ctypes.c_int64(n), ctypes.c_int(rate0), ctypes.c_int(rate1),
+                                  ctypes.c_int(degree), _p64(Cp), _p64(C))
+    return Cp, C

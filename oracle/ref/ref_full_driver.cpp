@@ -25,6 +25,7 @@
 //   ref_full aggcommit <logn> <k> <rate> <whir_k> <seed> <prng>  aggregate_commitments (Whir.cpp:547)
 //   ref_full tensor <logrows> <N> <rate> <my_id> <p0> <p1>         tensor_eval_vector (coPCS.cpp:602)
 //   ref_full phase3 <logrows> <N> <l> <rate> <my_id> <seed>        pcs_sumcheck_phase3 (coPCS.cpp:634)
+//   ref_full encconc <logn> <rate0> <rate1> <degree> <seed>       encode_concatenated (coPCS.cpp:653)
 #include "Distributed_Sumcheck.h"
 #include "Whir.h"
 #include "coPCS.h"
@@ -58,6 +59,8 @@ extern int my_id;                        // coPCS.cpp:19
 extern vector<vector<int>> _rates;       // New_PCS.cpp:6
 vector<F> tensor_eval_vector(vector<u32> point, int cols, int rows, int rate);
 void pcs_sumcheck_phase3(vector<F> &B, vector<vector<u32>> queries, F s, int iter, int N);
+void encode_concatenated(vector<F> &Commit_Data, vector<F> &C_prime, vector<vector<F>> &C, vector<int> rate,
+                         int degree);
 F aggregate_arrays(vector<F> &arr, vector<F> &b, vector<vector<F>> &arrays, vector<vector<F>> &B, vector<F> r1,
                    vector<F> r2);
 void compute_secret_shares(vector<F> &v, vector<vector<F>> &v_shares, int N, int k, int _k, bool privacy_preserving);
@@ -218,6 +221,16 @@ int main(int argc, char **argv) {
     _rates = {{rate}, {rate}};
     pcs_sumcheck_phase3(B, queries, s, 0, N);
     putFs(B);
+    return 0;
+  }
+  if (c == "encconc") {
+    int logn = I(2), rate0 = I(3), rate1 = I(4), degree = I(5);
+    SplitMix g(U(6));
+    vector<F> data = g.vec(1u << logn), Cp;
+    vector<vector<F>> C;
+    encode_concatenated(data, Cp, C, {rate0, rate1}, degree);
+    putFs(Cp);
+    for (auto &row : C) putFs(row);
     return 0;
   }
   if (c == "multifold5") {

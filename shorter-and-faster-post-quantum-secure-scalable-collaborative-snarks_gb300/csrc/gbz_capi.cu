@@ -650,6 +650,43 @@ gbz_status gbz_encode_rows(gbz_ctx *ctx, const uint64_t *rows, int nrows, int lo
   API_END(ctx)
 }
 
+gbz_status gbz_encode_concatenated(gbz_ctx *ctx, const uint64_t *data, uint64_t n, int rate0, int rate1, int degree,
+                                   uint64_t *Cprime, uint64_t *C, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(data, "data");
+  need(C, "C");
+  check_pow2(n, "encode_concatenated: n");
+  if (rate0 < 1 || rate1 < 1 || !is_pow2((uint64_t)rate0) || !is_pow2((uint64_t)rate1))
+    throw ArgError("encode_concatenated: rates must be powers of two");
+  if (degree < 1 || !is_pow2((uint64_t)degree)) throw ArgError("encode_concatenated: degree must be a power of two");
+  const uint64_t L = n * (uint64_t)rate0, D = (uint64_t)degree * rate1;
+  if (ilog2(L) > kMaxLogN) throw ArgError("encode_concatenated: codeword above 2^28");
+  if (D > (1u << 13)) throw ArgError("encode_concatenated: degree * rate1 above 2^13");
+  if ((uint64_t)degree > L) throw ArgError("encode_concatenated: degree above the codeword length");
+  const uint64_t rows = L / degree;
+  const fe *din = dev_view(ctx, 0, (const fe *)data, 16 * n, mem, true);
+  fe *dcp = (Cprime && mem == GBZ_MEM_DEVICE) ? (fe *)Cprime : (fe *)ctx->buf(1, 16 * L);
+  fe *tmp = (fe *)ctx->buf(2, 16 * L);
+  fe *dC = dev_view(ctx, 3, (fe *)C, 16 * rows * D, mem, false);
+  ntt_launch(ctx->tables(ilog2(L)), din, n, dcp, tmp, false, ctx->stream);
+  ntt_batched_strided(ctx->tables(ilog2(D)), dcp, rows, (uint32_t)degree, dC, rows, false, ctx->stream);
+  if (Cprime && mem == GBZ_MEM_HOST) copy_out(ctx, (fe *)Cprime, dcp, 16 * L, mem);
+  copy_out(ctx, (fe *)C, dC, 16 * rows * D, mem);
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+void gbz_leader_root(const uint8_t *root, int nparties, uint8_t *out) {
+  uint32_t h[8], m[16];
+  std::memcpy(h, root, 32);
+  for (int n = nparties; n > 1; n /= 2) {
+    for (int k = 0; k < 8; k++) m[k] = m[8 + k] = h[k];
+    blake3_block64(m, h);
+  }
+  std::memcpy(out, h, 32);
+}
+
 gbz_status gbz_column_merkle(gbz_ctx *ctx, const uint64_t *rows, int nrows, int logL, int nparties, uint8_t *levels,
                              uint8_t *root, int mem) {
   API_BEGIN(ctx)

@@ -110,6 +110,11 @@ int ntt_launch_count(int logn);
 // out[g * 2^logn + k].
 void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t j_valid, fe *out, uint64_t count,
                  bool inverse, cudaStream_t s);
+// count transforms of length 2^t.logn (<= 2^13) over columns: transform g
+// reads in[g + j * col_stride] for j < j_valid (zero beyond) and writes
+// out[g * 2^logn + k].
+void ntt_batched_strided(const NttTables &t, const fe *in, uint64_t col_stride, uint32_t j_valid, fe *out,
+                         uint64_t count, bool inverse, cudaStream_t s);
 void ntt_tables_free(NttTables &t);
 // Four-step shape of the two-pass transforms (lengths above 2^13): pass B
 // length 2^k1 (contiguous rows), 2^logBA columns per CTA in pass A and

@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
       for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
         const uint32_t b = e & ((1u << logB) - 1), j = e >> logB;
         const uint64_t addr = (g0 + b) * a.in_gstride + (uint64_t)j * a.in_jstride;
-        sm[swz((b << logS) + j)] = addr < a.n_valid ? a.in[addr] : fe_zero();
+        sm[swz((b << logS) + j)] = (addr < a.n_valid && j < a.j_valid) ? a.in[addr] : fe_zero();
       }
     }
     __syncthreads();
@@ -627,6 +627,41 @@ void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t 
   if (full < count) {  // remaining transforms one per CTA
     PassArgs r = a;
     r.in = in + full * in_stride;
+    r.out = out + (full << logS);
+    r.logB = 0;
+    launch_pass(r, count - full, s);
+  }
+}
+
+void ntt_batched_strided(const NttTables &t, const fe *in, uint64_t col_stride, uint32_t j_valid, fe *out,
+                         uint64_t count, bool inverse, cudaStream_t s) {
+  const int logS = t.logn;
+  if (logS > kSubLog) throw ArgError("batched transform longer than 2^13");
+  if (!count) return;
+  PassArgs a{};
+  a.wh = inverse ? t.sub_inv : t.sub_fwd;
+  a.scale = t.inv_len;
+  a.inverse = inverse ? 1 : 0;
+  a.in = in;
+  a.out = out;
+  a.n_valid = ~0ull;
+  a.j_valid = j_valid;
+  a.in_gstride = 1;            // transform g starts at in[g]
+  a.in_jstride = col_stride;   // its entry j at in[g + j * col_stride]
+  a.out_gstride = 1ull << logS;
+  a.out_kstride = 1;
+  a.logS = logS;
+  a.has_scale = inverse;
+  // neighbouring transforms share 32-byte sectors: stage at least two per CTA
+  int logB = std::max(0, 12 - logS);
+  while (logB > 0 && (1ull << logB) > count) logB--;
+  a.logB = logB;
+  const uint64_t B = 1ull << logB;
+  const uint64_t full = count / B * B;
+  if (full) launch_pass(a, full, s);
+  if (full < count) {
+    PassArgs r = a;
+    r.in = in + full;
     r.out = out + (full << logS);
     r.logB = 0;
     launch_pass(r, count - full, s);

@@ -46,7 +46,7 @@ EXPORTS = (
     "gbz_whir_aggregate_claims", "gbz_whir_aggregate_arrays", "gbz_whir_aggregate_commitments",
     "gbz_tensor_eval_vector", "gbz_pcs_sumcheck_phase3", "gbz_ntt_set_shape", "gbz_ntt_get_shape",
     "gbz_ntt_autotune", "gbz_merkle_set_fusion", "gbz_merkle_get_fusion", "gbz_merkle_autotune",
-    "gbz_set_graphs", "gbz_ntt_full_twiddles",
+    "gbz_set_graphs", "gbz_ntt_full_twiddles", "gbz_encode_concatenated", "gbz_leader_root",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -148,6 +148,8 @@ def _load():
         "gbz_merkle_set_fusion": (c_int, [c_int]),
         "gbz_set_graphs": (c_int, [vp, c_int]),
         "gbz_ntt_full_twiddles": (None, [c_int]),
+        "gbz_encode_concatenated": (c_int, [vp, vp, u64, c_int, c_int, c_int, vp, vp, c_int]),
+        "gbz_leader_root": (None, [vp, c_int, vp]),
         "gbz_merkle_get_fusion": (c_int, []),
         "gbz_merkle_autotune": (c_int, [vp, c_int, c_int, vp, vp, vp]),
         "gbz_tensor_eval_vector": (c_int, [vp, vp, c_int, u64, c_int, c_int, vp, c_int]),
@@ -495,6 +497,17 @@ class Context:
                                        _ptr(out), MEM_HOST))
         return out
 
+    def encode_concatenated(self, data, rate0, rate1, degree):
+        """encode_concatenated (coPCS.cpp:653): (C', C rows)."""
+        data = _fe(data)
+        n = data.shape[0]
+        L = n * rate0
+        Cp = fe_array(L)
+        C = np.zeros((L // degree, degree * rate1, 2), dtype=np.uint64)
+        self.check(lib.gbz_encode_concatenated(self.h, _ptr(data), n, rate0, rate1, degree, _ptr(Cp), _ptr(C),
+                                               MEM_HOST))
+        return Cp, C
+
     def distributed_MT(self, rows, nparties):
         """(levels (2L-1, 32), leader root (32,)) of one party's row batch."""
         rows = np.ascontiguousarray(rows, dtype=np.uint64)
@@ -604,6 +617,14 @@ def ntt_set_shape(logn, k1, log_cols_a, log_rows_b):
     st = lib.gbz_ntt_set_shape(logn, k1, log_cols_a, log_rows_b)
     if st != OK:
         raise GbzError(st, "invalid NTT shape")
+
+
+def leader_root(root, nparties):
+    """Root of create_tree_blake over {root, 0, ..., 0} of nparties."""
+    r = np.ascontiguousarray(root, dtype=np.uint8).reshape(32)
+    out = np.zeros(32, dtype=np.uint8)
+    lib.gbz_leader_root(_ptr(r), nparties, _ptr(out))
+    return out
 
 
 def prove_launches(logn, rate):

@@ -160,6 +160,8 @@ def gen_sumcheck():
         ("tensor_4_4_8_1", ("tensor", 4, 4, 8, 1, 0, 0)), ("phase3_6_8_3_2_1", ("phase3", 6, 8, 3, 2, 1, 88)),
         ("phase3_10_16_20_4_5", ("phase3", 10, 16, 20, 4, 5, 89)),
         ("phase3_8_64_7_2_63", ("phase3", 8, 64, 7, 2, 63, 90)),
+        ("encconc_8_2_2_4", ("encconc", 8, 2, 2, 4, 91)), ("encconc_10_4_2_16", ("encconc", 10, 4, 2, 16, 92)),
+        ("encconc_6_2_4_8", ("encconc", 6, 2, 4, 8, 93)),
     ]:
         save(name + ".bin", run_full(*args))
         out[name] = {"file": name + ".bin", "args": list(args)}

@@ -132,3 +132,13 @@ def test_reference_shim_compiles_against_reference_headers(gbz):
            "-I" + os.path.join(ROOT, "include"), shim]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_leader_root_matches_column_merkle(gbz, oracle):
+    """gbz_leader_root (host only) equals the leader root that the oracle's
+    distributed_MT builds over {root, 0, ..., 0}."""
+    rng = np.random.default_rng(5)
+    rows = rng.integers(0, (1 << 61) - 1, size=(3, 16, 2), dtype=np.uint64)
+    for N in (1, 2, 8, 64):
+        levels, root = oracle.column_merkle(rows, N)
+        assert np.array_equal(gbz.leader_root(levels[-1], N), root)

@@ -271,3 +271,28 @@ def test_cosumcheck_round_consistency(ctx):
         t = mul((int(x[0]), int(x[1])), (int(y[0]), int(y[1])))
         s = ((s[0] + t[0]) % P, (s[1] + t[1]) % P)
     assert s == acc
+
+
+@pytest.mark.parametrize("name", ["encconc_8_2_2_4", "encconc_10_4_2_16", "encconc_6_2_4_8"])
+def test_encode_concatenated_golden(ctx, golden, name):
+    e = golden["sumcheck"][name]
+    from conftest import golden_bytes
+    from test_oracle_copcs import Reader
+    r, (_, logn, rate0, rate1, degree, seed) = Reader(golden_bytes(e["file"])), e["args"]
+    n = 1 << logn
+    L = n * rate0
+    Cp = r.fe(L)
+    C = np.stack([r.fe(degree * rate1) for _ in range(L // degree)])
+    gCp, gC = ctx.encode_concatenated(splitmix_ext(seed, n), rate0, rate1, degree)
+    assert np.array_equal(gCp, Cp)
+    assert np.array_equal(gC, C)
+
+
+@pytest.mark.parametrize("logn,rate0,rate1,degree", [(14, 2, 2, 4), (16, 4, 4, 64), (18, 2, 8, 1024), (12, 8, 2, 4096)])
+def test_encode_concatenated_vs_oracle(ctx, oracle, logn, rate0, rate1, degree):
+    rng = np.random.default_rng(logn * 7 + degree)
+    data = rand_fe(rng, 1 << logn)
+    gCp, gC = ctx.encode_concatenated(data, rate0, rate1, degree)
+    oCp, oC = oracle.encode_concatenated(data, rate0, rate1, degree)
+    assert np.array_equal(gCp, oCp)
+    assert np.array_equal(gC, oC)

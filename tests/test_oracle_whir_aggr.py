@@ -98,3 +98,16 @@ def test_pcs_phase3(oracle, golden, name):
     B = r.fe(rows)
     r.done()
     assert np.array_equal(oracle.pcs_phase3(B0, q, s, N, rate, my_id), B)
+
+
+@pytest.mark.parametrize("name", ["encconc_8_2_2_4", "encconc_10_4_2_16", "encconc_6_2_4_8"])
+def test_encode_concatenated(oracle, golden, name):
+    r, (_, logn, rate0, rate1, degree, seed) = case(golden, name)
+    n = 1 << logn
+    L = n * rate0
+    Cp = r.fe(L)
+    C = np.stack([r.fe(degree * rate1) for _ in range(L // degree)])
+    r.done()
+    gCp, gC = oracle.encode_concatenated(splitmix_ext(seed, n), rate0, rate1, degree)
+    assert np.array_equal(gCp, Cp)
+    assert np.array_equal(gC, C)
