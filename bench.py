@@ -290,10 +290,11 @@ def run_many(gbz, O, ctx, repeats):
     keep3, st3 = transcripts(slog, srate)
     ctx.prove_batch(sws, slog, srate, sseeds, lanes=8, out=st3)  # warm plans and graphs
     served = {}
+    # plain: one proof at a time, each replayed from its graph like gbz_prove
     for name, arr, kw in [("served", arrivals, dict(lanes=8, depth=2)),
-                          ("plain", arrivals, dict(lanes=1, depth=1, graphs=False)),
+                          ("plain", arrivals, dict(lanes=1, depth=1)),
                           ("served_saturated", np.zeros(len(slog)), dict(lanes=8, depth=2)),
-                          ("plain_saturated", np.zeros(len(slog)), dict(lanes=1, depth=1, graphs=False))]:
+                          ("plain_saturated", np.zeros(len(slog)), dict(lanes=1, depth=1))]:
         _, lat, mk = ctx.serve(arr, sws, slog, srate, sseeds, out=st3, **kw)
         served[name] = {"proofs_per_s": len(slog) / mk, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                         "p99_ms": 1e3 * float(np.percentile(lat, 99))}
