@@ -36,6 +36,7 @@ constexpr int kTwLoBits = 12;        // outer twiddle table split
 constexpr int kMaxThreads = 1024;
 constexpr int kCtaElems = 1 << kSubLog;  // most elements staged per CTA
 constexpr int kPerThread = 8;            // elements per thread (CTA = max(32, E/8) threads)
+constexpr int kLoadGroup = 4;            // global loads a thread issues back to back
 
 // Four-step shape per length: the pass split (k1 = log2 of the contiguous
 // pass B length) and the sub-transforms staged per CTA in each pass.  Set
@@ -265,17 +266,41 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
     __syncthreads();
   } else {
     nonzero = 1;
+    // A thread stages at most kPerThread elements (blockDim >= total / 8);
+    // groups of kLoadGroup loads are issued before their shared-memory
+    // stores so that several global loads are in flight per thread.
     if (a.in_jstride == 1) {
-      for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
-        const uint32_t b = e >> logS, j = e & (S - 1);
-        const uint64_t addr = (g0 + b) * a.in_gstride + j;
-        sm[swz(e)] = (addr < a.n_valid && j < a.j_valid) ? a.in[addr] : fe_zero();
+      for (int i0 = 0; i0 < kPerThread; i0 += kLoadGroup) {
+        fe v[kLoadGroup];
+#pragma unroll
+        for (int i = 0; i < kLoadGroup; i++) {
+          const uint32_t e = threadIdx.x + (i0 + i) * blockDim.x;
+          const uint32_t b = e >> logS, j = e & (S - 1);
+          const uint64_t addr = (g0 + b) * a.in_gstride + j;
+          v[i] = (e < total && addr < a.n_valid && j < a.j_valid) ? a.in[addr] : fe_zero();
+        }
+#pragma unroll
+        for (int i = 0; i < kLoadGroup; i++) {
+          const uint32_t e = threadIdx.x + (i0 + i) * blockDim.x;
+          if (e < total) sm[swz(e)] = v[i];
+        }
       }
     } else {
-      for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
-        const uint32_t b = e & ((1u << logB) - 1), j = e >> logB;
-        const uint64_t addr = (g0 + b) * a.in_gstride + (uint64_t)j * a.in_jstride;
-        sm[swz((b << logS) + j)] = (addr < a.n_valid && j < a.j_valid) ? a.in[addr] : fe_zero();
+      for (int i0 = 0; i0 < kPerThread; i0 += kLoadGroup) {
+        fe v[kLoadGroup];
+#pragma unroll
+        for (int i = 0; i < kLoadGroup; i++) {
+          const uint32_t e = threadIdx.x + (i0 + i) * blockDim.x;
+          const uint32_t b = e & ((1u << logB) - 1), j = e >> logB;
+          const uint64_t addr = (g0 + b) * a.in_gstride + (uint64_t)j * a.in_jstride;
+          v[i] = (e < total && addr < a.n_valid && j < a.j_valid) ? a.in[addr] : fe_zero();
+        }
+#pragma unroll
+        for (int i = 0; i < kLoadGroup; i++) {
+          const uint32_t e = threadIdx.x + (i0 + i) * blockDim.x;
+          const uint32_t b = e & ((1u << logB) - 1), j = e >> logB;
+          if (e < total) sm[swz((b << logS) + j)] = v[i];
+        }
       }
     }
     __syncthreads();
@@ -298,6 +323,27 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
       const uint64_t addr = (g0 + b) * a.out_gstride + k;
       if (!a.acc) a.out[addr] = v;
       else if (addr < a.acc_n) a.out[addr] = fadd(a.out[addr], v);
+    }
+  } else if (a.tw_full && nonzero && !a.has_scale && !a.acc) {
+    // first pass with the full twiddle table: issue each group's table
+    // loads before its multiplies
+    for (int i0 = 0; i0 < kPerThread; i0 += kLoadGroup) {
+      fe tw[kLoadGroup];
+#pragma unroll
+      for (int i = 0; i < kLoadGroup; i++) {
+        const uint32_t e = threadIdx.x + (i0 + i) * blockDim.x;
+        const uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
+        const uint64_t addr = (g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride;
+        tw[i] = e < total ? a.tw_full[addr] : fe_zero();
+      }
+#pragma unroll
+      for (int i = 0; i < kLoadGroup; i++) {
+        const uint32_t e = threadIdx.x + (i0 + i) * blockDim.x;
+        if (e >= total) continue;
+        const uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
+        const uint64_t addr = (g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride;
+        a.out[addr] = fmul(sm[swz((b << logS) + k)], tw[i]);
+      }
     }
   } else {
     for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {

@@ -11,6 +11,8 @@
 // The fold of round i and the message of round i+1 are one pass: each
 // thread reads four consecutive entries of both vectors, writes the two
 // folded entries of each and accumulates the next message from them.
+#include <algorithm>
+
 #include "gbz_internal.cuh"
 
 namespace gbz {
@@ -167,15 +169,15 @@ __global__ void __launch_bounds__(256) beta_block_kernel(const fe *r, int nr, fe
 // products over the high variables of each block (16 threads, one block
 // each), so every output entry costs one product and the serial part of a
 // CTA is amortised over 2^15 entries.
-constexpr int kBetaChunksLog = 4;
-__global__ void __launch_bounds__(256) beta_tensor_kernel(const fe *r, int nr, fe *B) {
+constexpr int kBetaChunksLog = 4;  // at most 16 blocks of 2^11 entries per CTA
+__global__ void __launch_bounds__(256) beta_tensor_kernel(const fe *r, int nr, int chunks_log, fe *B) {
   __shared__ fe T[1 << kBetaBlockLog];
   __shared__ fe hi_pre[1 << kBetaChunksLog];
   __shared__ fe rs[64];
   if ((int)threadIdx.x < nr) rs[threadIdx.x] = r[threadIdx.x];
   __syncthreads();
-  if (threadIdx.x < (1u << kBetaChunksLog)) {
-    const uint64_t c = ((uint64_t)blockIdx.x << kBetaChunksLog) + threadIdx.x;  // block of 2^11 entries
+  if (threadIdx.x < (1u << chunks_log)) {
+    const uint64_t c = ((uint64_t)blockIdx.x << chunks_log) + threadIdx.x;  // block of 2^11 entries
     fe pre = fe_one();
     for (int i = kBetaBlockLog; i < nr; i++)
       pre = fmul(pre, ((c >> (i - kBetaBlockLog)) & 1) ? rs[i] : fsub(fe_one(), rs[i]));
@@ -202,8 +204,8 @@ __global__ void __launch_bounds__(256) beta_tensor_kernel(const fe *r, int nr, f
   fe lo[(1 << kBetaBlockLog) / 256];
 #pragma unroll
   for (int k = 0; k < (1 << kBetaBlockLog) / 256; k++) lo[k] = T[threadIdx.x + 256 * k];
-  fe *o = B + ((uint64_t)blockIdx.x << (kBetaBlockLog + kBetaChunksLog));
-  for (int c = 0; c < (1 << kBetaChunksLog); c++) {
+  fe *o = B + ((uint64_t)blockIdx.x << (kBetaBlockLog + chunks_log));
+  for (int c = 0; c < (1 << chunks_log); c++) {
     const fe h = hi_pre[c];
 #pragma unroll
     for (int k = 0; k < (1 << kBetaBlockLog) / 256; k++)
@@ -292,8 +294,10 @@ void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s) {
 
 void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s) {
   if (nr < 0 || nr > 60) throw ArgError("beta table: bad number of variables");
-  if (nr >= kBetaBlockLog + kBetaChunksLog) {
-    beta_tensor_kernel<<<(unsigned)(1ull << (nr - kBetaBlockLog - kBetaChunksLog)), 256, 0, s>>>(r, nr, B);
+  if (nr >= kBetaBlockLog + 4) {
+    // enough CTAs to cover the SMs (at least 2^9), up to 16 blocks each
+    const int chunks_log = std::max(0, std::min(kBetaChunksLog, nr - kBetaBlockLog - 9));
+    beta_tensor_kernel<<<(unsigned)(1ull << (nr - kBetaBlockLog - chunks_log)), 256, 0, s>>>(r, nr, chunks_log, B);
     GBZ_CUDA(cudaGetLastError());
     return;
   }
