@@ -45,6 +45,7 @@ struct ProofState {
   fe omega_q[kMaxQueries];    // omega_N^{q_i}
   uint32_t error;             // non-zero: a device-side consistency check failed
   uint32_t seed_in;           // PRNG seed of the next proof when it is replayed from a graph
+  fe epre;                    // prod_{k < i} eq1(z_k, chal_k): the folded eq prefix of the sumcheck
 };
 
 // Error capture for the C-ABI.
@@ -157,6 +158,13 @@ void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s);
 int sc_blocks(uint64_t pairs);
 void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2, fe *b2, bool reduce,
                     fe *partial, int blocks, cudaStream_t s);
+// The same steps for the sumcheck of sum_x w(x) eq(z, x) with the eq vector
+// kept as the shrinking table E_i of z_{i+1..}: chal == nullptr gives the
+// sums S(0), S(1) of (a, E); otherwise a is folded by *chal into a2 (m/2),
+// E2 = pairwise sums of E (m/4) and, when reduce, the sums of (a2, E2).
+// Partials are (S0, S1, 0) per block.
+void sc_eq_step_launch(const fe *a, const fe *E, uint64_t m, const fe *chal, fe *a2, fe *E2, bool reduce,
+                       fe *partial, int blocks, cudaStream_t s);
 // Round-message reduction of `blocks` partials into out[3].
 void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s);
 

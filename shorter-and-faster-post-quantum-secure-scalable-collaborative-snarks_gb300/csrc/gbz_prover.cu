@@ -36,10 +36,15 @@ __device__ __forceinline__ void put_fe(uint8_t *tr, uint64_t off, fe v) {
   p[3] = (uint32_t)(v.im >> 32);
 }
 
+// The glibc generator state is worked on in shared memory by one thread and
+// written back: its table is indexed dynamically, and hundreds of draws on
+// the global copy would each pay a memory round trip.
 __global__ void k_init(ProofState *st, uint32_t seed, int seed_in_state) {
+  __shared__ glibc_prng g;
   if (threadIdx.x) return;
   st->fs = fe_zero();
-  prng_seed(st->prng, seed_in_state ? st->seed_in : seed);
+  prng_seed(g, seed_in_state ? st->seed_in : seed);
+  st->prng = g;
   st->y = fe_zero();
   st->K = fe_zero();
   st->error = 0;
@@ -87,13 +92,24 @@ __device__ void sum_partials(const fe *partial, int blocks, fe out[3]) {
   }
 }
 
-// Sumcheck round i: message H from partials; claim check; Fiat-Shamir
-// challenge hash_to_field({H.a, H.b, H.c}); y = H(c).
-__global__ void k_sc_round(const fe *partial, int blocks, ProofState *st, int round, uint8_t *tr,
-                           int64_t off_claim, uint64_t off_poly, uint64_t off_chal) {
-  fe H[3];
-  sum_partials(partial, blocks, H);
+// Round i of the sumcheck of sum w(x) eq(z, x) from the S(0), S(1) sums:
+// H(X) = epre * eq1(z_i, X) * (S0 + X (S1 - S0)) (the reference's round
+// message of the pairs of w and the folded eq vector); claim check; the
+// Fiat-Shamir challenge hash_to_field({H.a, H.b, H.c}); y = H(c); and
+// epre *= eq1(z_i, c).
+__global__ void k_sc_round_eq(const fe *partial, int blocks, ProofState *st, int round, uint8_t *tr,
+                              int64_t off_claim, uint64_t off_poly, uint64_t off_chal) {
+  fe SS[3];
+  sum_partials(partial, blocks, SS);  // (S0, -S0-S1, S1)
   if (threadIdx.x) return;
+  if (round == 0) st->epre = fe_one();
+  const fe z = st->z[round], ep = st->epre;
+  const fe a1 = fsub(fadd(z, z), fe_one()), b1 = fsub(fe_one(), z);
+  const fe a2 = fsub(SS[2], SS[0]), b2 = SS[0];
+  fe H[3];
+  H[0] = fmul(ep, fmul(a1, a2));
+  H[1] = fmul(ep, fadd(fmul(a1, b2), fmul(b1, a2)));
+  H[2] = fmul(ep, fmul(b1, b2));
   fe h01 = fadd(quad_eval(H[0], H[1], H[2], fe_zero()), quad_eval(H[0], H[1], H[2], fe_one()));
   if (off_claim >= 0) {
     st->y = h01;
@@ -108,11 +124,13 @@ __global__ void k_sc_round(const fe *partial, int blocks, ProofState *st, int ro
   st->chal[round] = s;
   put_fe(tr, off_chal, s);
   st->y = quad_eval(H[0], H[1], H[2], s);
+  st->epre = fmul(ep, fadd(b1, fmul(a1, s)));
 }
 
 __global__ void k_sc_final(ProofState *st, const fe *v1, const fe *v2, uint8_t *tr, uint64_t off) {
   if (threadIdx.x) return;
-  fe a = v1[0], b = v2[0];
+  // v2 == nullptr: the eq vector was not folded, its last value is epre
+  fe a = v1[0], b = v2 ? v2[0] : st->epre;
   put_fe(tr, off, a);
   put_fe(tr, off + 16, b);
   st->K = a;  // Whir_Open: K = claims[0].first
@@ -131,7 +149,10 @@ __global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int 
     put_fe(tr, off_poly + 16 * k, H[k]);
     st->hw[i][k] = H[k];
   }
-  fe r = prng_field(st->prng);
+  __shared__ glibc_prng g;
+  g = st->prng;
+  fe r = prng_field(g);
+  st->prng = g;
   st->rw[i] = r;
   put_fe(tr, off_chal, r);
   st->K = quad_eval(H[0], H[1], H[2], r);
@@ -166,10 +187,13 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
   __shared__ fe rb_s;
   __shared__ fe red[kMaxQueries / 32];
   ProofState *st = a.st;
+  __shared__ glibc_prng g;
   if (threadIdx.x == 0) {
+    g = st->prng;
     const int32_t mod = (int32_t)(a.L / 4);  // whir_k <= 4 branch of whir_query
-    for (int i = 0; i < a.l; i++) q[i] = prng_next(st->prng) % mod;
-    rb_s = prng_field(st->prng);  // update_betas' F::_random(), drawn after the queries
+    for (int i = 0; i < a.l; i++) q[i] = prng_next(g) % mod;
+    rb_s = prng_field(g);  // update_betas' F::_random(), drawn after the queries
+    st->prng = g;
   }
   __syncthreads();
   const int i = threadIdx.x;
@@ -240,14 +264,17 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
 // log2|arr| F::_random draws and evaluate_vector(b, r).
 __global__ void k_final(ProofState *st, const fe *arr, fe *b, int m, uint8_t *tr, uint64_t off_poly,
                         uint64_t off_point, uint64_t off_eval) {
+  __shared__ glibc_prng g;
   if (threadIdx.x) return;
   for (int i = 0; i < m; i++) put_fe(tr, off_poly + 16 * i, arr[i]);
   const int lg = 31 - __clz(m);
   fe r[8];
+  g = st->prng;
   for (int i = 0; i < lg; i++) {
-    r[i] = prng_field(st->prng);
+    r[i] = prng_field(g);
     put_fe(tr, off_point + 16 * i, r[i]);
   }
+  st->prng = g;
   fe v[8];
   for (int i = 0; i < m; i++) v[i] = b[i];
   for (int i = 0; i < lg; i++) {
@@ -415,45 +442,50 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   // 2. evaluation point and its eq table.
   off = lay.rec(T_EVAL_POINT, logn, 16);
   RUN(PC_PROTOCOL, 1, k_point<<<1, 32, 0, s>>>(st, logn, tr, off));
-  RUN(PC_BETA, 1, beta_launch(st->z, logn, p.beta, s));
+  // eq table E_0 of z_1..z_{logn-1} (the eq factor of variable 0 is kept apart)
+  RUN(PC_BETA, 1, beta_launch(st->z + 1, logn - 1, p.vb[0], s));
 
-  // 3. sumcheck of sum w(x) eq(z, x).
+  // 3. sumcheck of sum w(x) eq(z, x): w is folded each round, the eq vector
+  //    is represented by the shrinking tables E_i (vb ping-pong) and the
+  //    prefix product epre (k_sc_round_eq).
   uint64_t off_claim = lay.rec(T_CLAIM, 1, 16);
   uint64_t m = p.n;
-  const fe *a = w, *b = p.beta;
-  int pp = 0;
+  const fe *a = w;
+  int pp = 0, ep = 0;  // va ping-pong for w, vb ping-pong for E
   for (int i = 0; i < logn; i++) {
     uint64_t off_poly = lay.rec(T_SC_POLY, 3, 16);
     uint64_t off_chal = lay.rec(T_SC_CHALLENGE, 1, 16);
     int blocks;
     if (i == 0) {
       blocks = sc_blocks(m / 2);
-      RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, nullptr, nullptr, nullptr, true, p.partial, blocks, s));
+      RUN(PC_SUMCHECK, 1, sc_eq_step_launch(a, p.vb[0], m, nullptr, nullptr, nullptr, true, p.partial, blocks, s));
     } else {
       blocks = sc_blocks(m / 4);
-      fe *a2 = p.va[pp], *b2 = p.vb[pp];
-      RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, &st->chal[i - 1], a2, b2, true, p.partial, blocks, s));
+      fe *a2 = p.va[pp];
+      RUN(PC_SUMCHECK, 1,
+          sc_eq_step_launch(a, p.vb[ep], m, &st->chal[i - 1], a2, p.vb[ep ^ 1], true, p.partial, blocks, s));
       a = a2;
-      b = b2;
       pp ^= 1;
+      ep ^= 1;
       m /= 2;
     }
     RUN(PC_PROTOCOL, 1,
-        k_sc_round<<<1, 256, 0, s>>>(p.partial, blocks, st, i, tr, i == 0 ? (int64_t)off_claim : -1, off_poly,
-                                     off_chal));
+        k_sc_round_eq<<<1, 256, 0, s>>>(p.partial, blocks, st, i, tr, i == 0 ? (int64_t)off_claim : -1, off_poly,
+                                        off_chal));
   }
   {
-    fe *a2 = p.va[pp], *b2 = p.vb[pp];
-    RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, &st->chal[logn - 1], a2, b2, false, p.partial, 1, s));
+    fe *a2 = p.va[pp];
+    RUN(PC_SUMCHECK, 1,
+        sc_eq_step_launch(a, p.vb[ep], m, &st->chal[logn - 1], a2, nullptr, false, p.partial, 1, s));
     off = lay.rec(T_SC_FINAL, 2, 16);
-    RUN(PC_PROTOCOL, 1, k_sc_final<<<1, 32, 0, s>>>(st, a2, b2, tr, off));
+    RUN(PC_PROTOCOL, 1, k_sc_final<<<1, 32, 0, s>>>(st, a2, nullptr, tr, off));
     pp ^= 1;
   }
 
   // 4. WHIR open of (v1[0], chal): b = precompute_beta(chal), arr = w.
   RUN(PC_BETA, 1, beta_launch(st->chal, logn, p.beta, s));
   a = w;
-  b = p.beta;
+  const fe *b = p.beta;
   m = p.n;
   uint64_t cur = (uint64_t)p.rate;
   // arr/b ping-pong: the first fold writes va/vb[0] (m/2), the second

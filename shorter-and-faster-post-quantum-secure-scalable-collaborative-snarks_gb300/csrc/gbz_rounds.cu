@@ -211,7 +211,10 @@ __global__ void form_finalize_kernel(const fe *partial, int blocks, int nc, Roun
   for (int k = 0; k < nc; k++) polys[(uint64_t)round * nc + k] = H[k];
   fe ch;
   if (use_prng) {
-    for (int k = 0; k < 4; k++) ch = prng_field(st->prng);
+    __shared__ glibc_prng g;  // dynamically indexed table: work on a shared copy
+    g = st->prng;
+    for (int k = 0; k < 4; k++) ch = prng_field(g);
+    st->prng = g;
   } else {
     for (int k = 0; k < nc; k++) st->fs = hash_F(st->fs, H[k]);
     ch = st->fs;

@@ -108,6 +108,64 @@ sc_fold_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t m, c
   }
 }
 
+// Sumcheck of sum_x w(x) eq(z, x) without folding the eq vector.  After i
+// rounds the folded eq vector is epre * eq1(z_i, x_0) * E_i[x'], E_i the eq
+// table of z_{i+1..} (eq1(z, x) = z x + (1 - z)(1 - x)), so the round
+// polynomial is epre * eq1(z_i, X) * S(X) with S(X) = sum_j l_j(X) E_i[j]:
+// only S(0) = sum w[2j] E_i[j] and S(1) = sum w[2j+1] E_i[j] are summed
+// over the vector (the same polynomial as the pairwise products of the
+// reference's loop, computed with half the reads and multiplies).
+// E_{i+1}[t] = E_i[2t] + E_i[2t+1].
+// partial[3 blk + {0, 1, 2}] = (S0, S1, 0).
+__global__ void __launch_bounds__(kScThreads)
+sc_eq_reduce_kernel(const fe *__restrict__ a, const fe *__restrict__ E, uint64_t pairs, fe *partial) {
+  fe S0 = fe_zero(), S1 = fe_zero(), Z = fe_zero();
+  const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
+  for (uint64_t j = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; j < pairs; j += stride) {
+    const fe e = E[j];
+    S0 = fadd(S0, fmul(a[2 * j], e));
+    S1 = fadd(S1, fmul(a[2 * j + 1], e));
+  }
+  block_sum3(S0, S1, Z);
+  if (threadIdx.x == 0) {
+    partial[3 * blockIdx.x] = S0;
+    partial[3 * blockIdx.x + 1] = S1;
+    partial[3 * blockIdx.x + 2] = fe_zero();
+  }
+}
+
+// Fold a (length m) by *chal into a2, E (length m/2) into E2 (length m/4)
+// by pairwise sums, and (reduce) the S sums of the folded pairs with E2.
+__global__ void __launch_bounds__(kScThreads)
+sc_eq_fold_kernel(const fe *__restrict__ a, uint64_t m, const fe *chal, fe *__restrict__ a2,
+                  const fe *__restrict__ E, fe *__restrict__ E2, int reduce, fe *partial) {
+  const fe r = *chal;
+  fe S0 = fe_zero(), S1 = fe_zero(), Z = fe_zero();
+  const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
+  const uint64_t quads = m / 4;
+  for (uint64_t t = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; t < quads; t += stride) {
+    const fe x0 = a[4 * t], x1 = a[4 * t + 1], x2 = a[4 * t + 2], x3 = a[4 * t + 3];
+    const fe e0 = E[2 * t], e1 = E[2 * t + 1];
+    const fe f0 = fadd(fmul(r, fsub(x1, x0)), x0), f1 = fadd(fmul(r, fsub(x3, x2)), x2);
+    a2[2 * t] = f0;
+    a2[2 * t + 1] = f1;
+    const fe e = fadd(e0, e1);
+    if (reduce) {
+      E2[t] = e;
+      S0 = fadd(S0, fmul(f0, e));
+      S1 = fadd(S1, fmul(f1, e));
+    }
+  }
+  if (m == 2 && blockIdx.x == 0 && threadIdx.x == 0) a2[0] = fadd(fmul(r, fsub(a[1], a[0])), a[0]);
+  if (!reduce) return;
+  block_sum3(S0, S1, Z);
+  if (threadIdx.x == 0) {
+    partial[3 * blockIdx.x] = S0;
+    partial[3 * blockIdx.x + 1] = S1;
+    partial[3 * blockIdx.x + 2] = fe_zero();
+  }
+}
+
 // out = (a, b, c) of the round message from (A, C, D) partials.
 __global__ void __launch_bounds__(kScThreads) sc_sum_kernel(const fe *partial, int blocks, fe *out) {
   fe A = fe_zero(), C = fe_zero(), D = fe_zero();
@@ -283,6 +341,16 @@ void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2
     sc_reduce_kernel<<<blocks, kScThreads, 0, s>>>(a, b, m / 2, partial);
   } else {
     sc_fold_kernel<<<blocks, kScThreads, 0, s>>>(a, b, m, chal, a2, b2, reduce ? 1 : 0, partial);
+  }
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void sc_eq_step_launch(const fe *a, const fe *E, uint64_t m, const fe *chal, fe *a2, fe *E2, bool reduce,
+                       fe *partial, int blocks, cudaStream_t s) {
+  if (!chal) {
+    sc_eq_reduce_kernel<<<blocks, kScThreads, 0, s>>>(a, E, m / 2, partial);
+  } else {
+    sc_eq_fold_kernel<<<blocks, kScThreads, 0, s>>>(a, m, chal, a2, E, E2, reduce ? 1 : 0, partial);
   }
   GBZ_CUDA(cudaGetLastError());
 }
