@@ -197,7 +197,6 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
   }
   __syncthreads();
   const int i = threadIdx.x;
-  const int depth = 63 - __clzll((long long)(a.L / 4));
   fe contrib = fe_zero();
   if (i < a.l) {
     const uint64_t qi = (uint64_t)q[i];
@@ -222,19 +221,7 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
     fe s = fadd(part[0], part[1]), d = fsub(part[0], part[1]);
     fe y = fmul(a.len_inv, fadd(fmul(fsub(one, r1), s), fmul(r1, fmul(po, d))));
     put_fe(a.tr, a.off_ans + 16 * i, y);
-    // open_tree_blake: sibling 2*(pos/2) + (1 - pos%2) on every level below the root
-    uint64_t pos = qi, cnt = a.L / 4, lvl = 0;
-    uint8_t *path = a.tr + a.off_path + 32ull * depth * i;
-    for (int dd = 0; dd < depth; dd++) {
-      const uint4 *src = reinterpret_cast<const uint4 *>(a.tree + 32 * (lvl + (pos ^ 1ull)));
-      uint32_t *dst = reinterpret_cast<uint32_t *>(path + 32 * dd);
-      const uint4 h0 = src[0], h1 = src[1];
-      dst[0] = h0.x; dst[1] = h0.y; dst[2] = h0.z; dst[3] = h0.w;
-      dst[4] = h1.x; dst[5] = h1.y; dst[6] = h1.z; dst[7] = h1.w;
-      lvl += cnt;
-      cnt >>= 1;
-      pos >>= 1;
-    }
+    // the authentication paths are copied by k_whir_paths (one hash per thread)
     const int32_t scaled = (int32_t)(q[i] * (int32_t)(kWhirK * a.NL / a.L));
     st->q[i] = scaled;
     st->omega_q[i] = pow_table(a.new_lo, a.new_hi, (uint64_t)(uint32_t)scaled);
@@ -262,6 +249,25 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
 
 // Final round of Whir_Open (Whir.cpp:426-446): the remaining polynomial,
 // log2|arr| F::_random draws and evaluate_vector(b, r).
+// open_tree_blake (merkle_tree.cpp:320-335) for every query: sibling
+// (pos >> d) ^ 1 of level d (levels of L/4, L/8, ... hashes stored back to
+// back, level d starting at L/2 - (L/2 >> d)), one hash per thread so that
+// all the scattered tree reads are in flight together.
+__global__ void k_whir_paths(const uint8_t *tree, uint64_t L, int l, uint8_t *tr, uint64_t off_q, uint64_t off_path) {
+  const int depth = 63 - __clzll((long long)(L / 4));
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)l * depth) return;
+  const int i = (int)(t / depth), d = (int)(t % depth);
+  const uint64_t q = (uint64_t)(uint32_t)reinterpret_cast<const int32_t *>(tr + off_q)[i];
+  const uint64_t lvl = L / 2 - ((L / 2) >> d);
+  const uint4 *src = reinterpret_cast<const uint4 *>(tree + 32 * (lvl + ((q >> d) ^ 1ull)));
+  const uint4 h0 = src[0], h1 = src[1];
+  // transcript payloads are only 4-byte aligned
+  uint32_t *dst = reinterpret_cast<uint32_t *>(tr + off_path + 32ull * ((uint64_t)depth * i + d));
+  dst[0] = h0.x; dst[1] = h0.y; dst[2] = h0.z; dst[3] = h0.w;
+  dst[4] = h1.x; dst[5] = h1.y; dst[6] = h1.z; dst[7] = h1.w;
+}
+
 __global__ void k_final(ProofState *st, const fe *arr, fe *b, int m, uint8_t *tr, uint64_t off_poly,
                         uint64_t off_point, uint64_t off_eval) {
   __shared__ glibc_prng g;
@@ -555,6 +561,12 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
       qa.len_inv = finv(fe_make(kWhirK, 0));
     }
     RUN(PC_QUERY, 1, k_whir_query<<<1, kMaxQueries, 0, s>>>(qa));
+    {
+      const uint64_t hashes = (uint64_t)l * depth;  // depth >= 2: every queried codeword has 16+ entries
+      RUN(PC_QUERY, 1,
+          k_whir_paths<<<(unsigned)((hashes + 127) / 128), 128, 0, s>>>(qa.tree, L, l, tr, qa.off_q, qa.off_path));
+      if (!dry && hashes == 0) throw ArgError("prover: empty authentication paths");
+    }
     // update_betas: b[j] += sum_i c_i omega_NL^{q_i j} is the forward
     // transform of a vector with l nonzeros.  When l * |b| exceeds a few
     // transform lengths, the sparse two-pass transform is cheaper than the
