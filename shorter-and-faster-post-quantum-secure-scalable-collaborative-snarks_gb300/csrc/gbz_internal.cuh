@@ -101,9 +101,11 @@ void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe 
 // acc[j] += sum_i c[i] * omega_L^{q[i] j} for j < nacc (L = 2^t.logn > 2^13):
 // the forward transform of the sparse vector sum_i c_i e_{q_i}, with the
 // empty columns of the first pass skipped and only the first nacc outputs
-// of the second pass accumulated.  tmp holds L elements.
+// of the second pass accumulated.  tmp holds L elements.  With q_shift > 0
+// the positions are q[i] >> q_shift (the caller guarantees the dropped bits
+// are zero, so omega_L^{q j} = omega_{L'}^{(q >> shift) j} on t of length L').
 void ntt_sparse_accumulate(const NttTables &t, const int32_t *q, const fe *c, int l, fe *acc, uint64_t nacc,
-                           fe *tmp, cudaStream_t s);
+                           fe *tmp, cudaStream_t s, int q_shift = 0);
 void ntt_tables_build(NttTables &t, int logn);
 int ntt_launch_count(int logn);
 // count independent transforms of length 2^t.logn (<= 2^13): transform g

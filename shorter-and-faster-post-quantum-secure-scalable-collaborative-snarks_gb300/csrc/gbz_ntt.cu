@@ -54,11 +54,11 @@ struct PassArgs {
   const fe *tw_full; // pass A: omega_L^{n1 k2} at the output address n1 + N1 k2 (optional)
   fe scale;
   int logS, logB, has_scale, inverse;
-  // Sparse input (pass A only): x[sp_q[i]] += sp_c[i] for i < sp_l, zero
-  // elsewhere.  Columns without an entry skip the transform.
+  // Sparse input (pass A only): x[sp_q[i] >> sp_shift] += sp_c[i] for
+  // i < sp_l, zero elsewhere.  Columns without an entry skip the transform.
   const int32_t *sp_q;
   const fe *sp_c;
-  int sp_l;
+  int sp_l, sp_shift;
   // Accumulating output: out[addr] += v for addr < acc_n, other outputs dropped.
   uint64_t acc_n;
   int acc;
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
       int nz = 0;
       const uint64_t ncol = a.in_jstride;  // column stride = number of columns
       for (int i = 0; i < a.sp_l; i++) {
-        const uint64_t q = (uint64_t)(uint32_t)a.sp_q[i];
+        const uint64_t q = (uint64_t)((uint32_t)a.sp_q[i] >> a.sp_shift);
         const uint64_t g = q & (ncol - 1);
         if (g >= g0 && g < g0 + (1u << logB)) {
           const uint32_t idx = swz((uint32_t)((g - g0) << logS) + (uint32_t)(q / ncol));
@@ -564,7 +564,7 @@ namespace {
 
 // Shared by the dense transform and the sparse/accumulating variant.
 void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
-                  const int32_t *sp_q, const fe *sp_c, int sp_l, uint64_t acc_n, cudaStream_t s) {
+                  const int32_t *sp_q, const fe *sp_c, int sp_l, int sp_shift, uint64_t acc_n, cudaStream_t s) {
   const int logn = t.logn;
   const uint64_t L = 1ull << logn;
   if (n_valid > L) n_valid = L;
@@ -613,6 +613,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   a.sp_q = sp_q;
   a.sp_c = sp_c;
   a.sp_l = sp_l;
+  a.sp_shift = sp_shift;
   launch_pass(a, N1, s);
   // pass B: rows k2 < N2, length N1, contiguous
   PassArgs b = a;
@@ -641,7 +642,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
 
 void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                 cudaStream_t s) {
-  ntt_two_pass(t, in, n_valid, out, tmp, inverse, nullptr, nullptr, 0, 0, s);
+  ntt_two_pass(t, in, n_valid, out, tmp, inverse, nullptr, nullptr, 0, 0, 0, s);
 }
 
 void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t j_valid, fe *out, uint64_t count,
@@ -715,9 +716,10 @@ void ntt_batched_strided(const NttTables &t, const fe *in, uint64_t col_stride, 
 }
 
 void ntt_sparse_accumulate(const NttTables &t, const int32_t *q, const fe *c, int l, fe *acc, uint64_t nacc,
-                           fe *tmp, cudaStream_t s) {
+                           fe *tmp, cudaStream_t s, int q_shift) {
   if (t.logn <= kSubLog) throw ArgError("sparse transform needs a two-pass length");
-  ntt_two_pass(t, nullptr, 0, acc, tmp, false, q, c, l, nacc, s);
+  if (q_shift < 0 || q_shift > 8) throw ArgError("sparse transform: position shift out of range");
+  ntt_two_pass(t, nullptr, 0, acc, tmp, false, q, c, l, q_shift, nacc, s);
 }
 
 }  // namespace gbz

@@ -389,7 +389,10 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   GBZ_CUDA(cudaMemcpy(p->transcript, img.data(), img.size(), cudaMemcpyHostToDevice));
   // Twiddle tables for every transform length the proof uses.
   p->tables(ilog2(L));
-  for (uint64_t m = n, cur = (uint64_t)rate; m > 4; m /= 4, cur *= 2) p->tables(ilog2(2 * cur * (m / 4)));
+  for (uint64_t m = n, cur = (uint64_t)rate; m > 4; m /= 4, cur *= 2) {
+    p->tables(ilog2(2 * cur * (m / 4)));
+    p->tables(ilog2(cur * (m / 4)));  // the half-length update_betas transform
+  }
   return p;
 }
 
@@ -518,6 +521,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     if (iter >= ProofPlan::kMaxIter) throw ArgError("prover: too many WHIR iterations");
     // commit arr at rate 2*cur on the commit stream, after the folds
     const uint64_t NL = 2 * cur * m;
+    if (2 * NL != L) throw ArgError("prover: WHIR codeword lengths must halve");
     const int nci = cwi ^ 1;
     off = lay.rec(T_WHIR_ROOT, 1, 32);
     if (!dry) {
@@ -571,8 +575,13 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     // transform of a vector with l nonzeros.  When l * |b| exceeds a few
     // transform lengths, the sparse two-pass transform is cheaper than the
     // direct sums.
-    if (update_betas_by_transform(l, m, NL)) {
-      RUN(PC_UPDATE_BETAS, 2, ntt_sparse_accumulate(p.tables(ilog2(NL)), st->q, st->comb, l, p.vb[1], m, p.tmp2, s));
+    // The query exponents q_i * (whir_k NL / L) are even (NL = L / 2), so
+    // omega_NL^{2 q_i j} = omega_{NL/2}^{q_i j}: the sparse transform runs
+    // at half the codeword length on the unscaled positions.
+    static_assert(kWhirK == 4, "update_betas: exponent scale 2 assumes folding by 4 with NL = L / 2");
+    if (update_betas_by_transform(l, m, NL / 2)) {
+      RUN(PC_UPDATE_BETAS, 2,
+          ntt_sparse_accumulate(p.tables(ilog2(NL) - 1), st->q, st->comb, l, p.vb[1], m, p.tmp2, s, 1));
     } else {
       RUN(PC_UPDATE_BETAS, 2, update_betas_launch(p.vb[1], m, st, l, p.ub_scratch, s));
     }
