@@ -1318,3 +1318,345 @@ void orc_encode_concatenated(const uint64_t *data, int64_t n, int rate0, int rat
     orc_fft(row, ilog2_64(D), 0, 1);
   }
 }
+
+/* ================================================ Whir_Batch_Open (a17) */
+/* Whir_Batch_Open (Whir.cpp:706-898) opens k polynomials of non-increasing
+ * sizes: the largest is folded by WHIR iterations, and whenever it reaches
+ * the size of the next ones they are merged into it (aggregate_arrays,
+ * aggregate_commitments).  bo_make_plan restates the control flow on the
+ * sizes alone: the kappa schedule of Whir.cpp:731-752 and the loop of
+ * :761-833, including the schedule read at :819-822 (whir_k =
+ * kappas[iter + 1] after iter was advanced).  Inputs on which the reference
+ * reads past its schedule or opens a Merkle leaf beyond the tree (it exits
+ * in open_tree_blake) are rejected. */
+#define BO_MAX_STEPS 64
+typedef struct {
+  int iterate, kappa;              /* a WHIR iteration folding by kappa */
+  int aggregate, group, first;     /* merge arrays first .. first+group-2 into the current one */
+  int64_t m, L;                    /* sizes when the step starts */
+  int rate;                        /* rate when the step starts */
+  int l, depth;                    /* iteration: queries, path length in the current tree */
+  int la, depth_a;                 /* aggregation: queries, path length */
+  int64_t leaves_after;            /* leaves of the tree the step leaves behind */
+} bo_exec;
+typedef struct {
+  int nsched, nexec;
+  int32_t kappa[BO_MAX_STEPS], aggr[BO_MAX_STEPS];
+  bo_exec ex[BO_MAX_STEPS];
+  int64_t m_final;
+  int64_t cw_len[64];
+  int64_t bytes;
+} bo_plan;
+
+static int is_p2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
+
+static int bo_make_plan(int k, const int64_t *sizes, int rate, int whir_k, bo_plan *P) {
+  memset(P, 0, sizeof(*P));
+  if (k < 1 || k > 64) return -1;
+  if (!(whir_k == 2 || whir_k == 4 || whir_k == 8 || whir_k == 16)) return -1;
+  if (rate < 2 || !is_p2(rate)) return -1;
+  for (int i = 0; i < k; i++) {
+    if (!is_p2(sizes[i])) return -1;
+    if (i && sizes[i] > sizes[i - 1]) return -1;
+  }
+  if (sizes[0] < 2 * whir_k || ilog2_64(sizes[0] * rate) > 28) return -1;
+  /* kappa schedule (Whir.cpp:731-752) */
+  int64_t size = sizes[0];
+  int si = 1;
+  for (;;) {
+    if (P->nsched >= BO_MAX_STEPS) return -1;
+    if (si >= k || size / whir_k > sizes[si]) {
+      P->kappa[P->nsched] = whir_k;
+      P->aggr[P->nsched++] = 0;
+      size /= whir_k;
+    } else {
+      int64_t kap = size / sizes[si];
+      int64_t s = sizes[si];
+      while (si < k && sizes[si] == s) si++;
+      P->kappa[P->nsched] = (int32_t)kap;
+      P->aggr[P->nsched++] = 1;
+      size /= kap;
+    }
+    if (size <= whir_k) break;
+  }
+  /* main loop (Whir.cpp:761-833) */
+  int64_t m = sizes[0], L = m * rate, leaves = L / 4;
+  int cur = rate, iter = 0, next = 1, wk = whir_k;
+  int64_t bytes = 8 + 8 * (int64_t)P->nsched;
+  P->cw_len[0] = L;
+  for (;;) {
+    if (iter >= P->nsched || P->nexec >= BO_MAX_STEPS) return -1;
+    bo_exec *e = &P->ex[P->nexec++];
+    wk = P->kappa[iter];
+    int ag = P->aggr[iter];
+    e->m = m;
+    e->L = L;
+    e->rate = cur;
+    if (!ag || wk != 1) {
+      int kap = wk, logk = ilog2_64(kap);
+      if (kap < 2 || m < kap) return -1;
+      int64_t qmod = kap > 4 ? L / kap : L / 4;
+      if (qmod > leaves) return -1; /* open_tree_blake would exit */
+      e->iterate = 1;
+      e->kappa = kap;
+      e->l = orc_whir_queries(cur);
+      e->depth = ilog2_64(leaves);
+      int64_t nm = m / kap, NL = 2 * (int64_t)cur * nm;
+      if (NL < 8 || e->l > 256) return -1;
+      bytes += (int64_t)logk * (8 + 48 + 8 + 16) + (8 + 32) + (8 + 4 * (int64_t)e->l) +
+               (8 + 16 * (int64_t)kap * e->l) + (8 + 16 * (int64_t)e->l) + (8 + 32 * (int64_t)e->l * e->depth) +
+               (8 + 16 * (int64_t)e->l) + (8 + 16);
+      m = nm;
+      L = NL;
+      leaves = L / 4;
+      cur *= 2;
+    }
+    iter++;
+    if (ag) {
+      int g = 1;
+      while (next + g - 1 < k && sizes[next + g - 1] == m) g++;
+      e->aggregate = 1;
+      e->group = g;
+      e->first = next;
+      for (int i = 0; i < g - 1; i++) P->cw_len[next + i] = L;
+      next += g - 1;
+      if (iter + 1 >= P->nsched) return -1; /* kappas[iter + 1] past the schedule */
+      int64_t wk2 = P->kappa[iter + 1];
+      if (next < k && m / wk2 <= sizes[next]) wk2 = m / sizes[next];
+      if (wk2 < 1 || L % wk2 || leaves != L / 4) return -1;
+      e->la = orc_whir_queries((int)(L / m));
+      e->depth_a = ilog2_64(leaves);
+      if (e->la > 256) return -1;
+      leaves = L / wk2;
+      wk = (int)wk2;
+      bytes += (8 + 32 * (int64_t)g) + (8 + 16) + (8 + 4 * (int64_t)e->la) + (8 + 32 * (int64_t)e->la * e->depth_a) +
+               (8 + 32);
+    }
+    e->leaves_after = leaves;
+    if (m <= wk) break;
+  }
+  P->m_final = m;
+  bytes += (8 + 16 * m) + (8 + 16 * (int64_t)ilog2_64(m)) + (8 + 16);
+  P->bytes = bytes;
+  return 0;
+}
+
+int orc_whir_batch_schedule(int k, const int64_t *sizes, int rate, int whir_k, int32_t *kappa, int32_t *aggr,
+                            int64_t *cw_len, int64_t *bytes) {
+  bo_plan P;
+  if (bo_make_plan(k, sizes, rate, whir_k, &P) < 0) return -1;
+  for (int i = 0; i < P.nsched; i++) {
+    if (kappa) kappa[i] = P.kappa[i];
+    if (aggr) aggr[i] = P.aggr[i];
+  }
+  for (int i = 0; i < k; i++)
+    if (cw_len) cw_len[i] = P.cw_len[i];
+  if (bytes) *bytes = P.bytes;
+  return P.nsched;
+}
+
+/* open_tree_blake (merkle_tree.cpp:320-335) over a tree of `leaves` leaf hashes. */
+static void bo_open(const uint8_t *levels, int64_t leaves, int64_t pos, uint8_t *out) {
+  const uint8_t *lv = levels;
+  int64_t cnt = leaves;
+  int d = 0;
+  while (cnt > 1) {
+    memcpy(out + 32 * d, lv + 32 * (pos ^ 1), 32);
+    d++;
+    lv += 32 * cnt;
+    cnt /= 2;
+    pos /= 2;
+  }
+}
+
+/* The transcript of the batch opening: SCHEDULE, then per executed step the
+ * WHIR iteration records (as in orc_prove, with kappa replies per query)
+ * and/or the aggregation records AGGR_CHALLENGES (the draws of Whir.cpp:809-814
+ * after the [0] = 1 overrides), AGGR_K (aggregate_arrays), AGGR_QUERIES and
+ * AGGR_PATHS (the openings of aggregate_commitments, Whir.cpp:574-585) and
+ * AGGR_ROOT (the tree over zero leaves it installs, :594-604); last the
+ * final polynomial, point and evaluation (Whir.cpp:840-869).  *check_ok
+ * (optional) receives whether K equals sum arr * b at the end
+ * (verification step 2, Whir.cpp:848-855). */
+enum { T_SCHEDULE = 19, T_AGGR_CHALLENGES = 20, T_AGGR_K = 21, T_AGGR_QUERIES = 22, T_AGGR_PATHS = 23,
+       T_AGGR_ROOT = 24 };
+
+int64_t orc_whir_batch_open(int k, const uint64_t *const *arrays, const int64_t *sizes,
+                            const uint64_t *const *codewords, const uint8_t *levels0, const uint64_t *const *betas,
+                            const uint64_t K0[2], int rate, int whir_k, orc_prng *g, uint8_t *transcript,
+                            int64_t cap, int *check_ok, int threads) {
+  bo_plan P;
+  if (bo_make_plan(k, sizes, rate, whir_k, &P) < 0) return -1;
+  tw_t tw = {transcript, 0, cap, 0};
+  {
+    uint32_t sch[2 * BO_MAX_STEPS];
+    for (int i = 0; i < P.nsched; i++) {
+      sch[2 * i] = (uint32_t)P.kappa[i];
+      sch[2 * i + 1] = (uint32_t)P.aggr[i];
+    }
+    tw_raw(&tw, T_SCHEDULE, sch, (uint32_t)(2 * P.nsched), 4);
+  }
+  int64_t n0 = sizes[0];
+  fe *arr = (fe *)malloc(sizeof(fe) * (size_t)n0), *b = (fe *)malloc(sizeof(fe) * (size_t)n0);
+  memcpy(arr, arrays[0], sizeof(fe) * (size_t)n0);
+  memcpy(b, betas[0], sizeof(fe) * (size_t)n0);
+  int64_t L = n0 * rate, m = n0, leaves = L / 4;
+  fe *cw = (fe *)malloc(sizeof(fe) * (size_t)L);
+  memcpy(cw, codewords[0], sizeof(fe) * (size_t)L);
+  uint8_t *tree = (uint8_t *)malloc((size_t)32 * (size_t)(2 * leaves));
+  memcpy(tree, levels0, (size_t)32 * (size_t)(2 * leaves - 1));
+  fe K = f_make(K0[0], K0[1]);
+  int cur = rate;
+  for (int s = 0; s < P.nexec; s++) {
+    const bo_exec *e = &P.ex[s];
+    if (e->iterate) {
+      const int kap = e->kappa, logk = ilog2_64(kap);
+      fe r[4];
+      for (int i = 0; i < logk; i++) { /* whir_sumcheck (Whir.cpp:233-249) */
+        uint64_t H6[6];
+        orc_sumcheck_quadratic((const uint64_t *)arr, (const uint64_t *)b, m, H6, threads);
+        fe h[3] = {f_make(H6[0], H6[1]), f_make(H6[2], H6[3]), f_make(H6[4], H6[5])};
+        tw_fe(&tw, T_WHIR_POLY, h, 3);
+        r[i] = prng_field(g);
+        tw_fe(&tw, T_WHIR_CHALLENGE, &r[i], 1);
+        K = quad_eval(h, r[i]);
+        uint64_t c2[2] = {r[i].re, r[i].im};
+        orc_sumcheck_fold((uint64_t *)arr, m, c2, threads);
+        orc_sumcheck_fold((uint64_t *)b, m, c2, threads);
+        m /= 2;
+      }
+      fe *ncw;
+      uint8_t *ntree;
+      whir_commit(arr, m, 2 * cur, &ncw, &ntree, threads);
+      int64_t NL = m * 2 * cur;
+      tw_raw(&tw, T_WHIR_ROOT, tree_root(ntree, NL), 1, 32);
+      /* whir_query (Whir.cpp:251-314) on the current codeword and tree */
+      const int l = e->l;
+      const int64_t qmod = kap > 4 ? L / kap : L / 4;
+      int32_t *q = (int32_t *)malloc(sizeof(int32_t) * (size_t)l);
+      for (int i = 0; i < l; i++) q[i] = orc_prng_next(g) % (int32_t)qmod;
+      tw_raw(&tw, T_WHIR_QUERIES, q, (uint32_t)l, 4);
+      fe *rep = (fe *)malloc(sizeof(fe) * (size_t)l * kap), *ans = (fe *)malloc(sizeof(fe) * (size_t)l);
+      for (int i = 0; i < l; i++) {
+        for (int j = 0; j < kap; j++) rep[i * kap + j] = cw[q[i] + j * (L / kap)];
+        ans[i] = rs_fold_tensor(rep + (int64_t)i * kap, logk, r, L, q[i]);
+      }
+      tw_fe(&tw, T_WHIR_REPLIES, rep, (uint32_t)(l * kap));
+      tw_fe(&tw, T_WHIR_ANSWERS, ans, (uint32_t)l);
+      uint8_t *paths = (uint8_t *)malloc((size_t)32 * (size_t)l * (size_t)(e->depth > 0 ? e->depth : 1));
+      for (int i = 0; i < l; i++) bo_open(tree, leaves, q[i], paths + (size_t)32 * e->depth * i);
+      tw_raw(&tw, T_WHIR_PATHS, paths, (uint32_t)(l * e->depth), 32);
+      free(paths);
+      free(rep);
+      for (int i = 0; i < l; i++) q[i] = q[i] * (int32_t)(kap * NL / L); /* Whir.cpp:371-372 */
+      free(cw);
+      free(tree);
+      cw = ncw;
+      tree = ntree;
+      L = NL;
+      leaves = L / 4;
+      fe rb = prng_field(g);
+      fe *ch = (fe *)malloc(sizeof(fe) * (size_t)l);
+      uint64_t rb2[2] = {rb.re, rb.im};
+      orc_update_betas((uint64_t *)b, m, q, l, L, rb2, (uint64_t *)ch, threads);
+      tw_fe(&tw, T_WHIR_COMBINE, ch, (uint32_t)l);
+      for (int i = 0; i < l; i++) K = f_add(K, f_mul(ch[i], ans[i]));
+      tw_fe(&tw, T_WHIR_K, &K, 1);
+      free(ch);
+      free(ans);
+      free(q);
+      cur *= 2;
+    }
+    if (e->aggregate) {
+      const int gsz = e->group;
+      fe *ch = (fe *)malloc(sizeof(fe) * 2 * (size_t)gsz); /* ch1 then ch2 */
+      for (int i = 0; i < 2 * gsz; i++) ch[i] = prng_field(g);
+      ch[0] = f_one();
+      ch[gsz] = f_one();
+      tw_fe(&tw, T_AGGR_CHALLENGES, ch, (uint32_t)(2 * gsz));
+      const fe *c1 = ch, *c2 = ch + gsz;
+      /* aggregate_arrays(arr, b, arr_aggr, B_aggr, r1 = ch2, r2 = ch1) (Whir.cpp:670-703) */
+      const fe **A = (const fe **)malloc(sizeof(fe *) * (size_t)gsz), **B = (const fe **)malloc(sizeof(fe *) * (size_t)gsz);
+      fe *a0 = (fe *)malloc(sizeof(fe) * (size_t)m), *b0 = (fe *)malloc(sizeof(fe) * (size_t)m);
+      memcpy(a0, arr, sizeof(fe) * (size_t)m);
+      memcpy(b0, b, sizeof(fe) * (size_t)m);
+      A[0] = a0;
+      B[0] = b0;
+      for (int i = 1; i < gsz; i++) {
+        A[i] = (const fe *)arrays[e->first + i - 1];
+        B[i] = (const fe *)betas[e->first + i - 1];
+      }
+      fe Kn = f_zero();
+      for (int i = 0; i < gsz; i++)
+        for (int j = 0; j < gsz; j++) {
+          fe d = f_zero();
+          for (int64_t t = 0; t < m; t++) d = f_add(d, f_mul(A[i][t], B[j][t]));
+          Kn = f_add(Kn, f_mul(f_mul(c2[i], c1[j]), d));
+        }
+      for (int i = 1; i < gsz; i++)
+        for (int64_t t = 0; t < m; t++) {
+          arr[t] = f_add(arr[t], f_mul(c2[i], A[i][t]));
+          b[t] = f_add(b[t], f_mul(c1[i], B[i][t]));
+        }
+      K = Kn;
+      tw_fe(&tw, T_AGGR_K, &K, 1);
+      /* aggregate_commitments(codeword, MT, codewords_aggr, MT_aggr, ch2, L / m) (Whir.cpp:547-606) */
+      fe *ncw = (fe *)malloc(sizeof(fe) * (size_t)L);
+      for (int64_t t = 0; t < L; t++) {
+        fe acc = f_mul(c2[0], cw[t]);
+        for (int i = 1; i < gsz; i++) acc = f_add(acc, f_mul(c2[i], ld(codewords[e->first + i - 1], t)));
+        ncw[t] = acc;
+      }
+      const int la = e->la;
+      int32_t *qa = (int32_t *)malloc(sizeof(int32_t) * (size_t)la);
+      for (int i = 0; i < la; i++) qa[i] = orc_prng_next(g) % (int32_t)(L / 4);
+      tw_raw(&tw, T_AGGR_QUERIES, qa, (uint32_t)la, 4);
+      uint8_t *paths = (uint8_t *)malloc((size_t)32 * (size_t)la * (size_t)(e->depth_a > 0 ? e->depth_a : 1));
+      for (int i = 0; i < la; i++) bo_open(tree, leaves, qa[i], paths + (size_t)32 * e->depth_a * i);
+      tw_raw(&tw, T_AGGR_PATHS, paths, (uint32_t)(la * e->depth_a), 32);
+      free(paths);
+      free(qa);
+      const int64_t nleaves = e->leaves_after;
+      uint8_t *ztree = (uint8_t *)calloc((size_t)(2 * nleaves), 32);
+      {
+        uint8_t *prev = ztree;
+        int64_t cnt = nleaves;
+        while (cnt > 1) {
+          uint8_t *nxt = prev + 32 * cnt;
+          cnt /= 2;
+          for (int64_t i = 0; i < cnt; i++) hash_self(prev + 32 * (2 * i), nxt + 32 * i);
+          prev = nxt;
+        }
+        tw_raw(&tw, T_AGGR_ROOT, prev, 1, 32);
+      }
+      free(cw);
+      free(tree);
+      cw = ncw;
+      tree = ztree;
+      leaves = nleaves;
+      free(a0);
+      free(b0);
+      free(A);
+      free(B);
+      free(ch);
+    }
+  }
+  /* final round (Whir.cpp:840-869) */
+  tw_fe(&tw, T_FINAL_POLY, arr, (uint32_t)m);
+  fe Kc = K;
+  for (int64_t t = 0; t < m; t++) Kc = f_sub(Kc, f_mul(arr[t], b[t]));
+  if (check_ok) *check_ok = f_eq(Kc, f_zero());
+  int lgm = ilog2_64(m);
+  fe rf[8];
+  for (int i = 0; i < lgm; i++) rf[i] = prng_field(g);
+  tw_fe(&tw, T_FINAL_POINT, rf, (uint32_t)lgm);
+  uint64_t ev[2];
+  orc_evaluate_vector((const uint64_t *)b, m, (const uint64_t *)rf, ev);
+  fe e = f_make(ev[0], ev[1]);
+  tw_fe(&tw, T_FINAL_EVAL, &e, 1);
+  free(arr);
+  free(b);
+  free(cw);
+  free(tree);
+  return tw.bad ? -1 : tw.len;
+}

@@ -170,6 +170,20 @@ void orc_pcs_phase3(uint64_t *B, int64_t rows, const uint32_t *queries, int l, c
 void orc_encode_concatenated(const uint64_t *data, int64_t n, int rate0, int rate1, int degree, uint64_t *Cprime,
                              uint64_t *C);
 
+/* ---- Whir_Batch_Open (Whir.cpp:706-898) ----------------------------- */
+/* Schedule of the batch opening of k polynomials of non-increasing sizes:
+ * returns the number of schedule steps (kappa[i], aggr[i]) or -1 for inputs
+ * the reference cannot run; cw_len[i] receives the codeword length that
+ * array i must come with (0: never merged), *bytes the transcript length. */
+int orc_whir_batch_schedule(int k, const int64_t *sizes, int rate, int whir_k, int32_t *kappa, int32_t *aggr,
+                            int64_t *cw_len, int64_t *bytes);
+/* The batch opening's transcript (length or -1); *check_ok: whether the
+ * final claim equals sum arr * b. */
+int64_t orc_whir_batch_open(int k, const uint64_t *const *arrays, const int64_t *sizes,
+                            const uint64_t *const *codewords, const uint8_t *levels0, const uint64_t *const *betas,
+                            const uint64_t K0[2], int rate, int whir_k, orc_prng *g, uint8_t *transcript,
+                            int64_t cap, int *check_ok, int threads);
+
 /* SplitMix64 witness generator shared by tests and bench. */
 void orc_witness(uint64_t seed, int64_t n, uint64_t *out);
 

@@ -439,3 +439,55 @@ def encode_concatenated(data, rate0, rate1, degree):
     lib().orc_encode_concatenated(_p64(data), ctypes.c_int64(n), ctypes.c_int(rate0), ctypes.c_int(rate1),
                                   ctypes.c_int(degree), _p64(Cp), _p64(C))
     return Cp, C
+
+
+def whir_batch_schedule(sizes, rate, whir_k=4):
+    """Schedule of Whir_Batch_Open (Whir.cpp:731-752 and the loop of
+    :761-833) for polynomials of the given non-increasing sizes: returns
+    (kappas, aggr flags, codeword length per array, transcript bytes), or
+    None when the reference cannot run the input."""
+    k = len(sizes)
+    sz = np.ascontiguousarray(sizes, dtype=np.int64)
+    kap, agg = np.zeros(64, dtype=np.int32), np.zeros(64, dtype=np.int32)
+    cwl, nb = np.zeros(max(k, 1), dtype=np.int64), ctypes.c_int64(0)
+    L = lib()
+    L.orc_whir_batch_schedule.restype = ctypes.c_int
+    n = L.orc_whir_batch_schedule(ctypes.c_int(k), ctypes.c_void_p(sz.ctypes.data), ctypes.c_int(rate),
+                                  ctypes.c_int(whir_k), ctypes.c_void_p(kap.ctypes.data),
+                                  ctypes.c_void_p(agg.ctypes.data), ctypes.c_void_p(cwl.ctypes.data),
+                                  ctypes.byref(nb))
+    if n < 0:
+        return None
+    return [int(x) for x in kap[:n]], [int(x) for x in agg[:n]], [int(x) for x in cwl[:k]], int(nb.value)
+
+
+def whir_batch_open(arrays, codewords, levels0, betas, K0, rate, whir_k=4, prng_seed=1, prng=None, threads=0):
+    """Whir_Batch_Open (Whir.cpp:706-898): returns (transcript bytes,
+    final-claim check, prng).  codewords[i] must have the length
+    whir_batch_schedule gives for array i (ignored when 0)."""
+    arrs = [np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2) for a in arrays]
+    bets = [np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2) for a in betas]
+    sizes = [a.shape[0] for a in arrs]
+    sch = whir_batch_schedule(sizes, rate, whir_k)
+    if sch is None:
+        raise ValueError("Whir_Batch_Open cannot run these sizes")
+    cws = []
+    for i, c in enumerate(codewords):
+        cws.append(np.ascontiguousarray(c, dtype=np.uint64).reshape(-1, 2) if c is not None
+                   else np.zeros((1, 2), dtype=np.uint64))
+    lv = np.ascontiguousarray(levels0, dtype=np.uint8)
+    K0 = np.ascontiguousarray(K0, dtype=np.uint64).reshape(2)
+    g = prng if prng is not None else Prng(prng_seed)
+    out = np.zeros(sch[3], dtype=np.uint8)
+    ok = ctypes.c_int(0)
+    sz = np.ascontiguousarray(sizes, dtype=np.int64)
+    L = lib()
+    L.orc_whir_batch_open.restype = ctypes.c_int64
+    n = L.orc_whir_batch_open(ctypes.c_int(len(arrs)), _ptr_array(arrs), ctypes.c_void_p(sz.ctypes.data),
+                              _ptr_array(cws), _p8(lv), _ptr_array(bets), _p64(K0), ctypes.c_int(rate),
+                              ctypes.c_int(whir_k), ctypes.byref(g.s), _p8(out), ctypes.c_int64(out.size),
+                              ctypes.byref(ok), ctypes.c_int(threads))
+    if n != out.size:
+        raise RuntimeError("batch open transcript length %d, expected %d" % (n, out.size))
+    return out.tobytes(), bool(ok.value), g
+

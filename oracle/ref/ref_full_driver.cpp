@@ -26,6 +26,7 @@
 //   ref_full tensor <logrows> <N> <rate> <my_id> <p0> <p1>         tensor_eval_vector (coPCS.cpp:602)
 //   ref_full phase3 <logrows> <N> <l> <rate> <my_id> <seed>        pcs_sumcheck_phase3 (coPCS.cpp:634)
 //   ref_full encconc <logn> <rate0> <rate1> <degree> <seed>       encode_concatenated (coPCS.cpp:653)
+//   ref_full batchopen <rate> <whir_k> <seed> <prng> <logn0> [<logn1> ...]  Whir_Batch_Open (Whir.cpp:706)
 #include "Distributed_Sumcheck.h"
 #include "Whir.h"
 #include "coPCS.h"
@@ -38,6 +39,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <unistd.h>
 #include <vector>
 
 using std::vector;
@@ -66,6 +68,23 @@ F aggregate_arrays(vector<F> &arr, vector<F> &b, vector<vector<F>> &arrays, vect
 void compute_secret_shares(vector<F> &v, vector<vector<F>> &v_shares, int N, int k, int _k, bool privacy_preserving);
 vector<F> unpack_secret_share(vector<F> &secret, int _k, int k);
 
+// Reference functions defined in Whir.cpp without a header declaration.
+quadratic_poly whir_sumcheck_step1(vector<F> &arr, vector<F> &b);
+void whir_sumcheck_step2(vector<F> &arr, vector<F> &b, F c);
+vector<F> whir_query(vector<F> &codeword, vector<vector<_hash>> &MT, vector<F> r, vector<int> &queries, int rate);
+vector<F> update_betas(vector<F> &b, vector<int> queries, int n);
+
+// rand() as glibc defines it (random()), logging the values while
+// g_log_rand is set: the queries aggregate_commitments draws internally
+// (Whir.cpp:574-576) are otherwise not observable.
+static bool g_log_rand = false;
+static vector<int> g_rand_log;
+extern "C" int rand(void) noexcept {
+  int v = (int)random();
+  if (g_log_rand) g_rand_log.push_back(v);
+  return v;
+}
+
 static const uint64_t P61 = 2305843009213693951ULL;
 struct SplitMix {
   uint64_t s;
@@ -91,6 +110,208 @@ static void putFs(const vector<F> &v) { for (auto &x : v) { put(&x.real, 8); put
 
 static void put_prefix(const vector<F> &v, size_t n) {
   for (size_t i = 0; i < n; i++) { put(&v[i].real, 8); put(&v[i].img, 8); }
+}
+
+// Transcript records (the tags of the prover's transcript format).
+enum { T_WHIR_POLY = 7, T_WHIR_CHALLENGE = 8, T_WHIR_ROOT = 9, T_WHIR_QUERIES = 10, T_WHIR_REPLIES = 11,
+       T_WHIR_ANSWERS = 12, T_WHIR_PATHS = 13, T_WHIR_COMBINE = 14, T_WHIR_K = 15, T_FINAL_POLY = 16,
+       T_FINAL_POINT = 17, T_FINAL_EVAL = 18, T_SCHEDULE = 19, T_AGGR_CHALLENGES = 20, T_AGGR_K = 21,
+       T_AGGR_QUERIES = 22, T_AGGR_PATHS = 23, T_AGGR_ROOT = 24 };
+static void rec(uint32_t tag, uint32_t count, const void *p, size_t unit) {
+  put(&tag, 4);
+  put(&count, 4);
+  put(p, unit * count);
+}
+static void recF(uint32_t tag, const vector<F> &v) {
+  uint32_t count = (uint32_t)v.size();
+  put(&tag, 4);
+  put(&count, 4);
+  putFs(v);
+}
+static void rec_paths(uint32_t tag, vector<vector<_hash>> &MT, const vector<int> &q) {
+  vector<uint8_t> paths;
+  for (int qi : q) {
+    vector<_hash> p = merkle_tree::merkle_tree_prover::open_tree_blake(MT, qi);
+    for (auto &h : p) paths.insert(paths.end(), h.arr, h.arr + 32);
+  }
+  rec(tag, (uint32_t)(paths.size() / 32), paths.data(), 32);
+}
+
+// Whir_Batch_Open on k polynomials of sizes 2^logs[i] (non-increasing):
+// arrays from the seed, betas = precompute_beta of seeded points, K0 the
+// true claim of array 0, codewords from Whir_Commit_initial at the rate
+// each array is merged at.  The loop of Whir.cpp:706-898 is followed step
+// by step with the reference's own functions (whir_sumcheck_step1/2,
+// F::_random, Whir_Commit_initial, whir_query, open_tree_blake,
+// update_betas, aggregate_arrays, aggregate_commitments, evaluate_vector)
+// so that every intermediate value can be written; then the unmodified
+// Whir_Batch_Open runs on the same inputs from the same generator state and
+// the generator positions after both runs must agree (exit code 3
+// otherwise).  Output: the records, then the next random() value.
+static int cmd_batchopen(int rate, int wk, uint64_t seed, unsigned prng, const vector<int> &logs) {
+  const int k = (int)logs.size();
+  SplitMix g(seed);
+  vector<vector<F>> arrays(k), betas(k);
+  for (int i = 0; i < k; i++) arrays[i] = g.vec(1u << logs[i]);
+  for (int i = 0; i < k; i++) precompute_beta(g.vec(logs[i]), betas[i]);
+  F K = F(0);
+  for (size_t j = 0; j < arrays[0].size(); j++) K += arrays[0][j] * betas[0][j];
+  const F K0 = K;
+  whir_k = wk;
+  vector<vector<F>> cws(k);
+  vector<vector<vector<_hash>>> MTs(k);
+  Whir_Commit_initial(arrays[0], cws[0], MTs[0], rate, wk);
+  // schedule (Whir.cpp:731-752)
+  vector<int> kappas, aggr, sizes;
+  for (int i = 1; i < k; i++) sizes.push_back((int)arrays[i].size());
+  {
+    int size = (int)arrays[0].size();
+    while (true) {
+      if (!sizes.size() || size / whir_k > sizes[0]) {
+        kappas.push_back(whir_k);
+        size /= whir_k;
+        aggr.push_back(0);
+      } else {
+        kappas.push_back(size / sizes[0]);
+        int s = sizes[0];
+        while (sizes.size() && sizes[0] == s) sizes.erase(sizes.begin());
+        size /= kappas.back();
+        aggr.push_back(1);
+      }
+      if (size <= whir_k) break;
+    }
+  }
+  {
+    vector<uint32_t> sch;
+    for (size_t i = 0; i < kappas.size(); i++) {
+      sch.push_back((uint32_t)kappas[i]);
+      sch.push_back((uint32_t)aggr[i]);
+    }
+    rec(T_SCHEDULE, (uint32_t)sch.size(), sch.data(), 4);
+  }
+  srandom(prng);
+  vector<F> arr = arrays[0], b = betas[0], codeword = cws[0];
+  vector<vector<_hash>> MT = MTs[0];
+  int next = 1, iter = 0, cur = rate;
+  while (true) {
+    whir_k = kappas[iter];
+    const bool ag = aggr[iter] != 0;
+    if (!ag || whir_k != 1) {
+      // Whir_Iteration (Whir.cpp:354-386)
+      const int kap = whir_k;
+      vector<F> r;
+      for (int i = 0; i < (int)log2(kap); i++) {
+        quadratic_poly h = whir_sumcheck_step1(arr, b);
+        if (K != h.eval(F(0)) + h.eval(F(1))) { fprintf(stderr, "whir sumcheck inconsistent\n"); return 2; }
+        recF(T_WHIR_POLY, {h.a, h.b, h.c});
+        r.push_back(F::_random());
+        recF(T_WHIR_CHALLENGE, {r[i]});
+        K = h.eval(r[i]);
+        whir_sumcheck_step2(arr, b, r[i]);
+      }
+      vector<F> new_cw;
+      vector<vector<_hash>> new_MT;
+      Whir_Commit_initial(arr, new_cw, new_MT, 2 * cur, kap);
+      rec(T_WHIR_ROOT, 1, new_MT.back()[0].arr, 32);
+      vector<int> queries;
+      vector<F> ys = whir_query(codeword, MT, r, queries, cur);
+      {
+        vector<uint32_t> q(queries.begin(), queries.end());
+        rec(T_WHIR_QUERIES, (uint32_t)q.size(), q.data(), 4);
+        vector<F> replies;
+        for (int qi : queries)
+          for (int j = 0; j < kap; j++) replies.push_back(codeword[qi + j * codeword.size() / kap]);
+        recF(T_WHIR_REPLIES, replies);
+        recF(T_WHIR_ANSWERS, ys);
+        rec_paths(T_WHIR_PATHS, MT, queries);
+      }
+      for (size_t i = 0; i < queries.size(); i++) queries[i] = queries[i] * (kap * new_cw.size() / codeword.size());
+      codeword = new_cw;
+      MT = new_MT;
+      vector<F> ch = update_betas(b, queries, (int)new_cw.size());
+      recF(T_WHIR_COMBINE, ch);
+      for (size_t i = 0; i < ch.size(); i++) K += ch[i] * ys[i];
+      recF(T_WHIR_K, {K});
+      cur *= 2;
+    }
+    iter++;
+    if (ag) {
+      vector<vector<F>> B_aggr{b}, arr_aggr{arr}, cw_aggr{codeword};
+      vector<vector<vector<_hash>>> MT_aggr{MT};
+      int g_cnt = 1;
+      for (int i = next; i < k; i++)
+        if (arrays[i].size() == arr.size()) {
+          Whir_Commit_initial(arrays[i], cws[i], MTs[i], (int)(codeword.size() / arr.size()), wk);
+          B_aggr.push_back(betas[i]);
+          arr_aggr.push_back(arrays[i]);
+          cw_aggr.push_back(cws[i]);
+          MT_aggr.push_back(MTs[i]);
+          g_cnt++;
+        }
+      next += g_cnt - 1;
+      vector<F> ch1, ch2;
+      for (int i = 0; i < g_cnt; i++) ch1.push_back(F::_random());
+      for (int i = 0; i < g_cnt; i++) ch2.push_back(F::_random());
+      ch1[0] = 1;
+      ch2[0] = 1;
+      {
+        vector<F> both = ch1;
+        both.insert(both.end(), ch2.begin(), ch2.end());
+        recF(T_AGGR_CHALLENGES, both);
+      }
+      K = aggregate_arrays(arr, b, arr_aggr, B_aggr, ch2, ch1);
+      recF(T_AGGR_K, {K});
+      if (iter + 1 >= (int)kappas.size()) { fprintf(stderr, "schedule read past its end\n"); return 4; }
+      whir_k = kappas[iter + 1];
+      if (next < k && arr.size() / whir_k <= arrays[next].size()) whir_k = arr.size() / arrays[next].size();
+      MT.clear();
+      g_rand_log.clear();
+      g_log_rand = true;
+      aggregate_commitments(codeword, MT, cw_aggr, MT_aggr, ch2, (int)(cw_aggr[0].size() / arr_aggr[0].size()));
+      g_log_rand = false;
+      vector<int> qa;
+      for (int v : g_rand_log) qa.push_back(v % (int)(codeword.size() / 4));
+      {
+        vector<uint32_t> q(qa.begin(), qa.end());
+        rec(T_AGGR_QUERIES, (uint32_t)q.size(), q.data(), 4);
+      }
+      rec_paths(T_AGGR_PATHS, MT_aggr[0], qa);
+      rec(T_AGGR_ROOT, 1, MT.back()[0].arr, 32);
+    }
+    if ((int)arr.size() <= whir_k) break;
+  }
+  recF(T_FINAL_POLY, arr);
+  {
+    F Kc = K;
+    for (size_t i = 0; i < arr.size(); i++) Kc -= arr[i] * b[i];
+    if (Kc != F(0)) { fprintf(stderr, "final claim inconsistent\n"); return 2; }
+  }
+  vector<F> rf;
+  for (int i = 0; i < (int)log2(arr.size()); i++) rf.push_back(F::_random());
+  recF(T_FINAL_POINT, rf);
+  recF(T_FINAL_EVAL, {evaluate_vector(b, rf)});
+  const int32_t nxt1 = (int32_t)random();
+
+  // The unmodified Whir_Batch_Open on the same inputs (its prints go to stderr).
+  for (int i = 1; i < k; i++)
+    if (cws[i].empty()) Whir_Commit_initial(arrays[i], cws[i], MTs[i], rate, wk);
+  vector<F> evals(k, F(0));
+  evals[0] = K0;
+  vector<vector<F>> a2 = arrays, c2 = cws, b2 = betas;
+  vector<vector<vector<_hash>>> m2 = MTs;
+  whir_k = wk;
+  srandom(prng);
+  fflush(stdout);
+  int saved = dup(1);
+  dup2(2, 1);
+  Whir_Batch_Open(a2, c2, m2, evals, b2, rate, true);
+  fflush(stdout);
+  dup2(saved, 1);
+  close(saved);
+  const int32_t nxt2 = (int32_t)random();
+  if (nxt1 != nxt2) { fprintf(stderr, "generator position differs from Whir_Batch_Open's\n"); return 3; }
+  put(&nxt1, 4);
+  return 0;
 }
 
 int main(int argc, char **argv) {
@@ -195,6 +416,12 @@ int main(int argc, char **argv) {
     int32_t nxt = (int32_t)random();
     put(&nxt, 4);
     return 0;
+  }
+  if (c == "batchopen") {
+    vector<int> logs;
+    for (int i = 6; i < argc; i++) logs.push_back(I(i));
+    if (logs.empty()) return 1;
+    return cmd_batchopen(I(2), I(3), U(4), (unsigned)U(5), logs);
   }
   if (c == "tensor") {
     int logrows = I(2), N = I(3), rate = I(4);

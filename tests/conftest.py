@@ -138,3 +138,35 @@ def splitmix_base(seed, n):
     out = np.zeros((n, 2), dtype=np.uint64)
     out[:, 0] = v
     return out
+
+
+def batch_open_inputs(oracle, rate, whir_k, seed, logs):
+    """Inputs of a Whir_Batch_Open case as the reference driver builds them
+    (oracle/ref/ref_full_driver.cpp cmd_batchopen): arrays, then one point
+    per array from the same SplitMix stream; betas = eq tables of the points;
+    K0 = <arrays[0], betas[0]>; codewords = RS encodings at the rate each
+    array is merged at; levels0 = the Merkle tree of codeword 0."""
+    n = [1 << l for l in logs]
+    raw = splitmix_ext(seed, sum(n) + sum(logs))
+    arrays, off = [], 0
+    for x in n:
+        arrays.append(raw[off:off + x])
+        off += x
+    betas = []
+    for l in logs:
+        betas.append(oracle.precompute_beta(raw[off:off + l]))
+        off += l
+    sch = oracle.whir_batch_schedule(n, rate, whir_k)
+    assert sch is not None
+    cws = []
+    for a, L in zip(arrays, sch[2]):
+        if L == 0:
+            cws.append(None)
+            continue
+        c = np.zeros((L, 2), dtype=np.uint64)
+        c[:a.shape[0]] = a
+        cws.append(oracle.fft(c))
+    levels0 = oracle.merkle_commit(cws[0])
+    _, _, K0 = oracle.aggregate_arrays(np.zeros_like(arrays[0]), np.zeros_like(betas[0]), [arrays[0]], [betas[0]],
+                                       [[1, 0]], [[1, 0]])
+    return arrays, betas, cws, levels0, K0, sch

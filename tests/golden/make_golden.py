@@ -56,6 +56,8 @@ def main():
             manifest["copcs"] = gen_copcs()
         if "sumcheck" in only:
             manifest["sumcheck"] = gen_sumcheck()
+        if "batchopen" in only:
+            manifest["batchopen"] = gen_batchopen()
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
             json.dump(manifest, f, indent=1)
         print("updated", sorted(only))
@@ -135,6 +137,7 @@ def main():
 
     manifest["copcs"] = gen_copcs()
     manifest["sumcheck"] = gen_sumcheck()
+    manifest["batchopen"] = gen_batchopen()
 
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
@@ -187,6 +190,33 @@ def gen_copcs():
         save(name + ".bin", data)
         copcs[name] = {"file": name + ".bin", "args": list(args)}
     return copcs
+
+
+def gen_batchopen():
+    """Whir_Batch_Open transcripts (ref_full batchopen: the loop of
+    Whir.cpp:706-898 on the reference's functions, cross-checked against
+    the unmodified Whir_Batch_Open).  Arguments: rate, whir_k, seed, prng
+    seed, log2 sizes.  The output ends with the next random() value."""
+    out = {}
+    for name, args in [
+        ("bo_7_5_r16", (16, 4, 101, 1, 7, 5)),
+        ("bo_8_8_r8", (8, 4, 102, 3, 8, 8)),
+        ("bo_9_7_7_r4", (4, 4, 103, 1, 9, 7, 7)),
+        ("bo_10_8_6_r8", (8, 4, 104, 5, 10, 8, 6)),
+        ("bo_10_9_r4", (4, 4, 105, 1, 10, 9)),
+        ("bo_9_6_r8_k2", (8, 2, 106, 1, 9, 6)),
+        ("bo_10_7_r4_k8", (4, 8, 107, 2, 10, 7)),
+        ("bo_12_10_10_7_r2", (2, 4, 108, 1, 12, 10, 10, 7)),
+        ("bo_13_9_9_9_6_r2", (2, 4, 109, 9, 13, 9, 9, 9, 6)),
+        ("bo_16_12_10_r2", (2, 4, 110, 1, 16, 12, 10)),
+    ]:
+        data = run_full("batchopen", *args)
+        e = {"args": list(args), "bytes": len(data), "sha256": hashlib.sha256(data).hexdigest()}
+        if name == "bo_7_5_r16":
+            save(name + ".bin", data)
+            e["file"] = name + ".bin"
+        out[name] = e
+    return out
 
 
 if __name__ == "__main__":
