@@ -17,11 +17,11 @@ Prints one JSON line:
                launching stream during a second timed pass
   cpu_baseline the oracle port (oracle/gbz_oracle.c) proving the same
                workload once on the host cores
-  batched      configuration 3 (64 proofs, 2^12..2^20, rate 1/4) through
+  batched      64 proofs (2^12..2^20, rate 1/4) through
                gbz_prove_batch (8 slots, graph replay) beside the plain
                prover (one synchronised gbz_prove per proof), same pinned
                host buffers, transcripts compared byte for byte
-  served       configuration 5 (400 Poisson arrivals at 200/s, 2^14..2^22,
+  served       400 Poisson arrivals at 200/s (2^14..2^22,
                rate 1/2 or 1/4) through gbz_serve: proofs/s, p50/p99
                latency, beside the plain prover on the same arrivals; and
                both at saturation (every request at t = 0)
@@ -53,7 +53,7 @@ sys.path.insert(0, PKG)
 sys.path.insert(0, ORACLE)
 
 LOGN, RATE = 24, 2
-SEED = 0x5EED0000 + 2 * 65536  # configuration 2, instance 0
+SEED = 0x5EED0000 + 2 * 65536  # witness seed of the 2^24 rate-1/2 workload
 METRIC = "proofs/s and p50/p99 latency, batched+served vs plain GPU prover, bit-exact"
 CONFIG = {
     "workload": "plain prover, n=2^24 uniform base-field witness, rate 1/2 (NTT 2^25), Blake3 Merkle over "
@@ -221,13 +221,13 @@ def run_reference_arm(args, ws, rank):
 
 
 def c3_jobs():
-    """Configuration 3: 64 witnesses, log2 n uniform in [12, 20], rate 1/4."""
+    """The batch workload: 64 witnesses, log2 n uniform in [12, 20], rate 1/4."""
     rng = np.random.default_rng(0x5EEF3)
     return [int(x) for x in rng.integers(12, 21, size=64)], [4] * 64
 
 
 def c5_requests(n_req, lam, seed=0x5EEF5):
-    """Configuration 5: Poisson arrivals (rate lam per second), log2 n uniform
+    """The serving workload: Poisson arrivals (rate lam per second), log2 n uniform
     in [14, 22], rate 1/2 or 1/4."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n_req))
@@ -278,7 +278,7 @@ def run_many(gbz, O, ctx, repeats):
         mks.append(mk)
     batched = len(ws) * repeats / (time.perf_counter() - t0)
     out["batched"] = {
-        "workload": "64 proofs, n = 2^12..2^20 log-uniform, rate 1/4 (configuration 3)",
+        "workload": "64 proofs, n = 2^12..2^20 log-uniform, rate 1/4",
         "proofs_per_s": batched, "plain_proofs_per_s": plain, "speedup_vs_plain": batched / plain,
         "device_makespan_ms": 1e3 * min(mks), "slots": 8, "graphs": True,
         "bit_identical_to_plain": [t.tobytes() for t in tb2] == ref,
@@ -302,7 +302,7 @@ def run_many(gbz, O, ctx, repeats):
     for w, l, r, s in zip(sws[:32], slog[:32], srate[:32], sseeds[:32]):
         sref.append(ctx.prove(w, l, r, s).tobytes())
     out["served"] = {
-        "workload": "400 requests, Poisson 200/s, n = 2^14..2^22 log-uniform, rate 1/2 or 1/4 (configuration 5)",
+        "workload": "400 requests, Poisson 200/s, n = 2^14..2^22 log-uniform, rate 1/2 or 1/4",
         "slots": 8, "depth": 2, **served,
         "bit_identical_to_alone": [t.tobytes() for t in st3[:32]] == sref,
     }
@@ -310,7 +310,7 @@ def run_many(gbz, O, ctx, repeats):
 
 
 def run_party_shares(gbz, O, ctx, repeats, P=16, log_share=22, rate=2):
-    """Configuration 4 on one device: a 2^26 base-field witness split
+    """Party shares on one device: a 2^26 base-field witness split
     additively into P = 16 party shares of 2^22; every party commits its
     share as PCS_commit does (16 rows of 2^18, coPCS Encode at rate 1/2,
     per-column Blake3 roots and the tree over them, leader root), then the
@@ -359,7 +359,7 @@ def run_party_shares(gbz, O, ctx, repeats, P=16, log_share=22, rate=2):
         t_s.append(t2 - t1)
     c_ms, s_ms = 1e3 * min(t_c), 1e3 * min(t_s)
     return {"party_shares": {
-        "workload": "2^26 witness as 16 party shares of 2^22 (configuration 4): per-party PCS_commit (16 rows of "
+        "workload": "2^26 witness as 16 party shares of 2^22: per-party PCS_commit (16 rows of "
                     "2^18, coPCS Encode rate 1/2, column Blake3 roots + tree, leader root) and the 16-party "
                     "distributed quadratic sumcheck with the leader's aggregation, one device",
         "parties": P, "share_len": M, "commit_ms": c_ms, "sumcheck_ms": s_ms, "total_ms": c_ms + s_ms,
@@ -420,7 +420,7 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
         rows[name] = r
 
     D = gbz.MEM_DEVICE
-    # a11: 16-party cubic distributed sumcheck over 2^24 entries (fused fold + message per round)
+    # 16-party cubic distributed sumcheck over 2^24 entries (fused fold + message per round)
     N, M = 16, 1 << (20 - shift)
     v = [rnd(N * M) for _ in range(3)]
     w = np.ascontiguousarray(np.random.default_rng(1).integers(0, P61, size=(N, 2), dtype=np.uint64))
@@ -441,13 +441,13 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     rec("party_sumcheck_cubic_2^%d" % (24 - shift), timed(party), hbm_bytes=byts,
         note="16 parties x 2^%d, 3 vectors" % (20 - shift))
     del v
-    # a4: coPCS Encode, 16 rows of 2^20 at rate 2
+    # coPCS Encode, 16 rows of 2^20 at rate 2
     R, lr = 16, 20 - shift
     rows_in, cw = rnd(R << lr), torch.empty(((R << lr) * 2, 2), dtype=torch.int64, device="cuda")
     enc = lambda: ctx.check(gbz.lib.gbz_encode_rows(ctx.h, rows_in.data_ptr(), R, lr, 2, 0, cw.data_ptr(), D))
     bfly = R * ((1 << lr) // 2 * lr + (2 << lr) // 2 * (lr + 1))
     rec("encode_rows_16x2^%d_rate2" % lr, timed(enc), fmuls=bfly, note="radix-2 butterflies of both transforms")
-    # a7: column Merkle over 32 rows of 2^20
+    # column Merkle over 32 rows of 2^20
     lc = 20 - shift
     cols = rnd(32 << lc)
     lv = torch.empty(((2 << lc) - 1, 32), dtype=torch.uint8, device="cuda")
@@ -457,7 +457,7 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     rec("column_merkle_32x2^%d" % lc, timed(cm), comps=4 * (1 << lc) + (1 << lc) - 1,
         note="4 compressions per column + tree over 2^20 column roots")
     del cols, lv
-    # a15: RS_multifold5 of a 2^24 codeword by 16
+    # RS_multifold5 of a 2^24 codeword by 16
     lm = 24 - shift
     cwb = rnd(1 << lm)
     a16 = np.ascontiguousarray(np.random.default_rng(2).integers(0, P61, size=(16, 2), dtype=np.uint64))
@@ -465,11 +465,11 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     mfc = lambda: ctx.check(gbz.lib.gbz_rs_multifold5(ctx.h, cwb.data_ptr(), 1 << lm, gbz._ptr(a16), 4,
                                                       mf.data_ptr(), D))
     rec("rs_multifold5_2^%d_by16" % lm, timed(mfc), hbm_bytes=16 * (1 << lm) + 16 * (1 << (lm - 4)))
-    # a12: coSumcheck phase 2 (fold by Lagrange weights), 2^24 by 16
+    # coSumcheck phase 2 (fold by Lagrange weights), 2^24 by 16
     c2 = lambda: ctx.check(gbz.lib.gbz_cosumcheck_phase2(ctx.h, cwb.data_ptr(), 1 << lm, gbz._ptr(a16), 4,
                                                          mf.data_ptr(), D))
     rec("cosumcheck_phase2_2^%d_d16" % lm, timed(c2), hbm_bytes=16 * (1 << lm) + 16 * (1 << (lm - 4)))
-    # a12: coSumcheck phase 1, cubic, 2^22 per vector, blocks of 8
+    # coSumcheck phase 1, cubic, 2^22 per vector, blocks of 8
     l1 = 22 - shift
     p4 = [rnd(1 << l1) for _ in range(4)]
     H = np.zeros((32, 2), dtype=np.uint64)
@@ -480,21 +480,21 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     rec("cosumcheck_phase1_cubic_2^%d_d8" % l1, timed(c1),
         fmuls=4 * nb * (8 // 2 * 3 + 32 // 2 * 5) + 3 * nb * 32, note="block transforms (butterflies) + products")
     del p4
-    # a14: packed Shamir shares, 2^22 values for 16 parties
+    # packed Shamir shares, 2^22 values for 16 parties
     ls = 22 - shift
     sv = rnd(1 << ls)
     sh = torch.empty((16, (1 << ls) // 4, 2), dtype=torch.int64, device="cuda")
     ssh = lambda: ctx.check(gbz.lib.gbz_secret_shares(ctx.h, sv.data_ptr(), 1 << ls, 16, 0, 1, sh.data_ptr(), D))
     rec("secret_shares_2^%d_N16" % ls, timed(ssh), fmuls=((1 << ls) // 4) * 16 * 8,
         hbm_bytes=16 * (1 << ls) + 16 * 16 * ((1 << ls) // 4))
-    # a13: leader aggregation of 64 party messages of 2^16
+    # leader aggregation of 64 party messages of 2^16
     msgs = rnd(64 << 16)
     bb = np.ascontiguousarray(np.random.default_rng(3).integers(0, P61, size=(16, 2), dtype=np.uint64))
     ao = torch.empty((1 << 16, 2), dtype=torch.int64, device="cuda")
     ag = lambda: ctx.check(gbz.lib.gbz_party_aggregate(ctx.h, msgs.data_ptr(), 64, 1 << 16, gbz._ptr(bb),
                                                        ao.data_ptr(), D))
     rec("party_aggregate_64x2^16", timed(ag), hbm_bytes=16 * (65 << 16))
-    # a17: aggregate_claims, 4 arrays x 4 points of 2^22
+    # aggregate_claims, 4 arrays x 4 points of 2^22
     la = 22 - shift
     arrs = [rnd(1 << la) for _ in range(4)]
     pts = np.ascontiguousarray(np.random.default_rng(4).integers(0, P61, size=(4, la, 2), dtype=np.uint64))
@@ -513,7 +513,7 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
         hbm_bytes=4 * n22 + (4 + 4) * n22 + (4 + 1) * n22 + (4 + 1) * n22,
         note="4 eq tables written, 16 inner products (one pass over 8 vectors), 2 combinations")
     del arrs, msgs
-    # a16: pcs_sumcheck_phase3, 2^20 rows, 100 queries, 16 parties
+    # pcs_sumcheck_phase3, 2^20 rows, 100 queries, 16 parties
     lb = 20 - shift
     Bv = rnd(1 << lb)
     qs = np.ascontiguousarray(np.stack([np.random.default_rng(5).integers(0, 8, 100),

@@ -374,7 +374,45 @@ gbz_status gbz_whir_aggregate_commitments(gbz_ctx *ctx, int k, const uint64_t *c
                                           const uint64_t *r, int rate, int whir_k, gbz_prng *prng,
                                           uint64_t *codeword, uint8_t *levels, int mem);
 
-/* ------------------------------------------------ coPCS open rounds (a16) */
+/* --------------------------------------------------- WHIR batch opening */
+
+/* Schedule of Whir_Batch_Open (kappas and merge flags of Whir.cpp:731-752,
+ * then the loop of :761-833) for k <= 64 polynomials of non-increasing
+ * power-of-two sizes: *steps entries kappa[i], aggr[i] (room for 64),
+ * cw_len[i] = the codeword length polynomial i must come with (0: the loop
+ * ends before it is merged), *transcript_bytes.  Every output may be NULL.
+ * Host only.  GBZ_EINVAL for inputs the reference cannot run: it reads its
+ * schedule past the end when a merge is among the last two steps, and
+ * exits in open_tree_blake when a query exceeds a merged tree. */
+gbz_status gbz_whir_batch_schedule(int k, const uint64_t *sizes, int rate, int whir_k, int *steps, int32_t *kappa,
+                                   int32_t *aggr, uint64_t *cw_len, uint64_t *transcript_bytes);
+
+/* Whir_Batch_Open(arrays, codewords, MTs, evals, betas, rate, true)
+ * (Whir.cpp:706-898) with the reference's global whir_k = whir_k (2, 4, 8
+ * or 16): arrays[i] (sizes[i] elements) with their claim vectors betas[i],
+ * K0 = evals[0] (the claim of array 0), codewords[i] (cw_len[i] elements,
+ * the RS encoding at the rate array i is merged at), levels0 = MTs[0] (the
+ * MT_commit_Blake levels of codewords[0]; the other trees are never read by
+ * the reference).  prng: the glibc generator state, advanced past every
+ * draw.  Transcript records:
+ *  19 SCHEDULE u32 x 2 steps (kappa, merge flag)
+ *  per executed step: a WHIR iteration with folding factor kappa
+ *    (log2 kappa x (7 WHIR_POLY, 8 WHIR_CHALLENGE), 9 WHIR_ROOT,
+ *    10 WHIR_QUERIES, 11 WHIR_REPLIES 16B x kappa l, 12 WHIR_ANSWERS,
+ *    13 WHIR_PATHS, 14 WHIR_COMBINE, 15 WHIR_K), then for a merge
+ *    20 AGGR_CHALLENGES 16B x 2g (ch1 then ch2, each starting with 1),
+ *    21 AGGR_K 16B, 22 AGGR_QUERIES u32 x l (aggregate_commitments'
+ *    openings), 23 AGGR_PATHS 32B x l depth, 24 AGGR_ROOT 32B (the tree over
+ *    zero leaves the reference installs)
+ *  16 FINAL_POLY 16B x m | 17 FINAL_POINT 16B x log2 m | 18 FINAL_EVAL 16B
+ * Returns GBZ_ECHECK (outputs still written) when a sumcheck claim or the
+ * final K == <arr, b> (verification step 2) fails on the device. */
+gbz_status gbz_whir_batch_open(gbz_ctx *ctx, int k, const uint64_t *const *arrays, const uint64_t *sizes,
+                               const uint64_t *const *codewords, const uint8_t *levels0,
+                               const uint64_t *const *betas, const uint64_t *K0, int rate, int whir_k,
+                               gbz_prng *prng, uint8_t *transcript, uint64_t capacity, int mem);
+
+/* ------------------------------------------------------ coPCS open rounds */
 
 /* tensor_eval_vector (coPCS.cpp:602-632) for party my_id (< 2 cols):
  * out[j] = c w1^j for j < rows, w1 = omega_{rate rows}^{point[1]}, c the

@@ -1024,7 +1024,7 @@ void orc_cophase2(const uint64_t *v, int64_t n, const uint64_t *L, int logd, uin
   }
 }
 
-/* ----------------------------------------- sumcheck round forms (a11) */
+/* ----------------------------------------- sumcheck round forms */
 /* Line of a pair: linear_poly(v[2j+1] - v[2j], v[2j]) (polynomial.h:46-59). */
 typedef struct { fe a, b; } lin_t;
 static inline lin_t lin_at(const uint64_t *v, int64_t j) {
@@ -1185,7 +1185,7 @@ void orc_party_sumcheck(int form, uint64_t *v1, uint64_t *v2, uint64_t *v3, int6
   y_io[0] = y.re; y_io[1] = y.im;
 }
 
-/* ------------------------------------------------ WHIR aggregation (a17) */
+/* ------------------------------------------------ WHIR aggregation */
 static fe dot(const uint64_t *a, const uint64_t *b, int64_t n) {
   fe acc = f_zero();
   for (int64_t t = 0; t < n; t++) acc = f_add(acc, f_mul(ld(a, t), ld(b, t)));
@@ -1266,7 +1266,7 @@ void orc_aggregate_commitments(int k, const uint64_t *const *cws, int64_t n, con
   }
 }
 
-/* ------------------------------------------- coPCS open rounds (a16) */
+/* ------------------------------------------- coPCS open rounds */
 /* tensor_eval_vector (coPCS.cpp:602-632): w1 = omega_{rate rows}^{p1},
  * w2 = omega_{4 cols}^{2 p0 + 1}; pow2[t] = w2^t (t < cols) goes through two
  * inverse transforms, is zero-padded to 2N = 4 cols and transformed; the
@@ -1319,7 +1319,7 @@ void orc_encode_concatenated(const uint64_t *data, int64_t n, int rate0, int rat
   }
 }
 
-/* ================================================ Whir_Batch_Open (a17) */
+/* ================================================ Whir_Batch_Open */
 /* Whir_Batch_Open (Whir.cpp:706-898) opens k polynomials of non-increasing
  * sizes: the largest is folded by WHIR iterations, and whenever it reaches
  * the size of the next ones they are merged into it (aggregate_arrays,

@@ -8,6 +8,7 @@
 #include <utility>
 
 #include "../../include/gbz.h"
+#include "gbz_batch_open.cuh"
 #include "gbz_copcs.cuh"
 #include "gbz_prover.cuh"
 #include "gbz_rounds.cuh"
@@ -1112,6 +1113,75 @@ gbz_status gbz_whir_aggregate_commitments(gbz_ctx *ctx, int k, const uint64_t *c
   copy_out(ctx, (fe *)codeword, dcw, 16 * n, mem);
   copy_out(ctx, levels, dlv, 32 * nh, mem);
   GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END(ctx)
+}
+
+gbz_status gbz_whir_batch_schedule(int k, const uint64_t *sizes, int rate, int whir_k, int *steps, int32_t *kappa,
+                                   int32_t *aggr, uint64_t *cw_len, uint64_t *transcript_bytes) {
+  try {
+    const BatchPlan P = batch_plan(k, sizes, rate, whir_k);
+    if (steps) *steps = (int)P.kappa.size();
+    for (size_t i = 0; i < P.kappa.size(); i++) {
+      if (kappa) kappa[i] = P.kappa[i];
+      if (aggr) aggr[i] = P.aggr[i];
+    }
+    if (cw_len)
+      for (int i = 0; i < k; i++) cw_len[i] = P.cw_len[i];
+    if (transcript_bytes) *transcript_bytes = P.transcript_bytes;
+  } catch (const ArgError &) {
+    return GBZ_EINVAL;
+  }
+  return GBZ_OK;
+}
+
+gbz_status gbz_whir_batch_open(gbz_ctx *ctx, int k, const uint64_t *const *arrays, const uint64_t *sizes,
+                               const uint64_t *const *codewords, const uint8_t *levels0,
+                               const uint64_t *const *betas, const uint64_t *K0, int rate, int whir_k,
+                               gbz_prng *prng, uint8_t *transcript, uint64_t capacity, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(arrays, "arrays");
+  need(codewords, "codewords");
+  need(betas, "betas");
+  need(levels0, "levels0");
+  need(K0, "K0");
+  need(prng, "prng");
+  need(transcript, "transcript");
+  const BatchPlan P = batch_plan(k, sizes, rate, whir_k);
+  if (capacity < P.transcript_bytes) throw ArgError("transcript capacity below gbz_whir_batch_schedule's size");
+  std::vector<const fe *> da(k, nullptr), db(k, nullptr), dc(k, nullptr);
+  for (int i = 0; i < k; i++) {
+    if (i && !P.cw_len[i]) continue;  // never merged: not read
+    need(arrays[i], "arrays[i]");
+    need(betas[i], "betas[i]");
+    need(codewords[i], "codewords[i]");
+    da[i] = dev_view(ctx, 400 + i, (const fe *)arrays[i], 16 * P.sizes[i], mem, true);
+    db[i] = dev_view(ctx, 470 + i, (const fe *)betas[i], 16 * P.sizes[i], mem, true);
+    dc[i] = dev_view(ctx, 540 + i, (const fe *)codewords[i], 16 * P.cw_len[i], mem, true);
+  }
+  const uint64_t L0 = P.cw_len[0];
+  const uint8_t *dlv = dev_view(ctx, 610, levels0, 32 * merkle_hashes(L0), mem, true);
+  if (!ctx->st) GBZ_CUDA(cudaMalloc(&ctx->st, sizeof(ProofState)));
+  if (!ctx->ub_scratch) GBZ_CUDA(cudaMalloc(&ctx->ub_scratch, sizeof(fe) * kUpdateBetasScratch));
+  uint8_t *dtr = mem == GBZ_MEM_DEVICE ? transcript : (uint8_t *)ctx->buf(620, P.transcript_bytes);
+  BatchResources R;
+  R.s = ctx->stream;
+  R.buf = [ctx](int slot, uint64_t bytes) { return ctx->buf(slot, bytes); };
+  R.tables = [ctx](int lg) -> NttTables & { return ctx->tables(lg); };
+  R.st = ctx->st;
+  R.ub_scratch = ctx->ub_scratch;
+  glibc_prng g;
+  static_assert(sizeof(g) == sizeof(gbz_prng), "generator state layout");
+  std::memcpy(&g, prng, sizeof(g));
+  batch_open_enqueue(R, P, da.data(), db.data(), dc.data(), dlv, fe_make(K0[0], K0[1]), g, dtr);
+  copy_out(ctx, transcript, dtr, P.transcript_bytes, mem);
+  uint32_t err = 0;
+  GBZ_CUDA(cudaMemcpyAsync(&g, &ctx->st->prng, sizeof(g), cudaMemcpyDeviceToHost, ctx->stream));
+  GBZ_CUDA(cudaMemcpyAsync(&err, &ctx->st->error, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(prng, &g, sizeof(g));
+  if (err) return fail(ctx, GBZ_ECHECK, "batch open: a device-side consistency check failed (flags " +
+                                         std::to_string(err) + ")");
   API_END(ctx)
 }
 

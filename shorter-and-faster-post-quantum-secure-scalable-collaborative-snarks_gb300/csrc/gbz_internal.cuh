@@ -12,8 +12,10 @@ namespace gbz {
 
 constexpr int kMaxLogN = 28;        // largest NTT / codeword: 2^28 elements
 constexpr int kMaxQueries = 256;    // WHIR queries per iteration (rate 2 needs 200)
-constexpr int kWhirLogK = 2;        // folding factor 4 (whir_k = 4)
+constexpr int kWhirLogK = 2;        // folding factor 4 (whir_k = 4) of the plain prover
 constexpr int kWhirK = 1 << kWhirLogK;
+constexpr int kMaxWhirLogK = 4;     // batch opening: folding factors up to 16
+constexpr int kFinalMax = 16;       // largest final polynomial of an opening
 
 // Transcript record tags (one u32 tag, one u32 count, then count units).
 enum : uint32_t {
@@ -21,8 +23,19 @@ enum : uint32_t {
   T_SC_FINAL = 6, T_WHIR_POLY = 7, T_WHIR_CHALLENGE = 8, T_WHIR_ROOT = 9,
   T_WHIR_QUERIES = 10, T_WHIR_REPLIES = 11, T_WHIR_ANSWERS = 12, T_WHIR_PATHS = 13,
   T_WHIR_COMBINE = 14, T_WHIR_K = 15, T_FINAL_POLY = 16, T_FINAL_POINT = 17,
-  T_FINAL_EVAL = 18
+  T_FINAL_EVAL = 18, T_SCHEDULE = 19, T_AGGR_CHALLENGES = 20, T_AGGR_K = 21, T_AGGR_QUERIES = 22,
+  T_AGGR_PATHS = 23, T_AGGR_ROOT = 24
 };
+
+// Transcript records start at 4-byte multiples (query records have 4-byte
+// units), so every store into the transcript is a 32-bit store.
+__device__ __forceinline__ void put_fe(uint8_t *tr, uint64_t off, fe v) {
+  uint32_t *p = reinterpret_cast<uint32_t *>(tr + off);
+  p[0] = (uint32_t)v.re;
+  p[1] = (uint32_t)(v.re >> 32);
+  p[2] = (uint32_t)v.im;
+  p[3] = (uint32_t)(v.im >> 32);
+}
 
 // Verifier-side randomness and running claims of one proof, resident in
 // device memory so that the whole proof is one stream of launches with no
@@ -36,8 +49,8 @@ struct ProofState {
   fe K;                       // WHIR running claim
   fe chal[64];                // sumcheck challenges (the claim point)
   fe z[64];                   // evaluation point
-  fe rw[kWhirLogK];           // WHIR round challenges of the current iteration
-  fe hw[kWhirLogK][3];        // WHIR round messages of the current iteration
+  fe rw[kMaxWhirLogK];        // WHIR round challenges of the current iteration
+  fe hw[kMaxWhirLogK][3];     // WHIR round messages of the current iteration
   fe fin_r[8];                // final point
   int32_t q[kMaxQueries];     // queries scaled to the new codeword
   fe comb[kMaxQueries];       // update_betas combination weights c_i = r^(i+1)

@@ -26,15 +26,6 @@ namespace {
 
 // ------------------------------------------------------------ kernels
 
-// Transcript records start at 4-byte multiples (query records have 4-byte
-// units), so every store into the transcript is a 32-bit store.
-__device__ __forceinline__ void put_fe(uint8_t *tr, uint64_t off, fe v) {
-  uint32_t *p = reinterpret_cast<uint32_t *>(tr + off);
-  p[0] = (uint32_t)v.re;
-  p[1] = (uint32_t)(v.re >> 32);
-  p[2] = (uint32_t)v.im;
-  p[3] = (uint32_t)(v.im >> 32);
-}
 
 // The glibc generator state is worked on in shared memory by one thread and
 // written back: its table is indexed dynamically, and hundreds of draws on
@@ -136,27 +127,6 @@ __global__ void k_sc_final(ProofState *st, const fe *v1, const fe *v2, uint8_t *
   st->K = a;  // Whir_Open: K = claims[0].first
 }
 
-// WHIR sumcheck round (whir_sumcheck, Whir.cpp:233-249): message h, the
-// consistency check K == h(0) + h(1), challenge F::_random(), K = h(r).
-__global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int i, uint8_t *tr,
-                             uint64_t off_poly, uint64_t off_chal) {
-  fe H[3];
-  sum_partials(partial, blocks, H);
-  if (threadIdx.x) return;
-  fe h01 = fadd(quad_eval(H[0], H[1], H[2], fe_zero()), quad_eval(H[0], H[1], H[2], fe_one()));
-  if (!fe_eq(h01, st->K)) st->error |= 2u;
-  for (int k = 0; k < 3; k++) {
-    put_fe(tr, off_poly + 16 * k, H[k]);
-    st->hw[i][k] = H[k];
-  }
-  __shared__ glibc_prng g;
-  g = st->prng;
-  fe r = prng_field(g);
-  st->prng = g;
-  st->rw[i] = r;
-  put_fe(tr, off_chal, r);
-  st->K = quad_eval(H[0], H[1], H[2], r);
-}
 
 // omega^e from a two-level power table (lo[e & 4095] * hi[e >> 12]).
 __device__ __forceinline__ fe pow_table(const fe *lo, const fe *hi, uint64_t e) {
@@ -247,19 +217,49 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
   }
 }
 
-// Final round of Whir_Open (Whir.cpp:426-446): the remaining polynomial,
-// log2|arr| F::_random draws and evaluate_vector(b, r).
-// open_tree_blake (merkle_tree.cpp:320-335) for every query: sibling
-// (pos >> d) ^ 1 of level d (levels of L/4, L/8, ... hashes stored back to
-// back, level d starting at L/2 - (L/2 >> d)), one hash per thread so that
-// all the scattered tree reads are in flight together.
-__global__ void k_whir_paths(const uint8_t *tree, uint64_t L, int l, uint8_t *tr, uint64_t off_q, uint64_t off_path) {
-  const int depth = 63 - __clzll((long long)(L / 4));
+__global__ void k_copy32(const uint8_t *src, uint8_t *dst) {
+  if (threadIdx.x < 8)
+    reinterpret_cast<uint32_t *>(dst)[threadIdx.x] = reinterpret_cast<const uint32_t *>(src)[threadIdx.x];
+}
+
+}  // namespace
+
+// --------------------------------------- kernels shared with the batch opening
+
+// WHIR sumcheck round (whir_sumcheck, Whir.cpp:233-249): message h, the
+// consistency check K == h(0) + h(1), challenge F::_random(), K = h(r).
+__global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int i, uint8_t *tr,
+                             uint64_t off_poly, uint64_t off_chal) {
+  fe H[3];
+  sum_partials(partial, blocks, H);
+  if (threadIdx.x) return;
+  fe h01 = fadd(quad_eval(H[0], H[1], H[2], fe_zero()), quad_eval(H[0], H[1], H[2], fe_one()));
+  if (!fe_eq(h01, st->K)) st->error |= 2u;
+  for (int k = 0; k < 3; k++) {
+    put_fe(tr, off_poly + 16 * k, H[k]);
+    st->hw[i][k] = H[k];
+  }
+  __shared__ glibc_prng g;
+  g = st->prng;
+  fe r = prng_field(g);
+  st->prng = g;
+  st->rw[i] = r;
+  put_fe(tr, off_chal, r);
+  st->K = quad_eval(H[0], H[1], H[2], r);
+}
+
+// open_tree_blake (merkle_tree.cpp:320-335) for every query in a tree of
+// `leaves` leaf hashes: sibling (pos >> d) ^ 1 of level d (levels stored back
+// to back, level d starting at 2 leaves - 2 (leaves >> d)), one hash per
+// thread so that all the scattered tree reads are in flight together.
+__global__ void k_whir_paths(const uint8_t *tree, uint64_t leaves, int l, uint8_t *tr, uint64_t off_q,
+                             uint64_t off_path) {
+  const int depth = 63 - __clzll((long long)leaves);
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (uint64_t)l * depth) return;
   const int i = (int)(t / depth), d = (int)(t % depth);
   const uint64_t q = (uint64_t)(uint32_t)reinterpret_cast<const int32_t *>(tr + off_q)[i];
-  const uint64_t lvl = L / 2 - ((L / 2) >> d);
+  const uint64_t lvl = 2 * leaves - 2 * (leaves >> d);
   const uint4 *src = reinterpret_cast<const uint4 *>(tree + 32 * (lvl + ((q >> d) ^ 1ull)));
   const uint4 h0 = src[0], h1 = src[1];
   // transcript payloads are only 4-byte aligned
@@ -268,11 +268,24 @@ __global__ void k_whir_paths(const uint8_t *tree, uint64_t L, int l, uint8_t *tr
   dst[4] = h1.x; dst[5] = h1.y; dst[6] = h1.z; dst[7] = h1.w;
 }
 
-__global__ void k_final(ProofState *st, const fe *arr, fe *b, int m, uint8_t *tr, uint64_t off_poly,
-                        uint64_t off_point, uint64_t off_eval) {
+// Final round of Whir_Open (Whir.cpp:426-446) and of Whir_Batch_Open
+// (:840-869): the remaining polynomial (m <= kFinalMax entries), log2 m
+// F::_random draws and evaluate_vector(b, r).  With check_K, the flag 8 is
+// raised unless K equals sum arr * b (verification step 2, :848-855).
+__global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
+                        uint64_t off_point, uint64_t off_eval, int check_K) {
   __shared__ glibc_prng g;
   if (threadIdx.x) return;
-  for (int i = 0; i < m; i++) put_fe(tr, off_poly + 16 * i, arr[i]);
+  if (m < 1 || m > kFinalMax) {
+    st->error |= 16u;
+    return;
+  }
+  fe Kc = st->K;
+  for (int i = 0; i < m; i++) {
+    put_fe(tr, off_poly + 16 * i, arr[i]);
+    Kc = fsub(Kc, fmul(arr[i], b[i]));
+  }
+  if (check_K && !fe_eq(Kc, fe_zero())) st->error |= 8u;
   const int lg = 31 - __clz(m);
   fe r[8];
   g = st->prng;
@@ -281,7 +294,7 @@ __global__ void k_final(ProofState *st, const fe *arr, fe *b, int m, uint8_t *tr
     put_fe(tr, off_point + 16 * i, r[i]);
   }
   st->prng = g;
-  fe v[8];
+  fe v[kFinalMax];
   for (int i = 0; i < m; i++) v[i] = b[i];
   for (int i = 0; i < lg; i++) {
     fe om = fsub(fe_one(), r[i]);
@@ -290,13 +303,6 @@ __global__ void k_final(ProofState *st, const fe *arr, fe *b, int m, uint8_t *tr
   }
   put_fe(tr, off_eval, v[0]);
 }
-
-__global__ void k_copy32(const uint8_t *src, uint8_t *dst) {
-  if (threadIdx.x < 8)
-    reinterpret_cast<uint32_t *>(dst)[threadIdx.x] = reinterpret_cast<const uint32_t *>(src)[threadIdx.x];
-}
-
-}  // namespace
 
 // ------------------------------------------------------------ host side
 
@@ -568,7 +574,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     {
       const uint64_t hashes = (uint64_t)l * depth;  // depth >= 2: every queried codeword has 16+ entries
       RUN(PC_QUERY, 1,
-          k_whir_paths<<<(unsigned)((hashes + 127) / 128), 128, 0, s>>>(qa.tree, L, l, tr, qa.off_q, qa.off_path));
+          k_whir_paths<<<(unsigned)((hashes + 127) / 128), 128, 0, s>>>(qa.tree, L / 4, l, tr, qa.off_q, qa.off_path));
       if (!dry && hashes == 0) throw ArgError("prover: empty authentication paths");
     }
     // update_betas: b[j] += sum_i c_i omega_NL^{q_i j} is the forward
@@ -594,7 +600,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   uint64_t off_poly = lay.rec(T_FINAL_POLY, (uint32_t)m, 16);
   uint64_t off_point = lay.rec(T_FINAL_POINT, ilog2(m), 16);
   uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
-  RUN(PC_PROTOCOL, 1, k_final<<<1, 32, 0, s>>>(st, a, p.vb[1], (int)m, tr, off_poly, off_point, off_eval));
+  RUN(PC_PROTOCOL, 1, k_final<<<1, 32, 0, s>>>(st, a, p.vb[1], (int)m, tr, off_poly, off_point, off_eval, 0));
   if (!dry) GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_commit[iter], 0));  // join the commit stream
 #undef RUN
 #undef RUN_ON

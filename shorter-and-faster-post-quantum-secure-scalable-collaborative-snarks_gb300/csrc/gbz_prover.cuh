@@ -89,6 +89,17 @@ struct ProofPlan {
   NttTables &tables(int lg);
 };
 
+// Protocol kernels shared by the prover and the batch opening
+// (gbz_prover.cu): a WHIR sumcheck round from the reduction partials, the
+// authentication paths of the queries in a tree of `leaves` leaf hashes,
+// and the final round.
+__global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int i, uint8_t *tr,
+                             uint64_t off_poly, uint64_t off_chal);
+__global__ void k_whir_paths(const uint8_t *tree, uint64_t leaves, int l, uint8_t *tr, uint64_t off_q,
+                             uint64_t off_path);
+__global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
+                        uint64_t off_point, uint64_t off_eval, int check_K);
+
 std::unique_ptr<ProofPlan> plan_create(int logn, int rate);
 // Enqueues one proof on stream s (dry: only computes the layout).  With
 // seed_in_state the PRNG seed is read from the plan's state (written by

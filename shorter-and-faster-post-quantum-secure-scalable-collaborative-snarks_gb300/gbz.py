@@ -47,6 +47,7 @@ EXPORTS = (
     "gbz_tensor_eval_vector", "gbz_pcs_sumcheck_phase3", "gbz_ntt_set_shape", "gbz_ntt_get_shape",
     "gbz_ntt_autotune", "gbz_merkle_set_fusion", "gbz_merkle_get_fusion", "gbz_merkle_autotune",
     "gbz_set_graphs", "gbz_ntt_full_twiddles", "gbz_encode_concatenated", "gbz_leader_root",
+    "gbz_whir_batch_schedule", "gbz_whir_batch_open",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -158,6 +159,8 @@ def _load():
         "gbz_whir_aggregate_arrays": (c_int, [vp, c_int, vp, c_int, vp, u64, vp, vp, vp, vp, vp, c_int]),
         "gbz_whir_aggregate_commitments": (c_int, [vp, c_int, vp, u64, vp, c_int, c_int, vp, vp, vp, c_int]),
         "gbz_party_sumcheck": (c_int, [vp, c_int, vp, vp, vp, u64, c_int, vp, c_int, vp, vp, vp, vp, vp, vp, c_int]),
+        "gbz_whir_batch_schedule": (c_int, [c_int, vp, c_int, c_int, vp, vp, vp, vp, vp]),
+        "gbz_whir_batch_open": (c_int, [vp, c_int, vp, vp, vp, vp, vp, vp, c_int, c_int, vp, vp, u64, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -444,6 +447,36 @@ class Context:
                                                  MEM_HOST))
         return arr, b, K
 
+    def whir_batch_open(self, arrays, codewords, levels0, betas, K0, rate, whir_k=4, prng=None, mem=None):
+        """Whir_Batch_Open (Whir.cpp:706-898): the transcript (uint8 array, on
+        the device when the inputs are torch CUDA tensors) and the advanced
+        generator.  codewords[i] must have whir_batch_schedule's length for
+        array i; entries of arrays that are never merged may be None."""
+        k = len(arrays)
+        on_dev = _mem(arrays[0]) == MEM_DEVICE if mem is None else mem == MEM_DEVICE
+        conv = (lambda x: x) if on_dev else _fe
+        arrs, bets = [conv(a) for a in arrays], [conv(b) for b in betas]
+        sizes = np.array([int(a.shape[0]) for a in arrs], dtype=np.uint64)
+        sch = whir_batch_schedule([int(x) for x in sizes], rate, whir_k)
+        if sch is None:
+            raise GbzError(EINVAL, "Whir_Batch_Open cannot run these sizes")
+        cws = [conv(c) if c is not None else None for c in codewords]
+        plist = lambda vs: ctypes.cast((ctypes.c_void_p * max(len(vs), 1))(*[_ptr(v) if v is not None else None
+                                                                           for v in vs]), ctypes.c_void_p)
+        lv = levels0 if on_dev else np.ascontiguousarray(levels0, dtype=np.uint8)
+        K0 = np.ascontiguousarray(K0, dtype=np.uint64).reshape(2)
+        g = prng if isinstance(prng, Prng) else Prng(1 if prng is None else prng)
+        nbytes = sch[3]
+        if on_dev:
+            import torch
+            out = torch.empty(nbytes, dtype=torch.uint8, device=arrays[0].device)
+        else:
+            out = np.zeros(nbytes, dtype=np.uint8)
+        self.check(lib.gbz_whir_batch_open(self.h, k, plist(arrs), _ptr(sizes), plist(cws), _ptr(lv), plist(bets),
+                                           _ptr(K0), rate, whir_k, ctypes.addressof(g), _ptr(out), nbytes,
+                                           MEM_DEVICE if on_dev else MEM_HOST))
+        return out, g
+
     def aggregate_commitments(self, codewords, r, rate, whir_k=4, prng=None):
         """aggregate_commitments (Whir.cpp:547): (codeword, levels, prng)."""
         cws = [_fe(x) for x in codewords]
@@ -678,6 +711,23 @@ class Prng(ctypes.Structure):
         out = np.zeros(2, dtype=np.uint64)
         lib.gbz_prng_field(ctypes.addressof(self), _ptr(out))
         return out
+
+
+def whir_batch_schedule(sizes, rate, whir_k=4):
+    """(kappas, merge flags, codeword length per array, transcript bytes) of
+    Whir_Batch_Open for these sizes, or None when the reference cannot run
+    them (gbz_whir_batch_schedule)."""
+    k = len(sizes)
+    sz = np.ascontiguousarray(sizes, dtype=np.uint64)
+    steps = ctypes.c_int(0)
+    kap, agg = np.zeros(64, dtype=np.int32), np.zeros(64, dtype=np.int32)
+    cwl, nb = np.zeros(max(k, 1), dtype=np.uint64), ctypes.c_uint64(0)
+    rc = lib.gbz_whir_batch_schedule(k, _ptr(sz), rate, whir_k, ctypes.byref(steps), _ptr(kap), _ptr(agg),
+                                     _ptr(cwl), ctypes.byref(nb))
+    if rc != OK:
+        return None
+    n = steps.value
+    return [int(x) for x in kap[:n]], [int(x) for x in agg[:n]], [int(x) for x in cwl[:k]], int(nb.value)
 
 
 def field_ops_host(a, b):

@@ -23,9 +23,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 FULL = os.path.join(ROOT, "oracle", "_ref", "ref_full")
 
-# Witness seed convention: 0x5EED0000 + config * 2^16 + instance.
-SEED_C1 = 0x5EED0000 + 1 * 65536
-SEED_C2 = 0x5EED0000 + 2 * 65536
+# Witness seeds: 0x5EED0000 + workload * 2^16 + instance (1: n = 2^18 at rate 1/4, 2: n = 2^24 at rate 1/2).
+SEED_2E18 = 0x5EED0000 + 1 * 65536
+SEED_2E24 = 0x5EED0000 + 2 * 65536
 
 
 def run(*args):
@@ -126,8 +126,8 @@ def main():
     proofs.append({"logn": 6, "rate": 4, "seed": 33, "prng_seed": 1, "file": "prove_6_4.bin"})
     cases = [(5, 2, 34, 1), (7, 2, 35, 1), (8, 4, 36, 7), (10, 2, 37, 1), (11, 4, 38, 99),
              (12, 2, 39, 1), (14, 4, 40, 1), (16, 2, 41, 5),
-             (18, 4, SEED_C1, 1),   # configuration 1: n = 2^18, rate 1/4
-             (24, 2, SEED_C2, 1)]   # configuration 2: n = 2^24, rate 1/2
+             (18, 4, SEED_2E18, 1),   # n = 2^18, rate 1/4
+             (24, 2, SEED_2E24, 1)]   # n = 2^24, rate 1/2
     for logn, rate, seed, ps in cases:
         data, dt = run("prove", logn, rate, seed, ps, 1)
         proofs.append({"logn": logn, "rate": rate, "seed": seed, "prng_seed": ps, "bytes": len(data),

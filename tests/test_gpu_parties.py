@@ -1,4 +1,4 @@
-"""Configuration 4 at test size: party shares committed and proved on one
+"""The party-share workload at test size: party shares committed and proved on one
 device (per-party coPCS Encode + column Merkle + leader root, then the
 distributed sumcheck over all parties) equal the oracle's composition of
 the same steps."""
