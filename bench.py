@@ -522,6 +522,36 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     ph3 = lambda: ctx.check(gbz.lib.gbz_pcs_sumcheck_phase3(ctx.h, Bv.data_ptr(), 1 << lb, gbz._ptr(qs), 100,
                                                             gbz._ptr(s3), 16, 2, 3, D))
     rec("pcs_phase3_2^%d_l100" % lb, timed(ph3), note="geometric update of 100 terms over 2^%d rows" % lb)
+    del Bv
+    # Whir_Batch_Open of three polynomials of 2^22, 2^20, 2^18 at rate 1/2 (folding 4), device resident
+    logs = [22 - shift, 20 - shift, 18 - shift]
+    sizes = [1 << x for x in logs]
+    sch = gbz.whir_batch_schedule(sizes, 2, 4)
+    if sch is not None:
+        barr = [rnd(x) for x in sizes]
+        bet = []
+        for x in logs:
+            pt = rnd(x)
+            b = torch.empty((1 << x, 2), dtype=torch.int64, device="cuda")
+            ctx.check(gbz.lib.gbz_precompute_beta(ctx.h, pt.data_ptr(), x, b.data_ptr(), D))
+            bet.append(b)
+        cws = []
+        lv0 = None
+        for i, (a, L) in enumerate(zip(barr, sch[2])):
+            c = torch.empty((L, 2), dtype=torch.int64, device="cuda")
+            lv = torch.empty((L // 2 - 1, 32), dtype=torch.uint8, device="cuda")
+            ctx.check(gbz.lib.gbz_whir_commit(ctx.h, a.data_ptr(), a.shape[0], L // a.shape[0], c.data_ptr(),
+                                              lv.data_ptr(), D))
+            cws.append(c)
+            if i == 0:
+                lv0 = lv
+        h = ctx.sumcheck_round(gbz.SC_QUADRATIC, [barr[0], bet[0]])
+        K0 = np.array([(int(h[0][k]) + int(h[1][k]) + 2 * int(h[2][k])) % P61 for k in (0, 1)], dtype=np.uint64)
+        ctx.whir_batch_open(barr, cws, lv0, bet, K0, 2, 4, prng=1)  # checked on the device (GBZ_ECHECK otherwise)
+        bo = lambda: ctx.whir_batch_open(barr, cws, lv0, bet, K0, 2, 4, prng=1)
+        rec("whir_batch_open_2^%d_2^%d_2^%d_rate2" % tuple(logs), timed(bo),
+            note="Whir_Batch_Open: %d schedule steps, 2 merges, %d transcript bytes (host call incl. planning "
+                 "and the final synchronisation)" % (len(sch[0]), sch[3]))
     return {"rows": rows}
 
 
