@@ -111,10 +111,11 @@ struct NttTables {
 // `tmp` must hold 2^logn elements when logn > 13.  in may equal out.
 void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                 cudaStream_t s);
-// acc[j] += sum_i c[i] * omega_L^{q[i] j} for j < nacc (L = 2^t.logn > 2^13):
-// the forward transform of the sparse vector sum_i c_i e_{q_i}, with the
-// empty columns of the first pass skipped and only the first nacc outputs
-// of the second pass accumulated.  tmp holds L elements.  With q_shift > 0
+// acc[j] += sum_i c[i] * omega_L^{q[i] j} for j < nacc (L = 2^t.logn > 2^13,
+// 1 <= l <= kMaxQueries): the forward transform of the sparse vector
+// sum_i c_i e_{q_i} as one second-pass launch whose rows are formed directly
+// from the entries (the first pass of a few nonzeros is skipped), only the
+// first nacc outputs accumulated.  tmp holds 768 bytes of column chains.  With q_shift > 0
 // the positions are q[i] >> q_shift (the caller guarantees the dropped bits
 // are zero, so omega_L^{q j} = omega_{L'}^{(q >> shift) j} on t of length L').
 void ntt_sparse_accumulate(const NttTables &t, const int32_t *q, const fe *c, int l, fe *acc, uint64_t nacc,

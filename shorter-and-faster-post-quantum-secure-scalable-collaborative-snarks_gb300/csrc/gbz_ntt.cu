@@ -54,11 +54,18 @@ struct PassArgs {
   const fe *tw_full; // pass A: omega_L^{n1 k2} at the output address n1 + N1 k2 (optional)
   fe scale;
   int logS, logB, has_scale, inverse;
-  // Sparse input (pass A only): x[sp_q[i] >> sp_shift] += sp_c[i] for
-  // i < sp_l, zero elsewhere.  Columns without an entry skip the transform.
+  // Sparse rows (second pass of a sparse transform, the first pass folded
+  // in): the input is sum_i sp_c[i] e_{q_i}, q_i = sp_q[i] >> sp_shift;
+  // entries of one column (q mod the row length) are chained by sp_next
+  // from the one flagged in sp_lead; sp_lo / sp_hi give omega_L^e and
+  // sp_mask = L - 1.
   const int32_t *sp_q;
   const fe *sp_c;
   int sp_l, sp_shift;
+  const int16_t *sp_next;
+  const uint8_t *sp_lead;
+  const fe *sp_lo, *sp_hi;
+  uint64_t sp_mask;
   // Accumulating output: out[addr] += v for addr < acc_n, other outputs dropped.
   uint64_t acc_n;
   int acc;
@@ -245,25 +252,30 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
   }
   __shared__ int nonzero;
   if (a.sp_l > 0) {
-    // Sparse input: zero the tile, then one thread adds the entries of this
-    // CTA's columns in list order (entries may share a position).
+    // Sparse rows: row k2 of the intermediate holds, in column n1, the sum
+    // over the entries q = n1 (mod row length) of c * omega_L^{q k2}: the
+    // first pass's column transform of a few nonzeros times its outer
+    // twiddle, formed directly, so the first pass and its intermediate
+    // array are skipped.  One thread per (first entry of a column, row).
     for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) sm[e] = fe_zero();
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int nz = 0;
-      const uint64_t ncol = a.in_jstride;  // column stride = number of columns
-      for (int i = 0; i < a.sp_l; i++) {
-        const uint64_t q = (uint64_t)((uint32_t)a.sp_q[i] >> a.sp_shift);
-        const uint64_t g = q & (ncol - 1);
-        if (g >= g0 && g < g0 + (1u << logB)) {
-          const uint32_t idx = swz((uint32_t)((g - g0) << logS) + (uint32_t)(q / ncol));
-          sm[idx] = fadd(sm[idx], a.sp_c[i]);
-          nz = 1;
-        }
+    const uint32_t l = (uint32_t)a.sp_l;
+    for (uint32_t t = threadIdx.x; t < (l << logB); t += blockDim.x) {
+      const uint32_t i = t % l, b = t / l;
+      if (!a.sp_lead[i]) continue;
+      const uint64_t k2 = g0 + b;
+      fe v = fe_zero();
+      int u = (int)i;
+      for (uint32_t it = 0; it < l && u >= 0; it++, u = a.sp_next[u]) {
+        const uint64_t q = (uint64_t)((uint32_t)a.sp_q[u] >> a.sp_shift);
+        const uint64_t ex = (q * k2) & a.sp_mask;
+        v = fadd(v, fmul(a.sp_c[u], fmul(a.sp_lo[ex & ((1u << kTwLoBits) - 1)], a.sp_hi[ex >> kTwLoBits])));
       }
-      nonzero = nz;
+      const uint32_t n1 = ((uint32_t)a.sp_q[i] >> a.sp_shift) & (S - 1);
+      sm[swz((b << logS) + n1)] = v;
     }
     __syncthreads();
+    nonzero = 1;
   } else {
     nonzero = 1;
     // A thread stages at most kPerThread elements (blockDim >= total / 8);
@@ -384,6 +396,27 @@ void ensure_wq() {
   }
   g_wq_device = dev;
   GBZ_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+}
+
+// Column chains of a sparse input: next[t] = the next entry with the same
+// column ((q >> shift) & colmask), -1 at the end; lead[t] = 1 for the first
+// entry of each column.  One thread per entry (l <= kMaxQueries).
+__global__ void sparse_chain_kernel(const int32_t *q, int l, int shift, uint32_t colmask, int16_t *next,
+                                    uint8_t *lead) {
+  __shared__ uint32_t col[kMaxQueries];
+  const int t = threadIdx.x;
+  if (t < l) col[t] = ((uint32_t)q[t] >> shift) & colmask;
+  __syncthreads();
+  if (t >= l) return;
+  int nx = -1;
+  uint8_t first = 1;
+  for (int u = 0; u < l; u++) {
+    if (col[u] != col[t]) continue;
+    if (u < t) first = 0;
+    else if (u > t && nx < 0) nx = u;
+  }
+  next[t] = (int16_t)nx;
+  lead[t] = first;
 }
 
 void launch_pass(const PassArgs &a, uint64_t groups, cudaStream_t s) {
@@ -564,7 +597,7 @@ namespace {
 
 // Shared by the dense transform and the sparse/accumulating variant.
 void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
-                  const int32_t *sp_q, const fe *sp_c, int sp_l, int sp_shift, uint64_t acc_n, cudaStream_t s) {
+                  cudaStream_t s) {
   const int logn = t.logn;
   const uint64_t L = 1ull << logn;
   if (n_valid > L) n_valid = L;
@@ -610,10 +643,6 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   a.tw_hi = inverse ? t.hi_inv : t.hi_fwd;
   a.tw_full = g_use_outer ? outer_table_get(logn, k1, inverse) : nullptr;
   a.has_scale = 0;
-  a.sp_q = sp_q;
-  a.sp_c = sp_c;
-  a.sp_l = sp_l;
-  a.sp_shift = sp_shift;
   launch_pass(a, N1, s);
   // pass B: rows k2 < N2, length N1, contiguous
   PassArgs b = a;
@@ -630,11 +659,6 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   b.tw_hi = nullptr;
   b.tw_full = nullptr;
   b.has_scale = inverse;
-  b.sp_q = nullptr;
-  b.sp_c = nullptr;
-  b.sp_l = 0;
-  b.acc = acc_n ? 1 : 0;
-  b.acc_n = acc_n;
   launch_pass(b, N2, s);
 }
 
@@ -642,7 +666,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
 
 void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                 cudaStream_t s) {
-  ntt_two_pass(t, in, n_valid, out, tmp, inverse, nullptr, nullptr, 0, 0, 0, s);
+  ntt_two_pass(t, in, n_valid, out, tmp, inverse, s);
 }
 
 void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t j_valid, fe *out, uint64_t count,
@@ -719,7 +743,44 @@ void ntt_sparse_accumulate(const NttTables &t, const int32_t *q, const fe *c, in
                            fe *tmp, cudaStream_t s, int q_shift) {
   if (t.logn <= kSubLog) throw ArgError("sparse transform needs a two-pass length");
   if (q_shift < 0 || q_shift > 8) throw ArgError("sparse transform: position shift out of range");
-  ntt_two_pass(t, nullptr, 0, acc, tmp, false, q, c, l, q_shift, nacc, s);
+  if (l < 1 || l > kMaxQueries) throw ArgError("sparse transform: 1..256 entries");
+  const int logn = t.logn;
+  const uint64_t L = 1ull << logn;
+  const NttShape sh = g_shape[logn].k1 > 0 ? g_shape[logn] : ntt_default_shape(logn);
+  const int k1 = sh.k1, k2 = logn - k1;
+  const uint64_t N1 = 1ull << k1, N2 = 1ull << k2;
+  // column chains in the (otherwise unused) scratch
+  int16_t *next = reinterpret_cast<int16_t *>(tmp);
+  uint8_t *lead = reinterpret_cast<uint8_t *>(next + kMaxQueries);
+  sparse_chain_kernel<<<1, kMaxQueries, 0, s>>>(q, l, q_shift, (uint32_t)(N1 - 1), next, lead);
+  GBZ_CUDA(cudaGetLastError());
+  PassArgs b{};
+  b.wh = t.sub_fwd;
+  b.scale = t.inv_len;
+  b.inverse = 0;
+  b.j_valid = 1u << kSubLog;
+  b.in = nullptr;
+  b.out = acc;
+  b.n_valid = L;
+  b.in_gstride = N1;
+  b.in_jstride = 1;
+  b.out_gstride = 1;
+  b.out_kstride = N2;
+  b.logS = k1;
+  b.logB = sh.logBB;
+  b.has_scale = 0;
+  b.acc = 1;
+  b.acc_n = nacc;
+  b.sp_q = q;
+  b.sp_c = c;
+  b.sp_l = l;
+  b.sp_shift = q_shift;
+  b.sp_next = next;
+  b.sp_lead = lead;
+  b.sp_lo = t.lo_fwd;
+  b.sp_hi = t.hi_fwd;
+  b.sp_mask = L - 1;
+  launch_pass(b, N2, s);
 }
 
 }  // namespace gbz
