@@ -442,7 +442,7 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
   const uint64_t off_point = lay.rec(T_FINAL_POINT, ilog2(m), 16);
   const uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
   if (!dry) {
-    k_final<<<1, 32, 0, s>>>(st, A[ai], B[ai], (int)m, tr, off_poly, off_point, off_eval, 1);
+    k_final<<<1, 32, 0, s>>>(st, A[ai], B[ai], (int)m, tr, off_poly, off_point, off_eval, 1, nullptr);
     GBZ_CUDA(cudaGetLastError());
   }
 }

@@ -16,6 +16,7 @@ constexpr int kWhirLogK = 2;        // folding factor 4 (whir_k = 4) of the plai
 constexpr int kWhirK = 1 << kWhirLogK;
 constexpr int kMaxWhirLogK = 4;     // batch opening: folding factors up to 16
 constexpr int kFinalMax = 16;       // largest final polynomial of an opening
+constexpr int kMaxWhirIter = 16;    // WHIR iterations of one proof (2^26 at rate 2 needs 12)
 
 // Transcript record tags (one u32 tag, one u32 count, then count units).
 enum : uint32_t {
@@ -59,6 +60,14 @@ struct ProofState {
   uint32_t error;             // non-zero: a device-side consistency check failed
   uint32_t seed_in;           // PRNG seed of the next proof when it is replayed from a graph
   fe epre;                    // prod_{k < i} eq1(z_k, chal_k): the folded eq prefix of the sumcheck
+  // The prover's WHIR randomness, drawn up front (it depends on the seed
+  // only): per iteration the two round challenges, the query positions and
+  // update_betas' r; and the round messages, kept per iteration for the
+  // query chain that checks and updates K.
+  fe wr[kMaxWhirIter][kWhirLogK];
+  fe wrb[kMaxWhirIter];
+  int32_t wq[kMaxWhirIter][kMaxQueries];
+  fe whw[kMaxWhirIter][kWhirLogK][3];
 };
 
 // Error capture for the C-ABI.

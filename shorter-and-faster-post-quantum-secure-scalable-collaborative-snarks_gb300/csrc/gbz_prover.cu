@@ -106,7 +106,7 @@ __global__ void k_sc_round_eq(const fe *partial, int blocks, ProofState *st, int
     st->y = h01;
     put_fe(tr, (uint64_t)off_claim, h01);
   } else if (!fe_eq(h01, st->y)) {
-    st->error |= 1u;
+    atomicOr(&st->error, 1u);
   }
   for (int k = 0; k < 3; k++) put_fe(tr, off_poly + 16 * k, H[k]);
   fe s = st->fs;
@@ -149,28 +149,73 @@ struct QueryArgs {
   fe len_inv;  // 4^{-1}
 };
 
-// whir_query (Whir.cpp:251-314), the query rescaling (:371-372) and the
-// combination weights / K update of update_betas (:325-342, :383-384).
-// Thread i handles query i.
-__global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
-  __shared__ int32_t q[kMaxQueries];
-  __shared__ fe rb_s;
+
+// The WHIR randomness of a proof, drawn up front.  Every F::_random() and
+// rand() of the opening comes from the glibc generator seeded once, and no
+// draw depends on the data, so the draws of Whir_Open in their order
+// (per iteration: the two round challenges of whir_sumcheck, the l query
+// positions of whir_query, update_betas' r; then the final point,
+// Whir.cpp:233-249, 262-268, 327, 426-446) can be made before the
+// opening starts.
+struct SchedArgs {
+  int T;                            // iterations
+  int l[kMaxWhirIter];              // queries per iteration
+  int32_t qmod[kMaxWhirIter];       // codeword length / 4 per iteration
+  int lg_final;                     // log2 of the final polynomial's length
+};
+__global__ void k_whir_schedule(ProofState *st, SchedArgs a) {
+  __shared__ glibc_prng g;
+  if (threadIdx.x) return;
+  g = st->prng;
+  for (int t = 0; t < a.T; t++) {
+    for (int i = 0; i < kWhirLogK; i++) st->wr[t][i] = prng_field(g);
+    for (int i = 0; i < a.l[t]; i++) st->wq[t][i] = prng_next(g) % a.qmod[t];
+    st->wrb[t] = prng_field(g);
+  }
+  for (int i = 0; i < a.lg_final; i++) st->fin_r[i] = prng_field(g);
+  st->prng = g;
+}
+
+// WHIR sumcheck round i of iteration t from the reduction partials: the
+// message is recorded (transcript and st->whw for the query chain, which
+// checks it against K) with the challenge drawn up front.  After the last
+// round, the threads also prepare update_betas of this iteration: scaled
+// queries 2 q_i, omega_NL^{2 q_i} and the weights c_i = r^(i+1).
+struct UbPrep {
+  int l;                 // 0: no preparation
+  const fe *lo, *hi;     // omega_NL^e
+};
+__global__ void k_whir_round_s(const fe *partial, int blocks, ProofState *st, int t, int i, uint8_t *tr,
+                               uint64_t off_poly, uint64_t off_chal, UbPrep u) {
+  fe H[3];
+  sum_partials(partial, blocks, H);
+  for (int j = threadIdx.x; j < u.l; j += blockDim.x) {
+    const uint32_t q2 = 2u * (uint32_t)st->wq[t][j];
+    st->q[j] = (int32_t)q2;
+    st->omega_q[j] = pow_table(u.lo, u.hi, q2);
+    st->comb[j] = fpow(st->wrb[t], (uint64_t)j + 1);
+  }
+  if (threadIdx.x) return;
+  for (int k = 0; k < 3; k++) {
+    put_fe(tr, off_poly + 16 * k, H[k]);
+    st->whw[t][i][k] = H[k];
+  }
+  put_fe(tr, off_chal, st->wr[t][i]);
+}
+
+// whir_query (Whir.cpp:251-314) of iteration t with the drawn positions, and
+// the running claim of whir_sumcheck and update_betas: K is checked against
+// both round messages (K == h(0) + h(1), K = h(r)), then K += sum_i c_i y_i
+// (Whir.cpp:383-384).  Thread i handles query i.
+__global__ void __launch_bounds__(kMaxQueries) k_whir_query_s(QueryArgs a, int t) {
   __shared__ fe red[kMaxQueries / 32];
   ProofState *st = a.st;
-  __shared__ glibc_prng g;
-  if (threadIdx.x == 0) {
-    g = st->prng;
-    const int32_t mod = (int32_t)(a.L / 4);  // whir_k <= 4 branch of whir_query
-    for (int i = 0; i < a.l; i++) q[i] = prng_next(g) % mod;
-    rb_s = prng_field(g);  // update_betas' F::_random(), drawn after the queries
-    st->prng = g;
-  }
-  __syncthreads();
   const int i = threadIdx.x;
   fe contrib = fe_zero();
   if (i < a.l) {
-    const uint64_t qi = (uint64_t)q[i];
-    reinterpret_cast<int32_t *>(a.tr + a.off_q)[i] = q[i];
+    const int32_t q = st->wq[t][i];
+    const uint64_t qi = (uint64_t)q;
+    reinterpret_cast<int32_t *>(a.tr + a.off_q)[i] = q;
     fe seg[kWhirK];
     for (int j = 0; j < kWhirK; j++) {
       seg[j] = a.cw[qi + j * (a.L / kWhirK)];
@@ -179,7 +224,7 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
     // get_RS_multifold_segment_tensor(seg, r, L, qi) with r = the two WHIR
     // round challenges: level 0 pairs (j, j+2) with omega_L^{-(qi + j L/4)},
     // level 1 pairs (0, 1) with omega_{L/2}^{-qi} = omega_L^{-2 qi}.
-    const fe one = fe_one(), r0 = st->rw[0], r1 = st->rw[1];
+    const fe one = fe_one(), r0 = st->wr[t][0], r1 = st->wr[t][1];
     fe inv_om = pow_table(a.inv_lo, a.inv_hi, qi);
     fe part[2];
     for (int j = 0; j < 2; j++) {
@@ -191,26 +236,26 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query(QueryArgs a) {
     fe s = fadd(part[0], part[1]), d = fsub(part[0], part[1]);
     fe y = fmul(a.len_inv, fadd(fmul(fsub(one, r1), s), fmul(r1, fmul(po, d))));
     put_fe(a.tr, a.off_ans + 16 * i, y);
-    // the authentication paths are copied by k_whir_paths (one hash per thread)
-    const int32_t scaled = (int32_t)(q[i] * (int32_t)(kWhirK * a.NL / a.L));
-    st->q[i] = scaled;
-    st->omega_q[i] = pow_table(a.new_lo, a.new_hi, (uint64_t)(uint32_t)scaled);
-    // combination weight c_i = r^(i+1) and its share of K += c_i * y_i
-    const fe c = fpow(rb_s, (uint64_t)i + 1);
-    st->comb[i] = c;
+    const fe c = fpow(st->wrb[t], (uint64_t)i + 1);
     put_fe(a.tr, a.off_comb + 16 * i, c);
     contrib = fmul(c, y);
   }
   for (int dd = 16; dd > 0; dd >>= 1) {
-    fe t;
-    t.re = __shfl_down_sync(0xffffffffu, contrib.re, dd);
-    t.im = __shfl_down_sync(0xffffffffu, contrib.im, dd);
-    contrib = fadd(contrib, t);
+    fe v;
+    v.re = __shfl_down_sync(0xffffffffu, contrib.re, dd);
+    v.im = __shfl_down_sync(0xffffffffu, contrib.im, dd);
+    contrib = fadd(contrib, v);
   }
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = contrib;
   __syncthreads();
   if (threadIdx.x == 0) {
     fe K = st->K;
+    for (int r = 0; r < kWhirLogK; r++) {
+      const fe *h = st->whw[t][r];
+      const fe h01 = fadd(quad_eval(h[0], h[1], h[2], fe_zero()), quad_eval(h[0], h[1], h[2], fe_one()));
+      if (!fe_eq(h01, K)) atomicOr(&st->error, 2u);
+      K = quad_eval(h[0], h[1], h[2], st->wr[t][r]);
+    }
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) K = fadd(K, red[w]);
     st->K = K;
     put_fe(a.tr, a.off_K, K);
@@ -234,7 +279,7 @@ __global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int 
   sum_partials(partial, blocks, H);
   if (threadIdx.x) return;
   fe h01 = fadd(quad_eval(H[0], H[1], H[2], fe_zero()), quad_eval(H[0], H[1], H[2], fe_one()));
-  if (!fe_eq(h01, st->K)) st->error |= 2u;
+  if (!fe_eq(h01, st->K)) atomicOr(&st->error, 2u);
   for (int k = 0; k < 3; k++) {
     put_fe(tr, off_poly + 16 * k, H[k]);
     st->hw[i][k] = H[k];
@@ -273,11 +318,11 @@ __global__ void k_whir_paths(const uint8_t *tree, uint64_t leaves, int l, uint8_
 // F::_random draws and evaluate_vector(b, r).  With check_K, the flag 8 is
 // raised unless K equals sum arr * b (verification step 2, :848-855).
 __global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
-                        uint64_t off_point, uint64_t off_eval, int check_K) {
+                        uint64_t off_point, uint64_t off_eval, int check_K, const fe *point) {
   __shared__ glibc_prng g;
   if (threadIdx.x) return;
   if (m < 1 || m > kFinalMax) {
-    st->error |= 16u;
+    atomicOr(&st->error, 16u);
     return;
   }
   fe Kc = st->K;
@@ -285,15 +330,15 @@ __global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8
     put_fe(tr, off_poly + 16 * i, arr[i]);
     Kc = fsub(Kc, fmul(arr[i], b[i]));
   }
-  if (check_K && !fe_eq(Kc, fe_zero())) st->error |= 8u;
+  if (check_K && !fe_eq(Kc, fe_zero())) atomicOr(&st->error, 8u);
   const int lg = 31 - __clz(m);
   fe r[8];
-  g = st->prng;
+  if (!point) g = st->prng;
   for (int i = 0; i < lg; i++) {
-    r[i] = prng_field(g);
+    r[i] = point ? point[i] : prng_field(g);
     put_fe(tr, off_point + 16 * i, r[i]);
   }
-  st->prng = g;
+  if (!point) st->prng = g;
   fe v[kFinalMax];
   for (int i = 0; i < m; i++) v[i] = b[i];
   for (int i = 0; i < lg; i++) {
@@ -323,6 +368,7 @@ uint64_t Layout::rec(uint32_t tag, uint32_t count, uint32_t unit) {
 
 ProofPlan::~ProofPlan() {
   if (s2) cudaStreamSynchronize(s2);
+  if (s3) cudaStreamSynchronize(s3);
   for (auto &g : graphs) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     if (g.graph) cudaGraphDestroy(g.graph);
@@ -334,7 +380,12 @@ ProofPlan::~ProofPlan() {
     if (e) cudaEventDestroy(e);
   for (auto &e : ev_commit)
     if (e) cudaEventDestroy(e);
+  for (auto &e : ev_query)
+    if (e) cudaEventDestroy(e);
+  if (ev_sched) cudaEventDestroy(ev_sched);
+  if (ev_init) cudaEventDestroy(ev_init);
   if (s2) cudaStreamDestroy(s2);
+  if (s3) cudaStreamDestroy(s3);
 }
 
 void *ProofPlan::dalloc(uint64_t bytes) {
@@ -370,11 +421,16 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   p->tmp = (fe *)p->dalloc(sizeof(fe) * L);
   p->tmp2 = (fe *)p->dalloc(sizeof(fe) * (L / 2));
   GBZ_CUDA(cudaStreamCreateWithFlags(&p->s2, cudaStreamNonBlocking));
+  GBZ_CUDA(cudaStreamCreateWithFlags(&p->s3, cudaStreamNonBlocking));
   GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
+  GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_sched, cudaEventDisableTiming));
+  GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_init, cudaEventDisableTiming));
   for (auto &e : p->ev_fold) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto &e : p->ev_commit) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  for (auto &e : p->ev_query) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   p->va[0] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
   p->va[1] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
+  p->arr = (fe *)p->dalloc(sizeof(fe) * (n / 2));
   p->vb[0] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
   p->vb[1] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
   p->beta = (fe *)p->dalloc(sizeof(fe) * n);
@@ -437,12 +493,36 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   // the caller enqueued on s (the witness copy) and s joins it at the end.
   // With the profiler on, the commits stay on s so that the per-category
   // event times do not include waits for the other stream's kernels.
-  cudaStream_t c = prof ? s : p.s2;
+  cudaStream_t c = prof ? s : p.s2, q = prof ? s : p.s3;
   if (!dry) {
     GBZ_CUDA(cudaEventRecord(p.ev_in, s));
     GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_in, 0));
   }
   RUN(PC_PROTOCOL, 1, k_init<<<1, 32, 0, s>>>(st, prng_seed, seed_in_state ? 1 : 0));
+  // The opening's randomness, drawn on the query stream while the
+  // commitment and the sumcheck run.
+  {
+    SchedArgs sa{};
+    uint64_t mm = p.n, LL = p.L, cc = (uint64_t)p.rate;
+    for (;;) {
+      if (sa.T >= kMaxWhirIter) throw ArgError("prover: too many WHIR iterations");
+      mm /= 4;
+      sa.l[sa.T] = whir_query_count((int)cc);
+      sa.qmod[sa.T] = (int32_t)(LL / 4);
+      if (sa.l[sa.T] < 1 || sa.l[sa.T] > kMaxQueries) throw ArgError("prover: query count out of range");
+      sa.T++;
+      LL = 2 * cc * mm;
+      cc *= 2;
+      if (mm <= (uint64_t)kWhirK) break;
+    }
+    sa.lg_final = ilog2(mm);
+    if (!dry) {
+      GBZ_CUDA(cudaEventRecord(p.ev_init, s));
+      GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_init, 0));
+    }
+    RUN_ON(q, PC_PROTOCOL, 1, k_whir_schedule<<<1, 32, 0, q>>>(st, sa));
+    if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_sched, q));
+  }
 
   // 1. commitment: codeword = NTT(w padded to rate*n), Merkle tree.
   uint64_t L = p.L;
@@ -498,53 +578,67 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   }
 
   // 4. WHIR open of (v1[0], chal): b = precompute_beta(chal), arr = w.
+  //    Three chains: folds and beta updates on s, commits on c, queries
+  //    and the running claim K on q.  The folded polynomials are written
+  //    once each (p.arr), so the commits read them while s moves on; a
+  //    commit reuses a codeword/tree buffer only after the query that
+  //    opened its previous content.
   RUN(PC_BETA, 1, beta_launch(st->chal, logn, p.beta, s));
+  if (!dry) GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_sched, 0));  // round challenges
   a = w;
   const fe *b = p.beta;
   m = p.n;
   uint64_t cur = (uint64_t)p.rate;
-  // arr/b ping-pong: the first fold writes va/vb[0] (m/2), the second
-  // va/vb[1] (m/4), which the next iteration reads.
+  fe *arr_next = p.arr;
   for (;;) {
+    if (iter >= ProofPlan::kMaxIter) throw ArgError("prover: too many WHIR iterations");
+    const int l = whir_query_count((int)cur);
+    const uint64_t NL = 2 * cur * (m / 4);
+    if (2 * NL != L) throw ArgError("prover: WHIR codeword lengths must halve");
     // round 0
     uint64_t op = lay.rec(T_WHIR_POLY, 3, 16), oc = lay.rec(T_WHIR_CHALLENGE, 1, 16);
     int blocks = sc_blocks(m / 2);
     RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, nullptr, nullptr, nullptr, true, p.partial, blocks, s));
-    RUN(PC_PROTOCOL, 1, k_whir_round<<<1, 256, 0, s>>>(p.partial, blocks, st, 0, tr, op, oc));
-    // round 1: fold by r0 into [0], message
+    RUN(PC_PROTOCOL, 1, k_whir_round_s<<<1, 256, 0, s>>>(p.partial, blocks, st, iter, 0, tr, op, oc, UbPrep{}));
+    // round 1: fold by r0 into va/vb[0], message; the round kernel also
+    // prepares this iteration's beta update
     op = lay.rec(T_WHIR_POLY, 3, 16);
     oc = lay.rec(T_WHIR_CHALLENGE, 1, 16);
     blocks = sc_blocks(m / 4);
-    RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, &st->rw[0], p.va[0], p.vb[0], true, p.partial, blocks, s));
-    RUN(PC_PROTOCOL, 1, k_whir_round<<<1, 256, 0, s>>>(p.partial, blocks, st, 1, tr, op, oc));
-    // fold by r1 into [1]
+    RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, &st->wr[iter][0], p.va[0], p.vb[0], true, p.partial, blocks, s));
+    {
+      UbPrep u{};
+      if (!dry) {
+        const NttTables &tnew = p.tables(ilog2(NL));
+        u.l = l;
+        u.lo = tnew.lo_fwd;
+        u.hi = tnew.hi_fwd;
+      }
+      RUN(PC_PROTOCOL, 1, k_whir_round_s<<<1, 256, 0, s>>>(p.partial, blocks, st, iter, 1, tr, op, oc, u));
+    }
+    // fold by r1: arr_{t+1} into its own slot of p.arr, b into vb[1]
     RUN(PC_SUMCHECK, 1,
-        sc_step_launch(p.va[0], p.vb[0], m / 2, &st->rw[1], p.va[1], p.vb[1], false, p.partial,
+        sc_step_launch(p.va[0], p.vb[0], m / 2, &st->wr[iter][1], arr_next, p.vb[1], false, p.partial,
                        sc_blocks(m / 8 ? m / 8 : 1), s));
-    a = p.va[1];
+    a = arr_next;
     b = p.vb[1];
     m /= 4;
-    if (iter >= ProofPlan::kMaxIter) throw ArgError("prover: too many WHIR iterations");
-    // commit arr at rate 2*cur on the commit stream, after the folds
-    const uint64_t NL = 2 * cur * m;
-    if (2 * NL != L) throw ArgError("prover: WHIR codeword lengths must halve");
+    arr_next += m;
+    if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_fold[iter], s));
+    // commit arr_{t+1} at rate 2*cur on c, once the query that opened the
+    // buffer's previous codeword (iteration t-1) is done
     const int nci = cwi ^ 1;
     off = lay.rec(T_WHIR_ROOT, 1, 32);
     if (!dry) {
-      GBZ_CUDA(cudaEventRecord(p.ev_fold[iter], s));
       GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_fold[iter], 0));
+      if (iter > 0) GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_query[iter - 1], 0));
     }
     RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(NL)), ntt_launch(p.tables(ilog2(NL)), a, m, p.cw[nci], p.tmp, false, c));
     RUN_ON(c, PC_MERKLE, merkle_launch_count(NL), merkle_commit_launch(p.cw[nci], NL, p.tree[nci], c));
     RUN_ON(c, PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, c>>>(p.tree[nci] + 32 * (merkle_hashes(NL) - 1), tr + off));
-    if (!dry) {
-      GBZ_CUDA(cudaEventRecord(p.ev_commit[iter + 1], c));
-      // the query opens the previous commit
-      GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_commit[iter], 0));
-    }
-    // queries on the previous codeword
-    const int l = whir_query_count((int)cur);
-    if (l > kMaxQueries || l < 1) throw ArgError("prover: query count out of range");
+    if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_commit[iter + 1], c));
+    // queries of iteration t on q: they open the codeword of commit t and
+    // check K against this iteration's round messages
     const int depth = ilog2(L / 4);
     QueryArgs qa;
     qa.st = st;
@@ -561,28 +655,33 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     qa.off_comb = lay.rec(T_WHIR_COMBINE, l, 16);
     qa.off_K = lay.rec(T_WHIR_K, 1, 16);
     if (!dry) {
-      const NttTables &told = p.tables(ilog2(L)), &tnew = p.tables(ilog2(NL));
+      const NttTables &told = p.tables(ilog2(L));
       qa.inv_lo = told.lo_inv;
       qa.inv_hi = told.hi_inv;
-      qa.new_lo = tnew.lo_fwd;
-      qa.new_hi = tnew.hi_fwd;
+      qa.new_lo = nullptr;
+      qa.new_hi = nullptr;
       const fe om_inv = finv(root_of_unity(ilog2(L)));
       qa.step0 = fpow(om_inv, L / kWhirK);
       qa.len_inv = finv(fe_make(kWhirK, 0));
+      // the codeword it opens, and this iteration's round messages (for
+      // iteration 0 also K = v1[0], set before on s)
+      GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_commit[iter], 0));
+      GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_fold[iter], 0));
     }
-    RUN(PC_QUERY, 1, k_whir_query<<<1, kMaxQueries, 0, s>>>(qa));
+    RUN_ON(q, PC_QUERY, 1, k_whir_query_s<<<1, kMaxQueries, 0, q>>>(qa, iter));
     {
       const uint64_t hashes = (uint64_t)l * depth;  // depth >= 2: every queried codeword has 16+ entries
-      RUN(PC_QUERY, 1,
-          k_whir_paths<<<(unsigned)((hashes + 127) / 128), 128, 0, s>>>(qa.tree, L / 4, l, tr, qa.off_q, qa.off_path));
+      RUN_ON(q, PC_QUERY, 1,
+             k_whir_paths<<<(unsigned)((hashes + 127) / 128), 128, 0, q>>>(qa.tree, L / 4, l, tr, qa.off_q,
+                                                                           qa.off_path));
       if (!dry && hashes == 0) throw ArgError("prover: empty authentication paths");
     }
-    // update_betas: b[j] += sum_i c_i omega_NL^{q_i j} is the forward
+    if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_query[iter], q));
+    // update_betas on s: b[j] += sum_i c_i omega_NL^{q_i j} is the forward
     // transform of a vector with l nonzeros.  When l * |b| exceeds a few
-    // transform lengths, the sparse two-pass transform is cheaper than the
-    // direct sums.
-    // The query exponents q_i * (whir_k NL / L) are even (NL = L / 2), so
-    // omega_NL^{2 q_i j} = omega_{NL/2}^{q_i j}: the sparse transform runs
+    // transform lengths, the sparse transform is cheaper than the direct
+    // sums.  The query exponents q_i * (whir_k NL / L) are even (NL = L / 2),
+    // so omega_NL^{2 q_i j} = omega_{NL/2}^{q_i j}: the sparse transform runs
     // at half the codeword length on the unscaled positions.
     static_assert(kWhirK == 4, "update_betas: exponent scale 2 assumes folding by 4 with NL = L / 2");
     if (update_betas_by_transform(l, m, NL / 2)) {
@@ -600,8 +699,12 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   uint64_t off_poly = lay.rec(T_FINAL_POLY, (uint32_t)m, 16);
   uint64_t off_point = lay.rec(T_FINAL_POINT, ilog2(m), 16);
   uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
-  RUN(PC_PROTOCOL, 1, k_final<<<1, 32, 0, s>>>(st, a, p.vb[1], (int)m, tr, off_poly, off_point, off_eval, 0));
-  if (!dry) GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_commit[iter], 0));  // join the commit stream
+  RUN(PC_PROTOCOL, 1,
+      k_final<<<1, 32, 0, s>>>(st, a, p.vb[1], (int)m, tr, off_poly, off_point, off_eval, 0, st->fin_r));
+  if (!dry) {  // join the commit and query chains
+    GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_commit[iter], 0));
+    GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_query[iter - 1], 0));
+  }
 #undef RUN
 #undef RUN_ON
 }
@@ -724,7 +827,7 @@ void launch_proof_graph(ProofPlan &p, const fe *w, uint32_t prng_seed, cudaStrea
 
 uint64_t plan_bytes(int logn, int rate) {
   const uint64_t n = 1ull << logn, L = n * (uint64_t)rate;
-  uint64_t b = sizeof(fe) * (n + L + L / 2 + L + L / 2 + 4 * (n / 2) + n);
+  uint64_t b = sizeof(fe) * (n + L + L / 2 + L + L / 2 + 5 * (n / 2) + n);
   b += 32 * (merkle_hashes(L) + merkle_hashes(L / 2 >= 4 ? L / 2 : 4));
   b += sizeof(fe) * (3 * (uint64_t)sc_blocks(n / 2) + kUpdateBetasScratch) + sizeof(ProofState);
   b += 64ull << 20;  // transcript, twiddle tables and allocation granularity (upper bound)

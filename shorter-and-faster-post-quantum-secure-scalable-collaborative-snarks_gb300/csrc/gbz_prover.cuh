@@ -59,12 +59,16 @@ struct ProofPlan {
   uint8_t *tree[2] = {nullptr, nullptr};
   fe *tmp = nullptr;              // NTT intermediate of the commits (L)
   fe *tmp2 = nullptr;             // NTT intermediate of the sparse beta updates (L/2)
-  // The commits (NTT + Merkle) run on a second stream joined by events:
-  // each WHIR query waits for the commit whose codeword it opens.
-  cudaStream_t s2 = nullptr;
-  static constexpr int kMaxIter = 32;
-  cudaEvent_t ev_in = nullptr, ev_fold[kMaxIter] = {}, ev_commit[kMaxIter + 1] = {};
+  // The opening runs as three chains joined by events: folds and beta
+  // updates on the caller's stream, commits (NTT + Merkle) on s2, queries
+  // (replies, answers, paths, the running claim K) on s3.  Each waits only
+  // for the data it reads; the WHIR randomness is drawn up front on s3.
+  cudaStream_t s2 = nullptr, s3 = nullptr;
+  static constexpr int kMaxIter = kMaxWhirIter;
+  cudaEvent_t ev_in = nullptr, ev_init = nullptr, ev_sched = nullptr, ev_fold[kMaxIter] = {}, ev_commit[kMaxIter + 1] = {},
+              ev_query[kMaxIter] = {};
   fe *va[2] = {nullptr, nullptr}; // folded first vector ping-pong (n/2 each)
+  fe *arr = nullptr;              // the folded polynomials arr_1, arr_2, ... back to back (read by the commits)
   fe *vb[2] = {nullptr, nullptr}; // folded second vector ping-pong
   fe *beta = nullptr;             // eq table (n)
   fe *partial = nullptr;          // per-CTA round-message partials
@@ -92,13 +96,14 @@ struct ProofPlan {
 // Protocol kernels shared by the prover and the batch opening
 // (gbz_prover.cu): a WHIR sumcheck round from the reduction partials, the
 // authentication paths of the queries in a tree of `leaves` leaf hashes,
-// and the final round.
+// and the final round (its point drawn from the generator, or read from
+// `point` when the randomness was drawn up front).
 __global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int i, uint8_t *tr,
                              uint64_t off_poly, uint64_t off_chal);
 __global__ void k_whir_paths(const uint8_t *tree, uint64_t leaves, int l, uint8_t *tr, uint64_t off_q,
                              uint64_t off_path);
 __global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
-                        uint64_t off_point, uint64_t off_eval, int check_K);
+                        uint64_t off_point, uint64_t off_eval, int check_K, const fe *point);
 
 std::unique_ptr<ProofPlan> plan_create(int logn, int rate);
 // Enqueues one proof on stream s (dry: only computes the layout).  With
