@@ -104,9 +104,12 @@ uint64_t Scheduler::cached_bytes() const {
 }
 
 void Scheduler::ensure_slots(int n) {
+  int least = 0, greatest = 0;
+  GBZ_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
   while ((int)slots_.size() < n) {
     Slot s;
-    GBZ_CUDA(cudaStreamCreateWithFlags(&s.s, cudaStreamNonBlocking));
+    s.high = (int)slots_.size() < kHighSlots;
+    GBZ_CUDA(cudaStreamCreateWithPriority(&s.s, cudaStreamNonBlocking, s.high ? greatest : least));
     slots_.push_back(std::move(s));
   }
 }
@@ -258,24 +261,34 @@ void Scheduler::run(const std::vector<ProofJob> &jobs, const double *arrival, in
       for (int i : order) {
         const auto target = t0 + std::chrono::duration_cast<clock::duration>(std::chrono::duration<double>(arrival[i]));
         if (clock::now() < target) std::this_thread::sleep_until(target);
+        // least-loaded slot with room, among the slots of the job's
+        // priority class first (long proofs: high-priority slots)
+        const bool big = jobs[i].logn >= kBigLogn && lanes > kHighSlots;
         int best = -1;
         for (;;) {
-          size_t best_n = ~(size_t)0;
-          double best_cost = 0;
           for (int l = 0; l < lanes; l++) {
             auto &q = inflight[l];
             q.erase(std::remove_if(q.begin(), q.end(),
                                    [&](int k) { return cudaEventQuery(ev.done[k]) == cudaSuccess; }),
                     q.end());
-            double c = 0;
-            for (int k : q) c += proof_cost(jobs[k].logn, jobs[k].rate);
-            if (q.size() < best_n || (q.size() == best_n && c < best_cost)) {
-              best = l;
-              best_n = q.size();
-              best_cost = c;
+          }
+          for (int pass = 0; pass < 2 && best < 0; pass++) {
+            size_t best_n = ~(size_t)0;
+            double best_cost = 0;
+            for (int l = 0; l < lanes; l++) {
+              if (pass == 0 && lanes > kHighSlots && slots_[l].high != big) continue;
+              const auto &q = inflight[l];
+              if (q.size() >= (size_t)depth) continue;
+              double c = 0;
+              for (int k : q) c += proof_cost(jobs[k].logn, jobs[k].rate);
+              if (q.size() < best_n || (q.size() == best_n && c < best_cost)) {
+                best = l;
+                best_n = q.size();
+                best_cost = c;
+              }
             }
           }
-          if (best_n < (size_t)depth) break;
+          if (best >= 0) break;
           std::this_thread::sleep_for(std::chrono::microseconds(20));
         }
         SlotPlan &sp = plan_for(best, jobs[i].logn, jobs[i].rate, o);

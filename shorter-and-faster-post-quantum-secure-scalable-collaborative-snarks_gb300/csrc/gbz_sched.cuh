@@ -25,6 +25,13 @@ struct SchedOpts {
   uint64_t reserve = 1ull << 30;     // device bytes left free when a new shape is admitted
 };
 
+// Serving: the first kHighSlots slots run at the device's greatest stream
+// priority and take proofs of 2^kBigLogn or more first, so that the long
+// proofs (the latency tail) are not slowed by the many short ones, which
+// fill the SMs they leave idle.
+constexpr int kHighSlots = 2;
+constexpr int kBigLogn = 20;
+
 struct ProofJob {
   const fe *witness = nullptr;       // host (pinned for overlap) or device, 2^logn elements
   int logn = 0, rate = 0;
@@ -47,6 +54,7 @@ struct SlotPlan {
 
 struct Slot {
   cudaStream_t s = nullptr;
+  bool high = false;                 // created with the device's greatest stream priority
   std::map<std::pair<int, int>, std::unique_ptr<SlotPlan>> plans;
 };
 
