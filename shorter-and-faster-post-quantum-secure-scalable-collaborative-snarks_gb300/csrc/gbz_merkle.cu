@@ -25,6 +25,17 @@ constexpr int kThreads = 256;
 // in shared memory take 24 or 48 KiB).  Larger subtrees leave fewer threads
 // idle in the upper levels of a CTA; set by merkle_set_fusion.
 int g_log_nodes = 10;
+// Small trees are latency bound (one dependent compression per level): the
+// subtree per CTA shrinks, down to 2^8 nodes, until the first level spreads
+// over at least two CTAs per SM of the 152 SMs, so that a thread hashes
+// about one node per level instead of eight.
+constexpr int kMinLogNodes = 8;
+constexpr uint64_t kFillCtas = 2 * 152;
+int fusion_for(uint64_t first_level_nodes) {
+  int lg = g_log_nodes;
+  while (lg > kMinLogNodes && (first_level_nodes >> lg) < kFillCtas) lg--;
+  return lg;
+}
 
 struct Hash {
   uint32_t w[8];
@@ -122,10 +133,12 @@ __global__ void blake3_batch_kernel(const uint8_t *in, uint8_t *out, uint64_t co
 void launch_levels(int logn_cta, const fe *elems, const uint8_t *child, uint64_t cnt, uint8_t *levels,
                    uint64_t off, int nlev, cudaStream_t s) {
   const uint64_t blocks = (cnt + (1ull << logn_cta) - 1) >> logn_cta;
-  if (logn_cta == 11)
-    merkle_levels_kernel<11><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev);
-  else
-    merkle_levels_kernel<10><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev);
+  switch (logn_cta) {
+    case 11: merkle_levels_kernel<11><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev); break;
+    case 10: merkle_levels_kernel<10><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev); break;
+    case 9: merkle_levels_kernel<9><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev); break;
+    default: merkle_levels_kernel<8><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev); break;
+  }
   GBZ_CUDA(cudaGetLastError());
 }
 
@@ -140,7 +153,7 @@ int merkle_get_fusion() { return g_log_nodes; }
 void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStream_t s) {
   if (N < 4 || !is_pow2(N)) throw ArgError("Merkle commitment needs a power-of-two length >= 4");
   const int depth = ilog2(N / 4);  // levels 0..depth
-  const int lg = g_log_nodes;
+  const int lg = fusion_for(N / 4);
   uint64_t cnt = N / 4, off = 0;
   int level = 0;
   uint64_t child_off = 0;
@@ -161,7 +174,7 @@ void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStre
 void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s) {
   if (!is_pow2(L)) throw ArgError("Merkle tree over leaves needs a power-of-two count");
   const int depth = ilog2(L);  // levels 1..depth above the leaves
-  const int lg = g_log_nodes;
+  const int lg = fusion_for(L / 2);
   uint64_t cnt = L / 2, off = L, child_off = 0;
   int level = 1;
   while (level <= depth) {
@@ -178,9 +191,10 @@ void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s) {
 
 int merkle_launch_count(uint64_t N) {
   const int depth = ilog2(N / 4);
+  const int lg = fusion_for(N / 4);
   int level = 0, k = 0;
   while (level <= depth) {
-    level += min(g_log_nodes + 1, depth - level + 1);
+    level += min(lg + 1, depth - level + 1);
     k++;
   }
   return k;
