@@ -88,11 +88,8 @@ __device__ void sum_partials(const fe *partial, int blocks, fe out[3]) {
 // message of the pairs of w and the folded eq vector); claim check; the
 // Fiat-Shamir challenge hash_to_field({H.a, H.b, H.c}); y = H(c); and
 // epre *= eq1(z_i, c).
-__global__ void k_sc_round_eq(const fe *partial, int blocks, ProofState *st, int round, uint8_t *tr,
-                              int64_t off_claim, uint64_t off_poly, uint64_t off_chal) {
-  fe SS[3];
-  sum_partials(partial, blocks, SS);  // (S0, -S0-S1, S1)
-  if (threadIdx.x) return;
+__device__ fe sc_round_eq_apply(const fe SS[3], ProofState *st, int round, uint8_t *tr, int64_t off_claim,
+                                uint64_t off_poly, uint64_t off_chal) {
   if (round == 0) st->epre = fe_one();
   const fe z = st->z[round], ep = st->epre;
   const fe a1 = fsub(fadd(z, z), fe_one()), b1 = fsub(fe_one(), z);
@@ -116,6 +113,89 @@ __global__ void k_sc_round_eq(const fe *partial, int blocks, ProofState *st, int
   put_fe(tr, off_chal, s);
   st->y = quad_eval(H[0], H[1], H[2], s);
   st->epre = fmul(ep, fadd(b1, fmul(a1, s)));
+  return s;
+}
+
+__global__ void k_sc_round_eq(const fe *partial, int blocks, ProofState *st, int round, uint8_t *tr,
+                              int64_t off_claim, uint64_t off_poly, uint64_t off_chal) {
+  fe SS[3];
+  sum_partials(partial, blocks, SS);  // (S0, -S0-S1, S1)
+  if (threadIdx.x) return;
+  (void)sc_round_eq_apply(SS, st, round, tr, off_claim, off_poly, off_chal);
+}
+
+// The last rounds of the same sumcheck in one CTA, once w (m entries) and
+// its eq table E (m / 2) fit in shared memory: per round r the fold of w by
+// chal[r-1], the pairwise sums of E, the sums S(0), S(1) and the round
+// itself (thread 0), with no launch or global round trip between rounds;
+// then the final fold and the SC_FINAL record.  Round r's SC_POLY payload
+// is at off_poly0 + 80 (r - round0), its SC_CHALLENGE 56 bytes after it.
+constexpr int kScTailMax = 4096;
+constexpr int kScTailThreads = 1024;
+__global__ void __launch_bounds__(kScTailThreads)
+k_sc_tail(ProofState *st, const fe *a, const fe *E, int m, int round0, int logn, uint8_t *tr, uint64_t off_poly0,
+          uint64_t off_final) {
+  extern __shared__ fe tail_sm[];
+  fe *w = tail_sm, *e = tail_sm + kScTailMax;
+  __shared__ fe red[2][kScTailThreads / 32];
+  __shared__ fe chal_s;
+  for (int j = threadIdx.x; j < m; j += blockDim.x) w[j] = a[j];
+  for (int j = threadIdx.x; j < m / 2; j += blockDim.x) e[j] = E[j];
+  if (threadIdx.x == 0) chal_s = st->chal[round0 - 1];
+  __syncthreads();
+  for (int r = round0; r <= logn; r++) {
+    // fold w by the previous challenge; E to pairwise sums (r < logn)
+    const fe c = chal_s;
+    const int half = m / 2;
+    fe nw[kScTailMax / 2 / kScTailThreads], ne[kScTailMax / 4 / kScTailThreads + 1];
+    int k = 0;
+    for (int j = threadIdx.x; j < half; j += blockDim.x, k++)
+      nw[k] = fadd(fmul(c, fsub(w[2 * j + 1], w[2 * j])), w[2 * j]);
+    k = 0;
+    if (r < logn)
+      for (int j = threadIdx.x; j < half / 2; j += blockDim.x, k++) ne[k] = fadd(e[2 * j], e[2 * j + 1]);
+    __syncthreads();
+    k = 0;
+    for (int j = threadIdx.x; j < half; j += blockDim.x, k++) w[j] = nw[k];
+    k = 0;
+    if (r < logn)
+      for (int j = threadIdx.x; j < half / 2; j += blockDim.x, k++) e[j] = ne[k];
+    m = half;
+    __syncthreads();
+    if (r == logn) break;
+    // S(0) = sum w[2j] E[j], S(1) = sum w[2j+1] E[j]
+    fe S0 = fe_zero(), S1 = fe_zero();
+    for (int j = threadIdx.x; j < m / 2; j += blockDim.x) {
+      S0 = fadd(S0, fmul(w[2 * j], e[j]));
+      S1 = fadd(S1, fmul(w[2 * j + 1], e[j]));
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+      fe t;
+      t.re = __shfl_down_sync(0xffffffffu, S0.re, d); t.im = __shfl_down_sync(0xffffffffu, S0.im, d); S0 = fadd(S0, t);
+      t.re = __shfl_down_sync(0xffffffffu, S1.re, d); t.im = __shfl_down_sync(0xffffffffu, S1.im, d); S1 = fadd(S1, t);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = S0;
+      red[1][threadIdx.x >> 5] = S1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      fe A = fe_zero(), B = fe_zero();
+      for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
+        A = fadd(A, red[0][q]);
+        B = fadd(B, red[1][q]);
+      }
+      const fe SS[3] = {A, fe_zero(), B};
+      const uint64_t op = off_poly0 + 80ull * (uint64_t)(r - round0);
+      chal_s = sc_round_eq_apply(SS, st, r, tr, -1, op, op + 56);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {  // k_sc_final: the folded w and the eq prefix
+    put_fe(tr, off_final, w[0]);
+    put_fe(tr, off_final + 16, st->epre);
+    st->K = w[0];
+  }
 }
 
 __global__ void k_sc_final(ProofState *st, const fe *v1, const fe *v2, uint8_t *tr, uint64_t off) {
@@ -437,6 +517,8 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   p->partial = (fe *)p->dalloc(sizeof(fe) * 3 * (uint64_t)sc_blocks(n / 2));
   p->ub_scratch = (fe *)p->dalloc(sizeof(fe) * kUpdateBetasScratch);
   p->st = (ProofState *)p->dalloc(sizeof(ProofState));
+  GBZ_CUDA(cudaFuncSetAttribute(k_sc_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(fe) * (kScTailMax + kScTailMax / 2))));
   // Build the transcript layout (record headers are constant).
   p->layout.record_headers = true;
   enqueue_proof(*p, nullptr, 1, nullptr, /*dry=*/true);  // layout and launch counts
@@ -547,7 +629,23 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   uint64_t m = p.n;
   const fe *a = w;
   int pp = 0, ep = 0;  // va ping-pong for w, vb ping-pong for E
+  bool tail_done = false;
   for (int i = 0; i < logn; i++) {
+    if (i >= 1 && m <= (uint64_t)kScTailMax) {
+      // the remaining rounds and the final fold in one CTA
+      const uint64_t op0 = lay.rec(T_SC_POLY, 3, 16);
+      for (int r = i; r < logn; r++) {
+        const uint64_t op = r == i ? op0 : lay.rec(T_SC_POLY, 3, 16);
+        const uint64_t oc = lay.rec(T_SC_CHALLENGE, 1, 16);
+        if (op != op0 + 80ull * (uint64_t)(r - i) || oc != op + 56) throw ArgError("prover: sumcheck record layout");
+      }
+      off = lay.rec(T_SC_FINAL, 2, 16);
+      RUN(PC_SUMCHECK, 1,
+          (k_sc_tail<<<1, kScTailThreads, sizeof(fe) * (kScTailMax + kScTailMax / 2), s>>>(st, a, p.vb[ep], (int)m, i,
+                                                                                         logn, tr, op0, off)));
+      tail_done = true;
+      break;
+    }
     uint64_t off_poly = lay.rec(T_SC_POLY, 3, 16);
     uint64_t off_chal = lay.rec(T_SC_CHALLENGE, 1, 16);
     int blocks;
@@ -568,7 +666,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
         k_sc_round_eq<<<1, 256, 0, s>>>(p.partial, blocks, st, i, tr, i == 0 ? (int64_t)off_claim : -1, off_poly,
                                         off_chal));
   }
-  {
+  if (!tail_done) {
     fe *a2 = p.va[pp];
     RUN(PC_SUMCHECK, 1,
         sc_eq_step_launch(a, p.vb[ep], m, &st->chal[logn - 1], a2, nullptr, false, p.partial, 1, s));
