@@ -243,17 +243,67 @@ struct SchedArgs {
   int32_t qmod[kMaxWhirIter];       // codeword length / 4 per iteration
   int lg_final;                     // log2 of the final polynomial's length
 };
-__global__ void k_whir_schedule(ProofState *st, SchedArgs a) {
-  __shared__ glibc_prng g;
-  if (threadIdx.x) return;
-  g = st->prng;
-  for (int t = 0; t < a.T; t++) {
-    for (int i = 0; i < kWhirLogK; i++) st->wr[t][i] = prng_field(g);
-    for (int i = 0; i < a.l[t]; i++) st->wq[t][i] = prng_next(g) % a.qmod[t];
-    st->wrb[t] = prng_field(g);
+constexpr int kFieldDraws = 40;     // random() outputs behind one F::_random() (two 20-digit numbers)
+constexpr int kMaxDraws = kMaxWhirIter * (3 * kFieldDraws + kMaxQueries) + 8 * kFieldDraws;
+
+// randomNumber (fieldElement.cpp:363-368) from 20 consecutive outputs.
+__device__ uint64_t number_from(const int32_t *d) {
+  uint64_t ret = (uint64_t)(d[0] % 10);
+  for (int i = 1; i < 20; i++) {
+    ret = ret * 10ull + (uint64_t)(d[i] % 10);
+    ret = ret >= P ? ret % P : ret;
   }
-  for (int i = 0; i < a.lg_final; i++) st->fin_r[i] = prng_field(g);
-  st->prng = g;
+  return ret;
+}
+
+// One thread runs the generator with its 31-word table in registers (the
+// table rotated so that the front index is 3 and the rear 0, which makes
+// every index of a 31-draw cycle a constant) and stores the N outputs in
+// shared memory; then all threads derive the field elements (40 outputs
+// each) and the query positions from them.
+__global__ void __launch_bounds__(256) k_whir_schedule(ProofState *st, SchedArgs a) {
+  __shared__ int32_t draws[kMaxDraws];
+  int N = kFieldDraws * a.lg_final;
+  for (int t = 0; t < a.T; t++) N += 3 * kFieldDraws + a.l[t];
+  if (threadIdx.x == 0) {
+    const int f0 = st->prng.f;
+    uint32_t reg[31];
+#pragma unroll
+    for (int k = 0; k < 31; k++) reg[k] = (uint32_t)st->prng.tbl[(k + f0 + 28) % 31];
+    for (int n = 0; n < N; n += 31) {
+#pragma unroll
+      for (int j = 0; j < 31; j++) {
+        if (n + j < N) {
+          reg[(j + 3) % 31] += reg[j];
+          draws[n + j] = (int32_t)(reg[(j + 3) % 31] >> 1);
+        }
+      }
+    }
+    // the table in place, both indices advanced by N (glibc's state after N draws)
+#pragma unroll
+    for (int k = 0; k < 31; k++) st->prng.tbl[(k + f0 + 28) % 31] = (int32_t)reg[k];
+    const int f = (f0 + N) % 31;
+    st->prng.f = f;
+    st->prng.r = (f + 28) % 31;
+  }
+  __syncthreads();
+  // per iteration: r0, r1 (40 outputs each), l queries, update_betas' r; then the final point
+  int off = 0;
+  for (int t = 0; t < a.T; t++) {
+    const int l = a.l[t];
+    for (int i = threadIdx.x; i < l; i += blockDim.x) st->wq[t][i] = draws[off + 2 * kFieldDraws + i] % a.qmod[t];
+    if (threadIdx.x < 3) {
+      const int o = threadIdx.x < 2 ? off + kFieldDraws * threadIdx.x : off + 2 * kFieldDraws + l;
+      const fe v = fe_make(number_from(draws + o) % P, number_from(draws + o + 20) % P);
+      if (threadIdx.x < 2) st->wr[t][threadIdx.x] = v;
+      else st->wrb[t] = v;
+    }
+    off += 3 * kFieldDraws + l;
+  }
+  for (int i = threadIdx.x; i < a.lg_final; i += blockDim.x) {
+    const int o = off + kFieldDraws * i;
+    st->fin_r[i] = fe_make(number_from(draws + o) % P, number_from(draws + o + 20) % P);
+  }
 }
 
 // WHIR sumcheck round i of iteration t from the reduction partials: the
@@ -602,7 +652,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
       GBZ_CUDA(cudaEventRecord(p.ev_init, s));
       GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_init, 0));
     }
-    RUN_ON(q, PC_PROTOCOL, 1, k_whir_schedule<<<1, 32, 0, q>>>(st, sa));
+    RUN_ON(q, PC_PROTOCOL, 1, k_whir_schedule<<<1, 256, 0, q>>>(st, sa));
     if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_sched, q));
   }
 
