@@ -637,14 +637,19 @@ gbz_status gbz_encode_rows(gbz_ctx *ctx, const uint64_t *rows, int nrows, int lo
   if (!nrows) return GBZ_OK;
   const fe *drows = dev_view(ctx, 0, (const fe *)rows, 16 * n * nrows, mem, true);
   fe *dout = dev_view(ctx, 1, (fe *)out, 16 * L * nrows, mem, false);
-  fe *tmp = (fe *)ctx->buf(2, 16 * L);
   const NttTables &tn = ctx->tables(logrow), &tL = ctx->tables(ilog2(L));
   const NttTables &tw = ctx->tables(1 + log_rate_offset + logrow);
-  for (int i = 0; i < nrows; i++) {
-    fe *o = dout + L * i;
-    ntt_launch(tn, drows + n * i, n, o, tmp, true, ctx->stream);
-    coset_launch(o, n, tw, ctx->stream);
-    ntt_launch(tL, o, n, o, tmp, false, ctx->stream);
+  // every row's inverse transform, coset shift and forward transform, the
+  // rows side by side in each launch (chunks of up to 2^28 elements of
+  // intermediate)
+  const int chunk = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)nrows, (1ull << 28) / L));
+  fe *tmp = (fe *)ctx->buf(2, 16 * L * (uint64_t)chunk);
+  for (int r0 = 0; r0 < nrows; r0 += chunk) {
+    const int rc = std::min(chunk, nrows - r0);
+    fe *o = dout + L * (uint64_t)r0;
+    ntt_launch_rows(tn, drows + n * (uint64_t)r0, n, n, o, L, rc, tmp, true, ctx->stream);
+    coset_launch(o, n, tw, ctx->stream, rc, L);
+    ntt_launch_rows(tL, o, n, L, o, L, rc, tmp, false, ctx->stream);
   }
   copy_out(ctx, (fe *)out, dout, 16 * L * nrows, mem);
   finish(ctx, mem);

@@ -60,8 +60,9 @@ __global__ void powers_kernel(fe r, uint64_t n, fe *out) {
 }
 
 // x[j] *= omega^{-j} for j < n (omega^{-e} from the inverse tables).
-__global__ void coset_kernel(fe *x, uint64_t n, const fe *inv_lo, const fe *inv_hi) {
+__global__ void coset_kernel(fe *x, uint64_t n, const fe *inv_lo, const fe *inv_hi, uint64_t row_stride) {
   const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  x += blockIdx.y * row_stride;
   if (j < n) x[j] = fmul(x[j], pow_tab(inv_lo, inv_hi, j));
 }
 
@@ -268,8 +269,9 @@ void powers_launch(fe r, uint64_t n, fe *out, cudaStream_t s) {
   GBZ_CUDA(cudaGetLastError());
 }
 
-void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s) {
-  coset_kernel<<<grid(n), 256, 0, s>>>(x, n, t.lo_inv, t.hi_inv);
+void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s, int rows, uint64_t row_stride) {
+  if (rows < 1) return;
+  coset_kernel<<<dim3(grid(n), (unsigned)rows), 256, 0, s>>>(x, n, t.lo_inv, t.hi_inv, row_stride);
   GBZ_CUDA(cudaGetLastError());
 }
 

@@ -13,7 +13,8 @@ void multifold5_launch(const fe *cw, uint64_t n, const fe *a, int logd, fe *out,
 // out[i] = r^i for i < n.
 void powers_launch(fe r, uint64_t n, fe *out, cudaStream_t s);
 // x[j] *= omega_T^{-j} for j < n, T = 2^t.logn.
-void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s);
+// rows vectors of n entries, row_stride apart
+void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s, int rows = 1, uint64_t row_stride = 0);
 // distributed_MT for one party (coPCS.cpp:152-202): levels (2L - 1 hashes,
 // column roots first) and the leader's root over 2^logN parties.
 void column_merkle_launch(const fe *rows, int nrows, uint64_t L, uint8_t *levels, int logN, uint8_t *root,

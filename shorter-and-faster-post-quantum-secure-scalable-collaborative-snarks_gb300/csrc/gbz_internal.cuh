@@ -120,6 +120,11 @@ struct NttTables {
 // `tmp` must hold 2^logn elements when logn > 13.  in may equal out.
 void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                 cudaStream_t s);
+// `rows` transforms of the same length in the same launches: row r reads
+// in + r in_stride (n_valid entries, zero beyond) and writes out + r
+// out_stride; tmp holds rows * 2^logn elements when logn > 13.
+void ntt_launch_rows(const NttTables &t, const fe *in, uint64_t n_valid, uint64_t in_stride, fe *out,
+                     uint64_t out_stride, int rows, fe *tmp, bool inverse, cudaStream_t s);
 // acc[j] += sum_i c[i] * omega_L^{q[i] j} for j < nacc (L = 2^t.logn > 2^13,
 // 1 <= l <= kMaxQueries): the forward transform of the sparse vector
 // sum_i c_i e_{q_i} as one second-pass launch whose rows are formed directly

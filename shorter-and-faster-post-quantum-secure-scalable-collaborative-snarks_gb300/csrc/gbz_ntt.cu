@@ -72,6 +72,9 @@ struct PassArgs {
   // Entries j >= j_valid of every sub-transform are zero (per-transform
   // padding of batched transforms; S when unused).
   uint32_t j_valid;
+  // Independent transforms side by side: grid row y works on in + y row_in
+  // and out + y row_out (0 for one transform).
+  uint64_t row_in, row_out;
 };
 
 // Shared-memory swizzle: element a lives at a ^ ((a >> 3) & 7), which keeps
@@ -240,6 +243,8 @@ __device__ void stockham(fe *sm, const fe *T, int logS, int logE) {
 
 __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
   extern __shared__ fe smem[];
+  a.in += blockIdx.y * a.row_in;
+  a.out += blockIdx.y * a.row_out;
   const int logS = a.logS, logB = a.logB, logE = logS + logB;
   const uint32_t S = 1u << logS, total = 1u << logE;
   fe *sm = smem;
@@ -419,12 +424,13 @@ __global__ void sparse_chain_kernel(const int32_t *q, int l, int shift, uint32_t
   lead[t] = first;
 }
 
-void launch_pass(const PassArgs &a, uint64_t groups, cudaStream_t s) {
+void launch_pass(const PassArgs &a, uint64_t groups, cudaStream_t s, int rows = 1) {
   const uint64_t blocks = groups >> a.logB;
   const uint32_t E = 1u << (a.logS + a.logB);
   const size_t smem = sizeof(fe) * (E + (a.logS >= 1 ? (1u << (a.logS - 1)) : 0));
   const unsigned threads = E / kPerThread > 32 ? E / kPerThread : 32;
-  ntt_pass_kernel<<<(unsigned)blocks, threads, smem, s>>>(a);
+  if (rows < 1 || rows > 65535) throw ArgError("transform: 1..65535 rows per launch");
+  ntt_pass_kernel<<<dim3((unsigned)blocks, (unsigned)rows), threads, smem, s>>>(a);
   GBZ_CUDA(cudaGetLastError());
 }
 
@@ -597,11 +603,13 @@ namespace {
 
 // Shared by the dense transform and the sparse/accumulating variant.
 void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
-                  cudaStream_t s) {
+                  cudaStream_t s, int rows = 1, uint64_t row_in = 0, uint64_t row_out = 0) {
   const int logn = t.logn;
   const uint64_t L = 1ull << logn;
   if (n_valid > L) n_valid = L;
   PassArgs a{};
+  a.row_in = row_in;
+  a.row_out = row_out;
   a.wh = inverse ? t.sub_inv : t.sub_fwd;
   a.scale = t.inv_len;
   a.inverse = inverse ? 1 : 0;
@@ -619,7 +627,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
     a.has_scale = inverse;
     a.tw_lo = nullptr;
     a.tw_hi = nullptr;
-    launch_pass(a, 1, s);
+    launch_pass(a, 1, s, rows);
     return;
   }
   const NttShape sh = g_shape[logn].k1 > 0 ? g_shape[logn] : ntt_default_shape(logn);
@@ -643,7 +651,8 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   a.tw_hi = inverse ? t.hi_inv : t.hi_fwd;
   a.tw_full = g_use_outer ? outer_table_get(logn, k1, inverse) : nullptr;
   a.has_scale = 0;
-  launch_pass(a, N1, s);
+  a.row_out = L;  // the intermediate holds one full row per transform
+  launch_pass(a, N1, s, rows);
   // pass B: rows k2 < N2, length N1, contiguous
   PassArgs b = a;
   b.in = tmp;
@@ -659,7 +668,9 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   b.tw_hi = nullptr;
   b.tw_full = nullptr;
   b.has_scale = inverse;
-  launch_pass(b, N2, s);
+  b.row_in = L;
+  b.row_out = row_out;
+  launch_pass(b, N2, s, rows);
 }
 
 }  // namespace
@@ -667,6 +678,12 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
 void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                 cudaStream_t s) {
   ntt_two_pass(t, in, n_valid, out, tmp, inverse, s);
+}
+
+void ntt_launch_rows(const NttTables &t, const fe *in, uint64_t n_valid, uint64_t in_stride, fe *out,
+                     uint64_t out_stride, int rows, fe *tmp, bool inverse, cudaStream_t s) {
+  if (rows < 1) return;
+  ntt_two_pass(t, in, n_valid, out, tmp, inverse, s, rows, in_stride, out_stride);
 }
 
 void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t j_valid, fe *out, uint64_t count,
