@@ -464,7 +464,9 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     mf = torch.empty((1 << (lm - 4), 2), dtype=torch.int64, device="cuda")
     mfc = lambda: ctx.check(gbz.lib.gbz_rs_multifold5(ctx.h, cwb.data_ptr(), 1 << lm, gbz._ptr(a16), 4,
                                                       mf.data_ptr(), D))
-    rec("rs_multifold5_2^%d_by16" % lm, timed(mfc), hbm_bytes=16 * (1 << lm) + 16 * (1 << (lm - 4)))
+    # per output: 4 butterfly levels of 8 (32 products), 15 twiddles + 3 squarings, 16 Lagrange weights, d^-1
+    rec("rs_multifold5_2^%d_by16" % lm, timed(mfc), hbm_bytes=16 * (1 << lm) + 16 * (1 << (lm - 4)),
+        fmuls=67 * (1 << (lm - 4)), note="integer-ALU bound: 67 F-muls per output")
     # coSumcheck phase 2 (fold by Lagrange weights), 2^24 by 16
     c2 = lambda: ctx.check(gbz.lib.gbz_cosumcheck_phase2(ctx.h, cwb.data_ptr(), 1 << lm, gbz._ptr(a16), 4,
                                                          mf.data_ptr(), D))

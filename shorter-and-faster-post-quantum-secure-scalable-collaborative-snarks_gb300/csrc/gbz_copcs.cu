@@ -17,40 +17,50 @@ __device__ __forceinline__ fe pow_tab(const fe *lo, const fe *hi, uint64_t e) { 
 // powers of omega_n^{-1} (level 0: omega_n^{-j}; level lv: omega_n^{-2^lv j}
 // for the kept index j), then y_i = d^{-1} sum_k a_k partial_i[k].
 constexpr int kMaxFoldLog = 4;
+// omega_n^{-(g step 2^lv) mod n} for level lv and group g (15 values for
+// d = 16), so that every twiddle of an output is (omega_n^{-i})^{2^lv}
+// times a constant: one table lookup per output instead of one per pair.
+struct FoldConsts {
+  fe c[kMaxFoldLog][1 << (kMaxFoldLog - 1)];
+};
+template <int LOGD>
 __global__ void __launch_bounds__(256)
-multifold5_kernel(const fe *cw, uint64_t n, const fe *a, int logd, fe *out, const fe *inv_lo, const fe *inv_hi,
-                  fe len_inv) {
-  const uint64_t d = 1ull << logd, nout = n >> logd;
+multifold5_kernel(const fe *cw, uint64_t n, const fe *a, fe *out, const fe *inv_lo, const fe *inv_hi, fe len_inv,
+                  FoldConsts k) {
+  constexpr int D = 1 << LOGD;
+  const uint64_t nout = n >> LOGD;
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nout) return;
-  fe buf[2][1 << kMaxFoldLog];
-  const uint64_t half = n / 2, step = n >> logd;
-  uint64_t groups = d / 2;
-  for (uint64_t t = 0; t < groups; t++) {
+  const uint64_t half = n / 2, step = nout;
+  fe buf[D], nb[D];
+  fe wl = pow_tab(inv_lo, inv_hi, i);  // (omega^{-i})^{2^lv}
+#pragma unroll
+  for (int t = 0; t < D / 2; t++) {
     const uint64_t j = i + t * step;
     const fe x = cw[j], y = cw[j + half];
-    buf[0][2 * t] = fadd(x, y);
-    buf[0][2 * t + 1] = fmul(pow_tab(inv_lo, inv_hi, j), fsub(x, y));
+    buf[2 * t] = fadd(x, y);
+    buf[2 * t + 1] = fmul(fmul(wl, k.c[0][t]), fsub(x, y));
   }
-  int src = 0;
-  uint64_t width = 2;
-  for (int lv = 1; lv < logd; lv++) {
-    const uint64_t ng = groups / 2;
-    for (uint64_t g = 0; g < ng; g++) {
-      const uint64_t j = i + g * step;
-      const fe po = pow_tab(inv_lo, inv_hi, (j << lv) & (n - 1));
-      for (uint64_t k = 0; k < width; k++) {
-        const fe x = buf[src][g * width + k], y = buf[src][(g + ng) * width + k];
-        buf[src ^ 1][g * 2 * width + k] = fadd(x, y);
-        buf[src ^ 1][g * 2 * width + k + width] = fmul(po, fsub(x, y));
+#pragma unroll
+  for (int lv = 1; lv < LOGD; lv++) {
+    wl = fmul(wl, wl);
+    const int groups = D >> lv, ng = groups / 2, width = 1 << lv;
+#pragma unroll
+    for (int g = 0; g < ng; g++) {
+      const fe po = fmul(wl, k.c[lv][g]);
+#pragma unroll
+      for (int q = 0; q < width; q++) {
+        const fe x = buf[g * width + q], y = buf[(g + ng) * width + q];
+        nb[g * 2 * width + q] = fadd(x, y);
+        nb[g * 2 * width + q + width] = fmul(po, fsub(x, y));
       }
     }
-    width *= 2;
-    groups = ng;
-    src ^= 1;
+#pragma unroll
+    for (int q = 0; q < D; q++) buf[q] = nb[q];
   }
   fe acc = fe_zero();
-  for (uint64_t k = 0; k < d; k++) acc = fadd(acc, fmul(a[k], buf[src][k]));
+#pragma unroll
+  for (int q = 0; q < D; q++) acc = fadd(acc, fmul(a[q], buf[q]));
   out[i] = fmul(acc, len_inv);
 }
 
@@ -260,7 +270,18 @@ void multifold5_launch(const fe *cw, uint64_t n, const fe *a, int logd, fe *out,
   if (logd < 1 || logd > kMaxFoldLog) throw ArgError("RS_multifold5: fold degree must be 2..16");
   if (n < (2ull << logd)) throw ArgError("RS_multifold5: codeword shorter than two folds");
   const fe len_inv = finv(fe_make(1ull << logd, 0));
-  multifold5_kernel<<<grid(n >> logd), 256, 0, s>>>(cw, n, a, logd, out, tn.lo_inv, tn.hi_inv, len_inv);
+  FoldConsts k{};
+  const fe om_inv = finv(root_of_unity(ilog2(n)));
+  const uint64_t step = n >> logd;
+  for (int lv = 0; lv < logd; lv++)
+    for (int g = 0; g < (1 << (logd - 1 - lv)); g++) k.c[lv][g] = fpow(om_inv, ((uint64_t)g * step << lv) & (n - 1));
+  const unsigned blocks = grid(n >> logd);
+  switch (logd) {
+    case 1: multifold5_kernel<1><<<blocks, 256, 0, s>>>(cw, n, a, out, tn.lo_inv, tn.hi_inv, len_inv, k); break;
+    case 2: multifold5_kernel<2><<<blocks, 256, 0, s>>>(cw, n, a, out, tn.lo_inv, tn.hi_inv, len_inv, k); break;
+    case 3: multifold5_kernel<3><<<blocks, 256, 0, s>>>(cw, n, a, out, tn.lo_inv, tn.hi_inv, len_inv, k); break;
+    default: multifold5_kernel<4><<<blocks, 256, 0, s>>>(cw, n, a, out, tn.lo_inv, tn.hi_inv, len_inv, k); break;
+  }
   GBZ_CUDA(cudaGetLastError());
 }
 
