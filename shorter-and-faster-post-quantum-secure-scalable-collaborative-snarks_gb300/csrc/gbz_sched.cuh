@@ -28,8 +28,9 @@ struct SchedOpts {
 // Serving: the first kHighSlots slots run at the device's greatest stream
 // priority and take proofs of 2^kBigLogn or more first, so that the long
 // proofs (the latency tail) are not slowed by the many short ones, which
-// fill the SMs they leave idle.
-constexpr int kHighSlots = 2;
+// fill the SMs they leave idle.  One such slot measured best: two long
+// proofs side by side slow each other down.
+constexpr int kHighSlots = 1;
 constexpr int kBigLogn = 20;
 
 struct ProofJob {
