@@ -449,7 +449,8 @@ uint64_t gbz_prove_transcript_bytes(int logn, int rate);
  *    12 WHIR_ANSWERS 16B x l, 13 WHIR_PATHS 32B x l*depth,
  *    14 WHIR_COMBINE 16B x l, 15 WHIR_K 16B
  *  16 FINAL_POLY 16B x m | 17 FINAL_POINT 16B x log2 m | 18 FINAL_EVAL 16B
- * witness: 2^logn elements; transcript: gbz_prove_transcript_bytes bytes.
+ * witness: 2^logn elements (3 <= logn <= 25, rate a power of two in [2, 64],
+ * codeword rate * 2^logn <= 2^26); transcript: gbz_prove_transcript_bytes bytes.
  * With GBZ_MEM_HOST the call also checks the device-side consistency flags
  * (every round's claim) and returns GBZ_ECHECK if one failed. */
 gbz_status gbz_prove(gbz_ctx *ctx, const uint64_t *witness, int logn, int rate, uint32_t prng_seed,

@@ -168,7 +168,7 @@ BatchPlan batch_plan(int k, const uint64_t *sizes, int rate, int whir_k) {
     if (i && sizes[i] > sizes[i - 1]) throw ArgError("batch open: sizes must not increase");
   }
   if (sizes[0] < 2 * (uint64_t)whir_k) throw ArgError("batch open: the largest polynomial needs 2 whir_k entries");
-  if (ilog2(sizes[0] * (uint64_t)rate) > kMaxLogN) throw ArgError("batch open: codeword longer than 2^28");
+  if (ilog2(sizes[0] * (uint64_t)rate) > kMaxNttLogN) throw ArgError("batch open: codeword longer than 2^26");
   P.k = k;
   P.rate = rate;
   P.whir_k = whir_k;

@@ -345,7 +345,7 @@ gbz_status gbz_fft(gbz_ctx *ctx, uint64_t *data, int logn, int inverse, int mem)
   API_BEGIN(ctx)
   check_mem(mem);
   need(data, "data");
-  if (logn < 0 || logn > kMaxLogN) throw ArgError("fft: logn out of range [0, 28]");
+  if (logn < 0 || logn > kMaxNttLogN) throw ArgError("fft: logn out of range [0, 26]");
   const uint64_t L = 1ull << logn, bytes = 16 * L;
   fe *d = dev_view(ctx, 0, (fe *)data, bytes, mem, true);
   fe *tmp = (fe *)ctx->buf(1, bytes);
@@ -363,7 +363,7 @@ gbz_status gbz_rs_encode(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int rate
   check_pow2(m, "rs_encode: m");
   if (rate < 1 || !is_pow2((uint64_t)rate)) throw ArgError("rs_encode: rate must be a power of two");
   const uint64_t L = m * (uint64_t)rate;
-  if (ilog2(L) > kMaxLogN) throw ArgError("rs_encode: codeword longer than 2^28");
+  if (ilog2(L) > kMaxNttLogN) throw ArgError("rs_encode: codeword longer than 2^26");
   const fe *din = dev_view(ctx, 0, (const fe *)arr, 16 * m, mem, true);
   fe *dout = dev_view(ctx, 1, (fe *)codeword, 16 * L, mem, false);
   fe *tmp = (fe *)ctx->buf(2, 16 * L);
@@ -416,7 +416,7 @@ gbz_status gbz_whir_commit(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int ra
   if (rate < 1 || !is_pow2((uint64_t)rate)) throw ArgError("whir_commit: rate must be a power of two");
   const uint64_t L = m * (uint64_t)rate;
   if (L < 4) throw ArgError("whir_commit: codeword shorter than one leaf");
-  if (ilog2(L) > kMaxLogN) throw ArgError("whir_commit: codeword longer than 2^28");
+  if (ilog2(L) > kMaxNttLogN) throw ArgError("whir_commit: codeword longer than 2^26");
   const fe *din = dev_view(ctx, 0, (const fe *)arr, 16 * m, mem, true);
   fe *dcw = dev_view(ctx, 1, (fe *)codeword, 16 * L, mem, false);
   uint8_t *dlv = dev_view(ctx, 2, levels, 32 * merkle_hashes(L), mem, false);
@@ -633,7 +633,7 @@ gbz_status gbz_encode_rows(gbz_ctx *ctx, const uint64_t *rows, int nrows, int lo
   if (nrows < 0 || logrow < 0 || log_rate_offset < 0) throw ArgError("encode: negative size");
   if (rate < 1 || !is_pow2((uint64_t)rate)) throw ArgError("encode: rate must be a power of two");
   const uint64_t n = 1ull << logrow, L = n * (uint64_t)rate;
-  if (ilog2(L) > kMaxLogN || 1 + log_rate_offset + logrow > kMaxLogN) throw ArgError("encode: length above 2^28");
+  if (ilog2(L) > kMaxNttLogN || 1 + log_rate_offset + logrow > kMaxLogN) throw ArgError("encode: length above 2^26");
   if (!nrows) return GBZ_OK;
   const fe *drows = dev_view(ctx, 0, (const fe *)rows, 16 * n * nrows, mem, true);
   fe *dout = dev_view(ctx, 1, (fe *)out, 16 * L * nrows, mem, false);
@@ -667,7 +667,7 @@ gbz_status gbz_encode_concatenated(gbz_ctx *ctx, const uint64_t *data, uint64_t 
     throw ArgError("encode_concatenated: rates must be powers of two");
   if (degree < 1 || !is_pow2((uint64_t)degree)) throw ArgError("encode_concatenated: degree must be a power of two");
   const uint64_t L = n * (uint64_t)rate0, D = (uint64_t)degree * rate1;
-  if (ilog2(L) > kMaxLogN) throw ArgError("encode_concatenated: codeword above 2^28");
+  if (ilog2(L) > kMaxNttLogN) throw ArgError("encode_concatenated: codeword above 2^26");
   if (D > (1u << 13)) throw ArgError("encode_concatenated: degree * rate1 above 2^13");
   if ((uint64_t)degree > L) throw ArgError("encode_concatenated: degree above the codeword length");
   const uint64_t rows = L / degree;
@@ -1310,7 +1310,7 @@ gbz_status gbz_merkle_autotune(gbz_ctx *ctx, int logN, int reps, int *log_nodes,
 
 gbz_status gbz_ntt_autotune(gbz_ctx *ctx, int logn, int reps, int *shape, double *ms_default, double *ms_best) {
   API_BEGIN(ctx)
-  if (logn <= 13 || logn > kMaxLogN) throw ArgError("ntt autotune: lengths 2^14 .. 2^28 (one pass below)");
+  if (logn <= 13 || logn > kMaxNttLogN) throw ArgError("ntt autotune: lengths 2^14 .. 2^26 (one pass below)");
   if (reps < 1) reps = 3;
   const uint64_t L = 1ull << logn;
   fe *buf = (fe *)ctx->buf(110, 16 * L);

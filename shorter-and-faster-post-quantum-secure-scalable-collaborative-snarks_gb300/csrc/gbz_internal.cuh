@@ -10,7 +10,8 @@
 
 namespace gbz {
 
-constexpr int kMaxLogN = 28;        // largest NTT / codeword: 2^28 elements
+constexpr int kMaxLogN = 28;        // largest vector, Merkle tree or eq table: 2^28 elements
+constexpr int kMaxNttLogN = 26;     // largest transform: two passes of at most 2^13
 constexpr int kMaxQueries = 256;    // WHIR queries per iteration (rate 2 needs 200)
 constexpr int kWhirLogK = 2;        // folding factor 4 (whir_k = 4) of the plain prover
 constexpr int kWhirK = 1 << kWhirLogK;

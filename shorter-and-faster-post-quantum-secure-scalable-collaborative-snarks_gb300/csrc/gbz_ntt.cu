@@ -556,7 +556,7 @@ NttShape ntt_default_shape(int logn) {
 }
 
 bool ntt_shape_valid(int logn, const NttShape &sh) {
-  if (logn <= kSubLog || logn > kMaxLogN) return false;
+  if (logn <= kSubLog || logn > kMaxNttLogN) return false;
   const int k2 = logn - sh.k1;
   if (sh.k1 < 1 || sh.k1 > kSubLog || k2 < 1 || k2 > kSubLog) return false;
   if (sh.logBA < 0 || sh.logBA > sh.k1 || k2 + sh.logBA > kSubLog) return false;
@@ -565,7 +565,7 @@ bool ntt_shape_valid(int logn, const NttShape &sh) {
 }
 
 NttShape ntt_get_shape(int logn) {
-  if (logn <= kSubLog || logn > kMaxLogN) return NttShape{};
+  if (logn <= kSubLog || logn > kMaxNttLogN) return NttShape{};
   return g_shape[logn].k1 > 0 ? g_shape[logn] : ntt_default_shape(logn);
 }
 
@@ -606,6 +606,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
                   cudaStream_t s, int rows = 1, uint64_t row_in = 0, uint64_t row_out = 0) {
   const int logn = t.logn;
   const uint64_t L = 1ull << logn;
+  if (logn > kMaxNttLogN) throw ArgError("transform longer than 2^26 (two passes of at most 2^13)");
   if (n_valid > L) n_valid = L;
   PassArgs a{};
   a.row_in = row_in;

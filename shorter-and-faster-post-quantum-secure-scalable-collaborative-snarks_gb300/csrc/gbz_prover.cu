@@ -482,7 +482,7 @@ __global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8
 // ------------------------------------------------------------ host side
 
 bool update_betas_by_transform(int l, uint64_t nb, uint64_t N) {
-  return ilog2(N) > 13 && nb <= N && (uint64_t)l * nb > 4 * N;
+  return ilog2(N) > 13 && ilog2(N) <= kMaxNttLogN && nb <= N && (uint64_t)l * nb > 4 * N;
 }
 
 int whir_query_count(int rate) { return (int)(-100.0 / log2(sqrt(1.0 / (double)rate))); }
@@ -534,10 +534,10 @@ NttTables &ProofPlan::tables(int lg) {
 }
 
 std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
-  if (logn < 3 || logn > 26) throw ArgError("prover: log2 witness length must be in [3, 26]");
+  if (logn < 3 || logn > 25) throw ArgError("prover: log2 witness length must be in [3, 25]");
   if (rate < 2 || rate > 64 || !is_pow2((uint64_t)rate)) throw ArgError("prover: rate must be a power of two in [2, 64]");
   const uint64_t n = 1ull << logn, L = n * (uint64_t)rate;
-  if (ilog2(L) > kMaxLogN) throw ArgError("prover: codeword longer than 2^28");
+  if (ilog2(L) > kMaxNttLogN) throw ArgError("prover: codeword longer than 2^26");
   auto p = std::unique_ptr<ProofPlan>(new ProofPlan());
   p->logn = logn;
   p->rate = rate;

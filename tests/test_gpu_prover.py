@@ -136,3 +136,22 @@ def test_prove_graph_per_device_address(ctx, gbz, oracle):
             ctx.prove(dw, logn, rate, 1 + k, out=out)
             torch.cuda.synchronize()
             assert out.cpu().numpy().tobytes() == oracle.prove(ws[k], logn, rate, 1 + k)
+
+
+@pytest.mark.parametrize("logn,rate,seed", [(25, 2, 3), (20, 64, 5), (18, 32, 1)])
+def test_prove_largest_shapes_vs_oracle(ctx, oracle, logn, rate, seed):
+    """The largest codewords the prover takes (2^26: a 2^25 witness at rate
+    1/2, or 2^20 at rate 1/64) and a high rate, against the oracle."""
+    w = oracle.witness(0x5EED0000 + 7 * 65536 + logn, 1 << logn)
+    got = ctx.prove(w, logn, rate, seed).tobytes()
+    ref = oracle.prove(w, logn, rate, seed)
+    assert len(got) == len(ref)
+    assert hashlib.sha256(got).hexdigest() == hashlib.sha256(ref).hexdigest()
+
+
+def test_prove_rejects_out_of_range_shapes(ctx, gbz, oracle):
+    w = oracle.witness(2, 1 << 8)
+    for logn, rate in ((26, 2), (21, 64), (27, 2), (2, 2), (8, 3), (8, 1), (8, 128)):
+        with pytest.raises(gbz.GbzError) as e:
+            ctx.prove(np.zeros((1 << min(logn, 8), 2), np.uint64), logn, rate, 1)
+        assert e.value.status in (gbz.EINVAL, gbz.ESMALL)
