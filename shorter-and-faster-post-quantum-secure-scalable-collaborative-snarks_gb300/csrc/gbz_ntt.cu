@@ -88,7 +88,8 @@ __device__ __forceinline__ uint32_t swz(uint32_t a) { return a ^ ((a >> 3) & 7u)
 __device__ __forceinline__ uint64_t lz_add(uint64_t a, uint64_t b) { return a + b; }
 // a - b + m*p for b < m*p (m a power of two times p keeps it cheap: kp - b).
 __device__ __forceinline__ uint64_t lz_sub(uint64_t a, uint64_t b, uint64_t mp) { return a + (mp - b); }
-// Fold any 64-bit value to [0, p] (p itself stands for zero).
+// Fold any 64-bit value to [0, p + 7]; values up to p + 7 fold to [0, p]
+// (p itself stands for zero).
 __device__ __forceinline__ uint64_t fold(uint64_t x) { return (x & P) + (x >> 61); }
 __device__ __forceinline__ uint64_t fold2(uint64_t x) { return fold(fold(x)); }
 // x * 2^k mod p for x in [0, p]: a rotation of the 61-bit word (p maps to p).
@@ -96,6 +97,9 @@ __device__ __forceinline__ uint64_t rotp(uint64_t x, int k) { return ((x << k) &
 __device__ __forceinline__ uint64_t canon(uint64_t x) {  // [0, p + 7] -> [0, p)
   return x >= P ? x - P : x;
 }
+// A staged value (folded to [0, p + 7] by the last radix-8 stage, or
+// canonical) made canonical for the output.
+__device__ __forceinline__ fe canon_fe(fe x) { return fe_make(canon(x.re), canon(x.im)); }
 
 struct lz {
   uint64_t re, im;
@@ -103,7 +107,6 @@ struct lz {
 __device__ __forceinline__ lz lz_of(fe x) { return lz{x.re, x.im}; }
 __device__ __forceinline__ lz lzadd(lz a, lz b) { return lz{lz_add(a.re, b.re), lz_add(a.im, b.im)}; }
 __device__ __forceinline__ lz lzsub(lz a, lz b, uint64_t mp) { return lz{lz_sub(a.re, b.re, mp), lz_sub(a.im, b.im, mp)}; }
-__device__ __forceinline__ fe lz_canon(lz a) { return fe_make(canon(fold(a.re)), canon(fold(a.im))); }
 
 // Multiplications by the small roots on lazy values below 2p.
 // getRootOfUnity(2) = -i and getRootOfUnity(3) = 2^30 (1 - i).
@@ -125,7 +128,8 @@ __device__ __forceinline__ lz lz_w8_3(lz x) {  // forward * 2^30 (-1 - i), inver
 }
 
 // In-register DFTs with natural-order output: V[k] = sum_q v[q] w_R^{qk}.
-// Inputs canonical, outputs canonical; additions in between are lazy.
+// dft2 and dft4 take and return canonical values (they only run as the first
+// stage); dft8 keeps its additions lazy (bounds at its definition).
 template <bool INV>
 __device__ __forceinline__ void dft2(fe *v) {
   fe a = v[0], b = v[1];
@@ -142,26 +146,33 @@ __device__ __forceinline__ void dft4(fe *v) {
   v[1] = fadd(d0, d1);
   v[3] = fsub(d0, d1);
 }
+// Inputs: v[0] <= p + 7 (a folded output of the previous stage), v[1..7]
+// <= p (canonical, or p standing for zero).  Every intermediate below stays
+// within 8p + 7 = 2^64 - 1, and the outputs are folded once to [0, p + 7]:
+// the next stage multiplies v[1..7] by twiddles (canonical products) and
+// takes v[0] as it is; the pass epilogue makes the last stage's values
+// canonical.
 template <bool INV>
 __device__ __forceinline__ void dft8(fe *v) {
   const uint64_t P2 = 2 * P, P4 = 4 * P;
   lz a[4], b[4];
 #pragma unroll
-  for (int q = 0; q < 4; q++) {  // < 2p
+  for (int q = 0; q < 4; q++) {  // <= 2p (<= 2p + 7 for q = 0)
     a[q] = lzadd(lz_of(v[q]), lz_of(v[q + 4]));
     b[q] = lzsub(lz_of(v[q]), lz_of(v[q + 4]), P);
   }
   b[1] = lz_w8<INV>(b[1]);    // <= p
   b[2] = lz_w4<INV>(b[2]);    // < 2p
   b[3] = lz_w8_3<INV>(b[3]);  // <= p
-  // two radix-4 DFTs on inputs < 2p: c < 4p, d < 4p, outputs < 8p
+  // two radix-4 DFTs on inputs <= 2p (x[0] <= 2p + 7): c, d <= 4p + 7,
+  // outputs <= 8p + 7
   lz out[8];
 #pragma unroll
   for (int h = 0; h < 2; h++) {
     lz *x = h ? b : a;
     lz c0 = lzadd(x[0], x[2]), c1 = lzadd(x[1], x[3]);
     lz d0 = lzsub(x[0], x[2], P2), d1 = lzsub(x[1], x[3], P2);
-    // d1 * w4 on a value < 4p: fold to <= p first
+    // d1 * w4 on a value <= 4p: fold to <= p + 3 first
     d1 = lz{fold(d1.re), fold(d1.im)};
     d1 = INV ? lz{P2 - d1.im, d1.re} : lz{d1.im, P2 - d1.re};  // < 2p
     out[h + 0] = lzadd(c0, c1);       // V[0 + h]
@@ -170,7 +181,7 @@ __device__ __forceinline__ void dft8(fe *v) {
     out[h + 6] = lzsub(d0, d1, P4);   // V[6 + h]
   }
 #pragma unroll
-  for (int k = 0; k < 8; k++) v[k] = lz_canon(out[k]);
+  for (int k = 0; k < 8; k++) v[k] = fe_make(fold(out[k].re), fold(out[k].im));
 }
 
 // omega_S^e from the half table T[t] = omega_S^t (t < S/2):
@@ -180,6 +191,15 @@ __device__ __forceinline__ fe twiddle(const fe *T, uint32_t e, int logS) {
   const fe w = T[e & ((1u << hshift) - 1)];
   if (e >> hshift) return fe_make(w.re ? P - w.re : 0, w.im ? P - w.im : 0);
   return w;
+}
+
+// The same for e < S with p standing for zero in the negated value (a
+// twiddle only enters fmul, which takes operands up to p).
+__device__ __forceinline__ fe twiddle_lazy(const fe *T, uint32_t e, int logS) {
+  const uint32_t half = 1u << (logS - 1);
+  const bool hi = e >= half;
+  const fe w = T[hi ? e - half : e];
+  return hi ? fe_make(P - w.re, P - w.im) : w;
 }
 
 // One radix-R Stockham stage over E staged elements (B sub-transforms of
@@ -204,8 +224,18 @@ __device__ __forceinline__ void stockham_stage(fe *sm, const fe *T, int logS, in
       if (logNs > 0) {
         const uint32_t k = j & ((1u << logNs) - 1);
         const int sh = logS - logNs - LOGR;
+        if (R == 8) {
+          // u < S/8, so the exponents r u of r <= 4 stay in the half table
+          // and only r = 5..7 may need the negation.
+          const uint32_t u = k << sh;
 #pragma unroll
-        for (int r = 1; r < R; r++) v[i * R + r] = fmul(v[i * R + r], twiddle(T, (r * k) << sh, logS));
+          for (int r = 1; r <= 4; r++) v[i * R + r] = fmul(v[i * R + r], T[r * u]);
+#pragma unroll
+          for (int r = 5; r < 8; r++) v[i * R + r] = fmul(v[i * R + r], twiddle_lazy(T, r * u, logS));
+        } else {
+#pragma unroll
+          for (int r = 1; r < R; r++) v[i * R + r] = fmul(v[i * R + r], twiddle(T, (r * k) << sh, logS));
+        }
       }
       if (R == 8) dft8<INV>(&v[i * R]);
       else if (R == 4) dft4<INV>(&v[i * R]);
@@ -331,7 +361,7 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
   if (a.out_kstride == 1) {
     for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
       const uint32_t b = e >> logS, k = e & (S - 1);
-      fe v = sm[swz(e)];
+      fe v = canon_fe(sm[swz(e)]);
       if (a.tw_lo && nonzero) {
         const uint64_t ex = (g0 + b) * k;
         v = fmul(v, fmul(a.tw_lo[ex & ((1u << kTwLoBits) - 1)], a.tw_hi[ex >> kTwLoBits]));
@@ -359,13 +389,13 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
         if (e >= total) continue;
         const uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
         const uint64_t addr = (g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride;
-        a.out[addr] = fmul(sm[swz((b << logS) + k)], tw[i]);
+        a.out[addr] = fmul(sm[swz((b << logS) + k)], tw[i]);  // takes the folded value as it is
       }
     }
   } else {
     for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
       const uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
-      fe v = sm[swz((b << logS) + k)];
+      fe v = canon_fe(sm[swz((b << logS) + k)]);
       const uint64_t addr = (g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride;
       if (a.tw_full && nonzero) {
         v = fmul(v, a.tw_full[addr]);
