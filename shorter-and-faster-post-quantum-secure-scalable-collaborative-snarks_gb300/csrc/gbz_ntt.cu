@@ -115,16 +115,21 @@ __device__ __forceinline__ lz lz_w4(lz x) {  // forward * (-i), inverse * i; inp
   const uint64_t p2 = 2 * P;
   return INV ? lz{p2 - x.im, x.re} : lz{x.im, p2 - x.re};
 }
+// s * 2^30 (mod p) for s < 2^63: s = h 2^31 + l gives h 2^61 + l 2^30 = h + l 2^30;
+// the result is below p + 2^32.
+__device__ __forceinline__ uint64_t mul2e30(uint64_t s) { return ((s << 30) & P) + (s >> 31); }
+// On inputs <= 2p per component the sums below stay within 4p; outputs < p + 2^32.
 template <bool INV>
-__device__ __forceinline__ lz lz_w8(lz x) {  // forward * 2^30 (1 - i), inverse * 2^30 (1 + i); output <= p
-  const uint64_t s = fold2(x.re + x.im), d = INV ? fold2(x.re + (2 * P - x.im)) : fold2(x.im + (2 * P - x.re));
-  return INV ? lz{rotp(d, 30), rotp(s, 30)} : lz{rotp(s, 30), rotp(d, 30)};
+__device__ __forceinline__ lz lz_w8(lz x) {  // forward * 2^30 (1 - i), inverse * 2^30 (1 + i)
+  const uint64_t s = mul2e30(x.re + x.im);
+  const uint64_t d = INV ? mul2e30(x.re + (2 * P - x.im)) : mul2e30(x.im + (2 * P - x.re));
+  return INV ? lz{d, s} : lz{s, d};
 }
 template <bool INV>
-__device__ __forceinline__ lz lz_w8_3(lz x) {  // forward * 2^30 (-1 - i), inverse * 2^30 (-1 + i); output <= p
-  const uint64_t s = fold2(x.re + x.im), ns = P - s;
-  const uint64_t d = INV ? fold2(x.re + (2 * P - x.im)) : fold2(x.im + (2 * P - x.re));
-  return INV ? lz{rotp(ns, 30), rotp(d, 30)} : lz{rotp(d, 30), rotp(ns, 30)};
+__device__ __forceinline__ lz lz_w8_3(lz x) {  // forward * 2^30 (-1 - i), inverse * 2^30 (-1 + i)
+  const uint64_t ns = mul2e30(4 * P - (x.re + x.im));
+  const uint64_t d = INV ? mul2e30(x.re + (2 * P - x.im)) : mul2e30(x.im + (2 * P - x.re));
+  return INV ? lz{ns, d} : lz{d, ns};
 }
 
 // In-register DFTs with natural-order output: V[k] = sum_q v[q] w_R^{qk}.
@@ -161,9 +166,9 @@ __device__ __forceinline__ void dft8(fe *v) {
     a[q] = lzadd(lz_of(v[q]), lz_of(v[q + 4]));
     b[q] = lzsub(lz_of(v[q]), lz_of(v[q + 4]), P);
   }
-  b[1] = lz_w8<INV>(b[1]);    // <= p
-  b[2] = lz_w4<INV>(b[2]);    // < 2p
-  b[3] = lz_w8_3<INV>(b[3]);  // <= p
+  b[1] = lz_w8<INV>(b[1]);    // < p + 2^32
+  b[2] = lz_w4<INV>(b[2]);    // <= 2p
+  b[3] = lz_w8_3<INV>(b[3]);  // < p + 2^32
   // two radix-4 DFTs on inputs <= 2p (x[0] <= 2p + 7): c, d <= 4p + 7,
   // outputs <= 8p + 7
   lz out[8];
@@ -193,24 +198,18 @@ __device__ __forceinline__ fe twiddle(const fe *T, uint32_t e, int logS) {
   return w;
 }
 
-// The same for e < S with p standing for zero in the negated value (a
-// twiddle only enters fmul, which takes operands up to p).
-__device__ __forceinline__ fe twiddle_lazy(const fe *T, uint32_t e, int logS) {
-  const uint32_t half = 1u << (logS - 1);
-  const bool hi = e >= half;
-  const fe w = T[hi ? e - half : e];
-  return hi ? fe_make(P - w.re, P - w.im) : w;
-}
-
 // One radix-R Stockham stage over E staged elements (B sub-transforms of
-// length S = 2^logS), Ns = product of the earlier radices:
+// length S = 2^LOGS), Ns = 2^LOGNS = product of the earlier radices:
 //   butterfly (b, j): v[r] = x[j + r S/R] * omega_{Ns R}^{r (j mod Ns)},
 //   DFT_R(v), x'[(j/Ns) Ns R + (j mod Ns) + r Ns] = v[r].
-template <int R, bool INV>
-__device__ __forceinline__ void stockham_stage(fe *sm, const fe *T, int logS, int logE, int logNs) {
+// S and Ns are compile-time, so shifts, masks and the swizzled offsets of a
+// butterfly's elements fold into immediates: when the stride between them is
+// a multiple of 64 elements, swz(a + r stride) = swz(a) + r stride.
+template <int R, bool INV, int LOGS, int LOGNS>
+__device__ __forceinline__ void stockham_stage(fe *sm, const fe *T, int logE) {
   constexpr int LOGR = R == 8 ? 3 : (R == 4 ? 2 : 1);
   constexpr int PER = kPerThread / R;
-  const int logSR = logS - LOGR;
+  constexpr int logSR = LOGS - LOGR;
   const uint32_t nb = 1u << (logE - LOGR);
   fe v[PER * R];
 #pragma unroll
@@ -218,23 +217,35 @@ __device__ __forceinline__ void stockham_stage(fe *sm, const fe *T, int logS, in
     const uint32_t u = threadIdx.x + i * blockDim.x;
     if (u < nb) {
       const uint32_t b = u >> logSR, j = u & ((1u << logSR) - 1);
-      const uint32_t base = (b << logS) + j;
+      const uint32_t base = (b << LOGS) + j;
+      if constexpr (logSR >= 6) {
+        const fe *src = sm + swz(base);
 #pragma unroll
-      for (int r = 0; r < R; r++) v[i * R + r] = sm[swz(base + ((uint32_t)r << logSR))];
-      if (logNs > 0) {
-        const uint32_t k = j & ((1u << logNs) - 1);
-        const int sh = logS - logNs - LOGR;
+        for (int r = 0; r < R; r++) v[i * R + r] = src[(uint32_t)r << logSR];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) v[i * R + r] = sm[swz(base + ((uint32_t)r << logSR))];
+      }
+      if (LOGNS > 0) {
+        const uint32_t k = j & ((1u << LOGNS) - 1);
+        constexpr int sh = LOGS - LOGNS - LOGR;
         if (R == 8) {
-          // u < S/8, so the exponents r u of r <= 4 stay in the half table
-          // and only r = 5..7 may need the negation.
-          const uint32_t u = k << sh;
+          // k << sh < S/8, so the exponents r (k << sh) of r <= 4 stay in the
+          // half table and only r = 5..7 may need the negation.
+          const fe *tw = T + (k << sh);
+          constexpr uint32_t half = 1u << (LOGS - 1);
 #pragma unroll
-          for (int r = 1; r <= 4; r++) v[i * R + r] = fmul(v[i * R + r], T[r * u]);
+          for (int r = 1; r <= 4; r++) v[i * R + r] = fmul(v[i * R + r], tw[(r - 1) * (k << sh)]);  // T[r (k << sh)]
 #pragma unroll
-          for (int r = 5; r < 8; r++) v[i * R + r] = fmul(v[i * R + r], twiddle_lazy(T, r * u, logS));
+          for (int r = 5; r < 8; r++) {
+            const uint32_t e = r * (k << sh);
+            const bool hi = e >= half;
+            const fe w = T[hi ? e - half : e];
+            v[i * R + r] = fmul(v[i * R + r], hi ? fe_make(P - w.re, P - w.im) : w);
+          }
         } else {
 #pragma unroll
-          for (int r = 1; r < R; r++) v[i * R + r] = fmul(v[i * R + r], twiddle(T, (r * k) << sh, logS));
+          for (int r = 1; r < R; r++) v[i * R + r] = fmul(v[i * R + r], twiddle(T, (r * k) << sh, LOGS));
         }
       }
       if (R == 8) dft8<INV>(&v[i * R]);
@@ -248,27 +259,62 @@ __device__ __forceinline__ void stockham_stage(fe *sm, const fe *T, int logS, in
     const uint32_t u = threadIdx.x + i * blockDim.x;
     if (u < nb) {
       const uint32_t b = u >> logSR, j = u & ((1u << logSR) - 1);
-      const uint32_t k = j & ((1u << logNs) - 1);
-      const uint32_t dst = (b << logS) + ((j >> logNs) << (logNs + LOGR)) + k;
+      const uint32_t k = j & ((1u << LOGNS) - 1);
+      const uint32_t dst = (b << LOGS) + ((j >> LOGNS) << (LOGNS + LOGR)) + k;
+      if constexpr (LOGNS >= 6) {
+        fe *d = sm + swz(dst);
 #pragma unroll
-      for (int r = 0; r < R; r++) sm[swz(dst + ((uint32_t)r << logNs))] = v[i * R + r];
+        for (int r = 0; r < R; r++) d[(uint32_t)r << LOGNS] = v[i * R + r];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) sm[swz(dst + ((uint32_t)r << LOGNS))] = v[i * R + r];
+      }
     }
   }
   __syncthreads();
 }
 
-template <bool INV>
-__device__ void stockham(fe *sm, const fe *T, int logS, int logE) {
-  int logNs = 0;
-  const int rem = logS % 3;
-  if (rem == 1) {
-    stockham_stage<2, INV>(sm, T, logS, logE, logNs);
-    logNs += 1;
-  } else if (rem == 2) {
-    stockham_stage<4, INV>(sm, T, logS, logE, logNs);
-    logNs += 2;
+template <bool INV, int LOGS, int LOGNS>
+__device__ __forceinline__ void stockham_radix8(fe *sm, const fe *T, int logE) {
+  if constexpr (LOGNS < LOGS) {
+    stockham_stage<8, INV, LOGS, LOGNS>(sm, T, logE);
+    stockham_radix8<INV, LOGS, LOGNS + 3>(sm, T, logE);
   }
-  for (; logNs < logS; logNs += 3) stockham_stage<8, INV>(sm, T, logS, logE, logNs);
+}
+
+// The stages of a length-2^LOGS transform: a radix-2 or radix-4 stage when
+// LOGS is not a multiple of 3, then radix-8 stages.
+template <bool INV, int LOGS>
+__device__ __forceinline__ void stockham(fe *sm, const fe *T, int logE) {
+  if constexpr (LOGS % 3 == 1) {
+    stockham_stage<2, INV, LOGS, 0>(sm, T, logE);
+    stockham_radix8<INV, LOGS, 1>(sm, T, logE);
+  } else if constexpr (LOGS % 3 == 2) {
+    stockham_stage<4, INV, LOGS, 0>(sm, T, logE);
+    stockham_radix8<INV, LOGS, 2>(sm, T, logE);
+  } else {
+    stockham_radix8<INV, LOGS, 0>(sm, T, logE);
+  }
+}
+
+template <bool INV>
+__device__ __forceinline__ void stockham_dispatch(fe *sm, const fe *T, int logS, int logE) {
+  switch (logS) {
+    case 1: stockham<INV, 1>(sm, T, logE); break;
+    case 2: stockham<INV, 2>(sm, T, logE); break;
+    case 3: stockham<INV, 3>(sm, T, logE); break;
+    case 4: stockham<INV, 4>(sm, T, logE); break;
+    case 5: stockham<INV, 5>(sm, T, logE); break;
+    case 6: stockham<INV, 6>(sm, T, logE); break;
+    case 7: stockham<INV, 7>(sm, T, logE); break;
+    case 8: stockham<INV, 8>(sm, T, logE); break;
+    case 9: stockham<INV, 9>(sm, T, logE); break;
+    case 10: stockham<INV, 10>(sm, T, logE); break;
+    case 11: stockham<INV, 11>(sm, T, logE); break;
+    case 12: stockham<INV, 12>(sm, T, logE); break;
+    case 13: stockham<INV, 13>(sm, T, logE); break;
+    default: break;  // length 1: nothing to do
+  }
 }
 
 __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
@@ -354,8 +400,8 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
   }
 
   if (nonzero) {
-    if (a.inverse) stockham<true>(sm, T, logS, logE);
-    else stockham<false>(sm, T, logS, logE);
+    if (a.inverse) stockham_dispatch<true>(sm, T, logS, logE);
+    else stockham_dispatch<false>(sm, T, logS, logE);
   }
 
   if (a.out_kstride == 1) {
