@@ -15,11 +15,14 @@
 //      pass B: for each row k2 < N2, a length-N1 DFT over the row,
 //              stored at k2 + N2*k1 (natural order, no bit reversal pass).
 //
-// Inside a pass every CTA stages B sub-transforms of length S in shared
-// memory (bit-reversed on load), runs the radix-2 decimation-in-time
-// stages with __syncthreads between them, and applies the outer twiddle
-// and the inverse scale on the way out.  Groups of B >= 2 neighbouring
-// columns make the strided pass read whole 32-byte sectors.
+// Inside a pass every CTA holds B sub-transforms of length S in shared
+// memory and runs self-sorting (Stockham) stages on them, radix 8 after one
+// radix-2 or radix-4 stage when log2 S is not a multiple of 3.  The first
+// stage runs on the values as they are loaded from global memory; the
+// others read and write shared memory with __syncthreads between them.  The
+// outer twiddle and the inverse scale are applied on the way out.  Groups of
+// B >= 2 neighbouring columns make the strided pass read whole 32-byte
+// sectors.
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -88,12 +91,8 @@ __device__ __forceinline__ uint32_t swz(uint32_t a) { return a ^ ((a >> 3) & 7u)
 __device__ __forceinline__ uint64_t lz_add(uint64_t a, uint64_t b) { return a + b; }
 // a - b + m*p for b < m*p (m a power of two times p keeps it cheap: kp - b).
 __device__ __forceinline__ uint64_t lz_sub(uint64_t a, uint64_t b, uint64_t mp) { return a + (mp - b); }
-// Fold any 64-bit value to [0, p + 7]; values up to p + 7 fold to [0, p]
-// (p itself stands for zero).
+// Fold any 64-bit value to [0, p + 7] (p itself stands for zero).
 __device__ __forceinline__ uint64_t fold(uint64_t x) { return (x & P) + (x >> 61); }
-__device__ __forceinline__ uint64_t fold2(uint64_t x) { return fold(fold(x)); }
-// x * 2^k mod p for x in [0, p]: a rotation of the 61-bit word (p maps to p).
-__device__ __forceinline__ uint64_t rotp(uint64_t x, int k) { return ((x << k) & P) | (x >> (61 - k)); }
 __device__ __forceinline__ uint64_t canon(uint64_t x) {  // [0, p + 7] -> [0, p)
   return x >= P ? x - P : x;
 }
@@ -317,6 +316,78 @@ __device__ __forceinline__ void stockham_dispatch(fe *sm, const fe *T, int logS,
   }
 }
 
+// The first stage (Ns = 1, no twiddles) fused into the staging from global
+// memory: a thread loads the R inputs x[b, j + r S/R] of its butterflies,
+// transforms them in registers and stores x'[b, R j + r], so the stage costs
+// no shared-memory round trip.  Contiguous sub-transforms give consecutive
+// threads consecutive j; strided ones (columns of the first four-step pass)
+// consecutive sub-transforms b, whose columns are adjacent in memory.
+template <bool INV, int LOGS>
+__device__ __forceinline__ void staged_first_stage(fe *sm, const PassArgs &a, uint64_t g0, int logB, int logE) {
+  constexpr int LOGR = LOGS % 3 == 1 ? 1 : (LOGS % 3 == 2 ? 2 : 3);
+  constexpr int R = 1 << LOGR, PER = kPerThread / R, logSR = LOGS - LOGR;
+  const uint32_t nb = 1u << (logE - LOGR);
+  const bool contiguous = a.in_jstride == 1;
+  fe v[PER][R];
+#pragma unroll
+  for (int i = 0; i < PER; i++) {  // all loads first: PER * R = 8 in flight
+    const uint32_t u = threadIdx.x + i * blockDim.x;
+    const uint32_t b = contiguous ? u >> logSR : u & ((1u << logB) - 1);
+    const uint32_t j = contiguous ? u & ((1u << logSR) - 1) : u >> logB;
+    const uint64_t row = (g0 + b) * a.in_gstride;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const uint32_t jj = j + ((uint32_t)r << logSR);
+      const uint64_t addr = row + (uint64_t)jj * a.in_jstride;
+      v[i][r] = (u < nb && addr < a.n_valid && jj < a.j_valid) ? a.in[addr] : fe_zero();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const uint32_t u = threadIdx.x + i * blockDim.x;
+    if (u < nb) {
+      const uint32_t b = contiguous ? u >> logSR : u & ((1u << logB) - 1);
+      const uint32_t j = contiguous ? u & ((1u << logSR) - 1) : u >> logB;
+      if (R == 8) dft8<INV>(v[i]);
+      else if (R == 4) dft4<INV>(v[i]);
+      else dft2<INV>(v[i]);
+      const uint32_t dst = (b << LOGS) + (j << LOGR);
+#pragma unroll
+      for (int r = 0; r < R; r++) sm[swz(dst + r)] = v[i][r];
+    }
+  }
+}
+
+template <bool INV, int LOGS>
+__device__ __forceinline__ void staged_transform(fe *sm, const fe *T, const PassArgs &a, uint64_t g0, int logB,
+                                                 int logE) {
+  constexpr int LOGR = LOGS % 3 == 1 ? 1 : (LOGS % 3 == 2 ? 2 : 3);
+  staged_first_stage<INV, LOGS>(sm, a, g0, logB, logE);
+  __syncthreads();
+  stockham_radix8<INV, LOGS, LOGR>(sm, T, logE);
+}
+
+template <bool INV>
+__device__ __forceinline__ void staged_dispatch(fe *sm, const fe *T, const PassArgs &a, uint64_t g0, int logS,
+                                                int logB, int logE) {
+  switch (logS) {
+    case 1: staged_transform<INV, 1>(sm, T, a, g0, logB, logE); break;
+    case 2: staged_transform<INV, 2>(sm, T, a, g0, logB, logE); break;
+    case 3: staged_transform<INV, 3>(sm, T, a, g0, logB, logE); break;
+    case 4: staged_transform<INV, 4>(sm, T, a, g0, logB, logE); break;
+    case 5: staged_transform<INV, 5>(sm, T, a, g0, logB, logE); break;
+    case 6: staged_transform<INV, 6>(sm, T, a, g0, logB, logE); break;
+    case 7: staged_transform<INV, 7>(sm, T, a, g0, logB, logE); break;
+    case 8: staged_transform<INV, 8>(sm, T, a, g0, logB, logE); break;
+    case 9: staged_transform<INV, 9>(sm, T, a, g0, logB, logE); break;
+    case 10: staged_transform<INV, 10>(sm, T, a, g0, logB, logE); break;
+    case 11: staged_transform<INV, 11>(sm, T, a, g0, logB, logE); break;
+    case 12: staged_transform<INV, 12>(sm, T, a, g0, logB, logE); break;
+    case 13: staged_transform<INV, 13>(sm, T, a, g0, logB, logE); break;
+    default: break;
+  }
+}
+
 __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
   extern __shared__ fe smem[];
   a.in += blockIdx.y * a.row_in;
@@ -331,7 +402,6 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
     const uint32_t nT = S >> 1;
     for (uint32_t t = threadIdx.x; t < nT; t += blockDim.x) T[t] = a.wh[t << (kSubLog - logS)];
   }
-  __shared__ int nonzero;
   if (a.sp_l > 0) {
     // Sparse rows: row k2 of the intermediate holds, in column n1, the sum
     // over the entries q = n1 (mod row length) of c * omega_L^{q k2}: the
@@ -356,9 +426,13 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
       sm[swz((b << logS) + n1)] = v;
     }
     __syncthreads();
-    nonzero = 1;
+    if (a.inverse) stockham_dispatch<true>(sm, T, logS, logE);
+    else stockham_dispatch<false>(sm, T, logS, logE);
+  } else if (logS >= 1) {
+    if (a.inverse) staged_dispatch<true>(sm, T, a, g0, logS, logB, logE);
+    else staged_dispatch<false>(sm, T, a, g0, logS, logB, logE);
   } else {
-    nonzero = 1;
+    // Sub-transforms of length 1: staging only.
     // A thread stages at most kPerThread elements (blockDim >= total / 8);
     // groups of kLoadGroup loads are issued before their shared-memory
     // stores so that several global loads are in flight per thread.
@@ -399,16 +473,11 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
     __syncthreads();
   }
 
-  if (nonzero) {
-    if (a.inverse) stockham_dispatch<true>(sm, T, logS, logE);
-    else stockham_dispatch<false>(sm, T, logS, logE);
-  }
-
   if (a.out_kstride == 1) {
     for (uint32_t e = threadIdx.x; e < total; e += blockDim.x) {
       const uint32_t b = e >> logS, k = e & (S - 1);
       fe v = canon_fe(sm[swz(e)]);
-      if (a.tw_lo && nonzero) {
+      if (a.tw_lo) {
         const uint64_t ex = (g0 + b) * k;
         v = fmul(v, fmul(a.tw_lo[ex & ((1u << kTwLoBits) - 1)], a.tw_hi[ex >> kTwLoBits]));
       }
@@ -417,7 +486,7 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
       if (!a.acc) a.out[addr] = v;
       else if (addr < a.acc_n) a.out[addr] = fadd(a.out[addr], v);
     }
-  } else if (a.tw_full && nonzero && !a.has_scale && !a.acc) {
+  } else if (a.tw_full && !a.has_scale && !a.acc) {
     // first pass with the full twiddle table: issue each group's table
     // loads before its multiplies
     for (int i0 = 0; i0 < kPerThread; i0 += kLoadGroup) {
@@ -443,9 +512,9 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
       const uint32_t b = e & ((1u << logB) - 1), k = e >> logB;
       fe v = canon_fe(sm[swz((b << logS) + k)]);
       const uint64_t addr = (g0 + b) * a.out_gstride + (uint64_t)k * a.out_kstride;
-      if (a.tw_full && nonzero) {
+      if (a.tw_full) {
         v = fmul(v, a.tw_full[addr]);
-      } else if (a.tw_lo && nonzero) {
+      } else if (a.tw_lo) {
         const uint64_t ex = (g0 + b) * k;
         v = fmul(v, fmul(a.tw_lo[ex & ((1u << kTwLoBits) - 1)], a.tw_hi[ex >> kTwLoBits]));
       }
