@@ -217,7 +217,6 @@ struct QueryArgs {
   ProofState *st;
   const fe *cw;          // previous codeword
   uint64_t L;            // its length
-  const uint8_t *tree;   // its Merkle levels
   uint64_t NL;           // new codeword length
   int l;                 // number of queries
   uint8_t *tr;
@@ -392,9 +391,60 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query_s(QueryArgs a, int t
   }
 }
 
-__global__ void k_copy32(const uint8_t *src, uint8_t *dst) {
-  if (threadIdx.x < 8)
-    reinterpret_cast<uint32_t *>(dst)[threadIdx.x] = reinterpret_cast<const uint32_t *>(src)[threadIdx.x];
+// ---- the Merkle nodes a proof reveals ------------------------------------
+// create_tree_blake (merkle_tree.cpp:267-299) hashes the LEFT child twice,
+// so node i of level k is G^k(leaf i 2^k) with G(h) = blake3(h || h), and
+// leaf j = blake3(e[4j..4j+3]) (MT_commit_Blake, merkle_tree.cpp:195-233).
+// The root and the authentication paths (open_tree_blake,
+// merkle_tree.cpp:320-335) are therefore chains of compressions from single
+// leaves; the prover computes only those instead of whole trees.  The same
+// bytes as the full tree (gbz_merkle_commit_blake), which the transcript
+// tests compare with the reference's.
+__device__ __forceinline__ void leaf_hash(const fe *cw, uint64_t j, uint32_t h[8]) {
+  uint32_t m[16];
+  const uint4 *src = reinterpret_cast<const uint4 *>(cw + 4 * j);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const uint4 v = src[k];
+    m[4 * k] = v.x; m[4 * k + 1] = v.y; m[4 * k + 2] = v.z; m[4 * k + 3] = v.w;
+  }
+  blake3_block64(m, h);
+}
+__device__ __forceinline__ void node_hash(uint32_t h[8]) {  // h <- blake3(h || h)
+  uint32_t m[16];
+#pragma unroll
+  for (int k = 0; k < 8; k++) m[k] = m[8 + k] = h[k];
+  blake3_block64(m, h);
+}
+__device__ __forceinline__ void put_hash(uint8_t *dst, const uint32_t h[8]) {  // 4-byte aligned
+  uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+#pragma unroll
+  for (int k = 0; k < 8; k++) d[k] = h[k];
+}
+
+// Root of the tree over a codeword of 4 * 2^depth elements: G^depth(leaf 0).
+__global__ void k_merkle_root(const fe *cw, int depth, uint8_t *tr, uint64_t off) {
+  if (threadIdx.x) return;
+  uint32_t h[8];
+  leaf_hash(cw, 0, h);
+  for (int d = 0; d < depth; d++) node_hash(h);
+  put_hash(tr + off, h);
+}
+
+// Authentication paths of the l queries: entry d of query i is the sibling
+// (q >> d) ^ 1 of level d, i.e. G^d(leaf ((q >> d) ^ 1) << d).  One thread
+// per entry, the deepest entries first.
+__global__ void k_whir_paths_chain(const fe *cw, uint64_t leaves, int l, uint8_t *tr, uint64_t off_q,
+                                   uint64_t off_path) {
+  const int depth = 63 - __clzll((long long)leaves);
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)l * depth) return;
+  const int d = depth - 1 - (int)(t / l), i = (int)(t % l);
+  const uint64_t q = (uint64_t)(uint32_t)reinterpret_cast<const int32_t *>(tr + off_q)[i];
+  uint32_t h[8];
+  leaf_hash(cw, ((q >> d) ^ 1ull) << d, h);
+  for (int k = 0; k < d; k++) node_hash(h);
+  put_hash(tr + off_path + 32ull * ((uint64_t)depth * i + d), h);
 }
 
 }  // namespace
@@ -513,6 +563,7 @@ ProofPlan::~ProofPlan() {
   for (auto &e : ev_query)
     if (e) cudaEventDestroy(e);
   if (ev_sched) cudaEventDestroy(ev_sched);
+  if (ev_root_tail) cudaEventDestroy(ev_root_tail);
   if (ev_init) cudaEventDestroy(ev_init);
   if (s2) cudaStreamDestroy(s2);
   if (s3) cudaStreamDestroy(s3);
@@ -546,8 +597,6 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   p->w = (fe *)p->dalloc(sizeof(fe) * n);
   p->cw[0] = (fe *)p->dalloc(sizeof(fe) * L);
   p->cw[1] = (fe *)p->dalloc(sizeof(fe) * (L / 2));
-  p->tree[0] = (uint8_t *)p->dalloc(32 * merkle_hashes(L));
-  p->tree[1] = (uint8_t *)p->dalloc(32 * merkle_hashes(L / 2 >= 4 ? L / 2 : 4));
   p->tmp = (fe *)p->dalloc(sizeof(fe) * L);
   p->tmp2 = (fe *)p->dalloc(sizeof(fe) * (L / 2));
   GBZ_CUDA(cudaStreamCreateWithFlags(&p->s2, cudaStreamNonBlocking));
@@ -555,6 +604,7 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
   GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_sched, cudaEventDisableTiming));
   GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_init, cudaEventDisableTiming));
+  GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_root_tail, cudaEventDisableTiming));
   for (auto &e : p->ev_fold) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto &e : p->ev_commit) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto &e : p->ev_query) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -661,8 +711,10 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   int cwi = 0;
   uint64_t off = lay.rec(T_COMMIT_ROOT, 1, 32);
   RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(L)), ntt_launch(p.tables(ilog2(L)), w, p.n, p.cw[0], p.tmp, false, c));
-  RUN_ON(c, PC_MERKLE, merkle_launch_count(L), merkle_commit_launch(p.cw[0], L, p.tree[0], c));
-  RUN_ON(c, PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, c>>>(p.tree[0] + 32 * (merkle_hashes(L) - 1), tr + off));
+  // The root (a chain of compressions from leaf 0) is computed on the query
+  // stream once the codeword exists, off the chain of commits.
+  uint64_t off_root[kMaxWhirIter + 1];
+  off_root[0] = off;
   if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_commit[0], c));
   int iter = 0;
 
@@ -782,8 +834,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
       if (iter > 0) GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_query[iter - 1], 0));
     }
     RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(NL)), ntt_launch(p.tables(ilog2(NL)), a, m, p.cw[nci], p.tmp, false, c));
-    RUN_ON(c, PC_MERKLE, merkle_launch_count(NL), merkle_commit_launch(p.cw[nci], NL, p.tree[nci], c));
-    RUN_ON(c, PC_PROTOCOL, 1, k_copy32<<<1, 32, 0, c>>>(p.tree[nci] + 32 * (merkle_hashes(NL) - 1), tr + off));
+    off_root[iter + 1] = off;
     if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_commit[iter + 1], c));
     // queries of iteration t on q: they open the codeword of commit t and
     // check K against this iteration's round messages
@@ -792,7 +843,6 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     qa.st = st;
     qa.cw = p.cw[cwi];
     qa.L = L;
-    qa.tree = p.tree[cwi];
     qa.NL = NL;
     qa.l = l;
     qa.tr = tr;
@@ -816,12 +866,13 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
       GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_commit[iter], 0));
       GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_fold[iter], 0));
     }
+    RUN_ON(q, PC_MERKLE, 1, k_merkle_root<<<1, 32, 0, q>>>(qa.cw, depth, tr, off_root[iter]));
     RUN_ON(q, PC_QUERY, 1, k_whir_query_s<<<1, kMaxQueries, 0, q>>>(qa, iter));
     {
       const uint64_t hashes = (uint64_t)l * depth;  // depth >= 2: every queried codeword has 16+ entries
       RUN_ON(q, PC_QUERY, 1,
-             k_whir_paths<<<(unsigned)((hashes + 127) / 128), 128, 0, q>>>(qa.tree, L / 4, l, tr, qa.off_q,
-                                                                           qa.off_path));
+             k_whir_paths_chain<<<(unsigned)((hashes + 127) / 128), 128, 0, q>>>(qa.cw, L / 4, l, tr, qa.off_q,
+                                                                                 qa.off_path));
       if (!dry && hashes == 0) throw ArgError("prover: empty authentication paths");
     }
     if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_query[iter], q));
@@ -849,9 +900,13 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
   RUN(PC_PROTOCOL, 1,
       k_final<<<1, 32, 0, s>>>(st, a, p.vb[1], (int)m, tr, off_poly, off_point, off_eval, 0, st->fin_r));
+  // root of the last commitment (never opened) on the query stream
+  if (!dry) GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_commit[iter], 0));
+  RUN_ON(q, PC_MERKLE, 1, k_merkle_root<<<1, 32, 0, q>>>(p.cw[cwi], ilog2(L / 4), tr, off_root[iter]));
   if (!dry) {  // join the commit and query chains
+    GBZ_CUDA(cudaEventRecord(p.ev_root_tail, q));
     GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_commit[iter], 0));
-    GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_query[iter - 1], 0));
+    GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_root_tail, 0));
   }
 #undef RUN
 #undef RUN_ON
@@ -976,7 +1031,6 @@ void launch_proof_graph(ProofPlan &p, const fe *w, uint32_t prng_seed, cudaStrea
 uint64_t plan_bytes(int logn, int rate) {
   const uint64_t n = 1ull << logn, L = n * (uint64_t)rate;
   uint64_t b = sizeof(fe) * (n + L + L / 2 + L + L / 2 + 5 * (n / 2) + n);
-  b += 32 * (merkle_hashes(L) + merkle_hashes(L / 2 >= 4 ? L / 2 : 4));
   b += sizeof(fe) * (3 * (uint64_t)sc_blocks(n / 2) + kUpdateBetasScratch) + sizeof(ProofState);
   b += 64ull << 20;  // transcript, twiddle tables and allocation granularity (upper bound)
   return b;

@@ -56,7 +56,6 @@ struct ProofPlan {
   uint64_t n = 0, L = 0;
   fe *w = nullptr;                // witness staging (host-input proofs)
   fe *cw[2] = {nullptr, nullptr}; // codeword ping-pong (L, L/2)
-  uint8_t *tree[2] = {nullptr, nullptr};
   fe *tmp = nullptr;              // NTT intermediate of the commits (L)
   fe *tmp2 = nullptr;             // NTT intermediate of the sparse beta updates (L/2)
   // The opening runs as three chains joined by events: folds and beta
@@ -66,7 +65,7 @@ struct ProofPlan {
   cudaStream_t s2 = nullptr, s3 = nullptr;
   static constexpr int kMaxIter = kMaxWhirIter;
   cudaEvent_t ev_in = nullptr, ev_init = nullptr, ev_sched = nullptr, ev_fold[kMaxIter] = {}, ev_commit[kMaxIter + 1] = {},
-              ev_query[kMaxIter] = {};
+              ev_query[kMaxIter] = {}, ev_root_tail = nullptr;
   fe *va[2] = {nullptr, nullptr}; // folded first vector ping-pong (n/2 each)
   fe *arr = nullptr;              // the folded polynomials arr_1, arr_2, ... back to back (read by the commits)
   fe *vb[2] = {nullptr, nullptr}; // folded second vector ping-pong
