@@ -189,6 +189,12 @@ void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s);
 int sc_blocks(uint64_t pairs);
 void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2, fe *b2, bool reduce,
                     fe *partial, int blocks, cudaStream_t s);
+// Two rounds whose challenges are known in advance, in one pass: the
+// messages of (a, b) and of its fold by *chal0 (partials of blocks CTAs in
+// partial0 and partial1, blocks <= sc_blocks(m / 4)), and (a4, b4) of length
+// m/4, the fold by *chal0 then *chal1.  m >= 4.
+void sc_fold2_launch(const fe *a, const fe *b, uint64_t m, const fe *chal0, const fe *chal1, fe *a4, fe *b4,
+                     fe *partial0, fe *partial1, int blocks, cudaStream_t s);
 // The same steps for the sumcheck of sum_x w(x) eq(z, x) with the eq vector
 // kept as the shrinking table E_i of z_{i+1..}: chal == nullptr gives the
 // sums S(0), S(1) of (a, E); otherwise a is folded by *chal into a2 (m/2),

@@ -615,6 +615,7 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   p->vb[1] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
   p->beta = (fe *)p->dalloc(sizeof(fe) * n);
   p->partial = (fe *)p->dalloc(sizeof(fe) * 3 * (uint64_t)sc_blocks(n / 2));
+  p->partial2 = (fe *)p->dalloc(sizeof(fe) * 3 * (uint64_t)sc_blocks(n / 2));
   p->ub_scratch = (fe *)p->dalloc(sizeof(fe) * kUpdateBetasScratch);
   p->st = (ProofState *)p->dalloc(sizeof(ProofState));
   GBZ_CUDA(cudaFuncSetAttribute(k_sc_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -795,18 +796,19 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     const int l = whir_query_count((int)cur);
     const uint64_t NL = 2 * cur * (m / 4);
     if (2 * NL != L) throw ArgError("prover: WHIR codeword lengths must halve");
-    // round 0
+    // both rounds in one pass over (a, b): their challenges were drawn up
+    // front; arr_{t+1} goes to its own slot of p.arr, b to vb[(t + 1) mod 2]
+    // (never the buffer it is read from)
     uint64_t op = lay.rec(T_WHIR_POLY, 3, 16), oc = lay.rec(T_WHIR_CHALLENGE, 1, 16);
-    int blocks = sc_blocks(m / 2);
-    RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, nullptr, nullptr, nullptr, true, p.partial, blocks, s));
+    const uint64_t op1 = lay.rec(T_WHIR_POLY, 3, 16), oc1 = lay.rec(T_WHIR_CHALLENGE, 1, 16);
+    fe *bd = p.vb[(iter + 1) & 1];
+    const int blocks = sc_blocks(m / 4);
+    RUN(PC_SUMCHECK, 1,
+        sc_fold2_launch(a, b, m, &st->wr[iter][0], &st->wr[iter][1], arr_next, bd, p.partial, p.partial2, blocks,
+                        s));
     RUN(PC_PROTOCOL, 1, k_whir_round_s<<<1, 256, 0, s>>>(p.partial, blocks, st, iter, 0, tr, op, oc, UbPrep{}));
-    // round 1: fold by r0 into va/vb[0], message; the round kernel also
-    // prepares this iteration's beta update
-    op = lay.rec(T_WHIR_POLY, 3, 16);
-    oc = lay.rec(T_WHIR_CHALLENGE, 1, 16);
-    blocks = sc_blocks(m / 4);
-    RUN(PC_SUMCHECK, 1, sc_step_launch(a, b, m, &st->wr[iter][0], p.va[0], p.vb[0], true, p.partial, blocks, s));
     {
+      // the second round kernel also prepares this iteration's beta update
       UbPrep u{};
       if (!dry) {
         const NttTables &tnew = p.tables(ilog2(NL));
@@ -814,14 +816,10 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
         u.lo = tnew.lo_fwd;
         u.hi = tnew.hi_fwd;
       }
-      RUN(PC_PROTOCOL, 1, k_whir_round_s<<<1, 256, 0, s>>>(p.partial, blocks, st, iter, 1, tr, op, oc, u));
+      RUN(PC_PROTOCOL, 1, k_whir_round_s<<<1, 256, 0, s>>>(p.partial2, blocks, st, iter, 1, tr, op1, oc1, u));
     }
-    // fold by r1: arr_{t+1} into its own slot of p.arr, b into vb[1]
-    RUN(PC_SUMCHECK, 1,
-        sc_step_launch(p.va[0], p.vb[0], m / 2, &st->wr[iter][1], arr_next, p.vb[1], false, p.partial,
-                       sc_blocks(m / 8 ? m / 8 : 1), s));
     a = arr_next;
-    b = p.vb[1];
+    b = bd;
     m /= 4;
     arr_next += m;
     if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_fold[iter], s));
@@ -885,9 +883,9 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     static_assert(kWhirK == 4, "update_betas: exponent scale 2 assumes folding by 4 with NL = L / 2");
     if (update_betas_by_transform(l, m, NL / 2)) {
       RUN(PC_UPDATE_BETAS, 2,
-          ntt_sparse_accumulate(p.tables(ilog2(NL) - 1), st->q, st->comb, l, p.vb[1], m, p.tmp2, s, 1));
+          ntt_sparse_accumulate(p.tables(ilog2(NL) - 1), st->q, st->comb, l, bd, m, p.tmp2, s, 1));
     } else {
-      RUN(PC_UPDATE_BETAS, 2, update_betas_launch(p.vb[1], m, st, l, p.ub_scratch, s));
+      RUN(PC_UPDATE_BETAS, 2, update_betas_launch(bd, m, st, l, p.ub_scratch, s));
     }
     cwi = nci;
     L = NL;
@@ -899,7 +897,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   uint64_t off_point = lay.rec(T_FINAL_POINT, ilog2(m), 16);
   uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
   RUN(PC_PROTOCOL, 1,
-      k_final<<<1, 32, 0, s>>>(st, a, p.vb[1], (int)m, tr, off_poly, off_point, off_eval, 0, st->fin_r));
+      k_final<<<1, 32, 0, s>>>(st, a, b, (int)m, tr, off_poly, off_point, off_eval, 0, st->fin_r));
   // root of the last commitment (never opened) on the query stream
   if (!dry) GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_commit[iter], 0));
   RUN_ON(q, PC_MERKLE, 1, k_merkle_root<<<1, 32, 0, q>>>(p.cw[cwi], ilog2(L / 4), tr, off_root[iter]));

@@ -71,6 +71,7 @@ struct ProofPlan {
   fe *vb[2] = {nullptr, nullptr}; // folded second vector ping-pong
   fe *beta = nullptr;             // eq table (n)
   fe *partial = nullptr;          // per-CTA round-message partials
+  fe *partial2 = nullptr;         // the second round's, when two rounds share a pass
   fe *ub_scratch = nullptr;       // update_betas power tables
   ProofState *st = nullptr;
   uint8_t *transcript = nullptr;

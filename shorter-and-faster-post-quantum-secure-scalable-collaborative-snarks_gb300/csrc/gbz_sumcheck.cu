@@ -108,6 +108,45 @@ sc_fold_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t m, c
   }
 }
 
+// Two WHIR sumcheck rounds in one pass (Whir.cpp:215-231 twice): the
+// challenges r0, r1 are drawn before the round messages exist (F::_random),
+// so a thread takes four consecutive entries of both vectors, adds the two
+// pairs to the first round's message, folds them by r0, adds the folded pair
+// to the second round's message and folds it by r1 into (a4, b4) of length
+// m/4.  One read of (a, b) instead of three passes.
+__global__ void __launch_bounds__(kScThreads)
+sc_fold2_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t m, const fe *chal0, const fe *chal1,
+                fe *__restrict__ a4, fe *__restrict__ b4, fe *partial0, fe *partial1) {
+  const fe r0 = *chal0, r1 = *chal1;
+  fe A0 = fe_zero(), C0 = fe_zero(), D0 = fe_zero(), A1 = fe_zero(), C1 = fe_zero(), D1 = fe_zero();
+  const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
+  const uint64_t quads = m / 4;
+  for (uint64_t t = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; t < quads; t += stride) {
+    const fe x0 = a[4 * t], x1 = a[4 * t + 1], x2 = a[4 * t + 2], x3 = a[4 * t + 3];
+    const fe y0 = b[4 * t], y1 = b[4 * t + 1], y2 = b[4 * t + 2], y3 = b[4 * t + 3];
+    acc_pair(x0, x1, y0, y1, A0, C0, D0);
+    acc_pair(x2, x3, y2, y3, A0, C0, D0);
+    const fe fa0 = fadd(fmul(r0, fsub(x1, x0)), x0), fa1 = fadd(fmul(r0, fsub(x3, x2)), x2);
+    const fe fb0 = fadd(fmul(r0, fsub(y1, y0)), y0), fb1 = fadd(fmul(r0, fsub(y3, y2)), y2);
+    acc_pair(fa0, fa1, fb0, fb1, A1, C1, D1);
+    a4[t] = fadd(fmul(r1, fsub(fa1, fa0)), fa0);
+    b4[t] = fadd(fmul(r1, fsub(fb1, fb0)), fb0);
+  }
+  block_sum3(A0, C0, D0);
+  if (threadIdx.x == 0) {
+    partial0[3 * blockIdx.x] = A0;
+    partial0[3 * blockIdx.x + 1] = C0;
+    partial0[3 * blockIdx.x + 2] = D0;
+  }
+  __syncthreads();  // block_sum3's shared scratch is reused
+  block_sum3(A1, C1, D1);
+  if (threadIdx.x == 0) {
+    partial1[3 * blockIdx.x] = A1;
+    partial1[3 * blockIdx.x + 1] = C1;
+    partial1[3 * blockIdx.x + 2] = D1;
+  }
+}
+
 // Sumcheck of sum_x w(x) eq(z, x) without folding the eq vector.  After i
 // rounds the folded eq vector is epre * eq1(z_i, x_0) * E_i[x'], E_i the eq
 // table of z_{i+1..} (eq1(z, x) = z x + (1 - z)(1 - x)), so the round
@@ -342,6 +381,13 @@ void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2
   } else {
     sc_fold_kernel<<<blocks, kScThreads, 0, s>>>(a, b, m, chal, a2, b2, reduce ? 1 : 0, partial);
   }
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void sc_fold2_launch(const fe *a, const fe *b, uint64_t m, const fe *chal0, const fe *chal1, fe *a4, fe *b4,
+                     fe *partial0, fe *partial1, int blocks, cudaStream_t s) {
+  if (m < 4) throw ArgError("two-round fold needs at least 4 entries");
+  sc_fold2_kernel<<<blocks, kScThreads, 0, s>>>(a, b, m, chal0, chal1, a4, b4, partial0, partial1);
   GBZ_CUDA(cudaGetLastError());
 }
 
