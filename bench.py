@@ -69,17 +69,20 @@ CONFIG = {
 def algorithmic_bytes(logn, rate):
     n, L = 1 << logn, (1 << logn) * rate
     out = {}
-    # sumcheck: every round reads 2 vectors of length m and writes 2 of m/2;
-    # main sumcheck + WHIR sumcheck rounds over halving lengths (~96 n bytes each)
-    sc = 0
+    # main sumcheck (eq-factored): round 0 reads w and the eq table E_0
+    # (n/2 entries); every fold at length m reads w_i and E_i (m/2) and
+    # writes w_{i+1} (m/2) and E_{i+1} (m/4): 36 m bytes
+    sc = 16 * n + 8 * n
     m = n
-    sc += 2 * 16 * m  # round 0 reads w and beta
     while m > 1:
-        sc += 2 * 16 * m + 2 * 16 * (m // 2)
+        sc += 36 * m
         m //= 2
+    # WHIR: both rounds of an iteration in one pass, reading arr and b and
+    # writing the quarter-length pair (40 m bytes); the first iteration reads
+    # the eq table of chal[2..] (m/4 entries) instead of b (28 m bytes)
     m, wsc = n, 0
     while m > 4:
-        wsc += 2 * 16 * m + (2 * 16 * m + 2 * 16 * (m // 2)) + (2 * 16 * (m // 2) + 2 * 16 * (m // 4))
+        wsc += (16 * m + 4 * m + 8 * m) if m == n else 40 * m
         m //= 4
     out["sumcheck"] = sc + wsc
     # NTT: read valid input + write codeword, per commit.  (The prover's
@@ -93,7 +96,7 @@ def algorithmic_bytes(logn, rate):
         ntt += 16 * m + 16 * NL
         cur *= 2
     out["ntt"] = ntt
-    out["beta"] = 2 * 16 * n
+    out["beta"] = 16 * (n // 2) + 16 * (n // 4)  # E_0 of z_1.. and E_2 of chal[2..], written once
     m, cur, ub = n, rate, 0
     while m > 4:
         m //= 4

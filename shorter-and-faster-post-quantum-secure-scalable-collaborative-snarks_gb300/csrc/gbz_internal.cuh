@@ -195,6 +195,10 @@ void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2
 // m/4, the fold by *chal0 then *chal1.  m >= 4.
 void sc_fold2_launch(const fe *a, const fe *b, uint64_t m, const fe *chal0, const fe *chal1, fe *a4, fe *b4,
                      fe *partial0, fe *partial1, int blocks, cudaStream_t s);
+// The same with b = precompute_beta(c) given by E2, the eq table of c[2..]
+// (m/4 entries): b is not read, b4 = eq1(c0, r0) eq1(c1, r1) E2.
+void sc_fold2_eq_launch(const fe *a, const fe *E2, uint64_t m, const fe *c, const fe *chal0, const fe *chal1, fe *a4,
+                        fe *b4, fe *partial0, fe *partial1, int blocks, cudaStream_t s);
 // The same steps for the sumcheck of sum_x w(x) eq(z, x) with the eq vector
 // kept as the shrinking table E_i of z_{i+1..}: chal == nullptr gives the
 // sums S(0), S(1) of (a, E); otherwise a is folded by *chal into a2 (m/2),

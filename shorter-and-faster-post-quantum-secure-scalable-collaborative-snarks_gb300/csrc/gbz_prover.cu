@@ -784,7 +784,10 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   //    once each (p.arr), so the commits read them while s moves on; a
   //    commit reuses a codeword/tree buffer only after the query that
   //    opened its previous content.
-  RUN(PC_BETA, 1, beta_launch(st->chal, logn, p.beta, s));
+  // b = precompute_beta(chal) has tensor structure: for the first
+  // iteration only the eq table E2 of chal[2..] is formed (a quarter of b)
+  const bool eq_first = logn >= 4;
+  RUN(PC_BETA, 1, eq_first ? beta_launch(st->chal + 2, logn - 2, p.beta, s) : beta_launch(st->chal, logn, p.beta, s));
   if (!dry) GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_sched, 0));  // round challenges
   a = w;
   const fe *b = p.beta;
@@ -803,9 +806,15 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     const uint64_t op1 = lay.rec(T_WHIR_POLY, 3, 16), oc1 = lay.rec(T_WHIR_CHALLENGE, 1, 16);
     fe *bd = p.vb[(iter + 1) & 1];
     const int blocks = sc_blocks(m / 4);
-    RUN(PC_SUMCHECK, 1,
-        sc_fold2_launch(a, b, m, &st->wr[iter][0], &st->wr[iter][1], arr_next, bd, p.partial, p.partial2, blocks,
-                        s));
+    if (iter == 0 && eq_first) {
+      RUN(PC_SUMCHECK, 1,
+          sc_fold2_eq_launch(a, b, m, st->chal, &st->wr[iter][0], &st->wr[iter][1], arr_next, bd, p.partial,
+                             p.partial2, blocks, s));
+    } else {
+      RUN(PC_SUMCHECK, 1,
+          sc_fold2_launch(a, b, m, &st->wr[iter][0], &st->wr[iter][1], arr_next, bd, p.partial, p.partial2, blocks,
+                          s));
+    }
     RUN(PC_PROTOCOL, 1, k_whir_round_s<<<1, 256, 0, s>>>(p.partial, blocks, st, iter, 0, tr, op, oc, UbPrep{}));
     {
       // the second round kernel also prepares this iteration's beta update

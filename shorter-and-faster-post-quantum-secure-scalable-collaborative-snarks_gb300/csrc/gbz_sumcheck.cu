@@ -147,6 +147,53 @@ sc_fold2_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t m, 
   }
 }
 
+// The same two rounds for the first WHIR iteration, whose b is the eq
+// vector of the sumcheck challenges c (precompute_beta, utils.cpp:198-243):
+// b[4t + 2 x1 + x0] = eq1(c0, x0) eq1(c1, x1) E2[t] with E2 the eq table of
+// c2.. (m/4 entries), so b is never read.  Per pair the messages need only
+// S0 = sum a0 g and S1 = sum a1 g (g the pair's factor without eq1(c0, .)):
+// A = (e1 - e0)(S1 - S0), C = e0 S0, D = e1 S1 (e_x = eq1(c0, x)), and after
+// the fold by r0 the pair's b is lambda0 eq1(c1, x1) E2[t], lambda0 =
+// eq1(c0, r0); b4 = lambda0 lambda1 E2 (lambda1 = eq1(c1, r1)).
+__global__ void __launch_bounds__(kScThreads)
+sc_fold2_eq_kernel(const fe *__restrict__ a, const fe *__restrict__ E2, uint64_t m, const fe *c, const fe *chal0,
+                   const fe *chal1, fe *__restrict__ a4, fe *__restrict__ b4, fe *partial0, fe *partial1) {
+  const fe r0 = *chal0, r1 = *chal1, c0 = c[0], c1 = c[1];
+  const fe e0 = fsub(fe_one(), c0), f0 = fsub(fe_one(), c1);
+  const fe lam0 = fadd(fmul(r0, fsub(c0, e0)), e0), lam1 = fadd(fmul(r1, fsub(c1, f0)), f0);
+  const fe lam = fmul(lam0, lam1);
+  fe S0 = fe_zero(), S1 = fe_zero(), T0 = fe_zero(), T1 = fe_zero();
+  const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
+  const uint64_t quads = m / 4;
+  for (uint64_t t = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; t < quads; t += stride) {
+    const fe x0 = a[4 * t], x1 = a[4 * t + 1], x2 = a[4 * t + 2], x3 = a[4 * t + 3];
+    const fe E = E2[t];
+    const fe g0 = fmul(f0, E), g1 = fmul(c1, E);
+    S0 = fadd(S0, fadd(fmul(x0, g0), fmul(x2, g1)));
+    S1 = fadd(S1, fadd(fmul(x1, g0), fmul(x3, g1)));
+    const fe fa0 = fadd(fmul(r0, fsub(x1, x0)), x0), fa1 = fadd(fmul(r0, fsub(x3, x2)), x2);
+    T0 = fadd(T0, fmul(fa0, E));
+    T1 = fadd(T1, fmul(fa1, E));
+    a4[t] = fadd(fmul(r1, fsub(fa1, fa0)), fa0);
+    b4[t] = fmul(lam, E);
+  }
+  fe Z = fe_zero();
+  block_sum3(S0, S1, Z);
+  if (threadIdx.x == 0) {
+    partial0[3 * blockIdx.x] = fmul(fsub(c0, e0), fsub(S1, S0));
+    partial0[3 * blockIdx.x + 1] = fmul(e0, S0);
+    partial0[3 * blockIdx.x + 2] = fmul(c0, S1);
+  }
+  __syncthreads();  // block_sum3's shared scratch is reused
+  Z = fe_zero();
+  block_sum3(T0, T1, Z);
+  if (threadIdx.x == 0) {
+    partial1[3 * blockIdx.x] = fmul(lam0, fmul(fsub(c1, f0), fsub(T1, T0)));
+    partial1[3 * blockIdx.x + 1] = fmul(lam0, fmul(f0, T0));
+    partial1[3 * blockIdx.x + 2] = fmul(lam0, fmul(c1, T1));
+  }
+}
+
 // Sumcheck of sum_x w(x) eq(z, x) without folding the eq vector.  After i
 // rounds the folded eq vector is epre * eq1(z_i, x_0) * E_i[x'], E_i the eq
 // table of z_{i+1..} (eq1(z, x) = z x + (1 - z)(1 - x)), so the round
@@ -388,6 +435,13 @@ void sc_fold2_launch(const fe *a, const fe *b, uint64_t m, const fe *chal0, cons
                      fe *partial0, fe *partial1, int blocks, cudaStream_t s) {
   if (m < 4) throw ArgError("two-round fold needs at least 4 entries");
   sc_fold2_kernel<<<blocks, kScThreads, 0, s>>>(a, b, m, chal0, chal1, a4, b4, partial0, partial1);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void sc_fold2_eq_launch(const fe *a, const fe *E2, uint64_t m, const fe *c, const fe *chal0, const fe *chal1, fe *a4,
+                        fe *b4, fe *partial0, fe *partial1, int blocks, cudaStream_t s) {
+  if (m < 4) throw ArgError("two-round fold needs at least 4 entries");
+  sc_fold2_eq_kernel<<<blocks, kScThreads, 0, s>>>(a, E2, m, c, chal0, chal1, a4, b4, partial0, partial1);
   GBZ_CUDA(cudaGetLastError());
 }
 
