@@ -120,7 +120,10 @@ def commit_lengths(logn, rate):
 
 def algorithmic_int_work(logn, rate):
     """Integer-pipe work per proof: radix-2 butterfly count (L/2 log2 L) of
-    the commitment transforms, and the Blake3 compressions of the Merkle
+    the commitment transforms (the witness commitment is a base-field
+    transform, done as a half-length transform of packed pairs plus one
+    multiply per output pair: M/2 log2 M + M for M = L/2), and the Blake3
+    compressions of the Merkle
     nodes the proof reveals (inner nodes hash their left child twice, so the
     root is a chain of depth + 1 compressions from leaf 0 and path entry d a
     chain of d + 1 from one leaf): root chains plus l depth (depth + 1) / 2
@@ -133,7 +136,9 @@ def algorithmic_int_work(logn, rate):
         if k + 1 < len(ls):  # every codeword but the last is opened
             l = int(-100 / np.log2(np.sqrt(1.0 / (rate << k))))
             comps += l * depth * (depth + 1) // 2
-    return {"ntt": sum(L // 2 * (L.bit_length() - 1) for L in ls), "merkle_chain": comps}
+    M = ls[0] // 2
+    ntt = M // 2 * (M.bit_length() - 1) + M + sum(L // 2 * (L.bit_length() - 1) for L in ls[1:])
+    return {"ntt": ntt, "merkle_chain": comps}
 
 
 class ClockSampler:

@@ -60,6 +60,7 @@ struct ProofState {
   fe omega_q[kMaxQueries];    // omega_N^{q_i}
   uint32_t error;             // non-zero: a device-side consistency check failed
   uint32_t seed_in;           // PRNG seed of the next proof when it is replayed from a graph
+  uint32_t nonreal;           // the witness has an imaginary word (general commit transform)
   fe epre;                    // prod_{k < i} eq1(z_k, chal_k): the folded eq prefix of the sumcheck
   // The prover's WHIR randomness, drawn up front (it depends on the seed
   // only): per iteration the two round challenges, the query positions and
@@ -121,6 +122,17 @@ struct NttTables {
 // `tmp` must hold 2^logn elements when logn > 13.  in may equal out.
 void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                 cudaStream_t s);
+// The forward transform (length N = 2^t_full.logn) of an input whose
+// entries are expected in the base field: pairs of them are packed into one
+// extension element, transformed at length N/2 (t_half) and unpacked by the
+// conjugate symmetry of a base-field input's spectrum.  The packed pass sets
+// *nonreal (device, to be zeroed by the caller) when an imaginary word is
+// non-zero, and then the general transform, which otherwise exits at once,
+// overwrites out: the result is the plain transform for every input.  tmp
+// holds N entries; n_valid is even.
+void ntt_launch_real(const NttTables &t_half, const NttTables &t_full, const fe *in, uint64_t n_valid, fe *out,
+                     fe *tmp, uint32_t *nonreal, cudaStream_t s);
+int ntt_launch_real_count(int logn);
 // `rows` transforms of the same length in the same launches: row r reads
 // in + r in_stride (n_valid entries, zero beyond) and writes out + r
 // out_stride; tmp holds rows * 2^logn elements when logn > 13.

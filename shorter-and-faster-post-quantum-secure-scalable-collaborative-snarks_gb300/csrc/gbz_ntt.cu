@@ -78,6 +78,13 @@ struct PassArgs {
   // Independent transforms side by side: grid row y works on in + y row_in
   // and out + y row_out (0 for one transform).
   uint64_t row_in, row_out;
+  // Packed real input: input entry j is (in[2j].re, in[2j+1].re) (two
+  // base-field values as one extension element); a non-zero imaginary word
+  // among them sets *nonreal.
+  int pack_real;
+  uint32_t *nonreal;
+  // When set, the pass does nothing unless *run_if is non-zero.
+  const uint32_t *run_if;
 };
 
 // Shared-memory swizzle: element a lives at a ^ ((a >> 3) & 7), which keeps
@@ -322,13 +329,14 @@ __device__ __forceinline__ void stockham_dispatch(fe *sm, const fe *T, int logS,
 // no shared-memory round trip.  Contiguous sub-transforms give consecutive
 // threads consecutive j; strided ones (columns of the first four-step pass)
 // consecutive sub-transforms b, whose columns are adjacent in memory.
-template <bool INV, int LOGS>
+template <bool INV, int LOGS, bool PACK>
 __device__ __forceinline__ void staged_first_stage(fe *sm, const PassArgs &a, uint64_t g0, int logB, int logE) {
   constexpr int LOGR = LOGS % 3 == 1 ? 1 : (LOGS % 3 == 2 ? 2 : 3);
   constexpr int R = 1 << LOGR, PER = kPerThread / R, logSR = LOGS - LOGR;
   const uint32_t nb = 1u << (logE - LOGR);
   const bool contiguous = a.in_jstride == 1;
   fe v[PER][R];
+  uint64_t nonreal = 0;
 #pragma unroll
   for (int i = 0; i < PER; i++) {  // all loads first: PER * R = 8 in flight
     const uint32_t u = threadIdx.x + i * blockDim.x;
@@ -339,9 +347,17 @@ __device__ __forceinline__ void staged_first_stage(fe *sm, const PassArgs &a, ui
     for (int r = 0; r < R; r++) {
       const uint32_t jj = j + ((uint32_t)r << logSR);
       const uint64_t addr = row + (uint64_t)jj * a.in_jstride;
-      v[i][r] = (u < nb && addr < a.n_valid && jj < a.j_valid) ? a.in[addr] : fe_zero();
+      const bool ok = u < nb && addr < a.n_valid && jj < a.j_valid;
+      if (!PACK) {
+        v[i][r] = ok ? a.in[addr] : fe_zero();
+      } else {
+        const fe e0 = ok ? a.in[2 * addr] : fe_zero(), e1 = ok ? a.in[2 * addr + 1] : fe_zero();
+        nonreal |= e0.im | e1.im;
+        v[i][r] = fe_make(e0.re, e1.re);
+      }
     }
   }
+  if (PACK && nonreal) atomicOr(a.nonreal, 1u);
 #pragma unroll
   for (int i = 0; i < PER; i++) {
     const uint32_t u = threadIdx.x + i * blockDim.x;
@@ -358,37 +374,41 @@ __device__ __forceinline__ void staged_first_stage(fe *sm, const PassArgs &a, ui
   }
 }
 
-template <bool INV, int LOGS>
+template <bool INV, int LOGS, bool PACK>
 __device__ __forceinline__ void staged_transform(fe *sm, const fe *T, const PassArgs &a, uint64_t g0, int logB,
                                                  int logE) {
   constexpr int LOGR = LOGS % 3 == 1 ? 1 : (LOGS % 3 == 2 ? 2 : 3);
-  staged_first_stage<INV, LOGS>(sm, a, g0, logB, logE);
+  staged_first_stage<INV, LOGS, PACK>(sm, a, g0, logB, logE);
   __syncthreads();
   stockham_radix8<INV, LOGS, LOGR>(sm, T, logE);
 }
 
-template <bool INV>
+template <bool INV, bool PACK>
 __device__ __forceinline__ void staged_dispatch(fe *sm, const fe *T, const PassArgs &a, uint64_t g0, int logS,
                                                 int logB, int logE) {
   switch (logS) {
-    case 1: staged_transform<INV, 1>(sm, T, a, g0, logB, logE); break;
-    case 2: staged_transform<INV, 2>(sm, T, a, g0, logB, logE); break;
-    case 3: staged_transform<INV, 3>(sm, T, a, g0, logB, logE); break;
-    case 4: staged_transform<INV, 4>(sm, T, a, g0, logB, logE); break;
-    case 5: staged_transform<INV, 5>(sm, T, a, g0, logB, logE); break;
-    case 6: staged_transform<INV, 6>(sm, T, a, g0, logB, logE); break;
-    case 7: staged_transform<INV, 7>(sm, T, a, g0, logB, logE); break;
-    case 8: staged_transform<INV, 8>(sm, T, a, g0, logB, logE); break;
-    case 9: staged_transform<INV, 9>(sm, T, a, g0, logB, logE); break;
-    case 10: staged_transform<INV, 10>(sm, T, a, g0, logB, logE); break;
-    case 11: staged_transform<INV, 11>(sm, T, a, g0, logB, logE); break;
-    case 12: staged_transform<INV, 12>(sm, T, a, g0, logB, logE); break;
-    case 13: staged_transform<INV, 13>(sm, T, a, g0, logB, logE); break;
+    case 1: staged_transform<INV, 1, PACK>(sm, T, a, g0, logB, logE); break;
+    case 2: staged_transform<INV, 2, PACK>(sm, T, a, g0, logB, logE); break;
+    case 3: staged_transform<INV, 3, PACK>(sm, T, a, g0, logB, logE); break;
+    case 4: staged_transform<INV, 4, PACK>(sm, T, a, g0, logB, logE); break;
+    case 5: staged_transform<INV, 5, PACK>(sm, T, a, g0, logB, logE); break;
+    case 6: staged_transform<INV, 6, PACK>(sm, T, a, g0, logB, logE); break;
+    case 7: staged_transform<INV, 7, PACK>(sm, T, a, g0, logB, logE); break;
+    case 8: staged_transform<INV, 8, PACK>(sm, T, a, g0, logB, logE); break;
+    case 9: staged_transform<INV, 9, PACK>(sm, T, a, g0, logB, logE); break;
+    case 10: staged_transform<INV, 10, PACK>(sm, T, a, g0, logB, logE); break;
+    case 11: staged_transform<INV, 11, PACK>(sm, T, a, g0, logB, logE); break;
+    case 12: staged_transform<INV, 12, PACK>(sm, T, a, g0, logB, logE); break;
+    case 13: staged_transform<INV, 13, PACK>(sm, T, a, g0, logB, logE); break;
     default: break;
   }
 }
 
+// PACK: the first pass of a packed real transform (a separate instantiation,
+// so that the general kernel keeps its register allocation).
+template <bool PACK>
 __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
+  if (a.run_if && *a.run_if == 0) return;  // uniform over the grid
   extern __shared__ fe smem[];
   a.in += blockIdx.y * a.row_in;
   a.out += blockIdx.y * a.row_out;
@@ -429,8 +449,8 @@ __global__ void __launch_bounds__(kMaxThreads) ntt_pass_kernel(PassArgs a) {
     if (a.inverse) stockham_dispatch<true>(sm, T, logS, logE);
     else stockham_dispatch<false>(sm, T, logS, logE);
   } else if (logS >= 1) {
-    if (a.inverse) staged_dispatch<true>(sm, T, a, g0, logS, logB, logE);
-    else staged_dispatch<false>(sm, T, a, g0, logS, logB, logE);
+    if (a.inverse) staged_dispatch<true, PACK>(sm, T, a, g0, logS, logB, logE);
+    else staged_dispatch<false, PACK>(sm, T, a, g0, logS, logB, logE);
   } else {
     // Sub-transforms of length 1: staging only.
     // A thread stages at most kPerThread elements (blockDim >= total / 8);
@@ -545,7 +565,8 @@ void ensure_wq() {
     GBZ_CUDA(cudaMemcpy(g_wq[dir], h.data(), sizeof(fe) * n, cudaMemcpyHostToDevice));
   }
   g_wq_device = dev;
-  GBZ_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+  GBZ_CUDA(cudaFuncSetAttribute(ntt_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+  GBZ_CUDA(cudaFuncSetAttribute(ntt_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
 }
 
 // Column chains of a sparse input: next[t] = the next entry with the same
@@ -575,7 +596,8 @@ void launch_pass(const PassArgs &a, uint64_t groups, cudaStream_t s, int rows = 
   const size_t smem = sizeof(fe) * (E + (a.logS >= 1 ? (1u << (a.logS - 1)) : 0));
   const unsigned threads = E / kPerThread > 32 ? E / kPerThread : 32;
   if (rows < 1 || rows > 65535) throw ArgError("transform: 1..65535 rows per launch");
-  ntt_pass_kernel<<<dim3((unsigned)blocks, (unsigned)rows), threads, smem, s>>>(a);
+  if (a.pack_real) ntt_pass_kernel<true><<<dim3((unsigned)blocks, (unsigned)rows), threads, smem, s>>>(a);
+  else ntt_pass_kernel<false><<<dim3((unsigned)blocks, (unsigned)rows), threads, smem, s>>>(a);
   GBZ_CUDA(cudaGetLastError());
 }
 
@@ -747,13 +769,26 @@ void ntt_tables_free(NttTables &t) {
 namespace {
 
 // Shared by the dense transform and the sparse/accumulating variant.
+// Options of a transform: packed real input (the pass that reads `in`) and
+// a device flag that gates every pass.
+struct PassGate {
+  int pack_real = 0;
+  uint32_t *nonreal = nullptr;
+  const uint32_t *run_if = nullptr;
+};
+
 void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
-                  cudaStream_t s, int rows = 1, uint64_t row_in = 0, uint64_t row_out = 0) {
+                  cudaStream_t s, int rows = 1, uint64_t row_in = 0, uint64_t row_out = 0,
+                  const PassGate &gate = PassGate()) {
   const int logn = t.logn;
   const uint64_t L = 1ull << logn;
   if (logn > kMaxNttLogN) throw ArgError("transform longer than 2^26 (two passes of at most 2^13)");
+  if (gate.pack_real && (logn < 1 || rows != 1)) throw ArgError("packed real transform: one row, length >= 2");
   if (n_valid > L) n_valid = L;
   PassArgs a{};
+  a.pack_real = gate.pack_real;
+  a.nonreal = gate.nonreal;
+  a.run_if = gate.run_if;
   a.row_in = row_in;
   a.row_out = row_out;
   a.wh = inverse ? t.sub_inv : t.sub_fwd;
@@ -801,6 +836,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   launch_pass(a, N1, s, rows);
   // pass B: rows k2 < N2, length N1, contiguous
   PassArgs b = a;
+  b.pack_real = 0;  // only the first pass reads the input
   b.in = tmp;
   b.out = out;
   b.n_valid = L;
@@ -825,6 +861,59 @@ void ntt_launch(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe 
                 cudaStream_t s) {
   ntt_two_pass(t, in, n_valid, out, tmp, inverse, s);
 }
+
+namespace {
+// x / 2 mod p for canonical x: 2 is invertible and x + p is even when x is odd.
+__device__ __forceinline__ uint64_t half_p(uint64_t x) { return (x + ((x & 1) ? P : 0)) >> 1; }
+__device__ __forceinline__ fe conj_fe(fe x) { return fe_make(x.re, x.im ? P - x.im : 0); }
+
+// Real-input transform, last step.  Z = DFT_M(z), z_j = x_2j + i x_2j+1
+// (M = N/2, omega_M = omega_N^2).  In F_{p^2} conjugation is the Frobenius
+// x -> x^p and p = -1 mod N, so conj(omega_N) = omega_N^{-1}; for base-field
+// x this gives E[k] = (Z[k] + conj Z[M-k]) / 2 = DFT_M(x_even)[k] and
+// O[k] = (Z[k] - conj Z[M-k]) / 2i = DFT_M(x_odd)[k], then X[k] = E + w^k O,
+// X[k+M] = E - w^k O (w = omega_N), and X[N-k] = conj X[k].  Thread t takes
+// k = t and M - t (t = 0 and t = M/2 alone): 2 reads, 4 writes, 2 multiplies.
+__global__ void real_unpack_kernel(const fe *__restrict__ Z, uint64_t M, const fe *lo, const fe *hi,
+                                   fe *__restrict__ X) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > M / 2) return;
+  const fe a = Z[t], b = Z[t == 0 ? 0 : M - t];
+  const fe E = fe_make(half_p(addp(a.re, b.re)), half_p(subp(a.im, b.im)));
+  const fe O = fe_make(half_p(addp(a.im, b.im)), half_p(subp(b.re, a.re)));
+  const fe w = fmul(lo[t & ((1u << kTwLoBits) - 1)], hi[t >> kTwLoBits]);
+  const fe wo = fmul(w, O);
+  const fe xk = fadd(E, wo), xkm = fsub(E, wo);
+  X[t] = xk;
+  X[t + M] = xkm;
+  if (t != 0 && t != M / 2) {
+    X[M - t] = conj_fe(xkm);
+    X[2 * M - t] = conj_fe(xk);
+  }
+}
+}  // namespace
+
+void ntt_launch_real(const NttTables &t_half, const NttTables &t_full, const fe *in, uint64_t n_valid, fe *out,
+                     fe *tmp, uint32_t *nonreal, cudaStream_t s) {
+  const int logn = t_full.logn;
+  if (t_half.logn != logn - 1 || logn < 2) throw ArgError("real transform: tables of lengths N/2 and N, N >= 4");
+  if (n_valid & 1) throw ArgError("real transform: even number of input entries");
+  const uint64_t N = 1ull << logn, M = N / 2;
+  fe *Z = tmp + M;  // tmp holds N entries: the half-length intermediate, then Z
+  PassGate g;
+  g.pack_real = 1;
+  g.nonreal = nonreal;
+  ntt_two_pass(t_half, in, n_valid / 2, Z, tmp, false, s, 1, 0, 0, g);
+  const uint64_t threads = M / 2 + 1;
+  real_unpack_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(Z, M, t_full.lo_fwd, t_full.hi_fwd, out);
+  GBZ_CUDA(cudaGetLastError());
+  // any imaginary word: the general transform replaces the result
+  PassGate f;
+  f.run_if = nonreal;
+  ntt_two_pass(t_full, in, n_valid, out, tmp, false, s, 1, 0, 0, f);
+}
+
+int ntt_launch_real_count(int logn) { return ntt_launch_count(logn - 1) + 1 + ntt_launch_count(logn); }
 
 void ntt_launch_rows(const NttTables &t, const fe *in, uint64_t n_valid, uint64_t in_stride, fe *out,
                      uint64_t out_stride, int rows, fe *tmp, bool inverse, cudaStream_t s) {

@@ -711,7 +711,12 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   uint64_t L = p.L;
   int cwi = 0;
   uint64_t off = lay.rec(T_COMMIT_ROOT, 1, 32);
-  RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(L)), ntt_launch(p.tables(ilog2(L)), w, p.n, p.cw[0], p.tmp, false, c));
+  // The witness is expected in the base field (the imaginary words zero):
+  // its transform is then a half-length transform of packed pairs
+  // (ntt_launch_real); any other witness takes the general transform.
+  if (!dry) GBZ_CUDA(cudaMemsetAsync(&st->nonreal, 0, sizeof(uint32_t), c));
+  RUN_ON(c, PC_NTT, ntt_launch_real_count(ilog2(L)),
+         ntt_launch_real(p.tables(ilog2(L) - 1), p.tables(ilog2(L)), w, p.n, p.cw[0], p.tmp, &st->nonreal, c));
   // The root (a chain of compressions from leaf 0) is computed on the query
   // stream once the codeword exists, off the chain of commits.
   uint64_t off_root[kMaxWhirIter + 1];

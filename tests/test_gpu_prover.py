@@ -155,3 +155,30 @@ def test_prove_rejects_out_of_range_shapes(ctx, gbz, oracle):
         with pytest.raises(gbz.GbzError) as e:
             ctx.prove(np.zeros((1 << min(logn, 8), 2), np.uint64), logn, rate, 1)
         assert e.value.status in (gbz.EINVAL, gbz.ESMALL)
+
+
+def _extension_witness(seed, n):
+    """Canonical F_{p^2} entries with non-zero imaginary words."""
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, (1 << 61) - 1, size=(n, 2), dtype=np.uint64)
+
+
+@pytest.mark.parametrize("logn,rate", [(3, 2), (5, 4), (8, 2), (11, 8), (13, 2), (14, 2), (16, 4)])
+def test_prove_extension_witness_vs_oracle(ctx, oracle, logn, rate):
+    """A witness outside the base field takes the general commit transform
+    (the packed real transform flags it) and still matches the oracle."""
+    w = _extension_witness(900 + logn, 1 << logn)
+    assert ctx.prove(w, logn, rate, 3).tobytes() == oracle.prove(w, logn, rate, 3)
+
+
+@pytest.mark.parametrize("pos", [0, 1, 4097, (1 << 14) - 1])
+def test_prove_single_imaginary_word_then_base_again(ctx, oracle, pos):
+    """One non-zero imaginary word anywhere is enough to switch the commit
+    to the general transform, and the flag is cleared for the next proof
+    replayed on the same buffers."""
+    logn, rate = 14, 2
+    base = oracle.witness(4242, 1 << logn)
+    one = base.copy()
+    one[pos, 1] = 12345
+    for w in (base, one, base):
+        assert ctx.prove(w, logn, rate, 1).tobytes() == oracle.prove(w, logn, rate, 1)
