@@ -457,10 +457,14 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
                                    gbz._ptr(polys), gbz._ptr(chal), gbz._ptr(fin), D)  # y = 0: ECHECK, timed all the same
     m, byts = N * M, 0
     byts += 3 * 16 * m
+    # cubic message of a pair: 3 + 6 products (linear x linear, then x linear);
+    # a fused round folds 4 entries of each vector (6) and adds one pair (9)
+    fm = 9 * (m // 2)
     while m >= 4:
         byts += 3 * 16 * m + 3 * 16 * (m // 2)
+        fm += 15 * (m // 4)
         m //= 2
-    rec("party_sumcheck_cubic_2^%d" % (24 - shift), timed(party), hbm_bytes=byts,
+    rec("party_sumcheck_cubic_2^%d" % (24 - shift), timed(party), hbm_bytes=byts, fmuls=fm,
         note="16 parties x 2^%d, 3 vectors" % (20 - shift))
     del v
     # coPCS Encode, 16 rows of 2^20 at rate 2
@@ -543,6 +547,7 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     n22 = 16 << la
     rec("whir_aggregate_claims_4x4_2^%d" % la, timed(aggc),
         hbm_bytes=4 * n22 + (4 + 4) * n22 + (4 + 1) * n22 + (4 + 1) * n22,
+        fmuls=(4 + 16 + 8) * (1 << la),  # eq tables, 4 x 4 inner products, two 4-term combinations
         note="4 eq tables written, 16 inner products (one pass over 8 vectors), 2 combinations")
     del arrs, msgs
     # pcs_sumcheck_phase3, 2^20 rows, 100 queries, 16 parties
