@@ -355,6 +355,20 @@ gbz_status gbz_fft(gbz_ctx *ctx, uint64_t *data, int logn, int inverse, int mem)
   API_END(ctx)
 }
 
+// Reed-Solomon encoding of m coefficients into L = m * rate evaluations.
+// Inputs in the base field take the half-length real-input transform; any
+// other input (flagged on the device) the general one, with the same bytes.
+static void rs_encode_launch(gbz_ctx *ctx, const fe *din, uint64_t m, uint64_t L, fe *dout, fe *tmp) {
+  const bool overlap = (const void *)din < (const void *)(dout + L) && (const void *)dout < (const void *)(din + m);
+  if (L < 4 || m < 2 || overlap) {
+    ntt_launch(ctx->tables(ilog2(L)), din, m, dout, tmp, false, ctx->stream);
+    return;
+  }
+  uint32_t *flag = (uint32_t *)ctx->buf(700, sizeof(uint32_t));
+  GBZ_CUDA(cudaMemsetAsync(flag, 0, sizeof(uint32_t), ctx->stream));
+  ntt_launch_real(ctx->tables(ilog2(L) - 1), ctx->tables(ilog2(L)), din, m, dout, tmp, flag, ctx->stream);
+}
+
 gbz_status gbz_rs_encode(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int rate, uint64_t *codeword, int mem) {
   API_BEGIN(ctx)
   check_mem(mem);
@@ -367,7 +381,7 @@ gbz_status gbz_rs_encode(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int rate
   const fe *din = dev_view(ctx, 0, (const fe *)arr, 16 * m, mem, true);
   fe *dout = dev_view(ctx, 1, (fe *)codeword, 16 * L, mem, false);
   fe *tmp = (fe *)ctx->buf(2, 16 * L);
-  ntt_launch(ctx->tables(ilog2(L)), din, m, dout, tmp, false, ctx->stream);
+  rs_encode_launch(ctx, din, m, L, dout, tmp);
   copy_out(ctx, (fe *)codeword, dout, 16 * L, mem);
   finish(ctx, mem);
   API_END(ctx)
@@ -421,7 +435,7 @@ gbz_status gbz_whir_commit(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int ra
   fe *dcw = dev_view(ctx, 1, (fe *)codeword, 16 * L, mem, false);
   uint8_t *dlv = dev_view(ctx, 2, levels, 32 * merkle_hashes(L), mem, false);
   fe *tmp = (fe *)ctx->buf(3, 16 * L);
-  ntt_launch(ctx->tables(ilog2(L)), din, m, dcw, tmp, false, ctx->stream);
+  rs_encode_launch(ctx, din, m, L, dcw, tmp);
   merkle_commit_launch(dcw, L, dlv, ctx->stream);
   copy_out(ctx, (fe *)codeword, dcw, 16 * L, mem);
   copy_out(ctx, levels, dlv, 32 * merkle_hashes(L), mem);

@@ -9,7 +9,7 @@ import struct
 import numpy as np
 import pytest
 
-from conftest import edge_fe, golden_bytes, rand_fe, splitmix_ext
+from conftest import splitmix_base, edge_fe, golden_bytes, rand_fe, splitmix_ext
 
 pytestmark = pytest.mark.gpu
 
@@ -95,6 +95,25 @@ def test_rs_encode_vs_oracle(ctx, oracle, logm, rate):
     padded = np.zeros(((1 << logm) * rate, 2), dtype=np.uint64)
     padded[: 1 << logm] = a
     assert np.array_equal(ctx.rs_encode(a, rate), oracle.fft(padded))
+
+
+@pytest.mark.parametrize("logm,rate", [(1, 2), (2, 2), (5, 4), (10, 2), (12, 4), (13, 2), (14, 8), (17, 2), (20, 2)])
+def test_rs_encode_base_field_vs_oracle(ctx, oracle, logm, rate):
+    """Base-field coefficients take the packed real-input transform."""
+    a = splitmix_base(15 + logm, 1 << logm)
+    padded = np.zeros(((1 << logm) * rate, 2), dtype=np.uint64)
+    padded[: 1 << logm] = a
+    assert np.array_equal(ctx.rs_encode(a, rate), oracle.fft(padded))
+
+
+def test_whir_commit_base_field(ctx, oracle):
+    a = splitmix_base(18, 1 << 12)
+    cw, flat = ctx.Whir_Commit_initial(a, 2)
+    padded = np.zeros((1 << 13, 2), dtype=np.uint64)
+    padded[: 1 << 12] = a
+    ocw = oracle.fft(padded)
+    assert np.array_equal(cw, ocw)
+    assert np.array_equal(flat, oracle.merkle_commit(ocw))
 
 
 @pytest.mark.parametrize("logN", [2, 3, 4, 5, 8, 11, 12, 13, 14, 15, 16])
