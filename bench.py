@@ -471,8 +471,11 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     R, lr = 16, 20 - shift
     rows_in, cw = rnd(R << lr), torch.empty(((R << lr) * 2, 2), dtype=torch.int64, device="cuda")
     enc = lambda: ctx.check(gbz.lib.gbz_encode_rows(ctx.h, rows_in.data_ptr(), R, lr, 2, 0, cw.data_ptr(), D))
-    bfly = R * ((1 << lr) // 2 * lr + (2 << lr) // 2 * (lr + 1))
-    rec("encode_rows_16x2^%d_rate2" % lr, timed(enc), fmuls=bfly, note="radix-2 butterflies of both transforms")
+    # rate 2, offset 0: the inverse transform and one length-n coset transform
+    # (the codeword's odd positions are the row itself), n coset multiplies
+    bfly = R * (2 * ((1 << lr) // 2 * lr) + (1 << lr))
+    rec("encode_rows_16x2^%d_rate2" % lr, timed(enc), fmuls=bfly,
+        note="radix-2 butterflies of the inverse and the half-length coset transform, plus the coset shift")
     # whole Blake3 Merkle tree (the drop-in MT_commit_Blake) over a 2^25 codeword
     lt = 25 - shift
     cwt = rnd(1 << lt)

@@ -661,9 +661,20 @@ gbz_status gbz_encode_rows(gbz_ctx *ctx, const uint64_t *rows, int nrows, int lo
   for (int r0 = 0; r0 < nrows; r0 += chunk) {
     const int rc = std::min(chunk, nrows - r0);
     fe *o = dout + L * (uint64_t)r0;
-    ntt_launch_rows(tn, drows + n * (uint64_t)r0, n, n, o, L, rc, tmp, true, ctx->stream);
+    const fe *x = drows + n * (uint64_t)r0;
+    ntt_launch_rows(tn, x, n, n, o, L, rc, tmp, true, ctx->stream);
     coset_launch(o, n, tw, ctx->stream, rc, L);
-    ntt_launch_rows(tL, o, n, L, o, L, rc, tmp, false, ctx->stream);
+    if (rate == 2 && log_rate_offset == 0 && n >= 2) {
+      // The codeword is the interpolant P of the row on <w_n> evaluated at
+      // w_2n^(m - 1): odd m give P(w_n^((m-1)/2)) = x[(m-1)/2], the row
+      // itself, and even m the length-n transform of the shifted
+      // coefficients (the same values as the zero-padded length-2n
+      // transform, at half its cost).
+      ntt_launch_rows(tn, o, n, L, o, L, rc, tmp, false, ctx->stream, 2);
+      strided_copy_launch(x, n, o, L, 2, 1, rc, ctx->stream);
+    } else {
+      ntt_launch_rows(tL, o, n, L, o, L, rc, tmp, false, ctx->stream);
+    }
   }
   copy_out(ctx, (fe *)out, dout, 16 * L * nrows, mem);
   finish(ctx, mem);

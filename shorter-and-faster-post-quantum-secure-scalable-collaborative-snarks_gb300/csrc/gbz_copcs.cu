@@ -290,6 +290,23 @@ void powers_launch(fe r, uint64_t n, fe *out, cudaStream_t s) {
   GBZ_CUDA(cudaGetLastError());
 }
 
+namespace {
+// out[r L + rate t + off] = x[r n + t]: a row's values at one residue of a
+// codeword's positions.
+__global__ void strided_copy_kernel(const fe *x, uint64_t n, fe *out, uint64_t L, int rate, int off) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  out[blockIdx.y * L + (uint64_t)rate * t + off] = x[blockIdx.y * n + t];
+}
+}  // namespace
+
+void strided_copy_launch(const fe *x, uint64_t n, fe *out, uint64_t L, int rate, int off, int rows, cudaStream_t s) {
+  if (rows < 1) return;
+  if (rows > 65535) throw ArgError("strided copy: at most 65535 rows per launch");
+  strided_copy_kernel<<<dim3(grid(n), (unsigned)rows), 256, 0, s>>>(x, n, out, L, rate, off);
+  GBZ_CUDA(cudaGetLastError());
+}
+
 void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s, int rows, uint64_t row_stride) {
   if (rows < 1) return;
   coset_kernel<<<dim3(grid(n), (unsigned)rows), 256, 0, s>>>(x, n, t.lo_inv, t.hi_inv, row_stride);

@@ -15,6 +15,8 @@ void powers_launch(fe r, uint64_t n, fe *out, cudaStream_t s);
 // x[j] *= omega_T^{-j} for j < n, T = 2^t.logn.
 // rows vectors of n entries, row_stride apart
 void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s, int rows = 1, uint64_t row_stride = 0);
+// out[r L + rate t + off] = x[r n + t] for t < n, r < rows.
+void strided_copy_launch(const fe *x, uint64_t n, fe *out, uint64_t L, int rate, int off, int rows, cudaStream_t s);
 // distributed_MT for one party (coPCS.cpp:152-202): levels (2L - 1 hashes,
 // column roots first) and the leader's root over 2^logN parties.
 void column_merkle_launch(const fe *rows, int nrows, uint64_t L, uint8_t *levels, int logN, uint8_t *root,

@@ -135,9 +135,11 @@ void ntt_launch_real(const NttTables &t_half, const NttTables &t_full, const fe 
 int ntt_launch_real_count(int logn);
 // `rows` transforms of the same length in the same launches: row r reads
 // in + r in_stride (n_valid entries, zero beyond) and writes out + r
-// out_stride; tmp holds rows * 2^logn elements when logn > 13.
+// out_stride, output k at out_elem_stride * k within the row; tmp holds
+// rows * 2^logn elements when logn > 13.
 void ntt_launch_rows(const NttTables &t, const fe *in, uint64_t n_valid, uint64_t in_stride, fe *out,
-                     uint64_t out_stride, int rows, fe *tmp, bool inverse, cudaStream_t s);
+                     uint64_t out_stride, int rows, fe *tmp, bool inverse, cudaStream_t s,
+                     uint64_t out_elem_stride = 1);
 // acc[j] += sum_i c[i] * omega_L^{q[i] j} for j < nacc (L = 2^t.logn > 2^13,
 // 1 <= l <= kMaxQueries): the forward transform of the sparse vector
 // sum_i c_i e_{q_i} as one second-pass launch whose rows are formed directly

@@ -779,7 +779,7 @@ struct PassGate {
 
 void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, fe *tmp, bool inverse,
                   cudaStream_t s, int rows = 1, uint64_t row_in = 0, uint64_t row_out = 0,
-                  const PassGate &gate = PassGate()) {
+                  const PassGate &gate = PassGate(), uint64_t out_elem_stride = 1) {
   const int logn = t.logn;
   const uint64_t L = 1ull << logn;
   if (logn > kMaxNttLogN) throw ArgError("transform longer than 2^26 (two passes of at most 2^13)");
@@ -802,7 +802,7 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
     a.in_gstride = L;
     a.in_jstride = 1;
     a.out_gstride = L;
-    a.out_kstride = 1;
+    a.out_kstride = out_elem_stride;
     a.logS = logn;
     a.logB = 0;
     a.has_scale = inverse;
@@ -842,8 +842,8 @@ void ntt_two_pass(const NttTables &t, const fe *in, uint64_t n_valid, fe *out, f
   b.n_valid = L;
   b.in_gstride = N1;
   b.in_jstride = 1;
-  b.out_gstride = 1;
-  b.out_kstride = N2;
+  b.out_gstride = out_elem_stride;
+  b.out_kstride = N2 * out_elem_stride;
   b.logS = k1;
   b.logB = sh.logBB;
   b.tw_lo = nullptr;
@@ -916,9 +916,10 @@ void ntt_launch_real(const NttTables &t_half, const NttTables &t_full, const fe 
 int ntt_launch_real_count(int logn) { return ntt_launch_count(logn - 1) + 1 + ntt_launch_count(logn); }
 
 void ntt_launch_rows(const NttTables &t, const fe *in, uint64_t n_valid, uint64_t in_stride, fe *out,
-                     uint64_t out_stride, int rows, fe *tmp, bool inverse, cudaStream_t s) {
+                     uint64_t out_stride, int rows, fe *tmp, bool inverse, cudaStream_t s, uint64_t out_elem_stride) {
   if (rows < 1) return;
-  ntt_two_pass(t, in, n_valid, out, tmp, inverse, s, rows, in_stride, out_stride);
+  if (out_elem_stride < 1) throw ArgError("transform: output element stride >= 1");
+  ntt_two_pass(t, in, n_valid, out, tmp, inverse, s, rows, in_stride, out_stride, PassGate(), out_elem_stride);
 }
 
 void ntt_batched(const NttTables &t, const fe *in, uint64_t in_stride, uint32_t j_valid, fe *out, uint64_t count,

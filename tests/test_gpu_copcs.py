@@ -81,7 +81,10 @@ def test_encode_golden(ctx, golden, name):
 
 
 @pytest.mark.parametrize("rows,logrow,rate,log_ro", [(1, 0, 2, 0), (2, 1, 4, 3), (3, 10, 2, 1), (2, 12, 8, 5),
-                                                     (1, 14, 2, 2), (1, 16, 4, 4)])
+                                                     (1, 14, 2, 2), (1, 16, 4, 4),
+                                                     # rate 2, offset 0: half-length transform + the row itself
+                                                     (1, 1, 2, 0), (3, 5, 2, 0), (2, 13, 2, 0), (2, 14, 2, 0),
+                                                     (16, 12, 2, 0), (1, 18, 2, 0)])
 def test_encode_vs_oracle(ctx, oracle, rows, logrow, rate, log_ro):
     rng = np.random.default_rng(300 + logrow)
     inp = np.stack([rand_fe(rng, 1 << logrow) for _ in range(rows)])
