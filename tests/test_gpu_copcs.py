@@ -8,7 +8,7 @@ Every call goes through the C ABI; results must be bit-identical.
 import numpy as np
 import pytest
 
-from conftest import rand_fe, splitmix_ext
+from conftest import splitmix_base, rand_fe, splitmix_ext
 from test_oracle_copcs import case
 
 pytestmark = pytest.mark.gpu
@@ -89,6 +89,25 @@ def test_encode_vs_oracle(ctx, oracle, rows, logrow, rate, log_ro):
     rng = np.random.default_rng(300 + logrow)
     inp = np.stack([rand_fe(rng, 1 << logrow) for _ in range(rows)])
     assert np.array_equal(ctx.Encode(inp, rate, log_ro), oracle.encode_rows(inp, rate, log_ro))
+
+
+@pytest.mark.parametrize("rows,logrow,rate,log_ro", [(1, 2, 2, 0), (3, 5, 2, 0), (2, 10, 4, 1), (16, 12, 2, 0),
+                                                     (2, 13, 2, 0), (2, 14, 2, 0), (4, 14, 8, 2), (1, 18, 2, 0)])
+def test_encode_base_field_rows_vs_oracle(ctx, oracle, rows, logrow, rate, log_ro):
+    """Base-field rows (party shares) take the real-input inverse transform."""
+    inp = np.stack([splitmix_base(700 + 31 * k + logrow, 1 << logrow) for k in range(rows)])
+    assert np.array_equal(ctx.Encode(inp, rate, log_ro), oracle.encode_rows(inp, rate, log_ro))
+
+
+def test_encode_mixed_rows_vs_oracle(ctx, oracle):
+    """One imaginary word in one row sends the whole launch to the general
+    inverse transform; the next call is back on the real-input path."""
+    logrow = 13
+    base = np.stack([splitmix_base(900 + k, 1 << logrow) for k in range(3)])
+    mixed = base.copy()
+    mixed[2, 4095, 1] = 7
+    for inp in (base, mixed, base):
+        assert np.array_equal(ctx.Encode(inp, 2, 0), oracle.encode_rows(inp, 2, 0))
 
 
 def test_encode_large_is_low_degree(ctx):
