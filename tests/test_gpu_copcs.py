@@ -94,14 +94,14 @@ def test_encode_vs_oracle(ctx, oracle, rows, logrow, rate, log_ro):
 @pytest.mark.parametrize("rows,logrow,rate,log_ro", [(1, 2, 2, 0), (3, 5, 2, 0), (2, 10, 4, 1), (16, 12, 2, 0),
                                                      (2, 13, 2, 0), (2, 14, 2, 0), (4, 14, 8, 2), (1, 18, 2, 0)])
 def test_encode_base_field_rows_vs_oracle(ctx, oracle, rows, logrow, rate, log_ro):
-    """Base-field rows (party shares) take the real-input inverse transform."""
+    """Base-field rows, as the party shares of the configurations are."""
     inp = np.stack([splitmix_base(700 + 31 * k + logrow, 1 << logrow) for k in range(rows)])
     assert np.array_equal(ctx.Encode(inp, rate, log_ro), oracle.encode_rows(inp, rate, log_ro))
 
 
 def test_encode_mixed_rows_vs_oracle(ctx, oracle):
-    """One imaginary word in one row sends the whole launch to the general
-    inverse transform; the next call is back on the real-input path."""
+    """Base-field rows, then the same rows with one imaginary word, then the
+    base-field rows again: every call matches the oracle."""
     logrow = 13
     base = np.stack([splitmix_base(900 + k, 1 << logrow) for k in range(3)])
     mixed = base.copy()
