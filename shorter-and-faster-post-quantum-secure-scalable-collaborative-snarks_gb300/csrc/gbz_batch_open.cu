@@ -267,7 +267,6 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
   ProofState *st = R.st;
   const uint64_t n0 = P.sizes[0], L0 = n0 * (uint64_t)P.rate;
   fe *A[2] = {nullptr, nullptr}, *B[2] = {nullptr, nullptr}, *C[2] = {nullptr, nullptr};
-  uint8_t *T[2] = {nullptr, nullptr};
   fe *tmp = nullptr, *tmp2 = nullptr, *partial = nullptr, *coef = nullptr, *evals = nullptr, *mdp = nullptr;
   if (!dry) {
     A[0] = (fe *)R.buf(300, 16 * n0);
@@ -276,8 +275,6 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
     B[1] = (fe *)R.buf(303, 16 * std::max<uint64_t>(n0 / 2, 1));
     C[0] = (fe *)R.buf(304, 16 * L0);
     C[1] = (fe *)R.buf(305, 16 * L0);
-    T[0] = (uint8_t *)R.buf(306, 32 * L0);
-    T[1] = (uint8_t *)R.buf(307, 32 * L0);
     tmp = (fe *)R.buf(308, 16 * L0);
     tmp2 = (fe *)R.buf(309, 16 * std::max<uint64_t>(L0 / 2, 1));
     partial = (fe *)R.buf(310, 16 * 3 * (uint64_t)sc_blocks(n0 / 2));
@@ -301,8 +298,25 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
   }
   int ai = 0;                 // arr / b live in A[ai] / B[ai]
   const fe *cw = codewords[0];
+  // The tree the next queries open: the caller's levels (first polynomial),
+  // a commitment over the current codeword (its nodes are computed as
+  // compression chains from the codeword, never stored), or the tree over
+  // zero leaves that aggregate_commitments builds.
+  enum { TREE_LEVELS, TREE_CODEWORD, TREE_ZERO } tree_kind = TREE_LEVELS;
   const uint8_t *tree = levels0;
-  int ci = -1, ti = -1;       // which working buffer holds cw / tree (-1: the caller's)
+  int ci = -1;                // which working buffer holds cw (-1: the caller's)
+  // open_tree_blake for l queries into the current tree of lv leaves
+  auto launch_paths = [&](int kind, const uint8_t *levels, const fe *codeword, uint64_t lv, int l, int depth,
+                          uint64_t off_path, uint64_t off_q) {
+    const uint64_t hashes = (uint64_t)l * depth;
+    if (!hashes) return;
+    if (depth != ilog2(lv)) throw ArgError("batch open: path length does not match the tree");
+    const unsigned blocks = (unsigned)((hashes + 127) / 128);
+    if (kind == TREE_LEVELS) k_whir_paths<<<blocks, 128, 0, s>>>(levels, lv, l, tr, off_q, off_path);
+    else if (kind == TREE_CODEWORD) k_whir_paths_chain<<<blocks, 128, 0, s>>>(codeword, lv, l, tr, off_q, off_path);
+    else k_zero_tree_paths<<<(unsigned)((depth + 31) / 32), 32, 0, s>>>(depth, l, tr, off_path);
+    GBZ_CUDA(cudaGetLastError());
+  };
   uint64_t m = n0, L = L0, leaves = L0 / 4;
   int cur = P.rate;
   for (const BatchStep &e : P.steps) {
@@ -332,12 +346,12 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
       m /= 2;
       // Whir_Commit_initial(arr, 2 rate) (Whir.cpp:158-190)
       const uint64_t NL = 2 * (uint64_t)cur * m;
-      const int nci = ci == 0 ? 1 : 0, nti = ti == 0 ? 1 : 0;
+      const int nci = ci == 0 ? 1 : 0;
       const uint64_t off_root = lay.rec(T_WHIR_ROOT, 1, 32);
       if (!dry) {
         ntt_launch(R.tables(ilog2(NL)), A[ai], m, C[nci], tmp, false, s);
-        merkle_commit_launch(C[nci], NL, T[nti], s);
-        GBZ_CUDA(cudaMemcpyAsync(tr + off_root, T[nti] + 32 * (merkle_hashes(NL) - 1), 32, cudaMemcpyDeviceToDevice, s));
+        k_merkle_root<<<1, 32, 0, s>>>(C[nci], ilog2(NL / 4), tr, off_root);
+        GBZ_CUDA(cudaGetLastError());
       }
       // whir_query on the current codeword and tree
       BoQueryArgs qa{};
@@ -363,11 +377,7 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
         qa.len_inv = finv(fe_make((uint64_t)e.kappa, 0));
         bo_query_kernel<<<1, kMaxQueries, 0, s>>>(qa);
         GBZ_CUDA(cudaGetLastError());
-        const uint64_t hashes = (uint64_t)e.l * e.depth;
-        if (hashes) {
-          k_whir_paths<<<(unsigned)((hashes + 127) / 128), 128, 0, s>>>(tree, leaves, e.l, tr, qa.off_q, off_path);
-          GBZ_CUDA(cudaGetLastError());
-        }
+        launch_paths(tree_kind, tree, cw, leaves, e.l, e.depth, off_path, qa.off_q);
         // update_betas on the new codeword length: exponents 2 q_i of
         // omega_NL, i.e. q_i of omega_{NL/2}
         if (update_betas_by_transform(e.l, m, NL / 2)) {
@@ -377,9 +387,8 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
         }
       }
       cw = dry ? nullptr : C[nci];
-      tree = dry ? nullptr : T[nti];
+      tree_kind = TREE_CODEWORD;
       ci = nci;
-      ti = nti;
       L = NL;
       leaves = L / 4;
       cur *= 2;
@@ -389,7 +398,7 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
       const uint64_t off_ch = lay.rec(T_AGGR_CHALLENGES, 2 * g, 16), off_K = lay.rec(T_AGGR_K, 1, 16);
       const uint64_t off_q = lay.rec(T_AGGR_QUERIES, e.la, 4), off_p = lay.rec(T_AGGR_PATHS, e.la * e.depth_a, 32);
       const uint64_t off_root = lay.rec(T_AGGR_ROOT, 1, 32);
-      const int nci = ci == 0 ? 1 : 0, nti = ti == 0 ? 1 : 0;
+      const int nci = ci == 0 ? 1 : 0;
       if (!dry) {
         bo_aggr_draw_kernel<<<1, 32, 0, s>>>(st, g, coef, tr, off_ch);
         GBZ_CUDA(cudaGetLastError());
@@ -421,20 +430,13 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
         lincomb_launch(vc, coef + g, g, L, C[nci], false, s);
         bo_aggr_queries_kernel<<<1, 32, 0, s>>>(st, e.la, (int32_t)(L / 4), tr, off_q);
         GBZ_CUDA(cudaGetLastError());
-        const uint64_t hashes = (uint64_t)e.la * e.depth_a;
-        if (hashes) {
-          k_whir_paths<<<(unsigned)((hashes + 127) / 128), 128, 0, s>>>(tree, leaves, e.la, tr, off_q, off_p);
-          GBZ_CUDA(cudaGetLastError());
-        }
-        const uint64_t nl = e.leaves_after;
-        GBZ_CUDA(cudaMemsetAsync(T[nti], 0, 32 * nl, s));
-        merkle_from_leaves_launch(T[nti], nl, s);
-        GBZ_CUDA(cudaMemcpyAsync(tr + off_root, T[nti] + 32 * (2 * nl - 2), 32, cudaMemcpyDeviceToDevice, s));
+        launch_paths(tree_kind, tree, cw, leaves, e.la, e.depth_a, off_p, off_q);
+        k_zero_tree_root<<<1, 32, 0, s>>>(ilog2(e.leaves_after), tr, off_root);
+        GBZ_CUDA(cudaGetLastError());
         cw = C[nci];
-        tree = T[nti];
       }
+      tree_kind = TREE_ZERO;
       ci = nci;
-      ti = nti;
       leaves = e.leaves_after;
     }
   }

@@ -391,6 +391,32 @@ __global__ void __launch_bounds__(kMaxQueries) k_whir_query_s(QueryArgs a, int t
   }
 }
 
+}  // namespace
+
+// --------------------------------------- kernels shared with the batch opening
+
+// WHIR sumcheck round (whir_sumcheck, Whir.cpp:233-249): message h, the
+// consistency check K == h(0) + h(1), challenge F::_random(), K = h(r).
+__global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int i, uint8_t *tr,
+                             uint64_t off_poly, uint64_t off_chal) {
+  fe H[3];
+  sum_partials(partial, blocks, H);
+  if (threadIdx.x) return;
+  fe h01 = fadd(quad_eval(H[0], H[1], H[2], fe_zero()), quad_eval(H[0], H[1], H[2], fe_one()));
+  if (!fe_eq(h01, st->K)) atomicOr(&st->error, 2u);
+  for (int k = 0; k < 3; k++) {
+    put_fe(tr, off_poly + 16 * k, H[k]);
+    st->hw[i][k] = H[k];
+  }
+  __shared__ glibc_prng g;
+  g = st->prng;
+  fe r = prng_field(g);
+  st->prng = g;
+  st->rw[i] = r;
+  put_fe(tr, off_chal, r);
+  st->K = quad_eval(H[0], H[1], H[2], r);
+}
+
 // ---- the Merkle nodes a proof reveals ------------------------------------
 // create_tree_blake (merkle_tree.cpp:267-299) hashes the LEFT child twice,
 // so node i of level k is G^k(leaf i 2^k) with G(h) = blake3(h || h), and
@@ -447,30 +473,21 @@ __global__ void k_whir_paths_chain(const fe *cw, uint64_t leaves, int l, uint8_t
   put_hash(tr + off_path + 32ull * ((uint64_t)depth * i + d), h);
 }
 
-}  // namespace
-
-// --------------------------------------- kernels shared with the batch opening
-
-// WHIR sumcheck round (whir_sumcheck, Whir.cpp:233-249): message h, the
-// consistency check K == h(0) + h(1), challenge F::_random(), K = h(r).
-__global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int i, uint8_t *tr,
-                             uint64_t off_poly, uint64_t off_chal) {
-  fe H[3];
-  sum_partials(partial, blocks, H);
+// The tree aggregate_commitments builds (Whir.cpp:594-605) has all-zero
+// leaf hashes, so its level-d nodes all equal G^d(0): the root of a tree of
+// 2^depth leaves, and every query's path entry d.
+__global__ void k_zero_tree_root(int depth, uint8_t *tr, uint64_t off) {
   if (threadIdx.x) return;
-  fe h01 = fadd(quad_eval(H[0], H[1], H[2], fe_zero()), quad_eval(H[0], H[1], H[2], fe_one()));
-  if (!fe_eq(h01, st->K)) atomicOr(&st->error, 2u);
-  for (int k = 0; k < 3; k++) {
-    put_fe(tr, off_poly + 16 * k, H[k]);
-    st->hw[i][k] = H[k];
-  }
-  __shared__ glibc_prng g;
-  g = st->prng;
-  fe r = prng_field(g);
-  st->prng = g;
-  st->rw[i] = r;
-  put_fe(tr, off_chal, r);
-  st->K = quad_eval(H[0], H[1], H[2], r);
+  uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int d = 0; d < depth; d++) node_hash(h);
+  put_hash(tr + off, h);
+}
+__global__ void k_zero_tree_paths(int depth, int l, uint8_t *tr, uint64_t off_path) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;  // one thread per level
+  if (d >= depth) return;
+  uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < d; k++) node_hash(h);
+  for (int i = 0; i < l; i++) put_hash(tr + off_path + 32ull * ((uint64_t)depth * i + d), h);
 }
 
 // open_tree_blake (merkle_tree.cpp:320-335) for every query in a tree of

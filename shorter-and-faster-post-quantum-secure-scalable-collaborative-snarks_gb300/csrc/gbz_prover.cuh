@@ -102,6 +102,15 @@ __global__ void k_whir_round(const fe *partial, int blocks, ProofState *st, int 
                              uint64_t off_poly, uint64_t off_chal);
 __global__ void k_whir_paths(const uint8_t *tree, uint64_t leaves, int l, uint8_t *tr, uint64_t off_q,
                              uint64_t off_path);
+// The same nodes without the tree (inner nodes hash their left child
+// twice, so every node is a chain of compressions from one leaf): the root
+// of the tree over a codeword, the paths of l queries into it, and the
+// root and paths of a tree whose leaf hashes are all zero.
+__global__ void k_merkle_root(const fe *cw, int depth, uint8_t *tr, uint64_t off);
+__global__ void k_whir_paths_chain(const fe *cw, uint64_t leaves, int l, uint8_t *tr, uint64_t off_q,
+                                   uint64_t off_path);
+__global__ void k_zero_tree_root(int depth, uint8_t *tr, uint64_t off);
+__global__ void k_zero_tree_paths(int depth, int l, uint8_t *tr, uint64_t off_path);
 __global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
                         uint64_t off_point, uint64_t off_eval, int check_K, const fe *point);
 
