@@ -55,6 +55,13 @@ sys.path.insert(0, PKG)
 sys.path.insert(0, ORACLE)
 
 LOGN, RATE = 24, 2
+# DRAM bytes of every transform launch of one proof (both passes of each
+# transform, the packed pass and the unpack), from one ncu capture of the
+# n = 2^22 proof (dram__bytes_read.sum, dram__bytes_write.sum, kernels
+# ntt_pass_kernel and real_unpack_kernel, four proofs within 0.3 %); scaled
+# by n for other sizes (the later, smaller transforms' writes stay in L2 at
+# 2^22, so the write figure is a lower bound).
+NTT_TRAFFIC_2E22 = {"read": 585.3e6, "write": 175.0e6}
 E2E_LANES = 3  # slots of the batched end-to-end pass
 SEED = 0x5EED0000 + 2 * 65536  # witness seed of the 2^24 rate-1/2 workload
 METRIC = "proofs/s and p50/p99 latency, batched+served vs plain GPU prover, bit-exact"
@@ -142,16 +149,56 @@ def algorithmic_int_work(logn, rate):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clocks and throttle reasons sampled during the timed region: NVML
+    queries (read only) every 5 ms from a thread, or nvidia-smi's 200 ms
+    loop when the NVML library cannot be loaded."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # NVML clock event reason bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
 
     def __init__(self, device):
         self.device, self.proc, self.lines = device, None, []
+        self.nvml, self.samples, self.max_mhz, self.stop = None, [], None, threading.Event()
+
+    def _nvml_open(self):
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = ctypes.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.device), ctypes.byref(h)) != 0:
+                return None
+            mx = ctypes.c_uint()
+            if lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:  # NVML_CLOCK_SM
+                self.max_mhz = float(mx.value)
+            fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            return lib, h, fn
+        except (OSError, AttributeError):
+            return None
+
+    def _nvml_loop(self):
+        lib, h, reasons_fn = self.nvml
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0:
+                r = rs.value if reasons_fn(h, ctypes.byref(rs)) == 0 else 0
+                self.samples.append((float(clk.value), r))
+            time.sleep(0.005)
 
     def __enter__(self):
+        self.nvml = self._nvml_open()
+        if self.nvml:
+            self.t = threading.Thread(target=self._nvml_loop, daemon=True)
+            self.t.start()
+            deadline = time.time() + 1.0
+            while not self.samples and time.time() < deadline:  # sampling before the region starts
+                time.sleep(0.002)
+            self.samples.clear()  # keep only samples taken inside the region
+            return self
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
@@ -167,6 +214,9 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *exc):
+        if self.nvml:
+            self.stop.set()
+            self.t.join(timeout=1)
         if self.proc:
             self.proc.terminate()
             try:
@@ -175,6 +225,11 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml:
+            reasons = sorted({nm for _, r in self.samples for bit, nm in self.REASONS.items() if r & bit})
+            return {"sm_mhz": statistics.median([c for c, _ in self.samples]) if self.samples else None,
+                    "sm_max_mhz": self.max_mhz, "reasons": reasons, "samples": len(self.samples),
+                    "source": "NVML, 5 ms"}
         sm, mx, reasons = [], None, set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
         for ln in self.lines:
@@ -190,7 +245,7 @@ class ClockSampler:
                 if parts[5 + k].lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, 200 ms"}
 
 
 def dist_info():
@@ -785,8 +840,15 @@ def main():
         rooflines[cat] = r
     d = rooflines.get(dom, {})
     primary = d.get("int") or d.get("hbm")
+    traffic = None
+    if dom == "ntt":
+        sc = 2.0 ** (logn - 22)
+        traffic = sc * (NTT_TRAFFIC_2E22["read"] + NTT_TRAFFIC_2E22["write"])
     roof = {"kernel": dom, "bound": "int" if "int" in d else "hbm", "ms_per_proof": per_proof_ms[dom],
-            "traffic": None}
+            "traffic": traffic,
+            "traffic_note": "DRAM bytes per proof of all transform launches: ncu capture of the n = 2^22 proof "
+                            "scaled by n; above the algorithmic bytes by the two-pass intermediate and the first "
+                            "pass's twiddle table" if traffic else None}
     if primary:
         roof.update({"achieved": primary["achieved"], "peak": primary["peak"], "unit": primary["unit"],
                      "frac": primary["frac"]})
