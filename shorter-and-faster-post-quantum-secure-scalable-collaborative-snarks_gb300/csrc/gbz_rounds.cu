@@ -132,10 +132,19 @@ __global__ void __launch_bounds__(kThreads) form_step_kernel(RoundArgs a) {
       }
       accumulate<FORM>(l, b, acc);
     } else if (MODE == 1) {
+      // every vector's four entries are loaded before any output is stored
+      // (the stores could alias later loads, so the compiler would not
+      // hoist them): one memory round trip per step instead of one per vector
+      fe xs[NV][4];
 #pragma unroll
       for (int k = 0; k < NV; k++) {
         const fe *p = a.in[k] + 4 * g;
-        fe x0 = p[0], x1 = p[1], x2 = p[2], x3 = p[3];
+#pragma unroll
+        for (int q = 0; q < 4; q++) xs[k][q] = p[q];
+      }
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        fe x0 = xs[k][0], x1 = xs[k][1], x2 = xs[k][2], x3 = xs[k][3];
         if (k == 2 && a.scale) {
           x0 = fmul(x0, a.scale[(4 * g) >> a.scale_log]);
           x1 = fmul(x1, a.scale[(4 * g + 1) >> a.scale_log]);
