@@ -305,6 +305,9 @@ void gbz_field_ops_host(const uint64_t *a, const uint64_t *b, uint64_t n, uint64
                               (_quadratic_batch_sumcheck_phase1, coSumcheck_MPI.cpp:156-176) */
 #define GBZ_SC_ZEROCHECK 3 /* (v1, v2, v3, beta1, r1, r2; b): sum (l1 l2 + b lr1 lr2 - x l3) lbeta1, 4
                               (_zero_check_sumcheck_phase1, coSumcheck_MPI.cpp:12-32) */
+#define GBZ_SC_QUADRUPLE 4 /* (v1, v2, v3, v4): sum l1 l2 l3 l4, 5 coefficients (the round message of
+                              quadruple_sumcheck, delegate_protocol.cpp:57-115, whose challenges are
+                              the fifth of five F::_random() draws per round) */
 
 /* One round of a form over vectors v[0..k) of m entries (m a power of two).
  * r == NULL: coeffs = the round polynomial of v (the reference's phase 1).
@@ -312,7 +315,7 @@ void gbz_field_ops_host(const uint64_t *a, const uint64_t *b, uint64_t n, uint64
  * v[j] = v[2j] + r (v[2j+1] - v[2j]) for j < m/2 (phase 2,
  * coSumcheck_MPI.cpp:34-44, 178-187), and coeffs is the round polynomial
  * of the folded vectors.  b (2 words, host) is required by the batch and
- * zero-check forms.  coeffs (host) receives 3 or 4 elements. */
+ * zero-check forms.  coeffs (host) receives 3, 4 or 5 elements. */
 gbz_status gbz_sumcheck_round(gbz_ctx *ctx, int form, uint64_t *const *v, uint64_t m, const uint64_t *b,
                               const uint64_t *r, uint64_t *coeffs, int mem);
 

@@ -1046,17 +1046,26 @@ static inline void quad_lin(const fe q[3], lin_t x, fe c[4]) {
   c[3] = f_mul(q[2], x.b);
 }
 
+/* cubic * linear -> quartic (polynomial.cpp:99-101) */
+static inline void cub_lin(const fe c[4], lin_t x, fe q[5]) {
+  q[0] = f_mul(c[0], x.a);
+  q[1] = f_add(f_mul(c[1], x.a), f_mul(c[0], x.b));
+  q[2] = f_add(f_mul(c[2], x.a), f_mul(c[1], x.b));
+  q[3] = f_add(f_mul(c[3], x.a), f_mul(c[2], x.b));
+  q[4] = f_mul(c[3], x.b);
+}
+
 int orc_sumcheck_form_vectors(int form) {
-  static const int nv[4] = {2, 3, 6, 6};
-  return form >= 0 && form < 4 ? nv[form] : 0;
+  static const int nv[5] = {2, 3, 6, 6, 4};
+  return form >= 0 && form < 5 ? nv[form] : 0;
 }
 int orc_sumcheck_form_degree(int form) {
-  static const int dg[4] = {2, 3, 2, 3};
-  return form >= 0 && form < 4 ? dg[form] : 0;
+  static const int dg[5] = {2, 3, 2, 3, 4};
+  return form >= 0 && form < 5 ? dg[form] : 0;
 }
 
 void orc_sumcheck_round(int form, const uint64_t *const *v, int64_t m, const uint64_t bb[2], uint64_t *out) {
-  fe acc[4] = {f_zero(), f_zero(), f_zero(), f_zero()};
+  fe acc[5] = {f_zero(), f_zero(), f_zero(), f_zero(), f_zero()};
   fe accr[3] = {f_zero(), f_zero(), f_zero()};
   fe b = bb ? f_make(bb[0], bb[1]) : f_zero();
   for (int64_t j = 0; j < m / 2; j++) {
@@ -1068,6 +1077,12 @@ void orc_sumcheck_round(int form, const uint64_t *const *v, int64_t m, const uin
       lin_mul(lin_at(v[0], j), lin_at(v[1], j), q);
       quad_lin(q, lin_at(v[2], j), c);
       for (int k = 0; k < 4; k++) acc[k] = f_add(acc[k], c[k]);
+    } else if (form == 4) { /* quadruple_sumcheck, delegate_protocol.cpp:66-76 */
+      fe q4[5];
+      lin_mul(lin_at(v[0], j), lin_at(v[1], j), q);
+      quad_lin(q, lin_at(v[2], j), c);
+      cub_lin(c, lin_at(v[3], j), q4);
+      for (int k = 0; k < 5; k++) acc[k] = f_add(acc[k], q4[k]);
     } else if (form == 2) { /* coSumcheck_MPI.cpp:156-176 */
       lin_mul(lin_at(v[0], j), lin_at(v[1], j), q);
       for (int k = 0; k < 3; k++) acc[k] = f_add(acc[k], q[k]);

@@ -134,7 +134,8 @@ void orc_cophase2(const uint64_t *v, int64_t n, const uint64_t *L, int logd, uin
  *   form 2 batch (v1, v2, v3, v4, r1, r2; b):
  *          sum l1 l2 + l3 l4 + b sum lr1 lr2               (coSumcheck_MPI.cpp:156-176)
  *   form 3 zero-check (v1, v2, v3, beta, r1, r2; b):
- *          sum (l1 l2 + b lr1 lr2 - x l3) lbeta            (coSumcheck_MPI.cpp:12-32) */
+ *          sum (l1 l2 + b lr1 lr2 - x l3) lbeta            (coSumcheck_MPI.cpp:12-32)
+ *   form 4 quadruple (v1, v2, v3, v4): sum l1 l2 l3 l4     (delegate_protocol.cpp:66-76) */
 int orc_sumcheck_form_vectors(int form);
 int orc_sumcheck_form_degree(int form);
 void orc_sumcheck_round(int form, const uint64_t *const *v, int64_t m, const uint64_t b[2], uint64_t *out);

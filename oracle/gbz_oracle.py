@@ -313,8 +313,8 @@ def cophase2(v, L):
     return out
 
 
-FORM_VECTORS = {0: 2, 1: 3, 2: 6, 3: 6}
-FORM_DEGREE = {0: 2, 1: 3, 2: 2, 3: 3}
+FORM_VECTORS = {0: 2, 1: 3, 2: 6, 3: 6, 4: 4}
+FORM_DEGREE = {0: 2, 1: 3, 2: 2, 3: 3, 4: 4}
 
 
 def sumcheck_round(form, vecs, b=None):

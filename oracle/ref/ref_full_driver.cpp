@@ -314,6 +314,10 @@ static int cmd_batchopen(int rate, int wk, uint64_t seed, unsigned prng, const v
   return 0;
 }
 
+// delegate_protocol.cpp defines it without a header
+vector<std::pair<F, vector<F>>> quadruple_sumcheck(F y, vector<F> &v1, vector<F> &v2, vector<F> &v3, vector<F> &v4,
+                                                   F previous_r, double &ps);
+
 int main(int argc, char **argv) {
   if (argc < 2) return 1;
   std::string c = argv[1];
@@ -339,6 +343,27 @@ int main(int argc, char **argv) {
       _quadratic_batch_sumcheck_phase2(iter, r, v[0], v[1], v[2], v[3], v[4], v[5]);
     }
     for (auto &x : v) put_prefix(x, half);
+    return 0;
+  }
+  if (c == "quadsc4") {
+    // quadruple_sumcheck (delegate_protocol.cpp:57-115): inputs v1..v4 of
+    // 2^logm from the seed, y the true sum, the glibc generator seeded with
+    // prng (five F::_random() draws per round, the last one the challenge).
+    // Output: y, the four final values, the number of challenges, the challenges.
+    int logm = I(2);
+    SplitMix g(U(3));
+    srandom((unsigned)U(4));
+    size_t m = 1u << logm;
+    vector<F> v1 = g.vec(m), v2 = g.vec(m), v3 = g.vec(m), v4 = g.vec(m);
+    F y = F(0);
+    for (size_t i = 0; i < m; i++) y = y + v1[i] * v2[i] * v3[i] * v4[i];
+    putFs({y});
+    double ps = 0;
+    vector<std::pair<F, vector<F>>> res = quadruple_sumcheck(y, v1, v2, v3, v4, F(0), ps);
+    for (auto &pr : res) putFs({pr.first});
+    uint32_t nr = (uint32_t)res[0].second.size();
+    put(&nr, 4);
+    putFs(res[0].second);
     return 0;
   }
   if (c == "cubicsc" || c == "quadsc") {

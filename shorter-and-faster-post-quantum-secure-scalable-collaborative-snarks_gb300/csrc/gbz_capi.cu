@@ -958,15 +958,15 @@ gbz_status gbz_sumcheck_round(gbz_ctx *ctx, int form, uint64_t *const *v, uint64
     dv[k] = dev_view(ctx, 40 + k, (fe *)v[k], 16 * m, mem, true);
     a.in[k] = dv[k];
   }
-  fe *dout = (fe *)ctx->buf(57, 16 * 4);
-  GBZ_CUDA(cudaMemsetAsync(dout, 0, 16 * 4, ctx->stream));
+  fe *dout = (fe *)ctx->buf(57, 16 * kMaxFormCoeffs);
+  GBZ_CUDA(cudaMemsetAsync(dout, 0, 16 * kMaxFormCoeffs, ctx->stream));
   if (r) {
     const uint64_t half = m / 2;
     for (int k = 0; k < nv; k++) a.out[k] = (fe *)ctx->buf(60 + k, 16 * half);
     if (m >= 4) {
       a.pairs = m / 4;
       const int blocks = round_blocks(a.pairs);
-      a.partial = (fe *)ctx->buf(56, 16 * 4 * (uint64_t)blocks);
+      a.partial = (fe *)ctx->buf(56, 16 * kMaxFormCoeffs * (uint64_t)blocks);
       form_step_launch(form, a, 1, blocks, ctx->stream);
       form_sum_launch(a.partial, blocks, nc, dout, ctx->stream);
     } else {
@@ -979,7 +979,7 @@ gbz_status gbz_sumcheck_round(gbz_ctx *ctx, int form, uint64_t *const *v, uint64
   } else {
     a.pairs = m / 2;
     const int blocks = round_blocks(a.pairs);
-    a.partial = (fe *)ctx->buf(56, 16 * 4 * (uint64_t)blocks);
+    a.partial = (fe *)ctx->buf(56, 16 * kMaxFormCoeffs * (uint64_t)blocks);
     form_step_launch(form, a, 0, blocks, ctx->stream);
     form_sum_launch(a.partial, blocks, nc, dout, ctx->stream);
   }

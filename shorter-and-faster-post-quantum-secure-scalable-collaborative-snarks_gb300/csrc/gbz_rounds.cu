@@ -9,6 +9,7 @@
 //   batch (v1..v4, r1, r2; b)     sum l1 l2 + l3 l4 + b lr1 lr2 coSumcheck_MPI.cpp:156-176
 //   zero-check (v1, v2, v3, beta, r1, r2; b)
 //                                 sum (l1 l2 + b lr1 lr2 - x l3) lbeta   coSumcheck_MPI.cpp:12-32
+//   quadruple (v1..v4)            sum l1 l2 l3 l4              delegate_protocol.cpp:66-76
 // and folds every vector by the round challenge r: v[j] = v[2j] + r (v[2j+1]
 // - v[2j]) (coSumcheck_MPI.cpp:34-44, 178-187).  The fold of round i and the
 // message of round i + 1 are one pass (four entries of every vector per
@@ -27,6 +28,7 @@ template <> struct Form<SC_QUADRATIC> { static constexpr int NV = 2, NC = 3; };
 template <> struct Form<SC_CUBIC> { static constexpr int NV = 3, NC = 4; };
 template <> struct Form<SC_BATCH> { static constexpr int NV = 6, NC = 3; };
 template <> struct Form<SC_ZEROCHECK> { static constexpr int NV = 6, NC = 4; };
+template <> struct Form<SC_QUADRUPLE> { static constexpr int NV = 4, NC = 5; };
 
 struct Line {
   fe a, b;
@@ -57,6 +59,15 @@ __device__ __forceinline__ void accumulate(const Line *l, fe b, fe *acc) {
     lmul(l[0], l[1], q);
     qlmul(q, l[2], c);
     for (int k = 0; k < 4; k++) acc[k] = fadd(acc[k], c[k]);
+  } else if (FORM == SC_QUADRUPLE) {
+    // ((l1 l2) l3) l4 as the reference multiplies them (polynomial.cpp:91-101)
+    lmul(l[0], l[1], q);
+    qlmul(q, l[2], c);
+    acc[0] = fadd(acc[0], fmul(c[0], l[3].a));
+    acc[1] = fadd(acc[1], fadd(fmul(c[1], l[3].a), fmul(c[0], l[3].b)));
+    acc[2] = fadd(acc[2], fadd(fmul(c[2], l[3].a), fmul(c[1], l[3].b)));
+    acc[3] = fadd(acc[3], fadd(fmul(c[3], l[3].a), fmul(c[2], l[3].b)));
+    acc[4] = fadd(acc[4], fmul(c[3], l[3].b));
   } else if (FORM == SC_BATCH) {
     fe q2[3], qr[3];
     lmul(l[0], l[1], q);
@@ -85,7 +96,7 @@ __device__ __forceinline__ fe shfl_down_fe(fe v, int d) {
 // Block sum of NC field elements; valid in thread 0.
 template <int NC>
 __device__ void block_sum(fe *x) {
-  __shared__ fe red[4][kThreads / 32];
+  __shared__ fe red[kMaxFormCoeffs][kThreads / 32];
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1)
 #pragma unroll
@@ -233,15 +244,16 @@ __global__ void form_finalize_kernel(const fe *partial, int blocks, int nc, Roun
 }
 
 __global__ void form_sum_kernel(const fe *partial, int blocks, int nc, fe *out) {
-  __shared__ fe red[4][kThreads];
-  fe acc[4] = {fe_zero(), fe_zero(), fe_zero(), fe_zero()};
+  __shared__ fe red[kMaxFormCoeffs][kThreads];
+  fe acc[kMaxFormCoeffs];
+  for (int k = 0; k < kMaxFormCoeffs; k++) acc[k] = fe_zero();
   for (int i = threadIdx.x; i < blocks; i += kThreads)
     for (int k = 0; k < nc; k++) acc[k] = fadd(acc[k], partial[(uint64_t)i * nc + k]);
-  for (int k = 0; k < 4; k++) red[k][threadIdx.x] = acc[k];
+  for (int k = 0; k < kMaxFormCoeffs; k++) red[k][threadIdx.x] = acc[k];
   __syncthreads();
   for (int w = kThreads / 2; w > 0; w >>= 1) {
     if ((int)threadIdx.x < w)
-      for (int k = 0; k < 4; k++) red[k][threadIdx.x] = fadd(red[k][threadIdx.x], red[k][threadIdx.x + w]);
+      for (int k = 0; k < kMaxFormCoeffs; k++) red[k][threadIdx.x] = fadd(red[k][threadIdx.x], red[k][threadIdx.x + w]);
     __syncthreads();
   }
   if (threadIdx.x < (unsigned)nc) out[threadIdx.x] = red[threadIdx.x][0];
@@ -268,6 +280,7 @@ int form_vectors(int form) {
     case SC_CUBIC: return 3;
     case SC_BATCH: return 6;
     case SC_ZEROCHECK: return 6;
+    case SC_QUADRUPLE: return 4;
     default: return 0;
   }
 }
@@ -277,6 +290,7 @@ int form_coeffs(int form) {
     case SC_CUBIC: return 4;
     case SC_BATCH: return 3;
     case SC_ZEROCHECK: return 4;
+    case SC_QUADRUPLE: return 5;
     default: return 0;
   }
 }
@@ -294,6 +308,7 @@ void form_step_launch(int form, const RoundArgs &a, int mode, int blocks, cudaSt
     case SC_CUBIC: launch_form<SC_CUBIC>(a, mode, blocks, s); break;
     case SC_BATCH: launch_form<SC_BATCH>(a, mode, blocks, s); break;
     case SC_ZEROCHECK: launch_form<SC_ZEROCHECK>(a, mode, blocks, s); break;
+    case SC_QUADRUPLE: launch_form<SC_QUADRUPLE>(a, mode, blocks, s); break;
     default: throw ArgError("sumcheck: unknown round form");
   }
 }

@@ -5,7 +5,8 @@
 
 namespace gbz {
 
-enum { SC_QUADRATIC = 0, SC_CUBIC = 1, SC_BATCH = 2, SC_ZEROCHECK = 3 };
+enum { SC_QUADRATIC = 0, SC_CUBIC = 1, SC_BATCH = 2, SC_ZEROCHECK = 3, SC_QUADRUPLE = 4 };
+constexpr int kMaxFormCoeffs = 5;  // the quadruple form's degree-4 message
 
 struct RoundArgs {
   const fe *in[6];      // vectors of the form, in order

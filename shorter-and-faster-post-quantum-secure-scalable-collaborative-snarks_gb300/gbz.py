@@ -53,9 +53,9 @@ EXPORTS = (
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
 
 
-SC_QUADRATIC, SC_CUBIC, SC_BATCH, SC_ZEROCHECK = range(4)
-FORM_VECTORS = {SC_QUADRATIC: 2, SC_CUBIC: 3, SC_BATCH: 6, SC_ZEROCHECK: 6}
-FORM_DEGREE = {SC_QUADRATIC: 2, SC_CUBIC: 3, SC_BATCH: 2, SC_ZEROCHECK: 3}
+SC_QUADRATIC, SC_CUBIC, SC_BATCH, SC_ZEROCHECK, SC_QUADRUPLE = range(5)
+FORM_VECTORS = {SC_QUADRATIC: 2, SC_CUBIC: 3, SC_BATCH: 6, SC_ZEROCHECK: 6, SC_QUADRUPLE: 4}
+FORM_DEGREE = {SC_QUADRATIC: 2, SC_CUBIC: 3, SC_BATCH: 2, SC_ZEROCHECK: 3, SC_QUADRUPLE: 4}
 
 
 class SchedOpts(ctypes.Structure):

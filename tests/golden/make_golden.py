@@ -154,6 +154,8 @@ def gen_sumcheck():
         ("cubicsc_8_4", ("cubicsc", 8, 4, 75, 1)), ("cubicsc_10_3", ("cubicsc", 10, 3, 76, 9)),
         ("cubicsc_3_4", ("cubicsc", 3, 4, 77, 1)), ("quadsc_8_4", ("quadsc", 8, 4, 78, 1)),
         ("quadsc_11_2", ("quadsc", 11, 2, 79, 5)),
+        ("quadsc4_6", ("quadsc4", 6, 95, 1)), ("quadsc4_9", ("quadsc4", 9, 96, 7)),
+        ("quadsc4_1", ("quadsc4", 1, 97, 3)),
         ("aggclaims_6_2_3", ("aggclaims", 6, 2, 3, 80, 1)), ("aggclaims_9_4_2", ("aggclaims", 9, 4, 2, 81, 7)),
         ("aggclaims_5_1_1", ("aggclaims", 5, 1, 1, 82, 1)), ("aggarrays_6_3", ("aggarrays", 6, 3, 83)),
         ("aggarrays_8_2", ("aggarrays", 8, 2, 84)), ("aggcommit_8_3_2_4", ("aggcommit", 8, 3, 2, 4, 85, 1)),

@@ -144,3 +144,67 @@ def test_party_sumcheck_large_consistent(ctx, oracle):
     got = ctx.party_sumcheck(1, vecs, N, w=w, offset=4, y=y)
     assert np.array_equal(got["challenges"], probe["challenges"])
     assert np.array_equal(got["fin"], probe["fin"])
+
+
+def _feval(coeffs, x):
+    P = (1 << 61) - 1
+    acc = (0, 0)
+    for c in coeffs:
+        acc = ((acc[0] * int(x[0]) - acc[1] * int(x[1]) + int(c[0])) % P,
+               (acc[0] * int(x[1]) + acc[1] * int(x[0]) + int(c[1])) % P)
+    return acc
+
+
+def _quadruple_on_device(ctx, gbz, vecs, y, prng_seed, oracle=None):
+    """quadruple_sumcheck (delegate_protocol.cpp:57-115) through
+    gbz_sumcheck_round: the message of the current vectors, five F::_random()
+    draws, the challenge folding the vectors in the next call."""
+    P = (1 << 61) - 1
+    g = gbz.Prng(prng_seed)
+    cur = [np.ascontiguousarray(v).copy() for v in vecs]
+    m = cur[0].shape[0]
+    claim = (int(y[0]), int(y[1]))
+    H = ctx.sumcheck_round(gbz.SC_QUADRUPLE, cur)
+    chal = []
+    while True:
+        if oracle is not None:
+            assert np.array_equal(H, oracle.sumcheck_round(4, [v[:m] for v in cur]))
+        h0, h1 = _feval(H, (0, 0)), _feval(H, (1, 0))
+        assert ((h0[0] + h1[0]) % P, (h0[1] + h1[1]) % P) == claim
+        for _ in range(5):
+            r = g.field()
+        chal.append(r)
+        claim = _feval(H, r)
+        H = ctx.sumcheck_round(gbz.SC_QUADRUPLE, [v[:m] for v in cur], r=r)
+        m //= 2
+        if m == 1:
+            break
+    return chal, [v[0] for v in cur], claim
+
+
+@pytest.mark.parametrize("name", ["quadsc4_6", "quadsc4_9", "quadsc4_1"])
+def test_quadruple_sumcheck_golden(ctx, gbz, golden, name):
+    r, (_, logm, seed, prng) = case(golden, name)
+    m = 1 << logm
+    raw = splitmix_ext(seed, 4 * m)
+    vecs = [raw[k * m:(k + 1) * m] for k in range(4)]
+    y = r.fe(1)[0]
+    fin = r.fe(4)
+    nr = r.u32()
+    ref_chal = r.fe(nr)
+    r.done()
+    chal, finals, claim = _quadruple_on_device(ctx, gbz, vecs, y, prng)
+    assert np.array_equal(np.array(chal, dtype=np.uint64).reshape(-1, 2), ref_chal)
+    assert np.array_equal(np.array(finals, dtype=np.uint64).reshape(-1, 2), fin)
+
+
+def test_quadruple_sumcheck_vs_oracle_large(ctx, gbz, oracle):
+    """2^16 entries: every round message equals the oracle's."""
+    rng = np.random.default_rng(4040)
+    m = 1 << 16
+    vecs = [rand_fe(rng, m) for _ in range(4)]
+    P = (1 << 61) - 1
+    H = oracle.sumcheck_round(4, vecs)
+    h0, h1 = _feval(H, (0, 0)), _feval(H, (1, 0))
+    y = np.array([(h0[0] + h1[0]) % P, (h0[1] + h1[1]) % P], dtype=np.uint64)
+    _quadruple_on_device(ctx, gbz, vecs, y, 11, oracle)

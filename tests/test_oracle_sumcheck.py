@@ -100,3 +100,48 @@ def test_party_sumcheck_many_parties_consistent(oracle):
             assert fadd(feval(poly, (0, 0)), feval(poly, (1, 0))) == claim
             claim = feval(poly, c)
         assert len(res["challenges"]) == (7 - 3) + (3 + 2)
+
+
+def fmul(a, b):
+    return ((a[0] * b[0] - a[1] * b[1]) % P, (a[0] * b[1] + a[1] * b[0]) % P)
+
+
+def quadruple_protocol(round_fn, fold_fn, vecs, y, prng):
+    """quadruple_sumcheck (delegate_protocol.cpp:57-115) driven by a round
+    function: each round's message must be consistent with the claim, five
+    F::_random() draws follow and the last is the challenge.  Returns the
+    challenges, the final values and the final claim."""
+    cur = vecs
+    claim = (int(y[0]), int(y[1]))
+    chal = []
+    while cur[0].shape[0] > 1:
+        H = round_fn(cur)
+        assert fadd(feval(H, (0, 0)), feval(H, (1, 0))) == claim
+        for _ in range(5):
+            r = prng.field()
+        chal.append(r)
+        claim = feval(H, r)
+        cur = fold_fn(cur, r)
+    return chal, [c[0] for c in cur], claim
+
+
+@pytest.mark.parametrize("name", ["quadsc4_6", "quadsc4_9", "quadsc4_1"])
+def test_quadruple_sumcheck_vs_reference(oracle, golden, name):
+    r, (_, logm, seed, prng) = case(golden, name)
+    m = 1 << logm
+    raw = splitmix_ext(seed, 4 * m)
+    vecs = [raw[k * m:(k + 1) * m] for k in range(4)]
+    y = r.fe(1)[0]
+    fin = r.fe(4)
+    nr = r.u32()
+    ref_chal = r.fe(nr)
+    r.done()
+    chal, finals, claim = quadruple_protocol(lambda cur: oracle.sumcheck_round(4, cur),
+                                             lambda cur, c: oracle.sumcheck_fold_many(cur, c),
+                                             vecs, y, oracle.Prng(prng))
+    assert np.array_equal(np.array(chal, dtype=np.uint64).reshape(-1, 2), ref_chal)
+    assert np.array_equal(np.array(finals, dtype=np.uint64).reshape(-1, 2), fin)
+    prod = (1, 0)
+    for f in finals:
+        prod = fmul(prod, (int(f[0]), int(f[1])))
+    assert claim == prod
