@@ -305,19 +305,23 @@ __global__ void __launch_bounds__(256) k_whir_schedule(ProofState *st, SchedArgs
   }
 }
 
-// WHIR sumcheck round i of iteration t from the reduction partials: the
-// message is recorded (transcript and st->whw for the query chain, which
-// checks it against K) with the challenge drawn up front.  After the last
-// round, the threads also prepare update_betas of this iteration: scaled
+// Preparation of an iteration's update_betas by the round kernel: scaled
 // queries 2 q_i, omega_NL^{2 q_i} and the weights c_i = r^(i+1).
 struct UbPrep {
   int l;                 // 0: no preparation
   const fe *lo, *hi;     // omega_NL^e
 };
-__global__ void k_whir_round_s(const fe *partial, int blocks, ProofState *st, int t, int i, uint8_t *tr,
-                               uint64_t off_poly, uint64_t off_chal, UbPrep u) {
-  fe H[3];
-  sum_partials(partial, blocks, H);
+// The two WHIR sumcheck rounds of iteration t from the partials of the fused
+// two-round pass, in one launch: each message is recorded (transcript and
+// st->whw for the query chain, which checks it against K) with its challenge
+// drawn up front, and the threads prepare the iteration's update_betas.
+__global__ void k_whir_rounds2_s(const fe *partial0, const fe *partial1, int blocks, ProofState *st, int t,
+                                 uint8_t *tr, uint64_t off_poly0, uint64_t off_chal0, uint64_t off_poly1,
+                                 uint64_t off_chal1, UbPrep u) {
+  fe H0[3], H1[3];
+  sum_partials(partial0, blocks, H0);
+  __syncthreads();  // sum_partials' shared scratch is reused
+  sum_partials(partial1, blocks, H1);
   for (int j = threadIdx.x; j < u.l; j += blockDim.x) {
     const uint32_t q2 = 2u * (uint32_t)st->wq[t][j];
     st->q[j] = (int32_t)q2;
@@ -326,10 +330,13 @@ __global__ void k_whir_round_s(const fe *partial, int blocks, ProofState *st, in
   }
   if (threadIdx.x) return;
   for (int k = 0; k < 3; k++) {
-    put_fe(tr, off_poly + 16 * k, H[k]);
-    st->whw[t][i][k] = H[k];
+    put_fe(tr, off_poly0 + 16 * k, H0[k]);
+    st->whw[t][0][k] = H0[k];
+    put_fe(tr, off_poly1 + 16 * k, H1[k]);
+    st->whw[t][1][k] = H1[k];
   }
-  put_fe(tr, off_chal, st->wr[t][i]);
+  put_fe(tr, off_chal0, st->wr[t][0]);
+  put_fe(tr, off_chal1, st->wr[t][1]);
 }
 
 // whir_query (Whir.cpp:251-314) of iteration t with the drawn positions, and
@@ -837,9 +844,8 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
           sc_fold2_launch(a, b, m, &st->wr[iter][0], &st->wr[iter][1], arr_next, bd, p.partial, p.partial2, blocks,
                           s));
     }
-    RUN(PC_PROTOCOL, 1, k_whir_round_s<<<1, 256, 0, s>>>(p.partial, blocks, st, iter, 0, tr, op, oc, UbPrep{}));
     {
-      // the second round kernel also prepares this iteration's beta update
+      // both round messages; the kernel also prepares this iteration's beta update
       UbPrep u{};
       if (!dry) {
         const NttTables &tnew = p.tables(ilog2(NL));
@@ -847,7 +853,8 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
         u.lo = tnew.lo_fwd;
         u.hi = tnew.hi_fwd;
       }
-      RUN(PC_PROTOCOL, 1, k_whir_round_s<<<1, 256, 0, s>>>(p.partial2, blocks, st, iter, 1, tr, op1, oc1, u));
+      RUN(PC_PROTOCOL, 1,
+          k_whir_rounds2_s<<<1, 256, 0, s>>>(p.partial, p.partial2, blocks, st, iter, tr, op, oc, op1, oc1, u));
     }
     a = arr_next;
     b = bd;
