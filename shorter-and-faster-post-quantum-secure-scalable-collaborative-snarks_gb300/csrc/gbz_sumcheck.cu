@@ -169,9 +169,20 @@ sc_fold2_eq_kernel(const fe *__restrict__ a, const fe *__restrict__ E2, uint64_t
     const fe x0 = a[4 * t], x1 = a[4 * t + 1], x2 = a[4 * t + 2], x3 = a[4 * t + 3];
     const fe E = E2[t];
     const fe g0 = fmul(f0, E), g1 = fmul(c1, E);
-    S0 = fadd(S0, fadd(fmul(x0, g0), fmul(x2, g1)));
-    S1 = fadd(S1, fadd(fmul(x1, g0), fmul(x3, g1)));
-    const fe fa0 = fadd(fmul(r0, fsub(x1, x0)), x0), fa1 = fadd(fmul(r0, fsub(x3, x2)), x2);
+    fe fa0, fa1;
+    if (!(x0.im | x1.im | x2.im | x3.im)) {
+      // base-field entries (the witness of the configurations): products
+      // with a base-field factor need two of the four partial products
+      S0 = fadd(S0, fadd(fmul_base(g0, x0.re), fmul_base(g1, x2.re)));
+      S1 = fadd(S1, fadd(fmul_base(g0, x1.re), fmul_base(g1, x3.re)));
+      fa0 = fadd(fmul_base(r0, subp(x1.re, x0.re)), x0);
+      fa1 = fadd(fmul_base(r0, subp(x3.re, x2.re)), x2);
+    } else {
+      S0 = fadd(S0, fadd(fmul(x0, g0), fmul(x2, g1)));
+      S1 = fadd(S1, fadd(fmul(x1, g0), fmul(x3, g1)));
+      fa0 = fadd(fmul(r0, fsub(x1, x0)), x0);
+      fa1 = fadd(fmul(r0, fsub(x3, x2)), x2);
+    }
     T0 = fadd(T0, fmul(fa0, E));
     T1 = fadd(T1, fmul(fa1, E));
     a4[t] = fadd(fmul(r1, fsub(fa1, fa0)), fa0);
