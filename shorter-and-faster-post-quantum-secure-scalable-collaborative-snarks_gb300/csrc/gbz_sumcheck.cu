@@ -219,9 +219,14 @@ sc_eq_reduce_kernel(const fe *__restrict__ a, const fe *__restrict__ E, uint64_t
   fe S0 = fe_zero(), S1 = fe_zero(), Z = fe_zero();
   const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
   for (uint64_t j = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; j < pairs; j += stride) {
-    const fe e = E[j];
-    S0 = fadd(S0, fmul(a[2 * j], e));
-    S1 = fadd(S1, fmul(a[2 * j + 1], e));
+    const fe e = E[j], w0 = a[2 * j], w1 = a[2 * j + 1];
+    if (!(w0.im | w1.im)) {  // base-field entries: two partial products each
+      S0 = fadd(S0, fmul_base(e, w0.re));
+      S1 = fadd(S1, fmul_base(e, w1.re));
+    } else {
+      S0 = fadd(S0, fmul(w0, e));
+      S1 = fadd(S1, fmul(w1, e));
+    }
   }
   block_sum3(S0, S1, Z);
   if (threadIdx.x == 0) {
@@ -243,7 +248,14 @@ sc_eq_fold_kernel(const fe *__restrict__ a, uint64_t m, const fe *chal, fe *__re
   for (uint64_t t = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; t < quads; t += stride) {
     const fe x0 = a[4 * t], x1 = a[4 * t + 1], x2 = a[4 * t + 2], x3 = a[4 * t + 3];
     const fe e0 = E[2 * t], e1 = E[2 * t + 1];
-    const fe f0 = fadd(fmul(r, fsub(x1, x0)), x0), f1 = fadd(fmul(r, fsub(x3, x2)), x2);
+    fe f0, f1;
+    if (!(x0.im | x1.im | x2.im | x3.im)) {  // base-field entries (the first fold of the witness)
+      f0 = fadd(fmul_base(r, subp(x1.re, x0.re)), x0);
+      f1 = fadd(fmul_base(r, subp(x3.re, x2.re)), x2);
+    } else {
+      f0 = fadd(fmul(r, fsub(x1, x0)), x0);
+      f1 = fadd(fmul(r, fsub(x3, x2)), x2);
+    }
     a2[2 * t] = f0;
     a2[2 * t + 1] = f1;
     const fe e = fadd(e0, e1);
