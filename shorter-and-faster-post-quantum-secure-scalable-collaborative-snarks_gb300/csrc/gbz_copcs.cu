@@ -130,13 +130,25 @@ shares_kernel(const fe *v, const fe *fill, uint64_t groups, int N, int k, int kk
   }
 }
 
-// out[i] = sum_p lambda_p msgs[p][i]
-__global__ void aggregate_kernel(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= len) return;
+// out[i] = sum_p lambda_p msgs[p][i].  A CTA takes 32 consecutive
+// coefficients (coalesced loads) and splits the parties over its 8 rows of
+// threads (p = y mod 8), whose sums meet in shared memory: eight times the
+// loads in flight of one thread per coefficient.
+constexpr int kAggrCols = 32, kAggrRows = 8;
+__global__ void __launch_bounds__(kAggrCols * kAggrRows)
+aggregate_kernel(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out) {
+  __shared__ fe red[kAggrRows][kAggrCols];
+  const uint64_t i = (uint64_t)blockIdx.x * kAggrCols + threadIdx.x;
   fe acc = fe_zero();
-  for (int p = 0; p < N; p++) acc = fadd(acc, fmul(lambda[p], msgs[(uint64_t)p * len + i]));
-  out[i] = acc;
+  if (i < len)
+    for (int p = threadIdx.y; p < N; p += kAggrRows) acc = fadd(acc, fmul(lambda[p], msgs[(uint64_t)p * len + i]));
+  red[threadIdx.y][threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.y == 0 && i < len) {
+    fe s = red[0][threadIdx.x];
+    for (int y = 1; y < kAggrRows; y++) s = fadd(s, red[y][threadIdx.x]);
+    out[i] = s;
+  }
 }
 
 // flags[blk] = 1 when block blk of v has a non-zero entry.
@@ -328,7 +340,8 @@ void shares_launch(const fe *v, const fe *fill, uint64_t groups, int N, const fe
 }
 
 void aggregate_launch(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out, cudaStream_t s) {
-  aggregate_kernel<<<grid(len), 256, 0, s>>>(msgs, N, len, lambda, out);
+  aggregate_kernel<<<(unsigned)((len + kAggrCols - 1) / kAggrCols), dim3(kAggrCols, kAggrRows), 0, s>>>(msgs, N, len,
+                                                                                                 lambda, out);
   GBZ_CUDA(cudaGetLastError());
 }
 
