@@ -31,6 +31,16 @@ struct gbz_ctx {
   std::map<std::pair<int, int>, std::unique_ptr<Profiler>> profilers;
   std::unique_ptr<Scheduler> sched;
   bool graphs = true;  // gbz_prove replays captured graphs (gbz_set_graphs)
+  SideStream side;     // second stream of the party sumcheck (created on first use)
+
+  const SideStream &side_stream() {
+    if (!side.stream) {
+      GBZ_CUDA(cudaStreamCreateWithFlags(&side.stream, cudaStreamNonBlocking));
+      GBZ_CUDA(cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming));
+      GBZ_CUDA(cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming));
+    }
+    return side;
+  }
 
   void *buf(int slot, uint64_t bytes) {
     auto &e = scratch[slot];
@@ -246,6 +256,12 @@ void gbz_destroy(gbz_ctx *ctx) {
     for (auto &kv : ctx->scratch) cudaFree(kv.second.first);
     cudaFree(ctx->st);
     cudaFree(ctx->ub_scratch);
+    if (ctx->side.stream) {
+      cudaStreamSynchronize(ctx->side.stream);
+      cudaEventDestroy(ctx->side.fork);
+      cudaEventDestroy(ctx->side.join);
+      cudaStreamDestroy(ctx->side.stream);
+    }
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   } catch (...) {
   }
@@ -1454,7 +1470,9 @@ gbz_status gbz_party_sumcheck(gbz_ctx *ctx, int form, const uint64_t *v1, const 
   fe *dpolys = (fe *)ctx->buf(45, 16 * (uint64_t)nc * std::max(rounds, 1));
   fe *dchal = (fe *)ctx->buf(46, 16 * (uint64_t)std::max(rounds, 1));
   fe *dfin = (fe *)ctx->buf(47, 16 * 3);
-  party_sumcheck_enqueue(form, dv, M, N, dw, offset, dst, scratch, partial, dpolys, dchal, dfin, ctx->stream);
+  fe *ddrawn = (fe *)ctx->buf(49, 16 * (uint64_t)std::max(rounds, 1));
+  party_sumcheck_enqueue(form, dv, M, N, dw, offset, dst, scratch, partial, dpolys, dchal, dfin, ddrawn,
+                         ctx->side_stream(), ctx->stream);
   if (rounds) {
     GBZ_CUDA(cudaMemcpyAsync(polys, dpolys, 16 * (uint64_t)nc * rounds, cudaMemcpyDeviceToHost, ctx->stream));
     GBZ_CUDA(cudaMemcpyAsync(challenges, dchal, 16 * (uint64_t)rounds, cudaMemcpyDeviceToHost, ctx->stream));

@@ -204,12 +204,34 @@ __device__ fe eval_poly(const fe *c, int nc, fe x) {
   return acc;
 }
 
-// Sums the partials into the round polynomial H (nc coefficients), checks
-// H(0) + H(1) against the running claim, draws the challenge (Fiat-Shamir
-// hash of the coefficients, or the fourth glibc draw for the leader's
-// rounds), and updates the claim.
-__global__ void form_finalize_kernel(const fe *partial, int blocks, int nc, RoundState *st, int round, int use_prng,
-                                     fe *polys, fe *chal) {
+// Thread-0 part of a round: checks H(0) + H(1) against the running claim y,
+// stores H, draws the challenge (Fiat-Shamir hash chain fs over the
+// coefficients, or the leader's glibc challenge drawn ahead of time by
+// prng_draw_kernel when drawn is set) and updates the claim.  The state is
+// passed by reference so that the one-CTA tail keeps it in registers.
+__device__ fe finish_round(const fe *H, int nc, fe &fs, fe &y, uint32_t &error, int round, const fe *drawn,
+                           fe *polys, fe *chal) {
+  // H(0) + H(1) = 2 c_last + sum of the other coefficients
+  fe s = H[nc - 1];
+  for (int k = 0; k < nc; k++) s = fadd(s, H[k]);
+  if (!fe_eq(s, y)) error |= 1u;
+  for (int k = 0; k < nc; k++) polys[(uint64_t)round * nc + k] = H[k];
+  fe ch;
+  if (drawn) {
+    ch = *drawn;
+  } else {
+    for (int k = 0; k < nc; k++) fs = hash_F(fs, H[k]);
+    ch = fs;
+  }
+  chal[round] = ch;
+  y = eval_poly(H, nc, ch);
+  return ch;
+}
+
+// Sums the partials into the round polynomial H (nc coefficients) and
+// finishes the round.
+__global__ void form_finalize_kernel(const fe *partial, int blocks, int nc, RoundState *st, int round,
+                                     const fe *drawn, fe *polys, fe *chal) {
   __shared__ fe red[4][kThreads];
   fe acc[4] = {fe_zero(), fe_zero(), fe_zero(), fe_zero()};
   for (int i = threadIdx.x; i < blocks; i += kThreads)
@@ -224,23 +246,125 @@ __global__ void form_finalize_kernel(const fe *partial, int blocks, int nc, Roun
   if (threadIdx.x) return;
   fe H[4];
   for (int k = 0; k < nc; k++) H[k] = red[k][0];
-  // H(0) + H(1) = 2 c_last + sum of the other coefficients
-  fe s = H[nc - 1];
-  for (int k = 0; k < nc; k++) s = fadd(s, H[k]);
-  if (!fe_eq(s, st->y)) st->error |= 1u;
-  for (int k = 0; k < nc; k++) polys[(uint64_t)round * nc + k] = H[k];
-  fe ch;
-  if (use_prng) {
-    __shared__ glibc_prng g;  // dynamically indexed table: work on a shared copy
-    g = st->prng;
+  fe fs = st->fs, y = st->y;
+  uint32_t error = st->error;
+  finish_round(H, nc, fs, y, error, round, drawn, polys, chal);
+  st->fs = fs;
+  st->y = y;
+  st->error = error;
+}
+
+// The leader's rounds take the fourth of every four F::_random() draws
+// (Distributed_Sumcheck.cpp); the glibc stream depends on nothing the rounds
+// compute, so its n challenges are drawn in one thread while the first,
+// largest rounds run, and the stream's final state goes back to st->prng.
+__global__ void prng_draw_kernel(RoundState *st, int n, fe *out) {
+  __shared__ glibc_prng g;  // dynamically indexed table: work on a shared copy
+  if (threadIdx.x) return;
+  g = st->prng;
+  for (int j = 0; j < n; j++) {
+    fe ch;
     for (int k = 0; k < 4; k++) ch = prng_field(g);
-    st->prng = g;
-  } else {
-    for (int k = 0; k < nc; k++) st->fs = hash_F(st->fs, H[k]);
-    ch = st->fs;
+    out[j] = ch;
   }
-  chal[round] = ch;
-  st->y = eval_poly(H, nc, ch);
+  st->prng = g;
+}
+
+constexpr int kTailThreads = 512;
+
+struct TailArgs {
+  const fe *in[3];  // entries entering round i0, before its fold
+  fe *buf[2][3];    // ping-pong outputs (buf[0] differs from in)
+  uint64_t cur;     // entries of every vector entering round i0
+  int i0, total, fs_rounds;
+  RoundState *st;
+  const fe *drawn;  // glibc challenges of rounds fs_rounds.. (or null)
+  fe *polys, *chal, *fin;
+};
+
+// Rounds i0..total-1 of the party sumcheck and the final fold in one CTA,
+// once the vectors are small: every round is the fused fold + message of
+// form_step_kernel<FORM, 1>, a block reduction and finish_round, with no
+// launch between rounds.
+template <int FORM>
+__global__ void __launch_bounds__(kTailThreads) form_tail_kernel(TailArgs t) {
+  constexpr int NV = Form<FORM>::NV, NC = Form<FORM>::NC;
+  __shared__ fe red[NC][kTailThreads / 32];
+  __shared__ fe sh_r;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const fe *in[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) in[k] = t.in[k];
+  fe r = t.chal[t.i0 - 1];
+  fe fs = fe_zero(), y = fe_zero();  // the running state, in thread 0's registers
+  uint32_t error = 0;
+  if (threadIdx.x == 0) {
+    fs = t.st->fs;
+    y = t.st->y;
+    error = t.st->error;
+  }
+  uint64_t cur = t.cur;
+  int pp = 0;
+  for (int i = t.i0; i < t.total; i++) {
+    fe acc[NC];
+#pragma unroll
+    for (int k = 0; k < NC; k++) acc[k] = fe_zero();
+    const uint64_t pairs = cur / 4;
+    for (uint64_t g = threadIdx.x; g < pairs; g += kTailThreads) {
+      fe xs[NV][4];
+#pragma unroll
+      for (int k = 0; k < NV; k++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) xs[k][q] = in[k][4 * g + q];
+      Line l[NV];
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        const fe f0 = fadd(xs[k][0], fmul(r, fsub(xs[k][1], xs[k][0])));
+        const fe f1 = fadd(xs[k][2], fmul(r, fsub(xs[k][3], xs[k][2])));
+        t.buf[pp][k][2 * g] = f0;
+        t.buf[pp][k][2 * g + 1] = f1;
+        l[k] = line(f0, f1);
+      }
+      accumulate<FORM>(l, fe_zero(), acc);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+      for (int k = 0; k < NC; k++) acc[k] = fadd(acc[k], shfl_down_fe(acc[k], d));
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < NC; k++) red[k][wid] = acc[k];
+    __syncthreads();  // also orders this round's stores before the next round's loads
+    if (wid == 0) {
+#pragma unroll
+      for (int k = 0; k < NC; k++) acc[k] = red[k][lane % (kTailThreads / 32)];
+      if (lane >= kTailThreads / 32)
+#pragma unroll
+        for (int k = 0; k < NC; k++) acc[k] = fe_zero();
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+        for (int k = 0; k < NC; k++) acc[k] = fadd(acc[k], shfl_down_fe(acc[k], d));
+      if (lane == 0)
+        sh_r = finish_round(acc, NC, fs, y, error, i,
+                            i >= t.fs_rounds && t.drawn ? t.drawn + (i - t.fs_rounds) : nullptr, t.polys, t.chal);
+    }
+    __syncthreads();
+    r = sh_r;
+#pragma unroll
+    for (int k = 0; k < NV; k++) in[k] = t.buf[pp][k];
+    pp ^= 1;
+    cur /= 2;
+  }
+  if (threadIdx.x == 0) {
+    t.st->fs = fs;
+    t.st->y = y;
+    t.st->error = error;
+  }
+  // final fold of the last length-2 vectors: the leader's v[0] values
+#pragma unroll
+  for (int k = 0; k < NV; k++)
+    if ((int)threadIdx.x == k) t.fin[k] = fadd(in[k][0], fmul(r, fsub(in[k][1], in[k][0])));
 }
 
 __global__ void form_sum_kernel(const fe *partial, int blocks, int nc, fe *out) {
@@ -318,9 +442,9 @@ void form_sum_launch(const fe *partial, int blocks, int nc, fe *out, cudaStream_
   GBZ_CUDA(cudaGetLastError());
 }
 
-void form_finalize_launch(const fe *partial, int blocks, int nc, RoundState *st, int round, bool use_prng, fe *polys,
+void form_finalize_launch(const fe *partial, int blocks, int nc, RoundState *st, int round, const fe *drawn, fe *polys,
                           fe *chal, cudaStream_t s) {
-  form_finalize_kernel<<<1, kThreads, 0, s>>>(partial, blocks, nc, st, round, use_prng ? 1 : 0, polys, chal);
+  form_finalize_kernel<<<1, kThreads, 0, s>>>(partial, blocks, nc, st, round, drawn, polys, chal);
   GBZ_CUDA(cudaGetLastError());
 }
 
@@ -341,7 +465,8 @@ int party_sumcheck_rounds(uint64_t M, int N, int offset, int *fs_rounds) {
 }
 
 void party_sumcheck_enqueue(int form, const fe *const *v, uint64_t M, int N, const fe *w, int offset, RoundState *st,
-                            fe *const *scratch, fe *partial, fe *polys, fe *chal, fe *fin, cudaStream_t s) {
+                            fe *const *scratch, fe *partial, fe *polys, fe *chal, fe *fin, fe *drawn,
+                            const SideStream &side, cudaStream_t s) {
   // The N parties' vectors are held party-major, so pair g of the
   // concatenation is pair g mod (cur/2) of party g / (cur/2) while every
   // party still has two entries or more: the parties' round polynomials
@@ -365,6 +490,26 @@ void party_sumcheck_enqueue(int form, const fe *const *v, uint64_t M, int N, con
     form_first_launch(a, nv, fin, s);
     return;
   }
+  // the leader's glibc challenges, drawn on the side stream while the first
+  // rounds run; the stream joins before the first round that takes one
+  const bool glibc = total > fs_rounds;
+  if (glibc) {
+    cudaStream_t ds = side.stream ? side.stream : s;
+    if (side.stream) {
+      GBZ_CUDA(cudaEventRecord(side.fork, s));
+      GBZ_CUDA(cudaStreamWaitEvent(side.stream, side.fork, 0));
+    }
+    prng_draw_kernel<<<1, 32, 0, ds>>>(st, total - fs_rounds, drawn);
+    GBZ_CUDA(cudaGetLastError());
+    if (side.stream) GBZ_CUDA(cudaEventRecord(side.join, side.stream));
+  }
+  bool joined = !glibc || !side.stream;
+  auto join = [&](int upto) {  // before a launch that finishes rounds up to upto
+    if (!joined && upto >= fs_rounds) {
+      GBZ_CUDA(cudaStreamWaitEvent(s, side.join, 0));
+      joined = true;
+    }
+  };
   int pp = 0;
   for (int i = 0; i < total; i++) {
     int blocks;
@@ -373,6 +518,29 @@ void party_sumcheck_enqueue(int form, const fe *const *v, uint64_t M, int N, con
       blocks = round_blocks(a.pairs);
       form_step_launch(form, a, 0, blocks, s);
     } else {
+      if (i >= 2 && cur <= kTailEntries) {
+        // the remaining rounds and the final fold in one CTA
+        TailArgs t{};
+        for (int k = 0; k < nv; k++) {
+          t.in[k] = a.in[k];
+          t.buf[0][k] = scratch[pp * 6 + k];
+          t.buf[1][k] = scratch[(pp ^ 1) * 6 + k];
+        }
+        t.cur = cur;
+        t.i0 = i;
+        t.total = total;
+        t.fs_rounds = fs_rounds;
+        t.st = st;
+        t.drawn = glibc ? drawn : nullptr;
+        t.polys = polys;
+        t.chal = chal;
+        t.fin = fin;
+        join(total - 1);
+        if (form == SC_QUADRATIC) form_tail_kernel<SC_QUADRATIC><<<1, kTailThreads, 0, s>>>(t);
+        else form_tail_kernel<SC_CUBIC><<<1, kTailThreads, 0, s>>>(t);
+        GBZ_CUDA(cudaGetLastError());
+        return;
+      }
       // fold by the previous challenge into scratch[pp], message of the result
       a.pairs = cur / 4;
       a.r = chal + (i - 1);
@@ -384,7 +552,9 @@ void party_sumcheck_enqueue(int form, const fe *const *v, uint64_t M, int N, con
       pp ^= 1;
       cur /= 2;
     }
-    form_finalize_launch(partial, blocks, nc, st, i, i >= fs_rounds, polys, chal, s);
+    join(i);
+    form_finalize_launch(partial, blocks, nc, st, i, i >= fs_rounds ? drawn + (i - fs_rounds) : nullptr, polys, chal,
+                         s);
   }
   // final fold of the last length-2 vectors: the leader's v[0] values
   a.pairs = 1;

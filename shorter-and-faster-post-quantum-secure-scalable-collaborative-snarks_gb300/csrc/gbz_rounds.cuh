@@ -46,7 +46,18 @@ int party_sumcheck_rounds(uint64_t M, int N, int offset, int *fs_rounds);
 // chain / generator / claim, scratch 12 buffers of N*M/2 entries (two sets
 // of six), partial round_blocks(N*M/2) * 4 entries; polys, chal and fin
 // receive the round polynomials, challenges and the leader's final values.
+// A second stream and two events (fork, join) for work that runs beside
+// the rounds; a null stream runs it in line.
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+// Entries per vector from which the party sumcheck runs its remaining
+// rounds in one CTA.
+constexpr uint64_t kTailEntries = 1u << 14;
+// drawn: room for one challenge per glibc round (rounds minus FS rounds).
 void party_sumcheck_enqueue(int form, const fe *const *v, uint64_t M, int N, const fe *w, int offset, RoundState *st,
-                            fe *const *scratch, fe *partial, fe *polys, fe *chal, fe *fin, cudaStream_t s);
+                            fe *const *scratch, fe *partial, fe *polys, fe *chal, fe *fin, fe *drawn,
+                            const SideStream &side, cudaStream_t s);
 
 }  // namespace gbz
