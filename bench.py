@@ -72,7 +72,7 @@ CONFIG = {
     "l2": "inputs larger than L2 (witness 256 MiB, codeword 512 MiB per step)",
 }
 
-# Algorithmic bytes per proof by kernel category (roofline).
+# Algorithmic bytes per proof by kernel category: what each category must read and write at least.
 def algorithmic_bytes(logn, rate):
     n, L = 1 << logn, (1 << logn) * rate
     out = {}
@@ -286,7 +286,7 @@ def run_reference_arm(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "proofs/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (F_{p^2}, p=2^61-1)",
-        "data": "synthetic", "config": CONFIG,
+        "data": "synthetic", "config": dict(CONFIG, parallelism="replicas%d" % args.gpus),
         "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
         "cpu_baseline": {"value": value, "unit": "proofs/s", "cores": cores, "kind": "port",
                          "sample": "full proofs of the same workload (oracle/gbz_oracle.c, pthreads)"},

@@ -942,18 +942,16 @@ void orc_column_merkle(const uint64_t *rows, int nrows, int logL, int N, uint8_t
   memcpy(root_out, cur, 32);
 }
 
-void orc_secret_shares(const uint64_t *v, int64_t M, int N, int privacy, uint32_t prng_seed, uint64_t *shares) {
+void orc_secret_shares_g(const uint64_t *v, int64_t M, int N, int privacy, orc_prng *g, uint64_t *shares) {
   int k = N / 4, kk = N / 2;
   int64_t groups = M / k;
-  orc_prng g;
-  orc_prng_seed(&g, prng_seed);
   uint64_t buff[2 * 1024];
   int lk = ilog2_64(kk), l2n = ilog2_64(2 * N);
   for (int64_t i = 0; i < groups; i++) {
     memset(buff, 0, sizeof(uint64_t) * 2 * 2 * N);
     for (int j = 0; j < k; j++) { buff[2 * j] = v[2 * (i * k + j)]; buff[2 * j + 1] = v[2 * (i * k + j) + 1]; }
     for (int j = k; j < kk; j++)
-      if (privacy) { buff[2 * j] = (uint64_t)orc_prng_next(&g); buff[2 * j + 1] = 0; } /* F(random()) */
+      if (privacy) { buff[2 * j] = (uint64_t)orc_prng_next(g); buff[2 * j + 1] = 0; } /* F(random()) */
     orc_fft(buff, lk, 1, 1);
     orc_fft(buff, l2n, 0, 1);  /* buff is zero beyond kk */
     for (int j = 0; j < N; j++) {
@@ -961,6 +959,33 @@ void orc_secret_shares(const uint64_t *v, int64_t M, int N, int privacy, uint32_
       shares[2 * (j * groups + i) + 1] = buff[2 * (2 * j + 1) + 1];
     }
   }
+}
+
+void orc_secret_shares(const uint64_t *v, int64_t M, int N, int privacy, uint32_t prng_seed, uint64_t *shares) {
+  orc_prng g;
+  orc_prng_seed(&g, prng_seed);
+  orc_secret_shares_g(v, M, N, privacy, &g, shares);
+}
+
+void orc_generate_randomness(orc_prng *g, int64_t n, uint64_t *out) {
+  uint64_t c = 0;
+  for (int64_t i = 0; i < n; i++) {
+    if (i % 100 == 0) c = (uint64_t)orc_prng_next(g); /* c = random() */
+    out[2 * i] = c + (uint64_t)orc_prng_next(g);       /* c + F(rand()): both below 2^31 */
+    out[2 * i + 1] = 0;
+  }
+}
+
+void orc_copcs_party_shares(int N, int64_t M, int64_t R, uint64_t *shares, uint64_t *random) {
+  orc_prng g;
+  orc_prng_seed(&g, 1); /* glibc's default state: the reference never seeds rank 0's generator */
+  int64_t n = M > R ? M : R;
+  uint64_t *buf = (uint64_t *)malloc(sizeof(uint64_t) * 2 * (size_t)(n ? n : 1));
+  orc_generate_randomness(&g, M, buf);
+  orc_secret_shares_g(buf, M, N, 1, &g, shares);
+  orc_generate_randomness(&g, R, buf);
+  orc_secret_shares_g(buf, R, N, 1, &g, random);
+  free(buf);
 }
 
 /* unpack_secret_share (MPI_utils.cpp:2769-2785) with _k = k = N */

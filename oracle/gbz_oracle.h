@@ -112,6 +112,19 @@ void orc_column_merkle(const uint64_t *rows, int nrows, int logL, int N, uint8_t
  * shares[j][i] for party j and group i; with privacy the slots k.._k-1 of
  * each group take random() from the glibc stream seeded with prng_seed. */
 void orc_secret_shares(const uint64_t *v, int64_t M, int N, int privacy, uint32_t prng_seed, uint64_t *shares);
+/* The same, drawing the random slots from a generator the caller holds. */
+void orc_secret_shares_g(const uint64_t *v, int64_t M, int N, int privacy, orc_prng *g, uint64_t *shares);
+
+/* generate_randomness (utils.cpp:1285-1295): x_i = c + F(rand()) with c =
+ * F(random()) refreshed every 100 entries, from the caller's generator. */
+void orc_generate_randomness(orc_prng *g, int64_t n, uint64_t *out);
+
+/* The party shares of the reference's coPCS test (main.cpp:49-68): rank 0
+ * draws, from glibc's default seed, secret_share_coefficients of M values
+ * and then of R random values (MPI_utils.cpp:2787-2810), each as
+ * generate_randomness + compute_secret_shares with privacy.  shares is
+ * N x (M / (N/4)), random N x (R / (N/4)), party-major. */
+void orc_copcs_party_shares(int N, int64_t M, int64_t R, uint64_t *shares, uint64_t *random);
 
 /* sumcheck_aggr leader computation (MPI_utils.cpp:2631-2644): msgs is N
  * party messages of len elements; b has N/4 weights. */

@@ -286,6 +286,16 @@ def secret_shares(v, N, privacy=False, prng_seed=1):
     return out
 
 
+def copcs_party_shares(N, M, R):
+    """Party shares of the reference's coPCS test (main.cpp:49-68) at N
+    parties: (shares N x 4M/N, random N x 4R/N), rank 0's glibc draws."""
+    k = N // 4
+    sh = np.zeros((N, M // k, 2), dtype=np.uint64)
+    rn = np.zeros((N, R // k, 2), dtype=np.uint64)
+    lib().orc_copcs_party_shares(ctypes.c_int(N), ctypes.c_int64(M), ctypes.c_int64(R), _p64(sh), _p64(rn))
+    return sh, rn
+
+
 def party_aggregate(msgs, b):
     msgs = np.ascontiguousarray(msgs, dtype=np.uint64)
     N, length = msgs.shape[0], msgs.shape[1]

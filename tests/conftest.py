@@ -17,7 +17,7 @@ PKG = os.path.join(ROOT, "shorter-and-faster-post-quantum-secure-scalable-collab
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
-for p in (PKG, ORACLE_DIR):
+for p in (PKG, ORACLE_DIR, ROOT):
     if p not in sys.path:
         sys.path.insert(0, p)
 

@@ -22,6 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 FULL = os.path.join(ROOT, "oracle", "_ref", "ref_full")
+PIGEON = os.path.join(ROOT, "oracle", "_ref", "pigeon_mpi")
 
 # Witness seeds: 0x5EED0000 + workload * 2^16 + instance (1: n = 2^18 at rate 1/4, 2: n = 2^24 at rate 1/2).
 SEED_2E18 = 0x5EED0000 + 1 * 65536
@@ -58,6 +59,8 @@ def main():
             manifest["sumcheck"] = gen_sumcheck()
         if "batchopen" in only:
             manifest["batchopen"] = gen_batchopen()
+        if "parties" in only:
+            manifest["parties"] = gen_parties()
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
             json.dump(manifest, f, indent=1)
         print("updated", sorted(only))
@@ -138,6 +141,7 @@ def main():
     manifest["copcs"] = gen_copcs()
     manifest["sumcheck"] = gen_sumcheck()
     manifest["batchopen"] = gen_batchopen()
+    manifest["parties"] = gen_parties()
 
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
@@ -218,6 +222,89 @@ def gen_batchopen():
             save(name + ".bin", data)
             e["file"] = name + ".bin"
         out[name] = e
+    return out
+
+
+# ------------------------------------------------------------ N-party runs
+# Per-rank capture records written by oracle/ref/minimpi/capture.cpp: tag,
+# count, then count units of these sizes.
+CAPTURE_UNIT = {"H2FI": 16, "H2FO": 16, "FRND": 16, "SHRS": 16, "PAGI": 16, "PAGO": 16, "SPDA": 16, "SPDB": 16,
+                "SPDC": 16, "WCIA": 16, "FIPK": 16, "GSYI": 16, "GSYO": 16, "GSSG": 16,
+                "GIDX": 4, "RAND": 4, "GSQU": 4, "MTCB": 36, "CTRB": 36, "WCIR": 36}
+
+
+def capture_records(path):
+    import struct
+    b = open(path, "rb").read()
+    o, out = 0, []
+    while o < len(b):
+        tag = b[o:o + 4].decode()
+        cnt = struct.unpack_from("<I", b, o + 4)[0]
+        o += 8
+        n = cnt * CAPTURE_UNIT[tag]
+        out.append((tag, cnt, b[o:o + n]))
+        o += n
+    return out
+
+
+def gen_parties():
+    """The reference's own coPCS test (main.cpp:49-163: PCS_commit then
+    PCS_open_new) run unmodified with N ranks as N processes (pigeon_mpi,
+    minimpi), each rank's transcript captured by link-time interposition.
+    Kept per case: what every rank computed that the one-device party
+    pipeline must reproduce (full values where small, SHA-256 otherwise)."""
+    import struct
+    import tempfile
+    out = {}
+    for N, logM in ((4, 14), (16, 16), (8, 19)):
+        with tempfile.TemporaryDirectory() as td:
+            prefix = os.path.join(td, "cap")
+            env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_CAPTURE=prefix, MINIMPI_TIMEOUT="300")
+            t = time.time()
+            log = subprocess.run([PIGEON, "0", str(logM)], env=env, check=True, capture_output=True, text=True)
+            dt = time.time() - t
+            ranks = [capture_records("%s.%d" % (prefix, r)) for r in range(N)]
+        sha = lambda b: hashlib.sha256(b).hexdigest()
+        hx = lambda b: b.hex()
+        lead = ranks[0]
+        npoint = logM + 1
+        h2fo = [r[2] for r in lead if r[0] == "H2FO"]
+        case = {"N": N, "logM": logM, "rates": [[4], [4], [4, 4], [4, 4]], "ref_seconds": round(dt, 2),
+                "stdout": log.stdout.strip().splitlines(),
+                "K": hx([r[2] for r in lead if r[0] == "FIPK"][0]),
+                "point_len": npoint,
+                "challenges": [hx(x) for x in h2fo[npoint:]],
+                "polys": [hx(r[2]) for r in lead if r[0] == "PAGO"],
+                "y": [hx(r[2]) for r in lead if r[0] == "GSYO"],
+                "segments_sha256": [sha(r[2]) for r in lead if r[0] == "GSSG"],
+                "ranks": []}
+        small = N * (1 << logM) <= (1 << 20)
+        for rk, recs in enumerate(ranks):
+            sh = [r[2] for r in recs if r[0] == "SHRS"]
+            ctrb = [r[2] for r in recs if r[0] == "CTRB"]
+            # commit roots of the opening: MT_commit_Blake calls other than the
+            # per-column ones (32 or 8 entries) and the leader's WHIR commitment
+            # of the gathered segments (the call right after a WCIA record)
+            big_roots = [r[2] for i, r in enumerate(recs) if r[0] == "MTCB"
+                         and struct.unpack_from("<I", r[2])[0] not in (32, 8) and recs[i - 1][0] != "WCIA"]
+            gidx = []
+            for r in recs:
+                if r[0] == "GIDX":
+                    w = struct.unpack("<%dI" % r[1], r[2])
+                    gidx.append(list(w[5::2]))
+            e = {"shares_sha256": [sha(x) for x in sh],
+                 "base_root": hx(ctrb[0][4:]),
+                 "tree_roots": [hx(x[4:]) + ":%d" % struct.unpack_from("<I", x)[0] for x in ctrb],
+                 "commit_roots": [hx(x[4:]) + ":%d" % struct.unpack_from("<I", x)[0] for x in big_roots[:3]],
+                 "party_polys": [hx(r[2]) for r in recs if r[0] == "PAGI"],
+                 "queries": gidx if small else [sha(str(g).encode()) for g in gidx],
+                 "final": [(hx if small else sha)(r[2]) for r in recs if r[0] in ("SPDA", "SPDB", "SPDC")]}
+            case["ranks"].append(e)
+        name = "parties_N%d_M%d" % (N, logM)
+        with open(os.path.join(HERE, name + ".json"), "w") as f:
+            json.dump(case, f, indent=0)
+        out[name] = {"file": name + ".json", "N": N, "logM": logM}
+        print("parties N=%d M=2^%d: reference %.1f s" % (N, logM, dt), flush=True)
     return out
 
 

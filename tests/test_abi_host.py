@@ -121,9 +121,9 @@ def test_reference_shim_compiles_against_reference_headers(gbz):
     """host/gbz_reference_shim.cpp keeps the reference's signatures; it must
     compile against the reference's own headers (x86-64 only: they need
     immintrin.h)."""
-    import platform
-    ref = os.environ.get("GBZ_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src")) or platform.machine() not in ("x86_64", "AMD64"):
+    import __graft_entry__
+    ref = __graft_entry__.reference_dir()
+    if not ref:
         pytest.skip("reference checkout not available here")
     import conftest
     shim = os.path.join(conftest.PKG, "host", "gbz_reference_shim.cpp")
