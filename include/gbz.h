@@ -431,6 +431,80 @@ gbz_status gbz_tensor_eval_vector(gbz_ctx *ctx, const uint32_t *point, int cols,
 gbz_status gbz_pcs_sumcheck_phase3(gbz_ctx *ctx, uint64_t *B, uint64_t rows, const uint32_t *queries, int l,
                                    const uint64_t *s, int N, int rate, int my_id, int mem);
 
+/* ------------------------------------------- collaborative PCS, N parties */
+
+/* The collaborative PCS of N parties on one device (N = 4..64, a power of
+ * two): the reference runs it with one MPI rank per party; here every
+ * party's share is a row of one party-major device array and the leader's
+ * aggregation runs on the device.
+ *
+ * rate0[i] = rates[i][0] and rate1[i] = rates[i][1] (0 where absent) of the
+ * reference's `rates` (e.g. {{4},{4},{4,4},{4,4}}, main.cpp:54), rounds =
+ * rates.size(); M = the number of shared coefficients (a power of two).
+ *
+ * gbz_pcs_schedule: prepare_parameters (coPCS.cpp:38-72; get_degrees /
+ * get_queries, New_PCS.cpp:23-77): the folding degrees and query counts of
+ * every round, and the random shares each party holds (randomness of
+ * coPCS.cpp:53-55; secret_share_coefficients deals randomness * N / 4
+ * values, main.cpp:68).  No GPU.
+ * replaces prepare_parameters (coPCS.cpp:38-72). */
+gbz_status gbz_pcs_schedule(int N, uint64_t M, int rounds, const int *rate0, const int *rate1, int *degrees,
+                            int *queries, uint64_t *random_per_party);
+
+typedef struct gbz_pcs gbz_pcs;
+
+/* PCS_commit of every party: prepare_data (coPCS.cpp:76-129), Encode
+ * (:131-147) and distributed_MT (:152-230).  shares: N x (4M/N) elements,
+ * random: N x random_per_party elements, party-major.  *out receives the
+ * commitment (device memory held until gbz_pcs_free); party_roots (N x 32 B)
+ * and leader_root (32 B; the leader's tree over {root_0, 0, ..., 0}) may be
+ * NULL.
+ * replaces PCS_commit (coPCS.cpp:236-250) on N ranks. */
+gbz_status gbz_pcs_commit(gbz_ctx *ctx, int N, uint64_t M, int rounds, const int *rate0, const int *rate1,
+                          const uint64_t *shares, const uint64_t *random, int mem, gbz_pcs **out,
+                          uint8_t *party_roots, uint8_t *leader_root);
+void gbz_pcs_free(gbz_pcs *pcs);
+/* Shape of a commitment: Commit_data rows with entries (batches), their
+ * length, the codeword length, and the transcript bytes of gbz_pcs_open. */
+gbz_status gbz_pcs_info(const gbz_pcs *pcs, int *batches, uint64_t *row_len, uint64_t *codeword_len,
+                        uint64_t *open_transcript_bytes);
+/* One party's Commit_data rows (batches x row_len), codewords (batches x
+ * codeword_len) and column-root tree (2 codeword_len - 1 hashes); any
+ * output may be NULL. */
+gbz_status gbz_pcs_commit_data(gbz_ctx *ctx, const gbz_pcs *pcs, int party, uint64_t *rows, uint64_t *codewords,
+                               uint8_t *levels, int mem);
+
+/* The parties' side of PCS_open_new with the leader's aggregation
+ * (coPCS.cpp:1310-1607, isPIOP = false): row batching and the batching
+ * round, batch_commitments_new (:1242-1308), per round pcs_sumcheck_phase1
+ * (aggregated as pcs_sumcheck_aggr does, MPI_utils.cpp:341-405), the
+ * leader's check and Fiat-Shamir challenge, pcs_sumcheck_phase2,
+ * encode_concatenated + commit_concatenated or RS_multifold5 +
+ * commit_tensorcode, delegate_checks' queries, folded answers and segment
+ * gather (:740-891), and pcs_sumcheck_phase3 (:634-648).
+ * r: the opening point, log2(N/4) + 5 + log2(row_len) elements; K: the
+ * claim (F_ip, MPI_utils.cpp:483); fs: the Fiat-Shamir chain value
+ * (prev_challenge) before the opening, updated in place.  The leader's
+ * delegation proofs and WHIR opening of the gathered segments follow in the
+ * reference and are not part of this call.  The commitment's device state
+ * is read, not changed: a commitment can be opened again.
+ * Transcript records {u32 tag, u32 count, payload}:
+ *   34 PARTY_POLYS 16B x 3N | 35 POLY 16B x3 | 36 CHALLENGE 16B | 41 K 16B |
+ *   32 ROOTS 32B x N | 33 LEADER_ROOT 32B | 37 QUERIES u32 x 2 l0
+ *   per round: 34 PARTY_POLYS 16B x 2dN, 35 POLY 16B x 2d, 36 CHALLENGE,
+ *     32 ROOTS, 33 LEADER_ROOT, 37 QUERIES u32 x 2l ((party, position)
+ *     pairs, party by party as the leader holds them), 38 Y 16B x l,
+ *     39 SEGMENTS 16B x l d, 40 S 16B, 41 K 16B
+ *   42 FINAL 16B x N (data, B, C') per party (send_pcs_data)
+ * The reference's quirk that commit_tensorcode reports the previous
+ * commitment's root (it reuses a deeper levels vector) is kept.
+ * GBZ_ECHECK when a round message does not match the claim or a delegate
+ * check fails.
+ * replaces PCS_open_new (coPCS.cpp:1310-1607) on N ranks, up to the leader's
+ * delegation. */
+gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
+                        uint8_t *transcript, uint64_t capacity, int mem);
+
 /* --------------------------------------------------------------- prover */
 
 /* Bytes of the transcript of one proof of a 2^logn witness at `rate`. */

@@ -8,6 +8,7 @@
 #include <utility>
 
 #include "../../include/gbz.h"
+#include "gbz_ctx.cuh"
 #include "gbz_batch_open.cuh"
 #include "gbz_copcs.cuh"
 #include "gbz_prover.cuh"
@@ -17,114 +18,9 @@
 
 using namespace gbz;
 
-struct gbz_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  std::string last_error;
-  std::map<int, std::pair<void *, uint64_t>> scratch;
-  std::map<int, NttTables> ntt;
-  std::map<std::pair<int, int>, std::unique_ptr<ProofPlan>> plans;
-  ProofState *st = nullptr;
-  fe *ub_scratch = nullptr;
-  bool profiling = false;
-  std::map<std::pair<int, int>, std::unique_ptr<Profiler>> profilers;
-  std::unique_ptr<Scheduler> sched;
-  bool graphs = true;  // gbz_prove replays captured graphs (gbz_set_graphs)
-  SideStream side;     // second stream of the party sumcheck (created on first use)
-
-  const SideStream &side_stream() {
-    if (!side.stream) {
-      GBZ_CUDA(cudaStreamCreateWithFlags(&side.stream, cudaStreamNonBlocking));
-      GBZ_CUDA(cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming));
-      GBZ_CUDA(cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming));
-    }
-    return side;
-  }
-
-  void *buf(int slot, uint64_t bytes) {
-    auto &e = scratch[slot];
-    if (e.second < bytes) {
-      if (e.first) GBZ_CUDA(cudaFree(e.first));
-      e.first = nullptr;
-      e.second = 0;
-      GBZ_CUDA(cudaMalloc(&e.first, bytes ? bytes : 16));
-      e.second = bytes;
-    }
-    return e.first;
-  }
-  NttTables &tables(int lg) {
-    auto it = ntt.find(lg);
-    if (it != ntt.end()) return it->second;
-    NttTables t;
-    ntt_tables_build(t, lg);
-    return ntt.emplace(lg, t).first->second;
-  }
-};
+using namespace gbz_api;
 
 namespace {
-
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) GBZ_CUDA(cudaSetDevice(dev));
-  }
-  ~DeviceGuard() {
-    int cur;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-  }
-};
-
-gbz_status fail(gbz_ctx *ctx, gbz_status code, const std::string &msg) {
-  if (ctx) ctx->last_error = msg;
-  return code;
-}
-
-#define API_BEGIN(ctx)                                    \
-  if (!(ctx)) return GBZ_EINVAL;                          \
-  try {                                                   \
-    DeviceGuard guard_((ctx)->device);
-#define API_END(ctx)                                                                    \
-  }                                                                                     \
-  catch (const ArgError &e) {                                                           \
-    return fail(ctx, GBZ_EINVAL, e.what);                                               \
-  }                                                                                     \
-  catch (const CudaError &e) {                                                          \
-    return fail(ctx, e.err == cudaErrorMemoryAllocation ? GBZ_ENOMEM : GBZ_ECUDA, e.what); \
-  }                                                                                     \
-  catch (const std::bad_alloc &) {                                                      \
-    return fail(ctx, GBZ_ENOMEM, "host allocation failed");                              \
-  }                                                                                     \
-  return GBZ_OK;
-
-void check_mem(int mem) {
-  if (mem != GBZ_MEM_HOST && mem != GBZ_MEM_DEVICE) throw ArgError("mem must be GBZ_MEM_HOST or GBZ_MEM_DEVICE");
-}
-void need(const void *p, const char *what) {
-  if (!p) throw ArgError(std::string("null pointer: ") + what);
-}
-void check_pow2(uint64_t n, const char *what) {
-  if (!is_pow2(n)) throw ArgError(std::string(what) + " must be a power of two");
-}
-
-// Device view of a caller buffer: the pointer itself (device memory) or a
-// scratch copy (host memory), copied in when `in`.
-template <typename T>
-T *dev_view(gbz_ctx *ctx, int slot, T *p, uint64_t bytes, int mem, bool in) {
-  if (mem == GBZ_MEM_DEVICE) return p;
-  T *d = (T *)ctx->buf(slot, bytes);
-  if (in && bytes) GBZ_CUDA(cudaMemcpyAsync((void *)d, (const void *)p, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  return d;
-}
-template <typename T>
-void copy_out(gbz_ctx *ctx, T *host, const T *dev, uint64_t bytes, int mem) {
-  if (mem == GBZ_MEM_DEVICE || !bytes) return;
-  GBZ_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-}
-void finish(gbz_ctx *ctx, int mem) {
-  if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
-}
 
 __global__ void field_ops_kernel(const fe *a, const fe *b, uint64_t n, fe *s, fe *d, fe *p) {
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -223,6 +119,40 @@ static void check_tensor_shape(int cols, uint64_t rows, int rate, int my_id) {
   if (!is_pow2(rows) || ilog2(rows * (uint64_t)rate) > kMaxLogN)
     throw ArgError("tensor: rows * rate must be a power of two <= 2^28");
 }
+
+namespace gbz_api {
+
+void encode_rows_device(gbz_ctx *ctx, const fe *drows, int nrows, int logrow, int rate, int log_rate_offset,
+                        fe *dout) {
+  const uint64_t n = 1ull << logrow, L = n * (uint64_t)rate;
+  const NttTables &tn = ctx->tables(logrow), &tL = ctx->tables(ilog2(L));
+  const NttTables &tw = ctx->tables(1 + log_rate_offset + logrow);
+  // every row's inverse transform, coset shift and forward transform, the
+  // rows side by side in each launch (chunks of up to 2^28 elements of
+  // intermediate)
+  const int chunk = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)nrows, (1ull << 28) / L));
+  fe *tmp = (fe *)ctx->buf(2, 16 * L * (uint64_t)chunk);
+  for (int r0 = 0; r0 < nrows; r0 += chunk) {
+    const int rc = std::min(chunk, nrows - r0);
+    fe *o = dout + L * (uint64_t)r0;
+    const fe *x = drows + n * (uint64_t)r0;
+    ntt_launch_rows(tn, x, n, n, o, L, rc, tmp, true, ctx->stream);
+    coset_launch(o, n, tw, ctx->stream, rc, L);
+    if (rate == 2 && log_rate_offset == 0 && n >= 2) {
+      // The codeword is the interpolant P of the row on <w_n> evaluated at
+      // w_2n^(m - 1): odd m give P(w_n^((m-1)/2)) = x[(m-1)/2], the row
+      // itself, and even m the length-n transform of the shifted
+      // coefficients (the same values as the zero-padded length-2n
+      // transform, at half its cost).
+      ntt_launch_rows(tn, o, n, L, o, L, rc, tmp, false, ctx->stream, 2);
+      strided_copy_launch(x, n, o, L, 2, 1, rc, ctx->stream);
+    } else {
+      ntt_launch_rows(tL, o, n, L, o, L, rc, tmp, false, ctx->stream);
+    }
+  }
+}
+
+}  // namespace gbz_api
 
 extern "C" {
 
@@ -667,31 +597,7 @@ gbz_status gbz_encode_rows(gbz_ctx *ctx, const uint64_t *rows, int nrows, int lo
   if (!nrows) return GBZ_OK;
   const fe *drows = dev_view(ctx, 0, (const fe *)rows, 16 * n * nrows, mem, true);
   fe *dout = dev_view(ctx, 1, (fe *)out, 16 * L * nrows, mem, false);
-  const NttTables &tn = ctx->tables(logrow), &tL = ctx->tables(ilog2(L));
-  const NttTables &tw = ctx->tables(1 + log_rate_offset + logrow);
-  // every row's inverse transform, coset shift and forward transform, the
-  // rows side by side in each launch (chunks of up to 2^28 elements of
-  // intermediate)
-  const int chunk = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)nrows, (1ull << 28) / L));
-  fe *tmp = (fe *)ctx->buf(2, 16 * L * (uint64_t)chunk);
-  for (int r0 = 0; r0 < nrows; r0 += chunk) {
-    const int rc = std::min(chunk, nrows - r0);
-    fe *o = dout + L * (uint64_t)r0;
-    const fe *x = drows + n * (uint64_t)r0;
-    ntt_launch_rows(tn, x, n, n, o, L, rc, tmp, true, ctx->stream);
-    coset_launch(o, n, tw, ctx->stream, rc, L);
-    if (rate == 2 && log_rate_offset == 0 && n >= 2) {
-      // The codeword is the interpolant P of the row on <w_n> evaluated at
-      // w_2n^(m - 1): odd m give P(w_n^((m-1)/2)) = x[(m-1)/2], the row
-      // itself, and even m the length-n transform of the shifted
-      // coefficients (the same values as the zero-padded length-2n
-      // transform, at half its cost).
-      ntt_launch_rows(tn, o, n, L, o, L, rc, tmp, false, ctx->stream, 2);
-      strided_copy_launch(x, n, o, L, 2, 1, rc, ctx->stream);
-    } else {
-      ntt_launch_rows(tL, o, n, L, o, L, rc, tmp, false, ctx->stream);
-    }
-  }
+  encode_rows_device(ctx, drows, nrows, logrow, rate, log_rate_offset, dout);
   copy_out(ctx, (fe *)out, dout, 16 * L * nrows, mem);
   finish(ctx, mem);
   API_END(ctx)

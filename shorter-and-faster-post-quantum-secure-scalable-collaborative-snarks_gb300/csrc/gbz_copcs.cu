@@ -258,15 +258,12 @@ std::vector<fe> shamir_share_matrix(int N) {
   return mu;
 }
 
-std::vector<fe> aggregate_weights(int N, const fe *b) {
-  // sumcheck_aggr (MPI_utils.cpp:2631-2644): per coefficient the N shares s
-  // are unpacked (unpack_secret_share with _k = k = N: E = DFT(D IDFT(s)),
-  // D = diag(omega_{2N}^{-i})) and combined as sum_{j < N/4} b_j E[2j] =
-  // g^T E with g[2j] = b_j.  Both transform matrices are symmetric, so the
-  // weights of the shares are lambda = IDFT(D DFT(g)).
+std::vector<fe> aggregate_weights_even(int N, const std::vector<fe> &g) {
+  // Per coefficient the N shares s are unpacked (unpack_secret_share with
+  // _k = k = N, MPI_utils.cpp:2769-2785: E = DFT(D IDFT(s)), D =
+  // diag(omega_{2N}^{-i})) and combined as g^T E.  Both transform matrices
+  // are symmetric, so the weights of the shares are lambda = IDFT(D DFT(g)).
   const int lg = ilog2(N);
-  std::vector<fe> g(N, fe_zero());
-  for (int j = 0; j < N / 4; j++) g[2 * j] = b[j];
   std::vector<fe> h = host_dft(g, root_of_unity(lg));
   const fe w2n_inv = finv(root_of_unity(1 + lg));
   fe mul = fe_one();
@@ -275,6 +272,13 @@ std::vector<fe> aggregate_weights(int N, const fe *b) {
     mul = fmul(w2n_inv, mul);
   }
   return host_idft(h);
+}
+
+std::vector<fe> aggregate_weights(int N, const fe *b) {
+  // sumcheck_aggr (MPI_utils.cpp:2631-2644): sum_{j < N/4} b_j E[2j], g[2j] = b_j.
+  std::vector<fe> g(N, fe_zero());
+  for (int j = 0; j < N / 4; j++) g[2 * j] = b[j];
+  return aggregate_weights_even(N, g);
 }
 
 void multifold5_launch(const fe *cw, uint64_t n, const fe *a, int logd, fe *out, const NttTables &tn,

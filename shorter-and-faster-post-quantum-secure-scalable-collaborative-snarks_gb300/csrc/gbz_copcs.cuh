@@ -26,6 +26,8 @@ std::vector<fe> shamir_share_matrix(int N);
 void shares_launch(const fe *v, const fe *fill, uint64_t groups, int N, const fe *mu, fe *shares, cudaStream_t s);
 // Leader aggregation of party messages (sumcheck_aggr, MPI_utils.cpp:2604-2670).
 std::vector<fe> aggregate_weights(int N, const fe *b);
+// The weights of g^T E for any g over the unpacked shares E.
+std::vector<fe> aggregate_weights_even(int N, const std::vector<fe> &g);
 void aggregate_launch(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out, cudaStream_t s);
 // coSumcheck phase 1 helpers; extended blocks of up to 2^13 entries (one
 // batched transform per block).

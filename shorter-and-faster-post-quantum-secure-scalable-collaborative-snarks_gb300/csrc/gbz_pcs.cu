@@ -1,0 +1,1066 @@
+// The collaborative PCS of N parties on one device: PCS_commit and the
+// parties' side of PCS_open_new with the leader's aggregation of their round
+// messages (coPCS.cpp:236-250, 1310-1607), as the reference runs them with
+// one MPI rank per party.
+//
+// PcsLayout: every per-party vector is one party-major device array
+// [party][entry]; a step that every rank runs on its own share is one launch
+// over all parties (grid.y = party) or one batched transform over the
+// concatenated rows.  The leader's work (unpacking the packed-Shamir round
+// messages, Fiat-Shamir challenges, the query draws and the running claim)
+// runs on the device too, in one-CTA kernels, so an opening is a stream of
+// launches with no host round trip.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gbz_copcs.cuh"
+#include "gbz_ctx.cuh"
+
+using namespace gbz_api;
+
+namespace gbz {
+namespace {
+
+constexpr int kPcsMaxParties = 64;     // packed Shamir with N / 2 <= 32 values per group
+constexpr int kPcsMaxQueries = 1024;   // queries of one delegate check
+constexpr int kPcsMaxRounds = 8;       // rates.size()
+constexpr int kPcsMaxLogDeg = 10;      // the block fold of phase 2 (d <= 1024)
+
+// Transcript tags of the opening (see include/gbz.h).
+enum : uint32_t {
+  T_PCS_ROOTS = 32, T_PCS_LEADER_ROOT = 33, T_PCS_PARTY_POLYS = 34, T_PCS_POLY = 35, T_PCS_CHALLENGE = 36,
+  T_PCS_QUERIES = 37, T_PCS_Y = 38, T_PCS_SEGMENTS = 39, T_PCS_S = 40, T_PCS_K = 41, T_PCS_FINAL = 42
+};
+
+// Verifier-side state of one opening, resident on the device.
+struct PcsDev {
+  fe fs;         // Fiat-Shamir chain (prev_challenge, Fiat_Shamir.cpp:5)
+  fe K;          // running claim
+  fe r_first;    // challenge of the batching round
+  fe c;          // challenge of the current round
+  fe s;          // phase-3 challenge of the current round
+  uint32_t error;  // bit 0: a round message does not match K; bit 1: a delegate check failed
+};
+
+__device__ __forceinline__ fe pow_tab(const fe *lo, const fe *hi, uint64_t e) {
+  return fmul(lo[e & 4095u], hi[e >> 12]);
+}
+
+__device__ __forceinline__ void put_hash(uint8_t *tr, uint64_t off, const uint32_t h[8]) {
+  uint32_t *p = reinterpret_cast<uint32_t *>(tr + off);
+  for (int k = 0; k < 8; k++) p[k] = h[k];
+}
+
+// G(h) = blake3(h || h): an inner node of create_tree_blake whose left child
+// is h (merkle_tree.cpp:267-299 hashes the left child twice).
+__device__ void self_hash(uint32_t h[8], int times) {
+  uint32_t m[16];
+  for (int t = 0; t < times; t++) {
+    for (int k = 0; k < 8; k++) m[k] = m[8 + k] = h[k];
+    blake3_block64(m, h);
+  }
+}
+
+// Record headers {tag, count} at their offsets (built by the host).
+struct Hdr {
+  uint64_t off;
+  uint32_t tag, count;
+};
+__global__ void k_headers(const Hdr *h, int n, uint8_t *tr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t *p = reinterpret_cast<uint32_t *>(tr + h[i].off);
+  p[0] = h[i].tag;
+  p[1] = h[i].count;
+}
+
+__global__ void k_init(PcsDev *st, fe fs, fe K) {
+  st->fs = fs;
+  st->K = K;
+  st->r_first = st->c = st->s = fe_zero();
+  st->error = 0;
+}
+
+// b3' = the packed-Shamir share map applied to b3 (coPCS.cpp:1370-1376):
+// party j's scale of the beta vector.
+__global__ void k_b3p(const fe *b3, int nb3, const fe *mu, int N, fe *b3p) {
+  const int j = threadIdx.x;
+  if (j >= N) return;
+  fe acc = fe_zero();
+  for (int t = 0; t < nb3; t++) acc = fadd(acc, fmul(mu[j * (N / 2) + t], b3[t]));
+  b3p[j] = acc;
+}
+
+// out[p][j] = sum_{i < nrows} coef[i] rows[p][i][j] (coPCS.cpp:1352-1356).
+__global__ void k_lincomb(const fe *rows, uint64_t pstride, uint64_t rstride, int nrows, uint64_t len, const fe *coef,
+                          fe *out, uint64_t ostride) {
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= len) return;
+  const fe *r = rows + blockIdx.y * pstride + j;
+  fe acc = fe_zero();
+  for (int i = 0; i < nrows; i++) acc = fadd(acc, fmul(coef[i], r[(uint64_t)i * rstride]));
+  out[blockIdx.y * ostride + j] = acc;
+}
+
+// After the inverse transforms: bcd, cdl *= omega^{-j}; B = b2 omega^j b3'[p]
+// (coPCS.cpp:1385-1397), omega = w_{2 rate_offset Bs}.
+__global__ void k_open_prep(fe *bcd, fe *cdl, fe *B, const fe *b2, const fe *b3p, uint64_t Bs, const fe *lo,
+                            const fe *hi, const fe *ilo, const fe *ihi) {
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= Bs) return;
+  const uint64_t at = blockIdx.y * Bs + j;
+  const fe wi = pow_tab(ilo, ihi, j);
+  bcd[at] = fmul(bcd[at], wi);
+  cdl[at] = fmul(cdl[at], wi);
+  B[at] = fmul(fmul(b2[j], pow_tab(lo, hi, j)), b3p[blockIdx.y]);
+}
+
+// First batching round (coPCS.cpp:1403-1410): per party
+// (sum (bcd - cdl) B, sum cdl B, 0), as per-CTA partials.
+constexpr int kRedThreads = 256;
+__global__ void __launch_bounds__(kRedThreads)
+k_first_partial(const fe *bcd, const fe *cdl, const fe *B, uint64_t Bs, fe *partial) {
+  __shared__ fe ra[kRedThreads], rb[kRedThreads];
+  const uint64_t base = blockIdx.y * Bs;
+  fe a = fe_zero(), b = fe_zero();
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < Bs; j += (uint64_t)gridDim.x * blockDim.x) {
+    const fe x = bcd[base + j], y = cdl[base + j], w = B[base + j];
+    a = fadd(a, fmul(fsub(x, y), w));
+    b = fadd(b, fmul(y, w));
+  }
+  ra[threadIdx.x] = a;
+  rb[threadIdx.x] = b;
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      ra[threadIdx.x] = fadd(ra[threadIdx.x], ra[threadIdx.x + s]);
+      rb[threadIdx.x] = fadd(rb[threadIdx.x], rb[threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    fe *o = partial + 2 * ((uint64_t)blockIdx.y * gridDim.x + blockIdx.x);
+    o[0] = ra[0];
+    o[1] = rb[0];
+  }
+}
+
+// Party messages H[p] = (a, b, 0) from the partials; also their record.
+__global__ void k_first_reduce(const fe *partial, int nblk, int N, fe *H, uint8_t *tr, uint64_t off_pp) {
+  const int p = threadIdx.x;
+  if (p >= N) return;
+  fe a = fe_zero(), b = fe_zero();
+  for (int k = 0; k < nblk; k++) {
+    a = fadd(a, partial[2 * ((uint64_t)p * nblk + k)]);
+    b = fadd(b, partial[2 * ((uint64_t)p * nblk + k) + 1]);
+  }
+  H[3 * p] = a;
+  H[3 * p + 1] = b;
+  H[3 * p + 2] = fe_zero();
+  put_fe(tr, off_pp + 48ull * p, a);
+  put_fe(tr, off_pp + 48ull * p + 16, b);
+  put_fe(tr, off_pp + 48ull * p + 32, fe_zero());
+}
+
+// The leader's check and challenge of the batching round (coPCS.cpp:1428-1435).
+__global__ void k_first_verify(PcsDev *st, const fe *poly, uint8_t *tr, uint64_t off_poly, uint64_t off_chal,
+                               uint64_t off_K) {
+  if (threadIdx.x) return;
+  const fe p0 = poly[0], p1 = poly[1], p2 = poly[2];
+  if (!fe_eq(fadd(p0, p1), st->K)) st->error |= 1;
+  fe fs = st->fs;
+  fs = hash_F(fs, p0);
+  fs = hash_F(fs, p1);
+  fs = hash_F(fs, p2);
+  st->fs = fs;
+  st->r_first = fs;
+  st->K = fmul(fs, fadd(p1, fmul(fs, p0)));
+  put_fe(tr, off_poly, p0);
+  put_fe(tr, off_poly + 16, p1);
+  put_fe(tr, off_poly + 32, p2);
+  put_fe(tr, off_chal, fs);
+  put_fe(tr, off_K, st->K);
+}
+
+// The fold of the batching round (coPCS.cpp:1438-1447): B *= r,
+// bcd = r bcd + (1 - r) cdl, C' = r C' + (1 - r) codeword[batches - 1].
+__global__ void k_first_fold(fe *bcd, const fe *cdl, fe *B, fe *Cp, const fe *cw_last, uint64_t cw_pstride,
+                             uint64_t Bs, uint64_t L, const PcsDev *st) {
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= L) return;
+  const fe r = st->r_first, om = fsub(fe_one(), r);
+  const uint64_t p = blockIdx.y;
+  Cp[p * L + j] = fadd(fmul(r, Cp[p * L + j]), fmul(om, cw_last[p * cw_pstride + j]));
+  if (j < Bs) {
+    const uint64_t at = p * Bs + j;
+    B[at] = fmul(r, B[at]);
+    bcd[at] = fadd(fmul(r, bcd[at]), fmul(om, cdl[at]));
+  }
+}
+
+// Commitment roots of every party and the leader's root.  A party's root
+// of MT_commit_Blake over a vector depends on its first leaf only: the
+// leaf hash of entries e_k = data[p pstride + k estride] (k < 4), hashed
+// `levels` more times (inner nodes hash their left child twice).  With
+// `stale`, the parties report those roots instead (commit_tensorcode on a
+// reused, deeper tree; see the host side).  The leader's root over N party
+// roots is party 0's root hashed log2(N) times.
+__global__ void k_roots(const fe *data, uint64_t pstride, uint64_t estride, int levels, int N, int logN,
+                        const uint8_t *stale, uint8_t *roots, uint8_t *tr, uint64_t off_roots, uint64_t off_leader) {
+  __shared__ uint32_t r0[8];
+  const int p = threadIdx.x;
+  if (p < N) {
+    uint32_t h[8];
+    if (stale) {
+      for (int k = 0; k < 8; k++) h[k] = reinterpret_cast<const uint32_t *>(stale + 32 * p)[k];
+    } else {
+      const fe *d = data + (uint64_t)p * pstride;
+      uint32_t m[16];
+      fe4_words(d[0], d[estride], d[2 * estride], d[3 * estride], m);
+      blake3_block64(m, h);
+      self_hash(h, levels);
+    }
+    for (int k = 0; k < 8; k++) reinterpret_cast<uint32_t *>(roots + 32 * p)[k] = h[k];
+    put_hash(tr, off_roots + 32ull * p, h);
+    if (p == 0)
+      for (int k = 0; k < 8; k++) r0[k] = h[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t h[8];
+    for (int k = 0; k < 8; k++) h[k] = r0[k];
+    self_hash(h, logN);
+    put_hash(tr, off_leader, h);
+  }
+}
+
+// get_indexes (Fiat_Shamir.cpp:37-56) for every party at once: l draws of
+// (party, position) from the chain, then the order the leader holds them in
+// after get_segments (MPI_utils.cpp:187-255): party 0's queries, then party
+// 1's, ..., each in draw order.
+__global__ void k_indexes(PcsDev *st, int l, int N, uint32_t Mq, int32_t *qp, int32_t *qpos, uint8_t *tr,
+                          uint64_t off) {
+  __shared__ int32_t sp[kPcsMaxQueries], sq[kPcsMaxQueries];
+  __shared__ int32_t start[kPcsMaxParties + 1];
+  if (threadIdx.x == 0) {
+    fe fs = st->fs;
+    for (int i = 0; i < l; i++) {
+      fs = hash_F(fs, fs);
+      sp[i] = (int32_t)(fs.re % (uint64_t)N);
+      sq[i] = (int32_t)(fs.im % (uint64_t)Mq);
+    }
+    st->fs = fs;
+    for (int p = 0; p <= N; p++) start[p] = 0;
+    for (int i = 0; i < l; i++) start[sp[i] + 1]++;
+    for (int p = 0; p < N; p++) start[p + 1] += start[p];
+    for (int i = 0; i < l; i++) {
+      const int at = start[sp[i]]++;
+      qp[at] = sp[i];
+      qpos[at] = sq[i];
+    }
+  }
+  __syncthreads();
+  uint32_t *w = reinterpret_cast<uint32_t *>(tr + off);
+  for (int i = threadIdx.x; i < l; i += blockDim.x) {
+    w[2 * i] = (uint32_t)qp[i];
+    w[2 * i + 1] = (uint32_t)qpos[i];
+  }
+}
+
+// The leader's check of round i and its challenge (coPCS.cpp:1463-1483):
+// sum_j poly[2j] = K, c = hash_to_field(poly), K = sum_k poly[k] L2[k] with
+// L2 = compute_lagrange_coeff(c, 2d), and the fold weights L = the same at
+// length d (utils.cpp:169-197: the inverse transform of the powers of c).
+// scratch: 2 * 2d entries.
+__global__ void __launch_bounds__(256)
+k_round_verify(PcsDev *st, const fe *poly, int logd, fe *L, fe *scratch, uint8_t *tr, uint64_t off_poly,
+               uint64_t off_chal) {
+  __shared__ fe red[256];
+  const int d = 1 << logd, D = 2 * d;
+  fe *cp = scratch, *wp = scratch + D;
+  if (threadIdx.x == 0) {
+    fe ev = fe_zero();
+    for (int j = 0; j < d; j++) ev = fadd(ev, poly[2 * j]);
+    if (!fe_eq(ev, st->K)) st->error |= 1;
+    fe fs = st->fs;
+    for (int k = 0; k < D; k++) fs = hash_F(fs, poly[k]);
+    st->fs = fs;
+    st->c = fs;
+    put_fe(tr, off_chal, fs);
+    fe x = fe_one();
+    for (int k = 0; k < D; k++) {
+      cp[k] = x;
+      x = fmul(x, fs);
+    }
+  }
+  __syncthreads();
+  const fe wi = finv(root_of_unity(logd + 1));
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    wp[k] = fpow(wi, (uint64_t)k);
+    put_fe(tr, off_poly + 16ull * k, poly[k]);
+  }
+  __syncthreads();
+  // L2[k] = (1/D) sum_j c^j w^{-jk}; K' = sum_k poly[k] L2[k]
+  const fe invD = finv(fe_make((uint64_t)D, 0)), invd = finv(fe_make((uint64_t)d, 0));
+  fe acc = fe_zero();
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    fe s = fe_zero();
+    for (int j = 0; j < D; j++) s = fadd(s, fmul(cp[j], wp[((uint64_t)j * k) & (D - 1)]));
+    acc = fadd(acc, fmul(poly[k], fmul(s, invD)));
+  }
+  // L[k] = (1/d) sum_{j<d} c^j w_d^{-jk}, w_d^{-1} = (w_D^{-1})^2
+  for (int k = threadIdx.x; k < d; k += blockDim.x) {
+    fe s = fe_zero();
+    for (int j = 0; j < d; j++) s = fadd(s, fmul(cp[j], wp[(2ull * j * k) & (D - 1)]));
+    L[k] = fmul(s, invd);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fadd(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) st->K = red[0];
+}
+
+// delegate_checks (coPCS.cpp:753-763): per query j (party a, position q),
+// the segment C'_a[q + k seg_n] (k < d) and its RS fold y_j (RS_multifold_segment
+// equals output q of RS_multifold5 over C'_a).
+__global__ void k_gather(const fe *Cp, uint64_t pstride, uint64_t seg_n, int d, const fe *fold, uint64_t fstride,
+                         const int32_t *qp, const int32_t *qpos, int l, fe *y, uint8_t *tr, uint64_t off_y,
+                         uint64_t off_seg) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)l * d) return;
+  const int j = (int)(t / d), k = (int)(t % d);
+  const uint64_t a = (uint64_t)qp[j], q = (uint64_t)qpos[j];
+  put_fe(tr, off_seg + 16 * t, Cp[a * pstride + q + k * seg_n]);
+  if (k == 0) {
+    const fe v = fold[a * fstride + q];
+    y[j] = v;
+    put_fe(tr, off_y + 16ull * j, v);
+  }
+}
+
+// The check of coPCS.cpp:1521-1529: the new codeword holds y_j at the
+// query's position scaled by rate_{i+2} / rate_{i+1}.
+__global__ void k_check_y(const fe *Cpn, uint64_t pstride, uint32_t mul, uint32_t div, const int32_t *qp,
+                          const int32_t *qpos, const fe *y, int l, PcsDev *st) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= l) return;
+  const uint64_t pos = (uint64_t)mul * (uint32_t)qpos[j] / div;
+  if (pos >= pstride || !fe_eq(Cpn[(uint64_t)qp[j] * pstride + pos], y[j])) atomicOr(&st->error, 2u);
+}
+
+// s = hash_to_field({0}) and, unless the last round, K += sum_j s^{j+1} y_j
+// (coPCS.cpp:1535-1547).
+__global__ void k_s_update(PcsDev *st, const fe *y, int l, int addK, uint8_t *tr, uint64_t off_s, uint64_t off_K) {
+  if (threadIdx.x) return;
+  const fe s = hash_F(st->fs, fe_zero());
+  st->fs = s;
+  st->s = s;
+  if (addK) {
+    fe K = st->K, pk = s;
+    for (int j = 0; j < l; j++) {
+      K = fadd(K, fmul(pk, y[j]));
+      pk = fmul(pk, s);
+    }
+    st->K = K;
+  }
+  put_fe(tr, off_s, s);
+  put_fe(tr, off_K, st->K);
+}
+
+// pcs_sumcheck_phase3 (coPCS.cpp:634-648) for every party: B_p[j] +=
+// sum_i s^{i+1} scale(a_i, p) (w^{q_i})^j, w = w_{rate rows}, q_i the query
+// position scaled as the reference scales it, scale(a, p) the tensor scale
+// of tensor_eval_vector (coPCS.cpp:610-632; a constant table).
+__global__ void k_phase3_prep(const PcsDev *st, const int32_t *qp, const int32_t *qpos, int l, uint32_t mul,
+                              uint32_t div, int logw, const fe *scale, int N, fe *base, fe *w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= l) return;
+  const uint64_t q = (uint64_t)mul * (uint32_t)qpos[i] / div;
+  base[i] = fpow(root_of_unity(logw), q & ((1ull << logw) - 1));
+  const fe si = fpow(st->s, (uint64_t)i + 1);
+  for (int p = 0; p < N; p++) w[(uint64_t)p * l + i] = fmul(si, scale[qp[i] * N + p]);
+}
+
+constexpr int kP3Chunk = 8;
+__global__ void k_phase3(fe *B, uint64_t rows, const fe *base, const fe *w, int l) {
+  const uint64_t j0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kP3Chunk;
+  if (j0 >= rows) return;
+  const uint64_t p = blockIdx.y;
+  const fe *wp = w + p * l;
+  fe acc[kP3Chunk];
+#pragma unroll
+  for (int c = 0; c < kP3Chunk; c++) acc[c] = fe_zero();
+  for (int i = 0; i < l; i++) {
+    const fe b = base[i];
+    fe x = fmul(wp[i], fpow(b, j0));
+#pragma unroll
+    for (int c = 0; c < kP3Chunk; c++) {
+      acc[c] = fadd(acc[c], x);
+      x = fmul(x, b);
+    }
+  }
+  fe *o = B + p * rows + j0;
+#pragma unroll
+  for (int c = 0; c < kP3Chunk; c++)
+    if (j0 + c < rows) o[c] = fadd(o[c], acc[c]);
+}
+
+// The RS fold of a codeword by d (RS_multifold5, coPCS_utils.cpp:386-437, and
+// RS_multifold_segment, :172-232) for any d: its butterflies compute, for
+// output i, d f_c(x^d) (c < d, f(X) = sum_c X^c f_c(X^d), x = w_n^i) and
+// return sum_c L[c] f_c(x^d).  With s_t = cw[i + t m] = f(x w_d^t) (m = n/d)
+// that is (1/d) sum_t s_t P_L(w_n^{-(i + t m)}), P_L(z) = sum_c L[c] z^c, and
+// Q[e] = P_L(w_n^{-e}) = n IDFT_n(L, zero-padded)[e].  So
+// out[p][i] = (n/d) sum_t cw[p][i + t m] iQ[i + t m],  iQ = IDFT_n(L padded).
+__global__ void k_fold_q(const fe *cw, uint64_t n, int logd, const fe *iQ, fe scale, fe *out, uint64_t ostride) {
+  const uint64_t m = n >> logd;
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const fe *c = cw + blockIdx.y * n;
+  fe acc = fe_zero();
+  for (int t = 0; t < (1 << logd); t++) acc = fadd(acc, fmul(c[i + t * m], iQ[i + t * m]));
+  out[blockIdx.y * ostride + i] = fmul(acc, scale);
+}
+
+// A record payload copied from party-major vectors: out[p][0..len) -> tr.
+__global__ void k_put_party(const fe *v, uint64_t len, int N, uint8_t *tr, uint64_t off, uint64_t rec_stride) {
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= len) return;
+  put_fe(tr, off + blockIdx.y * rec_stride + 16 * j, v[blockIdx.y * len + j]);
+}
+
+unsigned grid(uint64_t n, unsigned t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+}  // namespace gbz
+
+// ------------------------------------------------------------ host side
+
+using namespace gbz;
+
+namespace {
+
+// prepare_parameters (coPCS.cpp:38-72) with get_degrees / get_queries
+// (New_PCS.cpp:23-77).  The query counts are the reference's double
+// expressions, truncated as it truncates them.
+struct PcsSchedule {
+  int N = 0, rounds = 0;
+  uint64_t M = 0;
+  std::vector<int> rate0, rate1, degrees, queries, delegation;
+  int log_rate_offset = 0;
+  uint64_t randomness = 0;  // sum_i queries[i] degrees[i]
+};
+
+PcsSchedule make_schedule(int N, uint64_t M, int rounds, const int *rate0, const int *rate1) {
+  if (N < 4 || N > kPcsMaxParties || !is_pow2((uint64_t)N)) throw ArgError("pcs: N must be a power of two in [4, 64]");
+  if (rounds < 3 || rounds > kPcsMaxRounds) throw ArgError("pcs: 3..8 rounds (rates)");
+  if (!is_pow2(M)) throw ArgError("pcs: M must be a power of two");
+  PcsSchedule s;
+  s.N = N;
+  s.M = M;
+  s.rounds = rounds;
+  for (int i = 0; i < rounds; i++) {
+    if (rate0[i] < 2 || !is_pow2((uint64_t)rate0[i])) throw ArgError("pcs: tensor rates must be powers of two >= 2");
+    s.rate0.push_back(rate0[i]);
+    const int r1 = i >= 2 ? rate1[i] : 0;
+    if (i >= 2 && (r1 < 2 || !is_pow2((uint64_t)r1))) throw ArgError("pcs: row rates must be powers of two >= 2");
+    s.rate1.push_back(r1);
+  }
+  const uint64_t row_size = 2 * (4 * M / (uint64_t)N);
+  int log_size = ilog2(row_size);
+  s.degrees.push_back(32);
+  log_size -= 5;
+  s.degrees.push_back(8);
+  log_size -= 3;
+  const int deg = log_size / (rounds - 2);
+  if (log_size < 1 || deg < 1) throw ArgError("pcs: M too small for the degree schedule");
+  for (int i = 1; i < rounds - 2; i++) s.degrees.push_back(1 << deg);
+  s.degrees.push_back(1 << (log_size - deg * (rounds - 3)));
+  for (int i = 0; i < rounds; i++) {
+    volatile double q;
+    if (i <= 1) {
+      volatile double t = 1.0 - 1.0 / (double)rate0[0];
+      volatile double u = 0.25 * t;
+      volatile double v = 1 - u;
+      q = 100.0 / (-std::log2(v));
+      s.queries.push_back((int)q);
+    } else {
+      volatile double a = 1.0 - 1.0 / (double)rate0[i];
+      volatile double sq = std::sqrt(1.0 / (double)s.rate1[i]);
+      volatile double b = 0.5 * 0.5 * a;
+      volatile double c = b * (1 - sq);
+      volatile double e1 = 1 - c;
+      const int l1 = (int)(100.0 / (-std::log2(e1)));
+      volatile double e2 = 1 - b;
+      volatile double t1 = 100.0 / (-std::log2(e2));
+      volatile double t2 = 100.0 / (-std::log2(sq));
+      volatile double t3 = t1 + t2;
+      const int l2 = (int)t3;
+      s.queries.push_back(l1 > l2 ? l2 : l1);
+    }
+  }
+  int ro = 1;
+  for (int i = 1; i < rounds; i++) ro *= rate0[i];
+  s.log_rate_offset = ilog2((uint64_t)ro);
+  for (int i = 2; i < rounds; i++) {
+    uint64_t x = (uint64_t)s.degrees[i] * s.queries[i], p2 = 1;
+    while (p2 < x) p2 <<= 1;
+    s.delegation.push_back((int)p2);
+  }
+  for (int i = 0; i < rounds; i++) s.randomness += (uint64_t)s.queries[i] * s.degrees[i];
+  for (int i = 0; i < rounds; i++)
+    if (s.queries[i] < 1 || s.queries[i] > kPcsMaxQueries) throw ArgError("pcs: 1..1024 queries per round");
+  for (int i = 1; i < rounds; i++)
+    if (s.degrees[i] > (1 << kPcsMaxLogDeg)) throw ArgError("pcs: round degree above 2^10");
+  return s;
+}
+
+// One copy run of prepare_data (coPCS.cpp:76-129): `count` entries of the
+// shares (src 0) or the random shares (src 1) from src_off into row `row`
+// at column `col`.
+struct Run {
+  int row;
+  uint64_t col;
+  int src;
+  uint64_t src_off, count;
+};
+
+std::vector<Run> prepare_runs(uint64_t S, uint64_t R, uint64_t Bs, uint64_t q0, int *batches) {
+  if (q0 >= Bs) throw ArgError("pcs: the first round's queries fill a whole row (M too small)");
+  std::vector<Run> runs;
+  uint64_t dc = 0, rc = 0;
+  int last = -1;
+  for (int i = 0; i < 32; i++) {
+    const uint64_t take = std::min(Bs - q0, S - dc);
+    runs.push_back({i, 0, 0, dc, take});
+    dc += take;
+    if (rc + q0 > R) throw ArgError("pcs: too few random shares");
+    runs.push_back({i, Bs - q0, 1, rc, q0});
+    rc += q0;
+    if (dc == S) {
+      last = i;
+      break;
+    }
+  }
+  if (dc < S || last + 1 >= 32) throw ArgError("pcs: more batches are needed (M too large for 32 rows)");
+  const int lr = last + 1;
+  uint64_t count;
+  // The reference compares Shares.size() - rand_ctr as an unsigned value, so
+  // rand_ctr > Shares.size() takes the first case too.
+  if (S < rc || S - rc > Bs) {
+    if (rc >= R) throw ArgError("pcs: too few random shares");
+    count = std::min(Bs, R - rc);
+  } else {
+    count = Bs - (S - rc);
+    if (count > R - rc) throw ArgError("pcs: too few random shares");
+  }
+  runs.push_back({lr, 0, 1, rc, count});
+  *batches = lr + 1;
+  return runs;
+}
+
+// Packed-Shamir constants of N parties: the share map (compute_secret_shares)
+// and the tensor scales of tensor_eval_vector; both depend on N only.
+fe host_tensor_scale(uint32_t p0, int cols, int my_id) {
+  const int lg4 = ilog2(4ull * (uint64_t)cols);
+  const fe w2 = fpow(root_of_unity(lg4), 2ull * p0 + 1);
+  const fe step = fpow(root_of_unity(lg4), 2ull * (uint64_t)my_id + 1);
+  std::vector<fe> pw(cols);
+  fe x = fe_one();
+  for (int t = 0; t < cols; t++) {
+    pw[t] = x;
+    x = fmul(x, w2);
+  }
+  fe acc = fe_zero(), e = fe_one();
+  for (int t = 0; t < cols; t++) {
+    acc = fadd(acc, fmul(pw[(cols - t) % cols], e));
+    e = fmul(e, step);
+  }
+  return fmul(acc, finv(fe_make((uint64_t)cols, 0)));
+}
+
+}  // namespace
+
+struct gbz_pcs {
+  int device = 0;
+  PcsSchedule sc;
+  uint64_t S = 0, R = 0, Bs = 0, L = 0;  // share length, random length, row length, codeword length
+  int batches = 0;
+  fe *cd = nullptr;      // [N][batches][Bs] Commit_data
+  fe *cw = nullptr;      // [N][batches][L] codewords
+  uint8_t *levels = nullptr;  // [N][2L - 1] column-root trees of distributed_MT
+  uint8_t *roots = nullptr;   // [N][32] party roots, then [N][32] the leader root each party derives
+  std::vector<void *> owned;
+
+  ~gbz_pcs() {
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    for (void *p : owned) cudaFree(p);
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  template <typename T>
+  T *alloc(uint64_t count) {
+    void *p = nullptr;
+    GBZ_CUDA(cudaMalloc(&p, std::max<uint64_t>(count * sizeof(T), 16)));
+    owned.push_back(p);
+    return (T *)p;
+  }
+};
+
+namespace {
+
+// Device buffers of one opening (allocated per call, freed at its end).
+struct OpenBufs {
+  std::vector<void *> owned;
+  ~OpenBufs() {
+    for (void *p : owned) cudaFree(p);
+  }
+  template <typename T>
+  T *alloc(uint64_t count) {
+    void *p = nullptr;
+    GBZ_CUDA(cudaMalloc(&p, std::max<uint64_t>(count * sizeof(T), 16)));
+    owned.push_back(p);
+    return (T *)p;
+  }
+};
+
+// The record layout of an opening: header list and the payload offsets.
+struct PcsLayout {
+  std::vector<Hdr> hdr;
+  uint64_t bytes = 0;
+  uint64_t add(uint32_t tag, uint32_t count, uint64_t unit) {
+    hdr.push_back({bytes, tag, count});
+    const uint64_t payload = bytes + 8;
+    bytes += 8 + unit * count;
+    return payload;
+  }
+};
+
+struct RoundOffs {
+  uint64_t pp, poly, chal, roots, leader, queries, y, seg, s, K;
+};
+struct OpenOffs {
+  uint64_t pp0, poly0, chal0, K0, broots, bleader, bqueries, final_;
+  std::vector<RoundOffs> r;
+};
+
+OpenOffs open_layout(const gbz_pcs &pc, PcsLayout &lay) {
+  const PcsSchedule &sc = pc.sc;
+  const int N = sc.N;
+  OpenOffs o;
+  o.pp0 = lay.add(T_PCS_PARTY_POLYS, 3 * N, 16);
+  o.poly0 = lay.add(T_PCS_POLY, 3, 16);
+  o.chal0 = lay.add(T_PCS_CHALLENGE, 1, 16);
+  o.K0 = lay.add(T_PCS_K, 1, 16);
+  o.broots = lay.add(T_PCS_ROOTS, N, 32);
+  o.bleader = lay.add(T_PCS_LEADER_ROOT, 1, 32);
+  o.bqueries = lay.add(T_PCS_QUERIES, 2 * sc.queries[0], 4);
+  for (int i = 0; i + 1 < sc.rounds; i++) {
+    const int d = sc.degrees[i + 1], l = sc.queries[i + 1];
+    RoundOffs r;
+    r.pp = lay.add(T_PCS_PARTY_POLYS, 2 * d * N, 16);
+    r.poly = lay.add(T_PCS_POLY, 2 * d, 16);
+    r.chal = lay.add(T_PCS_CHALLENGE, 1, 16);
+    r.roots = lay.add(T_PCS_ROOTS, N, 32);
+    r.leader = lay.add(T_PCS_LEADER_ROOT, 1, 32);
+    r.queries = lay.add(T_PCS_QUERIES, 2 * l, 4);
+    r.y = lay.add(T_PCS_Y, l, 16);
+    r.seg = lay.add(T_PCS_SEGMENTS, l * d, 16);
+    r.s = lay.add(T_PCS_S, 1, 16);
+    r.K = lay.add(T_PCS_K, 1, 16);
+    o.r.push_back(r);
+  }
+  // final: per party bcd, B, C' (send_pcs_data, MPI_utils.cpp:58-116)
+  uint64_t n = pc.Bs, cpl = pc.L;
+  for (int i = 0; i + 1 < sc.rounds; i++) {
+    const uint64_t d = sc.degrees[i + 1];
+    n /= d;
+    cpl = (i + 2 < sc.rounds) ? n * sc.rate0[i + 2] : cpl / d;
+  }
+  o.final_ = lay.add(T_PCS_FINAL, (uint32_t)(N * (2 * n + cpl)), 16);
+  return o;
+}
+
+}  // namespace
+
+extern "C" {
+
+gbz_status gbz_pcs_schedule(int N, uint64_t M, int rounds, const int *rate0, const int *rate1, int *degrees,
+                            int *queries, uint64_t *random_per_party) {
+  try {
+    if (!rate0 || !rate1) return GBZ_EINVAL;
+    PcsSchedule s = make_schedule(N, M, rounds, rate0, rate1);
+    for (int i = 0; i < rounds; i++) {
+      if (degrees) degrees[i] = s.degrees[i];
+      if (queries) queries[i] = s.queries[i];
+    }
+    if (random_per_party) *random_per_party = s.randomness;
+  } catch (const ArgError &) {
+    return GBZ_EINVAL;
+  }
+  return GBZ_OK;
+}
+
+gbz_status gbz_pcs_commit(gbz_ctx *ctx, int N, uint64_t M, int rounds, const int *rate0, const int *rate1,
+                          const uint64_t *shares, const uint64_t *random, int mem, gbz_pcs **out,
+                          uint8_t *party_roots, uint8_t *leader_root) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(rate0, "rate0");
+  need(rate1, "rate1");
+  need(shares, "shares");
+  need(random, "random");
+  need(out, "out");
+  *out = nullptr;
+  std::unique_ptr<gbz_pcs> pc(new gbz_pcs());
+  pc->device = ctx->device;
+  pc->sc = make_schedule(N, M, rounds, rate0, rate1);
+  const PcsSchedule &sc = pc->sc;
+  pc->S = 4 * M / (uint64_t)N;
+  pc->R = sc.randomness;
+  pc->Bs = pc->S / 16;
+  if (pc->Bs < 4) throw ArgError("pcs: shares shorter than 64 entries");
+  pc->L = pc->Bs * (uint64_t)sc.rate0[0];
+  if (ilog2(pc->L) > kMaxNttLogN || 1 + sc.log_rate_offset + ilog2(pc->Bs) > kMaxLogN)
+    throw ArgError("pcs: codeword above 2^26");
+  std::vector<Run> runs = prepare_runs(pc->S, pc->R, pc->Bs, sc.queries[0], &pc->batches);
+  const uint64_t Bs = pc->Bs, L = pc->L, S = pc->S, R = pc->R;
+  const int nb = pc->batches;
+  cudaStream_t s = ctx->stream;
+  // inputs on the device
+  const fe *dsh = dev_view(ctx, 0, (const fe *)shares, 16 * S * N, mem, true);
+  const fe *drn = dev_view(ctx, 1, (const fe *)random, 16 * R * N, mem, true);
+  pc->cd = pc->alloc<fe>((uint64_t)N * nb * Bs);
+  pc->cw = pc->alloc<fe>((uint64_t)N * nb * L);
+  pc->levels = pc->alloc<uint8_t>(32ull * N * (2 * L - 1));
+  pc->roots = pc->alloc<uint8_t>(64ull * N);
+  // prepare_data: the rows of every party as 2-D copies (height = parties)
+  GBZ_CUDA(cudaMemsetAsync(pc->cd, 0, 16ull * N * nb * Bs, s));
+  for (const Run &r : runs) {
+    if (!r.count) continue;
+    const fe *src = (r.src ? drn : dsh) + r.src_off;
+    fe *dst = pc->cd + (uint64_t)r.row * Bs + r.col;
+    GBZ_CUDA(cudaMemcpy2DAsync(dst, 16 * nb * Bs, src, 16 * (r.src ? R : S), 16 * r.count, N,
+                               cudaMemcpyDeviceToDevice, s));
+  }
+  // Encode (coPCS.cpp:131-147): every party's rows in the same launches
+  encode_rows_device(ctx, pc->cd, N * nb, ilog2(Bs), sc.rate0[0], sc.log_rate_offset, pc->cw);
+  // distributed_MT (coPCS.cpp:152-202) per party
+  for (int p = 0; p < N; p++)
+    column_merkle_launch(pc->cw + (uint64_t)p * nb * L, nb, L, pc->levels + 32ull * p * (2 * L - 1), ilog2(N),
+                         pc->roots + 32ull * (N + p), s);
+  for (int p = 0; p < N; p++)
+    GBZ_CUDA(cudaMemcpyAsync(pc->roots + 32ull * p, pc->levels + 32ull * p * (2 * L - 1) + 32 * (2 * L - 2), 32,
+                             cudaMemcpyDeviceToDevice, s));
+  if (party_roots) {
+    if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaMemcpyAsync(party_roots, pc->roots, 32ull * N, cudaMemcpyDeviceToHost, s));
+    else GBZ_CUDA(cudaMemcpyAsync(party_roots, pc->roots, 32ull * N, cudaMemcpyDeviceToDevice, s));
+  }
+  if (leader_root) {
+    const cudaMemcpyKind k = mem == GBZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    GBZ_CUDA(cudaMemcpyAsync(leader_root, pc->roots + 32ull * N, 32, k, s));
+  }
+  GBZ_CUDA(cudaStreamSynchronize(s));  // the staged inputs are scratch of the context
+  *out = pc.release();
+  API_END(ctx)
+}
+
+void gbz_pcs_free(gbz_pcs *pcs) { delete pcs; }
+
+gbz_status gbz_pcs_info(const gbz_pcs *pcs, int *batches, uint64_t *row_len, uint64_t *codeword_len,
+                        uint64_t *open_transcript_bytes) {
+  if (!pcs) return GBZ_EINVAL;
+  if (batches) *batches = pcs->batches;
+  if (row_len) *row_len = pcs->Bs;
+  if (codeword_len) *codeword_len = pcs->L;
+  if (open_transcript_bytes) {
+    PcsLayout lay;
+    open_layout(*pcs, lay);
+    *open_transcript_bytes = lay.bytes;
+  }
+  return GBZ_OK;
+}
+
+gbz_status gbz_pcs_commit_data(gbz_ctx *ctx, const gbz_pcs *pcs, int party, uint64_t *rows, uint64_t *codewords,
+                               uint8_t *levels, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(pcs, "pcs");
+  if (party < 0 || party >= pcs->sc.N) throw ArgError("pcs: party out of range");
+  const cudaMemcpyKind k = mem == GBZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  const uint64_t nb = pcs->batches, Bs = pcs->Bs, L = pcs->L;
+  if (rows) GBZ_CUDA(cudaMemcpyAsync(rows, pcs->cd + party * nb * Bs, 16 * nb * Bs, k, ctx->stream));
+  if (codewords) GBZ_CUDA(cudaMemcpyAsync(codewords, pcs->cw + party * nb * L, 16 * nb * L, k, ctx->stream));
+  if (levels)
+    GBZ_CUDA(cudaMemcpyAsync(levels, pcs->levels + 32ull * party * (2 * L - 1), 32 * (2 * L - 1), k, ctx->stream));
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
+                        uint8_t *transcript, uint64_t capacity, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(pcs, "pcs");
+  need(r, "r");
+  need(K, "K");
+  need(fs, "fs");
+  need(transcript, "transcript");
+  if (pcs->device != ctx->device) throw ArgError("pcs: committed on another device");
+  const PcsSchedule &sc = pcs->sc;
+  const int N = sc.N, logN = ilog2(N), nb = pcs->batches;
+  const uint64_t Bs = pcs->Bs, L = pcs->L;
+  const int lk = ilog2(N / 4), logBs = ilog2(Bs);
+  if (nr != lk + 5 + logBs) throw ArgError("pcs: the point must have log2(N/4) + 5 + log2(row length) entries");
+  PcsLayout lay;
+  const OpenOffs off = open_layout(*pcs, lay);
+  if (capacity < lay.bytes) throw ArgError("pcs: transcript capacity below gbz_pcs_info's open_transcript_bytes");
+  cudaStream_t s = ctx->stream;
+  OpenBufs ob;
+  uint8_t *tr = mem == GBZ_MEM_DEVICE ? transcript : ob.alloc<uint8_t>(lay.bytes);
+  // headers
+  Hdr *dh = ob.alloc<Hdr>(lay.hdr.size());
+  GBZ_CUDA(cudaMemcpyAsync(dh, lay.hdr.data(), sizeof(Hdr) * lay.hdr.size(), cudaMemcpyHostToDevice, s));
+  k_headers<<<grid(lay.hdr.size()), 256, 0, s>>>(dh, (int)lay.hdr.size(), tr);
+  GBZ_CUDA(cudaGetLastError());
+  // point and constants
+  std::vector<fe> hr(nr);
+  for (int i = 0; i < nr; i++) {
+    if (mem == GBZ_MEM_DEVICE) break;
+    hr[i] = fe_make(r[2 * i], r[2 * i + 1]);
+  }
+  fe *dr = ob.alloc<fe>(nr);
+  GBZ_CUDA(cudaMemcpyAsync(dr, mem == GBZ_MEM_DEVICE ? (const void *)r : (const void *)hr.data(), 16ull * nr,
+                           mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  fe hK, hfs;
+  if (mem == GBZ_MEM_DEVICE) {
+    uint64_t t[4];
+    GBZ_CUDA(cudaMemcpyAsync(t, K, 16, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaMemcpyAsync(t + 2, fs, 16, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaStreamSynchronize(s));
+    hK = fe_make(t[0], t[1]);
+    hfs = fe_make(t[2], t[3]);
+  } else {
+    hK = fe_make(K[0], K[1]);
+    hfs = fe_make(fs[0], fs[1]);
+  }
+  PcsDev *st = ob.alloc<PcsDev>(1);
+  k_init<<<1, 1, 0, s>>>(st, hfs, hK);
+  GBZ_CUDA(cudaGetLastError());
+  std::vector<fe> mu = shamir_share_matrix(N), scale((size_t)N * N);
+  for (int a = 0; a < N; a++)
+    for (int p = 0; p < N; p++) scale[(size_t)a * N + p] = host_tensor_scale((uint32_t)a, N / 2, p);
+  // pcs_sumcheck_aggr (MPI_utils.cpp:362-371) sums the even entries of the
+  // unpacked shares, E[2j] for j < N/2: one fixed linear form of the N messages
+  std::vector<fe> g(N, fe_zero());
+  for (int j = 0; j < N / 2; j++) g[2 * j] = fe_one();
+  std::vector<fe> lambda = aggregate_weights_even(N, g);
+  fe *dmu = ob.alloc<fe>(mu.size()), *dscale = ob.alloc<fe>(scale.size()), *dlam = ob.alloc<fe>(N);
+  GBZ_CUDA(cudaMemcpyAsync(dmu, mu.data(), 16 * mu.size(), cudaMemcpyHostToDevice, s));
+  GBZ_CUDA(cudaMemcpyAsync(dscale, scale.data(), 16 * scale.size(), cudaMemcpyHostToDevice, s));
+  GBZ_CUDA(cudaMemcpyAsync(dlam, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
+
+  // betas of the point: r3 (log2 N/4), r1 (5), r2 (log2 Bs) (coPCS.cpp:1319-1325)
+  fe *b1 = ob.alloc<fe>(32), *b2 = ob.alloc<fe>(Bs), *b3 = ob.alloc<fe>(std::max(1, N / 4)), *b3p = ob.alloc<fe>(N);
+  beta_launch(dr + lk, 5, b1, s);
+  beta_launch(dr + lk + 5, logBs, b2, s);
+  if (lk) beta_launch(dr, lk, b3, s);
+  else {
+    const fe one = fe_one();
+    GBZ_CUDA(cudaMemcpyAsync(b3, &one, 16, cudaMemcpyHostToDevice, s));
+  }
+  k_b3p<<<1, 64, 0, s>>>(b3, N / 4, dmu, N, b3p);
+  GBZ_CUDA(cudaGetLastError());
+  // row batching (coPCS.cpp:1352-1356) and the transforms of :1359-1366
+  fe *Cp = ob.alloc<fe>((uint64_t)N * L), *bcd = ob.alloc<fe>((uint64_t)N * Bs), *cdl = ob.alloc<fe>((uint64_t)N * Bs);
+  fe *B = ob.alloc<fe>((uint64_t)N * Bs), *tmp = ob.alloc<fe>(std::max<uint64_t>((uint64_t)N * L, 1ull << 13));
+  k_lincomb<<<dim3(grid(L), N), 256, 0, s>>>(pcs->cw, (uint64_t)nb * L, L, nb - 1, L, b1, Cp, L);
+  k_lincomb<<<dim3(grid(Bs), N), 256, 0, s>>>(pcs->cd, (uint64_t)nb * Bs, Bs, nb - 1, Bs, b1, bcd, Bs);
+  GBZ_CUDA(cudaGetLastError());
+  GBZ_CUDA(cudaMemcpy2DAsync(cdl, 16 * Bs, pcs->cd + (uint64_t)(nb - 1) * Bs, 16ull * nb * Bs, 16 * Bs, N,
+                             cudaMemcpyDeviceToDevice, s));
+  const NttTables &tB = ctx->tables(logBs);
+  ntt_launch(tB, b2, Bs, b2, tmp, false, s);
+  ntt_launch_rows(tB, bcd, Bs, Bs, bcd, Bs, N, tmp, true, s);
+  ntt_launch_rows(tB, cdl, Bs, Bs, cdl, Bs, N, tmp, true, s);
+  const NttTables &tw = ctx->tables(1 + sc.log_rate_offset + logBs);
+  k_open_prep<<<dim3(grid(Bs), N), 256, 0, s>>>(bcd, cdl, B, b2, b3p, Bs, tw.lo_fwd, tw.hi_fwd, tw.lo_inv,
+                                                 tw.hi_inv);
+  GBZ_CUDA(cudaGetLastError());
+  // the batching round
+  const int nblk = (int)std::min<uint64_t>(64, (Bs + kRedThreads - 1) / kRedThreads);
+  fe *partial = ob.alloc<fe>(2ull * N * nblk), *H = ob.alloc<fe>((uint64_t)N * (2 << kPcsMaxLogDeg));
+  fe *poly = ob.alloc<fe>(2 << kPcsMaxLogDeg);
+  k_first_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(bcd, cdl, B, Bs, partial);
+  k_first_reduce<<<1, 64, 0, s>>>(partial, nblk, N, H, tr, off.pp0);
+  aggregate_launch(H, N, 3, dlam, poly, s);
+  k_first_verify<<<1, 1, 0, s>>>(st, poly, tr, off.poly0, off.chal0, off.K0);
+  k_first_fold<<<dim3(grid(L), N), 256, 0, s>>>(bcd, cdl, B, Cp, pcs->cw + (uint64_t)(nb - 1) * L, (uint64_t)nb * L,
+                                                Bs, L, st);
+  GBZ_CUDA(cudaGetLastError());
+  // batch_commitments_new (coPCS.cpp:1242-1308): the root over C' in columns
+  // of _degrees[1] entries depends on the first column's first leaf
+  // (C'[0], C'[c], C'[2c], C'[3c], c = L / d1): that leaf hashed
+  // log2(d1 / 4) times is the column root, then log2(c) times the party root.
+  uint8_t *rts = ob.alloc<uint8_t>(32ull * N), *prev_rts = ob.alloc<uint8_t>(32ull * N);
+  int batch_depth = 0;
+  {
+    const uint64_t c = L / sc.degrees[1];
+    k_roots<<<1, 64, 0, s>>>(Cp, L, c, ilog2(sc.degrees[1] / 4) + ilog2(c), N, logN, nullptr, rts, tr, off.broots,
+                             off.bleader);
+    GBZ_CUDA(cudaGetLastError());
+    // the batch tree is the commitment a tensor code would inherit when no
+    // concatenated commitment follows it (levels over c column roots)
+    GBZ_CUDA(cudaMemcpyAsync(prev_rts, rts, 32ull * N, cudaMemcpyDeviceToDevice, s));
+    batch_depth = ilog2(c);
+  }
+  int32_t *qp = ob.alloc<int32_t>(kPcsMaxQueries), *qpos = ob.alloc<int32_t>(kPcsMaxQueries);
+  k_indexes<<<1, 256, 0, s>>>(st, sc.queries[0], N, (uint32_t)L, qp, qpos, tr, off.bqueries);
+  GBZ_CUDA(cudaGetLastError());
+
+  // the rounds (coPCS.cpp:1452-1600)
+  fe *Ld = ob.alloc<fe>(1 << kPcsMaxLogDeg), *vscr = ob.alloc<fe>(4 << kPcsMaxLogDeg), *y = ob.alloc<fe>(kPcsMaxQueries);
+  fe *base = ob.alloc<fe>(kPcsMaxQueries), *wts = ob.alloc<fe>((uint64_t)N * kPcsMaxQueries);
+  uint64_t n = Bs, cpl = L;
+  int prev_depth = batch_depth;
+  // every party's RS fold of a codeword of length len by 2^logd with the
+  // current weights Ld (k_fold_q)
+  auto rs_fold = [&](const fe *cw, uint64_t len, int logd, fe *out, uint64_t ostride) {
+    fe *iQ = ob.alloc<fe>(len), *t2 = ob.alloc<fe>(len);
+    GBZ_CUDA(cudaMemsetAsync(iQ, 0, 16 * len, s));
+    GBZ_CUDA(cudaMemcpyAsync(iQ, Ld, 16ull << logd, cudaMemcpyDeviceToDevice, s));
+    ntt_launch(ctx->tables(ilog2(len)), iQ, len, iQ, t2, true, s);
+    const fe scale = fe_make(len >> logd, 0);
+    k_fold_q<<<dim3(grid(len >> logd), N), 256, 0, s>>>(cw, len, logd, iQ, scale, out, ostride);
+    GBZ_CUDA(cudaGetLastError());
+  };
+  const int nrounds = sc.rounds - 1;
+  for (int i = 0; i < nrounds; i++) {
+    const RoundOffs &ro = off.r[i];
+    const int d = sc.degrees[i + 1], logd = ilog2((uint64_t)d), D = 2 * d;
+    const uint64_t blocks = (uint64_t)N * n / d;
+    // pcs_sumcheck_phase1 (coPCS.cpp:547-566): every party's blocks in one
+    // batched transform, the products summed per party
+    const NttTables &td = ctx->tables(logd), &tD = ctx->tables(logd + 1);
+    fe *e1 = ob.alloc<fe>(blocks * D), *e2 = ob.alloc<fe>(blocks * D), *coef = ob.alloc<fe>((uint64_t)N * n);
+    ntt_batched(td, bcd, d, (uint32_t)d, coef, blocks, true, s);
+    ntt_batched(tD, coef, d, (uint32_t)d, e1, blocks, false, s);
+    ntt_batched(td, B, d, (uint32_t)d, coef, blocks, true, s);
+    ntt_batched(tD, coef, d, (uint32_t)d, e2, blocks, false, s);
+    const uint64_t pblocks = n / d;
+    const int lanes = D >= 256 ? 1 : 256 / D;
+    const int per_cta = (int)std::max<uint64_t>((uint64_t)lanes, (pblocks + 607) / 608);
+    fe *cpart = ob.alloc<fe>((uint64_t)D * cophase1_parts(pblocks, per_cta));
+    for (int p = 0; p < N; p++)
+      cophase1_reduce_launch(e1 + (uint64_t)p * pblocks * D, e2 + (uint64_t)p * pblocks * D, nullptr, nullptr, nullptr,
+                             pblocks, logd + 1, per_cta, cpart, H + (uint64_t)p * D, s);
+    k_put_party<<<dim3(grid(D), N), 256, 0, s>>>(H, D, N, tr, ro.pp, 16ull * D);
+    aggregate_launch(H, N, D, dlam, poly, s);
+    k_round_verify<<<1, 256, 0, s>>>(st, poly, logd, Ld, vscr, tr, ro.poly, ro.chal);
+    GBZ_CUDA(cudaGetLastError());
+    // pcs_sumcheck_phase2 (coPCS.cpp:571-587)
+    cophase2_launch(bcd, (uint64_t)N * n, Ld, logd, coef, s);
+    GBZ_CUDA(cudaMemcpyAsync(bcd, coef, 16ull * N * n / d, cudaMemcpyDeviceToDevice, s));
+    cophase2_launch(B, (uint64_t)N * n, Ld, logd, coef, s);
+    GBZ_CUDA(cudaMemcpyAsync(B, coef, 16ull * N * n / d, cudaMemcpyDeviceToDevice, s));
+    n /= d;
+    const bool last = i == nrounds - 1;
+    fe *Cpn, *fold;
+    uint64_t cpl_new;
+    const uint64_t seg_n = cpl / d;
+    if (!last) {
+      // encode_concatenated (coPCS.cpp:653-677) and commit_concatenated (:679-738)
+      const int r0 = sc.rate0[i + 2], r1 = sc.rate1[i + 2], d2 = sc.degrees[i + 2];
+      cpl_new = n * r0;
+      const uint64_t rows = cpl_new / d2, Dc = (uint64_t)d2 * r1;
+      if (ilog2(cpl_new) > kMaxNttLogN || Dc > (1u << 13) || (uint64_t)d2 > cpl_new)
+        throw ArgError("pcs: concatenated code shape out of range");
+      Cpn = ob.alloc<fe>((uint64_t)N * cpl_new);
+      fe *Cn = ob.alloc<fe>((uint64_t)N * rows * Dc);
+      fe *tmp2 = ob.alloc<fe>((uint64_t)N * cpl_new);
+      ntt_launch_rows(ctx->tables(ilog2(cpl_new)), bcd, n, n, Cpn, cpl_new, N, tmp2, false, s);
+      const NttTables &tc = ctx->tables(ilog2(Dc));
+      for (int p = 0; p < N; p++)
+        ntt_batched_strided(tc, Cpn + (uint64_t)p * cpl_new, rows, (uint32_t)d2, Cn + (uint64_t)p * rows * Dc, rows,
+                            false, s);
+      const uint64_t clen = rows * Dc;
+      k_roots<<<1, 64, 0, s>>>(Cn, clen, 1, ilog2(clen / 4), N, logN, nullptr, rts, tr, ro.roots, ro.leader);
+      GBZ_CUDA(cudaGetLastError());
+      GBZ_CUDA(cudaMemcpyAsync(prev_rts, rts, 32ull * N, cudaMemcpyDeviceToDevice, s));
+      prev_depth = ilog2(clen / 4);
+      fold = ob.alloc<fe>((uint64_t)N * seg_n);
+      rs_fold(Cp, cpl, logd, fold, seg_n);
+    } else {
+      // RS_multifold5 + commit_tensorcode (coPCS.cpp:1566-1570, 893-919)
+      cpl_new = cpl / d;
+      Cpn = ob.alloc<fe>((uint64_t)N * cpl_new);
+      rs_fold(Cp, cpl, logd, Cpn, cpl_new);
+      fold = Cpn;
+      // commit_tensorcode hands MT_commit_Blake the previous commitment's
+      // levels; MT_commit_Blake resizes only an empty levels vector
+      // (merkle_tree.cpp:205-208), so over a shallower tree the old top level
+      // stays and the root it reports is the previous root.
+      if (cpl_new < 4) throw ArgError("pcs: the tensor codeword is shorter than one leaf");
+      const int depth = ilog2(cpl_new / 4);
+      // a deeper new tree than the reused levels vector holds is undefined
+      // behaviour in the reference (create_tree_blake writes past its end)
+      if (depth > prev_depth) throw ArgError("pcs: tensor code deeper than the previous commitment");
+      const bool stale = prev_depth > depth;
+      k_roots<<<1, 64, 0, s>>>(Cpn, cpl_new, 1, depth, N, logN, stale ? prev_rts : nullptr, rts, tr, ro.roots,
+                               ro.leader);
+      GBZ_CUDA(cudaGetLastError());
+    }
+    // delegate_checks (coPCS.cpp:740-891)
+    const int l = sc.queries[i + 1];
+    k_indexes<<<1, 256, 0, s>>>(st, l, N, (uint32_t)seg_n, qp, qpos, tr, ro.queries);
+    k_gather<<<grid((uint64_t)l * d), 256, 0, s>>>(Cp, cpl, seg_n, d, fold, seg_n, qp, qpos, l, y, tr, ro.y, ro.seg);
+    GBZ_CUDA(cudaGetLastError());
+    if (!last) {
+      k_check_y<<<grid(l), 256, 0, s>>>(Cpn, cpl_new, (uint32_t)sc.rate0[i + 2], (uint32_t)sc.rate0[i + 1], qp, qpos,
+                                        y, l, st);
+      GBZ_CUDA(cudaGetLastError());
+    }
+    k_s_update<<<1, 1, 0, s>>>(st, y, l, last ? 0 : 1, tr, ro.s, ro.K);
+    GBZ_CUDA(cudaGetLastError());
+    if (!last) {
+      // pcs_sumcheck_phase3 (coPCS.cpp:634-648) with the scaled queries
+      const int logw = ilog2((uint64_t)sc.rate0[i + 2] * n);
+      k_phase3_prep<<<grid(l), 256, 0, s>>>(st, qp, qpos, l, (uint32_t)sc.rate0[i + 2], (uint32_t)sc.rate0[i + 1],
+                                             logw, dscale, N, base, wts);
+      k_phase3<<<dim3(grid((n + kP3Chunk - 1) / kP3Chunk), N), 256, 0, s>>>(B, n, base, wts, l);
+      GBZ_CUDA(cudaGetLastError());
+    }
+    Cp = Cpn;
+    cpl = cpl_new;
+  }
+  // send_pcs_data: every party's data, B and C'
+  {
+    const uint64_t per = 2 * n + cpl;
+    k_put_party<<<dim3(grid(n), N), 256, 0, s>>>(bcd, n, N, tr, off.final_, 16 * per);
+    k_put_party<<<dim3(grid(n), N), 256, 0, s>>>(B, n, N, tr, off.final_ + 16 * n, 16 * per);
+    k_put_party<<<dim3(grid(cpl), N), 256, 0, s>>>(Cp, cpl, N, tr, off.final_ + 32 * n, 16 * per);
+    GBZ_CUDA(cudaGetLastError());
+  }
+  // the chain state out, the flags checked
+  PcsDev hst;
+  GBZ_CUDA(cudaMemcpyAsync(&hst, st, sizeof(PcsDev), cudaMemcpyDeviceToHost, s));
+  if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaMemcpyAsync(transcript, tr, lay.bytes, cudaMemcpyDeviceToHost, s));
+  GBZ_CUDA(cudaStreamSynchronize(s));
+  if (mem == GBZ_MEM_HOST) {
+    fs[0] = hst.fs.re;
+    fs[1] = hst.fs.im;
+  } else {
+    GBZ_CUDA(cudaMemcpy(fs, &hst.fs, 16, cudaMemcpyHostToDevice));
+  }
+  if (hst.error) return fail(ctx, GBZ_ECHECK, hst.error & 1 ? "pcs: a round message does not match the claim"
+                                                            : "pcs: a delegate check failed");
+  API_END(ctx)
+}
+
+}  // extern "C"

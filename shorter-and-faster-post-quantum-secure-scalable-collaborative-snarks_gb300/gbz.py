@@ -47,7 +47,8 @@ EXPORTS = (
     "gbz_tensor_eval_vector", "gbz_pcs_sumcheck_phase3", "gbz_ntt_set_shape", "gbz_ntt_get_shape",
     "gbz_ntt_autotune", "gbz_merkle_set_fusion", "gbz_merkle_get_fusion", "gbz_merkle_autotune",
     "gbz_set_graphs", "gbz_ntt_full_twiddles", "gbz_encode_concatenated", "gbz_leader_root",
-    "gbz_whir_batch_schedule", "gbz_whir_batch_open",
+    "gbz_whir_batch_schedule", "gbz_whir_batch_open", "gbz_pcs_schedule", "gbz_pcs_commit", "gbz_pcs_free",
+    "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -161,6 +162,12 @@ def _load():
         "gbz_party_sumcheck": (c_int, [vp, c_int, vp, vp, vp, u64, c_int, vp, c_int, vp, vp, vp, vp, vp, vp, c_int]),
         "gbz_whir_batch_schedule": (c_int, [c_int, vp, c_int, c_int, vp, vp, vp, vp, vp]),
         "gbz_whir_batch_open": (c_int, [vp, c_int, vp, vp, vp, vp, vp, vp, c_int, c_int, vp, vp, u64, c_int]),
+        "gbz_pcs_schedule": (c_int, [c_int, u64, c_int, vp, vp, vp, vp, vp]),
+        "gbz_pcs_commit": (c_int, [vp, c_int, u64, c_int, vp, vp, vp, vp, c_int, ctypes.POINTER(vp), vp, vp]),
+        "gbz_pcs_free": (None, [vp]),
+        "gbz_pcs_info": (c_int, [vp, vp, vp, vp, vp]),
+        "gbz_pcs_commit_data": (c_int, [vp, vp, c_int, vp, vp, vp, c_int]),
+        "gbz_pcs_open": (c_int, [vp, vp, vp, c_int, vp, vp, vp, u64, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -738,11 +745,84 @@ def field_ops_host(a, b):
     return outs
 
 
+def _rates(rates):
+    r0 = np.array([r[0] for r in rates], dtype=np.int32)
+    r1 = np.array([r[1] if len(r) > 1 else 0 for r in rates], dtype=np.int32)
+    return r0, r1
+
+
+def pcs_schedule(N, M, rates):
+    """prepare_parameters (coPCS.cpp:38-72): (degrees, queries, random shares per party)."""
+    r0, r1 = _rates(rates)
+    k = len(rates)
+    deg, q, rnd = np.zeros(k, dtype=np.int32), np.zeros(k, dtype=np.int32), ctypes.c_uint64(0)
+    st = lib.gbz_pcs_schedule(N, M, k, _ptr(r0), _ptr(r1), _ptr(deg), _ptr(q), ctypes.byref(rnd))
+    if st != OK:
+        raise GbzError(st, "gbz_pcs_schedule rejected N=%d M=%d" % (N, M))
+    return [int(x) for x in deg], [int(x) for x in q], int(rnd.value)
+
+
+class PcsCommitment:
+    """A collaborative-PCS commitment of N parties held on the device (gbz_pcs)."""
+
+    def __init__(self, ctx, h, N, M, rates):
+        self.ctx, self.h, self.N, self.M, self.rates = ctx, h, N, M, rates
+        b, rl, cl, tb = ctypes.c_int(0), ctypes.c_uint64(0), ctypes.c_uint64(0), ctypes.c_uint64(0)
+        ctx.check(lib.gbz_pcs_info(h, ctypes.byref(b), ctypes.byref(rl), ctypes.byref(cl), ctypes.byref(tb)))
+        self.batches, self.row_len, self.codeword_len = b.value, rl.value, cl.value
+        self.open_bytes = tb.value
+
+    def data(self, party):
+        """(Commit_data rows, codewords, column-root tree levels) of one party."""
+        rows = np.zeros((self.batches, self.row_len, 2), dtype=np.uint64)
+        cws = np.zeros((self.batches, self.codeword_len, 2), dtype=np.uint64)
+        lv = np.zeros((2 * self.codeword_len - 1, 32), dtype=np.uint8)
+        self.ctx.check(lib.gbz_pcs_commit_data(self.ctx.h, self.h, party, _ptr(rows), _ptr(cws), _ptr(lv), MEM_HOST))
+        return rows, cws, lv
+
+    def open(self, r, K, fs):
+        """PCS_open_new's parties + aggregation: (transcript bytes, fs after)."""
+        r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+        K = np.ascontiguousarray(K, dtype=np.uint64).reshape(2)
+        f = np.array(np.asarray(fs, dtype=np.uint64).reshape(2), copy=True)
+        tr = np.zeros(self.open_bytes, dtype=np.uint8)
+        self.ctx.check(lib.gbz_pcs_open(self.ctx.h, self.h, _ptr(r), r.shape[0], _ptr(K), _ptr(f), _ptr(tr),
+                                        self.open_bytes, MEM_HOST))
+        return tr.tobytes(), f
+
+    def free(self):
+        if self.h:
+            lib.gbz_pcs_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def pcs_commit(ctx, N, M, rates, shares, random):
+    """PCS_commit (coPCS.cpp:236-250) of N parties: (commitment, party roots, leader root)."""
+    r0, r1 = _rates(rates)
+    sh = np.ascontiguousarray(shares, dtype=np.uint64)
+    rn = np.ascontiguousarray(random, dtype=np.uint64)
+    h = ctypes.c_void_p()
+    roots = np.zeros((N, 32), dtype=np.uint8)
+    leader = np.zeros(32, dtype=np.uint8)
+    ctx.check(lib.gbz_pcs_commit(ctx.h, N, M, len(rates), _ptr(r0), _ptr(r1), _ptr(sh), _ptr(rn), MEM_HOST,
+                                 ctypes.byref(h), _ptr(roots), _ptr(leader)))
+    return PcsCommitment(ctx, h, N, M, rates), roots, leader
+
+
+PCS_UNITS = {32: 32, 33: 32, 37: 4}
+
+
 def parse_transcript(buf):
     """[(tag, count, payload bytes)] of a transcript."""
     buf = bytes(buf)
     out, off = [], 0
-    units = {1: 32, 9: 32, 13: 32, 10: 4}
+    units = {1: 32, 9: 32, 13: 32, 10: 4, **PCS_UNITS}
     while off < len(buf):
         tag, count = np.frombuffer(buf, dtype=np.uint32, count=2, offset=off)
         unit = units.get(int(tag), 16)

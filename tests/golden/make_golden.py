@@ -298,7 +298,8 @@ def gen_parties():
                  "commit_roots": [hx(x[4:]) + ":%d" % struct.unpack_from("<I", x)[0] for x in big_roots[:3]],
                  "party_polys": [hx(r[2]) for r in recs if r[0] == "PAGI"],
                  "queries": gidx if small else [sha(str(g).encode()) for g in gidx],
-                 "final": [(hx if small else sha)(r[2]) for r in recs if r[0] in ("SPDA", "SPDB", "SPDC")]}
+                 "final": [(hx if small else sha)(r[2]) for r in recs if r[0] in ("SPDA", "SPDB", "SPDC")],
+                 "final_bytes": [len(r[2]) for r in recs if r[0] in ("SPDA", "SPDB", "SPDC")]}
             case["ranks"].append(e)
         name = "parties_N%d_M%d" % (N, logM)
         with open(os.path.join(HERE, name + ".json"), "w") as f:
