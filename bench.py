@@ -37,6 +37,7 @@ no collective); `value` sums the proofs of all ranks over the slowest rank's
 time.
 """
 import argparse
+import hashlib
 import ctypes
 import json
 import os
@@ -386,62 +387,90 @@ def run_many(gbz, O, ctx, repeats):
     return out
 
 
-def run_party_shares(gbz, O, ctx, repeats, P=16, log_share=22, rate=2):
-    """Party shares on one device: a 2^26 base-field witness split
-    additively into P = 16 party shares of 2^22; every party commits its
-    share as PCS_commit does (16 rows of 2^18, coPCS Encode at rate 1/2,
-    per-column Blake3 roots and the tree over them, leader root), then the
-    16 parties run the distributed quadratic sumcheck of sum w(x) eq(z, x)
-    with the leader's aggregation of their round messages, all device
-    resident (torch buffers, C-ABI calls on device pointers)."""
+PCS_RATES = [[4], [4], [4, 4], [4, 4]]  # the reference's coPCS test (main.cpp:54)
+
+
+def pcs_point(gbz, n):
+    """The opening point of the coPCS test: hash_to_field({0}) n times from a
+    fresh chain (main.cpp:83-85); returns (r, chain state)."""
+    fs = np.zeros(2, dtype=np.uint64)
+    r = []
+    for _ in range(n):
+        fs = gbz.hash_to_field(fs, np.zeros((1, 2), dtype=np.uint64))
+        r.append(fs.copy())
+    return np.array(r, dtype=np.uint64), fs
+
+
+def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
+    """Configuration 4: the reference's coPCS test (main.cpp:49-163) with
+    N = 16 parties on one device, M = 2^24 shared coefficients (2^22 share
+    entries per party): PCS_commit, the claim (F_ip) and PCS_open_new up to
+    the leader's delegation, all device resident (torch buffers, C-ABI calls
+    on device pointers).  The shares are the ones the reference's rank 0
+    deals (glibc's default stream, generated on the host before timing); the
+    transcript is compared with the reference's own 16-rank run when its
+    digest fixture is present (tests/golden/parties_N16_M24.json)."""
     import torch
-    M = 1 << log_share
-    R = 16                         # BATCH_FACTOR / 2 rows of shares per party
-    logrow = log_share - 4
-    rng = np.random.default_rng(0x5EEF4)
-    shares = torch.from_numpy(O.witness(0x5EED0000 + 4 * 65536, P * M).view(np.int64)).cuda()
-    nz = (P * M).bit_length() - 1
-    z = torch.from_numpy(rng.integers(0, (1 << 61) - 1, size=(nz, 2), dtype=np.uint64).view(np.int64)).cuda()
-    beta = torch.empty((P * M, 2), dtype=torch.int64, device="cuda")  # eq table of z, on the device
-    ctx.check(gbz.lib.gbz_precompute_beta(ctx.h, z.data_ptr(), nz, beta.data_ptr(), gbz.MEM_DEVICE))
-    cw = torch.empty((P, R, rate << logrow, 2), dtype=torch.int64, device="cuda")
-    L = rate << logrow
-    levels = torch.empty((P, 2 * L - 1, 32), dtype=torch.uint8, device="cuda")
-    roots = torch.empty((P, 32), dtype=torch.uint8, device="cuda")
+    M = 1 << logM
+    deg, q, rnd = gbz.pcs_schedule(N, M, PCS_RATES)
+    shares, random = O.copcs_party_shares(N, M, rnd * N // 4)
+    sh = torch.from_numpy(shares.view(np.int64)).cuda()
+    rn = torch.from_numpy(random.view(np.int64)).cuda()
+    r0 = np.array([x[0] for x in PCS_RATES], dtype=np.int32)
+    r1 = np.array([x[1] if len(x) > 1 else 0 for x in PCS_RATES], dtype=np.int32)
+    r, fs0 = pcs_point(gbz, logM + 1)
+    rd = torch.from_numpy(r.view(np.int64)).cuda()
+    Kd = torch.zeros(2, dtype=torch.int64, device="cuda")
+    fsd = torch.zeros(2, dtype=torch.int64, device="cuda")
     torch.cuda.synchronize()
+    lib = gbz.lib
 
     def commit():
-        for p in range(P):
-            rows = shares[p * M:(p + 1) * M]
-            ctx.check(gbz.lib.gbz_encode_rows(ctx.h, rows.data_ptr(), R, logrow, rate, 0, cw[p].data_ptr(),
-                                              gbz.MEM_DEVICE))
-            ctx.check(gbz.lib.gbz_column_merkle(ctx.h, cw[p].data_ptr(), R, logrow + (rate.bit_length() - 1), P,
-                                                levels[p].data_ptr(), roots[p].data_ptr(), gbz.MEM_DEVICE))
+        h = ctypes.c_void_p()
+        ctx.check(lib.gbz_pcs_commit(ctx.h, N, M, len(PCS_RATES), r0.ctypes.data, r1.ctypes.data, sh.data_ptr(),
+                                     rn.data_ptr(), gbz.MEM_DEVICE, ctypes.byref(h), None, None))
+        return h
+
+    def open_(h, tr):
+        ctx.check(lib.gbz_pcs_claim(ctx.h, h, rd.data_ptr(), r.shape[0], Kd.data_ptr(), gbz.MEM_DEVICE))
+        fsd.copy_(torch.from_numpy(fs0.view(np.int64)))
+        ctx.check(lib.gbz_pcs_open(ctx.h, h, rd.data_ptr(), r.shape[0], Kd.data_ptr(), fsd.data_ptr(),
+                                   tr.data_ptr(), tr.numel(), gbz.MEM_DEVICE))
         ctx.synchronize()
 
-    commit()
-    # the claim sum_x w(x) eq(z, x) = H(0) + H(1) of the first round message
-    h = ctx.sumcheck_round(gbz.SC_QUADRATIC, [shares, beta])
-    P61 = (1 << 61) - 1
-    y0 = [(int(h[0][k]) + int(h[1][k]) + 2 * int(h[2][k])) % P61 for k in (0, 1)]
-    sumcheck_y = ctx.party_sumcheck(gbz.SC_QUADRATIC, [shares, beta], P, offset=4, y=y0)  # warm-up, checked
-    t_c, t_s = [], []
+    h = commit()
+    nbytes = ctypes.c_uint64(0)
+    ctx.check(lib.gbz_pcs_info(h, None, None, None, ctypes.byref(nbytes)))
+    tr = torch.zeros(nbytes.value, dtype=torch.uint8, device="cuda")
+    open_(h, tr)  # warm-up (checked on the device: GBZ_ECHECK otherwise)
+    lib.gbz_pcs_free(h)
+    t_c, t_o = [], []
     for _ in range(repeats):
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        commit()
+        h = commit()
         t1 = time.perf_counter()
-        ctx.party_sumcheck(gbz.SC_QUADRATIC, [shares, beta], P, offset=4, y=y0)
+        open_(h, tr)
         t2 = time.perf_counter()
+        lib.gbz_pcs_free(h)
         t_c.append(t1 - t0)
-        t_s.append(t2 - t1)
-    c_ms, s_ms = 1e3 * min(t_c), 1e3 * min(t_s)
-    return {"party_shares": {
-        "workload": "2^26 witness as 16 party shares of 2^22: per-party PCS_commit (16 rows of "
-                    "2^18, coPCS Encode rate 1/2, column Blake3 roots + tree, leader root) and the 16-party "
-                    "distributed quadratic sumcheck with the leader's aggregation, one device",
-        "parties": P, "share_len": M, "commit_ms": c_ms, "sumcheck_ms": s_ms, "total_ms": c_ms + s_ms,
-        "runs_per_s": 1e3 / (c_ms + s_ms), "rounds": int(len(sumcheck_y["challenges"])),
-        "timing": "host wall clock around synchronised device calls, best of %d" % repeats}}
+        t_o.append(t2 - t1)
+    digest = hashlib.sha256(tr.cpu().numpy().tobytes()).hexdigest()
+    out = {"workload": "the reference's coPCS test (PCS_commit + F_ip + PCS_open_new to the leader's "
+                       "delegation) with %d parties on one device, M = 2^%d (2^%d share entries per party), "
+                       "rates {{4},{4},{4,4},{4,4}}" % (N, logM, logM + 2 - (N.bit_length() - 1)),
+           "parties": N, "share_len": 4 * M // N, "degrees": deg, "queries": q,
+           "commit_ms": 1e3 * min(t_c), "open_ms": 1e3 * min(t_o), "total_ms": 1e3 * (min(t_c) + min(t_o)),
+           "runs_per_s": 1.0 / (min(t_c) + min(t_o)), "transcript_bytes": int(nbytes.value),
+           "transcript_sha256": digest,
+           "timing": "host wall clock around the synchronised C-ABI calls (device pointers), best of %d" % repeats}
+    fx = os.path.join(ROOT, "tests", "golden", "parties_N%d_M%d.json" % (N, logM))
+    if os.path.exists(fx):
+        with open(fx) as f:
+            ref = json.load(f)
+        out["transcript_equals_reference"] = ref.get("gpu_transcript_sha256") == digest
+        out["reference_ranks_seconds_x86"] = ref.get("ref_seconds")
+    return {"party_shares": out}
 
 
 def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
@@ -663,6 +692,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default NTT and Merkle shapes")
     ap.add_argument("--rows-only", action="store_true", help="only the per-row measurements (profiling)")
     ap.add_argument("--rows-shift", type=int, default=0, help="divide the per-row sizes by 2^k")
+    ap.add_argument("--parties-only", action="store_true", help="only the party-shares (coPCS) measurement")
     args = ap.parse_args()
     ws, rank, local = dist_info()
     if ws > 1:
@@ -691,6 +721,11 @@ def main():
     rt.cudaEventSynchronize.argtypes = [ctypes.c_void_p]
     rt.cudaEventElapsedTime.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p]
     stream = gbz.lib.gbz_get_stream(ctx.h)
+
+    if args.parties_only:
+        print(json.dumps(run_party_shares(gbz, O, ctx, repeats=3)), flush=True)
+        ctx.close()
+        return
 
     if args.rows_only:
         fmul_peak, b3_peak = ctx.calibrate()

@@ -474,6 +474,14 @@ gbz_status gbz_pcs_info(const gbz_pcs *pcs, int *batches, uint64_t *row_len, uin
 gbz_status gbz_pcs_commit_data(gbz_ctx *ctx, const gbz_pcs *pcs, int party, uint64_t *rows, uint64_t *codewords,
                                uint8_t *levels, int mem);
 
+/* The claim the coPCS test opens (main.cpp:87-112): F_ip of the committed
+ * data at the point r (the same r as gbz_pcs_open): every party's inner
+ * product of its batched rows with precompute_beta(r[log2(N/4)..]), and the
+ * leader's unpack of the N values weighted by precompute_beta(r[0 ..
+ * log2(N/4))) into K (2 words).
+ * replaces F_ip (MPI_utils.cpp:483-553) on N ranks. */
+gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, int nr, uint64_t *K, int mem);
+
 /* The parties' side of PCS_open_new with the leader's aggregation
  * (coPCS.cpp:1310-1607, isPIOP = false): row batching and the batching
  * round, batch_commitments_new (:1242-1308), per round pcs_sumcheck_phase1

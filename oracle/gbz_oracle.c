@@ -942,23 +942,48 @@ void orc_column_merkle(const uint64_t *rows, int nrows, int logL, int N, uint8_t
   memcpy(root_out, cur, 32);
 }
 
+/* compute_secret_shares per group (MPI_utils.cpp:2747-2762): inverse
+ * transform of the _k group values, zero-pad to 2N, forward transform, party
+ * j takes entry 2j+1.  The map is linear, so it is built once (the images of
+ * the unit vectors through the same transforms) and applied to every group;
+ * the groups' random slots are drawn first, in the reference's order. */
+typedef struct { const uint64_t *v, *fill; const fe *mu; int64_t groups; int N, k, kk; uint64_t *shares; } shr_ctx;
+static void shares_range(void *p, int64_t lo, int64_t hi) {
+  shr_ctx *c = (shr_ctx *)p;
+  fe buf[32];
+  for (int64_t i = lo; i < hi; i++) {
+    for (int t = 0; t < c->k; t++) buf[t] = ld(c->v, i * c->k + t);
+    for (int t = c->k; t < c->kk; t++) buf[t] = c->fill ? ld(c->fill, i * (c->kk - c->k) + (t - c->k)) : f_zero();
+    for (int j = 0; j < c->N; j++) {
+      fe acc = f_zero();
+      for (int t = 0; t < c->kk; t++) acc = f_add(acc, f_mul(c->mu[j * c->kk + t], buf[t]));
+      st(c->shares, j * c->groups + i, acc);
+    }
+  }
+}
+
 void orc_secret_shares_g(const uint64_t *v, int64_t M, int N, int privacy, orc_prng *g, uint64_t *shares) {
   int k = N / 4, kk = N / 2;
   int64_t groups = M / k;
-  uint64_t buff[2 * 1024];
   int lk = ilog2_64(kk), l2n = ilog2_64(2 * N);
-  for (int64_t i = 0; i < groups; i++) {
+  fe *mu = (fe *)malloc(sizeof(fe) * (size_t)N * kk);
+  uint64_t buff[2 * 256];
+  for (int t = 0; t < kk; t++) {
     memset(buff, 0, sizeof(uint64_t) * 2 * 2 * N);
-    for (int j = 0; j < k; j++) { buff[2 * j] = v[2 * (i * k + j)]; buff[2 * j + 1] = v[2 * (i * k + j) + 1]; }
-    for (int j = k; j < kk; j++)
-      if (privacy) { buff[2 * j] = (uint64_t)orc_prng_next(g); buff[2 * j + 1] = 0; } /* F(random()) */
+    buff[2 * t] = 1;
     orc_fft(buff, lk, 1, 1);
-    orc_fft(buff, l2n, 0, 1);  /* buff is zero beyond kk */
-    for (int j = 0; j < N; j++) {
-      shares[2 * (j * groups + i)] = buff[2 * (2 * j + 1)];
-      shares[2 * (j * groups + i) + 1] = buff[2 * (2 * j + 1) + 1];
-    }
+    orc_fft(buff, l2n, 0, 1);
+    for (int j = 0; j < N; j++) mu[j * kk + t] = ld(buff, 2 * j + 1);
   }
+  uint64_t *fill = NULL;
+  if (privacy && kk > k) {
+    fill = (uint64_t *)malloc(sizeof(uint64_t) * 2 * (size_t)(groups * (kk - k)));
+    for (int64_t i = 0; i < groups * (kk - k); i++) { fill[2 * i] = (uint64_t)orc_prng_next(g); fill[2 * i + 1] = 0; }
+  }
+  shr_ctx c = {v, fill, mu, groups, N, k, kk, shares};
+  parallel_for(groups, 0, 1 << 12, shares_range, &c);
+  free(fill);
+  free(mu);
 }
 
 void orc_secret_shares(const uint64_t *v, int64_t M, int N, int privacy, uint32_t prng_seed, uint64_t *shares) {

@@ -427,6 +427,37 @@ __global__ void k_fold_q(const fe *cw, uint64_t n, int logd, const fe *iQ, fe sc
   out[blockIdx.y * ostride + i] = fmul(acc, scale);
 }
 
+// F_ip's local inner product (MPI_utils.cpp:489-491) of every party:
+// sum_{i < nrows} sum_j rows[p][i][j] b1[32 j + i] (v[32 j + i] = Commit_data[i][j],
+// main.cpp:99-103), as per-CTA partials.
+__global__ void __launch_bounds__(kRedThreads)
+k_fip_partial(const fe *rows, uint64_t pstride, int nrows, uint64_t len, const fe *b1, fe *partial) {
+  __shared__ fe red[kRedThreads];
+  fe acc = fe_zero();
+  const fe *r = rows + blockIdx.y * pstride;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < len; j += (uint64_t)gridDim.x * blockDim.x)
+    for (int i = 0; i < nrows; i++) acc = fadd(acc, fmul(r[(uint64_t)i * len + j], b1[32 * j + i]));
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fadd(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(uint64_t)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+
+// The leader's combination (MPI_utils.cpp:514-527): K = sum_p lambda_p y_p.
+__global__ void k_fip_combine(const fe *partial, int nblk, int N, const fe *lambda, fe *K) {
+  if (threadIdx.x) return;
+  fe acc = fe_zero();
+  for (int p = 0; p < N; p++) {
+    fe y = fe_zero();
+    for (int k = 0; k < nblk; k++) y = fadd(y, partial[(uint64_t)p * nblk + k]);
+    acc = fadd(acc, fmul(lambda[p], y));
+  }
+  *K = acc;
+}
+
 // A record payload copied from party-major vectors: out[p][0..len) -> tr.
 __global__ void k_put_party(const fe *v, uint64_t len, int N, uint8_t *tr, uint64_t off, uint64_t rec_stride) {
   const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -800,6 +831,51 @@ gbz_status gbz_pcs_commit_data(gbz_ctx *ctx, const gbz_pcs *pcs, int party, uint
   if (levels)
     GBZ_CUDA(cudaMemcpyAsync(levels, pcs->levels + 32ull * party * (2 * L - 1), 32 * (2 * L - 1), k, ctx->stream));
   finish(ctx, mem);
+  API_END(ctx)
+}
+
+gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, int nr, uint64_t *K, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(pcs, "pcs");
+  need(r, "r");
+  need(K, "K");
+  if (pcs->device != ctx->device) throw ArgError("pcs: committed on another device");
+  const int N = pcs->sc.N, nb = pcs->batches, lk = ilog2(N / 4), logBs = ilog2(pcs->Bs);
+  if (nr != lk + 5 + logBs) throw ArgError("pcs: the point must have log2(N/4) + 5 + log2(row length) entries");
+  cudaStream_t s = ctx->stream;
+  std::vector<fe> hr(nr);
+  if (mem == GBZ_MEM_DEVICE) {
+    GBZ_CUDA(cudaMemcpyAsync(hr.data(), r, 16ull * nr, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaStreamSynchronize(s));
+  } else {
+    for (int i = 0; i < nr; i++) hr[i] = fe_make(r[2 * i], r[2 * i + 1]);
+  }
+  // b2 = precompute_beta(r[0 .. log2(N/4))) weights the unpacked shares
+  // (MPI_utils.cpp:525-527): the same form as sumcheck_aggr's, g[2i] = b2[i]
+  std::vector<fe> b2(N / 4, fe_one());
+  for (int i = 0; i < (1 << lk); i++) {
+    fe v = fe_one();
+    for (int t = 0; t < lk; t++) {
+      const fe x = hr[t];
+      v = fmul(v, ((i >> t) & 1) ? x : fsub(fe_one(), x));
+    }
+    b2[i] = v;
+  }
+  std::vector<fe> lambda = aggregate_weights(N, b2.data());
+  OpenBufs ob;
+  fe *dr = ob.alloc<fe>(nr), *dl = ob.alloc<fe>(N), *b1 = ob.alloc<fe>(32ull * pcs->Bs), *dK = ob.alloc<fe>(1);
+  GBZ_CUDA(cudaMemcpyAsync(dr, hr.data(), 16ull * nr, cudaMemcpyHostToDevice, s));
+  GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
+  beta_launch(dr + lk, 5 + logBs, b1, s);
+  const int nblk = (int)std::min<uint64_t>(64, (pcs->Bs + kRedThreads - 1) / kRedThreads);
+  fe *partial = ob.alloc<fe>((uint64_t)N * nblk);
+  k_fip_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(pcs->cd, (uint64_t)nb * pcs->Bs, nb - 1, pcs->Bs, b1, partial);
+  k_fip_combine<<<1, 32, 0, s>>>(partial, nblk, N, dl, dK);
+  GBZ_CUDA(cudaGetLastError());
+  if (mem == GBZ_MEM_DEVICE) GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToDevice, s));
+  else GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToHost, s));
+  GBZ_CUDA(cudaStreamSynchronize(s));
   API_END(ctx)
 }
 

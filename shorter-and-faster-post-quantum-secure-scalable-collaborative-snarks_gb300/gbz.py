@@ -48,7 +48,7 @@ EXPORTS = (
     "gbz_ntt_autotune", "gbz_merkle_set_fusion", "gbz_merkle_get_fusion", "gbz_merkle_autotune",
     "gbz_set_graphs", "gbz_ntt_full_twiddles", "gbz_encode_concatenated", "gbz_leader_root",
     "gbz_whir_batch_schedule", "gbz_whir_batch_open", "gbz_pcs_schedule", "gbz_pcs_commit", "gbz_pcs_free",
-    "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open",
+    "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open", "gbz_pcs_claim",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -168,6 +168,7 @@ def _load():
         "gbz_pcs_info": (c_int, [vp, vp, vp, vp, vp]),
         "gbz_pcs_commit_data": (c_int, [vp, vp, c_int, vp, vp, vp, c_int]),
         "gbz_pcs_open": (c_int, [vp, vp, vp, c_int, vp, vp, vp, u64, c_int]),
+        "gbz_pcs_claim": (c_int, [vp, vp, vp, c_int, vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -779,6 +780,13 @@ class PcsCommitment:
         lv = np.zeros((2 * self.codeword_len - 1, 32), dtype=np.uint8)
         self.ctx.check(lib.gbz_pcs_commit_data(self.ctx.h, self.h, party, _ptr(rows), _ptr(cws), _ptr(lv), MEM_HOST))
         return rows, cws, lv
+
+    def claim(self, r):
+        """F_ip of the committed data at r (MPI_utils.cpp:483-553): K."""
+        r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+        K = np.zeros(2, dtype=np.uint64)
+        self.ctx.check(lib.gbz_pcs_claim(self.ctx.h, self.h, _ptr(r), r.shape[0], _ptr(K), MEM_HOST))
+        return K
 
     def open(self, r, K, fs):
         """PCS_open_new's parties + aggregation: (transcript bytes, fs after)."""

@@ -18,6 +18,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
@@ -247,6 +249,96 @@ def capture_records(path):
     return out
 
 
+def expected_open_transcript(ranks, N, logM, rates):
+    """The transcript gbz_pcs_open must write (layout: include/gbz.h), rebuilt
+    from the reference ranks' own records: every party's round messages
+    (PAGI), the leader's aggregates (PAGO) and challenges (H2FO), the roots
+    each rank reported, the queries each rank drew (merged party by party,
+    as get_segments orders them), the leader's gathered answers and segments
+    (GSYO, GSSG), the phase-3 challenges, the final data each party sent
+    (SPDA/SPDB/SPDC), and the running claim K, which the reference keeps in a
+    local: K0 = F_ip (FIPK), then the updates of coPCS.cpp:1433, 1481-1483,
+    1545-1547 on the captured values."""
+    import struct
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gbz_oracle as orc
+    import gbz_pcs_oracle as po
+    sched = po.schedule(N, 1 << logM, rates)
+    deg = sched["degrees"]
+    fe_list = lambda b: [tuple(int(x) for x in v) for v in np.frombuffer(b, dtype=np.uint64).reshape(-1, 2)]
+    rec = lambda tag, count, payload: struct.pack("<II", tag, count) + payload
+    lead = ranks[0]
+    h2fo = [r[2] for r in lead if r[0] == "H2FO"][logM + 1:]
+    pago = [r[2] for r in lead if r[0] == "PAGO"]
+    pagi = [[r[2] for r in rk if r[0] == "PAGI"] for rk in ranks]
+    gidx = [[r for r in rk if r[0] == "GIDX"] for rk in ranks]
+    gsyo = [r[2] for r in lead if r[0] == "GSYO"]
+    gssg = [r[2] for r in lead if r[0] == "GSSG"]
+    K = fe_list([r[2] for r in lead if r[0] == "FIPK"][0])[0]
+
+    def roots_of(kind):
+        out = []
+        for rk in ranks:
+            ctrb = [r[2] for r in rk if r[0] == "CTRB"]
+            mt = [r[2] for i, r in enumerate(rk) if r[0] == "MTCB"
+                  and struct.unpack_from("<I", r[2])[0] not in (32, 8) and rk[i - 1][0] != "WCIA"]
+            out.append(ctrb[1 if rk is not lead else 2][4:] if kind == "batch" else mt[kind][4:])
+        return out
+
+    lead_roots = [r[2][4:] for r in lead if r[0] == "CTRB" and struct.unpack_from("<I", r[2])[0] == N]
+
+    def queries(k):
+        w = b""
+        for rk in range(N):
+            words = struct.unpack("<%dI" % gidx[rk][k][1], gidx[rk][k][2])[4:]
+            for a, b in zip(words[0::2], words[1::2]):
+                w += struct.pack("<II", a, b)
+        return w
+
+    out = b""
+    out += rec(34, 3 * N, b"".join(pagi[rk][0] for rk in range(N)))
+    out += rec(35, 3, pago[0])
+    out += rec(36, 1, h2fo[0])
+    p = fe_list(pago[0])
+    rf = fe_list(h2fo[0])[0]
+    K = po.fmul(rf, po.fadd(p[1], po.fmul(rf, p[0])))
+    out += rec(41, 1, np.array([K], dtype=np.uint64).tobytes())
+    out += rec(32, N, b"".join(roots_of("batch")))
+    out += rec(33, 1, lead_roots[1])
+    out += rec(37, 2 * sched["queries"][0], queries(0))
+    nround = len(rates) - 1
+    for i in range(nround):
+        d = deg[i + 1]
+        out += rec(34, 2 * d * N, b"".join(pagi[rk][1 + i] for rk in range(N)))
+        out += rec(35, 2 * d, pago[1 + i])
+        c = h2fo[1 + 2 * i]
+        s_ = h2fo[2 + 2 * i]
+        out += rec(36, 1, c)
+        out += rec(32, N, b"".join(roots_of(i)))
+        out += rec(33, 1, lead_roots[2 + i])
+        out += rec(37, 2 * sched["queries"][i + 1], queries(1 + i))
+        out += rec(38, sched["queries"][i + 1], gsyo[i])
+        out += rec(39, sched["queries"][i + 1] * d, gssg[i])
+        out += rec(40, 1, s_)
+        poly = fe_list(pago[1 + i])
+        L2 = orc.lagrange_coeff(np.array(fe_list(c)[0], dtype=np.uint64), (2 * d).bit_length() - 1)
+        K = (0, 0)
+        for k in range(2 * d):
+            K = po.fadd(K, po.fmul(poly[k], tuple(int(x) for x in L2[k])))
+        if i < nround - 1:
+            sv, pk = fe_list(s_)[0], fe_list(s_)[0]
+            for y in fe_list(gsyo[i]):
+                K = po.fadd(K, po.fmul(pk, y))
+                pk = po.fmul(pk, sv)
+        out += rec(41, 1, np.array([K], dtype=np.uint64).tobytes())
+    fin = b""
+    for rk in ranks:
+        for tag in ("SPDA", "SPDB", "SPDC"):
+            fin += [r[2] for r in rk if r[0] == tag][0]
+    out += rec(42, len(fin) // 16, fin)
+    return out
+
+
 def gen_parties():
     """The reference's own coPCS test (main.cpp:49-163: PCS_commit then
     PCS_open_new) run unmodified with N ranks as N processes (pigeon_mpi,
@@ -256,7 +348,7 @@ def gen_parties():
     import struct
     import tempfile
     out = {}
-    for N, logM in ((4, 14), (16, 16), (8, 19)):
+    for N, logM in ((4, 14), (16, 16), (8, 19), (16, 24)):
         with tempfile.TemporaryDirectory() as td:
             prefix = os.path.join(td, "cap")
             env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_CAPTURE=prefix, MINIMPI_TIMEOUT="300")
@@ -269,7 +361,9 @@ def gen_parties():
         lead = ranks[0]
         npoint = logM + 1
         h2fo = [r[2] for r in lead if r[0] == "H2FO"]
+        expected = expected_open_transcript(ranks, N, logM, [[4], [4], [4, 4], [4, 4]])
         case = {"N": N, "logM": logM, "rates": [[4], [4], [4, 4], [4, 4]], "ref_seconds": round(dt, 2),
+                "gpu_transcript_bytes": len(expected), "gpu_transcript_sha256": sha(expected),
                 "stdout": log.stdout.strip().splitlines(),
                 "K": hx([r[2] for r in lead if r[0] == "FIPK"][0]),
                 "point_len": npoint,
@@ -296,7 +390,7 @@ def gen_parties():
                  "base_root": hx(ctrb[0][4:]),
                  "tree_roots": [hx(x[4:]) + ":%d" % struct.unpack_from("<I", x)[0] for x in ctrb],
                  "commit_roots": [hx(x[4:]) + ":%d" % struct.unpack_from("<I", x)[0] for x in big_roots[:3]],
-                 "party_polys": [hx(r[2]) for r in recs if r[0] == "PAGI"],
+                 "party_polys": [(hx if small else sha)(r[2]) for r in recs if r[0] == "PAGI"],
                  "queries": gidx if small else [sha(str(g).encode()) for g in gidx],
                  "final": [(hx if small else sha)(r[2]) for r in recs if r[0] in ("SPDA", "SPDB", "SPDC")],
                  "final_bytes": [len(r[2]) for r in recs if r[0] in ("SPDA", "SPDB", "SPDC")]}
