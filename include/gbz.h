@@ -513,6 +513,36 @@ gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, in
 gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
                         uint8_t *transcript, uint64_t capacity, int mem);
 
+/* quadratic_coSumcheck / cubic_coSumcheck of N parties on one device
+ * (form GBZ_SC_QUADRATIC or GBZ_SC_CUBIC).  p1, p2 (and p3): N x n party
+ * shares, party-major; R: the parties' sparse vectors, N x sum_i (2 or 4)
+ * degrees[i], R[i] back to back; r1 (cubic: log2 n entries, b1 =
+ * precompute_beta(r1)) and r2 (cubic: log2(N/4) entries, the aggregation
+ * weights b2 = precompute_beta(r2)); K, K_r: the claim and the sparse claim;
+ * fs: the Fiat-Shamir chain, updated.  Every round runs the parties' block
+ * transforms (phase 1, the cubic form skipping blocks whose p1 part is zero
+ * as the reference does), adds c R, aggregates the N messages as
+ * sumcheck_aggr, checks, draws the challenge, folds R and every vector
+ * (phase 2); then the parties' final values are unpacked and checked and the
+ * claims formed.  claims: rows x (eval, r[0..ndeg]) with rows = 5
+ * (quadratic) / 4 (cubic) and r = the final challenge then the round
+ * challenges, 2 (ndeg + 2) words per row.  The reference prints and
+ * continues when a check fails; *flags (may be NULL) gets the same
+ * information: bit i = round i's message did not match K, bit 29 = the
+ * final check, bit 30 = the cubic form's b1 check.  The inputs are not
+ * modified.  Transcript (may be NULL; gbz_cosumcheck_transcript_bytes):
+ *   36 CHALLENGE (c of {K, K_r}) | per round 34 PARTY_POLYS 16B x DN,
+ *   35 POLY 16B x D, 36 CHALLENGE (D = 2d / 4d) | 43 FINAL_SHARES 16B x
+ *   rows N (party-major) | 44 UNPACKED 16B x rows N/2 | 36 CHALLENGE |
+ *   45 CLAIMS 16B x rows
+ * replaces quadratic_coSumcheck (coSumcheck.cpp:233-331) and
+ * cubic_coSumcheck (coSumcheck.cpp:335-448) on N ranks. */
+gbz_status gbz_cosumcheck(gbz_ctx *ctx, int form, int N, uint64_t n, const uint64_t *p1, const uint64_t *p2,
+                          const uint64_t *p3, const uint64_t *R, const uint64_t *r1, int nr1, const uint64_t *r2,
+                          const uint64_t *K, const uint64_t *K_r, const int *degrees, int ndeg, uint64_t *fs,
+                          uint64_t *claims, uint32_t *flags, uint8_t *transcript, uint64_t capacity, int mem);
+uint64_t gbz_cosumcheck_transcript_bytes(int form, int N, const int *degrees, int ndeg);
+
 /* --------------------------------------------------------------- prover */
 
 /* Bytes of the transcript of one proof of a 2^logn witness at `rate`. */

@@ -202,4 +202,24 @@ void __wrap__Z12get_segmentsRSt6vectorIN5virgo12fieldElementESaIS1_EERS_IS3_SaIS
   put_words("GSQU", qs);
 }
 
+// MPI_utils.cpp:2604  vector<F> sumcheck_aggr(vector<F>& poly, vector<F>& b, int N)
+vector<F> __real__Z13sumcheck_aggrRSt6vectorIN5virgo12fieldElementESaIS1_EES4_i(vector<F> &poly, vector<F> &b, int N);
+vector<F> __wrap__Z13sumcheck_aggrRSt6vectorIN5virgo12fieldElementESaIS1_EES4_i(vector<F> &poly, vector<F> &b, int N) {
+  put_field("SAGI", poly);
+  vector<F> r = __real__Z13sumcheck_aggrRSt6vectorIN5virgo12fieldElementESaIS1_EES4_i(poly, b, N);
+  put_field("SAGO", r);
+  return r;
+}
+
+// MPI_utils.cpp:2672  vector<vector<F>> send_final_sumcheck_poly(vector<F> s, int N)
+vector<vector<F>> __real__Z24send_final_sumcheck_polySt6vectorIN5virgo12fieldElementESaIS1_EEi(vector<F> s, int N);
+vector<vector<F>> __wrap__Z24send_final_sumcheck_polySt6vectorIN5virgo12fieldElementESaIS1_EEi(vector<F> s, int N) {
+  put_field("SFSI", s);
+  vector<vector<F>> H = __real__Z24send_final_sumcheck_polySt6vectorIN5virgo12fieldElementESaIS1_EEi(s, N);
+  vector<F> flat;
+  for (auto &h : H) flat.insert(flat.end(), h.begin(), h.end());
+  put_field("SFSO", flat);
+  return H;
+}
+
 }  // extern "C"

@@ -31,7 +31,8 @@ constexpr int kPcsMaxLogDeg = 10;      // the block fold of phase 2 (d <= 1024)
 // Transcript tags of the opening (see include/gbz.h).
 enum : uint32_t {
   T_PCS_ROOTS = 32, T_PCS_LEADER_ROOT = 33, T_PCS_PARTY_POLYS = 34, T_PCS_POLY = 35, T_PCS_CHALLENGE = 36,
-  T_PCS_QUERIES = 37, T_PCS_Y = 38, T_PCS_SEGMENTS = 39, T_PCS_S = 40, T_PCS_K = 41, T_PCS_FINAL = 42
+  T_PCS_QUERIES = 37, T_PCS_Y = 38, T_PCS_SEGMENTS = 39, T_PCS_S = 40, T_PCS_K = 41, T_PCS_FINAL = 42,
+  T_COSC_FINAL_SHARES = 43, T_COSC_UNPACKED = 44, T_COSC_CLAIMS = 45
 };
 
 // Verifier-side state of one opening, resident on the device.
@@ -466,6 +467,231 @@ __global__ void k_put_party(const fe *v, uint64_t len, int N, uint8_t *tr, uint6
 }
 
 unsigned grid(uint64_t n, unsigned t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// ------------------------------------------------- coSumcheck round drivers
+// quadratic_coSumcheck / cubic_coSumcheck (coSumcheck.cpp:233-448) with N
+// parties on the device: per round every party's block transforms and
+// products (phase 1), plus the challenge-weighted sparse vectors R, the
+// leader's aggregation (sumcheck_aggr), its check and challenge, the sparse
+// fold of R and the block fold of every vector (phase 2); then the final
+// shares, the leader's unpack and check, the last challenge and the claims.
+
+constexpr int kCoscMaxRounds = 16;
+constexpr int kCoscMaxRows = 5;  // final values per party: 5 (quadratic) / 4 (cubic)
+
+struct CoscDev {
+  fe fs, K, c;
+  uint32_t flags;   // bit i: round i's message does not match K; bit 29: final check; bit 30: b1 check
+  fe r[kCoscMaxRounds];
+  fe fer[kPcsMaxParties];  // final_eval_r of every party
+};
+
+// c = hash_to_field({K, K_r}), K += c K_r (coSumcheck.cpp:234-235).
+__global__ void k_cosc_init(CoscDev *st, fe fs, fe K, fe Kr, uint8_t *tr, uint64_t off_c) {
+  fs = hash_F(fs, K);
+  fs = hash_F(fs, Kr);
+  st->fs = fs;
+  st->c = fs;
+  st->K = fadd(K, fmul(fs, Kr));
+  st->flags = 0;
+  put_fe(tr, off_c, fs);
+}
+
+// Offsets of the sparse vectors R[j] of one party (R holds them back to back).
+struct ROffs {
+  int n;
+  uint32_t off[kCoscMaxRounds + 1];
+};
+
+// H_p += c H_r with H_r = R_p[iter], H_r[0] += sum_{j > iter} sum_k R_p[j][step k]
+// (coSumcheck.cpp:47-60, 181-193).  One CTA per party.
+__global__ void k_cosc_add_hr(fe *H, int D, const fe *R, uint64_t rstride, ROffs ro, int iter, int step,
+                              const CoscDev *st) {
+  const uint64_t p = blockIdx.x;
+  const fe *Rp = R + p * rstride;
+  __shared__ fe extra;
+  if (threadIdx.x == 0) {
+    fe e = fe_zero();
+    for (int j = iter + 1; j < ro.n; j++) {
+      const int len = (int)(ro.off[j + 1] - ro.off[j]);
+      for (int k = 0; k < len / step; k++) e = fadd(e, Rp[ro.off[j] + step * k]);
+    }
+    extra = e;
+  }
+  __syncthreads();
+  const fe c = st->c;
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    fe hr = Rp[ro.off[iter] + k];
+    if (k == 0) hr = fadd(hr, extra);
+    H[p * D + k] = fadd(H[p * D + k], fmul(c, hr));
+  }
+}
+
+// The leader's round: sum_{j<d} H[j << ext] = K (flag otherwise), r =
+// hash_to_field(H), LD = compute_lagrange_coeff(r, D = d << ext), K = sum
+// H LD, Ld = compute_lagrange_coeff(r, d) (coSumcheck.cpp:258-293,
+// 362-396).  scratch: 2 D entries.
+__global__ void __launch_bounds__(256)
+k_cosc_verify(CoscDev *st, const fe *poly, int logd, int ext, int round, fe *LD, fe *Ld, fe *scratch, uint8_t *tr,
+              uint64_t off_poly, uint64_t off_chal) {
+  __shared__ fe red[256];
+  const int d = 1 << logd, D = d << ext;
+  fe *cp = scratch, *wp = scratch + D;
+  if (threadIdx.x == 0) {
+    fe ev = fe_zero();
+    for (int j = 0; j < d; j++) ev = fadd(ev, poly[j << ext]);
+    if (!fe_eq(ev, st->K)) st->flags |= 1u << round;
+    fe fs = st->fs;
+    for (int k = 0; k < D; k++) fs = hash_F(fs, poly[k]);
+    st->fs = fs;
+    st->r[round] = fs;
+    put_fe(tr, off_chal, fs);
+    fe x = fe_one();
+    for (int k = 0; k < D; k++) {
+      cp[k] = x;
+      x = fmul(x, fs);
+    }
+  }
+  __syncthreads();
+  const fe wi = finv(root_of_unity(logd + ext));
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    wp[k] = fpow(wi, (uint64_t)k);
+    put_fe(tr, off_poly + 16ull * k, poly[k]);
+  }
+  __syncthreads();
+  const fe invD = finv(fe_make((uint64_t)D, 0)), invd = finv(fe_make((uint64_t)d, 0));
+  fe acc = fe_zero();
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    fe s = fe_zero();
+    for (int j = 0; j < D; j++) s = fadd(s, fmul(cp[j], wp[((uint64_t)j * k) & (D - 1)]));
+    s = fmul(s, invD);
+    LD[k] = s;
+    acc = fadd(acc, fmul(poly[k], s));
+  }
+  for (int k = threadIdx.x; k < d; k += blockDim.x) {
+    fe s = fe_zero();
+    for (int j = 0; j < d; j++) s = fadd(s, fmul(cp[j], wp[(((uint64_t)j * k) << ext) & (D - 1)]));
+    Ld[k] = fmul(s, invd);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fadd(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) st->K = red[0];
+}
+
+// quadratic_coSumcheck_phase2_sparse (coSumcheck.cpp:215-228) for every party:
+// s = sum_j LD[j] R_p[iter][j]; R_p[j > iter] *= LD[0]; R_p[iter+1][0] += s.
+__global__ void k_cosc_sparse(fe *R, uint64_t rstride, ROffs ro, int iter, const fe *LD, int D, int N, CoscDev *st) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  fe *Rp = R + (uint64_t)p * rstride;
+  const int len = (int)(ro.off[iter + 1] - ro.off[iter]);
+  fe s = fe_zero();
+  for (int j = 0; j < len && j < D; j++) s = fadd(s, fmul(LD[j], Rp[ro.off[iter] + j]));
+  const fe l0 = LD[0];
+  for (uint32_t e = ro.off[iter + 1]; e < ro.off[ro.n]; e++) Rp[e] = fmul(Rp[e], l0);
+  if (iter + 1 < ro.n) Rp[ro.off[iter + 1]] = fadd(Rp[ro.off[iter + 1]], s);
+  st->fer[p] = s;
+}
+
+// The end of the round driver (coSumcheck.cpp:300-330, 399-446): the parties'
+// final values, the leader's unpack (unpack_secret_share(H, N/2, N), a fixed
+// N/2 x N map U), its check, the last challenge, the Lagrange weights over
+// N/4 points and the claims; for the cubic form also the check of b1[0]
+// against the round weights.  One thread.
+__global__ void k_cosc_final(CoscDev *st, int cubic, int N, const fe *p1, const fe *p2, const fe *p3, const fe *b1,
+                             uint64_t mstride, const fe *U, const fe *b2, const fe *Ld_hist, const int *logd_hist,
+                             int nrounds, const fe *r1, fe *claims, uint8_t *tr, uint64_t off_shares,
+                             uint64_t off_unpacked, uint64_t off_r, uint64_t off_claims) {
+  if (threadIdx.x) return;
+  const int rows = cubic ? 4 : 5, half = N / 2, quarter = N / 4;
+  fe H[kCoscMaxRows][kPcsMaxParties / 2];
+  for (int i = 0; i < rows; i++)
+    for (int j = 0; j < half; j++) H[i][j] = fe_zero();
+  for (int p = 0; p < N; p++) {
+    const uint64_t o = (uint64_t)p * mstride;
+    fe s[kCoscMaxRows];
+    if (cubic) {
+      s[0] = p1[o];
+      s[1] = p2[o];
+      s[2] = p3[o];
+      s[3] = st->fer[p];
+    } else {
+      s[0] = p1[o];
+      s[1] = p2[o];
+      s[2] = p1[o + 1];
+      s[3] = p2[o + 1];
+      s[4] = st->fer[p];
+    }
+    for (int i = 0; i < rows; i++) {
+      put_fe(tr, off_shares + 16ull * ((uint64_t)p * rows + i), s[i]);
+      for (int j = 0; j < half; j++) H[i][j] = fadd(H[i][j], fmul(U[j * N + p], s[i]));
+    }
+  }
+  for (int i = 0; i < rows; i++)
+    for (int j = 0; j < half; j++) put_fe(tr, off_unpacked + 16ull * (i * half + j), H[i][j]);
+  fe K = st->K;
+  const fe c = st->c;
+  for (int i = 0; i < quarter; i++) {
+    fe t;
+    if (cubic) t = fmul(b2[i], fadd(fmul(b1[0], fsub(fmul(H[0][i], H[1][i]), H[2][i])), fmul(c, H[3][i])));
+    else t = fadd(fadd(fmul(H[0][i], H[1][i]), fmul(H[2][i], H[3][i])), fmul(c, H[4][i]));
+    K = fsub(K, t);
+  }
+  if (!fe_eq(K, fe_zero())) st->flags |= 1u << 29;
+  fe fs = st->fs;
+  const int hashed = cubic ? 3 : rows;
+  for (int i = 0; i < hashed; i++)
+    for (int j = 0; j < half; j++) fs = hash_F(fs, H[i][j]);
+  st->fs = fs;
+  put_fe(tr, off_r, fs);
+  // L over N/4 points: compute_lagrange_coeff(r, N/4), or {1} for one point
+  fe L[kPcsMaxParties / 4];
+  if (quarter == 1) {
+    L[0] = fe_one();
+  } else {
+    int lq = 0;
+    while ((1 << lq) < quarter) lq++;
+    const fe wi = finv(root_of_unity(lq)), iq = finv(fe_make((uint64_t)quarter, 0));
+    for (int k = 0; k < quarter; k++) {
+      fe acc = fe_zero(), x = fe_one();
+      const fe step = fpow(wi, (uint64_t)k);
+      fe w = fe_one();
+      for (int j = 0; j < quarter; j++) {
+        acc = fadd(acc, fmul(x, w));
+        x = fmul(x, fs);
+        w = fmul(w, step);
+      }
+      L[k] = fmul(acc, iq);
+    }
+  }
+  for (int i = 0; i < rows; i++) {
+    fe e = fe_zero();
+    for (int j = 0; j < quarter; j++) e = fadd(e, fmul(L[j], H[i][j]));
+    claims[i] = e;
+    put_fe(tr, off_claims + 16ull * i, e);
+  }
+  if (cubic) {  // coSumcheck.cpp:432-443
+    fe y = fe_one();
+    int ctr = 0, at = 0;
+    for (int i = 0; i < nrounds; i++) {
+      const int ld = logd_hist[i], d = 1 << ld;
+      fe acc = fe_zero();
+      for (int j = 0; j < d; j++) {
+        fe b = fe_one();
+        for (int t = 0; t < ld; t++) b = fmul(b, ((j >> t) & 1) ? r1[ctr + t] : fsub(fe_one(), r1[ctr + t]));
+        acc = fadd(acc, fmul(b, Ld_hist[at + j]));
+      }
+      ctr += ld;
+      at += d;
+      y = fmul(y, acc);
+    }
+    if (!fe_eq(y, b1[0])) st->flags |= 1u << 30;
+  }
+}
 
 }  // namespace
 }  // namespace gbz
@@ -1137,6 +1363,236 @@ gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, c
   if (hst.error) return fail(ctx, GBZ_ECHECK, hst.error & 1 ? "pcs: a round message does not match the claim"
                                                             : "pcs: a delegate check failed");
   API_END(ctx)
+}
+
+gbz_status gbz_cosumcheck(gbz_ctx *ctx, int form, int N, uint64_t n, const uint64_t *p1, const uint64_t *p2,
+                          const uint64_t *p3, const uint64_t *R, const uint64_t *r1, int nr1, const uint64_t *r2,
+                          const uint64_t *K, const uint64_t *K_r, const int *degrees, int ndeg, uint64_t *fs,
+                          uint64_t *claims, uint32_t *flags, uint8_t *transcript, uint64_t capacity, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(p1, "p1");
+  need(p2, "p2");
+  need(R, "R");
+  need(K, "K");
+  need(K_r, "K_r");
+  need(degrees, "degrees");
+  need(fs, "fs");
+  need(claims, "claims");
+  if (form != GBZ_SC_QUADRATIC && form != GBZ_SC_CUBIC) throw ArgError("coSumcheck: form must be quadratic or cubic");
+  const bool cubic = form == GBZ_SC_CUBIC;
+  if (cubic) {
+    need(p3, "p3");
+    need(r1, "r1");
+  }
+  if (N < 4 || N > kPcsMaxParties || !is_pow2((uint64_t)N)) throw ArgError("coSumcheck: N must be a power of two in [4, 64]");
+  if (ndeg < 1 || ndeg > kCoscMaxRounds) throw ArgError("coSumcheck: 1..16 rounds");
+  check_pow2(n, "coSumcheck: n");
+  const int ext = cubic ? 2 : 1, step = 1 << ext, rows = cubic ? 4 : 5;
+  uint64_t m = n;
+  std::vector<int> logd(ndeg);
+  ROffs ro{};
+  ro.n = ndeg;
+  ro.off[0] = 0;
+  for (int i = 0; i < ndeg; i++) {
+    if (degrees[i] < 1 || !is_pow2((uint64_t)degrees[i]) || degrees[i] > 1024 || (uint64_t)degrees[i] > m)
+      throw ArgError("coSumcheck: degrees must be powers of two <= 1024 dividing the length");
+    logd[i] = ilog2((uint64_t)degrees[i]);
+    m /= degrees[i];
+    ro.off[i + 1] = ro.off[i] + (uint32_t)(step * degrees[i]);
+  }
+  if (m < (cubic ? 1u : 2u)) throw ArgError("coSumcheck: the folds must leave 2 (quadratic) / 1 (cubic) entries");
+  const int lq = ilog2((uint64_t)(N / 4));
+  if (cubic && (nr1 < 0 || (1ull << nr1) != n)) throw ArgError("coSumcheck: r1 must have log2(n) entries");
+  // transcript layout
+  PcsLayout lay;
+  const uint64_t off_c = lay.add(T_PCS_CHALLENGE, 1, 16);
+  std::vector<uint64_t> off_pp(ndeg), off_poly(ndeg), off_chal(ndeg);
+  for (int i = 0; i < ndeg; i++) {
+    const int D = degrees[i] << ext;
+    off_pp[i] = lay.add(T_PCS_PARTY_POLYS, D * N, 16);
+    off_poly[i] = lay.add(T_PCS_POLY, D, 16);
+    off_chal[i] = lay.add(T_PCS_CHALLENGE, 1, 16);
+  }
+  const uint64_t off_sh = lay.add(T_COSC_FINAL_SHARES, rows * N, 16);
+  const uint64_t off_un = lay.add(T_COSC_UNPACKED, rows * (N / 2), 16);
+  const uint64_t off_r = lay.add(T_PCS_CHALLENGE, 1, 16);
+  const uint64_t off_cl = lay.add(T_COSC_CLAIMS, rows, 16);
+  if (transcript && capacity < lay.bytes) throw ArgError("coSumcheck: transcript capacity too small");
+  cudaStream_t s = ctx->stream;
+  OpenBufs ob;
+  // party-major inputs, copied: the call folds them in place as the reference does
+  const uint64_t Rst = ro.off[ndeg];
+  fe *v1 = ob.alloc<fe>((uint64_t)N * n), *v2 = ob.alloc<fe>((uint64_t)N * n), *v3 = nullptr, *vb = nullptr;
+  fe *dR = ob.alloc<fe>((uint64_t)N * Rst);
+  const cudaMemcpyKind kin = mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  GBZ_CUDA(cudaMemcpyAsync(v1, p1, 16ull * N * n, kin, s));
+  GBZ_CUDA(cudaMemcpyAsync(v2, p2, 16ull * N * n, kin, s));
+  GBZ_CUDA(cudaMemcpyAsync(dR, R, 16ull * N * Rst, kin, s));
+  std::vector<fe> hr1(cubic ? nr1 : 0), hr2(lq);
+  if (cubic) {
+    v3 = ob.alloc<fe>((uint64_t)N * n);
+    vb = ob.alloc<fe>((uint64_t)N * n);
+    GBZ_CUDA(cudaMemcpyAsync(v3, p3, 16ull * N * n, kin, s));
+    if (mem == GBZ_MEM_DEVICE) {
+      GBZ_CUDA(cudaMemcpyAsync(hr1.data(), r1, 16ull * nr1, cudaMemcpyDeviceToHost, s));
+      if (lq) GBZ_CUDA(cudaMemcpyAsync(hr2.data(), r2, 16ull * lq, cudaMemcpyDeviceToHost, s));
+    } else {
+      for (int i = 0; i < nr1; i++) hr1[i] = fe_make(r1[2 * i], r1[2 * i + 1]);
+      for (int i = 0; i < lq; i++) hr2[i] = fe_make(r2[2 * i], r2[2 * i + 1]);
+    }
+  }
+  fe hK, hKr, hfs;
+  {
+    uint64_t t[6];
+    if (mem == GBZ_MEM_DEVICE) {
+      GBZ_CUDA(cudaMemcpyAsync(t, K, 16, cudaMemcpyDeviceToHost, s));
+      GBZ_CUDA(cudaMemcpyAsync(t + 2, K_r, 16, cudaMemcpyDeviceToHost, s));
+      GBZ_CUDA(cudaMemcpyAsync(t + 4, fs, 16, cudaMemcpyDeviceToHost, s));
+      GBZ_CUDA(cudaStreamSynchronize(s));
+    } else {
+      t[0] = K[0], t[1] = K[1], t[2] = K_r[0], t[3] = K_r[1], t[4] = fs[0], t[5] = fs[1];
+    }
+    hK = fe_make(t[0], t[1]);
+    hKr = fe_make(t[2], t[3]);
+    hfs = fe_make(t[4], t[5]);
+  }
+  // b1 = precompute_beta(r1) for every party (the same vector), b2 = precompute_beta(r2)
+  std::vector<fe> b2(N / 4, fe_one());
+  for (int i = 0; i < N / 4; i++) {
+    fe v = fe_one();
+    for (int t = 0; t < lq; t++) v = fmul(v, ((i >> t) & 1) ? hr2[t] : fsub(fe_one(), hr2[t]));
+    b2[i] = v;
+  }
+  fe *dr1 = ob.alloc<fe>(std::max(1, nr1)), *db2 = ob.alloc<fe>(N / 4);
+  GBZ_CUDA(cudaMemcpyAsync(db2, b2.data(), 16ull * (N / 4), cudaMemcpyHostToDevice, s));
+  if (cubic) {
+    GBZ_CUDA(cudaMemcpyAsync(dr1, hr1.data(), 16ull * nr1, cudaMemcpyHostToDevice, s));
+    beta_launch(dr1, nr1, vb, s);
+    for (int p = 1; p < N; p++) GBZ_CUDA(cudaMemcpyAsync(vb + (uint64_t)p * n, vb, 16 * n, cudaMemcpyDeviceToDevice, s));
+  }
+  // sumcheck_aggr's weights: ones (quadratic, coSumcheck.cpp:194) or b2 (cubic)
+  std::vector<fe> ones(N / 4, fe_one());
+  std::vector<fe> lambda = aggregate_weights(N, cubic ? b2.data() : ones.data());
+  // unpack_secret_share(H, N/2, N): row j of the map takes E[2j]
+  std::vector<fe> U((size_t)(N / 2) * N);
+  for (int j = 0; j < N / 2; j++) {
+    std::vector<fe> g(N, fe_zero());
+    g[2 * j] = fe_one();
+    std::vector<fe> l = aggregate_weights_even(N, g);
+    for (int p = 0; p < N; p++) U[(size_t)j * N + p] = l[p];
+  }
+  fe *dl = ob.alloc<fe>(N), *dU = ob.alloc<fe>(U.size());
+  GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
+  GBZ_CUDA(cudaMemcpyAsync(dU, U.data(), 16 * U.size(), cudaMemcpyHostToDevice, s));
+  uint8_t *tr = ob.alloc<uint8_t>(lay.bytes);
+  Hdr *dh = ob.alloc<Hdr>(lay.hdr.size());
+  GBZ_CUDA(cudaMemcpyAsync(dh, lay.hdr.data(), sizeof(Hdr) * lay.hdr.size(), cudaMemcpyHostToDevice, s));
+  k_headers<<<grid(lay.hdr.size()), 256, 0, s>>>(dh, (int)lay.hdr.size(), tr);
+  CoscDev *st = ob.alloc<CoscDev>(1);
+  k_cosc_init<<<1, 1, 0, s>>>(st, hfs, hK, hKr, tr, off_c);
+  GBZ_CUDA(cudaGetLastError());
+  const int maxD = 1024 << ext;
+  fe *H = ob.alloc<fe>((uint64_t)N * maxD), *poly = ob.alloc<fe>(maxD), *LD = ob.alloc<fe>(maxD);
+  fe *scr = ob.alloc<fe>(2ull * maxD), *coef = ob.alloc<fe>((uint64_t)N * n);
+  uint64_t dsum = 0;
+  for (int i = 0; i < ndeg; i++) dsum += degrees[i];
+  fe *Ldh = ob.alloc<fe>(dsum);
+  int *dlog = ob.alloc<int>(ndeg);
+  GBZ_CUDA(cudaMemcpyAsync(dlog, logd.data(), 4ull * ndeg, cudaMemcpyHostToDevice, s));
+  m = n;
+  uint64_t at = 0;
+  for (int i = 0; i < ndeg; i++) {
+    const int d = degrees[i], D = d << ext;
+    const uint64_t blocks = (uint64_t)N * m / d, pblocks = m / d;
+    // phase 1 (coSumcheck.cpp:9-46, 150-179): extended blocks of every vector
+    const NttTables &td = ctx->tables(logd[i]), &tD = ctx->tables(logd[i] + ext);
+    if (logd[i] + ext > kMaxCoLogD) throw ArgError("coSumcheck: extended block longer than 2^13");
+    fe *src[4] = {v1, v2, cubic ? vb : nullptr, cubic ? v3 : nullptr};
+    fe *ex[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int v = 0; v < (cubic ? 4 : 2); v++) {
+      ex[v] = ob.alloc<fe>(blocks * D);
+      ntt_batched(td, src[v], d, (uint32_t)d, coef, blocks, true, s);
+      ntt_batched(tD, coef, d, (uint32_t)d, ex[v], blocks, false, s);
+    }
+    uint8_t *zf = nullptr;
+    if (cubic) {  // blocks whose p1 part is all zero are skipped (coSumcheck.cpp:21-27)
+      zf = ob.alloc<uint8_t>(blocks);
+      nonzero_blocks_launch(v1, blocks, logd[i], zf, s);
+    }
+    const int lanes = D >= 256 ? 1 : 256 / D;
+    const int per_cta = (int)std::max<uint64_t>((uint64_t)lanes, (pblocks + 607) / 608);
+    fe *cpart = ob.alloc<fe>((uint64_t)D * cophase1_parts(pblocks, per_cta));
+    for (int p = 0; p < N; p++) {
+      const uint64_t o = (uint64_t)p * pblocks;
+      cophase1_reduce_launch(ex[0] + o * D, ex[1] + o * D, ex[2] ? ex[2] + o * D : nullptr,
+                             ex[3] ? ex[3] + o * D : nullptr, zf ? zf + o : nullptr, pblocks, logd[i] + ext, per_cta,
+                             cpart, H + (uint64_t)p * D, s);
+    }
+    k_cosc_add_hr<<<N, 256, 0, s>>>(H, D, dR, Rst, ro, i, step, st);
+    k_put_party<<<dim3(grid(D), N), 256, 0, s>>>(H, D, N, tr, off_pp[i], 16ull * D);
+    aggregate_launch(H, N, D, dl, poly, s);
+    k_cosc_verify<<<1, 256, 0, s>>>(st, poly, logd[i], ext, i, LD, Ldh + at, scr, tr, off_poly[i], off_chal[i]);
+    k_cosc_sparse<<<1, 64, 0, s>>>(dR, Rst, ro, i, LD, D, N, st);
+    GBZ_CUDA(cudaGetLastError());
+    // phase 2 (coSumcheck.cpp:66-148, 201-213): every vector folded by Ld
+    for (fe *v : {v1, v2, v3, vb}) {
+      if (!v) continue;
+      cophase2_launch(v, (uint64_t)N * m, Ldh + at, logd[i], coef, s);
+      GBZ_CUDA(cudaMemcpyAsync(v, coef, 16ull * N * m / d, cudaMemcpyDeviceToDevice, s));
+    }
+    m /= d;
+    at += d;
+  }
+  fe *dcl = ob.alloc<fe>(rows);
+  k_cosc_final<<<1, 32, 0, s>>>(st, cubic ? 1 : 0, N, v1, v2, v3, vb, m, dU, db2, Ldh, dlog, ndeg, dr1, dcl, tr,
+                                off_sh, off_un, off_r, off_cl);
+  GBZ_CUDA(cudaGetLastError());
+  CoscDev hst;
+  GBZ_CUDA(cudaMemcpyAsync(&hst, st, sizeof(CoscDev), cudaMemcpyDeviceToHost, s));
+  std::vector<fe> hcl(rows);
+  GBZ_CUDA(cudaMemcpyAsync(hcl.data(), dcl, 16ull * rows, cudaMemcpyDeviceToHost, s));
+  if (transcript) {
+    const cudaMemcpyKind ko = mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    GBZ_CUDA(cudaMemcpyAsync(transcript, tr, lay.bytes, ko, s));
+  }
+  GBZ_CUDA(cudaStreamSynchronize(s));
+  // claims: rows x (eval, r vector [r_final, r_0, ..., r_{ndeg-1}])
+  std::vector<uint64_t> out((size_t)rows * 2 * (ndeg + 2));
+  for (int i = 0; i < rows; i++) {
+    uint64_t *o = out.data() + (size_t)i * 2 * (ndeg + 2);
+    o[0] = hcl[i].re;
+    o[1] = hcl[i].im;
+    o[2] = hst.fs.re;
+    o[3] = hst.fs.im;
+    for (int k = 0; k < ndeg; k++) {
+      o[4 + 2 * k] = hst.r[k].re;
+      o[5 + 2 * k] = hst.r[k].im;
+    }
+  }
+  const cudaMemcpyKind ko = mem == GBZ_MEM_DEVICE ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
+  GBZ_CUDA(cudaMemcpy(claims, out.data(), 8 * out.size(), ko));
+  const uint64_t fsw[2] = {hst.fs.re, hst.fs.im};
+  GBZ_CUDA(cudaMemcpy(fs, fsw, 16, ko));
+  if (flags) *flags = hst.flags;
+  API_END(ctx)
+}
+
+uint64_t gbz_cosumcheck_transcript_bytes(int form, int N, const int *degrees, int ndeg) {
+  if (!degrees || ndeg < 1 || N < 4) return 0;
+  const int ext = form == GBZ_SC_CUBIC ? 2 : 1, rows = form == GBZ_SC_CUBIC ? 4 : 5;
+  PcsLayout lay;
+  lay.add(T_PCS_CHALLENGE, 1, 16);
+  for (int i = 0; i < ndeg; i++) {
+    lay.add(T_PCS_PARTY_POLYS, (degrees[i] << ext) * N, 16);
+    lay.add(T_PCS_POLY, degrees[i] << ext, 16);
+    lay.add(T_PCS_CHALLENGE, 1, 16);
+  }
+  lay.add(T_COSC_FINAL_SHARES, rows * N, 16);
+  lay.add(T_COSC_UNPACKED, rows * (N / 2), 16);
+  lay.add(T_PCS_CHALLENGE, 1, 16);
+  lay.add(T_COSC_CLAIMS, rows, 16);
+  return lay.bytes;
 }
 
 }  // extern "C"

@@ -48,7 +48,8 @@ EXPORTS = (
     "gbz_ntt_autotune", "gbz_merkle_set_fusion", "gbz_merkle_get_fusion", "gbz_merkle_autotune",
     "gbz_set_graphs", "gbz_ntt_full_twiddles", "gbz_encode_concatenated", "gbz_leader_root",
     "gbz_whir_batch_schedule", "gbz_whir_batch_open", "gbz_pcs_schedule", "gbz_pcs_commit", "gbz_pcs_free",
-    "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open", "gbz_pcs_claim",
+    "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open", "gbz_pcs_claim", "gbz_cosumcheck",
+    "gbz_cosumcheck_transcript_bytes",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -169,6 +170,9 @@ def _load():
         "gbz_pcs_commit_data": (c_int, [vp, vp, c_int, vp, vp, vp, c_int]),
         "gbz_pcs_open": (c_int, [vp, vp, vp, c_int, vp, vp, vp, u64, c_int]),
         "gbz_pcs_claim": (c_int, [vp, vp, vp, c_int, vp, c_int]),
+        "gbz_cosumcheck": (c_int, [vp, c_int, c_int, u64, vp, vp, vp, vp, vp, c_int, vp, vp, vp, vp, c_int, vp, vp,
+                                   vp, vp, u64, c_int]),
+        "gbz_cosumcheck_transcript_bytes": (u64, [c_int, c_int, vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -821,6 +825,31 @@ def pcs_commit(ctx, N, M, rates, shares, random):
     ctx.check(lib.gbz_pcs_commit(ctx.h, N, M, len(rates), _ptr(r0), _ptr(r1), _ptr(sh), _ptr(rn), MEM_HOST,
                                  ctypes.byref(h), _ptr(roots), _ptr(leader)))
     return PcsCommitment(ctx, h, N, M, rates), roots, leader
+
+
+def cosumcheck(ctx, form, N, p1, p2, R, K, K_r, degrees, p3=None, r1=None, r2=None, fs=(0, 0)):
+    """quadratic_coSumcheck / cubic_coSumcheck (coSumcheck.cpp:233, :335) of N
+    parties (party-major arrays): (claims [(eval, r)], flags, transcript, fs)."""
+    a = [np.ascontiguousarray(x, dtype=np.uint64) for x in (p1, p2)]
+    n = a[0].size // (2 * N)
+    deg = np.ascontiguousarray(degrees, dtype=np.int32)
+    rows = 4 if form == SC_CUBIC else 5
+    Rr = np.ascontiguousarray(R, dtype=np.uint64)
+    P3 = None if p3 is None else np.ascontiguousarray(p3, dtype=np.uint64)
+    R1 = None if r1 is None else np.ascontiguousarray(r1, dtype=np.uint64).reshape(-1, 2)
+    R2 = None if r2 is None else np.ascontiguousarray(r2, dtype=np.uint64).reshape(-1, 2)
+    Kk = np.ascontiguousarray(K, dtype=np.uint64).reshape(2)
+    Kr = np.ascontiguousarray(K_r, dtype=np.uint64).reshape(2)
+    f = np.array(np.asarray(fs, dtype=np.uint64).reshape(2), copy=True)
+    cl = np.zeros((rows, len(degrees) + 2, 2), dtype=np.uint64)
+    flags = ctypes.c_uint32(0)
+    nb = lib.gbz_cosumcheck_transcript_bytes(form, N, _ptr(deg), len(degrees))
+    tr = np.zeros(nb, dtype=np.uint8)
+    ctx.check(lib.gbz_cosumcheck(ctx.h, form, N, n, _ptr(a[0]), _ptr(a[1]), _ptr(P3), _ptr(Rr), _ptr(R1),
+                                 0 if R1 is None else R1.shape[0], _ptr(R2), _ptr(Kk), _ptr(Kr), _ptr(deg),
+                                 len(degrees), _ptr(f), _ptr(cl), ctypes.byref(flags), _ptr(tr), nb, MEM_HOST))
+    claims = [(cl[i, 0], cl[i, 1:]) for i in range(rows)]
+    return claims, flags.value, tr.tobytes(), f
 
 
 PCS_UNITS = {32: 32, 33: 32, 37: 4}

@@ -63,6 +63,8 @@ def main():
             manifest["batchopen"] = gen_batchopen()
         if "parties" in only:
             manifest["parties"] = gen_parties()
+        if "cosumcheck" in only:
+            manifest["cosumcheck"] = gen_cosumcheck()
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
             json.dump(manifest, f, indent=1)
         print("updated", sorted(only))
@@ -144,6 +146,7 @@ def main():
     manifest["sumcheck"] = gen_sumcheck()
     manifest["batchopen"] = gen_batchopen()
     manifest["parties"] = gen_parties()
+    manifest["cosumcheck"] = gen_cosumcheck()
 
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
@@ -231,7 +234,8 @@ def gen_batchopen():
 # Per-rank capture records written by oracle/ref/minimpi/capture.cpp: tag,
 # count, then count units of these sizes.
 CAPTURE_UNIT = {"H2FI": 16, "H2FO": 16, "FRND": 16, "SHRS": 16, "PAGI": 16, "PAGO": 16, "SPDA": 16, "SPDB": 16,
-                "SPDC": 16, "WCIA": 16, "FIPK": 16, "GSYI": 16, "GSYO": 16, "GSSG": 16,
+                "SPDC": 16, "WCIA": 16, "FIPK": 16, "GSYI": 16, "GSYO": 16, "GSSG": 16, "SAGI": 16, "SAGO": 16,
+                "SFSI": 16, "SFSO": 16,
                 "GIDX": 4, "RAND": 4, "GSQU": 4, "MTCB": 36, "CTRB": 36, "WCIR": 36}
 
 
@@ -401,6 +405,69 @@ def gen_parties():
         out[name] = {"file": name + ".json", "N": N, "logM": logM}
         print("parties N=%d M=2^%d: reference %.1f s" % (N, logM, dt), flush=True)
     return out
+
+
+COSC = os.path.join(ROOT, "oracle", "_ref", "pigeon_cosc")
+
+
+def gen_cosumcheck():
+    """quadratic_coSumcheck / cubic_coSumcheck run unmodified with N ranks
+    (oracle/ref/cosumcheck_mpi_driver.cpp).  Kept: the transcript
+    gbz_cosumcheck must write (rebuilt from every rank's captured aggregation
+    inputs, the leader's aggregates, challenges and final unpack), the
+    leader's claims, and the check flags the reference's messages give."""
+    import struct
+    import tempfile
+    out = {}
+    for form, N, logn, degs, seed in (("quad", 4, 10, (8, 4, 4), 21), ("quad", 16, 12, (8, 4, 8), 22),
+                                      ("quad", 8, 13, (64, 16), 23), ("cubic", 4, 10, (8, 4, 4), 24),
+                                      ("cubic", 16, 12, (16, 8, 4), 25), ("cubic", 8, 11, (4, 4, 4, 4), 26)):
+        with tempfile.TemporaryDirectory() as td:
+            prefix, res = os.path.join(td, "cap"), os.path.join(td, "claims.bin")
+            env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_CAPTURE=prefix, MINIMPI_TIMEOUT="300")
+            log = subprocess.run([COSC, form, str(logn), ",".join(map(str, degs)), str(seed), res], env=env,
+                                 check=True, capture_output=True, text=True)
+            ranks = [capture_records("%s.%d" % (prefix, r)) for r in range(N)]
+            raw = open(res, "rb").read()
+        KK, claims = raw[:32], raw[32:]
+        rows = 4 if form == "cubic" else 5
+        lead = ranks[0]
+        h2fo = [r[2] for r in lead if r[0] == "H2FO"]
+        sago = [r[2] for r in lead if r[0] == "SAGO"][2:]   # the first two: the driver's claim computation
+        sagi = [[r[2] for r in rk if r[0] == "SAGI"][2:] for rk in ranks]
+        rec = lambda tag, count, payload: struct.pack("<II", tag, count) + payload
+        t = rec(36, 1, h2fo[0])
+        for i, d in enumerate(degs):
+            D = d * (4 if form == "cubic" else 2)
+            t += rec(34, D * N, b"".join(sagi[rk][i] for rk in range(N)))
+            t += rec(35, D, sago[i])
+            t += rec(36, 1, h2fo[1 + i])
+        t += rec(43, rows * N, b"".join([r[2] for r in rk if r[0] == "SFSI"][0] for rk in ranks))
+        t += rec(44, rows * (N // 2), [r[2] for r in lead if r[0] == "SFSO"][0])
+        t += rec(36, 1, h2fo[-1])
+        cnt = struct.unpack_from("<I", claims)[0]
+        o, evals = 4, b""
+        for _ in range(cnt):
+            evals += claims[o:o + 16]
+            ln = struct.unpack_from("<I", claims, o + 16)[0]
+            o += 20 + 16 * ln
+        t += rec(45, cnt, evals)
+        msgs = log.stdout
+        flags = 0
+        for i in range(len(degs)):
+            if "ERROR %d\n" % i in msgs:
+                flags |= 1 << i
+        if "Error in final sumcheck check" in msgs:
+            flags |= 1 << 29
+        if "Error in final sumcheck verification 2" in msgs:
+            flags |= 1 << 30
+        name = "cosc_%s_N%d_%d_%s" % (form, N, logn, "_".join(map(str, degs)))
+        out[name] = {"form": form, "N": N, "logn": logn, "degrees": list(degs), "seed": seed,
+                     "K": KK[:16].hex(), "K_r": KK[16:].hex(), "claims": claims.hex(), "flags": flags, "transcript_bytes": len(t),
+                     "transcript_sha256": hashlib.sha256(t).hexdigest(), "stdout": sorted(set(msgs.splitlines()))}
+    with open(os.path.join(HERE, "cosumcheck.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    return {"file": "cosumcheck.json", "cases": sorted(out)}
 
 
 if __name__ == "__main__":
