@@ -105,6 +105,12 @@ gbz_status gbz_merkle_open_blake(const uint8_t *levels, uint64_t N, uint64_t pos
 gbz_status gbz_whir_commit(gbz_ctx *ctx, const uint64_t *arr, uint64_t m, int rate, uint64_t *codeword,
                            uint8_t *levels, int mem);
 
+/* The tree above L leaf hashes (L a power of two, 32 B each): levels gets
+ * the upper levels back to back, L/2, L/4, ..., 1 hashes (L - 1 in total);
+ * every inner node is blake3(left || left) as the reference builds it.
+ * replaces create_tree_blake (merkle_tree.cpp:267-299). */
+gbz_status gbz_merkle_tree_from_leaves(gbz_ctx *ctx, const uint8_t *leaves, uint64_t L, uint8_t *levels, int mem);
+
 /* eq table B[x] = prod_i (bit_i(x) ? r_i : 1 - r_i), 2^nr elements.
  * replaces precompute_beta (utils.cpp:198-243). */
 gbz_status gbz_precompute_beta(gbz_ctx *ctx, const uint64_t *r, int nr, uint64_t *B, int mem);
@@ -570,6 +576,23 @@ uint64_t gbz_prove_transcript_bytes(int logn, int rate);
  * (every round's claim) and returns GBZ_ECHECK if one failed. */
 gbz_status gbz_prove(gbz_ctx *ctx, const uint64_t *witness, int logn, int rate, uint32_t prng_seed,
                      uint8_t *transcript, uint64_t capacity, int mem);
+
+/* Whir_Open of one claim (Whir.cpp:388-467) on caller arrays, whir_k = 4:
+ * arr (2^logn elements), codeword = its rate-fold RS encoding (the codeword
+ * Whir_Commit_initial made; rate * 2^logn elements), point (logn elements)
+ * and K (2 words) the claim (K = sum_x arr(x) eq(point, x)).  prng is the
+ * glibc random() state the reference's F::_random / rand() draws continue
+ * from; it is advanced past every draw of the opening.  The commitment tree
+ * is not an input: the paths are recomputed from the codeword (inner nodes
+ * hash their left child twice, so every node is a chain from one leaf).
+ * Transcript: 1 COMMIT_ROOT of the codeword, then the WHIR records of
+ * gbz_prove (tags 7-18); gbz_whir_open_transcript_bytes bytes.
+ * GBZ_ECHECK when a round message does not match the running claim.
+ * replaces Whir_Open (Whir.cpp:388-467). */
+gbz_status gbz_whir_open(gbz_ctx *ctx, const uint64_t *arr, int logn, int rate, const uint64_t *codeword,
+                         const uint64_t *point, const uint64_t *K, gbz_prng *prng, uint8_t *transcript,
+                         uint64_t capacity, int mem);
+uint64_t gbz_whir_open_transcript_bytes(int logn, int rate);
 
 /* Kernel launches of one proof (host-side count, no GPU needed); 0 for an
  * unsupported shape. */

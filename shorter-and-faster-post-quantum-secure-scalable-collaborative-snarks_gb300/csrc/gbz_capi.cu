@@ -347,6 +347,24 @@ gbz_status gbz_merkle_commit_blake(gbz_ctx *ctx, const uint64_t *elems, uint64_t
   API_END(ctx)
 }
 
+gbz_status gbz_merkle_tree_from_leaves(gbz_ctx *ctx, const uint8_t *leaves, uint64_t L, uint8_t *levels, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(leaves, "leaves");
+  need(levels, "levels");
+  check_pow2(L, "create_tree_blake: leaf count");
+  if (ilog2(L) > kMaxLogN) throw ArgError("create_tree_blake: more than 2^28 leaves");
+  if (L == 1) return GBZ_OK;
+  uint8_t *buf = (uint8_t *)ctx->buf(0, 32 * (2 * L - 1));
+  const cudaMemcpyKind kin = mem == GBZ_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  GBZ_CUDA(cudaMemcpyAsync(buf, leaves, 32 * L, kin, ctx->stream));
+  merkle_from_leaves_launch(buf, L, ctx->stream);
+  const cudaMemcpyKind kout = mem == GBZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  GBZ_CUDA(cudaMemcpyAsync(levels, buf + 32 * L, 32 * (L - 1), kout, ctx->stream));
+  finish(ctx, mem);
+  API_END(ctx)
+}
+
 gbz_status gbz_merkle_open_blake(const uint8_t *levels, uint64_t N, uint64_t pos, uint8_t *path, uint32_t *depth) {
   if (!levels || !path || N < 4 || !is_pow2(N)) return GBZ_EINVAL;
   uint64_t cnt = N / 4;
@@ -1392,6 +1410,76 @@ gbz_status gbz_party_sumcheck(gbz_ctx *ctx, int form, const uint64_t *v1, const 
   y[0] = hs.y.re;
   y[1] = hs.y.im;
   if (hs.error) return fail(ctx, GBZ_ECHECK, "party sumcheck: a round polynomial did not match the running claim");
+  API_END(ctx)
+}
+
+uint64_t gbz_whir_open_transcript_bytes(int logn, int rate) {
+  try {
+    ProofPlan p;
+    p.logn = logn;
+    p.rate = rate;
+    if (logn < 3 || logn > 26 || rate < 2 || rate > 64 || !is_pow2((uint64_t)rate)) return 0;
+    p.n = 1ull << logn;
+    p.L = p.n * (uint64_t)rate;
+    OpenOnly o{};
+    enqueue_proof(p, nullptr, 1, nullptr, true, false, &o);
+    return p.layout.len;
+  } catch (...) {
+    return 0;
+  }
+}
+
+gbz_status gbz_whir_open(gbz_ctx *ctx, const uint64_t *arr, int logn, int rate, const uint64_t *codeword,
+                         const uint64_t *point, const uint64_t *K, gbz_prng *prng, uint8_t *transcript,
+                         uint64_t capacity, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(arr, "arr");
+  need(codeword, "codeword");
+  need(point, "point");
+  need(K, "K");
+  need(prng, "prng");
+  need(transcript, "transcript");
+  const uint64_t bytes = gbz_whir_open_transcript_bytes(logn, rate);
+  if (!bytes) throw ArgError("whir open: unsupported shape (3 <= logn, rate a power of two in [2, 64], rate * 2^logn <= 2^26)");
+  if (capacity < bytes) return fail(ctx, GBZ_ESMALL, "transcript buffer smaller than gbz_whir_open_transcript_bytes");
+  auto key = std::make_pair(logn, rate);
+  auto it = ctx->plans.find(key);
+  if (it == ctx->plans.end()) it = ctx->plans.emplace(key, plan_create(logn, rate)).first;
+  ProofPlan &p = *it->second;
+  p.prof = nullptr;
+  plan_prepare_open(p);
+  if (p.open_transcript_bytes != bytes) throw ArgError("whir open: transcript layout mismatch");
+  cudaStream_t s = ctx->stream;
+  OpenOnly o{};
+  uint64_t Kw[2];
+  if (mem == GBZ_MEM_HOST) {
+    GBZ_CUDA(cudaMemcpyAsync(p.w, arr, 16 * p.n, cudaMemcpyHostToDevice, s));
+    GBZ_CUDA(cudaMemcpyAsync(p.cw[0], codeword, 16 * p.L, cudaMemcpyHostToDevice, s));
+    fe *dpt = (fe *)ctx->buf(0, 16ull * logn);
+    GBZ_CUDA(cudaMemcpyAsync(dpt, point, 16ull * logn, cudaMemcpyHostToDevice, s));
+    o.codeword = p.cw[0];
+    o.point = dpt;
+    Kw[0] = K[0];
+    Kw[1] = K[1];
+  } else {
+    o.codeword = (const fe *)codeword;
+    o.point = (const fe *)point;
+    GBZ_CUDA(cudaMemcpyAsync(Kw, K, 16, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaStreamSynchronize(s));
+  }
+  o.K = fe_make(Kw[0], Kw[1]);
+  static_assert(sizeof(gbz_prng) == sizeof(glibc_prng), "gbz_prng layout");
+  std::memcpy(&o.prng, prng, sizeof(glibc_prng));
+  const fe *w = mem == GBZ_MEM_HOST ? p.w : (const fe *)arr;
+  enqueue_proof(p, w, 0, s, false, false, &o);
+  GBZ_CUDA(cudaMemcpyAsync(transcript, p.open_transcript, bytes,
+                           mem == GBZ_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  glibc_prng after;
+  GBZ_CUDA(cudaMemcpyAsync(&after, &p.st->prng, sizeof(glibc_prng), cudaMemcpyDeviceToHost, s));
+  const uint32_t err = plan_error_flags(p, s);  // synchronises s
+  std::memcpy(prng, &after, sizeof(glibc_prng));
+  if (err) return fail(ctx, GBZ_ECHECK, "whir open: a round message did not match the running claim");
   API_END(ctx)
 }
 

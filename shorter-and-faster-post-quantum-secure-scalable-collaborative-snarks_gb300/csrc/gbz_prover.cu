@@ -41,6 +41,18 @@ __global__ void k_init(ProofState *st, uint32_t seed, int seed_in_state) {
   st->error = 0;
 }
 
+// The state of an opening alone: the caller's generator, point and claim.
+__global__ void k_init_open(ProofState *st, glibc_prng g, const fe *point, int logn, fe K) {
+  if (threadIdx.x == 0) {
+    st->fs = fe_zero();
+    st->prng = g;
+    st->y = fe_zero();
+    st->K = K;
+    st->error = 0;
+  }
+  for (int i = threadIdx.x; i < logn; i += blockDim.x) st->chal[i] = point[i];
+}
+
 // z_i = hash_to_field({0}) for i < logn.
 __global__ void k_point(ProofState *st, int logn, uint8_t *tr, uint64_t off) {
   if (threadIdx.x) return;
@@ -665,10 +677,35 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   return p;
 }
 
+void plan_prepare_open(ProofPlan &p) {
+  if (p.open_transcript) return;
+  Layout saved = p.layout;
+  const int launches = p.launches;
+  int cat[PC_COUNT];
+  for (int c = 0; c < PC_COUNT; c++) cat[c] = p.cat_launches[c];
+  p.layout = Layout();
+  p.layout.record_headers = true;
+  OpenOnly o{};
+  enqueue_proof(p, nullptr, 0, nullptr, /*dry=*/true, false, &o);
+  const Layout open_layout = p.layout;
+  p.layout = saved;
+  p.launches = launches;
+  for (int c = 0; c < PC_COUNT; c++) p.cat_launches[c] = cat[c];
+  p.open_transcript_bytes = open_layout.len;
+  p.open_transcript = (uint8_t *)p.dalloc(open_layout.len);
+  std::vector<uint8_t> img(open_layout.len, 0);
+  for (auto &h : open_layout.headers) {
+    std::memcpy(&img[h.off], &h.tag, 4);
+    std::memcpy(&img[h.off + 4], &h.count, 4);
+  }
+  GBZ_CUDA(cudaMemcpy(p.open_transcript, img.data(), img.size(), cudaMemcpyHostToDevice));
+}
+
 // Enqueue one proof.  witness: device pointer (nullptr: use plan->w).
 // The dry run (dry = true) launches nothing; it fixes the transcript layout
 // and counts the launches per category.
-void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry, bool seed_in_state) {
+void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry, bool seed_in_state,
+                   const OpenOnly *open) {
   Layout &lay = p.layout;
   lay.len = 0;
   if (dry) {
@@ -677,7 +714,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   }
   const fe *w = witness ? witness : p.w;
   const int logn = p.logn;
-  uint8_t *tr = p.transcript;
+  uint8_t *tr = open ? p.open_transcript : p.transcript;
   ProofState *st = p.st;
   Profiler *prof = (!dry && p.prof && p.prof->enabled) ? p.prof : nullptr;
   // RUN(category, kernel launches, statement): counts in the dry run, else
@@ -705,7 +742,11 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     GBZ_CUDA(cudaEventRecord(p.ev_in, s));
     GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_in, 0));
   }
-  RUN(PC_PROTOCOL, 1, k_init<<<1, 32, 0, s>>>(st, prng_seed, seed_in_state ? 1 : 0));
+  if (open) {
+    RUN(PC_PROTOCOL, 1, k_init_open<<<1, 32, 0, s>>>(st, open->prng, open->point, logn, open->K));
+  } else {
+    RUN(PC_PROTOCOL, 1, k_init<<<1, 32, 0, s>>>(st, prng_seed, seed_in_state ? 1 : 0));
+  }
   // The opening's randomness, drawn on the query stream while the
   // commitment and the sumcheck run.
   {
@@ -738,9 +779,14 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   // The witness is expected in the base field (the imaginary words zero):
   // its transform is then a half-length transform of packed pairs
   // (ntt_launch_real); any other witness takes the general transform.
-  if (!dry) GBZ_CUDA(cudaMemsetAsync(&st->nonreal, 0, sizeof(uint32_t), c));
-  RUN_ON(c, PC_NTT, ntt_launch_real_count(ilog2(L)),
-         ntt_launch_real(p.tables(ilog2(L) - 1), p.tables(ilog2(L)), w, p.n, p.cw[0], p.tmp, &st->nonreal, c));
+  if (open) {
+    if (!dry && open->codeword != p.cw[0])
+      GBZ_CUDA(cudaMemcpyAsync(p.cw[0], open->codeword, 16 * L, cudaMemcpyDeviceToDevice, c));
+  } else {
+    if (!dry) GBZ_CUDA(cudaMemsetAsync(&st->nonreal, 0, sizeof(uint32_t), c));
+    RUN_ON(c, PC_NTT, ntt_launch_real_count(ilog2(L)),
+           ntt_launch_real(p.tables(ilog2(L) - 1), p.tables(ilog2(L)), w, p.n, p.cw[0], p.tmp, &st->nonreal, c));
+  }
   // The root (a chain of compressions from leaf 0) is computed on the query
   // stream once the codeword exists, off the chain of commits.
   uint64_t off_root[kMaxWhirIter + 1];
@@ -748,6 +794,10 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_commit[0], c));
   int iter = 0;
 
+  uint64_t m = p.n;
+  const fe *a = w;
+  if (open) goto opening;
+  {
   // 2. evaluation point and its eq table.
   off = lay.rec(T_EVAL_POINT, logn, 16);
   RUN(PC_PROTOCOL, 1, k_point<<<1, 32, 0, s>>>(st, logn, tr, off));
@@ -758,8 +808,6 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   //    is represented by the shrinking tables E_i (vb ping-pong) and the
   //    prefix product epre (k_sc_round_eq).
   uint64_t off_claim = lay.rec(T_CLAIM, 1, 16);
-  uint64_t m = p.n;
-  const fe *a = w;
   int pp = 0, ep = 0;  // va ping-pong for w, vb ping-pong for E
   bool tail_done = false;
   for (int i = 0; i < logn; i++) {
@@ -806,6 +854,8 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
     RUN(PC_PROTOCOL, 1, k_sc_final<<<1, 32, 0, s>>>(st, a2, nullptr, tr, off));
     pp ^= 1;
   }
+  }
+opening:
 
   // 4. WHIR open of (v1[0], chal): b = precompute_beta(chal), arr = w.
   //    Three chains: folds and beta updates on s, commits on c, queries

@@ -76,6 +76,8 @@ struct ProofPlan {
   ProofState *st = nullptr;
   uint8_t *transcript = nullptr;
   uint64_t transcript_bytes = 0;
+  uint8_t *open_transcript = nullptr;  // an opening alone (gbz_whir_open): its own records and headers
+  uint64_t open_transcript_bytes = 0;
   Layout layout;
   int launches = 0;               // kernel launches per proof (counted by the dry run)
   int cat_launches[PC_COUNT] = {0};
@@ -114,13 +116,29 @@ __global__ void k_zero_tree_paths(int depth, int l, uint8_t *tr, uint64_t off_pa
 __global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
                         uint64_t off_point, uint64_t off_eval, int check_K, const fe *point);
 
+// An opening alone (Whir_Open, Whir.cpp:388-467): the caller's codeword of
+// the polynomial (device, rate * n entries), the claim's point (device, logn
+// entries) and value K, and the glibc generator state the draws start from.
+struct OpenOnly {
+  const fe *codeword = nullptr;
+  const fe *point = nullptr;
+  fe K;
+  glibc_prng prng;
+};
+
 std::unique_ptr<ProofPlan> plan_create(int logn, int rate);
+// Allocates the plan's buffer for openings alone, with its record headers
+// (once; the proof's layout and launch counts are left as they are).
+void plan_prepare_open(ProofPlan &p);
 // Enqueues one proof on stream s (dry: only computes the layout).  With
 // seed_in_state the PRNG seed is read from the plan's state (written by
 // set_seed_launch), so that the enqueued work can be captured once as a CUDA
 // graph and replayed for any seed.
+// With `open`, only the opening of (witness, open->codeword) at the given
+// claim is enqueued: the commitment root of the codeword, then the WHIR
+// records (no evaluation point, claim or sumcheck records).
 void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry,
-                   bool seed_in_state = false);
+                   bool seed_in_state = false, const OpenOnly *open = nullptr);
 void set_seed_launch(ProofPlan &p, uint32_t seed, cudaStream_t s);
 // Enqueues one proof of the witness at w by replaying a captured graph
 // (captured on first use of this address; s must be a capturable stream).

@@ -49,7 +49,8 @@ EXPORTS = (
     "gbz_set_graphs", "gbz_ntt_full_twiddles", "gbz_encode_concatenated", "gbz_leader_root",
     "gbz_whir_batch_schedule", "gbz_whir_batch_open", "gbz_pcs_schedule", "gbz_pcs_commit", "gbz_pcs_free",
     "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open", "gbz_pcs_claim", "gbz_cosumcheck",
-    "gbz_cosumcheck_transcript_bytes",
+    "gbz_cosumcheck_transcript_bytes", "gbz_whir_open", "gbz_whir_open_transcript_bytes",
+    "gbz_merkle_tree_from_leaves",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -173,6 +174,9 @@ def _load():
         "gbz_cosumcheck": (c_int, [vp, c_int, c_int, u64, vp, vp, vp, vp, vp, c_int, vp, vp, vp, vp, c_int, vp, vp,
                                    vp, vp, u64, c_int]),
         "gbz_cosumcheck_transcript_bytes": (u64, [c_int, c_int, vp, c_int]),
+        "gbz_whir_open": (c_int, [vp, vp, c_int, c_int, vp, vp, vp, vp, vp, u64, c_int]),
+        "gbz_whir_open_transcript_bytes": (u64, [c_int, c_int]),
+        "gbz_merkle_tree_from_leaves": (c_int, [vp, vp, u64, vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -507,6 +511,26 @@ class Context:
         out = fe_array(rows)
         self.check(lib.gbz_tensor_eval_vector(self.h, _ptr(pt), cols, rows, rate, my_id, _ptr(out), MEM_HOST))
         return out
+
+    def create_tree_blake(self, leaves):
+        """create_tree_blake (merkle_tree.cpp:267) over (L, 32) leaf hashes:
+        the upper levels, L/2 + ... + 1 hashes, as an (L - 1, 32) array."""
+        lv = np.ascontiguousarray(leaves, dtype=np.uint8).reshape(-1, 32)
+        out = np.zeros((max(lv.shape[0] - 1, 1), 32), dtype=np.uint8)
+        self.check(lib.gbz_merkle_tree_from_leaves(self.h, _ptr(lv), lv.shape[0], _ptr(out), MEM_HOST))
+        return out[:lv.shape[0] - 1]
+
+    def Whir_Open(self, arr, logn, rate, codeword, point, K, prng):
+        """Whir_Open (Whir.cpp:388) of the claim (K, point); prng (gbz.Prng) is
+        advanced in place.  Returns the transcript bytes."""
+        arr, cw = _fe(arr), _fe(codeword)
+        pt = np.ascontiguousarray(point, dtype=np.uint64).reshape(-1, 2)
+        Kk = np.ascontiguousarray(K, dtype=np.uint64).reshape(2)
+        nb = lib.gbz_whir_open_transcript_bytes(logn, rate)
+        tr = np.zeros(nb, dtype=np.uint8)
+        self.check(lib.gbz_whir_open(self.h, _ptr(arr), logn, rate, _ptr(cw), _ptr(pt), _ptr(Kk),
+                                     ctypes.addressof(prng), _ptr(tr), nb, MEM_HOST))
+        return tr.tobytes()
 
     def pcs_sumcheck_phase3(self, B, queries, s, N, rate, my_id):
         """pcs_sumcheck_phase3 (coPCS.cpp:634) on a copy of B, returned."""
