@@ -64,6 +64,7 @@ LOGN, RATE = 24, 2
 # 2^22, so the write figure is a lower bound).
 NTT_TRAFFIC_2E22 = {"read": 585.3e6, "write": 175.0e6}
 E2E_LANES = 3  # slots of the batched end-to-end pass
+SERVE_REPEATS = 3  # interleaved repeats of the served and plain runs at 200 requests/s
 SEED = 0x5EED0000 + 2 * 65536  # witness seed of the 2^24 rate-1/2 workload
 METRIC = "proofs/s and p50/p99 latency, batched+served vs plain GPU prover, bit-exact"
 CONFIG = {
@@ -146,7 +147,33 @@ def algorithmic_int_work(logn, rate):
             comps += l * depth * (depth + 1) // 2
     M = ls[0] // 2
     ntt = M // 2 * (M.bit_length() - 1) + M + sum(L // 2 * (L.bit_length() - 1) for L in ls[1:])
-    return {"ntt": ntt, "merkle_chain": comps}
+    return {"ntt": ntt, "merkle_chain": comps, "update_betas": update_betas_fmuls(logn, rate)}
+
+
+def update_betas_fmuls(logn, rate):
+    """F_{p^2} multiplies of the WHIR beta updates of one proof, as the prover
+    runs them (gbz_prover.cu: update_betas_by_transform).  Iteration t adds
+    sum_i c_i w^{q_i j} (l queries) to the m new entries of b, with the
+    exponents taken at half the new codeword length T = NL / 2: when l m >
+    4 T (and T > 2^13) as one second pass of a length-T transform whose rows
+    are formed from the entries (T / N1 rows of N1 = 2^k1, k1 = ceil(log2 T
+    / 2): 3 multiplies per (entry, row) to form them, (N1 / 2) k1
+    butterflies per row), else as direct geometric sums (l m)."""
+    n = 1 << logn
+    m, cur, total = n, rate, 0
+    while m > 4:
+        l = int(-100 / np.log2(np.sqrt(1.0 / cur)))
+        m //= 4
+        NL = 2 * cur * m
+        T = NL // 2
+        lt = T.bit_length() - 1
+        if 13 < lt <= 26 and m <= T and l * m > 4 * T:
+            k1 = (lt + 1) // 2
+            total += 3 * l * (T >> k1) + (T // 2) * k1
+        else:
+            total += l * m
+        cur *= 2
+    return total
 
 
 class ClockSampler:
@@ -368,10 +395,23 @@ def run_many(gbz, O, ctx, repeats):
     keep3, st3 = transcripts(slog, srate)
     ctx.prove_batch(sws, slog, srate, sseeds, lanes=8, out=st3)  # warm plans and graphs
     served = {}
-    # plain: one proof at a time, each replayed from its graph like gbz_prove
-    for name, arr, kw in [("served", arrivals, dict(lanes=8, depth=2)),
-                          ("plain", arrivals, dict(lanes=1, depth=1)),
-                          ("served_saturated", np.zeros(len(slog)), dict(lanes=8, depth=2)),
+    # served and plain interleaved over SERVE_REPEATS repeats of the same
+    # arrivals (plain: one proof at a time, each replayed from its graph like
+    # gbz_prove); the median of each figure with its spread (min, max)
+    runs = {}
+    for _ in range(SERVE_REPEATS):
+        for name, arr, kw in [("served", arrivals, dict(lanes=8, depth=2)),
+                              ("plain", arrivals, dict(lanes=1, depth=1))]:
+            _, lat, mk = ctx.serve(arr, sws, slog, srate, sseeds, out=st3, **kw)
+            runs.setdefault(name, []).append((len(slog) / mk, 1e3 * float(np.percentile(lat, 50)),
+                                              1e3 * float(np.percentile(lat, 99))))
+    for name, rs in runs.items():
+        a = np.array(rs)
+        served[name] = {"proofs_per_s": float(np.median(a[:, 0])), "p50_ms": float(np.median(a[:, 1])),
+                        "p99_ms": float(np.median(a[:, 2])),
+                        "p50_ms_range": [float(a[:, 1].min()), float(a[:, 1].max())],
+                        "p99_ms_range": [float(a[:, 2].min()), float(a[:, 2].max())], "repeats": len(rs)}
+    for name, arr, kw in [("served_saturated", np.zeros(len(slog)), dict(lanes=8, depth=2)),
                           ("plain_saturated", np.zeros(len(slog)), dict(lanes=1, depth=1))]:
         _, lat, mk = ctx.serve(arr, sws, slog, srate, sseeds, out=st3, **kw)
         served[name] = {"proofs_per_s": len(slog) / mk, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
@@ -616,8 +656,25 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     ao = torch.empty((1 << 16, 2), dtype=torch.int64, device="cuda")
     ag = lambda: ctx.check(gbz.lib.gbz_party_aggregate(ctx.h, msgs.data_ptr(), 64, 1 << 16, gbz._ptr(bb),
                                                        ao.data_ptr(), D))
+    # the length-2^25 transform with the first pass's twiddles read from the
+    # full table (the prover's default) against formed on the fly from the
+    # two-level table: the same values, one multiply per element more
+    L25 = 1 << (25 - shift)
+    xs = rnd(L25)
+    lg25 = L25.bit_length() - 1
+    ffull = lambda: ctx.check(gbz.lib.gbz_fft(ctx.h, xs.data_ptr(), lg25, 0, D))
+    t_full = timed(ffull)
+    gbz.lib.gbz_ntt_full_twiddles(0)
+    t_fly = timed(ffull)
+    gbz.lib.gbz_ntt_full_twiddles(1)
+    bfl = L25 // 2 * lg25
+    rec("ntt_2^25_full_twiddle_table", t_full, fmuls=bfl, note="radix-2 butterfly count; first-pass twiddles "
+        "read from the full table (the prover's default)")
+    rec("ntt_2^25_twiddles_on_the_fly", t_fly, fmuls=bfl, note="the same transform with the first-pass twiddles "
+        "formed from the two-level table (one more multiply per element, 134 MB less read)")
     rec("party_aggregate_64x2^16", timed(ag), hbm_bytes=16 * (65 << 16),
-        note="the call builds the 64-point unpack map on the host and copies it; the kernel is a small part")
+        note="the 64-point unpack-and-weight map built on the device (one CTA) then one pass over the "
+             "messages; host call incl. the 16 weights' copy")
     # aggregate_claims, 4 arrays x 4 points of 2^22
     la = 22 - shift
     arrs = [rnd(1 << la) for _ in range(4)]
@@ -869,7 +926,14 @@ def main():
         if cat == "ntt":
             a = work["ntt"] / t / 1e9
             r["int"] = {"achieved": a, "peak": fmul_peak / 1e9, "unit": "G F-mul/s (radix-2 butterflies)",
-                        "frac": a / (fmul_peak / 1e9), "butterflies_per_proof": work["ntt"]}
+                        "frac": a / (fmul_peak / 1e9), "butterflies_per_proof": work["ntt"],
+                        "alu_pipe_ncu": "57 % (pass A) / 51 % (pass B), issue active 52 % / 46 % "
+                                        "(profiles/ntt_pass_2e23.md)"}
+        if cat == "update_betas":
+            a = work["update_betas"] / t / 1e9
+            r["int"] = {"achieved": a, "peak": fmul_peak / 1e9, "unit": "G F-mul/s",
+                        "frac": a / (fmul_peak / 1e9), "fmuls_per_proof": work["update_betas"],
+                        "alu_pipe_ncu": "54 % in the sparse-rows pass (profiles/update_betas_sparse_2e22.md)"}
         if cat == "merkle":
             r["compressions_per_proof"] = work["merkle_chain"]
             r["note"] = "root and path chains only (latency bound); whole trees: rows.merkle_tree"

@@ -255,6 +255,9 @@ gbz_status gbz_cosumcheck_phase1(gbz_ctx *ctx, const uint64_t *p1, const uint64_
 gbz_status gbz_cosumcheck_phase2(gbz_ctx *ctx, const uint64_t *v, uint64_t n, const uint64_t *L, int logd,
                                  uint64_t *out, int mem);
 
+/* With nb = 0 (or l = 0) b is left as it is and the l combination weights
+ * are still written to challenges (both update_betas entry points). */
+
 /* The same update as gbz_whir_update_betas, for callers that must not let
  * the library allocate device memory at call time (a service that has
  * already handed all device memory to request slots, or a host runtime with
@@ -267,8 +270,11 @@ gbz_status gbz_cosumcheck_phase2(gbz_ctx *ctx, const uint64_t *v, uint64_t n, co
  *   every GPU loading the library keeps until exit; it holds at most 256
  *   queries, so l > 256 returns GBZ_EINVAL (as do a null b/r, a null queries
  *   with l > 0, and N not a power of two or above 2^28).
- *   The first call on a device looks up that array's device address (with
- *   the device current); make that first call before any stream capture.
+ *   A call looks up that array's device address (with the device current),
+ *   so a context re-created after a device reset gets its own; a call made
+ *   while its stream is being captured uses the address that the last
+ *   uncaptured call on the device found, so make one call on each device
+ *   before any stream capture.
  *   All calls share the array: calls that overlap on the GPU (other streams,
  *   other host threads) race and must be serialised by the caller.  Nothing
  *   in it needs to start at zero: each call writes every entry it reads.

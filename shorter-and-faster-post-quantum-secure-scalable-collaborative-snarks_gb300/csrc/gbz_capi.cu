@@ -476,7 +476,9 @@ gbz_status gbz_whir_update_betas(gbz_ctx *ctx, uint64_t *b, uint64_t nb, const i
   const int32_t *dq = dev_view(ctx, 1, queries, 4ull * (l ? l : 1), mem, true);
   ub_prep_kernel<<<1, 256, 0, ctx->stream>>>(ctx->st, dq, l, ilog2(N), fe_make(r[0], r[1]));
   GBZ_CUDA(cudaGetLastError());
-  if (update_betas_by_transform(l, nb, N)) {
+  if (nb == 0 || l == 0) {
+    // nothing to update; the combination weights are still written
+  } else if (update_betas_by_transform(l, nb, N)) {
     fe *tmp = (fe *)ctx->buf(2, 16 * N);
     ntt_sparse_accumulate(ctx->tables(ilog2(N)), ctx->st->q, ctx->st->comb, l, db, nb, tmp, ctx->stream);
   } else {
@@ -718,10 +720,12 @@ gbz_status gbz_party_aggregate(gbz_ctx *ctx, const uint64_t *msgs, int N, uint64
   need(b, "b");
   need(out, "out");
   if (N < 4 || N > 1024 || !is_pow2((uint64_t)N)) throw ArgError("aggregate: N must be a power of two in [4, 1024]");
-  std::vector<fe> lambda = aggregate_weights(N, reinterpret_cast<const fe *>(b));
   const fe *dm = dev_view(ctx, 0, (const fe *)msgs, 16 * len * N, mem, true);
+  // the unpack-and-weight map, built on the device from the N/4 weights (host memory)
+  fe *db = (fe *)ctx->buf(3, 16ull * (N / 4));
+  GBZ_CUDA(cudaMemcpyAsync(db, b, 16ull * (N / 4), cudaMemcpyHostToDevice, ctx->stream));
   fe *dl = (fe *)ctx->buf(1, 16 * N);
-  GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16 * N, cudaMemcpyHostToDevice, ctx->stream));
+  aggregate_weights_launch(db, N, dl, ctx->stream);
   fe *dout = dev_view(ctx, 2, (fe *)out, 16 * len, mem, false);
   aggregate_launch(dm, N, len, dl, dout, ctx->stream);
   copy_out(ctx, (fe *)out, dout, 16 * len, mem);

@@ -151,6 +151,33 @@ aggregate_kernel(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out)
   }
 }
 
+// The leader's unpack-and-weight map on the device (one CTA, N <= 1024): the
+// form sum_{j < N/4} b_j E[2j] of the unpacked shares E = DFT(D IDFT(s)),
+// D = diag(omega_{2N}^{-i}), is lambda^T s with lambda = IDFT(D DFT(g)),
+// g[2j] = b_j (both transform matrices are symmetric).
+constexpr int kLambdaMax = 1024;
+__global__ void __launch_bounds__(1024) lambda_kernel(const fe *b, int N, int logN, fe *lambda) {
+  __shared__ fe g[kLambdaMax], h[kLambdaMax], W[kLambdaMax];
+  const int k = threadIdx.x;
+  const fe w = root_of_unity(logN);
+  if (k < N) {
+    W[k] = fpow(w, (uint64_t)k);
+    g[k] = ((k & 1) == 0 && (k >> 1) < N / 4) ? b[k >> 1] : fe_zero();
+  }
+  __syncthreads();
+  if (k < N) {  // h = D DFT(g)
+    fe acc = fe_zero();
+    for (int j = 0; j < N; j += 2) acc = fadd(acc, fmul(g[j], W[(j * k) & (N - 1)]));
+    h[k] = fmul(acc, fpow(finv(root_of_unity(logN + 1)), (uint64_t)k));
+  }
+  __syncthreads();
+  if (k < N) {  // lambda = IDFT(h)
+    fe acc = fe_zero();
+    for (int j = 0; j < N; j++) acc = fadd(acc, fmul(h[j], W[(N - ((j * k) & (N - 1))) & (N - 1)]));
+    lambda[k] = fmul(acc, finv(fe_make((uint64_t)N, 0)));
+  }
+}
+
 // flags[blk] = 1 when block blk of v has a non-zero entry.
 __global__ void nonzero_blocks_kernel(const fe *v, uint64_t nblocks, int logd, uint8_t *flags) {
   const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,6 +367,12 @@ void column_merkle_launch(const fe *rows, int nrows, uint64_t L, uint8_t *levels
 
 void shares_launch(const fe *v, const fe *fill, uint64_t groups, int N, const fe *mu, fe *shares, cudaStream_t s) {
   shares_kernel<<<grid(groups), 256, 0, s>>>(v, fill, groups, N, N / 4, N / 2, mu, shares);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void aggregate_weights_launch(const fe *b, int N, fe *lambda, cudaStream_t s) {
+  if (N < 4 || N > kLambdaMax || (N & (N - 1))) throw ArgError("aggregate: N must be a power of two in [4, 1024]");
+  lambda_kernel<<<1, N, 0, s>>>(b, N, ilog2((uint64_t)N), lambda);
   GBZ_CUDA(cudaGetLastError());
 }
 

@@ -29,6 +29,9 @@ std::vector<fe> aggregate_weights(int N, const fe *b);
 // The weights of g^T E for any g over the unpacked shares E.
 std::vector<fe> aggregate_weights_even(int N, const std::vector<fe> &g);
 void aggregate_launch(const fe *msgs, int N, uint64_t len, const fe *lambda, fe *out, cudaStream_t s);
+// The same weights as aggregate_weights, computed on the device from b
+// (N/4 weights, device) into lambda (N, device).
+void aggregate_weights_launch(const fe *b, int N, fe *lambda, cudaStream_t s);
 // coSumcheck phase 1 helpers; extended blocks of up to 2^13 entries (one
 // batched transform per block).
 constexpr int kMaxCoLogD = 13;

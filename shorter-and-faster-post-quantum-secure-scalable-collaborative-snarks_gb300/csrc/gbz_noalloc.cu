@@ -31,20 +31,29 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch array on the current device.  The host-side
-// symbol is only a stand-in; the address comes from cudaGetSymbolAddress,
-// once per device, with that device current.
-cudaError_t scratch_on_current_device(NoAllocScratch **out) {
+// Device address of the scratch array in the current device's context.  The
+// host-side symbol is only a stand-in; the address comes from
+// cudaGetSymbolAddress with that device current.  Outside a stream capture
+// it is looked up on every call (a context created after a device reset, or
+// another context made current on the device, has its own copy of the
+// array); during a capture the address the last uncaptured call cached for
+// the device is used, so that the capture contains no lookup.
+cudaError_t scratch_on_current_device(cudaStream_t s, NoAllocScratch **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_addr[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
     g_scratch_addr[dev] = p;
+  } else if (!g_scratch_addr[dev]) {
+    return cudaErrorStreamCaptureUnsupported;  // no uncaptured call on this device yet
   }
   *out = reinterpret_cast<NoAllocScratch *>(g_scratch_addr[dev]);
   return cudaSuccess;
@@ -80,13 +89,14 @@ extern "C" gbz_status gbz_whir_update_betas_noalloc(uint64_t *b, uint64_t nb, co
   if (!b || !r || (l > 0 && !queries)) return GBZ_EINVAL;
   if (l < 0 || l > kMaxQueries) return GBZ_EINVAL;  // scratch holds at most 256 queries
   if (!is_pow2(N) || ilog2(N) > kMaxLogN) return GBZ_EINVAL;
-  if (l == 0 || nb == 0) return GBZ_OK;
-  NoAllocScratch *scratch = nullptr;
-  if (scratch_on_current_device(&scratch) != cudaSuccess) return GBZ_ECUDA;
+  if (l == 0) return GBZ_OK;
   cudaStream_t s = (cudaStream_t)cuda_stream;
+  NoAllocScratch *scratch = nullptr;
+  if (scratch_on_current_device(s, &scratch) != cudaSuccess) return GBZ_ECUDA;
   noalloc_prep_kernel<<<1, 256, 0, s>>>(&scratch->st, queries, l, ilog2(N), fe_make(r[0], r[1]),
                                         reinterpret_cast<fe *>(challenges));
   if (cudaGetLastError() != cudaSuccess) return GBZ_ECUDA;
+  if (nb == 0) return GBZ_OK;  // the weights are written; there is nothing to update
   try {
     update_betas_launch(reinterpret_cast<fe *>(b), nb, &scratch->st, l, scratch->pw, s);
   } catch (const CudaError &) {

@@ -68,6 +68,27 @@ def test_noalloc_matches_allocating_entry_point_twice(ctx, gbz, logb, logN, l):
             buf.free()
 
 
+def test_empty_beta_vector_writes_the_weights_in_both_entry_points(ctx, gbz):
+    """nb = 0: nothing to update, the l combination weights still written,
+    the same by both entry points."""
+    rng = np.random.default_rng(7)
+    rt = _cudart()
+    q = rng.integers(0, 1 << 12, size=20).astype(np.int32)
+    r = rand_fe(rng, 1)[0].copy()
+    b = np.zeros((1, 2), dtype=np.uint64)
+    b1, q1 = DevBuf(ctx, gbz, b), DevBuf(ctx, gbz, q)
+    ch1 = np.zeros((20, 2), dtype=np.uint64)
+    ctx.check(gbz.lib.gbz_whir_update_betas(ctx.h, b1.p, 0, q1.p, 20, 1 << 12, r.ctypes.data, ch1.ctypes.data,
+                                            gbz.MEM_DEVICE))
+    ch2 = DevBuf(ctx, gbz, np.zeros((20, 2), dtype=np.uint64))
+    assert gbz.lib.gbz_whir_update_betas_noalloc(b1.p, 0, q1.p, 20, 1 << 12, r.ctypes.data, ch2.p, None) == gbz.OK
+    assert rt.cudaDeviceSynchronize() == 0
+    assert np.array_equal(ch2.read(ch1), ch1)
+    assert ch1[1].tolist() != [0, 0]
+    for buf in (b1, q1, ch2):
+        buf.free()
+
+
 def test_noalloc_rejects_more_queries_than_its_scratch_holds(ctx, gbz):
     b = np.zeros((16, 2), dtype=np.uint64)
     q = np.zeros(257, dtype=np.int32)
