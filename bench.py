@@ -444,16 +444,18 @@ def pcs_point(gbz, n):
 def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
     """Configuration 4: the reference's coPCS test (main.cpp:49-163) with
     N = 16 parties on one device, M = 2^24 shared coefficients (2^22 share
-    entries per party): PCS_commit, the claim (F_ip) and PCS_open_new up to
-    the leader's delegation, all device resident (torch buffers, C-ABI calls
-    on device pointers).  The shares are the ones the reference's rank 0
-    deals (glibc's default stream, generated on the host before timing); the
-    transcript is compared with the reference's own 16-rank run when its
-    digest fixture is present (tests/golden/parties_N16_M24.json)."""
+    entries per party): PCS_commit, the claim (F_ip) and PCS_open_new, once
+    up to the leader's delegation (gbz_pcs_open) and once whole
+    (gbz_pcs_open_full: the leader's delegation proofs, final checks and
+    WHIR opening too), all device resident (torch buffers, C-ABI calls on
+    device pointers).  The shares are the ones the reference's rank 0 deals
+    (glibc's default stream, generated on the host before timing); the
+    transcripts are compared with the reference's own 16-rank run when its
+    fixture is present (tests/golden/parties_N16_M24.json)."""
     import torch
     M = 1 << logM
     deg, q, rnd = gbz.pcs_schedule(N, M, PCS_RATES)
-    shares, random = O.copcs_party_shares(N, M, rnd * N // 4)
+    shares, random, g_deal = O.copcs_party_shares(N, M, rnd * N // 4, state=True)
     sh = torch.from_numpy(shares.view(np.int64)).cuda()
     rn = torch.from_numpy(random.view(np.int64)).cuda()
     r0 = np.array([x[0] for x in PCS_RATES], dtype=np.int32)
@@ -478,13 +480,30 @@ def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
                                    tr.data_ptr(), tr.numel(), gbz.MEM_DEVICE))
         ctx.synchronize()
 
+    # the whole of PCS_open_new: the leader's tail draws from rank 0's
+    # generator as the dealing leaves it
+    flags = ctypes.c_uint32(0)
+
+    def open_full(h, trf):
+        g = gbz.Prng(1)
+        ctypes.memmove(ctypes.addressof(g), g_deal, ctypes.sizeof(g))
+        ctx.check(lib.gbz_pcs_claim(ctx.h, h, rd.data_ptr(), r.shape[0], Kd.data_ptr(), gbz.MEM_DEVICE))
+        fsd.copy_(torch.from_numpy(fs0.view(np.int64)))
+        ctx.check(lib.gbz_pcs_open_full(ctx.h, h, rd.data_ptr(), r.shape[0], Kd.data_ptr(), fsd.data_ptr(),
+                                        ctypes.addressof(g), ctypes.byref(flags), trf.data_ptr(), trf.numel(),
+                                        gbz.MEM_DEVICE))
+        ctx.synchronize()
+
     h = commit()
-    nbytes = ctypes.c_uint64(0)
+    nbytes, fbytes = ctypes.c_uint64(0), ctypes.c_uint64(0)
     ctx.check(lib.gbz_pcs_info(h, None, None, None, ctypes.byref(nbytes)))
+    ctx.check(lib.gbz_pcs_open_full_bytes(h, ctypes.byref(fbytes)))
     tr = torch.zeros(nbytes.value, dtype=torch.uint8, device="cuda")
+    trf = torch.zeros(fbytes.value, dtype=torch.uint8, device="cuda")
     open_(h, tr)  # warm-up (checked on the device: GBZ_ECHECK otherwise)
+    open_full(h, trf)
     lib.gbz_pcs_free(h)
-    t_c, t_o = [], []
+    t_c, t_o, t_f = [], [], []
     for _ in range(repeats):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -492,17 +511,25 @@ def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
         t1 = time.perf_counter()
         open_(h, tr)
         t2 = time.perf_counter()
+        open_full(h, trf)
+        t3 = time.perf_counter()
         lib.gbz_pcs_free(h)
         t_c.append(t1 - t0)
         t_o.append(t2 - t1)
+        t_f.append(t3 - t2)
     digest = hashlib.sha256(tr.cpu().numpy().tobytes()).hexdigest()
-    out = {"workload": "the reference's coPCS test (PCS_commit + F_ip + PCS_open_new to the leader's "
-                       "delegation) with %d parties on one device, M = 2^%d (2^%d share entries per party), "
+    full = gbz.parse_transcript(trf.cpu().numpy().tobytes())
+    out = {"workload": "the reference's coPCS test (PCS_commit + F_ip + PCS_open_new; open_full adds the "
+                       "leader's delegation proofs, final checks and WHIR opening) with %d parties on one device, "
+                       "M = 2^%d (2^%d share entries per party), "
                        "rates {{4},{4},{4,4},{4,4}}" % (N, logM, logM + 2 - (N.bit_length() - 1)),
            "parties": N, "share_len": 4 * M // N, "degrees": deg, "queries": q,
            "commit_ms": 1e3 * min(t_c), "open_ms": 1e3 * min(t_o), "total_ms": 1e3 * (min(t_c) + min(t_o)),
            "runs_per_s": 1.0 / (min(t_c) + min(t_o)), "transcript_bytes": int(nbytes.value),
            "transcript_sha256": digest,
+           "open_full_ms": 1e3 * min(t_f), "full_total_ms": 1e3 * (min(t_c) + min(t_f)),
+           "full_runs_per_s": 1.0 / (min(t_c) + min(t_f)), "full_transcript_bytes": int(fbytes.value),
+           "leader_flags": int(flags.value),
            "timing": "host wall clock around the synchronised C-ABI calls (device pointers), best of %d" % repeats}
     fx = os.path.join(ROOT, "tests", "golden", "parties_N%d_M%d.json" % (N, logM))
     if os.path.exists(fx):
@@ -510,6 +537,17 @@ def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
             ref = json.load(f)
         out["transcript_equals_reference"] = ref.get("gpu_transcript_sha256") == digest
         out["reference_ranks_seconds_x86"] = ref.get("ref_seconds")
+        lead = ref.get("leader")
+        if lead:
+            # the leader's tail against rank 0's records: the segments'
+            # commitment roots, the delegation claims, the WHIR opening's
+            # final claim and the beta delegation's claim
+            tags = lambda t: [p for k, _, p in full if k == t]
+            ok = [x.hex() for x in tags(46)] == [rd["root"] for rd in lead["rounds"]]
+            ok &= [x.hex() for x in tags(52)] == [rd["pex"] for rd in lead["rounds"]]
+            ok &= all(c.hex().startswith(rd["pmf"]) for c, rd in zip(tags(50), lead["rounds"]))
+            ok &= tags(54)[0].hex() == lead["whir_claim"] and tags(56)[0].hex() == lead["beta_eval_y"]
+            out["leader_tail_equals_reference"] = bool(ok)
     return {"party_shares": out}
 
 

@@ -525,6 +525,42 @@ gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, in
 gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
                         uint8_t *transcript, uint64_t capacity, int mem);
 
+/* The whole of PCS_open_new: gbz_pcs_open's records, then the leader's tail,
+ * which draws from the leader's glibc generator *prng (rank 0's random()
+ * stream when the opening starts; updated in place) and never from the
+ * Fiat-Shamir chain:
+ *  per delegate check after the first (coPCS.cpp:770-831):
+ *   46 D_ROOT 32B (Whir_Commit_initial(segments padded to the largest
+ *   delegation size, rate 4): the root of MT_commit_Blake over its codeword)
+ *   | 47 D_QUERIES u32 x l (rand() % C[0].size()) | prove_multi_folding
+ *   (delegate_protocol.cpp:147-250): 48 D_POLYS 16B x 5R, 49 D_FINAL 16B x 4
+ *   (quadruple_sumcheck), 48 16B x 3 log2 d, 49 16B x 2 (_quadratic_sumcheck),
+ *   50 D_CLAIM 16B x (1 + log2 max_delegation) (value, point, zeros) |
+ *   51 D_OPEN 16B x l (the extended segments at the queries) |
+ *   prove_extension (:369-429): 48 16B x 4R', 49 16B x 3 (_cubic_sumcheck),
+ *   48 16B x 3 log2 C0, 49 16B x 2 (prove_fft's _quadratic_sumcheck),
+ *   52 D_EXT_CLAIM 16B x (1 + log2 d + log2 S)
+ *  then (coPCS.cpp:1697-1753): 53 UNPACKED 16B x N (the parties' final data
+ *   and B unpacked, N/2 each) | aggregate_claims and aggregate_commitments
+ *   (Whir.cpp:547-668): 20 AGGR_CHALLENGES (beta weights, array weights),
+ *   21 AGGR_K, 22 AGGR_QUERIES, 23 AGGR_PATHS, 24 AGGR_ROOT | _Whir_Open
+ *   (Whir.cpp:469-545, whir_k = 8) as the records 19, 7-18 of
+ *   gbz_whir_batch_open | 54 WHIR_CLAIM 16B x (1 + log2 max_delegation) |
+ *   55 RC 16B x 2 (r_c, B_eval_claim) | delegate_beta_eval
+ *   (delegate_protocol.cpp:431-504): 56 BETA_Y 16B, 48/49 (_cubic_sumcheck),
+ *   57 L_EVALS 16B x rounds, 48/49 (_quadratic_sumcheck; the reference reads
+ *   past the end of b there, here b is zero beyond its length)
+ * *flags (may be NULL) receives the checks the reference prints (bit 0: a
+ * quadruple/cubic round message, bit 3: final verification step 1, bit 5:
+ * WHIR verification step 3) and those it stops at (bit 1: a delegation
+ * check, bit 2: decoding, bit 4: the WHIR opening's checks, bit 6: the
+ * final verification step, bit 7: delegating the betas); the latter return
+ * GBZ_ECHECK.  Transcript bytes: gbz_pcs_open_full_bytes.
+ * replaces PCS_open_new (coPCS.cpp:1310-1607, 1610-1755) on N ranks. */
+gbz_status gbz_pcs_open_full(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
+                             gbz_prng *prng, uint32_t *flags, uint8_t *transcript, uint64_t capacity, int mem);
+gbz_status gbz_pcs_open_full_bytes(const gbz_pcs *pcs, uint64_t *bytes);
+
 /* quadratic_coSumcheck / cubic_coSumcheck of N parties on one device
  * (form GBZ_SC_QUADRATIC or GBZ_SC_CUBIC).  p1, p2 (and p3): N x n party
  * shares, party-major; R: the parties' sparse vectors, N x sum_i (2 or 4)

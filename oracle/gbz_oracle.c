@@ -158,6 +158,11 @@ int32_t orc_prng_next(orc_prng *g) {
   return out;
 }
 
+/* count random() calls whose outputs are dropped */
+void orc_prng_skip(orc_prng *g, uint64_t count) {
+  for (uint64_t i = 0; i < count; i++) (void)orc_prng_next(g);
+}
+
 /* randomNumber (fieldElement.cpp:363-368) */
 static uint64_t prng_number(orc_prng *g) {
   uint64_t ret = (uint64_t)(orc_prng_next(g) % 10);
@@ -1002,6 +1007,12 @@ void orc_generate_randomness(orc_prng *g, int64_t n, uint64_t *out) {
 }
 
 void orc_copcs_party_shares(int N, int64_t M, int64_t R, uint64_t *shares, uint64_t *random) {
+  orc_copcs_party_shares_g(N, M, R, shares, random, NULL);
+}
+
+/* The same, and rank 0's generator as the dealing leaves it in *g_out (may
+ * be NULL): nothing else draws from it until the leader's delegation. */
+void orc_copcs_party_shares_g(int N, int64_t M, int64_t R, uint64_t *shares, uint64_t *random, orc_prng *g_out) {
   orc_prng g;
   orc_prng_seed(&g, 1); /* glibc's default state: the reference never seeds rank 0's generator */
   int64_t n = M > R ? M : R;
@@ -1011,6 +1022,7 @@ void orc_copcs_party_shares(int N, int64_t M, int64_t R, uint64_t *shares, uint6
   orc_generate_randomness(&g, R, buf);
   orc_secret_shares_g(buf, R, N, 1, &g, random);
   free(buf);
+  if (g_out) *g_out = g;
 }
 
 /* unpack_secret_share (MPI_utils.cpp:2769-2785) with _k = k = N */

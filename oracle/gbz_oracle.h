@@ -28,6 +28,7 @@ typedef struct {
 
 void orc_prng_seed(orc_prng *g, uint32_t seed);
 int32_t orc_prng_next(orc_prng *g);
+void orc_prng_skip(orc_prng *g, uint64_t count);
 /* F::_random (fieldElement.cpp:119-125, 363-368). */
 void orc_prng_field(orc_prng *g, uint64_t out[2]);
 
@@ -125,6 +126,7 @@ void orc_generate_randomness(orc_prng *g, int64_t n, uint64_t *out);
  * generate_randomness + compute_secret_shares with privacy.  shares is
  * N x (M / (N/4)), random N x (R / (N/4)), party-major. */
 void orc_copcs_party_shares(int N, int64_t M, int64_t R, uint64_t *shares, uint64_t *random);
+void orc_copcs_party_shares_g(int N, int64_t M, int64_t R, uint64_t *shares, uint64_t *random, orc_prng *g_out);
 
 /* sumcheck_aggr leader computation (MPI_utils.cpp:2631-2644): msgs is N
  * party messages of len elements; b has N/4 weights. */

@@ -47,6 +47,7 @@ def lib():
         u8p = ctypes.POINTER(ctypes.c_uint8)
         i64 = ctypes.c_int64
         L.orc_prng_next.restype = ctypes.c_int32
+        L.orc_prng_skip.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
         L.orc_merkle_commit.restype = ctypes.c_int
         L.orc_merkle_open.restype = ctypes.c_int
         L.orc_whir_queries.restype = ctypes.c_int
@@ -153,6 +154,20 @@ class Prng:
 
     def next(self):
         return lib().orc_prng_next(ctypes.byref(self.s))
+
+    def skip(self, count):
+        """Drops count random() outputs."""
+        lib().orc_prng_skip(ctypes.byref(self.s), count)
+
+    def state(self):
+        """The 33 words of the generator (table, front and rear index)."""
+        return bytes(self.s)
+
+    @classmethod
+    def from_state(cls, state):
+        g = cls(1)
+        ctypes.memmove(ctypes.addressof(g.s), state, ctypes.sizeof(g.s))
+        return g
 
     def field(self):
         out = np.zeros(2, dtype=np.uint64)
@@ -286,14 +301,17 @@ def secret_shares(v, N, privacy=False, prng_seed=1):
     return out
 
 
-def copcs_party_shares(N, M, R):
+def copcs_party_shares(N, M, R, state=False):
     """Party shares of the reference's coPCS test (main.cpp:49-68) at N
-    parties: (shares N x 4M/N, random N x 4R/N), rank 0's glibc draws."""
+    parties: (shares N x 4M/N, random N x 4R/N), rank 0's glibc draws; with
+    state, also the generator's 33 words as the dealing leaves them."""
     k = N // 4
     sh = np.zeros((N, M // k, 2), dtype=np.uint64)
     rn = np.zeros((N, R // k, 2), dtype=np.uint64)
-    lib().orc_copcs_party_shares(ctypes.c_int(N), ctypes.c_int64(M), ctypes.c_int64(R), _p64(sh), _p64(rn))
-    return sh, rn
+    g = _Prng()
+    lib().orc_copcs_party_shares_g(ctypes.c_int(N), ctypes.c_int64(M), ctypes.c_int64(R), _p64(sh), _p64(rn),
+                                   ctypes.byref(g))
+    return (sh, rn, bytes(g)) if state else (sh, rn)
 
 
 def party_aggregate(msgs, b):

@@ -19,6 +19,7 @@
 #include <mpi.h>
 #include <vector>
 
+using std::pair;
 using std::vector;
 typedef vector<vector<_hash>> Levels;
 
@@ -220,6 +221,97 @@ vector<vector<F>> __wrap__Z24send_final_sumcheck_polySt6vectorIN5virgo12fieldEle
   for (auto &h : H) flat.insert(flat.end(), h.begin(), h.end());
   put_field("SFSO", flat);
   return H;
+}
+
+// The leader's side of PCS_open_new after the parties' rounds: the
+// delegation proofs of delegate_checks and the final WHIR opening
+// (coPCS.cpp:773-831, 1697-1754).  A claim is recorded as its value then its
+// point.
+void put_claim(const char tag[4], const pair<F, vector<F>> &c) {
+  vector<F> v{c.first};
+  v.insert(v.end(), c.second.begin(), c.second.end());
+  put_field(tag, v);
+}
+
+// delegate_protocol.cpp:147  prove_multi_folding(segments, L, y, queries, n, ps)
+pair<F, vector<F>> __real__Z19prove_multi_foldingRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES3_S3_S_IS_IjSaIjEESaIS8_EEiRd(
+    vector<vector<F>> &seg, vector<F> L, vector<F> y, vector<vector<u32>> q, int n, double &ps);
+pair<F, vector<F>> __wrap__Z19prove_multi_foldingRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES3_S3_S_IS_IjSaIjEESaIS8_EEiRd(
+    vector<vector<F>> &seg, vector<F> L, vector<F> y, vector<vector<u32>> q, int n, double &ps) {
+  pair<F, vector<F>> c =
+      __real__Z19prove_multi_foldingRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES3_S3_S_IS_IjSaIjEESaIS8_EEiRd(
+          seg, L, y, q, n, ps);
+  put_claim("PMFC", c);
+  return c;
+}
+
+// delegate_protocol.cpp:369  prove_extension(segments, extended, o, queries, rate, ps)
+pair<F, vector<F>> __real__Z15prove_extensionRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES6_S3_S_IiSaIiEEiRd(
+    vector<vector<F>> &seg, vector<vector<F>> &ext, vector<F> o, vector<int> q, int rate, double &ps);
+pair<F, vector<F>> __wrap__Z15prove_extensionRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES6_S3_S_IiSaIiEEiRd(
+    vector<vector<F>> &seg, vector<vector<F>> &ext, vector<F> o, vector<int> q, int rate, double &ps) {
+  put_field("PEXO", o);
+  pair<F, vector<F>> c =
+      __real__Z15prove_extensionRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES6_S3_S_IiSaIiEEiRd(seg, ext, o, q,
+                                                                                                         rate, ps);
+  put_claim("PEXC", c);
+  return c;
+}
+
+// delegate_protocol.cpp:431  delegate_beta_eval(r, L, y, offset, ps): the claim y it starts from
+F __real__Z18delegate_beta_evalSt6vectorIN5virgo12fieldElementESaIS1_EES_IS3_SaIS3_EES1_iRd(vector<F> r,
+                                                                                           vector<vector<F>> L, F y,
+                                                                                           int offset, double &ps);
+F __wrap__Z18delegate_beta_evalSt6vectorIN5virgo12fieldElementESaIS1_EES_IS3_SaIS3_EES1_iRd(vector<F> r,
+                                                                                           vector<vector<F>> L, F y,
+                                                                                           int offset, double &ps) {
+  put_field("DBEY", vector<F>{y});
+  F out = __real__Z18delegate_beta_evalSt6vectorIN5virgo12fieldElementESaIS1_EES_IS3_SaIS3_EES1_iRd(r, L, y, offset, ps);
+  put("DBEE", 0, nullptr, 0);
+  return out;
+}
+
+// Whir.cpp:608  aggregate_claims(arrays, arr, b_aggr, claims, K): the aggregated claim K and the
+// challenges (beta weights, then array weights)
+vector<vector<F>> __real__Z16aggregate_claimsRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EERS3_S7_S_IS_ISt4pairIS1_S3_ESaIS9_EESaISB_EERS1_(
+    vector<vector<F>> &arrays, vector<F> &arr, vector<F> &b, vector<vector<pair<F, vector<F>>>> claims, F &K);
+vector<vector<F>> __wrap__Z16aggregate_claimsRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EERS3_S7_S_IS_ISt4pairIS1_S3_ESaIS9_EESaISB_EERS1_(
+    vector<vector<F>> &arrays, vector<F> &arr, vector<F> &b, vector<vector<pair<F, vector<F>>>> claims, F &K) {
+  vector<vector<F>> ch =
+      __real__Z16aggregate_claimsRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EERS3_S7_S_IS_ISt4pairIS1_S3_ESaIS9_EESaISB_EERS1_(
+          arrays, arr, b, claims, K);
+  put_field("AGCK", vector<F>{K});
+  vector<F> flat;
+  for (auto &c : ch) flat.insert(flat.end(), c.begin(), c.end());
+  put_field("AGCC", flat);
+  return ch;
+}
+
+// Whir.cpp:469  _Whir_Open(arr, codeword, MT, b, claims, challenges, K, rate, Verify): the final claim
+pair<F, vector<F>> __real__Z10_Whir_OpenRSt6vectorIN5virgo12fieldElementESaIS1_EES4_RS_IS_I5_hashSaIS5_EESaIS7_EES4_S_IS_ISt4pairIS1_S3_ESaISC_EESaISE_EES3_S1_ib(
+    vector<F> &arr, vector<F> &cw, Levels &mt, vector<F> &b, vector<vector<pair<F, vector<F>>>> claims,
+    vector<F> challenges, F K, int rate, bool verify);
+pair<F, vector<F>> __wrap__Z10_Whir_OpenRSt6vectorIN5virgo12fieldElementESaIS1_EES4_RS_IS_I5_hashSaIS5_EESaIS7_EES4_S_IS_ISt4pairIS1_S3_ESaISC_EESaISE_EES3_S1_ib(
+    vector<F> &arr, vector<F> &cw, Levels &mt, vector<F> &b, vector<vector<pair<F, vector<F>>>> claims,
+    vector<F> challenges, F K, int rate, bool verify) {
+  put("WOPB", 0, nullptr, 0);
+  pair<F, vector<F>> c =
+      __real__Z10_Whir_OpenRSt6vectorIN5virgo12fieldElementESaIS1_EES4_RS_IS_I5_hashSaIS5_EESaIS7_EES4_S_IS_ISt4pairIS1_S3_ESaISC_EESaISE_EES3_S1_ib(
+          arr, cw, mt, b, claims, challenges, K, rate, verify);
+  put_claim("WOPC", c);
+  return c;
+}
+
+// utils.cpp:1201  evaluate_vector(v, r): its length and value
+F __real__Z15evaluate_vectorSt6vectorIN5virgo12fieldElementESaIS1_EES3_(vector<F> v, vector<F> r);
+F __wrap__Z15evaluate_vectorSt6vectorIN5virgo12fieldElementESaIS1_EES3_(vector<F> v, vector<F> r) {
+  const uint32_t n = (uint32_t)v.size();
+  F out = __real__Z15evaluate_vectorSt6vectorIN5virgo12fieldElementESaIS1_EES3_(v, r);
+  F len;
+  len.real = n;
+  len.img = 0;
+  put_field("EVLV", vector<F>{len, out});
+  return out;
 }
 
 }  // extern "C"

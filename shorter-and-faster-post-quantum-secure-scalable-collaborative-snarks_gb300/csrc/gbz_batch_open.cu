@@ -156,7 +156,7 @@ int ilog2i(uint64_t x) { return ilog2(x); }
 
 }  // namespace
 
-BatchPlan batch_plan(int k, const uint64_t *sizes, int rate, int whir_k) {
+BatchPlan batch_plan(int k, const uint64_t *sizes, int rate, int whir_k, uint64_t zero_leaves0) {
   BatchPlan P;
   if (k < 1 || k > kMaxVecs) throw ArgError("batch open: 1..64 polynomials");
   if (!sizes) throw ArgError("null pointer: sizes");
@@ -195,6 +195,11 @@ BatchPlan batch_plan(int k, const uint64_t *sizes, int rate, int whir_k) {
   }
   // the loop of Whir.cpp:761-833 on sizes only
   uint64_t m = sizes[0], L = m * (uint64_t)rate, leaves = L / 4;
+  if (zero_leaves0) {
+    if (!is_pow2(zero_leaves0) || zero_leaves0 > leaves) throw ArgError("batch open: bad zero tree size");
+    leaves = zero_leaves0;
+    P.zero_tree0 = true;
+  }
   int cur = rate, iter = 0, next = 1, wk = whir_k;
   uint64_t bytes = 8 + 8 * (uint64_t)P.kappa.size();
   P.cw_len.assign(k, 0);
@@ -257,12 +262,11 @@ BatchPlan batch_plan(int k, const uint64_t *sizes, int rate, int whir_k) {
   return P;
 }
 
-namespace {
-
 // Walks the opening once: with dry set it only lays out the records
 // (lay.headers), otherwise it enqueues the kernels that fill them.
-void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const fe *const *betas,
-          const fe *const *codewords, const uint8_t *levels0, uint8_t *tr, Layout &lay, bool dry) {
+void batch_open_walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const fe *const *betas,
+                     const fe *const *codewords, const uint8_t *levels0, uint8_t *tr, Layout &lay, bool dry,
+                     WalkTrace *trace) {
   cudaStream_t s = R.s;
   ProofState *st = R.st;
   const uint64_t n0 = P.sizes[0], L0 = n0 * (uint64_t)P.rate;
@@ -302,7 +306,7 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
   // a commitment over the current codeword (its nodes are computed as
   // compression chains from the codeword, never stored), or the tree over
   // zero leaves that aggregate_commitments builds.
-  enum { TREE_LEVELS, TREE_CODEWORD, TREE_ZERO } tree_kind = TREE_LEVELS;
+  enum { TREE_LEVELS, TREE_CODEWORD, TREE_ZERO } tree_kind = P.zero_tree0 ? TREE_ZERO : TREE_LEVELS;
   const uint8_t *tree = levels0;
   int ci = -1;                // which working buffer holds cw (-1: the caller's)
   // open_tree_blake for l queries into the current tree of lv leaves
@@ -317,7 +321,7 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
     else k_zero_tree_paths<<<(unsigned)((depth + 31) / 32), 32, 0, s>>>(depth, l, tr, off_path);
     GBZ_CUDA(cudaGetLastError());
   };
-  uint64_t m = n0, L = L0, leaves = L0 / 4;
+  uint64_t m = n0, L = L0, leaves = P.zero_tree0 && !P.steps.empty() ? (1ull << P.steps[0].depth) : L0 / 4;
   int cur = P.rate;
   for (const BatchStep &e : P.steps) {
     if (e.iterate) {
@@ -325,6 +329,7 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
       // whir_sumcheck (Whir.cpp:233-249): log2 kappa rounds, fold i fused with message i+1
       for (int i = 0; i < logk; i++) {
         const uint64_t op = lay.rec(T_WHIR_POLY, 3, 16), oc = lay.rec(T_WHIR_CHALLENGE, 1, 16);
+        if (trace) trace->chal.push_back(oc);
         const int blocks = sc_blocks(i == 0 ? m / 2 : std::max<uint64_t>(m / 4, 1));
         if (!dry) {
           if (i == 0)
@@ -361,6 +366,13 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
       const uint64_t off_path = lay.rec(T_WHIR_PATHS, e.l * e.depth, 32);
       qa.off_comb = lay.rec(T_WHIR_COMBINE, e.l, 16);
       qa.off_K = lay.rec(T_WHIR_K, 1, 16);
+      if (trace) {
+        trace->queries.push_back(qa.off_q);
+        trace->comb.push_back(qa.off_comb);
+        trace->l.push_back(e.l);
+        trace->kappa.push_back(e.kappa);
+        trace->NL.push_back(NL);
+      }
       if (!dry) {
         const NttTables &told = R.tables(ilog2(L)), &tnew = R.tables(ilog2(NL));
         qa.st = st;
@@ -443,20 +455,27 @@ void walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const 
   const uint64_t off_poly = lay.rec(T_FINAL_POLY, (uint32_t)m, 16);
   const uint64_t off_point = lay.rec(T_FINAL_POINT, ilog2(m), 16);
   const uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
+  if (trace) {
+    trace->final_poly = off_poly;
+    trace->final_point = off_point;
+    trace->final_eval = off_eval;
+    trace->m_final = m;
+    trace->L_final = L;
+    trace->last_codeword = cw;
+    trace->final_arr = A[ai];
+  }
   if (!dry) {
     k_final<<<1, 32, 0, s>>>(st, A[ai], B[ai], (int)m, tr, off_poly, off_point, off_eval, 1, nullptr);
     GBZ_CUDA(cudaGetLastError());
   }
 }
 
-}  // namespace
-
 void batch_open_enqueue(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const fe *const *betas,
                         const fe *const *codewords, const uint8_t *levels0, fe K0, const glibc_prng &g0,
                         uint8_t *dtr) {
   Layout lay;
   lay.record_headers = true;
-  walk(R, P, arrays, betas, codewords, levels0, nullptr, lay, true);
+  batch_open_walk(R, P, arrays, betas, codewords, levels0, nullptr, lay, true);
   if (lay.len != P.transcript_bytes) throw ArgError("batch open: transcript layout mismatch");
   // record headers, payloads filled by the kernels
   std::vector<uint8_t> img(lay.len, 0);
@@ -469,7 +488,7 @@ void batch_open_enqueue(BatchResources &R, const BatchPlan &P, const fe *const *
   bo_init_kernel<<<1, 32, 0, R.s>>>(R.st, g0, K0);
   GBZ_CUDA(cudaGetLastError());
   Layout lay2;
-  walk(R, P, arrays, betas, codewords, levels0, dtr, lay2, false);
+  batch_open_walk(R, P, arrays, betas, codewords, levels0, dtr, lay2, false);
 }
 
 }  // namespace gbz

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "gbz_internal.cuh"
+#include "gbz_prover.cuh"
 
 namespace gbz {
 
@@ -28,12 +29,16 @@ struct BatchPlan {
   std::vector<BatchStep> steps;
   std::vector<uint64_t> cw_len;     // codeword length array i comes with (0: never merged)
   uint64_t m_final = 0, transcript_bytes = 0;
+  bool zero_tree0 = false;          // the first queries open a tree over zero leaves
 };
 
 // The schedule and per-step sizes for k polynomials of non-increasing
 // power-of-two sizes; throws ArgError for inputs the reference cannot run
 // (it reads its schedule past the end, or opens a leaf beyond its tree).
-BatchPlan batch_plan(int k, const uint64_t *sizes, int rate, int whir_k);
+// With zero_leaves0 > 0 the tree of the first codeword is the one
+// aggregate_commitments installs (Whir.cpp:590-605): zero_leaves0 leaf
+// hashes, all zero.
+BatchPlan batch_plan(int k, const uint64_t *sizes, int rate, int whir_k, uint64_t zero_leaves0 = 0);
 
 struct BatchResources {
   cudaStream_t s = nullptr;
@@ -42,6 +47,26 @@ struct BatchResources {
   ProofState *st = nullptr;
   fe *ub_scratch = nullptr;                  // kUpdateBetasScratch elements
 };
+
+// Where the walk put what a verifier of the opening reads again: per
+// sumcheck round its challenge, per iteration its queries (raw draws), the
+// update_betas weights, the query count and the new codeword length; the
+// final point and evaluation.
+struct WalkTrace {
+  std::vector<uint64_t> chal, queries, comb, NL;
+  std::vector<int> l, kappa;
+  uint64_t final_point = 0, final_eval = 0, final_poly = 0;
+  uint64_t m_final = 0, L_final = 0;  // final polynomial and codeword lengths
+  const fe *last_codeword = nullptr;  // the codeword of the last iteration (device)
+  const fe *final_arr = nullptr;      // the final polynomial (device)
+};
+
+// The opening loop itself: with dry set only the records are laid out in
+// lay, otherwise the kernels are enqueued on R.s.  The generator, the
+// running claim K and the flags are R.st's, which the caller initialises.
+void batch_open_walk(BatchResources &R, const BatchPlan &P, const fe *const *arrays, const fe *const *betas,
+                     const fe *const *codewords, const uint8_t *levels0, uint8_t *tr, Layout &lay, bool dry,
+                     WalkTrace *trace = nullptr);
 
 // Enqueues the whole opening on R.s (no host synchronisation): inputs are
 // device pointers (arrays / betas / codewords of the merged polynomials,

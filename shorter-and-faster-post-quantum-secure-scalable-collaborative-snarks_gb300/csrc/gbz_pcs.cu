@@ -17,6 +17,7 @@
 
 #include "gbz_copcs.cuh"
 #include "gbz_ctx.cuh"
+#include "gbz_pcs_leader.cuh"
 
 using namespace gbz_api;
 
@@ -331,12 +332,14 @@ k_round_verify(PcsDev *st, const fe *poly, int logd, fe *L, fe *scratch, uint8_t
 // equals output q of RS_multifold5 over C'_a).
 __global__ void k_gather(const fe *Cp, uint64_t pstride, uint64_t seg_n, int d, const fe *fold, uint64_t fstride,
                          const int32_t *qp, const int32_t *qpos, int l, fe *y, uint8_t *tr, uint64_t off_y,
-                         uint64_t off_seg) {
+                         uint64_t off_seg, fe *seg_out) {
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (uint64_t)l * d) return;
   const int j = (int)(t / d), k = (int)(t % d);
   const uint64_t a = (uint64_t)qp[j], q = (uint64_t)qpos[j];
-  put_fe(tr, off_seg + 16 * t, Cp[a * pstride + q + k * seg_n]);
+  const fe v = Cp[a * pstride + q + k * seg_n];
+  put_fe(tr, off_seg + 16 * t, v);
+  if (seg_out) seg_out[t] = v;
   if (k == 0) {
     const fe v = fold[a * fstride + q];
     y[j] = v;
@@ -944,6 +947,47 @@ OpenOffs open_layout(const gbz_pcs &pc, PcsLayout &lay) {
   return o;
 }
 
+// The sizes of the leader's tail (pointers are filled in by the opening).
+LeaderInputs leader_shape(const gbz_pcs &pc) {
+  const PcsSchedule &sc = pc.sc;
+  LeaderInputs in;
+  in.N = sc.N;
+  in.Bs = pc.Bs;
+  in.log_rate_offset = sc.log_rate_offset;
+  in.rate0 = sc.rate0;
+  uint64_t n = pc.Bs, cpl = pc.L;
+  for (int i = 0; i + 1 < sc.rounds; i++) {
+    LeaderRound r;
+    r.d = sc.degrees[i + 1];
+    r.l = sc.queries[i + 1];
+    r.n = cpl;
+    r.C0 = i ? (uint64_t)sc.degrees[i + 1] * sc.rate1[i + 1] : 0;
+    r.rate_next = i + 2 < sc.rounds ? sc.rate0[i + 2] : 0;
+    r.rate_cur = sc.rate0[i + 1];
+    in.rounds.push_back(r);
+    n /= (uint64_t)r.d;
+    cpl = (i + 2 < sc.rounds) ? n * sc.rate0[i + 2] : cpl / r.d;
+  }
+  in.n_final = n;
+  in.cpl_final = cpl;
+  in.max_delegation = 0;
+  for (int v : sc.delegation) in.max_delegation = std::max<uint64_t>(in.max_delegation, (uint64_t)v);
+  return in;
+}
+
+// The records of the leader's tail after the parties' records (lay.bytes is
+// where they start).
+void tail_layout(const gbz_pcs &pc, PcsLayout &lay) {
+  LeaderInputs in = leader_shape(pc);
+  Layout tl;
+  tl.record_headers = true;
+  LeaderResources R;
+  leader_tail(R, in, nullptr, nullptr, nullptr, tl);
+  const uint64_t base = lay.bytes;
+  for (const auto &h : tl.headers) lay.hdr.push_back({base + h.off, h.tag, h.count});
+  lay.bytes = base + tl.len;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1105,10 +1149,12 @@ gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, in
   API_END(ctx)
 }
 
-gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
-                        uint8_t *transcript, uint64_t capacity, int mem) {
+static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K,
+                                uint64_t *fs, bool full, gbz_prng *prng, uint32_t *flags, uint8_t *transcript,
+                                uint64_t capacity, int mem) {
   API_BEGIN(ctx)
   check_mem(mem);
+  if (full) need(prng, "prng");
   need(pcs, "pcs");
   need(r, "r");
   need(K, "K");
@@ -1122,7 +1168,12 @@ gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, c
   if (nr != lk + 5 + logBs) throw ArgError("pcs: the point must have log2(N/4) + 5 + log2(row length) entries");
   PcsLayout lay;
   const OpenOffs off = open_layout(*pcs, lay);
-  if (capacity < lay.bytes) throw ArgError("pcs: transcript capacity below gbz_pcs_info's open_transcript_bytes");
+  const uint64_t tail_base = lay.bytes;
+  LeaderInputs lead = leader_shape(*pcs);
+  if (full) tail_layout(*pcs, lay);
+  if (capacity < lay.bytes)
+    throw ArgError(full ? "pcs: transcript capacity below gbz_pcs_open_full_bytes"
+                        : "pcs: transcript capacity below gbz_pcs_info's open_transcript_bytes");
   cudaStream_t s = ctx->stream;
   OpenBufs ob;
   uint8_t *tr = mem == GBZ_MEM_DEVICE ? transcript : ob.alloc<uint8_t>(lay.bytes);
@@ -1321,8 +1372,33 @@ gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, c
     // delegate_checks (coPCS.cpp:740-891)
     const int l = sc.queries[i + 1];
     k_indexes<<<1, 256, 0, s>>>(st, l, N, (uint32_t)seg_n, qp, qpos, tr, ro.queries);
-    k_gather<<<grid((uint64_t)l * d), 256, 0, s>>>(Cp, cpl, seg_n, d, fold, seg_n, qp, qpos, l, y, tr, ro.y, ro.seg);
+    LeaderRound &lr = lead.rounds[i];
+    lr.d = d;
+    lr.l = l;
+    lr.n = cpl;
+    lr.C0 = i ? (uint64_t)sc.degrees[i + 1] * sc.rate1[i + 1] : 0;
+    lr.rate_next = i + 2 < sc.rounds ? sc.rate0[i + 2] : 0;
+    lr.rate_cur = sc.rate0[i + 1];
+    fe *seg_copy = nullptr;
+    if (full) {
+      fe *Lc = ob.alloc<fe>(d), *yc = ob.alloc<fe>(l);
+      int32_t *qpc = ob.alloc<int32_t>(l), *qposc = ob.alloc<int32_t>(l);
+      if (i) seg_copy = ob.alloc<fe>((uint64_t)l * d);
+      lr.L = Lc;
+      lr.y = yc;
+      lr.qp = qpc;
+      lr.qpos = qposc;
+      lr.seg = seg_copy;
+    }
+    k_gather<<<grid((uint64_t)l * d), 256, 0, s>>>(Cp, cpl, seg_n, d, fold, seg_n, qp, qpos, l, y, tr, ro.y, ro.seg,
+                                                   seg_copy);
     GBZ_CUDA(cudaGetLastError());
+    if (full) {
+      GBZ_CUDA(cudaMemcpyAsync((void *)lr.L, Ld, 16ull * d, cudaMemcpyDeviceToDevice, s));
+      GBZ_CUDA(cudaMemcpyAsync((void *)lr.y, y, 16ull * l, cudaMemcpyDeviceToDevice, s));
+      GBZ_CUDA(cudaMemcpyAsync((void *)lr.qp, qp, 4ull * l, cudaMemcpyDeviceToDevice, s));
+      GBZ_CUDA(cudaMemcpyAsync((void *)lr.qpos, qpos, 4ull * l, cudaMemcpyDeviceToDevice, s));
+    }
     if (!last) {
       k_check_y<<<grid(l), 256, 0, s>>>(Cpn, cpl_new, (uint32_t)sc.rate0[i + 2], (uint32_t)sc.rate0[i + 1], qp, qpos,
                                         y, l, st);
@@ -1330,6 +1406,11 @@ gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, c
     }
     k_s_update<<<1, 1, 0, s>>>(st, y, l, last ? 0 : 1, tr, ro.s, ro.K);
     GBZ_CUDA(cudaGetLastError());
+    if (full) {
+      fe *sc_ = ob.alloc<fe>(1);
+      GBZ_CUDA(cudaMemcpyAsync(sc_, &st->s, 16, cudaMemcpyDeviceToDevice, s));
+      lr.s = sc_;
+    }
     if (!last) {
       // pcs_sumcheck_phase3 (coPCS.cpp:634-648) with the scaled queries
       const int logw = ilog2((uint64_t)sc.rate0[i + 2] * n);
@@ -1349,9 +1430,53 @@ gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, c
     k_put_party<<<dim3(grid(cpl), N), 256, 0, s>>>(Cp, cpl, N, tr, off.final_ + 32 * n, 16 * per);
     GBZ_CUDA(cudaGetLastError());
   }
+  // the leader's delegation proofs, final checks and WHIR opening
+  ProofState *pst = nullptr;
+  uint32_t *dfl = nullptr;
+  if (full) {
+    lead.bcd = bcd;
+    lead.B = B;
+    lead.Cp = Cp;
+    lead.K = &st->K;
+    lead.r_first = &st->r_first;
+    lead.b2 = b2;
+    lead.b3 = b3;
+    lead.r2 = dr + lk + 5;
+    // unpack_secret_share(., N/2, N) (MPI_utils.cpp:2769-2785): output j is
+    // entry 2j of the unpacked shares, a fixed linear form of the N shares
+    std::vector<fe> U((size_t)(N / 2) * N);
+    for (int j = 0; j < N / 2; j++) {
+      std::vector<fe> gj(N, fe_zero());
+      gj[2 * j] = fe_one();
+      const std::vector<fe> w = aggregate_weights_even(N, gj);
+      for (int p = 0; p < N; p++) U[(size_t)j * N + p] = w[p];
+    }
+    fe *dU = ob.alloc<fe>(U.size());
+    GBZ_CUDA(cudaMemcpyAsync(dU, U.data(), 16 * U.size(), cudaMemcpyHostToDevice, s));
+    lead.unpack = dU;
+    pst = ob.alloc<ProofState>(1);
+    dfl = ob.alloc<uint32_t>(1);
+    glibc_prng g0;
+    static_assert(sizeof(glibc_prng) == sizeof(gbz_prng), "generator layouts");
+    std::memcpy(&g0, prng, sizeof g0);
+    leader_tail_init(pst, g0, dfl, s);
+    LeaderResources LR;
+    LR.s = s;
+    LR.alloc = [&ob](uint64_t bytes) -> void * { return ob.alloc<uint8_t>(bytes); };
+    LR.tables = [ctx](int lg) -> NttTables & { return ctx->tables(lg); };
+    Layout tl;
+    leader_tail(LR, lead, pst, dfl, tr + tail_base, tl);
+    if (tail_base + tl.len != lay.bytes) throw ArgError("pcs: leader transcript layout mismatch");
+  }
   // the chain state out, the flags checked
   PcsDev hst;
+  uint32_t hfl = 0;
+  glibc_prng hg{};
   GBZ_CUDA(cudaMemcpyAsync(&hst, st, sizeof(PcsDev), cudaMemcpyDeviceToHost, s));
+  if (full) {
+    GBZ_CUDA(cudaMemcpyAsync(&hfl, dfl, 4, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaMemcpyAsync(&hg, &pst->prng, sizeof hg, cudaMemcpyDeviceToHost, s));
+  }
   if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaMemcpyAsync(transcript, tr, lay.bytes, cudaMemcpyDeviceToHost, s));
   GBZ_CUDA(cudaStreamSynchronize(s));
   if (mem == GBZ_MEM_HOST) {
@@ -1360,9 +1485,37 @@ gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, c
   } else {
     GBZ_CUDA(cudaMemcpy(fs, &hst.fs, 16, cudaMemcpyHostToDevice));
   }
+  if (full) {
+    std::memcpy(prng, &hg, sizeof hg);
+    if (flags) *flags = hfl;
+  }
   if (hst.error) return fail(ctx, GBZ_ECHECK, hst.error & 1 ? "pcs: a round message does not match the claim"
                                                             : "pcs: a delegate check failed");
+  if (hfl & LF_FATAL) return fail(ctx, GBZ_ECHECK, "pcs: a check of the leader's delegation or final opening failed");
   API_END(ctx)
+}
+
+gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
+                        uint8_t *transcript, uint64_t capacity, int mem) {
+  return pcs_open_impl(ctx, pcs, r, nr, K, fs, false, nullptr, nullptr, transcript, capacity, mem);
+}
+
+gbz_status gbz_pcs_open_full(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
+                             gbz_prng *prng, uint32_t *flags, uint8_t *transcript, uint64_t capacity, int mem) {
+  return pcs_open_impl(ctx, pcs, r, nr, K, fs, true, prng, flags, transcript, capacity, mem);
+}
+
+gbz_status gbz_pcs_open_full_bytes(const gbz_pcs *pcs, uint64_t *bytes) {
+  if (!pcs || !bytes) return GBZ_EINVAL;
+  try {
+    PcsLayout lay;
+    open_layout(*pcs, lay);
+    tail_layout(*pcs, lay);
+    *bytes = lay.bytes;
+  } catch (const ArgError &) {
+    return GBZ_EINVAL;
+  }
+  return GBZ_OK;
 }
 
 gbz_status gbz_cosumcheck(gbz_ctx *ctx, int form, int N, uint64_t n, const uint64_t *p1, const uint64_t *p2,

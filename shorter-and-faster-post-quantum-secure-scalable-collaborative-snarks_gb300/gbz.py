@@ -50,7 +50,7 @@ EXPORTS = (
     "gbz_whir_batch_schedule", "gbz_whir_batch_open", "gbz_pcs_schedule", "gbz_pcs_commit", "gbz_pcs_free",
     "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open", "gbz_pcs_claim", "gbz_cosumcheck",
     "gbz_cosumcheck_transcript_bytes", "gbz_whir_open", "gbz_whir_open_transcript_bytes",
-    "gbz_merkle_tree_from_leaves",
+    "gbz_merkle_tree_from_leaves", "gbz_pcs_open_full", "gbz_pcs_open_full_bytes",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -177,6 +177,8 @@ def _load():
         "gbz_whir_open": (c_int, [vp, vp, c_int, c_int, vp, vp, vp, vp, vp, u64, c_int]),
         "gbz_whir_open_transcript_bytes": (u64, [c_int, c_int]),
         "gbz_merkle_tree_from_leaves": (c_int, [vp, vp, u64, vp, c_int]),
+        "gbz_pcs_open_full": (c_int, [vp, vp, vp, c_int, vp, vp, vp, vp, vp, u64, c_int]),
+        "gbz_pcs_open_full_bytes": (c_int, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -826,6 +828,22 @@ class PcsCommitment:
                                         self.open_bytes, MEM_HOST))
         return tr.tobytes(), f
 
+    def open_full(self, r, K, fs, prng):
+        """The whole of PCS_open_new, the leader's tail included: (transcript
+        bytes, fs after, flags).  prng (a Prng: the leader's random() stream
+        when the opening starts) is advanced in place."""
+        r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+        K = np.ascontiguousarray(K, dtype=np.uint64).reshape(2)
+        f = np.array(np.asarray(fs, dtype=np.uint64).reshape(2), copy=True)
+        nb = ctypes.c_uint64(0)
+        self.ctx.check(lib.gbz_pcs_open_full_bytes(self.h, ctypes.byref(nb)))
+        tr = np.zeros(nb.value, dtype=np.uint8)
+        flags = ctypes.c_uint32(0)
+        st = lib.gbz_pcs_open_full(self.ctx.h, self.h, _ptr(r), r.shape[0], _ptr(K), _ptr(f),
+                                   ctypes.addressof(prng), ctypes.byref(flags), _ptr(tr), nb.value, MEM_HOST)
+        self.ctx.check(st)
+        return tr.tobytes(), f, flags.value
+
     def free(self):
         if self.h:
             lib.gbz_pcs_free(self.h)
@@ -876,14 +894,16 @@ def cosumcheck(ctx, form, N, p1, p2, R, K, K_r, degrees, p3=None, r1=None, r2=No
     return claims, flags.value, tr.tobytes(), f
 
 
-PCS_UNITS = {32: 32, 33: 32, 37: 4}
+PCS_UNITS = {32: 32, 33: 32, 37: 4, 46: 32, 47: 4}
+# records of the batch opening with units other than a field element
+BATCH_UNITS = {19: 4, 22: 4, 23: 32, 24: 32}
 
 
 def parse_transcript(buf):
     """[(tag, count, payload bytes)] of a transcript."""
     buf = bytes(buf)
     out, off = [], 0
-    units = {1: 32, 9: 32, 13: 32, 10: 4, **PCS_UNITS}
+    units = {1: 32, 9: 32, 13: 32, 10: 4, **BATCH_UNITS, **PCS_UNITS}
     while off < len(buf):
         tag, count = np.frombuffer(buf, dtype=np.uint32, count=2, offset=off)
         unit = units.get(int(tag), 16)

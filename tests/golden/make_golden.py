@@ -235,7 +235,8 @@ def gen_batchopen():
 # count, then count units of these sizes.
 CAPTURE_UNIT = {"H2FI": 16, "H2FO": 16, "FRND": 16, "SHRS": 16, "PAGI": 16, "PAGO": 16, "SPDA": 16, "SPDB": 16,
                 "SPDC": 16, "WCIA": 16, "FIPK": 16, "GSYI": 16, "GSYO": 16, "GSSG": 16, "SAGI": 16, "SAGO": 16,
-                "SFSI": 16, "SFSO": 16,
+                "SFSI": 16, "SFSO": 16, "PMFC": 16, "PEXO": 16, "PEXC": 16, "DBEY": 16, "DBEE": 0,
+                "AGCK": 16, "AGCC": 16, "WOPB": 0, "WOPC": 16, "EVLV": 16,
                 "GIDX": 4, "RAND": 4, "GSQU": 4, "MTCB": 36, "CTRB": 36, "WCIR": 36}
 
 
@@ -343,6 +344,93 @@ def expected_open_transcript(ranks, N, logM, rates):
     return out
 
 
+def leader_tail(lead):
+    """The leader's records after the parties' rounds of PCS_open_new: per
+    delegation round the WHIR commitment of the gathered segments, the
+    extension query draws, the claims of prove_multi_folding and
+    prove_extension with the evaluations their checks compute; then
+    aggregate_claims, the openings of aggregate_commitments, _Whir_Open
+    (per iteration its commitment root, query draws and the roots of the
+    replies it hashes; the final claim) and delegate_beta_eval (its claim and
+    the evaluations of its check).  The glibc draws are counted in random()
+    calls: forty per F::_random() (two randomNumber() of twenty digits,
+    fieldElement.cpp:119-125, 363-368), one per rand()."""
+    import struct
+    sha = lambda b: hashlib.sha256(b).hexdigest()
+    tags = [r[0] for r in lead]
+    calls = lambda rs: sum(40 if r[0] == "FRND" else 1 for r in rs if r[0] in ("FRND", "RAND"))
+    w0 = tags.index("WCIA")
+    # (the calls before the tail are not all seen here: the dealing calls
+    # random() directly too; the oracle's restatement of the dealing gives
+    # the generator's state where the tail starts)
+    out = {"prng_calls": calls(lead[w0:]), "rounds": []}
+    i = w0
+    while True:
+        while i < len(lead) and lead[i][0] not in ("WCIA", "SPDA"):
+            i += 1
+        if lead[i][0] == "SPDA":
+            break
+        rd = {}
+        while lead[i][0] != "WCIR":
+            i += 1
+        n, = struct.unpack_from("<I", lead[i][2])
+        rd["whir_commit"] = n
+        rd["root"] = lead[i][2][4:].hex()
+        i += 1
+        q = []
+        while lead[i][0] == "RAND":
+            q.append(struct.unpack("<I", lead[i][2])[0])
+            i += 1
+        rd["queries2"] = q
+        ev = []
+        while lead[i][0] != "PEXC":
+            t, _, p = lead[i]
+            if t == "EVLV":
+                ev.append(p[16:].hex())
+            elif t == "PMFC":
+                rd["pmf"] = p.hex()
+            elif t == "PEXO":
+                rd["pexo_sha256"] = sha(p)
+            i += 1
+        rd["pex"] = lead[i][2].hex()
+        rd["check_evals"] = ev
+        out["rounds"].append(rd)
+        i += 1
+    k = tags.index("AGCK", i)
+    out["aggr_K"] = lead[k][2].hex()
+    out["aggr_challenges"] = lead[k + 1][2].hex()
+    i = k + 2
+    q = []
+    while lead[i][0] == "RAND":
+        q.append(struct.unpack("<I", lead[i][2])[0])
+        i += 1
+    out["aggr_queries"] = q
+    b, e = tags.index("WOPB", i), tags.index("WOPC", i)
+    it = []
+    j = b
+    while j < e:
+        if lead[j][0] == "RAND":
+            root = lead[j - 1]
+            qs = []
+            while lead[j][0] == "RAND":
+                qs.append(struct.unpack("<I", lead[j][2])[0])
+                j += 1
+            rr = b"".join(lead[j + t][2][4:] for t in range(len(qs)))
+            it.append({"commit": struct.unpack_from("<I", root[2])[0], "root": root[2][4:].hex(), "queries": qs,
+                       "reply_roots_sha256": sha(rr)})
+            j += len(qs)
+        else:
+            j += 1
+    out["whir_iterations"] = it
+    out["whir_evals"] = [lead[t][2][16:].hex() for t in range(b, e) if lead[t][0] == "EVLV"]
+    out["whir_claim"] = lead[e][2].hex()
+    d = tags.index("DBEY", e)
+    out["beta_eval_y"] = lead[d][2].hex()
+    de = tags.index("DBEE", d)
+    out["beta_eval_evals"] = [lead[t][2][16:].hex() for t in range(d, de) if lead[t][0] == "EVLV"]
+    return out
+
+
 def gen_parties():
     """The reference's own coPCS test (main.cpp:49-163: PCS_commit then
     PCS_open_new) run unmodified with N ranks as N processes (pigeon_mpi,
@@ -375,6 +463,7 @@ def gen_parties():
                 "polys": [hx(r[2]) for r in lead if r[0] == "PAGO"],
                 "y": [hx(r[2]) for r in lead if r[0] == "GSYO"],
                 "segments_sha256": [sha(r[2]) for r in lead if r[0] == "GSSG"],
+                "leader": leader_tail(lead),
                 "ranks": []}
         small = N * (1 << logM) <= (1 << 20)
         for rk, recs in enumerate(ranks):
