@@ -788,6 +788,7 @@ def main():
     ap.add_argument("--rows-only", action="store_true", help="only the per-row measurements (profiling)")
     ap.add_argument("--rows-shift", type=int, default=0, help="divide the per-row sizes by 2^k")
     ap.add_argument("--parties-only", action="store_true", help="only the party-shares (coPCS) measurement")
+    ap.add_argument("--parties-repeats", type=int, default=3, help="timed repeats of the party-shares run")
     args = ap.parse_args()
     ws, rank, local = dist_info()
     if ws > 1:
@@ -818,7 +819,7 @@ def main():
     stream = gbz.lib.gbz_get_stream(ctx.h)
 
     if args.parties_only:
-        print(json.dumps(run_party_shares(gbz, O, ctx, repeats=3)), flush=True)
+        print(json.dumps(run_party_shares(gbz, O, ctx, repeats=args.parties_repeats)), flush=True)
         ctx.close()
         return
 

@@ -174,8 +174,10 @@ gbz_status gbz_serve(gbz_ctx *ctx, int count, const double *arrival_s, const uin
                      const uint64_t *capacity, int mem, const gbz_sched_opts *opts, double *latency_s,
                      double *makespan_s);
 
-/* Frees the scheduler's cached slot plans; *cached_bytes (optional) gets
- * the device bytes they held. */
+/* Frees the scheduler's cached slot plans and the scratch the N-party
+ * calls (gbz_pcs_claim, gbz_pcs_open, gbz_pcs_open_full, gbz_cosumcheck)
+ * keep per shape between calls; *cached_bytes (optional) gets the device
+ * bytes they held. */
 gbz_status gbz_sched_release(gbz_ctx *ctx, uint64_t *cached_bytes);
 
 /* ----------------------------------------------------- coPCS-side rows */

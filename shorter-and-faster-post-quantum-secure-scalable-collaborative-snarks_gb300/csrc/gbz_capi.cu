@@ -184,6 +184,8 @@ void gbz_destroy(gbz_ctx *ctx) {
     ctx->profilers.clear();
     for (auto &kv : ctx->ntt) ntt_tables_free(kv.second);
     for (auto &kv : ctx->scratch) cudaFree(kv.second.first);
+    for (auto &kv : ctx->pools)
+      for (auto &e : kv.second) cudaFree(e.first);
     cudaFree(ctx->st);
     cudaFree(ctx->ub_scratch);
     if (ctx->side.stream) {
@@ -874,8 +876,16 @@ gbz_status gbz_serve(gbz_ctx *ctx, int count, const double *arrival_s, const uin
 
 gbz_status gbz_sched_release(gbz_ctx *ctx, uint64_t *cached_bytes) {
   API_BEGIN(ctx)
-  if (cached_bytes) *cached_bytes = ctx->sched ? ctx->sched->cached_bytes() : 0;
+  uint64_t bytes = ctx->sched ? ctx->sched->cached_bytes() : 0;
   ctx->sched.reset();
+  GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (auto &kv : ctx->pools)
+    for (auto &e : kv.second) {
+      bytes += e.second;
+      cudaFree(e.first);
+    }
+  ctx->pools.clear();
+  if (cached_bytes) *cached_bytes = bytes;
   API_END(ctx)
 }
 

@@ -196,6 +196,14 @@ __global__ void __launch_bounds__(256)
 cophase1_partial_kernel(const fe *e1, const fe *e2, const fe *e3, const fe *e4, const uint8_t *flags,
                         uint64_t nblocks, int logD, int blocks_per_cta, fe *partial) {
   __shared__ fe red[256];
+  // grid.z: the party; its blocks and partials follow the previous party's
+  const uint64_t pe = (uint64_t)blockIdx.z * (nblocks << logD);
+  e1 += pe;
+  e2 += pe;
+  if (e3) e3 += pe;
+  if (e4) e4 += pe;
+  if (flags) flags += (uint64_t)blockIdx.z * nblocks;
+  partial += (uint64_t)blockIdx.z * ((uint64_t)gridDim.x << logD);
   const int logDc = logD < 8 ? logD : 8;
   const uint32_t Dc = 1u << logDc, lane = threadIdx.x >> logDc, lanes = 256u >> logDc;
   const uint32_t k = blockIdx.y * Dc + (threadIdx.x & (Dc - 1));
@@ -217,12 +225,21 @@ cophase1_partial_kernel(const fe *e1, const fe *e2, const fe *e3, const fe *e4, 
   }
 }
 
+// H[z D + k] = sum_c partial[z][c][k]: one warp per coefficient k, its
+// lanes over the partials (grid.y: the party).
 __global__ void sum_partials_kernel(const fe *partial, uint64_t nparts, uint32_t D, fe *H) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t k = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (k >= D) return;
+  partial += (uint64_t)blockIdx.y * nparts * D;
   fe acc = fe_zero();
-  for (uint64_t c = 0; c < nparts; c++) acc = fadd(acc, partial[c * D + k]);
-  H[k] = acc;
+  for (uint64_t c = lane; c < nparts; c += 32) acc = fadd(acc, partial[c * D + k]);
+  for (int d = 16; d > 0; d >>= 1) {
+    fe t;
+    t.re = __shfl_down_sync(0xffffffffu, acc.re, d);
+    t.im = __shfl_down_sync(0xffffffffu, acc.im, d);
+    acc = fadd(acc, t);
+  }
+  if (lane == 0) H[(uint64_t)blockIdx.y * D + k] = acc;
 }
 
 // coSumcheck phase 2: out[j] = sum_k L[k] v[j d + k].
@@ -392,14 +409,16 @@ uint64_t cophase1_parts(uint64_t nblocks, int blocks_per_cta) {
 }
 
 void cophase1_reduce_launch(const fe *e1, const fe *e2, const fe *e3, const fe *e4, const uint8_t *flags,
-                            uint64_t nblocks, int logD, int blocks_per_cta, fe *partial, fe *H, cudaStream_t s) {
+                            uint64_t nblocks, int logD, int blocks_per_cta, fe *partial, fe *H, cudaStream_t s,
+                            int parties) {
   if (logD > kMaxCoLogD) throw ArgError("coSumcheck: extended block longer than 2^13");
+  if (parties < 1 || parties > 65535) throw ArgError("coSumcheck: 1..65535 parties per launch");
   const uint64_t parts = cophase1_parts(nblocks, blocks_per_cta);
   const unsigned chunks = logD > 8 ? 1u << (logD - 8) : 1u;
-  cophase1_partial_kernel<<<dim3((unsigned)parts, chunks), 256, 0, s>>>(e1, e2, e3, e4, flags, nblocks, logD,
-                                                                        blocks_per_cta, partial);
+  cophase1_partial_kernel<<<dim3((unsigned)parts, chunks, (unsigned)parties), 256, 0, s>>>(
+      e1, e2, e3, e4, flags, nblocks, logD, blocks_per_cta, partial);
   GBZ_CUDA(cudaGetLastError());
-  sum_partials_kernel<<<grid(1ull << logD), 256, 0, s>>>(partial, parts, 1u << logD, H);
+  sum_partials_kernel<<<dim3(grid(1ull << logD, 8), (unsigned)parties), 256, 0, s>>>(partial, parts, 1u << logD, H);
   GBZ_CUDA(cudaGetLastError());
 }
 

@@ -37,8 +37,12 @@ void aggregate_weights_launch(const fe *b, int N, fe *lambda, cudaStream_t s);
 constexpr int kMaxCoLogD = 13;
 void nonzero_blocks_launch(const fe *v, uint64_t nblocks, int logd, uint8_t *flags, cudaStream_t s);
 uint64_t cophase1_parts(uint64_t nblocks, int blocks_per_cta);
+// parties > 1: that many parties one after the other in every array (e*:
+// nblocks << logD entries each, flags: nblocks, partial:
+// cophase1_parts(nblocks, blocks_per_cta) << logD, H: 1 << logD).
 void cophase1_reduce_launch(const fe *e1, const fe *e2, const fe *e3, const fe *e4, const uint8_t *flags,
-                            uint64_t nblocks, int logD, int blocks_per_cta, fe *partial, fe *H, cudaStream_t s);
+                            uint64_t nblocks, int logD, int blocks_per_cta, fe *partial, fe *H, cudaStream_t s,
+                            int parties = 1);
 // coSumcheck phase 2 (coSumcheck.cpp:66-148, 201-213).
 void cophase2_launch(const fe *v, uint64_t n, const fe *L, int logd, fe *out, cudaStream_t s);
 

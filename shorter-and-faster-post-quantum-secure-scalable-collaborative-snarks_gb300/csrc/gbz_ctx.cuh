@@ -21,6 +21,10 @@ struct gbz_ctx {
   bool own_stream = false;
   std::string last_error;
   std::map<int, std::pair<void *, uint64_t>> scratch;
+  // Scratch of calls that make the same sequence of allocations for the
+  // same shape (the N-party openings): keyed by the shape, buffer k of a
+  // pool serves the call's k-th allocation.
+  std::map<std::string, std::vector<std::pair<void *, uint64_t>>> pools;
   std::map<int, NttTables> ntt;
   std::map<std::pair<int, int>, std::unique_ptr<ProofPlan>> plans;
   ProofState *st = nullptr;

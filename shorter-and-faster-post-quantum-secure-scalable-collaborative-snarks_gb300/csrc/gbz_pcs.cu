@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "gbz_copcs.cuh"
@@ -247,11 +248,12 @@ __global__ void k_indexes(PcsDev *st, int l, int N, uint32_t Mq, int32_t *qp, in
   __shared__ int32_t sp[kPcsMaxQueries], sq[kPcsMaxQueries];
   __shared__ int32_t start[kPcsMaxParties + 1];
   if (threadIdx.x == 0) {
+    // N and Mq are powers of two (checked by the host): % is a mask
     fe fs = st->fs;
     for (int i = 0; i < l; i++) {
       fs = hash_F(fs, fs);
-      sp[i] = (int32_t)(fs.re % (uint64_t)N);
-      sq[i] = (int32_t)(fs.im % (uint64_t)Mq);
+      sp[i] = (int32_t)(fs.re & (uint64_t)(N - 1));
+      sq[i] = (int32_t)(fs.im & (uint64_t)(Mq - 1));
     }
     st->fs = fs;
     for (int p = 0; p <= N; p++) start[p] = 0;
@@ -377,41 +379,43 @@ __global__ void k_s_update(PcsDev *st, const fe *y, int l, int addK, uint8_t *tr
 }
 
 // pcs_sumcheck_phase3 (coPCS.cpp:634-648) for every party: B_p[j] +=
-// sum_i s^{i+1} scale(a_i, p) (w^{q_i})^j, w = w_{rate rows}, q_i the query
-// position scaled as the reference scales it, scale(a, p) the tensor scale
-// of tensor_eval_vector (coPCS.cpp:610-632; a constant table).
+// sum_i s^{i+1} scale(a_i, p) (w^{q_i})^j, w = w_W, W = rate rows, q_i the
+// query position scaled as the reference scales it, scale(a, p) the tensor
+// scale of tensor_eval_vector (coPCS.cpp:610-632; a constant table).  For
+// j < rows that is the forward transform of length W of the sparse vector
+// V_p[q_i] += s^{i+1} scale(a_i, p): the prep writes q_i and the weights,
+// the scatter sums the weights of equal positions (the first query at a
+// position writes it), one batched transform over the N rows follows.
 __global__ void k_phase3_prep(const PcsDev *st, const int32_t *qp, const int32_t *qpos, int l, uint32_t mul,
-                              uint32_t div, int logw, const fe *scale, int N, fe *base, fe *w) {
+                              uint32_t div, int logw, const fe *scale, int N, uint32_t *q, fe *w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= l) return;
-  const uint64_t q = (uint64_t)mul * (uint32_t)qpos[i] / div;
-  base[i] = fpow(root_of_unity(logw), q & ((1ull << logw) - 1));
+  q[i] = (uint32_t)(((uint64_t)mul * (uint32_t)qpos[i] / div) & ((1ull << logw) - 1));
   const fe si = fpow(st->s, (uint64_t)i + 1);
   for (int p = 0; p < N; p++) w[(uint64_t)p * l + i] = fmul(si, scale[qp[i] * N + p]);
 }
 
-constexpr int kP3Chunk = 8;
-__global__ void k_phase3(fe *B, uint64_t rows, const fe *base, const fe *w, int l) {
-  const uint64_t j0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kP3Chunk;
-  if (j0 >= rows) return;
+// V (N x W, zero) gets V[p][q_i] = sum of w[p][j] over the queries j at q_i.
+__global__ void k_phase3_scatter(const uint32_t *q, const fe *w, int l, uint64_t W, fe *V) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= l) return;
   const uint64_t p = blockIdx.y;
+  const uint32_t qi = q[i];
+  for (int j = 0; j < i; j++)
+    if (q[j] == qi) return;
   const fe *wp = w + p * l;
-  fe acc[kP3Chunk];
-#pragma unroll
-  for (int c = 0; c < kP3Chunk; c++) acc[c] = fe_zero();
-  for (int i = 0; i < l; i++) {
-    const fe b = base[i];
-    fe x = fmul(wp[i], fpow(b, j0));
-#pragma unroll
-    for (int c = 0; c < kP3Chunk; c++) {
-      acc[c] = fadd(acc[c], x);
-      x = fmul(x, b);
-    }
-  }
-  fe *o = B + p * rows + j0;
-#pragma unroll
-  for (int c = 0; c < kP3Chunk; c++)
-    if (j0 + c < rows) o[c] = fadd(o[c], acc[c]);
+  fe acc = wp[i];
+  for (int j = i + 1; j < l; j++)
+    if (q[j] == qi) acc = fadd(acc, wp[j]);
+  V[p * W + qi] = acc;
+}
+
+// B[p][j] += T[p][j] for j < rows (T: N rows of W entries).
+__global__ void k_phase3_add(fe *B, uint64_t rows, const fe *T, uint64_t W) {
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= rows) return;
+  const uint64_t p = blockIdx.y;
+  B[p * rows + j] = fadd(B[p * rows + j], T[p * W + j]);
 }
 
 // The RS fold of a codeword by d (RS_multifold5, coPCS_utils.cpp:386-437, and
@@ -875,16 +879,35 @@ struct gbz_pcs {
 
 namespace {
 
-// Device buffers of one opening (allocated per call, freed at its end).
+// Device buffers of one call: allocated per call and freed at its end, or,
+// with a pool, the pool's k-th buffer for the call's k-th allocation (a
+// larger or new one replaces it when it is too small).
 struct OpenBufs {
   std::vector<void *> owned;
+  std::vector<std::pair<void *, uint64_t>> *pool = nullptr;
+  size_t next = 0;
   ~OpenBufs() {
     for (void *p : owned) cudaFree(p);
   }
   template <typename T>
   T *alloc(uint64_t count) {
+    const uint64_t bytes = std::max<uint64_t>(count * sizeof(T), 16);
+    if (pool) {
+      auto &P = *pool;
+      if (next < P.size() && P[next].second >= bytes) return (T *)P[next++].first;
+      void *p = nullptr;
+      GBZ_CUDA(cudaMalloc(&p, bytes));
+      if (next < P.size()) {
+        cudaFree(P[next].first);
+        P[next] = {p, bytes};
+      } else {
+        P.push_back({p, bytes});
+      }
+      next++;
+      return (T *)p;
+    }
     void *p = nullptr;
-    GBZ_CUDA(cudaMalloc(&p, std::max<uint64_t>(count * sizeof(T), 16)));
+    GBZ_CUDA(cudaMalloc(&p, bytes));
     owned.push_back(p);
     return (T *)p;
   }
@@ -976,13 +999,14 @@ LeaderInputs leader_shape(const gbz_pcs &pc) {
 }
 
 // The records of the leader's tail after the parties' records (lay.bytes is
-// where they start).
-void tail_layout(const gbz_pcs &pc, PcsLayout &lay) {
+// where they start), and its draws (script, arena_len: may be null).
+void tail_layout(const gbz_pcs &pc, PcsLayout &lay, std::vector<DrawOp> *script = nullptr,
+                 uint64_t *arena_len = nullptr) {
   LeaderInputs in = leader_shape(pc);
   Layout tl;
   tl.record_headers = true;
   LeaderResources R;
-  leader_tail(R, in, nullptr, nullptr, nullptr, tl);
+  leader_tail(R, in, nullptr, nullptr, nullptr, tl, script, arena_len, nullptr);
   const uint64_t base = lay.bytes;
   for (const auto &h : tl.headers) lay.hdr.push_back({base + h.off, h.tag, h.count});
   lay.bytes = base + tl.len;
@@ -1134,6 +1158,8 @@ gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, in
   }
   std::vector<fe> lambda = aggregate_weights(N, b2.data());
   OpenBufs ob;
+  ob.pool = &ctx->pools["pcs_claim:" + std::to_string(N) + ":" + std::to_string(pcs->sc.M) + ":" +
+                        std::to_string(pcs->Bs) + ":" + std::to_string(nb)];
   fe *dr = ob.alloc<fe>(nr), *dl = ob.alloc<fe>(N), *b1 = ob.alloc<fe>(32ull * pcs->Bs), *dK = ob.alloc<fe>(1);
   GBZ_CUDA(cudaMemcpyAsync(dr, hr.data(), 16ull * nr, cudaMemcpyHostToDevice, s));
   GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
@@ -1170,18 +1196,52 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
   const OpenOffs off = open_layout(*pcs, lay);
   const uint64_t tail_base = lay.bytes;
   LeaderInputs lead = leader_shape(*pcs);
-  if (full) tail_layout(*pcs, lay);
+  std::vector<DrawOp> script;
+  uint64_t arena_len = 0;
+  if (full) tail_layout(*pcs, lay, &script, &arena_len);
   if (capacity < lay.bytes)
     throw ArgError(full ? "pcs: transcript capacity below gbz_pcs_open_full_bytes"
                         : "pcs: transcript capacity below gbz_pcs_info's open_transcript_bytes");
   cudaStream_t s = ctx->stream;
+  // an opening makes the same allocations for the same shape: the
+  // context's pool for this shape serves them after the first
   OpenBufs ob;
+  {
+    std::string key = "pcs_open" + std::to_string((int)full) + ":" + std::to_string(mem) + ":" + std::to_string(N) +
+                      ":" + std::to_string(pcs->sc.M) + ":" + std::to_string(sc.rounds);
+    for (int i = 0; i < sc.rounds; i++) key += ":" + std::to_string(sc.rate0[i]) + "/" + std::to_string(sc.rate1[i]);
+    ob.pool = &ctx->pools[key];
+  }
   uint8_t *tr = mem == GBZ_MEM_DEVICE ? transcript : ob.alloc<uint8_t>(lay.bytes);
   // headers
   Hdr *dh = ob.alloc<Hdr>(lay.hdr.size());
   GBZ_CUDA(cudaMemcpyAsync(dh, lay.hdr.data(), sizeof(Hdr) * lay.hdr.size(), cudaMemcpyHostToDevice, s));
   k_headers<<<grid(lay.hdr.size()), 256, 0, s>>>(dh, (int)lay.hdr.size(), tr);
   GBZ_CUDA(cudaGetLastError());
+  // The leader's draws depend on the generator alone: the script draws them
+  // on the side stream while the parties' rounds run.
+  ProofState *pst = nullptr;
+  uint32_t *dfl = nullptr;
+  LeaderDraws ldraws;
+  const SideStream *side = nullptr;
+  if (full) {
+    glibc_prng g0;
+    static_assert(sizeof(glibc_prng) == sizeof(gbz_prng), "generator layouts");
+    std::memcpy(&g0, prng, sizeof g0);
+    pst = ob.alloc<ProofState>(1);
+    dfl = ob.alloc<uint32_t>(1);
+    ldraws.arena = ob.alloc<fe>(std::max<uint64_t>(arena_len, 1));
+    ldraws.after_walk = ob.alloc<glibc_prng>(1);
+    ldraws.final_state = ob.alloc<glibc_prng>(1);
+    DrawOp *dops = ob.alloc<DrawOp>(script.size());
+    GBZ_CUDA(cudaMemcpyAsync(dops, script.data(), sizeof(DrawOp) * script.size(), cudaMemcpyHostToDevice, s));
+    leader_tail_init(pst, g0, dfl, s);
+    side = &ctx->side_stream();
+    GBZ_CUDA(cudaEventRecord(side->fork, s));
+    GBZ_CUDA(cudaStreamWaitEvent(side->stream, side->fork, 0));
+    leader_draws_launch(g0, dops, (int)script.size(), ldraws, tr + tail_base, pst, side->stream);
+    GBZ_CUDA(cudaEventRecord(side->join, side->stream));
+  }
   // point and constants
   std::vector<fe> hr(nr);
   for (int i = 0; i < nr; i++) {
@@ -1274,12 +1334,14 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     batch_depth = ilog2(c);
   }
   int32_t *qp = ob.alloc<int32_t>(kPcsMaxQueries), *qpos = ob.alloc<int32_t>(kPcsMaxQueries);
+  if (!is_pow2(L) || L > 0xFFFFFFFFull) throw ArgError("pcs: codeword length must be a power of two below 2^32");
   k_indexes<<<1, 256, 0, s>>>(st, sc.queries[0], N, (uint32_t)L, qp, qpos, tr, off.bqueries);
   GBZ_CUDA(cudaGetLastError());
 
   // the rounds (coPCS.cpp:1452-1600)
   fe *Ld = ob.alloc<fe>(1 << kPcsMaxLogDeg), *vscr = ob.alloc<fe>(4 << kPcsMaxLogDeg), *y = ob.alloc<fe>(kPcsMaxQueries);
-  fe *base = ob.alloc<fe>(kPcsMaxQueries), *wts = ob.alloc<fe>((uint64_t)N * kPcsMaxQueries);
+  uint32_t *q3 = ob.alloc<uint32_t>(kPcsMaxQueries);
+  fe *wts = ob.alloc<fe>((uint64_t)N * kPcsMaxQueries);
   uint64_t n = Bs, cpl = L;
   int prev_depth = batch_depth;
   // every party's RS fold of a codeword of length len by 2^logd with the
@@ -1309,10 +1371,8 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     const uint64_t pblocks = n / d;
     const int lanes = D >= 256 ? 1 : 256 / D;
     const int per_cta = (int)std::max<uint64_t>((uint64_t)lanes, (pblocks + 607) / 608);
-    fe *cpart = ob.alloc<fe>((uint64_t)D * cophase1_parts(pblocks, per_cta));
-    for (int p = 0; p < N; p++)
-      cophase1_reduce_launch(e1 + (uint64_t)p * pblocks * D, e2 + (uint64_t)p * pblocks * D, nullptr, nullptr, nullptr,
-                             pblocks, logd + 1, per_cta, cpart, H + (uint64_t)p * D, s);
+    fe *cpart = ob.alloc<fe>((uint64_t)N * D * cophase1_parts(pblocks, per_cta));
+    cophase1_reduce_launch(e1, e2, nullptr, nullptr, nullptr, pblocks, logd + 1, per_cta, cpart, H, s, N);
     k_put_party<<<dim3(grid(D), N), 256, 0, s>>>(H, D, N, tr, ro.pp, 16ull * D);
     aggregate_launch(H, N, D, dlam, poly, s);
     k_round_verify<<<1, 256, 0, s>>>(st, poly, logd, Ld, vscr, tr, ro.poly, ro.chal);
@@ -1371,6 +1431,7 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     }
     // delegate_checks (coPCS.cpp:740-891)
     const int l = sc.queries[i + 1];
+    if (!is_pow2(seg_n)) throw ArgError("pcs: segment count must be a power of two");
     k_indexes<<<1, 256, 0, s>>>(st, l, N, (uint32_t)seg_n, qp, qpos, tr, ro.queries);
     LeaderRound &lr = lead.rounds[i];
     lr.d = d;
@@ -1414,9 +1475,17 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     if (!last) {
       // pcs_sumcheck_phase3 (coPCS.cpp:634-648) with the scaled queries
       const int logw = ilog2((uint64_t)sc.rate0[i + 2] * n);
+      const uint64_t W = 1ull << logw;
+      if (logw > kMaxNttLogN) throw ArgError("pcs: phase-3 transform longer than 2^26");
+      fe *V = ob.alloc<fe>((uint64_t)N * W), *T = ob.alloc<fe>((uint64_t)N * W);
+      fe *tmp3 = logw > 13 ? ob.alloc<fe>((uint64_t)N * W) : nullptr;
+      GBZ_CUDA(cudaMemsetAsync(V, 0, 16ull * N * W, s));
       k_phase3_prep<<<grid(l), 256, 0, s>>>(st, qp, qpos, l, (uint32_t)sc.rate0[i + 2], (uint32_t)sc.rate0[i + 1],
-                                             logw, dscale, N, base, wts);
-      k_phase3<<<dim3(grid((n + kP3Chunk - 1) / kP3Chunk), N), 256, 0, s>>>(B, n, base, wts, l);
+                                             logw, dscale, N, q3, wts);
+      k_phase3_scatter<<<dim3(grid(l), N), 256, 0, s>>>(q3, wts, l, W, V);
+      GBZ_CUDA(cudaGetLastError());
+      ntt_launch_rows(ctx->tables(logw), V, W, W, T, W, N, tmp3, false, s);
+      k_phase3_add<<<dim3(grid(n), N), 256, 0, s>>>(B, n, T, W);
       GBZ_CUDA(cudaGetLastError());
     }
     Cp = Cpn;
@@ -1431,8 +1500,6 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     GBZ_CUDA(cudaGetLastError());
   }
   // the leader's delegation proofs, final checks and WHIR opening
-  ProofState *pst = nullptr;
-  uint32_t *dfl = nullptr;
   if (full) {
     lead.bcd = bcd;
     lead.B = B;
@@ -1454,18 +1521,15 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     fe *dU = ob.alloc<fe>(U.size());
     GBZ_CUDA(cudaMemcpyAsync(dU, U.data(), 16 * U.size(), cudaMemcpyHostToDevice, s));
     lead.unpack = dU;
-    pst = ob.alloc<ProofState>(1);
-    dfl = ob.alloc<uint32_t>(1);
-    glibc_prng g0;
-    static_assert(sizeof(glibc_prng) == sizeof(gbz_prng), "generator layouts");
-    std::memcpy(&g0, prng, sizeof g0);
-    leader_tail_init(pst, g0, dfl, s);
+    GBZ_CUDA(cudaStreamWaitEvent(s, side->join, 0));
     LeaderResources LR;
     LR.s = s;
     LR.alloc = [&ob](uint64_t bytes) -> void * { return ob.alloc<uint8_t>(bytes); };
     LR.tables = [ctx](int lg) -> NttTables & { return ctx->tables(lg); };
     Layout tl;
-    leader_tail(LR, lead, pst, dfl, tr + tail_base, tl);
+    uint64_t used = 0;
+    leader_tail(LR, lead, pst, dfl, tr + tail_base, tl, nullptr, &used, &ldraws);
+    if (used != arena_len) throw ArgError("pcs: leader draw count mismatch");
     if (tail_base + tl.len != lay.bytes) throw ArgError("pcs: leader transcript layout mismatch");
   }
   // the chain state out, the flags checked
@@ -1475,7 +1539,7 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
   GBZ_CUDA(cudaMemcpyAsync(&hst, st, sizeof(PcsDev), cudaMemcpyDeviceToHost, s));
   if (full) {
     GBZ_CUDA(cudaMemcpyAsync(&hfl, dfl, 4, cudaMemcpyDeviceToHost, s));
-    GBZ_CUDA(cudaMemcpyAsync(&hg, &pst->prng, sizeof hg, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaMemcpyAsync(&hg, ldraws.final_state, sizeof hg, cudaMemcpyDeviceToHost, s));
   }
   if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaMemcpyAsync(transcript, tr, lay.bytes, cudaMemcpyDeviceToHost, s));
   GBZ_CUDA(cudaStreamSynchronize(s));
@@ -1574,6 +1638,12 @@ gbz_status gbz_cosumcheck(gbz_ctx *ctx, int form, int N, uint64_t n, const uint6
   if (transcript && capacity < lay.bytes) throw ArgError("coSumcheck: transcript capacity too small");
   cudaStream_t s = ctx->stream;
   OpenBufs ob;
+  {
+    std::string key = "cosumcheck:" + std::to_string(form) + ":" + std::to_string(N) + ":" + std::to_string(n) + ":" +
+                      std::to_string(mem) + ":" + std::to_string(transcript != nullptr);
+    for (int i = 0; i < ndeg; i++) key += ":" + std::to_string(degrees[i]);
+    ob.pool = &ctx->pools[key];
+  }
   // party-major inputs, copied: the call folds them in place as the reference does
   const uint64_t Rst = ro.off[ndeg];
   fe *v1 = ob.alloc<fe>((uint64_t)N * n), *v2 = ob.alloc<fe>((uint64_t)N * n), *v3 = nullptr, *vb = nullptr;
@@ -1675,13 +1745,8 @@ gbz_status gbz_cosumcheck(gbz_ctx *ctx, int form, int N, uint64_t n, const uint6
     }
     const int lanes = D >= 256 ? 1 : 256 / D;
     const int per_cta = (int)std::max<uint64_t>((uint64_t)lanes, (pblocks + 607) / 608);
-    fe *cpart = ob.alloc<fe>((uint64_t)D * cophase1_parts(pblocks, per_cta));
-    for (int p = 0; p < N; p++) {
-      const uint64_t o = (uint64_t)p * pblocks;
-      cophase1_reduce_launch(ex[0] + o * D, ex[1] + o * D, ex[2] ? ex[2] + o * D : nullptr,
-                             ex[3] ? ex[3] + o * D : nullptr, zf ? zf + o : nullptr, pblocks, logd[i] + ext, per_cta,
-                             cpart, H + (uint64_t)p * D, s);
-    }
+    fe *cpart = ob.alloc<fe>((uint64_t)N * D * cophase1_parts(pblocks, per_cta));
+    cophase1_reduce_launch(ex[0], ex[1], ex[2], ex[3], zf, pblocks, logd[i] + ext, per_cta, cpart, H, s, N);
     k_cosc_add_hr<<<N, 256, 0, s>>>(H, D, dR, Rst, ro, i, step, st);
     k_put_party<<<dim3(grid(D), N), 256, 0, s>>>(H, D, N, tr, off_pp[i], 16ull * D);
     aggregate_launch(H, N, D, dl, poly, s);

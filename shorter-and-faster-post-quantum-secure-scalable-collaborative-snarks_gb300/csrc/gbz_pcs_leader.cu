@@ -71,27 +71,39 @@ __device__ fe block_sum_fe(fe v) {
 }
 
 // ---- the generator ---------------------------------------------------------
-// count F::_random() draws (fieldElement.cpp:119-125) into out, in order.
-__global__ void k_draw_fields(ProofState *st, int count, fe *out) {
+// The tail's draws in the reference's order, one thread: F::_random()
+// (fieldElement.cpp:119-125) into the arena, rand() % mod (coPCS.cpp:789,
+// Whir.cpp:574-576) into the transcript, the state the WHIR opening starts
+// from into st->prng, the calls the opening makes itself skipped (their
+// end state into after_walk), and the final state.
+__global__ void k_draw_script(glibc_prng g0, const DrawOp *ops, int nops, fe *arena, uint8_t *tr, ProofState *st,
+                              glibc_prng *after_walk, glibc_prng *final_state) {
   __shared__ glibc_prng g;  // dynamically indexed table: work on a shared copy
   if (threadIdx.x) return;
-  g = st->prng;
-  for (int i = 0; i < count; i++) out[i] = prng_field(g);
-  st->prng = g;
+  g = g0;
+  for (int k = 0; k < nops; k++) {
+    const DrawOp o = ops[k];
+    if (o.kind == DRAW_FIELDS) {
+      for (int i = 0; i < o.count; i++) arena[o.off + i] = prng_field(g);
+    } else if (o.kind == DRAW_INTS) {
+      uint32_t *q = reinterpret_cast<uint32_t *>(tr + o.off);
+      for (int i = 0; i < o.count; i++) q[i] = (uint32_t)(prng_next(g) % (int32_t)o.mod);
+    } else if (o.kind == DRAW_STATE) {
+      st->prng = g;
+    } else {
+      for (int i = 0; i < o.count; i++) (void)prng_next(g);
+      *after_walk = g;
+    }
+  }
+  *final_state = g;
 }
 
-// count rand() % mod draws (coPCS.cpp:789) into out and the transcript.
-__global__ void k_draw_mod(ProofState *st, int count, uint32_t mod, int32_t *out, uint8_t *tr, uint64_t off) {
-  __shared__ glibc_prng g;
+// The WHIR opening drew as many values as the script skipped for it.
+__global__ void k_prng_check(const ProofState *st, const glibc_prng *expect, uint32_t *flags) {
   if (threadIdx.x) return;
-  g = st->prng;
-  uint32_t *q = reinterpret_cast<uint32_t *>(tr + off);
-  for (int i = 0; i < count; i++) {
-    const int32_t v = prng_next(g) % (int32_t)mod;
-    out[i] = v;
-    q[i] = (uint32_t)v;
-  }
-  st->prng = g;
+  bool same = st->prng.f == expect->f && st->prng.r == expect->r;
+  for (int i = 0; i < 31; i++) same = same && st->prng.tbl[i] == expect->tbl[i];
+  if (!same) atomicOr(flags, LF_WHIR);
 }
 
 __global__ void k_tail_init(ProofState *st, glibc_prng g, uint32_t *flags) {
@@ -132,15 +144,6 @@ __global__ void k_sc_finish(const fe *partial, int blocks, int nc, fe *y, const 
   fe v = red[0][0];
   for (int k = 1; k < nc; k++) v = fadd(fmul(v, c), red[k][0]);
   *y = v;
-}
-
-// The vectors' final values (v[0] after the last fold).
-__global__ void k_sc_fin(RoundArgs a, int nv, fe *fin, uint8_t *tr, uint64_t off) {
-  const int k = threadIdx.x;
-  if (k >= nv) return;
-  const fe v = a.out[k][0];
-  fin[k] = v;
-  put_fe(tr, off + 16ull * k, v);
 }
 
 __global__ void k_set(fe *dst, const fe *src) {
@@ -236,13 +239,13 @@ __global__ void k_pmf_checks(const fe *fin, const fe *ch, int logd, int logS, co
   if (bad) atomicOr(flags, LF_DELEGATION);
 }
 
-// out[j] = sum_{t < l} w[t] seg[t d + j] for j < d (out holds at least d entries).
+// out[j] = sum_{t < l} w[t] seg[t d + j] for j < d (one CTA per j).
 __global__ void k_seg_comb(const fe *seg, const fe *w, int l, int d, fe *out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= d) return;
+  const int j = blockIdx.x;
   fe acc = fe_zero();
-  for (int t = 0; t < l; t++) acc = fadd(acc, fmul(w[t], seg[(uint64_t)t * d + j]));
-  out[j] = acc;
+  for (int t = threadIdx.x; t < l; t += kT) acc = fadd(acc, fmul(w[t], seg[(uint64_t)t * d + j]));
+  acc = block_sum_fe(acc);
+  if (threadIdx.x == 0) out[j] = acc;
 }
 
 // get_RS_multifold_reduced_matrix (coPCS_utils.cpp:235-266) over d entries:
@@ -494,59 +497,74 @@ struct FinalArgs {
   uint64_t off_rc;
 };
 
-// r_c's claims and the final verification step (coPCS.cpp:1711-1752):
-// B_eval_claim = sum_i r_c^i final_B[i]; the partial evaluations
-// r_first b2[0] b3(r_c) + sum over the queries of the rounds before the last
-// of s^(j+1) fast_eval_powers_x fast_eval_powers_y (New_PCS.cpp:582-634).
-__global__ void k_final_eval(FinalArgs a, uint32_t *flags, uint8_t *tr) {
-  __shared__ fe py[64];
-  const fe rc = *a.rc;
-  // fast_eval_powers_y per party: IDFT_{N/2} of the powers of omega_{2N}^(2p+1), at r_c
-  const int h = a.N / 2, lh = ilog2_dev((uint64_t)h);
-  if ((int)threadIdx.x < a.N) {
-    const int p = threadIdx.x;
-    const fe w1 = fpow(root_of_unity(1 + ilog2_dev((uint64_t)a.N)), 2ull * p + 1);
-    const fe winv = finv(root_of_unity(lh)), hinv = finv(fe_make((uint64_t)h, 0));
-    fe acc = fe_zero(), rk = fe_one();
-    for (int k = 0; k < h; k++) {
-      fe c = fe_zero();
-      const fe wk = fpow(winv, (uint64_t)k);
-      fe x = fe_one(), wi = fe_one();
-      for (int i = 0; i < h; i++) {
-        c = fadd(c, fmul(x, wi));
-        x = fmul(x, w1);
-        wi = fmul(wi, wk);
-      }
-      acc = fadd(acc, fmul(rk, fmul(c, hinv)));
-      rk = fmul(rk, rc);
+// fast_eval_powers_y (New_PCS.cpp:582-605) per party p < N, at r_c: the
+// inverse transform of length N/2 of the powers of omega_{2N}^(2p+1),
+// evaluated as a polynomial in r_c.
+__global__ void k_powers_y(int N, const fe *rcp, fe *py) {
+  const int p = threadIdx.x;
+  if (p >= N) return;
+  const fe rc = *rcp;
+  const int h = N / 2, lh = ilog2_dev((uint64_t)h);
+  const fe w1 = fpow(root_of_unity(1 + ilog2_dev((uint64_t)N)), 2ull * p + 1);
+  const fe winv = finv(root_of_unity(lh)), hinv = finv(fe_make((uint64_t)h, 0));
+  fe acc = fe_zero(), rk = fe_one();
+  for (int k = 0; k < h; k++) {
+    fe c = fe_zero();
+    const fe wk = fpow(winv, (uint64_t)k);
+    fe x = fe_one(), wi = fe_one();
+    for (int i = 0; i < h; i++) {
+      c = fadd(c, fmul(x, wi));
+      x = fmul(x, w1);
+      wi = fmul(wi, wk);
     }
-    py[p] = acc;
+    acc = fadd(acc, fmul(rk, fmul(c, hinv)));
+    rk = fmul(rk, rc);
   }
-  __syncthreads();
+  py[p] = acc;
+}
+
+// The partial evaluations of the queries of the rounds before the last
+// (coPCS.cpp:1733-1746): for query t of round r, s^(t+1)
+// fast_eval_powers_x(L_{r+1..}, position, rows, rate) (New_PCS.cpp:610-634)
+// times fast_eval_powers_y of its party.  One warp per query, its lanes over
+// the Lagrange weights; terms[g] for the g-th query over all rounds.
+__global__ void k_final_terms(FinalArgs a, const fe *py, fe *terms) {
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  int r = 0, t = g;
+  while (r < a.nq && t >= a.q[r].l) t -= a.q[r++].l;
+  if (r >= a.nq) return;
+  const FinalRound &q = a.q[r];
+  const uint64_t pos = (uint64_t)(uint32_t)q.qpos[t] * (uint64_t)q.mul / (uint64_t)q.div;
+  fe om = fpow(root_of_unity(ilog2_dev((uint64_t)q.rate * q.rows)), pos), fx = fe_one();
+  for (int k = 0; k < q.nL; k++) {
+    if (k) om = fpow(om, (uint64_t)q.d[k - 1]);
+    fe sum = fe_zero(), x = fpow(om, (uint64_t)lane);
+    const fe step = fpow(om, 32);
+    for (int j = lane; j < q.d[k]; j += 32) {
+      sum = fadd(sum, fmul(q.L[k][j], x));
+      x = fmul(x, step);
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+      fe u;
+      u.re = __shfl_xor_sync(0xffffffffu, sum.re, d);
+      u.im = __shfl_xor_sync(0xffffffffu, sum.im, d);
+      sum = fadd(sum, u);
+    }
+    fx = fmul(fx, sum);
+  }
+  if (lane == 0) terms[g] = fmul(fmul(fpow(*q.s, (uint64_t)t + 1), fx), py[(uint32_t)q.qp[t]]);
+}
+
+// B_eval_claim = sum_i r_c^i final_B[i], b3(r_c), and the check
+// r_first b2[0] b3(r_c) + sum of the terms = B_eval_claim ("final
+// verification step", coPCS.cpp:1711-1752).
+__global__ void k_final_eval(FinalArgs a, const fe *terms, int nterms, uint32_t *flags, uint8_t *tr) {
   fe acc = fe_zero();
-  for (int r = 0; r < a.nq; r++) {
-    const FinalRound &q = a.q[r];
-    for (int t = threadIdx.x; t < q.l; t += kT) {
-      const uint64_t pos = (uint64_t)(uint32_t)q.qpos[t] * (uint64_t)q.mul / (uint64_t)q.div;
-      fe om = fpow(root_of_unity(ilog2_dev((uint64_t)q.rate * q.rows)), pos), fx = fe_one();
-      for (int k = 0; k < q.nL; k++) {
-        if (k) {
-          fe t2 = om;
-          om = fpow(t2, (uint64_t)q.d[k - 1]);
-        }
-        fe s = fe_zero(), x = fe_one();
-        for (int j = 0; j < q.d[k]; j++) {
-          s = fadd(s, fmul(q.L[k][j], x));
-          x = fmul(x, om);
-        }
-        fx = fmul(fx, s);
-      }
-      const fe p = fpow(*q.s, (uint64_t)t + 1);
-      acc = fadd(acc, fmul(fmul(p, fx), py[(uint32_t)q.qp[t]]));
-    }
-  }
+  for (int g = threadIdx.x; g < nterms; g += kT) acc = fadd(acc, terms[g]);
   acc = block_sum_fe(acc);
   if (threadIdx.x) return;
+  const fe rc = *a.rc;
+  const int h = a.N / 2;
   fe be = fe_zero(), rk = fe_one();
   for (int i = 0; i < h; i++) {
     be = fadd(be, fmul(rk, a.fB[i]));
@@ -641,6 +659,10 @@ struct Tail {
   Layout &lay;
   bool dry;
   cudaStream_t s;
+  std::vector<DrawOp> *script;  // the dry pass records the draws here
+  const glibc_prng *after_walk; // the script's state after the WHIR opening's calls
+  fe *arena;                    // the run reads them from here
+  uint64_t arena_used;
   std::map<int, void *> slots;
 
   template <typename T>
@@ -677,7 +699,10 @@ struct Tail {
     form_step_launch(form, a, 0, round_blocks(a.pairs), s);
     k_sc_finish<<<1, kT, 0, s>>>(partial, round_blocks(a.pairs), nc, y, draw + first, ch, 0, flags, bit, tr, op);
     check();
-    for (int i = 1; i < rounds; i++) {
+    // rounds with at most 2^14 entries entering them, and the final fold,
+    // in one CTA (form_tail_drawn_kernel)
+    const int i0 = std::max(1, rounds - 13);
+    for (int i = 1; i < i0; i++) {
       RoundArgs b{};
       for (int k = 0; k < nv; k++) {
         b.in[k] = i == 1 ? v[k] : buf[(i - 2) & 1][k];
@@ -691,22 +716,40 @@ struct Tail {
                                    flags, bit, tr, op);
       check();
     }
-    RoundArgs c{};
+    DrawnTailArgs t{};
     for (int k = 0; k < nv; k++) {
-      c.in[k] = rounds == 1 ? v[k] : buf[(rounds - 2) & 1][k];
-      c.out[k] = buf[(rounds - 1) & 1][k];
+      t.in[k] = i0 == 1 ? v[k] : buf[(i0 - 2) & 1][k];
+      t.buf[0][k] = buf[(i0 - 1) & 1][k];
+      t.buf[1][k] = buf[i0 & 1][k];
     }
-    c.pairs = 1;
-    c.r = ch + (rounds - 1);
-    form_step_launch(form, c, 2, 1, s);
-    k_sc_fin<<<1, 32, 0, s>>>(c, nv, fin, tr, of);
-    check();
+    t.n = n;
+    t.i0 = i0;
+    t.rounds = rounds;
+    t.draw = draw;
+    t.first = first;
+    t.stride = stride;
+    t.ch = ch;
+    t.y = y;
+    t.fin = fin;
+    t.flags = flags;
+    t.bit = bit;
+    t.tr = tr;
+    t.off_polys = op;
+    t.off_fin = of;
+    form_tail_drawn_launch(form, t, s);
   }
 
-  void draw_fields(int count, fe *out) {
-    if (dry) return;
-    k_draw_fields<<<1, 32, 0, s>>>(st, count, out);
-    check();
+  // count F::_random() values, drawn ahead by the script
+  fe *draws(int count) {
+    if (script) script->push_back({DRAW_FIELDS, count, 0u, arena_used});
+    fe *p = dry ? nullptr : arena + arena_used;
+    arena_used += (uint64_t)count;
+    return p;
+  }
+  // count rand() % mod values, drawn by the script into the transcript at off
+  const int32_t *draw_mod(int count, uint32_t mod, uint64_t off) {
+    if (script) script->push_back({DRAW_INTS, count, mod, off});
+    return dry ? nullptr : reinterpret_cast<const int32_t *>(tr + off);
   }
 
   // The randomness the leader's delegation draws in one round:
@@ -745,16 +788,11 @@ struct Tail {
     }
     // queries2[i] = rand() % C[0].size() (coPCS.cpp:789)
     const uint64_t off_q2 = lay.rec(T_D_QUERIES, (uint32_t)l, 4);
-    int32_t *q2 = alloc<int32_t>(l);
-    if (!dry) {
-      k_draw_mod<<<1, 32, 0, s>>>(st, l, (uint32_t)C0, q2, tr, off_q2);
-      check();
-    }
+    const int32_t *q2 = draw_mod(l, (uint32_t)C0, off_q2);
     // ---- prove_multi_folding
     const int R4 = logS + logd;
     const int nd_pmf = logS + 1 + 5 * R4 + 3 * logd;
-    fe *D = alloc<fe>(nd_pmf);
-    draw_fields(nd_pmf, D);
+    const fe *D = draws(nd_pmf);
     fe *b1 = alloc<fe>(S), *twd = alloc<fe>(d), *y = alloc<fe>(1);
     fe *V[4];
     for (int k = 0; k < 4; k++) V[k] = alloc<fe>(S * d);
@@ -783,7 +821,7 @@ struct Tail {
     // the second sumcheck: sum_t b12[t] segment_t against the reduced matrix at r11
     fe *U1 = alloc<fe>(d), *U2 = alloc<fe>(d), *chq = alloc<fe>(logd), *finq = alloc<fe>(2);
     if (!dry) {
-      k_seg_comb<<<nblk(d), kT, 0, s>>>(rd.seg, b12, l, d, U1);
+      k_seg_comb<<<d, kT, 0, s>>>(rd.seg, b12, l, d, U1);
       k_reduced_matrix<<<nblk(d), kT, 0, s>>>(ch4, logd, d, twd, U2);
       k_set<<<1, 32, 0, s>>>(y, fin4);
       check();
@@ -810,8 +848,7 @@ struct Tail {
     const uint64_t off_o = lay.rec(T_D_OPEN, (uint32_t)l, 16);
     const int R3 = logS + logC0;
     const int nd_pe = logS + 4 * R3 + 1 + 3 * logC0;
-    fe *De = alloc<fe>(nd_pe);
-    draw_fields(nd_pe, De);
+    const fe *De = draws(nd_pe);
     fe *E = zeros(S * C0), *W2 = alloc<fe>(S * C0), *W3 = alloc<fe>(S * C0), *o = alloc<fe>(l), *bb = alloc<fe>(S);
     if (!dry) {
       ntt_batched(R.tables(logC0), rd.seg, (uint64_t)d, (uint32_t)d, E, (uint64_t)l, false, s);
@@ -832,7 +869,7 @@ struct Tail {
       beta_launch(ch3 + logC0, logS, b2e, s);
       k_pe_checks<<<1, kT, 0, s>>>(fin3, b1e, b2e, q2, l, ch3 + logC0, De, logS, flags);
       // prove_fft (delegate_protocol.cpp:119-145) of sum_t b2[t] segment_t at r1
-      k_seg_comb<<<nblk(d), kT, 0, s>>>(rd.seg, b2e, l, d, v);
+      k_seg_comb<<<d, kT, 0, s>>>(rd.seg, b2e, l, d, v);
       const NttTables &tc = R.tables(logC0);
       k_phi<<<nblk(C0), kT, 0, s>>>(ch3, logC0, logC0, tc.lo_fwd, tc.hi_fwd, Wp);
       k_set<<<1, 32, 0, s>>>(y, fin3);
@@ -879,7 +916,7 @@ struct Tail {
     }
     // aggregate_claims (Whir.cpp:608-668)
     const uint64_t off_ch = lay.rec(T_AGGR_CHALLENGES, (uint32_t)(2 * nR), 16), off_K = lay.rec(T_AGGR_K, 1, 16);
-    fe *betas[8] = {}, *ch = alloc<fe>(2 * nR), *sums = alloc<fe>((uint64_t)nR * nR);
+    fe *betas[8] = {}, *sums = alloc<fe>((uint64_t)nR * nR);
     fe *arr = alloc<fe>(md), *baggr = alloc<fe>(md), *cw = alloc<fe>(Lw);
     for (int c = 0; c < nR; c++) betas[c] = alloc<fe>(md);
     if (!dry) {
@@ -892,7 +929,7 @@ struct Tail {
       fe *mdp = alloc<fe>(multidot_scratch(md));
       multidot_launch(va, nR, vb, nR, md, mdp, sums, s);
     }
-    draw_fields(2 * nR, ch);
+    const fe *ch = draws(2 * nR);
     if (!dry) {
       k_aggr_K<<<1, 32, 0, s>>>(sums, ch, nR, st, tr, off_ch, off_K);
       check();
@@ -912,9 +949,8 @@ struct Tail {
     const uint64_t off_aq = lay.rec(T_AGGR_QUERIES, (uint32_t)la, 4);
     const uint64_t off_ap = lay.rec(T_AGGR_PATHS, (uint32_t)(la * depth_a), 32);
     const uint64_t off_ar = lay.rec(T_AGGR_ROOT, 1, 32);
+    draw_mod(la, (uint32_t)(Lw / 4), off_aq);
     if (!dry) {
-      int32_t *aq = alloc<int32_t>(la);
-      k_draw_mod<<<1, 32, 0, s>>>(st, la, (uint32_t)(Lw / 4), aq, tr, off_aq);
       k_whir_paths_chain<<<nblk((uint64_t)la * depth_a, 128), 128, 0, s>>>(ro[0].W, Lw / 4, la, tr, off_aq, off_ap);
       k_zero_tree_root<<<1, 32, 0, s>>>(ilog2(Lw / 8), tr, off_ar);
       check();
@@ -935,9 +971,25 @@ struct Tail {
     br.st = st;
     br.ub_scratch = alloc<fe>(kUpdateBetasScratch);
     WalkTrace wt;
+    // the opening draws from st->prng itself: the script leaves its state
+    // there and skips the opening's calls (per iteration log2 kappa
+    // F::_random(), the queries' rand(), update_betas' F::_random(); the
+    // final point's F::_random())
+    if (script) script->push_back({DRAW_STATE, 0, 0u, 0});
     {
       const fe *arrays[1] = {arr}, *bets[1] = {baggr}, *cws[1] = {cw};
       batch_open_walk(br, P, arrays, bets, cws, nullptr, tr, lay, dry, &wt);
+    }
+    {
+      uint64_t calls = 0;
+      for (const BatchStep &e : P.steps)
+        if (e.iterate) calls += 40ull * ilog2((uint64_t)e.kappa) + (uint64_t)e.l + 40;
+      calls += 40ull * ilog2(P.m_final);
+      if (script) script->push_back({DRAW_SKIP, (int)calls, 0u, 0});
+      if (!dry) {
+        k_prng_check<<<1, 32, 0, s>>>(st, after_walk, flags);
+        check();
+      }
     }
     const int npt = (int)wt.chal.size() + ilog2(wt.m_final);
     if (npt != logmd || (int)wt.chal.size() > 64 || (int)wt.queries.size() > kMaxTailIter)
@@ -987,8 +1039,7 @@ struct Tail {
     }
     // r_c and the final verification step
     const uint64_t off_rc = lay.rec(T_L_RC, 2, 16);
-    fe *rc = alloc<fe>(1);
-    draw_fields(1, rc);
+    const fe *rc = draws(1);
     // the leader's b2: omega^j times the transform of beta(r2), folded by every round's L
     const fe om_off = root_of_unity(1 + in.log_rate_offset + logBs);
     fe *om = alloc<fe>(in.Bs), *b2c = alloc<fe>(in.Bs), *b2t = alloc<fe>(in.Bs), *b2f = nullptr;
@@ -1034,14 +1085,18 @@ struct Tail {
       fa.b2f = b2f;
       fa.rc = rc;
       fa.off_rc = off_rc;
-      k_final_eval<<<1, kT, 0, s>>>(fa, flags, tr);
+      int nterms = 0;
+      for (int j = 0; j < fa.nq; j++) nterms += fa.q[j].l;
+      fe *py = alloc<fe>(64), *terms = alloc<fe>(std::max(nterms, 1));
+      k_powers_y<<<1, 64, 0, s>>>(N, rc, py);
+      if (nterms) k_final_terms<<<nblk((uint64_t)nterms * 32), kT, 0, s>>>(fa, py, terms);
+      k_final_eval<<<1, kT, 0, s>>>(fa, terms, nterms, flags, tr);
       check();
     }
     // delegate_beta_eval(r2, Lagrange_Evals, b2[0], offset)
     const uint64_t off_by = lay.rec(T_L_BETA_Y, 1, 16);
     const int nd_b = 1 + 4 * logBs + 1 + 3 * (logBs + 1);
-    fe *Db = alloc<fe>(nd_b);
-    draw_fields(nd_b, Db);
+    const fe *Db = draws(nd_b);
     TensorArgs ta{};
     ta.n = nr;
     for (int i = 0; i < nr; i++) {
@@ -1083,13 +1138,21 @@ struct Tail {
 }  // namespace
 
 void leader_tail(LeaderResources &R, const LeaderInputs &in, ProofState *st, uint32_t *flags, uint8_t *tr,
-                 Layout &lay) {
-  Tail t{R, in, st, flags, tr, lay, tr == nullptr, R.s, {}};
+                 Layout &lay, std::vector<DrawOp> *script, uint64_t *arena_len, const LeaderDraws *draws) {
+  Tail t{R, in, st, flags, tr, lay, tr == nullptr, R.s, script, draws ? draws->after_walk : nullptr,
+         draws ? draws->arena : nullptr, 0, {}};
   t.run();
+  if (arena_len) *arena_len = t.arena_used;
 }
 
 void leader_tail_init(ProofState *st, const glibc_prng &g, uint32_t *flags, cudaStream_t s) {
   k_tail_init<<<1, 32, 0, s>>>(st, g, flags);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+void leader_draws_launch(const glibc_prng &g0, const DrawOp *ops, int nops, const LeaderDraws &d, uint8_t *tr,
+                         ProofState *st, cudaStream_t s) {
+  k_draw_script<<<1, 32, 0, s>>>(g0, ops, nops, d.arena, tr, st, d.after_walk, d.final_state);
   GBZ_CUDA(cudaGetLastError());
 }
 

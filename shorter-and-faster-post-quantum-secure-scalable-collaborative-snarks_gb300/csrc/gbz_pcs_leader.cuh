@@ -62,12 +62,34 @@ struct LeaderResources {
   std::function<NttTables &(int)> tables;    // twiddle tables by log2 length
 };
 
-// Lays out (tr == nullptr) or enqueues the tail; records are appended to
-// lay (offsets relative to tr).  st: the generator state (prng) and flags
-// (error) of the tail; *flags receives the LF_* bits on the device.
+// The tail's draws from the leader's generator, in order: F::_random()
+// values into the arena at off, rand() % mod values into the transcript at
+// off, the state handed to the WHIR opening (which draws itself), the calls
+// the opening makes.
+enum { DRAW_FIELDS = 0, DRAW_INTS = 1, DRAW_STATE = 2, DRAW_SKIP = 3 };
+struct DrawOp {
+  int kind, count;
+  uint32_t mod;
+  uint64_t off;
+};
+struct LeaderDraws {
+  fe *arena = nullptr;               // the F::_random() values
+  glibc_prng *after_walk = nullptr;  // the state after the opening's calls (checked against the opening's)
+  glibc_prng *final_state = nullptr; // the generator at the end of the tail
+};
+
+// Lays out (tr == nullptr: records appended to lay, the draws to *script,
+// the arena length to *arena_len) or enqueues the tail (offsets relative
+// to tr; the draws read from d, which the script kernel fills).  st: the
+// generator the WHIR opening draws from and its flags; *flags receives the
+// LF_* bits on the device.
 void leader_tail(LeaderResources &R, const LeaderInputs &in, ProofState *st, uint32_t *flags, uint8_t *tr,
-                 Layout &lay);
+                 Layout &lay, std::vector<DrawOp> *script, uint64_t *arena_len, const LeaderDraws *d);
 // st's generator from g, its flags and *flags cleared (enqueued on s).
 void leader_tail_init(ProofState *st, const glibc_prng &g, uint32_t *flags, cudaStream_t s);
+// The script of draws (ops: device memory) from state g0, one thread on s;
+// it runs beside the parties' rounds: nothing it reads depends on them.
+void leader_draws_launch(const glibc_prng &g0, const DrawOp *ops, int nops, const LeaderDraws &d, uint8_t *tr,
+                         ProofState *st, cudaStream_t s);
 
 }  // namespace gbz

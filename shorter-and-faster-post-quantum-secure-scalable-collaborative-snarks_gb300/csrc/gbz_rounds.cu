@@ -367,6 +367,85 @@ __global__ void __launch_bounds__(kTailThreads) form_tail_kernel(TailArgs t) {
     if ((int)threadIdx.x == k) t.fin[k] = fadd(in[k][0], fmul(r, fsub(in[k][1], in[k][0])));
 }
 
+// Rounds i0..rounds-1 of a sumcheck whose challenges were drawn ahead
+// (the leader's glibc sumchecks of delegate_protocol.cpp) and its final
+// fold, in one CTA: every round the fused fold + message, a block
+// reduction, then thread 0 checks H(0) + H(1) against the running claim
+// (flag `bit` when it differs, none when bit is 0), stores H, takes the
+// round's challenge and updates the claim.
+template <int FORM>
+__global__ void __launch_bounds__(kTailThreads) form_tail_drawn_kernel(DrawnTailArgs t) {
+  constexpr int NV = Form<FORM>::NV, NC = Form<FORM>::NC;
+  __shared__ fe red[NC][kTailThreads / 32];
+  __shared__ fe sh_r;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const fe *in[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) in[k] = t.in[k];
+  fe r = t.ch[t.i0 - 1];
+  fe y = fe_zero();
+  if (threadIdx.x == 0) y = *t.y;
+  int pp = 0;
+  for (int i = t.i0; i < t.rounds; i++) {
+    fe acc[NC];
+#pragma unroll
+    for (int k = 0; k < NC; k++) acc[k] = fe_zero();
+    const uint64_t pairs = t.n >> (i + 1);
+    for (uint64_t g = threadIdx.x; g < pairs; g += kTailThreads) {
+      Line l[NV];
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        const fe *p = in[k] + 4 * g;
+        const fe f0 = fadd(p[0], fmul(r, fsub(p[1], p[0])));
+        const fe f1 = fadd(p[2], fmul(r, fsub(p[3], p[2])));
+        t.buf[pp][k][2 * g] = f0;
+        t.buf[pp][k][2 * g + 1] = f1;
+        l[k] = line(f0, f1);
+      }
+      accumulate<FORM>(l, fe_zero(), acc);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+      for (int k = 0; k < NC; k++) acc[k] = fadd(acc[k], shfl_down_fe(acc[k], d));
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < NC; k++) red[k][wid] = acc[k];
+    __syncthreads();  // also orders this round's stores before the next round's loads
+    if (wid == 0) {
+#pragma unroll
+      for (int k = 0; k < NC; k++) acc[k] = lane < kTailThreads / 32 ? red[k][lane] : fe_zero();
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+        for (int k = 0; k < NC; k++) acc[k] = fadd(acc[k], shfl_down_fe(acc[k], d));
+      if (lane == 0) {
+        fe s = acc[NC - 1];
+        for (int k = 0; k < NC; k++) s = fadd(s, acc[k]);
+        if (t.bit && !fe_eq(s, y)) atomicOr(t.flags, t.bit);
+        for (int k = 0; k < NC; k++) put_fe(t.tr, t.off_polys + 16ull * ((uint64_t)i * NC + k), acc[k]);
+        const fe c = t.draw[t.first + (uint64_t)t.stride * i];
+        t.ch[i] = c;
+        y = eval_poly(acc, NC, c);
+        sh_r = c;
+      }
+    }
+    __syncthreads();
+    r = sh_r;
+#pragma unroll
+    for (int k = 0; k < NV; k++) in[k] = t.buf[pp][k];
+    pp ^= 1;
+  }
+  if (threadIdx.x == 0) *t.y = y;
+  // the final fold of the length-2 vectors: their v[0]
+  if ((int)threadIdx.x < NV) {
+    const fe *p = in[threadIdx.x];
+    const fe v = fadd(p[0], fmul(r, fsub(p[1], p[0])));
+    t.fin[threadIdx.x] = v;
+    put_fe(t.tr, t.off_fin + 16ull * threadIdx.x, v);
+  }
+}
+
 __global__ void form_sum_kernel(const fe *partial, int blocks, int nc, fe *out) {
   __shared__ fe red[kMaxFormCoeffs][kThreads];
   fe acc[kMaxFormCoeffs];
@@ -435,6 +514,16 @@ void form_step_launch(int form, const RoundArgs &a, int mode, int blocks, cudaSt
     case SC_QUADRUPLE: launch_form<SC_QUADRUPLE>(a, mode, blocks, s); break;
     default: throw ArgError("sumcheck: unknown round form");
   }
+}
+
+void form_tail_drawn_launch(int form, const DrawnTailArgs &a, cudaStream_t s) {
+  switch (form) {
+    case SC_QUADRATIC: form_tail_drawn_kernel<SC_QUADRATIC><<<1, kTailThreads, 0, s>>>(a); break;
+    case SC_CUBIC: form_tail_drawn_kernel<SC_CUBIC><<<1, kTailThreads, 0, s>>>(a); break;
+    case SC_QUADRUPLE: form_tail_drawn_kernel<SC_QUADRUPLE><<<1, kTailThreads, 0, s>>>(a); break;
+    default: throw ArgError("sumcheck tail: quadratic, cubic or quadruple form");
+  }
+  GBZ_CUDA(cudaGetLastError());
 }
 
 void form_sum_launch(const fe *partial, int blocks, int nc, fe *out, cudaStream_t s) {

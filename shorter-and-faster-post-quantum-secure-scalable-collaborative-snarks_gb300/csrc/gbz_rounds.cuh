@@ -33,6 +33,27 @@ int round_blocks(uint64_t pairs);
 // mode 0: message of in; 1: fold by *r into out and message of the result;
 // 2: fold only.
 void form_step_launch(int form, const RoundArgs &a, int mode, int blocks, cudaStream_t s);
+// The rounds i0 (>= 1) .. rounds-1 and the final fold of a sumcheck of
+// n-entry vectors whose challenges are drawn ahead, in one CTA (for n >> i0
+// up to a few thousand entries): in holds the vectors entering round i0
+// (n >> (i0 - 1) entries), buf two sets of n >> i0 entries; round i's
+// challenge is draw[first + stride i] (ch[i0 - 1] the previous one); round
+// messages go to the transcript at off_polys (coefficients of round i at
+// i nc), the final values to fin and to off_fin; *y is the running claim.
+struct DrawnTailArgs {
+  const fe *in[4];
+  fe *buf[2][4];
+  uint64_t n;
+  int i0, rounds;
+  const fe *draw;
+  int first, stride;
+  fe *ch, *y, *fin;
+  uint32_t *flags;
+  uint32_t bit;
+  uint8_t *tr;
+  uint64_t off_polys, off_fin;
+};
+void form_tail_drawn_launch(int form, const DrawnTailArgs &a, cudaStream_t s);
 // Sum of `blocks` partials of nc coefficients into out (device).
 void form_sum_launch(const fe *partial, int blocks, int nc, fe *out, cudaStream_t s);
 
