@@ -155,8 +155,11 @@ typedef struct gbz_sched_opts {
  * proofs are assigned longest-first to the least-loaded slot and enqueued
  * round-robin over the slots.  witness[i] holds 2^logn[i] elements and
  * transcript[i] capacity[i] >= gbz_prove_transcript_bytes(logn[i], rate[i])
- * bytes, all host (pinned, e.g. gbz_host_alloc, for overlap) or all device
- * per mem.  latency_s[i] (optional) = completion of proof i after the
+ * bytes, all host or all device per mem.  Host transcripts in pageable
+ * memory are written through a pinned staging buffer the context keeps
+ * (a device-to-pageable copy would wait for each slot's earlier work) and
+ * copied out when the batch ends; pinned ones (gbz_host_alloc) directly.
+ * latency_s[i] (optional) = completion of proof i after the
  * batch started; *makespan_s (optional) = completion of the last one.
  * opts may be NULL (defaults).  No counterpart in the reference, which
  * proves one statement per process (main.cpp). */

@@ -4,9 +4,11 @@
 // occupancy and free device memory.
 #include <algorithm>
 #include <chrono>
+#include <cstring>
 #include <numeric>
 #include <thread>
 
+#include "../../include/gbz.h"
 #include "gbz_sched.cuh"
 
 namespace gbz {
@@ -91,6 +93,9 @@ void Scheduler::clear() {
     sl.s = nullptr;
   }
   slots_.clear();
+  if (staging_) cudaFreeHost(staging_);
+  staging_ = nullptr;
+  staging_cap_ = 0;
   if (dev_errors_) cudaFree(dev_errors_);
   dev_errors_ = nullptr;
   dev_errors_cap_ = 0;
@@ -196,12 +201,36 @@ void Scheduler::enqueue(int slot, SlotPlan &sp, const ProofJob &j, int mem, bool
   GBZ_CUDA(cudaEventRecord(sp.idle, s));
 }
 
-void Scheduler::run(const std::vector<ProofJob> &jobs, const double *arrival, int mem, const SchedOpts &o,
+void Scheduler::run(const std::vector<ProofJob> &jobs_in, const double *arrival, int mem, const SchedOpts &o,
                     double *latency, double *makespan, std::vector<uint32_t> &errors) {
-  const int nj = (int)jobs.size();
+  const int nj = (int)jobs_in.size();
   errors.assign(nj, 0);
   if (makespan) *makespan = 0;
   if (!nj) return;
+  // transcripts in pageable host memory go through the pinned staging buffer
+  std::vector<ProofJob> jobs = jobs_in;
+  std::vector<uint64_t> staged(nj, ~0ull);
+  if (mem == 0) {
+    uint64_t need = 0;
+    for (int i = 0; i < nj; i++) {
+      cudaPointerAttributes a{};
+      const cudaError_t e = cudaPointerGetAttributes(&a, jobs[i].transcript);
+      if (e != cudaSuccess) (void)cudaGetLastError();
+      if (e != cudaSuccess || a.type == cudaMemoryTypeUnregistered) {
+        staged[i] = need;
+        need += (gbz_prove_transcript_bytes(jobs[i].logn, jobs[i].rate) + 255) & ~255ull;
+      }
+    }
+    if (need > staging_cap_) {
+      if (staging_) GBZ_CUDA(cudaFreeHost(staging_));
+      staging_ = nullptr;
+      staging_cap_ = 0;
+      GBZ_CUDA(cudaHostAlloc((void **)&staging_, need, cudaHostAllocDefault));
+      staging_cap_ = need;
+    }
+    for (int i = 0; i < nj; i++)
+      if (staged[i] != ~0ull) jobs[i].transcript = staging_ + staged[i];
+  }
   const int lanes = std::max(1, o.lanes);
   const int depth = std::max(1, o.depth);
   ensure_slots(lanes);
@@ -312,6 +341,9 @@ void Scheduler::run(const std::vector<ProofJob> &jobs, const double *arrival, in
   }
   if (makespan) *makespan = last;
   GBZ_CUDA(cudaMemcpy(errors.data(), dev_errors_, sizeof(uint32_t) * nj, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < nj; i++)
+    if (staged[i] != ~0ull)
+      std::memcpy(jobs_in[i].transcript, staging_ + staged[i], gbz_prove_transcript_bytes(jobs[i].logn, jobs[i].rate));
 }
 
 }  // namespace gbz

@@ -83,6 +83,13 @@ class Scheduler {
   uint64_t tick_ = 0;
   uint32_t *dev_errors_ = nullptr;
   uint64_t dev_errors_cap_ = 0;
+  // Pinned staging for transcripts the caller passes in pageable host
+  // memory: a copy from the device into pageable memory returns only when
+  // the stream has finished all earlier work, which would serialise the
+  // slots; such transcripts are copied into this buffer and from it to the
+  // caller's buffers once every proof has completed.
+  uint8_t *staging_ = nullptr;
+  uint64_t staging_cap_ = 0;
 
   void ensure_slots(int n);
   SlotPlan &plan_for(int slot, int logn, int rate, const SchedOpts &o);
