@@ -177,6 +177,14 @@ gbz_status gbz_serve(gbz_ctx *ctx, int count, const double *arrival_s, const uin
                      const uint64_t *capacity, int mem, const gbz_sched_opts *opts, double *latency_s,
                      double *makespan_s);
 
+/* gbz_prove_batch groups the proofs of one shape into one batched plan
+ * (on by default): every kernel of the proof is launched once for the
+ * whole group (grid.y or grid.x = proof, per-proof buffers at fixed
+ * strides), so a batch of many small proofs is not bound by the device's
+ * launch rate.  Off: one plan and one graph replay per proof.  Transcripts
+ * are the same either way. */
+gbz_status gbz_sched_set_grouping(gbz_ctx *ctx, int on);
+
 /* Frees the scheduler's cached slot plans and the scratch the N-party
  * calls (gbz_pcs_claim, gbz_pcs_open, gbz_pcs_open_full, gbz_cosumcheck)
  * keep per shape between calls; *cached_bytes (optional) gets the device

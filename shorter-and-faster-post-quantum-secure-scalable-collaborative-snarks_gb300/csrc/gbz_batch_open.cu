@@ -317,7 +317,7 @@ void batch_open_walk(BatchResources &R, const BatchPlan &P, const fe *const *arr
     if (depth != ilog2(lv)) throw ArgError("batch open: path length does not match the tree");
     const unsigned blocks = (unsigned)((hashes + 127) / 128);
     if (kind == TREE_LEVELS) k_whir_paths<<<blocks, 128, 0, s>>>(levels, lv, l, tr, off_q, off_path);
-    else if (kind == TREE_CODEWORD) k_whir_paths_chain<<<blocks, 128, 0, s>>>(codeword, lv, l, tr, off_q, off_path);
+    else if (kind == TREE_CODEWORD) k_whir_paths_chain<<<blocks, 128, 0, s>>>(codeword, lv, l, tr, off_q, off_path, 0, 0);
     else k_zero_tree_paths<<<(unsigned)((depth + 31) / 32), 32, 0, s>>>(depth, l, tr, off_path);
     GBZ_CUDA(cudaGetLastError());
   };

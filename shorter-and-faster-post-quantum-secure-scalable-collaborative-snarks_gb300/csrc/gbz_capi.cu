@@ -818,6 +818,7 @@ gbz_status prove_many(gbz_ctx *ctx, int count, const double *arrival_s, const ui
     need(capacity, "capacity");
   }
   SchedOpts o;
+  o.group = ctx->group;
   if (opts) {
     if (opts->lanes < 0 || opts->lanes > 64) throw ArgError("sched: lanes must be in [0, 64]");
     if (opts->depth < 0) throw ArgError("sched: depth must be non-negative");
@@ -872,6 +873,12 @@ gbz_status gbz_serve(gbz_ctx *ctx, int count, const double *arrival_s, const uin
   }
   return prove_many(ctx, count, arrival_s, witness, logn, rate, prng_seed, transcript, capacity, mem, opts,
                     latency_s, makespan_s);
+}
+
+gbz_status gbz_sched_set_grouping(gbz_ctx *ctx, int on) {
+  if (!ctx) return GBZ_EINVAL;
+  ctx->group = on != 0;
+  return GBZ_OK;
 }
 
 gbz_status gbz_sched_release(gbz_ctx *ctx, uint64_t *cached_bytes) {

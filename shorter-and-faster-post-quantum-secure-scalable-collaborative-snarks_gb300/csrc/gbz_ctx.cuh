@@ -33,6 +33,7 @@ struct gbz_ctx {
   std::map<std::pair<int, int>, std::unique_ptr<Profiler>> profilers;
   std::unique_ptr<Scheduler> sched;
   bool graphs = true;  // gbz_prove replays captured graphs (gbz_set_graphs)
+  bool group = true;   // gbz_prove_batch: proofs of one shape share launches (gbz_sched_set_grouping)
   SideStream side;     // second stream of the party sumcheck (created on first use)
 
   const SideStream &side_stream() {

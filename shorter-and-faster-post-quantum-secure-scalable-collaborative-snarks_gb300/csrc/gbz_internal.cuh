@@ -29,6 +29,18 @@ enum : uint32_t {
   T_AGGR_PATHS = 23, T_AGGR_ROOT = 24
 };
 
+// Batched launches: proof p of a batch of same-shape proofs works on its
+// pointer arguments advanced by p times their per-proof byte strides (the
+// proof index is grid.y for kernels of many CTAs per proof, grid.x for
+// kernels of one CTA per proof).  A single proof passes zero strides.
+struct BStr {
+  uint64_t s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+};
+template <typename T>
+__device__ __forceinline__ T *badv(T *q, uint64_t stride, uint32_t p) {
+  return reinterpret_cast<T *>(reinterpret_cast<uintptr_t>(q) + stride * p);
+}
+
 // Transcript records start at 4-byte multiples (query records have 4-byte
 // units), so every store into the transcript is a 32-bit store.
 __device__ __forceinline__ void put_fe(uint8_t *tr, uint64_t off, fe v) {
@@ -207,29 +219,39 @@ void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2
 // messages of (a, b) and of its fold by *chal0 (partials of blocks CTAs in
 // partial0 and partial1, blocks <= sc_blocks(m / 4)), and (a4, b4) of length
 // m/4, the fold by *chal0 then *chal1.  m >= 4.
+// batch > 1: grid.y = proof, bs the strides of (a, b, chal0, chal1, a4, b4,
+// partial0, partial1) (sc_fold2) / (a, E2, c, chal0, chal1, a4, b4,
+// partial0, partial1) (sc_fold2_eq) / (a, E, chal, a2, E2, partial)
+// (sc_eq_step).
 void sc_fold2_launch(const fe *a, const fe *b, uint64_t m, const fe *chal0, const fe *chal1, fe *a4, fe *b4,
-                     fe *partial0, fe *partial1, int blocks, cudaStream_t s);
+                     fe *partial0, fe *partial1, int blocks, cudaStream_t s, int batch = 1, const BStr &bs = BStr());
 // The same with b = precompute_beta(c) given by E2, the eq table of c[2..]
 // (m/4 entries): b is not read, b4 = eq1(c0, r0) eq1(c1, r1) E2.
 void sc_fold2_eq_launch(const fe *a, const fe *E2, uint64_t m, const fe *c, const fe *chal0, const fe *chal1, fe *a4,
-                        fe *b4, fe *partial0, fe *partial1, int blocks, cudaStream_t s);
+                        fe *b4, fe *partial0, fe *partial1, int blocks, cudaStream_t s, int batch = 1,
+                        const BStr &bs = BStr());
 // The same steps for the sumcheck of sum_x w(x) eq(z, x) with the eq vector
 // kept as the shrinking table E_i of z_{i+1..}: chal == nullptr gives the
 // sums S(0), S(1) of (a, E); otherwise a is folded by *chal into a2 (m/2),
 // E2 = pairwise sums of E (m/4) and, when reduce, the sums of (a2, E2).
 // Partials are (S0, S1, 0) per block.
 void sc_eq_step_launch(const fe *a, const fe *E, uint64_t m, const fe *chal, fe *a2, fe *E2, bool reduce,
-                       fe *partial, int blocks, cudaStream_t s);
+                       fe *partial, int blocks, cudaStream_t s, int batch = 1, const BStr &bs = BStr());
 // Round-message reduction of `blocks` partials into out[3].
 void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s);
 
 // precompute_beta (utils.cpp:198-243) of r (nr values, device) into B.
-void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s);
+// batch > 1: grid.y = proof, r and B advanced by their byte strides per proof.
+void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s, int batch = 1, uint64_t r_stride = 0,
+                 uint64_t B_stride = 0);
 
 // update_betas (Whir.cpp:325-342): b[j] += sum_i comb[i] * omega_q[i]^j.
 // pw_scratch holds kUpdateBetasScratch elements.
 constexpr uint64_t kUpdateBetasScratch = (uint64_t)kMaxQueries * 256;
-void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s);
+// batch > 1: proof p updates b + p b_stride with st + p and its scratch at
+// pw_scratch + p pw_stride (byte strides).
+void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s,
+                         int batch = 1, uint64_t b_stride = 0, uint64_t pw_stride = 0);
 
 // ----------------------------------------------------------- calibration
 // Measured throughput of the F_{p^2} multiply and of the 64-byte Blake3

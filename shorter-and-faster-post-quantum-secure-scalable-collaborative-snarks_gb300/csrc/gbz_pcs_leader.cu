@@ -951,7 +951,8 @@ struct Tail {
     const uint64_t off_ar = lay.rec(T_AGGR_ROOT, 1, 32);
     draw_mod(la, (uint32_t)(Lw / 4), off_aq);
     if (!dry) {
-      k_whir_paths_chain<<<nblk((uint64_t)la * depth_a, 128), 128, 0, s>>>(ro[0].W, Lw / 4, la, tr, off_aq, off_ap);
+      k_whir_paths_chain<<<nblk((uint64_t)la * depth_a, 128), 128, 0, s>>>(ro[0].W, Lw / 4, la, tr, off_aq, off_ap,
+                                                                           0, 0);
       k_zero_tree_root<<<1, 32, 0, s>>>(ilog2(Lw / 8), tr, off_ar);
       check();
     }

@@ -32,6 +32,7 @@ namespace {
 // the global copy would each pay a memory round trip.
 __global__ void k_init(ProofState *st, uint32_t seed, int seed_in_state) {
   __shared__ glibc_prng g;
+  st += blockIdx.x;  // a batch: one CTA per proof
   if (threadIdx.x) return;
   st->fs = fe_zero();
   prng_seed(g, seed_in_state ? st->seed_in : seed);
@@ -54,7 +55,9 @@ __global__ void k_init_open(ProofState *st, glibc_prng g, const fe *point, int l
 }
 
 // z_i = hash_to_field({0}) for i < logn.
-__global__ void k_point(ProofState *st, int logn, uint8_t *tr, uint64_t off) {
+__global__ void k_point(ProofState *st, int logn, uint8_t *tr, uint64_t off, uint64_t trs) {
+  st += blockIdx.x;
+  tr += trs * blockIdx.x;
   if (threadIdx.x) return;
   fe s = st->fs;
   for (int i = 0; i < logn; i++) {
@@ -129,7 +132,10 @@ __device__ fe sc_round_eq_apply(const fe SS[3], ProofState *st, int round, uint8
 }
 
 __global__ void k_sc_round_eq(const fe *partial, int blocks, ProofState *st, int round, uint8_t *tr,
-                              int64_t off_claim, uint64_t off_poly, uint64_t off_chal) {
+                              int64_t off_claim, uint64_t off_poly, uint64_t off_chal, uint64_t ps, uint64_t trs) {
+  partial = badv(partial, ps, blockIdx.x);
+  st += blockIdx.x;
+  tr += trs * blockIdx.x;
   fe SS[3];
   sum_partials(partial, blocks, SS);  // (S0, -S0-S1, S1)
   if (threadIdx.x) return;
@@ -143,11 +149,20 @@ __global__ void k_sc_round_eq(const fe *partial, int blocks, ProofState *st, int
 // then the final fold and the SC_FINAL record.  Round r's SC_POLY payload
 // is at off_poly0 + 80 (r - round0), its SC_CHALLENGE 56 bytes after it.
 constexpr int kScTailMax = 4096;
+// Batched plans: codewords of 2^kBatchRealLog entries or more are committed
+// proof by proof with the real-input transform, shorter ones in one batched
+// general transform.
+constexpr int kBatchRealLog = 18;
 constexpr int kScTailThreads = 1024;
 __global__ void __launch_bounds__(kScTailThreads)
 k_sc_tail(ProofState *st, const fe *a, const fe *E, int m, int round0, int logn, uint8_t *tr, uint64_t off_poly0,
-          uint64_t off_final) {
+          uint64_t off_final, BStr bs) {
   extern __shared__ fe tail_sm[];
+  // a batch: one CTA per proof; bs = strides of (a, E, tr)
+  st += blockIdx.x;
+  a = badv(a, bs.s[0], blockIdx.x);
+  E = badv(E, bs.s[1], blockIdx.x);
+  tr = badv(tr, bs.s[2], blockIdx.x);
   fe *w = tail_sm, *e = tail_sm + kScTailMax;
   __shared__ fe red[2][kScTailThreads / 32];
   __shared__ fe chal_s;
@@ -210,7 +225,11 @@ k_sc_tail(ProofState *st, const fe *a, const fe *E, int m, int round0, int logn,
   }
 }
 
-__global__ void k_sc_final(ProofState *st, const fe *v1, const fe *v2, uint8_t *tr, uint64_t off) {
+__global__ void k_sc_final(ProofState *st, const fe *v1, const fe *v2, uint8_t *tr, uint64_t off, BStr bs) {
+  st += blockIdx.x;
+  v1 = badv(v1, bs.s[0], blockIdx.x);
+  if (v2) v2 = badv(v2, bs.s[1], blockIdx.x);
+  tr = badv(tr, bs.s[2], blockIdx.x);
   if (threadIdx.x) return;
   // v2 == nullptr: the eq vector was not folded, its last value is epre
   fe a = v1[0], b = v2 ? v2[0] : st->epre;
@@ -227,6 +246,7 @@ __device__ __forceinline__ fe pow_table(const fe *lo, const fe *hi, uint64_t e) 
 
 struct QueryArgs {
   ProofState *st;
+  uint64_t cws, trs;     // per-proof strides of cw and tr in a batch (one CTA per proof)
   const fe *cw;          // previous codeword
   uint64_t L;            // its length
   uint64_t NL;           // new codeword length
@@ -274,6 +294,7 @@ __device__ uint64_t number_from(const int32_t *d) {
 // each) and the query positions from them.
 __global__ void __launch_bounds__(256) k_whir_schedule(ProofState *st, SchedArgs a) {
   __shared__ int32_t draws[kMaxDraws];
+  st += blockIdx.x;
   int N = kFieldDraws * a.lg_final;
   for (int t = 0; t < a.T; t++) N += 3 * kFieldDraws + a.l[t];
   if (threadIdx.x == 0) {
@@ -329,7 +350,11 @@ struct UbPrep {
 // drawn up front, and the threads prepare the iteration's update_betas.
 __global__ void k_whir_rounds2_s(const fe *partial0, const fe *partial1, int blocks, ProofState *st, int t,
                                  uint8_t *tr, uint64_t off_poly0, uint64_t off_chal0, uint64_t off_poly1,
-                                 uint64_t off_chal1, UbPrep u) {
+                                 uint64_t off_chal1, UbPrep u, uint64_t ps, uint64_t trs) {
+  partial0 = badv(partial0, ps, blockIdx.x);
+  partial1 = badv(partial1, ps, blockIdx.x);
+  st += blockIdx.x;
+  tr += trs * blockIdx.x;
   fe H0[3], H1[3];
   sum_partials(partial0, blocks, H0);
   __syncthreads();  // sum_partials' shared scratch is reused
@@ -357,6 +382,9 @@ __global__ void k_whir_rounds2_s(const fe *partial0, const fe *partial1, int blo
 // (Whir.cpp:383-384).  Thread i handles query i.
 __global__ void __launch_bounds__(kMaxQueries) k_whir_query_s(QueryArgs a, int t) {
   __shared__ fe red[kMaxQueries / 32];
+  a.st += blockIdx.x;
+  a.cw = badv(a.cw, a.cws, blockIdx.x);
+  a.tr += a.trs * blockIdx.x;
   ProofState *st = a.st;
   const int i = threadIdx.x;
   fe contrib = fe_zero();
@@ -468,19 +496,29 @@ __device__ __forceinline__ void put_hash(uint8_t *dst, const uint32_t h[8]) {  /
 }
 
 // Root of the tree over a codeword of 4 * 2^depth elements: G^depth(leaf 0).
-__global__ void k_merkle_root(const fe *cw, int depth, uint8_t *tr, uint64_t off) {
-  if (threadIdx.x) return;
+__device__ void merkle_root_dev(const fe *cw, int depth, uint8_t *tr, uint64_t off) {
   uint32_t h[8];
   leaf_hash(cw, 0, h);
   for (int d = 0; d < depth; d++) node_hash(h);
   put_hash(tr + off, h);
+}
+__global__ void k_merkle_root(const fe *cw, int depth, uint8_t *tr, uint64_t off) {
+  if (threadIdx.x) return;
+  merkle_root_dev(cw, depth, tr, off);
+}
+// The same for a batch: proof p (grid.x) reads cw + p cws, writes tr + p trs.
+__global__ void k_merkle_root_b(const fe *cw, uint64_t cws, int depth, uint8_t *tr, uint64_t trs, uint64_t off) {
+  if (threadIdx.x) return;
+  merkle_root_dev(badv(cw, cws, blockIdx.x), depth, tr + trs * blockIdx.x, off);
 }
 
 // Authentication paths of the l queries: entry d of query i is the sibling
 // (q >> d) ^ 1 of level d, i.e. G^d(leaf ((q >> d) ^ 1) << d).  One thread
 // per entry, the deepest entries first.
 __global__ void k_whir_paths_chain(const fe *cw, uint64_t leaves, int l, uint8_t *tr, uint64_t off_q,
-                                   uint64_t off_path) {
+                                   uint64_t off_path, uint64_t cws, uint64_t trs) {
+  cw = badv(cw, cws, blockIdx.y);  // a batch: grid.y = proof
+  tr += trs * blockIdx.y;
   const int depth = 63 - __clzll((long long)leaves);
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (uint64_t)l * depth) return;
@@ -533,10 +571,8 @@ __global__ void k_whir_paths(const uint8_t *tree, uint64_t leaves, int l, uint8_
 // (:840-869): the remaining polynomial (m <= kFinalMax entries), log2 m
 // F::_random draws and evaluate_vector(b, r).  With check_K, the flag 8 is
 // raised unless K equals sum arr * b (verification step 2, :848-855).
-__global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
-                        uint64_t off_point, uint64_t off_eval, int check_K, const fe *point) {
-  __shared__ glibc_prng g;
-  if (threadIdx.x) return;
+__device__ void final_dev(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
+                          uint64_t off_point, uint64_t off_eval, int check_K, const fe *point, glibc_prng &g) {
   if (m < 1 || m > kFinalMax) {
     atomicOr(&st->error, 16u);
     return;
@@ -563,6 +599,22 @@ __global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8
     for (int j = 0; j < L; j++) v[j] = fadd(fmul(om, v[2 * j]), fmul(r[i], v[2 * j + 1]));
   }
   put_fe(tr, off_eval, v[0]);
+}
+__global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
+                        uint64_t off_point, uint64_t off_eval, int check_K, const fe *point) {
+  __shared__ glibc_prng g;
+  if (threadIdx.x) return;
+  final_dev(st, arr, b, m, tr, off_poly, off_point, off_eval, check_K, point, g);
+}
+// The same for a batch of proofs whose final point was drawn up front
+// (st->fin_r): proof p = grid.x, bs = strides of (arr, b, tr).
+__global__ void k_final_b(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
+                          uint64_t off_point, uint64_t off_eval, BStr bs) {
+  __shared__ glibc_prng g;
+  if (threadIdx.x) return;
+  st += blockIdx.x;
+  final_dev(st, badv(arr, bs.s[0], blockIdx.x), badv(b, bs.s[1], blockIdx.x), m, badv(tr, bs.s[2], blockIdx.x),
+            off_poly, off_point, off_eval, 0, st->fin_r, g);
 }
 
 // ------------------------------------------------------------ host side
@@ -620,9 +672,10 @@ NttTables &ProofPlan::tables(int lg) {
   return ntt.emplace(lg, t).first->second;
 }
 
-std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
+std::unique_ptr<ProofPlan> plan_create(int logn, int rate, int batch) {
   if (logn < 3 || logn > 25) throw ArgError("prover: log2 witness length must be in [3, 25]");
   if (rate < 2 || rate > 64 || !is_pow2((uint64_t)rate)) throw ArgError("prover: rate must be a power of two in [2, 64]");
+  if (batch < 1 || batch > 65535) throw ArgError("prover: 1..65535 proofs per plan");
   const uint64_t n = 1ull << logn, L = n * (uint64_t)rate;
   if (ilog2(L) > kMaxNttLogN) throw ArgError("prover: codeword longer than 2^26");
   auto p = std::unique_ptr<ProofPlan>(new ProofPlan());
@@ -630,11 +683,23 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   p->rate = rate;
   p->n = n;
   p->L = L;
-  p->w = (fe *)p->dalloc(sizeof(fe) * n);
-  p->cw[0] = (fe *)p->dalloc(sizeof(fe) * L);
-  p->cw[1] = (fe *)p->dalloc(sizeof(fe) * (L / 2));
-  p->tmp = (fe *)p->dalloc(sizeof(fe) * L);
-  p->tmp2 = (fe *)p->dalloc(sizeof(fe) * (L / 2));
+  p->B = batch;
+  const uint64_t B = (uint64_t)batch;
+  p->bs_w = sizeof(fe) * n;
+  p->bs_cw0 = sizeof(fe) * L;
+  p->bs_cw1 = sizeof(fe) * (L / 2);
+  p->bs_tmp = sizeof(fe) * L;
+  p->bs_tmp2 = sizeof(fe) * (L / 2);
+  p->bs_v = sizeof(fe) * (n / 2);
+  p->bs_arr = sizeof(fe) * (n / 2);
+  p->bs_beta = sizeof(fe) * n;
+  p->bs_part = sizeof(fe) * 3 * (uint64_t)sc_blocks(n / 2);
+  p->bs_ub = sizeof(fe) * kUpdateBetasScratch;
+  p->w = (fe *)p->dalloc(B * p->bs_w);
+  p->cw[0] = (fe *)p->dalloc(B * p->bs_cw0);
+  p->cw[1] = (fe *)p->dalloc(B * p->bs_cw1);
+  p->tmp = (fe *)p->dalloc(B * p->bs_tmp);
+  p->tmp2 = (fe *)p->dalloc(B * p->bs_tmp2);
   GBZ_CUDA(cudaStreamCreateWithFlags(&p->s2, cudaStreamNonBlocking));
   GBZ_CUDA(cudaStreamCreateWithFlags(&p->s3, cudaStreamNonBlocking));
   GBZ_CUDA(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
@@ -644,16 +709,16 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   for (auto &e : p->ev_fold) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto &e : p->ev_commit) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto &e : p->ev_query) GBZ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  p->va[0] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
-  p->va[1] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
-  p->arr = (fe *)p->dalloc(sizeof(fe) * (n / 2));
-  p->vb[0] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
-  p->vb[1] = (fe *)p->dalloc(sizeof(fe) * (n / 2));
-  p->beta = (fe *)p->dalloc(sizeof(fe) * n);
-  p->partial = (fe *)p->dalloc(sizeof(fe) * 3 * (uint64_t)sc_blocks(n / 2));
-  p->partial2 = (fe *)p->dalloc(sizeof(fe) * 3 * (uint64_t)sc_blocks(n / 2));
-  p->ub_scratch = (fe *)p->dalloc(sizeof(fe) * kUpdateBetasScratch);
-  p->st = (ProofState *)p->dalloc(sizeof(ProofState));
+  p->va[0] = (fe *)p->dalloc(B * p->bs_v);
+  p->va[1] = (fe *)p->dalloc(B * p->bs_v);
+  p->arr = (fe *)p->dalloc(B * p->bs_arr);
+  p->vb[0] = (fe *)p->dalloc(B * p->bs_v);
+  p->vb[1] = (fe *)p->dalloc(B * p->bs_v);
+  p->beta = (fe *)p->dalloc(B * p->bs_beta);
+  p->partial = (fe *)p->dalloc(B * p->bs_part);
+  p->partial2 = (fe *)p->dalloc(B * p->bs_part);
+  p->ub_scratch = (fe *)p->dalloc(B * p->bs_ub);
+  p->st = (ProofState *)p->dalloc(B * sizeof(ProofState));
   GBZ_CUDA(cudaFuncSetAttribute(k_sc_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(fe) * (kScTailMax + kScTailMax / 2))));
   // Build the transcript layout (record headers are constant).
@@ -661,13 +726,14 @@ std::unique_ptr<ProofPlan> plan_create(int logn, int rate) {
   enqueue_proof(*p, nullptr, 1, nullptr, /*dry=*/true);  // layout and launch counts
   p->layout.record_headers = false;
   p->transcript_bytes = p->layout.len;
-  p->transcript = (uint8_t *)p->dalloc(p->transcript_bytes);
+  p->transcript = (uint8_t *)p->dalloc(B * p->transcript_bytes);
   std::vector<uint8_t> img(p->transcript_bytes, 0);
   for (auto &h : p->layout.headers) {
     std::memcpy(&img[h.off], &h.tag, 4);
     std::memcpy(&img[h.off + 4], &h.count, 4);
   }
-  GBZ_CUDA(cudaMemcpy(p->transcript, img.data(), img.size(), cudaMemcpyHostToDevice));
+  for (uint64_t b = 0; b < B; b++)
+    GBZ_CUDA(cudaMemcpy(p->transcript + b * p->transcript_bytes, img.data(), img.size(), cudaMemcpyHostToDevice));
   // Twiddle tables for every transform length the proof uses.
   p->tables(ilog2(L));
   for (uint64_t m = n, cur = (uint64_t)rate; m > 4; m /= 4, cur *= 2) {
@@ -716,6 +782,11 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   const int logn = p.logn;
   uint8_t *tr = open ? p.open_transcript : p.transcript;
   ProofState *st = p.st;
+  // a batch: every launch covers the plan's B proofs (per-proof strides below)
+  const int B = p.B;
+  if (B > 1 && (open || (witness && witness != p.w))) throw ArgError("prover: a batch reads its witnesses from the plan");
+  const uint64_t trs = p.transcript_bytes, sts = sizeof(ProofState);
+  const uint64_t cw_s[2] = {p.bs_cw0, p.bs_cw1};
   Profiler *prof = (!dry && p.prof && p.prof->enabled) ? p.prof : nullptr;
   // RUN(category, kernel launches, statement): counts in the dry run, else
   // runs the statement (bracketed by profiler events when enabled).
@@ -745,7 +816,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   if (open) {
     RUN(PC_PROTOCOL, 1, k_init_open<<<1, 32, 0, s>>>(st, open->prng, open->point, logn, open->K));
   } else {
-    RUN(PC_PROTOCOL, 1, k_init<<<1, 32, 0, s>>>(st, prng_seed, seed_in_state ? 1 : 0));
+    RUN(PC_PROTOCOL, 1, k_init<<<B, 32, 0, s>>>(st, prng_seed, seed_in_state ? 1 : 0));
   }
   // The opening's randomness, drawn on the query stream while the
   // commitment and the sumcheck run.
@@ -768,7 +839,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
       GBZ_CUDA(cudaEventRecord(p.ev_init, s));
       GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_init, 0));
     }
-    RUN_ON(q, PC_PROTOCOL, 1, k_whir_schedule<<<1, 256, 0, q>>>(st, sa));
+    RUN_ON(q, PC_PROTOCOL, 1, k_whir_schedule<<<B, 256, 0, q>>>(st, sa));
     if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_sched, q));
   }
 
@@ -782,6 +853,24 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   if (open) {
     if (!dry && open->codeword != p.cw[0])
       GBZ_CUDA(cudaMemcpyAsync(p.cw[0], open->codeword, 16 * L, cudaMemcpyDeviceToDevice, c));
+  } else if (B > 1 && ilog2(L) < kBatchRealLog) {
+    // short codewords (launch bound): the batch's codewords as one batched
+    // transform (the same values as the real-input path of a single proof)
+    RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(L)),
+           ntt_launch_rows(p.tables(ilog2(L)), w, p.n, p.bs_w / sizeof(fe), p.cw[0], p.bs_cw0 / sizeof(fe), B, p.tmp,
+                           false, c));
+  } else if (B > 1) {
+    // long codewords (integer-pipe bound): the real-input transform of each
+    // proof, half the multiplies of the general one
+    for (int pb = 0; pb < B; pb++) {
+      if (!dry) GBZ_CUDA(cudaMemsetAsync(&st[pb].nonreal, 0, sizeof(uint32_t), c));
+      RUN_ON(c, PC_NTT, ntt_launch_real_count(ilog2(L)),
+             ntt_launch_real(p.tables(ilog2(L) - 1), p.tables(ilog2(L)),
+                             reinterpret_cast<const fe *>(reinterpret_cast<const char *>(w) + p.bs_w * pb), p.n,
+                             reinterpret_cast<fe *>(reinterpret_cast<char *>(p.cw[0]) + p.bs_cw0 * pb),
+                             reinterpret_cast<fe *>(reinterpret_cast<char *>(p.tmp) + p.bs_tmp * pb), &st[pb].nonreal,
+                             c));
+    }
   } else {
     if (!dry) GBZ_CUDA(cudaMemsetAsync(&st->nonreal, 0, sizeof(uint32_t), c));
     RUN_ON(c, PC_NTT, ntt_launch_real_count(ilog2(L)),
@@ -800,9 +889,9 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   {
   // 2. evaluation point and its eq table.
   off = lay.rec(T_EVAL_POINT, logn, 16);
-  RUN(PC_PROTOCOL, 1, k_point<<<1, 32, 0, s>>>(st, logn, tr, off));
+  RUN(PC_PROTOCOL, 1, k_point<<<B, 32, 0, s>>>(st, logn, tr, off, trs));
   // eq table E_0 of z_1..z_{logn-1} (the eq factor of variable 0 is kept apart)
-  RUN(PC_BETA, 1, beta_launch(st->z + 1, logn - 1, p.vb[0], s));
+  RUN(PC_BETA, 1, beta_launch(st->z + 1, logn - 1, p.vb[0], s, B, sts, p.bs_v));
 
   // 3. sumcheck of sum w(x) eq(z, x): w is folded each round, the eq vector
   //    is represented by the shrinking tables E_i (vb ping-pong) and the
@@ -810,6 +899,7 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
   uint64_t off_claim = lay.rec(T_CLAIM, 1, 16);
   int pp = 0, ep = 0;  // va ping-pong for w, vb ping-pong for E
   bool tail_done = false;
+  uint64_t as = p.bs_w;  // per-proof stride of a (the witness, then va)
   for (int i = 0; i < logn; i++) {
     if (i >= 1 && m <= (uint64_t)kScTailMax) {
       // the remaining rounds and the final fold in one CTA
@@ -820,38 +910,62 @@ void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStre
         if (op != op0 + 80ull * (uint64_t)(r - i) || oc != op + 56) throw ArgError("prover: sumcheck record layout");
       }
       off = lay.rec(T_SC_FINAL, 2, 16);
+      BStr tb;
+      tb.s[0] = as;
+      tb.s[1] = p.bs_v;
+      tb.s[2] = trs;
       RUN(PC_SUMCHECK, 1,
-          (k_sc_tail<<<1, kScTailThreads, sizeof(fe) * (kScTailMax + kScTailMax / 2), s>>>(st, a, p.vb[ep], (int)m, i,
-                                                                                         logn, tr, op0, off)));
+          (k_sc_tail<<<B, kScTailThreads, sizeof(fe) * (kScTailMax + kScTailMax / 2), s>>>(st, a, p.vb[ep], (int)m, i,
+                                                                                         logn, tr, op0, off, tb)));
       tail_done = true;
       break;
     }
     uint64_t off_poly = lay.rec(T_SC_POLY, 3, 16);
     uint64_t off_chal = lay.rec(T_SC_CHALLENGE, 1, 16);
     int blocks;
+    // strides of (a, E, chal, a2, E2, partial)
+    BStr es;
+    es.s[0] = as;
+    es.s[1] = p.bs_v;
+    es.s[2] = sts;
+    es.s[3] = p.bs_v;
+    es.s[4] = p.bs_v;
+    es.s[5] = p.bs_part;
     if (i == 0) {
       blocks = sc_blocks(m / 2);
-      RUN(PC_SUMCHECK, 1, sc_eq_step_launch(a, p.vb[0], m, nullptr, nullptr, nullptr, true, p.partial, blocks, s));
+      RUN(PC_SUMCHECK, 1,
+          sc_eq_step_launch(a, p.vb[0], m, nullptr, nullptr, nullptr, true, p.partial, blocks, s, B, es));
     } else {
       blocks = sc_blocks(m / 4);
       fe *a2 = p.va[pp];
       RUN(PC_SUMCHECK, 1,
-          sc_eq_step_launch(a, p.vb[ep], m, &st->chal[i - 1], a2, p.vb[ep ^ 1], true, p.partial, blocks, s));
+          sc_eq_step_launch(a, p.vb[ep], m, &st->chal[i - 1], a2, p.vb[ep ^ 1], true, p.partial, blocks, s, B, es));
       a = a2;
+      as = p.bs_v;
       pp ^= 1;
       ep ^= 1;
       m /= 2;
     }
     RUN(PC_PROTOCOL, 1,
-        k_sc_round_eq<<<1, 256, 0, s>>>(p.partial, blocks, st, i, tr, i == 0 ? (int64_t)off_claim : -1, off_poly,
-                                        off_chal));
+        k_sc_round_eq<<<B, 256, 0, s>>>(p.partial, blocks, st, i, tr, i == 0 ? (int64_t)off_claim : -1, off_poly,
+                                        off_chal, p.bs_part, trs));
   }
   if (!tail_done) {
     fe *a2 = p.va[pp];
+    BStr es;
+    es.s[0] = as;
+    es.s[1] = p.bs_v;
+    es.s[2] = sts;
+    es.s[3] = p.bs_v;
+    es.s[4] = p.bs_v;
+    es.s[5] = p.bs_part;
     RUN(PC_SUMCHECK, 1,
-        sc_eq_step_launch(a, p.vb[ep], m, &st->chal[logn - 1], a2, nullptr, false, p.partial, 1, s));
+        sc_eq_step_launch(a, p.vb[ep], m, &st->chal[logn - 1], a2, nullptr, false, p.partial, 1, s, B, es));
     off = lay.rec(T_SC_FINAL, 2, 16);
-    RUN(PC_PROTOCOL, 1, k_sc_final<<<1, 32, 0, s>>>(st, a2, nullptr, tr, off));
+    BStr fs;
+    fs.s[0] = p.bs_v;
+    fs.s[2] = trs;
+    RUN(PC_PROTOCOL, 1, k_sc_final<<<B, 32, 0, s>>>(st, a2, nullptr, tr, off, fs));
     pp ^= 1;
   }
   }
@@ -866,10 +980,13 @@ opening:
   // b = precompute_beta(chal) has tensor structure: for the first
   // iteration only the eq table E2 of chal[2..] is formed (a quarter of b)
   const bool eq_first = logn >= 4;
-  RUN(PC_BETA, 1, eq_first ? beta_launch(st->chal + 2, logn - 2, p.beta, s) : beta_launch(st->chal, logn, p.beta, s));
+  RUN(PC_BETA, 1,
+      eq_first ? beta_launch(st->chal + 2, logn - 2, p.beta, s, B, sts, p.bs_beta)
+               : beta_launch(st->chal, logn, p.beta, s, B, sts, p.bs_beta));
   if (!dry) GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_sched, 0));  // round challenges
   a = w;
   const fe *b = p.beta;
+  uint64_t ast = p.bs_w, bst = p.bs_beta;  // per-proof strides of a and b
   m = p.n;
   uint64_t cur = (uint64_t)p.rate;
   fe *arr_next = p.arr;
@@ -886,13 +1003,32 @@ opening:
     fe *bd = p.vb[(iter + 1) & 1];
     const int blocks = sc_blocks(m / 4);
     if (iter == 0 && eq_first) {
+      BStr fb;  // (a, E2, c, chal0, chal1, a4, b4, partial0, partial1)
+      fb.s[0] = ast;
+      fb.s[1] = bst;
+      fb.s[2] = sts;
+      fb.s[3] = sts;
+      fb.s[4] = sts;
+      fb.s[5] = p.bs_arr;
+      fb.s[6] = p.bs_v;
+      fb.s[7] = p.bs_part;
+      fb.s[8] = p.bs_part;
       RUN(PC_SUMCHECK, 1,
           sc_fold2_eq_launch(a, b, m, st->chal, &st->wr[iter][0], &st->wr[iter][1], arr_next, bd, p.partial,
-                             p.partial2, blocks, s));
+                             p.partial2, blocks, s, B, fb));
     } else {
+      BStr fb;  // (a, b, chal0, chal1, a4, b4, partial0, partial1)
+      fb.s[0] = ast;
+      fb.s[1] = bst;
+      fb.s[2] = sts;
+      fb.s[3] = sts;
+      fb.s[4] = p.bs_arr;
+      fb.s[5] = p.bs_v;
+      fb.s[6] = p.bs_part;
+      fb.s[7] = p.bs_part;
       RUN(PC_SUMCHECK, 1,
           sc_fold2_launch(a, b, m, &st->wr[iter][0], &st->wr[iter][1], arr_next, bd, p.partial, p.partial2, blocks,
-                          s));
+                          s, B, fb));
     }
     {
       // both round messages; the kernel also prepares this iteration's beta update
@@ -904,10 +1040,13 @@ opening:
         u.hi = tnew.hi_fwd;
       }
       RUN(PC_PROTOCOL, 1,
-          k_whir_rounds2_s<<<1, 256, 0, s>>>(p.partial, p.partial2, blocks, st, iter, tr, op, oc, op1, oc1, u));
+          k_whir_rounds2_s<<<B, 256, 0, s>>>(p.partial, p.partial2, blocks, st, iter, tr, op, oc, op1, oc1, u,
+                                             p.bs_part, trs));
     }
     a = arr_next;
     b = bd;
+    ast = p.bs_arr;
+    bst = p.bs_v;
     m /= 4;
     arr_next += m;
     if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_fold[iter], s));
@@ -919,7 +1058,13 @@ opening:
       GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_fold[iter], 0));
       if (iter > 0) GBZ_CUDA(cudaStreamWaitEvent(c, p.ev_query[iter - 1], 0));
     }
-    RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(NL)), ntt_launch(p.tables(ilog2(NL)), a, m, p.cw[nci], p.tmp, false, c));
+    if (B > 1) {
+      RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(NL)),
+             ntt_launch_rows(p.tables(ilog2(NL)), a, m, p.bs_arr / sizeof(fe), p.cw[nci], cw_s[nci] / sizeof(fe), B,
+                             p.tmp, false, c));
+    } else {
+      RUN_ON(c, PC_NTT, ntt_launch_count(ilog2(NL)), ntt_launch(p.tables(ilog2(NL)), a, m, p.cw[nci], p.tmp, false, c));
+    }
     off_root[iter + 1] = off;
     if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_commit[iter + 1], c));
     // queries of iteration t on q: they open the codeword of commit t and
@@ -927,6 +1072,8 @@ opening:
     const int depth = ilog2(L / 4);
     QueryArgs qa;
     qa.st = st;
+    qa.cws = cw_s[cwi];
+    qa.trs = trs;
     qa.cw = p.cw[cwi];
     qa.L = L;
     qa.NL = NL;
@@ -952,13 +1099,13 @@ opening:
       GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_commit[iter], 0));
       GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_fold[iter], 0));
     }
-    RUN_ON(q, PC_MERKLE, 1, k_merkle_root<<<1, 32, 0, q>>>(qa.cw, depth, tr, off_root[iter]));
-    RUN_ON(q, PC_QUERY, 1, k_whir_query_s<<<1, kMaxQueries, 0, q>>>(qa, iter));
+    RUN_ON(q, PC_MERKLE, 1, k_merkle_root_b<<<B, 32, 0, q>>>(qa.cw, qa.cws, depth, tr, trs, off_root[iter]));
+    RUN_ON(q, PC_QUERY, 1, k_whir_query_s<<<B, kMaxQueries, 0, q>>>(qa, iter));
     {
       const uint64_t hashes = (uint64_t)l * depth;  // depth >= 2: every queried codeword has 16+ entries
       RUN_ON(q, PC_QUERY, 1,
-             k_whir_paths_chain<<<(unsigned)((hashes + 127) / 128), 128, 0, q>>>(qa.cw, L / 4, l, tr, qa.off_q,
-                                                                                 qa.off_path));
+             k_whir_paths_chain<<<dim3((unsigned)((hashes + 127) / 128), B), 128, 0, q>>>(
+                 qa.cw, L / 4, l, tr, qa.off_q, qa.off_path, qa.cws, trs));
       if (!dry && hashes == 0) throw ArgError("prover: empty authentication paths");
     }
     if (!dry) GBZ_CUDA(cudaEventRecord(p.ev_query[iter], q));
@@ -970,10 +1117,14 @@ opening:
     // at half the codeword length on the unscaled positions.
     static_assert(kWhirK == 4, "update_betas: exponent scale 2 assumes folding by 4 with NL = L / 2");
     if (update_betas_by_transform(l, m, NL / 2)) {
-      RUN(PC_UPDATE_BETAS, 2,
-          ntt_sparse_accumulate(p.tables(ilog2(NL) - 1), st->q, st->comb, l, bd, m, p.tmp2, s, 1));
+      // one sparse transform per proof of a batch
+      RUN(PC_UPDATE_BETAS, 2 * B, for (int pb = 0; pb < B; pb++) {
+        ntt_sparse_accumulate(p.tables(ilog2(NL) - 1), st[pb].q, st[pb].comb, l,
+                              reinterpret_cast<fe *>(reinterpret_cast<char *>(bd) + p.bs_v * pb), m,
+                              reinterpret_cast<fe *>(reinterpret_cast<char *>(p.tmp2) + p.bs_tmp2 * pb), s, 1);
+      });
     } else {
-      RUN(PC_UPDATE_BETAS, 2, update_betas_launch(bd, m, st, l, p.ub_scratch, s));
+      RUN(PC_UPDATE_BETAS, 2, update_betas_launch(bd, m, st, l, p.ub_scratch, s, B, p.bs_v, p.bs_ub));
     }
     cwi = nci;
     L = NL;
@@ -984,11 +1135,17 @@ opening:
   uint64_t off_poly = lay.rec(T_FINAL_POLY, (uint32_t)m, 16);
   uint64_t off_point = lay.rec(T_FINAL_POINT, ilog2(m), 16);
   uint64_t off_eval = lay.rec(T_FINAL_EVAL, 1, 16);
-  RUN(PC_PROTOCOL, 1,
-      k_final<<<1, 32, 0, s>>>(st, a, b, (int)m, tr, off_poly, off_point, off_eval, 0, st->fin_r));
+  {
+    BStr fb;  // (arr, b, tr)
+    fb.s[0] = ast;
+    fb.s[1] = bst;
+    fb.s[2] = trs;
+    RUN(PC_PROTOCOL, 1, k_final_b<<<B, 32, 0, s>>>(st, a, b, (int)m, tr, off_poly, off_point, off_eval, fb));
+  }
   // root of the last commitment (never opened) on the query stream
   if (!dry) GBZ_CUDA(cudaStreamWaitEvent(q, p.ev_commit[iter], 0));
-  RUN_ON(q, PC_MERKLE, 1, k_merkle_root<<<1, 32, 0, q>>>(p.cw[cwi], ilog2(L / 4), tr, off_root[iter]));
+  RUN_ON(q, PC_MERKLE, 1,
+         k_merkle_root_b<<<B, 32, 0, q>>>(p.cw[cwi], cw_s[cwi], ilog2(L / 4), tr, trs, off_root[iter]));
   if (!dry) {  // join the commit and query chains
     GBZ_CUDA(cudaEventRecord(p.ev_root_tail, q));
     GBZ_CUDA(cudaStreamWaitEvent(s, p.ev_commit[iter], 0));
@@ -1043,11 +1200,27 @@ namespace {
 __global__ void k_set_seed(ProofState *st, uint32_t seed) {
   if (threadIdx.x == 0) st->seed_in = seed;
 }
+struct SeedChunk {
+  uint32_t v[64];
+};
+__global__ void k_set_seeds(ProofState *st, SeedChunk c, int count) {
+  if ((int)threadIdx.x < count) st[threadIdx.x].seed_in = c.v[threadIdx.x];
+}
 }  // namespace
 
 void set_seed_launch(ProofPlan &p, uint32_t seed, cudaStream_t s) {
   k_set_seed<<<1, 32, 0, s>>>(p.st, seed);
   GBZ_CUDA(cudaGetLastError());
+}
+
+void set_seeds_launch(ProofPlan &p, const uint32_t *seeds, int count, cudaStream_t s) {
+  for (int o = 0; o < count; o += 64) {
+    SeedChunk c{};
+    const int k = std::min(64, count - o);
+    for (int i = 0; i < k; i++) c.v[i] = seeds[o + i];
+    k_set_seeds<<<1, 64, 0, s>>>(p.st + o, c, k);
+    GBZ_CUDA(cudaGetLastError());
+  }
 }
 
 void launch_proof_graph(ProofPlan &p, const fe *w, uint32_t prng_seed, cudaStream_t s) {
@@ -1114,11 +1287,13 @@ void launch_proof_graph(ProofPlan &p, const fe *w, uint32_t prng_seed, cudaStrea
   GBZ_CUDA(cudaGraphLaunch(g->exec, s));
 }
 
-uint64_t plan_bytes(int logn, int rate) {
+uint64_t plan_bytes(int logn, int rate, int batch) {
   const uint64_t n = 1ull << logn, L = n * (uint64_t)rate;
   uint64_t b = sizeof(fe) * (n + L + L / 2 + L + L / 2 + 5 * (n / 2) + n);
-  b += sizeof(fe) * (3 * (uint64_t)sc_blocks(n / 2) + kUpdateBetasScratch) + sizeof(ProofState);
-  b += 64ull << 20;  // transcript, twiddle tables and allocation granularity (upper bound)
+  b += sizeof(fe) * (6 * (uint64_t)sc_blocks(n / 2) + kUpdateBetasScratch) + sizeof(ProofState);
+  b *= (uint64_t)batch;
+  b += 64ull << 20;  // transcripts, twiddle tables and allocation granularity (upper bound)
+  b += (uint64_t)batch << 20;
   return b;
 }
 

@@ -51,9 +51,16 @@ struct ProofGraph {
 };
 
 // Device buffers and tables for proofs of one shape (n = 2^logn, rate).
+// A plan for a batch holds B proofs of the shape: every buffer below is B
+// copies back to back (bs_* their byte strides, the states B consecutive
+// ProofStates, the transcripts B copies of transcript_bytes), and every
+// launch of the proof covers the whole batch.
 struct ProofPlan {
   int logn = 0, rate = 0;
   uint64_t n = 0, L = 0;
+  int B = 1;
+  uint64_t bs_w = 0, bs_cw0 = 0, bs_cw1 = 0, bs_tmp = 0, bs_tmp2 = 0, bs_v = 0, bs_arr = 0, bs_beta = 0,
+           bs_part = 0, bs_ub = 0;
   fe *w = nullptr;                // witness staging (host-input proofs)
   fe *cw[2] = {nullptr, nullptr}; // codeword ping-pong (L, L/2)
   fe *tmp = nullptr;              // NTT intermediate of the commits (L)
@@ -109,8 +116,9 @@ __global__ void k_whir_paths(const uint8_t *tree, uint64_t leaves, int l, uint8_
 // of the tree over a codeword, the paths of l queries into it, and the
 // root and paths of a tree whose leaf hashes are all zero.
 __global__ void k_merkle_root(const fe *cw, int depth, uint8_t *tr, uint64_t off);
+// cws, trs: per-proof strides of a batch (grid.y = proof), 0 for one proof.
 __global__ void k_whir_paths_chain(const fe *cw, uint64_t leaves, int l, uint8_t *tr, uint64_t off_q,
-                                   uint64_t off_path);
+                                   uint64_t off_path, uint64_t cws, uint64_t trs);
 __global__ void k_zero_tree_root(int depth, uint8_t *tr, uint64_t off);
 __global__ void k_zero_tree_paths(int depth, int l, uint8_t *tr, uint64_t off_path);
 __global__ void k_final(ProofState *st, const fe *arr, const fe *b, int m, uint8_t *tr, uint64_t off_poly,
@@ -126,7 +134,7 @@ struct OpenOnly {
   glibc_prng prng;
 };
 
-std::unique_ptr<ProofPlan> plan_create(int logn, int rate);
+std::unique_ptr<ProofPlan> plan_create(int logn, int rate, int batch = 1);
 // Allocates the plan's buffer for openings alone, with its record headers
 // (once; the proof's layout and launch counts are left as they are).
 void plan_prepare_open(ProofPlan &p);
@@ -140,11 +148,13 @@ void plan_prepare_open(ProofPlan &p);
 void enqueue_proof(ProofPlan &p, const fe *witness, uint32_t prng_seed, cudaStream_t s, bool dry,
                    bool seed_in_state = false, const OpenOnly *open = nullptr);
 void set_seed_launch(ProofPlan &p, uint32_t seed, cudaStream_t s);
+// The seeds of the first count proofs of a batched plan (passed by value).
+void set_seeds_launch(ProofPlan &p, const uint32_t *seeds, int count, cudaStream_t s);
 // Enqueues one proof of the witness at w by replaying a captured graph
 // (captured on first use of this address; s must be a capturable stream).
 void launch_proof_graph(ProofPlan &p, const fe *w, uint32_t prng_seed, cudaStream_t s);
 // Device bytes a plan of this shape allocates (an upper bound).
-uint64_t plan_bytes(int logn, int rate);
+uint64_t plan_bytes(int logn, int rate, int batch = 1);
 // Reads the device-side consistency flags (synchronises s).
 uint32_t plan_error_flags(ProofPlan &p, cudaStream_t s);
 int whir_query_count(int rate);

@@ -3,6 +3,7 @@
 // assignment, and a serving loop that admits timed arrivals by slot
 // occupancy and free device memory.
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstring>
 #include <numeric>
@@ -104,7 +105,7 @@ void Scheduler::clear() {
 uint64_t Scheduler::cached_bytes() const {
   uint64_t b = 0;
   for (auto &sl : slots_)
-    for (auto &kv : sl.plans) b += plan_bytes(kv.first.first, kv.first.second);
+    for (auto &kv : sl.plans) b += plan_bytes(kv.first[0], kv.first[1], kv.first[2]);
   return b;
 }
 
@@ -119,9 +120,9 @@ void Scheduler::ensure_slots(int n) {
   }
 }
 
-bool Scheduler::evict_one_idle(int keep_slot, std::pair<int, int> keep_key) {
+bool Scheduler::evict_one_idle(int keep_slot, PlanKey keep_key) {
   int best_slot = -1;
-  std::pair<int, int> best_key;
+  PlanKey best_key{};
   uint64_t best_use = ~0ull;
   for (int l = 0; l < (int)slots_.size(); l++)
     for (auto &kv : slots_[l].plans) {
@@ -138,8 +139,8 @@ bool Scheduler::evict_one_idle(int keep_slot, std::pair<int, int> keep_key) {
   return true;
 }
 
-SlotPlan &Scheduler::plan_for(int slot, int logn, int rate, const SchedOpts &o) {
-  const auto key = std::make_pair(logn, rate);
+SlotPlan &Scheduler::plan_for(int slot, int logn, int rate, const SchedOpts &o, int batch) {
+  const PlanKey key{logn, rate, batch};
   auto &m = slots_[slot].plans;
   auto it = m.find(key);
   if (it != m.end()) {
@@ -148,7 +149,7 @@ SlotPlan &Scheduler::plan_for(int slot, int logn, int rate, const SchedOpts &o) 
   }
   // Admission by free device memory: evict idle cached plans (least
   // recently used first), then wait for busy slots to drain.
-  const uint64_t need = plan_bytes(logn, rate) + o.reserve;
+  const uint64_t need = plan_bytes(logn, rate, batch) + o.reserve;
   for (;;) {
     size_t fr = 0, tot = 0;
     GBZ_CUDA(cudaMemGetInfo(&fr, &tot));
@@ -168,7 +169,7 @@ SlotPlan &Scheduler::plan_for(int slot, int logn, int rate, const SchedOpts &o) 
                                  __FILE__, __LINE__);
   }
   std::unique_ptr<SlotPlan> sp(new SlotPlan());
-  sp->plan = plan_create(logn, rate);
+  sp->plan = plan_create(logn, rate, batch);
   GBZ_CUDA(cudaEventCreateWithFlags(&sp->idle, cudaEventDisableTiming));
   sp->last_use = ++tick_;
   SlotPlan &ref = *sp;
@@ -198,6 +199,37 @@ void Scheduler::enqueue(int slot, SlotPlan &sp, const ProofJob &j, int mem, bool
   }
   GBZ_CUDA(cudaMemcpyAsync(j.transcript, p.transcript, p.transcript_bytes, out_kind, s));
   GBZ_CUDA(cudaMemcpyAsync(err_slot, &p.st->error, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  GBZ_CUDA(cudaEventRecord(sp.idle, s));
+}
+
+void Scheduler::enqueue_group(int slot, SlotPlan &sp, const std::vector<ProofJob> &jobs, const std::vector<int> &idx,
+                              int mem, bool graphs, uint32_t *errors) {
+  ProofPlan &p = *sp.plan;
+  const cudaStream_t s = slots_[slot].s;
+  p.prof = nullptr;
+  const bool host = mem == 0;
+  const cudaMemcpyKind in_kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const cudaMemcpyKind out_kind = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (graphs && !sp.exec) capture(sp, s);
+  std::vector<uint32_t> seeds(idx.size());
+  for (size_t b = 0; b < idx.size(); b++) {
+    const ProofJob &j = jobs[idx[b]];
+    GBZ_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(p.w) + p.bs_w * b, j.witness, p.bs_w, in_kind, s));
+    seeds[b] = j.seed;
+  }
+  // the seeds every proof's k_init reads, as kernel arguments (a copy from
+  // pageable memory may wait for the stream)
+  set_seeds_launch(p, seeds.data(), (int)seeds.size(), s);
+  if (graphs) {
+    GBZ_CUDA(cudaGraphLaunch(sp.exec, s));
+  } else {
+    enqueue_proof(p, p.w, 0, s, false, /*seed_in_state=*/true);
+  }
+  for (size_t b = 0; b < idx.size(); b++) {
+    const ProofJob &j = jobs[idx[b]];
+    GBZ_CUDA(cudaMemcpyAsync(j.transcript, p.transcript + p.transcript_bytes * b, p.transcript_bytes, out_kind, s));
+    GBZ_CUDA(cudaMemcpyAsync(errors + idx[b], &p.st[b].error, sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  }
   GBZ_CUDA(cudaEventRecord(sp.idle, s));
 }
 
@@ -248,7 +280,56 @@ void Scheduler::run(const std::vector<ProofJob> &jobs_in, const double *arrival,
     for (int l = 0; l < lanes; l++) cudaStreamSynchronize(slots_[l].s);
   };
   try {
-    if (!arrival) {
+    if (!arrival && o.group) {
+      // Batch, grouped: the proofs of each shape are one batched plan (every
+      // launch covers all of them), the groups longest first over the
+      // slots; plans and graphs prepared before the clock starts.
+      std::map<std::pair<int, int>, std::vector<int>> groups;
+      for (int i = 0; i < nj; i++) groups[{jobs[i].logn, jobs[i].rate}].push_back(i);
+      // a group costing more than an even share of the whole batch is cut
+      // into that many equal sub-batches, so that one shape's chain does not
+      // set the makespan while other slots idle
+      double total = 0;
+      for (auto &kv : groups) total += proof_cost(kv.first.first, kv.first.second) * (double)kv.second.size();
+      const double share = total / lanes;
+      std::vector<std::vector<int>> units;
+      std::vector<double> cost;
+      for (auto &kv : groups) {
+        const double c1 = proof_cost(kv.first.first, kv.first.second);
+        const int cnt = (int)kv.second.size();
+        const int parts = std::max(1, std::min(cnt, (int)std::ceil(c1 * cnt / share)));
+        for (int k = 0; k < parts; k++) {
+          const int a = (int)((int64_t)cnt * k / parts), b = (int)((int64_t)cnt * (k + 1) / parts);
+          units.emplace_back(kv.second.begin() + a, kv.second.begin() + b);
+          cost.push_back(c1 * (double)(b - a));
+        }
+      }
+      const std::vector<int> asg = lpt_assign(cost, lanes);
+      std::vector<int> order(units.size());
+      std::iota(order.begin(), order.end(), 0);
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+      std::vector<std::vector<int>> per(lanes);
+      for (int u : order) per[asg[u]].push_back(u);
+      for (int l = 0; l < lanes; l++)
+        for (int u : per[l]) {
+          const ProofJob &j0 = jobs[units[u][0]];
+          SlotPlan &sp = plan_for(l, j0.logn, j0.rate, o, (int)units[u].size());
+          if (o.graphs && !sp.exec) capture(sp, slots_[l].s);
+        }
+      GBZ_CUDA(cudaEventRecord(ev.ev0, slots_[0].s));
+      for (int l = 1; l < lanes; l++) GBZ_CUDA(cudaStreamWaitEvent(slots_[l].s, ev.ev0, 0));
+      size_t longest = 0;
+      for (auto &v : per) longest = std::max(longest, v.size());
+      for (size_t k = 0; k < longest; k++)
+        for (int l = 0; l < lanes; l++) {
+          if (k >= per[l].size()) continue;
+          const std::vector<int> &idx = units[per[l][k]];
+          const ProofJob &j0 = jobs[idx[0]];
+          SlotPlan &sp = plan_for(l, j0.logn, j0.rate, o, (int)idx.size());
+          enqueue_group(l, sp, jobs, idx, mem, o.graphs, dev_errors_);
+          for (int i : idx) GBZ_CUDA(cudaEventRecord(ev.done[i], slots_[l].s));
+        }
+    } else if (!arrival) {
       // Batch: longest first over the slots, plans and graphs prepared
       // before the clock starts, then enqueued round-robin over the slots.
       std::vector<double> cost(nj);

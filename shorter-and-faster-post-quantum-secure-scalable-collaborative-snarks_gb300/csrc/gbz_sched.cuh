@@ -10,6 +10,7 @@
 // Proofs in different slots overlap on the device; their results do not
 // depend on the mix because nothing is shared between slots.
 #pragma once
+#include <array>
 #include <map>
 #include <memory>
 #include <vector>
@@ -20,6 +21,7 @@ namespace gbz {
 
 struct SchedOpts {
   int lanes = 8;                     // concurrent slots (streams)
+  bool group = true;                 // batch: proofs of one shape share every launch (a batched plan)
   int depth = 2;                     // serving: proofs queued per slot before admission waits
   bool graphs = true;                // replay a captured graph per (slot, shape)
   uint64_t reserve = 1ull << 30;     // device bytes left free when a new shape is admitted
@@ -53,10 +55,12 @@ struct SlotPlan {
   ~SlotPlan();
 };
 
+// A slot's plans by (log2 n, rate, proofs per launch).
+using PlanKey = std::array<int, 3>;
 struct Slot {
   cudaStream_t s = nullptr;
   bool high = false;                 // created with the device's greatest stream priority
-  std::map<std::pair<int, int>, std::unique_ptr<SlotPlan>> plans;
+  std::map<PlanKey, std::unique_ptr<SlotPlan>> plans;
 };
 
 class Scheduler {
@@ -92,9 +96,13 @@ class Scheduler {
   uint64_t staging_cap_ = 0;
 
   void ensure_slots(int n);
-  SlotPlan &plan_for(int slot, int logn, int rate, const SchedOpts &o);
-  bool evict_one_idle(int keep_slot, std::pair<int, int> keep_key);
+  SlotPlan &plan_for(int slot, int logn, int rate, const SchedOpts &o, int batch = 1);
+  bool evict_one_idle(int keep_slot, PlanKey keep_key);
   void enqueue(int slot, SlotPlan &sp, const ProofJob &j, int mem, bool graphs, uint32_t *err_slot);
+  // Proofs of one shape as one batched plan (its B = idx.size()): every
+  // launch of the proof covers all of them.
+  void enqueue_group(int slot, SlotPlan &sp, const std::vector<ProofJob> &jobs, const std::vector<int> &idx, int mem,
+                     bool graphs, uint32_t *errors);
 };
 
 // Longest-processing-time assignment of jobs with the given costs to

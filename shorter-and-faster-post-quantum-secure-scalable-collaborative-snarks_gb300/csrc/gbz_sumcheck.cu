@@ -116,7 +116,16 @@ sc_fold_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t m, c
 // m/4.  One read of (a, b) instead of three passes.
 __global__ void __launch_bounds__(kScThreads)
 sc_fold2_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t m, const fe *chal0, const fe *chal1,
-                fe *__restrict__ a4, fe *__restrict__ b4, fe *partial0, fe *partial1) {
+                fe *__restrict__ a4, fe *__restrict__ b4, fe *partial0, fe *partial1, BStr bs) {
+  const uint32_t pb = blockIdx.y;
+  a = badv(a, bs.s[0], pb);
+  b = badv(b, bs.s[1], pb);
+  chal0 = badv(chal0, bs.s[2], pb);
+  chal1 = badv(chal1, bs.s[3], pb);
+  a4 = badv(a4, bs.s[4], pb);
+  b4 = badv(b4, bs.s[5], pb);
+  partial0 = badv(partial0, bs.s[6], pb);
+  partial1 = badv(partial1, bs.s[7], pb);
   const fe r0 = *chal0, r1 = *chal1;
   fe A0 = fe_zero(), C0 = fe_zero(), D0 = fe_zero(), A1 = fe_zero(), C1 = fe_zero(), D1 = fe_zero();
   const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
@@ -157,7 +166,17 @@ sc_fold2_kernel(const fe *__restrict__ a, const fe *__restrict__ b, uint64_t m, 
 // eq1(c0, r0); b4 = lambda0 lambda1 E2 (lambda1 = eq1(c1, r1)).
 __global__ void __launch_bounds__(kScThreads)
 sc_fold2_eq_kernel(const fe *__restrict__ a, const fe *__restrict__ E2, uint64_t m, const fe *c, const fe *chal0,
-                   const fe *chal1, fe *__restrict__ a4, fe *__restrict__ b4, fe *partial0, fe *partial1) {
+                   const fe *chal1, fe *__restrict__ a4, fe *__restrict__ b4, fe *partial0, fe *partial1, BStr bs) {
+  const uint32_t pb = blockIdx.y;
+  a = badv(a, bs.s[0], pb);
+  E2 = badv(E2, bs.s[1], pb);
+  c = badv(c, bs.s[2], pb);
+  chal0 = badv(chal0, bs.s[3], pb);
+  chal1 = badv(chal1, bs.s[4], pb);
+  a4 = badv(a4, bs.s[5], pb);
+  b4 = badv(b4, bs.s[6], pb);
+  partial0 = badv(partial0, bs.s[7], pb);
+  partial1 = badv(partial1, bs.s[8], pb);
   const fe r0 = *chal0, r1 = *chal1, c0 = c[0], c1 = c[1];
   const fe e0 = fsub(fe_one(), c0), f0 = fsub(fe_one(), c1);
   const fe lam0 = fadd(fmul(r0, fsub(c0, e0)), e0), lam1 = fadd(fmul(r1, fsub(c1, f0)), f0);
@@ -215,7 +234,11 @@ sc_fold2_eq_kernel(const fe *__restrict__ a, const fe *__restrict__ E2, uint64_t
 // E_{i+1}[t] = E_i[2t] + E_i[2t+1].
 // partial[3 blk + {0, 1, 2}] = (S0, S1, 0).
 __global__ void __launch_bounds__(kScThreads)
-sc_eq_reduce_kernel(const fe *__restrict__ a, const fe *__restrict__ E, uint64_t pairs, fe *partial) {
+sc_eq_reduce_kernel(const fe *__restrict__ a, const fe *__restrict__ E, uint64_t pairs, fe *partial, BStr bs) {
+  const uint32_t pb = blockIdx.y;
+  a = badv(a, bs.s[0], pb);
+  E = badv(E, bs.s[1], pb);
+  partial = badv(partial, bs.s[2], pb);
   fe S0 = fe_zero(), S1 = fe_zero(), Z = fe_zero();
   const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
   for (uint64_t j = (uint64_t)blockIdx.x * kScThreads + threadIdx.x; j < pairs; j += stride) {
@@ -240,7 +263,14 @@ sc_eq_reduce_kernel(const fe *__restrict__ a, const fe *__restrict__ E, uint64_t
 // by pairwise sums, and (reduce) the S sums of the folded pairs with E2.
 __global__ void __launch_bounds__(kScThreads)
 sc_eq_fold_kernel(const fe *__restrict__ a, uint64_t m, const fe *chal, fe *__restrict__ a2,
-                  const fe *__restrict__ E, fe *__restrict__ E2, int reduce, fe *partial) {
+                  const fe *__restrict__ E, fe *__restrict__ E2, int reduce, fe *partial, BStr bs) {
+  const uint32_t pb = blockIdx.y;
+  a = badv(a, bs.s[0], pb);
+  chal = badv(chal, bs.s[1], pb);
+  a2 = badv(a2, bs.s[2], pb);
+  E = badv(E, bs.s[3], pb);
+  E2 = badv(E2, bs.s[4], pb);
+  partial = badv(partial, bs.s[5], pb);
   const fe r = *chal;
   fe S0 = fe_zero(), S1 = fe_zero(), Z = fe_zero();
   const uint64_t stride = (uint64_t)gridDim.x * kScThreads;
@@ -297,9 +327,11 @@ __global__ void __launch_bounds__(kScThreads) sc_sum_kernel(const fe *partial, i
 // T[2j] = T[j] - T[j] r_i, one product per entry) and writes the block with
 // coalesced 16-byte stores.
 constexpr int kBetaBlockLog = 11;
-__global__ void __launch_bounds__(256) beta_block_kernel(const fe *r, int nr, fe *B) {
+__global__ void __launch_bounds__(256) beta_block_kernel(const fe *r, int nr, fe *B, BStr bs) {
   __shared__ fe T[1 << kBetaBlockLog];
   __shared__ fe rs[64];
+  r = badv(r, bs.s[0], blockIdx.y);
+  B = badv(B, bs.s[1], blockIdx.y);
   const int low = nr < kBetaBlockLog ? nr : kBetaBlockLog;
   if ((int)threadIdx.x < nr) rs[threadIdx.x] = r[threadIdx.x];
   __syncthreads();
@@ -337,10 +369,12 @@ __global__ void __launch_bounds__(256) beta_block_kernel(const fe *r, int nr, fe
 // each), so every output entry costs one product and the serial part of a
 // CTA is amortised over 2^15 entries.
 constexpr int kBetaChunksLog = 4;  // at most 16 blocks of 2^11 entries per CTA
-__global__ void __launch_bounds__(256) beta_tensor_kernel(const fe *r, int nr, int chunks_log, fe *B) {
+__global__ void __launch_bounds__(256) beta_tensor_kernel(const fe *r, int nr, int chunks_log, fe *B, BStr bs) {
   __shared__ fe T[1 << kBetaBlockLog];
   __shared__ fe hi_pre[1 << kBetaChunksLog];
   __shared__ fe rs[64];
+  r = badv(r, bs.s[0], blockIdx.y);
+  B = badv(B, bs.s[1], blockIdx.y);
   if ((int)threadIdx.x < nr) rs[threadIdx.x] = r[threadIdx.x];
   __syncthreads();
   if (threadIdx.x < (1u << chunks_log)) {
@@ -392,16 +426,21 @@ constexpr int kUbWarps = kUbThreads / 32;
 constexpr int kUbPer = 8;
 constexpr int kUbSpan = 32 * kUbPer;
 
-__global__ void __launch_bounds__(kUbThreads) ub_table_kernel(const ProofState *st, int l, fe *pw) {
+__global__ void __launch_bounds__(kUbThreads) ub_table_kernel(const ProofState *st, int l, fe *pw, BStr bs) {
   // pw[i*32 + L] = w_i^(L * kUbPer)
+  st = badv(st, bs.s[0], blockIdx.y);
+  pw = badv(pw, bs.s[1], blockIdx.y);
   const int i = blockIdx.x, t = threadIdx.x;
   if (i >= l || t >= 32) return;
   pw[i * 32 + t] = fpow(st->omega_q[i], (uint64_t)t * kUbPer);
 }
 
 __global__ void __launch_bounds__(kUbThreads)
-ub_kernel(fe *b, uint64_t nb, const ProofState *st, int l, const fe *pw) {
+ub_kernel(fe *b, uint64_t nb, const ProofState *st, int l, const fe *pw, BStr bs) {
   __shared__ fe s_start[kMaxQueries], s_w[kMaxQueries];
+  b = badv(b, bs.s[0], blockIdx.y);
+  st = badv(st, bs.s[1], blockIdx.y);
+  pw = badv(pw, bs.s[2], blockIdx.y);
   __shared__ fe part[kUbWarps][kUbSpan];
   const uint64_t cta0 = (uint64_t)blockIdx.x * kUbSpan;
   for (int i = threadIdx.x; i < l; i += kUbThreads) {
@@ -455,25 +494,38 @@ void sc_step_launch(const fe *a, const fe *b, uint64_t m, const fe *chal, fe *a2
 }
 
 void sc_fold2_launch(const fe *a, const fe *b, uint64_t m, const fe *chal0, const fe *chal1, fe *a4, fe *b4,
-                     fe *partial0, fe *partial1, int blocks, cudaStream_t s) {
+                     fe *partial0, fe *partial1, int blocks, cudaStream_t s, int batch, const BStr &bs) {
   if (m < 4) throw ArgError("two-round fold needs at least 4 entries");
-  sc_fold2_kernel<<<blocks, kScThreads, 0, s>>>(a, b, m, chal0, chal1, a4, b4, partial0, partial1);
+  sc_fold2_kernel<<<dim3(blocks, batch), kScThreads, 0, s>>>(a, b, m, chal0, chal1, a4, b4, partial0, partial1, bs);
   GBZ_CUDA(cudaGetLastError());
 }
 
 void sc_fold2_eq_launch(const fe *a, const fe *E2, uint64_t m, const fe *c, const fe *chal0, const fe *chal1, fe *a4,
-                        fe *b4, fe *partial0, fe *partial1, int blocks, cudaStream_t s) {
+                        fe *b4, fe *partial0, fe *partial1, int blocks, cudaStream_t s, int batch, const BStr &bs) {
   if (m < 4) throw ArgError("two-round fold needs at least 4 entries");
-  sc_fold2_eq_kernel<<<blocks, kScThreads, 0, s>>>(a, E2, m, c, chal0, chal1, a4, b4, partial0, partial1);
+  sc_fold2_eq_kernel<<<dim3(blocks, batch), kScThreads, 0, s>>>(a, E2, m, c, chal0, chal1, a4, b4, partial0,
+                                                                partial1, bs);
   GBZ_CUDA(cudaGetLastError());
 }
 
 void sc_eq_step_launch(const fe *a, const fe *E, uint64_t m, const fe *chal, fe *a2, fe *E2, bool reduce,
-                       fe *partial, int blocks, cudaStream_t s) {
+                       fe *partial, int blocks, cudaStream_t s, int batch, const BStr &bs) {
+  // bs: strides of (a, E, chal, a2, E2, partial)
   if (!chal) {
-    sc_eq_reduce_kernel<<<blocks, kScThreads, 0, s>>>(a, E, m / 2, partial);
+    BStr r;
+    r.s[0] = bs.s[0];
+    r.s[1] = bs.s[1];
+    r.s[2] = bs.s[5];
+    sc_eq_reduce_kernel<<<dim3(blocks, batch), kScThreads, 0, s>>>(a, E, m / 2, partial, r);
   } else {
-    sc_eq_fold_kernel<<<blocks, kScThreads, 0, s>>>(a, m, chal, a2, E, E2, reduce ? 1 : 0, partial);
+    BStr f;
+    f.s[0] = bs.s[0];
+    f.s[1] = bs.s[2];
+    f.s[2] = bs.s[3];
+    f.s[3] = bs.s[1];
+    f.s[4] = bs.s[4];
+    f.s[5] = bs.s[5];
+    sc_eq_fold_kernel<<<dim3(blocks, batch), kScThreads, 0, s>>>(a, m, chal, a2, E, E2, reduce ? 1 : 0, partial, f);
   }
   GBZ_CUDA(cudaGetLastError());
 }
@@ -483,26 +535,38 @@ void sc_sum_launch(const fe *partial, int blocks, fe *out3, cudaStream_t s) {
   GBZ_CUDA(cudaGetLastError());
 }
 
-void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s) {
+void beta_launch(const fe *r, int nr, fe *B, cudaStream_t s, int batch, uint64_t r_stride, uint64_t B_stride) {
   if (nr < 0 || nr > 60) throw ArgError("beta table: bad number of variables");
+  BStr bs;
+  bs.s[0] = r_stride;
+  bs.s[1] = B_stride;
   if (nr >= kBetaBlockLog + 4) {
     // enough CTAs to cover the SMs (at least 2^9), up to 16 blocks each
     const int chunks_log = std::max(0, std::min(kBetaChunksLog, nr - kBetaBlockLog - 9));
-    beta_tensor_kernel<<<(unsigned)(1ull << (nr - kBetaBlockLog - chunks_log)), 256, 0, s>>>(r, nr, chunks_log, B);
+    beta_tensor_kernel<<<dim3((unsigned)(1ull << (nr - kBetaBlockLog - chunks_log)), batch), 256, 0, s>>>(
+        r, nr, chunks_log, B, bs);
     GBZ_CUDA(cudaGetLastError());
     return;
   }
   const int low = nr < kBetaBlockLog ? nr : kBetaBlockLog;
-  beta_block_kernel<<<(unsigned)(1ull << (nr - low)), 256, 0, s>>>(r, nr, B);
+  beta_block_kernel<<<dim3((unsigned)(1ull << (nr - low)), batch), 256, 0, s>>>(r, nr, B, bs);
   GBZ_CUDA(cudaGetLastError());
 }
 
-void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s) {
+void update_betas_launch(fe *b, uint64_t nb, const ProofState *st, int l, fe *pw_scratch, cudaStream_t s, int batch,
+                         uint64_t b_stride, uint64_t pw_stride) {
   if (l <= 0) return;
   if (l > kMaxQueries) throw ArgError("update_betas: too many queries");
-  ub_table_kernel<<<l, 32, 0, s>>>(st, l, pw_scratch);
+  BStr t, u;
+  t.s[0] = sizeof(ProofState);
+  t.s[1] = pw_stride;
+  u.s[0] = b_stride;
+  u.s[1] = sizeof(ProofState);
+  u.s[2] = pw_stride;
+  if (batch == 1) t = u = BStr();
+  ub_table_kernel<<<dim3(l, batch), 32, 0, s>>>(st, l, pw_scratch, t);
   GBZ_CUDA(cudaGetLastError());
-  ub_kernel<<<(unsigned)((nb + kUbSpan - 1) / kUbSpan), kUbThreads, 0, s>>>(b, nb, st, l, pw_scratch);
+  ub_kernel<<<dim3((unsigned)((nb + kUbSpan - 1) / kUbSpan), batch), kUbThreads, 0, s>>>(b, nb, st, l, pw_scratch, u);
   GBZ_CUDA(cudaGetLastError());
 }
 

@@ -50,7 +50,7 @@ EXPORTS = (
     "gbz_whir_batch_schedule", "gbz_whir_batch_open", "gbz_pcs_schedule", "gbz_pcs_commit", "gbz_pcs_free",
     "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open", "gbz_pcs_claim", "gbz_cosumcheck",
     "gbz_cosumcheck_transcript_bytes", "gbz_whir_open", "gbz_whir_open_transcript_bytes",
-    "gbz_merkle_tree_from_leaves", "gbz_pcs_open_full", "gbz_pcs_open_full_bytes",
+    "gbz_merkle_tree_from_leaves", "gbz_pcs_open_full", "gbz_pcs_open_full_bytes", "gbz_sched_set_grouping",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -179,6 +179,7 @@ def _load():
         "gbz_merkle_tree_from_leaves": (c_int, [vp, vp, u64, vp, c_int]),
         "gbz_pcs_open_full": (c_int, [vp, vp, vp, c_int, vp, vp, vp, vp, vp, u64, c_int]),
         "gbz_pcs_open_full_bytes": (c_int, [vp, vp]),
+        "gbz_sched_set_grouping": (c_int, [vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -428,6 +429,10 @@ class Context:
         """Timed arrivals (seconds from the call) through the serving loop
         (gbz_serve).  Returns (transcripts, latencies, makespan)."""
         return self._prove_many(arrivals, witnesses, logns, rates, seeds, lanes, depth, graphs, reserve, out)
+
+    def set_grouping(self, on):
+        """Whether prove_batch shares every launch among the proofs of one shape."""
+        self.check(lib.gbz_sched_set_grouping(self.h, int(bool(on))))
 
     def sched_release(self):
         b = ctypes.c_uint64()

@@ -41,6 +41,27 @@ def test_batch_equals_alone(ctx, alone, lanes, graphs):
     assert np.all(lat > 0) and mk >= lat.max() - 1e-9
 
 
+@pytest.mark.parametrize("grouped", [True, False])
+def test_batch_groups_of_one_shape(ctx, oracle, grouped):
+    """Many proofs of a few shapes: grouped, every launch covers a whole
+    shape group (batched plans); the transcripts are the ones each proof
+    gives alone, with and without graph replay.  The shapes reach the sparse
+    update_betas transform (2^16 at rate 4, 2^17 at rate 2), the one-CTA
+    sumcheck tail (2^10) and the first fold without the eq table (2^3)."""
+    shapes = [(12, 4)] * 9 + [(16, 4)] * 5 + [(17, 2)] * 3 + [(10, 8)] * 2 + [(3, 2)] * 2
+    ws, ln, rt, sd = _mix(oracle, shapes, seed0=9100)
+    ref = [ctx.prove(w, l, r, s).tobytes() for w, l, r, s in zip(ws, ln, rt, sd)]
+    ctx.set_grouping(grouped)
+    try:
+        for graphs in (True, False):
+            out, lat, mk = ctx.prove_batch(ws, ln, rt, sd, lanes=4, graphs=graphs)
+            for k in range(len(ws)):
+                assert out[k].tobytes() == ref[k], "proof %d (2^%d, rate %d) differs" % (k, ln[k], rt[k])
+            assert np.all(lat > 0) and mk >= lat.max() - 1e-9
+    finally:
+        ctx.set_grouping(True)
+
+
 def test_batch_repeat_uses_cached_graphs(ctx, alone):
     ws, ln, rt, sd, ref = alone
     for _ in range(3):
