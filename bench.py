@@ -344,7 +344,7 @@ def c5_requests(n_req, lam, seed=0x5EEF5):
     return arrivals, logns, rates
 
 
-def run_many(gbz, O, ctx, repeats):
+def run_many(gbz, O, ctx, repeats, served=True):
     """Batched (C3) and served (C5) proving against the plain prover (one
     gbz_prove call per proof, synchronised) on the same jobs, pinned host
     buffers, transcripts compared byte for byte."""
@@ -400,6 +400,8 @@ def run_many(gbz, O, ctx, repeats):
         "ungrouped_proofs_per_s": ungrouped, "ungrouped_makespan_ms": 1e3 * mk_u,
         "bit_identical_to_plain": same_g and same_u,
     }
+    if not served:
+        return out
     # ---- C5: serving at 200 requests/s, and at saturation (all at once)
     arrivals, slog, srate = c5_requests(400, 200.0)
     sws = [witness(l, 5) for l in slog]
@@ -801,6 +803,8 @@ def main():
     ap.add_argument("--rows-shift", type=int, default=0, help="divide the per-row sizes by 2^k")
     ap.add_argument("--parties-only", action="store_true", help="only the party-shares (coPCS) measurement")
     ap.add_argument("--parties-repeats", type=int, default=3, help="timed repeats of the party-shares run")
+    ap.add_argument("--batch-only", action="store_true", help="only the batched (64 mixed proofs) measurement")
+    ap.add_argument("--batch-repeats", type=int, default=3, help="timed repeats of the batched measurement")
     args = ap.parse_args()
     ws, rank, local = dist_info()
     if ws > 1:
@@ -832,6 +836,10 @@ def main():
 
     if args.parties_only:
         print(json.dumps(run_party_shares(gbz, O, ctx, repeats=args.parties_repeats)), flush=True)
+        ctx.close()
+        return
+    if args.batch_only:
+        print(json.dumps(run_many(gbz, O, ctx, args.batch_repeats, served=False)), flush=True)
         ctx.close()
         return
 
