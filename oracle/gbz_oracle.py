@@ -301,6 +301,25 @@ def secret_shares(v, N, privacy=False, prng_seed=1):
     return out
 
 
+def generate_randomness(g, n):
+    """generate_randomness (utils.cpp:1285-1295) drawing from the Prng g:
+    c = random() every 100 entries, entry = c + rand()."""
+    out = fe_array(n)
+    lib().orc_generate_randomness(ctypes.byref(g.s), ctypes.c_int64(n), _p64(out))
+    return out
+
+
+def secret_shares_from(v, N, g, privacy=True):
+    """compute_secret_shares(v, ·, N, N/4, N/2, privacy) (MPI_utils.cpp:2738-2766),
+    the privacy entries drawn from the Prng g: N x len(v)/(N/4) shares."""
+    v = np.ascontiguousarray(v, dtype=np.uint64).reshape(-1, 2)
+    M = v.shape[0]
+    out = np.zeros((N, M // (N // 4), 2), dtype=np.uint64)
+    lib().orc_secret_shares_g(_p64(v), ctypes.c_int64(M), ctypes.c_int(N), ctypes.c_int(int(privacy)),
+                              ctypes.byref(g.s), _p64(out))
+    return out
+
+
 def copcs_party_shares(N, M, R, state=False):
     """Party shares of the reference's coPCS test (main.cpp:49-68) at N
     parties: (shares N x 4M/N, random N x 4R/N), rank 0's glibc draws; with

@@ -11,6 +11,7 @@
 // then `count` payload units: 16-byte field elements {real, img} for field
 // vectors, 32-byte digests for hashes, u32 words for index lists.
 #include "config_pc.hpp"
+#include "coPCS.h"
 #include "merkle_tree.h"
 #include <cstdint>
 #include <cstdio>
@@ -27,6 +28,10 @@ namespace {
 
 FILE *g_log = nullptr;
 bool g_tried = false;
+// glibc generator: the seed of the last srand/srandom (1 = never seeded) and
+// the draws since then
+uint32_t g_seed = 1;
+uint64_t g_draws = 0;
 
 FILE *log_file() {
   if (g_tried) return g_log;
@@ -108,8 +113,30 @@ F __wrap__ZN5virgo12fieldElement7_randomEv() {
 int __real_rand(void);
 int __wrap_rand(void) {
   int r = __real_rand();
+  g_draws++;
   put_words("RAND", vector<uint32_t>{(uint32_t)r});
   return r;
+}
+
+// glibc random(), srand(), srandom(): counted, not logged (rand() and
+// random() advance the same generator), so that a record can say how far
+// the generator stood from its last seeding when a dealing step began.
+long __real_random(void);
+long __wrap_random(void) {
+  g_draws++;
+  return __real_random();
+}
+void __real_srand(unsigned s);
+void __wrap_srand(unsigned s) {
+  g_seed = s;
+  g_draws = 0;
+  __real_srand(s);
+}
+void __real_srandom(unsigned s);
+void __wrap_srandom(unsigned s) {
+  g_seed = s;
+  g_draws = 0;
+  __real_srandom(s);
 }
 
 // MPI_utils.cpp:2787  secret_share_coefficients(vector<F>& w, int M, int N, int _k, int k)
@@ -312,6 +339,224 @@ F __wrap__Z15evaluate_vectorSt6vectorIN5virgo12fieldElementESaIS1_EES3_(vector<F
   len.img = 0;
   put_field("EVLV", vector<F>{len, out});
   return out;
+}
+
+// ---- the R1CS front end's first and second sumcheck phases (pigeon 1:
+// coPIOP_prove, coPIOP.cpp:1382-1648).  Recorded only when
+// MINIMPI_CAPTURE_PIOP is set, so the other captures keep their streams.
+}  // extern "C"
+
+extern vector<vector<F>> ip_vec;                         // coSumcheck.cpp:230
+extern vector<F> sumcheck1_ip, sumcheck2_ip, sumcheck3_ip;  // coPIOP.cpp:57
+extern F prev_challenge;                                 // Fiat_Shamir.cpp:5
+extern int logm, logn, mask_l;                           // coPIOP.cpp:19,45
+
+namespace {
+
+bool piop_on() {
+  static int on = -1;
+  if (on < 0) on = std::getenv("MINIMPI_CAPTURE_PIOP") != nullptr;
+  return on == 1;
+}
+
+// where the generator stood: {point, seed, draws since the seed (low, high)}
+void put_draws(uint32_t point) {
+  put_words("RNCT", vector<uint32_t>{point, g_seed, (uint32_t)g_draws, (uint32_t)(g_draws >> 32)});
+}
+
+vector<F> flat(const vector<vector<F>> &v) {
+  vector<F> out;
+  for (auto &x : v) out.insert(out.end(), x.begin(), x.end());
+  return out;
+}
+
+// claims as their values then points, with the point lengths beside
+void put_claims(const char tv[4], const char tn[4], const vector<pair<F, vector<F>>> &c) {
+  vector<F> v;
+  vector<uint32_t> n;
+  for (auto &x : c) {
+    v.push_back(x.first);
+    v.insert(v.end(), x.second.begin(), x.second.end());
+    n.push_back((uint32_t)x.second.size());
+  }
+  put_field(tv, v);
+  put_words(tn, n);
+}
+
+void put_ints(const char tag[4], const vector<int> &v) {
+  vector<uint32_t> w(v.begin(), v.end());
+  put_words(tag, w);
+}
+
+}  // namespace
+
+extern "C" {
+
+// MPI_utils.cpp:2813  distribute_proving_data(vL, vR, vO, w, N, M, _k, k, cir_type)
+void __real__Z23distribute_proving_dataRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S4_S4_iiiii(
+    vector<F> &vL, vector<F> &vR, vector<F> &vO, vector<F> &w, int N, int M, int _k, int k, int t);
+void __wrap__Z23distribute_proving_dataRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S4_S4_iiiii(
+    vector<F> &vL, vector<F> &vR, vector<F> &vO, vector<F> &w, int N, int M, int _k, int k, int t) {
+  if (piop_on()) {
+    put_draws(1);
+    put_words("PLMN", vector<uint32_t>{(uint32_t)logm, (uint32_t)logn, (uint32_t)mask_l});
+  }
+  __real__Z23distribute_proving_dataRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S4_S4_iiiii(vL, vR, vO, w, N, M, _k, k,
+                                                                                           t);
+  if (piop_on()) {
+    put_field("DPDL", vL);
+    put_field("DPDR", vR);
+    put_field("DPDO", vO);
+    put_field("DPDW", w);
+  }
+}
+
+// MPI_utils.cpp:3633  generate_sumcheck_randomness(R, degrees1, degrees2, N)
+F __real__Z28generate_sumcheck_randomnessRSt6vectorIS_IS_IN5virgo12fieldElementESaIS1_EESaIS3_EESaIS5_EES_IiSaIiEESA_i(
+    vector<vector<vector<F>>> &R, vector<int> d1, vector<int> d2, int N);
+F __wrap__Z28generate_sumcheck_randomnessRSt6vectorIS_IS_IN5virgo12fieldElementESaIS1_EESaIS3_EESaIS5_EES_IiSaIiEESA_i(
+    vector<vector<vector<F>>> &R, vector<int> d1, vector<int> d2, int N) {
+  if (piop_on()) put_draws(2);
+  F K = __real__Z28generate_sumcheck_randomnessRSt6vectorIS_IS_IN5virgo12fieldElementESaIS1_EESaIS3_EESaIS5_EES_IiSaIiEESA_i(
+      R, d1, d2, N);
+  if (piop_on()) {
+    put_field("GSR0", flat(R[0]));
+    put_field("GSR1", flat(R[1]));
+    put_field("GSRK", vector<F>{K});
+  }
+  return K;
+}
+
+// MPI_utils.cpp:2868  setup_randomness(R, N, _k, k, size)
+void __real__Z16setup_randomnessRSt6vectorIN5virgo12fieldElementESaIS1_EEiiii(vector<F> &R, int N, int _k, int k,
+                                                                              int size);
+void __wrap__Z16setup_randomnessRSt6vectorIN5virgo12fieldElementESaIS1_EEiiii(vector<F> &R, int N, int _k, int k,
+                                                                              int size) {
+  if (piop_on()) {
+    put_draws(3);
+    put_words("SURN", vector<uint32_t>{(uint32_t)size});
+  }
+  __real__Z16setup_randomnessRSt6vectorIN5virgo12fieldElementESaIS1_EEiiii(R, N, _k, k, size);
+  if (piop_on()) put_field("SURO", R);
+}
+
+// coPCS.cpp  PCS_commit(C, codeword, Commit_data, witness, randomness, rate, N)
+void __real__Z10PCS_commitR2MTRSt6vectorIS1_IN5virgo12fieldElementESaIS3_EESaIS5_EES8_RS5_S9_S1_IS1_IiSaIiEESaISB_EEi(
+    MT &C, vector<vector<F>> &cw, vector<vector<F>> &cd, vector<F> &w, vector<F> &rnd, vector<vector<int>> rate, int N);
+void __wrap__Z10PCS_commitR2MTRSt6vectorIS1_IN5virgo12fieldElementESaIS3_EESaIS5_EES8_RS5_S9_S1_IS1_IiSaIiEESaISB_EEi(
+    MT &C, vector<vector<F>> &cw, vector<vector<F>> &cd, vector<F> &w, vector<F> &rnd, vector<vector<int>> rate, int N) {
+  if (piop_on()) {
+    put_draws(4);
+    put_field("PCWI", w);
+    put_field("PCRI", rnd);
+  }
+  __real__Z10PCS_commitR2MTRSt6vectorIS1_IN5virgo12fieldElementESaIS3_EESaIS5_EES8_RS5_S9_S1_IS1_IiSaIiEESaISB_EEi(
+      C, cw, cd, w, rnd, rate, N);
+  if (piop_on()) {
+    vector<uint32_t> rows;
+    for (auto &r : cd) rows.push_back((uint32_t)r.size());
+    put_words("PCCN", rows);
+    put_field("PCCD", flat(cd));
+    put_field("PCFS", vector<F>{prev_challenge});
+  }
+}
+
+// MPI_utils.cpp:3620  compute_Kr(R, b, N)
+F __real__Z10compute_KrRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES3_i(vector<vector<F>> &R, vector<F> b,
+                                                                                int N);
+F __wrap__Z10compute_KrRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES3_i(vector<vector<F>> &R, vector<F> b,
+                                                                                int N) {
+  F K = __real__Z10compute_KrRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES3_i(R, b, N);
+  if (piop_on()) put_field("CKRO", vector<F>{K});
+  return K;
+}
+
+// coSumcheck.cpp:335  cubic_coSumcheck(p1, p2, p3, r1, r2, R, K, K_r, degrees, N, ps)
+vector<pair<F, vector<F>>> __real__Z16cubic_coSumcheckRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S4_S4_S4_S_IS3_SaIS3_EES1_S1_S_IiSaIiEEiRd(
+    vector<F> &p1, vector<F> &p2, vector<F> &p3, vector<F> &r1, vector<F> &r2, vector<vector<F>> R, F K, F K_r,
+    vector<int> degrees, int N, double &ps);
+vector<pair<F, vector<F>>> __wrap__Z16cubic_coSumcheckRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S4_S4_S4_S_IS3_SaIS3_EES1_S1_S_IiSaIiEEiRd(
+    vector<F> &p1, vector<F> &p2, vector<F> &p3, vector<F> &r1, vector<F> &r2, vector<vector<F>> R, F K, F K_r,
+    vector<int> degrees, int N, double &ps) {
+  if (piop_on()) {
+    put_field("CBP1", p1);
+    put_field("CBP2", p2);
+    put_field("CBP3", p3);
+    put_field("CBR1", r1);
+    put_field("CBR2", r2);
+    put_field("CBRR", flat(R));
+    put_field("CBKK", vector<F>{K, K_r});
+    put_ints("CBDG", degrees);
+  }
+  vector<pair<F, vector<F>>> c =
+      __real__Z16cubic_coSumcheckRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S4_S4_S4_S_IS3_SaIS3_EES1_S1_S_IiSaIiEEiRd(
+          p1, p2, p3, r1, r2, R, K, K_r, degrees, N, ps);
+  if (piop_on()) {
+    put_claims("CBCL", "CBCN", c);
+    put_field("CBIP", flat(ip_vec));
+  }
+  return c;
+}
+
+// Distributed_Sumcheck.cpp:2283  _reduce_R1CS_matrixes_multivariate(size, r, RA, RB, RC, degrees, N)
+void __real__Z34_reduce_R1CS_matrixes_multivariatemSt6vectorIN5virgo12fieldElementESaIS1_EERS3_S4_S4_S_IiSaIiEEi(
+    size_t size, vector<F> r, vector<F> &RA, vector<F> &RB, vector<F> &RC, vector<int> degrees, int N);
+void __wrap__Z34_reduce_R1CS_matrixes_multivariatemSt6vectorIN5virgo12fieldElementESaIS1_EERS3_S4_S4_S_IiSaIiEEi(
+    size_t size, vector<F> r, vector<F> &RA, vector<F> &RB, vector<F> &RC, vector<int> degrees, int N) {
+  if (piop_on()) {
+    put_field("RDIR", r);
+    put_ints("RDDG", degrees);
+    // the first sumcheck's inner-product vector, final after prove_phase1
+    put_field("SIP1", sumcheck1_ip);
+  }
+  __real__Z34_reduce_R1CS_matrixes_multivariatemSt6vectorIN5virgo12fieldElementESaIS1_EERS3_S4_S4_S_IiSaIiEEi(
+      size, r, RA, RB, RC, degrees, N);
+  if (piop_on()) {
+    put_field("RDRA", RA);
+    put_field("RDRB", RB);
+    put_field("RDRC", RC);
+  }
+}
+
+// Distributed_Sumcheck.cpp:2352  secret_share_vector(v, _k, k, N)
+void __real__Z19secret_share_vectorRSt6vectorIN5virgo12fieldElementESaIS1_EEiii(vector<F> &v, int _k, int k, int N);
+void __wrap__Z19secret_share_vectorRSt6vectorIN5virgo12fieldElementESaIS1_EEiii(vector<F> &v, int _k, int k, int N) {
+  if (piop_on()) put_field("SSVI", v);
+  __real__Z19secret_share_vectorRSt6vectorIN5virgo12fieldElementESaIS1_EEiii(v, _k, k, N);
+  if (piop_on()) put_field("SSVO", v);
+}
+
+// coSumcheck.cpp:233  quadratic_coSumcheck(p1, p2, R, K, K_r, degrees, N, ps)
+vector<pair<F, vector<F>>> __real__Z20quadratic_coSumcheckRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S_IS3_SaIS3_EES1_S1_S_IiSaIiEEiRd(
+    vector<F> &p1, vector<F> &p2, vector<vector<F>> R, F K, F K_r, vector<int> degrees, int N, double &ps);
+vector<pair<F, vector<F>>> __wrap__Z20quadratic_coSumcheckRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S_IS3_SaIS3_EES1_S1_S_IiSaIiEEiRd(
+    vector<F> &p1, vector<F> &p2, vector<vector<F>> R, F K, F K_r, vector<int> degrees, int N, double &ps) {
+  if (piop_on()) {
+    put_field("QDP1", p1);
+    put_field("QDP2", p2);
+    put_field("QDRR", flat(R));
+    put_field("QDKK", vector<F>{K, K_r});
+    put_ints("QDDG", degrees);
+  }
+  vector<pair<F, vector<F>>> c =
+      __real__Z20quadratic_coSumcheckRSt6vectorIN5virgo12fieldElementESaIS1_EES4_S_IS3_SaIS3_EES1_S1_S_IiSaIiEEiRd(
+          p1, p2, R, K, K_r, degrees, N, ps);
+  if (piop_on()) {
+    put_claims("QDCL", "QDCN", c);
+    put_field("QDIP", flat(ip_vec));
+  }
+  return c;
+}
+
+// MPI_utils.cpp  send_performance_data(v, N): called after every phase of
+// coPIOP_prove; after the second sumcheck it sees prove_phase2's outputs
+vector<double> __real__Z21send_performance_dataSt6vectorIdSaIdEEi(vector<double> v, int N);
+vector<double> __wrap__Z21send_performance_dataSt6vectorIdSaIdEEi(vector<double> v, int N) {
+  if (piop_on()) {
+    put_field("SIP2", sumcheck2_ip);
+    put_field("SIP3", sumcheck3_ip);
+  }
+  return __real__Z21send_performance_dataSt6vectorIdSaIdEEi(v, N);
 }
 
 }  // extern "C"

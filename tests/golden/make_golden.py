@@ -65,6 +65,8 @@ def main():
             manifest["parties"] = gen_parties()
         if "cosumcheck" in only:
             manifest["cosumcheck"] = gen_cosumcheck()
+        if "piop" in only:
+            manifest["piop"] = gen_piop()
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
             json.dump(manifest, f, indent=1)
         print("updated", sorted(only))
@@ -238,6 +240,12 @@ CAPTURE_UNIT = {"H2FI": 16, "H2FO": 16, "FRND": 16, "SHRS": 16, "PAGI": 16, "PAG
                 "SFSI": 16, "SFSO": 16, "PMFC": 16, "PEXO": 16, "PEXC": 16, "DBEY": 16, "DBEE": 0,
                 "AGCK": 16, "AGCC": 16, "WOPB": 0, "WOPC": 16, "EVLV": 16,
                 "GIDX": 4, "RAND": 4, "GSQU": 4, "MTCB": 36, "CTRB": 36, "WCIR": 36}
+# the R1CS front end's records (MINIMPI_CAPTURE_PIOP)
+CAPTURE_UNIT.update({t: 4 for t in ("RNCT", "PLMN", "SURN", "PCCN", "CBDG", "RDDG", "QDDG", "CBCN", "QDCN")})
+CAPTURE_UNIT.update({t: 16 for t in ("DPDL", "DPDR", "DPDO", "DPDW", "GSR0", "GSR1", "GSRK", "SURO", "PCWI", "PCRI",
+                                     "PCCD", "PCFS", "CKRO", "CBP1", "CBP2", "CBP3", "CBR1", "CBR2", "CBRR", "CBKK",
+                                     "CBCL", "CBIP", "RDIR", "SIP1", "RDRA", "RDRB", "RDRC", "SSVI", "SSVO", "QDP1",
+                                     "QDP2", "QDRR", "QDKK", "QDCL", "QDIP", "SIP2", "SIP3")})
 
 
 def capture_records(path):
@@ -557,6 +565,86 @@ def gen_cosumcheck():
     with open(os.path.join(HERE, "cosumcheck.json"), "w") as f:
         json.dump(out, f, indent=1)
     return {"file": "cosumcheck.json", "cases": sorted(out)}
+
+
+def gen_piop():
+    """The reference's R1CS front end (main.cpp:256-257: coPIOP_prove, pigeon
+    1) run unmodified with N ranks, recorded up to the end of its second
+    sumcheck (prove_phase1 / prove_phase2, coPIOP.cpp:241-627).  Kept per
+    case: where rank 0's generator stood at each dealing step, the digests of
+    every rank's dealt inputs (which oracle/gbz_piop_oracle.py regenerates),
+    the Fiat-Shamir state the first phase starts from, and what every rank
+    computed in the two phases (values where small, SHA-256 otherwise)."""
+    import struct
+    import tempfile
+    out = {}
+    for N, logM in ((8, 16), (16, 16), (8, 18)):
+        with tempfile.TemporaryDirectory() as td:
+            prefix = os.path.join(td, "cap")
+            env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_CAPTURE=prefix, MINIMPI_TIMEOUT="300",
+                       MINIMPI_CAPTURE_PIOP="1")
+            t = time.time()
+            log = subprocess.run([PIGEON, "1", str(logM)], env=env, check=True, capture_output=True, text=True)
+            dt = time.time() - t
+            ranks = [capture_records("%s.%d" % (prefix, r)) for r in range(N)]
+        sha = lambda b: hashlib.sha256(b).hexdigest()
+        words = lambda b: list(struct.unpack("<%dI" % (len(b) // 4), b))
+        fes = lambda b: [b[i:i + 16].hex() for i in range(0, len(b), 16)]
+
+        def first(recs, tag, after=None):
+            i0 = 0 if after is None else next(i for i, r in enumerate(recs) if r[0] == after)
+            return next(r[2] for r in recs[i0:] if r[0] == tag)
+
+        def every(recs, tag):
+            return [r[2] for r in recs if r[0] == tag]
+
+        lead = ranks[0]
+        # the leader's Fiat-Shamir draws from the end of PCS_commit to the end
+        # of the second sumcheck
+        tags = [r[0] for r in lead]
+        i0, i1 = tags.index("PCFS"), tags.index("QDCL")
+        draws = [lead[i][2].hex() for i in range(i0, i1) if tags[i] == "H2FO"]
+        rn = [words(b) for b in every(lead, "RNCT")]
+        plmn = words(first(lead, "PLMN"))
+        case = {"N": N, "logM": logM, "rates": [[4], [4], [4, 4], [4, 4]], "ref_seconds": round(dt, 2),
+                "logm": plmn[0], "logn": plmn[1], "mask_l": plmn[2],
+                "generator": {"seed": rn[0][1], "draws": [[w[0], w[2] + (w[3] << 32)] for w in rn]},
+                "pcs_randomness": words(first(lead, "SURN"))[0],
+                "degrees1": words(first(lead, "CBDG")), "degrees2": words(first(lead, "QDDG")),
+                "K": first(lead, "GSRK").hex(), "fs0": first(lead, "PCFS").hex(),
+                "commit_rows": words(first(lead, "PCCN")),
+                "draws": draws,
+                "phase1": {"r1": fes(first(lead, "CBR1")), "r2": fes(first(lead, "CBR2")),
+                           "K_Kr": fes(first(lead, "CBKK")), "Kr": first(lead, "CKRO").hex(),
+                           "claims": first(lead, "CBCL").hex(), "claim_points": words(first(lead, "CBCN")),
+                           "ip": first(lead, "CBIP").hex()},
+                "phase2": {"r": fes(first(lead, "RDIR")), "K_Kr": fes(first(lead, "QDKK")),
+                           "claims": first(lead, "QDCL").hex(), "claim_points": words(first(lead, "QDCN")),
+                           "ip": first(lead, "QDIP").hex()},
+                "errors": [l for l in log.stdout.splitlines() if "ERROR" in l or "Error" in l],
+                "ranks": []}
+        for recs in ranks:
+            suro = every(recs, "SURO")
+            e = {"dealt_sha256": {"vL": sha(first(recs, "DPDL")), "vR": sha(first(recs, "DPDR")),
+                                  "vO": sha(first(recs, "DPDO")), "W": sha(first(recs, "DPDW")),
+                                  "R1": sha(first(recs, "GSR0")), "R2": sha(first(recs, "GSR1")),
+                                  "pcs_random": sha(suro[0]), "R": sha(suro[1]),
+                                  "commit_data": sha(first(recs, "PCCD"))},
+                 "phase1_sha256": {"p1": sha(first(recs, "CBP1")), "p2": sha(first(recs, "CBP2")),
+                                   "p3": sha(first(recs, "CBP3")), "ip": sha(first(recs, "SIP1"))},
+                 "phase2_sha256": {"RA": sha(first(recs, "RDRA")), "RB": sha(first(recs, "RDRB")),
+                                   "RC": sha(first(recs, "RDRC")), "R_aggr": sha(first(recs, "SSVI")),
+                                   "reshared": sha(first(recs, "SSVO")), "p1": sha(first(recs, "QDP1")),
+                                   "p2": sha(first(recs, "QDP2")),
+                                   "ip2": sha(first(recs, "SIP2", after="QDCL")),
+                                   "ip3": sha(first(recs, "SIP3", after="QDCL"))}}
+            case["ranks"].append(e)
+        name = "piop_N%d_M%d" % (N, logM)
+        with open(os.path.join(HERE, name + ".json"), "w") as f:
+            json.dump(case, f, indent=0)
+        out[name] = {"file": name + ".json", "N": N, "logM": logM}
+        print("piop N=%d M=2^%d: reference %.1f s" % (N, logM, dt), flush=True)
+    return out
 
 
 if __name__ == "__main__":
