@@ -565,6 +565,118 @@ def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
     return {"party_shares": out}
 
 
+def run_piop(gbz, O, ctx, repeats, N=16, logM=20):
+    """The R1CS front end's two sumcheck phases (pigeon 1: prove_phase1 and
+    prove_phase2, coPIOP.cpp:241-627) with N = 16 parties on one device and
+    a circuit of M = 2^20 gates, every input device resident: the parties'
+    shares as rank 0 deals them (regenerated on the host before timing), the
+    witness laid out from gbz_pcs_commit's rows, the R1CS rows uploaded once.
+    Timed: gbz_piop_phase1 then gbz_piop_phase2 (host clock around the
+    synchronised calls, best of `repeats`).  Both phases' claims are compared
+    with the reference's own 16-rank run when its fixture is present
+    (tests/golden/piop_N16_M20.json)."""
+    import torch
+    import gbz_piop_oracle as po
+    M = 1 << logM
+    fx = os.path.join(ROOT, "tests", "golden", "piop_N%d_M%d.json" % (N, logM))
+    ref = json.load(open(fx)) if os.path.exists(fx) else None
+    circ = po.circuit(M)
+    mask_l = 333   # (int)(100 / -log2(1 - 0.25 (1 - 1/4))) (coPIOP.cpp:1392-1393)
+    k = N // 4
+    nW = (1 << circ["logn"]) // k
+    deg, q, rnd = gbz.pcs_schedule(N, nW * N // 4, PCS_RATES)
+    d = po.deal(N, M, circ["draws"], rnd, mask_l)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint64).view(np.int64)).cuda()
+    vL, vR, vO, R1, R2 = (dev(d[x]) for x in ("vL", "vR", "vO", "R1", "R2"))
+    masks = dev(d["R"][:, :12])
+    com, _, _ = gbz.pcs_commit(ctx, N, nW * N // 4, PCS_RATES, d["W"], d["pcs_random"])
+    w = []
+    for p in range(N):
+        rows, _, _ = com.data(p)
+        lst = [rows[j] for j in range(rows.shape[0])] + [np.zeros((0, 2), dtype=np.uint64)] * (32 - rows.shape[0])
+        w.append(po.witness_layout(lst, com.row_len, mask_l))
+    com.free()
+    w = np.stack(w)
+    nw = w.shape[1]
+    wd = dev(w)
+    parts = po.r1cs_rows(circ, N)
+    ptrs, cols = [], []
+    for m in "ABC":
+        pp, cc, base = [np.zeros(1, dtype=np.int64)], [], 0
+        for ptr, c in parts[m]:
+            pp.append(ptr[1:] + base)
+            cc.append(c)
+            base += c.shape[0]
+        ptrs.append(np.concatenate(pp))
+        cols.append(np.concatenate(cc))
+    r1cs = gbz.R1cs(ctx, N, (1 << circ["logn"]) // N, circ["logm"], ptrs, cols)
+    d1 = np.array(d["degrees1"], dtype=np.int32)
+    d2 = np.array(d["degrees2"], dtype=np.int32)
+    fs0 = np.zeros(2, dtype=np.uint64) if ref is None else np.frombuffer(bytes.fromhex(ref["fs0"]), dtype=np.uint64)
+    K = np.array([d["K"], 0], dtype=np.uint64)
+    n = d["vL"].shape[1]
+    lib = gbz.lib
+    b1_bytes = lib.gbz_piop_phase1_bytes(N, n, d1.ctypes.data, len(d1))
+    b2_bytes = lib.gbz_piop_phase2_bytes(N, d2.ctypes.data, len(d2))
+    tr1 = torch.zeros(b1_bytes, dtype=torch.uint8, device="cuda")
+    tr2 = torch.zeros(b2_bytes, dtype=torch.uint8, device="cuda")
+    cl1 = torch.zeros((4, len(d1) + 2, 2), dtype=torch.int64, device="cuda")
+    cl2 = torch.zeros((5, len(d2) + 2, 2), dtype=torch.int64, device="cuda")
+    ip1 = torch.zeros((N, 4 * int(d1.sum()), 2), dtype=torch.int64, device="cuda")
+    ip2 = torch.zeros((N, 2 * int(d2.sum()), 2), dtype=torch.int64, device="cuda")
+    ip3 = torch.zeros((N, 12, 2), dtype=torch.int64, device="cuda")
+    abc = torch.zeros((3, 2), dtype=torch.int64, device="cuda")
+    fsd = torch.zeros(2, dtype=torch.int64, device="cuda")
+    Kd = dev(K)
+    fl1, fl2 = ctypes.c_uint32(0), ctypes.c_uint32(0)
+
+    def phases():
+        fsd.copy_(torch.from_numpy(fs0.view(np.int64)))
+        torch.cuda.synchronize()
+        ctx.check(lib.gbz_piop_phase1(ctx.h, N, n, vL.data_ptr(), vR.data_ptr(), vO.data_ptr(), masks.data_ptr(),
+                                      R1.data_ptr(), d1.ctypes.data, len(d1), fsd.data_ptr(), cl1.data_ptr(),
+                                      ip1.data_ptr(), None, None, ctypes.byref(fl1), tr1.data_ptr(), b1_bytes,
+                                      gbz.MEM_DEVICE))
+        point1 = cl1[0, 1:].contiguous()
+        evals1 = cl1[:3, 0].contiguous()
+        torch.cuda.synchronize()
+        ctx.check(lib.gbz_piop_phase2(ctx.h, N, nw, wd.data_ptr(), masks.data_ptr(), r1cs.h, mask_l, R2.data_ptr(),
+                                      point1.data_ptr(), evals1.data_ptr(), d1.ctypes.data, len(d1), d2.ctypes.data,
+                                      len(d2), Kd.data_ptr(), fsd.data_ptr(), cl2.data_ptr(), abc.data_ptr(),
+                                      ip2.data_ptr(), ip3.data_ptr(), None, None, ctypes.byref(fl2),
+                                      tr2.data_ptr(), b2_bytes, gbz.MEM_DEVICE))
+
+    phases()  # warm-up (pools, twiddle tables)
+    ts = []
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        phases()
+        ts.append(time.perf_counter() - t0)
+    r1cs.free()
+    out = {"workload": "the R1CS front end's first and second sumcheck (prove_phase1 + prove_phase2) of %d parties "
+                       "on one device, circuit of M = 2^%d gates (pigeon 1's random circuit), vL/vR/vO 2^%d and "
+                       "witness 2^%d entries per party" % (N, logM, n.bit_length() - 1, nw.bit_length() - 1),
+           "parties": N, "degrees1": d["degrees1"], "degrees2": d["degrees2"],
+           "phases_ms": 1e3 * min(ts), "runs_per_s": 1.0 / min(ts), "flags": [fl1.value, fl2.value],
+           "timing": "host wall clock around the synchronised C-ABI calls (device pointers), best of %d" % repeats}
+    if ref is not None:
+        def blob(t, rows):
+            a = t.cpu().numpy().astype(np.uint64)
+            v = []
+            for i in range(rows):
+                v.append(a[i, 0])
+                v.extend(a[i, 1:])
+            return np.array(v, dtype=np.uint64).tobytes().hex()
+        c2 = cl2.cpu().numpy().astype(np.uint64).copy()
+        # prove_phase2 divides the second claim by L_last[0]; the fixture holds the coSumcheck's own
+        out["claims_equal_reference"] = (blob(cl1, 4) == ref["phase1"]["claims"] and
+                                         c2[0].tobytes().hex() == bytes.fromhex(ref["phase2"]["claims"])[
+                                             :16 * (len(d2) + 2)].hex())
+        out["reference_ranks_seconds_x86"] = ref.get("ref_seconds")
+    return {"piop": out}
+
+
 def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
     """One device-resident measurement per hot-path row outside the plain
     prover: CUDA events on the context's stream around each C-ABI call
@@ -804,6 +916,7 @@ def main():
     ap.add_argument("--parties-only", action="store_true", help="only the party-shares (coPCS) measurement")
     ap.add_argument("--parties-repeats", type=int, default=3, help="timed repeats of the party-shares run")
     ap.add_argument("--batch-only", action="store_true", help="only the batched (64 mixed proofs) measurement")
+    ap.add_argument("--piop-only", action="store_true", help="only the R1CS front end's two sumcheck phases")
     ap.add_argument("--batch-repeats", type=int, default=3, help="timed repeats of the batched measurement")
     args = ap.parse_args()
     ws, rank, local = dist_info()
@@ -840,6 +953,10 @@ def main():
         return
     if args.batch_only:
         print(json.dumps(run_many(gbz, O, ctx, args.batch_repeats, served=False)), flush=True)
+        ctx.close()
+        return
+    if args.piop_only:
+        print(json.dumps(run_piop(gbz, O, ctx, repeats=3)), flush=True)
         ctx.close()
         return
 
@@ -1041,6 +1158,7 @@ def main():
         line.update(run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak))
         line.update(run_many(gbz, O, ctx, repeats=3))
         line.update(run_party_shares(gbz, O, ctx, repeats=3))
+        line.update(run_piop(gbz, O, ctx, repeats=3))
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         t0 = time.perf_counter()

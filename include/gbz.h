@@ -604,6 +604,77 @@ gbz_status gbz_cosumcheck(gbz_ctx *ctx, int form, int N, uint64_t n, const uint6
                           uint64_t *claims, uint32_t *flags, uint8_t *transcript, uint64_t capacity, int mem);
 uint64_t gbz_cosumcheck_transcript_bytes(int form, int N, const int *degrees, int ndeg);
 
+/* ------------------------------------------------- R1CS front end (pigeon 1) */
+
+/* The parties' rows of the R1CS matrices A, B, C (what pA, pB, pC hold on
+ * every rank after distribute_index, MPI_utils.cpp:2205-2270, 2483-2597):
+ * per matrix a CSR over N x rows rows, party p owning rows [p rows,
+ * (p + 1) rows): ptr[t] (N rows + 1 entries, from 0 to nnz[t]) and cols[t]
+ * (the constraint index of every nonzero, below 2^logm; all nonzeros are 1),
+ * host arrays, uploaded once. */
+typedef struct gbz_r1cs gbz_r1cs;
+gbz_status gbz_r1cs_create(gbz_ctx *ctx, int N, uint64_t rows, int logm, const uint32_t *const *ptr,
+                           const uint32_t *const *cols, const uint64_t *nnz, gbz_r1cs **out);
+gbz_status gbz_r1cs_free(gbz_r1cs *m);
+
+/* _reduce_R1CS_matrixes_multivariate (Distributed_Sumcheck.cpp:2283-2350) of
+ * every party: with degrees' = (N/4, degrees1[0 .. ndeg1-2]), beta1 = the
+ * tensor of compute_lagrange_coeff(degrees'[i], r[i]) for i < ndeg1 - 1 (the
+ * first factor varying fastest) and beta2 = compute_lagrange_coeff(
+ * degrees'[ndeg1-1], r[ndeg1-1]), row j of party p of RA is the sum over its
+ * columns c of beta1[c mod S] beta2[c div S], S = |beta1| = 2^logm / |beta2|;
+ * RB, RC likewise.  r: ndeg1 = nr entries; RA, RB, RC: N x rows. */
+gbz_status gbz_r1cs_reduce(gbz_ctx *ctx, const gbz_r1cs *m, const uint64_t *r, int nr, const int *degrees1,
+                           int ndeg1, uint64_t *RA, uint64_t *RB, uint64_t *RC, int mem);
+
+/* prove_phase1 (coPIOP.cpp:241-346) of N parties: the first sumcheck of the
+ * R1CS front end.  vL, vR, vO: N x n party shares; masks: N x 12 (rL, rR,
+ * rO: the first 12 entries of each party's mask randomness R,
+ * coPIOP.cpp:1585-1589); R1: N x sum_i 4 degrees[i] (the parties' shares of
+ * the first sumcheck's randomness, rounds back to back); degrees: degrees1
+ * (their product is 2n); fs: the Fiat-Shamir chain, updated.  Draws _r1
+ * (log2 n) and _r2 (log2 N/4) by hash_to_field({0}), forms every party's
+ * y = sum_{i<4} _beta(i, _r1) (rL rR - rO) and the leader's interpolation,
+ * draws r1's last entry, doubles vL, vR, vO with the masks at the start of
+ * the new half, computes K_r (compute_Kr) and runs cubic_coSumcheck.
+ * Outputs: claims (4 rows x (ndeg + 2) field elements: eval, r_final, the
+ * round challenges, as gbz_cosumcheck), ip (N x sum 4 degrees: every party's
+ * sumcheck1_ip), ip_b1 (N/4: the Lagrange vector _sumcheck1_ip[1]; may be
+ * NULL), vectors (3 x N x 2n: the doubled vL, vR, vO; may be NULL), flags
+ * (gbz_cosumcheck's).  Transcript (gbz_piop_phase1_bytes; may be NULL):
+ *   58 PIOP_DRAWS 16B x (log2 n + log2(N/4) + 1) | 59 PIOP_Y 16B x (N + 2):
+ *   the parties' y, the leader's y, K_r | the cubic coSumcheck's records. */
+gbz_status gbz_piop_phase1(gbz_ctx *ctx, int N, uint64_t n, const uint64_t *vL, const uint64_t *vR,
+                           const uint64_t *vO, const uint64_t *masks, const uint64_t *R1, const int *degrees,
+                           int ndeg, uint64_t *fs, uint64_t *claims, uint64_t *ip, uint64_t *ip_b1,
+                           uint64_t *vectors, uint32_t *flags, uint8_t *transcript, uint64_t capacity, int mem);
+uint64_t gbz_piop_phase1_bytes(int N, uint64_t n, const int *degrees, int ndeg);
+
+/* prove_phase2 (coPIOP.cpp:406-627) of N parties: the second sumcheck.  w:
+ * N x nw (each party's witness as coPIOP_prove hands it over after
+ * PCS_commit); masks: as phase 1; m: the R1CS rows; mask_l: the PCS mask
+ * length (the gap in each of the 32 segments); R2: N x sum_i 2 degrees2[i];
+ * point1: phase 1's claim point (ndeg1 + 1 entries: r_final then the round
+ * challenges); evals1: phase 1's first three claim values (yL, yR, yO); K:
+ * the second sumcheck's randomness claim (generate_sumcheck_randomness).
+ * Reduces the R1CS rows at point1 without its last entry, draws a, b, c,
+ * forms L_last[0] (a RA + b RB + c RC), reshares it (secret_share_vector)
+ * into 32 segments, appends the parties' beta shares (times L_last[1]),
+ * pairs it with (w, a rL + b rR + c rO) and runs quadratic_coSumcheck on
+ * a yL + b yR + c yO.  Outputs: claims (5 rows x (ndeg2 + 2); row 1's value
+ * divided by L_last[0] as the reference returns it), abc (3), ip2 (N x sum
+ * 2 degrees2: sumcheck2_ip), ip3 (N x 12: sumcheck3_ip), ip_b1 (N/4), vectors
+ * (2 x N x 2nw: the coSumcheck's two vectors; may be NULL), flags.
+ * Transcript (gbz_piop_phase2_bytes): 60 PIOP_ABC 16B x 3 | the quadratic
+ * coSumcheck's records. */
+gbz_status gbz_piop_phase2(gbz_ctx *ctx, int N, uint64_t nw, const uint64_t *w, const uint64_t *masks,
+                           const gbz_r1cs *m, int mask_l, const uint64_t *R2, const uint64_t *point1,
+                           const uint64_t *evals1, const int *degrees1, int ndeg1, const int *degrees2, int ndeg2,
+                           const uint64_t *K, uint64_t *fs, uint64_t *claims, uint64_t *abc, uint64_t *ip2,
+                           uint64_t *ip3, uint64_t *ip_b1, uint64_t *vectors, uint32_t *flags, uint8_t *transcript,
+                           uint64_t capacity, int mem);
+uint64_t gbz_piop_phase2_bytes(int N, const int *degrees2, int ndeg2);
+
 /* --------------------------------------------------------------- prover */
 
 /* Bytes of the transcript of one proof of a 2^logn witness at `rate`. */

@@ -4,6 +4,8 @@
 
 #include "gbz_internal.cuh"
 
+struct gbz_ctx;
+
 namespace gbz {
 
 // RS_multifold5 (coPCS_utils.cpp:386-437): out (n / 2^logd) from cw (n),
@@ -45,5 +47,24 @@ void cophase1_reduce_launch(const fe *e1, const fe *e2, const fe *e3, const fe *
                             int parties = 1);
 // coSumcheck phase 2 (coSumcheck.cpp:66-148, 201-213).
 void cophase2_launch(const fe *v, uint64_t n, const fe *L, int logd, fe *out, cudaStream_t s);
+
+// quadratic_coSumcheck / cubic_coSumcheck of N parties (coSumcheck.cpp:
+// 233-331, 335-448), the body of gbz_cosumcheck.  p1, p2, p3 (cubic), R:
+// party-major arrays copied in with kin (the call folds copies); r1 (cubic,
+// nr1 = log2 n entries), r2 (log2(N/4) entries), K, K_r, fs: host values.
+// The transcript (cosumcheck_bytes) goes to `transcript` (may be null) by
+// tr_kind; when ip is not null it receives the coSumcheck's inner-product
+// vector ip_vec flattened (sum of (2 or 4) d_i entries, device).  Returns
+// rows x (ndeg + 2) claim words [eval, r_final, r_0 .. r_{ndeg-1}] (rows = 5
+// quadratic, 4 cubic), the chain state and the check flags.
+struct CoscOut {
+  std::vector<fe> claims;
+  fe fs;
+  uint32_t flags;
+};
+CoscOut cosumcheck_run(gbz_ctx *ctx, int form, int N, uint64_t n, const fe *p1, const fe *p2, const fe *p3,
+                       const fe *R, cudaMemcpyKind kin, const fe *r1, int nr1, const fe *r2, fe K, fe K_r,
+                       const int *degrees, int ndeg, fe fs, uint8_t *transcript, cudaMemcpyKind tr_kind, fe *ip);
+uint64_t cosumcheck_bytes(int form, int N, const int *degrees, int ndeg);
 
 }  // namespace gbz

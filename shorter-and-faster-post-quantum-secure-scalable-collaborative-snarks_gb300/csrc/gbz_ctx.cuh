@@ -2,11 +2,13 @@
 // translation unit with extern "C" entry points uses: device guard, error
 // mapping, argument checks and host/device views of caller buffers.
 #pragma once
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <new>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "../../include/gbz.h"
 #include "gbz_prover.cuh"
@@ -76,6 +78,40 @@ struct DeviceGuard {
   ~DeviceGuard() {
     int cur;
     if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Device buffers of one call: allocated per call and freed at its end, or,
+// with a pool, the pool's k-th buffer for the call's k-th allocation (a
+// larger or new one replaces it when it is too small).
+struct OpenBufs {
+  std::vector<void *> owned;
+  std::vector<std::pair<void *, uint64_t>> *pool = nullptr;
+  size_t next = 0;
+  ~OpenBufs() {
+    for (void *p : owned) cudaFree(p);
+  }
+  template <typename T>
+  T *alloc(uint64_t count) {
+    const uint64_t bytes = std::max<uint64_t>(count * sizeof(T), 16);
+    if (pool) {
+      auto &P = *pool;
+      if (next < P.size() && P[next].second >= bytes) return (T *)P[next++].first;
+      void *p = nullptr;
+      GBZ_CUDA(cudaMalloc(&p, bytes));
+      if (next < P.size()) {
+        cudaFree(P[next].first);
+        P[next] = {p, bytes};
+      } else {
+        P.push_back({p, bytes});
+      }
+      next++;
+      return (T *)p;
+    }
+    void *p = nullptr;
+    GBZ_CUDA(cudaMalloc(&p, bytes));
+    owned.push_back(p);
+    return (T *)p;
   }
 };
 

@@ -604,6 +604,18 @@ __global__ void k_cosc_sparse(fe *R, uint64_t rstride, ROffs ro, int iter, const
   st->fer[p] = s;
 }
 
+// The coSumcheck's inner-product vector (ip_vec, coSumcheck.cpp:240-275,
+// 345-381): round i's entry j is LD_i[j] times the first entry of every
+// other round's LD (each round scales all other rounds' entries by its
+// LD[0]).  One CTA per round.
+__global__ void k_cosc_ip(const fe *LD, ROffs ro, fe *ip) {
+  const int i = blockIdx.x;
+  fe others = fe_one();
+  for (int t = 0; t < ro.n; t++)
+    if (t != i) others = fmul(others, LD[ro.off[t]]);
+  for (uint32_t j = ro.off[i] + threadIdx.x; j < ro.off[i + 1]; j += blockDim.x) ip[j] = fmul(LD[j], others);
+}
+
 // The end of the round driver (coSumcheck.cpp:300-330, 399-446): the parties'
 // final values, the leader's unpack (unpack_secret_share(H, N/2, N), a fixed
 // N/2 x N map U), its check, the last challenge, the Lagrange weights over
@@ -879,40 +891,6 @@ struct gbz_pcs {
 
 namespace {
 
-// Device buffers of one call: allocated per call and freed at its end, or,
-// with a pool, the pool's k-th buffer for the call's k-th allocation (a
-// larger or new one replaces it when it is too small).
-struct OpenBufs {
-  std::vector<void *> owned;
-  std::vector<std::pair<void *, uint64_t>> *pool = nullptr;
-  size_t next = 0;
-  ~OpenBufs() {
-    for (void *p : owned) cudaFree(p);
-  }
-  template <typename T>
-  T *alloc(uint64_t count) {
-    const uint64_t bytes = std::max<uint64_t>(count * sizeof(T), 16);
-    if (pool) {
-      auto &P = *pool;
-      if (next < P.size() && P[next].second >= bytes) return (T *)P[next++].first;
-      void *p = nullptr;
-      GBZ_CUDA(cudaMalloc(&p, bytes));
-      if (next < P.size()) {
-        cudaFree(P[next].first);
-        P[next] = {p, bytes};
-      } else {
-        P.push_back({p, bytes});
-      }
-      next++;
-      return (T *)p;
-    }
-    void *p = nullptr;
-    GBZ_CUDA(cudaMalloc(&p, bytes));
-    owned.push_back(p);
-    return (T *)p;
-  }
-};
-
 // The record layout of an opening: header list and the payload offsets.
 struct PcsLayout {
   std::vector<Hdr> hdr;
@@ -1013,6 +991,201 @@ void tail_layout(const gbz_pcs &pc, PcsLayout &lay, std::vector<DrawOp> *script 
 }
 
 }  // namespace
+
+namespace gbz {
+
+CoscOut cosumcheck_run(gbz_ctx *ctx, int form, int N, uint64_t n, const fe *p1, const fe *p2, const fe *p3,
+                       const fe *R, cudaMemcpyKind kin, const fe *r1, int nr1, const fe *r2, fe hK, fe hKr,
+                       const int *degrees, int ndeg, fe hfs, uint8_t *transcript, cudaMemcpyKind tr_kind, fe *ip) {
+  if (form != GBZ_SC_QUADRATIC && form != GBZ_SC_CUBIC) throw ArgError("coSumcheck: form must be quadratic or cubic");
+  const bool cubic = form == GBZ_SC_CUBIC;
+  if (cubic && (!p3 || !r1)) throw ArgError("coSumcheck: the cubic form needs p3 and r1");
+  if (N < 4 || N > kPcsMaxParties || !is_pow2((uint64_t)N)) throw ArgError("coSumcheck: N must be a power of two in [4, 64]");
+  if (ndeg < 1 || ndeg > kCoscMaxRounds) throw ArgError("coSumcheck: 1..16 rounds");
+  check_pow2(n, "coSumcheck: n");
+  const int ext = cubic ? 2 : 1, step = 1 << ext, rows = cubic ? 4 : 5;
+  uint64_t m = n;
+  std::vector<int> logd(ndeg);
+  ROffs ro{};
+  ro.n = ndeg;
+  ro.off[0] = 0;
+  for (int i = 0; i < ndeg; i++) {
+    if (degrees[i] < 1 || !is_pow2((uint64_t)degrees[i]) || degrees[i] > 1024 || (uint64_t)degrees[i] > m)
+      throw ArgError("coSumcheck: degrees must be powers of two <= 1024 dividing the length");
+    logd[i] = ilog2((uint64_t)degrees[i]);
+    m /= degrees[i];
+    ro.off[i + 1] = ro.off[i] + (uint32_t)(step * degrees[i]);
+  }
+  if (m < (cubic ? 1u : 2u)) throw ArgError("coSumcheck: the folds must leave 2 (quadratic) / 1 (cubic) entries");
+  const int lq = ilog2((uint64_t)(N / 4));
+  if (cubic && (nr1 < 0 || (1ull << nr1) != n)) throw ArgError("coSumcheck: r1 must have log2(n) entries");
+  // transcript layout
+  PcsLayout lay;
+  const uint64_t off_c = lay.add(T_PCS_CHALLENGE, 1, 16);
+  std::vector<uint64_t> off_pp(ndeg), off_poly(ndeg), off_chal(ndeg);
+  for (int i = 0; i < ndeg; i++) {
+    const int D = degrees[i] << ext;
+    off_pp[i] = lay.add(T_PCS_PARTY_POLYS, D * N, 16);
+    off_poly[i] = lay.add(T_PCS_POLY, D, 16);
+    off_chal[i] = lay.add(T_PCS_CHALLENGE, 1, 16);
+  }
+  const uint64_t off_sh = lay.add(T_COSC_FINAL_SHARES, rows * N, 16);
+  const uint64_t off_un = lay.add(T_COSC_UNPACKED, rows * (N / 2), 16);
+  const uint64_t off_r = lay.add(T_PCS_CHALLENGE, 1, 16);
+  const uint64_t off_cl = lay.add(T_COSC_CLAIMS, rows, 16);
+  cudaStream_t s = ctx->stream;
+  OpenBufs ob;
+  {
+    std::string key = "cosumcheck:" + std::to_string(form) + ":" + std::to_string(N) + ":" + std::to_string(n) + ":" +
+                      std::to_string((int)kin) + ":" + std::to_string(transcript != nullptr) + ":" + std::to_string(ip != nullptr);
+    for (int i = 0; i < ndeg; i++) key += ":" + std::to_string(degrees[i]);
+    ob.pool = &ctx->pools[key];
+  }
+  // party-major inputs, copied: the call folds them in place as the reference does
+  const uint64_t Rst = ro.off[ndeg];
+  fe *v1 = ob.alloc<fe>((uint64_t)N * n), *v2 = ob.alloc<fe>((uint64_t)N * n), *v3 = nullptr, *vb = nullptr;
+  fe *dR = ob.alloc<fe>((uint64_t)N * Rst);
+  GBZ_CUDA(cudaMemcpyAsync(v1, p1, 16ull * N * n, kin, s));
+  GBZ_CUDA(cudaMemcpyAsync(v2, p2, 16ull * N * n, kin, s));
+  GBZ_CUDA(cudaMemcpyAsync(dR, R, 16ull * N * Rst, kin, s));
+  // the quadratic form takes no points (r1, r2 may be null there)
+  std::vector<fe> hr1(cubic ? r1 : nullptr, cubic ? r1 + nr1 : nullptr), hr2(lq, fe_zero());
+  if (cubic && lq) hr2.assign(r2, r2 + lq);
+  if (cubic) {
+    v3 = ob.alloc<fe>((uint64_t)N * n);
+    vb = ob.alloc<fe>((uint64_t)N * n);
+    GBZ_CUDA(cudaMemcpyAsync(v3, p3, 16ull * N * n, kin, s));
+  }
+  // b1 = precompute_beta(r1) for every party (the same vector), b2 = precompute_beta(r2)
+  std::vector<fe> b2(N / 4, fe_one());
+  for (int i = 0; i < N / 4; i++) {
+    fe v = fe_one();
+    for (int t = 0; t < lq; t++) v = fmul(v, ((i >> t) & 1) ? hr2[t] : fsub(fe_one(), hr2[t]));
+    b2[i] = v;
+  }
+  fe *dr1 = ob.alloc<fe>(std::max(1, nr1)), *db2 = ob.alloc<fe>(N / 4);
+  GBZ_CUDA(cudaMemcpyAsync(db2, b2.data(), 16ull * (N / 4), cudaMemcpyHostToDevice, s));
+  if (cubic) {
+    GBZ_CUDA(cudaMemcpyAsync(dr1, hr1.data(), 16ull * nr1, cudaMemcpyHostToDevice, s));
+    beta_launch(dr1, nr1, vb, s);
+    for (int p = 1; p < N; p++) GBZ_CUDA(cudaMemcpyAsync(vb + (uint64_t)p * n, vb, 16 * n, cudaMemcpyDeviceToDevice, s));
+  }
+  // sumcheck_aggr's weights: ones (quadratic, coSumcheck.cpp:194) or b2 (cubic)
+  std::vector<fe> ones(N / 4, fe_one());
+  std::vector<fe> lambda = aggregate_weights(N, cubic ? b2.data() : ones.data());
+  // unpack_secret_share(H, N/2, N): row j of the map takes E[2j]
+  std::vector<fe> U((size_t)(N / 2) * N);
+  for (int j = 0; j < N / 2; j++) {
+    std::vector<fe> g(N, fe_zero());
+    g[2 * j] = fe_one();
+    std::vector<fe> l = aggregate_weights_even(N, g);
+    for (int p = 0; p < N; p++) U[(size_t)j * N + p] = l[p];
+  }
+  fe *dl = ob.alloc<fe>(N), *dU = ob.alloc<fe>(U.size());
+  GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
+  GBZ_CUDA(cudaMemcpyAsync(dU, U.data(), 16 * U.size(), cudaMemcpyHostToDevice, s));
+  uint8_t *tr = ob.alloc<uint8_t>(lay.bytes);
+  Hdr *dh = ob.alloc<Hdr>(lay.hdr.size());
+  GBZ_CUDA(cudaMemcpyAsync(dh, lay.hdr.data(), sizeof(Hdr) * lay.hdr.size(), cudaMemcpyHostToDevice, s));
+  k_headers<<<grid(lay.hdr.size()), 256, 0, s>>>(dh, (int)lay.hdr.size(), tr);
+  CoscDev *st = ob.alloc<CoscDev>(1);
+  k_cosc_init<<<1, 1, 0, s>>>(st, hfs, hK, hKr, tr, off_c);
+  GBZ_CUDA(cudaGetLastError());
+  const int maxD = 1024 << ext;
+  // every round's Lagrange vector over its extended block, kept for ip_vec
+  fe *H = ob.alloc<fe>((uint64_t)N * maxD), *poly = ob.alloc<fe>(maxD), *LDall = ob.alloc<fe>(ro.off[ndeg]);
+  fe *scr = ob.alloc<fe>(2ull * maxD), *coef = ob.alloc<fe>((uint64_t)N * n);
+  uint64_t dsum = 0;
+  for (int i = 0; i < ndeg; i++) dsum += degrees[i];
+  fe *Ldh = ob.alloc<fe>(dsum);
+  int *dlog = ob.alloc<int>(ndeg);
+  GBZ_CUDA(cudaMemcpyAsync(dlog, logd.data(), 4ull * ndeg, cudaMemcpyHostToDevice, s));
+  m = n;
+  uint64_t at = 0;
+  for (int i = 0; i < ndeg; i++) {
+    const int d = degrees[i], D = d << ext;
+    const uint64_t blocks = (uint64_t)N * m / d, pblocks = m / d;
+    // phase 1 (coSumcheck.cpp:9-46, 150-179): extended blocks of every vector
+    const NttTables &td = ctx->tables(logd[i]), &tD = ctx->tables(logd[i] + ext);
+    if (logd[i] + ext > kMaxCoLogD) throw ArgError("coSumcheck: extended block longer than 2^13");
+    fe *src[4] = {v1, v2, cubic ? vb : nullptr, cubic ? v3 : nullptr};
+    fe *ex[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int v = 0; v < (cubic ? 4 : 2); v++) {
+      ex[v] = ob.alloc<fe>(blocks * D);
+      ntt_batched(td, src[v], d, (uint32_t)d, coef, blocks, true, s);
+      ntt_batched(tD, coef, d, (uint32_t)d, ex[v], blocks, false, s);
+    }
+    uint8_t *zf = nullptr;
+    if (cubic) {  // blocks whose p1 part is all zero are skipped (coSumcheck.cpp:21-27)
+      zf = ob.alloc<uint8_t>(blocks);
+      nonzero_blocks_launch(v1, blocks, logd[i], zf, s);
+    }
+    const int lanes = D >= 256 ? 1 : 256 / D;
+    const int per_cta = (int)std::max<uint64_t>((uint64_t)lanes, (pblocks + 607) / 608);
+    fe *cpart = ob.alloc<fe>((uint64_t)N * D * cophase1_parts(pblocks, per_cta));
+    cophase1_reduce_launch(ex[0], ex[1], ex[2], ex[3], zf, pblocks, logd[i] + ext, per_cta, cpart, H, s, N);
+    k_cosc_add_hr<<<N, 256, 0, s>>>(H, D, dR, Rst, ro, i, step, st);
+    k_put_party<<<dim3(grid(D), N), 256, 0, s>>>(H, D, N, tr, off_pp[i], 16ull * D);
+    aggregate_launch(H, N, D, dl, poly, s);
+    fe *LD = LDall + ro.off[i];
+    k_cosc_verify<<<1, 256, 0, s>>>(st, poly, logd[i], ext, i, LD, Ldh + at, scr, tr, off_poly[i], off_chal[i]);
+    k_cosc_sparse<<<1, 64, 0, s>>>(dR, Rst, ro, i, LD, D, N, st);
+    GBZ_CUDA(cudaGetLastError());
+    // phase 2 (coSumcheck.cpp:66-148, 201-213): every vector folded by Ld
+    for (fe *v : {v1, v2, v3, vb}) {
+      if (!v) continue;
+      cophase2_launch(v, (uint64_t)N * m, Ldh + at, logd[i], coef, s);
+      GBZ_CUDA(cudaMemcpyAsync(v, coef, 16ull * N * m / d, cudaMemcpyDeviceToDevice, s));
+    }
+    m /= d;
+    at += d;
+  }
+  fe *dcl = ob.alloc<fe>(rows);
+  k_cosc_final<<<1, 32, 0, s>>>(st, cubic ? 1 : 0, N, v1, v2, v3, vb, m, dU, db2, Ldh, dlog, ndeg, dr1, dcl, tr,
+                                off_sh, off_un, off_r, off_cl);
+  GBZ_CUDA(cudaGetLastError());
+  if (ip) {
+    k_cosc_ip<<<ndeg, 256, 0, s>>>(LDall, ro, ip);
+    GBZ_CUDA(cudaGetLastError());
+  }
+  CoscDev hst;
+  GBZ_CUDA(cudaMemcpyAsync(&hst, st, sizeof(CoscDev), cudaMemcpyDeviceToHost, s));
+  std::vector<fe> hcl(rows);
+  GBZ_CUDA(cudaMemcpyAsync(hcl.data(), dcl, 16ull * rows, cudaMemcpyDeviceToHost, s));
+  if (transcript) GBZ_CUDA(cudaMemcpyAsync(transcript, tr, lay.bytes, tr_kind, s));
+  GBZ_CUDA(cudaStreamSynchronize(s));
+  // claims: rows x (eval, r vector [r_final, r_0, ..., r_{ndeg-1}])
+  CoscOut out;
+  out.claims.resize((size_t)rows * (ndeg + 2));
+  for (int i = 0; i < rows; i++) {
+    fe *o = out.claims.data() + (size_t)i * (ndeg + 2);
+    o[0] = hcl[i];
+    o[1] = hst.fs;
+    for (int k = 0; k < ndeg; k++) o[2 + k] = hst.r[k];
+  }
+  out.fs = hst.fs;
+  out.flags = hst.flags;
+  return out;
+}
+
+uint64_t cosumcheck_bytes(int form, int N, const int *degrees, int ndeg) {
+  if (!degrees || ndeg < 1 || N < 4) return 0;
+  const int ext = form == GBZ_SC_CUBIC ? 2 : 1, rows = form == GBZ_SC_CUBIC ? 4 : 5;
+  PcsLayout lay;
+  lay.add(T_PCS_CHALLENGE, 1, 16);
+  for (int i = 0; i < ndeg; i++) {
+    lay.add(T_PCS_PARTY_POLYS, (degrees[i] << ext) * N, 16);
+    lay.add(T_PCS_POLY, degrees[i] << ext, 16);
+    lay.add(T_PCS_CHALLENGE, 1, 16);
+  }
+  lay.add(T_COSC_FINAL_SHARES, rows * N, 16);
+  lay.add(T_COSC_UNPACKED, rows * (N / 2), 16);
+  lay.add(T_PCS_CHALLENGE, 1, 16);
+  lay.add(T_COSC_CLAIMS, rows, 16);
+  return lay.bytes;
+}
+
+}  // namespace gbz
 
 extern "C" {
 
@@ -1596,221 +1769,49 @@ gbz_status gbz_cosumcheck(gbz_ctx *ctx, int form, int N, uint64_t n, const uint6
   need(degrees, "degrees");
   need(fs, "fs");
   need(claims, "claims");
-  if (form != GBZ_SC_QUADRATIC && form != GBZ_SC_CUBIC) throw ArgError("coSumcheck: form must be quadratic or cubic");
   const bool cubic = form == GBZ_SC_CUBIC;
   if (cubic) {
     need(p3, "p3");
     need(r1, "r1");
   }
-  if (N < 4 || N > kPcsMaxParties || !is_pow2((uint64_t)N)) throw ArgError("coSumcheck: N must be a power of two in [4, 64]");
-  if (ndeg < 1 || ndeg > kCoscMaxRounds) throw ArgError("coSumcheck: 1..16 rounds");
-  check_pow2(n, "coSumcheck: n");
-  const int ext = cubic ? 2 : 1, step = 1 << ext, rows = cubic ? 4 : 5;
-  uint64_t m = n;
-  std::vector<int> logd(ndeg);
-  ROffs ro{};
-  ro.n = ndeg;
-  ro.off[0] = 0;
-  for (int i = 0; i < ndeg; i++) {
-    if (degrees[i] < 1 || !is_pow2((uint64_t)degrees[i]) || degrees[i] > 1024 || (uint64_t)degrees[i] > m)
-      throw ArgError("coSumcheck: degrees must be powers of two <= 1024 dividing the length");
-    logd[i] = ilog2((uint64_t)degrees[i]);
-    m /= degrees[i];
-    ro.off[i + 1] = ro.off[i] + (uint32_t)(step * degrees[i]);
-  }
-  if (m < (cubic ? 1u : 2u)) throw ArgError("coSumcheck: the folds must leave 2 (quadratic) / 1 (cubic) entries");
+  if (transcript && capacity < cosumcheck_bytes(form, N, degrees, ndeg))
+    throw ArgError("coSumcheck: transcript capacity too small");
+  if (N < 4 || !is_pow2((uint64_t)N)) throw ArgError("coSumcheck: N must be a power of two in [4, 64]");
   const int lq = ilog2((uint64_t)(N / 4));
-  if (cubic && (nr1 < 0 || (1ull << nr1) != n)) throw ArgError("coSumcheck: r1 must have log2(n) entries");
-  // transcript layout
-  PcsLayout lay;
-  const uint64_t off_c = lay.add(T_PCS_CHALLENGE, 1, 16);
-  std::vector<uint64_t> off_pp(ndeg), off_poly(ndeg), off_chal(ndeg);
-  for (int i = 0; i < ndeg; i++) {
-    const int D = degrees[i] << ext;
-    off_pp[i] = lay.add(T_PCS_PARTY_POLYS, D * N, 16);
-    off_poly[i] = lay.add(T_PCS_POLY, D, 16);
-    off_chal[i] = lay.add(T_PCS_CHALLENGE, 1, 16);
-  }
-  const uint64_t off_sh = lay.add(T_COSC_FINAL_SHARES, rows * N, 16);
-  const uint64_t off_un = lay.add(T_COSC_UNPACKED, rows * (N / 2), 16);
-  const uint64_t off_r = lay.add(T_PCS_CHALLENGE, 1, 16);
-  const uint64_t off_cl = lay.add(T_COSC_CLAIMS, rows, 16);
-  if (transcript && capacity < lay.bytes) throw ArgError("coSumcheck: transcript capacity too small");
-  cudaStream_t s = ctx->stream;
-  OpenBufs ob;
-  {
-    std::string key = "cosumcheck:" + std::to_string(form) + ":" + std::to_string(N) + ":" + std::to_string(n) + ":" +
-                      std::to_string(mem) + ":" + std::to_string(transcript != nullptr);
-    for (int i = 0; i < ndeg; i++) key += ":" + std::to_string(degrees[i]);
-    ob.pool = &ctx->pools[key];
-  }
-  // party-major inputs, copied: the call folds them in place as the reference does
-  const uint64_t Rst = ro.off[ndeg];
-  fe *v1 = ob.alloc<fe>((uint64_t)N * n), *v2 = ob.alloc<fe>((uint64_t)N * n), *v3 = nullptr, *vb = nullptr;
-  fe *dR = ob.alloc<fe>((uint64_t)N * Rst);
-  const cudaMemcpyKind kin = mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  GBZ_CUDA(cudaMemcpyAsync(v1, p1, 16ull * N * n, kin, s));
-  GBZ_CUDA(cudaMemcpyAsync(v2, p2, 16ull * N * n, kin, s));
-  GBZ_CUDA(cudaMemcpyAsync(dR, R, 16ull * N * Rst, kin, s));
+  if (cubic && nr1 < 0) throw ArgError("coSumcheck: r1 must have log2(n) entries");
+  // the scalars and points to the host
   std::vector<fe> hr1(cubic ? nr1 : 0), hr2(lq);
-  if (cubic) {
-    v3 = ob.alloc<fe>((uint64_t)N * n);
-    vb = ob.alloc<fe>((uint64_t)N * n);
-    GBZ_CUDA(cudaMemcpyAsync(v3, p3, 16ull * N * n, kin, s));
-    if (mem == GBZ_MEM_DEVICE) {
-      GBZ_CUDA(cudaMemcpyAsync(hr1.data(), r1, 16ull * nr1, cudaMemcpyDeviceToHost, s));
-      if (lq) GBZ_CUDA(cudaMemcpyAsync(hr2.data(), r2, 16ull * lq, cudaMemcpyDeviceToHost, s));
-    } else {
+  fe hK, hKr, hfs;
+  const cudaStream_t s = ctx->stream;
+  if (mem == GBZ_MEM_DEVICE) {
+    if (cubic && nr1) GBZ_CUDA(cudaMemcpyAsync(hr1.data(), r1, 16ull * nr1, cudaMemcpyDeviceToHost, s));
+    if (cubic && lq) GBZ_CUDA(cudaMemcpyAsync(hr2.data(), r2, 16ull * lq, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaMemcpyAsync(&hK, K, 16, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaMemcpyAsync(&hKr, K_r, 16, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaMemcpyAsync(&hfs, fs, 16, cudaMemcpyDeviceToHost, s));
+    GBZ_CUDA(cudaStreamSynchronize(s));
+  } else {
+    if (cubic) {
       for (int i = 0; i < nr1; i++) hr1[i] = fe_make(r1[2 * i], r1[2 * i + 1]);
       for (int i = 0; i < lq; i++) hr2[i] = fe_make(r2[2 * i], r2[2 * i + 1]);
     }
+    hK = fe_make(K[0], K[1]);
+    hKr = fe_make(K_r[0], K_r[1]);
+    hfs = fe_make(fs[0], fs[1]);
   }
-  fe hK, hKr, hfs;
-  {
-    uint64_t t[6];
-    if (mem == GBZ_MEM_DEVICE) {
-      GBZ_CUDA(cudaMemcpyAsync(t, K, 16, cudaMemcpyDeviceToHost, s));
-      GBZ_CUDA(cudaMemcpyAsync(t + 2, K_r, 16, cudaMemcpyDeviceToHost, s));
-      GBZ_CUDA(cudaMemcpyAsync(t + 4, fs, 16, cudaMemcpyDeviceToHost, s));
-      GBZ_CUDA(cudaStreamSynchronize(s));
-    } else {
-      t[0] = K[0], t[1] = K[1], t[2] = K_r[0], t[3] = K_r[1], t[4] = fs[0], t[5] = fs[1];
-    }
-    hK = fe_make(t[0], t[1]);
-    hKr = fe_make(t[2], t[3]);
-    hfs = fe_make(t[4], t[5]);
-  }
-  // b1 = precompute_beta(r1) for every party (the same vector), b2 = precompute_beta(r2)
-  std::vector<fe> b2(N / 4, fe_one());
-  for (int i = 0; i < N / 4; i++) {
-    fe v = fe_one();
-    for (int t = 0; t < lq; t++) v = fmul(v, ((i >> t) & 1) ? hr2[t] : fsub(fe_one(), hr2[t]));
-    b2[i] = v;
-  }
-  fe *dr1 = ob.alloc<fe>(std::max(1, nr1)), *db2 = ob.alloc<fe>(N / 4);
-  GBZ_CUDA(cudaMemcpyAsync(db2, b2.data(), 16ull * (N / 4), cudaMemcpyHostToDevice, s));
-  if (cubic) {
-    GBZ_CUDA(cudaMemcpyAsync(dr1, hr1.data(), 16ull * nr1, cudaMemcpyHostToDevice, s));
-    beta_launch(dr1, nr1, vb, s);
-    for (int p = 1; p < N; p++) GBZ_CUDA(cudaMemcpyAsync(vb + (uint64_t)p * n, vb, 16 * n, cudaMemcpyDeviceToDevice, s));
-  }
-  // sumcheck_aggr's weights: ones (quadratic, coSumcheck.cpp:194) or b2 (cubic)
-  std::vector<fe> ones(N / 4, fe_one());
-  std::vector<fe> lambda = aggregate_weights(N, cubic ? b2.data() : ones.data());
-  // unpack_secret_share(H, N/2, N): row j of the map takes E[2j]
-  std::vector<fe> U((size_t)(N / 2) * N);
-  for (int j = 0; j < N / 2; j++) {
-    std::vector<fe> g(N, fe_zero());
-    g[2 * j] = fe_one();
-    std::vector<fe> l = aggregate_weights_even(N, g);
-    for (int p = 0; p < N; p++) U[(size_t)j * N + p] = l[p];
-  }
-  fe *dl = ob.alloc<fe>(N), *dU = ob.alloc<fe>(U.size());
-  GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
-  GBZ_CUDA(cudaMemcpyAsync(dU, U.data(), 16 * U.size(), cudaMemcpyHostToDevice, s));
-  uint8_t *tr = ob.alloc<uint8_t>(lay.bytes);
-  Hdr *dh = ob.alloc<Hdr>(lay.hdr.size());
-  GBZ_CUDA(cudaMemcpyAsync(dh, lay.hdr.data(), sizeof(Hdr) * lay.hdr.size(), cudaMemcpyHostToDevice, s));
-  k_headers<<<grid(lay.hdr.size()), 256, 0, s>>>(dh, (int)lay.hdr.size(), tr);
-  CoscDev *st = ob.alloc<CoscDev>(1);
-  k_cosc_init<<<1, 1, 0, s>>>(st, hfs, hK, hKr, tr, off_c);
-  GBZ_CUDA(cudaGetLastError());
-  const int maxD = 1024 << ext;
-  fe *H = ob.alloc<fe>((uint64_t)N * maxD), *poly = ob.alloc<fe>(maxD), *LD = ob.alloc<fe>(maxD);
-  fe *scr = ob.alloc<fe>(2ull * maxD), *coef = ob.alloc<fe>((uint64_t)N * n);
-  uint64_t dsum = 0;
-  for (int i = 0; i < ndeg; i++) dsum += degrees[i];
-  fe *Ldh = ob.alloc<fe>(dsum);
-  int *dlog = ob.alloc<int>(ndeg);
-  GBZ_CUDA(cudaMemcpyAsync(dlog, logd.data(), 4ull * ndeg, cudaMemcpyHostToDevice, s));
-  m = n;
-  uint64_t at = 0;
-  for (int i = 0; i < ndeg; i++) {
-    const int d = degrees[i], D = d << ext;
-    const uint64_t blocks = (uint64_t)N * m / d, pblocks = m / d;
-    // phase 1 (coSumcheck.cpp:9-46, 150-179): extended blocks of every vector
-    const NttTables &td = ctx->tables(logd[i]), &tD = ctx->tables(logd[i] + ext);
-    if (logd[i] + ext > kMaxCoLogD) throw ArgError("coSumcheck: extended block longer than 2^13");
-    fe *src[4] = {v1, v2, cubic ? vb : nullptr, cubic ? v3 : nullptr};
-    fe *ex[4] = {nullptr, nullptr, nullptr, nullptr};
-    for (int v = 0; v < (cubic ? 4 : 2); v++) {
-      ex[v] = ob.alloc<fe>(blocks * D);
-      ntt_batched(td, src[v], d, (uint32_t)d, coef, blocks, true, s);
-      ntt_batched(tD, coef, d, (uint32_t)d, ex[v], blocks, false, s);
-    }
-    uint8_t *zf = nullptr;
-    if (cubic) {  // blocks whose p1 part is all zero are skipped (coSumcheck.cpp:21-27)
-      zf = ob.alloc<uint8_t>(blocks);
-      nonzero_blocks_launch(v1, blocks, logd[i], zf, s);
-    }
-    const int lanes = D >= 256 ? 1 : 256 / D;
-    const int per_cta = (int)std::max<uint64_t>((uint64_t)lanes, (pblocks + 607) / 608);
-    fe *cpart = ob.alloc<fe>((uint64_t)N * D * cophase1_parts(pblocks, per_cta));
-    cophase1_reduce_launch(ex[0], ex[1], ex[2], ex[3], zf, pblocks, logd[i] + ext, per_cta, cpart, H, s, N);
-    k_cosc_add_hr<<<N, 256, 0, s>>>(H, D, dR, Rst, ro, i, step, st);
-    k_put_party<<<dim3(grid(D), N), 256, 0, s>>>(H, D, N, tr, off_pp[i], 16ull * D);
-    aggregate_launch(H, N, D, dl, poly, s);
-    k_cosc_verify<<<1, 256, 0, s>>>(st, poly, logd[i], ext, i, LD, Ldh + at, scr, tr, off_poly[i], off_chal[i]);
-    k_cosc_sparse<<<1, 64, 0, s>>>(dR, Rst, ro, i, LD, D, N, st);
-    GBZ_CUDA(cudaGetLastError());
-    // phase 2 (coSumcheck.cpp:66-148, 201-213): every vector folded by Ld
-    for (fe *v : {v1, v2, v3, vb}) {
-      if (!v) continue;
-      cophase2_launch(v, (uint64_t)N * m, Ldh + at, logd[i], coef, s);
-      GBZ_CUDA(cudaMemcpyAsync(v, coef, 16ull * N * m / d, cudaMemcpyDeviceToDevice, s));
-    }
-    m /= d;
-    at += d;
-  }
-  fe *dcl = ob.alloc<fe>(rows);
-  k_cosc_final<<<1, 32, 0, s>>>(st, cubic ? 1 : 0, N, v1, v2, v3, vb, m, dU, db2, Ldh, dlog, ndeg, dr1, dcl, tr,
-                                off_sh, off_un, off_r, off_cl);
-  GBZ_CUDA(cudaGetLastError());
-  CoscDev hst;
-  GBZ_CUDA(cudaMemcpyAsync(&hst, st, sizeof(CoscDev), cudaMemcpyDeviceToHost, s));
-  std::vector<fe> hcl(rows);
-  GBZ_CUDA(cudaMemcpyAsync(hcl.data(), dcl, 16ull * rows, cudaMemcpyDeviceToHost, s));
-  if (transcript) {
-    const cudaMemcpyKind ko = mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    GBZ_CUDA(cudaMemcpyAsync(transcript, tr, lay.bytes, ko, s));
-  }
-  GBZ_CUDA(cudaStreamSynchronize(s));
-  // claims: rows x (eval, r vector [r_final, r_0, ..., r_{ndeg-1}])
-  std::vector<uint64_t> out((size_t)rows * 2 * (ndeg + 2));
-  for (int i = 0; i < rows; i++) {
-    uint64_t *o = out.data() + (size_t)i * 2 * (ndeg + 2);
-    o[0] = hcl[i].re;
-    o[1] = hcl[i].im;
-    o[2] = hst.fs.re;
-    o[3] = hst.fs.im;
-    for (int k = 0; k < ndeg; k++) {
-      o[4 + 2 * k] = hst.r[k].re;
-      o[5 + 2 * k] = hst.r[k].im;
-    }
-  }
+  const cudaMemcpyKind kin = mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   const cudaMemcpyKind ko = mem == GBZ_MEM_DEVICE ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost;
-  GBZ_CUDA(cudaMemcpy(claims, out.data(), 8 * out.size(), ko));
-  const uint64_t fsw[2] = {hst.fs.re, hst.fs.im};
-  GBZ_CUDA(cudaMemcpy(fs, fsw, 16, ko));
-  if (flags) *flags = hst.flags;
+  const CoscOut res = cosumcheck_run(ctx, form, N, n, (const fe *)p1, (const fe *)p2, (const fe *)p3, (const fe *)R, kin,
+                                     hr1.data(), nr1, hr2.data(), hK, hKr, degrees, ndeg, hfs, transcript,
+                                     mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, nullptr);
+  GBZ_CUDA(cudaMemcpy(claims, res.claims.data(), 16 * res.claims.size(), ko));
+  GBZ_CUDA(cudaMemcpy(fs, &res.fs, 16, ko));
+  if (flags) *flags = res.flags;
   API_END(ctx)
 }
 
 uint64_t gbz_cosumcheck_transcript_bytes(int form, int N, const int *degrees, int ndeg) {
-  if (!degrees || ndeg < 1 || N < 4) return 0;
-  const int ext = form == GBZ_SC_CUBIC ? 2 : 1, rows = form == GBZ_SC_CUBIC ? 4 : 5;
-  PcsLayout lay;
-  lay.add(T_PCS_CHALLENGE, 1, 16);
-  for (int i = 0; i < ndeg; i++) {
-    lay.add(T_PCS_PARTY_POLYS, (degrees[i] << ext) * N, 16);
-    lay.add(T_PCS_POLY, degrees[i] << ext, 16);
-    lay.add(T_PCS_CHALLENGE, 1, 16);
-  }
-  lay.add(T_COSC_FINAL_SHARES, rows * N, 16);
-  lay.add(T_COSC_UNPACKED, rows * (N / 2), 16);
-  lay.add(T_PCS_CHALLENGE, 1, 16);
-  lay.add(T_COSC_CLAIMS, rows, 16);
-  return lay.bytes;
+  return cosumcheck_bytes(form, N, degrees, ndeg);
 }
 
 }  // extern "C"

@@ -51,6 +51,8 @@ EXPORTS = (
     "gbz_pcs_info", "gbz_pcs_commit_data", "gbz_pcs_open", "gbz_pcs_claim", "gbz_cosumcheck",
     "gbz_cosumcheck_transcript_bytes", "gbz_whir_open", "gbz_whir_open_transcript_bytes",
     "gbz_merkle_tree_from_leaves", "gbz_pcs_open_full", "gbz_pcs_open_full_bytes", "gbz_sched_set_grouping",
+    "gbz_r1cs_create", "gbz_r1cs_free", "gbz_r1cs_reduce", "gbz_piop_phase1", "gbz_piop_phase1_bytes",
+    "gbz_piop_phase2", "gbz_piop_phase2_bytes",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -180,6 +182,15 @@ def _load():
         "gbz_pcs_open_full": (c_int, [vp, vp, vp, c_int, vp, vp, vp, vp, vp, u64, c_int]),
         "gbz_pcs_open_full_bytes": (c_int, [vp, vp]),
         "gbz_sched_set_grouping": (c_int, [vp, c_int]),
+        "gbz_r1cs_create": (c_int, [vp, c_int, u64, c_int, vp, vp, vp, vp]),
+        "gbz_r1cs_free": (c_int, [vp]),
+        "gbz_r1cs_reduce": (c_int, [vp, vp, vp, c_int, vp, c_int, vp, vp, vp, c_int]),
+        "gbz_piop_phase1": (c_int, [vp, c_int, u64, vp, vp, vp, vp, vp, vp, c_int, vp, vp, vp, vp, vp, vp, vp, u64,
+                                    c_int]),
+        "gbz_piop_phase1_bytes": (u64, [c_int, u64, vp, c_int]),
+        "gbz_piop_phase2": (c_int, [vp, c_int, u64, vp, vp, vp, c_int, vp, vp, vp, vp, c_int, vp, c_int, vp, vp, vp,
+                                    vp, vp, vp, vp, vp, vp, vp, u64, c_int]),
+        "gbz_piop_phase2_bytes": (u64, [c_int, vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -897,6 +908,97 @@ def cosumcheck(ctx, form, N, p1, p2, R, K, K_r, degrees, p3=None, r1=None, r2=No
                                  len(degrees), _ptr(f), _ptr(cl), ctypes.byref(flags), _ptr(tr), nb, MEM_HOST))
     claims = [(cl[i, 0], cl[i, 1:]) for i in range(rows)]
     return claims, flags.value, tr.tobytes(), f
+
+
+class R1cs:
+    """The parties' R1CS rows on the device (gbz_r1cs_create): per matrix A,
+    B, C a CSR (row pointers over N x rows rows, columns)."""
+
+    def __init__(self, ctx, N, rows, logm, ptrs, cols):
+        self.ctx, self.N, self.rows, self.logm = ctx, N, rows, logm
+        self._p = [np.ascontiguousarray(p, dtype=np.uint32) for p in ptrs]
+        self._c = [np.ascontiguousarray(c, dtype=np.uint32) for c in cols]
+        P = (ctypes.c_void_p * 3)(*[x.ctypes.data for x in self._p])
+        C = (ctypes.c_void_p * 3)(*[x.ctypes.data if x.size else None for x in self._c])
+        nnz = np.array([x.size for x in self._c], dtype=np.uint64)
+        self.h = ctypes.c_void_p()
+        ctx.check(lib.gbz_r1cs_create(ctx.h, N, rows, logm, P, C, _ptr(nnz), ctypes.byref(self.h)))
+
+    def reduce(self, r, degrees1):
+        """_reduce_R1CS_matrixes_multivariate at r (one entry per degree):
+        (RA, RB, RC), each N x rows."""
+        r = np.ascontiguousarray(r, dtype=np.uint64).reshape(-1, 2)
+        deg = np.ascontiguousarray(degrees1, dtype=np.int32)
+        outs = [np.zeros((self.N, self.rows, 2), dtype=np.uint64) for _ in range(3)]
+        self.ctx.check(lib.gbz_r1cs_reduce(self.ctx.h, self.h, _ptr(r), r.shape[0], _ptr(deg), len(deg),
+                                           *[_ptr(o) for o in outs], MEM_HOST))
+        return outs
+
+    def free(self):
+        if self.h:
+            lib.gbz_r1cs_free(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def piop_phase1(ctx, N, vL, vR, vO, masks, R1, degrees, fs, vectors=False):
+    """prove_phase1 (coPIOP.cpp:241-346) of N parties: (claims [(eval,
+    point)], ip N x sum 4d, ip_b1, flags, transcript, fs[, vectors])."""
+    a = [np.ascontiguousarray(x, dtype=np.uint64) for x in (vL, vR, vO)]
+    n = a[0].size // (2 * N)
+    m = np.ascontiguousarray(masks, dtype=np.uint64)
+    R = np.ascontiguousarray(R1, dtype=np.uint64)
+    deg = np.ascontiguousarray(degrees, dtype=np.int32)
+    f = np.array(np.asarray(fs, dtype=np.uint64).reshape(2), copy=True)
+    cl = np.zeros((4, len(deg) + 2, 2), dtype=np.uint64)
+    ip = np.zeros((N, 4 * int(deg.sum()), 2), dtype=np.uint64)
+    b1 = np.zeros((N // 4, 2), dtype=np.uint64)
+    vec = np.zeros((3, N, 2 * n, 2), dtype=np.uint64) if vectors else None
+    flags = ctypes.c_uint32(0)
+    nb = lib.gbz_piop_phase1_bytes(N, n, _ptr(deg), len(deg))
+    tr = np.zeros(nb, dtype=np.uint8)
+    ctx.check(lib.gbz_piop_phase1(ctx.h, N, n, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(m), _ptr(R), _ptr(deg),
+                                  len(deg), _ptr(f), _ptr(cl), _ptr(ip), _ptr(b1), _ptr(vec), ctypes.byref(flags),
+                                  _ptr(tr), nb, MEM_HOST))
+    claims = [(cl[i, 0], cl[i, 1:]) for i in range(4)]
+    out = (claims, ip, b1, flags.value, tr.tobytes(), f)
+    return out + (vec,) if vectors else out
+
+
+def piop_phase2(ctx, N, w, masks, r1cs, mask_l, R2, point1, evals1, degrees1, degrees2, K, fs, vectors=False):
+    """prove_phase2 (coPIOP.cpp:406-627) of N parties: (claims [(eval,
+    point)], abc, ip2, ip3, ip_b1, flags, transcript, fs[, vectors])."""
+    w = np.ascontiguousarray(w, dtype=np.uint64)
+    nw = w.size // (2 * N)
+    m = np.ascontiguousarray(masks, dtype=np.uint64)
+    R = np.ascontiguousarray(R2, dtype=np.uint64)
+    pt = np.ascontiguousarray(point1, dtype=np.uint64).reshape(-1, 2)
+    ev = np.ascontiguousarray(evals1, dtype=np.uint64).reshape(-1, 2)
+    d1 = np.ascontiguousarray(degrees1, dtype=np.int32)
+    d2 = np.ascontiguousarray(degrees2, dtype=np.int32)
+    Kk = np.ascontiguousarray(K, dtype=np.uint64).reshape(2)
+    f = np.array(np.asarray(fs, dtype=np.uint64).reshape(2), copy=True)
+    cl = np.zeros((5, len(d2) + 2, 2), dtype=np.uint64)
+    abc = np.zeros((3, 2), dtype=np.uint64)
+    ip2 = np.zeros((N, 2 * int(d2.sum()), 2), dtype=np.uint64)
+    ip3 = np.zeros((N, 12, 2), dtype=np.uint64)
+    b1 = np.zeros((N // 4, 2), dtype=np.uint64)
+    vec = np.zeros((2, N, 2 * nw, 2), dtype=np.uint64) if vectors else None
+    flags = ctypes.c_uint32(0)
+    nb = lib.gbz_piop_phase2_bytes(N, _ptr(d2), len(d2))
+    tr = np.zeros(nb, dtype=np.uint8)
+    ctx.check(lib.gbz_piop_phase2(ctx.h, N, nw, _ptr(w), _ptr(m), r1cs.h, mask_l, _ptr(R), _ptr(pt), _ptr(ev),
+                                  _ptr(d1), len(d1), _ptr(d2), len(d2), _ptr(Kk), _ptr(f), _ptr(cl), _ptr(abc),
+                                  _ptr(ip2), _ptr(ip3), _ptr(b1), _ptr(vec), ctypes.byref(flags), _ptr(tr), nb,
+                                  MEM_HOST))
+    claims = [(cl[i, 0], cl[i, 1:]) for i in range(5)]
+    out = (claims, abc, ip2, ip3, b1, flags.value, tr.tobytes(), f)
+    return out + (vec,) if vectors else out
 
 
 PCS_UNITS = {32: 32, 33: 32, 37: 4, 46: 32, 47: 4}

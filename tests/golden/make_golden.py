@@ -578,7 +578,7 @@ def gen_piop():
     import struct
     import tempfile
     out = {}
-    for N, logM in ((8, 16), (16, 16), (8, 18)):
+    for N, logM in ((8, 16), (16, 16), (8, 18), (16, 20)):
         with tempfile.TemporaryDirectory() as td:
             prefix = os.path.join(td, "cap")
             env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_CAPTURE=prefix, MINIMPI_TIMEOUT="300",
