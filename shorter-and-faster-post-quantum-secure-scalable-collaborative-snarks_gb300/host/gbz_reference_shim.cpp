@@ -26,11 +26,12 @@
 // levels with no data-parallel work.
 //
 // The N-party calls of libgbz (gbz_pcs_commit / gbz_pcs_open,
-// gbz_cosumcheck, gbz_party_sumcheck) take every party's share at once, the
-// one-device model of the collaborative prover; they replace the N-rank
-// runs of PCS_commit / PCS_open_new, quadratic/cubic_coSumcheck and
-// _quadratic/_cubic_sumcheck, whose per-rank signatures hold one share, so
-// they are called through the C ABI directly (INTEGRATION.md).
+// gbz_cosumcheck, gbz_party_sumcheck, gbz_piop_phase1 / gbz_piop_phase2)
+// take every party's share at once, the one-device model of the
+// collaborative prover; they replace the N-rank runs of PCS_commit /
+// PCS_open_new, quadratic/cubic_coSumcheck, _quadratic/_cubic_sumcheck and
+// prove_phase1 / prove_phase2, whose per-rank signatures hold one share, so
+// they are called through the C ABI directly.
 //
 // Errors: the reference prints and exits; this shim does the same on a
 // non-OK status so that callers see unchanged behaviour.
