@@ -675,6 +675,33 @@ gbz_status gbz_piop_phase2(gbz_ctx *ctx, int N, uint64_t nw, const uint64_t *w, 
                            uint64_t capacity, int mem);
 uint64_t gbz_piop_phase2_bytes(int N, const int *degrees2, int ndeg2);
 
+/* ------------------------------------------------- distributed PCS (witness) */
+
+/* Batch_dCommit (distributed_PCS.cpp:56-147) of N parties (8 <= N <= 64):
+ * arr, arr2: N x A.  Row k < batch of party p is arr_p[k S, (k+1) S)
+ * (S = A / batch) zero-padded to L = rate S; the reference's distributed
+ * FFT over the N ranks (distributed_batch_FFT, MPI_utils.cpp:3133-3298) is
+ * the transform of length N L of the rows interleaved across the parties
+ * (party p's entry t is coefficient t N + p), party r keeping the L/N
+ * outputs from r L/N + m L for every m < N.  Each party's tree hashes the
+ * columns of its batch rows (MT_commit_Blake over the column) and builds
+ * create_tree_blake over the L column hashes; the leader's root is taken
+ * over {party 0's root, 0, ..., 0}.  Outputs (each may be NULL):
+ * commit_data (N x A: arr2, as the reference keeps it), codewords (N x
+ * batch x L), levels (N x (2L - 1) x 32, leaves first), roots (N x 32, host),
+ * leader_root (32, host).  batch: a power of two in [4, 64]. */
+gbz_status gbz_dpcs_batch_commit(gbz_ctx *ctx, int N, uint64_t A, const uint64_t *arr, const uint64_t *arr2, int rate,
+                                 int batch, uint64_t *commit_data, uint64_t *codewords, uint8_t *levels, uint8_t *roots,
+                                 uint8_t *leader_root, int mem);
+
+/* dCommit (distributed_PCS.cpp:150-170): one row of A entries per party,
+ * codeword N x (rate A) by the same distributed transform; the columns are
+ * d = 2^(log2 N - log2 N / 2) entries spaced rate A / d apart (the fold
+ * degree plaintext_degrees[1] of prepare_data, :28-54); levels: N x
+ * (2 rate A / d - 1) x 32. */
+gbz_status gbz_dpcs_commit(gbz_ctx *ctx, int N, uint64_t A, const uint64_t *arr, int rate, uint64_t *codeword,
+                           uint8_t *levels, uint8_t *roots, uint8_t *leader_root, int mem);
+
 /* --------------------------------------------------------------- prover */
 
 /* Bytes of the transcript of one proof of a 2^logn witness at `rate`. */

@@ -52,7 +52,7 @@ EXPORTS = (
     "gbz_cosumcheck_transcript_bytes", "gbz_whir_open", "gbz_whir_open_transcript_bytes",
     "gbz_merkle_tree_from_leaves", "gbz_pcs_open_full", "gbz_pcs_open_full_bytes", "gbz_sched_set_grouping",
     "gbz_r1cs_create", "gbz_r1cs_free", "gbz_r1cs_reduce", "gbz_piop_phase1", "gbz_piop_phase1_bytes",
-    "gbz_piop_phase2", "gbz_piop_phase2_bytes",
+    "gbz_piop_phase2", "gbz_piop_phase2_bytes", "gbz_dpcs_batch_commit", "gbz_dpcs_commit",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -191,6 +191,8 @@ def _load():
         "gbz_piop_phase2": (c_int, [vp, c_int, u64, vp, vp, vp, c_int, vp, vp, vp, vp, c_int, vp, c_int, vp, vp, vp,
                                     vp, vp, vp, vp, vp, vp, vp, u64, c_int]),
         "gbz_piop_phase2_bytes": (u64, [c_int, vp, c_int]),
+        "gbz_dpcs_batch_commit": (c_int, [vp, c_int, u64, vp, vp, c_int, c_int, vp, vp, vp, vp, vp, c_int]),
+        "gbz_dpcs_commit": (c_int, [vp, c_int, u64, vp, c_int, vp, vp, vp, vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -999,6 +1001,41 @@ def piop_phase2(ctx, N, w, masks, r1cs, mask_l, R2, point1, evals1, degrees1, de
     claims = [(cl[i, 0], cl[i, 1:]) for i in range(5)]
     out = (claims, abc, ip2, ip3, b1, flags.value, tr.tobytes(), f)
     return out + (vec,) if vectors else out
+
+
+def dpcs_batch_commit(ctx, arr, arr2, rate, batch):
+    """Batch_dCommit (distributed_PCS.cpp:56-147) of N parties (arr, arr2:
+    N x A): (commit_data, codewords N x batch x L, levels N x (2L-1) x 32,
+    roots N x 32, leader root)."""
+    arr = np.ascontiguousarray(arr, dtype=np.uint64)
+    arr2 = np.ascontiguousarray(arr2, dtype=np.uint64)
+    N, A = arr.shape[0], arr.shape[1]
+    L = A // batch * rate
+    cd = np.zeros_like(arr2)
+    cw = np.zeros((N, batch, L, 2), dtype=np.uint64)
+    lv = np.zeros((N, 2 * L - 1, 32), dtype=np.uint8)
+    roots = np.zeros((N, 32), dtype=np.uint8)
+    lead = np.zeros(32, dtype=np.uint8)
+    ctx.check(lib.gbz_dpcs_batch_commit(ctx.h, N, A, _ptr(arr), _ptr(arr2), rate, batch, _ptr(cd), _ptr(cw), _ptr(lv),
+                                        _ptr(roots), _ptr(lead), MEM_HOST))
+    return cd, cw, lv, roots, lead
+
+
+def dpcs_commit(ctx, arr, rate):
+    """dCommit (distributed_PCS.cpp:150-170) of N parties (arr: N x A):
+    (codeword N x rate A, levels, roots N x 32, leader root)."""
+    arr = np.ascontiguousarray(arr, dtype=np.uint64)
+    N, A = arr.shape[0], arr.shape[1]
+    lN = N.bit_length() - 1
+    d = 1 << (lN - lN // 2)
+    L = A * rate
+    cw = np.zeros((N, L, 2), dtype=np.uint64)
+    lv = np.zeros((N, 2 * (L // d) - 1, 32), dtype=np.uint8)
+    roots = np.zeros((N, 32), dtype=np.uint8)
+    lead = np.zeros(32, dtype=np.uint8)
+    ctx.check(lib.gbz_dpcs_commit(ctx.h, N, A, _ptr(arr), rate, _ptr(cw), _ptr(lv), _ptr(roots), _ptr(lead),
+                                  MEM_HOST))
+    return cw, lv, roots, lead
 
 
 PCS_UNITS = {32: 32, 33: 32, 37: 4, 46: 32, 47: 4}

@@ -67,6 +67,8 @@ def main():
             manifest["cosumcheck"] = gen_cosumcheck()
         if "piop" in only:
             manifest["piop"] = gen_piop()
+        if "dpcs" in only:
+            manifest["dpcs"] = gen_dpcs()
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
             json.dump(manifest, f, indent=1)
         print("updated", sorted(only))
@@ -645,6 +647,65 @@ def gen_piop():
         out[name] = {"file": name + ".json", "N": N, "logM": logM}
         print("piop N=%d M=2^%d: reference %.1f s" % (N, logM, dt), flush=True)
     return out
+
+
+DPCS = os.path.join(ROOT, "oracle", "_ref", "pigeon_dpcs")
+DPCS_CASES = [("batch", 8, 12, 8, 4, 5), ("batch", 16, 14, 16, 4, 6), ("batch", 8, 13, 4, 8, 7),
+              ("batch", 32, 10, 32, 2, 8), ("single", 8, 12, 0, 4, 9), ("single", 16, 13, 0, 2, 10),
+              ("single", 32, 10, 0, 4, 11)]
+
+
+def gen_dpcs():
+    """Batch_dCommit / dCommit (distributed_PCS.cpp:56-170) run unmodified
+    with N ranks (oracle/ref/dpcs_mpi_driver.cpp) on seeded per-rank
+    arrays.  Kept per case and rank: the digests of the codeword rows, of
+    commit_data (Batch_dCommit) and of every level of the rank's tree, its
+    root, and rank 0's leader root."""
+    import struct
+    import tempfile
+    out = {}
+    for mode, N, logA, batch, rate, seed in DPCS_CASES:
+        A = 1 << logA
+        with tempfile.TemporaryDirectory() as td:
+            prefix = os.path.join(td, "dp")
+            env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_TIMEOUT="300")
+            args = [DPCS, mode, str(logA)] + ([str(batch)] if mode == "batch" else []) + [str(rate), str(seed), prefix]
+            subprocess.run(args, env=env, check=True, capture_output=True, text=True)
+            ranks = []
+            for r in range(N):
+                b = open("%s.%d" % (prefix, r), "rb").read()
+                o = 0
+                if mode == "batch":
+                    nb, L = struct.unpack_from("<II", b, 0)
+                    o = 8
+                    cd = b[o:o + 16 * A]
+                    o += 16 * A
+                    cw = b[o:o + 16 * nb * L]
+                    o += 16 * nb * L
+                else:
+                    (L,) = struct.unpack_from("<I", b, 0)
+                    o = 4
+                    cd = None
+                    cw = b[o:o + 16 * L]
+                    o += 16 * L
+                root = b[o:o + 32]
+                o += 32
+                (cnt,) = struct.unpack_from("<I", b, o)
+                o += 4
+                lv = b[o:o + 32 * cnt]
+                o += 32 * cnt
+                e = {"codewords_sha256": hashlib.sha256(cw).hexdigest(), "root": root.hex(),
+                     "levels": cnt, "levels_sha256": hashlib.sha256(lv).hexdigest()}
+                if cd is not None:
+                    e["commit_data_sha256"] = hashlib.sha256(cd).hexdigest()
+                if r == 0:
+                    e["leader_root"] = b[o:o + 32].hex()
+                ranks.append(e)
+        name = "%s_N%d_A%d_b%d_r%d" % (mode, N, logA, batch, rate)
+        out[name] = {"mode": mode, "N": N, "logA": logA, "batch": batch, "rate": rate, "seed": seed, "ranks": ranks}
+    with open(os.path.join(HERE, "dpcs.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    return {"file": "dpcs.json", "cases": sorted(out)}
 
 
 if __name__ == "__main__":
