@@ -702,6 +702,29 @@ gbz_status gbz_dpcs_batch_commit(gbz_ctx *ctx, int N, uint64_t A, const uint64_t
 gbz_status gbz_dpcs_commit(gbz_ctx *ctx, int N, uint64_t A, const uint64_t *arr, int rate, uint64_t *codeword,
                            uint8_t *levels, uint8_t *roots, uint8_t *leader_root, int mem);
 
+/* ------------------------------------------------------------- verifier */
+
+/* Checks a gbz_prove transcript of a 2^logn witness at `rate` whose glibc
+ * stream was seeded with prng_seed, from the transcript alone (host code, no
+ * context): the evaluation point and every sumcheck challenge against the
+ * Fiat-Shamir chain, every round message against the running claim, the
+ * final values against the last claim and eq(z, challenges); per WHIR
+ * iteration the round messages against K, the challenges, queries and
+ * combination weights against the glibc stream, every folded answer against
+ * its replies, and K; then Whir_Open's verification steps 2 and 3
+ * (Whir.cpp:441-467) with the betas' final values formed from the closed
+ * forms of their terms.  The commitment roots and paths are not checked
+ * (with inner nodes hashing their left child twice, merkle_tree.cpp:267-299,
+ * a path does not bind a query's replies).  The reference has no standalone
+ * verifier; these are the checks its prover runs inline.  *failed (may be
+ * NULL) gets one bit per failed check: 1 layout, 2 evaluation point, 4
+ * sumcheck sum, 8 sumcheck challenge, 16 final values, 32 WHIR sum, 64 WHIR
+ * challenge, 128 queries, 256 answers, 512 combination weights, 1024 K,
+ * 2048 final point, 4096 step 2, 8192 step 3.  Returns GBZ_OK when every
+ * check holds, GBZ_ECHECK otherwise. */
+gbz_status gbz_verify_proof(const uint8_t *transcript, uint64_t bytes, int logn, int rate, uint32_t prng_seed,
+                            uint32_t *failed);
+
 /* --------------------------------------------------------------- prover */
 
 /* Bytes of the transcript of one proof of a 2^logn witness at `rate`. */

@@ -52,7 +52,7 @@ EXPORTS = (
     "gbz_cosumcheck_transcript_bytes", "gbz_whir_open", "gbz_whir_open_transcript_bytes",
     "gbz_merkle_tree_from_leaves", "gbz_pcs_open_full", "gbz_pcs_open_full_bytes", "gbz_sched_set_grouping",
     "gbz_r1cs_create", "gbz_r1cs_free", "gbz_r1cs_reduce", "gbz_piop_phase1", "gbz_piop_phase1_bytes",
-    "gbz_piop_phase2", "gbz_piop_phase2_bytes", "gbz_dpcs_batch_commit", "gbz_dpcs_commit",
+    "gbz_piop_phase2", "gbz_piop_phase2_bytes", "gbz_dpcs_batch_commit", "gbz_dpcs_commit", "gbz_verify_proof",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -193,6 +193,7 @@ def _load():
         "gbz_piop_phase2_bytes": (u64, [c_int, vp, c_int]),
         "gbz_dpcs_batch_commit": (c_int, [vp, c_int, u64, vp, vp, c_int, c_int, vp, vp, vp, vp, vp, c_int]),
         "gbz_dpcs_commit": (c_int, [vp, c_int, u64, vp, c_int, vp, vp, vp, vp, c_int]),
+        "gbz_verify_proof": (c_int, [vp, u64, c_int, c_int, ctypes.c_uint32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -1001,6 +1002,20 @@ def piop_phase2(ctx, N, w, masks, r1cs, mask_l, R2, point1, evals1, degrees1, de
     claims = [(cl[i, 0], cl[i, 1:]) for i in range(5)]
     out = (claims, abc, ip2, ip3, b1, flags.value, tr.tobytes(), f)
     return out + (vec,) if vectors else out
+
+
+VERIFY_CHECKS = ("layout", "point", "sumcheck_sum", "sumcheck_challenge", "sumcheck_final", "whir_sum",
+                 "whir_challenge", "queries", "answers", "combine", "whir_K", "final_point", "step2", "step3")
+
+
+def verify_proof(transcript, logn, rate, prng_seed=1):
+    """gbz_verify_proof: (ok, names of the failed checks)."""
+    tr = np.frombuffer(bytes(transcript), dtype=np.uint8)
+    failed = ctypes.c_uint32(0)
+    st = lib.gbz_verify_proof(_ptr(tr), tr.size, logn, rate, prng_seed, ctypes.byref(failed))
+    if st not in (0, 4):
+        raise GbzError(st, "gbz_verify_proof: bad arguments")
+    return st == 0, [n for i, n in enumerate(VERIFY_CHECKS) if failed.value >> i & 1]
 
 
 def dpcs_batch_commit(ctx, arr, arr2, rate, batch):
