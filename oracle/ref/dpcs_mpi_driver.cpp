@@ -9,6 +9,16 @@
 //
 //   pigeon_dpcs batch  <logA> <batch> <rate> <seed> <out prefix>   Batch_dCommit(arr, arr2, ..., rate, N, batch)
 //   pigeon_dpcs single <logA> <rate> <seed> <out prefix>           dCommit(arr, codeword, C, rate, N, 0)
+//   pigeon_dpcs open   <P> <logA> <batch> <rate> <seed> <out prefix>
+//       P (2 or 3) Batch_dCommit calls as coPIOP_prove makes them
+//       (coPIOP.cpp:868, 1708-1730), then PIOP_dOpen_batch_new
+//       (distributed_PCS.cpp:1175-1534) with Verify = {true, false} on
+//       points drawn from a stream all ranks share and claims y_l = the
+//       committed data's evaluations; the data (arr2) of every polynomial
+//       but the first is zero, as the dummy index's is, so that the first
+//       round's check holds.  Rank 0 then writes the opening's final WHIR
+//       inputs (whir_polys, whir_c, whir_betas, whir_claims, the tree root)
+//       at slot 1 of the WHIR batch (sorted_indexes = identity).
 //
 // Rank p's inputs: arr (then arr2) of 2^logA extension-field elements from a
 // SplitMix64 stream seeded with seed and p.  prepare_data(N, rate)
@@ -25,6 +35,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "coPCS.h"
@@ -79,11 +90,108 @@ void put_levels(FILE *f, const vector<vector<_hash>> &levels) {
 
 }  // namespace
 
+extern vector<vector<F>> whir_polys, whir_c, whir_betas;  // coPIOP.cpp:47-55
+extern vector<vector<vector<_hash>>> whir_MTs;
+extern vector<F> whir_claims;
+extern vector<int> whir_rates, sorted_indexes;
+extern std::unordered_map<int, int> whir_kappas;
+
+namespace {
+
+vector<F> beta_table(const vector<F> &r) {
+  vector<F> b;
+  precompute_beta(r, b);
+  return b;
+}
+
+int open_mode(int argc, char **argv, int rank, int N) {
+  if (argc < 8) {
+    if (!rank) fprintf(stderr, "usage: pigeon_dpcs open P logA batch rate seed out\n");
+    MPI_Abort(MPI_COMM_WORLD, 2);
+  }
+  const int P = atoi(argv[2]), logA = atoi(argv[3]), nb = atoi(argv[4]), rate = atoi(argv[5]);
+  const uint64_t seed = strtoull(argv[6], nullptr, 0);
+  const char *out = argv[7];
+  const size_t A = 1ull << logA, S = A / nb;
+  prepare_data(N, rate);
+  // the WHIR batch slots the opening writes into (get_whir_rates, Whir.cpp:18)
+  whir_rates = {rate, rate, rate, rate};
+  sorted_indexes = {0, 1, 2, 3};
+  for (size_t sz = 1; sz <= (1u << 26); sz <<= 1) whir_kappas[(int)sz] = 4;
+  whir_polys.resize(4);
+  whir_c.resize(4);
+  whir_betas.resize(4);
+  whir_MTs.resize(4);
+  whir_claims.resize(4);
+  vector<vector<vector<F>>> cd(P), cw(P);
+  vector<MT> C(P);
+  vector<vector<F>> r(P);
+  vector<F> y(P, F(0));
+  int lrows = 0;
+  while ((1 << lrows) < nb) lrows++;
+  int lN = 0;
+  while ((1 << lN) < N) lN++;
+  int lS = 0;
+  while (((size_t)1 << lS) < S) lS++;
+  SplitMix gs{seed * 0x7F4A7C15ull + 3};  // shared by all ranks
+  for (int l = 0; l < P; l++) {
+    // every rank's arrays, so that each can form the claim
+    vector<vector<F>> arr2_all(N);
+    vector<F> arr_mine;
+    for (int p = 0; p < N; p++) {
+      SplitMix g{seed * 0x10001ull + (uint64_t)p * 0x9E3779B1ull + 11 + 0x1000ull * l};
+      vector<F> a(A), a2(A);
+      for (auto &x : a) x = g.fe();
+      for (auto &x : a2) x = g.fe();
+      if (l > 0)
+        for (auto &x : a2) x = F(0);
+      if (p == rank) arr_mine = a;
+      arr2_all[p] = a2;
+    }
+    vector<F> arr2_mine = arr2_all[rank];
+    Batch_dCommit(arr_mine, arr2_mine, cd[l], cw[l], C[l], rate, N, nb);
+    for (int i = 0; i < lS + lrows + lN; i++) r[l].push_back(gs.fe());
+    // y_l = sum_p b1[p] sum_k b2[k] sum_h b3[h] arr2_p[h S + k]
+    // (r = (r2: log S, r3: log rows, r1: log N), distributed_PCS.cpp:1188-1203)
+    vector<F> r2(r[l].begin(), r[l].begin() + lS), r3(r[l].begin() + lS, r[l].begin() + lS + lrows),
+        r1(r[l].begin() + lS + lrows, r[l].end());
+    vector<F> b1 = beta_table(r1), b2 = beta_table(r2), b3 = beta_table(r3);
+    for (int p = 0; p < N; p++)
+      for (int h = 0; h < nb; h++)
+        for (size_t k = 0; k < S; k++) y[l] = y[l] + b1[p] * b2[k] * b3[h] * arr2_all[p][h * S + k];
+  }
+  vector<bool> verify = {true, false};
+  PIOP_dOpen_batch_new(cd, cw, C, r, y, verify, N);
+  if (rank == 0) {
+    char path[4096];
+    snprintf(path, sizeof path, "%s.%d", out, rank);
+    FILE *f = fopen(path, "wb");
+    if (!f) MPI_Abort(MPI_COMM_WORLD, 3);
+    vector<F> yv = y;
+    put_u32(f, (uint32_t)yv.size());
+    put_fes(f, yv);
+    put_u32(f, (uint32_t)whir_polys[1].size());
+    put_fes(f, whir_polys[1]);
+    put_u32(f, (uint32_t)whir_c[1].size());
+    put_fes(f, whir_c[1]);
+    put_u32(f, (uint32_t)whir_betas[1].size());
+    put_fes(f, whir_betas[1]);
+    put_fes(f, vector<F>{whir_claims[1]});
+    put_root(f, whir_MTs[1]);
+    fclose(f);
+  }
+  MPI_Finalize();
+  return 0;
+}
+
+}  // namespace
+
 int main(int argc, char **argv) {
   MPI_Init(&argc, &argv);
   int rank = 0, N = 1;
   MPI_Comm_rank(MPI_COMM_WORLD, &rank);
   MPI_Comm_size(MPI_COMM_WORLD, &N);
+  if (argc >= 2 && std::string(argv[1]) == "open") return open_mode(argc, argv, rank, N);
   const bool batch = argc >= 2 && std::string(argv[1]) == "batch";
   if ((batch && argc < 7) || (!batch && argc < 6)) {
     if (!rank) fprintf(stderr, "usage: pigeon_dpcs batch logA batch rate seed out | single logA rate seed out\n");

@@ -559,4 +559,32 @@ vector<double> __wrap__Z21send_performance_dataSt6vectorIdSaIdEEi(vector<double>
   return __real__Z21send_performance_dataSt6vectorIdSaIdEEi(v, N);
 }
 
+// coPCS.cpp:369  distributed_commit_batch(Com, N): every commitment's local
+// root, then the leader's (the distributed PCS opening's batched and FRI
+// commitments, distributed_PCS.cpp:357, 632)
+void __real__Z24distributed_commit_batchRSt6vectorI2MTSaIS0_EEi(vector<MT> &Com, int N);
+void __wrap__Z24distributed_commit_batchRSt6vectorI2MTSaIS0_EEi(vector<MT> &Com, int N) {
+  __real__Z24distributed_commit_batchRSt6vectorI2MTSaIS0_EEi(Com, N);
+  if (piop_on())
+    for (auto &c : Com) {
+      put_root("DCBL", (int)c.Base_MT[0].size(), c.Base_MT);
+      put_root("DCBR", N, c.Root_MT);
+    }
+}
+
+// MPI_utils.cpp:3508  send_codeword_batch(arr, B, codeword, fold_depth, N):
+// what the leader holds after gathering every party's data
+void __real__Z19send_codeword_batchRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES6_S6_ii(
+    vector<vector<F>> &arr, vector<vector<F>> &B, vector<vector<F>> &cw, int fold_depth, int N);
+void __wrap__Z19send_codeword_batchRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES6_S6_ii(
+    vector<vector<F>> &arr, vector<vector<F>> &B, vector<vector<F>> &cw, int fold_depth, int N) {
+  __real__Z19send_codeword_batchRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES6_S6_ii(arr, B, cw, fold_depth,
+                                                                                             N);
+  if (piop_on()) {
+    put_field("SCBA", arr[0]);
+    put_field("SCBB", B[0]);
+    put_field("SCBC", cw[0]);
+  }
+}
+
 }  // extern "C"

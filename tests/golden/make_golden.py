@@ -244,6 +244,7 @@ CAPTURE_UNIT = {"H2FI": 16, "H2FO": 16, "FRND": 16, "SHRS": 16, "PAGI": 16, "PAG
                 "GIDX": 4, "RAND": 4, "GSQU": 4, "MTCB": 36, "CTRB": 36, "WCIR": 36}
 # the R1CS front end's records (MINIMPI_CAPTURE_PIOP)
 CAPTURE_UNIT.update({t: 4 for t in ("RNCT", "PLMN", "SURN", "PCCN", "CBDG", "RDDG", "QDDG", "CBCN", "QDCN")})
+CAPTURE_UNIT.update({"DCBL": 36, "DCBR": 36, "SCBA": 16, "SCBB": 16, "SCBC": 16})
 CAPTURE_UNIT.update({t: 16 for t in ("DPDL", "DPDR", "DPDO", "DPDW", "GSR0", "GSR1", "GSRK", "SURO", "PCWI", "PCRI",
                                      "PCCD", "PCFS", "CKRO", "CBP1", "CBP2", "CBP3", "CBR1", "CBR2", "CBRR", "CBKK",
                                      "CBCL", "CBIP", "RDIR", "SIP1", "RDRA", "RDRB", "RDRC", "SSVI", "SSVO", "QDP1",
@@ -650,6 +651,7 @@ def gen_piop():
 
 
 DPCS = os.path.join(ROOT, "oracle", "_ref", "pigeon_dpcs")
+DPCS_OPEN_CASES = [(2, 8, 12, 8, 4, 21), (2, 16, 13, 8, 4, 22), (3, 8, 11, 4, 2, 23), (2, 32, 11, 4, 4, 24)]
 DPCS_CASES = [("batch", 8, 12, 8, 4, 5), ("batch", 16, 14, 16, 4, 6), ("batch", 8, 13, 4, 8, 7),
               ("batch", 32, 10, 32, 2, 8), ("single", 8, 12, 0, 4, 9), ("single", 16, 13, 0, 2, 10),
               ("single", 32, 10, 0, 4, 11)]
@@ -703,6 +705,50 @@ def gen_dpcs():
                 ranks.append(e)
         name = "%s_N%d_A%d_b%d_r%d" % (mode, N, logA, batch, rate)
         out[name] = {"mode": mode, "N": N, "logA": logA, "batch": batch, "rate": rate, "seed": seed, "ranks": ranks}
+    for P, N, logA, batch, rate, seed in DPCS_OPEN_CASES:
+        with tempfile.TemporaryDirectory() as td:
+            prefix, cap = os.path.join(td, "op"), os.path.join(td, "cap")
+            env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_TIMEOUT="300", MINIMPI_CAPTURE=cap,
+                       MINIMPI_CAPTURE_PIOP="1")
+            log = subprocess.run([DPCS, "open", str(P), str(logA), str(batch), str(rate), str(seed), prefix], env=env,
+                                 check=True, capture_output=True, text=True)
+            ranks = [capture_records("%s.%d" % (cap, r)) for r in range(N)]
+            b = open(prefix + ".0", "rb").read()
+        o = 0
+
+        def fes_at(n):
+            nonlocal o
+            v = b[o:o + 16 * n]
+            o += 16 * n
+            return v
+
+        def u32():
+            nonlocal o
+            (v,) = struct.unpack_from("<I", b, o)
+            o += 4
+            return v
+
+        y = fes_at(u32())
+        polys = fes_at(u32())
+        cw = fes_at(u32())
+        betas = fes_at(u32())
+        claim = fes_at(1)
+        root = b[o:o + 32]
+        lead = ranks[0]
+        tags = [t for t, _, _ in lead]
+        hin = [p for t, _, p in lead if t == "H2FI"]
+        case = {"mode": "open", "P": P, "N": N, "logA": logA, "batch": batch, "rate": rate, "seed": seed,
+                "y": y.hex(), "draws": [p.hex() for t, _, p in lead if t == "H2FO"],
+                "eval_claims": hin[0].hex(), "round_polys": [h.hex() for h in hin[4:]],
+                "leader_roots": [p[4:].hex() for t, _, p in lead if t == "DCBR"],
+                "whir_arr_sha256": hashlib.sha256(polys).hexdigest(), "whir_codeword_sha256": hashlib.sha256(cw).hexdigest(),
+                "whir_betas_sha256": hashlib.sha256(betas).hexdigest(), "whir_claim": claim.hex(), "whir_root": root.hex(),
+                "gathered_codeword_sha256": hashlib.sha256([p for t, _, p in lead if t == "SCBC"][0]).hexdigest(),
+                "errors": [l for l in log.stdout.splitlines() if "Error" in l],
+                "ranks": [{"roots": [p[4:].hex() for t, _, p in rk if t == "DCBL"],
+                           "queries": [hashlib.sha256(p).hexdigest() for t, _, p in rk if t == "GIDX"]} for rk in ranks]}
+        name = "open_P%d_N%d_A%d_b%d_r%d" % (P, N, logA, batch, rate)
+        out[name] = case
     with open(os.path.join(HERE, "dpcs.json"), "w") as f:
         json.dump(out, f, indent=1)
     return {"file": "dpcs.json", "cases": sorted(out)}
