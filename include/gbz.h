@@ -702,6 +702,38 @@ gbz_status gbz_dpcs_batch_commit(gbz_ctx *ctx, int N, uint64_t A, const uint64_t
 gbz_status gbz_dpcs_commit(gbz_ctx *ctx, int N, uint64_t A, const uint64_t *arr, int rate, uint64_t *codeword,
                            uint8_t *levels, uint8_t *roots, uint8_t *leader_root, int mem);
 
+/* PIOP_dOpen_batch_new (distributed_PCS.cpp:1175-1534) of N parties (8 <=
+ * N <= 64), P = 2 or 3 committed polynomials (batches = 1): commit_data,
+ * codewords: per polynomial what gbz_dpcs_batch_commit returns (P x N x rows
+ * x S, P x N x rows x L, L = rate S); points: P x (log2 S + log2 rows +
+ * log2 N) (r2, r3, r1 as the reference splits them); claims: P; verify: the
+ * reference's Verify[0].  Row-batches every party's data and codeword,
+ * forms the eval claims, draws a and b (b[0] set to zero), batches the data
+ * with weights {1, b[0], b[1]} as PIOP_dBatch_batched_new receives them,
+ * commits the batched codeword (every party's slice of the distributed
+ * codeword, columns of plaintext_degrees[1] entries; the leader's root is
+ * taken over N zero leaves, coPCS.cpp:398-408) and draws get_indexes; then
+ * per fold degree (prepare_data's, :28-54) the parties' block products, the
+ * leader's sum, check, challenge and claim, the folds of the data, the
+ * betas and (RS_distributed_fold, coPCS_utils.cpp:440-504: the multifold of
+ * the global codeword) the codeword, and a commitment of the folded
+ * codeword but after the last; finally the leader's Whir_Commit_initial of
+ * the gathered data at whir_rate.  Outputs (may be NULL): arr_out, betas_out
+ * (N S / prod(degrees): the gathered data and betas, party by party), K_out
+ * (the claim), whir_codeword (whir_rate times that), whir_root (32, host);
+ * flags bit 0: the first check failed (the reference prints "Sumcheck
+ * Error Round" and returns; so does this call, with GBZ_OK).  Transcript
+ * (gbz_dpcs_open_bytes): 61 EVAL_CLAIMS 16B x P(P-1) | 62 DRAWS 16B x 4 (a0,
+ * a1, b0 as drawn, b1) | per commitment 63 ROOTS 32B x (N + 1) (parties',
+ * leader's), 64 QUERIES u32 x 2l ((party, position) per draw) | per round
+ * 65 POLY 16B x 2d, 66 CHALLENGE, 67 K | 68 WHIR_ROOT 32B. */
+gbz_status gbz_dpcs_open(gbz_ctx *ctx, int N, int P, int rows, uint64_t S, int rate, const uint64_t *commit_data,
+                         const uint64_t *codewords, const uint64_t *points, const uint64_t *claims, int verify,
+                         int whir_rate, uint64_t *fs, uint64_t *arr_out, uint64_t *betas_out, uint64_t *K_out,
+                         uint64_t *whir_codeword, uint8_t *whir_root, uint32_t *flags, uint8_t *transcript,
+                         uint64_t capacity, int mem);
+uint64_t gbz_dpcs_open_bytes(int N, int P, int rate);
+
 /* ------------------------------------------------------------- verifier */
 
 /* Checks a gbz_prove transcript of a 2^logn witness at `rate` whose glibc

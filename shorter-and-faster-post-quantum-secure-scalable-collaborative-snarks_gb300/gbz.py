@@ -53,6 +53,7 @@ EXPORTS = (
     "gbz_merkle_tree_from_leaves", "gbz_pcs_open_full", "gbz_pcs_open_full_bytes", "gbz_sched_set_grouping",
     "gbz_r1cs_create", "gbz_r1cs_free", "gbz_r1cs_reduce", "gbz_piop_phase1", "gbz_piop_phase1_bytes",
     "gbz_piop_phase2", "gbz_piop_phase2_bytes", "gbz_dpcs_batch_commit", "gbz_dpcs_commit", "gbz_verify_proof",
+    "gbz_dpcs_open", "gbz_dpcs_open_bytes",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -194,6 +195,9 @@ def _load():
         "gbz_dpcs_batch_commit": (c_int, [vp, c_int, u64, vp, vp, c_int, c_int, vp, vp, vp, vp, vp, c_int]),
         "gbz_dpcs_commit": (c_int, [vp, c_int, u64, vp, c_int, vp, vp, vp, vp, c_int]),
         "gbz_verify_proof": (c_int, [vp, u64, c_int, c_int, ctypes.c_uint32, vp]),
+        "gbz_dpcs_open": (c_int, [vp, c_int, c_int, c_int, u64, c_int, vp, vp, vp, vp, c_int, c_int, vp, vp, vp, vp,
+                                  vp, vp, vp, vp, u64, c_int]),
+        "gbz_dpcs_open_bytes": (u64, [c_int, c_int, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -1036,6 +1040,33 @@ def dpcs_batch_commit(ctx, arr, arr2, rate, batch):
     return cd, cw, lv, roots, lead
 
 
+def dpcs_open(ctx, commit_data, codewords, points, claims, rate, whir_rate, fs=(0, 0), verify=True):
+    """PIOP_dOpen_batch_new (distributed_PCS.cpp:1175-1534) of N parties:
+    commit_data P x N x rows x S, codewords P x N x rows x L.  Returns
+    (arr, betas, K, whir codeword, whir root, flags, transcript, fs)."""
+    cd = np.ascontiguousarray(commit_data, dtype=np.uint64)
+    cw = np.ascontiguousarray(codewords, dtype=np.uint64)
+    P, N, rows, S = cd.shape[0], cd.shape[1], cd.shape[2], cd.shape[3]
+    pts = np.ascontiguousarray(points, dtype=np.uint64)
+    ys = np.ascontiguousarray(claims, dtype=np.uint64)
+    lN = N.bit_length() - 1
+    D = (1 << (lN - lN // 2)) * (1 << (lN // 2))
+    na = N * S // D
+    arr = np.zeros((na, 2), dtype=np.uint64)
+    bet = np.zeros((na, 2), dtype=np.uint64)
+    K = np.zeros(2, dtype=np.uint64)
+    wc = np.zeros((na * whir_rate, 2), dtype=np.uint64)
+    root = np.zeros(32, dtype=np.uint8)
+    f = np.array(np.asarray(fs, dtype=np.uint64).reshape(2), copy=True)
+    flags = ctypes.c_uint32(0)
+    nb = lib.gbz_dpcs_open_bytes(N, P, rate)
+    tr = np.zeros(nb, dtype=np.uint8)
+    ctx.check(lib.gbz_dpcs_open(ctx.h, N, P, rows, S, rate, _ptr(cd), _ptr(cw), _ptr(pts), _ptr(ys), int(verify),
+                                whir_rate, _ptr(f), _ptr(arr), _ptr(bet), _ptr(K), _ptr(wc), _ptr(root),
+                                ctypes.byref(flags), _ptr(tr), nb, MEM_HOST))
+    return arr, bet, K, wc, root, flags.value, tr.tobytes(), f
+
+
 def dpcs_commit(ctx, arr, rate):
     """dCommit (distributed_PCS.cpp:150-170) of N parties (arr: N x A):
     (codeword N x rate A, levels, roots N x 32, leader root)."""
@@ -1053,7 +1084,7 @@ def dpcs_commit(ctx, arr, rate):
     return cw, lv, roots, lead
 
 
-PCS_UNITS = {32: 32, 33: 32, 37: 4, 46: 32, 47: 4}
+PCS_UNITS = {32: 32, 33: 32, 37: 4, 46: 32, 47: 4, 63: 32, 64: 4, 68: 32}
 # records of the batch opening with units other than a field element
 BATCH_UNITS = {19: 4, 22: 4, 23: 32, 24: 32}
 
