@@ -9,6 +9,14 @@
 //
 //   pigeon_dpcs batch  <logA> <batch> <rate> <seed> <out prefix>   Batch_dCommit(arr, arr2, ..., rate, N, batch)
 //   pigeon_dpcs single <logA> <rate> <seed> <out prefix>           dCommit(arr, codeword, C, rate, N, 0)
+//   pigeon_dpcs pcs    <logM> <seed> <out prefix>
+//       the coPCS test's dealing and PCS_commit (main.cpp:49-76), then
+//       PCS_open_new with isPIOP = true (coPCS.cpp:1310-1700) as
+//       coPIOP_prove calls it (coPIOP.cpp:1767-1773): input vectors b1 =
+//       the Lagrange vector over 32 points, b2 = the tensor of two Lagrange
+//       vectors (Lagrange_evals) over the row length, b3 = the one over N/4
+//       points, at points from a SplitMix64 stream; K = 0.  Rank 0 then
+//       writes the WHIR batch slots 2 and 3 the opening fills.
 //   pigeon_dpcs open   <P> <logA> <batch> <rate> <seed> <out prefix>
 //       P (2 or 3) Batch_dCommit calls as coPIOP_prove makes them
 //       (coPIOP.cpp:868, 1708-1730), then PIOP_dOpen_batch_new
@@ -95,6 +103,8 @@ extern vector<vector<vector<_hash>>> whir_MTs;
 extern vector<F> whir_claims;
 extern vector<int> whir_rates, sorted_indexes;
 extern std::unordered_map<int, int> whir_kappas;
+extern int randomness;          // coPCS.cpp:18
+extern vector<int> _queries;    // New_PCS.cpp:5
 
 namespace {
 
@@ -184,6 +194,89 @@ int open_mode(int argc, char **argv, int rank, int N) {
   return 0;
 }
 
+int pcs_mode(int argc, char **argv, int rank, int N) {
+  if (argc < 5) {
+    if (!rank) fprintf(stderr, "usage: pigeon_dpcs pcs logM seed out\n");
+    MPI_Abort(MPI_COMM_WORLD, 2);
+  }
+  const int logM = atoi(argv[2]);
+  const uint64_t seed = strtoull(argv[3], nullptr, 0);
+  const char *out = argv[4];
+  const int M = 1 << logM, k = N / 4, _k = N / 2;
+  vector<vector<int>> rate = {{4}, {4}, {4, 4}, {4, 4}};
+  vector<vector<F>> codeword, Commit_data;
+  vector<F> random_shares, shares;
+  MT C;
+  prepare_parameters(rate, rate.size(), N, M);
+  secret_share_coefficients(shares, M, N, _k, k);
+  secret_share_coefficients(random_shares, randomness * N / 4, N, _k, k);
+  PCS_commit(C, codeword, Commit_data, shares, random_shares, rate, N);
+  sorted_indexes = {0, 1, 2, 3};
+  whir_polys.resize(4);
+  whir_c.resize(4);
+  whir_betas.resize(4);
+  whir_MTs.resize(4);
+  whir_claims.resize(4);
+  // the input vectors (coPIOP.cpp:1741-1762)
+  const int Bs = (int)Commit_data[0].size();
+  int lB = 0;
+  while ((1 << lB) < Bs) lB++;
+  const int la = lB / 2, lb = lB - la;
+  SplitMix gs{seed * 0x7F4A7C15ull + 3};
+  const F p0 = gs.fe(), p1 = gs.fe(), p2 = gs.fe(), p3 = gs.fe();
+  int lk = 0;
+  while ((1 << lk) < N / 4) lk++;
+  vector<vector<F>> inputs(3), Lagrange_evals;
+  inputs[0] = compute_lagrange_coeff(getRootOfUnity(5), p0, 32);
+  Lagrange_evals.push_back(compute_lagrange_coeff(getRootOfUnity(la), p1, 1 << la));
+  Lagrange_evals.push_back(compute_lagrange_coeff(getRootOfUnity(lb), p2, 1 << lb));
+  inputs[1] = Lagrange_evals[0];
+  {
+    vector<F> buff(inputs[1].size() * Lagrange_evals[1].size());
+    for (size_t j = 0; j < Lagrange_evals[1].size(); j++)
+      for (size_t kk = 0; kk < inputs[1].size(); kk++)
+        buff[kk + j * inputs[1].size()] = Lagrange_evals[1][j] * inputs[1][kk];
+    inputs[1] = buff;
+  }
+  inputs[2] = compute_lagrange_coeff(getRootOfUnity(lk), p3, N / 4);
+  // the claim these vectors give the committed data: F_ip as the coPCS test
+  // forms it (main.cpp:93-106), with the row weights b1 and, as
+  // PCS_open_new uses them in this mode (coPCS.cpp:1328-1335), b2 zero on
+  // the last _queries[0] entries of a row
+  int batches = 0;
+  for (auto &row : Commit_data) {
+    if (row.empty()) break;
+    batches++;
+  }
+  const size_t rows = Commit_data.size();
+  vector<F> v(rows * Bs, F(0)), v1(rows * Bs, F(0));
+  for (int i = 0; i < batches - 1; i++)
+    for (int j = 0; j < Bs; j++) v[j * rows + i] = Commit_data[i][j];
+  for (int j = 0; j < Bs - _queries[0]; j++)
+    for (int i = 0; i < batches - 1; i++) v1[j * rows + i] = inputs[0][i] * inputs[1][j];
+  F K = F_ip(v, v1, inputs[2], k, _k, N);
+  PCS_open_new(C, codeword, Commit_data, inputs, Lagrange_evals, K, rate, N, true);
+  if (rank == 0) {
+    char path[4096];
+    snprintf(path, sizeof path, "%s.%d", out, rank);
+    FILE *f = fopen(path, "wb");
+    if (!f) MPI_Abort(MPI_COMM_WORLD, 3);
+    for (int slot = 2; slot < 4; slot++) {
+      put_u32(f, (uint32_t)whir_polys[slot].size());
+      put_fes(f, whir_polys[slot]);
+      put_u32(f, (uint32_t)whir_c[slot].size());
+      put_fes(f, whir_c[slot]);
+      put_u32(f, (uint32_t)whir_betas[slot].size());
+      put_fes(f, whir_betas[slot]);
+      put_fes(f, vector<F>{whir_claims[slot]});
+      put_root(f, whir_MTs[slot]);
+    }
+    fclose(f);
+  }
+  MPI_Finalize();
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -192,6 +285,7 @@ int main(int argc, char **argv) {
   MPI_Comm_rank(MPI_COMM_WORLD, &rank);
   MPI_Comm_size(MPI_COMM_WORLD, &N);
   if (argc >= 2 && std::string(argv[1]) == "open") return open_mode(argc, argv, rank, N);
+  if (argc >= 2 && std::string(argv[1]) == "pcs") return pcs_mode(argc, argv, rank, N);
   const bool batch = argc >= 2 && std::string(argv[1]) == "batch";
   if ((batch && argc < 7) || (!batch && argc < 6)) {
     if (!rank) fprintf(stderr, "usage: pigeon_dpcs batch logA batch rate seed out | single logA rate seed out\n");

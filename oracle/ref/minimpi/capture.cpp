@@ -298,6 +298,18 @@ F __wrap__Z18delegate_beta_evalSt6vectorIN5virgo12fieldElementESaIS1_EES_IS3_SaI
   return out;
 }
 
+// delegate_protocol.cpp:603  delegate_lagrange_eval(L1, L2, y, offset, queries, ps): the claim it starts from
+F __real__Z22delegate_lagrange_evalSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES5_S1_iiRd(
+    vector<vector<F>> L1, vector<vector<F>> L2, F y, int offset, int queries, double &ps);
+F __wrap__Z22delegate_lagrange_evalSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES5_S1_iiRd(
+    vector<vector<F>> L1, vector<vector<F>> L2, F y, int offset, int queries, double &ps) {
+  put_field("DLEY", vector<F>{y});
+  F out = __real__Z22delegate_lagrange_evalSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EES5_S1_iiRd(
+      L1, L2, y, offset, queries, ps);
+  put("DLEE", 0, nullptr, 0);
+  return out;
+}
+
 // Whir.cpp:608  aggregate_claims(arrays, arr, b_aggr, claims, K): the aggregated claim K and the
 // challenges (beta weights, then array weights)
 vector<vector<F>> __real__Z16aggregate_claimsRSt6vectorIS_IN5virgo12fieldElementESaIS1_EESaIS3_EERS3_S7_S_IS_ISt4pairIS1_S3_ESaIS9_EESaISB_EERS1_(

@@ -69,6 +69,8 @@ def main():
             manifest["piop"] = gen_piop()
         if "dpcs" in only:
             manifest["dpcs"] = gen_dpcs()
+        if "pcspiop" in only:
+            manifest["pcspiop"] = gen_pcspiop()
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
             json.dump(manifest, f, indent=1)
         print("updated", sorted(only))
@@ -244,7 +246,7 @@ CAPTURE_UNIT = {"H2FI": 16, "H2FO": 16, "FRND": 16, "SHRS": 16, "PAGI": 16, "PAG
                 "GIDX": 4, "RAND": 4, "GSQU": 4, "MTCB": 36, "CTRB": 36, "WCIR": 36}
 # the R1CS front end's records (MINIMPI_CAPTURE_PIOP)
 CAPTURE_UNIT.update({t: 4 for t in ("RNCT", "PLMN", "SURN", "PCCN", "CBDG", "RDDG", "QDDG", "CBCN", "QDCN")})
-CAPTURE_UNIT.update({"DCBL": 36, "DCBR": 36, "SCBA": 16, "SCBB": 16, "SCBC": 16})
+CAPTURE_UNIT.update({"DCBL": 36, "DCBR": 36, "SCBA": 16, "SCBB": 16, "SCBC": 16, "DLEY": 16, "DLEE": 0})
 CAPTURE_UNIT.update({t: 16 for t in ("DPDL", "DPDR", "DPDO", "DPDW", "GSR0", "GSR1", "GSRK", "SURO", "PCWI", "PCRI",
                                      "PCCD", "PCFS", "CKRO", "CBP1", "CBP2", "CBP3", "CBR1", "CBR2", "CBRR", "CBKK",
                                      "CBCL", "CBIP", "RDIR", "SIP1", "RDRA", "RDRB", "RDRC", "SSVI", "SSVO", "QDP1",
@@ -265,7 +267,7 @@ def capture_records(path):
     return out
 
 
-def expected_open_transcript(ranks, N, logM, rates):
+def expected_open_transcript(ranks, N, logM, rates, npoint=None):
     """The transcript gbz_pcs_open must write (layout: include/gbz.h), rebuilt
     from the reference ranks' own records: every party's round messages
     (PAGI), the leader's aggregates (PAGO) and challenges (H2FO), the roots
@@ -284,7 +286,7 @@ def expected_open_transcript(ranks, N, logM, rates):
     fe_list = lambda b: [tuple(int(x) for x in v) for v in np.frombuffer(b, dtype=np.uint64).reshape(-1, 2)]
     rec = lambda tag, count, payload: struct.pack("<II", tag, count) + payload
     lead = ranks[0]
-    h2fo = [r[2] for r in lead if r[0] == "H2FO"][logM + 1:]
+    h2fo = [r[2] for r in lead if r[0] == "H2FO"][logM + 1 if npoint is None else npoint:]
     pago = [r[2] for r in lead if r[0] == "PAGO"]
     pagi = [[r[2] for r in rk if r[0] == "PAGI"] for rk in ranks]
     gidx = [[r for r in rk if r[0] == "GIDX"] for rk in ranks]
@@ -355,27 +357,15 @@ def expected_open_transcript(ranks, N, logM, rates):
     return out
 
 
-def leader_tail(lead):
-    """The leader's records after the parties' rounds of PCS_open_new: per
-    delegation round the WHIR commitment of the gathered segments, the
-    extension query draws, the claims of prove_multi_folding and
-    prove_extension with the evaluations their checks compute; then
-    aggregate_claims, the openings of aggregate_commitments, _Whir_Open
-    (per iteration its commitment root, query draws and the roots of the
-    replies it hashes; the final claim) and delegate_beta_eval (its claim and
-    the evaluations of its check).  The glibc draws are counted in random()
-    calls: forty per F::_random() (two randomNumber() of twenty digits,
-    fieldElement.cpp:119-125, 363-368), one per rand()."""
+def leader_rounds(lead, i):
+    """The delegation rounds of the leader's tail from record i (the first
+    WHIR commitment of gathered segments): per round the commitment's size
+    and root, the extension query draws, prove_multi_folding's and
+    prove_extension's claims and the evaluations their checks compute.
+    Returns (rounds, the index of the parties' final data)."""
     import struct
     sha = lambda b: hashlib.sha256(b).hexdigest()
-    tags = [r[0] for r in lead]
-    calls = lambda rs: sum(40 if r[0] == "FRND" else 1 for r in rs if r[0] in ("FRND", "RAND"))
-    w0 = tags.index("WCIA")
-    # (the calls before the tail are not all seen here: the dealing calls
-    # random() directly too; the oracle's restatement of the dealing gives
-    # the generator's state where the tail starts)
-    out = {"prng_calls": calls(lead[w0:]), "rounds": []}
-    i = w0
+    rounds = []
     while True:
         while i < len(lead) and lead[i][0] not in ("WCIA", "SPDA"):
             i += 1
@@ -405,8 +395,32 @@ def leader_tail(lead):
             i += 1
         rd["pex"] = lead[i][2].hex()
         rd["check_evals"] = ev
-        out["rounds"].append(rd)
+        rounds.append(rd)
         i += 1
+    return rounds, i
+
+
+def leader_tail(lead):
+    """The leader's records after the parties' rounds of PCS_open_new: per
+    delegation round the WHIR commitment of the gathered segments, the
+    extension query draws, the claims of prove_multi_folding and
+    prove_extension with the evaluations their checks compute; then
+    aggregate_claims, the openings of aggregate_commitments, _Whir_Open
+    (per iteration its commitment root, query draws and the roots of the
+    replies it hashes; the final claim) and delegate_beta_eval (its claim and
+    the evaluations of its check).  The glibc draws are counted in random()
+    calls: forty per F::_random() (two randomNumber() of twenty digits,
+    fieldElement.cpp:119-125, 363-368), one per rand()."""
+    import struct
+    sha = lambda b: hashlib.sha256(b).hexdigest()
+    tags = [r[0] for r in lead]
+    calls = lambda rs: sum(40 if r[0] == "FRND" else 1 for r in rs if r[0] in ("FRND", "RAND"))
+    w0 = tags.index("WCIA")
+    # (the calls before the tail are not all seen here: the dealing calls
+    # random() directly too; the oracle's restatement of the dealing gives
+    # the generator's state where the tail starts)
+    out = {"prng_calls": calls(lead[w0:])}
+    out["rounds"], i = leader_rounds(lead, w0)
     k = tags.index("AGCK", i)
     out["aggr_K"] = lead[k][2].hex()
     out["aggr_challenges"] = lead[k + 1][2].hex()
@@ -651,6 +665,65 @@ def gen_piop():
 
 
 DPCS = os.path.join(ROOT, "oracle", "_ref", "pigeon_dpcs")
+
+
+def gen_pcspiop():
+    """PCS_open_new with isPIOP = true (coPCS.cpp:1310-1700, as coPIOP_prove
+    calls it) run unmodified with N ranks after the coPCS test's dealing and
+    PCS_commit (oracle/ref/dpcs_mpi_driver.cpp pcs mode: input vectors from
+    Lagrange vectors at seeded points, K their F_ip claim).  Kept: the
+    transcript gbz_pcs_open_piop's parties' part must equal (rebuilt from
+    the ranks' records as for the coPCS test), the leader's delegation rounds,
+    r_c, delegate_lagrange_eval's claim and check evaluations, the glibc
+    calls of the tail, and the WHIR batch slots 2 and 3 the opening fills."""
+    import struct
+    import tempfile
+    out = {}
+    rates = [[4], [4], [4, 4], [4, 4]]
+    for N, logM, seed in ((8, 16, 31), (16, 16, 32), (16, 18, 33)):
+        with tempfile.TemporaryDirectory() as td:
+            prefix, cap = os.path.join(td, "pp"), os.path.join(td, "cap")
+            env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_TIMEOUT="300", MINIMPI_CAPTURE=cap)
+            log = subprocess.run([DPCS, "pcs", str(logM), str(seed), prefix], env=env, check=True,
+                                 capture_output=True, text=True)
+            ranks = [capture_records("%s.%d" % (cap, r)) for r in range(N)]
+            b = open(prefix + ".0", "rb").read()
+        o = 0
+        slots = []
+        for _ in range(2):
+            sl = {}
+            for key in ("arr", "codeword", "betas"):
+                (n,) = struct.unpack_from("<I", b, o)
+                o += 4
+                sl[key + "_sha256"] = hashlib.sha256(b[o:o + 16 * n]).hexdigest()
+                sl[key + "_len"] = n
+                o += 16 * n
+            sl["claim"] = b[o:o + 16].hex()
+            sl["root"] = b[o + 16:o + 48].hex()
+            o += 48
+            slots.append(sl)
+        expected = expected_open_transcript(ranks, N, logM, rates, npoint=0)
+        lead = ranks[0]
+        tags = [t for t, _, _ in lead]
+        w0 = tags.index("WCIA")
+        rounds, i = leader_rounds(lead, w0)
+        d0, d1 = tags.index("DLEY"), tags.index("DLEE")
+        calls = lambda rs: sum(40 if r[0] == "FRND" else 1 for r in rs if r[0] in ("FRND", "RAND"))
+        case = {"N": N, "logM": logM, "seed": seed, "rates": rates, "K": [p for t, _, p in lead if t == "FIPK"][0].hex(),
+                "gpu_transcript_bytes": len(expected), "gpu_transcript_sha256": hashlib.sha256(expected).hexdigest(),
+                "stdout": log.stdout.strip().splitlines(),
+                "leader": {"rounds": rounds, "prng_calls": calls(lead[w0:]),
+                           "r_c": [p for t, _, p in lead[i:d0] if t == "FRND"][0].hex(),
+                           "lag_y": lead[d0][2].hex(),
+                           "lag_evals": [p[16:].hex() for t, _, p in lead[d0:d1] if t == "EVLV"],
+                           "lag_draws": sum(1 for t in tags[d0:d1] if t == "FRND")},
+                "whir_slots": slots}
+        name = "pcspiop_N%d_M%d" % (N, logM)
+        with open(os.path.join(HERE, name + ".json"), "w") as f:
+            json.dump(case, f, indent=0)
+        out[name] = {"file": name + ".json", "N": N, "logM": logM}
+        print("pcspiop N=%d M=2^%d" % (N, logM), flush=True)
+    return out
 DPCS_OPEN_CASES = [(2, 8, 12, 8, 4, 21), (2, 16, 13, 8, 4, 22), (3, 8, 11, 4, 2, 23), (2, 32, 11, 4, 4, 24)]
 DPCS_CASES = [("batch", 8, 12, 8, 4, 5), ("batch", 16, 14, 16, 4, 6), ("batch", 8, 13, 4, 8, 7),
               ("batch", 32, 10, 32, 2, 8), ("single", 8, 12, 0, 4, 9), ("single", 16, 13, 0, 2, 10),
