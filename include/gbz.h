@@ -574,6 +574,46 @@ gbz_status gbz_pcs_open_full(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int 
                              gbz_prng *prng, uint32_t *flags, uint8_t *transcript, uint64_t capacity, int mem);
 gbz_status gbz_pcs_open_full_bytes(const gbz_pcs *pcs, uint64_t *bytes);
 
+/* One WHIR batch slot of the PIOP mode (whir_polys, whir_c, whir_betas,
+ * whir_claims, whir_MTs of coPCS.cpp:1620-1629); any pointer may be NULL.
+ * arr: slot_len field elements (the delegation round's gathered segments,
+ * zero-padded), codeword: 4 slot_len (rate 4), betas: slot_len
+ * (precompute_beta of the claim's point, zero beyond the reference's
+ * 2^(point length) entries), claim: one value, root: the 32-byte root of
+ * the codeword's tree. */
+typedef struct {
+  uint64_t *arr, *codeword, *betas, *claim;
+  uint8_t *root;
+} gbz_whir_slot;
+
+/* PCS_open_new with isPIOP = true, as coPIOP_prove calls it: the row
+ * weights b1 (nb1 entries; the first batches - 1 are used), the row vector
+ * b2 (the row length's entries; its last _queries[0] entries are zeroed as
+ * the reference does), the party weights b3 (N/4 entries) and the row
+ * vector's Lagrange factors (_Lagrange_Evals_input: nlag <= 8 vectors of
+ * 2^log_lengths[k] entries back to back, their tensor product factor 0 on
+ * the lowest index digits; the log lengths sum to log2 of the row length).
+ * The parties' records are gbz_pcs_open_full's; the leader's tail keeps the
+ * delegation rounds, 53 UNPACKED and 55 RC, skips aggregate_claims and
+ * _Whir_Open and fills the WHIR batch slots 2 and 3 (slots: 2 entries, may
+ * be NULL) from the first two delegation rounds; then
+ * delegate_lagrange_eval (delegate_protocol.cpp:603-710): 56 BETA_Y 16B
+ * (y), 48/49 (_cubic_sumcheck of the rounds' Lagrange tensor, the
+ * transform of the factors' tensor with its last _queries[0] entries
+ * zeroed, omega^j), 57 L_EVALS 16B x rounds, 48/49 (_cubic_sumcheck of
+ * phi / row length, the factors' tensor and the ones vector, unchecked), 69
+ * LAG_EVALS 16B x nlag.  *flags as gbz_pcs_open_full's, plus bit 8: a
+ * "delegating betas 2" check (returns GBZ_ECHECK) and bit 9: "delegating
+ * betas 3" (printed).  Transcript bytes and slot_len:
+ * gbz_pcs_open_piop_bytes.
+ * replaces PCS_open_new (coPCS.cpp:1310-1690, isPIOP) on N ranks. */
+gbz_status gbz_pcs_open_piop(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *b1, int nb1, const uint64_t *b2,
+                             uint64_t nb2, const uint64_t *b3, int nb3, const uint64_t *lagrange,
+                             const int *log_lengths, int nlag, const uint64_t *K, uint64_t *fs, gbz_prng *prng,
+                             uint32_t *flags, gbz_whir_slot *slots, uint8_t *transcript, uint64_t capacity, int mem);
+gbz_status gbz_pcs_open_piop_bytes(const gbz_pcs *pcs, const int *log_lengths, int nlag, uint64_t *bytes,
+                                   uint64_t *slot_len);
+
 /* quadratic_coSumcheck / cubic_coSumcheck of N parties on one device
  * (form GBZ_SC_QUADRATIC or GBZ_SC_CUBIC).  p1, p2 (and p3): N x n party
  * shares, party-major; R: the parties' sparse vectors, N x sum_i (2 or 4)

@@ -949,9 +949,25 @@ OpenOffs open_layout(const gbz_pcs &pc, PcsLayout &lay) {
 }
 
 // The sizes of the leader's tail (pointers are filled in by the opening).
-LeaderInputs leader_shape(const gbz_pcs &pc) {
+// The PIOP mode's inputs (gbz_pcs_open_piop; the caller's memory kind).
+struct PiopIn {
+  const uint64_t *b1 = nullptr, *b2 = nullptr, *b3 = nullptr, *lag = nullptr;
+  int nb1 = 0, nb3 = 0, nlag = 0;
+  uint64_t nb2 = 0;
+  const int *loglag = nullptr;
+  gbz_whir_slot *slots = nullptr;
+};
+
+LeaderInputs leader_shape(const gbz_pcs &pc, const PiopIn *pi = nullptr) {
   const PcsSchedule &sc = pc.sc;
   LeaderInputs in;
+  if (pi) {
+    if (pi->nlag < 1 || pi->nlag > 8) throw ArgError("pcs: 1..8 Lagrange factors");
+    in.piop = true;
+    in.nlag = pi->nlag;
+    for (int k = 0; k < pi->nlag; k++) in.loglag[k] = pi->loglag[k];
+    in.q0 = (uint64_t)sc.queries[0];
+  }
   in.N = sc.N;
   in.Bs = pc.Bs;
   in.log_rate_offset = sc.log_rate_offset;
@@ -979,8 +995,8 @@ LeaderInputs leader_shape(const gbz_pcs &pc) {
 // The records of the leader's tail after the parties' records (lay.bytes is
 // where they start), and its draws (script, arena_len: may be null).
 void tail_layout(const gbz_pcs &pc, PcsLayout &lay, std::vector<DrawOp> *script = nullptr,
-                 uint64_t *arena_len = nullptr) {
-  LeaderInputs in = leader_shape(pc);
+                 uint64_t *arena_len = nullptr, const PiopIn *pi = nullptr) {
+  LeaderInputs in = leader_shape(pc, pi);
   Layout tl;
   tl.record_headers = true;
   LeaderResources R;
@@ -1350,12 +1366,12 @@ gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, in
 
 static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K,
                                 uint64_t *fs, bool full, gbz_prng *prng, uint32_t *flags, uint8_t *transcript,
-                                uint64_t capacity, int mem) {
+                                uint64_t capacity, int mem, const PiopIn *pi = nullptr) {
   API_BEGIN(ctx)
   check_mem(mem);
   if (full) need(prng, "prng");
   need(pcs, "pcs");
-  need(r, "r");
+  if (!pi) need(r, "r");
   need(K, "K");
   need(fs, "fs");
   need(transcript, "transcript");
@@ -1364,14 +1380,27 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
   const int N = sc.N, logN = ilog2(N), nb = pcs->batches;
   const uint64_t Bs = pcs->Bs, L = pcs->L;
   const int lk = ilog2(N / 4), logBs = ilog2(Bs);
-  if (nr != lk + 5 + logBs) throw ArgError("pcs: the point must have log2(N/4) + 5 + log2(row length) entries");
+  if (pi) {
+    need(pi->b1, "b1");
+    need(pi->b2, "b2");
+    need(pi->b3, "b3");
+    need(pi->lag, "lagrange");
+    need(pi->loglag, "log_lengths");
+    if (pi->nb1 < 0) throw ArgError("pcs: b1 length");
+    if (pi->nb2 != Bs) throw ArgError("pcs: b2 must have the row length's entries");
+    if (pi->nb3 != N / 4) throw ArgError("pcs: b3 must have N/4 entries");
+    if ((uint64_t)sc.queries[0] >= Bs) throw ArgError("pcs: _queries[0] must be below the row length");
+    nr = 0;
+  } else if (nr != lk + 5 + logBs) {
+    throw ArgError("pcs: the point must have log2(N/4) + 5 + log2(row length) entries");
+  }
   PcsLayout lay;
   const OpenOffs off = open_layout(*pcs, lay);
   const uint64_t tail_base = lay.bytes;
-  LeaderInputs lead = leader_shape(*pcs);
+  LeaderInputs lead = leader_shape(*pcs, pi);
   std::vector<DrawOp> script;
   uint64_t arena_len = 0;
-  if (full) tail_layout(*pcs, lay, &script, &arena_len);
+  if (full) tail_layout(*pcs, lay, &script, &arena_len, pi);
   if (capacity < lay.bytes)
     throw ArgError(full ? "pcs: transcript capacity below gbz_pcs_open_full_bytes"
                         : "pcs: transcript capacity below gbz_pcs_info's open_transcript_bytes");
@@ -1380,7 +1409,8 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
   // context's pool for this shape serves them after the first
   OpenBufs ob;
   {
-    std::string key = "pcs_open" + std::to_string((int)full) + ":" + std::to_string(mem) + ":" + std::to_string(N) +
+    std::string key = "pcs_open" + std::to_string((int)full) + (pi ? "p" + std::to_string(pi->nlag) : std::string()) +
+                      ":" + std::to_string(mem) + ":" + std::to_string(N) +
                       ":" + std::to_string(pcs->sc.M) + ":" + std::to_string(sc.rounds);
     for (int i = 0; i < sc.rounds; i++) key += ":" + std::to_string(sc.rate0[i]) + "/" + std::to_string(sc.rate1[i]);
     ob.pool = &ctx->pools[key];
@@ -1421,9 +1451,10 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     if (mem == GBZ_MEM_DEVICE) break;
     hr[i] = fe_make(r[2 * i], r[2 * i + 1]);
   }
-  fe *dr = ob.alloc<fe>(nr);
-  GBZ_CUDA(cudaMemcpyAsync(dr, mem == GBZ_MEM_DEVICE ? (const void *)r : (const void *)hr.data(), 16ull * nr,
-                           mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  fe *dr = ob.alloc<fe>(std::max(nr, 1));
+  if (nr)
+    GBZ_CUDA(cudaMemcpyAsync(dr, mem == GBZ_MEM_DEVICE ? (const void *)r : (const void *)hr.data(), 16ull * nr,
+                             mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
   fe hK, hfs;
   if (mem == GBZ_MEM_DEVICE) {
     uint64_t t[4];
@@ -1453,13 +1484,31 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
   GBZ_CUDA(cudaMemcpyAsync(dlam, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
 
   // betas of the point: r3 (log2 N/4), r1 (5), r2 (log2 Bs) (coPCS.cpp:1319-1325)
+  // or, in the PIOP mode, the input vectors with b2's last _queries[0]
+  // entries zeroed (:1327-1335) and b1 cut to the batches (:1349)
   fe *b1 = ob.alloc<fe>(32), *b2 = ob.alloc<fe>(Bs), *b3 = ob.alloc<fe>(std::max(1, N / 4)), *b3p = ob.alloc<fe>(N);
-  beta_launch(dr + lk, 5, b1, s);
-  beta_launch(dr + lk + 5, logBs, b2, s);
-  if (lk) beta_launch(dr, lk, b3, s);
-  else {
-    const fe one = fe_one();
-    GBZ_CUDA(cudaMemcpyAsync(b3, &one, 16, cudaMemcpyHostToDevice, s));
+  fe *dlag = nullptr;
+  if (pi) {
+    const cudaMemcpyKind kin = mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const int n1 = std::min(pi->nb1, std::min(nb - 1, 32));
+    const uint64_t q0 = (uint64_t)sc.queries[0];
+    GBZ_CUDA(cudaMemsetAsync(b1, 0, 16 * 32, s));
+    if (n1 > 0) GBZ_CUDA(cudaMemcpyAsync(b1, pi->b1, 16ull * n1, kin, s));
+    GBZ_CUDA(cudaMemcpyAsync(b2, pi->b2, 16 * Bs, kin, s));
+    if (q0) GBZ_CUDA(cudaMemsetAsync(b2 + (Bs - q0), 0, 16 * q0, s));
+    GBZ_CUDA(cudaMemcpyAsync(b3, pi->b3, 16ull * (N / 4), kin, s));
+    uint64_t nl = 0;
+    for (int k = 0; k < pi->nlag; k++) nl += 1ull << pi->loglag[k];
+    dlag = ob.alloc<fe>(nl);
+    GBZ_CUDA(cudaMemcpyAsync(dlag, pi->lag, 16 * nl, kin, s));
+  } else {
+    beta_launch(dr + lk, 5, b1, s);
+    beta_launch(dr + lk + 5, logBs, b2, s);
+    if (lk) beta_launch(dr, lk, b3, s);
+    else {
+      const fe one = fe_one();
+      GBZ_CUDA(cudaMemcpyAsync(b3, &one, 16, cudaMemcpyHostToDevice, s));
+    }
   }
   k_b3p<<<1, 64, 0, s>>>(b3, N / 4, dmu, N, b3p);
   GBZ_CUDA(cudaGetLastError());
@@ -1681,7 +1730,24 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     lead.r_first = &st->r_first;
     lead.b2 = b2;
     lead.b3 = b3;
-    lead.r2 = dr + lk + 5;
+    lead.r2 = pi ? nullptr : dr + lk + 5;
+    if (pi) {
+      lead.lag = dlag;
+      const uint64_t md = lead.max_delegation;
+      for (int c = 0; c < 2 && pi->slots; c++) {
+        const gbz_whir_slot &u = pi->slots[c];
+        WhirSlotDev &o = lead.slot[c];
+        auto place = [&](void *user, uint64_t bytes) -> void * {
+          if (!user) return nullptr;
+          return mem == GBZ_MEM_DEVICE ? user : (void *)ob.alloc<uint8_t>(bytes);
+        };
+        o.arr = (fe *)place(u.arr, 16 * md);
+        o.cw = (fe *)place(u.codeword, 64 * md);
+        o.betas = (fe *)place(u.betas, 16 * md);
+        o.claim = (fe *)place(u.claim, 16);
+        o.root = (uint8_t *)place(u.root, 32);
+      }
+    }
     // unpack_secret_share(., N/2, N) (MPI_utils.cpp:2769-2785): output j is
     // entry 2j of the unpacked shares, a fixed linear form of the N shares
     std::vector<fe> U((size_t)(N / 2) * N);
@@ -1715,6 +1781,18 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     GBZ_CUDA(cudaMemcpyAsync(&hg, ldraws.final_state, sizeof hg, cudaMemcpyDeviceToHost, s));
   }
   if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaMemcpyAsync(transcript, tr, lay.bytes, cudaMemcpyDeviceToHost, s));
+  if (pi && pi->slots && mem == GBZ_MEM_HOST) {
+    const uint64_t md = lead.max_delegation;
+    for (int c = 0; c < 2; c++) {
+      const gbz_whir_slot &u = pi->slots[c];
+      const WhirSlotDev &o = lead.slot[c];
+      if (u.arr) GBZ_CUDA(cudaMemcpyAsync(u.arr, o.arr, 16 * md, cudaMemcpyDeviceToHost, s));
+      if (u.codeword) GBZ_CUDA(cudaMemcpyAsync(u.codeword, o.cw, 64 * md, cudaMemcpyDeviceToHost, s));
+      if (u.betas) GBZ_CUDA(cudaMemcpyAsync(u.betas, o.betas, 16 * md, cudaMemcpyDeviceToHost, s));
+      if (u.claim) GBZ_CUDA(cudaMemcpyAsync(u.claim, o.claim, 16, cudaMemcpyDeviceToHost, s));
+      if (u.root) GBZ_CUDA(cudaMemcpyAsync(u.root, o.root, 32, cudaMemcpyDeviceToHost, s));
+    }
+  }
   GBZ_CUDA(cudaStreamSynchronize(s));
   if (mem == GBZ_MEM_HOST) {
     fs[0] = hst.fs.re;
@@ -1740,6 +1818,43 @@ gbz_status gbz_pcs_open(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, c
 gbz_status gbz_pcs_open_full(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K, uint64_t *fs,
                              gbz_prng *prng, uint32_t *flags, uint8_t *transcript, uint64_t capacity, int mem) {
   return pcs_open_impl(ctx, pcs, r, nr, K, fs, true, prng, flags, transcript, capacity, mem);
+}
+
+gbz_status gbz_pcs_open_piop(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *b1, int nb1, const uint64_t *b2,
+                             uint64_t nb2, const uint64_t *b3, int nb3, const uint64_t *lagrange,
+                             const int *log_lengths, int nlag, const uint64_t *K, uint64_t *fs, gbz_prng *prng,
+                             uint32_t *flags, gbz_whir_slot *slots, uint8_t *transcript, uint64_t capacity, int mem) {
+  PiopIn pi;
+  pi.b1 = b1;
+  pi.nb1 = nb1;
+  pi.b2 = b2;
+  pi.nb2 = nb2;
+  pi.b3 = b3;
+  pi.nb3 = nb3;
+  pi.lag = lagrange;
+  pi.loglag = log_lengths;
+  pi.nlag = nlag;
+  pi.slots = slots;
+  if (!log_lengths || nlag < 1 || nlag > 8) return fail(ctx, GBZ_EINVAL, "pcs: 1..8 Lagrange factors with their log2 lengths");
+  return pcs_open_impl(ctx, pcs, nullptr, 0, K, fs, true, prng, flags, transcript, capacity, mem, &pi);
+}
+
+gbz_status gbz_pcs_open_piop_bytes(const gbz_pcs *pcs, const int *log_lengths, int nlag, uint64_t *bytes,
+                                   uint64_t *slot_len) {
+  if (!pcs || !bytes || !log_lengths || nlag < 1 || nlag > 8) return GBZ_EINVAL;
+  try {
+    PiopIn pi;
+    pi.loglag = log_lengths;
+    pi.nlag = nlag;
+    PcsLayout lay;
+    open_layout(*pcs, lay);
+    tail_layout(*pcs, lay, nullptr, nullptr, &pi);
+    *bytes = lay.bytes;
+    if (slot_len) *slot_len = leader_shape(*pcs).max_delegation;
+  } catch (const ArgError &) {
+    return GBZ_EINVAL;
+  }
+  return GBZ_OK;
 }
 
 gbz_status gbz_pcs_open_full_bytes(const gbz_pcs *pcs, uint64_t *bytes) {

@@ -37,7 +37,8 @@ namespace {
 // Transcript tags of the tail (include/gbz.h).
 enum : uint32_t {
   T_D_ROOT = 46, T_D_QUERIES = 47, T_D_POLYS = 48, T_D_FINAL = 49, T_D_CLAIM = 50, T_D_OPEN = 51,
-  T_D_EXT_CLAIM = 52, T_L_UNPACKED = 53, T_L_WHIR_CLAIM = 54, T_L_RC = 55, T_L_BETA_Y = 56, T_L_EVALS = 57
+  T_D_EXT_CLAIM = 52, T_L_UNPACKED = 53, T_L_WHIR_CLAIM = 54, T_L_RC = 55, T_L_BETA_Y = 56, T_L_EVALS = 57,
+  T_L_LAG_EVALS = 69
 };
 
 constexpr int kT = 256;
@@ -332,18 +333,18 @@ __global__ void k_pe_checks(const fe *fin, const fe *b1e, const fe *b2e, const i
   if (bad) atomicOr(flags, LF_DELEGATION);
 }
 
-// phiGInit(phi, r, 1, n, false) (utils.cpp:1131-1165) over 2^n entries:
-// phi[b] = prod_{m < n} (1 - r_m + r_m omega^(b 2^m)) for b < 2^(n-1), zero
-// above; omega = omega_{2^n} from the tables (lo, hi).  With nr < n the
-// missing r_m are zero (their factor is 1).
-__global__ void k_phi(const fe *r, int nr, int n, const fe *lo, const fe *hi, fe *out) {
+// phiGInit(phi, r, scale, n, false) (utils.cpp:1131-1165) over 2^n
+// entries: phi[b] = scale prod_{m < n} (1 - r_m + r_m omega^(b 2^m)) for
+// b < 2^(n-1), zero above; omega = omega_{2^n} from the tables (lo, hi).
+// With nr < n the missing r_m are zero (their factor is 1).
+__global__ void k_phi(const fe *r, int nr, int n, const fe *lo, const fe *hi, fe scale, fe *out) {
   const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, N = 1ull << n;
   if (b >= N) return;
   if (b >= N / 2) {
     out[b] = fe_zero();
     return;
   }
-  fe v = fe_one();
+  fe v = scale;
   for (int m = 0; m < nr; m++) v = fmul(v, fadd(fsub(fe_one(), r[m]), fmul(r[m], pow_tab(lo, hi, (b << m) & (N - 1)))));
   out[b] = v;
 }
@@ -607,10 +608,12 @@ __global__ void k_mul(const fe *a, const fe *b, uint64_t n, fe *out) {
   if (g < n) out[g] = fmul(a[g], b[g]);
 }
 
-// The check "Error in delegating betas 1": prod_k evaluate_vector(L_k, r_k)
-// against the cubic sumcheck's L_vector value; the evaluations go to the transcript.
-__global__ void k_beta_evals(TensorArgs a, const fe *r, const fe *fin, fe *scratch, uint32_t *flags, uint8_t *tr,
-                             uint64_t off) {
+// The check "Error in delegating betas 1" (and delegate_lagrange_eval's
+// second "Error in delegating betas 2"): prod_k evaluate_vector(L_k, r_k)
+// against the sumcheck's value *fin for that tensor (bit: the flag); the
+// evaluations go to the transcript.  scratch: 3/4 of the longest factor.
+__global__ void k_beta_evals(TensorArgs a, const fe *r, const fe *fin, uint32_t bit, fe *scratch, uint32_t *flags,
+                             uint8_t *tr, uint64_t off) {
   __shared__ fe ev[8];
   int base = 0;
   for (int k = 0; k < a.n; k++) {
@@ -636,7 +639,46 @@ __global__ void k_beta_evals(TensorArgs a, const fe *r, const fe *fin, fe *scrat
     put_fe(tr, off + 16ull * k, ev[k]);
     p = fmul(p, ev[k]);
   }
-  if (!fe_eq(p, fin[0])) atomicOr(flags, LF_BETAS);
+  if (!fe_eq(p, fin[0])) atomicOr(flags, bit);
+}
+
+// delegate_lagrange_eval's first "Error in delegating betas 2"
+// (delegate_protocol.cpp:668-675): the multilinear extension of omega^j at
+// the point, prod_i (1 - r_i + r_i omega^(2^i)), against the sumcheck's
+// value of the omega vector.
+__global__ void k_lag_omega(const fe *r, int n, fe omega, const fe *fin, uint32_t *flags) {
+  if (threadIdx.x) return;
+  fe p = fe_one();
+  for (int i = 0; i < n; i++) {
+    p = fmul(p, fadd(fsub(fe_one(), r[i]), fmul(r[i], omega)));
+    omega = fmul(omega, omega);
+  }
+  if (!fe_eq(p, fin[2])) atomicOr(flags, LF_LAG2);
+}
+
+// "Error in delegating betas 3" (delegate_protocol.cpp:696-707): the ones
+// vector's value plus the equality weights of its q zeroed entries
+// Bs - q .. Bs - 1 at the point is one.
+__global__ void k_lag_ones(const fe *fin, const fe *r, int n, uint64_t Bs, uint64_t q, uint32_t *flags) {
+  __shared__ fe part[kT];
+  fe acc = fe_zero();
+  for (uint64_t i = Bs - q + threadIdx.x; i < Bs; i += blockDim.x) {
+    fe b = fe_one();
+    for (int j = 0; j < n; j++) b = fmul(b, (i >> j) & 1 ? r[j] : fsub(fe_one(), r[j]));
+    acc = fadd(acc, b);
+  }
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x) return;
+  fe sum = fin[2];
+  for (int t = 0; t < (int)blockDim.x; t++) sum = fadd(sum, part[t]);
+  if (!fe_eq(sum, fe_one())) atomicOr(flags, LF_LAG3);
+}
+
+// v[i] = 1 for i < m, 0 for m <= i < n.
+__global__ void k_fill_prefix(fe *v, uint64_t n, uint64_t m) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n) v[g] = g < m ? fe_one() : fe_zero();
 }
 
 __global__ void k_put1(const fe *v, uint8_t *tr, uint64_t off) {
@@ -758,6 +800,7 @@ struct Tail {
   struct RoundOut {
     fe *A = nullptr, *W = nullptr;  // the WHIR array (max_delegation) and its codeword
     fe *claim = nullptr;            // (value, point of log2 max_delegation)
+    uint64_t off_root = 0;          // the root of its commitment in the transcript
   };
 
   RoundOut delegation_round(const LeaderRound &rd) {
@@ -776,6 +819,7 @@ struct Tail {
     // Whir_Commit_initial(arr, 4, 8) of the gathered segments (coPCS.cpp:773-779):
     // the codeword and the root of MT_commit_Blake over it
     const uint64_t off_root = lay.rec(T_D_ROOT, 1, 32);
+    out.off_root = off_root;
     out.A = alloc<fe>(md);
     out.W = alloc<fe>(Lw);
     if (!dry) {
@@ -871,7 +915,7 @@ struct Tail {
       // prove_fft (delegate_protocol.cpp:119-145) of sum_t b2[t] segment_t at r1
       k_seg_comb<<<d, kT, 0, s>>>(rd.seg, b2e, l, d, v);
       const NttTables &tc = R.tables(logC0);
-      k_phi<<<nblk(C0), kT, 0, s>>>(ch3, logC0, logC0, tc.lo_fwd, tc.hi_fwd, Wp);
+      k_phi<<<nblk(C0), kT, 0, s>>>(ch3, logC0, logC0, tc.lo_fwd, tc.hi_fwd, fe_one(), Wp);
       k_set<<<1, 32, 0, s>>>(y, fin3);
       check();
     }
@@ -887,6 +931,105 @@ struct Tail {
       check();
     }
     return out;
+  }
+
+  // The PIOP mode's WHIR batch slots 2 and 3 (coPCS.cpp:1620-1629): the
+  // first two delegation rounds' arrays, codewords and roots, the betas of
+  // their claims' points and the claims' values.
+  void piop_slots(const std::vector<RoundOut> &ro) {
+    if (ro.size() < 2) throw ArgError("pcs leader: the PIOP mode needs two delegation rounds");
+    const uint64_t md = in.max_delegation;
+    if (dry) return;
+    for (int c = 0; c < 2; c++) {
+      const WhirSlotDev &o = in.slot[c];
+      if (o.arr) GBZ_CUDA(cudaMemcpyAsync(o.arr, ro[c].A, 16 * md, cudaMemcpyDeviceToDevice, s));
+      if (o.cw) GBZ_CUDA(cudaMemcpyAsync(o.cw, ro[c].W, 64 * md, cudaMemcpyDeviceToDevice, s));
+      if (o.betas) beta_launch(ro[c].claim + 1, ilog2(md), o.betas, s);
+      if (o.claim) GBZ_CUDA(cudaMemcpyAsync(o.claim, ro[c].claim, 16, cudaMemcpyDeviceToDevice, s));
+      if (o.root) GBZ_CUDA(cudaMemcpyAsync(o.root, tr + ro[c].off_root, 32, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+
+  // delegate_lagrange_eval(L1 = the input's Lagrange factors, L2 = the
+  // rounds' Lagrange vectors, y = b2f, offset, _queries[0])
+  // (delegate_protocol.cpp:603-710): the cubic sumcheck of (L2's tensor,
+  // the transform of L1's tensor with its last q0 entries zeroed, omega^j)
+  // and the checks of its three values, then the cubic sumcheck of (phi at
+  // its point scaled by 1/Bs, L1's tensor, ones with the last q0 entries
+  // zeroed) without round checks, L1's evaluation and the sum of the ones
+  // vector.
+  void lagrange_delegation(const fe *b2f, const fe *om) {
+    const int nr = (int)in.rounds.size(), logBs = ilog2(in.Bs);
+    const uint64_t Bs = in.Bs, q = in.q0;
+    if (in.nlag < 1 || in.nlag > 8) throw ArgError("pcs leader: 1..8 Lagrange factors");
+    int lsum = 0, lmax = 0;
+    for (int k = 0; k < in.nlag; k++) {
+      if (in.loglag[k] < 1 || in.loglag[k] > 30) throw ArgError("pcs leader: Lagrange factor length");
+      lsum += in.loglag[k];
+      lmax = std::max(lmax, in.loglag[k]);
+    }
+    if (lsum != logBs) throw ArgError("pcs leader: the Lagrange factors must multiply to the row length");
+    if (q >= Bs) throw ArgError("pcs leader: _queries[0] must be below the row length");
+    const uint64_t off_y = lay.rec(T_L_BETA_Y, 1, 16);
+    const int nd = 2 * (1 + 4 * logBs);
+    const fe *D = draws(nd);
+    TensorArgs ta{}, t1{};
+    ta.n = nr;
+    for (int i = 0; i < nr; i++) {
+      ta.L[i] = in.rounds[i].L;
+      ta.logd[i] = ilog2((uint64_t)in.rounds[i].d);
+    }
+    t1.n = in.nlag;
+    {
+      uint64_t o = 0;
+      for (int k = 0; k < in.nlag; k++) {
+        t1.L[k] = in.lag ? in.lag + o : nullptr;
+        t1.logd[k] = in.loglag[k];
+        o += 1ull << in.loglag[k];
+      }
+    }
+    fe *L2v = alloc<fe>(Bs), *L1v = alloc<fe>(Bs), *L1f = alloc<fe>(Bs), *ones = alloc<fe>(Bs), *y = alloc<fe>(1);
+    if (!dry) {
+      k_tensor<<<nblk(Bs), kT, 0, s>>>(ta, Bs, L2v);
+      k_tensor<<<nblk(Bs), kT, 0, s>>>(t1, Bs, L1v);
+      GBZ_CUDA(cudaMemcpyAsync(L1f, L1v, 16 * Bs, cudaMemcpyDeviceToDevice, s));
+      if (q) GBZ_CUDA(cudaMemsetAsync(L1f + (Bs - q), 0, 16 * q, s));
+      fe *tmp = alloc<fe>(Bs);
+      ntt_launch(R.tables(logBs), L1f, Bs, L1f, tmp, false, s);
+      k_fill_prefix<<<nblk(Bs), kT, 0, s>>>(ones, Bs, Bs - q);
+      k_set<<<1, 32, 0, s>>>(y, b2f);
+      k_put1<<<1, 32, 0, s>>>(b2f, tr, off_y);
+      check();
+    }
+    fe *ch = alloc<fe>(logBs), *fin = alloc<fe>(3);
+    {
+      const fe *vv[3] = {L2v, L1f, om};
+      sumcheck(SC_CUBIC, vv, Bs, y, D, 1 + 3, 4, ch, fin, LF_ROUND);
+    }
+    const uint64_t off_le = lay.rec(T_L_EVALS, (uint32_t)nr, 16);
+    fe *W = alloc<fe>(Bs), *ch2 = alloc<fe>(logBs), *fin2 = alloc<fe>(3);
+    if (!dry) {
+      int dmax = 0;
+      for (int i = 0; i < nr; i++) dmax = std::max(dmax, in.rounds[i].d);
+      fe *es = alloc<fe>((uint64_t)std::max(dmax, 1 << lmax));
+      k_beta_evals<<<1, kT, 0, s>>>(ta, ch, fin, LF_BETAS, es, flags, tr, off_le);
+      k_lag_omega<<<1, 32, 0, s>>>(ch, logBs, root_of_unity(1 + in.log_rate_offset + logBs), fin, flags);
+      const NttTables &tb = R.tables(logBs);
+      k_phi<<<nblk(Bs), kT, 0, s>>>(ch, logBs, logBs, tb.lo_fwd, tb.hi_fwd, finv(fe_make(Bs, 0)), W);
+      k_set<<<1, 32, 0, s>>>(y, fin + 1);
+      check();
+    }
+    {
+      const fe *vv[3] = {W, L1v, ones};
+      sumcheck(SC_CUBIC, vv, Bs, y, D, (1 + 4 * logBs) + 1 + 3, 4, ch2, fin2, 0);
+    }
+    const uint64_t off_l1 = lay.rec(T_L_LAG_EVALS, (uint32_t)in.nlag, 16);
+    if (!dry) {
+      fe *es = alloc<fe>(1ull << lmax);
+      k_beta_evals<<<1, kT, 0, s>>>(t1, ch2, fin2 + 1, LF_LAG2, es, flags, tr, off_l1);
+      k_lag_ones<<<1, kT, 0, s>>>(fin2, ch2, logBs, Bs, q, flags);
+      check();
+    }
   }
 
   void run() {
@@ -914,129 +1057,133 @@ struct Tail {
       k_unpack_final<<<1, 32, 0, s>>>(in.unpack, in.bcd, in.B, N, in.K, fp, fB, flags, tr, off_unp);
       check();
     }
-    // aggregate_claims (Whir.cpp:608-668)
-    const uint64_t off_ch = lay.rec(T_AGGR_CHALLENGES, (uint32_t)(2 * nR), 16), off_K = lay.rec(T_AGGR_K, 1, 16);
-    fe *betas[8] = {}, *sums = alloc<fe>((uint64_t)nR * nR);
-    fe *arr = alloc<fe>(md), *baggr = alloc<fe>(md), *cw = alloc<fe>(Lw);
-    for (int c = 0; c < nR; c++) betas[c] = alloc<fe>(md);
-    if (!dry) {
-      for (int c = 0; c < nR; c++) beta_launch(ro[c].claim + 1, logmd, betas[c], s);
-      VecList va{}, vb{};
-      for (int i = 0; i < nR; i++) {
-        va.p[i] = ro[i].A;
-        vb.p[i] = betas[i];
-      }
-      fe *mdp = alloc<fe>(multidot_scratch(md));
-      multidot_launch(va, nR, vb, nR, md, mdp, sums, s);
-    }
-    const fe *ch = draws(2 * nR);
-    if (!dry) {
-      k_aggr_K<<<1, 32, 0, s>>>(sums, ch, nR, st, tr, off_ch, off_K);
-      check();
-      VecList va{}, vb{}, vc{};
-      for (int i = 0; i < nR; i++) {
-        va.p[i] = ro[i].A;
-        vb.p[i] = betas[i];
-        vc.p[i] = ro[i].W;
-      }
-      lincomb_launch(vb, ch, nR, md, baggr, false, s);
-      lincomb_launch(va, ch + nR, nR, md, arr, false, s);
-      // aggregate_commitments (Whir.cpp:547-606): the codeword, the openings
-      // in the first commitment, the tree over zero leaves (whir_k = 8)
-      lincomb_launch(vc, ch + nR, nR, Lw, cw, false, s);
-    }
-    const int la = whir_query_count(4), depth_a = ilog2(Lw / 4);
-    const uint64_t off_aq = lay.rec(T_AGGR_QUERIES, (uint32_t)la, 4);
-    const uint64_t off_ap = lay.rec(T_AGGR_PATHS, (uint32_t)(la * depth_a), 32);
-    const uint64_t off_ar = lay.rec(T_AGGR_ROOT, 1, 32);
-    draw_mod(la, (uint32_t)(Lw / 4), off_aq);
-    if (!dry) {
-      k_whir_paths_chain<<<nblk((uint64_t)la * depth_a, 128), 128, 0, s>>>(ro[0].W, Lw / 4, la, tr, off_aq, off_ap,
-                                                                           0, 0);
-      k_zero_tree_root<<<1, 32, 0, s>>>(ilog2(Lw / 8), tr, off_ar);
-      check();
-    }
-    // _Whir_Open (Whir.cpp:469-545) with whir_k = 8 from the zero-leaf tree
-    const uint64_t sizes[1] = {md};
-    const BatchPlan P = batch_plan(1, sizes, 4, 8, Lw / 8);
-    BatchResources br;
-    br.s = s;
-    br.buf = [this](int slot, uint64_t bytes) -> void * {
-      auto it = slots.find(slot);
-      if (it != slots.end()) return it->second;
-      void *p = R.alloc(bytes);
-      slots[slot] = p;
-      return p;
-    };
-    br.tables = R.tables;
-    br.st = st;
-    br.ub_scratch = alloc<fe>(kUpdateBetasScratch);
-    WalkTrace wt;
-    // the opening draws from st->prng itself: the script leaves its state
-    // there and skips the opening's calls (per iteration log2 kappa
-    // F::_random(), the queries' rand(), update_betas' F::_random(); the
-    // final point's F::_random())
-    if (script) script->push_back({DRAW_STATE, 0, 0u, 0});
-    {
-      const fe *arrays[1] = {arr}, *bets[1] = {baggr}, *cws[1] = {cw};
-      batch_open_walk(br, P, arrays, bets, cws, nullptr, tr, lay, dry, &wt);
-    }
-    {
-      uint64_t calls = 0;
-      for (const BatchStep &e : P.steps)
-        if (e.iterate) calls += 40ull * ilog2((uint64_t)e.kappa) + (uint64_t)e.l + 40;
-      calls += 40ull * ilog2(P.m_final);
-      if (script) script->push_back({DRAW_SKIP, (int)calls, 0u, 0});
+    if (in.piop) {
+      piop_slots(ro);
+    } else {
+      // aggregate_claims (Whir.cpp:608-668)
+      const uint64_t off_ch = lay.rec(T_AGGR_CHALLENGES, (uint32_t)(2 * nR), 16), off_K = lay.rec(T_AGGR_K, 1, 16);
+      fe *betas[8] = {}, *sums = alloc<fe>((uint64_t)nR * nR);
+      fe *arr = alloc<fe>(md), *baggr = alloc<fe>(md), *cw = alloc<fe>(Lw);
+      for (int c = 0; c < nR; c++) betas[c] = alloc<fe>(md);
       if (!dry) {
-        k_prng_check<<<1, 32, 0, s>>>(st, after_walk, flags);
+        for (int c = 0; c < nR; c++) beta_launch(ro[c].claim + 1, logmd, betas[c], s);
+        VecList va{}, vb{};
+        for (int i = 0; i < nR; i++) {
+          va.p[i] = ro[i].A;
+          vb.p[i] = betas[i];
+        }
+        fe *mdp = alloc<fe>(multidot_scratch(md));
+        multidot_launch(va, nR, vb, nR, md, mdp, sums, s);
+      }
+      const fe *ch = draws(2 * nR);
+      if (!dry) {
+        k_aggr_K<<<1, 32, 0, s>>>(sums, ch, nR, st, tr, off_ch, off_K);
+        check();
+        VecList va{}, vb{}, vc{};
+        for (int i = 0; i < nR; i++) {
+          va.p[i] = ro[i].A;
+          vb.p[i] = betas[i];
+          vc.p[i] = ro[i].W;
+        }
+        lincomb_launch(vb, ch, nR, md, baggr, false, s);
+        lincomb_launch(va, ch + nR, nR, md, arr, false, s);
+        // aggregate_commitments (Whir.cpp:547-606): the codeword, the openings
+        // in the first commitment, the tree over zero leaves (whir_k = 8)
+        lincomb_launch(vc, ch + nR, nR, Lw, cw, false, s);
+      }
+      const int la = whir_query_count(4), depth_a = ilog2(Lw / 4);
+      const uint64_t off_aq = lay.rec(T_AGGR_QUERIES, (uint32_t)la, 4);
+      const uint64_t off_ap = lay.rec(T_AGGR_PATHS, (uint32_t)(la * depth_a), 32);
+      const uint64_t off_ar = lay.rec(T_AGGR_ROOT, 1, 32);
+      draw_mod(la, (uint32_t)(Lw / 4), off_aq);
+      if (!dry) {
+        k_whir_paths_chain<<<nblk((uint64_t)la * depth_a, 128), 128, 0, s>>>(ro[0].W, Lw / 4, la, tr, off_aq, off_ap,
+                                                                             0, 0);
+        k_zero_tree_root<<<1, 32, 0, s>>>(ilog2(Lw / 8), tr, off_ar);
         check();
       }
-    }
-    const int npt = (int)wt.chal.size() + ilog2(wt.m_final);
-    if (npt != logmd || (int)wt.chal.size() > 64 || (int)wt.queries.size() > kMaxTailIter)
-      throw ArgError("pcs leader: WHIR opening shape");
-    const uint64_t off_wc = lay.rec(T_L_WHIR_CLAIM, (uint32_t)(1 + logmd), 16);
-    if (!dry) {
-      const NttTables &tf = R.tables(ilog2(wt.L_final));
-      k_reencode_check<<<nblk(wt.L_final), kT, 0, s>>>(wt.final_arr, (int)wt.m_final, wt.last_codeword, wt.L_final,
-                                                      tf.lo_fwd, tf.hi_fwd, st);
-      k_whir_flags<<<1, 32, 0, s>>>(st, flags);
-      // the final claim (evaluate_vector(_initial_b, total_r), total_r)
-      ChalOffs co{};
-      co.n = (int)wt.chal.size();
-      for (int i = 0; i < co.n; i++) co.off[i] = wt.chal[i];
-      fe *total_r = alloc<fe>(logmd), *eb = alloc<fe>(md), *val = alloc<fe>(1), *mdp = alloc<fe>(multidot_scratch(md));
-      k_gather_r<<<1, 64, 0, s>>>(tr, co, wt.final_point, ilog2(wt.m_final), total_r);
-      beta_launch(total_r, logmd, eb, s);
-      VecList a1{}, a2{};
-      a1.p[0] = eb;
-      a2.p[0] = baggr;
-      multidot_launch(a1, 1, a2, 1, md, mdp, val, s);
-      k_put_claim_value<<<1, 64, 0, s>>>(val, total_r, logmd, tr, off_wc);
-      check();
-      // verification step 3
-      Step3Args a3{};
-      a3.iters = (int)wt.queries.size();
-      a3.nr = logmd;
-      int skip = 0;
-      for (int i = 0; i < a3.iters; i++) {
-        skip += ilog2((uint64_t)wt.kappa[i]);
-        a3.off_q[i] = wt.queries[i];
-        a3.off_c[i] = wt.comb[i];
-        a3.NL[i] = wt.NL[i];
-        a3.l[i] = wt.l[i];
-        a3.skip[i] = skip;
+      // _Whir_Open (Whir.cpp:469-545) with whir_k = 8 from the zero-leaf tree
+      const uint64_t sizes[1] = {md};
+      const BatchPlan P = batch_plan(1, sizes, 4, 8, Lw / 8);
+      BatchResources br;
+      br.s = s;
+      br.buf = [this](int slot, uint64_t bytes) -> void * {
+        auto it = slots.find(slot);
+        if (it != slots.end()) return it->second;
+        void *p = R.alloc(bytes);
+        slots[slot] = p;
+        return p;
+      };
+      br.tables = R.tables;
+      br.st = st;
+      br.ub_scratch = alloc<fe>(kUpdateBetasScratch);
+      WalkTrace wt;
+      // the opening draws from st->prng itself: the script leaves its state
+      // there and skips the opening's calls (per iteration log2 kappa
+      // F::_random(), the queries' rand(), update_betas' F::_random(); the
+      // final point's F::_random())
+      if (script) script->push_back({DRAW_STATE, 0, 0u, 0});
+      {
+        const fe *arrays[1] = {arr}, *bets[1] = {baggr}, *cws[1] = {cw};
+        batch_open_walk(br, P, arrays, bets, cws, nullptr, tr, lay, dry, &wt);
       }
-      a3.R = nR;
-      a3.npt = logmd;
-      a3.off_eval = wt.final_eval;
-      a3.off_claim = off_wc;
-      fe *claims = alloc<fe>((uint64_t)nR * (1 + logmd));
-      for (int c = 0; c < nR; c++)
-        GBZ_CUDA(cudaMemcpyAsync(claims + (uint64_t)c * (1 + logmd), ro[c].claim, 16ull * (1 + logmd),
-                                 cudaMemcpyDeviceToDevice, s));
-      k_whir_step3<<<1, kT, 0, s>>>(tr, a3, claims, ch, total_r, flags);
-      check();
+      {
+        uint64_t calls = 0;
+        for (const BatchStep &e : P.steps)
+          if (e.iterate) calls += 40ull * ilog2((uint64_t)e.kappa) + (uint64_t)e.l + 40;
+        calls += 40ull * ilog2(P.m_final);
+        if (script) script->push_back({DRAW_SKIP, (int)calls, 0u, 0});
+        if (!dry) {
+          k_prng_check<<<1, 32, 0, s>>>(st, after_walk, flags);
+          check();
+        }
+      }
+      const int npt = (int)wt.chal.size() + ilog2(wt.m_final);
+      if (npt != logmd || (int)wt.chal.size() > 64 || (int)wt.queries.size() > kMaxTailIter)
+        throw ArgError("pcs leader: WHIR opening shape");
+      const uint64_t off_wc = lay.rec(T_L_WHIR_CLAIM, (uint32_t)(1 + logmd), 16);
+      if (!dry) {
+        const NttTables &tf = R.tables(ilog2(wt.L_final));
+        k_reencode_check<<<nblk(wt.L_final), kT, 0, s>>>(wt.final_arr, (int)wt.m_final, wt.last_codeword, wt.L_final,
+                                                        tf.lo_fwd, tf.hi_fwd, st);
+        k_whir_flags<<<1, 32, 0, s>>>(st, flags);
+        // the final claim (evaluate_vector(_initial_b, total_r), total_r)
+        ChalOffs co{};
+        co.n = (int)wt.chal.size();
+        for (int i = 0; i < co.n; i++) co.off[i] = wt.chal[i];
+        fe *total_r = alloc<fe>(logmd), *eb = alloc<fe>(md), *val = alloc<fe>(1), *mdp = alloc<fe>(multidot_scratch(md));
+        k_gather_r<<<1, 64, 0, s>>>(tr, co, wt.final_point, ilog2(wt.m_final), total_r);
+        beta_launch(total_r, logmd, eb, s);
+        VecList a1{}, a2{};
+        a1.p[0] = eb;
+        a2.p[0] = baggr;
+        multidot_launch(a1, 1, a2, 1, md, mdp, val, s);
+        k_put_claim_value<<<1, 64, 0, s>>>(val, total_r, logmd, tr, off_wc);
+        check();
+        // verification step 3
+        Step3Args a3{};
+        a3.iters = (int)wt.queries.size();
+        a3.nr = logmd;
+        int skip = 0;
+        for (int i = 0; i < a3.iters; i++) {
+          skip += ilog2((uint64_t)wt.kappa[i]);
+          a3.off_q[i] = wt.queries[i];
+          a3.off_c[i] = wt.comb[i];
+          a3.NL[i] = wt.NL[i];
+          a3.l[i] = wt.l[i];
+          a3.skip[i] = skip;
+        }
+        a3.R = nR;
+        a3.npt = logmd;
+        a3.off_eval = wt.final_eval;
+        a3.off_claim = off_wc;
+        fe *claims = alloc<fe>((uint64_t)nR * (1 + logmd));
+        for (int c = 0; c < nR; c++)
+          GBZ_CUDA(cudaMemcpyAsync(claims + (uint64_t)c * (1 + logmd), ro[c].claim, 16ull * (1 + logmd),
+                                   cudaMemcpyDeviceToDevice, s));
+        k_whir_step3<<<1, kT, 0, s>>>(tr, a3, claims, ch, total_r, flags);
+        check();
+      }
     }
     // r_c and the final verification step
     const uint64_t off_rc = lay.rec(T_L_RC, 2, 16);
@@ -1094,6 +1241,10 @@ struct Tail {
       k_final_eval<<<1, kT, 0, s>>>(fa, terms, nterms, flags, tr);
       check();
     }
+    if (in.piop) {
+      lagrange_delegation(b2f, om);
+      return;
+    }
     // delegate_beta_eval(r2, Lagrange_Evals, b2[0], offset)
     const uint64_t off_by = lay.rec(T_L_BETA_Y, 1, 16);
     const int nd_b = 1 + 4 * logBs + 1 + 3 * (logBs + 1);
@@ -1120,9 +1271,9 @@ struct Tail {
     fe *Wr = alloc<fe>(2 * in.Bs), *bx = zeros(2 * in.Bs), *chw = alloc<fe>(logBs + 1), *finw = alloc<fe>(2);
     if (!dry) {
       fe *es = alloc<fe>(1024);
-      k_beta_evals<<<1, kT, 0, s>>>(ta, chb, finb, es, flags, tr, off_le);
+      k_beta_evals<<<1, kT, 0, s>>>(ta, chb, finb, LF_BETAS, es, flags, tr, off_le);
       const NttTables &t2 = R.tables(logBs + 1);
-      k_phi<<<nblk(2 * in.Bs), kT, 0, s>>>(chb, logBs, logBs + 1, t2.lo_fwd, t2.hi_fwd, Wr);
+      k_phi<<<nblk(2 * in.Bs), kT, 0, s>>>(chb, logBs, logBs + 1, t2.lo_fwd, t2.hi_fwd, fe_one(), Wr);
       // b = precompute_beta(r2), zero beyond its length (the reference reads
       // past the end of b there: the value is never used)
       beta_launch(in.r2, logBs, bx, s);

@@ -5,7 +5,9 @@
 // parties' data, the aggregation of the delegation claims and the WHIR
 // opening of the gathered segments (coPCS.cpp:1697-1753 with
 // aggregate_claims, aggregate_commitments and _Whir_Open, Whir.cpp:469-668)
-// and delegate_beta_eval (delegate_protocol.cpp:431-504).
+// and delegate_beta_eval (delegate_protocol.cpp:431-504); in the PIOP mode
+// (isPIOP, coPCS.cpp:1619-1690) the WHIR batch slots instead of the opening
+// and delegate_lagrange_eval (delegate_protocol.cpp:603-710).
 #pragma once
 #include <functional>
 #include <vector>
@@ -27,6 +29,16 @@ struct LeaderRound {
   const fe *s = nullptr;   // the round's phase-3 challenge (every round but the last)
 };
 
+// One WHIR batch slot the PIOP mode fills (whir_polys, whir_c, whir_betas,
+// whir_claims, whir_MTs of coPCS.cpp:1620-1629): device buffers, each may be null.
+struct WhirSlotDev {
+  fe *arr = nullptr;      // max_delegation entries
+  fe *cw = nullptr;       // 4 max_delegation entries
+  fe *betas = nullptr;    // precompute_beta of the claim's point (max_delegation entries)
+  fe *claim = nullptr;    // the claim's value
+  uint8_t *root = nullptr;  // 32 bytes
+};
+
 struct LeaderInputs {
   int N = 0;
   uint64_t Bs = 0;               // row length (instance_size[0])
@@ -41,6 +53,15 @@ struct LeaderInputs {
   const fe *r2 = nullptr;        // r2 (log2 Bs entries)
   uint64_t max_delegation = 0;
   const fe *unpack = nullptr;    // (N/2) x N: share weights of unpack_secret_share(., N/2, N)
+  // the PIOP mode: the Lagrange factors of the input row vector
+  // (_Lagrange_Evals_input, back to back, 2^loglag[k] entries each), the
+  // entries _queries[0] zeroed at the end of a row, the slots to fill
+  bool piop = false;
+  int nlag = 0;
+  int loglag[8] = {};
+  const fe *lag = nullptr;
+  uint64_t q0 = 0;
+  WhirSlotDev slot[2];
 };
 
 // Flag bits of the tail, after the reference's messages.
@@ -53,7 +74,9 @@ enum : uint32_t {
   LF_WHIR_STEP3 = 32u,   // "Error in verification step 3" (printed)
   LF_FINAL = 64u,        // "Error in final verification step" (exits)
   LF_BETAS = 128u,       // "Error in delegating betas 1" (exits)
-  LF_FATAL = LF_DELEGATION | LF_DECODING | LF_WHIR | LF_FINAL | LF_BETAS
+  LF_LAG2 = 256u,        // "Error in delegating betas 2" of delegate_lagrange_eval (exits)
+  LF_LAG3 = 512u,        // "Error in delegating betas 3" of delegate_lagrange_eval (printed)
+  LF_FATAL = LF_DELEGATION | LF_DECODING | LF_WHIR | LF_FINAL | LF_BETAS | LF_LAG2
 };
 
 struct LeaderResources {

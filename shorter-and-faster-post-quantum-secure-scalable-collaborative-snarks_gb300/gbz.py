@@ -53,7 +53,7 @@ EXPORTS = (
     "gbz_merkle_tree_from_leaves", "gbz_pcs_open_full", "gbz_pcs_open_full_bytes", "gbz_sched_set_grouping",
     "gbz_r1cs_create", "gbz_r1cs_free", "gbz_r1cs_reduce", "gbz_piop_phase1", "gbz_piop_phase1_bytes",
     "gbz_piop_phase2", "gbz_piop_phase2_bytes", "gbz_dpcs_batch_commit", "gbz_dpcs_commit", "gbz_verify_proof",
-    "gbz_dpcs_open", "gbz_dpcs_open_bytes",
+    "gbz_dpcs_open", "gbz_dpcs_open_bytes", "gbz_pcs_open_piop", "gbz_pcs_open_piop_bytes",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -198,6 +198,9 @@ def _load():
         "gbz_dpcs_open": (c_int, [vp, c_int, c_int, c_int, u64, c_int, vp, vp, vp, vp, c_int, c_int, vp, vp, vp, vp,
                                   vp, vp, vp, vp, u64, c_int]),
         "gbz_dpcs_open_bytes": (u64, [c_int, c_int, c_int]),
+        "gbz_pcs_open_piop": (c_int, [vp, vp, vp, c_int, vp, u64, vp, c_int, vp, vp, c_int, vp, vp, vp, vp, vp, vp,
+                                      u64, c_int]),
+        "gbz_pcs_open_piop_bytes": (c_int, [vp, vp, c_int, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -816,6 +819,12 @@ def pcs_schedule(N, M, rates):
     return [int(x) for x in deg], [int(x) for x in q], int(rnd.value)
 
 
+class WhirSlot(ctypes.Structure):
+    """gbz_whir_slot: one WHIR batch slot the PIOP-mode opening fills."""
+    _fields_ = [("arr", ctypes.c_void_p), ("codeword", ctypes.c_void_p), ("betas", ctypes.c_void_p),
+                ("claim", ctypes.c_void_p), ("root", ctypes.c_void_p)]
+
+
 class PcsCommitment:
     """A collaborative-PCS commitment of N parties held on the device (gbz_pcs)."""
 
@@ -866,6 +875,40 @@ class PcsCommitment:
                                    ctypes.addressof(prng), ctypes.byref(flags), _ptr(tr), nb.value, MEM_HOST)
         self.ctx.check(st)
         return tr.tobytes(), f, flags.value
+
+    def open_piop(self, b1, b2, b3, lagrange, K, fs, prng, slots=True):
+        """PCS_open_new in the PIOP mode (isPIOP = true, as coPIOP_prove calls
+        it) with input vectors b1, b2, b3 and b2's Lagrange factors (a list of
+        arrays): (transcript bytes, fs after, flags, slots) where slots is a
+        list of two dicts (arr, codeword, betas, claim, root) or None.  prng
+        is advanced in place."""
+        vec = lambda a: np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2)
+        b1, b2, b3 = vec(b1), vec(b2), vec(b3)
+        lag = [vec(x) for x in lagrange]
+        logs = (ctypes.c_int * len(lag))(*[int(x.shape[0]).bit_length() - 1 for x in lag])
+        cat = np.ascontiguousarray(np.concatenate(lag), dtype=np.uint64)
+        K = np.ascontiguousarray(K, dtype=np.uint64).reshape(2)
+        f = np.array(np.asarray(fs, dtype=np.uint64).reshape(2), copy=True)
+        nb, sl = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        self.ctx.check(lib.gbz_pcs_open_piop_bytes(self.h, logs, len(lag), ctypes.byref(nb), ctypes.byref(sl)))
+        tr = np.zeros(nb.value, dtype=np.uint8)
+        flags = ctypes.c_uint32(0)
+        out, cs = None, None
+        if slots:
+            md = sl.value
+            out = [{"arr": np.zeros((md, 2), np.uint64), "codeword": np.zeros((4 * md, 2), np.uint64),
+                    "betas": np.zeros((md, 2), np.uint64), "claim": np.zeros(2, np.uint64),
+                    "root": np.zeros(32, np.uint8)} for _ in range(2)]
+            cs = (WhirSlot * 2)()
+            for c in range(2):
+                for k in ("arr", "codeword", "betas", "claim"):
+                    setattr(cs[c], k, out[c][k].ctypes.data)
+                cs[c].root = out[c]["root"].ctypes.data
+        st = lib.gbz_pcs_open_piop(self.ctx.h, self.h, _ptr(b1), b1.shape[0], _ptr(b2), b2.shape[0], _ptr(b3),
+                                   b3.shape[0], _ptr(cat), logs, len(lag), _ptr(K), _ptr(f), ctypes.addressof(prng),
+                                   ctypes.byref(flags), cs, _ptr(tr), nb.value, MEM_HOST)
+        self.ctx.check(st)
+        return tr.tobytes(), f, flags.value, out
 
     def free(self):
         if self.h:
