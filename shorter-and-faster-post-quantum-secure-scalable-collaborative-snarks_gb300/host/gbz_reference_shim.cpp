@@ -25,8 +25,9 @@
 // open_tree_blake is not replaced: it is a lookup in the caller's host
 // levels with no data-parallel work.
 //
-// The N-party calls of libgbz (gbz_pcs_commit / gbz_pcs_open,
-// gbz_cosumcheck, gbz_party_sumcheck, gbz_piop_phase1 / gbz_piop_phase2)
+// The N-party calls of libgbz (gbz_pcs_commit / gbz_pcs_open /
+// gbz_pcs_open_piop, gbz_cosumcheck, gbz_party_sumcheck, gbz_piop_phase1 /
+// gbz_piop_phase2, gbz_dpcs_*)
 // take every party's share at once, the one-device model of the
 // collaborative prover; they replace the N-rank runs of PCS_commit /
 // PCS_open_new, quadratic/cubic_coSumcheck, _quadratic/_cubic_sumcheck and
