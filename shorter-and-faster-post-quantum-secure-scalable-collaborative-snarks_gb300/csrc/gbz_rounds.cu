@@ -31,9 +31,27 @@ template <> struct Form<SC_ZEROCHECK> { static constexpr int NV = 6, NC = 4; };
 template <> struct Form<SC_QUADRUPLE> { static constexpr int NV = 4, NC = 5; };
 
 struct Line {
-  fe a, b;
+  fe a, b, h;  // a x + b, h = a + b (the value at 1)
 };
-__device__ __forceinline__ Line line(fe lo, fe hi) { return Line{fsub(hi, lo), lo}; }
+__device__ __forceinline__ Line line(fe lo, fe hi) { return Line{fsub(hi, lo), lo, hi}; }
+
+// x / 2 in F_p: (x + p x_0) / 2 of each word.
+__device__ __forceinline__ uint64_t halfp(uint64_t x) { return (x & 1) ? (x + P) >> 1 : x >> 1; }
+__device__ __forceinline__ fe fhalf(fe x) { return fe_make(halfp(x.re), halfp(x.im)); }
+
+// The cubic form accumulates, per thread, the sums of its products at 0, 1,
+// -1 and the leading coefficient (8 products a pair instead of 9); this
+// turns them into the coefficients (x^3, x^2, x, 1) before the sums are
+// combined across threads.  The map is linear and exact, so the messages
+// are the coefficient sums the reference forms pair by pair.
+template <int FORM>
+__device__ __forceinline__ void acc_to_coeffs(fe *acc) {
+  if (FORM == SC_CUBIC) {
+    const fe e_inf = acc[0], e1 = acc[1], em = acc[2], e0 = acc[3];
+    acc[1] = fsub(fhalf(fadd(e1, em)), e0);     // c(1) + c(-1) = 2 (c2 + c0)
+    acc[2] = fsub(fhalf(fsub(e1, em)), e_inf);  // c(1) - c(-1) = 2 (c3 + c1)
+  }
+}
 
 // (a1 x + b1)(a2 x + b2) with three products
 __device__ __forceinline__ void lmul(const Line &x, const Line &y, fe q[3]) {
@@ -56,9 +74,12 @@ __device__ __forceinline__ void accumulate(const Line *l, fe b, fe *acc) {
     lmul(l[0], l[1], q);
     for (int k = 0; k < 3; k++) acc[k] = fadd(acc[k], q[k]);
   } else if (FORM == SC_CUBIC) {
-    lmul(l[0], l[1], q);
-    qlmul(q, l[2], c);
-    for (int k = 0; k < 4; k++) acc[k] = fadd(acc[k], c[k]);
+    // leading coefficient, values at 1, -1 (b - a) and 0 (acc_to_coeffs)
+    const fe m0 = fsub(l[0].b, l[0].a), m1 = fsub(l[1].b, l[1].a), m2 = fsub(l[2].b, l[2].a);
+    acc[0] = fadd(acc[0], fmul(fmul(l[0].a, l[1].a), l[2].a));
+    acc[1] = fadd(acc[1], fmul(fmul(l[0].h, l[1].h), l[2].h));
+    acc[2] = fadd(acc[2], fmul(fmul(m0, m1), m2));
+    acc[3] = fadd(acc[3], fmul(fmul(l[0].b, l[1].b), l[2].b));
   } else if (FORM == SC_QUADRUPLE) {
     // ((l1 l2) l3) l4 as the reference multiplies them (polynomial.cpp:91-101)
     lmul(l[0], l[1], q);
@@ -182,6 +203,7 @@ __global__ void __launch_bounds__(kThreads) form_step_kernel(RoundArgs a) {
     }
   }
   if (MODE == 2) return;
+  acc_to_coeffs<FORM>(acc);
   block_sum<NC>(acc);
   if (threadIdx.x == 0)
 #pragma unroll
@@ -327,6 +349,7 @@ __global__ void __launch_bounds__(kTailThreads) form_tail_kernel(TailArgs t) {
       }
       accumulate<FORM>(l, fe_zero(), acc);
     }
+    acc_to_coeffs<FORM>(acc);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1)
 #pragma unroll
@@ -404,6 +427,7 @@ __global__ void __launch_bounds__(kTailThreads) form_tail_drawn_kernel(DrawnTail
       }
       accumulate<FORM>(l, fe_zero(), acc);
     }
+    acc_to_coeffs<FORM>(acc);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1)
 #pragma unroll

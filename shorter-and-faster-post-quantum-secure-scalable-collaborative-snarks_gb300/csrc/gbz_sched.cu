@@ -297,7 +297,13 @@ void Scheduler::run(const std::vector<ProofJob> &jobs_in, const double *arrival,
       for (auto &kv : groups) {
         const double c1 = proof_cost(kv.first.first, kv.first.second);
         const int cnt = (int)kv.second.size();
-        const int parts = std::max(1, std::min(cnt, (int)std::ceil(c1 * cnt / share)));
+        // and a batched plan holds at most kGroupMaxElems codeword elements:
+        // a proof that long fills the device by itself, so batching it
+        // saves no launches and only makes every witness upload of the
+        // sub-batch wait ahead of its first kernel
+        const int64_t L = ((int64_t)1 << kv.first.first) * kv.first.second;
+        const int cap = (int)std::max<int64_t>(1, std::min<int64_t>(cnt, kGroupMaxElems / L));
+        const int parts = std::max({1, (cnt + cap - 1) / cap, std::min(cnt, (int)std::ceil(c1 * cnt / share))});
         for (int k = 0; k < parts; k++) {
           const int a = (int)((int64_t)cnt * k / parts), b = (int)((int64_t)cnt * (k + 1) / parts);
           units.emplace_back(kv.second.begin() + a, kv.second.begin() + b);

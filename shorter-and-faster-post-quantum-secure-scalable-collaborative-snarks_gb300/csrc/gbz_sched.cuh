@@ -34,6 +34,8 @@ struct SchedOpts {
 // proofs side by side slow each other down.
 constexpr int kHighSlots = 1;
 constexpr int kBigLogn = 20;
+// Batch grouping: the codeword elements one batched plan covers at most.
+constexpr int64_t kGroupMaxElems = (int64_t)1 << 23;
 
 struct ProofJob {
   const fe *witness = nullptr;       // host (pinned for overlap) or device, 2^logn elements
