@@ -533,6 +533,47 @@ def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
         t_f.append(t3 - t2)
     digest = hashlib.sha256(tr.cpu().numpy().tobytes()).hexdigest()
     full = gbz.parse_transcript(trf.cpu().numpy().tobytes())
+    # PCS_open_new in the PIOP mode (isPIOP = true, as coPIOP_prove calls
+    # it) on the same commitment: b1, b2 = La x Lb and b3 Lagrange vectors
+    # at seeded points, their claim from gbz_pcs_claim_piop, the WHIR slots
+    # left on the device
+    h = commit()
+    rl = ctypes.c_uint64(0)
+    ctx.check(lib.gbz_pcs_info(h, None, ctypes.byref(rl), None, None))
+    Bs = rl.value
+    lB = Bs.bit_length() - 1
+    pts = O.witness(0x9107, 4)
+    b1 = O.lagrange_coeff(pts[0], 5)
+    La, Lb = O.lagrange_coeff(pts[1], lB // 2), O.lagrange_coeff(pts[2], lB - lB // 2)
+    b3 = O.lagrange_coeff(pts[3], (N // 4).bit_length() - 1)
+    b2 = O.field_ops(np.tile(La, (Lb.shape[0], 1)), np.repeat(Lb, La.shape[0], axis=0))[2]
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.int64)).cuda()
+    db1, db2, db3, dlag = dv(b1), dv(b2), dv(b3), dv(np.concatenate([La, Lb]))
+    logs = (ctypes.c_int * 2)(lB // 2, lB - lB // 2)
+    pbytes = ctypes.c_uint64(0)
+    ctx.check(lib.gbz_pcs_open_piop_bytes(h, logs, 2, ctypes.byref(pbytes), None))
+    trp = torch.zeros(pbytes.value, dtype=torch.uint8, device="cuda")
+    pflags = ctypes.c_uint32(0)
+
+    def open_piop():
+        g = gbz.Prng(1)
+        ctypes.memmove(ctypes.addressof(g), g_deal, ctypes.sizeof(g))
+        ctx.check(lib.gbz_pcs_claim_piop(ctx.h, h, db1.data_ptr(), 32, db2.data_ptr(), Bs, db3.data_ptr(), N // 4,
+                                         Kd.data_ptr(), gbz.MEM_DEVICE))
+        fsd.zero_()
+        ctx.check(lib.gbz_pcs_open_piop(ctx.h, h, db1.data_ptr(), 32, db2.data_ptr(), Bs, db3.data_ptr(), N // 4,
+                                        dlag.data_ptr(), logs, 2, Kd.data_ptr(), fsd.data_ptr(), ctypes.addressof(g),
+                                        ctypes.byref(pflags), None, trp.data_ptr(), trp.numel(), gbz.MEM_DEVICE))
+        ctx.synchronize()
+
+    open_piop()
+    t_p = []
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        open_piop()
+        t_p.append(time.perf_counter() - t0)
+    lib.gbz_pcs_free(h)
     out = {"workload": "the reference's coPCS test (PCS_commit + F_ip + PCS_open_new; open_full adds the "
                        "leader's delegation proofs, final checks and WHIR opening) with %d parties on one device, "
                        "M = 2^%d (2^%d share entries per party), "
@@ -544,6 +585,10 @@ def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
            "open_full_ms": 1e3 * min(t_f), "full_total_ms": 1e3 * (min(t_c) + min(t_f)),
            "full_runs_per_s": 1.0 / (min(t_c) + min(t_f)), "full_transcript_bytes": int(fbytes.value),
            "leader_flags": int(flags.value),
+           "open_piop_ms": 1e3 * min(t_p), "open_piop_flags": int(pflags.value),
+           "open_piop_workload": "PCS_open_new with isPIOP (gbz_pcs_claim_piop + gbz_pcs_open_piop): Lagrange input "
+                                 "vectors, the WHIR batch slots and delegate_lagrange_eval instead of the aggregated "
+                                 "opening and delegate_beta_eval",
            "timing": "host wall clock around the synchronised C-ABI calls (device pointers), best of %d" % repeats}
     fx = os.path.join(ROOT, "tests", "golden", "parties_N%d_M%d.json" % (N, logM))
     if os.path.exists(fx):

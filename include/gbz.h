@@ -614,6 +614,15 @@ gbz_status gbz_pcs_open_piop(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *b1, int
 gbz_status gbz_pcs_open_piop_bytes(const gbz_pcs *pcs, const int *log_lengths, int nlag, uint64_t *bytes,
                                    uint64_t *slot_len);
 
+/* F_ip of the committed data with input vectors (MPI_utils.cpp:483-553, as
+ * coPIOP_prove forms the claim of its PCS opening): K = sum_p lambda_p
+ * sum_{i < batches - 1} sum_j b1[i] b2[j] Commit_data_p[i][j], with
+ * lambda the party weights of b3 (N/4 entries) and b2 (the row length's
+ * entries) zero on its last _queries[0] entries as gbz_pcs_open_piop uses
+ * it.  K: 2 words (mem). */
+gbz_status gbz_pcs_claim_piop(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *b1, int nb1, const uint64_t *b2,
+                              uint64_t nb2, const uint64_t *b3, int nb3, uint64_t *K, int mem);
+
 /* quadratic_coSumcheck / cubic_coSumcheck of N parties on one device
  * (form GBZ_SC_QUADRATIC or GBZ_SC_CUBIC).  p1, p2 (and p3): N x n party
  * shares, party-major; R: the parties' sparse vectors, N x sum_i (2 or 4)

@@ -445,17 +445,18 @@ gbz_status gbz_dpcs_open(gbz_ctx *ctx, int N, int P, int rows, uint64_t S, int r
     GBZ_CUDA(cudaMemcpyAsync(&hfs, fs, 16, cudaMemcpyDeviceToHost, s));
     GBZ_CUDA(cudaStreamSynchronize(s));
   }
-  // each point as (r2: log2 S, r3: log2 rows, r1: log2 N) (:1188-1203)
-  std::vector<fe> b2h((size_t)P * S), b3h((size_t)P * rows), b1h((size_t)P * N);
+  // each point as (r2: log2 S, r3: log2 rows, r1: log2 N) (:1188-1203);
+  // the long beta (r2) on the device, the row and party betas on the host
+  std::vector<fe> b3h((size_t)P * rows), b1h((size_t)P * N);
   for (int q = 0; q < P; q++) {
     const fe *r = pts.data() + (size_t)q * np;
-    std::vector<fe> t2 = host_beta(r, lS), t3 = host_beta(r + lS, lR), t1 = host_beta(r + lS + lR, lN);
-    std::copy(t2.begin(), t2.end(), b2h.begin() + (size_t)q * S);
+    std::vector<fe> t3 = host_beta(r + lS, lR), t1 = host_beta(r + lS + lR, lN);
     std::copy(t3.begin(), t3.end(), b3h.begin() + (size_t)q * rows);
     std::copy(t1.begin(), t1.end(), b1h.begin() + (size_t)q * N);
   }
-  fe *db2 = ob.alloc<fe>((uint64_t)P * S), *db3 = ob.alloc<fe>((uint64_t)P * rows);
-  GBZ_CUDA(cudaMemcpyAsync(db2, b2h.data(), 16ull * P * S, cudaMemcpyHostToDevice, s));
+  fe *db2 = ob.alloc<fe>((uint64_t)P * S), *db3 = ob.alloc<fe>((uint64_t)P * rows), *dpts = ob.alloc<fe>(pts.size());
+  GBZ_CUDA(cudaMemcpyAsync(dpts, pts.data(), 16 * pts.size(), cudaMemcpyHostToDevice, s));
+  for (int q = 0; q < P; q++) beta_launch(dpts + (size_t)q * np, lS, db2 + (uint64_t)q * S, s);
   GBZ_CUDA(cudaMemcpyAsync(db3, b3h.data(), 16ull * P * rows, cudaMemcpyHostToDevice, s));
   // row batching of the data and of the codewords (global order)
   fe *cdb = ob.alloc<fe>((uint64_t)P * N * S), *cwb = ob.alloc<fe>((uint64_t)P * N * L);

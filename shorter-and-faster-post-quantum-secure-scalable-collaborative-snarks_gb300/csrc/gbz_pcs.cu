@@ -1364,6 +1364,59 @@ gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, in
   API_END(ctx)
 }
 
+// T[32 j + i] = b1[i] b2[j] (i < 32, j < len): the row-major v1 of F_ip.
+__global__ void k_outer32(const fe *b1, const fe *b2, uint64_t len, fe *T) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < 32 * len) T[g] = fmul(b1[g & 31], b2[g >> 5]);
+}
+
+gbz_status gbz_pcs_claim_piop(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *b1, int nb1, const uint64_t *b2,
+                              uint64_t nb2, const uint64_t *b3, int nb3, uint64_t *K, int mem) {
+  API_BEGIN(ctx)
+  check_mem(mem);
+  need(pcs, "pcs");
+  need(b1, "b1");
+  need(b2, "b2");
+  need(b3, "b3");
+  need(K, "K");
+  if (pcs->device != ctx->device) throw ArgError("pcs: committed on another device");
+  const int N = pcs->sc.N, nb = pcs->batches;
+  const uint64_t Bs = pcs->Bs, q0 = (uint64_t)pcs->sc.queries[0];
+  if (nb1 < 0) throw ArgError("pcs: b1 length");
+  if (nb2 != Bs) throw ArgError("pcs: b2 must have the row length's entries");
+  if (nb3 != N / 4) throw ArgError("pcs: b3 must have N/4 entries");
+  if (q0 >= Bs) throw ArgError("pcs: _queries[0] must be below the row length");
+  cudaStream_t s = ctx->stream;
+  const cudaMemcpyKind kin = mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  std::vector<fe> hb3(N / 4);
+  GBZ_CUDA(cudaMemcpyAsync(hb3.data(), b3, 16ull * (N / 4),
+                           mem == GBZ_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost, s));
+  GBZ_CUDA(cudaStreamSynchronize(s));
+  // F_ip's party weights (MPI_utils.cpp:514-527) from b3, as for a point
+  std::vector<fe> lambda = aggregate_weights(N, hb3.data());
+  OpenBufs ob;
+  ob.pool = &ctx->pools["pcs_claim_piop:" + std::to_string(N) + ":" + std::to_string(pcs->sc.M) + ":" +
+                        std::to_string(Bs) + ":" + std::to_string(nb)];
+  fe *d1 = ob.alloc<fe>(32), *d2 = ob.alloc<fe>(Bs), *dl = ob.alloc<fe>(N), *T = ob.alloc<fe>(32 * Bs),
+     *dK = ob.alloc<fe>(1);
+  const int n1 = std::min(nb1, 32);
+  GBZ_CUDA(cudaMemsetAsync(d1, 0, 16 * 32, s));
+  if (n1 > 0) GBZ_CUDA(cudaMemcpyAsync(d1, b1, 16ull * n1, kin, s));
+  GBZ_CUDA(cudaMemcpyAsync(d2, b2, 16 * Bs, kin, s));
+  if (q0) GBZ_CUDA(cudaMemsetAsync(d2 + (Bs - q0), 0, 16 * q0, s));
+  GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
+  k_outer32<<<grid(32 * Bs), 256, 0, s>>>(d1, d2, Bs, T);
+  const int nblk = (int)std::min<uint64_t>(64, (Bs + kRedThreads - 1) / kRedThreads);
+  fe *partial = ob.alloc<fe>((uint64_t)N * nblk);
+  k_fip_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(pcs->cd, (uint64_t)nb * Bs, nb - 1, Bs, T, partial);
+  k_fip_combine<<<1, 32, 0, s>>>(partial, nblk, N, dl, dK);
+  GBZ_CUDA(cudaGetLastError());
+  if (mem == GBZ_MEM_DEVICE) GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToDevice, s));
+  else GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToHost, s));
+  GBZ_CUDA(cudaStreamSynchronize(s));
+  API_END(ctx)
+}
+
 static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, int nr, const uint64_t *K,
                                 uint64_t *fs, bool full, gbz_prng *prng, uint32_t *flags, uint8_t *transcript,
                                 uint64_t capacity, int mem, const PiopIn *pi = nullptr) {

@@ -54,6 +54,7 @@ EXPORTS = (
     "gbz_r1cs_create", "gbz_r1cs_free", "gbz_r1cs_reduce", "gbz_piop_phase1", "gbz_piop_phase1_bytes",
     "gbz_piop_phase2", "gbz_piop_phase2_bytes", "gbz_dpcs_batch_commit", "gbz_dpcs_commit", "gbz_verify_proof",
     "gbz_dpcs_open", "gbz_dpcs_open_bytes", "gbz_pcs_open_piop", "gbz_pcs_open_piop_bytes",
+    "gbz_pcs_claim_piop",
 )
 
 PROF_CATEGORIES = ("ntt", "merkle", "sumcheck", "beta", "update_betas", "query", "protocol")
@@ -201,6 +202,7 @@ def _load():
         "gbz_pcs_open_piop": (c_int, [vp, vp, vp, c_int, vp, u64, vp, c_int, vp, vp, c_int, vp, vp, vp, vp, vp, vp,
                                       u64, c_int]),
         "gbz_pcs_open_piop_bytes": (c_int, [vp, vp, c_int, vp, vp]),
+        "gbz_pcs_claim_piop": (c_int, [vp, vp, vp, c_int, vp, u64, vp, c_int, vp, c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -875,6 +877,16 @@ class PcsCommitment:
                                    ctypes.addressof(prng), ctypes.byref(flags), _ptr(tr), nb.value, MEM_HOST)
         self.ctx.check(st)
         return tr.tobytes(), f, flags.value
+
+    def claim_piop(self, b1, b2, b3):
+        """F_ip of the committed data with input vectors (b2's last
+        _queries[0] entries as zero): K."""
+        vec = lambda a: np.ascontiguousarray(a, dtype=np.uint64).reshape(-1, 2)
+        b1, b2, b3 = vec(b1), vec(b2), vec(b3)
+        K = np.zeros(2, dtype=np.uint64)
+        self.ctx.check(lib.gbz_pcs_claim_piop(self.ctx.h, self.h, _ptr(b1), b1.shape[0], _ptr(b2), b2.shape[0],
+                                              _ptr(b3), b3.shape[0], _ptr(K), MEM_HOST))
+        return K
 
     def open_piop(self, b1, b2, b3, lagrange, K, fs, prng, slots=True):
         """PCS_open_new in the PIOP mode (isPIOP = true, as coPIOP_prove calls

@@ -69,12 +69,20 @@ def run(request, gbz, oracle, ctx):
     shares, random, g0 = oracle.copcs_party_shares(N, M, rnd * N // 4, state=True)
     com, _, _ = gbz.pcs_commit(ctx, N, M, rates, shares, random)
     b1, b2, b3, lag = inputs(oracle, N, com.row_len, case["seed"])
+    K_gpu = com.claim_piop(b1, b2, b3)
     K = np.frombuffer(bytes.fromhex(case["K"]), dtype=np.uint64)
     g = gen(gbz, g0)
     tr, _, flags, slots = com.open_piop(b1, b2, b3, lag, K, np.zeros(2, np.uint64), g)
     recs = gbz.parse_transcript(tr)
     com.free()
-    yield case, deg, tr, recs, flags, slots, (g, g0)
+    yield case, deg, tr, recs, flags, slots, (g, g0, K_gpu)
+
+
+def test_claim_equals_reference(run):
+    """gbz_pcs_claim_piop: F_ip with the input vectors, as the reference's
+    driver forms K for this opening."""
+    case, _, _, _, _, _, (_, _, K_gpu) = run
+    assert K_gpu.tobytes().hex() == case["K"]
 
 
 def test_parties_part_equals_reference(run):
@@ -151,7 +159,7 @@ def test_flags_match_the_reference_messages(run):
 
 
 def test_generator_ends_where_the_reference_does(run, gbz):
-    case, _, _, _, _, _, (g, g0) = run
+    case, _, _, _, _, _, (g, g0, _) = run
     assert bytes(g) == bytes(gen(gbz, g0, case["leader"]["prng_calls"]))
 
 
