@@ -976,9 +976,10 @@ def run_rows(gbz, ctx, rt, stream, fmul_peak, b3_peak, hbm_peak, shift=0):
                                                     ob.data_ptr(), gbz._ptr(K), gbz._ptr(ch), None, D))
     n22 = 16 << la
     rec("whir_aggregate_claims_4x4_2^%d" % la, timed(aggc),
-        hbm_bytes=4 * n22 + (4 + 4) * n22 + (4 + 1) * n22 + (4 + 1) * n22,
-        fmuls=(4 + 16 + 8) * (1 << la),  # eq tables, 4 x 4 inner products, two 4-term combinations
-        note="4 eq tables written, 16 inner products (one pass over 8 vectors), 2 combinations")
+        hbm_bytes=(4 + 2) * n22,  # the arrays read once, b_aggr and arr written
+        fmuls=(4 + 16 + 8) * (1 << la),  # eq entries, 4 x 4 inner products, two 4-term combinations
+        note="eq tables formed on the fly from half-length tables (never written), 16 inner products and "
+             "2 combinations in two passes of two points over the 4 arrays")
     del arrs, msgs
     # pcs_sumcheck_phase3, 2^20 rows, 100 queries, 16 parties
     lb = 20 - shift

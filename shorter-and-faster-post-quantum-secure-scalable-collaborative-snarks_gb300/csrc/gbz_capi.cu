@@ -982,6 +982,50 @@ gbz_status gbz_whir_aggregate_claims(gbz_ctx *ctx, int k, const uint64_t *const 
   const VecList A = vec_views(ctx, 100, arrays, k, n, mem);
   fe *dpts = (fe *)ctx->buf(90, 16 * (uint64_t)c * std::max(lg, 1));
   GBZ_CUDA(cudaMemcpyAsync(dpts, points, 16 * (uint64_t)c * lg, cudaMemcpyHostToDevice, ctx->stream));
+  if (k <= 4 && c <= 4 && lg >= 2) {
+    // one pass: the verifier's weights do not depend on the sums (they are
+    // glibc draws), so they are drawn first and the pass forms the sums,
+    // b_aggr and arr together from half-length eq tables
+    glibc_prng g;
+    std::memcpy(&g, prng, sizeof(g));
+    std::vector<fe> ch(c + k);
+    for (auto &x : ch) x = prng_field(g);
+    std::memcpy(prng, &g, sizeof(g));
+    fe *dch = (fe *)ctx->buf(94, 16 * (uint64_t)(c + k));
+    GBZ_CUDA(cudaMemcpyAsync(dch, ch.data(), 16 * ch.size(), cudaMemcpyHostToDevice, ctx->stream));
+    const int h = lg / 2;
+    const uint64_t nlo = 1ull << h, nhi = 1ull << (lg - h);
+    fe *elo = (fe *)ctx->buf(97, 16 * nlo * c), *ehi = (fe *)ctx->buf(98, 16 * nhi * c);
+    for (int j = 0; j < c; j++) {
+      beta_launch(dpts + (uint64_t)j * lg, h, elo + (uint64_t)j * nlo, ctx->stream);
+      beta_launch(dpts + (uint64_t)j * lg + h, lg - h, ehi + (uint64_t)j * nhi, ctx->stream);
+    }
+    fe *partial = (fe *)ctx->buf(92, 16 * multidot_scratch(n));
+    fe *dsums = (fe *)ctx->buf(93, 16 * (uint64_t)k * c);
+    fe *dba = dev_view(ctx, 95, (fe *)b_aggr, 16 * n, mem, false);
+    fe *darr = dev_view(ctx, 96, (fe *)arr, 16 * n, mem, false);
+    aggr_claims_fused(A, k, c, elo, ehi, h, lg, n, dch, darr, dba, partial, dsums, ctx->stream);
+    std::vector<fe> hs((size_t)k * c);
+    GBZ_CUDA(cudaMemcpyAsync(hs.data(), dsums, 16 * hs.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    copy_out(ctx, (fe *)b_aggr, dba, 16 * n, mem);
+    copy_out(ctx, (fe *)arr, darr, 16 * n, mem);
+    GBZ_CUDA(cudaStreamSynchronize(ctx->stream));
+    fe Kacc = fe_zero();
+    for (int i = 0; i < k; i++)
+      for (int j = 0; j < c; j++) Kacc = fadd(Kacc, fmul(fmul(ch[j], ch[c + i]), hs[(size_t)i * c + j]));
+    K[0] = Kacc.re;
+    K[1] = Kacc.im;
+    for (int i = 0; i < c + k; i++) {
+      challenges[2 * i] = ch[i].re;
+      challenges[2 * i + 1] = ch[i].im;
+    }
+    if (sums)
+      for (size_t q = 0; q < hs.size(); q++) {
+        sums[2 * q] = hs[q].re;
+        sums[2 * q + 1] = hs[q].im;
+      }
+    return GBZ_OK;
+  }
   fe *betas = (fe *)ctx->buf(91, 16 * n * (uint64_t)c);
   VecList Bt{};
   for (int j = 0; j < c; j++) {

@@ -454,15 +454,20 @@ k_fip_partial(const fe *rows, uint64_t pstride, int nrows, uint64_t len, const f
   if (threadIdx.x == 0) partial[(uint64_t)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
 }
 
-// The leader's combination (MPI_utils.cpp:514-527): K = sum_p lambda_p y_p.
+// The leader's combination (MPI_utils.cpp:514-527): K = sum_p lambda_p y_p,
+// thread p forming y_p (launched with at least N <= 64 threads).
 __global__ void k_fip_combine(const fe *partial, int nblk, int N, const fe *lambda, fe *K) {
-  if (threadIdx.x) return;
-  fe acc = fe_zero();
-  for (int p = 0; p < N; p++) {
+  __shared__ fe t[kPcsMaxParties];
+  const int p = threadIdx.x;
+  if (p < N) {
     fe y = fe_zero();
     for (int k = 0; k < nblk; k++) y = fadd(y, partial[(uint64_t)p * nblk + k]);
-    acc = fadd(acc, fmul(lambda[p], y));
+    t[p] = fmul(lambda[p], y);
   }
+  __syncthreads();
+  if (p) return;
+  fe acc = fe_zero();
+  for (int q = 0; q < N; q++) acc = fadd(acc, t[q]);
   *K = acc;
 }
 
@@ -591,15 +596,24 @@ k_cosc_verify(CoscDev *st, const fe *poly, int logd, int ext, int round, fe *LD,
 
 // quadratic_coSumcheck_phase2_sparse (coSumcheck.cpp:215-228) for every party:
 // s = sum_j LD[j] R_p[iter][j]; R_p[j > iter] *= LD[0]; R_p[iter+1][0] += s.
-__global__ void k_cosc_sparse(fe *R, uint64_t rstride, ROffs ro, int iter, const fe *LD, int D, int N, CoscDev *st) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+// One CTA of kCoscThreads per party.
+constexpr int kCoscThreads = 256;
+__global__ void __launch_bounds__(kCoscThreads)
+k_cosc_sparse(fe *R, uint64_t rstride, ROffs ro, int iter, const fe *LD, int D, int N, CoscDev *st) {
+  const int p = blockIdx.x;
   if (p >= N) return;
   fe *Rp = R + (uint64_t)p * rstride;
   const int len = (int)(ro.off[iter + 1] - ro.off[iter]);
+  __shared__ fe red[kCoscThreads];
   fe s = fe_zero();
-  for (int j = 0; j < len && j < D; j++) s = fadd(s, fmul(LD[j], Rp[ro.off[iter] + j]));
+  for (int j = threadIdx.x; j < len && j < D; j += kCoscThreads) s = fadd(s, fmul(LD[j], Rp[ro.off[iter] + j]));
+  red[threadIdx.x] = s;
   const fe l0 = LD[0];
-  for (uint32_t e = ro.off[iter + 1]; e < ro.off[ro.n]; e++) Rp[e] = fmul(Rp[e], l0);
+  for (uint32_t e = ro.off[iter + 1] + threadIdx.x; e < ro.off[ro.n]; e += kCoscThreads) Rp[e] = fmul(Rp[e], l0);
+  __syncthreads();
+  if (threadIdx.x) return;
+  s = fe_zero();
+  for (int t = 0; t < kCoscThreads; t++) s = fadd(s, red[t]);
   if (iter + 1 < ro.n) Rp[ro.off[iter + 1]] = fadd(Rp[ro.off[iter + 1]], s);
   st->fer[p] = s;
 }
@@ -620,38 +634,70 @@ __global__ void k_cosc_ip(const fe *LD, ROffs ro, fe *ip) {
 // final values, the leader's unpack (unpack_secret_share(H, N/2, N), a fixed
 // N/2 x N map U), its check, the last challenge, the Lagrange weights over
 // N/4 points and the claims; for the cubic form also the check of b1[0]
-// against the round weights.  One thread.
+// against the round weights.  One CTA of kCoscThreads: the parties' values,
+// the unpack and the check's terms in parallel, the Fiat-Shamir chain and
+// the claims on thread 0.
 __global__ void k_cosc_final(CoscDev *st, int cubic, int N, const fe *p1, const fe *p2, const fe *p3, const fe *b1,
                              uint64_t mstride, const fe *U, const fe *b2, const fe *Ld_hist, const int *logd_hist,
                              int nrounds, const fe *r1, fe *claims, uint8_t *tr, uint64_t off_shares,
                              uint64_t off_unpacked, uint64_t off_r, uint64_t off_claims) {
-  if (threadIdx.x) return;
   const int rows = cubic ? 4 : 5, half = N / 2, quarter = N / 4;
-  fe H[kCoscMaxRows][kPcsMaxParties / 2];
-  for (int i = 0; i < rows; i++)
-    for (int j = 0; j < half; j++) H[i][j] = fe_zero();
-  for (int p = 0; p < N; p++) {
+  __shared__ fe H[kCoscMaxRows][kPcsMaxParties / 2];
+  __shared__ fe S[kPcsMaxParties][kCoscMaxRows];
+  __shared__ fe red[kCoscThreads];
+  // the parties' final values (thread p), then the unpack (thread (i, j))
+  for (int p = threadIdx.x; p < N; p += blockDim.x) {
     const uint64_t o = (uint64_t)p * mstride;
-    fe s[kCoscMaxRows];
+    fe *sp = S[p];
     if (cubic) {
-      s[0] = p1[o];
-      s[1] = p2[o];
-      s[2] = p3[o];
-      s[3] = st->fer[p];
+      sp[0] = p1[o];
+      sp[1] = p2[o];
+      sp[2] = p3[o];
+      sp[3] = st->fer[p];
     } else {
-      s[0] = p1[o];
-      s[1] = p2[o];
-      s[2] = p1[o + 1];
-      s[3] = p2[o + 1];
-      s[4] = st->fer[p];
+      sp[0] = p1[o];
+      sp[1] = p2[o];
+      sp[2] = p1[o + 1];
+      sp[3] = p2[o + 1];
+      sp[4] = st->fer[p];
     }
-    for (int i = 0; i < rows; i++) {
-      put_fe(tr, off_shares + 16ull * ((uint64_t)p * rows + i), s[i]);
-      for (int j = 0; j < half; j++) H[i][j] = fadd(H[i][j], fmul(U[j * N + p], s[i]));
+    for (int i = 0; i < rows; i++) put_fe(tr, off_shares + 16ull * ((uint64_t)p * rows + i), sp[i]);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < rows * half; q += blockDim.x) {
+    const int i = q / half, j = q % half;
+    fe h = fe_zero();
+    for (int p = 0; p < N; p++) h = fadd(h, fmul(U[j * N + p], S[p][i]));
+    H[i][j] = h;
+    put_fe(tr, off_unpacked + 16ull * (i * half + j), h);
+  }
+  __syncthreads();
+  // the cubic form's b1 check (coSumcheck.cpp:432-443): per round the d
+  // terms in parallel, their sum and the product by thread 0
+  fe y = fe_one();
+  if (cubic) {
+    int ctr = 0, at = 0;
+    for (int i = 0; i < nrounds; i++) {
+      const int ld = logd_hist[i], d = 1 << ld;
+      fe acc = fe_zero();
+      for (int j = threadIdx.x; j < d; j += blockDim.x) {
+        fe b = fe_one();
+        for (int t = 0; t < ld; t++) b = fmul(b, ((j >> t) & 1) ? r1[ctr + t] : fsub(fe_one(), r1[ctr + t]));
+        acc = fadd(acc, fmul(b, Ld_hist[at + j]));
+      }
+      red[threadIdx.x] = acc;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        fe a = fe_zero();
+        for (int t = 0; t < (int)blockDim.x; t++) a = fadd(a, red[t]);
+        y = fmul(y, a);
+      }
+      __syncthreads();
+      ctr += ld;
+      at += d;
     }
   }
-  for (int i = 0; i < rows; i++)
-    for (int j = 0; j < half; j++) put_fe(tr, off_unpacked + 16ull * (i * half + j), H[i][j]);
+  if (threadIdx.x) return;
   fe K = st->K;
   const fe c = st->c;
   for (int i = 0; i < quarter; i++) {
@@ -693,23 +739,7 @@ __global__ void k_cosc_final(CoscDev *st, int cubic, int N, const fe *p1, const 
     claims[i] = e;
     put_fe(tr, off_claims + 16ull * i, e);
   }
-  if (cubic) {  // coSumcheck.cpp:432-443
-    fe y = fe_one();
-    int ctr = 0, at = 0;
-    for (int i = 0; i < nrounds; i++) {
-      const int ld = logd_hist[i], d = 1 << ld;
-      fe acc = fe_zero();
-      for (int j = 0; j < d; j++) {
-        fe b = fe_one();
-        for (int t = 0; t < ld; t++) b = fmul(b, ((j >> t) & 1) ? r1[ctr + t] : fsub(fe_one(), r1[ctr + t]));
-        acc = fadd(acc, fmul(b, Ld_hist[at + j]));
-      }
-      ctr += ld;
-      at += d;
-      y = fmul(y, acc);
-    }
-    if (!fe_eq(y, b1[0])) st->flags |= 1u << 30;
-  }
+  if (cubic && !fe_eq(y, b1[0])) st->flags |= 1u << 30;
 }
 
 }  // namespace
@@ -1145,7 +1175,7 @@ CoscOut cosumcheck_run(gbz_ctx *ctx, int form, int N, uint64_t n, const fe *p1, 
     aggregate_launch(H, N, D, dl, poly, s);
     fe *LD = LDall + ro.off[i];
     k_cosc_verify<<<1, 256, 0, s>>>(st, poly, logd[i], ext, i, LD, Ldh + at, scr, tr, off_poly[i], off_chal[i]);
-    k_cosc_sparse<<<1, 64, 0, s>>>(dR, Rst, ro, i, LD, D, N, st);
+    k_cosc_sparse<<<N, kCoscThreads, 0, s>>>(dR, Rst, ro, i, LD, D, N, st);
     GBZ_CUDA(cudaGetLastError());
     // phase 2 (coSumcheck.cpp:66-148, 201-213): every vector folded by Ld
     for (fe *v : {v1, v2, v3, vb}) {
@@ -1157,7 +1187,7 @@ CoscOut cosumcheck_run(gbz_ctx *ctx, int form, int N, uint64_t n, const fe *p1, 
     at += d;
   }
   fe *dcl = ob.alloc<fe>(rows);
-  k_cosc_final<<<1, 32, 0, s>>>(st, cubic ? 1 : 0, N, v1, v2, v3, vb, m, dU, db2, Ldh, dlog, ndeg, dr1, dcl, tr,
+  k_cosc_final<<<1, kCoscThreads, 0, s>>>(st, cubic ? 1 : 0, N, v1, v2, v3, vb, m, dU, db2, Ldh, dlog, ndeg, dr1, dcl, tr,
                                 off_sh, off_un, off_r, off_cl);
   GBZ_CUDA(cudaGetLastError());
   if (ip) {
@@ -1356,7 +1386,7 @@ gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, in
   const int nblk = (int)std::min<uint64_t>(64, (pcs->Bs + kRedThreads - 1) / kRedThreads);
   fe *partial = ob.alloc<fe>((uint64_t)N * nblk);
   k_fip_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(pcs->cd, (uint64_t)nb * pcs->Bs, nb - 1, pcs->Bs, b1, partial);
-  k_fip_combine<<<1, 32, 0, s>>>(partial, nblk, N, dl, dK);
+  k_fip_combine<<<1, kPcsMaxParties, 0, s>>>(partial, nblk, N, dl, dK);
   GBZ_CUDA(cudaGetLastError());
   if (mem == GBZ_MEM_DEVICE) GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToDevice, s));
   else GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToHost, s));
@@ -1409,7 +1439,7 @@ gbz_status gbz_pcs_claim_piop(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *
   const int nblk = (int)std::min<uint64_t>(64, (Bs + kRedThreads - 1) / kRedThreads);
   fe *partial = ob.alloc<fe>((uint64_t)N * nblk);
   k_fip_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(pcs->cd, (uint64_t)nb * Bs, nb - 1, Bs, T, partial);
-  k_fip_combine<<<1, 32, 0, s>>>(partial, nblk, N, dl, dK);
+  k_fip_combine<<<1, kPcsMaxParties, 0, s>>>(partial, nblk, N, dl, dK);
   GBZ_CUDA(cudaGetLastError());
   if (mem == GBZ_MEM_DEVICE) GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToDevice, s));
   else GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToHost, s));

@@ -65,13 +65,23 @@ __global__ void __launch_bounds__(kThreads) multidot_kernel(VecList a, VecList b
   }
 }
 
-// out[q] = sum over blocks of partial[block * nq + q]
-__global__ void sum_cols_kernel(const fe *partial, int blocks, int nq, fe *out) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq) return;
+// out[q] = sum over blocks of partial[block * nq + q]: one CTA per q
+// (launched with nq CTAs of kThreads), the blocks spread over its threads.
+__global__ void __launch_bounds__(kThreads) sum_cols_kernel(const fe *partial, int blocks, int nq, fe *out) {
+  const int q = blockIdx.x;
   fe s = fe_zero();
-  for (int b = 0; b < blocks; b++) s = fadd(s, partial[(uint64_t)b * nq + q]);
-  out[q] = s;
+  for (int b = threadIdx.x; b < blocks; b += kThreads) s = fadd(s, partial[(uint64_t)b * nq + q]);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) s = fadd(s, shfl_down_fe(s, d));
+  __shared__ fe red[kThreads / 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) red[w] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fe t = fe_zero();
+    for (int k = 0; k < kThreads / 32; k++) t = fadd(t, red[k]);
+    out[q] = t;
+  }
 }
 
 int grid_for(uint64_t n) {
@@ -123,12 +133,104 @@ void multidot_launch(const VecList &a, int ka, const VecList &b, int kb, uint64_
       md_dispatch(ta, tb, at, bt, n, partial, blocks, s);
       // tile results go to a staging row, then into out[i][j] (row-major ka x kb)
       fe *tile = partial + (uint64_t)blocks * 16;
-      sum_cols_kernel<<<1, 32, 0, s>>>(partial, blocks, ta * tb, tile);
+      sum_cols_kernel<<<ta * tb, kThreads, 0, s>>>(partial, blocks, ta * tb, tile);
       GBZ_CUDA(cudaGetLastError());
       for (int i = 0; i < ta; i++)
         GBZ_CUDA(cudaMemcpyAsync(out + (uint64_t)(i0 + i) * kb + j0, tile + i * tb, sizeof(fe) * tb,
                                  cudaMemcpyDeviceToDevice, s));
     }
+}
+
+namespace {
+
+// aggregate_claims by streaming passes (Whir.cpp:608-668): the eq tables
+// of the claim points are never written; entry x of table j is elo_j[x mod
+// 2^h] times ehi_j[x >> h] (the two halves of the point: the products
+// precompute_beta forms, in another order).  One pass takes TC points: it
+// reads the TA arrays and forms the TA x TC sums <a_i, eq_j> (per-CTA
+// partials), adds sum_j bw[j] eq_j into b_aggr (stores it in the first
+// pass) and, when aw is set, stores arr = sum_i aw[i] a_i.  Two points a
+// pass keep the accumulators in registers at two CTAs per SM.
+template <int TA, int TC>
+__global__ void __launch_bounds__(kThreads, 2)
+aggr_claims_pass_kernel(VecList a, const fe *elo, const fe *ehi, int h, uint64_t lo_len, uint64_t hi_len,
+                        uint64_t n, const fe *bw, const fe *aw, int first, fe *arr, fe *baggr, fe *partial) {
+  __shared__ fe sw[TA + TC];
+  if (threadIdx.x < TC) sw[threadIdx.x] = bw[threadIdx.x];
+  if (aw && threadIdx.x < TA) sw[TC + threadIdx.x] = aw[threadIdx.x];
+  __syncthreads();
+  fe acc[TA * TC];
+#pragma unroll
+  for (int q = 0; q < TA * TC; q++) acc[q] = fe_zero();
+  const uint64_t stride = (uint64_t)gridDim.x * kThreads, mask = lo_len - 1;
+  for (uint64_t t = (uint64_t)blockIdx.x * kThreads + threadIdx.x; t < n; t += stride) {
+    fe x[TA];
+#pragma unroll
+    for (int i = 0; i < TA; i++) x[i] = a.p[i][t];
+    fe b = first ? fe_zero() : baggr[t];
+#pragma unroll
+    for (int j = 0; j < TC; j++) {
+      const fe e = fmul(elo[j * lo_len + (t & mask)], ehi[j * hi_len + (t >> h)]);
+      b = fadd(b, fmul(sw[j], e));
+#pragma unroll
+      for (int i = 0; i < TA; i++) acc[i * TC + j] = fadd(acc[i * TC + j], fmul(x[i], e));
+    }
+    baggr[t] = b;
+    if (aw) {
+      fe v = fe_zero();
+#pragma unroll
+      for (int i = 0; i < TA; i++) v = fadd(v, fmul(sw[TC + i], x[i]));
+      arr[t] = v;
+    }
+  }
+  __shared__ fe red[TA * TC][kThreads / 32];
+  const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < TA * TC; q++) {
+    fe sum = acc[q];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) sum = fadd(sum, shfl_down_fe(sum, d));
+    if (lane == 0) red[q][wq] = sum;
+  }
+  __syncthreads();
+  if (threadIdx.x < TA * TC) {
+    fe sum = fe_zero();
+    for (int k = 0; k < kThreads / 32; k++) sum = fadd(sum, red[threadIdx.x][k]);
+    partial[(uint64_t)blockIdx.x * TA * TC + threadIdx.x] = sum;
+  }
+}
+
+template <int TA, int TC>
+void pass_launch(const VecList &a, const fe *elo, const fe *ehi, int h, int lg, uint64_t n, const fe *bw,
+                 const fe *aw, int first, fe *arr, fe *baggr, fe *partial, int blocks, cudaStream_t s) {
+  aggr_claims_pass_kernel<TA, TC><<<blocks, kThreads, 0, s>>>(a, elo, ehi, h, 1ull << h, 1ull << (lg - h), n, bw,
+                                                              aw, first, arr, baggr, partial);
+  GBZ_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+bool aggr_claims_fused(const VecList &a, int k, int c, const fe *elo, const fe *ehi, int h, int lg, uint64_t n,
+                       const fe *w, fe *arr, fe *baggr, fe *partial, fe *sums, cudaStream_t s) {
+  if (k < 1 || c < 1 || k > 4 || c > 4) return false;
+  const int blocks = grid_for(n);
+  const uint64_t nlo = 1ull << h, nhi = 1ull << (lg - h);
+  fe *tile = partial + (uint64_t)blocks * 16;
+  for (int j0 = 0; j0 < c; j0 += 2) {
+    const int tc = std::min(2, c - j0);
+    const fe *aw = j0 + tc >= c ? w + c : nullptr;  // arr in the last pass
+    const fe *el = elo + (uint64_t)j0 * nlo, *eh = ehi + (uint64_t)j0 * nhi;
+#define GBZ_AP(A, C) \
+    if (k == A && tc == C) pass_launch<A, C>(a, el, eh, h, lg, n, w + j0, aw, j0 == 0, arr, baggr, partial, blocks, s);
+    GBZ_AP(1, 1) GBZ_AP(1, 2) GBZ_AP(2, 1) GBZ_AP(2, 2) GBZ_AP(3, 1) GBZ_AP(3, 2) GBZ_AP(4, 1) GBZ_AP(4, 2)
+#undef GBZ_AP
+    sum_cols_kernel<<<k * tc, kThreads, 0, s>>>(partial, blocks, k * tc, tile);
+    GBZ_CUDA(cudaGetLastError());
+    // the pass's k x tc sums into columns j0.. of the row-major k x c sums
+    GBZ_CUDA(cudaMemcpy2DAsync(sums + j0, sizeof(fe) * c, tile, sizeof(fe) * tc, sizeof(fe) * tc, k,
+                               cudaMemcpyDeviceToDevice, s));
+  }
+  return true;
 }
 
 }  // namespace gbz

@@ -20,5 +20,15 @@ void lincomb_launch(const VecList &v, const fe *coef, int k, uint64_t n, fe *out
 uint64_t multidot_scratch(uint64_t n);
 void multidot_launch(const VecList &a, int ka, const VecList &b, int kb, uint64_t n, fe *partial, fe *out,
                      cudaStream_t s);
+// aggregate_claims for k <= 4 arrays and c <= 4 points in passes of two
+// points over the arrays, no eq table written: elo /
+// ehi hold the c eq tables of the points' first h and last lg - h
+// coordinates (2^h and 2^(lg - h) entries each, table j at j times that);
+// w: the c beta weights then the k array weights (device).  Writes arr,
+// baggr (n entries) and sums[i * c + j] = <a_i, eq_j>; partial holds
+// multidot_scratch(n) elements.  Returns false (nothing launched) outside
+// those counts.
+bool aggr_claims_fused(const VecList &a, int k, int c, const fe *elo, const fe *ehi, int h, int lg, uint64_t n,
+                       const fe *w, fe *arr, fe *baggr, fe *partial, fe *sums, cudaStream_t s);
 
 }  // namespace gbz

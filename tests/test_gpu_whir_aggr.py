@@ -22,7 +22,8 @@ def test_aggregate_claims_golden(ctx, golden, name):
     assert np.array_equal(gch, np.concatenate([bch, ach]))
 
 
-@pytest.mark.parametrize("k,c,logn", [(1, 1, 3), (5, 7, 12), (9, 2, 16), (3, 3, 20)])
+@pytest.mark.parametrize("k,c,logn", [(1, 1, 3), (5, 7, 12), (9, 2, 16), (3, 3, 20), (4, 4, 13), (2, 1, 2),
+                                        (4, 2, 1)])
 def test_aggregate_claims_vs_oracle(ctx, oracle, k, c, logn):
     rng = np.random.default_rng(300 + k * 10 + c)
     n = 1 << logn
