@@ -279,11 +279,17 @@ __global__ void k_indexes(PcsDev *st, int l, int N, uint32_t Mq, int32_t *qp, in
 // length d (utils.cpp:169-197: the inverse transform of the powers of c).
 // scratch: 2 * 2d entries.
 __global__ void __launch_bounds__(256)
-k_round_verify(PcsDev *st, const fe *poly, int logd, fe *L, fe *scratch, uint8_t *tr, uint64_t off_poly,
-               uint64_t off_chal) {
+k_round_verify(PcsDev *st, const fe *poly, int logd, fe wi, fe invD, fe invd, fe *L, fe *scratch, uint8_t *tr,
+               uint64_t off_poly, uint64_t off_chal) {
   __shared__ fe red[256];
+  __shared__ fe chal;
   const int d = 1 << logd, D = 2 * d;
   fe *cp = scratch, *wp = scratch + D;
+  // (wi = omega_D^-1, invD, invd: constants of the shape, formed on the host)
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    wp[k] = fpow(wi, (uint64_t)k);
+    put_fe(tr, off_poly + 16ull * k, poly[k]);
+  }
   if (threadIdx.x == 0) {
     fe ev = fe_zero();
     for (int j = 0; j < d; j++) ev = fadd(ev, poly[2 * j]);
@@ -293,21 +299,12 @@ k_round_verify(PcsDev *st, const fe *poly, int logd, fe *L, fe *scratch, uint8_t
     st->fs = fs;
     st->c = fs;
     put_fe(tr, off_chal, fs);
-    fe x = fe_one();
-    for (int k = 0; k < D; k++) {
-      cp[k] = x;
-      x = fmul(x, fs);
-    }
+    chal = fs;
   }
   __syncthreads();
-  const fe wi = finv(root_of_unity(logd + 1));
-  for (int k = threadIdx.x; k < D; k += blockDim.x) {
-    wp[k] = fpow(wi, (uint64_t)k);
-    put_fe(tr, off_poly + 16ull * k, poly[k]);
-  }
+  for (int k = threadIdx.x; k < D; k += blockDim.x) cp[k] = fpow(chal, (uint64_t)k);
   __syncthreads();
   // L2[k] = (1/D) sum_j c^j w^{-jk}; K' = sum_k poly[k] L2[k]
-  const fe invD = finv(fe_make((uint64_t)D, 0)), invd = finv(fe_make((uint64_t)d, 0));
   fe acc = fe_zero();
   for (int k = threadIdx.x; k < D; k += blockDim.x) {
     fe s = fe_zero();
@@ -544,11 +541,17 @@ __global__ void k_cosc_add_hr(fe *H, int D, const fe *R, uint64_t rstride, ROffs
 // H LD, Ld = compute_lagrange_coeff(r, d) (coSumcheck.cpp:258-293,
 // 362-396).  scratch: 2 D entries.
 __global__ void __launch_bounds__(256)
-k_cosc_verify(CoscDev *st, const fe *poly, int logd, int ext, int round, fe *LD, fe *Ld, fe *scratch, uint8_t *tr,
-              uint64_t off_poly, uint64_t off_chal) {
+k_cosc_verify(CoscDev *st, const fe *poly, int logd, int ext, int round, fe wi, fe invD, fe invd, fe *LD, fe *Ld,
+              fe *scratch, uint8_t *tr, uint64_t off_poly, uint64_t off_chal) {
   __shared__ fe red[256];
+  __shared__ fe chal;
   const int d = 1 << logd, D = d << ext;
   fe *cp = scratch, *wp = scratch + D;
+  // (wi = omega_D^-1, invD, invd: constants of the shape, formed on the host)
+  for (int k = threadIdx.x; k < D; k += blockDim.x) {
+    wp[k] = fpow(wi, (uint64_t)k);
+    put_fe(tr, off_poly + 16ull * k, poly[k]);
+  }
   if (threadIdx.x == 0) {
     fe ev = fe_zero();
     for (int j = 0; j < d; j++) ev = fadd(ev, poly[j << ext]);
@@ -558,20 +561,11 @@ k_cosc_verify(CoscDev *st, const fe *poly, int logd, int ext, int round, fe *LD,
     st->fs = fs;
     st->r[round] = fs;
     put_fe(tr, off_chal, fs);
-    fe x = fe_one();
-    for (int k = 0; k < D; k++) {
-      cp[k] = x;
-      x = fmul(x, fs);
-    }
+    chal = fs;
   }
   __syncthreads();
-  const fe wi = finv(root_of_unity(logd + ext));
-  for (int k = threadIdx.x; k < D; k += blockDim.x) {
-    wp[k] = fpow(wi, (uint64_t)k);
-    put_fe(tr, off_poly + 16ull * k, poly[k]);
-  }
+  for (int k = threadIdx.x; k < D; k += blockDim.x) cp[k] = fpow(chal, (uint64_t)k);
   __syncthreads();
-  const fe invD = finv(fe_make((uint64_t)D, 0)), invd = finv(fe_make((uint64_t)d, 0));
   fe acc = fe_zero();
   for (int k = threadIdx.x; k < D; k += blockDim.x) {
     fe s = fe_zero();
@@ -1174,7 +1168,9 @@ CoscOut cosumcheck_run(gbz_ctx *ctx, int form, int N, uint64_t n, const fe *p1, 
     k_put_party<<<dim3(grid(D), N), 256, 0, s>>>(H, D, N, tr, off_pp[i], 16ull * D);
     aggregate_launch(H, N, D, dl, poly, s);
     fe *LD = LDall + ro.off[i];
-    k_cosc_verify<<<1, 256, 0, s>>>(st, poly, logd[i], ext, i, LD, Ldh + at, scr, tr, off_poly[i], off_chal[i]);
+    k_cosc_verify<<<1, 256, 0, s>>>(st, poly, logd[i], ext, i, finv(root_of_unity(logd[i] + ext)),
+                                    finv(fe_make((uint64_t)D, 0)), finv(fe_make(1ull << logd[i], 0)), LD, Ldh + at,
+                                    scr, tr, off_poly[i], off_chal[i]);
     k_cosc_sparse<<<N, kCoscThreads, 0, s>>>(dR, Rst, ro, i, LD, D, N, st);
     GBZ_CUDA(cudaGetLastError());
     // phase 2 (coSumcheck.cpp:66-148, 201-213): every vector folded by Ld
@@ -1680,7 +1676,8 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
     cophase1_reduce_launch(e1, e2, nullptr, nullptr, nullptr, pblocks, logd + 1, per_cta, cpart, H, s, N);
     k_put_party<<<dim3(grid(D), N), 256, 0, s>>>(H, D, N, tr, ro.pp, 16ull * D);
     aggregate_launch(H, N, D, dlam, poly, s);
-    k_round_verify<<<1, 256, 0, s>>>(st, poly, logd, Ld, vscr, tr, ro.poly, ro.chal);
+    k_round_verify<<<1, 256, 0, s>>>(st, poly, logd, finv(root_of_unity(logd + 1)), finv(fe_make(2ull << logd, 0)),
+                                     finv(fe_make(1ull << logd, 0)), Ld, vscr, tr, ro.poly, ro.chal);
     GBZ_CUDA(cudaGetLastError());
     // pcs_sumcheck_phase2 (coPCS.cpp:571-587)
     cophase2_launch(bcd, (uint64_t)N * n, Ld, logd, coef, s);
