@@ -71,10 +71,9 @@ void trees(gbz_ctx *ctx, uint8_t *levels, uint64_t leaves, int N, uint8_t *roots
   const cudaStream_t s = ctx->stream;
   const uint64_t nh = 2 * leaves - 1;
   for (int p = 0; p < N; p++) merkle_from_leaves_launch(levels + (uint64_t)p * 32 * nh, leaves, s);
+  // every party's root (the last hash of its levels) in one strided copy
   std::vector<uint8_t> roots((size_t)32 * N);
-  for (int p = 0; p < N; p++)
-    GBZ_CUDA(cudaMemcpyAsync(roots.data() + 32 * p, levels + ((uint64_t)p * nh + nh - 1) * 32, 32,
-                             cudaMemcpyDeviceToHost, s));
+  GBZ_CUDA(cudaMemcpy2DAsync(roots.data(), 32, levels + (nh - 1) * 32, 32 * nh, 32, N, cudaMemcpyDeviceToHost, s));
   GBZ_CUDA(cudaStreamSynchronize(s));
   if (roots_h) std::memcpy(roots_h, roots.data(), roots.size());
   // rank 0's tree over {its root, 0, ..., 0} (coPCS.cpp:338-349, distributed_PCS.cpp:101-110)
