@@ -81,9 +81,12 @@ __global__ void coset_kernel(fe *x, uint64_t n, const fe *inv_lo, const fe *inv_
 // (rows 0..3), because every inner node hashes its left child twice; the
 // other seven leaves the reference hashes are discarded, so they are not
 // computed here.
-__global__ void column_root_kernel(const fe *rows, int nrows, uint64_t L, uint8_t *roots) {
+__global__ void column_root_kernel(const fe *rows, int nrows, uint64_t L, uint8_t *roots, uint64_t rows_stride,
+                                   uint64_t roots_stride) {
   const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= L) return;
+  rows += rows_stride * blockIdx.y;  // grid.y: parties
+  roots += roots_stride * blockIdx.y;
   fe e[4];
   for (int k = 0; k < 4; k++) e[k] = k < nrows ? rows[(uint64_t)k * L + j] : fe_zero();
   uint32_t m[16], h[8];
@@ -100,8 +103,10 @@ __global__ void column_root_kernel(const fe *rows, int nrows, uint64_t L, uint8_
 
 // The leader's root tree over {root, 0, ..., 0} of N parties: its root is
 // log2(N) self-hashes of the party root (coPCS.cpp:193-201).
-__global__ void party_root_kernel(const uint8_t *root, int logN, uint8_t *out) {
+__global__ void party_root_kernel(const uint8_t *root, int logN, uint8_t *out, uint64_t root_stride) {
   if (threadIdx.x) return;
+  root += root_stride * blockIdx.x;  // one CTA per party
+  out += 32 * blockIdx.x;
   uint32_t m[16], h[8];
   for (int k = 0; k < 8; k++) h[k] = reinterpret_cast<const uint32_t *>(root)[k];
   for (int lv = 0; lv < logN; lv++) {
@@ -374,11 +379,13 @@ void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s, int row
 }
 
 void column_merkle_launch(const fe *rows, int nrows, uint64_t L, uint8_t *levels, int logN, uint8_t *root,
-                          cudaStream_t s) {
-  column_root_kernel<<<grid(L), 256, 0, s>>>(rows, nrows, L, levels);
+                          cudaStream_t s, int parties, uint64_t rows_stride) {
+  if (parties < 1 || parties > 65535) throw ArgError("column trees: 1..65535 parties per launch");
+  const uint64_t tree = 32 * (2 * L - 1);
+  column_root_kernel<<<dim3(grid(L), (unsigned)parties), 256, 0, s>>>(rows, nrows, L, levels, rows_stride, tree);
   GBZ_CUDA(cudaGetLastError());
-  merkle_from_leaves_launch(levels, L, s);
-  party_root_kernel<<<1, 32, 0, s>>>(levels + 32 * (2 * L - 2), logN, root);
+  merkle_from_leaves_launch(levels, L, s, parties);
+  party_root_kernel<<<parties, 32, 0, s>>>(levels + 32 * (2 * L - 2), logN, root, tree);
   GBZ_CUDA(cudaGetLastError());
 }
 

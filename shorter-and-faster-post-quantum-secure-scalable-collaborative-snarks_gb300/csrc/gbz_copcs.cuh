@@ -19,10 +19,12 @@ void powers_launch(fe r, uint64_t n, fe *out, cudaStream_t s);
 void coset_launch(fe *x, uint64_t n, const NttTables &t, cudaStream_t s, int rows = 1, uint64_t row_stride = 0);
 // out[r L + rate t + off] = x[r n + t] for t < n, r < rows.
 void strided_copy_launch(const fe *x, uint64_t n, fe *out, uint64_t L, int rate, int off, int rows, cudaStream_t s);
-// distributed_MT for one party (coPCS.cpp:152-202): levels (2L - 1 hashes,
-// column roots first) and the leader's root over 2^logN parties.
+// distributed_MT (coPCS.cpp:152-202) of `parties` parties in the same
+// launches: party p's rows at rows + p rows_stride, its levels (2L - 1
+// hashes, column roots first) at levels + p (2L - 1) hashes and its leader
+// root over 2^logN parties at root + 32 p.
 void column_merkle_launch(const fe *rows, int nrows, uint64_t L, uint8_t *levels, int logN, uint8_t *root,
-                          cudaStream_t s);
+                          cudaStream_t s, int parties = 1, uint64_t rows_stride = 0);
 // Packed Shamir shares (compute_secret_shares, MPI_utils.cpp:2738-2764).
 std::vector<fe> shamir_share_matrix(int N);
 void shares_launch(const fe *v, const fe *fill, uint64_t groups, int N, const fe *mu, fe *shares, cudaStream_t s);

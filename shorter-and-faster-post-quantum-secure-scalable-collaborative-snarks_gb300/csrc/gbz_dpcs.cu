@@ -70,7 +70,7 @@ __global__ void k_dpcs_columns(const fe *rows, int nrows, uint64_t len, uint64_t
 void trees(gbz_ctx *ctx, uint8_t *levels, uint64_t leaves, int N, uint8_t *roots_h, uint8_t *leader_h) {
   const cudaStream_t s = ctx->stream;
   const uint64_t nh = 2 * leaves - 1;
-  for (int p = 0; p < N; p++) merkle_from_leaves_launch(levels + (uint64_t)p * 32 * nh, leaves, s);
+  merkle_from_leaves_launch(levels, leaves, s, N);
   // every party's root (the last hash of its levels) in one strided copy
   std::vector<uint8_t> roots((size_t)32 * N);
   GBZ_CUDA(cudaMemcpy2DAsync(roots.data(), 32, levels + (nh - 1) * 32, 32 * nh, 32, N, cudaMemcpyDeviceToHost, s));

@@ -204,7 +204,9 @@ void merkle_set_fusion(int log_nodes_per_cta);
 int merkle_get_fusion();
 // create_tree_blake (merkle_tree.cpp:267-299) over L leaf hashes stored at
 // levels[0 .. L): writes levels 1.. after them (2L - 1 hashes in total).
-void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s);
+// trees > 1: that many trees of the same shape, 2L - 1 hashes apart, in the
+// same launches.
+void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s, int trees = 1);
 
 // ------------------------------------------------------------- sumcheck
 // One fused sumcheck step over vectors (a, b) of length m:

@@ -58,7 +58,11 @@ __device__ __forceinline__ void store_hash(uint8_t *p, const uint32_t w[8]) {
 template <int LOGN>
 __global__ void __launch_bounds__(kThreads)
 merkle_levels_kernel(const fe *elems, const uint8_t *child, uint64_t cnt0, uint8_t *levels,
-                     uint64_t level_off0, int nlevels) {
+                     uint64_t level_off0, int nlevels, uint64_t tree_hashes) {
+  // grid.y: independent trees of the same shape, tree_hashes apart (the
+  // child levels live in the same tree)
+  levels += 32 * tree_hashes * blockIdx.y;
+  if (child) child += 32 * tree_hashes * blockIdx.y;
   constexpr int kNodesPerCta = 1 << LOGN;
   // Only even nodes feed the level above (the right child is never read),
   // so each ping-pong buffer keeps the even half of a level.
@@ -131,13 +135,13 @@ __global__ void blake3_batch_kernel(const uint8_t *in, uint8_t *out, uint64_t co
 }
 
 void launch_levels(int logn_cta, const fe *elems, const uint8_t *child, uint64_t cnt, uint8_t *levels,
-                   uint64_t off, int nlev, cudaStream_t s) {
-  const uint64_t blocks = (cnt + (1ull << logn_cta) - 1) >> logn_cta;
+                   uint64_t off, int nlev, cudaStream_t s, int trees = 1, uint64_t tree_hashes = 0) {
+  const dim3 g((unsigned)((cnt + (1ull << logn_cta) - 1) >> logn_cta), (unsigned)trees);
   switch (logn_cta) {
-    case 11: merkle_levels_kernel<11><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev); break;
-    case 10: merkle_levels_kernel<10><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev); break;
-    case 9: merkle_levels_kernel<9><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev); break;
-    default: merkle_levels_kernel<8><<<(unsigned)blocks, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev); break;
+    case 11: merkle_levels_kernel<11><<<g, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev, tree_hashes); break;
+    case 10: merkle_levels_kernel<10><<<g, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev, tree_hashes); break;
+    case 9: merkle_levels_kernel<9><<<g, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev, tree_hashes); break;
+    default: merkle_levels_kernel<8><<<g, kThreads, 0, s>>>(elems, child, cnt, levels, off, nlev, tree_hashes); break;
   }
   GBZ_CUDA(cudaGetLastError());
 }
@@ -171,15 +175,16 @@ void merkle_commit_launch(const fe *elems, uint64_t N, uint8_t *levels, cudaStre
   }
 }
 
-void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s) {
+void merkle_from_leaves_launch(uint8_t *levels, uint64_t L, cudaStream_t s, int trees) {
   if (!is_pow2(L)) throw ArgError("Merkle tree over leaves needs a power-of-two count");
+  if (trees < 1 || trees > 65535) throw ArgError("Merkle trees: 1..65535 per launch");
   const int depth = ilog2(L);  // levels 1..depth above the leaves
-  const int lg = fusion_for(L / 2);
+  const int lg = fusion_for(L / 2 * (uint64_t)trees);
   uint64_t cnt = L / 2, off = L, child_off = 0;
   int level = 1;
   while (level <= depth) {
     const int nlev = min(lg + 1, depth - level + 1);
-    launch_levels(lg, nullptr, levels + 32 * child_off, cnt, levels, off, nlev, s);
+    launch_levels(lg, nullptr, levels + 32 * child_off, cnt, levels, off, nlev, s, trees, 2 * L - 1);
     for (int k = 0; k < nlev; k++) {
       child_off = off;
       off += cnt;

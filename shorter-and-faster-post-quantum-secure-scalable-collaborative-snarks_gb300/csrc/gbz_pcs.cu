@@ -1292,11 +1292,8 @@ gbz_status gbz_pcs_commit(gbz_ctx *ctx, int N, uint64_t M, int rounds, const int
   // Encode (coPCS.cpp:131-147): every party's rows in the same launches
   encode_rows_device(ctx, pc->cd, N * nb, ilog2(Bs), sc.rate0[0], sc.log_rate_offset, pc->cw);
   // distributed_MT (coPCS.cpp:152-202) per party
-  for (int p = 0; p < N; p++)
-    column_merkle_launch(pc->cw + (uint64_t)p * nb * L, nb, L, pc->levels + 32ull * p * (2 * L - 1), ilog2(N),
-                         pc->roots + 32ull * (N + p), s);
-  for (int p = 0; p < N; p++)
-    GBZ_CUDA(cudaMemcpyAsync(pc->roots + 32ull * p, pc->levels + 32ull * p * (2 * L - 1) + 32 * (2 * L - 2), 32,
+  column_merkle_launch(pc->cw, nb, L, pc->levels, ilog2(N), pc->roots + 32ull * N, s, N, (uint64_t)nb * L);
+  GBZ_CUDA(cudaMemcpy2DAsync(pc->roots, 32, pc->levels + 32 * (2 * L - 2), 32 * (2 * L - 1), 32, N,
                              cudaMemcpyDeviceToDevice, s));
   if (party_roots) {
     if (mem == GBZ_MEM_HOST) GBZ_CUDA(cudaMemcpyAsync(party_roots, pc->roots, 32ull * N, cudaMemcpyDeviceToHost, s));

@@ -680,7 +680,7 @@ def gen_pcspiop():
     import tempfile
     out = {}
     rates = [[4], [4], [4, 4], [4, 4]]
-    for N, logM, seed in ((8, 16, 31), (16, 16, 32), (16, 18, 33)):
+    for N, logM, seed in ((8, 16, 31), (16, 16, 32), (16, 18, 33), (32, 17, 34)):
         with tempfile.TemporaryDirectory() as td:
             prefix, cap = os.path.join(td, "pp"), os.path.join(td, "cap")
             env = dict(os.environ, MINIMPI_NP=str(N), MINIMPI_TIMEOUT="300", MINIMPI_CAPTURE=cap)

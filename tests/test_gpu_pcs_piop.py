@@ -1,6 +1,6 @@
 """PCS_open_new in the PIOP mode (isPIOP = true, coPCS.cpp:1310-1690, as
 coPIOP_prove calls it, coPIOP.cpp:1741-1773) on one device
-(gbz_pcs_open_piop), against the reference run unmodified with N = 8 and 16
+(gbz_pcs_open_piop), against the reference run unmodified with N = 8, 16 and 32
 MPI ranks (tests/golden/pcspiop_*.json, written by tests/golden/make_golden.py
 through oracle/ref's pigeon_dpcs pcs mode).
 
@@ -32,7 +32,7 @@ from test_gpu_pcs_leader import D_CLAIM, D_EXT, D_FINAL, D_OPEN, D_QUERIES, D_RO
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["pcspiop_N8_M16.json", "pcspiop_N16_M16.json", "pcspiop_N16_M18.json"]
+CASES = ["pcspiop_N8_M16.json", "pcspiop_N16_M16.json", "pcspiop_N16_M18.json", "pcspiop_N32_M17.json"]
 LAG_EVALS = 69
 AGGR_K, W_ROOT = 21, 9
 M64 = (1 << 64) - 1
