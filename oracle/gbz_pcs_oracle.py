@@ -283,6 +283,34 @@ def f_ip(parties, sched, r):
     return s
 
 
+def f_ip_vectors(parties, sched, b1, b2, b3):
+    """F_ip (MPI_utils.cpp:483-553) with input vectors as coPIOP_prove forms
+    the claim of its PCS opening (the pcs mode of oracle/ref/dpcs_mpi_driver.cpp):
+    row weights b1 (32 entries), the row vector b2 with its last _queries[0]
+    entries zero (coPCS.cpp:1328-1335), the party weights b3 (N/4 entries)."""
+    N = sched["N"]
+    b2 = arr(b2).copy()
+    q0 = sched["queries"][0]
+    b2[len(b2) - q0:] = 0
+    b1 = arr(b1)
+    Y = []
+    for p in range(N):
+        cd = parties[p]["cd"]
+        batches = cd.shape[0]
+        acc = (0, 0)
+        for i in range(batches - 1):
+            acc = fadd(acc, fmul(fe(b1[i]), fe(vdot(cd[i], b2))))
+        Y.append(acc)
+    Yv = orc.fft(arr(Y), inverse=True)
+    Yv = vmul(Yv, powers(finv(rou(1 + int(math.log2(N)))), N))
+    Yv = orc.fft(Yv)
+    b3 = arr(b3)
+    s = (0, 0)
+    for i in range(b3.shape[0]):
+        s = fadd(s, fmul(fe(b3[i]), fe(Yv[N * i // (N // 2)])))
+    return s
+
+
 class Chain:
     """Fiat-Shamir prev_challenge (Fiat_Shamir.cpp:5-56)."""
 
