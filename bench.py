@@ -674,7 +674,16 @@ def run_dpcs(gbz, O, ctx, repeats, N=16, logA=20, batch=16, rate=4):
         t0 = time.perf_counter()
         open_()
         to.append(time.perf_counter() - t0)
-    return {"dpcs": {"open_ms": 1e3 * min(to),
+    ref = {}
+    fx = os.path.join(ROOT, "tests", "golden", "dpcs_timing.json")
+    if os.path.exists(fx) and (N, logA, batch, rate) == (16, 20, 16, 4):
+        with open(fx) as f:
+            rj = json.load(f)
+        # the reference's Batch_dCommit and PIOP_dOpen_batch_new at this size,
+        # 16 ranks on an 8-core x86 host (recorded by tests/golden/make_golden.py)
+        ref = {"reference_ranks_seconds_x86": {"commit": rj["commit_seconds"], "open": rj["open_seconds"],
+                                               "ranks": rj["ranks"], "host_cores": rj["host_cores"]}}
+    return {"dpcs": dict(ref, **{"open_ms": 1e3 * min(to),
                      "open_workload": "PIOP_dOpen_batch_new of the witness commitment and a zero index commitment "
                                       "(2 x 16 rows of 2^%d per party), unchecked claims" % (lS,),
                      "workload": "Batch_dCommit of %d parties, 2^%d entries each in %d rows, rate %d: %d transforms "
@@ -683,7 +692,7 @@ def run_dpcs(gbz, O, ctx, repeats, N=16, logA=20, batch=16, rate=4):
                                                                               L.bit_length() - 1),
                      "ms": 1e3 * t, "commits_per_s": 1.0 / t, "bytes_moved": moved, "gbs": moved / t / 1e9,
                      "timing": "host wall clock around the synchronised C-ABI call (device pointers), best of %d"
-                               % repeats}}
+                               % repeats})}
 
 
 def run_piop(gbz, O, ctx, repeats, N=16, logM=20):

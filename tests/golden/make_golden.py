@@ -71,6 +71,8 @@ def main():
             manifest["dpcs"] = gen_dpcs()
         if "pcspiop" in only:
             manifest["pcspiop"] = gen_pcspiop()
+        if "dpcs_timing" in only:
+            manifest["dpcs_timing"] = gen_dpcs_timing()
         with open(os.path.join(HERE, "manifest.json"), "w") as f:
             json.dump(manifest, f, indent=1)
         print("updated", sorted(only))
@@ -724,6 +726,26 @@ def gen_pcspiop():
         out[name] = {"file": name + ".json", "N": N, "logM": logM}
         print("pcspiop N=%d M=2^%d" % (N, logM), flush=True)
     return out
+def gen_dpcs_timing():
+    """The reference's own time for the distributed PCS at the benchmark's
+    size (bench.py run_dpcs: 16 parties, 2^20 entries each in 16 rows, rate
+    4): Batch_dCommit and PIOP_dOpen_batch_new run unmodified with 16 ranks
+    on this host's cores (oracle/ref/dpcs_mpi_driver.cpp open mode,
+    DPCS_TIMING=1: rank 0's wall time of the first commitment and of the
+    opening)."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        env = dict(os.environ, MINIMPI_NP="16", MINIMPI_TIMEOUT="1500", DPCS_TIMING="1")
+        log = subprocess.run([DPCS, "open", "2", "20", "16", "4", "41", os.path.join(td, "o")], env=env, check=True,
+                             capture_output=True, text=True)
+    line = [x for x in log.stdout.splitlines() if x.startswith("seconds:")][0].split()
+    out = {"N": 16, "logA": 20, "batch": 16, "rate": 4, "P": 2, "commit_seconds": float(line[2]),
+           "open_seconds": float(line[4]), "host_cores": os.cpu_count(), "ranks": 16}
+    with open(os.path.join(HERE, "dpcs_timing.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    return {"file": "dpcs_timing.json"}
+
+
 DPCS_OPEN_CASES = [(2, 8, 12, 8, 4, 21), (2, 16, 13, 8, 4, 22), (3, 8, 11, 4, 2, 23), (2, 32, 11, 4, 4, 24)]
 DPCS_CASES = [("batch", 8, 12, 8, 4, 5), ("batch", 16, 14, 16, 4, 6), ("batch", 8, 13, 4, 8, 7),
               ("batch", 32, 10, 32, 2, 8), ("single", 8, 12, 0, 4, 9), ("single", 16, 13, 0, 2, 10),
