@@ -590,6 +590,14 @@ def run_party_shares(gbz, O, ctx, repeats, N=16, logM=24):
                                  "vectors, the WHIR batch slots and delegate_lagrange_eval instead of the aggregated "
                                  "opening and delegate_beta_eval",
            "timing": "host wall clock around the synchronised C-ABI calls (device pointers), best of %d" % repeats}
+    tx = os.path.join(ROOT, "tests", "golden", "dpcs_timing.json")
+    if os.path.exists(tx):
+        with open(tx) as f:
+            pp = json.load(f).get("pcs_piop", {})
+        if (pp.get("N"), pp.get("logM")) == (N, logM):
+            # the reference's PCS_open_new(..., true) at this size, 16 ranks on an
+            # 8-core x86 host (recorded by tests/golden/make_golden.py)
+            out["open_piop_reference_seconds_x86"] = pp["open_seconds"]
     fx = os.path.join(ROOT, "tests", "golden", "parties_N%d_M%d.json" % (N, logM))
     if os.path.exists(fx):
         with open(fx) as f:

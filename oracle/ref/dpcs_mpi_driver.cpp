@@ -263,7 +263,10 @@ int pcs_mode(int argc, char **argv, int rank, int N) {
   for (int j = 0; j < Bs - _queries[0]; j++)
     for (int i = 0; i < batches - 1; i++) v1[j * rows + i] = inputs[0][i] * inputs[1][j];
   F K = F_ip(v, v1, inputs[2], k, _k, N);
+  const double t0 = MPI_Wtime();
   PCS_open_new(C, codeword, Commit_data, inputs, Lagrange_evals, K, rate, N, true);
+  // DPCS_TIMING=1: rank 0 reports the opening's wall time
+  if (rank == 0 && getenv("DPCS_TIMING")) printf("seconds: open_piop %.6f\n", MPI_Wtime() - t0);
   if (rank == 0) {
     char path[4096];
     snprintf(path, sizeof path, "%s.%d", out, rank);

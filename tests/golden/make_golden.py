@@ -741,6 +741,13 @@ def gen_dpcs_timing():
     line = [x for x in log.stdout.splitlines() if x.startswith("seconds:")][0].split()
     out = {"N": 16, "logA": 20, "batch": 16, "rate": 4, "P": 2, "commit_seconds": float(line[2]),
            "open_seconds": float(line[4]), "host_cores": os.cpu_count(), "ranks": 16}
+    # PCS_open_new with isPIOP at the party-shares size (16 parties, M = 2^24;
+    # bench.py run_party_shares' open_piop_ms), the driver's pcs mode
+    with tempfile.TemporaryDirectory() as td:
+        log = subprocess.run([DPCS, "pcs", "24", "35", os.path.join(td, "p")], env=env, check=True,
+                             capture_output=True, text=True)
+    line = [x for x in log.stdout.splitlines() if x.startswith("seconds: open_piop")][0].split()
+    out["pcs_piop"] = {"N": 16, "logM": 24, "open_seconds": float(line[2])}
     with open(os.path.join(HERE, "dpcs_timing.json"), "w") as f:
         json.dump(out, f, indent=1)
     return {"file": "dpcs_timing.json"}
