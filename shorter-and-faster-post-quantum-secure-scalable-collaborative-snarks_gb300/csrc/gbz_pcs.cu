@@ -433,15 +433,25 @@ __global__ void k_fold_q(const fe *cw, uint64_t n, int logd, const fe *iQ, fe sc
 }
 
 // F_ip's local inner product (MPI_utils.cpp:489-491) of every party:
-// sum_{i < nrows} sum_j rows[p][i][j] b1[32 j + i] (v[32 j + i] = Commit_data[i][j],
-// main.cpp:99-103), as per-CTA partials.
+// sum_{i < nrows} sum_j rows[p][i][j] v1[32 j + i] (v[32 j + i] =
+// Commit_data[i][j], main.cpp:99-103) with the separable weights v1[32 j +
+// i] = brow[i] bcol[j] (the point's beta, or the input vectors' product) as
+// sum_j bcol[j] sum_i brow[i] rows[p][i][j]: no 32 x len table is read.
+// Per-CTA partials.
 __global__ void __launch_bounds__(kRedThreads)
-k_fip_partial(const fe *rows, uint64_t pstride, int nrows, uint64_t len, const fe *b1, fe *partial) {
+k_fip_partial(const fe *rows, uint64_t pstride, int nrows, uint64_t len, const fe *brow, const fe *bcol,
+              fe *partial) {
   __shared__ fe red[kRedThreads];
+  __shared__ fe sr[32];
+  if (threadIdx.x < 32) sr[threadIdx.x] = brow[threadIdx.x];
+  __syncthreads();
   fe acc = fe_zero();
   const fe *r = rows + blockIdx.y * pstride;
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < len; j += (uint64_t)gridDim.x * blockDim.x)
-    for (int i = 0; i < nrows; i++) acc = fadd(acc, fmul(r[(uint64_t)i * len + j], b1[32 * j + i]));
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < len; j += (uint64_t)gridDim.x * blockDim.x) {
+    fe c = fe_zero();
+    for (int i = 0; i < nrows; i++) c = fadd(c, fmul(r[(uint64_t)i * len + j], sr[i]));
+    acc = fadd(acc, fmul(c, bcol[j]));
+  }
   red[threadIdx.x] = acc;
   __syncthreads();
   for (int s = kRedThreads / 2; s > 0; s >>= 1) {
@@ -1372,25 +1382,24 @@ gbz_status gbz_pcs_claim(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *r, in
   OpenBufs ob;
   ob.pool = &ctx->pools["pcs_claim:" + std::to_string(N) + ":" + std::to_string(pcs->sc.M) + ":" +
                         std::to_string(pcs->Bs) + ":" + std::to_string(nb)];
-  fe *dr = ob.alloc<fe>(nr), *dl = ob.alloc<fe>(N), *b1 = ob.alloc<fe>(32ull * pcs->Bs), *dK = ob.alloc<fe>(1);
+  fe *dr = ob.alloc<fe>(nr), *dl = ob.alloc<fe>(N), *brow = ob.alloc<fe>(32), *bcol = ob.alloc<fe>(pcs->Bs),
+     *dK = ob.alloc<fe>(1);
   GBZ_CUDA(cudaMemcpyAsync(dr, hr.data(), 16ull * nr, cudaMemcpyHostToDevice, s));
   GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
-  beta_launch(dr + lk, 5 + logBs, b1, s);
+  // the weights of v[32 j + i]: beta over (r1: 5, r2: log2 Bs) = brow[i] bcol[j]
+  beta_launch(dr + lk, 5, brow, s);
+  beta_launch(dr + lk + 5, logBs, bcol, s);
   const int nblk = (int)std::min<uint64_t>(64, (pcs->Bs + kRedThreads - 1) / kRedThreads);
   fe *partial = ob.alloc<fe>((uint64_t)N * nblk);
-  k_fip_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(pcs->cd, (uint64_t)nb * pcs->Bs, nb - 1, pcs->Bs, b1, partial);
+  if (nb - 1 > 32) throw ArgError("pcs: F_ip over more than 32 rows");
+  k_fip_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(pcs->cd, (uint64_t)nb * pcs->Bs, nb - 1, pcs->Bs, brow, bcol,
+                                                       partial);
   k_fip_combine<<<1, kPcsMaxParties, 0, s>>>(partial, nblk, N, dl, dK);
   GBZ_CUDA(cudaGetLastError());
   if (mem == GBZ_MEM_DEVICE) GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToDevice, s));
   else GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToHost, s));
   GBZ_CUDA(cudaStreamSynchronize(s));
   API_END(ctx)
-}
-
-// T[32 j + i] = b1[i] b2[j] (i < 32, j < len): the row-major v1 of F_ip.
-__global__ void k_outer32(const fe *b1, const fe *b2, uint64_t len, fe *T) {
-  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g < 32 * len) T[g] = fmul(b1[g & 31], b2[g >> 5]);
 }
 
 gbz_status gbz_pcs_claim_piop(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *b1, int nb1, const uint64_t *b2,
@@ -1420,18 +1429,17 @@ gbz_status gbz_pcs_claim_piop(gbz_ctx *ctx, const gbz_pcs *pcs, const uint64_t *
   OpenBufs ob;
   ob.pool = &ctx->pools["pcs_claim_piop:" + std::to_string(N) + ":" + std::to_string(pcs->sc.M) + ":" +
                         std::to_string(Bs) + ":" + std::to_string(nb)];
-  fe *d1 = ob.alloc<fe>(32), *d2 = ob.alloc<fe>(Bs), *dl = ob.alloc<fe>(N), *T = ob.alloc<fe>(32 * Bs),
-     *dK = ob.alloc<fe>(1);
+  fe *d1 = ob.alloc<fe>(32), *d2 = ob.alloc<fe>(Bs), *dl = ob.alloc<fe>(N), *dK = ob.alloc<fe>(1);
   const int n1 = std::min(nb1, 32);
   GBZ_CUDA(cudaMemsetAsync(d1, 0, 16 * 32, s));
   if (n1 > 0) GBZ_CUDA(cudaMemcpyAsync(d1, b1, 16ull * n1, kin, s));
   GBZ_CUDA(cudaMemcpyAsync(d2, b2, 16 * Bs, kin, s));
   if (q0) GBZ_CUDA(cudaMemsetAsync(d2 + (Bs - q0), 0, 16 * q0, s));
   GBZ_CUDA(cudaMemcpyAsync(dl, lambda.data(), 16ull * N, cudaMemcpyHostToDevice, s));
-  k_outer32<<<grid(32 * Bs), 256, 0, s>>>(d1, d2, Bs, T);
   const int nblk = (int)std::min<uint64_t>(64, (Bs + kRedThreads - 1) / kRedThreads);
   fe *partial = ob.alloc<fe>((uint64_t)N * nblk);
-  k_fip_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(pcs->cd, (uint64_t)nb * Bs, nb - 1, Bs, T, partial);
+  if (nb - 1 > 32) throw ArgError("pcs: F_ip over more than 32 rows");
+  k_fip_partial<<<dim3(nblk, N), kRedThreads, 0, s>>>(pcs->cd, (uint64_t)nb * Bs, nb - 1, Bs, d1, d2, partial);
   k_fip_combine<<<1, kPcsMaxParties, 0, s>>>(partial, nblk, N, dl, dK);
   GBZ_CUDA(cudaGetLastError());
   if (mem == GBZ_MEM_DEVICE) GBZ_CUDA(cudaMemcpyAsync(K, dK, 16, cudaMemcpyDeviceToDevice, s));
