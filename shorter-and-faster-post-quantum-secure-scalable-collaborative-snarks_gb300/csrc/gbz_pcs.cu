@@ -1599,9 +1599,12 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
   // row batching (coPCS.cpp:1352-1356) and the transforms of :1359-1366
   fe *Cp = ob.alloc<fe>((uint64_t)N * L), *bcd = ob.alloc<fe>((uint64_t)N * Bs), *cdl = ob.alloc<fe>((uint64_t)N * Bs);
   fe *B = ob.alloc<fe>((uint64_t)N * Bs), *tmp = ob.alloc<fe>(std::max<uint64_t>((uint64_t)N * L, 1ull << 13));
-  k_lincomb<<<dim3(grid(L), N), 256, 0, s>>>(pcs->cw, (uint64_t)nb * L, L, nb - 1, L, b1, Cp, L);
   k_lincomb<<<dim3(grid(Bs), N), 256, 0, s>>>(pcs->cd, (uint64_t)nb * Bs, Bs, nb - 1, Bs, b1, bcd, Bs);
   GBZ_CUDA(cudaGetLastError());
+  // C' = sum_i b1[i] Codeword[i] is Encode of the batched data: every
+  // codeword row is Encode(Commit_data row) and Encode is linear, so one
+  // encode of bcd per party replaces reading the nb - 1 codeword rows
+  encode_rows_device(ctx, bcd, N, logBs, sc.rate0[0], sc.log_rate_offset, Cp);
   GBZ_CUDA(cudaMemcpy2DAsync(cdl, 16 * Bs, pcs->cd + (uint64_t)(nb - 1) * Bs, 16ull * nb * Bs, 16 * Bs, N,
                              cudaMemcpyDeviceToDevice, s));
   const NttTables &tB = ctx->tables(logBs);
