@@ -358,21 +358,30 @@ __global__ void k_check_y(const fe *Cpn, uint64_t pstride, uint32_t mul, uint32_
 
 // s = hash_to_field({0}) and, unless the last round, K += sum_j s^{j+1} y_j
 // (coPCS.cpp:1535-1547).
-__global__ void k_s_update(PcsDev *st, const fe *y, int l, int addK, uint8_t *tr, uint64_t off_s, uint64_t off_K) {
-  if (threadIdx.x) return;
-  const fe s = hash_F(st->fs, fe_zero());
-  st->fs = s;
-  st->s = s;
-  if (addK) {
-    fe K = st->K, pk = s;
-    for (int j = 0; j < l; j++) {
-      K = fadd(K, fmul(pk, y[j]));
-      pk = fmul(pk, s);
-    }
-    st->K = K;
+// K += sum_j s^(j+1) y_j: term j on thread j mod 256 (s^(j+1) by
+// squarings), the block's sum on thread 0.  Launched with 256 threads.
+__global__ void __launch_bounds__(256)
+k_s_update(PcsDev *st, const fe *y, int l, int addK, uint8_t *tr, uint64_t off_s, uint64_t off_K) {
+  __shared__ fe sh_s;
+  __shared__ fe red[256];
+  if (threadIdx.x == 0) {
+    sh_s = hash_F(st->fs, fe_zero());
+    st->fs = sh_s;
+    st->s = sh_s;
   }
+  __syncthreads();
+  const fe s = sh_s;
+  fe acc = fe_zero();
+  if (addK)
+    for (int j = threadIdx.x; j < l; j += blockDim.x) acc = fadd(acc, fmul(fpow(s, (uint64_t)j + 1), y[j]));
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x) return;
+  fe K = st->K;
+  for (int t = 0; t < (int)blockDim.x; t++) K = fadd(K, red[t]);
+  st->K = K;
   put_fe(tr, off_s, s);
-  put_fe(tr, off_K, st->K);
+  put_fe(tr, off_K, K);
 }
 
 // pcs_sumcheck_phase3 (coPCS.cpp:634-648) for every party: B_p[j] +=
@@ -1775,7 +1784,7 @@ static gbz_status pcs_open_impl(gbz_ctx *ctx, gbz_pcs *pcs, const uint64_t *r, i
                                         y, l, st);
       GBZ_CUDA(cudaGetLastError());
     }
-    k_s_update<<<1, 1, 0, s>>>(st, y, l, last ? 0 : 1, tr, ro.s, ro.K);
+    k_s_update<<<1, 256, 0, s>>>(st, y, l, last ? 0 : 1, tr, ro.s, ro.K);
     GBZ_CUDA(cudaGetLastError());
     if (full) {
       fe *sc_ = ob.alloc<fe>(1);
