@@ -283,8 +283,9 @@ k_round_verify(PcsDev *st, const fe *poly, int logd, fe wi, fe invD, fe invd, fe
                uint64_t off_poly, uint64_t off_chal) {
   __shared__ fe red[256];
   __shared__ fe chal;
+  __shared__ fe sh_cw[2 * 1024];  // the powers of c and of w^-1 (global scratch beyond 1024 points)
   const int d = 1 << logd, D = 2 * d;
-  fe *cp = scratch, *wp = scratch + D;
+  fe *cp = D <= 1024 ? sh_cw : scratch, *wp = D <= 1024 ? sh_cw + D : scratch + D;
   // (wi = omega_D^-1, invD, invd: constants of the shape, formed on the host)
   for (int k = threadIdx.x; k < D; k += blockDim.x) {
     wp[k] = fpow(wi, (uint64_t)k);
@@ -564,8 +565,9 @@ k_cosc_verify(CoscDev *st, const fe *poly, int logd, int ext, int round, fe wi, 
               fe *scratch, uint8_t *tr, uint64_t off_poly, uint64_t off_chal) {
   __shared__ fe red[256];
   __shared__ fe chal;
+  __shared__ fe sh_cw[2 * 1024];  // the powers of c and of w^-1 (global scratch beyond 1024 points)
   const int d = 1 << logd, D = d << ext;
-  fe *cp = scratch, *wp = scratch + D;
+  fe *cp = D <= 1024 ? sh_cw : scratch, *wp = D <= 1024 ? sh_cw + D : scratch + D;
   // (wi = omega_D^-1, invD, invd: constants of the shape, formed on the host)
   for (int k = threadIdx.x; k < D; k += blockDim.x) {
     wp[k] = fpow(wi, (uint64_t)k);
